@@ -1,0 +1,165 @@
+/*
+ * qdkgb.h — C ABI of the GB300-native selected-CI / CASCI core.
+ *
+ * This is the drop-in boundary for the hot path that qdk-chemistry runs
+ * through MACIS: determinant-driven Hamiltonian build, Davidson eigensolve,
+ * spin-resolved 1-/2-RDMs and the ASCI determinant search.  All compute runs
+ * in hand-written sm_103a CUDA kernels; there is no CPU fallback.
+ *
+ * Conventions
+ *   - Every call returns an int status (QDKGB_OK == 0).  On failure the
+ *     message is available from qdkgb_last_error(ctx).  No C++ exception
+ *     crosses this boundary.
+ *   - Buffers passed as plain pointers are caller-owned HOST memory unless a
+ *     function name ends in _device, in which case they are device pointers on
+ *     the context's GPU.
+ *   - Integrals are MACIS's column-major spans: T(p,q) = T[p + n q],
+ *     V(p,q,r,s) = V[p + n q + n^2 r + n^3 s] (layout QDKGB_LAYOUT_COLMAJOR),
+ *     or qdk's row-major dense buffer (QDKGB_LAYOUT_ROWMAJOR).
+ *   - A determinant is a pair of uint64 spin strings (bit i = spatial orbital
+ *     i occupied), alpha and beta in separate arrays.  This covers MACIS's
+ *     wfn_t<N> for N <= 128 (alpha = low N/2 bits, beta = high N/2 bits of the
+ *     std::bitset<N>).
+ *   - One context per host thread; a context owns device memory and a CUDA
+ *     stream (the caller may substitute its own with qdkgb_set_stream).
+ */
+#ifndef QDKGB_H
+#define QDKGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QDKGB_OK 0
+#define QDKGB_ERR_INVALID 1       /* bad argument (maps to std::invalid_argument / runtime_error) */
+#define QDKGB_ERR_CUDA 2          /* CUDA runtime error */
+#define QDKGB_ERR_OOM 3           /* device allocation failed */
+#define QDKGB_ERR_NOT_CONVERGED 4 /* "Davidson Did Not Converge!" (davidson.hpp:368) */
+#define QDKGB_ERR_UNSUPPORTED 5   /* input outside what the GPU path handles */
+#define QDKGB_ERR_STATE 6         /* call made before its prerequisites */
+
+#define QDKGB_LAYOUT_COLMAJOR 0
+#define QDKGB_LAYOUT_ROWMAJOR 1
+
+/* Storage of the Hamiltonian values on the device. */
+#define QDKGB_H_FP64 0    /* FP64 values: 8 B/nnz + int32 column */
+#define QDKGB_H_SPLIT32 1 /* FP32 high part + FP32 low part (h ~= hi + lo to 2^-48 |h|) */
+
+/* Davidson precision modes. */
+#define QDKGB_PREC_FP64 0  /* plain FP64 SpMV and vectors */
+#define QDKGB_PREC_MIXED 1 /* FP32 SpMV (FP32 values, x, y, accumulation) + FP64 defect-correction restarts */
+
+typedef struct qdkgb_context qdkgb_context;
+
+/* ------------------------------------------------------------ context */
+int qdkgb_create(qdkgb_context** ctx, int device);
+int qdkgb_destroy(qdkgb_context* ctx);
+const char* qdkgb_last_error(const qdkgb_context* ctx);
+/* cudaStream_t passed as void*; NULL restores the context's own stream. */
+int qdkgb_set_stream(qdkgb_context* ctx, void* stream);
+/* Bytes of device memory currently held by the context. */
+int qdkgb_device_bytes(const qdkgb_context* ctx, int64_t* bytes);
+
+/* ------------------------------------------------------------ integrals
+ * Replaces the HamiltonianGeneratorBase constructor and
+ * generate_integral_intermediates_ (external/macis/src/macis/
+ * hamiltonian_generator/base.ipp:27-77): uploads T, V and builds
+ * G_red, V_red, G2_red, V2_red on the device.  norb <= 64. */
+int qdkgb_set_integrals(qdkgb_context* ctx, int norb, const double* T, const double* V, int layout);
+
+/* ------------------------------------------------------------ determinants
+ * generate_combs / generate_hilbert_space
+ * (external/macis/include/macis/sd_operations.hpp:305-351): all
+ * (nalpha, nbeta) determinants over norb orbitals in MACIS order (alpha
+ * major, strings in std::prev_permutation order).  Call with alpha == NULL to
+ * query *ndets only. */
+int qdkgb_fci_dets(int norb, int nalpha, int nbeta, uint64_t* alpha, uint64_t* beta, int64_t* ndets);
+
+/* Uploads a determinant list and builds its alpha grouping
+ * (get_unique_alpha, sd_operations.hpp:449-468) and the alpha/beta string
+ * connectivity used by every kernel.  The list must be alpha-grouped (equal
+ * alpha strings contiguous) with the beta strings of every group in one
+ * common order, as both MACIS producers give it (generate_hilbert_space and
+ * std::sort by spin_comparator, raw_bitset.hpp:119-141); otherwise
+ * QDKGB_ERR_UNSUPPORTED. */
+int qdkgb_set_dets(qdkgb_context* ctx, int64_t ndets, const uint64_t* alpha, const uint64_t* beta);
+
+/* ------------------------------------------------------------ Hamiltonian
+ * Replaces SortedDoubleLoopHamiltonianGenerator::make_csr_hamiltonian_block_
+ * (include/macis/hamiltonian_generator/sorted_double_loop.hpp:86-451) for the
+ * symmetric case, including threshold_parallel
+ * (sparsexx/matrix_types/csr_matrix.hpp:317-372): keeps |h| > thresh (all
+ * entries when thresh <= 0), columns sorted per row, values of the mirrored
+ * entry computed with the lower-index determinant as bra.  The CSR stays on
+ * the device (int64 row pointers, int32 columns); *nnz receives its size. */
+int qdkgb_build_hamiltonian(qdkgb_context* ctx, double thresh, int storage, int64_t* nnz);
+/* Copies the device CSR to host buffers (rowptr: ndets+1, colind/values: nnz).
+ * For QDKGB_H_SPLIT32 storage, values receive (double)hi + (double)lo.
+ * The 32-bit and 64-bit variants mirror make_csr_hamiltonian_block_32bit_ /
+ * _64bit_ (include/macis/hamiltonian_generator.hpp:32-294). */
+int qdkgb_get_csr32(qdkgb_context* ctx, int32_t* rowptr, int32_t* colind, double* values);
+int qdkgb_get_csr64(qdkgb_context* ctx, int64_t* rowptr, int64_t* colind, double* values);
+/* extract_diagonal_elements (sparsexx/util/submatrix.hpp:354-384). */
+int qdkgb_diagonal(qdkgb_context* ctx, double* D);
+
+/* y = H x with the device CSR (gespmbv, sparsexx/spblas/spmbv.hpp:49-85).
+ * precision QDKGB_PREC_FP64 uses the full-precision values with FP64
+ * accumulation; QDKGB_PREC_MIXED uses FP32 values, x and accumulation. */
+int qdkgb_spmv(qdkgb_context* ctx, int precision, const double* x, double* y);
+/* Same on device vectors: FP64 mode takes double*, MIXED mode float*. */
+int qdkgb_spmv_device(qdkgb_context* ctx, int precision, const void* x, void* y);
+
+/* ------------------------------------------------------------ eigensolver */
+typedef struct qdkgb_davidson_settings {
+  int64_t max_m;      /* ci_max_subspace / max_solver_iterations (default 200) */
+  double res_tol;     /* ci_res_tol: residual 2-norm (default 1e-8) */
+  int precision;      /* QDKGB_PREC_FP64 or QDKGB_PREC_MIXED */
+  int use_guess;      /* 1: C holds a guess (used when max|C| > 1/N, selected_ci_diag.hpp:130-140) */
+  double min_abs_denominator; /* preconditioner clamp (default 1e-12) */
+} qdkgb_davidson_settings;
+
+typedef struct qdkgb_davidson_info {
+  int64_t iterations;       /* Davidson iterations (all precisions) */
+  int64_t spmv_fp64;        /* full-precision sigma applications */
+  int64_t spmv_fp32;        /* FP32 sigma applications (mixed mode) */
+  int64_t restarts;         /* defect-correction restarts (mixed mode) */
+  double residual_norm;     /* final full-precision residual 2-norm */
+  double seconds;           /* wall time of the eigensolve */
+} qdkgb_davidson_info;
+
+void qdkgb_davidson_default_settings(qdkgb_davidson_settings* s);
+/* serial_selected_ci_diag + davidson (include/macis/solvers/
+ * selected_ci_diag.hpp:111-158, davidson.hpp:259-372) on the device CSR:
+ * lowest eigenpair.  C (host, ndets) is the guess on input when use_guess,
+ * and the eigenvector on output; *E the eigenvalue (electronic). */
+int qdkgb_davidson(qdkgb_context* ctx, const qdkgb_davidson_settings* s, double* E, double* C,
+                   qdkgb_davidson_info* info);
+
+/* ------------------------------------------------------------ RDMs
+ * SortedDoubleLoopHamiltonianGenerator::form_rdms_spin_dep
+ * (sorted_double_loop.hpp:626-753, contributions util/rdms.hpp:39-612):
+ * spin-resolved 1-RDMs (n x n) and 2-RDMs (n^4), column-major, MACIS index
+ * convention, ACCUMULATED into the caller's buffers (+=).  A NULL buffer
+ * skips that block.  C is the host CI vector of the current determinants. */
+int qdkgb_rdms_spin_dep(qdkgb_context* ctx, const double* C, double* ordm_aa, double* ordm_bb, double* trdm_aaaa,
+                        double* trdm_bbbb, double* trdm_aabb);
+
+/* ------------------------------------------------------------ CASCI driver
+ * cas_helper::impl / compute_casci_rdms (cpp/src/qdk/chemistry/algorithms/
+ * microsoft/macis_cas.cpp:35-117, include/macis/mcscf/cas.hpp:33-64): FCI
+ * space, H build, Davidson.  E receives the electronic energy (the caller
+ * adds the core energy, macis_cas.cpp:113); C (may be NULL) the CI vector in
+ * MACIS determinant order. */
+int qdkgb_casci(qdkgb_context* ctx, int norb, int nalpha, int nbeta, const double* T, const double* V, int layout,
+                const qdkgb_davidson_settings* s, double matel_tol, double* E, double* C, qdkgb_davidson_info* info);
+
+/* ------------------------------------------------------------ version */
+const char* qdkgb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* QDKGB_H */

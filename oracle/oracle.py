@@ -1,0 +1,195 @@
+"""ctypes binding of the CPU oracle (test infrastructure only; see __init__)."""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_SRC = os.path.join(_HERE, "macis_oracle.cpp")
+_OUT_DIR = os.path.join(_HERE, "_build")
+_LIB_PATH = os.path.join(_OUT_DIR, "libmacis_oracle.so")
+_lib = None
+
+_u64p = np.ctypeslib.ndpointer(np.uint64, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+_i64p = np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")
+
+
+def build(force=False):
+    """Compile the oracle with g++ (OpenMP, no FMA contraction)."""
+    os.makedirs(_OUT_DIR, exist_ok=True)
+    if (not force and os.path.exists(_LIB_PATH)
+            and os.path.getmtime(_LIB_PATH) >= os.path.getmtime(_SRC)):
+        return _LIB_PATH
+    cmd = ["g++", "-O2", "-std=c++17", "-fopenmp", "-fPIC", "-shared",
+           "-ffp-contract=off", _SRC, "-o", _LIB_PATH + ".tmp"]
+    subprocess.check_call(cmd)
+    os.replace(_LIB_PATH + ".tmp", _LIB_PATH)
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(_LIB_PATH)
+        vp, i64, f64, ci = ctypes.c_void_p, ctypes.c_int64, ctypes.c_double, ctypes.c_int
+        L.orc_last_error.restype = ctypes.c_char_p
+        L.orc_num_threads.restype = ci
+        L.orc_combs.restype = i64
+        L.orc_combs.argtypes = [ci, ci, ctypes.c_void_p]
+        L.orc_ham_create.restype = vp
+        L.orc_ham_create.argtypes = [ci, _f64p, _f64p]
+        L.orc_ham_destroy.argtypes = [vp]
+        L.orc_ham_intermediates.argtypes = [vp, _f64p, _f64p, _f64p, _f64p]
+        L.orc_matrix_element.restype = f64
+        L.orc_matrix_element.argtypes = [vp, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64]
+        L.orc_csr_build.restype = vp
+        L.orc_csr_build.argtypes = [vp, _u64p, _u64p, i64, f64]
+        L.orc_csr_nnz.restype = i64
+        L.orc_csr_nnz.argtypes = [vp]
+        L.orc_csr_copy.argtypes = [vp, _i64p, _i64p, _f64p]
+        L.orc_csr_destroy.argtypes = [vp]
+        L.orc_csr_spmv.argtypes = [vp, _f64p, _f64p]
+        L.orc_csr_diag.argtypes = [vp, _f64p]
+        L.orc_selected_ci_diag.restype = ci
+        L.orc_selected_ci_diag.argtypes = [vp, i64, f64, _f64p, ctypes.POINTER(f64), ctypes.POINTER(i64)]
+        L.orc_syev.argtypes = [ci, _f64p, _f64p]
+        L.orc_rdms_spin_dep.argtypes = [ci, _u64p, _u64p, i64, _f64p] + [ctypes.c_void_p] * 5
+        _lib = L
+    return _lib
+
+
+def num_threads():
+    return lib().orc_num_threads()
+
+
+def combs(nbits, nset):
+    """generate_combs order (prev_permutation from the lowest orbitals)."""
+    L = lib()
+    cnt = L.orc_combs(nbits, nset, None)
+    out = np.zeros(cnt, dtype=np.uint64)
+    L.orc_combs(nbits, nset, out.ctypes.data)
+    return out
+
+
+def fci_dets(norb, na, nb):
+    """generate_hilbert_space: alpha-major product of the two string lists."""
+    a = combs(norb, na)
+    b = combs(norb, nb)
+    return np.repeat(a, len(b)), np.tile(b, len(a))
+
+
+class Hamiltonian:
+    """Integrals + MACIS intermediates (HamiltonianGeneratorBase)."""
+
+    def __init__(self, T, V):
+        self.n = int(T.shape[0])
+        # column-major buffers as MACIS reads them
+        self._T = np.ascontiguousarray(np.asarray(T, dtype=np.float64).ravel(order="F"))
+        self._V = np.ascontiguousarray(np.asarray(V, dtype=np.float64).ravel(order="F"))
+        self._h = lib().orc_ham_create(self.n, self._T, self._V)
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().orc_ham_destroy(self._h)
+            self._h = None
+
+    def intermediates(self):
+        n = self.n
+        G = np.zeros(n ** 3)
+        Vr = np.zeros(n ** 3)
+        G2 = np.zeros(n ** 2)
+        V2 = np.zeros(n ** 2)
+        lib().orc_ham_intermediates(self._h, G, Vr, G2, V2)
+        return G, Vr, G2, V2
+
+    def matrix_element(self, bra, ket):
+        return lib().orc_matrix_element(self._h, int(bra[0]), int(bra[1]), int(ket[0]), int(ket[1]))
+
+
+class Csr:
+    def __init__(self, handle, n):
+        self._m = handle
+        self.n = n
+
+    def __del__(self):
+        if getattr(self, "_m", None):
+            lib().orc_csr_destroy(self._m)
+            self._m = None
+
+    @property
+    def nnz(self):
+        return lib().orc_csr_nnz(self._m)
+
+    def arrays(self):
+        nnz = self.nnz
+        rp = np.zeros(self.n + 1, dtype=np.int64)
+        ci = np.zeros(nnz, dtype=np.int64)
+        nz = np.zeros(nnz, dtype=np.float64)
+        lib().orc_csr_copy(self._m, rp, ci, nz)
+        return rp, ci, nz
+
+    def spmv(self, x):
+        y = np.zeros(self.n)
+        lib().orc_csr_spmv(self._m, np.ascontiguousarray(x, dtype=np.float64), y)
+        return y
+
+    def diag(self):
+        d = np.zeros(self.n)
+        lib().orc_csr_diag(self._m, d)
+        return d
+
+    def selected_ci_diag(self, max_m=200, tol=1e-8, X=None):
+        """Returns (E, X, iterations); raises on non-convergence."""
+        X = np.zeros(self.n) if X is None else np.array(X, dtype=np.float64)
+        E = ctypes.c_double()
+        it = ctypes.c_int64()
+        rc = lib().orc_selected_ci_diag(self._m, max_m, tol, X, ctypes.byref(E), ctypes.byref(it))
+        if rc == 1:
+            raise RuntimeError("Davidson Did Not Converge!")
+        if rc != 0:
+            raise RuntimeError(lib().orc_last_error().decode())
+        return E.value, X, it.value
+
+
+def build_csr(ham, alpha, beta, thresh=np.finfo(np.float64).eps):
+    alpha = np.ascontiguousarray(alpha, dtype=np.uint64)
+    beta = np.ascontiguousarray(beta, dtype=np.uint64)
+    h = lib().orc_csr_build(ham._h, alpha, beta, len(alpha), float(thresh))
+    if not h:
+        raise RuntimeError(lib().orc_last_error().decode())
+    return Csr(h, len(alpha))
+
+
+def syev(A):
+    A = np.array(A, dtype=np.float64, order="F")
+    k = A.shape[0]
+    buf = np.ascontiguousarray(A.ravel(order="F"))
+    w = np.zeros(k)
+    lib().orc_syev(k, buf, w)
+    return w, buf.reshape((k, k), order="F")
+
+
+def rdms_spin_dep(norb, alpha, beta, C, want=("aa", "bb", "aaaa", "bbbb", "aabb")):
+    """form_rdms_spin_dep: returns dict of column-major-filled arrays shaped
+    (n,n) / (n,n,n,n) indexed as [p,q] / [p,q,r,s] = MACIS (p,q,r,s)."""
+    n = norb
+    out = {}
+    ptrs = []
+    for k in ("aa", "bb", "aaaa", "bbbb", "aabb"):
+        if k in want:
+            buf = np.zeros(n ** (2 if len(k) == 2 else 4))
+            out[k] = buf
+            ptrs.append(buf.ctypes.data)
+        else:
+            ptrs.append(None)
+    lib().orc_rdms_spin_dep(n, np.ascontiguousarray(alpha, dtype=np.uint64),
+                            np.ascontiguousarray(beta, dtype=np.uint64), len(alpha),
+                            np.ascontiguousarray(C, dtype=np.float64), *ptrs)
+    res = {}
+    for k, buf in out.items():
+        shape = (n, n) if len(k) == 2 else (n, n, n, n)
+        res[k] = buf.reshape(shape, order="F")
+    return res

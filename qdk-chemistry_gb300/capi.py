@@ -1,0 +1,276 @@
+"""ctypes binding of libqdkgb.so (the C ABI in include/qdkgb.h).
+
+This is the same binding a qdk-chemistry maintainer would add on the Python
+side of the boundary.  The library is required: importing this module on a
+machine without the built library raises, and every call that needs the GPU
+raises the library's own error when no CUDA device is present.  There is no
+CPU fallback.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libqdkgb.so")
+
+OK = 0
+ERR_INVALID = 1
+ERR_CUDA = 2
+ERR_OOM = 3
+ERR_NOT_CONVERGED = 4
+ERR_UNSUPPORTED = 5
+ERR_STATE = 6
+
+LAYOUT_COLMAJOR = 0
+LAYOUT_ROWMAJOR = 1
+H_FP64 = 0
+H_SPLIT32 = 1
+PREC_FP64 = 0
+PREC_MIXED = 1
+
+EXPORTED = [
+    "qdkgb_create", "qdkgb_destroy", "qdkgb_last_error", "qdkgb_set_stream", "qdkgb_device_bytes",
+    "qdkgb_set_integrals", "qdkgb_fci_dets", "qdkgb_set_dets", "qdkgb_build_hamiltonian", "qdkgb_get_csr32",
+    "qdkgb_get_csr64", "qdkgb_diagonal", "qdkgb_spmv", "qdkgb_spmv_device", "qdkgb_davidson_default_settings",
+    "qdkgb_davidson", "qdkgb_rdms_spin_dep", "qdkgb_casci", "qdkgb_version",
+]
+
+
+class QdkgbError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("qdkgb error %d: %s" % (code, msg))
+        self.code = code
+
+
+class NotConverged(QdkgbError):
+    pass
+
+
+class DavidsonSettings(ctypes.Structure):
+    _fields_ = [("max_m", ctypes.c_int64), ("res_tol", ctypes.c_double), ("precision", ctypes.c_int),
+                ("use_guess", ctypes.c_int), ("min_abs_denominator", ctypes.c_double)]
+
+
+class DavidsonInfo(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int64), ("spmv_fp64", ctypes.c_int64), ("spmv_fp32", ctypes.c_int64),
+                ("restarts", ctypes.c_int64), ("residual_norm", ctypes.c_double), ("seconds", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_lib = None
+
+
+def lib():
+    """Load the library (it must have been built: python qdk-chemistry_gb300/build.py)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError("libqdkgb.so is not built (%s); run qdk-chemistry_gb300/build.py" % LIB_PATH)
+    L = ctypes.CDLL(LIB_PATH)
+    vp, i64, ci, dp = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_double
+    P = ctypes.POINTER
+    L.qdkgb_create.argtypes = [P(vp), ci]
+    L.qdkgb_destroy.argtypes = [vp]
+    L.qdkgb_last_error.argtypes = [vp]
+    L.qdkgb_last_error.restype = ctypes.c_char_p
+    L.qdkgb_set_stream.argtypes = [vp, vp]
+    L.qdkgb_device_bytes.argtypes = [vp, P(i64)]
+    L.qdkgb_set_integrals.argtypes = [vp, ci, vp, vp, ci]
+    L.qdkgb_fci_dets.argtypes = [ci, ci, ci, vp, vp, P(i64)]
+    L.qdkgb_set_dets.argtypes = [vp, i64, vp, vp]
+    L.qdkgb_build_hamiltonian.argtypes = [vp, dp, ci, P(i64)]
+    L.qdkgb_get_csr32.argtypes = [vp, vp, vp, vp]
+    L.qdkgb_get_csr64.argtypes = [vp, vp, vp, vp]
+    L.qdkgb_diagonal.argtypes = [vp, vp]
+    L.qdkgb_spmv.argtypes = [vp, ci, vp, vp]
+    L.qdkgb_spmv_device.argtypes = [vp, ci, vp, vp]
+    L.qdkgb_davidson_default_settings.argtypes = [P(DavidsonSettings)]
+    L.qdkgb_davidson_default_settings.restype = None
+    L.qdkgb_davidson.argtypes = [vp, P(DavidsonSettings), P(dp), vp, P(DavidsonInfo)]
+    L.qdkgb_rdms_spin_dep.argtypes = [vp, vp, vp, vp, vp, vp, vp]
+    L.qdkgb_casci.argtypes = [vp, ci, ci, ci, vp, vp, ci, P(DavidsonSettings), dp, P(dp), vp, P(DavidsonInfo)]
+    L.qdkgb_version.restype = ctypes.c_char_p
+    _lib = L
+    return L
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def fci_dets(norb, nalpha, nbeta):
+    """All determinants in MACIS order (generate_hilbert_space)."""
+    n = ctypes.c_int64()
+    rc = lib().qdkgb_fci_dets(norb, nalpha, nbeta, None, None, ctypes.byref(n))
+    if rc:
+        raise QdkgbError(rc, "invalid FCI space")
+    a = np.zeros(n.value, dtype=np.uint64)
+    b = np.zeros(n.value, dtype=np.uint64)
+    rc = lib().qdkgb_fci_dets(norb, nalpha, nbeta, _ptr(a), _ptr(b), ctypes.byref(n))
+    if rc:
+        raise QdkgbError(rc, "fci_dets failed")
+    return a, b
+
+
+def default_davidson_settings():
+    s = DavidsonSettings()
+    lib().qdkgb_davidson_default_settings(ctypes.byref(s))
+    return s
+
+
+class Context:
+    """One GPU context: integrals, determinant space, device CSR, solver workspace."""
+
+    def __init__(self, device=0):
+        L = lib()
+        h = ctypes.c_void_p()
+        rc = L.qdkgb_create(ctypes.byref(h), device)
+        if rc:
+            raise QdkgbError(rc, "qdkgb_create failed (no usable CUDA device?)")
+        self._h = h
+        self.norb = None
+        self.ndets = None
+        self.nnz = None
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().qdkgb_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc):
+        if rc:
+            msg = lib().qdkgb_last_error(self._h).decode()
+            if rc == ERR_NOT_CONVERGED:
+                raise NotConverged(rc, msg)
+            raise QdkgbError(rc, msg)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def device_bytes(self):
+        b = ctypes.c_int64()
+        self._check(lib().qdkgb_device_bytes(self._h, ctypes.byref(b)))
+        return b.value
+
+    def set_stream(self, stream_ptr):
+        self._check(lib().qdkgb_set_stream(self._h, stream_ptr))
+
+    def set_integrals(self, T, V, layout=LAYOUT_COLMAJOR):
+        """T, V as numpy arrays indexed [p,q] / [p,q,r,s]; passed column-major."""
+        T = np.asarray(T, dtype=np.float64)
+        V = np.asarray(V, dtype=np.float64)
+        n = T.shape[0]
+        if layout == LAYOUT_COLMAJOR:
+            Tb = _f64(T.ravel(order="F"))
+            Vb = _f64(V.ravel(order="F"))
+        else:
+            Tb = _f64(T.ravel(order="C"))
+            Vb = _f64(V.ravel(order="C"))
+        self._check(lib().qdkgb_set_integrals(self._h, n, _ptr(Tb), _ptr(Vb), layout))
+        self.norb = n
+
+    def set_dets(self, alpha, beta):
+        alpha = np.ascontiguousarray(alpha, dtype=np.uint64)
+        beta = np.ascontiguousarray(beta, dtype=np.uint64)
+        self._check(lib().qdkgb_set_dets(self._h, len(alpha), _ptr(alpha), _ptr(beta)))
+        self.ndets = len(alpha)
+
+    def build_hamiltonian(self, thresh=np.finfo(np.float64).eps, storage=H_FP64):
+        nnz = ctypes.c_int64()
+        self._check(lib().qdkgb_build_hamiltonian(self._h, float(thresh), storage, ctypes.byref(nnz)))
+        self.nnz = nnz.value
+        return self.nnz
+
+    def get_csr(self, index_bits=64):
+        n, nnz = self.ndets, self.nnz
+        it = np.int64 if index_bits == 64 else np.int32
+        rp = np.zeros(n + 1, dtype=it)
+        ci = np.zeros(nnz, dtype=it)
+        nz = np.zeros(nnz, dtype=np.float64)
+        fn = lib().qdkgb_get_csr64 if index_bits == 64 else lib().qdkgb_get_csr32
+        self._check(fn(self._h, _ptr(rp), _ptr(ci), _ptr(nz)))
+        return rp, ci, nz
+
+    def diagonal(self):
+        d = np.zeros(self.ndets)
+        self._check(lib().qdkgb_diagonal(self._h, _ptr(d)))
+        return d
+
+    def spmv(self, x, precision=PREC_FP64):
+        x = _f64(x)
+        y = np.zeros(self.ndets)
+        self._check(lib().qdkgb_spmv(self._h, precision, _ptr(x), _ptr(y)))
+        return y
+
+    def spmv_device(self, x_ptr, y_ptr, precision=PREC_FP64):
+        self._check(lib().qdkgb_spmv_device(self._h, precision, x_ptr, y_ptr))
+
+    def davidson(self, max_m=200, tol=1e-8, precision=PREC_FP64, guess=None):
+        s = default_davidson_settings()
+        s.max_m = max_m
+        s.res_tol = tol
+        s.precision = precision
+        C = np.zeros(self.ndets) if guess is None else _f64(guess).copy()
+        s.use_guess = 0 if guess is None else 1
+        E = ctypes.c_double()
+        info = DavidsonInfo()
+        self._check(lib().qdkgb_davidson(self._h, ctypes.byref(s), ctypes.byref(E), _ptr(C), ctypes.byref(info)))
+        return E.value, C, info.as_dict()
+
+    def rdms_spin_dep(self, C, want=("aa", "bb", "aaaa", "bbbb", "aabb")):
+        n = self.norb
+        C = _f64(C)
+        bufs = {}
+        ptrs = []
+        for k in ("aa", "bb", "aaaa", "bbbb", "aabb"):
+            if k in want:
+                bufs[k] = np.zeros(n ** (2 if len(k) == 2 else 4))
+                ptrs.append(_ptr(bufs[k]))
+            else:
+                ptrs.append(None)
+        self._check(lib().qdkgb_rdms_spin_dep(self._h, _ptr(C), *ptrs))
+        return {k: v.reshape((n, n) if len(k) == 2 else (n, n, n, n), order="F") for k, v in bufs.items()}
+
+    def casci(self, T, V, nalpha, nbeta, max_m=200, tol=1e-8, precision=PREC_FP64, matel_tol=np.finfo(float).eps,
+              want_vector=True):
+        T = np.asarray(T, dtype=np.float64)
+        V = np.asarray(V, dtype=np.float64)
+        n = T.shape[0]
+        Tb = _f64(T.ravel(order="F"))
+        Vb = _f64(V.ravel(order="F"))
+        s = default_davidson_settings()
+        s.max_m = max_m
+        s.res_tol = tol
+        s.precision = precision
+        nd = ctypes.c_int64()
+        lib().qdkgb_fci_dets(n, nalpha, nbeta, None, None, ctypes.byref(nd))
+        C = np.zeros(nd.value) if want_vector else None
+        E = ctypes.c_double()
+        info = DavidsonInfo()
+        self._check(lib().qdkgb_casci(self._h, n, nalpha, nbeta, _ptr(Tb), _ptr(Vb), LAYOUT_COLMAJOR,
+                                      ctypes.byref(s), float(matel_tol), ctypes.byref(E), _ptr(C),
+                                      ctypes.byref(info)))
+        self.norb = n
+        self.ndets = nd.value
+        return E.value, C, info.as_dict()

@@ -1,0 +1,357 @@
+// C ABI entry points (include/qdkgb.h).  Every function converts internal
+// exceptions into a status code plus a message kept in the context.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "internal.h"
+
+namespace qdkgb {
+
+void* dev_alloc(Context* c, DeviceBuffer& b, size_t bytes) {
+  if (b.ptr && b.bytes >= bytes) return b.ptr;
+  dev_free(c, b);
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, std::max<size_t>(bytes, 16));
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    throw Error(QDKGB_ERR_OOM, "cudaMalloc of " + std::to_string(bytes) + " bytes failed: " + cudaGetErrorString(e));
+  }
+  b.ptr = p;
+  b.bytes = bytes;
+  c->dev_bytes += (int64_t)bytes;
+  return p;
+}
+
+void dev_free(Context* c, DeviceBuffer& b) {
+  if (b.ptr) {
+    cudaFree(b.ptr);
+    c->dev_bytes -= (int64_t)b.bytes;
+  }
+  b.ptr = nullptr;
+  b.bytes = 0;
+}
+
+// generate_combs (sd_operations.hpp:305-323): std::prev_permutation order,
+// i.e. combinations of occupied positions in lexicographic order.
+static std::vector<uint64_t> combs(int nbits, int nset) {
+  std::vector<uint64_t> out;
+  std::vector<int> pos(nset);
+  for (int i = 0; i < nset; ++i) pos[i] = i;
+  while (true) {
+    uint64_t s = 0;
+    for (int p : pos) s |= 1ull << p;
+    out.push_back(s);
+    int i = nset - 1;
+    while (i >= 0 && pos[i] == nbits - nset + i) --i;
+    if (i < 0) break;
+    pos[i]++;
+    for (int j = i + 1; j < nset; ++j) pos[j] = pos[j - 1] + 1;
+  }
+  return out;
+}
+
+static int64_t binom(int n, int k) {
+  if (k < 0 || k > n) return 0;
+  long double r = 1;
+  for (int i = 1; i <= k; ++i) r = r * (n - k + i) / i;
+  return (int64_t)std::llround(r);
+}
+
+}  // namespace qdkgb
+
+using namespace qdkgb;
+
+template <class F>
+static int guarded(qdkgb_context* ctx, F&& f) {
+  try {
+    f();
+    if (ctx) ctx->err.clear();
+    return QDKGB_OK;
+  } catch (const Error& e) {
+    if (ctx) ctx->err = e.what();
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    if (ctx) ctx->err = "host allocation failed";
+    return QDKGB_ERR_OOM;
+  } catch (const std::exception& e) {
+    if (ctx) ctx->err = e.what();
+    return QDKGB_ERR_INVALID;
+  }
+}
+
+template <typename I>
+static void get_csr(Context* c, I* rowptr, I* colind, double* values) {
+  Hcsr& H = c->H;
+  if (!H.valid) throw Error(QDKGB_ERR_STATE, "Hamiltonian not built");
+  if (sizeof(I) == 4 && H.nnz > INT32_MAX) throw Error(QDKGB_ERR_UNSUPPORTED, "nnz exceeds int32");
+  std::vector<int64_t> rp(H.n + 1);
+  QDKGB_CUDA(cudaMemcpyAsync(rp.data(), H.rowptr.ptr, (H.n + 1) * 8, cudaMemcpyDeviceToHost, c->stream));
+  std::vector<int32_t> ci;
+  if (colind) {
+    ci.resize(H.nnz);
+    QDKGB_CUDA(cudaMemcpyAsync(ci.data(), H.colind.ptr, H.nnz * 4, cudaMemcpyDeviceToHost, c->stream));
+  }
+  if (values) {
+    if (H.storage == QDKGB_H_FP64) {
+      QDKGB_CUDA(cudaMemcpyAsync(values, H.val.ptr, H.nnz * 8, cudaMemcpyDeviceToHost, c->stream));
+    } else {
+      DeviceBuffer tmp;
+      double* d = dev_array<double>(c, tmp, H.nnz);
+      csr_values_to_double(c, d);
+      QDKGB_CUDA(cudaMemcpyAsync(values, d, H.nnz * 8, cudaMemcpyDeviceToHost, c->stream));
+      QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+      dev_free(c, tmp);
+    }
+  }
+  QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+  if (rowptr)
+    for (int64_t i = 0; i <= H.n; ++i) rowptr[i] = (I)rp[i];
+  if (colind)
+    for (int64_t i = 0; i < H.nnz; ++i) colind[i] = (I)ci[i];
+}
+
+extern "C" {
+
+const char* qdkgb_version(void) { return "qdkgb 0.1 (sm_103a)"; }
+
+int qdkgb_create(qdkgb_context** out, int device) {
+  if (!out) return QDKGB_ERR_INVALID;
+  *out = nullptr;
+  qdkgb_context* c = new (std::nothrow) qdkgb_context();
+  if (!c) return QDKGB_ERR_OOM;
+  int rc = guarded(c, [&] {
+    int ndev = 0;
+    QDKGB_CUDA(cudaGetDeviceCount(&ndev));
+    if (device < 0 || device >= ndev) throw Error(QDKGB_ERR_INVALID, "no such CUDA device");
+    QDKGB_CUDA(cudaSetDevice(device));
+    c->device = device;
+    QDKGB_CUDA(cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device));
+    QDKGB_CUDA(cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking));
+    c->stream = c->own_stream;
+    QDKGB_CUDA(cudaMallocHost((void**)&c->pinned, 64 * sizeof(double)));
+  });
+  if (rc != QDKGB_OK) {
+    delete c;
+    return rc;
+  }
+  *out = c;
+  return QDKGB_OK;
+}
+
+int qdkgb_destroy(qdkgb_context* c) {
+  if (!c) return QDKGB_OK;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  for (DeviceBuffer* b : {&c->T, &c->V, &c->G_red, &c->V_red, &c->G2, &c->V2, &c->dets.galpha, &c->dets.gstart,
+                          &c->dets.det_group, &c->dets.brank, &c->dets.ubeta, &c->dets.gcomplete, &c->dets.acon_ptr,
+                          &c->dets.acon_idx, &c->dets.acon_lvl, &c->dets.b2_ptr, &c->dets.b2_idx, &c->dets.b1_ptr,
+                          &c->dets.b1_idx, &c->H.rowptr, &c->H.colind, &c->H.val, &c->H.hi, &c->H.lo, &c->H.diag,
+                          &c->H.row_nnz, &c->H.scan_tmp, &c->dav.V, &c->dav.AV, &c->dav.xf, &c->dav.yf, &c->dav.Hk,
+                          &c->dav.evec, &c->dav.eval, &c->dav.scratch, &c->dav.partial, &c->dav.small})
+    dev_free(c, *b);
+  if (c->pinned) cudaFreeHost(c->pinned);
+  if (c->own_stream) cudaStreamDestroy(c->own_stream);
+  delete c;
+  return QDKGB_OK;
+}
+
+const char* qdkgb_last_error(const qdkgb_context* c) { return c ? c->err.c_str() : "null context"; }
+
+int qdkgb_set_stream(qdkgb_context* c, void* stream) {
+  if (!c) return QDKGB_ERR_INVALID;
+  return guarded(c, [&] {
+    QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+    c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+  });
+}
+
+int qdkgb_device_bytes(const qdkgb_context* c, int64_t* bytes) {
+  if (!c || !bytes) return QDKGB_ERR_INVALID;
+  *bytes = c->dev_bytes;
+  return QDKGB_OK;
+}
+
+int qdkgb_set_integrals(qdkgb_context* c, int norb, const double* T, const double* V, int layout) {
+  if (!c) return QDKGB_ERR_INVALID;
+  return guarded(c, [&] {
+    if (norb <= 0 || norb > 64) throw Error(QDKGB_ERR_INVALID, "norb must be in [1, 64]");
+    if (!T || !V) throw Error(QDKGB_ERR_INVALID, "null integral buffer");
+    if (layout != QDKGB_LAYOUT_COLMAJOR && layout != QDKGB_LAYOUT_ROWMAJOR)
+      throw Error(QDKGB_ERR_INVALID, "unknown integral layout");
+    QDKGB_CUDA(cudaSetDevice(c->device));
+    const size_t n = norb, n2 = n * n, n4 = n2 * n2;
+    c->h_T.resize(n2);
+    c->h_V.resize(n4);
+    if (layout == QDKGB_LAYOUT_COLMAJOR) {
+      std::memcpy(c->h_T.data(), T, n2 * 8);
+      std::memcpy(c->h_V.data(), V, n4 * 8);
+    } else {
+      // qdk's row-major i*n^3 + j*n^2 + k*n + l buffer -> column-major
+      for (size_t p = 0; p < n; ++p)
+        for (size_t q = 0; q < n; ++q) c->h_T[p + n * q] = T[p * n + q];
+      for (size_t p = 0; p < n; ++p)
+        for (size_t q = 0; q < n; ++q)
+          for (size_t r = 0; r < n; ++r)
+            for (size_t s = 0; s < n; ++s) c->h_V[p + n * (q + n * (r + n * s))] = V[((p * n + q) * n + r) * n + s];
+    }
+    c->norb = norb;
+    build_integral_intermediates(c);
+    c->have_ints = true;
+    c->H.valid = false;
+  });
+}
+
+int qdkgb_fci_dets(int norb, int nalpha, int nbeta, uint64_t* alpha, uint64_t* beta, int64_t* ndets) {
+  if (norb <= 0 || norb > 64 || nalpha < 0 || nbeta < 0 || nalpha > norb || nbeta > norb || !ndets)
+    return QDKGB_ERR_INVALID;
+  const int64_t na = binom(norb, nalpha), nb = binom(norb, nbeta);
+  *ndets = na * nb;
+  if (!alpha) return QDKGB_OK;
+  if (!beta) return QDKGB_ERR_INVALID;
+  try {
+    std::vector<uint64_t> A = combs(norb, nalpha), B = combs(norb, nbeta);
+    for (int64_t i = 0; i < na; ++i)
+      for (int64_t j = 0; j < nb; ++j) {
+        alpha[i * nb + j] = A[i];
+        beta[i * nb + j] = B[j];
+      }
+  } catch (...) {
+    return QDKGB_ERR_OOM;
+  }
+  return QDKGB_OK;
+}
+
+int qdkgb_set_dets(qdkgb_context* c, int64_t ndets, const uint64_t* alpha, const uint64_t* beta) {
+  if (!c) return QDKGB_ERR_INVALID;
+  return guarded(c, [&] {
+    if (!alpha || !beta) throw Error(QDKGB_ERR_INVALID, "null determinant buffer");
+    QDKGB_CUDA(cudaSetDevice(c->device));
+    build_det_space(c, ndets, alpha, beta);
+  });
+}
+
+int qdkgb_build_hamiltonian(qdkgb_context* c, double thresh, int storage, int64_t* nnz) {
+  if (!c) return QDKGB_ERR_INVALID;
+  return guarded(c, [&] {
+    QDKGB_CUDA(cudaSetDevice(c->device));
+    build_hamiltonian(c, thresh, storage);
+    if (nnz) *nnz = c->H.nnz;
+  });
+}
+
+int qdkgb_get_csr32(qdkgb_context* c, int32_t* rowptr, int32_t* colind, double* values) {
+  if (!c) return QDKGB_ERR_INVALID;
+  return guarded(c, [&] { get_csr<int32_t>(c, rowptr, colind, values); });
+}
+int qdkgb_get_csr64(qdkgb_context* c, int64_t* rowptr, int64_t* colind, double* values) {
+  if (!c) return QDKGB_ERR_INVALID;
+  return guarded(c, [&] { get_csr<int64_t>(c, rowptr, colind, values); });
+}
+
+int qdkgb_diagonal(qdkgb_context* c, double* D) {
+  if (!c) return QDKGB_ERR_INVALID;
+  return guarded(c, [&] {
+    if (!c->H.valid) throw Error(QDKGB_ERR_STATE, "Hamiltonian not built");
+    QDKGB_CUDA(cudaMemcpyAsync(D, c->H.diag.ptr, c->H.n * 8, cudaMemcpyDeviceToHost, c->stream));
+    QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+  });
+}
+
+int qdkgb_spmv_device(qdkgb_context* c, int precision, const void* x, void* y) {
+  if (!c) return QDKGB_ERR_INVALID;
+  return guarded(c, [&] {
+    if (precision == QDKGB_PREC_FP64)
+      spmv_fp64(c, (const double*)x, (double*)y);
+    else if (precision == QDKGB_PREC_MIXED)
+      spmv_fp32(c, (const float*)x, (float*)y);
+    else
+      throw Error(QDKGB_ERR_INVALID, "unknown precision");
+  });
+}
+
+int qdkgb_spmv(qdkgb_context* c, int precision, const double* x, double* y) {
+  if (!c) return QDKGB_ERR_INVALID;
+  return guarded(c, [&] {
+    Hcsr& H = c->H;
+    if (!H.valid) throw Error(QDKGB_ERR_STATE, "Hamiltonian not built");
+    DeviceBuffer bx, by;
+    const int64_t n = H.n;
+    double* dx = dev_array<double>(c, bx, n);
+    double* dy = dev_array<double>(c, by, n);
+    QDKGB_CUDA(cudaMemcpyAsync(dx, x, n * 8, cudaMemcpyHostToDevice, c->stream));
+    if (precision == QDKGB_PREC_FP64) {
+      spmv_fp64(c, dx, dy);
+    } else if (precision == QDKGB_PREC_MIXED) {
+      DeviceBuffer bf;
+      float* xf = dev_array<float>(c, bf, 2 * n);
+      f64_to_f32(c, dx, xf, n);
+      spmv_fp32(c, xf, xf + n);
+      f32_to_f64(c, xf + n, dy, n);
+      QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+      dev_free(c, bf);
+    } else {
+      throw Error(QDKGB_ERR_INVALID, "unknown precision");
+    }
+    QDKGB_CUDA(cudaMemcpyAsync(y, dy, n * 8, cudaMemcpyDeviceToHost, c->stream));
+    QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+    dev_free(c, bx);
+    dev_free(c, by);
+  });
+}
+
+void qdkgb_davidson_default_settings(qdkgb_davidson_settings* s) {
+  if (!s) return;
+  s->max_m = 200;
+  s->res_tol = 1e-8;
+  s->precision = QDKGB_PREC_FP64;
+  s->use_guess = 0;
+  s->min_abs_denominator = 1e-12;
+}
+
+int qdkgb_davidson(qdkgb_context* c, const qdkgb_davidson_settings* s, double* E, double* C,
+                   qdkgb_davidson_info* info) {
+  if (!c) return QDKGB_ERR_INVALID;
+  return guarded(c, [&] {
+    if (!E) throw Error(QDKGB_ERR_INVALID, "null energy pointer");
+    qdkgb_davidson_settings def;
+    qdkgb_davidson_default_settings(&def);
+    QDKGB_CUDA(cudaSetDevice(c->device));
+    davidson(c, s ? s : &def, E, C, info);
+  });
+}
+
+int qdkgb_rdms_spin_dep(qdkgb_context* c, const double* C, double* aa, double* bb, double* aaaa, double* bbbb,
+                        double* aabb) {
+  if (!c) return QDKGB_ERR_INVALID;
+  return guarded(c, [&] {
+    if (!C) throw Error(QDKGB_ERR_INVALID, "null CI vector");
+    if (!c->have_dets) throw Error(QDKGB_ERR_STATE, "determinants not set");
+    QDKGB_CUDA(cudaSetDevice(c->device));
+    rdms_spin_dep(c, C, aa, bb, aaaa, bbbb, aabb);
+  });
+}
+
+int qdkgb_casci(qdkgb_context* c, int norb, int nalpha, int nbeta, const double* T, const double* V, int layout,
+                const qdkgb_davidson_settings* s, double matel_tol, double* E, double* C,
+                qdkgb_davidson_info* info) {
+  if (!c) return QDKGB_ERR_INVALID;
+  int rc = qdkgb_set_integrals(c, norb, T, V, layout);
+  if (rc) return rc;
+  int64_t nd = 0;
+  rc = qdkgb_fci_dets(norb, nalpha, nbeta, nullptr, nullptr, &nd);
+  if (rc) return rc;
+  return guarded(c, [&] {
+    std::vector<uint64_t> a(nd), b(nd);
+    if (qdkgb_fci_dets(norb, nalpha, nbeta, a.data(), b.data(), &nd)) throw Error(QDKGB_ERR_INVALID, "fci dets");
+    build_det_space(c, nd, a.data(), b.data());
+    qdkgb_davidson_settings def;
+    qdkgb_davidson_default_settings(&def);
+    const qdkgb_davidson_settings* ss = s ? s : &def;
+    build_hamiltonian(c, matel_tol, ss->precision == QDKGB_PREC_MIXED ? QDKGB_H_SPLIT32 : QDKGB_H_FP64);
+    davidson(c, ss, E, C, info);
+  });
+}
+
+}  // extern "C"

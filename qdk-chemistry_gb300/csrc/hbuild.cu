@@ -1,0 +1,480 @@
+// Determinant-space preparation and the CSR Hamiltonian build.
+//
+// Replaces SortedDoubleLoopHamiltonianGenerator::make_csr_hamiltonian_block_
+// (include/macis/hamiltonian_generator/sorted_double_loop.hpp:86-451).
+//
+// GPU design (not a translation of the reference's loops): the reference
+// visits alpha-group pairs and then all beta x beta pairs of the two groups,
+// testing each with a popcount, fills with atomic slot capture and sorts each
+// row afterwards.  Here one warp owns one CSR row and generates only the
+// connected columns, already in ascending order:
+//   * alpha groups connected to the row's group (<= 4 differing bits) come
+//     from a precomputed, sorted alpha-connectivity list, tagged with their
+//     excitation level e_a in {0,1,2};
+//   * inside a connected group the admissible beta strings are those within
+//     level 2 - e_a of the row's beta string; they come from precomputed,
+//     sorted beta-connectivity lists (level <= 1 and level <= 2) and are
+//     located in the group by identity (groups holding every beta string),
+//     by binary search, or by a direct scan of small groups;
+//   * the row's candidate list is the concatenation of these per-group lists;
+//     the 32 lanes walk it as one flat index space (load-balanced across the
+//     uneven per-group sizes), evaluate the Slater-Condon element, apply the
+//     strict |h| > thresh rule, and compact survivors with a ballot.
+// A count pass and an emit pass run the same code; an exclusive scan between
+// them gives the row pointers.  No sort and no atomics are needed, and the
+// result is deterministic.
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+#include <queue>
+#include <unordered_map>
+
+#include "common.cuh"
+#include "internal.h"
+#include "rowwalk.cuh"
+
+namespace qdkgb {
+
+// ------------------------------------------------------------------ integrals
+// generate_integral_intermediates_ (src/macis/hamiltonian_generator/base.ipp:38-77)
+__global__ void k_intermediates(int n, const double* __restrict__ V, double* G_red, double* V_red, double* G2,
+                                double* V2) {
+  const size_t nn = (size_t)n;
+  const int64_t total = (int64_t)n * n * n;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int k = (int)(t % n), i = (int)((t / n) % n), j = (int)(t / (nn * nn));
+    auto v = [&](int p, int q, int r, int s) { return V[p + nn * (q + nn * (r + nn * s))]; };
+    G_red[t] = v(k, k, i, j) - v(k, j, i, k);
+    V_red[t] = v(k, k, i, j);
+    if (k == 0) {
+      G2[i + nn * j] = 0.5 * (v(i, i, j, j) - v(i, j, j, i));
+      V2[i + nn * j] = v(i, i, j, j);
+    }
+  }
+}
+
+void build_integral_intermediates(Context* c) {
+  const int n = c->norb;
+  const size_t n2 = (size_t)n * n, n3 = n2 * n, n4 = n3 * n;
+  double* T = dev_array<double>(c, c->T, n2);
+  double* V = dev_array<double>(c, c->V, n4);
+  double* G = dev_array<double>(c, c->G_red, n3);
+  double* Vr = dev_array<double>(c, c->V_red, n3);
+  double* G2 = dev_array<double>(c, c->G2, n2);
+  double* V2 = dev_array<double>(c, c->V2, n2);
+  QDKGB_CUDA(cudaMemcpyAsync(T, c->h_T.data(), n2 * 8, cudaMemcpyHostToDevice, c->stream));
+  QDKGB_CUDA(cudaMemcpyAsync(V, c->h_V.data(), n4 * 8, cudaMemcpyHostToDevice, c->stream));
+  int blocks = (int)std::min<int64_t>((n3 + 255) / 256, 4096);
+  k_intermediates<<<blocks, 256, 0, c->stream>>>(n, V, G, Vr, G2, V2);
+  QDKGB_CHECK_LAUNCH();
+  QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+}
+
+Integrals integrals_view(Context* c) {
+  Integrals I;
+  I.T = (const double*)c->T.ptr;
+  I.V = (const double*)c->V.ptr;
+  I.G_red = (const double*)c->G_red.ptr;
+  I.V_red = (const double*)c->V_red.ptr;
+  I.G2 = (const double*)c->G2.ptr;
+  I.V2 = (const double*)c->V2.ptr;
+  I.n = c->norb;
+  return I;
+}
+
+// ------------------------------------------------------------------ scan
+__global__ void k_scan_block_sums(const int64_t* in, int64_t n, int64_t* sums) {
+  __shared__ int64_t s[32];
+  const int64_t base = (int64_t)blockIdx.x * 1024;
+  int64_t v = 0;
+  for (int k = threadIdx.x; k < 1024; k += blockDim.x)
+    if (base + k < n) v += in[base + k];
+  v = warp_sum(v);
+  if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    int64_t w = (threadIdx.x < (blockDim.x >> 5)) ? s[threadIdx.x] : 0;
+    w = warp_sum(w);
+    if (threadIdx.x == 0) sums[blockIdx.x] = w;
+  }
+}
+// single block: exclusive scan of the block sums, in place; total at sums[nb]
+__global__ void k_scan_sums(int64_t* sums, int64_t nb) {
+  __shared__ int64_t carry;
+  __shared__ int64_t warp_tot[32];
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int64_t base = 0; base < nb; base += blockDim.x) {
+    const int64_t i = base + threadIdx.x;
+    int64_t v = (i < nb) ? sums[i] : 0, incl = v;
+    for (int d = 1; d < 32; d <<= 1) {
+      int64_t t = __shfl_up_sync(QDKGB_FULL_MASK, incl, d);
+      if (lane >= d) incl += t;
+    }
+    if (lane == 31) warp_tot[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+      int64_t t = (lane < (int)(blockDim.x >> 5)) ? warp_tot[lane] : 0, ti = t;
+      for (int d = 1; d < 32; d <<= 1) {
+        int64_t u = __shfl_up_sync(QDKGB_FULL_MASK, ti, d);
+        if (lane >= d) ti += u;
+      }
+      warp_tot[lane] = ti - t;
+    }
+    __syncthreads();
+    const int64_t excl = carry + warp_tot[w] + incl - v;
+    __syncthreads();
+    if (i < nb) sums[i] = excl;
+    if (threadIdx.x == blockDim.x - 1) carry = excl + v;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) sums[nb] = carry;
+}
+__global__ void k_scan_apply(const int64_t* in, int64_t n, const int64_t* sums, int64_t* out) {
+  // one block of 1024 threads per 1024 elements
+  __shared__ int64_t warp_tot[32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t i = (int64_t)blockIdx.x * 1024 + threadIdx.x;
+  int64_t v = (i < n) ? in[i] : 0, incl = v;
+  for (int d = 1; d < 32; d <<= 1) {
+    int64_t t = __shfl_up_sync(QDKGB_FULL_MASK, incl, d);
+    if (lane >= d) incl += t;
+  }
+  if (lane == 31) warp_tot[w] = incl;
+  __syncthreads();
+  if (w == 0) {
+    int64_t t = warp_tot[lane], ti = t;
+    for (int d = 1; d < 32; d <<= 1) {
+      int64_t u = __shfl_up_sync(QDKGB_FULL_MASK, ti, d);
+      if (lane >= d) ti += u;
+    }
+    warp_tot[lane] = ti - t;
+  }
+  __syncthreads();
+  if (i < n) out[i] = sums[blockIdx.x] + warp_tot[w] + incl - v;
+  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) out[n] = sums[gridDim.x];
+}
+
+// out[0..n] = exclusive scan of in[0..n), out[n] = total.
+void exclusive_scan_i64(Context* c, const int64_t* in, int64_t* out, int64_t n, DeviceBuffer& tmp) {
+  const int64_t nb = std::max<int64_t>(1, (n + 1023) / 1024);
+  int64_t* sums = dev_array<int64_t>(c, tmp, nb + 1);
+  k_scan_block_sums<<<(unsigned)nb, 256, 0, c->stream>>>(in, n, sums);
+  QDKGB_CHECK_LAUNCH();
+  k_scan_sums<<<1, 1024, 0, c->stream>>>(sums, nb);
+  QDKGB_CHECK_LAUNCH();
+  k_scan_apply<<<(unsigned)nb, 1024, 0, c->stream>>>(in, n, sums, out);
+  QDKGB_CHECK_LAUNCH();
+}
+
+// ------------------------------------------------------------------ string connectivity
+// For every string i, the sorted list of strings j with popc(s_i ^ s_j) <=
+// maxbits.  skip_zero drops the empty string on both sides (the reference
+// skips alpha groups whose string has no electrons,
+// sorted_double_loop.hpp:145,153).  Warp per i, ballot compaction.
+template <bool EMIT>
+__global__ void k_conn(const uint64_t* __restrict__ s, int64_t m, int maxbits, bool skip_zero, int64_t* cnt,
+                       const int64_t* ptr, int32_t* idx, int8_t* lvl) {
+  const int lane = threadIdx.x & 31;
+  const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t i = wid; i < m; i += nw) {
+    const uint64_t si = s[i];
+    int64_t out = EMIT ? ptr[i] : 0;
+    int64_t c = 0;
+    const bool dead = skip_zero && si == 0;
+    for (int64_t j0 = 0; j0 < m && !dead; j0 += 32) {
+      const int64_t j = j0 + lane;
+      bool hit = false;
+      int d = 0;
+      if (j < m) {
+        const uint64_t sj = s[j];
+        d = popc64(si ^ sj);
+        hit = d <= maxbits && !(skip_zero && sj == 0);
+      }
+      const unsigned b = __ballot_sync(QDKGB_FULL_MASK, hit);
+      if (EMIT && hit) {
+        const int64_t pos = out + c + __popc(b & ((1u << lane) - 1u));
+        idx[pos] = (int32_t)j;
+        if (lvl) lvl[pos] = (int8_t)(d >> 1);
+      }
+      c += __popc(b);
+    }
+    if (!EMIT && lane == 0) cnt[i] = c;
+  }
+}
+
+static void build_conn(Context* c, const uint64_t* d_s, int64_t m, int maxbits, bool skip_zero, DeviceBuffer& ptr,
+                       DeviceBuffer& idx, DeviceBuffer* lvl, int64_t& total) {
+  DeviceBuffer cnt, tmp;
+  int64_t* d_cnt = dev_array<int64_t>(c, cnt, m + 1);
+  int64_t* d_ptr = dev_array<int64_t>(c, ptr, m + 1);
+  const int threads = 256;
+  const int64_t blocks = std::min<int64_t>((m * 32 + threads - 1) / threads, (int64_t)c->sm_count * 64);
+  k_conn<false><<<(unsigned)blocks, threads, 0, c->stream>>>(d_s, m, maxbits, skip_zero, d_cnt, nullptr, nullptr,
+                                                             nullptr);
+  QDKGB_CHECK_LAUNCH();
+  exclusive_scan_i64(c, d_cnt, d_ptr, m, tmp);
+  QDKGB_CUDA(cudaMemcpyAsync(&total, d_ptr + m, sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
+  QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+  int32_t* d_idx = dev_array<int32_t>(c, idx, std::max<int64_t>(total, 1));
+  int8_t* d_lvl = lvl ? dev_array<int8_t>(c, *lvl, std::max<int64_t>(total, 1)) : nullptr;
+  k_conn<true><<<(unsigned)blocks, threads, 0, c->stream>>>(d_s, m, maxbits, skip_zero, nullptr, d_ptr, d_idx, d_lvl);
+  QDKGB_CHECK_LAUNCH();
+  QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+  dev_free(c, cnt);
+  dev_free(c, tmp);
+}
+
+// ------------------------------------------------------------------ determinant space
+// Host part: alpha runs (get_unique_alpha, sd_operations.hpp:449-468) and a
+// single order on the distinct beta strings that every group's beta sequence
+// follows.  Tried in turn: ascending integer order (lists sorted by
+// spin_comparator), the common sequence of a full product space
+// (generate_hilbert_space), and a topological order of the per-group
+// successions.
+void build_det_space(Context* c, int64_t nd, const uint64_t* alpha, const uint64_t* beta) {
+  DetSpace& D = c->dets;
+  for (DeviceBuffer* b : {&D.galpha, &D.gstart, &D.det_group, &D.brank, &D.ubeta, &D.gcomplete, &D.acon_ptr,
+                          &D.acon_idx, &D.acon_lvl, &D.b2_ptr, &D.b2_idx, &D.b1_ptr, &D.b1_idx})
+    dev_free(c, *b);
+  D = DetSpace();
+  c->have_dets = false;
+  c->H.valid = false;
+  if (nd <= 0) throw Error(QDKGB_ERR_INVALID, "empty determinant list");
+  if (nd >= (int64_t)INT32_MAX) throw Error(QDKGB_ERR_UNSUPPORTED, "more than 2^31-1 determinants");
+  D.ndets = nd;
+  D.h_alpha.assign(alpha, alpha + nd);
+  D.h_beta.assign(beta, beta + nd);
+  D.h_gstart.push_back(0);
+  D.h_galpha.push_back(alpha[0]);
+  for (int64_t i = 1; i < nd; ++i)
+    if (alpha[i] != alpha[i - 1]) {
+      D.h_galpha.push_back(alpha[i]);
+      D.h_gstart.push_back(i);
+    }
+  D.h_gstart.push_back(nd);
+  D.ngroups = (int64_t)D.h_galpha.size();
+  const int64_t G = D.ngroups;
+
+  std::vector<uint64_t> ubeta;
+  std::vector<int32_t> brank(nd);
+  bool ascending = true;
+  for (int64_t g = 0; g < G && ascending; ++g)
+    for (int64_t i = D.h_gstart[g] + 1; i < D.h_gstart[g + 1]; ++i)
+      if (!(beta[i - 1] < beta[i])) {
+        ascending = false;
+        break;
+      }
+  if (ascending) {
+    ubeta.assign(beta, beta + nd);
+    std::sort(ubeta.begin(), ubeta.end());
+    ubeta.erase(std::unique(ubeta.begin(), ubeta.end()), ubeta.end());
+    for (int64_t i = 0; i < nd; ++i)
+      brank[i] = (int32_t)(std::lower_bound(ubeta.begin(), ubeta.end(), beta[i]) - ubeta.begin());
+  } else {
+    // product space: every group repeats group 0's beta sequence
+    const int64_t s0 = D.h_gstart[1];
+    bool product = (nd % s0) == 0 && G * s0 == nd;
+    for (int64_t g = 1; g < G && product; ++g) {
+      if (D.h_gstart[g + 1] - D.h_gstart[g] != s0) product = false;
+      for (int64_t k = 0; k < s0 && product; ++k)
+        if (beta[D.h_gstart[g] + k] != beta[k]) product = false;
+    }
+    std::unordered_map<uint64_t, int32_t> rank;
+    if (product) {
+      ubeta.assign(beta, beta + s0);
+      for (int64_t k = 0; k < s0; ++k)
+        if (!rank.emplace(beta[k], (int32_t)k).second)
+          throw Error(QDKGB_ERR_UNSUPPORTED, "repeated determinant in the list");
+    } else {
+      // topological order of "b precedes b'" edges from consecutive dets of each group
+      std::unordered_map<uint64_t, int32_t> id;
+      std::vector<uint64_t> strs;
+      for (int64_t i = 0; i < nd; ++i)
+        if (id.emplace(beta[i], (int32_t)strs.size()).second) strs.push_back(beta[i]);
+      const int64_t U = (int64_t)strs.size();
+      std::vector<std::vector<int32_t>> succ(U);
+      std::vector<int32_t> indeg(U, 0);
+      for (int64_t g = 0; g < G; ++g)
+        for (int64_t i = D.h_gstart[g] + 1; i < D.h_gstart[g + 1]; ++i) {
+          const int32_t a = id[beta[i - 1]], b = id[beta[i]];
+          succ[a].push_back(b);
+          indeg[b]++;
+        }
+      std::priority_queue<std::pair<uint64_t, int32_t>, std::vector<std::pair<uint64_t, int32_t>>,
+                          std::greater<std::pair<uint64_t, int32_t>>>
+          pq;
+      for (int64_t u = 0; u < U; ++u)
+        if (!indeg[u]) pq.push({strs[u], (int32_t)u});
+      while (!pq.empty()) {
+        auto [s, u] = pq.top();
+        pq.pop();
+        rank[s] = (int32_t)ubeta.size();
+        ubeta.push_back(s);
+        for (int32_t v : succ[u])
+          if (--indeg[v] == 0) pq.push({strs[v], v});
+      }
+      if ((int64_t)ubeta.size() != U)
+        throw Error(QDKGB_ERR_UNSUPPORTED,
+                    "determinant list is not alpha-grouped with one common beta order (sort it by spin_comparator)");
+    }
+    for (int64_t i = 0; i < nd; ++i) brank[i] = rank[beta[i]];
+    D.product = product;
+  }
+  // strict increase inside every group (no repeated determinant)
+  for (int64_t g = 0; g < G; ++g)
+    for (int64_t i = D.h_gstart[g] + 1; i < D.h_gstart[g + 1]; ++i)
+      if (!(brank[i - 1] < brank[i]))
+        throw Error(QDKGB_ERR_UNSUPPORTED, "repeated determinant or inconsistent beta order in an alpha group");
+  D.nbeta = (int64_t)ubeta.size();
+
+  std::vector<int32_t> det_group(nd);
+  std::vector<uint8_t> complete(G);
+  for (int64_t g = 0; g < G; ++g) {
+    for (int64_t i = D.h_gstart[g]; i < D.h_gstart[g + 1]; ++i) det_group[i] = (int32_t)g;
+    complete[g] = (D.h_gstart[g + 1] - D.h_gstart[g]) == D.nbeta;
+  }
+
+  auto up = [&](DeviceBuffer& b, const void* src, size_t bytes) {
+    void* p = dev_alloc(c, b, bytes + 16);
+    QDKGB_CUDA(cudaMemcpyAsync(p, src, bytes, cudaMemcpyHostToDevice, c->stream));
+  };
+  up(D.galpha, D.h_galpha.data(), G * 8);
+  up(D.gstart, D.h_gstart.data(), (G + 1) * 8);
+  up(D.det_group, det_group.data(), nd * 4);
+  up(D.brank, brank.data(), nd * 4);
+  up(D.ubeta, ubeta.data(), D.nbeta * 8);
+  up(D.gcomplete, complete.data(), G);
+  QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+
+  build_conn(c, (const uint64_t*)D.galpha.ptr, G, 4, true, D.acon_ptr, D.acon_idx, &D.acon_lvl, D.acon_total);
+  build_conn(c, (const uint64_t*)D.ubeta.ptr, D.nbeta, 4, false, D.b2_ptr, D.b2_idx, nullptr, D.b2_total);
+  build_conn(c, (const uint64_t*)D.ubeta.ptr, D.nbeta, 2, false, D.b1_ptr, D.b1_idx, nullptr, D.b1_total);
+  c->have_dets = true;
+}
+
+// ------------------------------------------------------------------ CSR rows
+__global__ void __launch_bounds__(kRowWarps * 32) k_row_count(RowArgs a, int64_t* __restrict__ row_nnz) {
+  __shared__ RowWalkSmem sm;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int64_t r = (int64_t)blockIdx.x * kRowWarps + w; r < a.ndets; r += (int64_t)gridDim.x * kRowWarps) {
+    int64_t cnt = 0;
+    walk_row(a, r, w, lane, sm, [&](int64_t ket, int64_t row, uint64_t ra, uint64_t rb, uint64_t ka, uint64_t kb) {
+      bool keep = false;
+      if (ket >= 0) {
+        const double v = pair_value(a.I, row, ket, ra, rb, ka, kb);
+        keep = !(a.thresh > 0.) || fabs(v) > a.thresh;
+      }
+      cnt += __popc(__ballot_sync(QDKGB_FULL_MASK, keep));
+    });
+    if (lane == 0) row_nnz[r] = cnt;
+  }
+}
+
+template <int STORAGE>
+__global__ void __launch_bounds__(kRowWarps * 32)
+    k_row_emit(RowArgs a, const int64_t* __restrict__ rowptr, int32_t* __restrict__ colind, double* __restrict__ val,
+               float* __restrict__ hi, float* __restrict__ lo, double* __restrict__ diag) {
+  __shared__ RowWalkSmem sm;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int64_t r = (int64_t)blockIdx.x * kRowWarps + w; r < a.ndets; r += (int64_t)gridDim.x * kRowWarps) {
+    int64_t pos0 = rowptr[r];
+    walk_row(a, r, w, lane, sm, [&](int64_t ket, int64_t row, uint64_t ra, uint64_t rb, uint64_t ka, uint64_t kb) {
+      bool keep = false;
+      double v = 0.;
+      if (ket >= 0) {
+        v = pair_value(a.I, row, ket, ra, rb, ka, kb);
+        keep = !(a.thresh > 0.) || fabs(v) > a.thresh;
+        if (ket == row) diag[row] = keep ? v : 0.;
+      }
+      const unsigned m = __ballot_sync(QDKGB_FULL_MASK, keep);
+      if (keep) {
+        const int64_t p = pos0 + __popc(m & ((1u << lane) - 1u));
+        colind[p] = (int32_t)ket;
+        if (STORAGE == QDKGB_H_FP64) {
+          val[p] = v;
+        } else {
+          const float h = __double2float_rn(v);
+          hi[p] = h;
+          lo[p] = __double2float_rn(v - (double)h);
+        }
+      }
+      pos0 += __popc(m);
+    });
+  }
+}
+
+RowArgs row_args(Context* c, double thresh) {
+  DetSpace& D = c->dets;
+  RowArgs a;
+  a.I = integrals_view(c);
+  a.ndets = D.ndets;
+  a.galpha = (const uint64_t*)D.galpha.ptr;
+  a.gstart = (const int64_t*)D.gstart.ptr;
+  a.det_group = (const int32_t*)D.det_group.ptr;
+  a.brank = (const int32_t*)D.brank.ptr;
+  a.ubeta = (const uint64_t*)D.ubeta.ptr;
+  a.gcomplete = (const uint8_t*)D.gcomplete.ptr;
+  a.acon_ptr = (const int64_t*)D.acon_ptr.ptr;
+  a.acon_idx = (const int32_t*)D.acon_idx.ptr;
+  a.acon_lvl = (const int8_t*)D.acon_lvl.ptr;
+  a.b2_ptr = (const int64_t*)D.b2_ptr.ptr;
+  a.b2_idx = (const int32_t*)D.b2_idx.ptr;
+  a.b1_ptr = (const int64_t*)D.b1_ptr.ptr;
+  a.b1_idx = (const int32_t*)D.b1_idx.ptr;
+  a.thresh = thresh;
+  return a;
+}
+
+void build_hamiltonian(Context* c, double thresh, int storage) {
+  if (!c->have_ints) throw Error(QDKGB_ERR_STATE, "integrals not set");
+  if (!c->have_dets) throw Error(QDKGB_ERR_STATE, "determinants not set");
+  if (storage != QDKGB_H_FP64 && storage != QDKGB_H_SPLIT32) throw Error(QDKGB_ERR_INVALID, "unknown storage");
+  Hcsr& H = c->H;
+  H.valid = false;
+  const int64_t n = c->dets.ndets;
+  RowArgs a = row_args(c, thresh);
+  int64_t* row_nnz = dev_array<int64_t>(c, H.row_nnz, n + 1);
+  int64_t* rowptr = dev_array<int64_t>(c, H.rowptr, n + 1);
+  const int64_t blocks = std::min<int64_t>((n + kRowWarps - 1) / kRowWarps, (int64_t)c->sm_count * 64);
+  k_row_count<<<(unsigned)blocks, kRowWarps * 32, 0, c->stream>>>(a, row_nnz);
+  QDKGB_CHECK_LAUNCH();
+  exclusive_scan_i64(c, row_nnz, rowptr, n, H.scan_tmp);
+  int64_t nnz = 0;
+  QDKGB_CUDA(cudaMemcpyAsync(&nnz, rowptr + n, sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
+  QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+  // release the other storage's arrays before allocating this one
+  if (storage == QDKGB_H_FP64) {
+    dev_free(c, H.hi);
+    dev_free(c, H.lo);
+  } else {
+    dev_free(c, H.val);
+  }
+  int32_t* colind = dev_array<int32_t>(c, H.colind, std::max<int64_t>(nnz, 1));
+  double* val = nullptr;
+  float *hi = nullptr, *lo = nullptr;
+  if (storage == QDKGB_H_FP64)
+    val = dev_array<double>(c, H.val, std::max<int64_t>(nnz, 1));
+  else {
+    hi = dev_array<float>(c, H.hi, std::max<int64_t>(nnz, 1));
+    lo = dev_array<float>(c, H.lo, std::max<int64_t>(nnz, 1));
+  }
+  double* diag = dev_array<double>(c, H.diag, n);
+  QDKGB_CUDA(cudaMemsetAsync(diag, 0, n * sizeof(double), c->stream));
+  if (storage == QDKGB_H_FP64)
+    k_row_emit<QDKGB_H_FP64><<<(unsigned)blocks, kRowWarps * 32, 0, c->stream>>>(a, rowptr, colind, val, hi, lo, diag);
+  else
+    k_row_emit<QDKGB_H_SPLIT32>
+        <<<(unsigned)blocks, kRowWarps * 32, 0, c->stream>>>(a, rowptr, colind, val, hi, lo, diag);
+  QDKGB_CHECK_LAUNCH();
+  QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+  H.n = n;
+  H.nnz = nnz;
+  H.storage = storage;
+  H.thresh = thresh;
+  H.valid = true;
+}
+
+}  // namespace qdkgb

@@ -1,0 +1,120 @@
+// Internal declarations shared by the library's translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/qdkgb.h"
+
+namespace qdkgb {
+
+// Thrown inside the library, converted to a status code at the C ABI.
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+#define QDKGB_CUDA(call)                                                                              \
+  do {                                                                                                \
+    cudaError_t e_ = (call);                                                                          \
+    if (e_ != cudaSuccess)                                                                            \
+      throw ::qdkgb::Error(e_ == cudaErrorMemoryAllocation ? QDKGB_ERR_OOM : QDKGB_ERR_CUDA,          \
+                           std::string(#call) + ": " + cudaGetErrorString(e_));                      \
+  } while (0)
+
+#define QDKGB_CHECK_LAUNCH() QDKGB_CUDA(cudaGetLastError())
+
+// Device allocation owned by a context (tracked so the context can report and
+// release what it holds).
+struct DeviceBuffer {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+};
+
+struct Context;
+struct Integrals;
+
+void* dev_alloc(Context* c, DeviceBuffer& b, size_t bytes);  // (re)allocates when too small
+void dev_free(Context* c, DeviceBuffer& b);
+
+template <typename T>
+T* dev_array(Context* c, DeviceBuffer& b, size_t n) {
+  return (T*)dev_alloc(c, b, n * sizeof(T) + 16);
+}
+
+// Determinant list prepared for the kernels.
+struct DetSpace {
+  int64_t ndets = 0;
+  int64_t ngroups = 0;  // alpha groups (runs of equal alpha strings)
+  int64_t nbeta = 0;    // distinct beta strings
+  bool product = false; // every group holds every beta string (FCI-like)
+  std::vector<uint64_t> h_alpha, h_beta;
+  std::vector<uint64_t> h_galpha;
+  std::vector<int64_t> h_gstart;
+  // device
+  DeviceBuffer galpha, gstart, det_group, brank, ubeta, gcomplete;
+  DeviceBuffer acon_ptr, acon_idx, acon_lvl;  // alpha-group connectivity (<= double)
+  DeviceBuffer b2_ptr, b2_idx;                // beta-string connectivity, level <= 2 (<= 4 differing bits)
+  DeviceBuffer b1_ptr, b1_idx;                // beta-string connectivity, level <= 1
+  int64_t acon_total = 0, b2_total = 0, b1_total = 0;
+};
+
+struct Hcsr {
+  int64_t n = 0, nnz = 0;
+  int storage = QDKGB_H_FP64;
+  double thresh = 0.;
+  DeviceBuffer rowptr, colind, val, hi, lo, diag, row_nnz, scan_tmp;
+  bool valid = false;
+};
+
+struct DavidsonWork {
+  DeviceBuffer V, AV, xf, yf, Hk, evec, eval, scratch, partial, small;
+  int64_t n = 0, maxm = 0;
+};
+
+struct Context {
+  int device = 0;
+  cudaStream_t own_stream = nullptr, stream = nullptr;
+  std::string err;
+  int64_t dev_bytes = 0;
+  int sm_count = 0;
+  // integrals
+  int norb = 0;
+  DeviceBuffer T, V, G_red, V_red, G2, V2;
+  std::vector<double> h_T, h_V;  // column-major host copies
+  bool have_ints = false;
+  DetSpace dets;
+  bool have_dets = false;
+  Hcsr H;
+  DavidsonWork dav;
+  DeviceBuffer host_pinned_dummy;
+  double* pinned = nullptr;  // small pinned host staging (64 doubles)
+};
+
+Integrals integrals_view(Context* c);
+
+// hbuild.cu
+void build_integral_intermediates(Context* c);
+void build_det_space(Context* c, int64_t ndets, const uint64_t* alpha, const uint64_t* beta);
+void build_hamiltonian(Context* c, double thresh, int storage);
+void exclusive_scan_i64(Context* c, const int64_t* in, int64_t* out, int64_t n, DeviceBuffer& tmp);
+
+// spmv.cu
+void spmv_fp64(Context* c, const double* x, double* y);
+void spmv_fp32(Context* c, const float* x, float* y);
+void csr_values_to_double(Context* c, double* out);
+void f64_to_f32(Context* c, const double* x, float* y, int64_t n);
+void f32_to_f64(Context* c, const float* x, double* y, int64_t n);
+
+// davidson.cu
+void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C, qdkgb_davidson_info* info);
+
+// rdm.cu
+void rdms_spin_dep(Context* c, const double* C, double* aa, double* bb, double* aaaa, double* bbbb, double* aabb);
+
+}  // namespace qdkgb
+
+struct qdkgb_context : qdkgb::Context {};

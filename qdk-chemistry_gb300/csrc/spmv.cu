@@ -1,0 +1,124 @@
+// Sigma = H x on the device CSR (replaces sparsexx::spblas::gespmbv,
+// sparsexx/spblas/spmbv.hpp:49-85, as driven by SparseMatrixOperator,
+// include/macis/solvers/davidson.hpp:79-90).
+//
+// HBM-bound: a sigma streams nnz * (value + 4 B column) once; x (<= a few MB)
+// stays L2-resident.  One warp per row (FCI rows hold ~10^2..10^3 elements),
+// lanes stride the row with coalesced loads, several loads in flight per lane,
+// and a fixed-order shuffle reduction (deterministic results).
+//   fp64  : FP64 values, FP64 x/y, FP64 FMA
+//   fp32  : FP32 values (the high part of the split storage), FP32 x/y/accumulation
+//   split : (double)hi + (double)lo values, FP64 x/y/accumulation - the
+//           full-precision sigma of the mixed-precision path
+#include "common.cuh"
+#include "internal.h"
+
+namespace qdkgb {
+
+constexpr int kSpmvWarps = 8;
+
+struct ValF64 {
+  const double* v;
+  __device__ __forceinline__ double operator()(int64_t k) const { return __ldcs(v + k); }
+};
+struct ValSplit {
+  const float* hi;
+  const float* lo;
+  __device__ __forceinline__ double operator()(int64_t k) const {
+    return (double)__ldcs(hi + k) + (double)__ldcs(lo + k);
+  }
+};
+struct ValF32 {
+  const float* v;
+  __device__ __forceinline__ float operator()(int64_t k) const { return __ldcs(v + k); }
+};
+
+template <typename Acc, typename X, typename Val>
+__global__ void __launch_bounds__(kSpmvWarps * 32)
+    k_spmv_csr(int64_t n, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col, Val val,
+               const X* __restrict__ x, X* __restrict__ y) {
+  const int lane = threadIdx.x & 31;
+  const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t r = w0; r < n; r += nw) {
+    const int64_t st = rowptr[r], en = rowptr[r + 1];
+    Acc acc0 = 0, acc1 = 0, acc2 = 0, acc3 = 0;
+    int64_t k = st + lane;
+    for (; k + 96 < en; k += 128) {
+      const int32_t c0 = __ldcs(col + k), c1 = __ldcs(col + k + 32), c2 = __ldcs(col + k + 64),
+                    c3 = __ldcs(col + k + 96);
+      const Acc v0 = val(k), v1 = val(k + 32), v2 = val(k + 64), v3 = val(k + 96);
+      acc0 += v0 * (Acc)__ldg(x + c0);
+      acc1 += v1 * (Acc)__ldg(x + c1);
+      acc2 += v2 * (Acc)__ldg(x + c2);
+      acc3 += v3 * (Acc)__ldg(x + c3);
+    }
+    for (; k < en; k += 32) acc0 += val(k) * (Acc)__ldg(x + __ldcs(col + k));
+    Acc acc = (acc0 + acc1) + (acc2 + acc3);
+    acc = warp_sum(acc);
+    if (lane == 0) y[r] = (X)acc;
+  }
+}
+
+static unsigned spmv_blocks(Context* c, int64_t n) {
+  const int64_t want = (n + kSpmvWarps - 1) / kSpmvWarps;
+  return (unsigned)std::min<int64_t>(want, (int64_t)c->sm_count * 32);
+}
+
+void spmv_fp64(Context* c, const double* x, double* y) {
+  Hcsr& H = c->H;
+  if (!H.valid) throw Error(QDKGB_ERR_STATE, "Hamiltonian not built");
+  const int64_t* rp = (const int64_t*)H.rowptr.ptr;
+  const int32_t* ci = (const int32_t*)H.colind.ptr;
+  if (H.storage == QDKGB_H_FP64)
+    k_spmv_csr<double, double><<<spmv_blocks(c, H.n), kSpmvWarps * 32, 0, c->stream>>>(
+        H.n, rp, ci, ValF64{(const double*)H.val.ptr}, x, y);
+  else
+    k_spmv_csr<double, double><<<spmv_blocks(c, H.n), kSpmvWarps * 32, 0, c->stream>>>(
+        H.n, rp, ci, ValSplit{(const float*)H.hi.ptr, (const float*)H.lo.ptr}, x, y);
+  QDKGB_CHECK_LAUNCH();
+}
+
+void spmv_fp32(Context* c, const float* x, float* y) {
+  Hcsr& H = c->H;
+  if (!H.valid) throw Error(QDKGB_ERR_STATE, "Hamiltonian not built");
+  if (H.storage != QDKGB_H_SPLIT32)
+    throw Error(QDKGB_ERR_STATE, "FP32 sigma needs the Hamiltonian built with QDKGB_H_SPLIT32 storage");
+  k_spmv_csr<float, float><<<spmv_blocks(c, H.n), kSpmvWarps * 32, 0, c->stream>>>(
+      H.n, (const int64_t*)H.rowptr.ptr, (const int32_t*)H.colind.ptr, ValF32{(const float*)H.hi.ptr}, x, y);
+  QDKGB_CHECK_LAUNCH();
+}
+
+__global__ void k_split_to_double(int64_t nnz, const float* hi, const float* lo, double* out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nnz; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = (double)hi[i] + (double)lo[i];
+}
+void csr_values_to_double(Context* c, double* out) {
+  Hcsr& H = c->H;
+  if (H.storage == QDKGB_H_FP64) {
+    QDKGB_CUDA(cudaMemcpyAsync(out, H.val.ptr, H.nnz * 8, cudaMemcpyDeviceToDevice, c->stream));
+  } else {
+    k_split_to_double<<<c->sm_count * 8, 256, 0, c->stream>>>(H.nnz, (const float*)H.hi.ptr,
+                                                              (const float*)H.lo.ptr, out);
+    QDKGB_CHECK_LAUNCH();
+  }
+}
+
+__global__ void k_f64_to_f32(const double* x, float* y, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = __double2float_rn(x[i]);
+}
+__global__ void k_f32_to_f64(const float* x, double* y, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = (double)x[i];
+}
+void f64_to_f32(Context* c, const double* x, float* y, int64_t n) {
+  k_f64_to_f32<<<c->sm_count * 4, 256, 0, c->stream>>>(x, y, n);
+  QDKGB_CHECK_LAUNCH();
+}
+void f32_to_f64(Context* c, const float* x, double* y, int64_t n) {
+  k_f32_to_f64<<<c->sm_count * 4, 256, 0, c->stream>>>(x, y, n);
+  QDKGB_CHECK_LAUNCH();
+}
+
+}  // namespace qdkgb

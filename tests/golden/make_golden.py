@@ -1,0 +1,89 @@
+"""Regenerate the golden fixtures in this folder from the reference checkout.
+
+Run in a container where the reference is mounted at /root/reference:
+
+    python tests/golden/make_golden.py [/root/reference]
+
+It copies the reference's own test inputs and known answers for the CI hot
+path into compact numpy files, so that the tests never read the reference at
+run time:
+
+* FCIDUMP integral lines (index quadruples + values) of
+  - external/macis/tests/ref_data/h2o.ccpvdz.fci.dat (water cc-pVDZ, 24 orbitals)
+  - external/macis/python/tests/data/n2_selected_6e6o.hamiltonian.fcidump
+  - external/macis/python/tests/data/n2_full_14e18o.hamiltonian.fcidump
+* the CSR row-pointer golden of the water CISD Hamiltonian
+  (external/macis/tests/ref_data/h2o.ccpvdz.cisd.rowptr.bin, int32)
+* the O2 CI wavefunction external/macis/tests/ref_data/o2.wfn.dat
+* known_answers.json: the energies / sums the reference tests pin, with the
+  file:line each one comes from.
+"""
+import json
+import os
+import re
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def parse_fcidump_lines(path):
+    text = open(path).read()
+    m = re.search(r"&END|^\s*/\s*$", text, re.M | re.I)
+    head, body = text[:m.start()], text[m.end():]
+    hdr = {k: int(re.search(k + r"\s*=\s*(-?\d+)", head, re.I).group(1)) for k in ("NORB", "NELEC")}
+    ms2 = re.search(r"MS2\s*=\s*(-?\d+)", head, re.I)
+    rows = np.loadtxt(body.splitlines(), ndmin=2)
+    return dict(norb=hdr["NORB"], nelec=hdr["NELEC"], ms2=int(ms2.group(1)) if ms2 else 0,
+                idx=rows[:, 1:5].astype(np.int8), vals=rows[:, 0].astype(np.float64))
+
+
+def main(ref="/root/reference"):
+    macis = os.path.join(ref, "external", "macis")
+    dumps = {
+        "h2o_ccpvdz": os.path.join(macis, "tests", "ref_data", "h2o.ccpvdz.fci.dat"),
+        "n2_6e6o": os.path.join(macis, "python", "tests", "data", "n2_selected_6e6o.hamiltonian.fcidump"),
+        "n2_14e18o": os.path.join(macis, "python", "tests", "data", "n2_full_14e18o.hamiltonian.fcidump"),
+    }
+    for name, path in dumps.items():
+        d = parse_fcidump_lines(path)
+        np.savez_compressed(os.path.join(HERE, name + "_fcidump.npz"), **d)
+
+    rp = np.fromfile(os.path.join(macis, "tests", "ref_data", "h2o.ccpvdz.cisd.rowptr.bin"), dtype=np.int32)
+    np.save(os.path.join(HERE, "h2o_ccpvdz_cisd_rowptr.npy"), rp)
+
+    lines = open(os.path.join(macis, "tests", "ref_data", "o2.wfn.dat")).read().splitlines()
+    nstate, norb, na, nb = (int(x) for x in lines[0].split())
+    coeffs, strs = [], []
+    for ln in lines[1:]:
+        if ln.strip():
+            c, s = ln.split()
+            coeffs.append(float(c))
+            strs.append(s)
+    alpha = np.array([sum(1 << i for i, ch in enumerate(s) if ch in "2u") for s in strs], dtype=np.uint64)
+    beta = np.array([sum(1 << i for i, ch in enumerate(s) if ch in "2d") for s in strs], dtype=np.uint64)
+    np.savez_compressed(os.path.join(HERE, "o2_wfn.npz"), alpha=alpha, beta=beta, coeffs=np.array(coeffs),
+                        norb=norb, nalpha=na, nbeta=nb)
+
+    known = {
+        "h2o_cisd_csr": {"n": 12636, "nnz": 3517816, "thresh": 1e-16,
+                         "source": "external/macis/tests/csr_hamiltonian.cxx:46-77"},
+        "h2o_cisd_davidson": {"E0_total": -7.623197835987e01, "max_m": 15, "tol": 1e-8, "atol": 1e-8,
+                              "source": "external/macis/tests/davidson.cxx:44-58"},
+        "n2_6e6o_casci": {"E_total": -9.155573e00, "ndets": 400, "nalpha": 3, "nbeta": 3,
+                          "source": "external/macis/python/tests/test_pymacis.py:114-142"},
+        "n2_14e18o_asci": {"E_total": -1.205187165264e02, "ndets": 2000, "grow_factor": 2,
+                           "ntdets_max": 2000, "max_refine_iter": 15, "max_subspace": 1000,
+                           "source": "external/macis/python/tests/test_pymacis.py:158-187"},
+        "h2o_asci_10k": {"E0_grow": -8.542926580489e01, "E0_refine": -8.542926585527e01, "ntdets_max": 10000,
+                         "source": "external/macis/tests/asci.cxx:488-574"},
+        "o2_rdms": {"n_dets_padded": 5000, "sum_abs_ordm": 8.0000005763, "sum_abs_trdm": 44.1092472977,
+                    "atol": 1e-6, "source": "external/macis/tests/double_loop.cxx:506-579"},
+    }
+    with open(os.path.join(HERE, "known_answers.json"), "w") as f:
+        json.dump(known, f, indent=1)
+
+
+if __name__ == "__main__":
+    main(*sys.argv[1:])

@@ -1,0 +1,68 @@
+"""C ABI checks that need no GPU: the library builds/loads, exports every
+function declared in include/qdkgb.h, host-only entry points work, and the
+device entry points fail with a status code (not a crash) without a GPU."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+
+def _declared():
+    text = open(os.path.join(ROOT, "include", "qdkgb.h")).read()
+    return sorted(set(re.findall(r"\b(qdkgb_[a-z0-9_]+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def capi(pkg):
+    pkg.build.build()
+    return pkg.capi
+
+
+def test_exports_every_declared_symbol(capi):
+    L = capi.lib()
+    declared = _declared()
+    assert len(declared) >= 19
+    for name in declared:
+        assert hasattr(L, name), name
+    assert set(capi.EXPORTED) <= set(declared)
+    assert b"sm_103a" in L.qdkgb_version()
+
+
+def test_fci_dets_host_order(capi, oracle):
+    for n, na, nb in [(6, 3, 3), (8, 4, 3), (12, 6, 6), (40, 1, 1)]:
+        a, b = capi.fci_dets(n, na, nb)
+        oa, ob = oracle.fci_dets(n, na, nb)
+        assert np.array_equal(a, oa) and np.array_equal(b, ob)
+
+
+def test_fci_dets_rejects_bad_arguments(capi):
+    n = ctypes.c_int64()
+    assert capi.lib().qdkgb_fci_dets(0, 1, 1, None, None, ctypes.byref(n)) == capi.ERR_INVALID
+    assert capi.lib().qdkgb_fci_dets(8, 9, 1, None, None, ctypes.byref(n)) == capi.ERR_INVALID
+    assert capi.lib().qdkgb_fci_dets(65, 1, 1, None, None, ctypes.byref(n)) == capi.ERR_INVALID
+
+
+def test_null_context_is_an_error_not_a_crash(capi):
+    L = capi.lib()
+    assert L.qdkgb_set_dets(None, 1, None, None) == capi.ERR_INVALID
+    assert L.qdkgb_build_hamiltonian(None, 0.0, 0, None) == capi.ERR_INVALID
+    assert L.qdkgb_destroy(None) == capi.OK
+
+
+def test_create_without_gpu_reports_status(capi):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    h = ctypes.c_void_p()
+    rc = capi.lib().qdkgb_create(ctypes.byref(h), 0)
+    assert rc != capi.OK and not h.value
+
+
+def test_default_settings_mirror_reference(capi):
+    s = capi.default_davidson_settings()
+    # ci_max_subspace / max_solver_iterations 200, ci_res_tol 1e-8, clamp 1e-12
+    assert s.max_m == 200 and s.res_tol == 1e-8 and s.min_abs_denominator == 1e-12

@@ -1,0 +1,226 @@
+"""GPU parity against the CPU oracle and the reference's golden vectors, all
+through the C ABI (libqdkgb.so).
+
+Tolerances: determinant lists, CSR row pointers and columns are compared
+bit-exact; FP64 matrix elements bit-exact as well (the kernels reproduce the
+reference's operation order), with 1e-12 relative as the documented bar;
+energies 1e-10 Eh (FP64) and 1e-8 Eh (mixed precision); RDMs 1e-12 absolute.
+"""
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def capi(pkg):
+    pkg.build.build()
+    return pkg.capi
+
+
+@pytest.fixture(scope="module")
+def ctx(capi):
+    c = capi.Context(0)
+    yield c
+    c.close()
+
+
+def _cas(pkg, norb, nel, nchol, seed, spacing=0.25):
+    T, V, _ = pkg.integrals.synthetic_integrals(norb, nchol, seed, diag_spacing=spacing)
+    a, b = pkg.determinants.fci_space(norb, nel // 2, nel // 2)
+    return T, V, a, b
+
+
+def _check_csr(ctx, oracle, T, V, a, b, thresh):
+    ctx.set_integrals(T, V)
+    ctx.set_dets(a, b)
+    nnz = ctx.build_hamiltonian(thresh)
+    rp, ci, nz = ctx.get_csr(64)
+    M = oracle.build_csr(oracle.Hamiltonian(T, V), a, b, thresh)
+    orp, oci, onz = M.arrays()
+    assert nnz == M.nnz
+    np.testing.assert_array_equal(rp, orp)
+    np.testing.assert_array_equal(ci, oci)
+    # bit-exact values (the documented bar is 1e-12 relative)
+    np.testing.assert_allclose(nz, onz, rtol=1e-12, atol=0)
+    assert np.array_equal(nz, onz), "FP64 values differ from the oracle in the last bits"
+    np.testing.assert_array_equal(ctx.diagonal(), M.diag())
+    return M
+
+
+def test_cas88_csr_bit_exact(ctx, oracle, pkg):
+    T, V, a, b = _cas(pkg, 8, 8, 16, seed=11)
+    M = _check_csr(ctx, oracle, T, V, a, b, np.finfo(float).eps)
+    assert M.nnz == 4900 * 361
+
+
+def test_h2o_cisd_csr_golden(ctx, oracle, pkg, h2o, known):
+    d = pkg.determinants
+    a, b = d.spin_sort(*d.cisd_space(24, *d.canonical_hf(5, 5)))
+    M = _check_csr(ctx, oracle, h2o["T"], h2o["V"], a, b, 1e-16)
+    rp32, ci32, _ = ctx.get_csr(32)
+    golden = np.load(GOLDEN + "/h2o_ccpvdz_cisd_rowptr.npy")
+    np.testing.assert_array_equal(rp32, golden)
+    assert ctx.nnz == known["h2o_cisd_csr"]["nnz"]
+
+
+def test_thresh_zero_keeps_structural_zeros(ctx, oracle, pkg, n2_6e6o):
+    a, b = pkg.determinants.fci_space(6, 3, 3)
+    _check_csr(ctx, oracle, n2_6e6o["T"], n2_6e6o["V"], a, b, 0.0)
+    _check_csr(ctx, oracle, n2_6e6o["T"], n2_6e6o["V"], a, b, 1e-6)
+
+
+def test_uneven_spaces_and_edge_cases(ctx, oracle, pkg):
+    T, V, _ = pkg.integrals.synthetic_integrals(10, 12, seed=5)
+    # open shell, nalpha != nbeta
+    a, b = pkg.determinants.fci_space(10, 4, 2)
+    _check_csr(ctx, oracle, T, V, a, b, 1e-14)
+    # a selected (ragged) subset sorted by spin_comparator
+    rng = np.random.default_rng(0)
+    a, b = pkg.determinants.fci_space(10, 3, 3)
+    keep = np.sort(rng.choice(len(a), 3000, replace=False))
+    sa, sb = pkg.determinants.spin_sort(a[keep], b[keep])
+    _check_csr(ctx, oracle, T, V, sa, sb, 1e-14)
+    # single determinant
+    _check_csr(ctx, oracle, T, V, sa[:1], sb[:1], 1e-14)
+    # one electron per spin
+    a, b = pkg.determinants.fci_space(10, 1, 1)
+    _check_csr(ctx, oracle, T, V, a, b, 1e-14)
+
+
+def test_build_is_deterministic(ctx, pkg):
+    T, V, a, b = _cas(pkg, 8, 8, 16, seed=2)
+    ctx.set_integrals(T, V)
+    ctx.set_dets(a, b)
+    ctx.build_hamiltonian()
+    r1 = ctx.get_csr()
+    ctx.build_hamiltonian()
+    r2 = ctx.get_csr()
+    for x, y in zip(r1, r2):
+        assert np.array_equal(x, y)
+
+
+def test_split_storage_and_spmv(ctx, oracle, pkg, capi):
+    T, V, a, b = _cas(pkg, 8, 8, 16, seed=4)
+    ctx.set_integrals(T, V)
+    ctx.set_dets(a, b)
+    ctx.build_hamiltonian(storage=capi.H_FP64)
+    _, _, nz64 = ctx.get_csr()
+    x = np.random.default_rng(1).normal(size=len(a))
+    y64 = ctx.spmv(x, capi.PREC_FP64)
+    M = oracle.build_csr(oracle.Hamiltonian(T, V), a, b)
+    yo = M.spmv(x)
+    assert np.max(np.abs(y64 - yo)) <= 1e-12 * np.max(np.abs(yo))
+    ctx.build_hamiltonian(storage=capi.H_SPLIT32)
+    _, _, nzs = ctx.get_csr()
+    assert np.all(np.abs(nzs - nz64) <= 2.0 ** -47 * np.abs(nz64))
+    ys = ctx.spmv(x, capi.PREC_FP64)  # hi+lo values, FP64 accumulation
+    assert np.max(np.abs(ys - yo)) <= 1e-12 * np.max(np.abs(yo))
+    y32 = ctx.spmv(x, capi.PREC_MIXED)  # FP32 values/x/accumulation
+    rel = np.max(np.abs(y32 - yo)) / np.max(np.abs(yo))
+    assert 1e-9 < rel < 1e-5
+
+
+def test_davidson_fp64_matches_oracle(ctx, oracle, pkg):
+    T, V, a, b = _cas(pkg, 8, 8, 16, seed=7)
+    ctx.set_integrals(T, V)
+    ctx.set_dets(a, b)
+    ctx.build_hamiltonian()
+    E, C, info = ctx.davidson(tol=1e-8)
+    M = oracle.build_csr(oracle.Hamiltonian(T, V), a, b)
+    Eo, Co, ito = M.selected_ci_diag(tol=1e-8)
+    assert abs(E - Eo) < 1e-10
+    assert abs(abs(C @ Co) - 1.0) < 1e-10
+    assert info["residual_norm"] < 1e-8
+    assert info["iterations"] == ito  # same algorithm, same iteration count
+
+
+def test_davidson_h2o_cisd_golden(ctx, pkg, h2o, known):
+    ref = known["h2o_cisd_davidson"]
+    d = pkg.determinants
+    a, b = d.spin_sort(*d.cisd_space(24, *d.canonical_hf(5, 5)))
+    ctx.set_integrals(h2o["T"], h2o["V"])
+    ctx.set_dets(a, b)
+    ctx.build_hamiltonian(1e-16)
+    E, C, info = ctx.davidson(max_m=ref["max_m"], tol=ref["tol"])
+    assert abs(E + h2o["E_core"] - ref["E0_total"]) < ref["atol"]
+    assert abs(np.linalg.norm(C) - 1) < 1e-12
+
+
+def test_davidson_n2_casci_golden(ctx, pkg, n2_6e6o, known):
+    E, C, info = ctx.casci(n2_6e6o["T"], n2_6e6o["V"], 3, 3)
+    assert np.isclose(E, known["n2_6e6o_casci"]["E_total"])
+
+
+def test_mixed_precision_energy(ctx, oracle, pkg, capi):
+    T, V, a, b = _cas(pkg, 10, 10, 20, seed=8)
+    M = oracle.build_csr(oracle.Hamiltonian(T, V), a, b)
+    Eo, _, _ = M.selected_ci_diag(tol=1e-9)
+    ctx.set_integrals(T, V)
+    ctx.set_dets(a, b)
+    ctx.build_hamiltonian(storage=capi.H_SPLIT32)
+    E, C, info = ctx.davidson(tol=1e-8, precision=capi.PREC_MIXED)
+    assert abs(E - Eo) < 1e-8, (E - Eo, info)
+    assert info["residual_norm"] < 1e-8
+    assert info["spmv_fp32"] > info["spmv_fp64"]
+
+
+def test_davidson_not_converged_raises(ctx, pkg, capi):
+    T, V, a, b = _cas(pkg, 8, 8, 16, seed=9)
+    ctx.set_integrals(T, V)
+    ctx.set_dets(a, b)
+    ctx.build_hamiltonian()
+    with pytest.raises(capi.NotConverged):
+        ctx.davidson(max_m=3, tol=1e-12)
+
+
+def _rdm_check(ctx, oracle, n, a, b, C, atol=1e-12):
+    R = ctx.rdms_spin_dep(C)
+    Ro = oracle.rdms_spin_dep(n, a, b, C)
+    for k in Ro:
+        np.testing.assert_allclose(R[k], Ro[k], atol=atol, rtol=0, err_msg=k)
+    return R
+
+
+def test_rdms_match_oracle_cas(ctx, oracle, pkg):
+    T, V, a, b = _cas(pkg, 8, 8, 16, seed=12)
+    ctx.set_integrals(T, V)
+    ctx.set_dets(a, b)
+    ctx.build_hamiltonian()
+    E, C, _ = ctx.davidson()
+    R = _rdm_check(ctx, oracle, 8, a, b, C)
+    E_rdm = (np.sum(T * (R["aa"] + R["bb"])) + np.sum(V * (R["aaaa"] + R["bbbb"])) + 2 * np.sum(V * R["aabb"]))
+    assert abs(E_rdm - E) < 1e-10
+
+
+def test_rdms_sliced_tile_norb14(ctx, oracle, pkg):
+    # n = 14: the n^4 tile is split over last-index slices
+    T, V, _ = pkg.integrals.synthetic_integrals(14, 6, seed=2)
+    a, b = pkg.determinants.fci_space(14, 2, 2)
+    ctx.set_integrals(T, V)
+    ctx.set_dets(a, b)
+    C = np.random.default_rng(3).normal(size=len(a))
+    C /= np.linalg.norm(C)
+    _rdm_check(ctx, oracle, 14, a, b, C)
+
+
+def test_rdms_o2_wavefunction_golden(ctx, oracle, pkg):
+    """external/macis/tests/double_loop.cxx:506-579 through the GPU (n = 34:
+    global-memory accumulation path).  The list is sorted by spin_comparator
+    (RDMs are invariant under the permutation); the empty padding
+    determinants are dropped (the reference skips them)."""
+    w = np.load(GOLDEN + "/o2_wfn.npz")
+    C = w["coeffs"] / np.linalg.norm(w["coeffs"])
+    order = np.lexsort((w["beta"], w["alpha"]))
+    a, b, C = w["alpha"][order], w["beta"][order], C[order]
+    T = np.zeros((34, 34))
+    V = np.zeros((34,) * 4)
+    ctx.set_integrals(T, V)
+    ctx.set_dets(a, b)
+    R = _rdm_check(ctx, oracle, 34, a, b, C)
+    ordm = R["aa"] + R["bb"]
+    trdm = R["aaaa"] + R["bbbb"] + R["aabb"] + R["aabb"].transpose(2, 3, 0, 1)
+    assert abs(np.abs(ordm).sum() - 8.0000005763) < 1e-6
+    assert abs(np.abs(trdm).sum() - 44.1092472977) < 1e-6

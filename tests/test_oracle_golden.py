@@ -1,0 +1,121 @@
+"""The CPU oracle pinned against the reference's own golden vectors and known
+answers (external/macis/tests, external/macis/python/tests).  No GPU."""
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, load_package
+
+
+def _h2o_cisd(pkg):
+    d = pkg.determinants
+    a, b = d.cisd_space(24, *d.canonical_hf(5, 5))
+    return d.spin_sort(a, b)
+
+
+def test_fci_order_matches_generate_combs(oracle, pkg):
+    # prev_permutation order == lexicographic combinations
+    for n, k in [(6, 3), (8, 4), (10, 3), (12, 6)]:
+        assert np.array_equal(oracle.combs(n, k), pkg.determinants.combs(n, k))
+    a, b = pkg.determinants.fci_space(6, 3, 2)
+    oa, ob = oracle.fci_dets(6, 3, 2)
+    assert np.array_equal(a, oa) and np.array_equal(b, ob)
+    assert a[0] == 0b111 and b[0] == 0b11  # first string = lowest orbitals (HF)
+
+
+def test_h2o_cisd_csr_matches_reference_rowptr(oracle, pkg, h2o, known):
+    """external/macis/tests/csr_hamiltonian.cxx:46-106: n, nnz and rowptr."""
+    a, b = _h2o_cisd(pkg)
+    ref = known["h2o_cisd_csr"]
+    assert len(a) == ref["n"]
+    H = oracle.Hamiltonian(h2o["T"], h2o["V"])
+    M = oracle.build_csr(H, a, b, ref["thresh"])
+    rp, ci, nz = M.arrays()
+    assert M.nnz == ref["nnz"]
+    golden = np.load(GOLDEN + "/h2o_ccpvdz_cisd_rowptr.npy")
+    assert np.array_equal(rp, golden.astype(np.int64))
+    # columns sorted within rows, symmetric pattern
+    for i in range(0, len(a), 997):
+        cols = ci[rp[i]:rp[i + 1]]
+        assert np.all(np.diff(cols) > 0)
+
+
+def test_h2o_cisd_davidson_energy(oracle, pkg, h2o, known):
+    """external/macis/tests/davidson.cxx:44-75."""
+    ref = known["h2o_cisd_davidson"]
+    d = pkg.determinants
+    a, b = d.cisd_space(24, *d.canonical_hf(5, 5))  # reference order (not sorted)
+    H = oracle.Hamiltonian(h2o["T"], h2o["V"])
+    M = oracle.build_csr(H, a, b, 1e-16)
+    E, X, it = M.selected_ci_diag(max_m=ref["max_m"], tol=ref["tol"])
+    assert abs(E + h2o["E_core"] - ref["E0_total"]) < ref["atol"]
+    assert abs(np.linalg.norm(X) - 1.0) < 1e-12
+    assert abs(X @ M.spmv(X) - E) < 1e-12
+
+
+def test_n2_casci_energy(oracle, pkg, n2_6e6o, known):
+    """external/macis/python/tests/test_pymacis.py:114-142 (electronic energy)."""
+    ref = known["n2_6e6o_casci"]
+    a, b = pkg.determinants.fci_space(6, 3, 3)
+    assert len(a) == ref["ndets"]
+    H = oracle.Hamiltonian(n2_6e6o["T"], n2_6e6o["V"])
+    M = oracle.build_csr(H, a, b)
+    E, X, _ = M.selected_ci_diag()
+    assert np.isclose(E, ref["E_total"])
+
+
+def test_o2_rdms_pinned_sums_and_identities(oracle, pkg):
+    """external/macis/tests/double_loop.cxx:506-579 (O2 wavefunction, padded
+    to 5000 states with empty determinants)."""
+    w = np.load(GOLDEN + "/o2_wfn.npz")
+    known = {"sum_abs_ordm": 8.0000005763, "sum_abs_trdm": 44.1092472977}
+    n = 34
+    a = np.zeros(5000, dtype=np.uint64)
+    b = np.zeros(5000, dtype=np.uint64)
+    C = np.zeros(5000)
+    m = len(w["alpha"])
+    a[:m], b[:m], C[:m] = w["alpha"], w["beta"], w["coeffs"]
+    C /= np.linalg.norm(C)
+    R = oracle.rdms_spin_dep(n, a, b, C)
+    ordm = R["aa"] + R["bb"]
+    trdm = R["aaaa"] + R["bbbb"] + R["aabb"] + R["aabb"].transpose(2, 3, 0, 1)
+    assert abs(np.abs(ordm).sum() - known["sum_abs_ordm"]) < 1e-6
+    assert abs(np.abs(trdm).sum() - known["sum_abs_trdm"]) < 1e-6
+    assert abs(np.trace(ordm) - (int(w["nalpha"]) + int(w["nbeta"]))) < 1e-6
+    assert np.allclose(ordm, ordm.T, atol=1e-6)
+
+
+def test_rdm_energy_identity_cas(oracle, pkg):
+    """E = T.(g_a+g_b) + V.(G_aaaa+G_bbbb) + 2 V.G_aabb (double_loop.cxx:215-241)."""
+    T, V, _ = pkg.integrals.synthetic_integrals(6, 8, seed=3)
+    a, b = pkg.determinants.fci_space(6, 3, 3)
+    H = oracle.Hamiltonian(T, V)
+    M = oracle.build_csr(H, a, b)
+    E, X, _ = M.selected_ci_diag()
+    R = oracle.rdms_spin_dep(6, a, b, X)
+    E_rdm = (np.sum(T * (R["aa"] + R["bb"])) + np.sum(V * (R["aaaa"] + R["bbbb"]))
+             + 2 * np.sum(V * R["aabb"]))
+    assert abs(E_rdm - E) < 1e-10
+
+
+def test_matrix_element_symmetry_and_diag(oracle, pkg):
+    T, V, _ = pkg.integrals.synthetic_integrals(8, 16, seed=1)
+    assert np.array_equal(V, V.transpose(1, 0, 2, 3)) and np.array_equal(V, V.transpose(2, 3, 0, 1))
+    H = oracle.Hamiltonian(T, V)
+    a, b = pkg.determinants.fci_space(8, 4, 4)
+    M = oracle.build_csr(H, a, b)
+    rp, ci, nz = M.arrays()
+    # symmetric matrix, 361 elements per row for CAS(8,8)
+    assert np.all(np.diff(rp) == 361)
+    import scipy.sparse as sp
+    A = sp.csr_matrix((nz, ci, rp), shape=(len(a), len(a)))
+    assert abs(A - A.T).max() < 1e-14
+
+
+def test_jacobi_syev(oracle):
+    rng = np.random.default_rng(0)
+    A = rng.normal(size=(17, 17))
+    A = A + A.T
+    w, Q = oracle.syev(A)
+    wr = np.linalg.eigvalsh(A)
+    assert np.allclose(w, wr, atol=1e-12)
+    assert np.allclose(Q.T @ A @ Q, np.diag(w), atol=1e-11)
