@@ -1,0 +1,349 @@
+#!/usr/bin/env python
+"""Benchmark: CASCI(12e,12o) time-to-energy on one GB300.
+
+Workload: 853,776 determinants (n_alpha = n_beta = 6 in 12 orbitals), seeded
+synthetic integrals (h1 = diag(-2 + 0.25 p) + N(0, 0.05^2) off-diagonal,
+V = sum over 24 symmetric Cholesky vectors with N(0, 0.1^2) entries).
+One step = the hot path from integrals and determinants resident in HBM to
+the ground-state energy: CSR Hamiltonian build (1.55e9 nonzeros) + Davidson
+to a full-precision residual norm of 1e-8, in the mixed-precision form (FP32
+sigma, FP64 subspace / refinement).  The plain FP64 path is timed beside it.
+
+The CSR (12-19 GB) is far larger than L2 (129 MB), so no L2 flush is needed
+between steps.
+
+  python bench.py [--steps K] [--warmup W] [--impl ours|reference]
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NORB, NEL, NCHOL, SEED = 12, 12, 24, 20261203
+RES_TOL = 1e-8
+WORKLOAD = "CASCI(12e,12o) FP64 integrals, 853,776 determinants, H build + Davidson to |r| < 1e-8"
+METRIC = "casci_12e12o_time_to_energy"
+
+
+def _package():
+    import __graft_entry__ as g
+
+    return g._package()
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = str(gpu_index)
+        self.lines = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", self.gpu, "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ CPU baseline
+def cpu_estimate(T, V, a, b, iters, stride=16, spmv_groups=2):
+    """The reference's CPU algorithm (oracle restatement of MACIS's SDL H
+    build and CSR SpMV, OpenMP on every host core) timed on a bounded sample
+    and scaled to the full CAS(12,12) time-to-energy:
+      build  = time of the SDL count+fill passes for every `stride`-th bra
+               alpha group (an unbiased sample of the symmetric loop) x stride
+               (the per-row sort and threshold passes are left out, which
+               favours the CPU);
+      sigma  = time of the reference SpMV over `spmv_groups` alpha groups of
+               rows x (groups / spmv_groups);
+      total  = build + iters x sigma (Gram-Schmidt and Rayleigh-Ritz omitted,
+               which favours the CPU)."""
+    import oracle
+
+    oracle.build()
+    H = oracle.Hamiltonian(T, V)
+    eps = np.finfo(float).eps
+    ngroups = len(np.unique(a))
+    t0 = time.perf_counter()
+    oracle.sdl_sample(H, a, b, eps, stride, stride // 2)
+    t_build_sample = time.perf_counter() - t0
+    nb = len(a) // ngroups
+    g0 = ngroups // 2
+    M = oracle.build_rows(H, a, b, g0 * nb, (g0 + spmv_groups) * nb, eps)
+    x = np.random.default_rng(0).normal(size=len(a))
+    M.spmv_block(x)
+    reps = 5
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        M.spmv_block(x)
+    t_spmv_sample = (time.perf_counter() - t0) / reps
+    build = t_build_sample * stride
+    sigma = t_spmv_sample * ngroups / spmv_groups
+    total = build + iters * sigma
+    return {"value": total, "unit": "s", "cores": oracle.num_threads(), "kind": "port",
+            "sample": ("SDL count+fill for every %d-th of %d bra alpha groups (%.2f s) scaled x%d; "
+                       "CSR sigma over %d of %d alpha groups of rows (%.4f s) scaled x%.0f; "
+                       "%d sigma applications (the FP64 Davidson iteration count)"
+                       % (stride, ngroups, t_build_sample, stride, spmv_groups, ngroups, t_spmv_sample,
+                          ngroups / spmv_groups, iters)),
+            "build_s": build, "sigma_s": sigma}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    pkg = _package()
+    T, V, _ = pkg.integrals.synthetic_integrals(NORB, NCHOL, SEED)
+    a, b = pkg.determinants.fci_space(NORB, NEL // 2, NEL // 2)
+    iters = args.fp64_iters
+    vals = []
+    cb = None
+    for step in range(args.warmup + args.steps):
+        # each step: a smaller bounded sample, so the whole run takes minutes
+        cb = cpu_estimate(T, V, a, b, iters, stride=args.cpu_stride)
+        if step >= args.warmup:
+            vals.append(cb["value"])
+    v = float(np.mean(vals))
+    cb["value"] = v
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "norb": NORB, "nalpha": NEL // 2, "nbeta": NEL // 2,
+                       "n_chol": NCHOL, "seed": SEED, "res_tol": RES_TOL},
+            "cpu_baseline": cb, "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+# ------------------------------------------------------------------ GPU arm
+def run_ours(args):
+    import torch
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+    torch.cuda.set_device(local)
+    pkg = _package()
+    pkg.build.build()
+    capi = pkg.capi
+    T, V, _ = pkg.integrals.synthetic_integrals(NORB, NCHOL, SEED)
+    a, b = capi.fci_dets(NORB, NEL // 2, NEL // 2)
+    N = len(a)
+    stream = torch.cuda.current_stream()
+    ctx = capi.Context(local)
+    ctx.set_stream(stream.cuda_stream)
+    ctx.set_integrals(T, V)
+    ctx.set_dets(a, b)
+
+    def ev():
+        e = torch.cuda.Event(enable_timing=True)
+        e.record(stream)
+        return e
+
+    def step(storage, precision):
+        e0 = ev()
+        ctx.build_hamiltonian(storage=storage)
+        e1 = ev()
+        E, _, info = ctx.davidson(tol=RES_TOL, precision=precision, want_vector=False)
+        e2 = ev()
+        torch.cuda.synchronize()
+        return E, info, e0.elapsed_time(e1) / 1e3, e1.elapsed_time(e2) / 1e3
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    # plain FP64 path (the reference's precision) for the comparison
+    E64, info64, hb64, dv64 = step(capi.H_FP64, capi.PREC_FP64)
+    nnz = ctx.nnz
+    # FP64 SpMV roofline (FP64 values + int32 columns)
+    x64 = torch.randn(N, dtype=torch.float64, device="cuda")
+    y64 = torch.empty_like(x64)
+    t_spmv64 = time_spmv(ctx, capi.PREC_FP64, x64, y64, stream)
+    fp64_times = []
+    for _ in range(max(1, min(args.steps, 2))):
+        _, _, h, d = step(capi.H_FP64, capi.PREC_FP64)
+        fp64_times.append(h + d)
+    # mixed path: warm-up, then the timed steps
+    for _ in range(args.warmup):
+        step(capi.H_SPLIT32, capi.PREC_MIXED)
+    barrier()
+    launches0 = capi.kernel_launches()
+    times, hbs, dvs, infos, Es = [], [], [], [], []
+    with ClockSampler(local) as clk:
+        barrier()
+        t_wall = time.perf_counter()
+        for _ in range(args.steps):
+            E, info, h, d = step(capi.H_SPLIT32, capi.PREC_MIXED)
+            times.append(h + d)
+            hbs.append(h)
+            dvs.append(d)
+            infos.append(info)
+            Es.append(E)
+        barrier()
+        t_wall = time.perf_counter() - t_wall
+    launches = capi.kernel_launches() - launches0
+    t_step = float(np.mean(times))
+    if world > 1:
+        tt = torch.tensor([t_step], dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_step = float(tt.item())
+    # FP32 SpMV roofline on the split storage (FP32 values + int32 columns)
+    x32 = torch.randn(N, dtype=torch.float32, device="cuda")
+    y32 = torch.empty_like(x32)
+    t_spmv32 = time_spmv(ctx, capi.PREC_MIXED, x32, y32, stream)
+    peak, peak_kind = _peaks()
+    bytes32 = nnz * 8 + (N + 1) * 8 + N * 4 + N * 4
+    bytes64 = nnz * 12 + (N + 1) * 8 + N * 8 + N * 8
+    achieved32 = bytes32 / t_spmv32 / 1e9
+    achieved64 = bytes64 / t_spmv64 / 1e9
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "spmv_traffic.json")
+    if os.path.exists(tp):
+        traffic = json.load(open(tp)).get("spmv_fp32_dram_bytes_per_launch")
+
+    # end to end through the C ABI with host buffers: integrals in, energy and
+    # CI vector out (host->device copies of T, V and the determinant list inside)
+    ctx_e2e = capi.Context(local)
+    e2e_times = []
+    for i in range(1 + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        Ee, Ce, _ = ctx_e2e.casci(T, V, NEL // 2, NEL // 2, tol=RES_TOL, precision=capi.PREC_MIXED)
+        torch.cuda.synchronize()
+        if i > 0:
+            e2e_times.append(time.perf_counter() - t0)
+    ctx_e2e.close()
+    h2d = T.nbytes + V.nbytes + 2 * N * 8
+    d2h = N * 8 + 8
+
+    cb = None
+    if rank == 0 and not args.no_cpu:
+        cb = cpu_estimate(T, V, np.asarray(a), np.asarray(b), info64["iterations"] + 1, stride=args.cpu_stride)
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": t_step, "unit": "s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 sigma / f64 subspace+refinement", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "norb": NORB, "nalpha": NEL // 2, "nbeta": NEL // 2, "ndets": N,
+                   "nnz": nnz, "n_chol": NCHOL, "seed": SEED, "res_tol": RES_TOL, "precision": "mixed",
+                   "l2": "inputs larger than L2 (CSR %.1f GB), no flush" % (nnz * 12 / 1e9),
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "roofline": {"bound": "hbm", "kernel": "k_spmv_csr<float> (FP32 sigma)", "achieved": achieved32,
+                     "peak": peak, "unit": "GB/s", "frac": achieved32 / peak, "peak_source": peak_kind,
+                     "traffic": traffic, "algorithmic_bytes": bytes32, "launch_ms": t_spmv32 * 1e3},
+        "spmv_fp64": {"achieved_gbs": achieved64, "frac": achieved64 / peak, "launch_ms": t_spmv64 * 1e3,
+                      "algorithmic_bytes": bytes64},
+        "hbuild_s": float(np.mean(hbs)), "davidson_s": float(np.mean(dvs)),
+        "davidson": {k: infos[-1][k] for k in ("iterations", "spmv_fp64", "spmv_fp32", "restarts", "residual_norm")},
+        "fp64_path": {"time_to_energy_s": float(np.mean(fp64_times)), "hbuild_s": hb64, "davidson_s": dv64,
+                      "iterations": info64["iterations"], "energy": E64},
+        "mixed_speedup_vs_fp64": float(np.mean(fp64_times)) / t_step,
+        "energy": Es[-1], "energy_error_vs_fp64": abs(Es[-1] - E64),
+        "e2e": {"value": float(np.mean(e2e_times)), "unit": "s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "energy_error_vs_fp64": abs(Ee - E64)},
+        "gpu_launches": launches, "wall_s_timed": t_wall,
+        "clocks": clk.summary(),
+        "cpu_baseline": cb,
+    }
+    print(json.dumps(line))
+
+
+def time_spmv(ctx, precision, x, y, stream, reps=20):
+    import torch
+
+    for _ in range(3):
+        ctx.spmv_device(x.data_ptr(), y.data_ptr(), precision)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        ctx.spmv_device(x.data_ptr(), y.data_ptr(), precision)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / 1e3 / reps
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-stride", type=int, default=16)
+    ap.add_argument("--fp64-iters", type=int, default=36,
+                    help="reference arm: sigma applications of the FP64 Davidson (measured on the GPU path)")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

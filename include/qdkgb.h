@@ -156,8 +156,10 @@ int qdkgb_rdms_spin_dep(qdkgb_context* ctx, const double* C, double* ordm_aa, do
 int qdkgb_casci(qdkgb_context* ctx, int norb, int nalpha, int nbeta, const double* T, const double* V, int layout,
                 const qdkgb_davidson_settings* s, double matel_tol, double* E, double* C, qdkgb_davidson_info* info);
 
-/* ------------------------------------------------------------ version */
+/* ------------------------------------------------------------ version, counters */
 const char* qdkgb_version(void);
+/* Number of kernel launches this library has issued in this process. */
+int64_t qdkgb_kernel_launches(void);
 
 #ifdef __cplusplus
 }

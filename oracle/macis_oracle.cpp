@@ -674,6 +674,158 @@ void rdms_spin_dep(const uint64_t* alpha, const uint64_t* beta, int64_t nd, cons
   }
 }
 
+// A bounded sample of the reference's symmetric SDL H build for timing on the
+// host: the count and fill passes of build_csr_sdl (sorted_double_loop.hpp:
+// 137-360) for the bra alpha groups ib = offset, offset + stride, ...
+// (each against all ket groups >= ib, as the reference loops them).  The
+// element values go to thread-local buffers (the per-row sort and the
+// threshold compaction are not part of the sample).  Returns the number of
+// elements the sampled groups produce (each upper-triangle pair counted for
+// both (i,j) and (j,i), as the reference stores them).
+int64_t sdl_sample(const Ham& H, const uint64_t* alpha, const uint64_t* beta, int64_t nd, double thresh,
+                   int64_t stride, int64_t offset) {
+  std::vector<uint64_t> ua;
+  std::vector<int64_t> off;
+  unique_alpha(alpha, nd, ua, off);
+  const int64_t nu = (int64_t)ua.size();
+  int64_t total = 0;
+#pragma omp parallel reduction(+ : total)
+  {
+    std::vector<uint32_t> oa, ob;
+    std::vector<double> vals;
+    std::vector<int64_t> cols;
+    int64_t counted = 0;
+#pragma omp for schedule(dynamic)
+    for (int64_t ib = offset; ib < nu; ib += stride) {
+      if (!ua[ib]) continue;
+      const uint64_t ba = ua[ib];
+      bits_to_indices(ba, oa);
+      // count pass
+      for (int64_t ik = ib; ik < nu; ++ik) {
+        const uint64_t ka = ua[ik];
+        if (!ka) continue;
+        const uint64_t exa = ba ^ ka;
+        const int ca = popc(exa);
+        if (ca > 4) continue;
+        if (ca == 4 && std::abs(H.me_4(ba, ka, exa)) < thresh) continue;
+        for (int64_t i = off[ib]; i < off[ib + 1]; ++i)
+          for (int64_t j = off[ik]; j < off[ik + 1]; ++j) {
+            if (j < i) continue;
+            const uint64_t exb = beta[i] ^ beta[j];
+            const int cb = popc(exb);
+            if (ca + cb > 4) continue;
+            if (cb == 4 && std::abs(H.me_4(beta[i], beta[j], exb)) < thresh) continue;
+            counted += (i != j) ? 2 : 1;
+          }
+      }
+      // fill pass
+      for (int64_t ik = ib; ik < nu; ++ik) {
+        const uint64_t ka = ua[ik];
+        if (!ka) continue;
+        const uint64_t exa = ba ^ ka;
+        const int ca = popc(exa);
+        if (ca > 4) continue;
+        for (int64_t i = off[ib]; i < off[ib + 1]; ++i) {
+          const uint64_t bb = beta[i];
+          bits_to_indices(bb, ob);
+          for (int64_t j = off[ik]; j < off[ik + 1]; ++j) {
+            if (j < i) continue;
+            const uint64_t kb = beta[j];
+            const uint64_t exb = bb ^ kb;
+            const int cb = popc(exb);
+            if (ca + cb > 4) continue;
+            double h;
+            if (ca == 4) {
+              h = H.me_4(ba, ka, exa);
+              if (std::abs(h) < thresh) continue;
+            } else if (cb == 4) {
+              h = H.me_4(bb, kb, exb);
+              if (std::abs(h) < thresh) continue;
+            } else if (ca == 2) {
+              h = (cb == 2) ? H.me_22(ba, ka, exa, bb, kb, exb) : H.me_2(ba, ka, exa, oa, ob);
+            } else if (cb == 2) {
+              h = H.me_2(bb, kb, exb, ob, oa);
+            } else {
+              h = H.me_diag(oa, ob);
+            }
+            vals.push_back(h);
+            cols.push_back(j);
+          }
+        }
+      }
+      vals.clear();
+      cols.clear();
+    }
+    total += counted;
+  }
+  return total;
+}
+
+// The rows [r0, r1) of the CSR (a whole number of alpha groups) against all
+// kets, with the reference's non-symmetric SDL loop (is_symm == false):
+// every ket group, every beta pair, values with the row determinant as bra,
+// per-row sort, |h| > thresh.  Used to time a sample of the CPU sigma.
+Csr* build_rows(const Ham& H, const uint64_t* alpha, const uint64_t* beta, int64_t nd, double thresh, int64_t r0,
+                int64_t r1) {
+  std::vector<uint64_t> ua;
+  std::vector<int64_t> off;
+  unique_alpha(alpha, nd, ua, off);
+  const int64_t nu = (int64_t)ua.size();
+  const int64_t nr = r1 - r0;
+  std::vector<std::vector<std::pair<int64_t, double>>> rows(nr);
+#pragma omp parallel
+  {
+    std::vector<uint32_t> oa, ob;
+#pragma omp for schedule(dynamic)
+    for (int64_t i = r0; i < r1; ++i) {
+      const uint64_t ba = alpha[i], bb = beta[i];
+      if (!ba) continue;
+      bits_to_indices(ba, oa);
+      bits_to_indices(bb, ob);
+      auto& row = rows[i - r0];
+      for (int64_t ik = 0; ik < nu; ++ik) {
+        const uint64_t ka = ua[ik];
+        if (!ka) continue;
+        const uint64_t exa = ba ^ ka;
+        const int ca = popc(exa);
+        if (ca > 4) continue;
+        for (int64_t j = off[ik]; j < off[ik + 1]; ++j) {
+          const uint64_t kb = beta[j];
+          const uint64_t exb = bb ^ kb;
+          const int cb = popc(exb);
+          if (ca + cb > 4) continue;
+          double h;
+          if (ca == 4)
+            h = H.me_4(ba, ka, exa);
+          else if (cb == 4)
+            h = H.me_4(bb, kb, exb);
+          else if (ca == 2)
+            h = (cb == 2) ? H.me_22(ba, ka, exa, bb, kb, exb) : H.me_2(ba, ka, exa, oa, ob);
+          else if (cb == 2)
+            h = H.me_2(bb, kb, exb, ob, oa);
+          else
+            h = H.me_diag(oa, ob);
+          if (thresh > 0 && !(std::abs(h) > thresh)) continue;
+          row.push_back({j, h});
+        }
+      }
+      std::sort(row.begin(), row.end());
+    }
+  }
+  Csr* M = new Csr;
+  M->n = nr;
+  M->rowptr.assign(nr + 1, 0);
+  for (int64_t i = 0; i < nr; ++i) M->rowptr[i + 1] = M->rowptr[i] + (int64_t)rows[i].size();
+  M->colind.resize(M->rowptr[nr]);
+  M->nzval.resize(M->rowptr[nr]);
+  for (int64_t i = 0; i < nr; ++i)
+    for (size_t k = 0; k < rows[i].size(); ++k) {
+      M->colind[M->rowptr[i] + k] = rows[i][k].first;
+      M->nzval[M->rowptr[i] + k] = rows[i][k].second;
+    }
+  return M;
+}
+
 thread_local char g_err[512];
 template <class F>
 int guard(F&& f) {
@@ -782,6 +934,19 @@ int orc_selected_ci_diag(void* m, int64_t max_m, double tol, double* X, double* 
 }
 
 void orc_syev(int k, double* A, double* w) { jacobi_syev(k, A, k, w); }
+
+int64_t orc_sdl_sample(void* h, const uint64_t* alpha, const uint64_t* beta, int64_t nd, double thresh, int64_t stride,
+                       int64_t offset) {
+  return sdl_sample(*(Ham*)h, alpha, beta, nd, thresh, stride, offset);
+}
+void* orc_csr_build_rows(void* h, const uint64_t* alpha, const uint64_t* beta, int64_t nd, double thresh, int64_t r0,
+                         int64_t r1) {
+  Csr* M = nullptr;
+  if (guard([&] { M = build_rows(*(Ham*)h, alpha, beta, nd, thresh, r0, r1); })) return nullptr;
+  return M;
+}
+// y[0:rows) = block * x (x over all columns)
+void orc_csr_spmv_block(void* m, const double* x, double* y) { spmv(*(Csr*)m, x, y); }
 
 void orc_rdms_spin_dep(int n, const uint64_t* alpha, const uint64_t* beta, int64_t nd, const double* C, double* aa,
                        double* bb, double* aaaa, double* bbbb, double* aabb) {

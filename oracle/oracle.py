@@ -57,6 +57,11 @@ def lib():
         L.orc_selected_ci_diag.argtypes = [vp, i64, f64, _f64p, ctypes.POINTER(f64), ctypes.POINTER(i64)]
         L.orc_syev.argtypes = [ci, _f64p, _f64p]
         L.orc_rdms_spin_dep.argtypes = [ci, _u64p, _u64p, i64, _f64p] + [ctypes.c_void_p] * 5
+        L.orc_sdl_sample.restype = i64
+        L.orc_sdl_sample.argtypes = [vp, _u64p, _u64p, i64, f64, i64, i64]
+        L.orc_csr_build_rows.restype = vp
+        L.orc_csr_build_rows.argtypes = [vp, _u64p, _u64p, i64, f64, i64, i64]
+        L.orc_csr_spmv_block.argtypes = [vp, _f64p, _f64p]
         _lib = L
     return _lib
 
@@ -193,3 +198,28 @@ def rdms_spin_dep(norb, alpha, beta, C, want=("aa", "bb", "aaaa", "bbbb", "aabb"
         shape = (n, n) if len(k) == 2 else (n, n, n, n)
         res[k] = buf.reshape(shape, order="F")
     return res
+
+
+def sdl_sample(ham, alpha, beta, thresh, stride, offset=0):
+    """Reference SDL count+fill work for every stride-th bra alpha group
+    (timing sample of the CPU H build).  Returns elements produced."""
+    alpha = np.ascontiguousarray(alpha, dtype=np.uint64)
+    beta = np.ascontiguousarray(beta, dtype=np.uint64)
+    return lib().orc_sdl_sample(ham._h, alpha, beta, len(alpha), float(thresh), int(stride), int(offset))
+
+
+class CsrRows(Csr):
+    def spmv_block(self, x):
+        y = np.zeros(self.n)
+        lib().orc_csr_spmv_block(self._m, np.ascontiguousarray(x, dtype=np.float64), y)
+        return y
+
+
+def build_rows(ham, alpha, beta, r0, r1, thresh=np.finfo(np.float64).eps):
+    """CSR rows [r0, r1) against all kets (reference non-symmetric SDL)."""
+    alpha = np.ascontiguousarray(alpha, dtype=np.uint64)
+    beta = np.ascontiguousarray(beta, dtype=np.uint64)
+    h = lib().orc_csr_build_rows(ham._h, alpha, beta, len(alpha), float(thresh), int(r0), int(r1))
+    if not h:
+        raise RuntimeError(lib().orc_last_error().decode())
+    return CsrRows(h, r1 - r0)

@@ -33,7 +33,7 @@ EXPORTED = [
     "qdkgb_create", "qdkgb_destroy", "qdkgb_last_error", "qdkgb_set_stream", "qdkgb_device_bytes",
     "qdkgb_set_integrals", "qdkgb_fci_dets", "qdkgb_set_dets", "qdkgb_build_hamiltonian", "qdkgb_get_csr32",
     "qdkgb_get_csr64", "qdkgb_diagonal", "qdkgb_spmv", "qdkgb_spmv_device", "qdkgb_davidson_default_settings",
-    "qdkgb_davidson", "qdkgb_rdms_spin_dep", "qdkgb_casci", "qdkgb_version",
+    "qdkgb_davidson", "qdkgb_rdms_spin_dep", "qdkgb_casci", "qdkgb_version", "qdkgb_kernel_launches",
 ]
 
 
@@ -94,6 +94,7 @@ def lib():
     L.qdkgb_rdms_spin_dep.argtypes = [vp, vp, vp, vp, vp, vp, vp]
     L.qdkgb_casci.argtypes = [vp, ci, ci, ci, vp, vp, ci, P(DavidsonSettings), dp, P(dp), vp, P(DavidsonInfo)]
     L.qdkgb_version.restype = ctypes.c_char_p
+    L.qdkgb_kernel_launches.restype = ctypes.c_int64
     _lib = L
     return L
 
@@ -118,6 +119,11 @@ def fci_dets(norb, nalpha, nbeta):
     if rc:
         raise QdkgbError(rc, "fci_dets failed")
     return a, b
+
+
+def kernel_launches():
+    """Kernel launches issued by the library in this process."""
+    return lib().qdkgb_kernel_launches()
 
 
 def default_davidson_settings():
@@ -226,12 +232,14 @@ class Context:
     def spmv_device(self, x_ptr, y_ptr, precision=PREC_FP64):
         self._check(lib().qdkgb_spmv_device(self._h, precision, x_ptr, y_ptr))
 
-    def davidson(self, max_m=200, tol=1e-8, precision=PREC_FP64, guess=None):
+    def davidson(self, max_m=200, tol=1e-8, precision=PREC_FP64, guess=None, want_vector=True):
         s = default_davidson_settings()
         s.max_m = max_m
         s.res_tol = tol
         s.precision = precision
         C = np.zeros(self.ndets) if guess is None else _f64(guess).copy()
+        if not want_vector and guess is None:
+            C = None
         s.use_guess = 0 if guess is None else 1
         E = ctypes.c_double()
         info = DavidsonInfo()

@@ -7,7 +7,12 @@
 
 #include "internal.h"
 
+#include <atomic>
+
 namespace qdkgb {
+
+static std::atomic<int64_t> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 void* dev_alloc(Context* c, DeviceBuffer& b, size_t bytes) {
   if (b.ptr && b.bytes >= bytes) return b.ptr;
@@ -115,6 +120,8 @@ static void get_csr(Context* c, I* rowptr, I* colind, double* values) {
 extern "C" {
 
 const char* qdkgb_version(void) { return "qdkgb 0.1 (sm_103a)"; }
+
+int64_t qdkgb_kernel_launches(void) { return g_launches.load(); }
 
 int qdkgb_create(qdkgb_context** out, int device) {
   if (!out) return QDKGB_ERR_INVALID;

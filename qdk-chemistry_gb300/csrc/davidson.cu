@@ -652,7 +652,10 @@ void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C
 
   QDKGB_CUDA(cudaStreamSynchronize(c->stream));
   *E = lam0;
-  if (C) QDKGB_CUDA(cudaMemcpy(C, d.X, N * sizeof(double), cudaMemcpyDeviceToHost));
+  if (C) {
+    QDKGB_CUDA(cudaMemcpyAsync(C, d.X, N * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+  }
   loc.residual_norm = res;
   loc.seconds = std::chrono::duration<double>(clk::now() - t0).count();
   if (info) *info = loc;

@@ -25,7 +25,12 @@ struct Error : std::runtime_error {
                            std::string(#call) + ": " + cudaGetErrorString(e_));                      \
   } while (0)
 
-#define QDKGB_CHECK_LAUNCH() QDKGB_CUDA(cudaGetLastError())
+// Every kernel launch site ends with this check; it also counts the launch.
+#define QDKGB_CHECK_LAUNCH()        \
+  do {                              \
+    ::qdkgb::count_launch();        \
+    QDKGB_CUDA(cudaGetLastError()); \
+  } while (0)
 
 // Device allocation owned by a context (tracked so the context can report and
 // release what it holds).
@@ -36,6 +41,8 @@ struct DeviceBuffer {
 
 struct Context;
 struct Integrals;
+
+void count_launch();
 
 void* dev_alloc(Context* c, DeviceBuffer& b, size_t bytes);  // (re)allocates when too small
 void dev_free(Context* c, DeviceBuffer& b);
