@@ -190,7 +190,9 @@ def run_ours(args):
     T, V, _ = pkg.integrals.synthetic_integrals(NORB, NCHOL, SEED)
     a, b = capi.fci_dets(NORB, NEL // 2, NEL // 2)
     N = len(a)
-    stream = torch.cuda.current_stream()
+    # a real stream (torch's default stream has handle 0, which the library reads as 'use your own')
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     ctx = capi.Context(local)
     ctx.set_stream(stream.cuda_stream)
     ctx.set_integrals(T, V)

@@ -83,10 +83,13 @@ __global__ void k_gemv(const double* __restrict__ A, int64_t lda, int k, const d
     y[i] = s;
   }
 }
-// w *= 1/sqrt(*nrm2) when sqrt(*nrm2) > min_norm
-__global__ void k_normalize(double* w, int64_t n, const double* nrm2, double min_norm) {
+// w *= 1/sqrt(*nrm2) when sqrt(*nrm2) > min_norm, else raise *flag
+__global__ void k_normalize(double* w, int64_t n, const double* nrm2, double min_norm, double* flag) {
   const double nrm = sqrt(*nrm2);
-  if (!(nrm > min_norm)) return;
+  if (!(nrm > min_norm)) {
+    if (flag && blockIdx.x == 0 && threadIdx.x == 0) *flag = 1.;
+    return;
+  }
   const double sc = 1. / nrm;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     w[i] *= sc;
@@ -202,7 +205,7 @@ __global__ void k_store_row(const double* v, int i, double* Hk, int ld) {
 // The working matrices live in shared memory when they fit, otherwise in
 // the global buffers gA / gQ.
 __global__ void __launch_bounds__(1024) k_jacobi(int k, const double* __restrict__ H, int ldh, double* gA,
-                                                 double* gQ, double* eval, double* evec, int max_sweeps) {
+                                                 double* gQ, double* eval, double* evec, int max_sweeps, int warm) {
   extern __shared__ double dyn[];
   __shared__ double s_c[kMaxSubspace / 2 + 1], s_s[kMaxSubspace / 2 + 1];
   __shared__ int s_p[kMaxSubspace / 2 + 1], s_q[kMaxSubspace / 2 + 1];
@@ -212,11 +215,38 @@ __global__ void __launch_bounds__(1024) k_jacobi(int k, const double* __restrict
   double* A = gA ? gA : dyn;
   double* Q = gA ? gQ : dyn + (size_t)k * k;
   const int tid = threadIdx.x, nt = blockDim.x;
-  for (int t = tid; t < k * k; t += nt) {
-    const int i = t % k, j = t / k;
-    const double lowv = (i >= j) ? H[i + (size_t)j * ldh] : H[j + (size_t)i * ldh];
-    A[t] = lowv;
-    Q[t] = (i == j) ? 1. : 0.;
+  if (!warm) {
+    for (int t = tid; t < k * k; t += nt) {
+      const int i = t % k, j = t / k;
+      const double lowv = (i >= j) ? H[i + (size_t)j * ldh] : H[j + (size_t)i * ldh];
+      A[t] = lowv;
+      Q[t] = (i == j) ? 1. : 0.;
+    }
+  } else {
+    // H is the previous (k-1)x(k-1) matrix, already diagonalised by the
+    // previous eigenvectors (evec, ld k-1, eigenvalues eval), bordered by a new
+    // row.  Start from Q = diag(Q_prev, 1): A = Q^T H Q is an arrowhead.
+    const int m1 = k - 1;
+    for (int t = tid; t < k * k; t += nt) {
+      const int i = t % k, j = t / k;
+      Q[t] = (i < m1 && j < m1) ? evec[i + (size_t)m1 * j] : (i == j ? 1. : 0.);
+    }
+    __syncthreads();
+    for (int t = tid; t < k * k; t += nt) {
+      const int i = t % k, j = t / k;
+      double v;
+      if (i < m1 && j < m1) {
+        v = (i == j) ? eval[i] : 0.;
+      } else if (i == m1 && j == m1) {
+        v = H[m1 + (size_t)m1 * ldh];
+      } else {
+        const int c = (i < m1) ? i : j;  // column of Q_prev
+        double acc = 0.;
+        for (int l = 0; l < m1; ++l) acc += Q[l + (size_t)k * c] * H[m1 + (size_t)l * ldh];
+        v = acc;
+      }
+      A[t] = v;
+    }
   }
   __syncthreads();
   const int m = k + (k & 1);
@@ -333,20 +363,26 @@ __global__ void __launch_bounds__(1024) k_jacobi(int k, const double* __restrict
 // ---------------------------------------------------------------- driver
 namespace {
 
+// slots in the small scratch array
+constexpr int kSlotRes = kMaxSubspace + 4;   // residual norm^2 (device reduce target)
+constexpr int kSlotNrm = kMaxSubspace + 8;   // Gram-Schmidt norm^2
+constexpr int kSlotE = kMaxSubspace + 12;    // full-precision Rayleigh quotient
+constexpr int kSlotFlag = kMaxSubspace + 16; // Gram-Schmidt degeneracy flag
+constexpr int kSlotIdx = 3 * kMaxSubspace;   // argmin index (int64)
+
 struct Dav {
   Context* c;
   int64_t n;
   int64_t maxm;
   double *V, *AV, *D, *X, *Hk, *evec, *eval, *partial, *small, *work;
-  float *xf, *yf;
-  int nb;  // blocks for dot products / vector kernels
+  int nb;
   double* gA = nullptr;
   double* gQ = nullptr;
   cudaStream_t st;
+  int warm_k = 0;  // evec/eval hold the decomposition of the leading warm_k x warm_k block
 
   double* col(double* base, int64_t j) { return base + (size_t)j * n; }
 
-  // out[j*stride] = A[:, j] . w, j < k
   void multidot(const double* A, int k, const double* w, double* out, int stride) {
     dim3 g(nb, k);
     k_multidot<<<g, 256, 0, st>>>(A, n, k, w, n, partial);
@@ -354,54 +390,55 @@ struct Dav {
     k_reduce_partials<<<(k + 7) / 8, 256, 0, st>>>(partial, nb, k, out, stride);
     QDKGB_CHECK_LAUNCH();
   }
-  // squared norm of w into *out (device)
   void norm2(const double* w, double* out) { multidot(w, 1, w, out, 1); }
 
-  double fetch(const double* dptr) {
-    QDKGB_CUDA(cudaMemcpyAsync(c->pinned, dptr, sizeof(double), cudaMemcpyDeviceToHost, st));
+  void fetch(const double* a, double& va) {
+    QDKGB_CUDA(cudaMemcpyAsync(c->pinned, a, sizeof(double), cudaMemcpyDeviceToHost, st));
     QDKGB_CUDA(cudaStreamSynchronize(st));
-    return c->pinned[0];
+    va = c->pinned[0];
   }
-  void fetch2(const double* a, const double* b, double& va, double& vb) {
+  // residual norm^2, lowest Ritz value and the pending Gram-Schmidt flag in one sync
+  void fetch3(const double* a, const double* b, double& va, double& vb, bool& flag) {
     QDKGB_CUDA(cudaMemcpyAsync(c->pinned, a, sizeof(double), cudaMemcpyDeviceToHost, st));
     QDKGB_CUDA(cudaMemcpyAsync(c->pinned + 1, b, sizeof(double), cudaMemcpyDeviceToHost, st));
+    QDKGB_CUDA(cudaMemcpyAsync(c->pinned + 2, small + kSlotFlag, sizeof(double), cudaMemcpyDeviceToHost, st));
     QDKGB_CUDA(cudaStreamSynchronize(st));
     va = c->pinned[0];
     vb = c->pinned[1];
+    flag = c->pinned[2] != 0.;
   }
+  void clear_flag() { QDKGB_CUDA(cudaMemsetAsync(small + kSlotFlag, 0, sizeof(double), st)); }
 
-  // gram_schmidt (davidson.hpp:185-238): w against V[:, 0:K], twice; normalise.
-  void gram_schmidt(int K, double* w, double min_norm = 1e-12) {
-    double* inner = small;  // K doubles
-    if (K > 0) {
-      for (int pass = 0; pass < 2; ++pass) {
-        multidot(V, K, w, inner, 1);
-        k_sub_gemv<<<nb, 256, 0, st>>>(V, n, K, inner, w, n);
-        QDKGB_CHECK_LAUNCH();
-      }
-    }
-    double* nrm2 = small + kMaxSubspace + 8;
-    norm2(w, nrm2);
-    const double nv = std::sqrt(fetch(nrm2));
-    if (nv > min_norm) {
-      k_normalize<<<nb, 256, 0, st>>>(w, n, nrm2, min_norm);
+  void orth_passes(int K, double* w) {
+    for (int pass = 0; pass < 2 && K > 0; ++pass) {
+      multidot(V, K, w, small, 1);
+      k_sub_gemv<<<nb, 256, 0, st>>>(V, n, K, small, w, n);
       QDKGB_CHECK_LAUNCH();
-      return;
     }
-    // canonical-vector fallback
+  }
+  // gram_schmidt (davidson.hpp:185-238): two CGS passes against V[:, 0:K],
+  // normalise; a degenerate result raises the device flag (checked at the
+  // next host sync, then repaired by fallback()).
+  void gram_schmidt(int K, double* w, double min_norm = 1e-12) {
+    orth_passes(K, w);
+    norm2(w, small + kSlotNrm);
+    k_normalize<<<nb, 256, 0, st>>>(w, n, small + kSlotNrm, min_norm, small + kSlotFlag);
+    QDKGB_CHECK_LAUNCH();
+  }
+  // canonical-vector fallback of gram_schmidt (davidson.hpp:211-236)
+  void fallback(int K, double* w, double min_norm = 1e-12) {
     for (int64_t idx = 0; idx < n; ++idx) {
       QDKGB_CUDA(cudaMemsetAsync(w, 0, n * sizeof(double), st));
       const double one = 1.0;
       QDKGB_CUDA(cudaMemcpyAsync(w + idx, &one, sizeof(double), cudaMemcpyHostToDevice, st));
-      for (int pass = 0; pass < 2 && K > 0; ++pass) {
-        multidot(V, K, w, inner, 1);
-        k_sub_gemv<<<nb, 256, 0, st>>>(V, n, K, inner, w, n);
+      orth_passes(K, w);
+      norm2(w, small + kSlotNrm);
+      double nv;
+      fetch(small + kSlotNrm, nv);
+      if (std::sqrt(nv) > min_norm) {
+        k_normalize<<<nb, 256, 0, st>>>(w, n, small + kSlotNrm, min_norm, nullptr);
         QDKGB_CHECK_LAUNCH();
-      }
-      norm2(w, nrm2);
-      if (std::sqrt(fetch(nrm2)) > min_norm) {
-        k_normalize<<<nb, 256, 0, st>>>(w, n, nrm2, min_norm);
-        QDKGB_CHECK_LAUNCH();
+        clear_flag();
         return;
       }
     }
@@ -412,25 +449,27 @@ struct Dav {
     const size_t need = 2ull * k * k * sizeof(double);
     const bool in_smem = need <= 200 * 1024;
     const int threads = k <= 32 ? 256 : 1024;
+    const int warm = (warm_k == k - 1 && k >= 2) ? 1 : 0;
     k_jacobi<<<1, threads, in_smem ? need : 0, st>>>(k, Hk, (int)(maxm + 1), in_smem ? nullptr : gA, gQ, eval, evec,
-                                                     60);
+                                                     60, warm);
     QDKGB_CHECK_LAUNCH();
+    warm_k = k;
   }
 
-  // new row i of the projected matrix: Hk(i, c) = V_i . AV_c, c <= i (+ mirror)
+  // new row i of the projected matrix, Hk(i, c) = V_i . AV_c for c <= i,
+  // mirrored (syev reads the lower triangle, rayleigh_ritz.hpp:70-77)
   void projected_row(int i) {
     multidot(AV, i + 1, col(V, i), small, 1);
     k_store_row<<<1, 256, 0, st>>>(small, i, Hk, (int)(maxm + 1));
     QDKGB_CHECK_LAUNCH();
   }
 
-  // X = V C0, R = AV C0 - lam0 X; returns |R|
-  double ritz_residual(int k, double* R) {
+  // X = V C0, R = AV C0 - lam0 X; |R|^2 into small[kSlotRes]
+  void ritz_residual(int k, double* R) {
     k_ritz_residual<<<nb, 256, 0, st>>>(V, AV, n, k, evec, eval, X, R, n, partial);
     QDKGB_CHECK_LAUNCH();
-    k_reduce_partials<<<1, 32, 0, st>>>(partial, nb, 1, small + kMaxSubspace + 4, 1);
+    k_reduce_partials<<<1, 32, 0, st>>>(partial, nb, 1, small + kSlotRes, 1);
     QDKGB_CHECK_LAUNCH();
-    return std::sqrt(fetch(small + kMaxSubspace + 4));
   }
 };
 
@@ -445,6 +484,7 @@ void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C
   const bool mixed = s->precision == QDKGB_PREC_MIXED;
   if (mixed && H.storage != QDKGB_H_SPLIT32)
     throw Error(QDKGB_ERR_STATE, "mixed precision needs the Hamiltonian built with QDKGB_H_SPLIT32 storage");
+  if (s->precision != QDKGB_PREC_FP64 && !mixed) throw Error(QDKGB_ERR_INVALID, "unknown precision");
   if (s->max_m < 2 && N > 1) throw Error(QDKGB_ERR_INVALID, "max_m must be >= 2");
   int64_t max_m = std::min<int64_t>(s->max_m, N);
   if (max_m > kMaxSubspace - 2) throw Error(QDKGB_ERR_INVALID, "max_m above 254 is not supported");
@@ -455,11 +495,11 @@ void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C
   d.n = N;
   d.maxm = max_m;
   d.st = c->stream;
-  d.nb = std::min<int64_t>((N + 255) / 256, (int64_t)c->sm_count * kDotBlocksPerSm);
-  d.nb = std::max(d.nb, 1);
+  d.nb = (int)std::max<int64_t>(1, std::min<int64_t>((N + 255) / 256, (int64_t)c->sm_count * kDotBlocksPerSm));
   d.V = dev_array<double>(c, W.V, (size_t)N * (max_m + 1));
   d.AV = dev_array<double>(c, W.AV, (size_t)N * (max_m + 1));
-  d.X = dev_array<double>(c, W.scratch, (size_t)N * 8);
+  constexpr int kKeep = 6;  // thick-restart size of the mixed path
+  d.X = dev_array<double>(c, W.scratch, (size_t)N * (3 + 2 * kKeep));
   d.work = d.X + N;
   d.Hk = dev_array<double>(c, W.Hk, (size_t)(max_m + 1) * (max_m + 1));
   d.evec = dev_array<double>(c, W.evec, (size_t)(max_m + 1) * (max_m + 1));
@@ -476,6 +516,7 @@ void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C
     attr_set = true;
   }
   d.D = (double*)H.diag.ptr;
+  d.clear_flag();
   float* xf = nullptr;
   float* yf = nullptr;
   if (mixed) {
@@ -497,7 +538,7 @@ void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C
     loc.spmv_fp32++;
   };
 
-  // guess (selected_ci_diag.hpp:130-140)
+  // guess (selected_ci_diag.hpp:130-140, diagonal_guess davidson.hpp:106-113)
   double* V0 = d.V;
   bool use_c = false;
   if (s->use_guess && C) {
@@ -508,7 +549,7 @@ void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C
   if (use_c) {
     QDKGB_CUDA(cudaMemcpyAsync(V0, C, N * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   } else {
-    int64_t* idx = (int64_t*)(d.small + 3 * kMaxSubspace);
+    int64_t* idx = (int64_t*)(d.small + kSlotIdx);
     k_argmin<<<1, 1024, 0, c->stream>>>(d.D, N, idx);
     QDKGB_CHECK_LAUNCH();
     k_set_onehot<<<d.nb, 256, 0, c->stream>>>(V0, N, idx);
@@ -518,8 +559,9 @@ void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C
   if (N == 1) {
     // davidson.hpp:280-288: evaluate the 1x1 operator on X = [1]
     k_set_value<<<1, 1, 0, c->stream>>>(V0, 1.0);
+    QDKGB_CHECK_LAUNCH();
     sigma_full(V0, d.AV);
-    *E = d.fetch(d.AV);
+    d.fetch(d.AV, *E);
     if (C) C[0] = 1.0;
     loc.residual_norm = 0.;
     loc.seconds = std::chrono::duration<double>(clk::now() - t0).count();
@@ -529,14 +571,15 @@ void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C
 
   double lam0 = 0., res = 0.;
   bool converged = false;
-  double* nrm2 = d.small + kMaxSubspace + 8;
 
   if (!mixed) {
-    // ---------------- plain FP64 Davidson, the reference's algorithm
+    // ---------------- plain FP64 Davidson: the reference's algorithm
+    // V1 = GS(A V0) (Krylov start, davidson.hpp:290-299)
     sigma_full(V0, d.AV);
     QDKGB_CUDA(cudaMemcpyAsync(d.col(d.V, 1), d.AV, N * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
     d.gram_schmidt(1, d.col(d.V, 1));
-    d.multidot(d.AV, 1, V0, d.Hk, 1);  // Hk(0,0)
+    d.projected_row(0);
+    d.jacobi(1);
     int64_t iter = 1;
     for (int64_t i = 1; i < max_m; ++i, ++iter) {
       const int k = (int)i + 1;
@@ -544,8 +587,19 @@ void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C
       d.projected_row((int)i);
       d.jacobi(k);
       double* R = d.col(d.V, i + 1);
-      res = d.ritz_residual(k, R);
-      lam0 = d.fetch(d.eval);
+      d.ritz_residual(k, R);
+      double r2 = 0.;
+      bool degenerate = false;
+      d.fetch3(d.small + kSlotRes, d.eval, r2, lam0, degenerate);
+      if (degenerate) {
+        // V[:, i] was not normalisable: repair it and redo this iteration
+        d.fallback((int)i, d.col(d.V, i));
+        d.warm_k = 0;
+        --i;
+        --iter;
+        continue;
+      }
+      res = std::sqrt(r2);
       loc.iterations = iter;
       if (res < s->res_tol) {
         converged = true;
@@ -557,77 +611,87 @@ void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C
     }
   } else {
     // ---------------- mixed: FP32 sigma for new directions, full-precision refresh
-    const double refresh_ratio = 1e-4;
-    const int keep = 3;
-    double* sig = d.work;         // full-precision sigma of the current Ritz vector
-    double* Rt = d.work + N;      // full-precision residual
-    double* tmpV = d.work + 2 * N;               // keep-1 rotated V columns
-    double* tmpAV = d.work + (2 + keep - 1) * N; // keep-1 rotated AV columns
-    double* Eptr = d.small + kMaxSubspace + 12;
-    // column 0 = guess with its exact sigma
+    // The same Krylov-started Davidson runs with FP32 sigma columns until the
+    // residual estimate stops improving (the FP32 noise floor) or has fallen by
+    // `drop` since the last full-precision check.  Then the Ritz vector gets a
+    // full-precision sigma; if its true residual is below res_tol the solve
+    // is done, otherwise the subspace restarts on the kKeep lowest Ritz
+    // vectors, the first carrying the exact sigma, and iterates on.
+    const double drop = 1e-4;
+    double* sig = d.work;
+    double* Rt = d.work + N;
+    double* tmpV = d.work + 2 * N;
+    double* tmpAV = d.work + (2 + kKeep) * N;
+    double* Eptr = d.small + kSlotE;
     sigma_full(V0, d.AV);
-    d.multidot(d.AV, 1, V0, d.Hk, 1);
-    k_axpy_residual<<<d.nb, 256, 0, c->stream>>>(d.AV, V0, d.Hk, Rt, N, d.partial);
+    QDKGB_CUDA(cudaMemcpyAsync(d.col(d.V, 1), d.AV, N * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    d.gram_schmidt(1, d.col(d.V, 1));
+    d.projected_row(0);
+    d.jacobi(1);
+    // residual of the guess (exact): reference level for the first refresh
+    d.multidot(d.AV, 1, V0, Eptr, 1);
+    k_axpy_residual<<<d.nb, 256, 0, c->stream>>>(d.AV, V0, Eptr, Rt, N, d.partial);
     QDKGB_CHECK_LAUNCH();
-    k_reduce_partials<<<1, 32, 0, c->stream>>>(d.partial, d.nb, 1, nrm2, 1);
+    k_reduce_partials<<<1, 32, 0, c->stream>>>(d.partial, d.nb, 1, d.small + kSlotRes, 1);
     QDKGB_CHECK_LAUNCH();
-    double last_true = std::sqrt(d.fetch(nrm2));
-    lam0 = d.fetch(d.Hk);
-    res = last_true;
-    QDKGB_CUDA(cudaMemcpyAsync(d.X, V0, N * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
-    int k = 1;
-    if (res < s->res_tol) converged = true;
-    auto next_from_true_residual = [&]() {
-      QDKGB_CUDA(cudaMemcpyAsync(d.col(d.V, k), Rt, N * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
-      QDKGB_CUDA(cudaMemcpyAsync(d.eval, d.Hk, sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
-      k_precondition<<<d.nb, 256, 0, c->stream>>>(d.col(d.V, k), d.D, Eptr, N, s->min_abs_denominator);
-      QDKGB_CHECK_LAUNCH();
-      d.gram_schmidt(k, d.col(d.V, k));
-    };
-    QDKGB_CUDA(cudaMemcpyAsync(Eptr, d.Hk, sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
-    if (!converged) next_from_true_residual();
+    double last_true = 0.;
+    d.fetch(d.small + kSlotRes, last_true);
+    last_true = std::sqrt(last_true);
+    int k = 1;  // valid columns; V[:, k] holds the next direction
     int64_t iter = 0;
-    double prev_est = 1e300;
-    int stall = 0;
-    while (!converged && iter < 4 * max_m) {
-      // expand with column k (orthonormal, already in V[:, k])
+    double best = 1e300;
+    int since_best = 0;
+    while (iter < 4 * max_m) {
       sigma_sub(d.col(d.V, k), d.col(d.AV, k));
       d.projected_row(k);
       ++k;
       ++iter;
       d.jacobi(k);
       double* R = (k <= max_m - 1) ? d.col(d.V, k) : Rt;
-      const double est = d.ritz_residual(k, R);
-      lam0 = d.fetch(d.eval);
+      d.ritz_residual(k, R);
+      double r2 = 0.;
+      bool degenerate = false;
+      d.fetch3(d.small + kSlotRes, d.eval, r2, lam0, degenerate);
+      if (degenerate) {
+        --k;
+        --iter;
+        d.fallback(k, d.col(d.V, k));
+        d.warm_k = 0;
+        continue;
+      }
+      const double est = std::sqrt(r2);
       loc.iterations = iter;
-      stall = (est > 0.7 * prev_est) ? stall + 1 : 0;
-      prev_est = std::min(prev_est, est);
+      if (est < 0.9 * best) {
+        best = est;
+        since_best = 0;
+      } else {
+        ++since_best;
+      }
       const bool refresh =
-          est < refresh_ratio * last_true || est < 0.5 * s->res_tol || stall >= 4 || k >= max_m - 1;
+          est < 0.5 * s->res_tol || est < drop * last_true || since_best >= 6 || k >= max_m - 1;
       if (!refresh) {
         k_precondition<<<d.nb, 256, 0, c->stream>>>(R, d.D, d.eval, N, s->min_abs_denominator);
         QDKGB_CHECK_LAUNCH();
         d.gram_schmidt(k, R);
         continue;
       }
-      // full-precision sigma, energy and residual of the Ritz vector X (unit norm)
+      // full-precision sigma, Rayleigh quotient and residual of X (unit norm)
       sigma_full(d.X, sig);
       d.multidot(sig, 1, d.X, Eptr, 1);
       k_axpy_residual<<<d.nb, 256, 0, c->stream>>>(sig, d.X, Eptr, Rt, N, d.partial);
       QDKGB_CHECK_LAUNCH();
-      k_reduce_partials<<<1, 32, 0, c->stream>>>(d.partial, d.nb, 1, nrm2, 1);
+      k_reduce_partials<<<1, 32, 0, c->stream>>>(d.partial, d.nb, 1, d.small + kSlotRes, 1);
       QDKGB_CHECK_LAUNCH();
-      d.fetch2(nrm2, Eptr, last_true, lam0);
-      last_true = std::sqrt(last_true);
+      d.fetch3(d.small + kSlotRes, Eptr, r2, lam0, degenerate);
+      last_true = std::sqrt(r2);
       res = last_true;
       loc.restarts++;
       if (res < s->res_tol) {
         converged = true;
         break;
       }
-      // thick restart on the `keep` lowest Ritz vectors: V' = V Q[:, 0:keep],
-      // AV' = AV Q[:, 0:keep]; column 0 = X with its exact sigma.
-      const int kk = std::min(keep, k);
+      // thick restart: V' = V Q[:, 0:kk], AV' = AV Q[:, 0:kk]; column 0 = X with its exact sigma
+      const int kk = std::min(kKeep, k);
       for (int j = 1; j < kk; ++j) {
         k_gemv<<<d.nb, 256, 0, c->stream>>>(d.V, N, k, d.evec + (size_t)j * k, 1, tmpV + (size_t)(j - 1) * N, N);
         QDKGB_CHECK_LAUNCH();
@@ -643,10 +707,16 @@ void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C
                                    cudaMemcpyDeviceToDevice, c->stream));
       }
       for (int j = 0; j < kk; ++j) d.projected_row(j);
+      d.warm_k = 0;
+      d.jacobi(kk);
       k = kk;
-      next_from_true_residual();
-      prev_est = 1e300;
-      stall = 0;
+      // next direction: preconditioned true residual
+      QDKGB_CUDA(cudaMemcpyAsync(d.col(d.V, k), Rt, N * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+      k_precondition<<<d.nb, 256, 0, c->stream>>>(d.col(d.V, k), d.D, Eptr, N, s->min_abs_denominator);
+      QDKGB_CHECK_LAUNCH();
+      d.gram_schmidt(k, d.col(d.V, k));
+      best = 1e300;
+      since_best = 0;
     }
   }
 

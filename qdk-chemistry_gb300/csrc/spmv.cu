@@ -8,8 +8,8 @@
 // and a fixed-order shuffle reduction (deterministic results).
 //   fp64  : FP64 values, FP64 x/y, FP64 FMA
 //   fp32  : FP32 values (the high part of the split storage), FP32 x/y/accumulation
-//   split : (double)hi + (double)lo values, FP64 x/y/accumulation - the
-//           full-precision sigma of the mixed-precision path
+//   split : hi + lo values with float-float products and sums (FP32 pipe),
+//           FP64 x/y - the full-precision sigma of the mixed-precision path
 #include "common.cuh"
 #include "internal.h"
 
@@ -20,13 +20,6 @@ constexpr int kSpmvWarps = 8;
 struct ValF64 {
   const double* v;
   __device__ __forceinline__ double operator()(int64_t k) const { return __ldcs(v + k); }
-};
-struct ValSplit {
-  const float* hi;
-  const float* lo;
-  __device__ __forceinline__ double operator()(int64_t k) const {
-    return (double)__ldcs(hi + k) + (double)__ldcs(lo + k);
-  }
 };
 struct ValF32 {
   const float* v;
@@ -60,6 +53,80 @@ __global__ void __launch_bounds__(kSpmvWarps * 32)
   }
 }
 
+// Full-precision sigma from the split storage without the FP64 pipe (slow on
+// GB300): h = hi + lo and x = xh + xl are float pairs, each product
+// (hi + lo)(xh + xl) is formed with an error-free FP32 product of hi*xh plus
+// the cross terms, and the row sum is kept as an unevaluated float-float pair
+// (two-sum).  Relative accuracy ~2^-44 per product, far below what the
+// defect correction needs; the row result is rounded to FP64 once.
+struct FF {
+  float s, c;
+};
+__device__ __forceinline__ void ff_add(FF& a, float p, float e) {
+  const float t = a.s + p;
+  const float bv = t - a.s;
+  const float err = (a.s - (t - bv)) + (p - bv);
+  a.s = t;
+  a.c += err + e;
+}
+__device__ __forceinline__ FF ff_merge(FF a, FF b) {
+  FF r = a;
+  ff_add(r, b.s, b.c);
+  return r;
+}
+__global__ void __launch_bounds__(kSpmvWarps * 32)
+    k_spmv_split_ff(int64_t n, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                    const float* __restrict__ hi, const float* __restrict__ lo, const float* __restrict__ xh,
+                    const float* __restrict__ xl, double* __restrict__ y) {
+  const int lane = threadIdx.x & 31;
+  const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t r = w0; r < n; r += nw) {
+    const int64_t st = rowptr[r], en = rowptr[r + 1];
+    FF a0{0.f, 0.f}, a1{0.f, 0.f};
+    int64_t k = st + lane;
+    for (; k + 32 < en; k += 64) {
+      const int32_t c0 = __ldcs(col + k), c1 = __ldcs(col + k + 32);
+      const float h0 = __ldcs(hi + k), h1 = __ldcs(hi + k + 32);
+      const float l0 = __ldcs(lo + k), l1 = __ldcs(lo + k + 32);
+      const float x0 = __ldg(xh + c0), x1 = __ldg(xh + c1);
+      const float y0 = __ldg(xl + c0), y1 = __ldg(xl + c1);
+      float p0 = h0 * x0, p1 = h1 * x1;
+      float e0 = fmaf(h0, x0, -p0), e1 = fmaf(h1, x1, -p1);
+      e0 = fmaf(h0, y0, fmaf(l0, x0, e0));
+      e1 = fmaf(h1, y1, fmaf(l1, x1, e1));
+      ff_add(a0, p0, e0);
+      ff_add(a1, p1, e1);
+    }
+    for (; k < en; k += 32) {
+      const int32_t c0 = __ldcs(col + k);
+      const float h0 = __ldcs(hi + k), l0 = __ldcs(lo + k);
+      const float x0 = __ldg(xh + c0), y0 = __ldg(xl + c0);
+      const float p0 = h0 * x0;
+      float e0 = fmaf(h0, x0, -p0);
+      e0 = fmaf(h0, y0, fmaf(l0, x0, e0));
+      ff_add(a0, p0, e0);
+    }
+    FF a = ff_merge(a0, a1);
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+      FF o;
+      o.s = __shfl_xor_sync(QDKGB_FULL_MASK, a.s, d);
+      o.c = __shfl_xor_sync(QDKGB_FULL_MASK, a.c, d);
+      a = (lane & d) ? ff_merge(o, a) : ff_merge(a, o);
+    }
+    if (lane == 0) y[r] = (double)a.s + (double)a.c;
+  }
+}
+__global__ void k_split_x(const double* __restrict__ x, float* __restrict__ xh, float* __restrict__ xl, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double v = x[i];
+    const float h = __double2float_rn(v);
+    xh[i] = h;
+    xl[i] = __double2float_rn(v - (double)h);
+  }
+}
+
 static unsigned spmv_blocks(Context* c, int64_t n) {
   const int64_t want = (n + kSpmvWarps - 1) / kSpmvWarps;
   return (unsigned)std::min<int64_t>(want, (int64_t)c->sm_count * 32);
@@ -73,9 +140,13 @@ void spmv_fp64(Context* c, const double* x, double* y) {
   if (H.storage == QDKGB_H_FP64)
     k_spmv_csr<double, double><<<spmv_blocks(c, H.n), kSpmvWarps * 32, 0, c->stream>>>(
         H.n, rp, ci, ValF64{(const double*)H.val.ptr}, x, y);
-  else
-    k_spmv_csr<double, double><<<spmv_blocks(c, H.n), kSpmvWarps * 32, 0, c->stream>>>(
-        H.n, rp, ci, ValSplit{(const float*)H.hi.ptr, (const float*)H.lo.ptr}, x, y);
+  else {
+    float* xs = dev_array<float>(c, H.xsplit, 2 * (size_t)H.n);
+    k_split_x<<<c->sm_count * 4, 256, 0, c->stream>>>(x, xs, xs + H.n, H.n);
+    QDKGB_CHECK_LAUNCH();
+    k_spmv_split_ff<<<spmv_blocks(c, H.n), kSpmvWarps * 32, 0, c->stream>>>(
+        H.n, rp, ci, (const float*)H.hi.ptr, (const float*)H.lo.ptr, xs, xs + H.n, y);
+  }
   QDKGB_CHECK_LAUNCH();
 }
 
