@@ -28,10 +28,20 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-NORB, NEL, NCHOL, SEED = 12, 12, 24, 20261203
+NORB, NEL, NCHOL, SEED = 12, 12, 24, 20261203  # the headline workload (--norb/--nel/--nchol shrink it for profiling)
 RES_TOL = 1e-8
 WORKLOAD = "CASCI(12e,12o) FP64 integrals, 853,776 determinants, H build + Davidson to |r| < 1e-8"
 METRIC = "casci_12e12o_time_to_energy"
+
+
+def set_workload(norb, nel, nchol):
+    """Smaller CASCI(nel, norb) cases of the same recipe (profiling captures)."""
+    global NORB, NEL, NCHOL, WORKLOAD, METRIC
+    if (norb, nel, nchol) == (NORB, NEL, NCHOL):
+        return
+    NORB, NEL, NCHOL = norb, nel, nchol
+    WORKLOAD = "CASCI(%de,%do) FP64 integrals, H build + Davidson to |r| < 1e-8" % (nel, norb)
+    METRIC = "casci_%de%do_time_to_energy" % (nel, norb)
 
 
 def _package():
@@ -340,7 +350,11 @@ def main():
     ap.add_argument("--fp64-iters", type=int, default=36,
                     help="reference arm: sigma applications of the FP64 Davidson (measured on the GPU path)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--norb", type=int, default=NORB)
+    ap.add_argument("--nel", type=int, default=NEL)
+    ap.add_argument("--nchol", type=int, default=NCHOL)
     args = ap.parse_args()
+    set_workload(args.norb, args.nel, args.nchol)
     if args.impl == "reference":
         run_reference(args)
     else:
