@@ -154,7 +154,7 @@ int qdkgb_destroy(qdkgb_context* c) {
   for (DeviceBuffer* b : {&c->T, &c->V, &c->G_red, &c->V_red, &c->G2, &c->V2, &c->dets.galpha, &c->dets.gstart,
                           &c->dets.det_group, &c->dets.brank, &c->dets.ubeta, &c->dets.gcomplete, &c->dets.acon_ptr,
                           &c->dets.acon_idx, &c->dets.acon_lvl, &c->dets.b2_ptr, &c->dets.b2_idx, &c->dets.b1_ptr,
-                          &c->dets.b1_idx, &c->H.rowptr, &c->H.colind, &c->H.val, &c->H.hi, &c->H.lo, &c->H.diag,
+                          &c->dets.b1_idx, &c->H.rowptr, &c->H.colind, &c->H.val, &c->H.hi, &c->H.lo, &c->H.diag, &c->H.diag_raw,
                           &c->H.row_nnz, &c->H.scan_tmp, &c->H.xsplit, &c->dav.V, &c->dav.AV, &c->dav.xf, &c->dav.yf, &c->dav.Hk,
                           &c->dav.evec, &c->dav.eval, &c->dav.scratch, &c->dav.partial, &c->dav.small})
     dev_free(c, *b);

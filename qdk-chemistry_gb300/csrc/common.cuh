@@ -38,6 +38,17 @@ struct Integrals {
 
 __device__ __forceinline__ double ld(const double* p) { return __ldg(p); }
 
+// Sign flip and |v| > t on the integer pipes.  GB300's FP64 pipe is narrow;
+// flipping the sign bit is bit-identical to multiplying by -1.0, and for
+// finite values |a| > |b| orders like the magnitude bit patterns.
+__device__ __forceinline__ double flip_if(double v, bool neg) {
+  return __longlong_as_double(__double_as_longlong(v) ^ ((long long)neg << 63));
+}
+// tbits < 0 means "keep everything" (threshold <= 0)
+__device__ __forceinline__ bool above_thresh(double v, long long tbits) {
+  return tbits < 0 || (__double_as_longlong(v) & 0x7fffffffffffffffLL) > tbits;
+}
+
 __device__ __forceinline__ double Vat(const Integrals& I, uint32_t p, uint32_t q, uint32_t r, uint32_t s) {
   const size_t n = (size_t)I.n;
   return ld(I.V + p + n * (q + n * (r + n * s)));
@@ -65,7 +76,7 @@ __device__ __forceinline__ double me_same_spin_double(const Integrals& I, uint64
   ex ^= flip;
   SingleEx b = single_ex(bra, ket, ex);
   const double g = Vat(I, a.v, a.o, b.v, b.o) - Vat(I, a.v, b.o, b.v, a.o);
-  return (a.neg != b.neg) ? -g : g;
+  return flip_if(g, a.neg != b.neg);
 }
 
 // matrix_element_22 (matrix_elements.hpp:140-151)
@@ -75,7 +86,7 @@ __device__ __forceinline__ double me_opposite_spin_double(const Integrals& I, ui
   SingleEx a = single_ex(bra_a, ket_a, ex_a);
   SingleEx b = single_ex(bra_b, ket_b, ex_b);
   const double v = Vat(I, a.v, a.o, b.v, b.o);
-  return (a.neg != b.neg) ? -v : v;
+  return flip_if(v, a.neg != b.neg);
 }
 
 // matrix_element_2 (matrix_elements.hpp:169-189): T(v,o) + sum over the bra's
@@ -90,7 +101,7 @@ __device__ __forceinline__ double me_single(const Integrals& I, uint64_t bra, ui
   for (uint64_t m = bra; m; m &= m - 1) h += ld(g + low_bit(m));
   const double* vr = I.V_red + n * (s.v + n * s.o);
   for (uint64_t m = bra_other; m; m &= m - 1) h += ld(vr + low_bit(m));
-  return s.neg ? -h : h;
+  return flip_if(h, s.neg);
 }
 
 // matrix_element_diag (matrix_elements.hpp:203-230)
@@ -132,6 +143,18 @@ __device__ __forceinline__ double matrix_element(const Integrals& I, uint64_t br
   if (ca == 2) return me_single(I, bra_a, ket_a, exa, bra_b);
   if (cb == 2) return me_single(I, bra_b, ket_b, exb, bra_a);
   return me_diag(I, bra_a, bra_b);
+}
+
+// Off-diagonal element (the pair differs), as matrix_element.
+__device__ __forceinline__ double offdiag_element(const Integrals& I, uint64_t bra_a, uint64_t bra_b, uint64_t ket_a,
+                                                  uint64_t ket_b) {
+  const uint64_t exa = bra_a ^ ket_a, exb = bra_b ^ ket_b;
+  const int ca = popc64(exa), cb = popc64(exb);
+  if (ca == 4) return me_same_spin_double(I, bra_a, ket_a, exa);
+  if (cb == 4) return me_same_spin_double(I, bra_b, ket_b, exb);
+  if (ca == 2 && cb == 2) return me_opposite_spin_double(I, bra_a, ket_a, exa, bra_b, ket_b, exb);
+  if (ca == 2) return me_single(I, bra_a, ket_a, exa, bra_b);
+  return me_single(I, bra_b, ket_b, exb, bra_a);
 }
 
 // Warp-wide inclusive scan of an int.

@@ -4,7 +4,8 @@
 //
 // Everything except the convergence test runs on the GPU in FP64: the
 // subspace V and A*V (column-major, N x (max_m+1)), the projected matrix, its
-// eigen-decomposition (one-CTA parallel cyclic Jacobi), the Ritz vector and
+// lowest eigenpair (one-CTA Householder tridiagonalisation + Sturm
+// multisection + inverse iteration), the Ritz vector and
 // residual, the diagonal preconditioner and classical Gram-Schmidt applied
 // twice.  The host reads two scalars per iteration (residual norm, Ritz
 // value) to decide convergence.
@@ -196,167 +197,243 @@ __global__ void k_store_row(const double* v, int i, double* Hk, int ld) {
   }
 }
 
-// ---------------------------------------------------------------- Jacobi
-// One CTA: eigen-decomposition of the symmetric k x k matrix H (leading
-// dimension ldh; the lower triangle, as syev(Uplo::Lower) reads it, is
-// mirrored).  Parallel cyclic Jacobi in round-robin order: each round
-// rotates k/2 disjoint (p,q) pairs at once (rows, then columns).  Eigenvalues
-// ascending into eval, eigenvectors into evec (k x k, column-major, ld = k).
-// The working matrices live in shared memory when they fit, otherwise in
-// the global buffers gA / gQ.
-__global__ void __launch_bounds__(1024) k_jacobi(int k, const double* __restrict__ H, int ldh, double* gA,
-                                                 double* gQ, double* eval, double* evec, int max_sweeps, int warm) {
+// ---------------------------------------------------------------- lowest eigenpairs
+// One CTA: the `nev` lowest eigenpairs of the symmetric k x k matrix H (lower
+// triangle read, as syev(Uplo::Lower)).  Householder reduction to tridiagonal
+// form (O(k^3) once, instead of Jacobi's O(k^3) per sweep - the FP64 pipe of
+// one SM is the budget here), eigenvalues by multisection on the
+// division-free Sturm sequence, eigenvectors by inverse iteration on the
+// tridiagonal matrix (partial pivoting, re-orthogonalised against the lower
+// ones), back-transformed through the reflectors.  Results: eval[0:nev)
+// ascending, evec[:, 0:nev) with leading dimension k.
+constexpr int kEigThreads = 256;
+constexpr int kEigSmemK = 150;  // matrices up to this size live in shared memory
+
+__device__ double block_sum_eig(double v, double* red) {
+  v = warp_sum(v);
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  __syncthreads();
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  double t = 0.;
+  if (threadIdx.x < 32) {
+    t = (lane < (int)(blockDim.x >> 5)) ? red[lane] : 0.;
+    t = warp_sum(t);
+    if (lane == 0) red[32] = t;
+  }
+  __syncthreads();
+  return red[32];
+}
+
+// number of eigenvalues of tridiag(d, e) below x (division-free Sturm sequence
+// of leading minors, rescaled by exact powers of two)
+__device__ int sturm_count(int k, const double* d, const double* e2, double x) {
+  double p0 = 1., p1 = d[0] - x;
+  int cnt = (p1 < 0.) ? 1 : 0;
+  int s_prev = (p1 < 0.) ? -1 : 1;
+  for (int i = 1; i < k; ++i) {
+    double p2 = (d[i] - x) * p1 - e2[i - 1] * p0;
+    const double a2 = fabs(p2);
+    if (a2 > 0x1p+600) {
+      p2 *= 0x1p-600;
+      p1 *= 0x1p-600;
+    } else if (a2 < 0x1p-600 && a2 != 0. && fabs(p1) < 0x1p-600) {
+      p2 *= 0x1p+600;
+      p1 *= 0x1p+600;
+    }
+    int sg = (p2 < 0.) ? -1 : (p2 > 0. ? 1 : -s_prev);
+    if (sg != s_prev) ++cnt;
+    s_prev = sg;
+    p0 = p1;
+    p1 = p2;
+  }
+  return cnt;
+}
+
+__global__ void __launch_bounds__(kEigThreads) k_lowest_eig(int k, const double* __restrict__ H, int ldh,
+                                                            double* gA, int nev, double* eval, double* evec) {
   extern __shared__ double dyn[];
-  __shared__ double s_c[kMaxSubspace / 2 + 1], s_s[kMaxSubspace / 2 + 1];
-  __shared__ int s_p[kMaxSubspace / 2 + 1], s_q[kMaxSubspace / 2 + 1];
-  __shared__ double red[32];
-  __shared__ int rank_of[kMaxSubspace];
-  __shared__ int s_done;
-  double* A = gA ? gA : dyn;
-  double* Q = gA ? gQ : dyn + (size_t)k * k;
+  __shared__ double d[kMaxSubspace], e[kMaxSubspace], e2[kMaxSubspace], beta[kMaxSubspace];
+  __shared__ double red[33];
+  __shared__ double s_lo, s_hi;
+  __shared__ double s_u[3 * kMaxSubspace];
+  double* A = gA ? gA : dyn;  // k x k, column-major; reflector j kept in column j below the diagonal
   const int tid = threadIdx.x, nt = blockDim.x;
-  if (!warm) {
-    for (int t = tid; t < k * k; t += nt) {
-      const int i = t % k, j = t / k;
-      const double lowv = (i >= j) ? H[i + (size_t)j * ldh] : H[j + (size_t)i * ldh];
-      A[t] = lowv;
-      Q[t] = (i == j) ? 1. : 0.;
-    }
-  } else {
-    // H is the previous (k-1)x(k-1) matrix, already diagonalised by the
-    // previous eigenvectors (evec, ld k-1, eigenvalues eval), bordered by a new
-    // row.  Start from Q = diag(Q_prev, 1): A = Q^T H Q is an arrowhead.
-    const int m1 = k - 1;
-    for (int t = tid; t < k * k; t += nt) {
-      const int i = t % k, j = t / k;
-      Q[t] = (i < m1 && j < m1) ? evec[i + (size_t)m1 * j] : (i == j ? 1. : 0.);
-    }
-    __syncthreads();
-    for (int t = tid; t < k * k; t += nt) {
-      const int i = t % k, j = t / k;
-      double v;
-      if (i < m1 && j < m1) {
-        v = (i == j) ? eval[i] : 0.;
-      } else if (i == m1 && j == m1) {
-        v = H[m1 + (size_t)m1 * ldh];
-      } else {
-        const int c = (i < m1) ? i : j;  // column of Q_prev
-        double acc = 0.;
-        for (int l = 0; l < m1; ++l) acc += Q[l + (size_t)k * c] * H[m1 + (size_t)l * ldh];
-        v = acc;
-      }
-      A[t] = v;
-    }
-  }
-  __syncthreads();
-  const int m = k + (k & 1);
-  const int np = m / 2;
-  for (int sweep = 0; sweep < max_sweeps; ++sweep) {
-    double off = 0., tot = 0.;
-    for (int t = tid; t < k * k; t += nt) {
-      const double v = A[t] * A[t];
-      tot += v;
-      if (t % k != t / k) off += v;
-    }
-    off = warp_sum(off);
-    tot = warp_sum(tot);
-    if ((tid & 31) == 0) {
-      red[tid >> 5] = off;
-    }
-    __syncthreads();
-    if (tid == 0) {
-      double o = 0.;
-      for (int w = 0; w < (nt >> 5); ++w) o += red[w];
-      red[31] = o;
-    }
-    __syncthreads();
-    const double off_all = red[31];
-    __syncthreads();
-    if ((tid & 31) == 0) red[tid >> 5] = tot;
-    __syncthreads();
-    if (tid == 0) {
-      double o = 0.;
-      for (int w = 0; w < (nt >> 5); ++w) o += red[w];
-      s_done = !(off_all > 1e-30 * o) ? 1 : 0;
-    }
-    __syncthreads();
-    if (s_done) break;
-    for (int round = 0; round < m - 1; ++round) {
-      for (int i = tid; i < np; i += nt) {
-        int p, q;
-        if (i == 0) {
-          p = round;
-          q = m - 1;
-        } else {
-          p = (round + i) % (m - 1);
-          q = (round - i + (m - 1)) % (m - 1);
-        }
-        if (p > q) {
-          const int t = p;
-          p = q;
-          q = t;
-        }
-        double c = 1., s = 0.;
-        if (q < k) {
-          const double apq = A[p + (size_t)k * q];
-          if (apq != 0.) {
-            const double app = A[p + (size_t)k * p], aqq = A[q + (size_t)k * q];
-            const double theta = (aqq - app) / (2. * apq);
-            const double t = (theta >= 0 ? 1. : -1.) / (fabs(theta) + sqrt(theta * theta + 1.));
-            c = 1. / sqrt(t * t + 1.);
-            s = t * c;
-          }
-        }
-        s_p[i] = p;
-        s_q[i] = (q < k) ? q : -1;
-        s_c[i] = c;
-        s_s[i] = s;
-      }
-      __syncthreads();
-      // rows p, q:  A[p][j] = c A[p][j] - s A[q][j];  A[q][j] = s A[p][j] + c A[q][j]
-      for (int t = tid; t < np * k; t += nt) {
-        const int i = t / k, j = t % k;
-        const int q = s_q[i];
-        if (q < 0 || s_s[i] == 0.) continue;
-        const int p = s_p[i];
-        const double c = s_c[i], s = s_s[i];
-        const double apj = A[p + (size_t)k * j], aqj = A[q + (size_t)k * j];
-        A[p + (size_t)k * j] = c * apj - s * aqj;
-        A[q + (size_t)k * j] = s * apj + c * aqj;
-      }
-      __syncthreads();
-      // columns p, q of A and Q
-      for (int t = tid; t < np * k; t += nt) {
-        const int i = t / k, j = t % k;
-        const int q = s_q[i];
-        if (q < 0 || s_s[i] == 0.) continue;
-        const int p = s_p[i];
-        const double c = s_c[i], s = s_s[i];
-        const double ajp = A[j + (size_t)k * p], ajq = A[j + (size_t)k * q];
-        A[j + (size_t)k * p] = c * ajp - s * ajq;
-        A[j + (size_t)k * q] = s * ajp + c * ajq;
-        const double qjp = Q[j + (size_t)k * p], qjq = Q[j + (size_t)k * q];
-        Q[j + (size_t)k * p] = c * qjp - s * qjq;
-        Q[j + (size_t)k * q] = s * qjp + c * qjq;
-      }
-      __syncthreads();
-    }
-  }
-  // ascending order, ties by index
-  for (int t = tid; t < k; t += nt) {
-    const double lt = A[t + (size_t)k * t];
-    int r = 0;
-    for (int j = 0; j < k; ++j) {
-      const double lj = A[j + (size_t)k * j];
-      r += (lj < lt) || (lj == lt && j < t);
-    }
-    rank_of[t] = r;
-  }
-  __syncthreads();
-  for (int t = tid; t < k; t += nt) eval[rank_of[t]] = A[t + (size_t)k * t];
   for (int t = tid; t < k * k; t += nt) {
     const int i = t % k, j = t / k;
-    evec[i + (size_t)k * rank_of[j]] = Q[i + (size_t)k * j];
+    A[t] = (i >= j) ? H[i + (size_t)j * ldh] : H[j + (size_t)i * ldh];
+  }
+  __syncthreads();
+  // ---- Householder tridiagonalisation
+  for (int j = 0; j + 2 < k; ++j) {
+    const int m0 = j + 1;
+    double xx = 0.;
+    for (int i = m0 + tid; i < k; i += nt) xx += A[i + (size_t)k * j] * A[i + (size_t)k * j];
+    xx = block_sum_eig(xx, red);
+    if (tid == 0) {
+      const double x0 = A[m0 + (size_t)k * j];
+      const double nrm = sqrt(xx);
+      if (nrm == 0.) {
+        beta[j] = 0.;
+        e[j] = 0.;
+      } else {
+        const double alpha = (x0 >= 0.) ? -nrm : nrm;
+        const double v0 = x0 - alpha;
+        const double vv = xx - x0 * x0 + v0 * v0;
+        beta[j] = (vv > 0.) ? 2. / vv : 0.;
+        e[j] = alpha;
+        A[m0 + (size_t)k * j] = v0;
+      }
+      d[j] = A[j + (size_t)k * j];
+    }
+    __syncthreads();
+    const double b = beta[j];
+    if (b == 0.) continue;
+    const double* v = A + (size_t)k * j;  // v_i for i >= m0
+    // p = b * A_sub v, kept in column j's upper part?  use the d/e-free scratch: A row j (i < j unused after)
+    // p is stored transiently in e2[] (length k)
+    for (int i = m0 + tid; i < k; i += nt) {
+      double acc = 0.;
+      for (int l = m0; l < k; ++l) acc += A[i + (size_t)k * l] * v[l];
+      e2[i] = b * acc;
+    }
+    __syncthreads();
+    double vp = 0.;
+    for (int i = m0 + tid; i < k; i += nt) vp += v[i] * e2[i];
+    vp = block_sum_eig(vp, red);
+    const double K = 0.5 * b * vp;
+    for (int i = m0 + tid; i < k; i += nt) e2[i] -= K * v[i];  // w
+    __syncthreads();
+    const int m = k - m0;
+    for (int t = tid; t < m * m; t += nt) {
+      const int i = m0 + t % m, l = m0 + t / m;
+      A[i + (size_t)k * l] -= v[i] * e2[l] + e2[i] * v[l];
+    }
+    __syncthreads();
+  }
+  if (tid == 0) {
+    if (k >= 2) {
+      d[k - 2] = A[(k - 2) + (size_t)k * (k - 2)];
+      e[k - 2] = A[(k - 1) + (size_t)k * (k - 2)];
+      beta[k - 2] = 0.;
+    }
+    d[k - 1] = A[(k - 1) + (size_t)k * (k - 1)];
+    if (k >= 1) beta[k - 1] = 0.;
+  }
+  __syncthreads();
+  for (int i = tid; i < k - 1; i += nt) e2[i] = e[i] * e[i];
+  __syncthreads();
+  // ---- eigenvalues: multisection on the Sturm count (one warp: 32 points per round)
+  for (int jv = 0; jv < nev; ++jv) {
+    if (tid == 0) {
+      double lo = 1e300, hi = -1e300;
+      for (int i = 0; i < k; ++i) {
+        const double r = (i > 0 ? fabs(e[i - 1]) : 0.) + (i + 1 < k ? fabs(e[i]) : 0.);
+        lo = fmin(lo, d[i] - r);
+        hi = fmax(hi, d[i] + r);
+      }
+      const double pad = 1e-12 * fmax(1., fmax(fabs(lo), fabs(hi)));
+      s_lo = lo - pad;
+      s_hi = hi + pad;
+    }
+    __syncthreads();
+    if (tid < 32) {
+      for (int round = 0; round < 80; ++round) {
+        const double lo = s_lo, hi = s_hi;
+        if (!(hi - lo > 4e-16 * fmax(fabs(lo), fabs(hi))) || hi - lo < 1e-300) break;
+        const double x = lo + (hi - lo) * (double)(tid + 1) / 33.;
+        const int cnt = sturm_count(k, d, e2, x);
+        const unsigned above = __ballot_sync(QDKGB_FULL_MASK, cnt > jv);
+        const int t = above ? (__ffs(above) - 1) : 32;  // first point with count > jv
+        if (tid == 0) {
+          s_lo = (t == 0) ? lo : lo + (hi - lo) * (double)t / 33.;
+          s_hi = (t == 32) ? hi : lo + (hi - lo) * (double)(t + 1) / 33.;
+        }
+        __syncwarp();
+      }
+      if (tid == 0) eval[jv] = 0.5 * (s_lo + s_hi);
+    }
+    __syncthreads();
+  }
+  // ---- eigenvectors of T: inverse iteration with partial pivoting (thread 0)
+  double* Y = evec;  // k x nev, ld k
+  if (tid == 0) {
+    double* Ua = s_u;
+    double* Ub = s_u + kMaxSubspace;
+    double* Uc = s_u + 2 * kMaxSubspace;
+    for (int jv = 0; jv < nev; ++jv) {
+      double* y = Y + (size_t)k * jv;
+      const double lam0 = eval[jv];
+      const double lam = lam0 + (jv % 2 ? 1. : -1.) * 1e-17 * fmax(1., fabs(lam0));
+      for (int i = 0; i < k; ++i) y[i] = 1.0 + 0.01 * (double)((i * 7 + jv * 3) % 11);
+      for (int it = 0; it < 3; ++it) {
+        // forward elimination of T - lam I (rows i: [a b c] at columns i, i+1, i+2)
+        double a_i = d[0] - lam, b_i = (k > 1) ? e[0] : 0., c_i = 0., yi = y[0];
+        for (int i = 0; i < k - 1; ++i) {
+          const double a1 = e[i], b1 = d[i + 1] - lam, c1 = (i + 2 < k) ? e[i + 1] : 0., y1 = y[i + 1];
+          if (fabs(a_i) >= fabs(a1)) {
+            const double f = (a_i != 0.) ? a1 / a_i : 0.;
+            Ua[i] = a_i;
+            Ub[i] = b_i;
+            Uc[i] = c_i;
+            y[i] = yi;
+            a_i = b1 - f * b_i;
+            b_i = c1 - f * c_i;
+            yi = y1 - f * yi;
+          } else {
+            const double f = a_i / a1;
+            Ua[i] = a1;
+            Ub[i] = b1;
+            Uc[i] = c1;
+            y[i] = y1;
+            const double na = b_i - f * b1, nb = c_i - f * c1;
+            yi = yi - f * y1;
+            a_i = na;
+            b_i = nb;
+          }
+          c_i = 0.;
+        }
+        Ua[k - 1] = a_i;
+        y[k - 1] = yi;
+        double big = 0.;
+        for (int i = k - 1; i >= 0; --i) {
+          double r = y[i];
+          if (i + 1 < k) r -= Ub[i] * y[i + 1];
+          if (i + 2 < k) r -= Uc[i] * y[i + 2];
+          const double piv = (Ua[i] != 0.) ? Ua[i] : 1e-300;
+          y[i] = r / piv;
+          big = fmax(big, fabs(y[i]));
+        }
+        // rescale to avoid overflow, orthogonalise against lower vectors, normalise
+        for (int i = 0; i < k; ++i) y[i] /= big;
+        for (int q = 0; q < jv; ++q) {
+          const double* z = Y + (size_t)k * q;
+          double dz = 0.;
+          for (int i = 0; i < k; ++i) dz += z[i] * y[i];
+          for (int i = 0; i < k; ++i) y[i] -= dz * z[i];
+        }
+        double nrm = 0.;
+        for (int i = 0; i < k; ++i) nrm += y[i] * y[i];
+        nrm = sqrt(nrm);
+        for (int i = 0; i < k; ++i) y[i] /= nrm;
+      }
+    }
+  }
+  __syncthreads();
+  // ---- back-transform: y <- H_0 H_1 ... H_{k-3} y
+  for (int j = k - 3; j >= 0; --j) {
+    const double b = beta[j];
+    if (b == 0.) continue;
+    const int m0 = j + 1;
+    const double* v = A + (size_t)k * j;
+    for (int jv = 0; jv < nev; ++jv) {
+      double* y = Y + (size_t)k * jv;
+      double dv = 0.;
+      for (int i = m0 + tid; i < k; i += nt) dv += v[i] * y[i];
+      dv = block_sum_eig(dv, red);
+      for (int i = m0 + tid; i < k; i += nt) y[i] -= b * dv * v[i];
+      __syncthreads();
+    }
   }
 }
 
@@ -377,9 +454,7 @@ struct Dav {
   double *V, *AV, *D, *X, *Hk, *evec, *eval, *partial, *small, *work;
   int nb;
   double* gA = nullptr;
-  double* gQ = nullptr;
   cudaStream_t st;
-  int warm_k = 0;  // evec/eval hold the decomposition of the leading warm_k x warm_k block
 
   double* col(double* base, int64_t j) { return base + (size_t)j * n; }
 
@@ -445,15 +520,12 @@ struct Dav {
     throw Error(QDKGB_ERR_INVALID, "gram_schmidt: Unable to find orthogonal vector");
   }
 
-  void jacobi(int k) {
-    const size_t need = 2ull * k * k * sizeof(double);
-    const bool in_smem = need <= 200 * 1024;
-    const int threads = k <= 32 ? 256 : 1024;
-    const int warm = (warm_k == k - 1 && k >= 2) ? 1 : 0;
-    k_jacobi<<<1, threads, in_smem ? need : 0, st>>>(k, Hk, (int)(maxm + 1), in_smem ? nullptr : gA, gQ, eval, evec,
-                                                     60, warm);
+  // lowest `nev` eigenpairs of the leading k x k projected matrix
+  void lowest(int k, int nev = 1) {
+    const bool in_smem = k <= kEigSmemK;
+    k_lowest_eig<<<1, kEigThreads, in_smem ? (size_t)k * k * sizeof(double) : 0, st>>>(
+        k, Hk, (int)(maxm + 1), in_smem ? nullptr : gA, std::min(nev, k), eval, evec);
     QDKGB_CHECK_LAUNCH();
-    warm_k = k;
   }
 
   // new row i of the projected matrix, Hk(i, c) = V_i . AV_c for c <= i,
@@ -506,13 +578,11 @@ void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C
   d.eval = dev_array<double>(c, W.eval, (size_t)(max_m + 1));
   d.partial = dev_array<double>(c, W.partial, (size_t)d.nb * (kMaxSubspace + 2));
   d.small = dev_array<double>(c, W.small, 4 * kMaxSubspace);
-  if (2ull * (max_m + 1) * (max_m + 1) * 8 > 200 * 1024) {
-    d.gA = dev_array<double>(c, W.yf, 2ull * (max_m + 1) * (max_m + 1));
-    d.gQ = d.gA + (size_t)(max_m + 1) * (max_m + 1);
-  }
+  if (max_m + 1 > kEigSmemK) d.gA = dev_array<double>(c, W.yf, (size_t)(max_m + 1) * (max_m + 1));
   static bool attr_set = false;
   if (!attr_set) {
-    QDKGB_CUDA(cudaFuncSetAttribute(k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    QDKGB_CUDA(cudaFuncSetAttribute(k_lowest_eig, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    kEigSmemK * kEigSmemK * (int)sizeof(double)));
     attr_set = true;
   }
   d.D = (double*)H.diag.ptr;
@@ -579,13 +649,12 @@ void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C
     QDKGB_CUDA(cudaMemcpyAsync(d.col(d.V, 1), d.AV, N * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
     d.gram_schmidt(1, d.col(d.V, 1));
     d.projected_row(0);
-    d.jacobi(1);
     int64_t iter = 1;
     for (int64_t i = 1; i < max_m; ++i, ++iter) {
       const int k = (int)i + 1;
       sigma_full(d.col(d.V, i), d.col(d.AV, i));
       d.projected_row((int)i);
-      d.jacobi(k);
+      d.lowest(k);
       double* R = d.col(d.V, i + 1);
       d.ritz_residual(k, R);
       double r2 = 0.;
@@ -594,7 +663,6 @@ void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C
       if (degenerate) {
         // V[:, i] was not normalisable: repair it and redo this iteration
         d.fallback((int)i, d.col(d.V, i));
-        d.warm_k = 0;
         --i;
         --iter;
         continue;
@@ -627,7 +695,6 @@ void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C
     QDKGB_CUDA(cudaMemcpyAsync(d.col(d.V, 1), d.AV, N * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
     d.gram_schmidt(1, d.col(d.V, 1));
     d.projected_row(0);
-    d.jacobi(1);
     // residual of the guess (exact): reference level for the first refresh
     d.multidot(d.AV, 1, V0, Eptr, 1);
     k_axpy_residual<<<d.nb, 256, 0, c->stream>>>(d.AV, V0, Eptr, Rt, N, d.partial);
@@ -646,7 +713,7 @@ void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C
       d.projected_row(k);
       ++k;
       ++iter;
-      d.jacobi(k);
+      d.lowest(k);
       double* R = (k <= max_m - 1) ? d.col(d.V, k) : Rt;
       d.ritz_residual(k, R);
       double r2 = 0.;
@@ -656,7 +723,6 @@ void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C
         --k;
         --iter;
         d.fallback(k, d.col(d.V, k));
-        d.warm_k = 0;
         continue;
       }
       const double est = std::sqrt(r2);
@@ -692,6 +758,7 @@ void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C
       }
       // thick restart: V' = V Q[:, 0:kk], AV' = AV Q[:, 0:kk]; column 0 = X with its exact sigma
       const int kk = std::min(kKeep, k);
+      d.lowest(k, kk);  // the kk lowest Ritz vectors (column 0 reproduces X)
       for (int j = 1; j < kk; ++j) {
         k_gemv<<<d.nb, 256, 0, c->stream>>>(d.V, N, k, d.evec + (size_t)j * k, 1, tmpV + (size_t)(j - 1) * N, N);
         QDKGB_CHECK_LAUNCH();
@@ -707,8 +774,6 @@ void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C
                                    cudaMemcpyDeviceToDevice, c->stream));
       }
       for (int j = 0; j < kk; ++j) d.projected_row(j);
-      d.warm_k = 0;
-      d.jacobi(kk);
       k = kk;
       // next direction: preconditioned true residual
       QDKGB_CUDA(cudaMemcpyAsync(d.col(d.V, k), Rt, N * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));

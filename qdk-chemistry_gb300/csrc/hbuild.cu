@@ -356,38 +356,123 @@ void build_det_space(Context* c, int64_t nd, const uint64_t* alpha, const uint64
 }
 
 // ------------------------------------------------------------------ CSR rows
+// Diagonal elements, one thread per determinant (matrix_element_diag in the
+// reference's order); alpha-empty determinants get 0 (the reference skips
+// their rows).
+__global__ void k_diag(Integrals I, int64_t n, const int32_t* __restrict__ det_group,
+                       const int32_t* __restrict__ brank, const uint64_t* __restrict__ galpha,
+                       const uint64_t* __restrict__ ubeta, double* __restrict__ D) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    const uint64_t a = galpha[det_group[r]];
+    D[r] = a ? me_diag(I, a, ubeta[brank[r]]) : 0.;
+  }
+}
+
+// Pre-threshold row lengths: the number of connected determinants present in
+// the list.  Integer work only: groups holding every beta string contribute
+// their candidate-list length directly; the others are checked candidate by
+// candidate (binary search or scan).
 __global__ void __launch_bounds__(kRowWarps * 32) k_row_count(RowArgs a, int64_t* __restrict__ row_nnz) {
   __shared__ RowWalkSmem sm;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   for (int64_t r = (int64_t)blockIdx.x * kRowWarps + w; r < a.ndets; r += (int64_t)gridDim.x * kRowWarps) {
+    const int32_t g = a.det_group[r];
+    const int32_t b = a.brank[r];
+    const uint64_t rb = a.ubeta[b];
     int64_t cnt = 0;
-    walk_row(a, r, w, lane, sm, [&](int64_t ket, int64_t row, uint64_t ra, uint64_t rb, uint64_t ka, uint64_t kb) {
-      bool keep = false;
-      if (ket >= 0) {
-        const double v = pair_value(a.I, row, ket, ra, rb, ka, kb);
-        keep = !(a.thresh > 0.) || fabs(v) > a.thresh;
+    if (a.galpha[g] != 0) {
+      const int64_t b1 = a.b1_ptr[b], n1 = a.b1_ptr[b + 1] - b1;
+      const int64_t b2 = a.b2_ptr[b], n2 = a.b2_ptr[b + 1] - b2;
+      const int64_t e_end = a.acon_ptr[g + 1];
+      for (int64_t e0 = a.acon_ptr[g]; e0 < e_end; e0 += 32) {
+        const int64_t e = e0 + lane;
+        int my = 0, h = 0, lvl = 0, mode = kIdent;
+        int64_t direct = 0;
+        if (e < e_end) {
+          h = a.acon_idx[e];
+          lvl = a.acon_lvl[e];
+          const int64_t gs = a.gstart[h + 1] - a.gstart[h];
+          const int64_t cand = lvl == 0 ? n2 : (lvl == 1 ? n1 : 1);
+          if (a.gcomplete[h]) {
+            direct = cand;
+          } else if (gs <= cand) {
+            mode = kScan;
+            my = (int)gs;
+          } else {
+            mode = kSearch;
+            my = (int)cand;
+          }
+        }
+        int64_t dsum = direct;
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) dsum += __shfl_xor_sync(QDKGB_FULL_MASK, dsum, d);
+        cnt += dsum;
+        const int incl = warp_inclusive_scan(my, lane);
+        const int total = __shfl_sync(QDKGB_FULL_MASK, incl, 31);
+        if (total == 0) continue;
+        sm.off[w][lane + 1] = incl;
+        if (lane == 0) sm.off[w][0] = 0;
+        sm.h[w][lane] = h;
+        sm.lvl[w][lane] = (int8_t)lvl;
+        sm.mode[w][lane] = (int8_t)mode;
+        __syncwarp();
+        for (int base = 0; base < total; base += 32) {
+          const int f = base + lane;
+          bool hit = false;
+          if (f < total) {
+            int lo = 0, hi = 31;
+            while (lo < hi) {
+              const int mid = (lo + hi + 1) >> 1;
+              if (sm.off[w][mid] <= f)
+                lo = mid;
+              else
+                hi = mid - 1;
+            }
+            const int k = f - sm.off[w][lo];
+            const int hh = sm.h[w][lo], ll = sm.lvl[w][lo];
+            const int64_t g0 = a.gstart[hh];
+            if (sm.mode[w][lo] == kScan) {
+              hit = popc64(rb ^ a.ubeta[a.brank[g0 + k]]) <= 2 * (2 - ll);
+            } else {
+              const int32_t cr = ll == 0 ? a.b2_idx[b2 + k] : (ll == 1 ? a.b1_idx[b1 + k] : b);
+              hit = find_rank(a.brank, g0, a.gstart[hh + 1], cr) >= 0;
+            }
+          }
+          cnt += __popc(__ballot_sync(QDKGB_FULL_MASK, hit));
+        }
+        __syncwarp();
       }
-      cnt += __popc(__ballot_sync(QDKGB_FULL_MASK, keep));
-    });
+    }
     if (lane == 0) row_nnz[r] = cnt;
   }
 }
 
+// Emission into the pre-threshold slots: each row's kept elements are packed
+// at the start of its slot range (ballot compaction), the kept count is
+// recorded.  Values: the precomputed diagonal, or the off-diagonal element with
+// the lower-index determinant as bra (sorted_double_loop.hpp:325-355).
 template <int STORAGE>
 __global__ void __launch_bounds__(kRowWarps * 32)
-    k_row_emit(RowArgs a, const int64_t* __restrict__ rowptr, int32_t* __restrict__ colind, double* __restrict__ val,
+    k_row_emit(RowArgs a, long long tbits, const double* __restrict__ diag_raw, const int64_t* __restrict__ rowptr,
+               int64_t* __restrict__ kept, int32_t* __restrict__ colind, double* __restrict__ val,
                float* __restrict__ hi, float* __restrict__ lo, double* __restrict__ diag) {
   __shared__ RowWalkSmem sm;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   for (int64_t r = (int64_t)blockIdx.x * kRowWarps + w; r < a.ndets; r += (int64_t)gridDim.x * kRowWarps) {
-    int64_t pos0 = rowptr[r];
+    const int64_t start = rowptr[r];
+    int64_t pos0 = start;
     walk_row(a, r, w, lane, sm, [&](int64_t ket, int64_t row, uint64_t ra, uint64_t rb, uint64_t ka, uint64_t kb) {
       bool keep = false;
       double v = 0.;
       if (ket >= 0) {
-        v = pair_value(a.I, row, ket, ra, rb, ka, kb);
-        keep = !(a.thresh > 0.) || fabs(v) > a.thresh;
-        if (ket == row) diag[row] = keep ? v : 0.;
+        if (ket == row) {
+          v = diag_raw[row];
+          keep = above_thresh(v, tbits);
+          diag[row] = keep ? v : 0.;
+        } else {
+          v = (ket > row) ? offdiag_element(a.I, ra, rb, ka, kb) : offdiag_element(a.I, ka, kb, ra, rb);
+          keep = above_thresh(v, tbits);
+        }
       }
       const unsigned m = __ballot_sync(QDKGB_FULL_MASK, keep);
       if (keep) {
@@ -403,6 +488,31 @@ __global__ void __launch_bounds__(kRowWarps * 32)
       }
       pos0 += __popc(m);
     });
+    if (lane == 0) kept[r] = pos0 - start;
+  }
+}
+
+// Moves each row's kept prefix from its pre-threshold slot range to the final
+// compact position (only when the threshold removed elements).
+template <int STORAGE>
+__global__ void k_row_compact(int64_t n, const int64_t* __restrict__ pre_ptr, const int64_t* __restrict__ new_ptr,
+                              const int32_t* __restrict__ ci, const double* __restrict__ v,
+                              const float* __restrict__ h, const float* __restrict__ l, int32_t* __restrict__ ci2,
+                              double* __restrict__ v2, float* __restrict__ h2, float* __restrict__ l2) {
+  const int lane = threadIdx.x & 31;
+  const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t r = w0; r < n; r += nw) {
+    const int64_t src = pre_ptr[r], dst = new_ptr[r], len = new_ptr[r + 1] - dst;
+    for (int64_t k = lane; k < len; k += 32) {
+      ci2[dst + k] = ci[src + k];
+      if (STORAGE == QDKGB_H_FP64) {
+        v2[dst + k] = v[src + k];
+      } else {
+        h2[dst + k] = h[src + k];
+        l2[dst + k] = l[src + k];
+      }
+    }
   }
 }
 
@@ -434,16 +544,26 @@ void build_hamiltonian(Context* c, double thresh, int storage) {
   if (storage != QDKGB_H_FP64 && storage != QDKGB_H_SPLIT32) throw Error(QDKGB_ERR_INVALID, "unknown storage");
   Hcsr& H = c->H;
   H.valid = false;
-  const int64_t n = c->dets.ndets;
+  DetSpace& D = c->dets;
+  const int64_t n = D.ndets;
   RowArgs a = row_args(c, thresh);
+  long long tbits = -1;
+  if (thresh > 0.) {
+    std::memcpy(&tbits, &thresh, sizeof(double));
+  }
   int64_t* row_nnz = dev_array<int64_t>(c, H.row_nnz, n + 1);
   int64_t* rowptr = dev_array<int64_t>(c, H.rowptr, n + 1);
+  double* diag_raw = dev_array<double>(c, H.diag_raw, n);
+  double* diag = dev_array<double>(c, H.diag, n);
+  const unsigned tblocks = (unsigned)std::min<int64_t>((n + 255) / 256, (int64_t)c->sm_count * 16);
+  k_diag<<<tblocks, 256, 0, c->stream>>>(a.I, n, a.det_group, a.brank, a.galpha, a.ubeta, diag_raw);
+  QDKGB_CHECK_LAUNCH();
   const int64_t blocks = std::min<int64_t>((n + kRowWarps - 1) / kRowWarps, (int64_t)c->sm_count * 64);
   k_row_count<<<(unsigned)blocks, kRowWarps * 32, 0, c->stream>>>(a, row_nnz);
   QDKGB_CHECK_LAUNCH();
   exclusive_scan_i64(c, row_nnz, rowptr, n, H.scan_tmp);
-  int64_t nnz = 0;
-  QDKGB_CUDA(cudaMemcpyAsync(&nnz, rowptr + n, sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
+  int64_t nnz_pre = 0;
+  QDKGB_CUDA(cudaMemcpyAsync(&nnz_pre, rowptr + n, sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
   QDKGB_CUDA(cudaStreamSynchronize(c->stream));
   // release the other storage's arrays before allocating this one
   if (storage == QDKGB_H_FP64) {
@@ -452,24 +572,64 @@ void build_hamiltonian(Context* c, double thresh, int storage) {
   } else {
     dev_free(c, H.val);
   }
-  int32_t* colind = dev_array<int32_t>(c, H.colind, std::max<int64_t>(nnz, 1));
+  const int64_t cap = std::max<int64_t>(nnz_pre, 1);
+  int32_t* colind = dev_array<int32_t>(c, H.colind, cap);
   double* val = nullptr;
   float *hi = nullptr, *lo = nullptr;
   if (storage == QDKGB_H_FP64)
-    val = dev_array<double>(c, H.val, std::max<int64_t>(nnz, 1));
+    val = dev_array<double>(c, H.val, cap);
   else {
-    hi = dev_array<float>(c, H.hi, std::max<int64_t>(nnz, 1));
-    lo = dev_array<float>(c, H.lo, std::max<int64_t>(nnz, 1));
+    hi = dev_array<float>(c, H.hi, cap);
+    lo = dev_array<float>(c, H.lo, cap);
   }
-  double* diag = dev_array<double>(c, H.diag, n);
   QDKGB_CUDA(cudaMemsetAsync(diag, 0, n * sizeof(double), c->stream));
+  // row_nnz now receives the kept counts
   if (storage == QDKGB_H_FP64)
-    k_row_emit<QDKGB_H_FP64><<<(unsigned)blocks, kRowWarps * 32, 0, c->stream>>>(a, rowptr, colind, val, hi, lo, diag);
+    k_row_emit<QDKGB_H_FP64><<<(unsigned)blocks, kRowWarps * 32, 0, c->stream>>>(a, tbits, diag_raw, rowptr, row_nnz,
+                                                                                colind, val, hi, lo, diag);
   else
-    k_row_emit<QDKGB_H_SPLIT32>
-        <<<(unsigned)blocks, kRowWarps * 32, 0, c->stream>>>(a, rowptr, colind, val, hi, lo, diag);
+    k_row_emit<QDKGB_H_SPLIT32><<<(unsigned)blocks, kRowWarps * 32, 0, c->stream>>>(
+        a, tbits, diag_raw, rowptr, row_nnz, colind, val, hi, lo, diag);
   QDKGB_CHECK_LAUNCH();
+  // kept total
+  DeviceBuffer newptr_b, tmp;
+  int64_t* newptr = dev_array<int64_t>(c, newptr_b, n + 1);
+  exclusive_scan_i64(c, row_nnz, newptr, n, H.scan_tmp);
+  int64_t nnz = 0;
+  QDKGB_CUDA(cudaMemcpyAsync(&nnz, newptr + n, sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
   QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+  if (nnz != nnz_pre) {
+    // threshold_parallel's compaction (csr_matrix.hpp:317-372), into fresh arrays
+    DeviceBuffer ci2b, v2b, h2b, l2b;
+    const int64_t cap2 = std::max<int64_t>(nnz, 1);
+    int32_t* ci2 = dev_array<int32_t>(c, ci2b, cap2);
+    double* v2 = storage == QDKGB_H_FP64 ? dev_array<double>(c, v2b, cap2) : nullptr;
+    float* h2 = storage == QDKGB_H_SPLIT32 ? dev_array<float>(c, h2b, cap2) : nullptr;
+    float* l2 = storage == QDKGB_H_SPLIT32 ? dev_array<float>(c, l2b, cap2) : nullptr;
+    const unsigned cblocks = (unsigned)std::min<int64_t>((n + 7) / 8, (int64_t)c->sm_count * 32);
+    if (storage == QDKGB_H_FP64)
+      k_row_compact<QDKGB_H_FP64>
+          <<<cblocks, 256, 0, c->stream>>>(n, rowptr, newptr, colind, val, hi, lo, ci2, v2, h2, l2);
+    else
+      k_row_compact<QDKGB_H_SPLIT32>
+          <<<cblocks, 256, 0, c->stream>>>(n, rowptr, newptr, colind, val, hi, lo, ci2, v2, h2, l2);
+    QDKGB_CHECK_LAUNCH();
+    QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+    std::swap(H.colind, ci2b);
+    dev_free(c, ci2b);
+    if (storage == QDKGB_H_FP64) {
+      std::swap(H.val, v2b);
+      dev_free(c, v2b);
+    } else {
+      std::swap(H.hi, h2b);
+      std::swap(H.lo, l2b);
+      dev_free(c, h2b);
+      dev_free(c, l2b);
+    }
+  }
+  std::swap(H.rowptr, newptr_b);
+  dev_free(c, newptr_b);
+  dev_free(c, tmp);
   H.n = n;
   H.nnz = nnz;
   H.storage = storage;

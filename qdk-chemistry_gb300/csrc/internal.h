@@ -73,7 +73,7 @@ struct Hcsr {
   int64_t n = 0, nnz = 0;
   int storage = QDKGB_H_FP64;
   double thresh = 0.;
-  DeviceBuffer rowptr, colind, val, hi, lo, diag, row_nnz, scan_tmp, xsplit;
+  DeviceBuffer rowptr, colind, val, hi, lo, diag, diag_raw, row_nnz, scan_tmp, xsplit;
   bool valid = false;
 };
 
