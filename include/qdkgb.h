@@ -57,6 +57,7 @@ typedef struct qdkgb_context qdkgb_context;
 /* ------------------------------------------------------------ context */
 int qdkgb_create(qdkgb_context** ctx, int device);
 int qdkgb_destroy(qdkgb_context* ctx);
+/* Message of the last failure; NULL asks for the last failed context-free call. */
 const char* qdkgb_last_error(const qdkgb_context* ctx);
 /* cudaStream_t passed as void*; NULL restores the context's own stream. */
 int qdkgb_set_stream(qdkgb_context* ctx, void* stream);
@@ -155,6 +156,33 @@ int qdkgb_rdms_spin_dep(qdkgb_context* ctx, const double* C, double* ordm_aa, do
  * MACIS determinant order. */
 int qdkgb_casci(qdkgb_context* ctx, int norb, int nalpha, int nbeta, const double* T, const double* V, int layout,
                 const qdkgb_davidson_settings* s, double matel_tol, double* E, double* C, qdkgb_davidson_info* info);
+
+/* ------------------------------------------------------------ allocation-free sigma
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc
+ * while they run: code being captured into a CUDA graph (allocation is not
+ * allowed during stream capture), applications whose device memory is owned
+ * by another allocator (a framework's caching pool, a fixed arena), and
+ * latency-critical loops that must not synchronise.  It is the full-precision
+ * sigma of the split storage (y = (hi + lo) x, float-float products and sums,
+ * FP64 result) on caller-owned device arrays, with its scratch (x split into
+ * two FP32 halves) in a fixed file-scope device array instead of an
+ * allocation.
+ *   - n <= QDKGB_NOALLOC_MAX_ROWS (1,048,576 rows; 8 MiB of scratch that every
+ *     GPU loading the library holds until exit); larger n returns
+ *     QDKGB_ERR_INVALID with the reason in qdkgb_last_error(NULL).
+ *   - rowptr (n+1, int64), colind (int32), hi/lo (FP32, as QDKGB_H_SPLIT32
+ *     stores them), x and y (FP64, n) are device pointers on the current
+ *     device; stream is a cudaStream_t (NULL = legacy default stream).
+ *   - The first call on a device looks up the scratch's device address (once
+ *     per device, with that device current); make that first call before any
+ *     stream capture.
+ *   - The scratch is overwritten completely by every call, so nothing has to
+ *     be cleared; all calls share it, so calls that overlap on the GPU (two
+ *     streams at once) race.
+ *   - No cudaMalloc, cudaFree or allocating library routine is called. */
+#define QDKGB_NOALLOC_MAX_ROWS (1 << 20)
+int qdkgb_sigma_split_noalloc(int64_t n, const int64_t* rowptr, const int32_t* colind, const float* hi,
+                              const float* lo, const double* x, double* y, void* stream);
 
 /* ------------------------------------------------------------ version, counters */
 const char* qdkgb_version(void);

@@ -34,6 +34,7 @@ EXPORTED = [
     "qdkgb_set_integrals", "qdkgb_fci_dets", "qdkgb_set_dets", "qdkgb_build_hamiltonian", "qdkgb_get_csr32",
     "qdkgb_get_csr64", "qdkgb_diagonal", "qdkgb_spmv", "qdkgb_spmv_device", "qdkgb_davidson_default_settings",
     "qdkgb_davidson", "qdkgb_rdms_spin_dep", "qdkgb_casci", "qdkgb_version", "qdkgb_kernel_launches",
+    "qdkgb_sigma_split_noalloc",
 ]
 
 
@@ -95,6 +96,7 @@ def lib():
     L.qdkgb_casci.argtypes = [vp, ci, ci, ci, vp, vp, ci, P(DavidsonSettings), dp, P(dp), vp, P(DavidsonInfo)]
     L.qdkgb_version.restype = ctypes.c_char_p
     L.qdkgb_kernel_launches.restype = ctypes.c_int64
+    L.qdkgb_sigma_split_noalloc.argtypes = [i64, vp, vp, vp, vp, vp, vp, vp]
     _lib = L
     return L
 
@@ -124,6 +126,17 @@ def fci_dets(norb, nalpha, nbeta):
 def kernel_launches():
     """Kernel launches issued by the library in this process."""
     return lib().qdkgb_kernel_launches()
+
+
+NOALLOC_MAX_ROWS = 1 << 20
+
+
+def sigma_split_noalloc(n, rowptr_ptr, colind_ptr, hi_ptr, lo_ptr, x_ptr, y_ptr, stream_ptr=None):
+    """Allocation-free full-precision sigma on caller-owned device arrays
+    (qdkgb_sigma_split_noalloc); raises on a non-zero status."""
+    rc = lib().qdkgb_sigma_split_noalloc(n, rowptr_ptr, colind_ptr, hi_ptr, lo_ptr, x_ptr, y_ptr, stream_ptr)
+    if rc:
+        raise QdkgbError(rc, lib().qdkgb_last_error(None).decode())
 
 
 def default_davidson_settings():

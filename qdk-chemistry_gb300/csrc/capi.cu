@@ -14,6 +14,9 @@ namespace qdkgb {
 static std::atomic<int64_t> g_launches{0};
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
+static thread_local std::string g_context_free_err;
+void set_context_free_error(const std::string& msg) { g_context_free_err = msg; }
+
 void* dev_alloc(Context* c, DeviceBuffer& b, size_t bytes) {
   if (b.ptr && b.bytes >= bytes) return b.ptr;
   dev_free(c, b);
@@ -164,7 +167,7 @@ int qdkgb_destroy(qdkgb_context* c) {
   return QDKGB_OK;
 }
 
-const char* qdkgb_last_error(const qdkgb_context* c) { return c ? c->err.c_str() : "null context"; }
+const char* qdkgb_last_error(const qdkgb_context* c) { return c ? c->err.c_str() : g_context_free_err.c_str(); }
 
 int qdkgb_set_stream(qdkgb_context* c, void* stream) {
   if (!c) return QDKGB_ERR_INVALID;

@@ -43,6 +43,8 @@ struct Context;
 struct Integrals;
 
 void count_launch();
+// message of the last failed call that takes no context (qdkgb_last_error(NULL))
+void set_context_free_error(const std::string& msg);
 
 void* dev_alloc(Context* c, DeviceBuffer& b, size_t bytes);  // (re)allocates when too small
 void dev_free(Context* c, DeviceBuffer& b);

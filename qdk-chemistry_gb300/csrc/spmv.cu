@@ -10,6 +10,8 @@
 //   fp32  : FP32 values (the high part of the split storage), FP32 x/y/accumulation
 //   split : hi + lo values with float-float products and sums (FP32 pipe),
 //           FP64 x/y - the full-precision sigma of the mixed-precision path
+#include <mutex>
+
 #include "common.cuh"
 #include "internal.h"
 
@@ -192,4 +194,83 @@ void f32_to_f64(Context* c, const float* x, double* y, int64_t n) {
   QDKGB_CHECK_LAUNCH();
 }
 
+// ------------------------------------------------------------------ allocation-free sigma
+// Scratch of qdkgb_sigma_split_noalloc: the x vector split into FP32 high and
+// low halves.  A file-scope device array, so the entry point never allocates;
+// every GPU that loads the library holds it (8 MiB) until the process exits.
+constexpr int64_t kNoAllocMaxRows = QDKGB_NOALLOC_MAX_ROWS;
+static __device__ __align__(256) float g_noalloc_split_x[2 * kNoAllocMaxRows];
+
+namespace {
+struct NoAllocDevice {
+  bool ready = false;
+  float* scratch = nullptr;  // device address of g_noalloc_split_x on this device
+  int sm_count = 0;
+};
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+NoAllocDevice g_noalloc_dev[kNoAllocMaxDevices];
+}  // namespace
+
 }  // namespace qdkgb
+
+extern "C" int qdkgb_sigma_split_noalloc(int64_t n, const int64_t* rowptr, const int32_t* colind, const float* hi,
+                                         const float* lo, const double* x, double* y, void* stream) {
+  using namespace qdkgb;
+  if (n < 0 || n > kNoAllocMaxRows) {
+    set_context_free_error("qdkgb_sigma_split_noalloc: " + std::to_string(n) +
+                           " rows is outside [0, QDKGB_NOALLOC_MAX_ROWS = " + std::to_string(kNoAllocMaxRows) + "]");
+    return QDKGB_ERR_INVALID;
+  }
+  if (n == 0) return QDKGB_OK;
+  if (!rowptr || !colind || !hi || !lo || !x || !y) {
+    set_context_free_error("qdkgb_sigma_split_noalloc: null pointer");
+    return QDKGB_ERR_INVALID;
+  }
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) {
+    set_context_free_error(std::string("qdkgb_sigma_split_noalloc: no current CUDA device: ") +
+                           cudaGetErrorString(e));
+    return QDKGB_ERR_CUDA;
+  }
+  NoAllocDevice st;
+  {
+    // one-time set-up per device, with that device current: the host-side
+    // symbol is only a stand-in, the kernels need the device address
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    NoAllocDevice& d = g_noalloc_dev[dev];
+    if (!d.ready) {
+      void* p = nullptr;
+      e = cudaGetSymbolAddress(&p, g_noalloc_split_x);
+      if (e != cudaSuccess) {
+        set_context_free_error(std::string("qdkgb_sigma_split_noalloc: cudaGetSymbolAddress failed: ") +
+                               cudaGetErrorString(e));
+        return QDKGB_ERR_CUDA;
+      }
+      e = cudaDeviceGetAttribute(&d.sm_count, cudaDevAttrMultiProcessorCount, dev);
+      if (e != cudaSuccess) {
+        set_context_free_error(std::string("qdkgb_sigma_split_noalloc: ") + cudaGetErrorString(e));
+        return QDKGB_ERR_CUDA;
+      }
+      d.scratch = (float*)p;
+      d.ready = true;
+    }
+    st = d;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  float* xh = st.scratch;
+  float* xl = st.scratch + kNoAllocMaxRows;
+  k_split_x<<<st.sm_count * 4, 256, 0, s>>>(x, xh, xl, n);
+  count_launch();
+  const unsigned blocks = (unsigned)std::min<int64_t>((n + kSpmvWarps - 1) / kSpmvWarps, (int64_t)st.sm_count * 32);
+  k_spmv_split_ff<<<blocks, kSpmvWarps * 32, 0, s>>>(n, rowptr, colind, hi, lo, xh, xl, y);
+  count_launch();
+  e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_context_free_error(std::string("qdkgb_sigma_split_noalloc: launch failed: ") + cudaGetErrorString(e));
+    return QDKGB_ERR_CUDA;
+  }
+  return QDKGB_OK;
+}
+
