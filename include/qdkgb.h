@@ -103,6 +103,11 @@ int qdkgb_build_hamiltonian(qdkgb_context* ctx, double thresh, int storage, int6
  * _64bit_ (include/macis/hamiltonian_generator.hpp:32-294). */
 int qdkgb_get_csr32(qdkgb_context* ctx, int32_t* rowptr, int32_t* colind, double* values);
 int qdkgb_get_csr64(qdkgb_context* ctx, int64_t* rowptr, int64_t* colind, double* values);
+/* A caller's symmetric CSR matrix (0-based, n rows, host buffers) becomes the
+ * device operator for qdkgb_spmv / qdkgb_davidson, FP64 storage.  This is the
+ * entry of davidson_solver(csr, tol, max_m) (python/src/pybind11/algorithms/
+ * davidson_solver.cpp:60-107), which feeds a scipy CSR to macis::davidson. */
+int qdkgb_set_csr(qdkgb_context* ctx, int64_t n, const int64_t* rowptr, const int64_t* colind, const double* values);
 /* extract_diagonal_elements (sparsexx/util/submatrix.hpp:354-384). */
 int qdkgb_diagonal(qdkgb_context* ctx, double* D);
 

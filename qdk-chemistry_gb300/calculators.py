@@ -1,0 +1,307 @@
+"""qdk-chemistry's multi-configuration plugin surface, backed by the GB300 core.
+
+Mirrors, with the same names, defaults and error behaviour:
+* the algorithm registry: ``create("multi_configuration_calculator", name)``,
+  ``available(...)``, ``register(...)``
+  (python/src/qdk_chemistry/algorithms/registry.py:295,
+  cpp/include/qdk/chemistry/algorithms/algorithm.hpp:242-369);
+* ``MultiConfigurationSettings`` + the MACIS settings
+  (cpp/include/qdk/chemistry/algorithms/mc.hpp:26-62,
+  cpp/src/qdk/chemistry/algorithms/microsoft/macis_base.hpp:27-36): typed
+  defaults, bound checks, locked once ``run`` starts (``SettingsAreLocked``);
+* ``MultiConfigurationCalculator.run(hamiltonian, n_alpha, n_beta) ->
+  (total energy, Wavefunction)`` (mc.hpp:87-172), the CASCI plugin
+  (macis_cas.cpp:35-148) and the ASCI plugin (macis_asci.cpp:44-234);
+* ``davidson_solver(csr, tol=1e-8, max_m=20) -> (eigenvalue, eigenvector)``
+  (python/src/pybind11/algorithms/davidson_solver.cpp:56-108).
+All computation runs in libqdkgb.so on the GPU.
+"""
+import numpy as np
+
+from . import capi, determinants, integrals
+
+
+class SettingsAreLocked(RuntimeError):
+    pass
+
+
+class Settings:
+    """Typed settings with defaults and optional bounds (data::Settings)."""
+
+    def __init__(self):
+        self._values = {}
+        self._types = {}
+        self._bounds = {}
+        self._doc = {}
+        self._locked = False
+
+    def set_default(self, key, typ, value, doc="", bounds=None):
+        self._types[key] = typ
+        self._values[key] = typ(value)
+        self._bounds[key] = bounds
+        self._doc[key] = doc
+
+    def set(self, key, value):
+        if self._locked:
+            raise SettingsAreLocked("settings are locked (the algorithm has run)")
+        if key not in self._types:
+            raise KeyError("unknown setting '%s'" % key)
+        typ = self._types[key]
+        if typ is bool and not isinstance(value, (bool, np.bool_)):
+            raise TypeError("setting '%s' expects bool" % key)
+        if typ in (int, float) and isinstance(value, bool):
+            raise TypeError("setting '%s' expects %s" % (key, typ.__name__))
+        v = typ(value)
+        b = self._bounds.get(key)
+        if b is not None:
+            lo, hi = b
+            if not (lo <= v <= hi):
+                raise ValueError("setting '%s' = %r outside [%r, %r]" % (key, v, lo, hi))
+        self._values[key] = v
+
+    def get(self, key):
+        return self._values[key]
+
+    def get_or_default(self, key, default):
+        return self._values.get(key, default)
+
+    def has(self, key):
+        return key in self._values
+
+    def keys(self):
+        return list(self._values)
+
+    def lock(self):
+        self._locked = True
+
+    def locked(self):
+        return self._locked
+
+    def to_dict(self):
+        return dict(self._values)
+
+
+class MultiConfigurationSettings(Settings):
+    """mc.hpp:34-62 defaults."""
+
+    def __init__(self):
+        super().__init__()
+        self.set_default("calculate_one_rdm", bool, False)
+        self.set_default("calculate_two_rdm", bool, False)
+        self.set_default("calculate_single_orbital_entropies", bool, False)
+        self.set_default("calculate_two_orbital_entropies", bool, False)
+        self.set_default("calculate_mutual_information", bool, False)
+        self.set_default("ci_residual_tolerance", float, 1.0e-6, "CI residual convergence tolerance", (0.0, 1.0))
+        self.set_default("max_solver_iterations", int, 200, "Maximum number of Davidson iterations", (1, 2 ** 63 - 1))
+        self.set_default("iterative_solver_dimension_cutoff", int, 2000,
+                         "Matrix size cutoff for using iterative eigensolver", (1, 2 ** 63 - 1))
+
+
+class Gb300Settings(MultiConfigurationSettings):
+    """MacisSettings (macis_base.hpp:27-36) plus the GPU controls."""
+
+    def __init__(self):
+        super().__init__()
+        self.set_default("ci_matel_tol", float, np.finfo(np.float64).eps,
+                         "Hamiltonian matrix element sparsification threshold", (0.0, 1.0))
+        self.set_default("precision", str, "fp64", "fp64 or mixed (FP32 sigma with FP64 defect correction)")
+        self.set_default("device", int, 0, "CUDA device ordinal", (0, 1024))
+
+
+class Hamiltonian:
+    """Active-space Hamiltonian: one-body T (n x n), two-body V (n^4, (pq|rs)),
+    core energy (data::Hamiltonian's get_one_body_integrals /
+    get_two_body_integrals / get_core_energy)."""
+
+    def __init__(self, one_body, two_body, core_energy=0.0):
+        self._T = np.asarray(one_body, dtype=np.float64)
+        n = self._T.shape[0]
+        V = np.asarray(two_body, dtype=np.float64)
+        self._V = V.reshape(n, n, n, n)
+        self._ecore = float(core_energy)
+
+    @classmethod
+    def from_fcidump(cls, path):
+        d = integrals.read_fcidump(path)
+        return cls(d["T"], d["V"], d["E_core"])
+
+    @property
+    def norb(self):
+        return self._T.shape[0]
+
+    def get_one_body_integrals(self):
+        return self._T
+
+    def get_two_body_integrals(self):
+        return self._V
+
+    def get_core_energy(self):
+        return self._ecore
+
+
+class Wavefunction:
+    """Determinants + CI coefficients (+ optional RDMs), the StateVectorContainer
+    the reference builds (macis_base.hpp:134-283).  The spin-resolved two-body
+    RDMs carry the reference's factor 2 (macis_base.hpp:203-212)."""
+
+    def __init__(self, norb, alpha, beta, coeffs, rdms=None):
+        self.norb = norb
+        self.alpha = np.asarray(alpha, dtype=np.uint64)
+        self.beta = np.asarray(beta, dtype=np.uint64)
+        self.coefficients = np.asarray(coeffs, dtype=np.float64)
+        self._rdms = rdms or {}
+
+    def size(self):
+        return len(self.coefficients)
+
+    def get_configurations(self):
+        return [determinants.to_canonical_string(a, b, self.norb) for a, b in zip(self.alpha, self.beta)]
+
+    def has_one_rdm(self):
+        return "aa" in self._rdms
+
+    def has_two_rdm(self):
+        return "aaaa" in self._rdms
+
+    def get_active_one_rdm_spin_dependent(self):
+        if not self.has_one_rdm():
+            raise RuntimeError("one-body RDM was not requested (calculate_one_rdm)")
+        return self._rdms["aa"], self._rdms["bb"]
+
+    def get_active_one_rdm_spin_traced(self):
+        aa, bb = self.get_active_one_rdm_spin_dependent()
+        return aa + bb
+
+    def get_active_two_rdm_spin_dependent(self):
+        """(aabb, aaaa, bbbb), flattened column-major, times 2 as qdk stores them."""
+        if not self.has_two_rdm():
+            raise RuntimeError("two-body RDM was not requested (calculate_two_rdm)")
+        f = lambda t: 2.0 * t.ravel(order="F")
+        return f(self._rdms["aabb"]), f(self._rdms["aaaa"]), f(self._rdms["bbbb"])
+
+    def get_active_two_rdm_spin_traced(self):
+        """MACIS spin-traced 2-RDM (E = T.g + V.G): aaaa + bbbb + aabb + aabb^T(rs,pq)."""
+        if not self.has_two_rdm():
+            raise RuntimeError("two-body RDM was not requested (calculate_two_rdm)")
+        r = self._rdms
+        return r["aaaa"] + r["bbbb"] + r["aabb"] + r["aabb"].transpose(2, 3, 0, 1)
+
+
+class MultiConfigurationCalculator:
+    """Algorithm::run locks the settings, then calls _run_impl (algorithm.hpp:67-70)."""
+
+    def __init__(self):
+        self._settings = self._make_settings()
+
+    def _make_settings(self):
+        return Gb300Settings()
+
+    def settings(self):
+        return self._settings
+
+    def name(self):
+        raise NotImplementedError
+
+    def type_name(self):
+        return "multi_configuration_calculator"
+
+    def run(self, hamiltonian, n_alpha, n_beta):
+        self._settings.lock()
+        return self._run_impl(hamiltonian, int(n_alpha), int(n_beta))
+
+    def _run_impl(self, hamiltonian, n_alpha, n_beta):
+        raise NotImplementedError
+
+    # shared by the CI plugins
+    def _check_unsupported(self):
+        s = self._settings
+        for k in ("calculate_single_orbital_entropies", "calculate_two_orbital_entropies",
+                  "calculate_mutual_information"):
+            if s.get(k):
+                raise NotImplementedError("%s is outside this GPU core (orbital entropies)" % k)
+
+    def _solve(self, ctx, hamiltonian, a, b):
+        """H build + Davidson (+ RDMs) on a determinant list; returns (E_total, Wavefunction)."""
+        s = self._settings
+        prec = s.get("precision")
+        if prec not in ("fp64", "mixed"):
+            raise ValueError("precision must be 'fp64' or 'mixed'")
+        mixed = prec == "mixed"
+        n = len(a)
+        ctx.set_dets(a, b)
+        ctx.build_hamiltonian(s.get("ci_matel_tol"), capi.H_SPLIT32 if mixed else capi.H_FP64)
+        tol = s.get("ci_residual_tolerance")
+        max_m = s.get("max_solver_iterations")
+        if n <= s.get("iterative_solver_dimension_cutoff"):
+            # the reference diagonalises small spaces densely (macis_cas.cpp:89-101);
+            # here the same Davidson runs to a tight residual (an exact eigenpair
+            # up to rounding) with room for the whole space
+            tol = min(tol, 1e-10)
+            max_m = max(2, min(n, 254))
+        E, C, info = ctx.davidson(max_m=min(max_m, 254), tol=tol,
+                                  precision=capi.PREC_MIXED if mixed else capi.PREC_FP64)
+        rdms = None
+        want = []
+        if s.get("calculate_one_rdm"):
+            want += ["aa", "bb"]
+        if s.get("calculate_two_rdm"):
+            want += ["aaaa", "bbbb", "aabb"]
+        if want:
+            rdms = ctx.rdms_spin_dep(C, want=tuple(want))
+        wfn = Wavefunction(hamiltonian.norb, a, b, C, rdms)
+        wfn.info = info
+        return E + hamiltonian.get_core_energy(), wfn
+
+
+class Gb300Cas(MultiConfigurationCalculator):
+    """CASCI over the full (n_alpha, n_beta) space (MacisCas, macis_cas.cpp:120-148)."""
+
+    def name(self):
+        return "gb300_cas"
+
+    def _run_impl(self, hamiltonian, n_alpha, n_beta):
+        self._check_unsupported()
+        n = hamiltonian.norb
+        if not (0 <= n_alpha <= n and 0 <= n_beta <= n):
+            raise ValueError("electron counts must lie in [0, norb]")
+        if n > 64:
+            raise ValueError("at most 64 active orbitals per spin")
+        a, b = capi.fci_dets(n, n_alpha, n_beta)
+        with capi.Context(self._settings.get("device")) as ctx:
+            ctx.set_integrals(hamiltonian.get_one_body_integrals(), hamiltonian.get_two_body_integrals())
+            return self._solve(ctx, hamiltonian, a, b)
+
+
+_REGISTRY = {"multi_configuration_calculator": {"gb300_cas": Gb300Cas}}
+_DEFAULT = {"multi_configuration_calculator": "gb300_cas"}
+
+
+def register(kind, factory):
+    """register_instance (algorithm.hpp:310): keyed by the instance's name()."""
+    inst = factory()
+    _REGISTRY.setdefault(kind, {})[inst.name()] = factory
+
+
+def available(kind="multi_configuration_calculator"):
+    return sorted(_REGISTRY.get(kind, {}))
+
+
+def create(kind, name=None):
+    """create(kind, name) (registry.py:295); the default name as mc.hpp:213."""
+    if kind not in _REGISTRY:
+        raise KeyError("unknown algorithm type '%s'" % kind)
+    name = name or _DEFAULT.get(kind)
+    if name not in _REGISTRY[kind]:
+        raise KeyError("no '%s' named '%s' (available: %s)" % (kind, name, ", ".join(available(kind))))
+    return _REGISTRY[kind][name]()
+
+
+def davidson_solver(csr_matrix, tol=1e-8, max_m=20, device=0):
+    """Lowest eigenpair of a symmetric scipy CSR matrix on the GPU
+    (davidson_solver.cpp:60-107: diagonal guess, macis::davidson)."""
+    A = csr_matrix.tocsr()
+    A.sort_indices()
+    with capi.Context(device) as ctx:
+        ctx.set_csr(A.indptr, A.indices, A.data)
+        E, X, _ = ctx.davidson(max_m=max_m, tol=tol)
+    return E, X

@@ -34,7 +34,7 @@ EXPORTED = [
     "qdkgb_set_integrals", "qdkgb_fci_dets", "qdkgb_set_dets", "qdkgb_build_hamiltonian", "qdkgb_get_csr32",
     "qdkgb_get_csr64", "qdkgb_diagonal", "qdkgb_spmv", "qdkgb_spmv_device", "qdkgb_davidson_default_settings",
     "qdkgb_davidson", "qdkgb_rdms_spin_dep", "qdkgb_casci", "qdkgb_version", "qdkgb_kernel_launches",
-    "qdkgb_sigma_split_noalloc",
+    "qdkgb_sigma_split_noalloc", "qdkgb_set_csr",
 ]
 
 
@@ -87,6 +87,7 @@ def lib():
     L.qdkgb_get_csr32.argtypes = [vp, vp, vp, vp]
     L.qdkgb_get_csr64.argtypes = [vp, vp, vp, vp]
     L.qdkgb_diagonal.argtypes = [vp, vp]
+    L.qdkgb_set_csr.argtypes = [vp, i64, vp, vp, vp]
     L.qdkgb_spmv.argtypes = [vp, ci, vp, vp]
     L.qdkgb_spmv_device.argtypes = [vp, ci, vp, vp]
     L.qdkgb_davidson_default_settings.argtypes = [P(DavidsonSettings)]
@@ -230,6 +231,16 @@ class Context:
         fn = lib().qdkgb_get_csr64 if index_bits == 64 else lib().qdkgb_get_csr32
         self._check(fn(self._h, _ptr(rp), _ptr(ci), _ptr(nz)))
         return rp, ci, nz
+
+    def set_csr(self, rowptr, colind, values):
+        """Use a caller's CSR matrix (0-based) as the device operator."""
+        rp = np.ascontiguousarray(rowptr, dtype=np.int64)
+        ci = np.ascontiguousarray(colind, dtype=np.int64)
+        nz = _f64(values)
+        n = len(rp) - 1
+        self._check(lib().qdkgb_set_csr(self._h, n, _ptr(rp), _ptr(ci), _ptr(nz)))
+        self.ndets = n
+        self.nnz = len(nz)
 
     def diagonal(self):
         d = np.zeros(self.ndets)

@@ -260,6 +260,15 @@ int qdkgb_get_csr64(qdkgb_context* c, int64_t* rowptr, int64_t* colind, double* 
   return guarded(c, [&] { get_csr<int64_t>(c, rowptr, colind, values); });
 }
 
+int qdkgb_set_csr(qdkgb_context* c, int64_t n, const int64_t* rowptr, const int64_t* colind, const double* values) {
+  if (!c) return QDKGB_ERR_INVALID;
+  return guarded(c, [&] {
+    if (!rowptr || (!colind && n > 0) || (!values && n > 0)) throw Error(QDKGB_ERR_INVALID, "null CSR buffer");
+    QDKGB_CUDA(cudaSetDevice(c->device));
+    set_csr(c, n, rowptr, colind, values);
+  });
+}
+
 int qdkgb_diagonal(qdkgb_context* c, double* D) {
   if (!c) return QDKGB_ERR_INVALID;
   return guarded(c, [&] {

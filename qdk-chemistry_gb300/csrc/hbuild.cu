@@ -516,6 +516,63 @@ __global__ void k_row_compact(int64_t n, const int64_t* __restrict__ pre_ptr, co
   }
 }
 
+// extract_diagonal_elements (sparsexx/util/submatrix.hpp:354-384): first
+// stored (i, i) element of each row, 0 when absent.  Warp per row.
+__global__ void k_extract_diag(int64_t n, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ colind,
+                               const double* __restrict__ val, double* __restrict__ D) {
+  const int lane = threadIdx.x & 31;
+  const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t r = w0; r < n; r += nw) {
+    const int64_t st = rowptr[r], en = rowptr[r + 1];
+    int64_t found = -1;
+    for (int64_t k0 = st; k0 < en && found < 0; k0 += 32) {
+      const int64_t k = k0 + lane;
+      const unsigned m = __ballot_sync(QDKGB_FULL_MASK, k < en && colind[k] == r);
+      if (m) found = k0 + __ffs(m) - 1;
+    }
+    if (lane == 0) D[r] = (found >= 0) ? val[found] : 0.;
+  }
+}
+
+// A caller's CSR matrix (0-based) becomes the device operator, FP64 storage
+// (the matrix davidson_solver receives, pybind11/algorithms/davidson_solver.cpp:60-107).
+void set_csr(Context* c, int64_t n, const int64_t* rowptr, const int64_t* colind, const double* values) {
+  if (n <= 0) throw Error(QDKGB_ERR_INVALID, "empty matrix");
+  if (n >= (int64_t)INT32_MAX) throw Error(QDKGB_ERR_UNSUPPORTED, "more than 2^31-1 rows");
+  Hcsr& H = c->H;
+  H.valid = false;
+  const int64_t nnz = rowptr[n] - rowptr[0];
+  if (rowptr[0] != 0 || nnz < 0) throw Error(QDKGB_ERR_INVALID, "row pointers must start at 0 and not decrease");
+  std::vector<int32_t> ci(std::max<int64_t>(nnz, 1));
+  for (int64_t k = 0; k < nnz; ++k) {
+    if (colind[k] < 0 || colind[k] >= n) throw Error(QDKGB_ERR_INVALID, "column index out of range");
+    ci[k] = (int32_t)colind[k];
+  }
+  for (int64_t i = 0; i < n; ++i)
+    if (rowptr[i + 1] < rowptr[i]) throw Error(QDKGB_ERR_INVALID, "row pointers must not decrease");
+  dev_free(c, H.hi);
+  dev_free(c, H.lo);
+  int64_t* rp = dev_array<int64_t>(c, H.rowptr, n + 1);
+  int32_t* dci = dev_array<int32_t>(c, H.colind, std::max<int64_t>(nnz, 1));
+  double* dv = dev_array<double>(c, H.val, std::max<int64_t>(nnz, 1));
+  double* D = dev_array<double>(c, H.diag, n);
+  QDKGB_CUDA(cudaMemcpyAsync(rp, rowptr, (n + 1) * 8, cudaMemcpyHostToDevice, c->stream));
+  if (nnz) {
+    QDKGB_CUDA(cudaMemcpyAsync(dci, ci.data(), nnz * 4, cudaMemcpyHostToDevice, c->stream));
+    QDKGB_CUDA(cudaMemcpyAsync(dv, values, nnz * 8, cudaMemcpyHostToDevice, c->stream));
+  }
+  const unsigned blocks = (unsigned)std::min<int64_t>((n + 7) / 8, (int64_t)c->sm_count * 32);
+  k_extract_diag<<<blocks, 256, 0, c->stream>>>(n, rp, dci, dv, D);
+  QDKGB_CHECK_LAUNCH();
+  QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+  H.n = n;
+  H.nnz = nnz;
+  H.storage = QDKGB_H_FP64;
+  H.thresh = 0.;
+  H.valid = true;
+}
+
 RowArgs row_args(Context* c, double thresh) {
   DetSpace& D = c->dets;
   RowArgs a;

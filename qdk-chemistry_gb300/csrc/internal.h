@@ -109,6 +109,7 @@ Integrals integrals_view(Context* c);
 void build_integral_intermediates(Context* c);
 void build_det_space(Context* c, int64_t ndets, const uint64_t* alpha, const uint64_t* beta);
 void build_hamiltonian(Context* c, double thresh, int storage);
+void set_csr(Context* c, int64_t n, const int64_t* rowptr, const int64_t* colind, const double* values);
 void exclusive_scan_i64(Context* c, const int64_t* in, int64_t* out, int64_t n, DeviceBuffer& tmp);
 
 // spmv.cu

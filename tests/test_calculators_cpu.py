@@ -1,0 +1,71 @@
+"""qdk-style plugin surface: registry, settings (names, defaults, bounds,
+locking), containers.  No GPU."""
+import numpy as np
+import pytest
+
+
+def test_registry_and_defaults(pkg):
+    calc = pkg.calculators
+    assert "gb300_cas" in calc.available()
+    c = calc.create("multi_configuration_calculator")
+    assert c.name() == "gb300_cas"
+    s = c.settings()
+    # mc.hpp:34-62 and macis_base.hpp:27-36 defaults
+    assert s.get("ci_residual_tolerance") == 1e-6
+    assert s.get("max_solver_iterations") == 200
+    assert s.get("iterative_solver_dimension_cutoff") == 2000
+    assert s.get("calculate_one_rdm") is False and s.get("calculate_two_rdm") is False
+    assert s.get("ci_matel_tol") == np.finfo(float).eps
+    with pytest.raises(KeyError):
+        calc.create("multi_configuration_calculator", "no_such_solver")
+    with pytest.raises(KeyError):
+        calc.create("no_such_kind", "gb300_cas")
+
+
+def test_settings_validation_and_lock(pkg):
+    c = pkg.calculators.create("multi_configuration_calculator", "gb300_cas")
+    s = c.settings()
+    with pytest.raises(ValueError):
+        s.set("ci_residual_tolerance", 2.0)  # BoundConstraint [0, 1]
+    with pytest.raises(ValueError):
+        s.set("max_solver_iterations", 0)
+    with pytest.raises(TypeError):
+        s.set("calculate_one_rdm", 1)
+    with pytest.raises(KeyError):
+        s.set("not_a_setting", 1)
+    s.set("ci_residual_tolerance", 1e-9)
+    s.lock()
+    with pytest.raises(pkg.calculators.SettingsAreLocked):
+        s.set("ci_residual_tolerance", 1e-7)
+
+
+def test_wavefunction_container(pkg):
+    d = pkg.determinants
+    a, b = d.fci_space(4, 2, 2)
+    C = np.ones(len(a)) / np.sqrt(len(a))
+    w = pkg.calculators.Wavefunction(4, a, b, C)
+    cfg = w.get_configurations()
+    assert cfg[0] == "2200" and len(cfg) == 36
+    with pytest.raises(RuntimeError):
+        w.get_active_one_rdm_spin_dependent()
+
+
+def test_hamiltonian_from_fcidump_roundtrip(pkg, tmp_path):
+    T, V, _ = pkg.integrals.synthetic_integrals(5, 6, seed=2)
+    p = tmp_path / "x.fcidump"
+    pkg.integrals.write_fcidump(str(p), T, V, E_core=1.25, nelec=4)
+    H = pkg.calculators.Hamiltonian.from_fcidump(str(p))
+    assert H.norb == 5 and H.get_core_energy() == 1.25
+    assert np.allclose(H.get_one_body_integrals(), T, atol=1e-15)
+    assert np.allclose(H.get_two_body_integrals(), V, atol=1e-15)
+
+
+def test_synthetic_integrals_recipe(pkg):
+    T, V, ec = pkg.integrals.synthetic_integrals(12, 24, seed=7)
+    assert ec == 0.0 and T.shape == (12, 12) and V.shape == (12,) * 4
+    assert np.array_equal(T, T.T)
+    for perm in [(1, 0, 2, 3), (0, 1, 3, 2), (2, 3, 0, 1), (3, 2, 1, 0)]:
+        assert np.array_equal(V, V.transpose(perm))
+    M = V.reshape(144, 144)
+    assert np.linalg.eigvalsh(M).min() > -1e-12  # PSD
+    assert np.allclose(np.diag(T), -2.0 + 0.25 * np.arange(12))
