@@ -97,6 +97,17 @@ int qdkgb_set_dets(qdkgb_context* ctx, int64_t ndets, const uint64_t* alpha, con
  * entry computed with the lower-index determinant as bra.  The CSR stays on
  * the device (int64 row pointers, int32 columns); *nnz receives its size. */
 int qdkgb_build_hamiltonian(qdkgb_context* ctx, double thresh, int storage, int64_t* nnz);
+/* Direct (recompute-on-the-fly) sigma for complete active spaces whose CSR
+ * would not fit in HBM: replaces the stored H of make_csr_hamiltonian_block_ +
+ * SparseMatrixOperator (davidson.hpp:79-90) by sigma = diag C + S_aa(C) +
+ * S_bb(C) + S_ab(C) evaluated from per-spin string tables on every
+ * application, in FP64 (qdkgb_spmv / Davidson FP64) or FP32 (mixed mode).
+ * Needs a full (n_alpha, n_beta) product space (qdkgb_fci_dets order or any
+ * complete alpha-grouped list), at most 20 orbitals and 4096 strings per spin.
+ * After this call qdkgb_spmv, qdkgb_davidson and qdkgb_diagonal use it; a later
+ * qdkgb_build_hamiltonian switches back to the CSR. */
+int qdkgb_build_direct_sigma(qdkgb_context* ctx);
+
 /* Copies the device CSR to host buffers (rowptr: ndets+1, colind/values: nnz).
  * For QDKGB_H_SPLIT32 storage, values receive (double)hi + (double)lo.
  * The 32-bit and 64-bit variants mirror make_csr_hamiltonian_block_32bit_ /

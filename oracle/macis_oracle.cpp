@@ -17,6 +17,8 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <limits>
+#include <memory>
 #include <numeric>
 #include <stdexcept>
 #include <vector>
@@ -826,6 +828,377 @@ Csr* build_rows(const Ham& H, const uint64_t* alpha, const uint64_t* beta, int64
   return M;
 }
 
+// ---------------------------------------------------------------- ASCI
+// ASCISettings (include/macis/asci/determinant_search.hpp:95-199) subset
+struct AsciSettings {
+  int64_t ntdets_max = 100000, ntdets_min = 100, ncdets_max = 100;
+  int core_fixed = 0;  // 0: Percentage, 1: Fixed
+  double core_threshold = 0.95, h_el_tol = 1e-8, rv_prune_tol = 1e-8;
+  double grow_factor = 8.0, min_grow_factor = 1.01, backoff = 0.5, recovery = 1.1;
+  int64_t max_refine_iter = 6;
+  double refine_energy_tol = 1e-6;
+  int warm_start = 1;
+  double min_warm_start_overlap = 0.5;
+  // MCSCFSettings (include/macis/mcscf/mcscf.hpp:22-52)
+  double ci_res_tol = 1e-8;
+  int64_t ci_max_subspace = 200;
+  double ci_matel_tol = 2.220446049250313e-16;
+};
+
+struct Det {
+  uint64_t a, b;
+  bool operator==(const Det& o) const { return a == o.a && b == o.b; }
+};
+// spin_comparator (include/macis/wfn/raw_bitset.hpp:119-141)
+inline bool spin_less(const Det& x, const Det& y) { return x.a != y.a ? x.a < y.a : x.b < y.b; }
+
+struct Contrib {
+  Det q;
+  double c_h, h_diag;  // c * <Q|H|P>, E0 - H_QQ
+  double rv() const { return c_h / h_diag; }
+};
+
+// single_orbital_ens (src/macis/hamiltonian_generator/fast_diagonals.ipp:30-50)
+std::vector<double> orbital_ens(const Ham& H, const std::vector<uint32_t>& ss, const std::vector<uint32_t>& os) {
+  const int n = H.n;
+  std::vector<double> e(n);
+  for (int i = 0; i < n; ++i) {
+    double x = H.t(i, i);
+    for (auto q : ss) x += H.G2_red[i + (size_t)n * q] + H.G2_red[q + (size_t)n * i];
+    x -= H.G2_red[i + (size_t)n * i];
+    for (auto q : os) x += H.V2_red[i + (size_t)n * q];
+    e[i] = x;
+  }
+  return e;
+}
+inline double g2(const Ham& H, uint32_t p, uint32_t q) { return H.G2_red[p + (size_t)H.n * q]; }
+inline double v2(const Ham& H, uint32_t p, uint32_t q) { return H.V2_red[p + (size_t)H.n * q]; }
+
+// append_singles / append_ss_doubles / append_os_doubles_asci_contributions
+// (include/macis/asci/determinant_contributions.hpp:93-297) with the fast
+// diagonals (fast_diagonals.ipp:52-127), for one spin convention: `same` is
+// the excited spin, `other` the spectator.
+void singles_contribs(const Ham& H, double coeff, uint64_t same, uint64_t other, bool alpha,
+                      const std::vector<uint32_t>& occ_s, const std::vector<uint32_t>& vir_s,
+                      const std::vector<uint32_t>& occ_o, const std::vector<double>& eps, double hdiag, double E0,
+                      double tol, std::vector<Contrib>& out) {
+  const int n = H.n;
+  for (auto i : occ_s)
+    for (auto a : vir_s) {
+      double h = H.t(a, i);
+      const double* G = &H.G_red[(size_t)n * (a + (size_t)n * i)];
+      const double* Vr = &H.V_red[(size_t)n * (a + (size_t)n * i)];
+      for (auto p : occ_s) h += G[p];
+      for (auto p : occ_o) h += Vr[p];
+      if (std::abs(coeff * h) < tol) continue;
+      const uint64_t ex = (same ^ (1ull << i)) | (1ull << a);
+      h *= single_excitation_sign(same, a, i);
+      const double hd = hdiag + eps[a] - eps[i] - g2(H, a, i) - g2(H, i, a);
+      Det q = alpha ? Det{ex, other} : Det{other, ex};
+      out.push_back({q, coeff * h, E0 - hd});
+    }
+}
+void ss_doubles_contribs(const Ham& H, double coeff, uint64_t same, uint64_t other, bool alpha,
+                         const std::vector<uint32_t>& occ, const std::vector<uint32_t>& vir,
+                         const std::vector<double>& eps, double hdiag, double E0, double tol,
+                         std::vector<Contrib>& out) {
+  for (size_t ii = 0; ii < occ.size(); ++ii)
+    for (size_t aa = 0; aa < vir.size(); ++aa) {
+      const uint32_t i = occ[ii], a = vir[aa];
+      for (size_t jj = ii + 1; jj < occ.size(); ++jj)
+        for (size_t bb = aa + 1; bb < vir.size(); ++bb) {
+          const uint32_t j = occ[jj], b = vir[bb];
+          const double G = H.v(b, j, a, i) - H.v(b, i, a, j);
+          if (std::abs(coeff * G) < tol) continue;
+          const uint64_t full = (1ull << i) | (1ull << j) | (1ull << a) | (1ull << b);
+          const uint64_t ex = same ^ full;
+          const double sign = doubles_sign_indices(same, ex, full).sign;
+          const double h = sign * G;
+          const double hd = hdiag + eps[a] + eps[b] - eps[i] - eps[j] + g2(H, i, j) + g2(H, j, i) + g2(H, a, b) +
+                            g2(H, b, a) - g2(H, a, i) - g2(H, i, a) - g2(H, b, i) - g2(H, i, b) - g2(H, a, j) -
+                            g2(H, j, a) - g2(H, b, j) - g2(H, j, b);
+          Det q = alpha ? Det{ex, other} : Det{other, ex};
+          out.push_back({q, coeff * h, E0 - hd});
+        }
+    }
+}
+void os_doubles_contribs(const Ham& H, double coeff, uint64_t sa, uint64_t sb, const std::vector<uint32_t>& oa,
+                         const std::vector<uint32_t>& va, const std::vector<uint32_t>& ob,
+                         const std::vector<uint32_t>& vb, const std::vector<double>& ea,
+                         const std::vector<double>& eb, double hdiag, double E0, double tol,
+                         std::vector<Contrib>& out) {
+  for (auto i : oa)
+    for (auto a : va) {
+      const double s_a = single_excitation_sign(sa, a, i);
+      for (auto j : ob)
+        for (auto b : vb) {
+          const double V = H.v(a, i, b, j);
+          if (std::abs(coeff * V) < tol) continue;
+          const double s = s_a * single_excitation_sign(sb, b, j);
+          const double hd = hdiag + ea[a] + eb[b] - ea[i] - eb[j] + v2(H, i, j) + v2(H, a, b) - g2(H, a, i) -
+                            g2(H, i, a) - g2(H, b, j) - g2(H, j, b) - v2(H, a, j) - v2(H, i, b);
+          Det q{(sa ^ (1ull << i)) | (1ull << a), (sb ^ (1ull << j)) | (1ull << b)};
+          out.push_back({q, coeff * s * V, E0 - hd});
+        }
+    }
+}
+
+// asci_search (include/macis/asci/determinant_search.hpp:808-1123) on the
+// full contribution list: enumerate, sort by determinant and accumulate
+// (determinant_sort.hpp:115-370), drop the core (infinite score), prune
+// |rv| <= rv_prune_tol, keep the top ndets_max - ncore by |rv| with ties at
+// the cutoff kept (:994-1080), append the core.  (The reference partitions the
+// enumeration by alpha constraints for parallelism; every target determinant
+// lies in one constraint, so the accumulated scores are the same.)
+std::vector<Det> asci_search(const Ham& H, const AsciSettings& S, int64_t ndets_max, const std::vector<Det>& core,
+                             const std::vector<double>& C, double E0) {
+  const int n = H.n;
+  const int64_t ncore = (int64_t)core.size();
+  int nth = 1;
+#ifdef _OPENMP
+  nth = omp_get_max_threads();
+#endif
+  std::vector<std::vector<Contrib>> per(nth);
+#pragma omp parallel
+  {
+    int tid = 0;
+#ifdef _OPENMP
+    tid = omp_get_thread_num();
+#endif
+    std::vector<Contrib>& out = per[tid];
+    std::vector<uint32_t> oa, va, ob, vb;
+#pragma omp for schedule(dynamic)
+    for (int64_t ip = 0; ip < ncore; ++ip) {
+      const Det P = core[ip];
+      const double c = C[ip];
+      oa.clear(); va.clear(); ob.clear(); vb.clear();
+      for (int p = 0; p < n; ++p) {
+        ((P.a >> p) & 1 ? oa : va).push_back(p);
+        ((P.b >> p) & 1 ? ob : vb).push_back(p);
+      }
+      const double hdiag = H.me_diag(oa, ob);
+      const std::vector<double> ea = orbital_ens(H, oa, ob), eb = orbital_ens(H, ob, oa);
+      singles_contribs(H, c, P.a, P.b, true, oa, va, ob, ea, hdiag, E0, S.h_el_tol, out);
+      ss_doubles_contribs(H, c, P.a, P.b, true, oa, va, ea, hdiag, E0, S.h_el_tol, out);
+      os_doubles_contribs(H, c, P.a, P.b, oa, va, ob, vb, ea, eb, hdiag, E0, S.h_el_tol, out);
+      singles_contribs(H, c, P.b, P.a, false, ob, vb, oa, eb, hdiag, E0, S.h_el_tol, out);
+      ss_doubles_contribs(H, c, P.b, P.a, false, ob, vb, eb, hdiag, E0, S.h_el_tol, out);
+      out.push_back({P, std::numeric_limits<double>::infinity(), 1.0});
+    }
+  }
+  std::vector<Contrib> all;
+  for (auto& v : per) all.insert(all.end(), v.begin(), v.end());
+  std::stable_sort(all.begin(), all.end(), [](const Contrib& x, const Contrib& y) { return spin_less(x.q, y.q); });
+  std::vector<Contrib> acc;
+  for (size_t k = 0; k < all.size();) {
+    size_t e = k + 1;
+    Contrib c0 = all[k];
+    for (; e < all.size() && all[e].q == all[k].q; ++e) c0.c_h += all[e].c_h;
+    if (!std::isinf(c0.c_h) && std::abs(c0.rv()) > S.rv_prune_tol) acc.push_back(c0);
+    k = e;
+  }
+  const int64_t topk = ndets_max - ncore;
+  std::vector<Det> out;
+  if ((int64_t)acc.size() > topk && topk >= 0) {
+    std::vector<double> sc(acc.size());
+    for (size_t i = 0; i < acc.size(); ++i) sc[i] = std::abs(acc[i].rv());
+    std::vector<double> tmp = sc;
+    double kth = 0.;
+    if (topk > 0) {
+      std::nth_element(tmp.begin(), tmp.begin() + (topk - 1), tmp.end(), std::greater<double>());
+      kth = tmp[topk - 1];
+    } else {
+      kth = std::numeric_limits<double>::infinity();
+    }
+    for (size_t i = 0; i < acc.size(); ++i)
+      if (sc[i] >= kth) out.push_back(acc[i].q);
+  } else {
+    for (auto& c : acc) out.push_back(c.q);
+  }
+  out.insert(out.end(), core.begin(), core.end());
+  return out;
+}
+
+// selected_ci_diag (selected_ci_diag.hpp:111-158) on a sorted determinant list
+double sci_diag(const Ham& H, const AsciSettings& S, const std::vector<Det>& dets, std::vector<double>& X) {
+  std::vector<uint64_t> a(dets.size()), b(dets.size());
+  for (size_t i = 0; i < dets.size(); ++i) {
+    a[i] = dets[i].a;
+    b[i] = dets[i].b;
+  }
+  std::unique_ptr<Csr> M(build_csr_sdl(H, a.data(), b.data(), (int64_t)dets.size(), S.ci_matel_tol));
+  X.resize(dets.size(), 0.);
+  std::vector<double> D(M->n);
+  for (int64_t i = 0; i < M->n; ++i) {
+    D[i] = 0.;
+    for (int64_t k = M->rowptr[i]; k < M->rowptr[i + 1]; ++k)
+      if (M->colind[k] == i) {
+        D[i] = M->nzval[k];
+        break;
+      }
+  }
+  double maxc = 0.;
+  for (double x : X) maxc = std::max(maxc, std::abs(x));
+  if (!(maxc > 1. / (double)X.size())) {
+    std::fill(X.begin(), X.end(), 0.);
+    X[std::min_element(D.begin(), D.end()) - D.begin()] = 1.;
+  }
+  double E = 0.;
+  int64_t it = 0;
+  if (davidson(*M, S.ci_max_subspace, D.data(), S.ci_res_tol, X.data(), &E, &it))
+    throw std::runtime_error("Davidson Did Not Converge!");
+  return E;
+}
+
+// asci_iter (include/macis/asci/iteration.hpp:50-226)
+double asci_iter(const Ham& H, const AsciSettings& S, int64_t ndets_max, double E0, std::vector<Det>& wfn,
+                 std::vector<double>& X) {
+  if (wfn.size() > 1) {  // reorder_ci_on_coeff (determinant_sort.hpp:45-64)
+    std::vector<size_t> idx(wfn.size());
+    std::iota(idx.begin(), idx.end(), 0);
+    std::sort(idx.begin(), idx.end(), [&](size_t i, size_t j) { return std::abs(X[i]) > std::abs(X[j]); });
+    std::vector<Det> w2(wfn.size());
+    std::vector<double> x2(wfn.size());
+    for (size_t i = 0; i < idx.size(); ++i) {
+      w2[i] = wfn[idx[i]];
+      x2[i] = X[idx[i]];
+    }
+    wfn.swap(w2);
+    X.swap(x2);
+  }
+  size_t nkeep = 0;
+  if (S.core_fixed) {
+    nkeep = std::min<size_t>(S.ncdets_max, wfn.size());
+  } else {
+    double w = 0.;
+    for (size_t i = 0; i < wfn.size(); ++i) {
+      w += X[i] * X[i];
+      nkeep++;
+      if (w >= S.core_threshold) break;
+    }
+  }
+  if (wfn.size() > 1) {  // reorder_ci_on_alpha of the core (determinant_sort.hpp:66-90)
+    std::vector<size_t> idx(nkeep);
+    std::iota(idx.begin(), idx.end(), 0);
+    std::sort(idx.begin(), idx.end(), [&](size_t i, size_t j) { return spin_less(wfn[i], wfn[j]); });
+    std::vector<Det> w2(nkeep);
+    std::vector<double> x2(nkeep);
+    for (size_t i = 0; i < nkeep; ++i) {
+      w2[i] = wfn[idx[i]];
+      x2[i] = X[idx[i]];
+    }
+    std::copy(w2.begin(), w2.end(), wfn.begin());
+    std::copy(x2.begin(), x2.end(), X.begin());
+  }
+  std::vector<Det> old_wfn = wfn;
+  std::vector<double> old_X = X;
+  std::vector<Det> core(wfn.begin(), wfn.begin() + nkeep);
+  std::vector<double> ccore(X.begin(), X.begin() + nkeep);
+  wfn = asci_search(H, S, ndets_max, core, ccore, E0);
+  std::sort(wfn.begin(), wfn.end(), spin_less);
+  std::vector<double> Xl;
+  if (S.warm_start) {
+    std::vector<size_t> idx(old_wfn.size());
+    std::iota(idx.begin(), idx.end(), 0);
+    std::sort(idx.begin(), idx.end(), [&](size_t i, size_t j) { return spin_less(old_wfn[i], old_wfn[j]); });
+    Xl.assign(wfn.size(), 0.);
+    for (size_t i = 0; i < wfn.size(); ++i) {
+      auto it = std::lower_bound(idx.begin(), idx.end(), wfn[i],
+                                 [&](size_t k, const Det& d) { return spin_less(old_wfn[k], d); });
+      if (it != idx.end() && old_wfn[*it] == wfn[i]) Xl[i] = old_X[*it];
+    }
+    double nrm = 0.;
+    for (double x : Xl) nrm += x * x;
+    nrm = std::sqrt(nrm);
+    if (nrm < std::max(S.min_warm_start_overlap, 2.220446049250313e-16))
+      Xl.clear();
+    else
+      for (double& x : Xl) x /= nrm;
+  }
+  const double E = sci_diag(H, S, wfn, Xl);
+  X = Xl;
+  return E;
+}
+
+// asci_grow (include/macis/asci/grow.hpp:45-268), without the optional rotations
+double asci_grow(const Ham& H, const AsciSettings& S, double E0, std::vector<Det>& wfn, std::vector<double>& X) {
+  size_t prev = wfn.size();
+  double gf = S.grow_factor;
+  while ((int64_t)wfn.size() < S.ntdets_max) {
+    int64_t nnew = std::min<int64_t>(std::max<int64_t>(S.ntdets_min, (int64_t)std::ceil(wfn.size() * gf)), S.ntdets_max);
+    if (nnew <= (int64_t)wfn.size()) {
+      nnew = std::min<int64_t>(wfn.size() + 1, S.ntdets_max);
+      if (nnew <= (int64_t)wfn.size()) break;
+    }
+    const double E = asci_iter(H, S, nnew, E0, wfn, X);
+    if ((int64_t)wfn.size() < nnew) {
+      gf = std::max(S.min_grow_factor, gf * S.backoff);
+      if (wfn.size() <= prev) break;
+    } else {
+      gf = std::min(S.grow_factor, gf * S.recovery);
+    }
+    prev = wfn.size();
+    E0 = E;
+  }
+  return E0;
+}
+
+// asci_refine (include/macis/asci/refine.hpp:44-237), union stabilisation included
+double asci_refine(const Ham& H, const AsciSettings& S, double E0, std::vector<Det>& wfn, std::vector<double>& X) {
+  int64_t ndets = (int64_t)wfn.size();
+  bool converged = false;
+  double prev_dE = 0.;
+  int osc = 0;
+  int64_t max_iter = S.max_refine_iter, ext = 0;
+  std::vector<Det> prev_wfn;
+  for (int64_t iter = 0; iter < max_iter; ++iter) {
+    const double E = asci_iter(H, S, ndets, E0, wfn, X);
+    if ((int64_t)wfn.size() != ndets) {
+      ndets = (int64_t)wfn.size();
+      if (ndets < S.ntdets_min) break;
+    }
+    const double dE = E - E0;
+    if (std::abs(dE) < S.refine_energy_tol) {
+      E0 = E;
+      converged = true;
+      break;
+    }
+    if (iter > 0 && prev_dE * dE < 0 && std::abs(prev_dE + dE) < S.refine_energy_tol) {
+      osc++;
+      if (osc >= 2 && !prev_wfn.empty()) {
+        std::vector<Det> uni;
+        std::set_union(prev_wfn.begin(), prev_wfn.end(), wfn.begin(), wfn.end(), std::back_inserter(uni), spin_less);
+        std::vector<double> Xu(uni.size(), 0.);
+        for (size_t i = 0; i < wfn.size(); ++i) {
+          auto it = std::lower_bound(uni.begin(), uni.end(), wfn[i], spin_less);
+          if (it != uni.end() && *it == wfn[i]) Xu[it - uni.begin()] = X[i];
+        }
+        const double Eu = sci_diag(H, S, uni, Xu);
+        const int64_t e = std::min<int64_t>(osc, S.max_refine_iter - ext);
+        if (e > 0) {
+          max_iter += e;
+          ext += e;
+        }
+        wfn = uni;
+        X = Xu;
+        ndets = (int64_t)wfn.size();
+        E0 = Eu;
+        prev_wfn.clear();
+        osc = 0;
+        prev_dE = 0.;
+        continue;
+      }
+    } else {
+      osc = 0;
+    }
+    prev_dE = dE;
+    prev_wfn = wfn;
+    E0 = E;
+  }
+  if (!converged) throw std::runtime_error("ASCI Refine did not converge");
+  return E0;
+}
+
 thread_local char g_err[512];
 template <class F>
 int guard(F&& f) {
@@ -934,6 +1307,76 @@ int orc_selected_ci_diag(void* m, int64_t max_m, double tol, double* X, double* 
 }
 
 void orc_syev(int k, double* A, double* w) { jacobi_syev(k, A, k, w); }
+
+// ASCI driver: settings as a flat double array (order of AsciSettings fields
+// below), the initial wavefunction, and the phase ("grow", "refine" or both).
+// Returns the number of determinants (<= cap) written to out_a/out_b/out_c,
+// or -1 on error (orc_last_error).
+int64_t orc_asci(void* h, const double* set, int64_t n0, const uint64_t* a0, const uint64_t* b0, const double* c0,
+                 double E0, int do_grow, int do_refine, int64_t cap, uint64_t* out_a, uint64_t* out_b, double* out_c,
+                 double* E_out, double* E_grow_out) {
+  const Ham& H = *(Ham*)h;
+  AsciSettings S;
+  S.ntdets_max = (int64_t)set[0];
+  S.ntdets_min = (int64_t)set[1];
+  S.ncdets_max = (int64_t)set[2];
+  S.core_fixed = (int)set[3];
+  S.core_threshold = set[4];
+  S.h_el_tol = set[5];
+  S.rv_prune_tol = set[6];
+  S.grow_factor = set[7];
+  S.min_grow_factor = set[8];
+  S.backoff = set[9];
+  S.recovery = set[10];
+  S.max_refine_iter = (int64_t)set[11];
+  S.refine_energy_tol = set[12];
+  S.warm_start = (int)set[13];
+  S.min_warm_start_overlap = set[14];
+  S.ci_res_tol = set[15];
+  S.ci_max_subspace = (int64_t)set[16];
+  S.ci_matel_tol = set[17];
+  int64_t nret = -1;
+  guard([&] {
+    std::vector<Det> wfn(n0);
+    std::vector<double> X(c0, c0 + n0);
+    for (int64_t i = 0; i < n0; ++i) wfn[i] = {a0[i], b0[i]};
+    double E = E0;
+    if (do_grow) E = asci_grow(H, S, E, wfn, X);
+    if (E_grow_out) *E_grow_out = E;
+    if (do_refine) E = asci_refine(H, S, E, wfn, X);
+    *E_out = E;
+    nret = (int64_t)wfn.size();
+    for (int64_t i = 0; i < std::min(nret, cap); ++i) {
+      out_a[i] = wfn[i].a;
+      out_b[i] = wfn[i].b;
+      out_c[i] = X[i];
+    }
+  });
+  return nret;
+}
+
+// One asci_search call (the selection step alone), for parity of selected sets.
+int64_t orc_asci_search(void* h, const double* set, int64_t ncore, const uint64_t* a, const uint64_t* b,
+                        const double* c, double E0, int64_t ndets_max, int64_t cap, uint64_t* out_a,
+                        uint64_t* out_b) {
+  const Ham& H = *(Ham*)h;
+  AsciSettings S;
+  S.h_el_tol = set[5];
+  S.rv_prune_tol = set[6];
+  int64_t nret = -1;
+  guard([&] {
+    std::vector<Det> core(ncore);
+    for (int64_t i = 0; i < ncore; ++i) core[i] = {a[i], b[i]};
+    std::vector<double> C(c, c + ncore);
+    std::vector<Det> out = asci_search(H, S, ndets_max, core, C, E0);
+    nret = (int64_t)out.size();
+    for (int64_t i = 0; i < std::min(nret, cap); ++i) {
+      out_a[i] = out[i].a;
+      out_b[i] = out[i].b;
+    }
+  });
+  return nret;
+}
 
 int64_t orc_sdl_sample(void* h, const uint64_t* alpha, const uint64_t* beta, int64_t nd, double thresh, int64_t stride,
                        int64_t offset) {

@@ -62,6 +62,11 @@ def lib():
         L.orc_csr_build_rows.restype = vp
         L.orc_csr_build_rows.argtypes = [vp, _u64p, _u64p, i64, f64, i64, i64]
         L.orc_csr_spmv_block.argtypes = [vp, _f64p, _f64p]
+        L.orc_asci.restype = i64
+        L.orc_asci.argtypes = [vp, _f64p, i64, _u64p, _u64p, _f64p, f64, ci, ci, i64, _u64p, _u64p, _f64p,
+                               ctypes.POINTER(f64), ctypes.POINTER(f64)]
+        L.orc_asci_search.restype = i64
+        L.orc_asci_search.argtypes = [vp, _f64p, i64, _u64p, _u64p, _f64p, f64, i64, i64, _u64p, _u64p]
         _lib = L
     return _lib
 
@@ -223,3 +228,52 @@ def build_rows(ham, alpha, beta, r0, r1, thresh=np.finfo(np.float64).eps):
     if not h:
         raise RuntimeError(lib().orc_last_error().decode())
     return CsrRows(h, r1 - r0)
+
+
+ASCI_DEFAULTS = dict(ntdets_max=100000, ntdets_min=100, ncdets_max=100, core_fixed=0, core_threshold=0.95,
+                     h_el_tol=1e-8, rv_prune_tol=1e-8, grow_factor=8.0, min_grow_factor=1.01, backoff=0.5,
+                     recovery=1.1, max_refine_iter=6, refine_energy_tol=1e-6, warm_start=1,
+                     min_warm_start_overlap=0.5, ci_res_tol=1e-8, ci_max_subspace=200,
+                     ci_matel_tol=float(np.finfo(np.float64).eps))
+_ASCI_ORDER = list(ASCI_DEFAULTS)
+
+
+def _asci_settings(**kw):
+    d = dict(ASCI_DEFAULTS)
+    for k, v in kw.items():
+        if k not in d:
+            raise KeyError(k)
+        d[k] = v
+    return np.array([float(d[k]) for k in _ASCI_ORDER])
+
+
+def asci(ham, alpha0, beta0, c0, E0, grow=True, refine=True, **settings):
+    """asci_grow then asci_refine (MACIS semantics); returns
+    (E, alpha, beta, C, E_after_grow)."""
+    s = _asci_settings(**settings)
+    cap = int(max(s[0] * 4, 16))
+    oa = np.zeros(cap, dtype=np.uint64)
+    ob = np.zeros(cap, dtype=np.uint64)
+    oc = np.zeros(cap)
+    E = ctypes.c_double()
+    Eg = ctypes.c_double()
+    n = lib().orc_asci(ham._h, s, len(alpha0), np.ascontiguousarray(alpha0, dtype=np.uint64),
+                       np.ascontiguousarray(beta0, dtype=np.uint64), np.ascontiguousarray(c0, dtype=np.float64),
+                       float(E0), int(grow), int(refine), cap, oa, ob, oc, ctypes.byref(E), ctypes.byref(Eg))
+    if n < 0:
+        raise RuntimeError(lib().orc_last_error().decode())
+    return E.value, oa[:n].copy(), ob[:n].copy(), oc[:n].copy(), Eg.value
+
+
+def asci_search(ham, alpha, beta, c, E0, ndets_max, **settings):
+    """One asci_search step on a core (sorted by spin_comparator)."""
+    s = _asci_settings(**settings)
+    cap = int(ndets_max * 4 + len(alpha) + 16)
+    oa = np.zeros(cap, dtype=np.uint64)
+    ob = np.zeros(cap, dtype=np.uint64)
+    n = lib().orc_asci_search(ham._h, s, len(alpha), np.ascontiguousarray(alpha, dtype=np.uint64),
+                              np.ascontiguousarray(beta, dtype=np.uint64), np.ascontiguousarray(c, dtype=np.float64),
+                              float(E0), int(ndets_max), cap, oa, ob)
+    if n < 0:
+        raise RuntimeError(lib().orc_last_error().decode())
+    return oa[:n].copy(), ob[:n].copy()

@@ -34,7 +34,7 @@ EXPORTED = [
     "qdkgb_set_integrals", "qdkgb_fci_dets", "qdkgb_set_dets", "qdkgb_build_hamiltonian", "qdkgb_get_csr32",
     "qdkgb_get_csr64", "qdkgb_diagonal", "qdkgb_spmv", "qdkgb_spmv_device", "qdkgb_davidson_default_settings",
     "qdkgb_davidson", "qdkgb_rdms_spin_dep", "qdkgb_casci", "qdkgb_version", "qdkgb_kernel_launches",
-    "qdkgb_sigma_split_noalloc", "qdkgb_set_csr",
+    "qdkgb_sigma_split_noalloc", "qdkgb_set_csr", "qdkgb_build_direct_sigma",
 ]
 
 
@@ -88,6 +88,7 @@ def lib():
     L.qdkgb_get_csr64.argtypes = [vp, vp, vp, vp]
     L.qdkgb_diagonal.argtypes = [vp, vp]
     L.qdkgb_set_csr.argtypes = [vp, i64, vp, vp, vp]
+    L.qdkgb_build_direct_sigma.argtypes = [vp]
     L.qdkgb_spmv.argtypes = [vp, ci, vp, vp]
     L.qdkgb_spmv_device.argtypes = [vp, ci, vp, vp]
     L.qdkgb_davidson_default_settings.argtypes = [P(DavidsonSettings)]
@@ -221,6 +222,11 @@ class Context:
         self._check(lib().qdkgb_build_hamiltonian(self._h, float(thresh), storage, ctypes.byref(nnz)))
         self.nnz = nnz.value
         return self.nnz
+
+    def build_direct_sigma(self):
+        """Recompute-on-the-fly sigma for a complete space (no CSR stored)."""
+        self._check(lib().qdkgb_build_direct_sigma(self._h))
+        self.nnz = None
 
     def get_csr(self, index_bits=64):
         n, nnz = self.ndets, self.nnz

@@ -92,7 +92,7 @@ static int guarded(qdkgb_context* ctx, F&& f) {
 template <typename I>
 static void get_csr(Context* c, I* rowptr, I* colind, double* values) {
   Hcsr& H = c->H;
-  if (!H.valid) throw Error(QDKGB_ERR_STATE, "Hamiltonian not built");
+  if (!H.valid || c->op_direct) throw Error(QDKGB_ERR_STATE, "no CSR Hamiltonian built");
   if (sizeof(I) == 4 && H.nnz > INT32_MAX) throw Error(QDKGB_ERR_UNSUPPORTED, "nnz exceeds int32");
   std::vector<int64_t> rp(H.n + 1);
   QDKGB_CUDA(cudaMemcpyAsync(rp.data(), H.rowptr.ptr, (H.n + 1) * 8, cudaMemcpyDeviceToHost, c->stream));
@@ -161,6 +161,7 @@ int qdkgb_destroy(qdkgb_context* c) {
                           &c->H.row_nnz, &c->H.scan_tmp, &c->H.xsplit, &c->dav.V, &c->dav.AV, &c->dav.xf, &c->dav.yf, &c->dav.Hk,
                           &c->dav.evec, &c->dav.eval, &c->dav.scratch, &c->dav.partial, &c->dav.small})
     dev_free(c, *b);
+  free_direct(c);
   if (c->pinned) cudaFreeHost(c->pinned);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
   delete c;
@@ -266,6 +267,14 @@ int qdkgb_set_csr(qdkgb_context* c, int64_t n, const int64_t* rowptr, const int6
     if (!rowptr || (!colind && n > 0) || (!values && n > 0)) throw Error(QDKGB_ERR_INVALID, "null CSR buffer");
     QDKGB_CUDA(cudaSetDevice(c->device));
     set_csr(c, n, rowptr, colind, values);
+  });
+}
+
+int qdkgb_build_direct_sigma(qdkgb_context* c) {
+  if (!c) return QDKGB_ERR_INVALID;
+  return guarded(c, [&] {
+    QDKGB_CUDA(cudaSetDevice(c->device));
+    build_direct_sigma(c);
   });
 }
 

@@ -242,6 +242,8 @@ void build_det_space(Context* c, int64_t nd, const uint64_t* alpha, const uint64
   D = DetSpace();
   c->have_dets = false;
   c->H.valid = false;
+  free_direct(c);
+  c->op_direct = false;
   if (nd <= 0) throw Error(QDKGB_ERR_INVALID, "empty determinant list");
   if (nd >= (int64_t)INT32_MAX) throw Error(QDKGB_ERR_UNSUPPORTED, "more than 2^31-1 determinants");
   D.ndets = nd;
@@ -329,6 +331,7 @@ void build_det_space(Context* c, int64_t nd, const uint64_t* alpha, const uint64
       if (!(brank[i - 1] < brank[i]))
         throw Error(QDKGB_ERR_UNSUPPORTED, "repeated determinant or inconsistent beta order in an alpha group");
   D.nbeta = (int64_t)ubeta.size();
+  D.h_ubeta = ubeta;
 
   std::vector<int32_t> det_group(nd);
   std::vector<uint8_t> complete(G);
@@ -542,6 +545,7 @@ void set_csr(Context* c, int64_t n, const int64_t* rowptr, const int64_t* colind
   if (n >= (int64_t)INT32_MAX) throw Error(QDKGB_ERR_UNSUPPORTED, "more than 2^31-1 rows");
   Hcsr& H = c->H;
   H.valid = false;
+  c->op_direct = false;
   const int64_t nnz = rowptr[n] - rowptr[0];
   if (rowptr[0] != 0 || nnz < 0) throw Error(QDKGB_ERR_INVALID, "row pointers must start at 0 and not decrease");
   std::vector<int32_t> ci(std::max<int64_t>(nnz, 1));
@@ -601,6 +605,7 @@ void build_hamiltonian(Context* c, double thresh, int storage) {
   if (storage != QDKGB_H_FP64 && storage != QDKGB_H_SPLIT32) throw Error(QDKGB_ERR_INVALID, "unknown storage");
   Hcsr& H = c->H;
   H.valid = false;
+  c->op_direct = false;
   DetSpace& D = c->dets;
   const int64_t n = D.ndets;
   RowArgs a = row_args(c, thresh);

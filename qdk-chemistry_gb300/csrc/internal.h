@@ -41,6 +41,7 @@ struct DeviceBuffer {
 
 struct Context;
 struct Integrals;
+struct DirectSigma;
 
 void count_launch();
 // message of the last failed call that takes no context (qdkgb_last_error(NULL))
@@ -62,6 +63,7 @@ struct DetSpace {
   bool product = false; // every group holds every beta string (FCI-like)
   std::vector<uint64_t> h_alpha, h_beta;
   std::vector<uint64_t> h_galpha;
+  std::vector<uint64_t> h_ubeta;  // distinct beta strings in rank order
   std::vector<int64_t> h_gstart;
   // device
   DeviceBuffer galpha, gstart, det_group, brank, ubeta, gcomplete;
@@ -99,6 +101,8 @@ struct Context {
   bool have_dets = false;
   Hcsr H;
   DavidsonWork dav;
+  DirectSigma* direct = nullptr;  // recompute-on-the-fly operator (complete spaces)
+  bool op_direct = false;         // Davidson / spmv use the direct sigma instead of the CSR
   DeviceBuffer host_pinned_dummy;
   double* pinned = nullptr;  // small pinned host staging (64 doubles)
 };
@@ -118,6 +122,12 @@ void spmv_fp32(Context* c, const float* x, float* y);
 void csr_values_to_double(Context* c, double* out);
 void f64_to_f32(Context* c, const double* x, float* y, int64_t n);
 void f32_to_f64(Context* c, const float* x, double* y, int64_t n);
+
+// direct.cu
+void build_direct_sigma(Context* c);
+void free_direct(Context* c);
+void direct_sigma_fp64(Context* c, const double* x, double* y);
+void direct_sigma_fp32(Context* c, const float* x, float* y);
 
 // davidson.cu
 void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C, qdkgb_davidson_info* info);

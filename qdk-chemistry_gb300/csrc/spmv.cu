@@ -137,6 +137,10 @@ static unsigned spmv_blocks(Context* c, int64_t n) {
 void spmv_fp64(Context* c, const double* x, double* y) {
   Hcsr& H = c->H;
   if (!H.valid) throw Error(QDKGB_ERR_STATE, "Hamiltonian not built");
+  if (c->op_direct) {
+    direct_sigma_fp64(c, x, y);
+    return;
+  }
   const int64_t* rp = (const int64_t*)H.rowptr.ptr;
   const int32_t* ci = (const int32_t*)H.colind.ptr;
   if (H.storage == QDKGB_H_FP64)
@@ -155,6 +159,10 @@ void spmv_fp64(Context* c, const double* x, double* y) {
 void spmv_fp32(Context* c, const float* x, float* y) {
   Hcsr& H = c->H;
   if (!H.valid) throw Error(QDKGB_ERR_STATE, "Hamiltonian not built");
+  if (c->op_direct) {
+    direct_sigma_fp32(c, x, y);
+    return;
+  }
   if (H.storage != QDKGB_H_SPLIT32)
     throw Error(QDKGB_ERR_STATE, "FP32 sigma needs the Hamiltonian built with QDKGB_H_SPLIT32 storage");
   k_spmv_csr<float, float><<<spmv_blocks(c, H.n), kSpmvWarps * 32, 0, c->stream>>>(

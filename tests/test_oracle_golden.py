@@ -119,3 +119,29 @@ def test_jacobi_syev(oracle):
     wr = np.linalg.eigvalsh(A)
     assert np.allclose(w, wr, atol=1e-12)
     assert np.allclose(Q.T @ A @ Q, np.diag(w), atol=1e-11)
+
+
+def test_h2o_asci_grow_refine_energies(oracle, pkg, h2o, known):
+    """external/macis/tests/asci.cxx:488-574 (Fixed core, ntdets_max 10000)."""
+    ref = known["h2o_asci_10k"]
+    H = oracle.Hamiltonian(h2o["T"], h2o["V"])
+    a0, b0 = pkg.determinants.canonical_hf(5, 5)
+    E0 = H.matrix_element((a0, b0), (a0, b0))
+    E, a, b, c, Eg = oracle.asci(H, [a0], [b0], [1.0], E0, ntdets_max=ref["ntdets_max"], core_fixed=1)
+    assert abs(Eg - ref["E0_grow"]) < 1e-8
+    assert abs(E - ref["E0_refine"]) < 1e-8
+    assert len(a) == 10000 and abs(c @ c - 1.0) < 1e-12
+
+
+def test_n2_asci_energy(oracle, pkg, n2_14e18o, known):
+    """external/macis/python/tests/test_pymacis.py:158-187."""
+    ref = known["n2_14e18o_asci"]
+    H = oracle.Hamiltonian(n2_14e18o["T"], n2_14e18o["V"])
+    a0, b0 = pkg.determinants.canonical_hf(7, 7)
+    E0 = H.matrix_element((a0, b0), (a0, b0))
+    E, a, b, c, _ = oracle.asci(H, [a0], [b0], [1.0], E0, ntdets_max=ref["ntdets_max"],
+                                grow_factor=ref["grow_factor"], max_refine_iter=ref["max_refine_iter"],
+                                ci_max_subspace=ref["max_subspace"])
+    assert np.isclose(E, ref["E_total"])
+    assert abs(E - ref["E_total"]) < 1e-8
+    assert len(a) == ref["ndets"] and np.isclose(np.linalg.norm(c), 1.0)
