@@ -164,6 +164,48 @@ int qdkgb_davidson(qdkgb_context* ctx, const qdkgb_davidson_settings* s, double*
 int qdkgb_rdms_spin_dep(qdkgb_context* ctx, const double* C, double* ordm_aa, double* ordm_bb, double* trdm_aaaa,
                         double* trdm_bbbb, double* trdm_aabb);
 
+/* ------------------------------------------------------------ ASCI
+ * ASCISettings (external/macis/include/macis/asci/determinant_search.hpp:95-199),
+ * the fields the search, grow and refine steps read. */
+typedef struct qdkgb_asci_settings {
+  int64_t ntdets_max;              /* default 100000 */
+  int64_t ntdets_min;              /* default 100 */
+  int64_t ncdets_max;              /* default 100 */
+  int core_selection_fixed;        /* 0: Percentage (default), 1: Fixed */
+  double core_selection_threshold; /* default 0.95 */
+  double h_el_tol;                 /* default 1e-8 */
+  double rv_prune_tol;             /* default 1e-8 */
+  double grow_factor;              /* default 8 */
+  double min_grow_factor;          /* default 1.01 */
+  double growth_backoff_rate;      /* default 0.5 */
+  double growth_recovery_rate;     /* default 1.1 */
+  int64_t max_refine_iter;         /* default 6 */
+  double refine_energy_tol;        /* default 1e-6 */
+  int warm_start;                  /* default 1 */
+  double min_warm_start_overlap;   /* default 0.5 */
+} qdkgb_asci_settings;
+
+void qdkgb_asci_default_settings(qdkgb_asci_settings* s);
+
+/* One determinant search (asci_search, determinant_search.hpp:808-1123) from a
+ * core list (alpha-major sorted) with coefficients: returns in out_a/out_b the
+ * selected targets (tie-inclusive top ndets_max - ncore by |rv|) followed by
+ * the core; *n_out receives the count (written only up to cap). */
+int qdkgb_asci_search(qdkgb_context* ctx, const qdkgb_asci_settings* s, int64_t ncore, const uint64_t* core_alpha,
+                      const uint64_t* core_beta, const double* core_coeff, double E0, int64_t ndets_max, int64_t cap,
+                      uint64_t* out_a, uint64_t* out_b, int64_t* n_out);
+
+/* asci_grow then asci_refine (grow.hpp:45-268, refine.hpp:44-237, iteration
+ * asci_iter, iteration.hpp:50-226) with the search, the H build and the
+ * Davidson on the device.  Starts from (n0 determinants, coefficients, E0 =
+ * electronic energy of the start); returns the final list sorted by
+ * spin_comparator with its eigenvector, the electronic energy and the energy
+ * after the grow phase.  Integrals must be set. */
+int qdkgb_asci(qdkgb_context* ctx, const qdkgb_asci_settings* s, const qdkgb_davidson_settings* ci, double matel_tol,
+               int64_t n0, const uint64_t* a0, const uint64_t* b0, const double* c0, double E0, int do_grow,
+               int do_refine, int64_t cap, uint64_t* out_a, uint64_t* out_b, double* out_c, int64_t* n_out,
+               double* E_out, double* E_grow_out);
+
 /* ------------------------------------------------------------ CASCI driver
  * cas_helper::impl / compute_casci_rdms (cpp/src/qdk/chemistry/algorithms/
  * microsoft/macis_cas.cpp:35-117, include/macis/mcscf/cas.hpp:33-64): FCI

@@ -35,6 +35,7 @@ EXPORTED = [
     "qdkgb_get_csr64", "qdkgb_diagonal", "qdkgb_spmv", "qdkgb_spmv_device", "qdkgb_davidson_default_settings",
     "qdkgb_davidson", "qdkgb_rdms_spin_dep", "qdkgb_casci", "qdkgb_version", "qdkgb_kernel_launches",
     "qdkgb_sigma_split_noalloc", "qdkgb_set_csr", "qdkgb_build_direct_sigma",
+    "qdkgb_asci_default_settings", "qdkgb_asci_search", "qdkgb_asci",
 ]
 
 
@@ -51,6 +52,16 @@ class NotConverged(QdkgbError):
 class DavidsonSettings(ctypes.Structure):
     _fields_ = [("max_m", ctypes.c_int64), ("res_tol", ctypes.c_double), ("precision", ctypes.c_int),
                 ("use_guess", ctypes.c_int), ("min_abs_denominator", ctypes.c_double)]
+
+
+class AsciSettings(ctypes.Structure):
+    _fields_ = [("ntdets_max", ctypes.c_int64), ("ntdets_min", ctypes.c_int64), ("ncdets_max", ctypes.c_int64),
+                ("core_selection_fixed", ctypes.c_int), ("core_selection_threshold", ctypes.c_double),
+                ("h_el_tol", ctypes.c_double), ("rv_prune_tol", ctypes.c_double), ("grow_factor", ctypes.c_double),
+                ("min_grow_factor", ctypes.c_double), ("growth_backoff_rate", ctypes.c_double),
+                ("growth_recovery_rate", ctypes.c_double), ("max_refine_iter", ctypes.c_int64),
+                ("refine_energy_tol", ctypes.c_double), ("warm_start", ctypes.c_int),
+                ("min_warm_start_overlap", ctypes.c_double)]
 
 
 class DavidsonInfo(ctypes.Structure):
@@ -89,6 +100,11 @@ def lib():
     L.qdkgb_diagonal.argtypes = [vp, vp]
     L.qdkgb_set_csr.argtypes = [vp, i64, vp, vp, vp]
     L.qdkgb_build_direct_sigma.argtypes = [vp]
+    L.qdkgb_asci_default_settings.argtypes = [P(AsciSettings)]
+    L.qdkgb_asci_default_settings.restype = None
+    L.qdkgb_asci_search.argtypes = [vp, P(AsciSettings), i64, vp, vp, vp, dp, i64, i64, vp, vp, P(i64)]
+    L.qdkgb_asci.argtypes = [vp, P(AsciSettings), P(DavidsonSettings), dp, i64, vp, vp, vp, dp, ci, ci, i64, vp, vp, vp,
+                             P(i64), P(dp), P(dp)]
     L.qdkgb_spmv.argtypes = [vp, ci, vp, vp]
     L.qdkgb_spmv_device.argtypes = [vp, ci, vp, vp]
     L.qdkgb_davidson_default_settings.argtypes = [P(DavidsonSettings)]
@@ -139,6 +155,16 @@ def sigma_split_noalloc(n, rowptr_ptr, colind_ptr, hi_ptr, lo_ptr, x_ptr, y_ptr,
     rc = lib().qdkgb_sigma_split_noalloc(n, rowptr_ptr, colind_ptr, hi_ptr, lo_ptr, x_ptr, y_ptr, stream_ptr)
     if rc:
         raise QdkgbError(rc, lib().qdkgb_last_error(None).decode())
+
+
+def default_asci_settings(**kw):
+    s = AsciSettings()
+    lib().qdkgb_asci_default_settings(ctypes.byref(s))
+    for k, v in kw.items():
+        if not hasattr(s, k):
+            raise KeyError(k)
+        setattr(s, k, v)
+    return s
 
 
 def default_davidson_settings():
@@ -312,3 +338,49 @@ class Context:
         self.norb = n
         self.ndets = nd.value
         return E.value, C, info.as_dict()
+
+
+def _asci_ctx_check(ctx, rc):
+    ctx._check(rc)
+
+
+def asci_search(ctx, core_alpha, core_beta, core_coeff, E0, ndets_max, **settings):
+    """One GPU determinant search (qdkgb_asci_search)."""
+    s = default_asci_settings(**settings)
+    ca = np.ascontiguousarray(core_alpha, dtype=np.uint64)
+    cb = np.ascontiguousarray(core_beta, dtype=np.uint64)
+    cc = _f64(core_coeff)
+    n = ctypes.c_int64()
+    ctx._check(lib().qdkgb_asci_search(ctx.handle, ctypes.byref(s), len(ca), _ptr(ca), _ptr(cb), _ptr(cc), float(E0),
+                                       int(ndets_max), 0, None, None, ctypes.byref(n)))
+    oa = np.zeros(n.value, dtype=np.uint64)
+    ob = np.zeros(n.value, dtype=np.uint64)
+    ctx._check(lib().qdkgb_asci_search(ctx.handle, ctypes.byref(s), len(ca), _ptr(ca), _ptr(cb), _ptr(cc), float(E0),
+                                       int(ndets_max), n.value, _ptr(oa), _ptr(ob), ctypes.byref(n)))
+    return oa, ob
+
+
+def asci(ctx, alpha0, beta0, c0, E0, grow=True, refine=True, tol=1e-8, max_m=200, precision=PREC_FP64,
+         matel_tol=np.finfo(float).eps, **settings):
+    """asci_grow + asci_refine on the GPU (qdkgb_asci); integrals must be set.
+    Returns (E, alpha, beta, C, E_after_grow)."""
+    s = default_asci_settings(**settings)
+    ci = default_davidson_settings()
+    ci.res_tol = tol
+    ci.max_m = max_m
+    ci.precision = precision
+    a0 = np.ascontiguousarray(alpha0, dtype=np.uint64)
+    b0 = np.ascontiguousarray(beta0, dtype=np.uint64)
+    c0 = _f64(c0)
+    cap = int(max(s.ntdets_max * 4, 16))
+    oa = np.zeros(cap, dtype=np.uint64)
+    ob = np.zeros(cap, dtype=np.uint64)
+    oc = np.zeros(cap)
+    n = ctypes.c_int64()
+    E = ctypes.c_double()
+    Eg = ctypes.c_double()
+    ctx._check(lib().qdkgb_asci(ctx.handle, ctypes.byref(s), ctypes.byref(ci), float(matel_tol), len(a0), _ptr(a0),
+                                _ptr(b0), _ptr(c0), float(E0), int(grow), int(refine), cap, _ptr(oa), _ptr(ob),
+                                _ptr(oc), ctypes.byref(n), ctypes.byref(E), ctypes.byref(Eg)))
+    m = min(n.value, cap)
+    return E.value, oa[:m].copy(), ob[:m].copy(), oc[:m].copy(), Eg.value

@@ -1,0 +1,667 @@
+// ASCI determinant search on the device (replaces asci_search /
+// asci_contributions_constraint, include/macis/asci/determinant_search.hpp:
+// 349-1123, with the contribution formulas of determinant_contributions.hpp:
+// 93-297 and the fast diagonals of src/macis/hamiltonian_generator/
+// fast_diagonals.ipp:52-127).
+//
+// GPU design: one warp per core determinant P enumerates every single and
+// double excitation Q of P as one flat index space (alpha singles, beta
+// singles, alpha-alpha, beta-beta, alpha-beta doubles), evaluates c_P <Q|H|P>
+// and the fast diagonal E0 - H_QQ exactly as the reference does, drops
+// |c h| < h_el_tol, and accumulates into an open-addressing hash table keyed by
+// the full (alpha, beta) pair (128-bit atomicCAS, FP64 atomicAdd of c h).
+// That replaces the reference's constraint partitioning plus sort-and-
+// accumulate: every Q's contributions meet in one slot.  The core itself is
+// inserted with an infinite score and so drops out.  Then |rv| = |sum / (E0 -
+// H_QQ)| is pruned (|rv| > rv_prune_tol), the k-th largest |rv| is found by a
+// radix select on the bit patterns (four 16-bit digits), and every candidate
+// with |rv| >= that value is kept - the reference's tie-inclusive top-k.
+// Summation order inside a slot follows the atomic order, so scores agree
+// with the reference to rounding; selected sets are identical unless two
+// scores tie to the last bits at the cutoff.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "common.cuh"
+#include "internal.h"
+
+namespace qdkgb {
+
+namespace {
+
+typedef unsigned __int128 u128;
+constexpr u128 kEmpty = ~(u128)0;
+constexpr int kAsciWarps = 8;
+constexpr int kMaxOrb = 64;
+
+__device__ __forceinline__ uint64_t mix64(uint64_t x) {
+  x ^= x >> 33;
+  x *= 0xff51afd7ed558ccdULL;
+  x ^= x >> 33;
+  x *= 0xc4ceb9fe1a85ec53ULL;
+  x ^= x >> 33;
+  return x;
+}
+
+struct Table {
+  u128* keys;
+  double* sum;
+  double* hd;
+  uint64_t mask;
+  int* err;  // set when probing exhausts the table
+};
+
+__device__ __forceinline__ void table_add(const Table& t, uint64_t qa, uint64_t qb, double ch, double hd) {
+  const u128 key = ((u128)qb << 64) | (u128)qa;
+  uint64_t h = mix64(qa * 0x9e3779b97f4a7c15ULL ^ mix64(qb)) & t.mask;
+  for (uint64_t probe = 0; probe <= t.mask; ++probe) {
+    const u128 old = atomicCAS(t.keys + h, kEmpty, key);
+    if (old == kEmpty) {
+      t.hd[h] = hd;
+      atomicAdd(t.sum + h, ch);
+      return;
+    }
+    if (old == key) {
+      atomicAdd(t.sum + h, ch);
+      return;
+    }
+    h = (h + 1) & t.mask;
+  }
+  *t.err = 1;
+}
+
+struct CoreArgs {
+  Integrals I;
+  int n;
+  int64_t ncore;
+  const uint64_t* ca;
+  const uint64_t* cb;
+  const double* cc;
+  double E0;
+  double h_el_tol;
+  Table T;
+};
+
+// (i, j) with i < j from a pair index p = j (j - 1) / 2 + i
+__device__ __forceinline__ void pair_of(int p, int& i, int& j) {
+  int jj = (int)((1.0f + sqrtf(1.0f + 8.0f * (float)p)) * 0.5f);
+  while (jj * (jj - 1) / 2 > p) --jj;
+  while ((jj + 1) * jj / 2 <= p) ++jj;
+  j = jj;
+  i = p - jj * (jj - 1) / 2;
+}
+
+struct WarpSm {
+  double ea[kMaxOrb], eb[kMaxOrb];
+  uint8_t oa[kMaxOrb], va[kMaxOrb], ob[kMaxOrb], vb[kMaxOrb];
+};
+
+__device__ __forceinline__ double G2at(const Integrals& I, uint32_t p, uint32_t q) {
+  return ld(I.G2 + p + (size_t)I.n * q);
+}
+__device__ __forceinline__ double V2at(const Integrals& I, uint32_t p, uint32_t q) {
+  return ld(I.V2 + p + (size_t)I.n * q);
+}
+// single_excitation_sign(state, a, i) as a double (+1 / -1)
+__device__ __forceinline__ double sgn(uint64_t state, uint32_t a, uint32_t i) {
+  return excitation_sign_odd(state, a, i) ? -1. : 1.;
+}
+
+__global__ void __launch_bounds__(kAsciWarps * 32) k_asci_enum(CoreArgs A) {
+  __shared__ WarpSm wsm[kAsciWarps];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  WarpSm& s = wsm[w];
+  const Integrals& I = A.I;
+  const int n = A.n;
+  const uint64_t full = (n == 64) ? ~0ull : ((1ull << n) - 1ull);
+  for (int64_t ip = (int64_t)blockIdx.x * kAsciWarps + w; ip < A.ncore; ip += (int64_t)gridDim.x * kAsciWarps) {
+    const uint64_t Pa = A.ca[ip], Pb = A.cb[ip];
+    const double c = A.cc[ip];
+    const int ka = popc64(Pa), kb = popc64(Pb), na_v = n - ka, nb_v = n - kb;
+    // occupied / virtual lists and orbital energies (single_orbital_ens, fast_diagonals.ipp:30-50)
+    if (lane == 0) {
+      int x = 0, y = 0, u = 0, v = 0;
+      for (int p = 0; p < n; ++p) {
+        if ((Pa >> p) & 1)
+          s.oa[x++] = p;
+        else
+          s.va[y++] = p;
+        if ((Pb >> p) & 1)
+          s.ob[u++] = p;
+        else
+          s.vb[v++] = p;
+      }
+    }
+    for (int i = lane; i < n; i += 32) {
+      double e = ld(I.T + i + (size_t)n * i);
+      for (uint64_t m = Pa; m; m &= m - 1) {
+        const uint32_t q = low_bit(m);
+        e += G2at(I, i, q) + G2at(I, q, i);
+      }
+      e -= G2at(I, i, i);
+      for (uint64_t m = Pb; m; m &= m - 1) e += V2at(I, i, low_bit(m));
+      s.ea[i] = e;
+      double f = ld(I.T + i + (size_t)n * i);
+      for (uint64_t m = Pb; m; m &= m - 1) {
+        const uint32_t q = low_bit(m);
+        f += G2at(I, i, q) + G2at(I, q, i);
+      }
+      f -= G2at(I, i, i);
+      for (uint64_t m = Pa; m; m &= m - 1) f += V2at(I, i, low_bit(m));
+      s.eb[i] = f;
+    }
+    double hdiag = 0.;
+    if (lane == 0) hdiag = me_diag(I, Pa, Pb);
+    hdiag = __shfl_sync(QDKGB_FULL_MASK, hdiag, 0);
+    __syncwarp();
+    // the core determinant itself: infinite score (removed later)
+    if (lane == 0) table_add(A.T, Pa, Pb, INFINITY, 1.0);
+    const int64_t nsa = (int64_t)ka * na_v, nsb = (int64_t)kb * nb_v;
+    const int64_t pa_o = (int64_t)ka * (ka - 1) / 2, pa_v = (int64_t)na_v * (na_v - 1) / 2;
+    const int64_t pb_o = (int64_t)kb * (kb - 1) / 2, pb_v = (int64_t)nb_v * (nb_v - 1) / 2;
+    const int64_t nda = pa_o * pa_v, ndb = pb_o * pb_v, nab = nsa * nsb;
+    const int64_t total = nsa + nsb + nda + ndb + nab;
+    for (int64_t e = lane; e < total; e += 32) {
+      double ch = 0., hd = 0.;
+      uint64_t qa = Pa, qb = Pb;
+      bool ok = false;
+      int64_t x = e;
+      if (x < nsa + nsb) {
+        // append_singles_asci_contributions (determinant_contributions.hpp:93-133)
+        const bool alpha = x < nsa;
+        if (!alpha) x -= nsa;
+        const int nv = alpha ? na_v : nb_v;
+        const uint32_t i = alpha ? s.oa[x / nv] : s.ob[x / nv];
+        const uint32_t a = alpha ? s.va[x % nv] : s.vb[x % nv];
+        const uint64_t same = alpha ? Pa : Pb, other = alpha ? Pb : Pa;
+        const size_t nn = (size_t)n;
+        double h = ld(I.T + a + nn * i);
+        const double* G = I.G_red + nn * (a + nn * i);
+        const double* Vr = I.V_red + nn * (a + nn * i);
+        for (uint64_t m = same; m; m &= m - 1) h += ld(G + low_bit(m));
+        for (uint64_t m = other; m; m &= m - 1) h += ld(Vr + low_bit(m));
+        if (fabs(c * h) >= A.h_el_tol) {
+          h *= sgn(same, a, i);
+          const double* eps = alpha ? s.ea : s.eb;
+          const double hdq = hdiag + eps[a] - eps[i] - G2at(I, a, i) - G2at(I, i, a);
+          const uint64_t ex = (same ^ (1ull << i)) | (1ull << a);
+          if (alpha)
+            qa = ex;
+          else
+            qb = ex;
+          ch = c * h;
+          hd = A.E0 - hdq;
+          ok = true;
+        }
+      } else if ((x -= nsa + nsb) < nda + ndb) {
+        // append_ss_doubles_asci_contributions (determinant_contributions.hpp:149-210)
+        const bool alpha = x < nda;
+        if (!alpha) x -= nda;
+        const int64_t pv = alpha ? pa_v : pb_v;
+        int ii, jj, aa, bb;
+        pair_of((int)(x / pv), ii, jj);
+        pair_of((int)(x % pv), aa, bb);
+        const uint8_t* occ = alpha ? s.oa : s.ob;
+        const uint8_t* vir = alpha ? s.va : s.vb;
+        const uint32_t i = occ[ii], j = occ[jj], a = vir[aa], b = vir[bb];
+        const double Gv = Vat(I, b, j, a, i) - Vat(I, b, i, a, j);
+        if (fabs(c * Gv) >= A.h_el_tol) {
+          const uint64_t same = alpha ? Pa : Pb;
+          const uint64_t fullex = (1ull << i) | (1ull << j) | (1ull << a) | (1ull << b);
+          const uint64_t ex = same ^ fullex;
+          // doubles_sign(state_same, ex_det, full_ex): bra = P, ket = Q
+          SingleEx s1 = single_ex(same, ex, fullex);
+          const uint64_t f1 = (1ull << s1.o) | (1ull << s1.v);
+          SingleEx s2 = single_ex(same, ex ^ f1, fullex ^ f1);
+          const double h = (s1.neg != s2.neg) ? -Gv : Gv;
+          const double* eps = alpha ? s.ea : s.eb;
+          const double hdq = hdiag + eps[a] + eps[b] - eps[i] - eps[j] + G2at(I, i, j) + G2at(I, j, i) +
+                             G2at(I, a, b) + G2at(I, b, a) - G2at(I, a, i) - G2at(I, i, a) - G2at(I, b, i) -
+                             G2at(I, i, b) - G2at(I, a, j) - G2at(I, j, a) - G2at(I, b, j) - G2at(I, j, b);
+          if (alpha)
+            qa = ex;
+          else
+            qb = ex;
+          ch = c * h;
+          hd = A.E0 - hdq;
+          ok = true;
+        }
+      } else {
+        // append_os_doubles_asci_contributions (determinant_contributions.hpp:226-297)
+        x -= nda + ndb;
+        const int64_t xa = x / nsb, xb = x % nsb;
+        const uint32_t i = s.oa[xa / na_v], a = s.va[xa % na_v];
+        const uint32_t j = s.ob[xb / nb_v], b = s.vb[xb % nb_v];
+        const double V = Vat(I, a, i, b, j);
+        if (fabs(c * V) >= A.h_el_tol) {
+          const double sg = sgn(Pa, a, i) * sgn(Pb, b, j);
+          const double hdq = hdiag + s.ea[a] + s.eb[b] - s.ea[i] - s.eb[j] + V2at(I, i, j) + V2at(I, a, b) -
+                             G2at(I, a, i) - G2at(I, i, a) - G2at(I, b, j) - G2at(I, j, b) - V2at(I, a, j) -
+                             V2at(I, i, b);
+          qa = (Pa ^ (1ull << i)) | (1ull << a);
+          qb = (Pb ^ (1ull << j)) | (1ull << b);
+          ch = c * sg * V;
+          hd = A.E0 - hdq;
+          ok = true;
+        }
+      }
+      if (ok) table_add(A.T, qa, qb, ch, hd);
+    }
+    __syncwarp();
+    (void)full;
+  }
+}
+
+// candidates: finite score with |rv| > prune; key = bit pattern of |rv|
+__global__ void k_asci_extract(Table T, uint64_t cap, double prune, uint64_t* __restrict__ keys,
+                               uint64_t* __restrict__ slots, unsigned long long* __restrict__ count) {
+  const int lane = threadIdx.x & 31;
+  for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x; i0 < cap; i0 += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t i = i0 + threadIdx.x;
+    bool take = false;
+    double arv = 0.;
+    if (i < cap && T.keys[i] != kEmpty) {
+      const double sm = T.sum[i];
+      if (!isinf(sm)) {
+        arv = fabs(sm / T.hd[i]);
+        take = arv > prune;
+      }
+    }
+    const unsigned m = __ballot_sync(QDKGB_FULL_MASK, take);
+    unsigned long long base = 0;
+    if (lane == 0 && m) base = atomicAdd(count, (unsigned long long)__popc(m));
+    base = __shfl_sync(QDKGB_FULL_MASK, base, 0);
+    if (take) {
+      const unsigned long long p = base + __popc(m & ((1u << lane) - 1u));
+      keys[p] = (uint64_t)__double_as_longlong(arv);
+      slots[p] = i;
+    }
+  }
+}
+
+// histogram (2^width bins, block-local in shared memory) of the digit at
+// `shift` among keys whose higher digits equal `prefix`
+constexpr int kRadixBits = 11;
+__global__ void k_radix_hist(const uint64_t* __restrict__ keys, uint64_t n, int shift, int width, uint64_t prefix,
+                             uint64_t hi_mask, unsigned long long* __restrict__ hist) {
+  __shared__ unsigned int sh[1 << kRadixBits];
+  const int nb = 1 << width;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) sh[i] = 0;
+  __syncthreads();
+  const uint64_t dm = (uint64_t)nb - 1;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t k = keys[i];
+    if ((k & hi_mask) == prefix) atomicAdd(sh + ((k >> shift) & dm), 1u);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nb; i += blockDim.x)
+    if (sh[i]) atomicAdd(hist + i, (unsigned long long)sh[i]);
+}
+
+__global__ void k_asci_select(const uint64_t* __restrict__ keys, const uint64_t* __restrict__ slots, uint64_t n,
+                              uint64_t kth, Table T, uint64_t* __restrict__ oa, uint64_t* __restrict__ ob,
+                              unsigned long long* __restrict__ count) {
+  const int lane = threadIdx.x & 31;
+  for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x; i0 < n; i0 += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t i = i0 + threadIdx.x;
+    const bool take = i < n && keys[i] >= kth;
+    const unsigned m = __ballot_sync(QDKGB_FULL_MASK, take);
+    unsigned long long base = 0;
+    if (lane == 0 && m) base = atomicAdd(count, (unsigned long long)__popc(m));
+    base = __shfl_sync(QDKGB_FULL_MASK, base, 0);
+    if (take) {
+      const unsigned long long p = base + __popc(m & ((1u << lane) - 1u));
+      const u128 key = T.keys[slots[i]];
+      oa[p] = (uint64_t)key;
+      ob[p] = (uint64_t)(key >> 64);
+    }
+  }
+}
+
+__global__ void k_fill_empty(u128* keys, double* sum, uint64_t cap) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < cap; i += (uint64_t)gridDim.x * blockDim.x) {
+    keys[i] = kEmpty;
+    sum[i] = 0.;
+  }
+}
+
+int64_t binom64(int n, int k) {
+  if (k < 0 || k > n) return 0;
+  long double r = 1;
+  for (int i = 1; i <= k; ++i) r = r * (n - k + i) / i;
+  return (int64_t)std::llround(r);
+}
+
+}  // namespace
+
+// Returns the new determinant list (top-k candidates followed by the core).
+void asci_search_gpu(Context* c, int64_t ncore, const uint64_t* ca, const uint64_t* cb, const double* cc, double E0,
+                     int64_t ndets_max, double h_el_tol, double rv_prune_tol, std::vector<uint64_t>& out_a,
+                     std::vector<uint64_t>& out_b, int64_t* n_candidates) {
+  if (!c->have_ints) throw Error(QDKGB_ERR_STATE, "integrals not set");
+  if (ncore <= 0) throw Error(QDKGB_ERR_INVALID, "empty core");
+  const int n = c->norb;
+  // table capacity from the number of contributions (a bound on distinct targets)
+  int64_t total = ncore;
+  for (int64_t i = 0; i < ncore; ++i) {
+    const int ka = __builtin_popcountll(ca[i]), kb = __builtin_popcountll(cb[i]);
+    const int64_t sa = (int64_t)ka * (n - ka), sb = (int64_t)kb * (n - kb);
+    total += sa + sb + sa * sb + binom64(ka, 2) * binom64(n - ka, 2) + binom64(kb, 2) * binom64(n - kb, 2);
+  }
+  size_t freeb = 0, totb = 0;
+  QDKGB_CUDA(cudaMemGetInfo(&freeb, &totb));
+  const size_t slot_bytes = 16 + 8 + 8 + 16;  // key, sum, hd, candidate key + slot
+  uint64_t cap = 1024;
+  while (cap < (uint64_t)(total + total / 2)) cap <<= 1;
+  while (cap * slot_bytes > freeb / 2 && cap > 1024) cap >>= 1;
+  if ((int64_t)cap < std::min<int64_t>(total, (int64_t)1 << 40) / 2)
+    throw Error(QDKGB_ERR_OOM, "ASCI search: hash table does not fit in device memory");
+  DeviceBuffer bkeys, bsum, bhd, bck, bcs, bcnt, berr, bcore, bout, bhist;
+  u128* keys = (u128*)dev_alloc(c, bkeys, cap * 16 + 256);
+  keys = (u128*)(((uintptr_t)keys + 15) & ~(uintptr_t)15);
+  double* sum = dev_array<double>(c, bsum, cap);
+  double* hd = dev_array<double>(c, bhd, cap);
+  int* err = dev_array<int>(c, berr, 1);
+  unsigned long long* cnt = dev_array<unsigned long long>(c, bcnt, 2);
+  QDKGB_CUDA(cudaMemsetAsync(err, 0, sizeof(int), c->stream));
+  QDKGB_CUDA(cudaMemsetAsync(cnt, 0, 2 * sizeof(unsigned long long), c->stream));
+  const unsigned fb = (unsigned)std::min<uint64_t>((cap + 255) / 256, (uint64_t)c->sm_count * 64);
+  k_fill_empty<<<fb, 256, 0, c->stream>>>(keys, sum, cap);
+  QDKGB_CHECK_LAUNCH();
+  uint64_t* dcore = dev_array<uint64_t>(c, bcore, 3 * ncore);
+  QDKGB_CUDA(cudaMemcpyAsync(dcore, ca, ncore * 8, cudaMemcpyHostToDevice, c->stream));
+  QDKGB_CUDA(cudaMemcpyAsync(dcore + ncore, cb, ncore * 8, cudaMemcpyHostToDevice, c->stream));
+  QDKGB_CUDA(cudaMemcpyAsync(dcore + 2 * ncore, cc, ncore * 8, cudaMemcpyHostToDevice, c->stream));
+  CoreArgs A;
+  A.I = integrals_view(c);
+  A.n = n;
+  A.ncore = ncore;
+  A.ca = dcore;
+  A.cb = dcore + ncore;
+  A.cc = (const double*)(dcore + 2 * ncore);
+  A.E0 = E0;
+  A.h_el_tol = h_el_tol;
+  A.T = Table{keys, sum, hd, cap - 1, err};
+  const unsigned eb = (unsigned)std::min<int64_t>((ncore + kAsciWarps - 1) / kAsciWarps, (int64_t)c->sm_count * 16);
+  k_asci_enum<<<eb, kAsciWarps * 32, 0, c->stream>>>(A);
+  QDKGB_CHECK_LAUNCH();
+  uint64_t* ckeys = dev_array<uint64_t>(c, bck, cap);
+  uint64_t* cslots = dev_array<uint64_t>(c, bcs, cap);
+  k_asci_extract<<<fb, 256, 0, c->stream>>>(A.T, cap, rv_prune_tol, ckeys, cslots, cnt);
+  QDKGB_CHECK_LAUNCH();
+  int herr = 0;
+  unsigned long long ncand = 0;
+  QDKGB_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  QDKGB_CUDA(cudaMemcpyAsync(&ncand, cnt, sizeof(ncand), cudaMemcpyDeviceToHost, c->stream));
+  QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+  if (herr) throw Error(QDKGB_ERR_OOM, "ASCI search: hash table overflow");
+  if (n_candidates) *n_candidates = (int64_t)ncand;
+  const int64_t topk = ndets_max - ncore;
+  uint64_t kth = 0;  // keep everything
+  if (topk <= 0) {
+    kth = ~0ull;  // keep nothing but the core
+  } else if ((int64_t)ncand > topk) {
+    // radix select of the topk-th largest key, digits from the top
+    unsigned long long* hist = dev_array<unsigned long long>(c, bhist, 1 << kRadixBits);
+    uint64_t prefix = 0, hi_mask = 0;
+    int64_t k = topk;
+    std::vector<unsigned long long> h(1 << kRadixBits);
+    const unsigned hb = (unsigned)std::min<uint64_t>((ncand + 255) / 256, (uint64_t)c->sm_count * 32);
+    for (int top = 64; top > 0;) {
+      const int width = std::min(kRadixBits, top);
+      const int shift = top - width;
+      const int nb = 1 << width;
+      QDKGB_CUDA(cudaMemsetAsync(hist, 0, nb * 8, c->stream));
+      k_radix_hist<<<hb, 256, 0, c->stream>>>(ckeys, ncand, shift, width, prefix, hi_mask, hist);
+      QDKGB_CHECK_LAUNCH();
+      QDKGB_CUDA(cudaMemcpyAsync(h.data(), hist, nb * 8, cudaMemcpyDeviceToHost, c->stream));
+      QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+      int64_t acc = 0;
+      int d = nb - 1;
+      for (; d >= 0; --d) {
+        if (acc + (int64_t)h[d] >= k) break;
+        acc += (int64_t)h[d];
+      }
+      if (d < 0) d = 0;
+      k -= acc;
+      prefix |= (uint64_t)d << shift;
+      hi_mask |= ((uint64_t)nb - 1) << shift;
+      top = shift;
+    }
+    kth = prefix;
+  }
+  uint64_t* dout = dev_array<uint64_t>(c, bout, 2 * std::max<uint64_t>(ncand, 1));
+  QDKGB_CUDA(cudaMemsetAsync(cnt + 1, 0, sizeof(unsigned long long), c->stream));
+  unsigned long long nsel = 0;
+  if (ncand > 0 && kth != ~0ull) {
+    const unsigned sb = (unsigned)std::min<uint64_t>((ncand + 255) / 256, (uint64_t)c->sm_count * 32);
+    k_asci_select<<<sb, 256, 0, c->stream>>>(ckeys, cslots, ncand, kth, A.T, dout, dout + ncand, cnt + 1);
+    QDKGB_CHECK_LAUNCH();
+    QDKGB_CUDA(cudaMemcpyAsync(&nsel, cnt + 1, sizeof(nsel), cudaMemcpyDeviceToHost, c->stream));
+    QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+  }
+  out_a.resize(nsel + ncore);
+  out_b.resize(nsel + ncore);
+  if (nsel) {
+    QDKGB_CUDA(cudaMemcpyAsync(out_a.data(), dout, nsel * 8, cudaMemcpyDeviceToHost, c->stream));
+    QDKGB_CUDA(cudaMemcpyAsync(out_b.data(), dout + ncand, nsel * 8, cudaMemcpyDeviceToHost, c->stream));
+  }
+  QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+  std::copy(ca, ca + ncore, out_a.begin() + nsel);
+  std::copy(cb, cb + ncore, out_b.begin() + nsel);
+  for (DeviceBuffer* b : {&bkeys, &bsum, &bhd, &bck, &bcs, &bcnt, &berr, &bcore, &bout, &bhist}) dev_free(c, *b);
+}
+
+}  // namespace qdkgb
+
+// ---------------------------------------------------------------- drivers
+namespace qdkgb {
+
+namespace {
+
+struct HDet {
+  uint64_t a, b;
+};
+inline bool hspin_less(const HDet& x, const HDet& y) { return x.a != y.a ? x.a < y.a : x.b < y.b; }
+inline bool hdet_eq(const HDet& x, const HDet& y) { return x.a == y.a && x.b == y.b; }
+
+// selected_ci_diag (selected_ci_diag.hpp:111-158) on the device for a list
+// sorted by spin_comparator; X is the guess (empty: diagonal guess) and the
+// eigenvector on return.
+double sci_diag_gpu(Context* c, const qdkgb_asci_settings& S, const qdkgb_davidson_settings& ci, double matel_tol,
+                    const std::vector<HDet>& dets, std::vector<double>& X) {
+  const int64_t n = (int64_t)dets.size();
+  std::vector<uint64_t> a(n), b(n);
+  for (int64_t i = 0; i < n; ++i) {
+    a[i] = dets[i].a;
+    b[i] = dets[i].b;
+  }
+  build_det_space(c, n, a.data(), b.data());
+  const bool mixed = ci.precision == QDKGB_PREC_MIXED;
+  build_hamiltonian(c, matel_tol, mixed ? QDKGB_H_SPLIT32 : QDKGB_H_FP64);
+  qdkgb_davidson_settings s = ci;
+  s.use_guess = X.empty() ? 0 : 1;
+  X.resize(n, 0.);
+  if (!s.use_guess) std::fill(X.begin(), X.end(), 0.);
+  double E = 0.;
+  davidson(c, &s, &E, X.data(), nullptr);
+  (void)S;
+  return E;
+}
+
+// asci_iter (include/macis/asci/iteration.hpp:50-226)
+double asci_iter_gpu(Context* c, const qdkgb_asci_settings& S, const qdkgb_davidson_settings& ci, double matel_tol,
+                     int64_t ndets_max, double E0, std::vector<HDet>& wfn, std::vector<double>& X,
+                     int64_t* ncand) {
+  if (wfn.size() > 1) {  // reorder_ci_on_coeff (determinant_sort.hpp:45-64)
+    std::vector<size_t> idx(wfn.size());
+    for (size_t i = 0; i < idx.size(); ++i) idx[i] = i;
+    std::sort(idx.begin(), idx.end(), [&](size_t i, size_t j) { return std::fabs(X[i]) > std::fabs(X[j]); });
+    std::vector<HDet> w2(wfn.size());
+    std::vector<double> x2(wfn.size());
+    for (size_t i = 0; i < idx.size(); ++i) {
+      w2[i] = wfn[idx[i]];
+      x2[i] = X[idx[i]];
+    }
+    wfn.swap(w2);
+    X.swap(x2);
+  }
+  size_t nkeep = 0;
+  if (S.core_selection_fixed) {
+    nkeep = std::min<size_t>((size_t)S.ncdets_max, wfn.size());
+  } else {
+    if (!(S.core_selection_threshold >= 2.220446049250313e-16 && S.core_selection_threshold <= 1.0))
+      throw Error(QDKGB_ERR_INVALID, "core_selection_threshold must be in [epsilon, 1.0]");
+    double w = 0.;
+    for (size_t i = 0; i < wfn.size(); ++i) {
+      w += X[i] * X[i];
+      nkeep++;
+      if (w >= S.core_selection_threshold) break;
+    }
+  }
+  if (wfn.size() > 1) {  // reorder_ci_on_alpha of the core (determinant_sort.hpp:66-90)
+    std::vector<size_t> idx(nkeep);
+    for (size_t i = 0; i < nkeep; ++i) idx[i] = i;
+    std::sort(idx.begin(), idx.end(), [&](size_t i, size_t j) { return hspin_less(wfn[i], wfn[j]); });
+    std::vector<HDet> w2(nkeep);
+    std::vector<double> x2(nkeep);
+    for (size_t i = 0; i < nkeep; ++i) {
+      w2[i] = wfn[idx[i]];
+      x2[i] = X[idx[i]];
+    }
+    std::copy(w2.begin(), w2.end(), wfn.begin());
+    std::copy(x2.begin(), x2.end(), X.begin());
+  }
+  std::vector<HDet> old_wfn = wfn;
+  std::vector<double> old_X = X;
+  std::vector<uint64_t> ca(nkeep), cb(nkeep);
+  for (size_t i = 0; i < nkeep; ++i) {
+    ca[i] = wfn[i].a;
+    cb[i] = wfn[i].b;
+  }
+  std::vector<uint64_t> na, nb;
+  asci_search_gpu(c, (int64_t)nkeep, ca.data(), cb.data(), X.data(), E0, ndets_max, S.h_el_tol, S.rv_prune_tol, na,
+                  nb, ncand);
+  wfn.resize(na.size());
+  for (size_t i = 0; i < na.size(); ++i) wfn[i] = {na[i], nb[i]};
+  std::sort(wfn.begin(), wfn.end(), hspin_less);
+  std::vector<double> Xl;
+  if (S.warm_start) {
+    std::vector<size_t> idx(old_wfn.size());
+    for (size_t i = 0; i < idx.size(); ++i) idx[i] = i;
+    std::sort(idx.begin(), idx.end(), [&](size_t i, size_t j) { return hspin_less(old_wfn[i], old_wfn[j]); });
+    Xl.assign(wfn.size(), 0.);
+    for (size_t i = 0; i < wfn.size(); ++i) {
+      auto it = std::lower_bound(idx.begin(), idx.end(), wfn[i],
+                                 [&](size_t k, const HDet& d) { return hspin_less(old_wfn[k], d); });
+      if (it != idx.end() && hdet_eq(old_wfn[*it], wfn[i])) Xl[i] = old_X[*it];
+    }
+    double nrm = 0.;
+    for (double x : Xl) nrm += x * x;
+    nrm = std::sqrt(nrm);
+    if (nrm < std::max(S.min_warm_start_overlap, 2.220446049250313e-16))
+      Xl.clear();
+    else
+      for (double& x : Xl) x /= nrm;
+  }
+  const double E = sci_diag_gpu(c, S, ci, matel_tol, wfn, Xl);
+  X = Xl;
+  return E;
+}
+
+}  // namespace
+
+void asci_run(Context* c, const qdkgb_asci_settings& S, const qdkgb_davidson_settings& ci, double matel_tol,
+              std::vector<uint64_t>& a, std::vector<uint64_t>& b, std::vector<double>& X, double& E0, bool grow,
+              bool refine, double* E_grow) {
+  std::vector<HDet> wfn(a.size());
+  for (size_t i = 0; i < a.size(); ++i) wfn[i] = {a[i], b[i]};
+  int64_t ncand = 0;
+  if (grow) {
+    // asci_grow (include/macis/asci/grow.hpp:45-268), without rotations
+    size_t prev = wfn.size();
+    double gf = S.grow_factor;
+    while ((int64_t)wfn.size() < S.ntdets_max) {
+      int64_t nnew = std::min<int64_t>(
+          std::max<int64_t>(S.ntdets_min, (int64_t)std::ceil((double)wfn.size() * gf)), S.ntdets_max);
+      if (nnew <= (int64_t)wfn.size()) {
+        nnew = std::min<int64_t>((int64_t)wfn.size() + 1, S.ntdets_max);
+        if (nnew <= (int64_t)wfn.size()) break;
+      }
+      const double E = asci_iter_gpu(c, S, ci, matel_tol, nnew, E0, wfn, X, &ncand);
+      if ((int64_t)wfn.size() < nnew) {
+        gf = std::max(S.min_grow_factor, gf * S.growth_backoff_rate);
+        if (wfn.size() <= prev) break;
+      } else {
+        gf = std::min(S.grow_factor, gf * S.growth_recovery_rate);
+      }
+      prev = wfn.size();
+      E0 = E;
+    }
+  }
+  if (E_grow) *E_grow = E0;
+  if (refine) {
+    // asci_refine (include/macis/asci/refine.hpp:44-237)
+    int64_t ndets = (int64_t)wfn.size();
+    bool converged = false;
+    double prev_dE = 0.;
+    int osc = 0;
+    int64_t max_iter = S.max_refine_iter, ext = 0;
+    std::vector<HDet> prev_wfn;
+    for (int64_t iter = 0; iter < max_iter; ++iter) {
+      const double E = asci_iter_gpu(c, S, ci, matel_tol, ndets, E0, wfn, X, &ncand);
+      if ((int64_t)wfn.size() != ndets) {
+        ndets = (int64_t)wfn.size();
+        if (ndets < S.ntdets_min) break;
+      }
+      const double dE = E - E0;
+      if (std::fabs(dE) < S.refine_energy_tol) {
+        E0 = E;
+        converged = true;
+        break;
+      }
+      if (iter > 0 && prev_dE * dE < 0 && std::fabs(prev_dE + dE) < S.refine_energy_tol) {
+        osc++;
+        if (osc >= 2 && !prev_wfn.empty()) {
+          std::vector<HDet> uni;
+          std::set_union(prev_wfn.begin(), prev_wfn.end(), wfn.begin(), wfn.end(), std::back_inserter(uni),
+                         hspin_less);
+          std::vector<double> Xu(uni.size(), 0.);
+          for (size_t i = 0; i < wfn.size(); ++i) {
+            auto it = std::lower_bound(uni.begin(), uni.end(), wfn[i], hspin_less);
+            if (it != uni.end() && hdet_eq(*it, wfn[i])) Xu[it - uni.begin()] = X[i];
+          }
+          const double Eu = sci_diag_gpu(c, S, ci, matel_tol, uni, Xu);
+          const int64_t e = std::min<int64_t>(osc, S.max_refine_iter - ext);
+          if (e > 0) {
+            max_iter += e;
+            ext += e;
+          }
+          wfn = uni;
+          X = Xu;
+          ndets = (int64_t)wfn.size();
+          E0 = Eu;
+          prev_wfn.clear();
+          osc = 0;
+          prev_dE = 0.;
+          continue;
+        }
+      } else {
+        osc = 0;
+      }
+      prev_dE = dE;
+      prev_wfn = wfn;
+      E0 = E;
+    }
+    if (!converged) throw Error(QDKGB_ERR_NOT_CONVERGED, "ASCI Refine did not converge");
+  }
+  a.resize(wfn.size());
+  b.resize(wfn.size());
+  for (size_t i = 0; i < wfn.size(); ++i) {
+    a[i] = wfn[i].a;
+    b[i] = wfn[i].b;
+  }
+}
+
+}  // namespace qdkgb

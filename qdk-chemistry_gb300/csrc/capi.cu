@@ -361,6 +361,67 @@ int qdkgb_rdms_spin_dep(qdkgb_context* c, const double* C, double* aa, double* b
   });
 }
 
+void qdkgb_asci_default_settings(qdkgb_asci_settings* s) {
+  if (!s) return;
+  s->ntdets_max = 100000;
+  s->ntdets_min = 100;
+  s->ncdets_max = 100;
+  s->core_selection_fixed = 0;
+  s->core_selection_threshold = 0.95;
+  s->h_el_tol = 1e-8;
+  s->rv_prune_tol = 1e-8;
+  s->grow_factor = 8.0;
+  s->min_grow_factor = 1.01;
+  s->growth_backoff_rate = 0.5;
+  s->growth_recovery_rate = 1.1;
+  s->max_refine_iter = 6;
+  s->refine_energy_tol = 1e-6;
+  s->warm_start = 1;
+  s->min_warm_start_overlap = 0.5;
+}
+
+int qdkgb_asci_search(qdkgb_context* c, const qdkgb_asci_settings* s, int64_t ncore, const uint64_t* ca,
+                      const uint64_t* cb, const double* cc, double E0, int64_t ndets_max, int64_t cap, uint64_t* out_a,
+                      uint64_t* out_b, int64_t* n_out) {
+  if (!c) return QDKGB_ERR_INVALID;
+  return guarded(c, [&] {
+    if (!s || !ca || !cb || !cc || !n_out) throw Error(QDKGB_ERR_INVALID, "null argument");
+    QDKGB_CUDA(cudaSetDevice(c->device));
+    std::vector<uint64_t> a, b;
+    asci_search_gpu(c, ncore, ca, cb, cc, E0, ndets_max, s->h_el_tol, s->rv_prune_tol, a, b, nullptr);
+    *n_out = (int64_t)a.size();
+    for (int64_t i = 0; i < std::min<int64_t>((int64_t)a.size(), cap); ++i) {
+      if (out_a) out_a[i] = a[i];
+      if (out_b) out_b[i] = b[i];
+    }
+  });
+}
+
+int qdkgb_asci(qdkgb_context* c, const qdkgb_asci_settings* s, const qdkgb_davidson_settings* ci, double matel_tol,
+               int64_t n0, const uint64_t* a0, const uint64_t* b0, const double* c0, double E0, int do_grow,
+               int do_refine, int64_t cap, uint64_t* out_a, uint64_t* out_b, double* out_c, int64_t* n_out,
+               double* E_out, double* E_grow_out) {
+  if (!c) return QDKGB_ERR_INVALID;
+  return guarded(c, [&] {
+    if (!s || !a0 || !b0 || !c0 || n0 <= 0 || !n_out || !E_out) throw Error(QDKGB_ERR_INVALID, "null argument");
+    if (!c->have_ints) throw Error(QDKGB_ERR_STATE, "integrals not set");
+    QDKGB_CUDA(cudaSetDevice(c->device));
+    qdkgb_davidson_settings def;
+    qdkgb_davidson_default_settings(&def);
+    std::vector<uint64_t> a(a0, a0 + n0), b(b0, b0 + n0);
+    std::vector<double> X(c0, c0 + n0);
+    double E = E0;
+    asci_run(c, *s, ci ? *ci : def, matel_tol, a, b, X, E, do_grow != 0, do_refine != 0, E_grow_out);
+    *n_out = (int64_t)a.size();
+    *E_out = E;
+    for (int64_t i = 0; i < std::min<int64_t>((int64_t)a.size(), cap); ++i) {
+      if (out_a) out_a[i] = a[i];
+      if (out_b) out_b[i] = b[i];
+      if (out_c) out_c[i] = X[i];
+    }
+  });
+}
+
 int qdkgb_casci(qdkgb_context* c, int norb, int nalpha, int nbeta, const double* T, const double* V, int layout,
                 const qdkgb_davidson_settings* s, double matel_tol, double* E, double* C,
                 qdkgb_davidson_info* info) {

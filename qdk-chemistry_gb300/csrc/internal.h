@@ -129,6 +129,14 @@ void free_direct(Context* c);
 void direct_sigma_fp64(Context* c, const double* x, double* y);
 void direct_sigma_fp32(Context* c, const float* x, float* y);
 
+// asci.cu
+void asci_search_gpu(Context* c, int64_t ncore, const uint64_t* ca, const uint64_t* cb, const double* cc, double E0,
+                     int64_t ndets_max, double h_el_tol, double rv_prune_tol, std::vector<uint64_t>& out_a,
+                     std::vector<uint64_t>& out_b, int64_t* n_candidates);
+void asci_run(Context* c, const qdkgb_asci_settings& S, const qdkgb_davidson_settings& ci, double matel_tol,
+              std::vector<uint64_t>& a, std::vector<uint64_t>& b, std::vector<double>& X, double& E0, bool grow,
+              bool refine, double* E_grow);
+
 // davidson.cu
 void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C, qdkgb_davidson_info* info);
 

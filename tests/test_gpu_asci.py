@@ -1,0 +1,66 @@
+"""GPU ASCI (search, grow, refine) against the oracle and the reference's
+golden energies.  Selected determinant sets are compared as sets, bit-exact;
+energies to 1e-8 Eh (the reference's davidson_tolerance)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx(pkg):
+    pkg.build.build()
+    c = pkg.capi.Context(0)
+    yield c
+    c.close()
+
+
+def _as_set(a, b):
+    return set(zip(a.tolist(), b.tolist()))
+
+
+def test_asci_search_selected_set_matches_oracle(ctx, pkg, oracle, h2o):
+    """One search step from a water wavefunction of 800 determinants (core =
+    the 100 largest), asking for 6400: the GPU set equals the oracle's set."""
+    H = oracle.Hamiltonian(h2o["T"], h2o["V"])
+    a0, b0 = pkg.determinants.canonical_hf(5, 5)
+    E0 = H.matrix_element((a0, b0), (a0, b0))
+    E, a, b, c, _ = oracle.asci(H, [a0], [b0], [1.0], E0, ntdets_max=800, core_fixed=1, max_refine_iter=0,
+                                refine=False)
+    order = np.argsort(-np.abs(c), kind="stable")[:100]
+    ca, cb, cc = a[order], b[order], c[order]
+    srt = np.lexsort((cb, ca))
+    ca, cb, cc = ca[srt], cb[srt], cc[srt]
+    oa, ob = oracle.asci_search(H, ca, cb, cc, E, 6400)
+    ctx.set_integrals(h2o["T"], h2o["V"])
+    ga, gb = pkg.capi.asci_search(ctx, ca, cb, cc, E, 6400)
+    assert len(ga) == len(oa) == 6400
+    assert _as_set(ga, gb) == _as_set(oa, ob)
+
+
+def test_asci_water_10k_golden(ctx, pkg, oracle, h2o, known):
+    """external/macis/tests/asci.cxx:488-574 on the GPU path."""
+    ref = known["h2o_asci_10k"]
+    H = oracle.Hamiltonian(h2o["T"], h2o["V"])
+    a0, b0 = pkg.determinants.canonical_hf(5, 5)
+    E0 = H.matrix_element((a0, b0), (a0, b0))
+    ctx.set_integrals(h2o["T"], h2o["V"])
+    E, a, b, c, Eg = pkg.capi.asci(ctx, [a0], [b0], [1.0], E0, ntdets_max=10000, core_selection_fixed=1)
+    assert abs(Eg - ref["E0_grow"]) < 1e-8
+    assert abs(E - ref["E0_refine"]) < 1e-8
+    assert len(a) == 10000 and abs(c @ c - 1) < 1e-12
+    Eo, oa, ob, oc, _ = oracle.asci(H, [a0], [b0], [1.0], E0, ntdets_max=10000, core_fixed=1)
+    assert _as_set(a, b) == _as_set(oa, ob)
+
+
+def test_asci_n2_golden(ctx, pkg, oracle, n2_14e18o, known):
+    """external/macis/python/tests/test_pymacis.py:158-187 on the GPU path."""
+    ref = known["n2_14e18o_asci"]
+    H = oracle.Hamiltonian(n2_14e18o["T"], n2_14e18o["V"])
+    a0, b0 = pkg.determinants.canonical_hf(7, 7)
+    E0 = H.matrix_element((a0, b0), (a0, b0))
+    ctx.set_integrals(n2_14e18o["T"], n2_14e18o["V"])
+    E, a, b, c, _ = pkg.capi.asci(ctx, [a0], [b0], [1.0], E0, ntdets_max=ref["ntdets_max"],
+                                  grow_factor=ref["grow_factor"], max_refine_iter=ref["max_refine_iter"], max_m=254)
+    assert abs(E - ref["E_total"]) < 1e-8
+    assert len(a) == ref["ndets"]
