@@ -252,7 +252,7 @@ class Context:
     def build_direct_sigma(self):
         """Recompute-on-the-fly sigma for a complete space (no CSR stored)."""
         self._check(lib().qdkgb_build_direct_sigma(self._h))
-        self.nnz = None
+        self.nnz = 0  # no CSR: get_csr reports the library's error
 
     def get_csr(self, index_bits=64):
         n, nnz = self.ndets, self.nnz
