@@ -189,6 +189,22 @@ __global__ void k_set_onehot(double* x, int64_t n, const int64_t* idx) {
     x[i] = (i == *idx) ? 1. : 0.;
 }
 __global__ void k_set_value(double* p, double v) { *p = v; }
+// x <- (x + s x^T) / 2 for x viewed as an n x n matrix (coefficients C[Ia, Ib]
+// of a product space whose alpha and beta string lists coincide): projection
+// on the spin-flip sector of parity s
+__global__ void k_flip_project(double* x, int64_t n, double s) {
+  const int64_t total = n * n;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = t / n, j = t % n;
+    if (i < j) {
+      const double avg = 0.5 * (x[i * n + j] + s * x[j * n + i]);
+      x[i * n + j] = avg;
+      x[j * n + i] = s * avg;
+    } else if (i == j && s < 0) {
+      x[t] = 0.;
+    }
+  }
+}
 // Hk(i, c) = Hk(c, i) = v[c], c <= i
 __global__ void k_store_row(const double* v, int i, double* Hk, int ld) {
   for (int c = threadIdx.x; c <= i; c += blockDim.x) {
@@ -691,8 +707,45 @@ void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C
     double* tmpV = d.work + 2 * N;
     double* tmpAV = d.work + (2 + kKeep) * N;
     double* Eptr = d.small + kSlotE;
+    // The reference's FP64 iteration keeps the guess's spin-flip symmetry
+    // (C[Ia, Ib] = +-C[Ib, Ia] when both spins share one string list): H and
+    // the preconditioner commute with the flip.  FP32 sigma noise does not, and
+    // can steer the solve into the other sector when that one holds a lower
+    // state; new directions are therefore projected on the guess's sector.
+    double flip = 0.;
+    int64_t nstr = 0;
+    {
+      const DetSpace& S = c->dets;
+      bool square = c->have_dets && S.ndets == N && S.ngroups == S.nbeta && S.ngroups * S.nbeta == N &&
+                    S.h_galpha == S.h_ubeta;
+      for (int64_t g = 0; g < S.ngroups && square; ++g) square = (S.h_gstart[g + 1] - S.h_gstart[g]) == S.nbeta;
+      if (square) {
+        nstr = S.nbeta;
+        std::vector<double> g0(N);
+        QDKGB_CUDA(cudaMemcpyAsync(g0.data(), V0, N * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+        double dp = 0., dm = 0., nn = 0.;
+        for (int64_t i = 0; i < nstr; ++i)
+          for (int64_t j = 0; j < nstr; ++j) {
+            const double x = g0[i * nstr + j], y = g0[j * nstr + i];
+            dp += (x - y) * (x - y);
+            dm += (x + y) * (x + y);
+            nn += x * x;
+          }
+        if (dp <= 1e-24 * nn)
+          flip = 1.;
+        else if (dm <= 1e-24 * nn)
+          flip = -1.;
+      }
+    }
+    auto project = [&](double* v) {
+      if (flip == 0.) return;
+      k_flip_project<<<d.nb, 256, 0, c->stream>>>(v, nstr, flip);
+      QDKGB_CHECK_LAUNCH();
+    };
     sigma_full(V0, d.AV);
     QDKGB_CUDA(cudaMemcpyAsync(d.col(d.V, 1), d.AV, N * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    project(d.col(d.V, 1));
     d.gram_schmidt(1, d.col(d.V, 1));
     d.projected_row(0);
     // residual of the guess (exact): reference level for the first refresh
@@ -738,6 +791,7 @@ void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C
       if (!refresh) {
         k_precondition<<<d.nb, 256, 0, c->stream>>>(R, d.D, d.eval, N, s->min_abs_denominator);
         QDKGB_CHECK_LAUNCH();
+        project(R);
         d.gram_schmidt(k, R);
         continue;
       }
@@ -779,6 +833,7 @@ void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C
       QDKGB_CUDA(cudaMemcpyAsync(d.col(d.V, k), Rt, N * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
       k_precondition<<<d.nb, 256, 0, c->stream>>>(d.col(d.V, k), d.D, Eptr, N, s->min_abs_denominator);
       QDKGB_CHECK_LAUNCH();
+      project(d.col(d.V, k));
       d.gram_schmidt(k, d.col(d.V, k));
       best = 1e300;
       since_best = 0;

@@ -224,3 +224,17 @@ def test_rdms_o2_wavefunction_golden(ctx, oracle, pkg):
     trdm = R["aaaa"] + R["bbbb"] + R["aabb"] + R["aabb"].transpose(2, 3, 0, 1)
     assert abs(np.abs(ordm).sum() - 8.0000005763) < 1e-6
     assert abs(np.abs(trdm).sum() - 44.1092472977) < 1e-6
+
+
+def test_mixed_precision_stays_in_the_guess_symmetry_sector(ctx, oracle, pkg, capi):
+    """Seeded case whose lowest S_z = 0 state is odd under spin flip: the
+    reference's FP64 iteration from the closed-shell guess stays in the even
+    sector; the mixed solve must land on the same state."""
+    T, V, a, b = _cas(pkg, 10, 10, 20, seed=9)
+    M = oracle.build_csr(oracle.Hamiltonian(T, V), a, b)
+    Eo, _, _ = M.selected_ci_diag(tol=1e-9)
+    ctx.set_integrals(T, V)
+    ctx.set_dets(a, b)
+    ctx.build_hamiltonian(storage=capi.H_SPLIT32)
+    E, C, info = ctx.davidson(tol=1e-8, precision=capi.PREC_MIXED)
+    assert abs(E - Eo) < 1e-8, (E, Eo)
