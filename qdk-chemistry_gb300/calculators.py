@@ -272,7 +272,87 @@ class Gb300Cas(MultiConfigurationCalculator):
             return self._solve(ctx, hamiltonian, a, b)
 
 
-_REGISTRY = {"multi_configuration_calculator": {"gb300_cas": Gb300Cas}}
+class Gb300AsciSettings(Gb300Settings):
+    """MacisAsciSettings names and defaults (macis_asci.hpp:36-189, from
+    ASCISettings, determinant_search.hpp:95-199)."""
+
+    def __init__(self):
+        super().__init__()
+        self.set_default("ntdets_max", int, 100000, "Maximum number of determinants", (1, 2 ** 63 - 1))
+        self.set_default("ntdets_min", int, 100, "Minimum number of determinants", (1, 2 ** 63 - 1))
+        self.set_default("ncdets_max", int, 100, "Maximum number of core determinants", (1, 2 ** 63 - 1))
+        self.set_default("search_matel_tol", float, 1e-8, "ASCI search matrix element threshold", (0.0, 1.0))
+        self.set_default("rv_prune_tol", float, 1e-8, "ASCI score pruning threshold", (0.0, 1.0))
+        self.set_default("refine_energy_tol", float, 1e-6, "refinement energy tolerance", (0.0, 1.0))
+        self.set_default("grow_factor", float, 8.0, "growth factor", (1.0, 1e6))
+        self.set_default("min_grow_factor", float, 1.01, "minimum growth factor", (1.0, 1e6))
+        self.set_default("growth_backoff_rate", float, 0.5, "grow factor backoff", (0.0, 1.0))
+        self.set_default("growth_recovery_rate", float, 1.1, "grow factor recovery", (1.0, 1e6))
+        self.set_default("max_refine_iter", int, 6, "maximum refinement iterations", (0, 2 ** 63 - 1))
+        self.set_default("core_selection_strategy", str, "percentage", "'percentage' or 'fixed'")
+        self.set_default("core_selection_threshold", float, 0.95, "core weight fraction", (0.0, 1.0))
+        self.set_default("warm_start_davidson", bool, True)
+        self.set_default("min_warm_start_overlap", float, 0.5, "", (0.0, 1.0))
+
+
+class Gb300Asci(MultiConfigurationCalculator):
+    """Selected CI grown by ASCI (MacisAsci, macis_asci.cpp:44-234): the full
+    space when ntdets_max exceeds its dimension, otherwise asci_grow from the
+    Hartree-Fock determinant then asci_refine (when max_refine_iter > 0)."""
+
+    def _make_settings(self):
+        return Gb300AsciSettings()
+
+    def name(self):
+        return "gb300_asci"
+
+    def _run_impl(self, hamiltonian, n_alpha, n_beta):
+        self._check_unsupported()
+        s = self._settings
+        n = hamiltonian.norb
+        if not (0 <= n_alpha <= n and 0 <= n_beta <= n):
+            raise ValueError("electron counts must lie in [0, norb]")
+        strategy = s.get("core_selection_strategy").lower()
+        if strategy not in ("percentage", "fixed"):
+            raise ValueError("Invalid core_selection_strategy: '%s'. Valid options are 'fixed' or 'percentage'."
+                             % strategy)
+        from math import comb
+        if s.get("ntdets_max") > comb(n, n_alpha) * comb(n, n_beta):
+            return Gb300Cas._run_impl(self, hamiltonian, n_alpha, n_beta)
+        prec = s.get("precision")
+        with capi.Context(s.get("device")) as ctx:
+            ctx.set_integrals(hamiltonian.get_one_body_integrals(), hamiltonian.get_two_body_integrals())
+            a0, b0 = determinants.canonical_hf(n_alpha, n_beta)
+            ctx.set_dets([a0], [b0])
+            # E0 = <HF|H|HF> (macis_asci.cpp:159-163)
+            ctx.build_hamiltonian(0.0)
+            E0 = float(ctx.diagonal()[0])
+            E, a, b, C, _ = capi.asci(
+                ctx, [a0], [b0], [1.0], E0, grow=True, refine=s.get("max_refine_iter") > 0,
+                tol=s.get("ci_residual_tolerance"), max_m=min(s.get("max_solver_iterations"), 254),
+                precision=capi.PREC_MIXED if prec == "mixed" else capi.PREC_FP64, matel_tol=s.get("ci_matel_tol"),
+                ntdets_max=s.get("ntdets_max"), ntdets_min=s.get("ntdets_min"), ncdets_max=s.get("ncdets_max"),
+                core_selection_fixed=1 if strategy == "fixed" else 0,
+                core_selection_threshold=s.get("core_selection_threshold"), h_el_tol=s.get("search_matel_tol"),
+                rv_prune_tol=s.get("rv_prune_tol"), grow_factor=s.get("grow_factor"),
+                min_grow_factor=s.get("min_grow_factor"), growth_backoff_rate=s.get("growth_backoff_rate"),
+                growth_recovery_rate=s.get("growth_recovery_rate"), max_refine_iter=s.get("max_refine_iter"),
+                refine_energy_tol=s.get("refine_energy_tol"), warm_start=int(s.get("warm_start_davidson")),
+                min_warm_start_overlap=s.get("min_warm_start_overlap"))
+            rdms = None
+            want = []
+            if s.get("calculate_one_rdm"):
+                want += ["aa", "bb"]
+            if s.get("calculate_two_rdm"):
+                want += ["aaaa", "bbbb", "aabb"]
+            if want:
+                ctx.set_dets(a, b)
+                rdms = ctx.rdms_spin_dep(C, want=tuple(want))
+        wfn = Wavefunction(n, a, b, C, rdms)
+        return E + hamiltonian.get_core_energy(), wfn
+
+
+_REGISTRY = {"multi_configuration_calculator": {"gb300_cas": Gb300Cas, "gb300_asci": Gb300Asci}}
 _DEFAULT = {"multi_configuration_calculator": "gb300_cas"}
 
 

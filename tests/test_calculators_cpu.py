@@ -6,7 +6,7 @@ import pytest
 
 def test_registry_and_defaults(pkg):
     calc = pkg.calculators
-    assert "gb300_cas" in calc.available()
+    assert "gb300_cas" in calc.available() and "gb300_asci" in calc.available()
     c = calc.create("multi_configuration_calculator")
     assert c.name() == "gb300_cas"
     s = c.settings()

@@ -94,3 +94,29 @@ def test_autograd_rdm_gradients_match_finite_differences(pkg):
             fd = (energy(T, V + h * dV) - energy(T, V - h * dV)) / (2 * h)
             an = sum(gV[idx] for idx in orbit)
         assert abs(fd - an) < 1e-6, (trial, fd, an)
+
+
+def test_gb300_asci_calculator_n2(pkg, n2_14e18o, known):
+    """The qdk-style ASCI plugin with the pymacis test's settings."""
+    ref = known["n2_14e18o_asci"]
+    calc = pkg.calculators.create("multi_configuration_calculator", "gb300_asci")
+    s = calc.settings()
+    s.set("ci_residual_tolerance", 1e-8)
+    s.set("ntdets_max", ref["ntdets_max"])
+    s.set("grow_factor", float(ref["grow_factor"]))
+    s.set("max_refine_iter", ref["max_refine_iter"])
+    s.set("calculate_one_rdm", True)
+    H = pkg.calculators.Hamiltonian(n2_14e18o["T"], n2_14e18o["V"], n2_14e18o["E_core"])
+    E, wfn = calc.run(H, 7, 7)
+    assert abs(E - n2_14e18o["E_core"] - ref["E_total"]) < 1e-8
+    assert wfn.size() == ref["ndets"]
+    aa, bb = wfn.get_active_one_rdm_spin_dependent()
+    assert abs(np.trace(aa) - 7) < 1e-8 and abs(np.trace(bb) - 7) < 1e-8
+
+
+def test_gb300_asci_falls_back_to_cas_for_small_spaces(pkg, n2_6e6o, known):
+    calc = pkg.calculators.create("multi_configuration_calculator", "gb300_asci")
+    calc.settings().set("ci_residual_tolerance", 1e-8)
+    H = pkg.calculators.Hamiltonian(n2_6e6o["T"], n2_6e6o["V"], 0.0)
+    E, wfn = calc.run(H, 3, 3)
+    assert wfn.size() == 400 and np.isclose(E, known["n2_6e6o_casci"]["E_total"])
