@@ -162,6 +162,7 @@ int qdkgb_destroy(qdkgb_context* c) {
                           &c->dav.evec, &c->dav.eval, &c->dav.scratch, &c->dav.partial, &c->dav.small})
     dev_free(c, *b);
   free_direct(c);
+  free_struct(c);
   if (c->pinned) cudaFreeHost(c->pinned);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
   delete c;

@@ -243,6 +243,7 @@ void build_det_space(Context* c, int64_t nd, const uint64_t* alpha, const uint64
   c->have_dets = false;
   c->H.valid = false;
   free_direct(c);
+  free_struct(c);
   c->op_direct = false;
   if (nd <= 0) throw Error(QDKGB_ERR_INVALID, "empty determinant list");
   if (nd >= (int64_t)INT32_MAX) throw Error(QDKGB_ERR_UNSUPPORTED, "more than 2^31-1 determinants");
@@ -355,6 +356,7 @@ void build_det_space(Context* c, int64_t nd, const uint64_t* alpha, const uint64
   build_conn(c, (const uint64_t*)D.galpha.ptr, G, 4, true, D.acon_ptr, D.acon_idx, &D.acon_lvl, D.acon_total);
   build_conn(c, (const uint64_t*)D.ubeta.ptr, D.nbeta, 4, false, D.b2_ptr, D.b2_idx, nullptr, D.b2_total);
   build_conn(c, (const uint64_t*)D.ubeta.ptr, D.nbeta, 2, false, D.b1_ptr, D.b1_idx, nullptr, D.b1_total);
+  build_struct(c);
   c->have_dets = true;
 }
 
@@ -369,6 +371,13 @@ __global__ void k_diag(Integrals I, int64_t n, const int32_t* __restrict__ det_g
     const uint64_t a = galpha[det_group[r]];
     D[r] = a ? me_diag(I, a, ubeta[brank[r]]) : 0.;
   }
+}
+
+void k_diag_launch(Context* c, const Integrals& I, double* D, unsigned blocks) {
+  const DetSpace& S = c->dets;
+  k_diag<<<blocks, 256, 0, c->stream>>>(I, S.ndets, (const int32_t*)S.det_group.ptr, (const int32_t*)S.brank.ptr,
+                                        (const uint64_t*)S.galpha.ptr, (const uint64_t*)S.ubeta.ptr, D);
+  QDKGB_CHECK_LAUNCH();
 }
 
 // Pre-threshold row lengths: the number of connected determinants present in
@@ -545,6 +554,7 @@ void set_csr(Context* c, int64_t n, const int64_t* rowptr, const int64_t* colind
   if (n >= (int64_t)INT32_MAX) throw Error(QDKGB_ERR_UNSUPPORTED, "more than 2^31-1 rows");
   Hcsr& H = c->H;
   H.valid = false;
+  H.structured = false;
   c->op_direct = false;
   const int64_t nnz = rowptr[n] - rowptr[0];
   if (rowptr[0] != 0 || nnz < 0) throw Error(QDKGB_ERR_INVALID, "row pointers must start at 0 and not decrease");
@@ -605,7 +615,12 @@ void build_hamiltonian(Context* c, double thresh, int storage) {
   if (storage != QDKGB_H_FP64 && storage != QDKGB_H_SPLIT32) throw Error(QDKGB_ERR_INVALID, "unknown storage");
   Hcsr& H = c->H;
   H.valid = false;
+  H.structured = false;
   c->op_direct = false;
+  if (c->fci) {
+    build_hamiltonian_struct(c, thresh, storage);
+    return;
+  }
   DetSpace& D = c->dets;
   const int64_t n = D.ndets;
   RowArgs a = row_args(c, thresh);

@@ -42,6 +42,7 @@ struct DeviceBuffer {
 struct Context;
 struct Integrals;
 struct DirectSigma;
+struct FciStruct;
 
 void count_launch();
 // message of the last failed call that takes no context (qdkgb_last_error(NULL))
@@ -79,6 +80,7 @@ struct Hcsr {
   double thresh = 0.;
   DeviceBuffer rowptr, colind, val, hi, lo, diag, diag_raw, row_nnz, scan_tmp, xsplit;
   bool valid = false;
+  bool structured = false;  // complete space, nothing thresholded: columns implied by the row tables
 };
 
 struct DavidsonWork {
@@ -102,6 +104,7 @@ struct Context {
   Hcsr H;
   DavidsonWork dav;
   DirectSigma* direct = nullptr;  // recompute-on-the-fly operator (complete spaces)
+  FciStruct* fci = nullptr;       // row-shape tables of a complete space (structured kernels)
   bool op_direct = false;         // Davidson / spmv use the direct sigma instead of the CSR
   DeviceBuffer host_pinned_dummy;
   double* pinned = nullptr;  // small pinned host staging (64 doubles)
@@ -122,6 +125,15 @@ void spmv_fp32(Context* c, const float* x, float* y);
 void csr_values_to_double(Context* c, double* out);
 void f64_to_f32(Context* c, const double* x, float* y, int64_t n);
 void f32_to_f64(Context* c, const float* x, double* y, int64_t n);
+
+// fci_struct.cu
+void build_struct(Context* c);
+void free_struct(Context* c);
+bool struct_ready(Context* c);
+void struct_spmv_fp64(Context* c, const double* x, double* y);
+void struct_spmv_fp32(Context* c, const float* x, float* y);
+void build_hamiltonian_struct(Context* c, double thresh, int storage);
+void k_diag_launch(Context* c, const Integrals& I, double* D, unsigned blocks);
 
 // direct.cu
 void build_direct_sigma(Context* c);

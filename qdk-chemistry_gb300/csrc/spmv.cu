@@ -141,6 +141,10 @@ void spmv_fp64(Context* c, const double* x, double* y) {
     direct_sigma_fp64(c, x, y);
     return;
   }
+  if (struct_ready(c) && H.storage == QDKGB_H_FP64) {
+    struct_spmv_fp64(c, x, y);
+    return;
+  }
   const int64_t* rp = (const int64_t*)H.rowptr.ptr;
   const int32_t* ci = (const int32_t*)H.colind.ptr;
   if (H.storage == QDKGB_H_FP64)
@@ -161,6 +165,10 @@ void spmv_fp32(Context* c, const float* x, float* y) {
   if (!H.valid) throw Error(QDKGB_ERR_STATE, "Hamiltonian not built");
   if (c->op_direct) {
     direct_sigma_fp32(c, x, y);
+    return;
+  }
+  if (struct_ready(c) && H.storage == QDKGB_H_SPLIT32) {
+    struct_spmv_fp32(c, x, y);
     return;
   }
   if (H.storage != QDKGB_H_SPLIT32)
