@@ -97,7 +97,23 @@ static void get_csr(Context* c, I* rowptr, I* colind, double* values) {
   std::vector<int64_t> rp(H.n + 1);
   QDKGB_CUDA(cudaMemcpyAsync(rp.data(), H.rowptr.ptr, (H.n + 1) * 8, cudaMemcpyDeviceToHost, c->stream));
   std::vector<int32_t> ci;
-  if (colind) {
+  if (H.structured) {
+    // slab layout: produce the CSR arrays on the device
+    DeviceBuffer cib, vb;
+    const int64_t cap = std::max<int64_t>(H.nnz, 1);
+    int32_t* dci = dev_array<int32_t>(c, cib, cap);
+    double* dv = dev_array<double>(c, vb, cap);
+    struct_export(c, dci, dv, nullptr, nullptr);
+    if (colind) {
+      ci.resize(H.nnz);
+      QDKGB_CUDA(cudaMemcpyAsync(ci.data(), dci, H.nnz * 4, cudaMemcpyDeviceToHost, c->stream));
+    }
+    if (values) QDKGB_CUDA(cudaMemcpyAsync(values, dv, H.nnz * 8, cudaMemcpyDeviceToHost, c->stream));
+    QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+    dev_free(c, cib);
+    dev_free(c, vb);
+    values = nullptr;
+  } else if (colind) {
     ci.resize(H.nnz);
     QDKGB_CUDA(cudaMemcpyAsync(ci.data(), H.colind.ptr, H.nnz * 4, cudaMemcpyDeviceToHost, c->stream));
   }

@@ -174,4 +174,30 @@ __device__ __forceinline__ T warp_sum(T v) {
   return v;
 }
 
+// Unevaluated float-float sum (two-sum), used by the full-precision sigma
+// from split storage: a.s + a.c carries ~2^-44 relative accuracy on the FP32
+// pipe.
+struct FF {
+  float s, c;
+};
+__device__ __forceinline__ void ff_add(FF& a, float p, float e) {
+  const float t = a.s + p;
+  const float bv = t - a.s;
+  const float err = (a.s - (t - bv)) + (p - bv);
+  a.s = t;
+  a.c += err + e;
+}
+__device__ __forceinline__ FF ff_merge(FF a, FF b) {
+  FF r = a;
+  ff_add(r, b.s, b.c);
+  return r;
+}
+// (h + l)(x + y) as p + e with p = fl(h x) and e its rounding error plus the
+// cross terms (the l*y term is below the pair's resolution)
+__device__ __forceinline__ void ff_prod(float h, float l, float x, float y, float& p, float& e) {
+  p = h * x;
+  e = fmaf(h, x, -p);
+  e = fmaf(h, y, fmaf(l, x, e));
+}
+
 }  // namespace qdkgb

@@ -1,25 +1,27 @@
-// Structured kernels for complete (CAS) determinant spaces.
+// Slab kernels for complete (CAS) determinant spaces.
 //
 // In a full (n_alpha, n_beta) product space every row has the same shape: the
 // row of determinant r = g * N_b + b (alpha group g, beta string b) holds, in
 // ascending column order, one block per alpha group h within a double
 // excitation of g - the beta strings within level 2 of b for h = g, within
-// level 1 for an alpha single, b alone for an alpha double.  The position of
-// every element inside its row is therefore known from (g, entry, k) alone:
-// per alpha group three short tables (the level-1 and level-2 groups with the
-// offset of their block in the row, and the offset of the own-group block)
-// replace the per-element search of the general row walk.
+// level 1 for an alpha single, b alone for an alpha double.  The sequence of
+// blocks depends on g only, so a row position p names the same (h, beta-list
+// entry) for every b of the group.
 //
-// Two uses:
-//  * emission: each element is written at its fixed slot (columns and values),
-//    elements that fail |h| > thresh are marked and removed by a compaction
-//    pass only when any exist;
-//  * sigma without column indices: when no element was removed, the CSR
-//    columns of row r are implied by these tables, so the sigma streams only
-//    the values (4 B per nonzero in FP32, 8 B in FP64) and regenerates the
-//    columns from tables that stay in L1/L2.
+// Slab layout: the Hamiltonian of such a space is stored values-only as
+//     value(g, p, b) at ((g * rowlen + p) * N_b + b),
+// beta string fastest.  A thread owns one row (one b) of a group and walks the
+// positions: the per-position descriptor is warp-uniform, the value and
+// beta-list loads are coalesced, and the x of the own group and of the alpha
+// singles (the blocks of the position range a CTA covers) is staged in shared
+// memory, so each element costs one streamed value, one cached list entry, one
+// shared-memory gather and an FMA.  Elements dropped by the threshold are
+// stored as zero (the operator is unchanged); the CSR arrays the reference
+// defines are produced from the slab on request (export), or in place of it
+// when most elements are dropped.
 #include <algorithm>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "common.cuh"
@@ -27,17 +29,39 @@
 
 namespace qdkgb {
 
+constexpr int kListAlphaDouble = 2047;       // beta-list index meaning "b itself"
+constexpr size_t kSlabSmemMax = 200 * 1024;  // staged x + segment record per CTA
+constexpr int kSlabUnroll = 8;               // independent value loads in flight per thread
+constexpr int kSlabThreads = 1024;           // sigma CTA size (one CTA per SM)
+constexpr int kEmitSegments = 4;             // position ranges per group in emission / export
+
+// Sigma work split for one staged-x element size: CTA per (group, segment);
+// a segment is a run of whole row items (the own-group block, alpha-single
+// blocks, alpha-double elements).  Per (g, s) a record of R int32:
+//   [0] own-group block present, [1] its offset p * Nb, [2] its slot * Nb,
+//   [3] n1b, then n1b pairs (p_e * Nb, slot_e * Nb) of alpha-single blocks,
+//   then nd and one pad word, then nd pairs (p_j * Nb, h_j * Nb) of alpha
+//   doubles,
+// and segh[g][s][0..M) the alpha group whose x slice each slot holds.
+struct SlabPlan {
+  int S = 0, M = 0, R = 0;
+  DeviceBuffer rec, segh;
+};
+
 struct FciStruct {
   int64_t G = 0, Nb = 0;
   int n1 = 0, n2 = 0;  // beta list lengths (level <= 1, level <= 2), uniform
-  int c1 = 0, c2 = 0;  // alpha singles / doubles per group, uniform
-  int64_t rowlen = 0;  // n2 + c1 * n1 + c2
-  DeviceBuffer l0_off, l1_h, l1_off, l2_h, l2_off;
+  int rowlen = 0;      // n2 + c1 * n1 + c2
+  DeviceBuffer blT;    // [n2 + n1][Nb] int32: entry k of b's level-2 list, then of its level-1 list
+  DeviceBuffer gdesc;  // [G][rowlen] h << 11 | list entry (kListAlphaDouble: b itself)
+  SlabPlan plan[2];    // staged x of 4 bytes (FP32) / 8 bytes (FP64, split pair)
+  DeviceBuffer ypart;  // [S][n] partial sums (S > 1)
 };
 
 void free_struct(Context* c) {
   if (!c->fci) return;
-  for (DeviceBuffer* b : {&c->fci->l0_off, &c->fci->l1_h, &c->fci->l1_off, &c->fci->l2_h, &c->fci->l2_off})
+  for (DeviceBuffer* b : {&c->fci->blT, &c->fci->gdesc, &c->fci->plan[0].rec, &c->fci->plan[0].segh,
+                          &c->fci->plan[1].rec, &c->fci->plan[1].segh, &c->fci->ypart})
     dev_free(c, *b);
   delete c->fci;
   c->fci = nullptr;
@@ -49,20 +73,20 @@ void build_struct(Context* c) {
   free_struct(c);
   DetSpace& D = c->dets;
   const int64_t G = D.ngroups, Nb = D.nbeta;
-  if (G * Nb != D.ndets || G < 1) return;
+  if (G * Nb != D.ndets || G < 1 || G >= (1 << 20)) return;
   for (int64_t g = 0; g < G; ++g) {
     if (D.h_gstart[g + 1] - D.h_gstart[g] != Nb) return;
     if (D.h_galpha[g] == 0) return;
   }
-  if (D.ndets >= (int64_t)INT32_MAX) return;
-  // beta list lengths
   std::vector<int64_t> b1p(Nb + 1), b2p(Nb + 1);
   QDKGB_CUDA(cudaMemcpy(b1p.data(), D.b1_ptr.ptr, (Nb + 1) * 8, cudaMemcpyDeviceToHost));
   QDKGB_CUDA(cudaMemcpy(b2p.data(), D.b2_ptr.ptr, (Nb + 1) * 8, cudaMemcpyDeviceToHost));
   const int64_t n1 = b1p[1] - b1p[0], n2 = b2p[1] - b2p[0];
+  if (n1 + n2 >= kListAlphaDouble) return;
   for (int64_t b = 0; b < Nb; ++b)
     if (b1p[b + 1] - b1p[b] != n1 || b2p[b + 1] - b2p[b] != n2) return;
-  // alpha connectivity, split by level with each block's offset in the row
+  // one staged block must fit the shared-memory budget
+  if ((size_t)Nb * 8 > kSlabSmemMax / 2) return;
   std::vector<int64_t> ap(G + 1);
   QDKGB_CUDA(cudaMemcpy(ap.data(), D.acon_ptr.ptr, (G + 1) * 8, cudaMemcpyDeviceToHost));
   std::vector<int32_t> aidx(ap[G]);
@@ -71,129 +95,237 @@ void build_struct(Context* c) {
     QDKGB_CUDA(cudaMemcpy(aidx.data(), D.acon_idx.ptr, ap[G] * 4, cudaMemcpyDeviceToHost));
     QDKGB_CUDA(cudaMemcpy(alvl.data(), D.acon_lvl.ptr, ap[G], cudaMemcpyDeviceToHost));
   }
-  int c1 = -1, c2 = -1;
-  std::vector<int32_t> l0(G), l1h, l1o, l2h, l2o;
+  // descriptors in row order; per position the staged block it belongs to
+  // (index of the own-group / alpha-single block in the row, -1 for an
+  // alpha double)
+  int rowlen = -1, c1 = -1, c2 = -1;
+  struct PlanHost {
+    int S, M, R;
+    std::vector<int32_t> rec, segh;
+  } plan_tmp[2];
+  std::vector<uint32_t> gdesc;
+  std::vector<int32_t> pblock;  // [G][rowlen]
   for (int64_t g = 0; g < G; ++g) {
-    int64_t off = 0;
-    int k1 = 0, k2 = 0, k0 = 0;
+    const size_t row0 = gdesc.size();
+    int k0 = 0, k1 = 0, k2 = 0, nb = 0;
     for (int64_t e = ap[g]; e < ap[g + 1]; ++e) {
-      const int lv = alvl[e];
-      if (lv == 0) {
+      const uint32_t h = (uint32_t)aidx[e];
+      if (alvl[e] == 0) {
         if (aidx[e] != g) return;  // repeated alpha string
-        l0[g] = (int32_t)off;
-        off += n2;
+        for (int64_t k = 0; k < n2; ++k) {
+          gdesc.push_back((h << 11) | (uint32_t)k);
+          pblock.push_back(nb);
+        }
+        ++nb;
         ++k0;
-      } else if (lv == 1) {
-        l1h.push_back(aidx[e]);
-        l1o.push_back((int32_t)off);
-        off += n1;
+      } else if (alvl[e] == 1) {
+        for (int64_t k = 0; k < n1; ++k) {
+          gdesc.push_back((h << 11) | (uint32_t)(n2 + k));
+          pblock.push_back(nb);
+        }
+        ++nb;
         ++k1;
       } else {
-        l2h.push_back(aidx[e]);
-        l2o.push_back((int32_t)off);
-        off += 1;
+        gdesc.push_back((h << 11) | (uint32_t)kListAlphaDouble);
+        pblock.push_back(-1);
         ++k2;
       }
     }
     if (k0 != 1) return;
-    if (c1 < 0) {
+    if (rowlen < 0) {
+      rowlen = (int)(gdesc.size() - row0);
       c1 = k1;
       c2 = k2;
+      if ((int64_t)rowlen * G * 4 > ((int64_t)1 << 30)) return;  // tables above 1 GiB
     }
-    if (k1 != c1 || k2 != c2) return;
+    if (k1 != c1 || k2 != c2 || (int)(gdesc.size() - row0) != rowlen) return;
+  }
+  if (n2 + (int64_t)c1 * n1 + c2 != rowlen) return;
+  if ((int64_t)rowlen * Nb >= INT32_MAX) return;  // int32 slab offsets within a group
+  // row items of every group: (first position, length, alpha group)
+  struct Item {
+    int p, len, h;
+  };
+  std::vector<Item> items;
+  std::vector<int> item0(G + 1, 0);
+  for (int64_t g = 0; g < G; ++g) {
+    int p = 0;
+    while (p < rowlen) {
+      const size_t i = (size_t)g * rowlen + p;
+      const int bk = pblock[i];
+      int len = 1;
+      if (bk >= 0)
+        while (p + len < rowlen && pblock[i + len] == bk) ++len;
+      items.push_back({p, bk >= 0 ? len : 0, (int)(gdesc[i] >> 11)});  // len 0: alpha double
+      p += len;
+    }
+    item0[g + 1] = (int)items.size();
+  }
+  auto seg_of = [&](const Item& it, int S) {
+    const int len = std::max(it.len, 1);
+    return std::min(S - 1, (int)(((int64_t)(2 * it.p + len) * S) / (2 * (int64_t)rowlen)));
+  };
+  // per plan: the segment count that fits the budget and fills the SMs best
+  for (int pl = 0; pl < 2; ++pl) {
+    const size_t xsize = pl == 0 ? 4 : 8;
+    auto shape = [&](int S, int& M, int& R) {
+      M = 1;
+      R = 6;
+      for (int64_t g = 0; g < G; ++g) {
+        std::vector<int> nb(S, 0), nd(S, 0);
+        for (int i = item0[g]; i < item0[g + 1]; ++i) {
+          const int sg = seg_of(items[i], S);
+          if (items[i].len) ++nb[sg];
+          else ++nd[sg];
+        }
+        for (int sg = 0; sg < S; ++sg) {
+          M = std::max(M, nb[sg]);
+          R = std::max(R, 6 + 2 * (nb[sg] + nd[sg]));
+        }
+      }
+    };
+    auto smem_of = [&](int M, int R) { return (size_t)M * Nb * xsize + ((size_t)R * 4 + 15) / 16 * 16; };
+    int best_S = -1, best_M = 0, best_R = 0;
+    double best = -1.;
+    const int threads = std::min<int64_t>(kSlabThreads, (Nb + 31) / 32 * 32);
+    for (int S = 1; S <= 16 && S <= rowlen; ++S) {
+      int M, R;
+      shape(S, M, R);
+      const size_t sm = smem_of(M, R);
+      if (sm > kSlabSmemMax) continue;
+      const int64_t per_sm = std::max<int64_t>(1, std::min<int64_t>(2048 / threads, (227 * 1024) / (int64_t)sm));
+      const int64_t slots = per_sm * c->sm_count, n_items = G * S;
+      const double eff = (double)n_items / (double)(((n_items + slots - 1) / slots) * slots);
+      const double score = eff - 0.01 * S;
+      if (score > best) {
+        best = score;
+        best_S = S;
+        best_M = M;
+        best_R = R;
+      }
+    }
+    if (best_S < 0) return;
+    const int S = best_S, M = best_M, R = best_R;
+    std::vector<int32_t> rec((size_t)G * S * R, 0), segh((size_t)G * S * M, -1);
+    for (int64_t g = 0; g < G; ++g) {
+      std::vector<std::vector<int32_t>> b1(S), dd(S);
+      std::vector<int> nslot(S, 0);
+      for (int i = item0[g]; i < item0[g + 1]; ++i) {
+        const Item& it = items[i];
+        const int sg = seg_of(it, S);
+        int32_t* r = &rec[((size_t)g * S + sg) * R];
+        if (it.len == 0) {
+          dd[sg].push_back((int32_t)(it.p * Nb));
+          dd[sg].push_back((int32_t)(it.h * Nb));
+          continue;
+        }
+        const int slot = nslot[sg]++;
+        segh[((size_t)g * S + sg) * M + slot] = it.h;
+        if (it.h == g) {
+          r[0] = 1;
+          r[1] = (int32_t)(it.p * Nb);
+          r[2] = (int32_t)(slot * Nb);
+        } else {
+          b1[sg].push_back((int32_t)(it.p * Nb));
+          b1[sg].push_back((int32_t)(slot * Nb));
+        }
+      }
+      for (int sg = 0; sg < S; ++sg) {
+        int32_t* r = &rec[((size_t)g * S + sg) * R];
+        r[3] = (int32_t)(b1[sg].size() / 2);
+        std::copy(b1[sg].begin(), b1[sg].end(), r + 4);
+        r[4 + b1[sg].size()] = (int32_t)(dd[sg].size() / 2);
+        std::copy(dd[sg].begin(), dd[sg].end(), r + 6 + b1[sg].size());
+      }
+    }
+    plan_tmp[pl] = {S, M, R, std::move(rec), std::move(segh)};
+  }
+  // transposed beta lists
+  std::vector<int32_t> b1(Nb * n1), b2(Nb * n2), blT((n1 + n2) * Nb);
+  QDKGB_CUDA(cudaMemcpy(b1.data(), D.b1_idx.ptr, b1.size() * 4, cudaMemcpyDeviceToHost));
+  QDKGB_CUDA(cudaMemcpy(b2.data(), D.b2_idx.ptr, b2.size() * 4, cudaMemcpyDeviceToHost));
+  for (int64_t b = 0; b < Nb; ++b) {
+    for (int64_t k = 0; k < n2; ++k) blT[k * Nb + b] = b2[b * n2 + k];
+    for (int64_t k = 0; k < n1; ++k) blT[(n2 + k) * Nb + b] = b1[b * n1 + k];
   }
   FciStruct* F = new FciStruct();
   F->G = G;
   F->Nb = Nb;
   F->n1 = (int)n1;
   F->n2 = (int)n2;
-  F->c1 = c1;
-  F->c2 = c2;
-  F->rowlen = n2 + (int64_t)c1 * n1 + c2;
-  auto up = [&](DeviceBuffer& b, const std::vector<int32_t>& v) {
-    void* p = dev_alloc(c, b, std::max<size_t>(v.size(), 1) * 4 + 16);
-    if (!v.empty()) QDKGB_CUDA(cudaMemcpy(p, v.data(), v.size() * 4, cudaMemcpyHostToDevice));
+  F->rowlen = rowlen;
+  auto up = [&](DeviceBuffer& buf, const void* src, size_t bytes) {
+    void* p = dev_alloc(c, buf, std::max<size_t>(bytes, 4) + 16);
+    if (bytes) QDKGB_CUDA(cudaMemcpy(p, src, bytes, cudaMemcpyHostToDevice));
   };
-  up(F->l0_off, l0);
-  up(F->l1_h, l1h);
-  up(F->l1_off, l1o);
-  up(F->l2_h, l2h);
-  up(F->l2_off, l2o);
+  up(F->blT, blT.data(), blT.size() * 4);
+  up(F->gdesc, gdesc.data(), gdesc.size() * 4);
+  for (int pl = 0; pl < 2; ++pl) {
+    F->plan[pl].S = plan_tmp[pl].S;
+    F->plan[pl].M = plan_tmp[pl].M;
+    F->plan[pl].R = plan_tmp[pl].R;
+    up(F->plan[pl].rec, plan_tmp[pl].rec.data(), plan_tmp[pl].rec.size() * 4);
+    up(F->plan[pl].segh, plan_tmp[pl].segh.data(), plan_tmp[pl].segh.size() * 4);
+  }
   c->fci = F;
 }
 
 namespace {
 
-struct SArgs {
-  int64_t G, Nb;
-  int n1, n2, c1, c2;
-  int64_t rowlen;
-  const int32_t* l0_off;
-  const int32_t* l1_h;
-  const int32_t* l1_off;
-  const int32_t* l2_h;
-  const int32_t* l2_off;
-  const int32_t* b1_idx;  // [Nb][n1]
-  const int32_t* b2_idx;  // [Nb][n2]
+struct SlabArgs {
+  int G, Nb, rowlen, n1, n2;
+  int seglen;  // emission / export position range per CTA
+  const int32_t* blT;
+  const uint32_t* gdesc;
 };
 
-SArgs sargs(Context* c) {
+SlabArgs slab_args(Context* c) {
   FciStruct* F = c->fci;
-  SArgs s;
-  s.G = F->G;
-  s.Nb = F->Nb;
-  s.n1 = F->n1;
-  s.n2 = F->n2;
-  s.c1 = F->c1;
-  s.c2 = F->c2;
-  s.rowlen = F->rowlen;
-  s.l0_off = (const int32_t*)F->l0_off.ptr;
-  s.l1_h = (const int32_t*)F->l1_h.ptr;
-  s.l1_off = (const int32_t*)F->l1_off.ptr;
-  s.l2_h = (const int32_t*)F->l2_h.ptr;
-  s.l2_off = (const int32_t*)F->l2_off.ptr;
-  s.b1_idx = (const int32_t*)c->dets.b1_idx.ptr;
-  s.b2_idx = (const int32_t*)c->dets.b2_idx.ptr;
-  return s;
+  SlabArgs a;
+  a.G = (int)F->G;
+  a.Nb = (int)F->Nb;
+  a.rowlen = F->rowlen;
+  a.n1 = F->n1;
+  a.n2 = F->n2;
+  a.seglen = (F->rowlen + kEmitSegments - 1) / kEmitSegments;
+  a.blT = (const int32_t*)F->blT.ptr;
+  a.gdesc = (const uint32_t*)F->gdesc.ptr;
+  return a;
 }
 
-// Calls f(pos_in_row, col) for every element of row r (g = r / Nb, b = r % Nb),
-// lanes striding three flat ranges; the order is free, positions are exact.
-template <typename F>
-__device__ __forceinline__ void for_each_struct(const SArgs& s, int64_t g, int64_t b, int lane, F&& f) {
-  const int64_t gb = g * s.Nb;
-  const int32_t o0 = __ldg(s.l0_off + g);
-  const int32_t* b2 = s.b2_idx + b * s.n2;
-  for (int k = lane; k < s.n2; k += 32) f((int64_t)o0 + k, gb + __ldg(b2 + k));
-  const int32_t* b1 = s.b1_idx + b * s.n1;
-  const int64_t t1 = (int64_t)s.c1 * s.n1;
-  for (int64_t t = lane; t < t1; t += 32) {
-    const int e = (int)(t / s.n1), k = (int)(t - (int64_t)e * s.n1);
-    const int64_t ge = g * s.c1 + e;
-    f((int64_t)__ldg(s.l1_off + ge) + k, (int64_t)__ldg(s.l1_h + ge) * s.Nb + __ldg(b1 + k));
-  }
-  for (int t = lane; t < s.c2; t += 32) {
-    const int64_t ge = g * s.c2 + t;
-    f((int64_t)__ldg(s.l2_off + ge), (int64_t)__ldg(s.l2_h + ge) * s.Nb + b);
-  }
-}
+struct PlanArgs {
+  int S, M, R;
+  const int32_t* rec;
+  const int32_t* segh;
+};
+
+unsigned slab_threads(int Nb) { return (unsigned)std::min(kSlabThreads, (Nb + 31) / 32 * 32); }
+
+// ------------------------------------------------------------------ emission
+// CTA per (group, segment), a thread per beta string, positions in order.
+// Every element is written (zero when dropped); kept counts go to kept[r].
+constexpr int kEmitThreads = 256;
 
 template <int STORAGE>
-__global__ void __launch_bounds__(256)
-    k_struct_emit(SArgs s, Integrals I, const uint64_t* __restrict__ galpha, const uint64_t* __restrict__ ubeta,
-                  long long tbits, const double* __restrict__ diag_raw, int32_t* __restrict__ colind,
-                  double* __restrict__ val, float* __restrict__ hi, float* __restrict__ lo,
-                  double* __restrict__ diag, int64_t* __restrict__ kept) {
-  const int lane = threadIdx.x & 31;
-  const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  const int64_t n = s.G * s.Nb;
-  for (int64_t r = w0; r < n; r += nw) {
-    const int64_t g = r / s.Nb, b = r - g * s.Nb;
-    const uint64_t ra = galpha[g], rb = ubeta[b];
-    const int64_t base = r * s.rowlen;
-    int cnt = 0;
-    for_each_struct(s, g, b, lane, [&](int64_t pos, int64_t col) {
+__global__ void __launch_bounds__(kEmitThreads)
+    k_slab_emit(SlabArgs A, Integrals I, const uint64_t* __restrict__ galpha, const uint64_t* __restrict__ ubeta,
+                long long tbits, const double* __restrict__ diag_raw, double* __restrict__ val,
+                float* __restrict__ hi, float* __restrict__ lo, double* __restrict__ diag,
+                unsigned long long* __restrict__ kept) {
+  const int g = blockIdx.x / kEmitSegments, s = blockIdx.x - g * kEmitSegments;
+  const int p0 = s * A.seglen, p1 = min(A.rowlen, p0 + A.seglen);
+  const int Nb = A.Nb;
+  const uint64_t ra = galpha[g];
+  const int b = blockIdx.y * blockDim.x + threadIdx.x;  // grid.y tiles the beta strings
+  if (b < Nb) {
+    const int64_t r = (int64_t)g * Nb + b;
+    const uint64_t rb = ubeta[b];
+    unsigned cnt = 0;
+    for (int p = p0; p < p1; ++p) {
+      const uint32_t d = __ldg(A.gdesc + (int64_t)g * A.rowlen + p);
+      const int h = (int)(d >> 11), k = (int)(d & 2047u);
+      const int bc = k == kListAlphaDouble ? b : __ldg(A.blT + (int64_t)k * Nb + b);
+      const int64_t col = (int64_t)h * Nb + bc;
       double v;
       bool keep;
       if (col == r) {
@@ -201,113 +333,312 @@ __global__ void __launch_bounds__(256)
         keep = above_thresh(v, tbits);
         diag[r] = keep ? v : 0.;
       } else {
-        const int64_t h = col / s.Nb, cb = col - h * s.Nb;
-        const uint64_t ka = galpha[h], kb = ubeta[cb];
+        const uint64_t ka = galpha[h], kb = ubeta[bc];
         v = (col > r) ? offdiag_element(I, ra, rb, ka, kb) : offdiag_element(I, ka, kb, ra, rb);
         keep = above_thresh(v, tbits);
       }
-      const int64_t p = base + pos;
-      colind[p] = keep ? (int32_t)col : -1;
+      if (!keep) v = 0.;
+      cnt += keep;
+      const int64_t q = ((int64_t)g * A.rowlen + p) * Nb + b;
       if (STORAGE == QDKGB_H_FP64) {
-        val[p] = v;
+        val[q] = v;
       } else {
         const float h32 = __double2float_rn(v);
-        hi[p] = h32;
-        lo[p] = __double2float_rn(v - (double)h32);
+        hi[q] = h32;
+        lo[q] = __double2float_rn(v - (double)h32);
       }
-      cnt += keep;
-    });
-    cnt = warp_sum(cnt);
-    if (lane == 0) kept[r] = cnt;
+    }
+    atomicAdd(kept + r, (unsigned long long)cnt);
   }
 }
 
-// compaction of the marked slots into the final CSR (threshold_parallel's
-// rule, csr_matrix.hpp:317-372): warp per row, ballot packing in order
+// ------------------------------------------------------------------ export
+// Slab -> CSR (rowptr given): a thread per row writes it in column order.
+// Kept rule: every position when thresh <= 0, else the nonzero stored values
+// (a kept element exceeds thresh > 0, a dropped one is stored as zero).
 template <int STORAGE>
-__global__ void k_struct_compact(int64_t n, int64_t rowlen, const int64_t* __restrict__ new_ptr,
-                                 const int32_t* __restrict__ ci, const double* __restrict__ v,
-                                 const float* __restrict__ h, const float* __restrict__ l, int32_t* __restrict__ ci2,
-                                 double* __restrict__ v2, float* __restrict__ h2, float* __restrict__ l2) {
-  const int lane = threadIdx.x & 31;
-  const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t r = w0; r < n; r += nw) {
-    const int64_t src = r * rowlen;
-    int64_t dst = new_ptr[r];
-    for (int64_t k0 = 0; k0 < rowlen; k0 += 32) {
-      const int64_t k = k0 + lane;
-      const bool keep = k < rowlen && ci[src + k] >= 0;
-      const unsigned m = __ballot_sync(QDKGB_FULL_MASK, keep);
-      if (keep) {
-        const int64_t p = dst + __popc(m & ((1u << lane) - 1u));
-        ci2[p] = ci[src + k];
-        if (STORAGE == QDKGB_H_FP64) {
-          v2[p] = v[src + k];
-        } else {
-          h2[p] = h[src + k];
-          l2[p] = l[src + k];
-        }
+__global__ void __launch_bounds__(256)
+    k_slab_export(SlabArgs A, bool keep_all, const double* __restrict__ val, const float* __restrict__ hi,
+                  const float* __restrict__ lo, const int64_t* __restrict__ rowptr, int32_t* __restrict__ ci,
+                  double* __restrict__ v64, float* __restrict__ h32, float* __restrict__ l32) {
+  const int64_t n = (int64_t)A.G * A.Nb;
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  const int Nb = A.Nb;
+  const int g = (int)(r / Nb), b = (int)(r - (int64_t)g * Nb);
+  int64_t o = rowptr[r];
+  const int64_t oend = rowptr[r + 1];
+  for (int p = 0; p < A.rowlen && o < oend; ++p) {
+    const uint32_t d = __ldg(A.gdesc + (int64_t)g * A.rowlen + p);
+    const int h = (int)(d >> 11), k = (int)(d & 2047u);
+    const int bc = k == kListAlphaDouble ? b : __ldg(A.blT + (int64_t)k * Nb + b);
+    const int64_t q = ((int64_t)g * A.rowlen + p) * Nb + b;
+    if (STORAGE == QDKGB_H_FP64) {
+      const double v = val[q];
+      if (keep_all || v != 0.) {
+        ci[o] = (int32_t)((int64_t)h * Nb + bc);
+        v64[o] = v;
+        ++o;
       }
-      dst += __popc(m);
+    } else {
+      const float vh = hi[q], vl = lo[q];
+      if (keep_all || vh != 0.f || vl != 0.f) {
+        ci[o] = (int32_t)((int64_t)h * Nb + bc);
+        if (v64) {
+          v64[o] = (double)vh + (double)vl;
+        } else {
+          h32[o] = vh;
+          l32[o] = vl;
+        }
+        ++o;
+      }
     }
   }
 }
 
-template <typename Acc, typename X, typename Val>
-__global__ void __launch_bounds__(256)
-    k_struct_spmv(SArgs s, Val val, const X* __restrict__ x, X* __restrict__ y) {
-  const int lane = threadIdx.x & 31;
-  const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  const int64_t n = s.G * s.Nb;
-  for (int64_t r = w0; r < n; r += nw) {
-    const int64_t g = r / s.Nb, b = r - g * s.Nb;
-    const int64_t base = r * s.rowlen;
-    Acc acc = 0;
-    for_each_struct(s, g, b, lane, [&](int64_t pos, int64_t col) { acc += val(base + pos) * (Acc)__ldg(x + col); });
-    acc = warp_sum(acc);
-    if (lane == 0) y[r] = (X)acc;
+// ------------------------------------------------------------------ sigma
+// CTA per (group g, segment s), a thread per beta string b (row g * Nb + b).
+// The x slices of the segment's staged blocks are copied to shared memory;
+// the own-group block runs over b's level-2 list, the alpha-single blocks
+// share b's level-1 list (each list entry is loaded once and used for every
+// block of the segment), the alpha doubles read x[h * Nb + b] (coalesced).
+//   MODE 0: FP32 values, FP32 x, FP32 accumulation
+//   MODE 1: FP64 values, FP64 x, FP64 accumulation
+//   MODE 2: split values (hi, lo) with split x (xh, xl), float-float sums
+template <int MODE>
+struct SlabPol;
+template <>
+struct SlabPol<0> {
+  using Xs = float;
+  using Acc = float;
+  using Out = float;
+  struct Val {
+    float h;
+  };
+  static __device__ __forceinline__ Val load(const void* v, const float*, int64_t q) {
+    return {__ldcs((const float*)v + q)};
+  }
+  static __device__ __forceinline__ Xs gx(const void* x, const float*, int64_t i) { return __ldg((const float*)x + i); }
+  static __device__ __forceinline__ void add(Acc& a, Val v, Xs x) { a = fmaf(v.h, x, a); }
+  static __device__ __forceinline__ Acc zero() { return 0.f; }
+  static __device__ __forceinline__ Acc merge(Acc a, Acc b) { return a + b; }
+  static __device__ __forceinline__ Out fin(Acc a) { return a; }
+};
+template <>
+struct SlabPol<1> {
+  using Xs = double;
+  using Acc = double;
+  using Out = double;
+  struct Val {
+    double h;
+  };
+  static __device__ __forceinline__ Val load(const void* v, const float*, int64_t q) {
+    return {__ldcs((const double*)v + q)};
+  }
+  static __device__ __forceinline__ Xs gx(const void* x, const float*, int64_t i) {
+    return __ldg((const double*)x + i);
+  }
+  static __device__ __forceinline__ void add(Acc& a, Val v, Xs x) { a = fma(v.h, x, a); }
+  static __device__ __forceinline__ Acc zero() { return 0.; }
+  static __device__ __forceinline__ Acc merge(Acc a, Acc b) { return a + b; }
+  static __device__ __forceinline__ Out fin(Acc a) { return a; }
+};
+template <>
+struct SlabPol<2> {
+  using Xs = float2;
+  using Acc = FF;
+  using Out = double;
+  struct Val {
+    float h, l;
+  };
+  static __device__ __forceinline__ Val load(const void* v, const float* vlo, int64_t q) {
+    return {__ldcs((const float*)v + q), __ldcs(vlo + q)};
+  }
+  static __device__ __forceinline__ Xs gx(const void* x, const float* xlo, int64_t i) {
+    return make_float2(__ldg((const float*)x + i), __ldg(xlo + i));
+  }
+  static __device__ __forceinline__ void add(Acc& a, Val v, Xs x) {
+    float p, e;
+    ff_prod(v.h, v.l, x.x, x.y, p, e);
+    ff_add(a, p, e);
+  }
+  static __device__ __forceinline__ Acc zero() { return FF{0.f, 0.f}; }
+  static __device__ __forceinline__ Acc merge(Acc a, Acc b) { return ff_merge(a, b); }
+  static __device__ __forceinline__ Out fin(Acc a) { return (double)a.s + (double)a.c; }
+};
+
+template <int MODE>
+__global__ void __launch_bounds__(kSlabThreads, 1)
+    k_slab_sigma(SlabArgs A, PlanArgs P, const void* __restrict__ vals, const float* __restrict__ vlo,
+                 const void* __restrict__ xv, const float* __restrict__ xlo, void* __restrict__ yv,
+                 int64_t part_stride) {
+  using Pol = SlabPol<MODE>;
+  using Xs = typename Pol::Xs;
+  using Acc = typename Pol::Acc;
+  using Val = typename Pol::Val;
+  constexpr int U = MODE == 2 ? kSlabUnroll / 2 : kSlabUnroll;  // loads in flight per thread
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int Nb = A.Nb;
+  const int g = blockIdx.x / P.S, s = blockIdx.x - g * P.S;
+  Xs* xs = reinterpret_cast<Xs*>(smem_raw);
+  int32_t* rec = reinterpret_cast<int32_t*>(xs + (size_t)P.M * Nb);
+  const int32_t* rg = P.rec + ((int64_t)g * P.S + s) * P.R;
+  for (int i = threadIdx.x; i < P.R; i += blockDim.x) rec[i] = __ldg(rg + i);
+  const int32_t* sh = P.segh + ((int64_t)g * P.S + s) * P.M;
+  for (int j = 0; j < P.M; ++j) {
+    const int h = __ldg(sh + j);
+    if (h < 0) continue;
+    for (int i = threadIdx.x; i < Nb; i += blockDim.x) xs[(size_t)j * Nb + i] = Pol::gx(xv, xlo, (int64_t)h * Nb + i);
+  }
+  __syncthreads();
+  const int has0 = rec[0], off0 = rec[1], sb0 = rec[2], n1b = rec[3];
+  const int32_t* e1 = rec + 4;
+  const int nd = rec[4 + 2 * n1b];
+  const int32_t* e2 = rec + 6 + 2 * n1b;
+  for (int b = threadIdx.x; b < Nb; b += blockDim.x) {
+    const int64_t gbase = (int64_t)g * A.rowlen * Nb + b;  // slab index of (g, p = 0, b)
+    const int32_t* lst = A.blT + b;
+    Acc acc[U];
+#pragma unroll
+    for (int j = 0; j < U; ++j) acc[j] = Pol::zero();
+    // own-group block over b's level-2 list
+    if (has0) {
+      int k = 0;
+      for (; k + U <= A.n2; k += U) {
+        Val v[U];
+        int l[U];
+#pragma unroll
+        for (int j = 0; j < U; ++j) {
+          l[j] = __ldg(lst + (k + j) * Nb);
+          v[j] = Pol::load(vals, vlo, gbase + off0 + (k + j) * Nb);
+        }
+#pragma unroll
+        for (int j = 0; j < U; ++j) Pol::add(acc[j], v[j], xs[sb0 + l[j]]);
+      }
+      for (; k < A.n2; ++k)
+        Pol::add(acc[0], Pol::load(vals, vlo, gbase + off0 + k * Nb), xs[sb0 + __ldg(lst + k * Nb)]);
+    }
+    // alpha-single blocks: each entry of b's level-1 list is loaded once and
+    // used for every block of the segment
+    for (int k = 0; k < A.n1; ++k) {
+      const int l = __ldg(lst + (A.n2 + k) * Nb);
+      const int kk = k * Nb;
+      int e = 0;
+      for (; e + U <= n1b; e += U) {
+        Val v[U];
+#pragma unroll
+        for (int j = 0; j < U; ++j) v[j] = Pol::load(vals, vlo, gbase + e1[2 * (e + j)] + kk);
+#pragma unroll
+        for (int j = 0; j < U; ++j) Pol::add(acc[j], v[j], xs[e1[2 * (e + j) + 1] + l]);
+      }
+      for (; e < n1b; ++e) Pol::add(acc[0], Pol::load(vals, vlo, gbase + e1[2 * e] + kk), xs[e1[2 * e + 1] + l]);
+    }
+    // alpha doubles: x of the same beta string in group h
+    {
+      int j0 = 0;
+      for (; j0 + U <= nd; j0 += U) {
+        Val v[U];
+        Xs xx[U];
+#pragma unroll
+        for (int j = 0; j < U; ++j) {
+          v[j] = Pol::load(vals, vlo, gbase + e2[2 * (j0 + j)]);
+          xx[j] = Pol::gx(xv, xlo, (int64_t)e2[2 * (j0 + j) + 1] + b);
+        }
+#pragma unroll
+        for (int j = 0; j < U; ++j) Pol::add(acc[j], v[j], xx[j]);
+      }
+      for (; j0 < nd; ++j0)
+        Pol::add(acc[0], Pol::load(vals, vlo, gbase + e2[2 * j0]), Pol::gx(xv, xlo, (int64_t)e2[2 * j0 + 1] + b));
+    }
+#pragma unroll
+    for (int j = 1; j < U; ++j) acc[0] = Pol::merge(acc[0], acc[j]);
+    ((typename Pol::Out*)yv)[s * part_stride + (int64_t)g * Nb + b] = Pol::fin(acc[0]);
   }
 }
 
-struct SValF64 {
-  const double* v;
-  __device__ __forceinline__ double operator()(int64_t k) const { return __ldcs(v + k); }
-};
-struct SValF32 {
-  const float* v;
-  __device__ __forceinline__ float operator()(int64_t k) const { return __ldcs(v + k); }
-};
+template <typename T>
+__global__ void k_slab_combine(int64_t n, int S, const T* __restrict__ part, T* __restrict__ y) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    T a = part[i];
+    for (int s = 1; s < S; ++s) a += part[s * n + i];
+    y[i] = a;
+  }
+}
+
+template <int MODE>
+void slab_sigma(Context* c, const void* vals, const float* vlo, const void* x, const float* xlo, void* y) {
+  FciStruct* F = c->fci;
+  SlabPlan& PL = F->plan[MODE == 0 ? 0 : 1];
+  PlanArgs P{PL.S, PL.M, PL.R, (const int32_t*)PL.rec.ptr, (const int32_t*)PL.segh.ptr};
+  using Pol = SlabPol<MODE>;
+  using Out = typename Pol::Out;
+  const size_t smem = (size_t)PL.M * F->Nb * sizeof(typename Pol::Xs) + ((size_t)PL.R * 4 + 15) / 16 * 16;
+  static thread_local int configured_dev = -1;
+  if (configured_dev != c->device) {
+    QDKGB_CUDA(cudaFuncSetAttribute(k_slab_sigma<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)kSlabSmemMax));
+    configured_dev = c->device;
+  }
+  const int64_t n = F->G * F->Nb;
+  void* out = y;
+  if (PL.S > 1) out = dev_alloc(c, F->ypart, (size_t)PL.S * n * sizeof(Out));
+  k_slab_sigma<MODE><<<(unsigned)(F->G * PL.S), slab_threads((int)F->Nb), smem, c->stream>>>(
+      slab_args(c), P, vals, vlo, x, xlo, out, n);
+  QDKGB_CHECK_LAUNCH();
+  if (PL.S > 1) {
+    const unsigned cb = (unsigned)std::min<int64_t>((n + 255) / 256, (int64_t)c->sm_count * 8);
+    k_slab_combine<Out><<<cb, 256, 0, c->stream>>>(n, PL.S, (const Out*)out, (Out*)y);
+    QDKGB_CHECK_LAUNCH();
+  }
+}
 
 }  // namespace
 
 bool struct_ready(Context* c) { return c->fci && c->H.valid && !c->op_direct && c->H.structured; }
 
-unsigned struct_blocks(Context* c, int64_t n) {
-  return (unsigned)std::min<int64_t>((n + 7) / 8, (int64_t)c->sm_count * 32);
-}
-
 void struct_spmv_fp64(Context* c, const double* x, double* y) {
-  SArgs s = sargs(c);
-  k_struct_spmv<double, double><<<struct_blocks(c, c->H.n), 256, 0, c->stream>>>(
-      s, SValF64{(const double*)c->H.val.ptr}, x, y);
-  QDKGB_CHECK_LAUNCH();
+  Hcsr& H = c->H;
+  if (H.storage == QDKGB_H_FP64) {
+    slab_sigma<1>(c, H.val.ptr, nullptr, x, nullptr, y);
+  } else {
+    float* xs = split_x(c, x);
+    slab_sigma<2>(c, H.hi.ptr, (const float*)H.lo.ptr, xs, xs + H.n, y);
+  }
 }
+
 void struct_spmv_fp32(Context* c, const float* x, float* y) {
-  SArgs s = sargs(c);
-  k_struct_spmv<float, float><<<struct_blocks(c, c->H.n), 256, 0, c->stream>>>(
-      s, SValF32{(const float*)c->H.hi.ptr}, x, y);
+  Hcsr& H = c->H;
+  if (H.storage != QDKGB_H_SPLIT32)
+    throw Error(QDKGB_ERR_STATE, "FP32 sigma needs the Hamiltonian built with QDKGB_H_SPLIT32 storage");
+  slab_sigma<0>(c, H.hi.ptr, nullptr, x, nullptr, y);
+}
+
+// CSR arrays of a slab Hamiltonian into device buffers of nnz entries: the
+// columns, and the values as FP64 (v64) or as the split pair (h32, l32).
+void struct_export(Context* c, int32_t* ci, double* v64, float* h32, float* l32) {
+  Hcsr& H = c->H;
+  SlabArgs A = slab_args(c);
+  const unsigned nb = (unsigned)((H.n + 255) / 256);
+  const bool keep_all = !(H.thresh > 0.);
+  if (H.storage == QDKGB_H_FP64)
+    k_slab_export<QDKGB_H_FP64><<<nb, 256, 0, c->stream>>>(A, keep_all, (const double*)H.val.ptr, nullptr, nullptr,
+                                                           (const int64_t*)H.rowptr.ptr, ci, v64, h32, l32);
+  else
+    k_slab_export<QDKGB_H_SPLIT32><<<nb, 256, 0, c->stream>>>(A, keep_all, nullptr, (const float*)H.hi.ptr,
+                                                              (const float*)H.lo.ptr, (const int64_t*)H.rowptr.ptr,
+                                                              ci, v64, h32, l32);
   QDKGB_CHECK_LAUNCH();
 }
 
-// Structured build for complete spaces (build_hamiltonian dispatches here).
+// Slab build for complete spaces (build_hamiltonian dispatches here).  When
+// fewer than half of the elements survive the threshold the slab is turned
+// into the reference's CSR arrays and freed.
 void build_hamiltonian_struct(Context* c, double thresh, int storage) {
   Hcsr& H = c->H;
   DetSpace& D = c->dets;
   FciStruct* F = c->fci;
   const int64_t n = D.ndets;
-  const int64_t nnz_pre = n * F->rowlen;
+  const int64_t nslab = n * F->rowlen;
   long long tbits = -1;
   if (thresh > 0.) std::memcpy(&tbits, &thresh, sizeof(double));
   Integrals I = integrals_view(c);
@@ -316,66 +647,63 @@ void build_hamiltonian_struct(Context* c, double thresh, int storage) {
   int64_t* kept = dev_array<int64_t>(c, H.row_nnz, n + 1);
   const unsigned tb = (unsigned)std::min<int64_t>((n + 255) / 256, (int64_t)c->sm_count * 16);
   k_diag_launch(c, I, diag_raw, tb);
+  dev_free(c, H.colind);
   if (storage == QDKGB_H_FP64) {
     dev_free(c, H.hi);
     dev_free(c, H.lo);
   } else {
     dev_free(c, H.val);
   }
-  int32_t* colind = dev_array<int32_t>(c, H.colind, nnz_pre);
-  double* val = storage == QDKGB_H_FP64 ? dev_array<double>(c, H.val, nnz_pre) : nullptr;
-  float* hi = storage == QDKGB_H_SPLIT32 ? dev_array<float>(c, H.hi, nnz_pre) : nullptr;
-  float* lo = storage == QDKGB_H_SPLIT32 ? dev_array<float>(c, H.lo, nnz_pre) : nullptr;
+  double* val = storage == QDKGB_H_FP64 ? dev_array<double>(c, H.val, nslab) : nullptr;
+  float* hi = storage == QDKGB_H_SPLIT32 ? dev_array<float>(c, H.hi, nslab) : nullptr;
+  float* lo = storage == QDKGB_H_SPLIT32 ? dev_array<float>(c, H.lo, nslab) : nullptr;
   QDKGB_CUDA(cudaMemsetAsync(diag, 0, n * sizeof(double), c->stream));
-  SArgs s = sargs(c);
-  const unsigned eb = struct_blocks(c, n);
+  QDKGB_CUDA(cudaMemsetAsync(kept, 0, (n + 1) * sizeof(int64_t), c->stream));
+  SlabArgs A = slab_args(c);
+  const dim3 grid((unsigned)(F->G * kEmitSegments), (unsigned)((F->Nb + kEmitThreads - 1) / kEmitThreads));
+  const unsigned thr = kEmitThreads;
   const uint64_t* ga = (const uint64_t*)D.galpha.ptr;
   const uint64_t* ub = (const uint64_t*)D.ubeta.ptr;
+  unsigned long long* kc = (unsigned long long*)kept;
   if (storage == QDKGB_H_FP64)
-    k_struct_emit<QDKGB_H_FP64><<<eb, 256, 0, c->stream>>>(s, I, ga, ub, tbits, diag_raw, colind, val, hi, lo, diag,
-                                                            kept);
+    k_slab_emit<QDKGB_H_FP64><<<grid, thr, 0, c->stream>>>(A, I, ga, ub, tbits, diag_raw, val, hi, lo, diag, kc);
   else
-    k_struct_emit<QDKGB_H_SPLIT32><<<eb, 256, 0, c->stream>>>(s, I, ga, ub, tbits, diag_raw, colind, val, hi, lo,
-                                                               diag, kept);
+    k_slab_emit<QDKGB_H_SPLIT32><<<grid, thr, 0, c->stream>>>(A, I, ga, ub, tbits, diag_raw, val, hi, lo, diag, kc);
   QDKGB_CHECK_LAUNCH();
   int64_t* rowptr = dev_array<int64_t>(c, H.rowptr, n + 1);
   exclusive_scan_i64(c, kept, rowptr, n, H.scan_tmp);
   int64_t nnz = 0;
   QDKGB_CUDA(cudaMemcpyAsync(&nnz, rowptr + n, sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
   QDKGB_CUDA(cudaStreamSynchronize(c->stream));
-  H.structured = (nnz == nnz_pre);
-  if (!H.structured) {
-    DeviceBuffer ci2b, v2b, h2b, l2b;
-    const int64_t cap2 = std::max<int64_t>(nnz, 1);
-    int32_t* ci2 = dev_array<int32_t>(c, ci2b, cap2);
-    double* v2 = storage == QDKGB_H_FP64 ? dev_array<double>(c, v2b, cap2) : nullptr;
-    float* h2 = storage == QDKGB_H_SPLIT32 ? dev_array<float>(c, h2b, cap2) : nullptr;
-    float* l2 = storage == QDKGB_H_SPLIT32 ? dev_array<float>(c, l2b, cap2) : nullptr;
-    if (storage == QDKGB_H_FP64)
-      k_struct_compact<QDKGB_H_FP64>
-          <<<eb, 256, 0, c->stream>>>(n, F->rowlen, rowptr, colind, val, hi, lo, ci2, v2, h2, l2);
-    else
-      k_struct_compact<QDKGB_H_SPLIT32>
-          <<<eb, 256, 0, c->stream>>>(n, F->rowlen, rowptr, colind, val, hi, lo, ci2, v2, h2, l2);
-    QDKGB_CHECK_LAUNCH();
-    QDKGB_CUDA(cudaStreamSynchronize(c->stream));
-    std::swap(H.colind, ci2b);
-    dev_free(c, ci2b);
-    if (storage == QDKGB_H_FP64) {
-      std::swap(H.val, v2b);
-      dev_free(c, v2b);
-    } else {
-      std::swap(H.hi, h2b);
-      std::swap(H.lo, l2b);
-      dev_free(c, h2b);
-      dev_free(c, l2b);
-    }
-  }
   H.n = n;
   H.nnz = nnz;
   H.storage = storage;
   H.thresh = thresh;
+  H.structured = true;
   H.valid = true;
+  if (2 * nnz < nslab) {
+    // mostly thresholded away: the CSR arrays are smaller than the slab
+    DeviceBuffer cib, vb, hb, lb;
+    const int64_t cap = std::max<int64_t>(nnz, 1);
+    int32_t* ci = dev_array<int32_t>(c, cib, cap);
+    double* v64 = storage == QDKGB_H_FP64 ? dev_array<double>(c, vb, cap) : nullptr;
+    float* h32 = storage == QDKGB_H_SPLIT32 ? dev_array<float>(c, hb, cap) : nullptr;
+    float* l32 = storage == QDKGB_H_SPLIT32 ? dev_array<float>(c, lb, cap) : nullptr;
+    struct_export(c, ci, v64, h32, l32);
+    QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+    std::swap(H.colind, cib);
+    dev_free(c, cib);
+    if (storage == QDKGB_H_FP64) {
+      std::swap(H.val, vb);
+      dev_free(c, vb);
+    } else {
+      std::swap(H.hi, hb);
+      std::swap(H.lo, lb);
+      dev_free(c, hb);
+      dev_free(c, lb);
+    }
+    H.structured = false;
+  }
 }
 
 }  // namespace qdkgb

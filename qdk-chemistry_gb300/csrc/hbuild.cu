@@ -617,7 +617,9 @@ void build_hamiltonian(Context* c, double thresh, int storage) {
   H.valid = false;
   H.structured = false;
   c->op_direct = false;
-  if (c->fci) {
+  // slab layout for complete spaces; its kept rule (nonzero stored value)
+  // needs every kept element to stay nonzero in the split pair
+  if (c->fci && (!(thresh > 0.) || thresh >= 1e-30)) {
     build_hamiltonian_struct(c, thresh, storage);
     return;
   }

@@ -80,7 +80,7 @@ struct Hcsr {
   double thresh = 0.;
   DeviceBuffer rowptr, colind, val, hi, lo, diag, diag_raw, row_nnz, scan_tmp, xsplit;
   bool valid = false;
-  bool structured = false;  // complete space, nothing thresholded: columns implied by the row tables
+  bool structured = false;  // complete space in the slab layout (values only, columns implied by the row tables)
 };
 
 struct DavidsonWork {
@@ -132,6 +132,8 @@ void free_struct(Context* c);
 bool struct_ready(Context* c);
 void struct_spmv_fp64(Context* c, const double* x, double* y);
 void struct_spmv_fp32(Context* c, const float* x, float* y);
+void struct_export(Context* c, int32_t* ci, double* v64, float* h32, float* l32);
+float* split_x(Context* c, const double* x);
 void build_hamiltonian_struct(Context* c, double thresh, int storage);
 void k_diag_launch(Context* c, const Integrals& I, double* D, unsigned blocks);
 

@@ -61,21 +61,6 @@ __global__ void __launch_bounds__(kSpmvWarps * 32)
 // the cross terms, and the row sum is kept as an unevaluated float-float pair
 // (two-sum).  Relative accuracy ~2^-44 per product, far below what the
 // defect correction needs; the row result is rounded to FP64 once.
-struct FF {
-  float s, c;
-};
-__device__ __forceinline__ void ff_add(FF& a, float p, float e) {
-  const float t = a.s + p;
-  const float bv = t - a.s;
-  const float err = (a.s - (t - bv)) + (p - bv);
-  a.s = t;
-  a.c += err + e;
-}
-__device__ __forceinline__ FF ff_merge(FF a, FF b) {
-  FF r = a;
-  ff_add(r, b.s, b.c);
-  return r;
-}
 __global__ void __launch_bounds__(kSpmvWarps * 32)
     k_spmv_split_ff(int64_t n, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
                     const float* __restrict__ hi, const float* __restrict__ lo, const float* __restrict__ xh,
@@ -129,6 +114,15 @@ __global__ void k_split_x(const double* __restrict__ x, float* __restrict__ xh, 
   }
 }
 
+// x -> (xh, xl) float pair in the context's scratch, xh at [0, n), xl at [n, 2n)
+float* split_x(Context* c, const double* x) {
+  const int64_t n = c->H.n;
+  float* xs = dev_array<float>(c, c->H.xsplit, 2 * (size_t)n);
+  k_split_x<<<c->sm_count * 4, 256, 0, c->stream>>>(x, xs, xs + n, n);
+  QDKGB_CHECK_LAUNCH();
+  return xs;
+}
+
 static unsigned spmv_blocks(Context* c, int64_t n) {
   const int64_t want = (n + kSpmvWarps - 1) / kSpmvWarps;
   return (unsigned)std::min<int64_t>(want, (int64_t)c->sm_count * 32);
@@ -141,7 +135,7 @@ void spmv_fp64(Context* c, const double* x, double* y) {
     direct_sigma_fp64(c, x, y);
     return;
   }
-  if (struct_ready(c) && H.storage == QDKGB_H_FP64) {
+  if (struct_ready(c)) {
     struct_spmv_fp64(c, x, y);
     return;
   }
@@ -151,9 +145,7 @@ void spmv_fp64(Context* c, const double* x, double* y) {
     k_spmv_csr<double, double><<<spmv_blocks(c, H.n), kSpmvWarps * 32, 0, c->stream>>>(
         H.n, rp, ci, ValF64{(const double*)H.val.ptr}, x, y);
   else {
-    float* xs = dev_array<float>(c, H.xsplit, 2 * (size_t)H.n);
-    k_split_x<<<c->sm_count * 4, 256, 0, c->stream>>>(x, xs, xs + H.n, H.n);
-    QDKGB_CHECK_LAUNCH();
+    float* xs = split_x(c, x);
     k_spmv_split_ff<<<spmv_blocks(c, H.n), kSpmvWarps * 32, 0, c->stream>>>(
         H.n, rp, ci, (const float*)H.hi.ptr, (const float*)H.lo.ptr, xs, xs + H.n, y);
   }
