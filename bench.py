@@ -5,12 +5,13 @@ Workload: 853,776 determinants (n_alpha = n_beta = 6 in 12 orbitals), seeded
 synthetic integrals (h1 = diag(-2 + 0.25 p) + N(0, 0.05^2) off-diagonal,
 V = sum over 24 symmetric Cholesky vectors with N(0, 0.1^2) entries).
 One step = the hot path from integrals and determinants resident in HBM to
-the ground-state energy: CSR Hamiltonian build (1.55e9 nonzeros) + Davidson
-to a full-precision residual norm of 1e-8, in the mixed-precision form (FP32
+the ground-state energy: Hamiltonian build (1.55e9 matrix elements; a
+complete space is stored in the slab layout, values only) + Davidson to a
+full-precision residual norm of 1e-8, in the mixed-precision form (FP32
 sigma, FP64 subspace / refinement).  The plain FP64 path is timed beside it.
 
-The CSR (12-19 GB) is far larger than L2 (129 MB), so no L2 flush is needed
-between steps.
+The stored matrix (6.2 GB FP32 + 6.2 GB low parts, or 12.4 GB FP64) is far
+larger than L2 (129 MB), so no L2 flush is needed between steps.
 
   python bench.py [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -230,6 +231,7 @@ def run_ours(args):
     # plain FP64 path (the reference's precision) for the comparison
     E64, info64, hb64, dv64 = step(capi.H_FP64, capi.PREC_FP64)
     nnz = ctx.nnz
+    lay64, stored64 = ctx.operator_layout()
     # FP64 SpMV roofline (FP64 values + int32 columns)
     x64 = torch.randn(N, dtype=torch.float64, device="cuda")
     y64 = torch.empty_like(x64)
@@ -266,15 +268,30 @@ def run_ours(args):
     x32 = torch.randn(N, dtype=torch.float32, device="cuda")
     y32 = torch.empty_like(x32)
     t_spmv32 = time_spmv(ctx, capi.PREC_MIXED, x32, y32, stream)
+    lay32, stored32 = ctx.operator_layout()
     peak, peak_kind = _peaks()
-    bytes32 = nnz * 8 + (N + 1) * 8 + N * 4 + N * 4
-    bytes64 = nnz * 12 + (N + 1) * 8 + N * 8 + N * 8
+    # algorithmic bytes of one sigma: the stored values once, x once (L2
+    # resident), y once; the CSR layout adds int32 columns and int64 rowptr
+    if lay32 == capi.OP_SLAB:
+        bytes32 = stored32 * 4 + N * 4 + N * 4
+        kern32 = "k_slab_sigma<0> (FP32 sigma, slab layout: values only)"
+    else:
+        bytes32 = nnz * 8 + (N + 1) * 8 + N * 4 + N * 4
+        kern32 = "k_spmv_csr<float> (FP32 sigma, CSR)"
+    if lay64 == capi.OP_SLAB:
+        bytes64 = stored64 * 8 + N * 8 + N * 8
+        kern64 = "k_slab_sigma<1> (FP64 sigma, slab layout; FP64-pipe bound)"
+    else:
+        bytes64 = nnz * 12 + (N + 1) * 8 + N * 8 + N * 8
+        kern64 = "k_spmv_csr<double> (FP64 sigma, CSR)"
     achieved32 = bytes32 / t_spmv32 / 1e9
     achieved64 = bytes64 / t_spmv64 / 1e9
     traffic = None
     tp = os.path.join(ROOT, "profiles", "spmv_traffic.json")
-    if os.path.exists(tp):
-        traffic = json.load(open(tp)).get("spmv_fp32_dram_bytes_per_launch")
+    if os.path.exists(tp) and lay32 == capi.OP_SLAB:
+        per_el = json.load(open(tp)).get("slab_fp32_dram_bytes_per_element")
+        if per_el:
+            traffic = int(round(per_el * stored32))
 
     # end to end through the C ABI with host buffers: integrals in, energy and
     # CI vector out (host->device copies of T, V and the determinant list inside)
@@ -302,13 +319,13 @@ def run_ours(args):
         "vs_baseline": None, "dtype": "f32 sigma / f64 subspace+refinement", "data": "synthetic",
         "config": {"workload": WORKLOAD, "norb": NORB, "nalpha": NEL // 2, "nbeta": NEL // 2, "ndets": N,
                    "nnz": nnz, "n_chol": NCHOL, "seed": SEED, "res_tol": RES_TOL, "precision": "mixed",
-                   "l2": "inputs larger than L2 (CSR %.1f GB), no flush" % (nnz * 12 / 1e9),
+                   "l2": "inputs larger than L2 (stored H %.1f GB), no flush" % (stored32 * 8 / 1e9),
                    "parallelism": "replicas" if world > 1 else "single GPU"},
-        "roofline": {"bound": "hbm", "kernel": "k_spmv_csr<float> (FP32 sigma)", "achieved": achieved32,
+        "roofline": {"bound": "hbm", "kernel": kern32, "achieved": achieved32,
                      "peak": peak, "unit": "GB/s", "frac": achieved32 / peak, "peak_source": peak_kind,
                      "traffic": traffic, "algorithmic_bytes": bytes32, "launch_ms": t_spmv32 * 1e3},
-        "spmv_fp64": {"achieved_gbs": achieved64, "frac": achieved64 / peak, "launch_ms": t_spmv64 * 1e3,
-                      "algorithmic_bytes": bytes64},
+        "spmv_fp64": {"kernel": kern64, "achieved_gbs": achieved64, "frac": achieved64 / peak,
+                      "launch_ms": t_spmv64 * 1e3, "algorithmic_bytes": bytes64},
         "hbuild_s": float(np.mean(hbs)), "davidson_s": float(np.mean(dvs)),
         "davidson": {k: infos[-1][k] for k in ("iterations", "spmv_fp64", "spmv_fp32", "restarts", "residual_norm")},
         "fp64_path": {"time_to_energy_s": float(np.mean(fp64_times)), "hbuild_s": hb64, "davidson_s": dv64,

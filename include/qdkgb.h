@@ -64,6 +64,21 @@ int qdkgb_set_stream(qdkgb_context* ctx, void* stream);
 /* Bytes of device memory currently held by the context. */
 int qdkgb_device_bytes(const qdkgb_context* ctx, int64_t* bytes);
 
+/* Storage of the operator the last build produced (no counterpart in the
+ * reference, whose operator is always a sparsexx::csr_matrix):
+ *   QDKGB_LAYOUT_CSR     the reference's CSR arrays (rowptr, colind, values);
+ *   QDKGB_LAYOUT_SLAB    complete (CAS) space: values only, stored
+ *                        group-major with beta strings fastest, columns
+ *                        implied by the space; qdkgb_get_csr* exports CSR;
+ *   QDKGB_LAYOUT_DIRECT  no stored matrix (qdkgb_build_direct_sigma).
+ * stored_elements = matrix elements held on the device (slab: every
+ * position, zeros for thresholded elements); NULL to skip. */
+#define QDKGB_LAYOUT_NONE 0
+#define QDKGB_LAYOUT_CSR 1
+#define QDKGB_LAYOUT_SLAB 2
+#define QDKGB_LAYOUT_DIRECT 3
+int qdkgb_operator_layout(const qdkgb_context* ctx, int* layout, int64_t* stored_elements);
+
 /* ------------------------------------------------------------ integrals
  * Replaces the HamiltonianGeneratorBase constructor and
  * generate_integral_intermediates_ (external/macis/src/macis/

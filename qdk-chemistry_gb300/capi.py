@@ -28,9 +28,11 @@ H_FP64 = 0
 H_SPLIT32 = 1
 PREC_FP64 = 0
 PREC_MIXED = 1
+OP_NONE, OP_CSR, OP_SLAB, OP_DIRECT = 0, 1, 2, 3
 
 EXPORTED = [
     "qdkgb_create", "qdkgb_destroy", "qdkgb_last_error", "qdkgb_set_stream", "qdkgb_device_bytes",
+    "qdkgb_operator_layout",
     "qdkgb_set_integrals", "qdkgb_fci_dets", "qdkgb_set_dets", "qdkgb_build_hamiltonian", "qdkgb_get_csr32",
     "qdkgb_get_csr64", "qdkgb_diagonal", "qdkgb_spmv", "qdkgb_spmv_device", "qdkgb_davidson_default_settings",
     "qdkgb_davidson", "qdkgb_rdms_spin_dep", "qdkgb_casci", "qdkgb_version", "qdkgb_kernel_launches",
@@ -91,6 +93,7 @@ def lib():
     L.qdkgb_last_error.restype = ctypes.c_char_p
     L.qdkgb_set_stream.argtypes = [vp, vp]
     L.qdkgb_device_bytes.argtypes = [vp, P(i64)]
+    L.qdkgb_operator_layout.argtypes = [vp, P(ctypes.c_int), P(i64)]
     L.qdkgb_set_integrals.argtypes = [vp, ci, vp, vp, ci]
     L.qdkgb_fci_dets.argtypes = [ci, ci, ci, vp, vp, P(i64)]
     L.qdkgb_set_dets.argtypes = [vp, i64, vp, vp]
@@ -219,6 +222,14 @@ class Context:
         b = ctypes.c_int64()
         self._check(lib().qdkgb_device_bytes(self._h, ctypes.byref(b)))
         return b.value
+
+    def operator_layout(self):
+        """(layout, stored elements): OP_CSR, OP_SLAB (complete space, values
+        only) or OP_DIRECT (no stored matrix); OP_NONE before a build."""
+        lay = ctypes.c_int()
+        st = ctypes.c_int64()
+        self._check(lib().qdkgb_operator_layout(self._h, ctypes.byref(lay), ctypes.byref(st)))
+        return lay.value, st.value
 
     def set_stream(self, stream_ptr):
         self._check(lib().qdkgb_set_stream(self._h, stream_ptr))

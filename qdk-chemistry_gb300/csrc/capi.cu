@@ -201,6 +201,25 @@ int qdkgb_device_bytes(const qdkgb_context* c, int64_t* bytes) {
   return QDKGB_OK;
 }
 
+int qdkgb_operator_layout(const qdkgb_context* c, int* layout, int64_t* stored) {
+  if (!c || !layout) return QDKGB_ERR_INVALID;
+  const Hcsr& H = c->H;
+  int64_t st = 0;
+  if (!H.valid) {
+    *layout = QDKGB_LAYOUT_NONE;
+  } else if (c->op_direct) {
+    *layout = QDKGB_LAYOUT_DIRECT;
+  } else if (H.structured) {
+    *layout = QDKGB_LAYOUT_SLAB;
+    st = struct_slab_elements(const_cast<qdkgb_context*>(c));
+  } else {
+    *layout = QDKGB_LAYOUT_CSR;
+    st = H.nnz;
+  }
+  if (stored) *stored = st;
+  return QDKGB_OK;
+}
+
 int qdkgb_set_integrals(qdkgb_context* c, int norb, const double* T, const double* V, int layout) {
   if (!c) return QDKGB_ERR_INVALID;
   return guarded(c, [&] {

@@ -594,6 +594,8 @@ void slab_sigma(Context* c, const void* vals, const float* vlo, const void* x, c
 
 }  // namespace
 
+int64_t struct_slab_elements(Context* c) { return c->fci ? c->fci->G * c->fci->Nb * c->fci->rowlen : 0; }
+
 bool struct_ready(Context* c) { return c->fci && c->H.valid && !c->op_direct && c->H.structured; }
 
 void struct_spmv_fp64(Context* c, const double* x, double* y) {

@@ -133,6 +133,7 @@ bool struct_ready(Context* c);
 void struct_spmv_fp64(Context* c, const double* x, double* y);
 void struct_spmv_fp32(Context* c, const float* x, float* y);
 void struct_export(Context* c, int32_t* ci, double* v64, float* h32, float* l32);
+int64_t struct_slab_elements(Context* c);
 float* split_x(Context* c, const double* x);
 void build_hamiltonian_struct(Context* c, double thresh, int storage);
 void k_diag_launch(Context* c, const Integrals& I, double* D, unsigned blocks);

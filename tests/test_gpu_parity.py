@@ -238,3 +238,37 @@ def test_mixed_precision_stays_in_the_guess_symmetry_sector(ctx, oracle, pkg, ca
     ctx.build_hamiltonian(storage=capi.H_SPLIT32)
     E, C, info = ctx.davidson(tol=1e-8, precision=capi.PREC_MIXED)
     assert abs(E - Eo) < 1e-8, (E, Eo)
+
+
+def test_operator_layouts(ctx, oracle, pkg, capi):
+    """Complete spaces are held in the slab layout (values only) and export
+    the reference's CSR bit-exactly; a threshold that drops most elements
+    turns the slab into CSR; selected spaces and direct sigma report theirs."""
+    T, V, a, b = _cas(pkg, 8, 8, 16, seed=13)
+    ctx.set_integrals(T, V)
+    ctx.set_dets(a, b)
+    ctx.build_hamiltonian(np.finfo(float).eps)
+    lay, stored = ctx.operator_layout()
+    assert lay == capi.OP_SLAB and stored == len(a) * 361 == ctx.nnz
+    # most elements below the threshold: CSR, still identical to the oracle
+    big = float(np.quantile(np.abs(oracle.build_csr(oracle.Hamiltonian(T, V), a, b).arrays()[2]), 0.7))
+    _check_csr(ctx, oracle, T, V, a, b, big)
+    assert ctx.operator_layout()[0] == capi.OP_CSR
+    # a few elements dropped: slab with zeros, CSR export identical
+    small = float(np.quantile(np.abs(oracle.build_csr(oracle.Hamiltonian(T, V), a, b).arrays()[2]), 0.1))
+    _check_csr(ctx, oracle, T, V, a, b, small)
+    assert ctx.operator_layout()[0] == capi.OP_SLAB
+    x = np.random.default_rng(4).normal(size=len(a))
+    M = oracle.build_csr(oracle.Hamiltonian(T, V), a, b, small)
+    yo = M.spmv(x)
+    assert np.max(np.abs(ctx.spmv(x, capi.PREC_FP64) - yo)) <= 1e-12 * np.max(np.abs(yo))
+    # a selected (non-product) space uses CSR
+    rng = np.random.default_rng(1)
+    keep = np.sort(rng.choice(len(a), 1000, replace=False))
+    sa, sb = pkg.determinants.spin_sort(a[keep], b[keep])
+    ctx.set_dets(sa, sb)
+    ctx.build_hamiltonian()
+    assert ctx.operator_layout()[0] == capi.OP_CSR
+    ctx.set_dets(a, b)
+    ctx.build_direct_sigma()
+    assert ctx.operator_layout()[0] == capi.OP_DIRECT
