@@ -230,6 +230,44 @@ int qdkgb_asci(qdkgb_context* ctx, const qdkgb_asci_settings* s, const qdkgb_dav
 int qdkgb_casci(qdkgb_context* ctx, int norb, int nalpha, int nbeta, const double* T, const double* V, int layout,
                 const qdkgb_davidson_settings* s, double matel_tol, double* E, double* C, qdkgb_davidson_info* info);
 
+/* ------------------------------------------------------------ batched CASCI
+ * Many independent complete active spaces in one call.  The reference solves
+ * them one at a time (MultiConfigurationCalculator::run -> cas_helper::impl,
+ * cpp/src/qdk/chemistry/algorithms/microsoft/macis_cas.cpp:35-117, per
+ * instance); here instances of one shape share their determinant space and
+ * every solver step is one launch over all of them (inner iteration replayed
+ * from a CUDA graph).  Energies are electronic (add each core energy);
+ * the spin-summed 1-RDM of instance i (alpha + beta, norb_i x norb_i) lands at
+ * rdm1 + sum_{j<i} norb_j^2 (rdm1 may be NULL).  QDKGB_ERR_NOT_CONVERGED when
+ * an instance did not reach res_tol within max_cycles restarts (its energy is
+ * still written). */
+typedef struct {
+  int norb, nalpha, nbeta;
+  const double* T; /* norb x norb, column-major, host */
+  const double* V; /* norb^4, column-major, host */
+} qdkgb_cas_instance;
+
+typedef struct {
+  double res_tol;             /* full-precision residual norm per instance (1e-8) */
+  int precision;              /* QDKGB_PREC_MIXED (default) or QDKGB_PREC_FP64 */
+  int max_subspace;           /* subspace size of one cycle, 2..64 (24) */
+  int max_cycles;             /* restarts before giving up (200) */
+  double matel_tol;           /* Hamiltonian threshold (machine epsilon) */
+  double min_abs_denominator; /* preconditioner clamp (1e-12) */
+  int use_graph;              /* replay the inner iteration from a CUDA graph (1) */
+  int64_t max_slab_bytes;     /* stored-matrix bytes per sub-batch (96 GiB) */
+} qdkgb_batch_settings;
+
+typedef struct {
+  int iterations;    /* sigma applications, maximum over instances */
+  int graph_replays; /* inner iterations launched from the graph */
+  double seconds;    /* wall time of the call */
+} qdkgb_batch_info;
+
+int qdkgb_batch_default_settings(qdkgb_batch_settings* s);
+int qdkgb_casci_batch(qdkgb_context* ctx, int ninst, const qdkgb_cas_instance* inst, const qdkgb_batch_settings* s,
+                      double* energies, double* rdm1, int* iterations, qdkgb_batch_info* info);
+
 /* ------------------------------------------------------------ allocation-free sigma
  * No counterpart in the reference.  For callers that cannot call cudaMalloc
  * while they run: code being captured into a CUDA graph (allocation is not

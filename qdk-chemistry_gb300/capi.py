@@ -38,6 +38,7 @@ EXPORTED = [
     "qdkgb_davidson", "qdkgb_rdms_spin_dep", "qdkgb_casci", "qdkgb_version", "qdkgb_kernel_launches",
     "qdkgb_sigma_split_noalloc", "qdkgb_set_csr", "qdkgb_build_direct_sigma",
     "qdkgb_asci_default_settings", "qdkgb_asci_search", "qdkgb_asci",
+    "qdkgb_batch_default_settings", "qdkgb_casci_batch",
 ]
 
 
@@ -64,6 +65,25 @@ class AsciSettings(ctypes.Structure):
                 ("growth_recovery_rate", ctypes.c_double), ("max_refine_iter", ctypes.c_int64),
                 ("refine_energy_tol", ctypes.c_double), ("warm_start", ctypes.c_int),
                 ("min_warm_start_overlap", ctypes.c_double)]
+
+
+class CasInstance(ctypes.Structure):
+    _fields_ = [("norb", ctypes.c_int), ("nalpha", ctypes.c_int), ("nbeta", ctypes.c_int),
+                ("T", ctypes.c_void_p), ("V", ctypes.c_void_p)]
+
+
+class BatchSettings(ctypes.Structure):
+    _fields_ = [("res_tol", ctypes.c_double), ("precision", ctypes.c_int), ("max_subspace", ctypes.c_int),
+                ("max_cycles", ctypes.c_int), ("matel_tol", ctypes.c_double),
+                ("min_abs_denominator", ctypes.c_double), ("use_graph", ctypes.c_int),
+                ("max_slab_bytes", ctypes.c_int64)]
+
+
+class BatchInfo(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int), ("graph_replays", ctypes.c_int), ("seconds", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class DavidsonInfo(ctypes.Structure):
@@ -118,6 +138,8 @@ def lib():
     L.qdkgb_version.restype = ctypes.c_char_p
     L.qdkgb_kernel_launches.restype = ctypes.c_int64
     L.qdkgb_sigma_split_noalloc.argtypes = [i64, vp, vp, vp, vp, vp, vp, vp]
+    L.qdkgb_batch_default_settings.argtypes = [P(BatchSettings)]
+    L.qdkgb_casci_batch.argtypes = [vp, ci, P(CasInstance), P(BatchSettings), vp, vp, vp, P(BatchInfo)]
     _lib = L
     return L
 
@@ -395,3 +417,39 @@ def asci(ctx, alpha0, beta0, c0, E0, grow=True, refine=True, tol=1e-8, max_m=200
                                 _ptr(oc), ctypes.byref(n), ctypes.byref(E), ctypes.byref(Eg)))
     m = min(n.value, cap)
     return E.value, oa[:m].copy(), ob[:m].copy(), oc[:m].copy(), Eg.value
+
+
+def default_batch_settings(**kw):
+    s = BatchSettings()
+    lib().qdkgb_batch_default_settings(ctypes.byref(s))
+    for k, v in kw.items():
+        if not hasattr(s, k):
+            raise KeyError(k)
+        setattr(s, k, v)
+    return s
+
+
+def casci_batch(ctx, instances, want_rdm1=True, **settings):
+    """Batched CASCI (qdkgb_casci_batch).  instances: sequence of
+    (norb, nalpha, nbeta, T, V) with T[p, q] and V[p, q, r, s] numpy arrays.
+    Returns (energies, [1-RDM per instance or None], iterations, info)."""
+    s = default_batch_settings(**settings)
+    n = len(instances)
+    arr = (CasInstance * max(n, 1))()
+    keep = []
+    for i, (norb, na, nb, T, V) in enumerate(instances):
+        Tb = _f64(np.asarray(T, dtype=np.float64).ravel(order="F"))
+        Vb = _f64(np.asarray(V, dtype=np.float64).ravel(order="F"))
+        keep += [Tb, Vb]
+        arr[i] = CasInstance(int(norb), int(na), int(nb), Tb.ctypes.data, Vb.ctypes.data)
+    E = np.zeros(n)
+    its = np.zeros(n, dtype=np.int32)
+    offs = np.concatenate([[0], np.cumsum([int(x[0]) ** 2 for x in instances])]).astype(np.int64)
+    R = np.zeros(int(offs[-1])) if want_rdm1 else None
+    info = BatchInfo()
+    ctx._check(lib().qdkgb_casci_batch(ctx.handle, n, arr, ctypes.byref(s), _ptr(E), _ptr(R), _ptr(its),
+                                       ctypes.byref(info)))
+    rdms = None
+    if want_rdm1:
+        rdms = [R[offs[i]:offs[i + 1]].reshape(int(instances[i][0]), int(instances[i][0])) for i in range(n)]
+    return E, rdms, its, info.as_dict()

@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <limits>
 #include <vector>
 
 #include "internal.h"
@@ -476,6 +477,31 @@ int qdkgb_casci(qdkgb_context* c, int norb, int nalpha, int nbeta, const double*
     const qdkgb_davidson_settings* ss = s ? s : &def;
     build_hamiltonian(c, matel_tol, ss->precision == QDKGB_PREC_MIXED ? QDKGB_H_SPLIT32 : QDKGB_H_FP64);
     davidson(c, ss, E, C, info);
+  });
+}
+
+int qdkgb_batch_default_settings(qdkgb_batch_settings* s) {
+  if (!s) return QDKGB_ERR_INVALID;
+  s->res_tol = 1e-8;
+  s->precision = QDKGB_PREC_MIXED;
+  s->max_subspace = 24;
+  s->max_cycles = 200;
+  s->matel_tol = std::numeric_limits<double>::epsilon();
+  s->min_abs_denominator = 1e-12;
+  s->use_graph = 1;
+  s->max_slab_bytes = (int64_t)96 << 30;
+  return QDKGB_OK;
+}
+
+int qdkgb_casci_batch(qdkgb_context* c, int ninst, const qdkgb_cas_instance* inst, const qdkgb_batch_settings* s,
+                      double* energies, double* rdm1, int* iterations, qdkgb_batch_info* info) {
+  if (!c) return QDKGB_ERR_INVALID;
+  return guarded(c, [&] {
+    if (ninst > 0 && !inst) throw Error(QDKGB_ERR_INVALID, "null instance array");
+    QDKGB_CUDA(cudaSetDevice(c->device));
+    qdkgb_batch_settings def;
+    qdkgb_batch_default_settings(&def);
+    casci_batch(c, ninst, inst, s ? *s : def, energies, rdm1, iterations, info);
   });
 }
 

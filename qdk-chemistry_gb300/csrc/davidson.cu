@@ -266,8 +266,8 @@ __device__ int sturm_count(int k, const double* d, const double* e2, double x) {
   return cnt;
 }
 
-__global__ void __launch_bounds__(kEigThreads) k_lowest_eig(int k, const double* __restrict__ H, int ldh,
-                                                            double* gA, int nev, double* eval, double* evec) {
+__device__ void lowest_eig_cta(int k, const double* __restrict__ H, int ldh, double* gA, int nev, double* eval,
+                               double* evec) {
   extern __shared__ double dyn[];
   __shared__ double d[kMaxSubspace], e[kMaxSubspace], e2[kMaxSubspace], beta[kMaxSubspace];
   __shared__ double red[33];
@@ -451,6 +451,39 @@ __global__ void __launch_bounds__(kEigThreads) k_lowest_eig(int k, const double*
       __syncthreads();
     }
   }
+}
+
+__global__ void __launch_bounds__(kEigThreads) k_lowest_eig(int k, const double* __restrict__ H, int ldh,
+                                                            double* gA, int nev, double* eval, double* evec) {
+  lowest_eig_cta(k, H, ldh, gA, nev, eval, evec);
+}
+
+// One CTA per instance of a batch: the lowest pair of the leading k x k block
+// of Hs[b] (k = *kdev + kadd, matrices hstride apart, ld ldh); CTAs of
+// inactive instances leave at once.
+__global__ void __launch_bounds__(kEigThreads)
+    k_lowest_eig_batch(const int* __restrict__ kdev, int kadd, const double* __restrict__ Hs, int ldh,
+                       int64_t hstride, double* eval, double* evec, int64_t estride, const int* __restrict__ active) {
+  const int b = blockIdx.x;
+  if (active && !active[b]) return;
+  const int k = *kdev + kadd;
+  lowest_eig_cta(k, Hs + b * hstride, ldh, nullptr, 1, eval + b, evec + b * estride);
+}
+
+void lowest_eig_batch(cudaStream_t st, int B, const int* kdev, int kadd, int kmax, const double* Hs, int ldh,
+                      int64_t hstride, double* eval, double* evec, int64_t estride, const int* active) {
+  if (kmax > kEigSmemK) throw Error(QDKGB_ERR_INVALID, "batched subspace larger than the shared-memory eigensolver");
+  static thread_local int configured_dev = -1;
+  int dev = 0;
+  QDKGB_CUDA(cudaGetDevice(&dev));
+  if (configured_dev != dev) {
+    QDKGB_CUDA(cudaFuncSetAttribute(k_lowest_eig_batch, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)(kEigSmemK * kEigSmemK * sizeof(double))));
+    configured_dev = dev;
+  }
+  k_lowest_eig_batch<<<B, kEigThreads, (size_t)kmax * kmax * sizeof(double), st>>>(kdev, kadd, Hs, ldh, hstride, eval,
+                                                                                   evec, estride, active);
+  QDKGB_CHECK_LAUNCH();
 }
 
 // ---------------------------------------------------------------- driver

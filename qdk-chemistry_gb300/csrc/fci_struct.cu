@@ -308,15 +308,25 @@ constexpr int kEmitThreads = 256;
 
 template <int STORAGE>
 __global__ void __launch_bounds__(kEmitThreads)
-    k_slab_emit(SlabArgs A, Integrals I, const uint64_t* __restrict__ galpha, const uint64_t* __restrict__ ubeta,
-                long long tbits, const double* __restrict__ diag_raw, double* __restrict__ val,
-                float* __restrict__ hi, float* __restrict__ lo, double* __restrict__ diag,
-                unsigned long long* __restrict__ kept) {
+    k_slab_emit(SlabArgs A, Integrals I0, const Integrals* __restrict__ Iinst, int64_t vstride, int64_t nstride,
+                const uint64_t* __restrict__ galpha, const uint64_t* __restrict__ ubeta, long long tbits,
+                const double* __restrict__ diag_raw, double* __restrict__ val, float* __restrict__ hi,
+                float* __restrict__ lo, double* __restrict__ diag, unsigned long long* __restrict__ kept) {
   const int g = blockIdx.x / kEmitSegments, s = blockIdx.x - g * kEmitSegments;
   const int p0 = s * A.seglen, p1 = min(A.rowlen, p0 + A.seglen);
   const int Nb = A.Nb;
   const uint64_t ra = galpha[g];
   const int b = blockIdx.y * blockDim.x + threadIdx.x;  // grid.y tiles the beta strings
+  // grid.z: instance of a batch (integrals Iinst[z], slabs vstride apart,
+  // per-determinant arrays nstride apart); a single build passes I0
+  const int inst = blockIdx.z;
+  const Integrals I = Iinst ? Iinst[inst] : I0;
+  diag_raw += inst * nstride;
+  if (STORAGE == QDKGB_H_FP64) val += inst * vstride;
+  else {
+    hi += inst * vstride;
+    lo += inst * vstride;
+  }
   if (b < Nb) {
     const int64_t r = (int64_t)g * Nb + b;
     const uint64_t rb = ubeta[b];
@@ -331,7 +341,7 @@ __global__ void __launch_bounds__(kEmitThreads)
       if (col == r) {
         v = diag_raw[r];
         keep = above_thresh(v, tbits);
-        diag[r] = keep ? v : 0.;
+        if (diag) diag[r] = keep ? v : 0.;
       } else {
         const uint64_t ka = galpha[h], kb = ubeta[bc];
         v = (col > r) ? offdiag_element(I, ra, rb, ka, kb) : offdiag_element(I, ka, kb, ra, rb);
@@ -348,7 +358,7 @@ __global__ void __launch_bounds__(kEmitThreads)
         lo[q] = __double2float_rn(v - (double)h32);
       }
     }
-    atomicAdd(kept + r, (unsigned long long)cnt);
+    if (kept) atomicAdd(kept + r, (unsigned long long)cnt);
   }
 }
 
@@ -471,7 +481,7 @@ template <int MODE>
 __global__ void __launch_bounds__(kSlabThreads, 1)
     k_slab_sigma(SlabArgs A, PlanArgs P, const void* __restrict__ vals, const float* __restrict__ vlo,
                  const void* __restrict__ xv, const float* __restrict__ xlo, void* __restrict__ yv,
-                 int64_t part_stride) {
+                 int64_t part_stride, int64_t vstride, const int* __restrict__ active) {
   using Pol = SlabPol<MODE>;
   using Xs = typename Pol::Xs;
   using Acc = typename Pol::Acc;
@@ -480,6 +490,28 @@ __global__ void __launch_bounds__(kSlabThreads, 1)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int Nb = A.Nb;
   const int g = blockIdx.x / P.S, s = blockIdx.x - g * P.S;
+  // grid.y: instance of a batch (slab vstride apart, vectors n apart); the
+  // CTAs of an inactive instance leave at once
+  const int inst = blockIdx.y;
+  if (active && !active[inst]) return;
+  {
+    const int64_t n = (int64_t)A.G * Nb;
+    if constexpr (MODE == 0) {
+      vals = (const float*)vals + inst * vstride;
+      xv = (const float*)xv + inst * n;
+      yv = (float*)yv + inst * n;
+    } else if constexpr (MODE == 1) {
+      vals = (const double*)vals + inst * vstride;
+      xv = (const double*)xv + inst * n;
+      yv = (double*)yv + inst * n;
+    } else {
+      vals = (const float*)vals + inst * vstride;
+      vlo += inst * vstride;
+      xv = (const float*)xv + inst * n;
+      xlo += inst * n;
+      yv = (double*)yv + inst * n;
+    }
+  }
   Xs* xs = reinterpret_cast<Xs*>(smem_raw);
   int32_t* rec = reinterpret_cast<int32_t*>(xs + (size_t)P.M * Nb);
   const int32_t* rg = P.rec + ((int64_t)g * P.S + s) * P.R;
@@ -566,7 +598,8 @@ __global__ void k_slab_combine(int64_t n, int S, const T* __restrict__ part, T* 
 }
 
 template <int MODE>
-void slab_sigma(Context* c, const void* vals, const float* vlo, const void* x, const float* xlo, void* y) {
+void slab_sigma(Context* c, int B, const int* active, const void* vals, const float* vlo, const void* x,
+                const float* xlo, void* y) {
   FciStruct* F = c->fci;
   SlabPlan& PL = F->plan[MODE == 0 ? 0 : 1];
   PlanArgs P{PL.S, PL.M, PL.R, (const int32_t*)PL.rec.ptr, (const int32_t*)PL.segh.ptr};
@@ -580,14 +613,18 @@ void slab_sigma(Context* c, const void* vals, const float* vlo, const void* x, c
     configured_dev = c->device;
   }
   const int64_t n = F->G * F->Nb;
+  const int64_t vstride = n * F->rowlen;
   void* out = y;
-  if (PL.S > 1) out = dev_alloc(c, F->ypart, (size_t)PL.S * n * sizeof(Out));
-  k_slab_sigma<MODE><<<(unsigned)(F->G * PL.S), slab_threads((int)F->Nb), smem, c->stream>>>(
-      slab_args(c), P, vals, vlo, x, xlo, out, n);
+  // partial sums [S][B][n], combined in segment order (deterministic)
+  if (PL.S > 1) out = dev_alloc(c, F->ypart, (size_t)PL.S * B * n * sizeof(Out));
+  const dim3 grid((unsigned)(F->G * PL.S), (unsigned)B);
+  k_slab_sigma<MODE><<<grid, slab_threads((int)F->Nb), smem, c->stream>>>(slab_args(c), P, vals, vlo, x, xlo, out,
+                                                                          (int64_t)B * n, vstride, active);
   QDKGB_CHECK_LAUNCH();
   if (PL.S > 1) {
-    const unsigned cb = (unsigned)std::min<int64_t>((n + 255) / 256, (int64_t)c->sm_count * 8);
-    k_slab_combine<Out><<<cb, 256, 0, c->stream>>>(n, PL.S, (const Out*)out, (Out*)y);
+    const int64_t tot = (int64_t)B * n;
+    const unsigned cb = (unsigned)std::min<int64_t>((tot + 255) / 256, (int64_t)c->sm_count * 8);
+    k_slab_combine<Out><<<cb, 256, 0, c->stream>>>(tot, PL.S, (const Out*)out, (Out*)y);
     QDKGB_CHECK_LAUNCH();
   }
 }
@@ -601,10 +638,10 @@ bool struct_ready(Context* c) { return c->fci && c->H.valid && !c->op_direct && 
 void struct_spmv_fp64(Context* c, const double* x, double* y) {
   Hcsr& H = c->H;
   if (H.storage == QDKGB_H_FP64) {
-    slab_sigma<1>(c, H.val.ptr, nullptr, x, nullptr, y);
+    slab_sigma<1>(c, 1, nullptr, H.val.ptr, nullptr, x, nullptr, y);
   } else {
     float* xs = split_x(c, x);
-    slab_sigma<2>(c, H.hi.ptr, (const float*)H.lo.ptr, xs, xs + H.n, y);
+    slab_sigma<2>(c, 1, nullptr, H.hi.ptr, (const float*)H.lo.ptr, xs, xs + H.n, y);
   }
 }
 
@@ -612,7 +649,50 @@ void struct_spmv_fp32(Context* c, const float* x, float* y) {
   Hcsr& H = c->H;
   if (H.storage != QDKGB_H_SPLIT32)
     throw Error(QDKGB_ERR_STATE, "FP32 sigma needs the Hamiltonian built with QDKGB_H_SPLIT32 storage");
-  slab_sigma<0>(c, H.hi.ptr, nullptr, x, nullptr, y);
+  slab_sigma<0>(c, 1, nullptr, H.hi.ptr, nullptr, x, nullptr, y);
+}
+
+// ------------------------------------------------------------------ batches
+// Instances sharing this context's complete space, each with its own
+// integrals: slabs [B][stored], per-determinant arrays [B][n].
+void slab_emit_batch(Context* c, int B, const Integrals* d_ints, const double* diag_raw, int storage, double* val,
+                     float* hi, float* lo, double thresh) {
+  FciStruct* F = c->fci;
+  const int64_t n = F->G * F->Nb;
+  long long tbits = -1;
+  if (thresh > 0.) std::memcpy(&tbits, &thresh, sizeof(double));
+  const dim3 grid((unsigned)(F->G * kEmitSegments), (unsigned)((F->Nb + kEmitThreads - 1) / kEmitThreads),
+                  (unsigned)B);
+  const uint64_t* ga = (const uint64_t*)c->dets.galpha.ptr;
+  const uint64_t* ub = (const uint64_t*)c->dets.ubeta.ptr;
+  Integrals none{};
+  if (storage == QDKGB_H_FP64)
+    k_slab_emit<QDKGB_H_FP64><<<grid, kEmitThreads, 0, c->stream>>>(slab_args(c), none, d_ints, n * F->rowlen, n, ga,
+                                                                     ub, tbits, diag_raw, val, hi, lo, nullptr,
+                                                                     nullptr);
+  else
+    k_slab_emit<QDKGB_H_SPLIT32><<<grid, kEmitThreads, 0, c->stream>>>(slab_args(c), none, d_ints, n * F->rowlen, n,
+                                                                        ga, ub, tbits, diag_raw, val, hi, lo, nullptr,
+                                                                        nullptr);
+  QDKGB_CHECK_LAUNCH();
+}
+
+// Sizes the partial-sum scratch for B instances in every mode, so that no
+// later sigma reallocates it (a captured graph keeps its address).
+void slab_reserve_batch(Context* c, int B) {
+  FciStruct* F = c->fci;
+  const int64_t n = F->G * F->Nb;
+  const size_t need = std::max<size_t>((size_t)F->plan[0].S * 4, (size_t)F->plan[1].S * 8) * B * n;
+  dev_alloc(c, F->ypart, need);
+}
+
+// mode 0: FP32 (vals = hi, x/y float); 1: FP64; 2: float-float from (hi, lo)
+// with split x (x = xh, xlo = xl) into FP64 y.  active[B] masks instances.
+void slab_sigma_batch(Context* c, int mode, int B, const int* active, const void* vals, const float* vlo,
+                      const void* x, const float* xlo, void* y) {
+  if (mode == 0) slab_sigma<0>(c, B, active, vals, nullptr, x, nullptr, y);
+  else if (mode == 1) slab_sigma<1>(c, B, active, vals, nullptr, x, nullptr, y);
+  else slab_sigma<2>(c, B, active, vals, vlo, x, xlo, y);
 }
 
 // CSR arrays of a slab Hamiltonian into device buffers of nnz entries: the
@@ -668,9 +748,11 @@ void build_hamiltonian_struct(Context* c, double thresh, int storage) {
   const uint64_t* ub = (const uint64_t*)D.ubeta.ptr;
   unsigned long long* kc = (unsigned long long*)kept;
   if (storage == QDKGB_H_FP64)
-    k_slab_emit<QDKGB_H_FP64><<<grid, thr, 0, c->stream>>>(A, I, ga, ub, tbits, diag_raw, val, hi, lo, diag, kc);
+    k_slab_emit<QDKGB_H_FP64><<<grid, thr, 0, c->stream>>>(A, I, nullptr, 0, 0, ga, ub, tbits, diag_raw, val, hi, lo,
+                                                            diag, kc);
   else
-    k_slab_emit<QDKGB_H_SPLIT32><<<grid, thr, 0, c->stream>>>(A, I, ga, ub, tbits, diag_raw, val, hi, lo, diag, kc);
+    k_slab_emit<QDKGB_H_SPLIT32><<<grid, thr, 0, c->stream>>>(A, I, nullptr, 0, 0, ga, ub, tbits, diag_raw, val, hi,
+                                                               lo, diag, kc);
   QDKGB_CHECK_LAUNCH();
   int64_t* rowptr = dev_array<int64_t>(c, H.rowptr, n + 1);
   exclusive_scan_i64(c, kept, rowptr, n, H.scan_tmp);

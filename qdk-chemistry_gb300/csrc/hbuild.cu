@@ -53,6 +53,15 @@ __global__ void k_intermediates(int n, const double* __restrict__ V, double* G_r
   }
 }
 
+// intermediates of integrals already on the device (batched instances)
+void build_integral_intermediates_into(Context* c, int n, const double* V, double* G, double* Vr, double* G2,
+                                       double* V2) {
+  const int64_t n3 = (int64_t)n * n * n;
+  const int blocks = (int)std::min<int64_t>((n3 + 255) / 256, 4096);
+  k_intermediates<<<blocks, 256, 0, c->stream>>>(n, V, G, Vr, G2, V2);
+  QDKGB_CHECK_LAUNCH();
+}
+
 void build_integral_intermediates(Context* c) {
   const int n = c->norb;
   const size_t n2 = (size_t)n * n, n3 = n2 * n, n4 = n3 * n;

@@ -134,6 +134,17 @@ void struct_spmv_fp64(Context* c, const double* x, double* y);
 void struct_spmv_fp32(Context* c, const float* x, float* y);
 void struct_export(Context* c, int32_t* ci, double* v64, float* h32, float* l32);
 int64_t struct_slab_elements(Context* c);
+// batch.cu
+void casci_batch(Context* ctx, int ninst, const qdkgb_cas_instance* inst, const qdkgb_batch_settings& st,
+                 double* energies, double* rdm1, int* iters, qdkgb_batch_info* info);
+// davidson.cu: lowest eigenpair of B small matrices, one CTA each
+void lowest_eig_batch(cudaStream_t st, int B, const int* kdev, int kadd, int kmax, const double* Hs, int ldh,
+                      int64_t hstride, double* eval, double* evec, int64_t estride, const int* active);
+void slab_emit_batch(Context* c, int B, const Integrals* d_ints, const double* diag_raw, int storage, double* val,
+                     float* hi, float* lo, double thresh);
+void slab_reserve_batch(Context* c, int B);
+void slab_sigma_batch(Context* c, int mode, int B, const int* active, const void* vals, const float* vlo,
+                      const void* x, const float* xlo, void* y);
 float* split_x(Context* c, const double* x);
 void build_hamiltonian_struct(Context* c, double thresh, int storage);
 void k_diag_launch(Context* c, const Integrals& I, double* D, unsigned blocks);
