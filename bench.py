@@ -183,6 +183,42 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def run_reference_batched(args):
+    """The reference's per-instance CPU path (oracle restatement of the SDL
+    build + Davidson, OpenMP on all host cores) over a bounded sample of the
+    512 instances (every 32nd), scaled to the batch."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import oracle
+
+    oracle.build()
+    pkg = _package()
+    inst = batch_instances(pkg)
+    sample = inst[::32]
+    vals = []
+    for step in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        for no, na, nb, T, V in sample:
+            a, b = pkg.determinants.fci_space(no, na, nb)
+            M = oracle.build_csr(oracle.Hamiltonian(T, V), a, b)
+            M.selected_ci_diag(tol=RES_TOL)
+        dt = (time.perf_counter() - t0) * len(inst) / len(sample)
+        if step >= args.warmup:
+            vals.append(len(inst) / dt)
+    v = float(np.mean(vals))
+    cb = {"value": v, "unit": "instances/s", "cores": oracle.num_threads(), "kind": "port",
+          "sample": "every 32nd instance (%d of %d): SDL CSR build + Davidson to |r| < 1e-8, scaled"
+                    % (len(sample), len(inst))}
+    line = {"impl": "reference", "metric": "casci_batch512_instances_per_s", "value": v, "unit": "instances/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": len(inst) / v * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": "512 CASCI instances, norb in {6,8,10}", "seed": BATCH_SEED},
+            "cpu_baseline": cb, "e2e": {"value": v, "unit": "instances/s", "h2d_bytes_per_step": 0,
+                                        "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
 # ------------------------------------------------------------------ GPU arm
 def run_ours(args):
     import torch
@@ -341,6 +377,109 @@ def run_ours(args):
     print(json.dumps(line))
 
 
+# ------------------------------------------------------------------ batched CASCI
+BATCH_N, BATCH_SEED, BATCH_SIZES = 512, 20261204, (6, 8, 10)
+
+
+def batch_instances(pkg, n=BATCH_N, seed=BATCH_SEED):
+    """512 instances, norb drawn uniformly from {6, 8, 10} (seeded), n_alpha =
+    n_beta = norb / 2, integrals of the same recipe with 2 norb Cholesky
+    vectors and a per-instance seed."""
+    rng = np.random.default_rng(seed)
+    norbs = rng.choice(BATCH_SIZES, size=n)
+    out = []
+    for i, no in enumerate(norbs):
+        no = int(no)
+        T, V, _ = pkg.integrals.synthetic_integrals(no, 2 * no, seed + 1 + i)
+        out.append((no, no // 2, no // 2, T, V))
+    return out
+
+
+def _batch_bytes(inst):
+    """Stored values read by one FP32 sigma over every instance (slab: rowlen
+    per determinant) plus x and y."""
+    from math import comb
+
+    tot = 0
+    for no, na, nb, _, _ in inst:
+        ga, gb = comb(no, na), comb(no, nb)
+        ka, kb = na * (no - na), nb * (no - nb)
+        n1a, n1b = 1 + ka, 1 + kb
+        n2b = 1 + kb + comb(nb, 2) * comb(no - nb, 2)
+        c2a = comb(na, 2) * comb(no - na, 2)
+        rowlen = n2b + ka * n1b + c2a
+        nd = ga * gb
+        tot += nd * rowlen * 4 + nd * 8
+    return tot
+
+
+def run_batched(args):
+    import torch
+
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    pkg = _package()
+    pkg.build.build()
+    capi = pkg.capi
+    inst = batch_instances(pkg)
+    ctx = capi.Context(local)
+    for _ in range(max(1, args.warmup)):
+        capi.casci_batch(ctx, inst, res_tol=RES_TOL)
+    launches0 = capi.kernel_launches()
+    times, infos = [], []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            E, R, its, info = capi.casci_batch(ctx, inst, res_tol=RES_TOL)
+            torch.cuda.synchronize()
+            times.append(time.perf_counter() - t0)
+            infos.append(info)
+    launches = capi.kernel_launches() - launches0
+    t = float(np.mean(times))
+    # plain per-instance FP64 GPU path on a sample (every 8th instance), scaled
+    sample = inst[::8]
+    ctx1 = capi.Context(local)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    dE = []
+    for j, (no, na, nb, T, V) in enumerate(sample):
+        E64, _, _ = ctx1.casci(T, V, na, nb, tol=RES_TOL, want_vector=False)
+        dE.append(abs(E64 - E[8 * j]))
+    torch.cuda.synchronize()
+    t_loop = (time.perf_counter() - t0) * len(inst) / len(sample)
+    ctx1.close()
+    ctx.close()
+    if rank != 0:
+        return
+    counts = {str(k): int(sum(1 for x in inst if x[0] == k)) for k in BATCH_SIZES}
+    h2d = int(sum(x[3].nbytes + x[4].nbytes for x in inst))
+    d2h = int(sum(8 + x[0] ** 2 * 8 for x in inst))
+    line = {
+        "metric": "casci_batch512_instances_per_s", "value": len(inst) / t, "unit": "instances/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 sigma / f64 subspace+refinement",
+        "data": "synthetic",
+        "config": {"workload": "512 independent CASCI instances, norb uniform in {6,8,10} (n_alpha = n_beta = "
+                               "norb/2: 400 / 4,900 / 63,504 determinants), seeded integrals of the same recipe "
+                               "with 2 norb Cholesky vectors; energy to |r| < 1e-8 and spin-summed 1-RDM per "
+                               "instance", "instances": counts, "seed": BATCH_SEED, "res_tol": RES_TOL,
+                   "l2": "stored matrices %.1f GB, larger than L2; no flush" % (_batch_bytes(inst) * 2 / 1e9)},
+        "per_instance_fp64_gpu": {"instances_per_s": len(inst) / t_loop,
+                                  "sample": "every 8th instance (%d) through qdkgb_casci FP64, scaled" % len(sample),
+                                  "max_abs_energy_diff_vs_batch": float(max(dE))},
+        "batch_speedup_vs_per_instance_fp64": t_loop / t,
+        "sigma_gbs_per_fp32_sweep_bytes": _batch_bytes(inst),
+        "max_sigma_applications": max(i["iterations"] for i in infos),
+        "graph_replays": infos[-1]["graph_replays"],
+        "e2e": {"value": len(inst) / t, "unit": "instances/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "note": "the call takes host integrals and returns host energies and 1-RDMs"},
+        "gpu_launches": launches, "clocks": clk.summary(),
+    }
+    print(json.dumps(line))
+
+
 def time_spmv(ctx, precision, x, y, stream, reps=20):
     import torch
 
@@ -370,9 +509,16 @@ def main():
     ap.add_argument("--norb", type=int, default=NORB)
     ap.add_argument("--nel", type=int, default=NEL)
     ap.add_argument("--nchol", type=int, default=NCHOL)
+    ap.add_argument("--workload", default="cas12", choices=["cas12", "batched"],
+                    help="cas12: the headline CASCI(12e,12o); batched: 512 small instances")
     args = ap.parse_args()
     set_workload(args.norb, args.nel, args.nchol)
-    if args.impl == "reference":
+    if args.workload == "batched":
+        if args.impl == "reference":
+            run_reference_batched(args)
+        else:
+            run_batched(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

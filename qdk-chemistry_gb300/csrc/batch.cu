@@ -117,12 +117,13 @@ __global__ void __launch_bounds__(kBT)
   }
 }
 
-// x = V y, ax = AV y, r = ax - theta x; partial |r|^2 per chunk
+// x = V y (the previous x kept in xprev), ax = AV y, r = ax - theta x;
+// partial |r|^2 per chunk
 __global__ void __launch_bounds__(kBT)
     k_b_ritz(const double* __restrict__ Vb, const double* __restrict__ AVb, int64_t astride, int64_t ld,
              const int* __restrict__ kdev, const double* __restrict__ yv, int KM, const double* __restrict__ theta,
-             double* __restrict__ x, double* __restrict__ ax, double* __restrict__ r, int64_t n, int nchunk,
-             double* __restrict__ partial, const int* __restrict__ mask) {
+             double* __restrict__ x, double* __restrict__ xprev, double* __restrict__ ax, double* __restrict__ r,
+             int64_t n, int nchunk, double* __restrict__ partial, const int* __restrict__ mask) {
   __shared__ double red[33];
   const int b = blockIdx.y;
   if (mask && !mask[b]) return;
@@ -140,6 +141,7 @@ __global__ void __launch_bounds__(kBT)
       sa += AVb[b * astride + j * ld + i] * yb[j];
     }
     const double rr = sa - th * sx;
+    xprev[b * n + i] = x[b * n + i];
     x[b * n + i] = sx;
     ax[b * n + i] = sa;
     r[b * n + i] = rr;
@@ -257,12 +259,12 @@ __global__ void k_b_wait(int B, const double* __restrict__ est2, const double* _
 }
 
 // refresh: x <- x / |x| into V[b][0] and the packed x; split pair (xh, xl)
-__global__ void k_b_refresh_x(double* __restrict__ x, const double* __restrict__ nrm2, double* __restrict__ Vb,
-                              int64_t astride, float* __restrict__ xh, float* __restrict__ xl, int64_t n,
-                              const int* __restrict__ mask) {
+__global__ void k_b_refresh_x(double* __restrict__ x, const double* __restrict__ nrm2, int ns,
+                              double* __restrict__ Vb, int64_t astride, float* __restrict__ xh,
+                              float* __restrict__ xl, int64_t n, const int* __restrict__ mask) {
   const int b = blockIdx.y;
   if (mask && !mask[b]) return;
-  const double inv = 1. / sqrt(nrm2[(int64_t)b * 2]);
+  const double inv = 1. / sqrt(nrm2[(int64_t)b * ns]);
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const double q = x[b * n + i] * inv;
     x[b * n + i] = q;
@@ -297,8 +299,105 @@ __global__ void __launch_bounds__(kBT)
   if (threadIdx.x == 0) partial[(int64_t)b * nchunk + blockIdx.x] = acc;
 }
 
+// deterministic filler in [-1, 1): the last-resort second restart vector,
+// inside the spin-flip sector s of an nstr x nstr coefficient matrix when
+// s != 0 (f(i, j) = s f(j, i))
+__device__ __forceinline__ double filler(int64_t i, int64_t nstr, double s) {
+  int64_t key = i;
+  double sg = 1.;
+  if (s != 0.) {
+    const int64_t g = i / nstr, b = i - g * nstr;
+    if (g == b && s < 0.) return 0.;
+    key = g < b ? g * nstr + b : b * nstr + g;
+    sg = (g > b) ? s : 1.;
+  }
+  uint64_t h = (uint64_t)key * 0x9E3779B97F4A7C15ull;
+  h ^= h >> 31;
+  h *= 0xBF58476D1CE4E5B9ull;
+  h ^= h >> 29;
+  return sg * ((double)(h >> 11) * 0x1p-52 - 1.0);
+}
+
+// GD+1 restart: partial sums of x.v and v.v for the candidates
+// v = xprev, r, filler (six sums per chunk)
+__global__ void __launch_bounds__(kBT)
+    k_b_second_dots(const double* __restrict__ x, const double* __restrict__ xprev, const double* __restrict__ r,
+                    int64_t n, int64_t nstr, const double* __restrict__ flip, int nchunk, double* __restrict__ partial,
+                    const int* __restrict__ mask) {
+  __shared__ double red[33];
+  const int b = blockIdx.y;
+  if (mask && !mask[b]) return;
+  const double fs = flip ? flip[b] : 0.;
+  const int64_t i0 = (int64_t)blockIdx.x * kChunk;
+  double a[6] = {0., 0., 0., 0., 0., 0.};
+  for (int t = 0; t < kChunk / kBT; ++t) {
+    const int64_t i = i0 + threadIdx.x + (int64_t)t * kBT;
+    if (i >= n) break;
+    const double xi = x[b * n + i], p = xprev[b * n + i], q = r[b * n + i], z = filler(i, nstr, fs);
+    a[0] += xi * p;
+    a[1] += p * p;
+    a[2] += xi * q;
+    a[3] += q * q;
+    a[4] += xi * z;
+    a[5] += z * z;
+  }
+  for (int j = 0; j < 6; ++j) {
+    const double v = bsum(a[j], red);
+    if (threadIdx.x == 0) partial[((int64_t)b * nchunk + blockIdx.x) * 6 + j] = v;
+  }
+}
+
+// V[b][1] = (v - (x.v) x) / |.| for the first candidate that keeps a 1e-4
+// relative norm (x is unit); its split pair into (h2, l2)
+__global__ void k_b_second_set(const double* __restrict__ x, const double* __restrict__ xprev,
+                               const double* __restrict__ r, const double* __restrict__ dots, double* __restrict__ Vb,
+                               int64_t astride, int64_t ld, float* __restrict__ h2, float* __restrict__ l2, int64_t n,
+                               int64_t nstr, const double* __restrict__ flip, const int* __restrict__ mask) {
+  const int b = blockIdx.y;
+  if (mask && !mask[b]) return;
+  const double fs = flip ? flip[b] : 0.;
+  const double* d = dots + (int64_t)b * 6;
+  int pick = 2;
+  double nrm2 = d[5] - d[4] * d[4];
+  if (d[1] - d[0] * d[0] > 1e-8 * d[1]) {
+    pick = 0;
+    nrm2 = d[1] - d[0] * d[0];
+  } else if (d[3] - d[2] * d[2] > 1e-8 * d[3]) {
+    pick = 1;
+    nrm2 = d[3] - d[2] * d[2];
+  }
+  const double c = d[2 * pick], inv = 1. / sqrt(nrm2);
+  double* v1 = Vb + b * astride + ld;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double v = pick == 0 ? xprev[b * n + i] : (pick == 1 ? r[b * n + i] : filler(i, nstr, fs));
+    const double q = (v - c * x[b * n + i]) * inv;
+    v1[i] = q;
+    const float h = __double2float_rn(q);
+    h2[b * n + i] = h;
+    l2[b * n + i] = __double2float_rn(q - (double)h);
+  }
+}
+
+__global__ void k_b_col_to_packed(const double* __restrict__ Vb, int64_t astride, int64_t ld, int col,
+                                  double* __restrict__ y, int64_t n, const int* __restrict__ mask) {
+  const int b = blockIdx.y;
+  if (mask && !mask[b]) return;
+  const double* v = Vb + b * astride + (int64_t)col * ld;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    y[b * n + i] = v[i];
+}
+
+__global__ void k_b_copy_col(const double* __restrict__ y, double* __restrict__ AVb, int64_t astride, int64_t ld,
+                             int col, int64_t n, const int* __restrict__ mask) {
+  const int b = blockIdx.y;
+  if (mask && !mask[b]) return;
+  double* a = AVb + b * astride + (int64_t)col * ld;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    a[i] = y[b * n + i];
+}
+
 // convergence test of the refreshed pair; restarts the subspace at k = 1
-__global__ void k_b_check(int B, const double* __restrict__ th2, const double* __restrict__ res2, double tol,
+__global__ void k_b_check(int B, const double* __restrict__ th2, const double* __restrict__ res2, int rs, double tol,
                           int* __restrict__ notdone, int* __restrict__ act, int* __restrict__ nref,
                           double* __restrict__ last_true,
                           double* __restrict__ theta, double* __restrict__ energy, double* __restrict__ Hs, int m,
@@ -315,7 +414,7 @@ __global__ void k_b_check(int B, const double* __restrict__ th2, const double* _
     if (!notdone[b]) continue;
     nref[b] += 1;
     const double th = th2[(int64_t)b * 2];
-    const double rn = sqrt(res2[(int64_t)b * 2]);
+    const double rn = sqrt(res2[(int64_t)b * rs]);
     theta[b] = th;
     energy[b] = th;
     resid[b] = rn;
@@ -550,12 +649,13 @@ void casci_batch(Context* ctx, int ninst, const qdkgb_cas_instance* inst, const 
                    &bt = bs.b[17], &bt32 = bs.b[18], &bs32 = bs.b[19], &bxh = bs.b[20], &bxl = bs.b[21],
                    &by = bs.b[22], &bev = bs.b[23], &bth = bs.b[24], &bco = bs.b[25], &bpart = bs.b[26],
                    &bsc = bs.b[27], &bsc2 = bs.b[28], &bflip = bs.b[29], &bint = bs.b[30], &bidx = bs.b[31],
-                   &blt = bs.b[32], &ben = bs.b[33], &bres = bs.b[34];
+                   &blt = bs.b[32], &ben = bs.b[33], &bres = bs.b[34], &bxp = bs.b[37];
       const int64_t astride = (int64_t)m * N;
       double* Vb = dev_array<double>(cc, bV, (size_t)B * astride);
       double* AVb = dev_array<double>(cc, bAV, (size_t)B * astride);
       double* Hs = dev_array<double>(cc, bHs, (size_t)B * m * m);
       double* x = dev_array<double>(cc, bx, (size_t)B * N);
+      double* xprev = dev_array<double>(cc, bxp, (size_t)B * N);
       double* ax = dev_array<double>(cc, bax, (size_t)B * N);
       double* r = dev_array<double>(cc, br, (size_t)B * N);
       double* t = dev_array<double>(cc, bt, (size_t)B * N);
@@ -567,8 +667,8 @@ void casci_batch(Context* ctx, int ninst, const qdkgb_cas_instance* inst, const 
       double* yv = dev_array<double>(cc, bev, (size_t)B * KM);
       double* theta = dev_array<double>(cc, bth, (size_t)B);
       double* coef = dev_array<double>(cc, bco, (size_t)B * KM);
-      double* partial = dev_array<double>(cc, bpart, (size_t)B * nchunk * KM);
-      double* sc = dev_array<double>(cc, bsc, (size_t)B * 2);    // per-instance scalar (stride 2)
+      double* partial = dev_array<double>(cc, bpart, (size_t)B * nchunk * std::max(KM, 6));
+      double* sc = dev_array<double>(cc, bsc, (size_t)B * 6);    // per-instance scalars
       double* sc2 = dev_array<double>(cc, bsc2, (size_t)B * 2);  // second scalar
       double* flip = dev_array<double>(cc, bflip, (size_t)B);
       double* last_true = dev_array<double>(cc, blt, (size_t)B);
@@ -608,14 +708,41 @@ void casci_batch(Context* ctx, int ninst, const qdkgb_cas_instance* inst, const 
         QDKGB_CUDA(cudaStreamSynchronize(s0));
         return hstat[0];
       };
-      // ---- refresh: full-precision sigma of the normalised Ritz vector
-      auto refresh = [&]() {
+      // ---- refresh: full-precision sigma of the normalised Ritz vector; from
+      // the second cycle on (gd) the subspace restarts on [x, x_prev] (GD+1:
+      // the previous Ritz vector orthogonalised against x, also multiplied
+      // in full precision) instead of x alone
+      auto refresh = [&](bool gd) {
         k_b_multidot<<<gc, kBT, 0, s0>>>(x, N, N, nullptr, 1, x, N, 0, N, nchunk, partial, KM, notdone);
         QDKGB_CHECK_LAUNCH();
-        k_b_reduce<<<B, 32, 0, s0>>>(partial, nchunk, KM, nullptr, 1, sc, 2, notdone);
+        k_b_reduce<<<B, 32, 0, s0>>>(partial, nchunk, KM, nullptr, 1, sc, 6, notdone);
         QDKGB_CHECK_LAUNCH();
-        k_b_refresh_x<<<gv, kBT, 0, s0>>>(x, sc, Vb, astride, xh, xl, N, notdone);
+        k_b_refresh_x<<<gv, kBT, 0, s0>>>(x, sc, 6, Vb, astride, xh, xl, N, notdone);
         QDKGB_CHECK_LAUNCH();
+        if (gd) {
+          // candidates kept in the guess's spin-flip sector: the estimated
+          // residual carries the FP32 sigma's out-of-sector noise
+          const double* fl = (square && mixed) ? flip : nullptr;
+          if (fl) {
+            k_b_flip<<<gv, kBT, 0, s0>>>(xprev, S.nbeta, flip, notdone);
+            QDKGB_CHECK_LAUNCH();
+            k_b_flip<<<gv, kBT, 0, s0>>>(r, S.nbeta, flip, notdone);
+            QDKGB_CHECK_LAUNCH();
+          }
+          k_b_second_dots<<<gc, kBT, 0, s0>>>(x, xprev, r, N, S.nbeta, fl, nchunk, partial, notdone);
+          QDKGB_CHECK_LAUNCH();
+          k_b_reduce<<<B, 32, 0, s0>>>(partial, nchunk, 6, nullptr, 6, sc, 6, notdone);
+          QDKGB_CHECK_LAUNCH();
+          k_b_second_set<<<gv, kBT, 0, s0>>>(x, xprev, r, sc, Vb, astride, ld, t32, s32, N, S.nbeta, fl, notdone);
+          QDKGB_CHECK_LAUNCH();
+          if (mixed) {
+            slab_sigma_batch(cc, 2, B, notdone, hi, lo, t32, s32, ax);
+          } else {
+            k_b_col_to_packed<<<gv, kBT, 0, s0>>>(Vb, astride, ld, 1, t, N, notdone);
+            QDKGB_CHECK_LAUNCH();
+            slab_sigma_batch(cc, 1, B, notdone, val, nullptr, t, nullptr, ax);
+          }
+        }
         if (mixed) slab_sigma_batch(cc, 2, B, notdone, hi, lo, xh, xl, yfull);
         else slab_sigma_batch(cc, 1, B, notdone, val, nullptr, x, nullptr, yfull);
         k_b_multidot<<<gc, kBT, 0, s0>>>(x, N, N, nullptr, 1, yfull, N, 0, N, nchunk, partial, KM, notdone);
@@ -624,11 +751,28 @@ void casci_batch(Context* ctx, int ninst, const qdkgb_cas_instance* inst, const 
         QDKGB_CHECK_LAUNCH();
         k_b_refresh_res<<<gc, kBT, 0, s0>>>(x, yfull, sc2, AVb, astride, r, N, nchunk, partial, notdone);
         QDKGB_CHECK_LAUNCH();
-        k_b_reduce<<<B, 32, 0, s0>>>(partial, nchunk, 1, nullptr, 1, sc, 2, notdone);
+        k_b_reduce<<<B, 32, 0, s0>>>(partial, nchunk, 1, nullptr, 1, sc, 6, notdone);
         QDKGB_CHECK_LAUNCH();
-        k_b_check<<<1, 1024, 0, s0>>>(B, sc2, sc, st.res_tol, notdone, act, nref, last_true, theta, energy, Hs, m,
+        k_b_check<<<1, 1024, 0, s0>>>(B, sc2, sc, 6, st.res_tol, notdone, act, nref, last_true, theta, energy, Hs, m,
                                       kdev, nact, resid);
         QDKGB_CHECK_LAUNCH();
+        if (gd) {
+          k_b_copy_col<<<gv, kBT, 0, s0>>>(ax, AVb, astride, ld, 1, N, act);
+          QDKGB_CHECK_LAUNCH();
+          // row 1 of the projected matrix (kdev = 1 after the check), then k = 2
+          k_b_multidot<<<gc, kBT, 0, s0>>>(AVb, astride, ld, kdev, 1, Vb, astride, ld, N, nchunk, partial, KM, act);
+          QDKGB_CHECK_LAUNCH();
+          k_b_reduce<<<B, 64, 0, s0>>>(partial, nchunk, KM, kdev, 1, coef, KM, act);
+          QDKGB_CHECK_LAUNCH();
+          k_b_hsrow<<<B, 64, 0, s0>>>(coef, KM, Hs, m, kdev, act);
+          QDKGB_CHECK_LAUNCH();
+          k_b_kinc<<<1, 1, 0, s0>>>(kdev);
+          QDKGB_CHECK_LAUNCH();
+          lowest_eig_batch(s0, B, kdev, 0, m, Hs, m, (int64_t)m * m, theta, yv, KM, act);
+          k_b_ritz<<<gc, kBT, 0, s0>>>(Vb, AVb, astride, ld, kdev, yv, KM, theta, x, xprev, ax, r, N, nchunk, partial,
+                                       act);
+          QDKGB_CHECK_LAUNCH();
+        }
       };
       // ---- one inner iteration (graph-captured): new direction from (r, theta)
       auto inner = [&]() {
@@ -672,7 +816,8 @@ void casci_batch(Context* ctx, int ninst, const qdkgb_cas_instance* inst, const 
         k_b_kinc<<<1, 1, 0, s0>>>(kdev);
         QDKGB_CHECK_LAUNCH();
         lowest_eig_batch(s0, B, kdev, 0, m, Hs, m, (int64_t)m * m, theta, yv, KM, act);
-        k_b_ritz<<<gc, kBT, 0, s0>>>(Vb, AVb, astride, ld, kdev, yv, KM, theta, x, ax, r, N, nchunk, partial, act);
+        k_b_ritz<<<gc, kBT, 0, s0>>>(Vb, AVb, astride, ld, kdev, yv, KM, theta, x, xprev, ax, r, N, nchunk, partial,
+                                     act);
         QDKGB_CHECK_LAUNCH();
         k_b_reduce<<<B, 32, 0, s0>>>(partial, nchunk, 1, nullptr, 1, sc, 2, act);
         QDKGB_CHECK_LAUNCH();
@@ -691,7 +836,7 @@ void casci_batch(Context* ctx, int ninst, const qdkgb_cas_instance* inst, const 
         }
       } gown{&graph, &gexec};
       slab_reserve_batch(cc, B);
-      refresh();
+      refresh(false);
       int cycles = 0;
       bool warmed = false;  // one eager iteration first: it makes the allocations a capture may not
       while (read_nact() > 0) {
@@ -710,9 +855,9 @@ void casci_batch(Context* ctx, int ninst, const qdkgb_cas_instance* inst, const 
             inner();
             warmed = true;
           }
-          if (read_nact() == 0) break;
+          if (read_nact() == 0 || hstat[1] >= m) break;
         }
-        refresh();
+        refresh(true);
       }
       // ---- results
       std::vector<double> hE(B), hR(B);
