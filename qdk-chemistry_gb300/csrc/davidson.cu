@@ -26,6 +26,7 @@
 
 #include "common.cuh"
 #include "internal.h"
+#include "small_eig.cuh"
 
 namespace qdkgb {
 
@@ -213,246 +214,6 @@ __global__ void k_store_row(const double* v, int i, double* Hk, int ld) {
   }
 }
 
-// ---------------------------------------------------------------- lowest eigenpairs
-// One CTA: the `nev` lowest eigenpairs of the symmetric k x k matrix H (lower
-// triangle read, as syev(Uplo::Lower)).  Householder reduction to tridiagonal
-// form (O(k^3) once, instead of Jacobi's O(k^3) per sweep - the FP64 pipe of
-// one SM is the budget here), eigenvalues by multisection on the
-// division-free Sturm sequence, eigenvectors by inverse iteration on the
-// tridiagonal matrix (partial pivoting, re-orthogonalised against the lower
-// ones), back-transformed through the reflectors.  Results: eval[0:nev)
-// ascending, evec[:, 0:nev) with leading dimension k.
-constexpr int kEigThreads = 256;
-constexpr int kEigSmemK = 150;  // matrices up to this size live in shared memory
-
-__device__ double block_sum_eig(double v, double* red) {
-  v = warp_sum(v);
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  __syncthreads();
-  if (lane == 0) red[w] = v;
-  __syncthreads();
-  double t = 0.;
-  if (threadIdx.x < 32) {
-    t = (lane < (int)(blockDim.x >> 5)) ? red[lane] : 0.;
-    t = warp_sum(t);
-    if (lane == 0) red[32] = t;
-  }
-  __syncthreads();
-  return red[32];
-}
-
-// number of eigenvalues of tridiag(d, e) below x (division-free Sturm sequence
-// of leading minors, rescaled by exact powers of two)
-__device__ int sturm_count(int k, const double* d, const double* e2, double x) {
-  double p0 = 1., p1 = d[0] - x;
-  int cnt = (p1 < 0.) ? 1 : 0;
-  int s_prev = (p1 < 0.) ? -1 : 1;
-  for (int i = 1; i < k; ++i) {
-    double p2 = (d[i] - x) * p1 - e2[i - 1] * p0;
-    const double a2 = fabs(p2);
-    if (a2 > 0x1p+600) {
-      p2 *= 0x1p-600;
-      p1 *= 0x1p-600;
-    } else if (a2 < 0x1p-600 && a2 != 0. && fabs(p1) < 0x1p-600) {
-      p2 *= 0x1p+600;
-      p1 *= 0x1p+600;
-    }
-    int sg = (p2 < 0.) ? -1 : (p2 > 0. ? 1 : -s_prev);
-    if (sg != s_prev) ++cnt;
-    s_prev = sg;
-    p0 = p1;
-    p1 = p2;
-  }
-  return cnt;
-}
-
-__device__ void lowest_eig_cta(int k, const double* __restrict__ H, int ldh, double* gA, int nev, double* eval,
-                               double* evec) {
-  extern __shared__ double dyn[];
-  __shared__ double d[kMaxSubspace], e[kMaxSubspace], e2[kMaxSubspace], beta[kMaxSubspace];
-  __shared__ double red[33];
-  __shared__ double s_lo, s_hi;
-  __shared__ double s_u[3 * kMaxSubspace];
-  double* A = gA ? gA : dyn;  // k x k, column-major; reflector j kept in column j below the diagonal
-  const int tid = threadIdx.x, nt = blockDim.x;
-  for (int t = tid; t < k * k; t += nt) {
-    const int i = t % k, j = t / k;
-    A[t] = (i >= j) ? H[i + (size_t)j * ldh] : H[j + (size_t)i * ldh];
-  }
-  __syncthreads();
-  // ---- Householder tridiagonalisation
-  for (int j = 0; j + 2 < k; ++j) {
-    const int m0 = j + 1;
-    double xx = 0.;
-    for (int i = m0 + tid; i < k; i += nt) xx += A[i + (size_t)k * j] * A[i + (size_t)k * j];
-    xx = block_sum_eig(xx, red);
-    if (tid == 0) {
-      const double x0 = A[m0 + (size_t)k * j];
-      const double nrm = sqrt(xx);
-      if (nrm == 0.) {
-        beta[j] = 0.;
-        e[j] = 0.;
-      } else {
-        const double alpha = (x0 >= 0.) ? -nrm : nrm;
-        const double v0 = x0 - alpha;
-        const double vv = xx - x0 * x0 + v0 * v0;
-        beta[j] = (vv > 0.) ? 2. / vv : 0.;
-        e[j] = alpha;
-        A[m0 + (size_t)k * j] = v0;
-      }
-      d[j] = A[j + (size_t)k * j];
-    }
-    __syncthreads();
-    const double b = beta[j];
-    if (b == 0.) continue;
-    const double* v = A + (size_t)k * j;  // v_i for i >= m0
-    // p = b * A_sub v, kept in column j's upper part?  use the d/e-free scratch: A row j (i < j unused after)
-    // p is stored transiently in e2[] (length k)
-    for (int i = m0 + tid; i < k; i += nt) {
-      double acc = 0.;
-      for (int l = m0; l < k; ++l) acc += A[i + (size_t)k * l] * v[l];
-      e2[i] = b * acc;
-    }
-    __syncthreads();
-    double vp = 0.;
-    for (int i = m0 + tid; i < k; i += nt) vp += v[i] * e2[i];
-    vp = block_sum_eig(vp, red);
-    const double K = 0.5 * b * vp;
-    for (int i = m0 + tid; i < k; i += nt) e2[i] -= K * v[i];  // w
-    __syncthreads();
-    const int m = k - m0;
-    for (int t = tid; t < m * m; t += nt) {
-      const int i = m0 + t % m, l = m0 + t / m;
-      A[i + (size_t)k * l] -= v[i] * e2[l] + e2[i] * v[l];
-    }
-    __syncthreads();
-  }
-  if (tid == 0) {
-    if (k >= 2) {
-      d[k - 2] = A[(k - 2) + (size_t)k * (k - 2)];
-      e[k - 2] = A[(k - 1) + (size_t)k * (k - 2)];
-      beta[k - 2] = 0.;
-    }
-    d[k - 1] = A[(k - 1) + (size_t)k * (k - 1)];
-    if (k >= 1) beta[k - 1] = 0.;
-  }
-  __syncthreads();
-  for (int i = tid; i < k - 1; i += nt) e2[i] = e[i] * e[i];
-  __syncthreads();
-  // ---- eigenvalues: multisection on the Sturm count (one warp: 32 points per round)
-  for (int jv = 0; jv < nev; ++jv) {
-    if (tid == 0) {
-      double lo = 1e300, hi = -1e300;
-      for (int i = 0; i < k; ++i) {
-        const double r = (i > 0 ? fabs(e[i - 1]) : 0.) + (i + 1 < k ? fabs(e[i]) : 0.);
-        lo = fmin(lo, d[i] - r);
-        hi = fmax(hi, d[i] + r);
-      }
-      const double pad = 1e-12 * fmax(1., fmax(fabs(lo), fabs(hi)));
-      s_lo = lo - pad;
-      s_hi = hi + pad;
-    }
-    __syncthreads();
-    if (tid < 32) {
-      for (int round = 0; round < 80; ++round) {
-        const double lo = s_lo, hi = s_hi;
-        if (!(hi - lo > 4e-16 * fmax(fabs(lo), fabs(hi))) || hi - lo < 1e-300) break;
-        const double x = lo + (hi - lo) * (double)(tid + 1) / 33.;
-        const int cnt = sturm_count(k, d, e2, x);
-        const unsigned above = __ballot_sync(QDKGB_FULL_MASK, cnt > jv);
-        const int t = above ? (__ffs(above) - 1) : 32;  // first point with count > jv
-        if (tid == 0) {
-          s_lo = (t == 0) ? lo : lo + (hi - lo) * (double)t / 33.;
-          s_hi = (t == 32) ? hi : lo + (hi - lo) * (double)(t + 1) / 33.;
-        }
-        __syncwarp();
-      }
-      if (tid == 0) eval[jv] = 0.5 * (s_lo + s_hi);
-    }
-    __syncthreads();
-  }
-  // ---- eigenvectors of T: inverse iteration with partial pivoting (thread 0)
-  double* Y = evec;  // k x nev, ld k
-  if (tid == 0) {
-    double* Ua = s_u;
-    double* Ub = s_u + kMaxSubspace;
-    double* Uc = s_u + 2 * kMaxSubspace;
-    for (int jv = 0; jv < nev; ++jv) {
-      double* y = Y + (size_t)k * jv;
-      const double lam0 = eval[jv];
-      const double lam = lam0 + (jv % 2 ? 1. : -1.) * 1e-17 * fmax(1., fabs(lam0));
-      for (int i = 0; i < k; ++i) y[i] = 1.0 + 0.01 * (double)((i * 7 + jv * 3) % 11);
-      for (int it = 0; it < 3; ++it) {
-        // forward elimination of T - lam I (rows i: [a b c] at columns i, i+1, i+2)
-        double a_i = d[0] - lam, b_i = (k > 1) ? e[0] : 0., c_i = 0., yi = y[0];
-        for (int i = 0; i < k - 1; ++i) {
-          const double a1 = e[i], b1 = d[i + 1] - lam, c1 = (i + 2 < k) ? e[i + 1] : 0., y1 = y[i + 1];
-          if (fabs(a_i) >= fabs(a1)) {
-            const double f = (a_i != 0.) ? a1 / a_i : 0.;
-            Ua[i] = a_i;
-            Ub[i] = b_i;
-            Uc[i] = c_i;
-            y[i] = yi;
-            a_i = b1 - f * b_i;
-            b_i = c1 - f * c_i;
-            yi = y1 - f * yi;
-          } else {
-            const double f = a_i / a1;
-            Ua[i] = a1;
-            Ub[i] = b1;
-            Uc[i] = c1;
-            y[i] = y1;
-            const double na = b_i - f * b1, nb = c_i - f * c1;
-            yi = yi - f * y1;
-            a_i = na;
-            b_i = nb;
-          }
-          c_i = 0.;
-        }
-        Ua[k - 1] = a_i;
-        y[k - 1] = yi;
-        double big = 0.;
-        for (int i = k - 1; i >= 0; --i) {
-          double r = y[i];
-          if (i + 1 < k) r -= Ub[i] * y[i + 1];
-          if (i + 2 < k) r -= Uc[i] * y[i + 2];
-          const double piv = (Ua[i] != 0.) ? Ua[i] : 1e-300;
-          y[i] = r / piv;
-          big = fmax(big, fabs(y[i]));
-        }
-        // rescale to avoid overflow, orthogonalise against lower vectors, normalise
-        for (int i = 0; i < k; ++i) y[i] /= big;
-        for (int q = 0; q < jv; ++q) {
-          const double* z = Y + (size_t)k * q;
-          double dz = 0.;
-          for (int i = 0; i < k; ++i) dz += z[i] * y[i];
-          for (int i = 0; i < k; ++i) y[i] -= dz * z[i];
-        }
-        double nrm = 0.;
-        for (int i = 0; i < k; ++i) nrm += y[i] * y[i];
-        nrm = sqrt(nrm);
-        for (int i = 0; i < k; ++i) y[i] /= nrm;
-      }
-    }
-  }
-  __syncthreads();
-  // ---- back-transform: y <- H_0 H_1 ... H_{k-3} y
-  for (int j = k - 3; j >= 0; --j) {
-    const double b = beta[j];
-    if (b == 0.) continue;
-    const int m0 = j + 1;
-    const double* v = A + (size_t)k * j;
-    for (int jv = 0; jv < nev; ++jv) {
-      double* y = Y + (size_t)k * jv;
-      double dv = 0.;
-      for (int i = m0 + tid; i < k; i += nt) dv += v[i] * y[i];
-      dv = block_sum_eig(dv, red);
-      for (int i = m0 + tid; i < k; i += nt) y[i] -= b * dv * v[i];
-      __syncthreads();
-    }
-  }
-}
-
 __global__ void __launch_bounds__(kEigThreads) k_lowest_eig(int k, const double* __restrict__ H, int ldh,
                                                             double* gA, int nev, double* eval, double* evec) {
   lowest_eig_cta(k, H, ldh, gA, nev, eval, evec);
@@ -478,11 +239,11 @@ void lowest_eig_batch(cudaStream_t st, int B, const int* kdev, int kadd, int kma
   QDKGB_CUDA(cudaGetDevice(&dev));
   if (configured_dev != dev) {
     QDKGB_CUDA(cudaFuncSetAttribute(k_lowest_eig_batch, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)(kEigSmemK * kEigSmemK * sizeof(double))));
+                                    (int)kEigDynSmemMax));
     configured_dev = dev;
   }
-  k_lowest_eig_batch<<<B, kEigThreads, (size_t)kmax * kmax * sizeof(double), st>>>(kdev, kadd, Hs, ldh, hstride, eval,
-                                                                                   evec, estride, active);
+  k_lowest_eig_batch<<<B, kEigThreads, eig_dyn_smem(kmax), st>>>(kdev, kadd, Hs, ldh, hstride, eval, evec, estride,
+                                                                 active);
   QDKGB_CHECK_LAUNCH();
 }
 
@@ -572,7 +333,7 @@ struct Dav {
   // lowest `nev` eigenpairs of the leading k x k projected matrix
   void lowest(int k, int nev = 1) {
     const bool in_smem = k <= kEigSmemK;
-    k_lowest_eig<<<1, kEigThreads, in_smem ? (size_t)k * k * sizeof(double) : 0, st>>>(
+    k_lowest_eig<<<1, kEigThreads, in_smem ? eig_dyn_smem(k) : 0, st>>>(
         k, Hk, (int)(maxm + 1), in_smem ? nullptr : gA, std::min(nev, k), eval, evec);
     QDKGB_CHECK_LAUNCH();
   }
@@ -631,7 +392,7 @@ void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C
   static bool attr_set = false;
   if (!attr_set) {
     QDKGB_CUDA(cudaFuncSetAttribute(k_lowest_eig, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    kEigSmemK * kEigSmemK * (int)sizeof(double)));
+                                    (int)kEigDynSmemMax));
     attr_set = true;
   }
   d.D = (double*)H.diag.ptr;
