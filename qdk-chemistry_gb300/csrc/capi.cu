@@ -469,9 +469,15 @@ int qdkgb_casci(qdkgb_context* c, int norb, int nalpha, int nbeta, const double*
   rc = qdkgb_fci_dets(norb, nalpha, nbeta, nullptr, nullptr, &nd);
   if (rc) return rc;
   return guarded(c, [&] {
-    std::vector<uint64_t> a(nd), b(nd);
-    if (qdkgb_fci_dets(norb, nalpha, nbeta, a.data(), b.data(), &nd)) throw Error(QDKGB_ERR_INVALID, "fci dets");
-    build_det_space(c, nd, a.data(), b.data());
+    // the complete space of this shape is reused when the context holds it
+    if (!(c->have_dets && c->fci_shape[0] == norb && c->fci_shape[1] == nalpha && c->fci_shape[2] == nbeta)) {
+      std::vector<uint64_t> a(nd), b(nd);
+      if (qdkgb_fci_dets(norb, nalpha, nbeta, a.data(), b.data(), &nd)) throw Error(QDKGB_ERR_INVALID, "fci dets");
+      build_det_space(c, nd, a.data(), b.data());
+      c->fci_shape[0] = norb;
+      c->fci_shape[1] = nalpha;
+      c->fci_shape[2] = nbeta;
+    }
     qdkgb_davidson_settings def;
     qdkgb_davidson_default_settings(&def);
     const qdkgb_davidson_settings* ss = s ? s : &def;

@@ -105,6 +105,13 @@ void build_struct(Context* c) {
   } plan_tmp[2];
   std::vector<uint32_t> gdesc;
   std::vector<int32_t> pblock;  // [G][rowlen]
+  {
+    const size_t guess = (size_t)G * (size_t)(n2 + (ap[1] - ap[0]) * std::max<int64_t>(n1, 1));
+    if (guess < ((size_t)1 << 31)) {
+      gdesc.reserve(guess);
+      pblock.reserve(guess);
+    }
+  }
   for (int64_t g = 0; g < G; ++g) {
     const size_t row0 = gdesc.size();
     int k0 = 0, k1 = 0, k2 = 0, nb = 0;
@@ -165,32 +172,38 @@ void build_struct(Context* c) {
     const int len = std::max(it.len, 1);
     return std::min(S - 1, (int)(((int64_t)(2 * it.p + len) * S) / (2 * (int64_t)rowlen)));
   };
+  // staged blocks (M) and record length (R) per segment count; segments are
+  // runs of items in row order, so one pass per group counts them
+  constexpr int kMaxS = 16;
+  int shapeM[kMaxS + 1], shapeR[kMaxS + 1];
+  for (int S = 1; S <= kMaxS && S <= rowlen; ++S) {
+    int M = 1, R = 6;
+    for (int64_t g = 0; g < G; ++g) {
+      int cur = -1, nb = 0, ndd = 0;
+      for (int i = item0[g]; i <= item0[g + 1]; ++i) {
+        const int sg = i < item0[g + 1] ? seg_of(items[i], S) : S;
+        if (sg != cur) {
+          M = std::max(M, nb);
+          R = std::max(R, 6 + 2 * (nb + ndd));
+          cur = sg;
+          nb = ndd = 0;
+        }
+        if (i < item0[g + 1]) (items[i].len ? nb : ndd) += 1;
+      }
+    }
+    shapeM[S] = M;
+    shapeR[S] = R;
+  }
   // per plan: the segment count that fits the budget and fills the SMs best
+  std::vector<int32_t> dd;
   for (int pl = 0; pl < 2; ++pl) {
     const size_t xsize = pl == 0 ? 4 : 8;
-    auto shape = [&](int S, int& M, int& R) {
-      M = 1;
-      R = 6;
-      for (int64_t g = 0; g < G; ++g) {
-        std::vector<int> nb(S, 0), nd(S, 0);
-        for (int i = item0[g]; i < item0[g + 1]; ++i) {
-          const int sg = seg_of(items[i], S);
-          if (items[i].len) ++nb[sg];
-          else ++nd[sg];
-        }
-        for (int sg = 0; sg < S; ++sg) {
-          M = std::max(M, nb[sg]);
-          R = std::max(R, 6 + 2 * (nb[sg] + nd[sg]));
-        }
-      }
-    };
     auto smem_of = [&](int M, int R) { return (size_t)M * Nb * xsize + ((size_t)R * 4 + 15) / 16 * 16; };
     int best_S = -1, best_M = 0, best_R = 0;
     double best = -1.;
     const int threads = std::min<int64_t>(kSlabThreads, (Nb + 31) / 32 * 32);
-    for (int S = 1; S <= 16 && S <= rowlen; ++S) {
-      int M, R;
-      shape(S, M, R);
+    for (int S = 1; S <= kMaxS && S <= rowlen; ++S) {
+      const int M = shapeM[S], R = shapeR[S];
       const size_t sm = smem_of(M, R);
       if (sm > kSlabSmemMax) continue;
       const int64_t per_sm = std::max<int64_t>(1, std::min<int64_t>(2048 / threads, (227 * 1024) / (int64_t)sm));
@@ -208,35 +221,42 @@ void build_struct(Context* c) {
     const int S = best_S, M = best_M, R = best_R;
     std::vector<int32_t> rec((size_t)G * S * R, 0), segh((size_t)G * S * M, -1);
     for (int64_t g = 0; g < G; ++g) {
-      std::vector<std::vector<int32_t>> b1(S), dd(S);
-      std::vector<int> nslot(S, 0);
+      int cur = -1, nslot = 0, nb1 = 0;
+      int32_t* r = nullptr;
+      auto close = [&]() {
+        if (!r) return;
+        r[3] = nb1;
+        r[4 + 2 * nb1] = (int32_t)(dd.size() / 2);
+        std::copy(dd.begin(), dd.end(), r + 6 + 2 * nb1);
+      };
       for (int i = item0[g]; i < item0[g + 1]; ++i) {
         const Item& it = items[i];
         const int sg = seg_of(it, S);
-        int32_t* r = &rec[((size_t)g * S + sg) * R];
+        if (sg != cur) {
+          close();
+          cur = sg;
+          r = &rec[((size_t)g * S + sg) * R];
+          nslot = nb1 = 0;
+          dd.clear();
+        }
         if (it.len == 0) {
-          dd[sg].push_back((int32_t)(it.p * Nb));
-          dd[sg].push_back((int32_t)(it.h * Nb));
+          dd.push_back((int32_t)(it.p * Nb));
+          dd.push_back((int32_t)(it.h * Nb));
           continue;
         }
-        const int slot = nslot[sg]++;
+        const int slot = nslot++;
         segh[((size_t)g * S + sg) * M + slot] = it.h;
         if (it.h == g) {
           r[0] = 1;
           r[1] = (int32_t)(it.p * Nb);
           r[2] = (int32_t)(slot * Nb);
         } else {
-          b1[sg].push_back((int32_t)(it.p * Nb));
-          b1[sg].push_back((int32_t)(slot * Nb));
+          r[4 + 2 * nb1] = (int32_t)(it.p * Nb);
+          r[5 + 2 * nb1] = (int32_t)(slot * Nb);
+          ++nb1;
         }
       }
-      for (int sg = 0; sg < S; ++sg) {
-        int32_t* r = &rec[((size_t)g * S + sg) * R];
-        r[3] = (int32_t)(b1[sg].size() / 2);
-        std::copy(b1[sg].begin(), b1[sg].end(), r + 4);
-        r[4 + b1[sg].size()] = (int32_t)(dd[sg].size() / 2);
-        std::copy(dd[sg].begin(), dd[sg].end(), r + 6 + b1[sg].size());
-      }
+      close();
     }
     plan_tmp[pl] = {S, M, R, std::move(rec), std::move(segh)};
   }

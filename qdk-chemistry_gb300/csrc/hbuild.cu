@@ -250,6 +250,7 @@ void build_det_space(Context* c, int64_t nd, const uint64_t* alpha, const uint64
     dev_free(c, *b);
   D = DetSpace();
   c->have_dets = false;
+  c->fci_shape[0] = c->fci_shape[1] = c->fci_shape[2] = -1;
   c->H.valid = false;
   free_direct(c);
   free_struct(c);
@@ -272,14 +273,33 @@ void build_det_space(Context* c, int64_t nd, const uint64_t* alpha, const uint64
 
   std::vector<uint64_t> ubeta;
   std::vector<int32_t> brank(nd);
-  bool ascending = true;
+  // product space (generate_hilbert_space): every group repeats group 0's beta
+  // sequence - ranks by position, O(n)
+  bool product0 = G >= 1 && nd % D.h_gstart[1] == 0 && G * D.h_gstart[1] == nd;
+  {
+    const int64_t s0 = D.h_gstart[1];
+    for (int64_t g = 1; g < G && product0; ++g) {
+      if (D.h_gstart[g + 1] - D.h_gstart[g] != s0) product0 = false;
+      else product0 = std::memcmp(beta + D.h_gstart[g], beta, s0 * sizeof(uint64_t)) == 0;
+    }
+    for (int64_t k = 1; k < s0 && product0; ++k) product0 = beta[k - 1] < beta[k];
+  }
+  bool ascending = !product0;
+  if (product0) {
+    const int64_t s0 = D.h_gstart[1];
+    ubeta.assign(beta, beta + s0);
+    for (int64_t i = 0; i < nd; ++i) brank[i] = (int32_t)(i % s0);
+    D.product = true;
+  }
   for (int64_t g = 0; g < G && ascending; ++g)
     for (int64_t i = D.h_gstart[g] + 1; i < D.h_gstart[g + 1]; ++i)
       if (!(beta[i - 1] < beta[i])) {
         ascending = false;
         break;
       }
-  if (ascending) {
+  if (product0) {
+    // ranks set above
+  } else if (ascending) {
     ubeta.assign(beta, beta + nd);
     std::sort(ubeta.begin(), ubeta.end());
     ubeta.erase(std::unique(ubeta.begin(), ubeta.end()), ubeta.end());

@@ -101,6 +101,7 @@ struct Context {
   bool have_ints = false;
   DetSpace dets;
   bool have_dets = false;
+  int fci_shape[3] = {-1, -1, -1};  // (norb, n_alpha, n_beta) when the dets are that complete space
   Hcsr H;
   DavidsonWork dav;
   DirectSigma* direct = nullptr;  // recompute-on-the-fly operator (complete spaces)

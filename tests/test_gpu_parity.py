@@ -272,3 +272,18 @@ def test_operator_layouts(ctx, oracle, pkg, capi):
     ctx.set_dets(a, b)
     ctx.build_direct_sigma()
     assert ctx.operator_layout()[0] == capi.OP_DIRECT
+
+
+def test_casci_reuses_the_complete_space(ctx, oracle, pkg):
+    """Repeated qdkgb_casci calls of one shape keep the determinant space;
+    new integrals, a different shape or an explicit set_dets rebuild what
+    they must."""
+    for seed, (norb, na) in [(21, (8, 4)), (22, (8, 4)), (23, (6, 3)), (24, (8, 4))]:
+        T, V, _ = pkg.integrals.synthetic_integrals(norb, 2 * norb, seed)
+        a, b = pkg.determinants.fci_space(norb, na, na)
+        Eo, _, _ = oracle.build_csr(oracle.Hamiltonian(T, V), a, b).selected_ci_diag(tol=1e-10)
+        E, C, _ = ctx.casci(T, V, na, na, tol=1e-9)
+        assert abs(E - Eo) < 1e-9, (seed, E, Eo)
+        if seed == 22:
+            # a selected list in between must not be mistaken for the space
+            ctx.set_dets(a[:100], b[:100])
