@@ -341,7 +341,9 @@ def run_ours(args):
         if i > 0:
             e2e_times.append(time.perf_counter() - t0)
     ctx_e2e.close()
-    h2d = T.nbytes + V.nbytes + 2 * N * 8
+    # per call: the integrals in (the complete space of an unchanged shape
+    # stays on the device), the energy and CI vector out
+    h2d = T.nbytes + V.nbytes
     d2h = N * 8 + 8
 
     cb = None
