@@ -30,9 +30,10 @@
 namespace qdkgb {
 
 constexpr int kListAlphaDouble = 2047;       // beta-list index meaning "b itself"
-constexpr size_t kSlabSmemMax = 200 * 1024;  // staged x + segment record per CTA
+constexpr size_t kSlabSmemMax = 110 * 1024;  // staged x + segment record per CTA (two CTAs per SM)
 constexpr int kSlabUnroll = 8;               // independent value loads in flight per thread
-constexpr int kSlabThreads = 1024;           // sigma CTA size (one CTA per SM)
+constexpr int kSlabThreads = 512;            // sigma CTA size at most; a group's beta strings are split
+                                             // over ceil(Nb / 512) CTAs (grid.z)
 constexpr int kEmitSegments = 4;             // position ranges per group in emission / export
 
 // Sigma work split for one staged-x element size: CTA per (group, segment);
@@ -201,13 +202,16 @@ void build_struct(Context* c) {
     auto smem_of = [&](int M, int R) { return (size_t)M * Nb * xsize + ((size_t)R * 4 + 15) / 16 * 16; };
     int best_S = -1, best_M = 0, best_R = 0;
     double best = -1.;
-    const int threads = std::min<int64_t>(kSlabThreads, (Nb + 31) / 32 * 32);
+    const int bz = (int)((Nb + kSlabThreads - 1) / kSlabThreads);
+    const int threads = (int)(((Nb + bz - 1) / bz + 31) / 32 * 32);
     for (int S = 1; S <= kMaxS && S <= rowlen; ++S) {
       const int M = shapeM[S], R = shapeR[S];
       const size_t sm = smem_of(M, R);
       if (sm > kSlabSmemMax) continue;
-      const int64_t per_sm = std::max<int64_t>(1, std::min<int64_t>(2048 / threads, (227 * 1024) / (int64_t)sm));
-      const int64_t slots = per_sm * c->sm_count, n_items = G * S;
+      // resident CTAs per SM: threads, 64 registers per thread, shared memory
+      const int64_t per_sm = std::max<int64_t>(
+          1, std::min<int64_t>(std::min<int64_t>(2048 / threads, 65536 / (64 * threads)), (227 * 1024) / (int64_t)sm));
+      const int64_t slots = per_sm * c->sm_count, n_items = G * S * bz;
       const double eff = (double)n_items / (double)(((n_items + slots - 1) / slots) * slots);
       const double score = eff - 0.01 * S;
       if (score > best) {
@@ -319,7 +323,12 @@ struct PlanArgs {
   const int32_t* segh;
 };
 
-unsigned slab_threads(int Nb) { return (unsigned)std::min(kSlabThreads, (Nb + 31) / 32 * 32); }
+// CTA size and beta-range split of a group: bz CTAs of slab_threads each
+unsigned slab_bz(int Nb) { return (unsigned)((Nb + kSlabThreads - 1) / kSlabThreads); }
+unsigned slab_threads(int Nb) {
+  const int bz = (int)slab_bz(Nb);
+  return (unsigned)(((Nb + bz - 1) / bz + 31) / 32 * 32);
+}
 
 // ------------------------------------------------------------------ emission
 // CTA per (group, segment), a thread per beta string, positions in order.
@@ -497,8 +506,20 @@ struct SlabPol<2> {
   static __device__ __forceinline__ Out fin(Acc a) { return (double)a.s + (double)a.c; }
 };
 
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
+
 template <int MODE>
-__global__ void __launch_bounds__(kSlabThreads, 1)
+__global__ void __launch_bounds__(kSlabThreads, 2)
     k_slab_sigma(SlabArgs A, PlanArgs P, const void* __restrict__ vals, const float* __restrict__ vlo,
                  const void* __restrict__ xv, const float* __restrict__ xlo, void* __restrict__ yv,
                  int64_t part_stride, int64_t vstride, const int* __restrict__ active) {
@@ -536,18 +557,33 @@ __global__ void __launch_bounds__(kSlabThreads, 1)
   int32_t* rec = reinterpret_cast<int32_t*>(xs + (size_t)P.M * Nb);
   const int32_t* rg = P.rec + ((int64_t)g * P.S + s) * P.R;
   for (int i = threadIdx.x; i < P.R; i += blockDim.x) rec[i] = __ldg(rg + i);
+  // staging: every slice copy in flight at once (cp.async), then one wait
   const int32_t* sh = P.segh + ((int64_t)g * P.S + s) * P.M;
   for (int j = 0; j < P.M; ++j) {
     const int h = __ldg(sh + j);
     if (h < 0) continue;
-    for (int i = threadIdx.x; i < Nb; i += blockDim.x) xs[(size_t)j * Nb + i] = Pol::gx(xv, xlo, (int64_t)h * Nb + i);
+    for (int i = threadIdx.x; i < Nb; i += blockDim.x) {
+      const int64_t src = (int64_t)h * Nb + i;
+      Xs* dst = xs + (size_t)j * Nb + i;
+      if constexpr (MODE == 0) {
+        cp_async4(dst, (const float*)xv + src);
+      } else if constexpr (MODE == 1) {
+        cp_async8(dst, (const double*)xv + src);
+      } else {
+        cp_async4(&dst->x, (const float*)xv + src);
+        cp_async4(&dst->y, xlo + src);
+      }
+    }
   }
+  cp_async_wait_all();
   __syncthreads();
   const int has0 = rec[0], off0 = rec[1], sb0 = rec[2], n1b = rec[3];
   const int32_t* e1 = rec + 4;
   const int nd = rec[4 + 2 * n1b];
   const int32_t* e2 = rec + 6 + 2 * n1b;
-  for (int b = threadIdx.x; b < Nb; b += blockDim.x) {
+  // grid.z: the part of the group's beta strings this CTA owns
+  const int bend = min(Nb, (int)(blockIdx.z + 1) * (int)blockDim.x);
+  for (int b = blockIdx.z * blockDim.x + threadIdx.x; b < bend; b += blockDim.x) {
     const int64_t gbase = (int64_t)g * A.rowlen * Nb + b;  // slab index of (g, p = 0, b)
     const int32_t* lst = A.blT + b;
     Acc acc[U];
@@ -608,6 +644,149 @@ __global__ void __launch_bounds__(kSlabThreads, 1)
   }
 }
 
+// FP32 sigma, VEC adjacent beta strings per thread (Nb % VEC == 0): float4 /
+// float2 value loads (one 16- or 8-byte load per position covers VEC rows, a
+// warp reads 32 * 4 * VEC contiguous bytes of a position row), the beta-list
+// entries of the VEC rows in one vector load, the alpha doubles' x likewise.
+// Same work split, staging and summation structure as k_slab_sigma<0>.
+template <int VEC>
+struct VecT;
+template <>
+struct VecT<4> {
+  using F = float4;
+  using I = int4;
+  static __device__ __forceinline__ float at(const float4& v, int c) {
+    return c == 0 ? v.x : (c == 1 ? v.y : (c == 2 ? v.z : v.w));
+  }
+  static __device__ __forceinline__ int at(const int4& v, int c) {
+    return c == 0 ? v.x : (c == 1 ? v.y : (c == 2 ? v.z : v.w));
+  }
+};
+template <>
+struct VecT<2> {
+  using F = float2;
+  using I = int2;
+  static __device__ __forceinline__ float at(const float2& v, int c) { return c == 0 ? v.x : v.y; }
+  static __device__ __forceinline__ int at(const int2& v, int c) { return c == 0 ? v.x : v.y; }
+};
+
+constexpr int kSlabVecThreads = 256;
+
+template <int VEC>
+__global__ void __launch_bounds__(kSlabVecThreads)
+    k_slab_sigma32v(SlabArgs A, PlanArgs P, const float* __restrict__ vals, const float* __restrict__ xv,
+                    float* __restrict__ yv, int64_t part_stride, int64_t vstride, const int* __restrict__ active) {
+  using VT = VecT<VEC>;
+  using F = typename VT::F;
+  using I = typename VT::I;
+  constexpr int U = 4;  // positions in flight per thread (U * VEC values)
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int Nb = A.Nb;
+  const int g = blockIdx.x / P.S, s = blockIdx.x - g * P.S;
+  const int inst = blockIdx.y;
+  if (active && !active[inst]) return;
+  const int64_t n = (int64_t)A.G * Nb;
+  vals += inst * vstride;
+  xv += inst * n;
+  yv += inst * n;
+  float* xs = reinterpret_cast<float*>(smem_raw);
+  int32_t* rec = reinterpret_cast<int32_t*>(xs + (size_t)P.M * Nb);
+  const int32_t* rg = P.rec + ((int64_t)g * P.S + s) * P.R;
+  for (int i = threadIdx.x; i < P.R; i += blockDim.x) rec[i] = __ldg(rg + i);
+  const int32_t* sh = P.segh + ((int64_t)g * P.S + s) * P.M;
+  for (int j = 0; j < P.M; ++j) {
+    const int h = __ldg(sh + j);
+    if (h < 0) continue;
+    for (int i = threadIdx.x; i < Nb; i += blockDim.x) cp_async4(xs + (size_t)j * Nb + i, xv + (int64_t)h * Nb + i);
+  }
+  cp_async_wait_all();
+  __syncthreads();
+  const int has0 = rec[0], off0 = rec[1], sb0 = rec[2], n1b = rec[3];
+  const int32_t* e1 = rec + 4;
+  const int nd = rec[4 + 2 * n1b];
+  const int32_t* e2 = rec + 6 + 2 * n1b;
+  const int nvec = Nb / VEC;
+  for (int t = blockIdx.z * blockDim.x + threadIdx.x; t < nvec; t += gridDim.z * blockDim.x) {
+    const int b0 = t * VEC;
+    // row (g, b0 .. b0+VEC-1): vector index of (p = 0) and the beta-list base
+    const F* vb = reinterpret_cast<const F*>(vals + (int64_t)g * A.rowlen * Nb + b0);
+    const I* lb = reinterpret_cast<const I*>(A.blT + b0);
+    const int nv = Nb / VEC;  // vector stride of one position row / list row
+    float acc[VEC];
+#pragma unroll
+    for (int c = 0; c < VEC; ++c) acc[c] = 0.f;
+    if (has0) {
+      const int ov = off0 / VEC;
+      int k = 0;
+      for (; k + U <= A.n2; k += U) {
+        F v[U];
+        I l[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          v[u] = __ldcs(vb + ov + (k + u) * nv);
+          l[u] = __ldg(lb + (k + u) * nv);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+#pragma unroll
+          for (int c = 0; c < VEC; ++c) acc[c] = fmaf(VT::at(v[u], c), xs[sb0 + VT::at(l[u], c)], acc[c]);
+      }
+      for (; k < A.n2; ++k) {
+        const F v = __ldcs(vb + ov + k * nv);
+        const I l = __ldg(lb + k * nv);
+#pragma unroll
+        for (int c = 0; c < VEC; ++c) acc[c] = fmaf(VT::at(v, c), xs[sb0 + VT::at(l, c)], acc[c]);
+      }
+    }
+    for (int k = 0; k < A.n1; ++k) {
+      const I l = __ldg(lb + (A.n2 + k) * nv);
+      const int kk = k * nv;
+      int e = 0;
+      for (; e + U <= n1b; e += U) {
+        F v[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) v[u] = __ldcs(vb + e1[2 * (e + u)] / VEC + kk);
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int sb = e1[2 * (e + u) + 1];
+#pragma unroll
+          for (int c = 0; c < VEC; ++c) acc[c] = fmaf(VT::at(v[u], c), xs[sb + VT::at(l, c)], acc[c]);
+        }
+      }
+      for (; e < n1b; ++e) {
+        const F v = __ldcs(vb + e1[2 * e] / VEC + kk);
+        const int sb = e1[2 * e + 1];
+#pragma unroll
+        for (int c = 0; c < VEC; ++c) acc[c] = fmaf(VT::at(v, c), xs[sb + VT::at(l, c)], acc[c]);
+      }
+    }
+    {
+      const F* xvv = reinterpret_cast<const F*>(xv + b0);
+      int j0 = 0;
+      for (; j0 + U <= nd; j0 += U) {
+        F v[U], xx[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          v[u] = __ldcs(vb + e2[2 * (j0 + u)] / VEC);
+          xx[u] = __ldg(xvv + e2[2 * (j0 + u) + 1] / VEC);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+#pragma unroll
+          for (int c = 0; c < VEC; ++c) acc[c] = fmaf(VT::at(v[u], c), VT::at(xx[u], c), acc[c]);
+      }
+      for (; j0 < nd; ++j0) {
+        const F v = __ldcs(vb + e2[2 * j0] / VEC);
+        const F xx = __ldg(xvv + e2[2 * j0 + 1] / VEC);
+#pragma unroll
+        for (int c = 0; c < VEC; ++c) acc[c] = fmaf(VT::at(v, c), VT::at(xx, c), acc[c]);
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < VEC; ++c) yv[s * part_stride + (int64_t)g * Nb + b0 + c] = acc[c];
+  }
+}
+
 template <typename T>
 __global__ void k_slab_combine(int64_t n, int S, const T* __restrict__ part, T* __restrict__ y) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -630,6 +809,12 @@ void slab_sigma(Context* c, int B, const int* active, const void* vals, const fl
   if (configured_dev != c->device) {
     QDKGB_CUDA(cudaFuncSetAttribute(k_slab_sigma<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)kSlabSmemMax));
+    if (MODE == 0) {
+      QDKGB_CUDA(cudaFuncSetAttribute(k_slab_sigma32v<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)kSlabSmemMax));
+      QDKGB_CUDA(cudaFuncSetAttribute(k_slab_sigma32v<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)kSlabSmemMax));
+    }
     configured_dev = c->device;
   }
   const int64_t n = F->G * F->Nb;
@@ -637,9 +822,28 @@ void slab_sigma(Context* c, int B, const int* active, const void* vals, const fl
   void* out = y;
   // partial sums [S][B][n], combined in segment order (deterministic)
   if (PL.S > 1) out = dev_alloc(c, F->ypart, (size_t)PL.S * B * n * sizeof(Out));
-  const dim3 grid((unsigned)(F->G * PL.S), (unsigned)B);
-  k_slab_sigma<MODE><<<grid, slab_threads((int)F->Nb), smem, c->stream>>>(slab_args(c), P, vals, vlo, x, xlo, out,
-                                                                          (int64_t)B * n, vstride, active);
+  const int Nb = (int)F->Nb;
+  const int vec = (MODE == 0 && ((uintptr_t)vals & 15) == 0 && ((uintptr_t)x & 15) == 0 &&
+                   ((uintptr_t)F->blT.ptr & 15) == 0)
+                      ? (Nb % 4 == 0 ? 4 : (Nb % 2 == 0 ? 2 : 1))
+                      : 1;
+  if (vec > 1) {
+    // vectorised FP32 sigma: VEC beta strings per thread
+    const int nvec = Nb / vec;
+    const unsigned thr = (unsigned)std::min(kSlabVecThreads, (nvec + 31) / 32 * 32);
+    const unsigned bz = (unsigned)((nvec + thr - 1) / thr);
+    const dim3 grid((unsigned)(F->G * PL.S), (unsigned)B, bz);
+    if (vec == 4)
+      k_slab_sigma32v<4><<<grid, thr, smem, c->stream>>>(slab_args(c), P, (const float*)vals, (const float*)x,
+                                                         (float*)out, (int64_t)B * n, vstride, active);
+    else
+      k_slab_sigma32v<2><<<grid, thr, smem, c->stream>>>(slab_args(c), P, (const float*)vals, (const float*)x,
+                                                         (float*)out, (int64_t)B * n, vstride, active);
+  } else {
+    const dim3 grid((unsigned)(F->G * PL.S), (unsigned)B, slab_bz(Nb));
+    k_slab_sigma<MODE><<<grid, slab_threads(Nb), smem, c->stream>>>(slab_args(c), P, vals, vlo, x, xlo, out,
+                                                                    (int64_t)B * n, vstride, active);
+  }
   QDKGB_CHECK_LAUNCH();
   if (PL.S > 1) {
     const int64_t tot = (int64_t)B * n;
