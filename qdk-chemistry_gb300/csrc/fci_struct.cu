@@ -31,7 +31,9 @@ namespace qdkgb {
 
 constexpr int kListAlphaDouble = 2047;       // beta-list index meaning "b itself"
 constexpr size_t kSlabSmemMax = 110 * 1024;  // staged x + segment record per CTA (two CTAs per SM)
+constexpr size_t kSlabPlanMax[2] = {32 * 1024, kSlabSmemMax};  // per plan: 4-byte (FP32) x, 8-byte x
 constexpr int kSlabUnroll = 8;               // independent value loads in flight per thread
+constexpr int kSlabVecThreads = 256;         // vectorised FP32 sigma: CTA size at most
 constexpr int kSlabThreads = 512;            // sigma CTA size at most; a group's beta strings are split
                                              // over ceil(Nb / 512) CTAs (grid.z)
 constexpr int kEmitSegments = 4;             // position ranges per group in emission / export
@@ -202,12 +204,22 @@ void build_struct(Context* c) {
     auto smem_of = [&](int M, int R) { return (size_t)M * Nb * xsize + ((size_t)R * 4 + 15) / 16 * 16; };
     int best_S = -1, best_M = 0, best_R = 0;
     double best = -1.;
-    const int bz = (int)((Nb + kSlabThreads - 1) / kSlabThreads);
-    const int threads = (int)(((Nb + bz - 1) / bz + 31) / 32 * 32);
+    // CTA shape of the sigma that uses the plan (the FP32 one is vectorised
+    // over 4 or 2 beta strings when Nb allows)
+    const int vec = pl == 0 ? (Nb % 4 == 0 ? 4 : (Nb % 2 == 0 ? 2 : 1)) : 1;
+    int bz, threads;
+    if (vec > 1) {
+      const int nvec = (int)(Nb / vec);
+      threads = std::min(kSlabVecThreads, (nvec + 31) / 32 * 32);
+      bz = (nvec + threads - 1) / threads;
+    } else {
+      bz = (int)((Nb + kSlabThreads - 1) / kSlabThreads);
+      threads = (int)(((Nb + bz - 1) / bz + 31) / 32 * 32);
+    }
     for (int S = 1; S <= kMaxS && S <= rowlen; ++S) {
       const int M = shapeM[S], R = shapeR[S];
       const size_t sm = smem_of(M, R);
-      if (sm > kSlabSmemMax) continue;
+      if (sm > kSlabPlanMax[pl]) continue;
       // resident CTAs per SM: threads, 64 registers per thread, shared memory
       const int64_t per_sm = std::max<int64_t>(
           1, std::min<int64_t>(std::min<int64_t>(2048 / threads, 65536 / (64 * threads)), (227 * 1024) / (int64_t)sm));
@@ -669,8 +681,6 @@ struct VecT<2> {
   static __device__ __forceinline__ float at(const float2& v, int c) { return c == 0 ? v.x : v.y; }
   static __device__ __forceinline__ int at(const int2& v, int c) { return c == 0 ? v.x : v.y; }
 };
-
-constexpr int kSlabVecThreads = 256;
 
 template <int VEC>
 __global__ void __launch_bounds__(kSlabVecThreads)
