@@ -200,4 +200,41 @@ __device__ __forceinline__ void ff_prod(float h, float l, float x, float y, floa
   e = fmaf(h, y, fmaf(l, x, e));
 }
 
+// (hi, lo) = (fl32(v), fl32(v - fl32(v))), both round-to-nearest-even: the
+// split storage of an FP64 value.  On the integer pipes for |v| in
+// [2^-74, 2^127) (the FP64 pipe is narrow on GB300): the 53-bit significand is
+// rounded to 24 bits by hand, and the exact remainder (at most 29 bits) is
+// converted and scaled by a power of two.  Zeros, tiny and huge values, NaN
+// and Inf take the FP64 conversions.  Bit-identical to the FP64 form.
+__device__ __forceinline__ void split_f64(double v, float& hi, float& lo) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(v);
+  const unsigned int sign = (unsigned int)(u >> 32) & 0x80000000u;
+  const int e = (int)((u >> 52) & 0x7ff) - 1023;
+  if ((u << 1) == 0) {
+    hi = __uint_as_float(sign);
+    lo = 0.f;
+    return;
+  }
+  if (e < -74 || e > 126) {
+    const float h = __double2float_rn(v);
+    hi = h;
+    lo = __double2float_rn(v - (double)h);
+    return;
+  }
+  const unsigned long long M = (u & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+  unsigned int q = (unsigned int)(M >> 29);
+  const unsigned int r = (unsigned int)(M & 0x1FFFFFFFu);
+  const bool up = r > 0x10000000u || (r == 0x10000000u && (q & 1u));
+  const int res = up ? (int)r - (1 << 29) : (int)r;  // v - hi in units of 2^(e - 52)
+  q += up ? 1u : 0u;
+  int eh = e;
+  if (q == (1u << 24)) {
+    q >>= 1;
+    ++eh;
+  }
+  hi = __uint_as_float(sign | ((unsigned int)(eh + 127) << 23) | (q & 0x7FFFFFu));
+  const float lf = __int2float_rn(res) * __uint_as_float((unsigned int)(e - 52 + 127) << 23);
+  lo = res == 0 ? 0.f : (sign ? -lf : lf);
+}
+
 }  // namespace qdkgb

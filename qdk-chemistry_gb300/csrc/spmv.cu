@@ -107,10 +107,10 @@ __global__ void __launch_bounds__(kSpmvWarps * 32)
 }
 __global__ void k_split_x(const double* __restrict__ x, float* __restrict__ xh, float* __restrict__ xl, int64_t n) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const double v = x[i];
-    const float h = __double2float_rn(v);
+    float h, l;
+    split_f64(x[i], h, l);
     xh[i] = h;
-    xl[i] = __double2float_rn(v - (double)h);
+    xl[i] = l;
   }
 }
 
