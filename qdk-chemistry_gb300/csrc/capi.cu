@@ -4,6 +4,8 @@
 #include <cmath>
 #include <cstring>
 #include <limits>
+#include <map>
+#include <mutex>
 #include <vector>
 
 #include "internal.h"
@@ -17,6 +19,19 @@ void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 static thread_local std::string g_context_free_err;
 void set_context_free_error(const std::string& msg) { g_context_free_err = msg; }
+
+void set_max_dynamic_smem(const void* func, int bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, int> done;
+  int dev = 0;
+  QDKGB_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(mu);
+  const auto key = std::make_pair(func, dev);
+  const auto it = done.find(key);
+  if (it != done.end() && it->second >= bytes) return;
+  QDKGB_CUDA(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  done[key] = bytes;
+}
 
 void* dev_alloc(Context* c, DeviceBuffer& b, size_t bytes) {
   if (b.ptr && b.bytes >= bytes) return b.ptr;

@@ -234,14 +234,7 @@ __global__ void __launch_bounds__(kEigThreads)
 void lowest_eig_batch(cudaStream_t st, int B, const int* kdev, int kadd, int kmax, const double* Hs, int ldh,
                       int64_t hstride, double* eval, double* evec, int64_t estride, const int* active) {
   if (kmax > kEigSmemK) throw Error(QDKGB_ERR_INVALID, "batched subspace larger than the shared-memory eigensolver");
-  static thread_local int configured_dev = -1;
-  int dev = 0;
-  QDKGB_CUDA(cudaGetDevice(&dev));
-  if (configured_dev != dev) {
-    QDKGB_CUDA(cudaFuncSetAttribute(k_lowest_eig_batch, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)kEigDynSmemMax));
-    configured_dev = dev;
-  }
+  set_max_dynamic_smem((const void*)k_lowest_eig_batch, (int)kEigDynSmemMax);
   k_lowest_eig_batch<<<B, kEigThreads, eig_dyn_smem(kmax), st>>>(kdev, kadd, Hs, ldh, hstride, eval, evec, estride,
                                                                  active);
   QDKGB_CHECK_LAUNCH();
@@ -389,12 +382,7 @@ void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C
   d.partial = dev_array<double>(c, W.partial, (size_t)d.nb * (kMaxSubspace + 2));
   d.small = dev_array<double>(c, W.small, 4 * kMaxSubspace);
   if (max_m + 1 > kEigSmemK) d.gA = dev_array<double>(c, W.yf, (size_t)(max_m + 1) * (max_m + 1));
-  static bool attr_set = false;
-  if (!attr_set) {
-    QDKGB_CUDA(cudaFuncSetAttribute(k_lowest_eig, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)kEigDynSmemMax));
-    attr_set = true;
-  }
+  set_max_dynamic_smem((const void*)k_lowest_eig, (int)kEigDynSmemMax);
   d.D = (double*)H.diag.ptr;
   d.clear_flag();
   float* xf = nullptr;

@@ -374,14 +374,8 @@ void build_direct_sigma(Context* c) {
   k_diag_product<<<blocks, 256, 0, c->stream>>>(integrals_view(c), S.ngroups, S.nbeta,
                                                (const uint64_t*)S.galpha.ptr, (const uint64_t*)S.ubeta.ptr, D);
   QDKGB_CHECK_LAUNCH();
-  static bool attr = false;
-  if (!attr) {
-    QDKGB_CUDA(cudaFuncSetAttribute(k_ds_opposite<double, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    200 * 1024));
-    QDKGB_CUDA(cudaFuncSetAttribute(k_ds_opposite<float, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    200 * 1024));
-    attr = true;
-  }
+  set_max_dynamic_smem((const void*)k_ds_opposite<double, 4>, 200 * 1024);
+  set_max_dynamic_smem((const void*)k_ds_opposite<float, 8>, 200 * 1024);
   QDKGB_CUDA(cudaStreamSynchronize(c->stream));
   H.n = N;
   H.nnz = 0;

@@ -815,17 +815,10 @@ void slab_sigma(Context* c, int B, const int* active, const void* vals, const fl
   using Pol = SlabPol<MODE>;
   using Out = typename Pol::Out;
   const size_t smem = (size_t)PL.M * F->Nb * sizeof(typename Pol::Xs) + ((size_t)PL.R * 4 + 15) / 16 * 16;
-  static thread_local int configured_dev = -1;
-  if (configured_dev != c->device) {
-    QDKGB_CUDA(cudaFuncSetAttribute(k_slab_sigma<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)kSlabSmemMax));
-    if (MODE == 0) {
-      QDKGB_CUDA(cudaFuncSetAttribute(k_slab_sigma32v<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)kSlabSmemMax));
-      QDKGB_CUDA(cudaFuncSetAttribute(k_slab_sigma32v<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)kSlabSmemMax));
-    }
-    configured_dev = c->device;
+  set_max_dynamic_smem((const void*)k_slab_sigma<MODE>, (int)kSlabSmemMax);
+  if (MODE == 0) {
+    set_max_dynamic_smem((const void*)k_slab_sigma32v<4>, (int)kSlabSmemMax);
+    set_max_dynamic_smem((const void*)k_slab_sigma32v<2>, (int)kSlabSmemMax);
   }
   const int64_t n = F->G * F->Nb;
   const int64_t vstride = n * F->rowlen;

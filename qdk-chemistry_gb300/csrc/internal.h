@@ -45,6 +45,9 @@ struct DirectSigma;
 struct FciStruct;
 
 void count_launch();
+// cudaFuncAttributeMaxDynamicSharedMemorySize of a kernel on the current
+// device, raised to at least `bytes` (idempotent, thread-safe)
+void set_max_dynamic_smem(const void* func, int bytes);
 // message of the last failed call that takes no context (qdkgb_last_error(NULL))
 void set_context_free_error(const std::string& msg);
 

@@ -196,11 +196,7 @@ void rdms_spin_dep(Context* c, const double* C, double* aa, double* bb, double* 
   const bool use_shared = n <= 16;
   int s_step = use_shared ? (int)std::min<size_t>((size_t)n, (smem_cap - n2 * 8) / slice) : n;
   if (s_step < 1) s_step = 1;
-  static bool attr = false;
-  if (!attr) {
-    QDKGB_CUDA(cudaFuncSetAttribute(k_rdm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cap));
-    attr = true;
-  }
+  set_max_dynamic_smem((const void*)k_rdm, (int)smem_cap);
   const int64_t blocks = std::min<int64_t>((N + kRdmWarps - 1) / kRdmWarps, (int64_t)c->sm_count * (use_shared ? 1 : 4));
   double* outs4[3] = {aaaa, bbbb, aabb};
   double* outs2[3] = {aa, bb, nullptr};
