@@ -30,25 +30,120 @@
 
 namespace qdkgb {
 
-constexpr int kDotBlocksPerSm = 2;
 constexpr int kMaxSubspace = 256;
+// Row-parallel vector kernels: 256 threads, two rows per thread per step
+// (rows i and i + 256 of a 512-row tile), grids of kVecBlocksPerSm blocks per
+// SM striding over the tiles.  Every row sum runs over the columns in order,
+// so a row's value does not depend on the launch shape.
+constexpr int kVecThreads = 256;
+constexpr int kVecTile = 2 * kVecThreads;
+constexpr int kVecBlocksPerSm = 4;
+constexpr int kDotCols = 8;  // columns per block of k_multidot (one per warp in its final sum)
+constexpr int kDotChunks = (kMaxSubspace + 2 + kDotCols - 1) / kDotCols;
 
-// partial[j * nb + blk] = sum over this block's rows of A[:, j] . w
-__global__ void k_multidot(const double* __restrict__ A, int64_t lda, int k, const double* __restrict__ w, int64_t n,
-                           double* __restrict__ partial) {
-  __shared__ double red[32];
-  const int j = blockIdx.y;
-  const double* a = A + (size_t)j * lda;
-  double s = 0.;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    s += a[i] * w[i];
-  s = warp_sum(s);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+// Sum of v over the block, valid in thread 0 (red: kVecThreads/32 doubles).
+__device__ __forceinline__ double block_sum_vec(double v, double* red) {
+  v = warp_sum(v);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
   __syncthreads();
+  double t = 0.;
   if (threadIdx.x < 32) {
-    double t = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.;
+    t = (threadIdx.x < (kVecThreads >> 5)) ? red[threadIdx.x] : 0.;
     t = warp_sum(t);
-    if (threadIdx.x == 0) partial[(size_t)j * gridDim.x + blockIdx.x] = t;
+  }
+  return t;
+}
+
+// Called by every thread after this block stored its partial sums: true in
+// the block that finished last (count[slot] is then reset for the next
+// launch).  Its reads of the other blocks' partials go through L2 (__ldcg).
+__device__ __forceinline__ bool last_block_done(unsigned* count, int slot, unsigned nblocks) {
+  __shared__ bool last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    last = atomicAdd(count + slot, 1u) == nblocks - 1;
+    if (last) count[slot] = 0u;
+  }
+  __syncthreads();
+  if (last) __threadfence();
+  return last;
+}
+
+// out[j * out_stride] = A[:, j] . w for j < k.  Block (x, y) takes columns
+// y*kDotCols .. +kDotCols over a grid-stride share of the rows, so w is read
+// once per column block; partial sums go to partial[j * gridDim.x + x] and the
+// block of column block y that finishes last adds them in block order (the
+// result does not depend on the order in which blocks run).  self_out, when
+// given, receives w . w as well (partial row k); a non-zero *skip makes the
+// launch a no-op.
+__global__ void __launch_bounds__(kVecThreads)
+    k_multidot(const double* __restrict__ A, int64_t lda, int k, const double* __restrict__ w, int64_t n,
+               double* __restrict__ partial, unsigned* __restrict__ count, double* __restrict__ out, int out_stride,
+               double* __restrict__ self_out, const double* __restrict__ skip) {
+  if (skip && *skip != 0.) return;
+  __shared__ double red[kVecThreads / 32][kDotCols + 1];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int j0 = blockIdx.y * kDotCols;
+  const int nc = min(kDotCols, k - j0);
+  const double* a = A + (size_t)j0 * lda;
+  const bool self = self_out && blockIdx.y == 0;
+  double acc[kDotCols];
+#pragma unroll
+  for (int c = 0; c < kDotCols; ++c) acc[c] = 0.;
+  double accw = 0.;
+  const int64_t step = (int64_t)gridDim.x * kVecTile;
+  for (int64_t i = (int64_t)blockIdx.x * kVecTile + threadIdx.x; i < n; i += step) {
+    const int64_t i1 = i + kVecThreads;
+    const bool has1 = i1 < n;
+    const double w0 = w[i], w1 = has1 ? w[i1] : 0.;
+    if (self) accw = fma(w1, w1, fma(w0, w0, accw));
+#pragma unroll
+    for (int c = 0; c < kDotCols; ++c) {
+      if (c < nc) {
+        const double a0 = a[i + (size_t)c * lda];
+        const double a1 = has1 ? a[i1 + (size_t)c * lda] : 0.;
+        acc[c] = fma(a0, w0, acc[c]);
+        acc[c] = fma(a1, w1, acc[c]);
+      }
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < kDotCols; ++c) {
+    if (c < nc) {
+      const double t = warp_sum(acc[c]);
+      if (lane == 0) red[wid][c] = t;
+    }
+  }
+  if (self) {
+    const double t = warp_sum(accw);
+    if (lane == 0) red[wid][kDotCols] = t;
+  }
+  __syncthreads();
+  if (threadIdx.x < nc) {
+    double t = 0.;
+    for (int q = 0; q < kVecThreads / 32; ++q) t += red[q][threadIdx.x];
+    partial[(size_t)(j0 + threadIdx.x) * gridDim.x + blockIdx.x] = t;
+  }
+  if (self && threadIdx.x == kDotCols) {
+    double t = 0.;
+    for (int q = 0; q < kVecThreads / 32; ++q) t += red[q][kDotCols];
+    partial[(size_t)k * gridDim.x + blockIdx.x] = t;
+  }
+  if (!last_block_done(count, blockIdx.y, gridDim.x)) return;
+  if (wid < nc) {
+    const double* p = partial + (size_t)(j0 + wid) * gridDim.x;
+    double t = 0.;
+    for (int b = lane; b < (int)gridDim.x; b += 32) t += __ldcg(p + b);
+    t = warp_sum(t);
+    if (lane == 0) out[(size_t)(j0 + wid) * out_stride] = t;
+  }
+  if (self && wid == kVecThreads / 32 - 1) {
+    const double* p = partial + (size_t)k * gridDim.x;
+    double t = 0.;
+    for (int b = lane; b < (int)gridDim.x; b += 32) t += __ldcg(p + b);
+    t = warp_sum(t);
+    if (lane == 0) *self_out = t;
   }
 }
 // out[j * out_stride] = sum_b partial[j * nb + b], fixed order; one warp per j
@@ -61,28 +156,95 @@ __global__ void k_reduce_partials(const double* __restrict__ partial, int nb, in
   s = warp_sum(s);
   if (lane == 0) out[(size_t)j * out_stride] = s;
 }
-// w -= A[:, 0:k] * coef
-__global__ void k_sub_gemv(const double* __restrict__ A, int64_t lda, int k, const double* __restrict__ coef,
-                           double* __restrict__ w, int64_t n) {
-  __shared__ double c[kMaxSubspace + 2];
-  for (int j = threadIdx.x; j < k; j += blockDim.x) c[j] = coef[j];
-  __syncthreads();
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    double s = 0.;
-    for (int j = 0; j < k; ++j) s += A[i + (size_t)j * lda] * c[j];
-    w[i] -= s;
-  }
-}
-// y = A[:, 0:k] * coef (coef strided)
-__global__ void k_gemv(const double* __restrict__ A, int64_t lda, int k, const double* __restrict__ coef,
-                       int coef_stride, double* __restrict__ y, int64_t n) {
+// y = A[:, 0:k] coef (SUB: y -= A[:, 0:k] coef), coef strided; each row sums
+// over j in order, four columns' loads in flight per row.  A non-zero *skip
+// makes the launch a no-op.  skip_out, when given, receives the selective
+// reorthogonalisation test of a Gram-Schmidt pass (coef = V^T y for
+// orthonormal V, *w2 = |y|^2 before it): 1 when |y - V coef|^2 = *w2 - |coef|^2
+// keeps at least half of *w2 (a second pass is not needed), else 0.
+template <bool SUB>
+__global__ void __launch_bounds__(kVecThreads)
+    k_gemv_rows(const double* __restrict__ A, int64_t lda, int k, const double* __restrict__ coef, int coef_stride,
+                double* __restrict__ y, int64_t n, const double* __restrict__ skip = nullptr,
+                const double* __restrict__ w2 = nullptr, double* __restrict__ skip_out = nullptr) {
+  if (skip && *skip != 0.) return;
   __shared__ double c[kMaxSubspace + 2];
   for (int j = threadIdx.x; j < k; j += blockDim.x) c[j] = coef[(size_t)j * coef_stride];
   __syncthreads();
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    double s = 0.;
-    for (int j = 0; j < k; ++j) s += A[i + (size_t)j * lda] * c[j];
-    y[i] = s;
+  if (skip_out && blockIdx.x == 0 && threadIdx.x == 0) {
+    double cc = 0.;
+    for (int j = 0; j < k; ++j) cc += c[j] * c[j];
+    *skip_out = (*w2 - cc >= 0.5 * *w2) ? 1. : 0.;
+  }
+  const int64_t step = (int64_t)gridDim.x * kVecTile;
+  for (int64_t i = (int64_t)blockIdx.x * kVecTile + threadIdx.x; i < n; i += step) {
+    const int64_t i1 = i + kVecThreads;
+    const bool has1 = i1 < n;
+    double s0 = 0., s1 = 0.;
+    int j = 0;
+    for (; j + 4 <= k; j += 4) {
+      double a0[4], a1[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        a0[q] = A[i + (size_t)(j + q) * lda];
+        a1[q] = has1 ? A[i1 + (size_t)(j + q) * lda] : 0.;
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        s0 = fma(a0[q], c[j + q], s0);
+        s1 = fma(a1[q], c[j + q], s1);
+      }
+    }
+    for (; j < k; ++j) {
+      s0 = fma(A[i + (size_t)j * lda], c[j], s0);
+      if (has1) s1 = fma(A[i1 + (size_t)j * lda], c[j], s1);
+    }
+    if (SUB) {
+      y[i] -= s0;
+      if (has1) y[i1] -= s1;
+    } else {
+      y[i] = s0;
+      if (has1) y[i1] = s1;
+    }
+  }
+}
+// Y[:, o] = A[:, 0:k] Q[:, o] for o < nout <= kMaxOut (Q column-major, ld k):
+// the thick restart's new basis in one pass over A; each output's row sum runs
+// over j in order (the same value as k_gemv_rows on that column of Q).
+constexpr int kMaxOut = 8;
+__global__ void __launch_bounds__(kVecThreads)
+    k_gemv_multi(const double* __restrict__ A, int64_t lda, int k, const double* __restrict__ Q, int nout,
+                 double* __restrict__ Y, int64_t ldy, int64_t n) {
+  __shared__ double q[kMaxSubspace + 2][kMaxOut];
+  for (int t = threadIdx.x; t < k * kMaxOut; t += blockDim.x) {
+    const int j = t / kMaxOut, o = t % kMaxOut;
+    q[j][o] = o < nout ? Q[(size_t)o * k + j] : 0.;
+  }
+  __syncthreads();
+  for (int64_t i = (int64_t)blockIdx.x * kVecThreads + threadIdx.x; i < n; i += (int64_t)gridDim.x * kVecThreads) {
+    double acc[kMaxOut];
+#pragma unroll
+    for (int o = 0; o < kMaxOut; ++o) acc[o] = 0.;
+    int j = 0;
+    for (; j + 4 <= k; j += 4) {
+      double a[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) a[u] = A[i + (size_t)(j + u) * lda];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int o = 0; o < kMaxOut; ++o)
+          if (o < nout) acc[o] = fma(a[u], q[j + u][o], acc[o]);
+    }
+    for (; j < k; ++j) {
+      const double a = A[i + (size_t)j * lda];
+#pragma unroll
+      for (int o = 0; o < kMaxOut; ++o)
+        if (o < nout) acc[o] = fma(a, q[j][o], acc[o]);
+    }
+#pragma unroll
+    for (int o = 0; o < kMaxOut; ++o)
+      if (o < nout) Y[i + (size_t)o * ldy] = acc[o];
   }
 }
 // w *= 1/sqrt(*nrm2) when sqrt(*nrm2) > min_norm, else raise *flag
@@ -96,45 +258,85 @@ __global__ void k_normalize(double* w, int64_t n, const double* nrm2, double min
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     w[i] *= sc;
 }
-// X = V C0, R = AV C0 - lam0 X; partial sums of R^2
-__global__ void k_ritz_residual(const double* __restrict__ V, const double* __restrict__ AV, int64_t ld, int k,
-                                const double* __restrict__ C0, const double* __restrict__ lam, double* __restrict__ X,
-                                double* __restrict__ R, int64_t n, double* __restrict__ partial) {
+// diagonal preconditioner of one element: -r / (D - lam0) with |D - lam0|
+// clamped to min_abs (davidson.hpp:352-361)
+__device__ __forceinline__ double precondition_one(double r, double d, double min_abs) {
+  if (fabs(d) < min_abs) d = (d >= 0) ? min_abs : -min_abs;
+  return -r / d;
+}
+// X = V C0, R = AV C0 - lam0 X, *out = |R|^2 (partial sums per block, the
+// last block adds them in block order).  With D, R is stored preconditioned
+// (the residual itself is not needed again once its norm is known).
+__global__ void __launch_bounds__(kVecThreads)
+    k_ritz_residual(const double* __restrict__ V, const double* __restrict__ AV, int64_t ld, int k,
+                    const double* __restrict__ C0, const double* __restrict__ lam, double* __restrict__ X,
+                    double* __restrict__ R, int64_t n, const double* __restrict__ D, double min_abs,
+                    double* __restrict__ partial, unsigned* __restrict__ count, double* __restrict__ out) {
   __shared__ double c[kMaxSubspace + 2];
-  __shared__ double red[32];
+  __shared__ double red[kVecThreads / 32];
   for (int j = threadIdx.x; j < k; j += blockDim.x) c[j] = C0[j];
   __syncthreads();
   const double l0 = lam[0];
   double s2 = 0.;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    double x = 0., ax = 0.;
-    for (int j = 0; j < k; ++j) {
-      x += V[i + (size_t)j * ld] * c[j];
-      ax += AV[i + (size_t)j * ld] * c[j];
+  const int64_t step = (int64_t)gridDim.x * kVecTile;
+  for (int64_t i = (int64_t)blockIdx.x * kVecTile + threadIdx.x; i < n; i += step) {
+    const int64_t i1 = i + kVecThreads;
+    const bool has1 = i1 < n;
+    double x0 = 0., ax0 = 0., x1 = 0., ax1 = 0.;
+    int j = 0;
+    for (; j + 4 <= k; j += 4) {
+      double v0[4], v1[4], w0[4], w1[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const size_t o = (size_t)(j + q) * ld;
+        v0[q] = V[i + o];
+        w0[q] = AV[i + o];
+        v1[q] = has1 ? V[i1 + o] : 0.;
+        w1[q] = has1 ? AV[i1 + o] : 0.;
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        x0 = fma(v0[q], c[j + q], x0);
+        ax0 = fma(w0[q], c[j + q], ax0);
+        x1 = fma(v1[q], c[j + q], x1);
+        ax1 = fma(w1[q], c[j + q], ax1);
+      }
     }
-    const double r = ax - l0 * x;
-    X[i] = x;
-    R[i] = r;
-    s2 += r * r;
+    for (; j < k; ++j) {
+      const size_t o = (size_t)j * ld;
+      x0 = fma(V[i + o], c[j], x0);
+      ax0 = fma(AV[i + o], c[j], ax0);
+      if (has1) {
+        x1 = fma(V[i1 + o], c[j], x1);
+        ax1 = fma(AV[i1 + o], c[j], ax1);
+      }
+    }
+    const double r0 = ax0 - l0 * x0;
+    X[i] = x0;
+    R[i] = D ? precondition_one(r0, D[i] - l0, min_abs) : r0;
+    s2 += r0 * r0;
+    if (has1) {
+      const double r1 = ax1 - l0 * x1;
+      X[i1] = x1;
+      R[i1] = D ? precondition_one(r1, D[i1] - l0, min_abs) : r1;
+      s2 += r1 * r1;
+    }
   }
-  s2 = warp_sum(s2);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s2;
+  const double t = block_sum_vec(s2, red);
+  if (threadIdx.x == 0) partial[blockIdx.x] = t;
+  if (!last_block_done(count, kDotChunks, gridDim.x)) return;
+  double u = 0.;
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += kVecThreads) u += __ldcg(partial + b);
   __syncthreads();
-  if (threadIdx.x < 32) {
-    double t = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.;
-    t = warp_sum(t);
-    if (threadIdx.x == 0) partial[blockIdx.x] = t;
-  }
+  u = block_sum_vec(u, red);
+  if (threadIdx.x == 0) *out = u;
 }
 // R = -R / (D - lam0) with |D - lam0| clamped to min_abs (davidson.hpp:352-361)
 __global__ void k_precondition(double* R, const double* __restrict__ D, const double* lam, int64_t n,
                                double min_abs) {
   const double l0 = lam[0];
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    double d = D[i] - l0;
-    if (fabs(d) < min_abs) d = (d >= 0) ? min_abs : -min_abs;
-    R[i] = -R[i] / d;
-  }
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    R[i] = precondition_one(R[i], D[i] - l0, min_abs);
 }
 // r = s - e x, partial sums of r^2 (e = *eptr)
 __global__ void k_axpy_residual(const double* __restrict__ s, const double* __restrict__ x, const double* eptr,
@@ -192,17 +394,38 @@ __global__ void k_set_onehot(double* x, int64_t n, const int64_t* idx) {
 __global__ void k_set_value(double* p, double v) { *p = v; }
 // x <- (x + s x^T) / 2 for x viewed as an n x n matrix (coefficients C[Ia, Ib]
 // of a product space whose alpha and beta string lists coincide): projection
-// on the spin-flip sector of parity s
-__global__ void k_flip_project(double* x, int64_t n, double s) {
-  const int64_t total = n * n;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = t / n, j = t % n;
-    if (i < j) {
-      const double avg = 0.5 * (x[i * n + j] + s * x[j * n + i]);
-      x[i * n + j] = avg;
-      x[j * n + i] = s * avg;
-    } else if (i == j && s < 0) {
-      x[t] = 0.;
+// on the spin-flip sector of parity s.  Block (J, I), I <= J, owns the 32 x 32
+// tile pair P = x[I-tile, J-tile] and Q = x[J-tile, I-tile] (one tile when
+// I == J), staged in shared memory so both are read and written row-wise.
+constexpr int kFlipTile = 32;
+__global__ void __launch_bounds__(kFlipTile * 8) k_flip_project(double* x, int64_t n, double s) {
+  const int I = blockIdx.y, J = blockIdx.x;
+  if (I > J) return;
+  __shared__ double P[kFlipTile][kFlipTile + 1], Q[kFlipTile][kFlipTile + 1];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int64_t r0 = (int64_t)I * kFlipTile, c0 = (int64_t)J * kFlipTile;
+  for (int r = ty; r < kFlipTile; r += 8) {
+    const int64_t pr = r0 + r, pc = c0 + tx, qr = c0 + r, qc = r0 + tx;
+    P[r][tx] = (pr < n && pc < n) ? x[pr * n + pc] : 0.;
+    Q[r][tx] = (qr < n && qc < n) ? x[qr * n + qc] : 0.;
+  }
+  __syncthreads();
+  for (int r = ty; r < kFlipTile; r += 8) {
+    const int64_t pr = r0 + r, pc = c0 + tx, qr = c0 + r, qc = r0 + tx;
+    if (I < J) {
+      // element (pr, pc) has pr < pc: avg of it and its mirror Q[tx][r]
+      if (pr < n && pc < n) x[pr * n + pc] = 0.5 * (P[r][tx] + s * Q[tx][r]);
+      // element (qr, qc) = mirror of P[tx][r]: s * avg
+      if (qr < n && qc < n) x[qr * n + qc] = s * (0.5 * (P[tx][r] + s * Q[r][tx]));
+    } else if (pr < n && pc < n) {
+      double v;
+      if (r < tx)
+        v = 0.5 * (P[r][tx] + s * P[tx][r]);
+      else if (r > tx)
+        v = s * (0.5 * (P[tx][r] + s * P[r][tx]));
+      else
+        v = s < 0 ? 0. : P[r][tx];
+      x[pr * n + pc] = v;
     }
   }
 }
@@ -248,24 +471,34 @@ constexpr int kSlotRes = kMaxSubspace + 4;   // residual norm^2 (device reduce t
 constexpr int kSlotNrm = kMaxSubspace + 8;   // Gram-Schmidt norm^2
 constexpr int kSlotE = kMaxSubspace + 12;    // full-precision Rayleigh quotient
 constexpr int kSlotFlag = kMaxSubspace + 16; // Gram-Schmidt degeneracy flag
+constexpr int kSlotW2 = kMaxSubspace + 20;   // |w|^2 before a Gram-Schmidt pass
+constexpr int kSlotSkip = kMaxSubspace + 24; // selective second pass: 1 = not needed
 constexpr int kSlotIdx = 3 * kMaxSubspace;   // argmin index (int64)
+constexpr int kSlotCount = 3 * kMaxSubspace + 16;  // block-completion counters (unsigned, kDotChunks + 1)
 
 struct Dav {
   Context* c;
   int64_t n;
   int64_t maxm;
   double *V, *AV, *D, *X, *Hk, *evec, *eval, *partial, *small, *work;
-  int nb;
+  int nb;  // blocks of the row-parallel kernels (partial sums per column)
+  int sm_count;
   double* gA = nullptr;
   cudaStream_t st;
 
+  unsigned* counts() { return (unsigned*)(small + kSlotCount); }
+
   double* col(double* base, int64_t j) { return base + (size_t)j * n; }
 
-  void multidot(const double* A, int k, const double* w, double* out, int stride) {
-    dim3 g(nb, k);
-    k_multidot<<<g, 256, 0, st>>>(A, n, k, w, n, partial);
-    QDKGB_CHECK_LAUNCH();
-    k_reduce_partials<<<(k + 7) / 8, 256, 0, st>>>(partial, nb, k, out, stride);
+  // out[j * stride] = A[:, j] . w, j < k: column blocks of kDotCols on
+  // grid.y, the row split on grid.x shrunk as column blocks are added (down to
+  // one block per SM) so the grid stays near one resident wave
+  void multidot(const double* A, int k, const double* w, double* out, int stride, double* self_out = nullptr,
+                const double* skip = nullptr) {
+    const int chunks = (k + kDotCols - 1) / kDotCols;
+    const int bx = std::max(1, std::min(nb, std::max(sm_count, nb / chunks)));
+    k_multidot<<<dim3(bx, chunks), kVecThreads, 0, st>>>(A, n, k, w, n, partial, counts(), out, stride, self_out,
+                                                         skip);
     QDKGB_CHECK_LAUNCH();
   }
   void norm2(const double* w, double* out) { multidot(w, 1, w, out, 1); }
@@ -287,18 +520,33 @@ struct Dav {
   }
   void clear_flag() { QDKGB_CUDA(cudaMemsetAsync(small + kSlotFlag, 0, sizeof(double), st)); }
 
-  void orth_passes(int K, double* w) {
-    for (int pass = 0; pass < 2 && K > 0; ++pass) {
-      multidot(V, K, w, small, 1);
-      k_sub_gemv<<<nb, 256, 0, st>>>(V, n, K, small, w, n);
-      QDKGB_CHECK_LAUNCH();
+  // Two CGS passes against V[:, 0:K].  selective: the second pass only when
+  // the first removed more than half of |w|^2 (the Daniel-Gragg-Kaufman-
+  // Stewart test, decided on the device; the mixed path's choice - the
+  // reference always makes two passes).
+  void orth_passes(int K, double* w, bool selective = false) {
+    if (K <= 0) return;
+    if (!selective) {
+      for (int pass = 0; pass < 2; ++pass) {
+        multidot(V, K, w, small, 1);
+        k_gemv_rows<true><<<nb, kVecThreads, 0, st>>>(V, n, K, small, 1, w, n);
+        QDKGB_CHECK_LAUNCH();
+      }
+      return;
     }
+    multidot(V, K, w, small, 1, small + kSlotW2);
+    k_gemv_rows<true><<<nb, kVecThreads, 0, st>>>(V, n, K, small, 1, w, n, nullptr, small + kSlotW2,
+                                                  small + kSlotSkip);
+    QDKGB_CHECK_LAUNCH();
+    multidot(V, K, w, small, 1, nullptr, small + kSlotSkip);
+    k_gemv_rows<true><<<nb, kVecThreads, 0, st>>>(V, n, K, small, 1, w, n, small + kSlotSkip);
+    QDKGB_CHECK_LAUNCH();
   }
   // gram_schmidt (davidson.hpp:185-238): two CGS passes against V[:, 0:K],
   // normalise; a degenerate result raises the device flag (checked at the
   // next host sync, then repaired by fallback()).
-  void gram_schmidt(int K, double* w, double min_norm = 1e-12) {
-    orth_passes(K, w);
+  void gram_schmidt(int K, double* w, double min_norm = 1e-12, bool selective = false) {
+    orth_passes(K, w, selective);
     norm2(w, small + kSlotNrm);
     k_normalize<<<nb, 256, 0, st>>>(w, n, small + kSlotNrm, min_norm, small + kSlotFlag);
     QDKGB_CHECK_LAUNCH();
@@ -339,11 +587,12 @@ struct Dav {
     QDKGB_CHECK_LAUNCH();
   }
 
-  // X = V C0, R = AV C0 - lam0 X; |R|^2 into small[kSlotRes]
-  void ritz_residual(int k, double* R) {
-    k_ritz_residual<<<nb, 256, 0, st>>>(V, AV, n, k, evec, eval, X, R, n, partial);
-    QDKGB_CHECK_LAUNCH();
-    k_reduce_partials<<<1, 32, 0, st>>>(partial, nb, 1, small + kSlotRes, 1);
+  // X = V C0, R = AV C0 - lam0 X with |R|^2 into small[kSlotRes]; R is
+  // stored preconditioned with the diagonal D (the next direction before
+  // orthogonalisation)
+  void ritz_residual(int k, double* R, double min_abs) {
+    k_ritz_residual<<<nb, kVecThreads, 0, st>>>(V, AV, n, k, evec, eval, X, R, n, D, min_abs, partial, counts(),
+                                                small + kSlotRes);
     QDKGB_CHECK_LAUNCH();
   }
 };
@@ -370,7 +619,8 @@ void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C
   d.n = N;
   d.maxm = max_m;
   d.st = c->stream;
-  d.nb = (int)std::max<int64_t>(1, std::min<int64_t>((N + 255) / 256, (int64_t)c->sm_count * kDotBlocksPerSm));
+  d.sm_count = std::max(1, c->sm_count);
+  d.nb = (int)std::max<int64_t>(1, std::min<int64_t>((N + kVecTile - 1) / kVecTile, (int64_t)d.sm_count * kVecBlocksPerSm));
   d.V = dev_array<double>(c, W.V, (size_t)N * (max_m + 1));
   d.AV = dev_array<double>(c, W.AV, (size_t)N * (max_m + 1));
   constexpr int kKeep = 6;  // thick-restart size of the mixed path
@@ -385,6 +635,7 @@ void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C
   set_max_dynamic_smem((const void*)k_lowest_eig, (int)kEigDynSmemMax);
   d.D = (double*)H.diag.ptr;
   d.clear_flag();
+  QDKGB_CUDA(cudaMemsetAsync(d.counts(), 0, (kDotChunks + 1) * sizeof(unsigned), c->stream));
   float* xf = nullptr;
   float* yf = nullptr;
   if (mixed) {
@@ -454,7 +705,7 @@ void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C
       d.projected_row((int)i);
       d.lowest(k);
       double* R = d.col(d.V, i + 1);
-      d.ritz_residual(k, R);
+      d.ritz_residual(k, R, s->min_abs_denominator);
       double r2 = 0.;
       bool degenerate = false;
       d.fetch3(d.small + kSlotRes, d.eval, r2, lam0, degenerate);
@@ -471,8 +722,6 @@ void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C
         converged = true;
         break;
       }
-      k_precondition<<<d.nb, 256, 0, c->stream>>>(R, d.D, d.eval, N, s->min_abs_denominator);
-      QDKGB_CHECK_LAUNCH();
       d.gram_schmidt(k, R);
     }
   } else {
@@ -522,13 +771,14 @@ void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C
     }
     auto project = [&](double* v) {
       if (flip == 0.) return;
-      k_flip_project<<<d.nb, 256, 0, c->stream>>>(v, nstr, flip);
+      const unsigned nt = (unsigned)((nstr + kFlipTile - 1) / kFlipTile);
+      k_flip_project<<<dim3(nt, nt), dim3(kFlipTile, 8), 0, c->stream>>>(v, nstr, flip);
       QDKGB_CHECK_LAUNCH();
     };
     sigma_full(V0, d.AV);
     QDKGB_CUDA(cudaMemcpyAsync(d.col(d.V, 1), d.AV, N * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
     project(d.col(d.V, 1));
-    d.gram_schmidt(1, d.col(d.V, 1));
+    d.gram_schmidt(1, d.col(d.V, 1), 1e-12, true);
     d.projected_row(0);
     // residual of the guess (exact): reference level for the first refresh
     d.multidot(d.AV, 1, V0, Eptr, 1);
@@ -550,7 +800,7 @@ void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C
       ++iter;
       d.lowest(k);
       double* R = (k <= max_m - 1) ? d.col(d.V, k) : Rt;
-      d.ritz_residual(k, R);
+      d.ritz_residual(k, R, s->min_abs_denominator);
       double r2 = 0.;
       bool degenerate = false;
       d.fetch3(d.small + kSlotRes, d.eval, r2, lam0, degenerate);
@@ -571,10 +821,8 @@ void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C
       const bool refresh =
           est < 0.5 * s->res_tol || est < drop * last_true || since_best >= 6 || k >= max_m - 1;
       if (!refresh) {
-        k_precondition<<<d.nb, 256, 0, c->stream>>>(R, d.D, d.eval, N, s->min_abs_denominator);
-        QDKGB_CHECK_LAUNCH();
         project(R);
-        d.gram_schmidt(k, R);
+        d.gram_schmidt(k, R, 1e-12, true);
         continue;
       }
       // full-precision sigma, Rayleigh quotient and residual of X (unit norm)
@@ -595,10 +843,11 @@ void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C
       // thick restart: V' = V Q[:, 0:kk], AV' = AV Q[:, 0:kk]; column 0 = X with its exact sigma
       const int kk = std::min(kKeep, k);
       d.lowest(k, kk);  // the kk lowest Ritz vectors (column 0 reproduces X)
-      for (int j = 1; j < kk; ++j) {
-        k_gemv<<<d.nb, 256, 0, c->stream>>>(d.V, N, k, d.evec + (size_t)j * k, 1, tmpV + (size_t)(j - 1) * N, N);
+      if (kk > 1) {
+        static_assert(kKeep - 1 <= kMaxOut, "restart block wider than k_gemv_multi");
+        k_gemv_multi<<<d.nb, kVecThreads, 0, c->stream>>>(d.V, N, k, d.evec + k, kk - 1, tmpV, N, N);
         QDKGB_CHECK_LAUNCH();
-        k_gemv<<<d.nb, 256, 0, c->stream>>>(d.AV, N, k, d.evec + (size_t)j * k, 1, tmpAV + (size_t)(j - 1) * N, N);
+        k_gemv_multi<<<d.nb, kVecThreads, 0, c->stream>>>(d.AV, N, k, d.evec + k, kk - 1, tmpAV, N, N);
         QDKGB_CHECK_LAUNCH();
       }
       QDKGB_CUDA(cudaMemcpyAsync(d.col(d.V, 0), d.X, N * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
@@ -616,7 +865,7 @@ void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C
       k_precondition<<<d.nb, 256, 0, c->stream>>>(d.col(d.V, k), d.D, Eptr, N, s->min_abs_denominator);
       QDKGB_CHECK_LAUNCH();
       project(d.col(d.V, k));
-      d.gram_schmidt(k, d.col(d.V, k));
+      d.gram_schmidt(k, d.col(d.V, k), 1e-12, true);
       best = 1e300;
       since_best = 0;
     }

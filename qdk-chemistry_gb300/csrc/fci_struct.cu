@@ -345,7 +345,12 @@ unsigned slab_threads(int Nb) {
 // ------------------------------------------------------------------ emission
 // CTA per (group, segment), a thread per beta string, positions in order.
 // Every element is written (zero when dropped); kept counts go to kept[r].
+// STORAGE: QDKGB_H_FP64 (val), QDKGB_H_SPLIT32 (hi, lo: the batched layout)
+// or kSlabF64F32 (val and its FP32 rounding in hi: the single-instance layout
+// of QDKGB_H_SPLIT32 storage, one FP64-pipe conversion per element instead of
+// the four of the hi/lo split; the full-precision sigma then runs on val).
 constexpr int kEmitThreads = 256;
+constexpr int kSlabF64F32 = 2;
 
 template <int STORAGE>
 __global__ void __launch_bounds__(kEmitThreads)
@@ -363,11 +368,9 @@ __global__ void __launch_bounds__(kEmitThreads)
   const int inst = blockIdx.z;
   const Integrals I = Iinst ? Iinst[inst] : I0;
   diag_raw += inst * nstride;
-  if (STORAGE == QDKGB_H_FP64) val += inst * vstride;
-  else {
-    hi += inst * vstride;
-    lo += inst * vstride;
-  }
+  if (STORAGE != QDKGB_H_SPLIT32) val += inst * vstride;
+  if (STORAGE != QDKGB_H_FP64) hi += inst * vstride;
+  if (STORAGE == QDKGB_H_SPLIT32) lo += inst * vstride;
   if (b < Nb) {
     const int64_t r = (int64_t)g * Nb + b;
     const uint64_t rb = ubeta[b];
@@ -393,6 +396,9 @@ __global__ void __launch_bounds__(kEmitThreads)
       const int64_t q = ((int64_t)g * A.rowlen + p) * Nb + b;
       if (STORAGE == QDKGB_H_FP64) {
         val[q] = v;
+      } else if (STORAGE == kSlabF64F32) {
+        val[q] = v;
+        hi[q] = __double2float_rn(v);
       } else {
         const float h32 = __double2float_rn(v);
         hi[q] = h32;
@@ -429,6 +435,20 @@ __global__ void __launch_bounds__(256)
       if (keep_all || v != 0.) {
         ci[o] = (int32_t)((int64_t)h * Nb + bc);
         v64[o] = v;
+        ++o;
+      }
+    } else if (STORAGE == kSlabF64F32) {
+      // split on the way out: the same (hi, lo) pair the split layout stores
+      const double v = val[q];
+      if (keep_all || v != 0.) {
+        ci[o] = (int32_t)((int64_t)h * Nb + bc);
+        const float vh = __double2float_rn(v), vl = __double2float_rn(v - (double)vh);
+        if (v64) {
+          v64[o] = (double)vh + (double)vl;
+        } else {
+          h32[o] = vh;
+          l32[o] = vl;
+        }
         ++o;
       }
     } else {
@@ -862,14 +882,9 @@ int64_t struct_slab_elements(Context* c) { return c->fci ? c->fci->G * c->fci->N
 
 bool struct_ready(Context* c) { return c->fci && c->H.valid && !c->op_direct && c->H.structured; }
 
+// Both storages keep the FP64 values of a single-instance slab (val).
 void struct_spmv_fp64(Context* c, const double* x, double* y) {
-  Hcsr& H = c->H;
-  if (H.storage == QDKGB_H_FP64) {
-    slab_sigma<1>(c, 1, nullptr, H.val.ptr, nullptr, x, nullptr, y);
-  } else {
-    float* xs = split_x(c, x);
-    slab_sigma<2>(c, 1, nullptr, H.hi.ptr, (const float*)H.lo.ptr, xs, xs + H.n, y);
-  }
+  slab_sigma<1>(c, 1, nullptr, c->H.val.ptr, nullptr, x, nullptr, y);
 }
 
 void struct_spmv_fp32(Context* c, const float* x, float* y) {
@@ -933,9 +948,8 @@ void struct_export(Context* c, int32_t* ci, double* v64, float* h32, float* l32)
     k_slab_export<QDKGB_H_FP64><<<nb, 256, 0, c->stream>>>(A, keep_all, (const double*)H.val.ptr, nullptr, nullptr,
                                                            (const int64_t*)H.rowptr.ptr, ci, v64, h32, l32);
   else
-    k_slab_export<QDKGB_H_SPLIT32><<<nb, 256, 0, c->stream>>>(A, keep_all, nullptr, (const float*)H.hi.ptr,
-                                                              (const float*)H.lo.ptr, (const int64_t*)H.rowptr.ptr,
-                                                              ci, v64, h32, l32);
+    k_slab_export<kSlabF64F32><<<nb, 256, 0, c->stream>>>(A, keep_all, (const double*)H.val.ptr, nullptr, nullptr,
+                                                          (const int64_t*)H.rowptr.ptr, ci, v64, h32, l32);
   QDKGB_CHECK_LAUNCH();
 }
 
@@ -957,15 +971,10 @@ void build_hamiltonian_struct(Context* c, double thresh, int storage) {
   const unsigned tb = (unsigned)std::min<int64_t>((n + 255) / 256, (int64_t)c->sm_count * 16);
   k_diag_launch(c, I, diag_raw, tb);
   dev_free(c, H.colind);
-  if (storage == QDKGB_H_FP64) {
-    dev_free(c, H.hi);
-    dev_free(c, H.lo);
-  } else {
-    dev_free(c, H.val);
-  }
-  double* val = storage == QDKGB_H_FP64 ? dev_array<double>(c, H.val, nslab) : nullptr;
+  dev_free(c, H.lo);
+  if (storage == QDKGB_H_FP64) dev_free(c, H.hi);
+  double* val = dev_array<double>(c, H.val, nslab);
   float* hi = storage == QDKGB_H_SPLIT32 ? dev_array<float>(c, H.hi, nslab) : nullptr;
-  float* lo = storage == QDKGB_H_SPLIT32 ? dev_array<float>(c, H.lo, nslab) : nullptr;
   QDKGB_CUDA(cudaMemsetAsync(diag, 0, n * sizeof(double), c->stream));
   QDKGB_CUDA(cudaMemsetAsync(kept, 0, (n + 1) * sizeof(int64_t), c->stream));
   SlabArgs A = slab_args(c);
@@ -975,11 +984,11 @@ void build_hamiltonian_struct(Context* c, double thresh, int storage) {
   const uint64_t* ub = (const uint64_t*)D.ubeta.ptr;
   unsigned long long* kc = (unsigned long long*)kept;
   if (storage == QDKGB_H_FP64)
-    k_slab_emit<QDKGB_H_FP64><<<grid, thr, 0, c->stream>>>(A, I, nullptr, 0, 0, ga, ub, tbits, diag_raw, val, hi, lo,
-                                                            diag, kc);
+    k_slab_emit<QDKGB_H_FP64><<<grid, thr, 0, c->stream>>>(A, I, nullptr, 0, 0, ga, ub, tbits, diag_raw, val,
+                                                            nullptr, nullptr, diag, kc);
   else
-    k_slab_emit<QDKGB_H_SPLIT32><<<grid, thr, 0, c->stream>>>(A, I, nullptr, 0, 0, ga, ub, tbits, diag_raw, val, hi,
-                                                               lo, diag, kc);
+    k_slab_emit<kSlabF64F32><<<grid, thr, 0, c->stream>>>(A, I, nullptr, 0, 0, ga, ub, tbits, diag_raw, val, hi,
+                                                           nullptr, diag, kc);
   QDKGB_CHECK_LAUNCH();
   int64_t* rowptr = dev_array<int64_t>(c, H.rowptr, n + 1);
   exclusive_scan_i64(c, kept, rowptr, n, H.scan_tmp);
@@ -1012,6 +1021,7 @@ void build_hamiltonian_struct(Context* c, double thresh, int storage) {
       std::swap(H.lo, lb);
       dev_free(c, hb);
       dev_free(c, lb);
+      dev_free(c, H.val);
     }
     H.structured = false;
   }
