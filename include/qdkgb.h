@@ -221,6 +221,21 @@ int qdkgb_asci(qdkgb_context* ctx, const qdkgb_asci_settings* s, const qdkgb_dav
                int do_refine, int64_t cap, uint64_t* out_a, uint64_t* out_b, double* out_c, int64_t* n_out,
                double* E_out, double* E_grow_out);
 
+/* ASCI-PT2 (asci_pt2_constraint, external/macis/include/macis/asci/pt2.hpp:
+ * 59-565): E_PT2 = sum over the determinants Q outside the wavefunction of
+ * (sum_P C_P <Q|H|P>)^2 / (E0 - H_QQ), single contributions with
+ * |C_P <Q|H|P>| < pt2_tol dropped (the reference default is 1e-16), H_QQ by
+ * the fast diagonals.  The wavefunction (alpha[i], beta[i], C[i]) must be
+ * sorted by spin_comparator (alpha string, then beta; QDKGB_ERR_INVALID
+ * "PT2 Only Works with Sorted Wfns" otherwise); E0 is its electronic energy.
+ * Integrals must be set.  max_slots bounds the hash table of target
+ * determinants (the memory role of the reference's pt2_reserve_count; 0: half
+ * of the free device memory): when every contribution would not fit, the
+ * target space is split by a hash into passes.  *ept2 receives E_PT2,
+ * *n_external (may be NULL) the number of distinct external determinants. */
+int qdkgb_asci_pt2(qdkgb_context* ctx, int64_t ndets, const uint64_t* alpha, const uint64_t* beta, const double* C,
+                   double E0, double pt2_tol, int64_t max_slots, double* ept2, int64_t* n_external);
+
 /* ------------------------------------------------------------ CASCI driver
  * cas_helper::impl / compute_casci_rdms (cpp/src/qdk/chemistry/algorithms/
  * microsoft/macis_cas.cpp:35-117, include/macis/mcscf/cas.hpp:33-64): FCI

@@ -24,6 +24,7 @@
 #include <vector>
 #ifdef _OPENMP
 #include <omp.h>
+#include <parallel/algorithm>
 #endif
 
 namespace {
@@ -943,6 +944,28 @@ void os_doubles_contribs(const Ham& H, double coeff, uint64_t sa, uint64_t sb, c
     }
 }
 
+// Every contribution of one wavefunction determinant P (coefficient c): the
+// singles and doubles of each spin and the opposite-spin doubles, in the
+// order of the reference's per-determinant loop (determinant_search.hpp:
+// 386-474, pt2.hpp:298-344), then P itself with an infinite score (it is in
+// the wavefunction, so it drops out after accumulation).
+void contribs_of(const Ham& H, const Det& P, double c, double E0, double tol, std::vector<Contrib>& out) {
+  const int n = H.n;
+  std::vector<uint32_t> oa, va, ob, vb;
+  for (int p = 0; p < n; ++p) {
+    ((P.a >> p) & 1 ? oa : va).push_back(p);
+    ((P.b >> p) & 1 ? ob : vb).push_back(p);
+  }
+  const double hdiag = H.me_diag(oa, ob);
+  const std::vector<double> ea = orbital_ens(H, oa, ob), eb = orbital_ens(H, ob, oa);
+  singles_contribs(H, c, P.a, P.b, true, oa, va, ob, ea, hdiag, E0, tol, out);
+  ss_doubles_contribs(H, c, P.a, P.b, true, oa, va, ea, hdiag, E0, tol, out);
+  os_doubles_contribs(H, c, P.a, P.b, oa, va, ob, vb, ea, eb, hdiag, E0, tol, out);
+  singles_contribs(H, c, P.b, P.a, false, ob, vb, oa, eb, hdiag, E0, tol, out);
+  ss_doubles_contribs(H, c, P.b, P.a, false, ob, vb, eb, hdiag, E0, tol, out);
+  out.push_back({P, std::numeric_limits<double>::infinity(), 1.0});
+}
+
 // asci_search (include/macis/asci/determinant_search.hpp:808-1123) on the
 // full contribution list: enumerate, sort by determinant and accumulate
 // (determinant_sort.hpp:115-370), drop the core (infinite score), prune
@@ -966,26 +989,10 @@ std::vector<Det> asci_search(const Ham& H, const AsciSettings& S, int64_t ndets_
     tid = omp_get_thread_num();
 #endif
     std::vector<Contrib>& out = per[tid];
-    std::vector<uint32_t> oa, va, ob, vb;
 #pragma omp for schedule(dynamic)
-    for (int64_t ip = 0; ip < ncore; ++ip) {
-      const Det P = core[ip];
-      const double c = C[ip];
-      oa.clear(); va.clear(); ob.clear(); vb.clear();
-      for (int p = 0; p < n; ++p) {
-        ((P.a >> p) & 1 ? oa : va).push_back(p);
-        ((P.b >> p) & 1 ? ob : vb).push_back(p);
-      }
-      const double hdiag = H.me_diag(oa, ob);
-      const std::vector<double> ea = orbital_ens(H, oa, ob), eb = orbital_ens(H, ob, oa);
-      singles_contribs(H, c, P.a, P.b, true, oa, va, ob, ea, hdiag, E0, S.h_el_tol, out);
-      ss_doubles_contribs(H, c, P.a, P.b, true, oa, va, ea, hdiag, E0, S.h_el_tol, out);
-      os_doubles_contribs(H, c, P.a, P.b, oa, va, ob, vb, ea, eb, hdiag, E0, S.h_el_tol, out);
-      singles_contribs(H, c, P.b, P.a, false, ob, vb, oa, eb, hdiag, E0, S.h_el_tol, out);
-      ss_doubles_contribs(H, c, P.b, P.a, false, ob, vb, eb, hdiag, E0, S.h_el_tol, out);
-      out.push_back({P, std::numeric_limits<double>::infinity(), 1.0});
-    }
+    for (int64_t ip = 0; ip < ncore; ++ip) contribs_of(H, core[ip], C[ip], E0, S.h_el_tol, out);
   }
+  (void)n;
   std::vector<Contrib> all;
   for (auto& v : per) all.insert(all.end(), v.begin(), v.end());
   std::stable_sort(all.begin(), all.end(), [](const Contrib& x, const Contrib& y) { return spin_less(x.q, y.q); });
@@ -1017,6 +1024,87 @@ std::vector<Det> asci_search(const Ham& H, const AsciSettings& S, int64_t ndets_
   }
   out.insert(out.end(), core.begin(), core.end());
   return out;
+}
+
+// asci_pt2_constraint (include/macis/asci/pt2.hpp:59-565): the second-order
+// energy E_PT2 = sum over determinants Q outside the wavefunction of
+// (sum_P c_P <Q|H|P>)^2 / (E0 - H_QQ) (asci_contrib::pt2, determinant_
+// contributions.hpp:49-55), single contributions with |c_P <Q|H|P>| < pt2_tol
+// dropped, H_QQ by the fast diagonals; the wavefunction must be sorted by
+// spin_comparator (pt2.hpp:79-80).  The reference splits the Q space by alpha
+// constraints to balance MPI ranks and threads and to bound the memory of its
+// sort-and-accumulate; here Q is split by a hash into passes of at most
+// `pass_max` contributions.  Every Q lies in one part of either split, so the
+// accumulated sums are the same.
+inline uint64_t det_mix(const Det& q) {
+  uint64_t x = q.a * 0x9e3779b97f4a7c15ULL ^ (q.b + 0x632be59bd9b4e019ULL);
+  x ^= x >> 31;
+  x *= 0xd6e8feb86659fd93ULL;
+  x ^= x >> 32;
+  return x;
+}
+double asci_pt2(const Ham& H, const std::vector<Det>& dets, const std::vector<double>& C, double E0, double tol,
+                int64_t* npt2, int64_t pass_max = (int64_t)1 << 25) {
+  if (!std::is_sorted(dets.begin(), dets.end(), spin_less)) throw std::runtime_error("PT2 Only Works with Sorted Wfns");
+  const int n = H.n;
+  int64_t total = 0;
+  for (const Det& P : dets) {
+    const int ka = __builtin_popcountll(P.a), kb = __builtin_popcountll(P.b);
+    const int64_t sa = (int64_t)ka * (n - ka), sb = (int64_t)kb * (n - kb);
+    total += 1 + sa + sb + sa * sb + (int64_t)ka * (ka - 1) / 2 * ((n - ka) * (n - ka - 1) / 2) +
+             (int64_t)kb * (kb - 1) / 2 * ((n - kb) * (n - kb - 1) / 2);
+  }
+  const uint64_t npass = (uint64_t)std::max<int64_t>(1, (total + pass_max - 1) / pass_max);
+  int nth = 1;
+#ifdef _OPENMP
+  nth = omp_get_max_threads();
+#endif
+  double EPT2 = 0.;
+  int64_t NPT2 = 0;
+  for (uint64_t pass = 0; pass < npass; ++pass) {
+    std::vector<std::vector<Contrib>> per(nth);
+#pragma omp parallel
+    {
+      int tid = 0;
+#ifdef _OPENMP
+      tid = omp_get_thread_num();
+#endif
+      std::vector<Contrib> tmp;
+#pragma omp for schedule(dynamic, 16)
+      for (int64_t ip = 0; ip < (int64_t)dets.size(); ++ip) {
+        tmp.clear();
+        contribs_of(H, dets[ip], C[ip], E0, tol, tmp);
+        for (const Contrib& x : tmp)
+          if (npass == 1 || det_mix(x.q) % npass == pass) per[tid].push_back(x);
+      }
+    }
+    std::vector<Contrib> all;
+    size_t m = 0;
+    for (auto& v : per) m += v.size();
+    all.reserve(m);
+    for (auto& v : per) {
+      all.insert(all.end(), v.begin(), v.end());
+      std::vector<Contrib>().swap(v);
+    }
+    auto less = [](const Contrib& x, const Contrib& y) { return spin_less(x.q, y.q); };
+#ifdef _OPENMP
+    __gnu_parallel::sort(all.begin(), all.end(), less);
+#else
+    std::sort(all.begin(), all.end(), less);
+#endif
+    for (size_t k = 0; k < all.size();) {
+      size_t e = k + 1;
+      Contrib c0 = all[k];
+      for (; e < all.size() && all[e].q == all[k].q; ++e) c0.c_h += all[e].c_h;
+      if (!std::isinf(c0.c_h)) {
+        EPT2 += c0.c_h * c0.c_h / c0.h_diag;
+        ++NPT2;
+      }
+      k = e;
+    }
+  }
+  if (npt2) *npt2 = NPT2;
+  return EPT2;
 }
 
 // selected_ci_diag (selected_ci_diag.hpp:111-158) on a sorted determinant list
@@ -1376,6 +1464,18 @@ int64_t orc_asci_search(void* h, const double* set, int64_t ncore, const uint64_
     }
   });
   return nret;
+}
+
+// asci_pt2 on a wavefunction (sorted by spin_comparator); 0 on success.
+int orc_asci_pt2(void* h, int64_t nd, const uint64_t* a, const uint64_t* b, const double* c, double E0, double tol,
+                 int64_t pass_max, double* ept2, int64_t* npt2) {
+  const Ham& H = *(Ham*)h;
+  return guard([&] {
+    std::vector<Det> dets(nd);
+    for (int64_t i = 0; i < nd; ++i) dets[i] = {a[i], b[i]};
+    std::vector<double> C(c, c + nd);
+    *ept2 = asci_pt2(H, dets, C, E0, tol, npt2, pass_max > 0 ? pass_max : (int64_t)1 << 25);
+  });
 }
 
 int64_t orc_sdl_sample(void* h, const uint64_t* alpha, const uint64_t* beta, int64_t nd, double thresh, int64_t stride,

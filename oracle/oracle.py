@@ -67,6 +67,9 @@ def lib():
                                ctypes.POINTER(f64), ctypes.POINTER(f64)]
         L.orc_asci_search.restype = i64
         L.orc_asci_search.argtypes = [vp, _f64p, i64, _u64p, _u64p, _f64p, f64, i64, i64, _u64p, _u64p]
+        L.orc_asci_pt2.restype = ci
+        L.orc_asci_pt2.argtypes = [vp, i64, _u64p, _u64p, _f64p, f64, f64, i64, ctypes.POINTER(f64),
+                                   ctypes.POINTER(i64)]
         _lib = L
     return _lib
 
@@ -277,3 +280,16 @@ def asci_search(ham, alpha, beta, c, E0, ndets_max, **settings):
     if n < 0:
         raise RuntimeError(lib().orc_last_error().decode())
     return oa[:n].copy(), ob[:n].copy()
+
+
+def asci_pt2(ham, alpha, beta, c, E0, pt2_tol=1e-16, pass_max=0):
+    """asci_pt2_constraint (pt2.hpp:59-565) on a wavefunction sorted by
+    spin_comparator; returns (E_PT2, number of external determinants)."""
+    e = ctypes.c_double()
+    npt = ctypes.c_int64()
+    rc = lib().orc_asci_pt2(ham._h, len(alpha), np.ascontiguousarray(alpha, dtype=np.uint64),
+                            np.ascontiguousarray(beta, dtype=np.uint64), np.ascontiguousarray(c, dtype=np.float64),
+                            float(E0), float(pt2_tol), int(pass_max), ctypes.byref(e), ctypes.byref(npt))
+    if rc != 0:
+        raise RuntimeError(lib().orc_last_error().decode())
+    return e.value, npt.value

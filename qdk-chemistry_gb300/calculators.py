@@ -12,6 +12,8 @@ Mirrors, with the same names, defaults and error behaviour:
 * ``MultiConfigurationCalculator.run(hamiltonian, n_alpha, n_beta) ->
   (total energy, Wavefunction)`` (mc.hpp:87-172), the CASCI plugin
   (macis_cas.cpp:35-148) and the ASCI plugin (macis_asci.cpp:44-234);
+* ``ProjectedMultiConfigurationCalculator.run(hamiltonian, configurations)``
+  (pmc.hpp:31-150) and the PMC plugin (macis_pmc.cpp:42-178);
 * ``davidson_solver(csr, tol=1e-8, max_m=20) -> (eigenvalue, eigenvector)``
   (python/src/pybind11/algorithms/davidson_solver.cpp:56-108).
 All computation runs in libqdkgb.so on the GPU.
@@ -293,6 +295,26 @@ class Gb300AsciSettings(Gb300Settings):
         self.set_default("core_selection_threshold", float, 0.95, "core weight fraction", (0.0, 1.0))
         self.set_default("warm_start_davidson", bool, True)
         self.set_default("min_warm_start_overlap", float, 0.5, "", (0.0, 1.0))
+        # ASCI-PT2 (asci_pt2, pt2.hpp:59-565): pt2_tol drops single contributions
+        # |c <Q|H|P>| below it.  The reference's work-split knobs (constraint
+        # levels, big-constraint threshold, reserve and prune of its pair
+        # buffers, next-value batching) are accepted with their defaults; the
+        # GPU search and PT2 split the target space by a hash instead.
+        big = 2 ** 63 - 1
+        self.set_default("pt2_tol", float, 1e-16, "PT2 correction tolerance", (0.0, 1.0))
+        self.set_default("pt2_reserve_count", int, 70000000, "Reserve count for PT2 calculations", (0, big))
+        self.set_default("pt2_prune", bool, False)
+        self.set_default("pt2_precompute_eps", bool, False)
+        self.set_default("pt2_precompute_idx", bool, False)
+        self.set_default("pt2_print_progress", bool, False)
+        self.set_default("pt2_bigcon_thresh", int, 250, "Threshold for using bigcon PT2 algorithm", (0, big))
+        self.set_default("pair_size_max", int, 500000000, "Maximum number of ASCI contribution pairs", (1, big))
+        self.set_default("nxtval_bcount_thresh", int, 1000, "Threshold for next value batch count", (1, big))
+        self.set_default("nxtval_bcount_inc", int, 10, "Increment for next value batch count", (1, big))
+        self.set_default("constraint_level", int, 2, "Constraint level for excitation generation", (0, big))
+        self.set_default("pt2_max_constraint_level", int, 5, "Maximum constraint level for PT2", (0, big))
+        self.set_default("pt2_min_constraint_level", int, 0, "Minimum constraint level for PT2", (0, big))
+        self.set_default("pt2_constraint_refine_force", int, 0, "Force constraint refinement for PT2", (0, big))
 
 
 class Gb300Asci(MultiConfigurationCalculator):
@@ -352,8 +374,98 @@ class Gb300Asci(MultiConfigurationCalculator):
         return E + hamiltonian.get_core_energy(), wfn
 
 
-_REGISTRY = {"multi_configuration_calculator": {"gb300_cas": Gb300Cas, "gb300_asci": Gb300Asci}}
-_DEFAULT = {"multi_configuration_calculator": "gb300_cas"}
+class ProjectedMultiConfigurationCalculator(MultiConfigurationCalculator):
+    """run(hamiltonian, configurations) -> (total energy, Wavefunction): the
+    projected multi-configuration calculator (pmc.hpp:31-150): the CI problem
+    on a caller's determinant list."""
+
+    def type_name(self):
+        return "projected_multi_configuration_calculator"
+
+    def run(self, hamiltonian, configurations):
+        self._settings.lock()
+        return self._run_impl(hamiltonian, configurations)
+
+
+class Gb300Pmc(ProjectedMultiConfigurationCalculator):
+    """MacisPmc (macis_pmc.cpp:42-178): H build and Davidson on the given
+    configurations, in their order (canonical strings '2', 'u', 'd', '0' per
+    orbital, or (alpha, beta) bit-string pairs); one determinant gives <D|H|D>.
+    The list is solved in spin order and the coefficients come back in the
+    caller's order (the eigenpair does not depend on the order).
+    With calculate_one_rdm / calculate_two_rdm the wavefunction carries the
+    RDMs (the reference forms the spin-traced ones, macis_pmc.cpp:126-161; here
+    the spin-resolved blocks are kept and the traced views derive from them)."""
+
+    def name(self):
+        return "gb300_pmc"
+
+    @staticmethod
+    def _parse(configurations, norb):
+        a, b = [], []
+        for cfg in configurations:
+            if isinstance(cfg, str):
+                if set(cfg) - set("2ud0"):
+                    raise ValueError("configuration '%s': characters must be '2', 'u', 'd' or '0'" % cfg)
+                if len(cfg) < norb:
+                    raise RuntimeError("Configuration orbital capacity does not match Hamiltonian active space.")
+                x, y = determinants.from_canonical_string(cfg[:norb])
+                if any(ch not in "0" for ch in cfg[norb:]):
+                    raise ValueError("configuration '%s' occupies orbitals beyond the active space" % cfg)
+            else:
+                x, y = int(cfg[0]), int(cfg[1])
+                if norb < 64 and ((x >> norb) or (y >> norb)):
+                    raise ValueError("configuration occupies orbitals beyond the active space")
+            a.append(x)
+            b.append(y)
+        return np.array(a, dtype=np.uint64), np.array(b, dtype=np.uint64)
+
+    def _run_impl(self, hamiltonian, configurations):
+        self._check_unsupported()
+        configurations = list(configurations)
+        if not configurations:
+            raise RuntimeError("Configuration basis cannot be empty")
+        n = hamiltonian.norb
+        if n > 64:
+            raise ValueError("at most 64 active orbitals per spin")
+        a, b = self._parse(configurations, n)
+        with capi.Context(self._settings.get("device")) as ctx:
+            ctx.set_integrals(hamiltonian.get_one_body_integrals(), hamiltonian.get_two_body_integrals())
+            if len(a) == 1:
+                # a single determinant: E = <D|H|D>, C = [1] (macis_pmc.cpp:93-96)
+                ctx.set_dets(a, b)
+                ctx.build_hamiltonian(0.0)
+                E = float(ctx.diagonal()[0])
+                C = np.ones(1)
+                rdms = None
+                want = self._rdm_blocks()
+                if want:
+                    rdms = ctx.rdms_spin_dep(C, want=want)
+                return E + hamiltonian.get_core_energy(), Wavefunction(n, a, b, C, rdms)
+            # solved on the spin-sorted list (the layout the H build groups by
+            # alpha string), the CI vector returned in the caller's order
+            order = np.lexsort((b, a))
+            E, ws = self._solve(ctx, hamiltonian, a[order], b[order])
+            C = np.empty_like(ws.coefficients)
+            C[order] = ws.coefficients
+            wfn = Wavefunction(n, a, b, C, ws._rdms)
+            wfn.info = ws.info
+            return E, wfn
+
+    def _rdm_blocks(self):
+        s = self._settings
+        want = []
+        if s.get("calculate_one_rdm"):
+            want += ["aa", "bb"]
+        if s.get("calculate_two_rdm"):
+            want += ["aaaa", "bbbb", "aabb"]
+        return tuple(want)
+
+
+_REGISTRY = {"multi_configuration_calculator": {"gb300_cas": Gb300Cas, "gb300_asci": Gb300Asci},
+             "projected_multi_configuration_calculator": {"gb300_pmc": Gb300Pmc}}
+_DEFAULT = {"multi_configuration_calculator": "gb300_cas",
+            "projected_multi_configuration_calculator": "gb300_pmc"}
 
 
 def register(kind, factory):

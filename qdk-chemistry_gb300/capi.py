@@ -37,7 +37,7 @@ EXPORTED = [
     "qdkgb_get_csr64", "qdkgb_diagonal", "qdkgb_spmv", "qdkgb_spmv_device", "qdkgb_davidson_default_settings",
     "qdkgb_davidson", "qdkgb_rdms_spin_dep", "qdkgb_casci", "qdkgb_version", "qdkgb_kernel_launches",
     "qdkgb_sigma_split_noalloc", "qdkgb_set_csr", "qdkgb_build_direct_sigma",
-    "qdkgb_asci_default_settings", "qdkgb_asci_search", "qdkgb_asci",
+    "qdkgb_asci_default_settings", "qdkgb_asci_search", "qdkgb_asci", "qdkgb_asci_pt2",
     "qdkgb_batch_default_settings", "qdkgb_casci_batch",
 ]
 
@@ -126,6 +126,7 @@ def lib():
     L.qdkgb_asci_default_settings.argtypes = [P(AsciSettings)]
     L.qdkgb_asci_default_settings.restype = None
     L.qdkgb_asci_search.argtypes = [vp, P(AsciSettings), i64, vp, vp, vp, dp, i64, i64, vp, vp, P(i64)]
+    L.qdkgb_asci_pt2.argtypes = [vp, i64, vp, vp, vp, dp, dp, i64, P(dp), P(i64)]
     L.qdkgb_asci.argtypes = [vp, P(AsciSettings), P(DavidsonSettings), dp, i64, vp, vp, vp, dp, ci, ci, i64, vp, vp, vp,
                              P(i64), P(dp), P(dp)]
     L.qdkgb_spmv.argtypes = [vp, ci, vp, vp]
@@ -391,6 +392,24 @@ def asci_search(ctx, core_alpha, core_beta, core_coeff, E0, ndets_max, **setting
     ctx._check(lib().qdkgb_asci_search(ctx.handle, ctypes.byref(s), len(ca), _ptr(ca), _ptr(cb), _ptr(cc), float(E0),
                                        int(ndets_max), n.value, _ptr(oa), _ptr(ob), ctypes.byref(n)))
     return oa, ob
+
+
+def asci_pt2(ctx, alpha, beta, coeff, E0, pt2_tol=1e-16, max_slots=0):
+    """ASCI-PT2 on the GPU (qdkgb_asci_pt2, asci_pt2_constraint pt2.hpp:59-565)
+    for a wavefunction sorted by spin_comparator; integrals must be set.
+    max_slots bounds the target table (0: by free memory; smaller tables
+    split the target space into passes).  Returns (E_PT2, number of external
+    determinants)."""
+    a = np.ascontiguousarray(alpha, dtype=np.uint64)
+    b = np.ascontiguousarray(beta, dtype=np.uint64)
+    c = _f64(coeff)
+    if not (len(a) == len(b) == len(c)):
+        raise ValueError("alpha, beta and coeff must have the same length")
+    e = ctypes.c_double()
+    n = ctypes.c_int64()
+    ctx._check(lib().qdkgb_asci_pt2(ctx.handle, len(a), _ptr(a), _ptr(b), _ptr(c), float(E0), float(pt2_tol),
+                                    int(max_slots), ctypes.byref(e), ctypes.byref(n)))
+    return e.value, n.value
 
 
 def asci(ctx, alpha0, beta0, c0, E0, grow=True, refine=True, tol=1e-8, max_m=200, precision=PREC_FP64,

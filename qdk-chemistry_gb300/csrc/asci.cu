@@ -81,7 +81,14 @@ struct CoreArgs {
   double E0;
   double h_el_tol;
   Table T;
+  uint32_t npass = 1, pass = 0;  // targets whose part_of() == pass are inserted (npass > 1: PT2 passes)
 };
+
+// part of the target space of a determinant in a split into npass passes (a
+// hash independent of the table slot)
+__device__ __forceinline__ uint32_t part_of(uint64_t qa, uint64_t qb, uint32_t npass) {
+  return (uint32_t)(mix64(qb * 0x9e3779b97f4a7c15ULL ^ mix64(qa + 0x632be59bd9b4e019ULL)) % npass);
+}
 
 // (i, j) with i < j from a pair index p = j (j - 1) / 2 + i
 __device__ __forceinline__ void pair_of(int p, int& i, int& j) {
@@ -156,7 +163,7 @@ __global__ void __launch_bounds__(kAsciWarps * 32) k_asci_enum(CoreArgs A) {
     hdiag = __shfl_sync(QDKGB_FULL_MASK, hdiag, 0);
     __syncwarp();
     // the core determinant itself: infinite score (removed later)
-    if (lane == 0) table_add(A.T, Pa, Pb, INFINITY, 1.0);
+    if (lane == 0 && (A.npass == 1 || part_of(Pa, Pb, A.npass) == A.pass)) table_add(A.T, Pa, Pb, INFINITY, 1.0);
     const int64_t nsa = (int64_t)ka * na_v, nsb = (int64_t)kb * nb_v;
     const int64_t pa_o = (int64_t)ka * (ka - 1) / 2, pa_v = (int64_t)na_v * (na_v - 1) / 2;
     const int64_t pb_o = (int64_t)kb * (kb - 1) / 2, pb_v = (int64_t)nb_v * (nb_v - 1) / 2;
@@ -246,7 +253,7 @@ __global__ void __launch_bounds__(kAsciWarps * 32) k_asci_enum(CoreArgs A) {
           ok = true;
         }
       }
-      if (ok) table_add(A.T, qa, qb, ch, hd);
+      if (ok && (A.npass == 1 || part_of(qa, qb, A.npass) == A.pass)) table_add(A.T, qa, qb, ch, hd);
     }
     __syncwarp();
     (void)full;
@@ -316,6 +323,42 @@ __global__ void k_asci_select(const uint64_t* __restrict__ keys, const uint64_t*
       oa[p] = (uint64_t)key;
       ob[p] = (uint64_t)(key >> 64);
     }
+  }
+}
+
+// PT2 terms of the filled slots: sum^2 / (E0 - H_QQ) over finite sums (the
+// wavefunction's own determinants carry an infinite sum), per block
+__global__ void __launch_bounds__(256) k_pt2_sum(Table T, uint64_t cap, double* __restrict__ partial,
+                                                 unsigned long long* __restrict__ count) {
+  __shared__ double rs[8];
+  __shared__ unsigned long long rc[8];
+  double s = 0.;
+  unsigned long long m = 0;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < cap; i += (uint64_t)gridDim.x * blockDim.x) {
+    if (T.keys[i] != kEmpty) {
+      const double v = T.sum[i];
+      if (!isinf(v)) {
+        s += v * v / T.hd[i];
+        ++m;
+      }
+    }
+  }
+  s = warp_sum(s);
+  for (int d = 16; d > 0; d >>= 1) m += __shfl_xor_sync(QDKGB_FULL_MASK, m, d);
+  if ((threadIdx.x & 31) == 0) {
+    rs[threadIdx.x >> 5] = s;
+    rc[threadIdx.x >> 5] = m;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.;
+    unsigned long long u = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      t += rs[w];
+      u += rc[w];
+    }
+    partial[blockIdx.x] = t;
+    count[blockIdx.x] = u;
   }
 }
 
@@ -451,6 +494,100 @@ void asci_search_gpu(Context* c, int64_t ncore, const uint64_t* ca, const uint64
   std::copy(ca, ca + ncore, out_a.begin() + nsel);
   std::copy(cb, cb + ncore, out_b.begin() + nsel);
   for (DeviceBuffer* b : {&bkeys, &bsum, &bhd, &bck, &bcs, &bcnt, &berr, &bcore, &bout, &bhist}) dev_free(c, *b);
+}
+
+// asci_pt2_constraint (include/macis/asci/pt2.hpp:59-565) on the device:
+// E_PT2 = sum over the determinants Q outside the wavefunction of
+// (sum_P c_P <Q|H|P>)^2 / (E0 - H_QQ), single contributions with
+// |c_P <Q|H|P>| < pt2_tol dropped (determinant_contributions.hpp:49-55,
+// mask_constraints.hpp:400-670).  The enumeration of the search runs over the
+// whole wavefunction (each determinant inserted with an infinite score, so
+// that it drops out), into the hash table; the reference's constraint split
+// (there for MPI / OpenMP balance and memory) becomes a split of the target
+// space by a hash into passes when the table for every contribution would
+// not fit in half of the free device memory.  Every Q lies in one part of
+// either split, so the sums are the same.
+double asci_pt2_gpu(Context* c, int64_t nd, const uint64_t* a, const uint64_t* b, const double* C, double E0,
+                    double pt2_tol, int64_t max_slots, int64_t* npt2) {
+  if (!c->have_ints) throw Error(QDKGB_ERR_STATE, "integrals not set");
+  if (nd <= 0) throw Error(QDKGB_ERR_INVALID, "empty wavefunction");
+  for (int64_t i = 1; i < nd; ++i)
+    if (a[i] < a[i - 1] || (a[i] == a[i - 1] && b[i] < b[i - 1]))
+      throw Error(QDKGB_ERR_INVALID, "PT2 Only Works with Sorted Wfns");
+  const int n = c->norb;
+  int64_t total = nd;
+  for (int64_t i = 0; i < nd; ++i) {
+    const int ka = __builtin_popcountll(a[i]), kb = __builtin_popcountll(b[i]);
+    const int64_t sa = (int64_t)ka * (n - ka), sb = (int64_t)kb * (n - kb);
+    total += sa + sb + sa * sb + binom64(ka, 2) * binom64(n - ka, 2) + binom64(kb, 2) * binom64(n - kb, 2);
+  }
+  size_t freeb = 0, totb = 0;
+  QDKGB_CUDA(cudaMemGetInfo(&freeb, &totb));
+  const size_t slot_bytes = 16 + 8 + 8;  // key, sum, E0 - H_QQ
+  const size_t budget = (freeb > (size_t)3 * nd * 8 ? freeb - (size_t)3 * nd * 8 : 0) / 2;
+  const uint64_t slot_max = max_slots > 0 ? (uint64_t)max_slots : ~0ull;
+  uint64_t cap = 1024;
+  while (cap < (uint64_t)(total + total / 2) && (cap << 1) * slot_bytes <= budget && (cap << 1) <= slot_max)
+    cap <<= 1;
+  if (cap * slot_bytes > budget && cap > 1024) cap >>= 1;
+  const uint64_t npass = std::max<uint64_t>(1, ((uint64_t)(total + total / 2) + cap - 1) / cap);
+  if (npass > 0xffffffffull) throw Error(QDKGB_ERR_OOM, "ASCI PT2: too many passes for the device memory");
+  DeviceBuffer bkeys, bsum, bhd, berr, bcore, bpart;
+  u128* keys = (u128*)dev_alloc(c, bkeys, cap * 16 + 256);
+  keys = (u128*)(((uintptr_t)keys + 15) & ~(uintptr_t)15);
+  double* sum = dev_array<double>(c, bsum, cap);
+  double* hd = dev_array<double>(c, bhd, cap);
+  int* err = dev_array<int>(c, berr, 1);
+  const unsigned fb = (unsigned)std::min<uint64_t>((cap + 255) / 256, (uint64_t)c->sm_count * 64);
+  const unsigned sb = (unsigned)std::min<uint64_t>((cap + 255) / 256, (uint64_t)c->sm_count * 8);
+  double* partial = (double*)dev_alloc(c, bpart, (size_t)sb * 16 + 64);
+  unsigned long long* pcount = (unsigned long long*)(partial + sb);
+  uint64_t* dcore = dev_array<uint64_t>(c, bcore, 3 * nd);
+  QDKGB_CUDA(cudaMemcpyAsync(dcore, a, nd * 8, cudaMemcpyHostToDevice, c->stream));
+  QDKGB_CUDA(cudaMemcpyAsync(dcore + nd, b, nd * 8, cudaMemcpyHostToDevice, c->stream));
+  QDKGB_CUDA(cudaMemcpyAsync(dcore + 2 * nd, C, nd * 8, cudaMemcpyHostToDevice, c->stream));
+  QDKGB_CUDA(cudaMemsetAsync(err, 0, sizeof(int), c->stream));
+  CoreArgs A;
+  A.I = integrals_view(c);
+  A.n = n;
+  A.ncore = nd;
+  A.ca = dcore;
+  A.cb = dcore + nd;
+  A.cc = (const double*)(dcore + 2 * nd);
+  A.E0 = E0;
+  A.h_el_tol = pt2_tol;
+  A.T = Table{keys, sum, hd, cap - 1, err};
+  A.npass = (uint32_t)npass;
+  const unsigned eb = (unsigned)std::min<int64_t>((nd + kAsciWarps - 1) / kAsciWarps, (int64_t)c->sm_count * 16);
+  std::vector<double> hp(sb);
+  std::vector<unsigned long long> hc(sb);
+  double ept2 = 0.;
+  int64_t count = 0;
+  for (uint64_t pass = 0; pass < npass; ++pass) {
+    A.pass = (uint32_t)pass;
+    k_fill_empty<<<fb, 256, 0, c->stream>>>(keys, sum, cap);
+    QDKGB_CHECK_LAUNCH();
+    k_asci_enum<<<eb, kAsciWarps * 32, 0, c->stream>>>(A);
+    QDKGB_CHECK_LAUNCH();
+    k_pt2_sum<<<sb, 256, 0, c->stream>>>(A.T, cap, partial, pcount);
+    QDKGB_CHECK_LAUNCH();
+    int herr = 0;
+    QDKGB_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    QDKGB_CUDA(cudaMemcpyAsync(hp.data(), partial, sb * 8, cudaMemcpyDeviceToHost, c->stream));
+    QDKGB_CUDA(cudaMemcpyAsync(hc.data(), pcount, sb * 8, cudaMemcpyDeviceToHost, c->stream));
+    QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+    if (herr) {
+      for (DeviceBuffer* x : {&bkeys, &bsum, &bhd, &berr, &bcore, &bpart}) dev_free(c, *x);
+      throw Error(QDKGB_ERR_OOM, "ASCI PT2: hash table overflow");
+    }
+    for (unsigned i = 0; i < sb; ++i) {
+      ept2 += hp[i];
+      count += (int64_t)hc[i];
+    }
+  }
+  for (DeviceBuffer* x : {&bkeys, &bsum, &bhd, &berr, &bcore, &bpart}) dev_free(c, *x);
+  if (npt2) *npt2 = count;
+  return ept2;
 }
 
 }  // namespace qdkgb

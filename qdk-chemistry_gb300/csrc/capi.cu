@@ -449,6 +449,18 @@ int qdkgb_asci_search(qdkgb_context* c, const qdkgb_asci_settings* s, int64_t nc
   });
 }
 
+int qdkgb_asci_pt2(qdkgb_context* c, int64_t ndets, const uint64_t* alpha, const uint64_t* beta, const double* C,
+                   double E0, double pt2_tol, int64_t max_slots, double* ept2, int64_t* n_external) {
+  if (!c) return QDKGB_ERR_INVALID;
+  return guarded(c, [&] {
+    if (!alpha || !beta || !C || !ept2 || ndets <= 0) throw Error(QDKGB_ERR_INVALID, "null argument");
+    if (!(pt2_tol >= 0.)) throw Error(QDKGB_ERR_INVALID, "pt2_tol must be >= 0");
+    QDKGB_CUDA(cudaSetDevice(c->device));
+    if (max_slots < 0) throw Error(QDKGB_ERR_INVALID, "max_slots must be >= 0");
+    *ept2 = asci_pt2_gpu(c, ndets, alpha, beta, C, E0, pt2_tol, max_slots, n_external);
+  });
+}
+
 int qdkgb_asci(qdkgb_context* c, const qdkgb_asci_settings* s, const qdkgb_davidson_settings* ci, double matel_tol,
                int64_t n0, const uint64_t* a0, const uint64_t* b0, const double* c0, double E0, int do_grow,
                int do_refine, int64_t cap, uint64_t* out_a, uint64_t* out_b, double* out_c, int64_t* n_out,

@@ -69,3 +69,43 @@ def test_synthetic_integrals_recipe(pkg):
     M = V.reshape(144, 144)
     assert np.linalg.eigvalsh(M).min() > -1e-12  # PSD
     assert np.allclose(np.diag(T), -2.0 + 0.25 * np.arange(12))
+
+
+def test_pmc_plugin_surface(pkg):
+    """ProjectedMultiConfigurationCalculator (pmc.hpp:31-150, macis_pmc.cpp:
+    42-178): type and default name, settings, and the errors raised before any
+    device work."""
+    calc = pkg.calculators
+    kind = "projected_multi_configuration_calculator"
+    assert calc.available(kind) == ["gb300_pmc"]
+    c = calc.create(kind)
+    assert c.name() == "gb300_pmc" and c.type_name() == kind
+    s = c.settings()
+    assert s.get("iterative_solver_dimension_cutoff") == 2000 and s.get("ci_matel_tol") == np.finfo(float).eps
+    H = calc.Hamiltonian(np.eye(4), np.zeros(4 ** 4))
+    with pytest.raises(RuntimeError, match="cannot be empty"):
+        c.run(H, [])
+    with pytest.raises(RuntimeError, match="orbital capacity"):
+        calc.create(kind).run(H, ["220"])
+    with pytest.raises(ValueError):
+        calc.create(kind).run(H, ["22x0"])
+    with pytest.raises(ValueError):
+        calc.create(kind).run(H, ["2200u"])  # beyond the active space
+    a, b = calc.Gb300Pmc._parse(["2ud0", (0b11, 0b101)], 4)
+    assert a.tolist() == [0b011, 0b11] and b.tolist() == [0b101, 0b101]
+    # settings are locked once run starts, even when it fails
+    with pytest.raises(calc.SettingsAreLocked):
+        c.settings().set("ci_residual_tolerance", 1e-9)
+
+
+def test_asci_pt2_settings(pkg):
+    """MacisAsciSettings PT2 / constraint defaults (macis_asci.hpp:59-138 from
+    ASCISettings, determinant_search.hpp:113-191)."""
+    s = pkg.calculators.create("multi_configuration_calculator", "gb300_asci").settings()
+    assert s.get("pt2_tol") == 1e-16
+    assert s.get("pt2_reserve_count") == 70000000 and s.get("pt2_bigcon_thresh") == 250
+    assert s.get("pt2_prune") is False and s.get("pt2_precompute_eps") is False
+    assert s.get("pt2_max_constraint_level") == 5 and s.get("pt2_min_constraint_level") == 0
+    assert s.get("constraint_level") == 2 and s.get("pair_size_max") == 500000000
+    with pytest.raises(ValueError):
+        s.set("pt2_tol", 2.0)

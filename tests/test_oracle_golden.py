@@ -131,6 +131,15 @@ def test_h2o_asci_grow_refine_energies(oracle, pkg, h2o, known):
     assert abs(Eg - ref["E0_grow"]) < 1e-8
     assert abs(E - ref["E0_refine"]) < 1e-8
     assert len(a) == 10000 and abs(c @ c - 1.0) < 1e-12
+    # ASCI-PT2 of the refined wavefunction (asci.cxx:556-570); one pass and a
+    # hash-partitioned run agree
+    ept2, npt2 = oracle.asci_pt2(H, a, b, c, E)
+    assert abs(ept2 - ref["EPT2"]) < ref["atol"]
+    e4, n4 = oracle.asci_pt2(H, a, b, c, E, pass_max=1 << 23)
+    assert n4 == npt2 and abs(e4 - ept2) < 1e-14
+    # the reference refuses an unsorted wavefunction (pt2.hpp:79-80)
+    with pytest.raises(RuntimeError, match="Sorted"):
+        oracle.asci_pt2(H, a[::-1].copy(), b[::-1].copy(), c[::-1].copy(), E)
 
 
 def test_n2_asci_energy(oracle, pkg, n2_14e18o, known):
