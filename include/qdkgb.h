@@ -179,6 +179,16 @@ int qdkgb_davidson(qdkgb_context* ctx, const qdkgb_davidson_settings* s, double*
 int qdkgb_rdms_spin_dep(qdkgb_context* ctx, const double* C, double* ordm_aa, double* ordm_bb, double* trdm_aaaa,
                         double* trdm_bbbb, double* trdm_aabb);
 
+/* Orbital entropies of the CI vector C over the context's determinants
+ * (SortedDoubleLoopHamiltonianGenerator::form_entropies, external/macis/
+ * include/macis/hamiltonian_generator/sorted_double_loop.hpp:755-903, with
+ * the orbital-RDM intermediates of include/macis/util/entropies.hpp):
+ * s1[norb] the single-orbital entropies; s2[norb*norb] the two-orbital
+ * entropies and mi[norb*norb] the mutual information s1_i + s1_j - s2_ij
+ * (symmetric, zero diagonal).  s2 and mi may be NULL (both NULL: only the
+ * one-orbital terms are accumulated).  Integrals must be set (orbital count). */
+int qdkgb_orbital_entropies(qdkgb_context* ctx, const double* C, double* s1, double* s2, double* mi);
+
 /* ------------------------------------------------------------ ASCI
  * ASCISettings (external/macis/include/macis/asci/determinant_search.hpp:95-199),
  * the fields the search, grow and refine steps read. */

@@ -677,6 +677,287 @@ void rdms_spin_dep(const uint64_t* alpha, const uint64_t* beta, int64_t nd, cons
   }
 }
 
+// ---------------------------------------------------------------- orbital entropies
+// OrbitalRDMIntermediates and its contribution and assembly functions
+// (include/macis/util/entropies.hpp) driven by the determinant-pair loop of
+// SortedDoubleLoopHamiltonianGenerator::form_entropies
+// (include/macis/hamiltonian_generator/sorted_double_loop.hpp:755-903).  The
+// n x n intermediates are indexed M(i, j) = m[i * n + j]; names follow the
+// reference's (a/b: alpha/beta; ii, ij, iijj ...: orbital pattern).
+struct OrbInter {
+  int n = 0;
+  bool s2 = false;
+  std::vector<double> a_ii, b_ii, ab_iiii;
+  enum {
+    A_IJ, B_IJ, AA_IIJJ, BB_IIJJ, AB_IIJJ, AB_IJJJ, AB_JIJJ, AB_JJIJ, AB_JJJI, AB_IJIJ, AB_IJJI, AAB_IIJJJJ,
+    ABB_JJIIJJ, AAB_IIJJII, ABB_IIIIJJ, ABB_IJIIJJ, AAB_IIJJIJ, AABB_IIJJIIJJ, NMAT
+  };
+  std::vector<double> m[NMAT];
+  void init(int norb, bool need_s2) {
+    n = norb;
+    s2 = need_s2;
+    a_ii.assign(n, 0.);
+    b_ii.assign(n, 0.);
+    ab_iiii.assign(n, 0.);
+    for (auto& x : m) x.assign(need_s2 ? (size_t)n * n : 0, 0.);
+  }
+  double& M(int k, uint32_t i, uint32_t j) { return m[k][(size_t)i * n + j]; }
+  double M(int k, uint32_t i, uint32_t j) const { return m[k][(size_t)i * n + j]; }
+  void add(const OrbInter& o) {
+    for (int i = 0; i < n; ++i) {
+      a_ii[i] += o.a_ii[i];
+      b_ii[i] += o.b_ii[i];
+      ab_iiii[i] += o.ab_iiii[i];
+    }
+    for (int k = 0; k < NMAT; ++k)
+      for (size_t i = 0; i < m[k].size(); ++i) m[k][i] += o.m[k][i];
+  }
+};
+
+// orbital_rdm_contrib_diag_s1 / orbital_rdm_contrib_diag (entropies.hpp:155-253)
+void orb_diag(OrbInter& X, const std::vector<uint32_t>& oa, const std::vector<uint32_t>& ob, double val) {
+  for (auto p : oa) X.a_ii[p] += val;
+  for (auto p : ob) X.b_ii[p] += val;
+  if (!X.s2) {
+    for (auto q : ob)
+      for (auto p : oa)
+        if (p == q) X.ab_iiii[q] += val;
+    return;
+  }
+  std::vector<char> isa(X.n, 0), isb(X.n, 0);
+  for (auto p : oa) isa[p] = 1;
+  for (auto p : ob) isb[p] = 1;
+  for (auto q : oa)
+    for (auto p : oa) {
+      if (p == q) continue;
+      X.M(OrbInter::AA_IIJJ, p, q) += val;
+      if (isb[p]) {
+        X.M(OrbInter::AAB_IIJJII, p, q) += val;
+        if (isb[q]) X.M(OrbInter::AABB_IIJJIIJJ, p, q) += val;
+      }
+      if (isb[q]) X.M(OrbInter::AAB_IIJJJJ, p, q) += val;
+    }
+  for (auto q : ob)
+    for (auto p : ob) {
+      if (p == q) continue;
+      X.M(OrbInter::BB_IIJJ, p, q) += val;
+      if (isa[p]) X.M(OrbInter::ABB_JJIIJJ, q, p) += val;
+      if (isa[q]) X.M(OrbInter::ABB_IIIIJJ, q, p) += val;
+    }
+  for (auto q : ob)
+    for (auto p : oa) {
+      if (p == q) X.ab_iiii[q] += val;
+      X.M(OrbInter::AB_IIJJ, p, q) += val;
+    }
+}
+
+// orbital_rdm_contrib_2<transpose> (entropies.hpp:255-313): a single
+// excitation of one spin (beta when transposed); occ_os = the other spin's
+// occupied orbitals of the bra
+void orb_single(OrbInter& X, bool transpose, uint64_t bra, uint64_t ket, uint64_t ex,
+                const std::vector<uint32_t>& occ_os, double val) {
+  const Single s = single_excitation_sign_indices(bra, ket, ex);
+  const uint32_t o1 = s.o, v1 = s.v;
+  const double sv = s.sign * val;
+  const int xij = transpose ? OrbInter::B_IJ : OrbInter::A_IJ;
+  X.M(xij, v1, o1) += sv;
+  X.M(xij, o1, v1) += sv;
+  const int k1 = transpose ? OrbInter::AB_JJIJ : OrbInter::AB_IJJJ;
+  const int k2 = transpose ? OrbInter::AB_JJJI : OrbInter::AB_JIJJ;
+  bool o_in = false, v_in = false;
+  for (auto p : occ_os) {
+    if (o1 == p) {
+      o_in = true;
+      X.M(k1, v1, o1) += sv;
+      X.M(k2, v1, o1) += sv;
+    } else if (v1 == p) {
+      v_in = true;
+      X.M(k1, o1, v1) += sv;
+      X.M(k2, o1, v1) += sv;
+    }
+  }
+  if (o_in && v_in) {
+    const int k3 = transpose ? OrbInter::AAB_IIJJIJ : OrbInter::ABB_IJIIJJ;
+    X.M(k3, o1, v1) += sv;
+    X.M(k3, v1, o1) += sv;
+  }
+}
+
+// orbital_rdm_contrib_22 (entropies.hpp:315-340): one single per spin
+void orb_double_os(OrbInter& X, uint64_t ba, uint64_t ka, uint64_t exa, uint64_t bb, uint64_t kb, uint64_t exb,
+                   double val) {
+  const Single sa = single_excitation_sign_indices(ba, ka, exa);  // (o2, v2)
+  const Single sb = single_excitation_sign_indices(bb, kb, exb);  // (o1, v1)
+  const double sv = sa.sign * sb.sign * val;
+  const uint32_t o1 = sb.o, v1 = sb.v, o2 = sa.o, v2 = sa.v;
+  if (o1 == o2 && v1 == v2) {
+    X.M(OrbInter::AB_IJIJ, v1, o1) += sv;
+    X.M(OrbInter::AB_IJIJ, o1, v1) += sv;
+  } else if (o1 == v2 && v1 == o2) {
+    X.M(OrbInter::AB_IJJI, v1, o1) += sv;
+    X.M(OrbInter::AB_IJJI, o1, v1) += sv;
+  }
+}
+
+void orb_entropy_pairs(OrbInter& X, const uint64_t* alpha, const uint64_t* beta, int64_t nd, const double* C) {
+  std::vector<uint64_t> ua;
+  std::vector<int64_t> off;
+  unique_alpha(alpha, nd, ua, off);
+  const int64_t nu = (int64_t)ua.size();
+  const int lim = X.s2 ? 2 : 0;
+  int nth = 1;
+#ifdef _OPENMP
+  nth = omp_get_max_threads();
+#endif
+  std::vector<OrbInter> part(nth);
+  for (auto& p : part) p.init(X.n, X.s2);
+#pragma omp parallel
+  {
+    int tid = 0;
+#ifdef _OPENMP
+    tid = omp_get_thread_num();
+#endif
+    OrbInter& Y = part[tid];
+    std::vector<uint32_t> oa, ob;
+#pragma omp for schedule(dynamic)
+    for (int64_t ib = 0; ib < nu; ++ib) {
+      if (!ua[ib]) continue;
+      const uint64_t ba = ua[ib];
+      for (int64_t ik = ib; ik < nu; ++ik) {
+        if (!ua[ik]) continue;
+        const uint64_t ka = ua[ik];
+        const uint64_t exa = ba ^ ka;
+        const int ca = popc(exa);
+        if (ca > lim) continue;
+        bits_to_indices(ba, oa);
+        for (int64_t i = off[ib]; i < off[ib + 1]; ++i) {
+          const uint64_t bb = beta[i];
+          bits_to_indices(bb, ob);
+          for (int64_t j = off[ik]; j < off[ik + 1]; ++j) {
+            if (j < i) continue;
+            const uint64_t kb = beta[j];
+            const uint64_t exb = bb ^ kb;
+            const int cb = popc(exb);
+            if (cb > lim) continue;
+            const double val = C[i] * C[j];
+            if (!(std::abs(val) > 1e-16)) continue;
+            // eval_ordm_intermediates (entropies.hpp:662-719)
+            if (ca == 0 && cb == 0)
+              orb_diag(Y, oa, ob, val);
+            else if (!X.s2)
+              continue;
+            else if (ca == 2 && cb == 0)
+              orb_single(Y, false, ba, ka, exa, ob, val);
+            else if (ca == 0 && cb == 2)
+              orb_single(Y, true, bb, kb, exb, oa, val);
+            else
+              orb_double_os(Y, ba, ka, exa, bb, kb, exb, val);
+          }
+        }
+      }
+    }
+  }
+  for (auto& p : part) X.add(p);
+}
+
+inline void add_ent(double& s, double v) {
+  if (v > std::numeric_limits<double>::epsilon()) s -= v * std::log(v);
+}
+
+// build_s1_entropy (entropies.hpp:342-370)
+void build_s1(const OrbInter& X, double* s1) {
+  for (int i = 0; i < X.n; ++i) {
+    double s = 0.;
+    add_ent(s, 1 - X.a_ii[i] - X.b_ii[i] + X.ab_iiii[i]);
+    add_ent(s, X.a_ii[i] - X.ab_iiii[i]);
+    add_ent(s, X.b_ii[i] - X.ab_iiii[i]);
+    add_ent(s, X.ab_iiii[i]);
+    s1[i] = s;
+  }
+}
+
+// build_s2_entropy (entropies.hpp:397-528): the two-orbital RDM of (i, j) in
+// its symmetry blocks (1 + 2x2 + 2x2 + 1 + 1 + 4x4 + 2x2 + 2x2 + 1), the
+// entropy of their eigenvalues
+void build_s2(const OrbInter& X, double* s2) {
+  using O = OrbInter;
+  const int n = X.n;
+  auto eig2 = [](double a, double b, double d, double& s) {
+    const double hs = 0.5 * (a + d), hd = 0.5 * (a - d);
+    const double w = std::sqrt(hd * hd + b * b);
+    add_ent(s, hs - w);
+    add_ent(s, hs + w);
+  };
+  for (int i = 0; i < n; ++i) {
+    s2[(size_t)i * n + i] = 0.;
+    for (int j = i + 1; j < n; ++j) {
+      auto M = [&](int k, int p, int q) { return X.M(k, p, q); };
+      const double aabb = M(O::AABB_IIJJIIJJ, i, j);
+      double s = 0.;
+      add_ent(s, 1 - X.a_ii[i] - X.b_ii[i] - X.a_ii[j] - X.b_ii[j] + X.ab_iiii[i] + X.ab_iiii[j] +
+                     M(O::AA_IIJJ, i, j) + M(O::AB_IIJJ, i, j) + M(O::AB_IIJJ, j, i) + M(O::BB_IIJJ, i, j) -
+                     M(O::AAB_IIJJJJ, i, j) - M(O::ABB_JJIIJJ, i, j) - M(O::AAB_IIJJII, i, j) -
+                     M(O::ABB_IIIIJJ, i, j) + aabb);
+      eig2(X.a_ii[j] - M(O::AB_IIJJ, j, i) - M(O::AA_IIJJ, i, j) - M(O::AB_IIJJ, j, j) + M(O::AAB_IIJJJJ, i, j) +
+               M(O::AAB_IIJJII, i, j) + M(O::ABB_JJIIJJ, i, j) - aabb,
+           M(O::A_IJ, i, j) - M(O::AB_JIJJ, j, i) - M(O::AB_IJJJ, i, j) + M(O::ABB_IJIIJJ, i, j),
+           X.a_ii[i] - M(O::AB_IIJJ, i, j) - M(O::AA_IIJJ, i, j) - M(O::AB_IIJJ, i, i) + M(O::AAB_IIJJJJ, i, j) +
+               M(O::AAB_IIJJII, i, j) + M(O::ABB_IIIIJJ, i, j) - aabb,
+           s);
+      eig2(X.b_ii[j] - M(O::AB_IIJJ, i, j) - M(O::BB_IIJJ, i, j) - M(O::AB_IIJJ, j, j) + M(O::ABB_IIIIJJ, i, j) +
+               M(O::AAB_IIJJJJ, i, j) + M(O::ABB_JJIIJJ, i, j) - aabb,
+           M(O::B_IJ, i, j) - M(O::AB_JJIJ, j, i) - M(O::AB_JJJI, i, j) + M(O::AAB_IIJJIJ, i, j),
+           X.b_ii[i] - M(O::AB_IIJJ, j, i) - M(O::BB_IIJJ, i, j) - M(O::AB_IIJJ, i, i) + M(O::ABB_JJIIJJ, i, j) +
+               M(O::AAB_IIJJII, i, j) + M(O::ABB_IIIIJJ, i, j) - aabb,
+           s);
+      add_ent(s, M(O::AA_IIJJ, i, j) - M(O::AAB_IIJJII, i, j) - M(O::AAB_IIJJJJ, i, j) + aabb);
+      add_ent(s, M(O::BB_IIJJ, i, j) - M(O::ABB_IIIIJJ, i, j) - M(O::ABB_JJIIJJ, i, j) + aabb);
+      double B[16];
+      B[0] = M(O::AB_IIJJ, j, j) - M(O::AAB_IIJJJJ, i, j) - M(O::ABB_JJIIJJ, i, j) + aabb;
+      B[1] = B[4] = M(O::AB_IJJJ, i, j) - M(O::ABB_IJIIJJ, i, j);
+      B[2] = B[8] = -M(O::AB_JJIJ, i, j) + M(O::AAB_IIJJIJ, i, j);
+      B[3] = B[12] = M(O::AB_IJIJ, i, j);
+      B[5] = M(O::AB_IIJJ, i, j) - M(O::ABB_IIIIJJ, i, j) - M(O::AAB_IIJJJJ, i, j) + aabb;
+      B[6] = B[9] = -M(O::AB_IJJI, j, i);
+      B[7] = B[13] = M(O::AB_JJJI, j, i) - M(O::AAB_IIJJIJ, i, j);
+      B[10] = M(O::AB_IIJJ, j, i) - M(O::AAB_IIJJII, i, j) - M(O::ABB_JJIIJJ, i, j) + aabb;
+      B[11] = B[14] = -M(O::AB_JIJJ, j, i) + M(O::ABB_IJIIJJ, i, j);
+      B[15] = X.ab_iiii[i] - M(O::AAB_IIJJII, i, j) - M(O::ABB_IIIIJJ, i, j) + aabb;
+      double w4[4];
+      jacobi_syev(4, B, 4, w4);
+      for (double v : w4) add_ent(s, v);
+      eig2(M(O::AAB_IIJJJJ, i, j) - aabb, -M(O::AAB_IIJJIJ, i, j), M(O::AAB_IIJJII, i, j) - aabb, s);
+      eig2(M(O::ABB_JJIIJJ, i, j) - aabb, -M(O::ABB_IJIIJJ, i, j), M(O::ABB_IIIIJJ, i, j) - aabb, s);
+      add_ent(s, aabb);
+      s2[(size_t)i * n + j] = s2[(size_t)j * n + i] = s;
+    }
+  }
+}
+
+// form_entropies on a determinant list: s1 (n), s2 and mi (n x n, either may
+// be null); mutual information I_ij = s1_i + s1_j - s2_ij (entropies.hpp:
+// 638-651)
+void form_entropies(int n, const uint64_t* alpha, const uint64_t* beta, int64_t nd, const double* C, double* s1,
+                    double* s2, double* mi) {
+  OrbInter X;
+  X.init(n, s2 || mi);
+  orb_entropy_pairs(X, alpha, beta, nd, C);
+  build_s1(X, s1);
+  if (!X.s2) return;
+  std::vector<double> loc;
+  double* t = s2;
+  if (!t) {
+    loc.assign((size_t)n * n, 0.);
+    t = loc.data();
+  }
+  build_s2(X, t);
+  if (mi)
+    for (int i = 0; i < n; ++i) {
+      mi[(size_t)i * n + i] = 0.;
+      for (int j = i + 1; j < n; ++j) mi[(size_t)i * n + j] = mi[(size_t)j * n + i] = s1[i] + s1[j] - t[(size_t)i * n + j];
+    }
+}
+
 // A bounded sample of the reference's symmetric SDL H build for timing on the
 // host: the count and fill passes of build_csr_sdl (sorted_double_loop.hpp:
 // 137-360) for the bra alpha groups ib = offset, offset + stride, ...
@@ -1476,6 +1757,12 @@ int orc_asci_pt2(void* h, int64_t nd, const uint64_t* a, const uint64_t* b, cons
     std::vector<double> C(c, c + nd);
     *ept2 = asci_pt2(H, dets, C, E0, tol, npt2, pass_max > 0 ? pass_max : (int64_t)1 << 25);
   });
+}
+
+// orbital entropies of a CI vector; s2 / mi may be null; 0 on success
+int orc_entropies(int n, const uint64_t* alpha, const uint64_t* beta, int64_t nd, const double* C, double* s1,
+                  double* s2, double* mi) {
+  return guard([&] { form_entropies(n, alpha, beta, nd, C, s1, s2, mi); });
 }
 
 int64_t orc_sdl_sample(void* h, const uint64_t* alpha, const uint64_t* beta, int64_t nd, double thresh, int64_t stride,

@@ -67,6 +67,8 @@ def lib():
                                ctypes.POINTER(f64), ctypes.POINTER(f64)]
         L.orc_asci_search.restype = i64
         L.orc_asci_search.argtypes = [vp, _f64p, i64, _u64p, _u64p, _f64p, f64, i64, i64, _u64p, _u64p]
+        L.orc_entropies.restype = ci
+        L.orc_entropies.argtypes = [ci, _u64p, _u64p, i64, _f64p, _f64p, _f64p, _f64p]
         L.orc_asci_pt2.restype = ci
         L.orc_asci_pt2.argtypes = [vp, i64, _u64p, _u64p, _f64p, f64, f64, i64, ctypes.POINTER(f64),
                                    ctypes.POINTER(i64)]
@@ -293,3 +295,18 @@ def asci_pt2(ham, alpha, beta, c, E0, pt2_tol=1e-16, pass_max=0):
     if rc != 0:
         raise RuntimeError(lib().orc_last_error().decode())
     return e.value, npt.value
+
+
+def entropies(norb, alpha, beta, C):
+    """form_entropies (sorted_double_loop.hpp:755-903, entropies.hpp):
+    (single-orbital entropies (n), two-orbital entropies (n x n), mutual
+    information (n x n))."""
+    n = int(norb)
+    s1 = np.zeros(n)
+    s2 = np.zeros((n, n))
+    mi = np.zeros((n, n))
+    rc = lib().orc_entropies(n, np.ascontiguousarray(alpha, dtype=np.uint64), np.ascontiguousarray(beta, dtype=np.uint64),
+                             len(alpha), np.ascontiguousarray(C, dtype=np.float64), s1, s2, mi)
+    if rc != 0:
+        raise RuntimeError(lib().orc_last_error().decode())
+    return s1, s2, mi

@@ -146,12 +146,13 @@ class Wavefunction:
     the reference builds (macis_base.hpp:134-283).  The spin-resolved two-body
     RDMs carry the reference's factor 2 (macis_base.hpp:203-212)."""
 
-    def __init__(self, norb, alpha, beta, coeffs, rdms=None):
+    def __init__(self, norb, alpha, beta, coeffs, rdms=None, entropies=None):
         self.norb = norb
         self.alpha = np.asarray(alpha, dtype=np.uint64)
         self.beta = np.asarray(beta, dtype=np.uint64)
         self.coefficients = np.asarray(coeffs, dtype=np.float64)
         self._rdms = rdms or {}
+        self._ent = entropies or {}
 
     def size(self):
         return len(self.coefficients)
@@ -180,6 +181,30 @@ class Wavefunction:
             raise RuntimeError("two-body RDM was not requested (calculate_two_rdm)")
         f = lambda t: 2.0 * t.ravel(order="F")
         return f(self._rdms["aabb"]), f(self._rdms["aaaa"]), f(self._rdms["bbbb"])
+
+    def has_single_orbital_entropies(self):
+        return "s1" in self._ent
+
+    def has_two_orbital_entropies(self):
+        return "s2" in self._ent
+
+    def has_mutual_information(self):
+        return "mi" in self._ent
+
+    def get_single_orbital_entropies(self):
+        if "s1" not in self._ent:
+            raise RuntimeError("single-orbital entropies were not requested (calculate_single_orbital_entropies)")
+        return self._ent["s1"]
+
+    def get_two_orbital_entropies(self):
+        if "s2" not in self._ent:
+            raise RuntimeError("two-orbital entropies were not requested (calculate_two_orbital_entropies)")
+        return self._ent["s2"]
+
+    def get_mutual_information(self):
+        if "mi" not in self._ent:
+            raise RuntimeError("mutual information was not requested (calculate_mutual_information)")
+        return self._ent["mi"]
 
     def get_active_two_rdm_spin_traced(self):
         """MACIS spin-traced 2-RDM (E = T.g + V.G): aaaa + bbbb + aabb + aabb^T(rs,pq)."""
@@ -216,11 +241,24 @@ class MultiConfigurationCalculator:
 
     # shared by the CI plugins
     def _check_unsupported(self):
+        pass
+
+    def _entropies(self, ctx, C):
+        """Orbital entropies / mutual information of C over the context's
+        determinants when the settings ask for them (form_entropies)."""
         s = self._settings
-        for k in ("calculate_single_orbital_entropies", "calculate_two_orbital_entropies",
-                  "calculate_mutual_information"):
-            if s.get(k):
-                raise NotImplementedError("%s is outside this GPU core (orbital entropies)" % k)
+        w1 = s.get("calculate_single_orbital_entropies")
+        w2 = s.get("calculate_two_orbital_entropies")
+        wm = s.get("calculate_mutual_information")
+        if not (w1 or w2 or wm):
+            return None
+        s1, s2, mi = ctx.orbital_entropies(C, two_orbital=w2, mutual_information=wm)
+        out = {"s1": s1}
+        if w2:
+            out["s2"] = s2
+        if wm:
+            out["mi"] = mi
+        return out
 
     def _solve(self, ctx, hamiltonian, a, b):
         """H build + Davidson (+ RDMs) on a determinant list; returns (E_total, Wavefunction)."""
@@ -250,7 +288,7 @@ class MultiConfigurationCalculator:
             want += ["aaaa", "bbbb", "aabb"]
         if want:
             rdms = ctx.rdms_spin_dep(C, want=tuple(want))
-        wfn = Wavefunction(hamiltonian.norb, a, b, C, rdms)
+        wfn = Wavefunction(hamiltonian.norb, a, b, C, rdms, self._entropies(ctx, C))
         wfn.info = info
         return E + hamiltonian.get_core_energy(), wfn
 
@@ -367,10 +405,14 @@ class Gb300Asci(MultiConfigurationCalculator):
                 want += ["aa", "bb"]
             if s.get("calculate_two_rdm"):
                 want += ["aaaa", "bbbb", "aabb"]
-            if want:
+            ent = None
+            if want or any(s.get(k) for k in ("calculate_single_orbital_entropies",
+                                               "calculate_two_orbital_entropies", "calculate_mutual_information")):
                 ctx.set_dets(a, b)
-                rdms = ctx.rdms_spin_dep(C, want=tuple(want))
-        wfn = Wavefunction(n, a, b, C, rdms)
+                if want:
+                    rdms = ctx.rdms_spin_dep(C, want=tuple(want))
+                ent = self._entropies(ctx, C)
+        wfn = Wavefunction(n, a, b, C, rdms, ent)
         return E + hamiltonian.get_core_energy(), wfn
 
 
@@ -441,14 +483,14 @@ class Gb300Pmc(ProjectedMultiConfigurationCalculator):
                 want = self._rdm_blocks()
                 if want:
                     rdms = ctx.rdms_spin_dep(C, want=want)
-                return E + hamiltonian.get_core_energy(), Wavefunction(n, a, b, C, rdms)
+                return E + hamiltonian.get_core_energy(), Wavefunction(n, a, b, C, rdms, self._entropies(ctx, C))
             # solved on the spin-sorted list (the layout the H build groups by
             # alpha string), the CI vector returned in the caller's order
             order = np.lexsort((b, a))
             E, ws = self._solve(ctx, hamiltonian, a[order], b[order])
             C = np.empty_like(ws.coefficients)
             C[order] = ws.coefficients
-            wfn = Wavefunction(n, a, b, C, ws._rdms)
+            wfn = Wavefunction(n, a, b, C, ws._rdms, ws._ent)
             wfn.info = ws.info
             return E, wfn
 

@@ -35,7 +35,7 @@ EXPORTED = [
     "qdkgb_operator_layout",
     "qdkgb_set_integrals", "qdkgb_fci_dets", "qdkgb_set_dets", "qdkgb_build_hamiltonian", "qdkgb_get_csr32",
     "qdkgb_get_csr64", "qdkgb_diagonal", "qdkgb_spmv", "qdkgb_spmv_device", "qdkgb_davidson_default_settings",
-    "qdkgb_davidson", "qdkgb_rdms_spin_dep", "qdkgb_casci", "qdkgb_version", "qdkgb_kernel_launches",
+    "qdkgb_davidson", "qdkgb_rdms_spin_dep", "qdkgb_orbital_entropies", "qdkgb_casci", "qdkgb_version", "qdkgb_kernel_launches",
     "qdkgb_sigma_split_noalloc", "qdkgb_set_csr", "qdkgb_build_direct_sigma",
     "qdkgb_asci_default_settings", "qdkgb_asci_search", "qdkgb_asci", "qdkgb_asci_pt2",
     "qdkgb_batch_default_settings", "qdkgb_casci_batch",
@@ -135,6 +135,7 @@ def lib():
     L.qdkgb_davidson_default_settings.restype = None
     L.qdkgb_davidson.argtypes = [vp, P(DavidsonSettings), P(dp), vp, P(DavidsonInfo)]
     L.qdkgb_rdms_spin_dep.argtypes = [vp, vp, vp, vp, vp, vp, vp]
+    L.qdkgb_orbital_entropies.argtypes = [vp, vp, vp, vp, vp]
     L.qdkgb_casci.argtypes = [vp, ci, ci, ci, vp, vp, ci, P(DavidsonSettings), dp, P(dp), vp, P(DavidsonInfo)]
     L.qdkgb_version.restype = ctypes.c_char_p
     L.qdkgb_kernel_launches.restype = ctypes.c_int64
@@ -349,6 +350,19 @@ class Context:
                 ptrs.append(None)
         self._check(lib().qdkgb_rdms_spin_dep(self._h, _ptr(C), *ptrs))
         return {k: v.reshape((n, n) if len(k) == 2 else (n, n, n, n), order="F") for k, v in bufs.items()}
+
+    def orbital_entropies(self, C, two_orbital=True, mutual_information=True):
+        """(single-orbital entropies (n), two-orbital entropies (n x n) or None,
+        mutual information (n x n) or None) of C over the current determinants
+        (qdkgb_orbital_entropies)."""
+        n = self.norb
+        C = _f64(C)
+        s1 = np.zeros(n)
+        s2 = np.zeros((n, n)) if two_orbital else None
+        mi = np.zeros((n, n)) if mutual_information else None
+        self._check(lib().qdkgb_orbital_entropies(self._h, _ptr(C), _ptr(s1), _ptr(s2) if s2 is not None else None,
+                                                  _ptr(mi) if mi is not None else None))
+        return s1, s2, mi
 
     def casci(self, T, V, nalpha, nbeta, max_m=200, tol=1e-8, precision=PREC_FP64, matel_tol=np.finfo(float).eps,
               want_vector=True):

@@ -385,6 +385,11 @@ void asci_search_gpu(Context* c, int64_t ncore, const uint64_t* ca, const uint64
   if (!c->have_ints) throw Error(QDKGB_ERR_STATE, "integrals not set");
   if (ncore <= 0) throw Error(QDKGB_ERR_INVALID, "empty core");
   const int n = c->norb;
+  {
+    uint64_t u = 0;
+    for (int64_t i = 0; i < ncore; ++i) u |= ca[i] | cb[i];
+    if (n < 64 && (u >> n)) throw Error(QDKGB_ERR_INVALID, "a determinant occupies an orbital beyond the integrals' norb");
+  }
   // table capacity from the number of contributions (a bound on distinct targets)
   int64_t total = ncore;
   for (int64_t i = 0; i < ncore; ++i) {
@@ -515,6 +520,11 @@ double asci_pt2_gpu(Context* c, int64_t nd, const uint64_t* a, const uint64_t* b
     if (a[i] < a[i - 1] || (a[i] == a[i - 1] && b[i] < b[i - 1]))
       throw Error(QDKGB_ERR_INVALID, "PT2 Only Works with Sorted Wfns");
   const int n = c->norb;
+  {
+    uint64_t u = 0;
+    for (int64_t i = 0; i < nd; ++i) u |= a[i] | b[i];
+    if (n < 64 && (u >> n)) throw Error(QDKGB_ERR_INVALID, "a determinant occupies an orbital beyond the integrals' norb");
+  }
   int64_t total = nd;
   for (int64_t i = 0; i < nd; ++i) {
     const int ka = __builtin_popcountll(a[i]), kb = __builtin_popcountll(b[i]);

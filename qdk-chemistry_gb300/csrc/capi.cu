@@ -413,6 +413,16 @@ int qdkgb_rdms_spin_dep(qdkgb_context* c, const double* C, double* aa, double* b
   });
 }
 
+int qdkgb_orbital_entropies(qdkgb_context* c, const double* C, double* s1, double* s2, double* mi) {
+  if (!c) return QDKGB_ERR_INVALID;
+  return guarded(c, [&] {
+    if (!C || !s1) throw Error(QDKGB_ERR_INVALID, "null argument");
+    if (!c->have_dets) throw Error(QDKGB_ERR_STATE, "determinants not set");
+    QDKGB_CUDA(cudaSetDevice(c->device));
+    orbital_entropies(c, C, s1, s2, mi);
+  });
+}
+
 void qdkgb_asci_default_settings(qdkgb_asci_settings* s) {
   if (!s) return;
   s->ntdets_max = 100000;

@@ -260,6 +260,7 @@ void build_det_space(Context* c, int64_t nd, const uint64_t* alpha, const uint64
   D.ndets = nd;
   D.h_alpha.assign(alpha, alpha + nd);
   D.h_beta.assign(beta, beta + nd);
+  for (int64_t i = 0; i < nd; ++i) D.occ_union |= alpha[i] | beta[i];
   D.h_gstart.push_back(0);
   D.h_galpha.push_back(alpha[0]);
   for (int64_t i = 1; i < nd; ++i)
@@ -638,9 +639,15 @@ RowArgs row_args(Context* c, double thresh) {
   return a;
 }
 
+void check_dets_in_orbitals(const Context* c) {
+  if (c->norb < 64 && (c->dets.occ_union >> c->norb))
+    throw Error(QDKGB_ERR_INVALID, "a determinant occupies an orbital beyond the integrals' norb");
+}
+
 void build_hamiltonian(Context* c, double thresh, int storage) {
   if (!c->have_ints) throw Error(QDKGB_ERR_STATE, "integrals not set");
   if (!c->have_dets) throw Error(QDKGB_ERR_STATE, "determinants not set");
+  check_dets_in_orbitals(c);
   if (storage != QDKGB_H_FP64 && storage != QDKGB_H_SPLIT32) throw Error(QDKGB_ERR_INVALID, "unknown storage");
   Hcsr& H = c->H;
   H.valid = false;

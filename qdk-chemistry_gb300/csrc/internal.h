@@ -65,6 +65,7 @@ struct DetSpace {
   int64_t ngroups = 0;  // alpha groups (runs of equal alpha strings)
   int64_t nbeta = 0;    // distinct beta strings
   bool product = false; // every group holds every beta string (FCI-like)
+  uint64_t occ_union = 0;  // OR of every alpha and beta string (orbitals in use)
   std::vector<uint64_t> h_alpha, h_beta;
   std::vector<uint64_t> h_galpha;
   std::vector<uint64_t> h_ubeta;  // distinct beta strings in rank order
@@ -115,6 +116,9 @@ struct Context {
 };
 
 Integrals integrals_view(Context* c);
+// throws QDKGB_ERR_INVALID when a determinant occupies an orbital >= norb
+// (the integral and RDM indices of the kernels stop at norb)
+void check_dets_in_orbitals(const Context* c);
 
 // hbuild.cu
 void build_integral_intermediates(Context* c);
@@ -174,6 +178,7 @@ void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C
 
 // rdm.cu
 void rdms_spin_dep(Context* c, const double* C, double* aa, double* bb, double* aaaa, double* bbbb, double* aabb);
+void orbital_entropies(Context* c, const double* C, double* s1, double* s2, double* mi);
 
 }  // namespace qdkgb
 
