@@ -246,6 +246,38 @@ int qdkgb_asci(qdkgb_context* ctx, const qdkgb_asci_settings* s, const qdkgb_dav
 int qdkgb_asci_pt2(qdkgb_context* ctx, int64_t ndets, const uint64_t* alpha, const uint64_t* beta, const double* C,
                    double E0, double pt2_tol, int64_t max_slots, double* ept2, int64_t* n_external);
 
+/* ------------------------------------------------------------ CASSCF
+ * MCSCFSettings (external/macis/include/macis/mcscf/mcscf.hpp:22-52). */
+typedef struct qdkgb_mcscf_settings {
+  int64_t max_macro_iter;  /* default 100 */
+  double max_orbital_step; /* default 0.5 */
+  double orb_grad_tol;     /* orb_grad_tol_mcscf, RMS of the orbital gradient (default 5e-6) */
+  int enable_diis;         /* default 1 */
+  int64_t diis_start_iter; /* default 3 */
+  int64_t diis_nkeep;      /* default 10 */
+  double ci_res_tol;       /* default 1e-8 */
+  int64_t ci_max_subspace; /* default 200 (at most 254 here) */
+  double ci_matel_tol;     /* default machine epsilon */
+} qdkgb_mcscf_settings;
+
+void qdkgb_mcscf_default_settings(qdkgb_mcscf_settings* s);
+
+/* CASSCF (casscf_diis, external/macis/include/macis/mcscf/mcscf.hpp:54-60,
+ * mcscf_impl.hpp:25-262): orbital optimisation of a CAS(nalpha + nbeta
+ * electrons, nact orbitals) wavefunction over norb molecular orbitals (ninact
+ * doubly occupied below the active ones, the rest virtual), from the
+ * column-major full integrals T (norb^2) and V (norb^4) and the core energy;
+ * the CASCI and RDMs of every macro iteration and the integral transform run
+ * on the device.  A1 (nact^2) / A2 (nact^4) are the spin-traced active RDMs:
+ * used as the start when trace(A1) = nalpha + nbeta, overwritten with the
+ * final ones.  *E receives the total energy (also when not converged, as the
+ * reference returns it); U (norb^2, may be NULL) the total orbital rotation;
+ * *iterations and *converged (may be NULL) the macro iterations and the
+ * convergence flag. */
+int qdkgb_casscf(qdkgb_context* ctx, const qdkgb_mcscf_settings* s, int nalpha, int nbeta, int norb, int ninact,
+                 int nact, double E_core, const double* T, const double* V, double* A1, double* A2, double* E,
+                 double* U, int64_t* iterations, int* converged);
+
 /* ------------------------------------------------------------ CASCI driver
  * cas_helper::impl / compute_casci_rdms (cpp/src/qdk/chemistry/algorithms/
  * microsoft/macis_cas.cpp:35-117, include/macis/mcscf/cas.hpp:33-64): FCI

@@ -35,7 +35,8 @@ EXPORTED = [
     "qdkgb_operator_layout",
     "qdkgb_set_integrals", "qdkgb_fci_dets", "qdkgb_set_dets", "qdkgb_build_hamiltonian", "qdkgb_get_csr32",
     "qdkgb_get_csr64", "qdkgb_diagonal", "qdkgb_spmv", "qdkgb_spmv_device", "qdkgb_davidson_default_settings",
-    "qdkgb_davidson", "qdkgb_rdms_spin_dep", "qdkgb_orbital_entropies", "qdkgb_casci", "qdkgb_version", "qdkgb_kernel_launches",
+    "qdkgb_davidson", "qdkgb_rdms_spin_dep", "qdkgb_orbital_entropies", "qdkgb_casci",
+    "qdkgb_mcscf_default_settings", "qdkgb_casscf", "qdkgb_version", "qdkgb_kernel_launches",
     "qdkgb_sigma_split_noalloc", "qdkgb_set_csr", "qdkgb_build_direct_sigma",
     "qdkgb_asci_default_settings", "qdkgb_asci_search", "qdkgb_asci", "qdkgb_asci_pt2",
     "qdkgb_batch_default_settings", "qdkgb_casci_batch",
@@ -55,6 +56,14 @@ class NotConverged(QdkgbError):
 class DavidsonSettings(ctypes.Structure):
     _fields_ = [("max_m", ctypes.c_int64), ("res_tol", ctypes.c_double), ("precision", ctypes.c_int),
                 ("use_guess", ctypes.c_int), ("min_abs_denominator", ctypes.c_double)]
+
+
+class McscfSettings(ctypes.Structure):
+    """qdkgb_mcscf_settings (MCSCFSettings, mcscf.hpp:22-52)."""
+    _fields_ = [("max_macro_iter", ctypes.c_int64), ("max_orbital_step", ctypes.c_double),
+                ("orb_grad_tol", ctypes.c_double), ("enable_diis", ctypes.c_int), ("diis_start_iter", ctypes.c_int64),
+                ("diis_nkeep", ctypes.c_int64), ("ci_res_tol", ctypes.c_double), ("ci_max_subspace", ctypes.c_int64),
+                ("ci_matel_tol", ctypes.c_double)]
 
 
 class AsciSettings(ctypes.Structure):
@@ -125,6 +134,9 @@ def lib():
     L.qdkgb_build_direct_sigma.argtypes = [vp]
     L.qdkgb_asci_default_settings.argtypes = [P(AsciSettings)]
     L.qdkgb_asci_default_settings.restype = None
+    L.qdkgb_mcscf_default_settings.argtypes = [P(McscfSettings)]
+    L.qdkgb_mcscf_default_settings.restype = None
+    L.qdkgb_casscf.argtypes = [vp, P(McscfSettings), ci, ci, ci, ci, ci, dp, vp, vp, vp, vp, P(dp), vp, P(i64), P(ci)]
     L.qdkgb_asci_search.argtypes = [vp, P(AsciSettings), i64, vp, vp, vp, dp, i64, i64, vp, vp, P(i64)]
     L.qdkgb_asci_pt2.argtypes = [vp, i64, vp, vp, vp, dp, dp, i64, P(dp), P(i64)]
     L.qdkgb_asci.argtypes = [vp, P(AsciSettings), P(DavidsonSettings), dp, i64, vp, vp, vp, dp, ci, ci, i64, vp, vp, vp,
@@ -192,6 +204,40 @@ def default_asci_settings(**kw):
             raise KeyError(k)
         setattr(s, k, v)
     return s
+
+
+def default_mcscf_settings(**kw):
+    s = McscfSettings()
+    lib().qdkgb_mcscf_default_settings(ctypes.byref(s))
+    for k, v in kw.items():
+        if not hasattr(s, k):
+            raise KeyError(k)
+        setattr(s, k, v)
+    return s
+
+
+def casscf(ctx, T, V, E_core, nalpha, nbeta, ninact, nact, rdm1=None, rdm2=None, **settings):
+    """CASSCF (qdkgb_casscf, casscf_diis mcscf.hpp:54-60) from full molecular-
+    orbital integrals T (n x n) and V (n^4, (pq|rs)); starts from the given
+    spin-traced active RDMs when their trace is the electron count.  Returns
+    (total energy, 1-RDM (nact x nact), 2-RDM (nact^4), orbital rotation U,
+    macro iterations, converged)."""
+    T = np.asarray(T, dtype=np.float64)
+    n = T.shape[0]
+    Tb = _f64(T.ravel(order="F"))
+    Vb = _f64(np.asarray(V, dtype=np.float64).reshape(n, n, n, n).ravel(order="F"))
+    s = default_mcscf_settings(**settings)
+    A1 = np.zeros(nact * nact) if rdm1 is None else _f64(np.asarray(rdm1, dtype=np.float64).ravel(order="F")).copy()
+    A2 = np.zeros(nact ** 4) if rdm2 is None else _f64(np.asarray(rdm2, dtype=np.float64).ravel(order="F")).copy()
+    U = np.zeros(n * n)
+    E = ctypes.c_double()
+    it = ctypes.c_int64()
+    conv = ctypes.c_int()
+    ctx._check(lib().qdkgb_casscf(ctx.handle, ctypes.byref(s), int(nalpha), int(nbeta), n, int(ninact), int(nact),
+                                  float(E_core), _ptr(Tb), _ptr(Vb), _ptr(A1), _ptr(A2), ctypes.byref(E), _ptr(U),
+                                  ctypes.byref(it), ctypes.byref(conv)))
+    return (E.value, A1.reshape(nact, nact, order="F"), A2.reshape((nact,) * 4, order="F"),
+            U.reshape(n, n, order="F"), it.value, bool(conv.value))
 
 
 def default_davidson_settings():

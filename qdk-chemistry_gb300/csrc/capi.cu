@@ -423,6 +423,32 @@ int qdkgb_orbital_entropies(qdkgb_context* c, const double* C, double* s1, doubl
   });
 }
 
+void qdkgb_mcscf_default_settings(qdkgb_mcscf_settings* s) {
+  if (!s) return;
+  s->max_macro_iter = 100;
+  s->max_orbital_step = 0.5;
+  s->orb_grad_tol = 5e-6;
+  s->enable_diis = 1;
+  s->diis_start_iter = 3;
+  s->diis_nkeep = 10;
+  s->ci_res_tol = 1e-8;
+  s->ci_max_subspace = 200;
+  s->ci_matel_tol = std::numeric_limits<double>::epsilon();
+}
+
+int qdkgb_casscf(qdkgb_context* c, const qdkgb_mcscf_settings* s, int nalpha, int nbeta, int norb, int ninact,
+                 int nact, double E_core, const double* T, const double* V, double* A1, double* A2, double* E,
+                 double* U, int64_t* iterations, int* converged) {
+  if (!c) return QDKGB_ERR_INVALID;
+  return guarded(c, [&] {
+    if (!T || !V || !A1 || !A2 || !E) throw Error(QDKGB_ERR_INVALID, "null argument");
+    qdkgb_mcscf_settings def;
+    qdkgb_mcscf_default_settings(&def);
+    QDKGB_CUDA(cudaSetDevice(c->device));
+    *E = casscf(c, s ? *s : def, nalpha, nbeta, norb, ninact, nact, E_core, T, V, A1, A2, U, iterations, converged);
+  });
+}
+
 void qdkgb_asci_default_settings(qdkgb_asci_settings* s) {
   if (!s) return;
   s->ntdets_max = 100000;

@@ -180,6 +180,11 @@ void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C
 void rdms_spin_dep(Context* c, const double* C, double* aa, double* bb, double* aaaa, double* bbbb, double* aabb);
 void orbital_entropies(Context* c, const double* C, double* s1, double* s2, double* mi);
 
+// mcscf.cu
+double casscf(Context* c, const qdkgb_mcscf_settings& S, int nalpha, int nbeta, int norb, int ninact, int nact,
+              double E_core, const double* T0, const double* V0, double* A1, double* A2, double* U_out,
+              int64_t* iterations, int* converged_out);
+
 }  // namespace qdkgb
 
 struct qdkgb_context : qdkgb::Context {};

@@ -79,6 +79,8 @@ def main(ref="/root/reference"):
         "h2o_asci_10k": {"E0_grow": -8.542926580489e01, "E0_refine": -8.542926585527e01, "ntdets_max": 10000,
                          "EPT2": -5.701535028967e-03, "atol": 1e-8,
                          "source": "external/macis/tests/asci.cxx:488-574 (EPT2: :556-570)"},
+        "h2o_casscf": {"E_total": -7.61114493227e01, "ninact": 1, "nact": 8, "nalpha": 4, "nbeta": 4, "atol": 1e-8,
+                       "source": "external/macis/tests/mcscf.cxx:26-66"},
         "o2_rdms": {"n_dets_padded": 5000, "sum_abs_ordm": 8.0000005763, "sum_abs_trdm": 44.1092472977,
                     "atol": 1e-6, "source": "external/macis/tests/double_loop.cxx:506-579"},
     }
