@@ -677,6 +677,107 @@ def run_pt2(args):
     print(json.dumps(line))
 
 
+def run_entropies(args):
+    """Orbital entropies and mutual information (form_entropies) of the
+    CASCI(10e,10o) ground state (63,504 determinants, synthetic integrals of
+    the bench's recipe): a step is one qdkgb_orbital_entropies call from the
+    host CI vector to the host s1 / s2 / I matrices; the CPU baseline runs the
+    oracle's form_entropies on the same vector with every host core."""
+    import torch
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    rank = int(os.environ.get("RANK", "0"))
+    torch.cuda.set_device(local)
+    pkg = _package()
+    pkg.build.build()
+    capi = pkg.capi
+    norb, na = 10, 5
+    T, V, _ = pkg.integrals.synthetic_integrals(norb, 2 * norb, SEED)
+    ctx = capi.Context(local)
+    E, C, _ = ctx.casci(T, V, na, na, tol=1e-8)
+    a, b = capi.fci_dets(norb, na, na)
+    ctx.set_integrals(T, V)
+    ctx.set_dets(a, b)
+    for _ in range(max(3, args.warmup)):
+        ctx.orbital_entropies(C)
+    torch.cuda.synchronize()
+    launches0 = capi.kernel_launches()
+    times = []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            s1, s2, mi = ctx.orbital_entropies(C)
+            times.append(time.perf_counter() - t0)
+    launches = capi.kernel_launches() - launches0
+    t = float(np.mean(times))
+    if rank != 0:
+        return
+    line = {"metric": "orbital_entropies_casci10_time", "value": t, "unit": "s", "n_gpus": 1, "steps": args.steps,
+            "warmup": max(3, args.warmup), "ms_per_step": t * 1e3, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "single-/two-orbital entropies and mutual information of the CASCI(10e,10o) "
+                                   "ground state, 63,504 determinants", "seed": SEED},
+            "s1_sum": float(s1.sum()), "mi_max": float(mi.max()),
+            "e2e": {"value": t, "unit": "s", "h2d_bytes_per_step": int(len(C)) * 8,
+                    "d2h_bytes_per_step": 8 * (norb + 2 * norb * norb)},
+            "gpu_launches": launches // max(1, args.steps), "clocks": clk.summary()}
+    if not args.no_cpu:
+        import oracle
+
+        oracle.build()
+        t0 = time.perf_counter()
+        o1, o2, om = oracle.entropies(norb, a, b, C)
+        tc = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": tc, "unit": "s", "cores": oracle.num_threads(), "kind": "port",
+                                "sample": "the full workload (one form_entropies of the same vector)",
+                                "max_abs_diff_s2": float(np.abs(o2 - s2).max())}
+    print(json.dumps(line))
+
+
+def run_casscf(args):
+    """CASSCF in the reference's own test configuration (external/macis/tests/
+    mcscf.cxx:26-66): water cc-pVDZ (FCIDUMP under tests/golden), 1 inactive +
+    8 active orbitals, 4 + 4 active electrons, from the start orbitals; a step
+    is one qdkgb_casscf call (device CASCI, RDMs and integral transform per
+    macro iteration).  The oracle holds no CASSCF, so there is no CPU line."""
+    import torch
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    rank = int(os.environ.get("RANK", "0"))
+    torch.cuda.set_device(local)
+    pkg = _package()
+    pkg.build.build()
+    capi = pkg.capi
+    d = np.load(os.path.join(ROOT, "tests", "golden", "h2o_ccpvdz_fcidump.npz"))
+    f = pkg.integrals.integrals_from_lines(int(d["norb"]), d["idx"], d["vals"], int(d["nelec"]), int(d["ms2"]))
+    ctx = capi.Context(local)
+    for _ in range(max(1, args.warmup)):
+        capi.casscf(ctx, f["T"], f["V"], f["E_core"], 4, 4, 1, 8)
+    torch.cuda.synchronize()
+    launches0 = capi.kernel_launches()
+    times = []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            E, g, _, U, iters, conv = capi.casscf(ctx, f["T"], f["V"], f["E_core"], 4, 4, 1, 8)
+            times.append(time.perf_counter() - t0)
+    launches = capi.kernel_launches() - launches0
+    t = float(np.mean(times))
+    if rank != 0:
+        return
+    line = {"metric": "casscf_h2o_ccpvdz_8e8o_time", "value": t, "unit": "s", "n_gpus": 1, "steps": args.steps,
+            "warmup": max(1, args.warmup), "ms_per_step": t * 1e3, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "water cc-pVDZ FCIDUMP (tests/golden)",
+            "config": {"workload": "CASSCF, water cc-pVDZ, 1 inactive + CAS(8e,8o), 24 orbitals (mcscf.cxx:26-66)"},
+            "energy": E, "energy_reference": -76.1114493227, "energy_error": E + 76.1114493227,
+            "macro_iterations": iters, "converged": conv,
+            "e2e": {"value": t, "unit": "s", "h2d_bytes_per_step": 8 * (24 ** 2 + 24 ** 4),
+                    "d2h_bytes_per_step": 8 * (1 + 64 + 8 ** 4 + 24 ** 2)},
+            "gpu_launches": launches // max(1, args.steps), "clocks": clk.summary(),
+            "cpu_baseline": None, "cpu_baseline_note": "the oracle holds no CASSCF"}
+    print(json.dumps(line))
+
+
 def time_spmv(ctx, precision, x, y, stream, reps=20):
     import torch
 
@@ -707,7 +808,8 @@ def main():
     ap.add_argument("--nel", type=int, default=NEL)
     ap.add_argument("--nchol", type=int, default=NCHOL)
     ap.add_argument("--asci-dets", type=int, default=2000000)
-    ap.add_argument("--workload", default="cas12", choices=["cas12", "batched", "cas14", "asci", "pt2"],
+    ap.add_argument("--workload", default="cas12",
+                    choices=["cas12", "batched", "cas14", "asci", "pt2", "entropies", "casscf"],
                     help="cas12: the headline CASCI(12e,12o); batched: 512 small instances; "
                          "cas14: CASCI(14e,14o) with the direct sigma")
     args = ap.parse_args()
@@ -718,6 +820,10 @@ def main():
         run_asci(args)
     elif args.workload == "pt2":
         run_pt2(args)
+    elif args.workload == "entropies":
+        run_entropies(args)
+    elif args.workload == "casscf":
+        run_casscf(args)
     elif args.workload == "batched":
         if args.impl == "reference":
             run_reference_batched(args)
