@@ -405,7 +405,10 @@ void asci_search_gpu(Context* c, int64_t ncore, const uint64_t* ca, const uint64
   while (cap * slot_bytes > freeb / 2 && cap > 1024) cap >>= 1;
   if ((int64_t)cap < std::min<int64_t>(total, (int64_t)1 << 40) / 2)
     throw Error(QDKGB_ERR_OOM, "ASCI search: hash table does not fit in device memory");
-  DeviceBuffer bkeys, bsum, bhd, bck, bcs, bcnt, berr, bcore, bout, bhist;
+  ScopedBuffers<10> scratch(c);
+  DeviceBuffer &bkeys = scratch.b[0], &bsum = scratch.b[1], &bhd = scratch.b[2], &bck = scratch.b[3],
+               &bcs = scratch.b[4], &bcnt = scratch.b[5], &berr = scratch.b[6], &bcore = scratch.b[7],
+               &bout = scratch.b[8], &bhist = scratch.b[9];
   u128* keys = (u128*)dev_alloc(c, bkeys, cap * 16 + 256);
   keys = (u128*)(((uintptr_t)keys + 15) & ~(uintptr_t)15);
   double* sum = dev_array<double>(c, bsum, cap);
@@ -498,7 +501,6 @@ void asci_search_gpu(Context* c, int64_t ncore, const uint64_t* ca, const uint64
   QDKGB_CUDA(cudaStreamSynchronize(c->stream));
   std::copy(ca, ca + ncore, out_a.begin() + nsel);
   std::copy(cb, cb + ncore, out_b.begin() + nsel);
-  for (DeviceBuffer* b : {&bkeys, &bsum, &bhd, &bck, &bcs, &bcnt, &berr, &bcore, &bout, &bhist}) dev_free(c, *b);
 }
 
 // asci_pt2_constraint (include/macis/asci/pt2.hpp:59-565) on the device:
@@ -542,7 +544,9 @@ double asci_pt2_gpu(Context* c, int64_t nd, const uint64_t* a, const uint64_t* b
   if (cap * slot_bytes > budget && cap > 1024) cap >>= 1;
   const uint64_t npass = std::max<uint64_t>(1, ((uint64_t)(total + total / 2) + cap - 1) / cap);
   if (npass > 0xffffffffull) throw Error(QDKGB_ERR_OOM, "ASCI PT2: too many passes for the device memory");
-  DeviceBuffer bkeys, bsum, bhd, berr, bcore, bpart;
+  ScopedBuffers<6> scratch(c);
+  DeviceBuffer &bkeys = scratch.b[0], &bsum = scratch.b[1], &bhd = scratch.b[2], &berr = scratch.b[3],
+               &bcore = scratch.b[4], &bpart = scratch.b[5];
   u128* keys = (u128*)dev_alloc(c, bkeys, cap * 16 + 256);
   keys = (u128*)(((uintptr_t)keys + 15) & ~(uintptr_t)15);
   double* sum = dev_array<double>(c, bsum, cap);
@@ -586,16 +590,12 @@ double asci_pt2_gpu(Context* c, int64_t nd, const uint64_t* a, const uint64_t* b
     QDKGB_CUDA(cudaMemcpyAsync(hp.data(), partial, sb * 8, cudaMemcpyDeviceToHost, c->stream));
     QDKGB_CUDA(cudaMemcpyAsync(hc.data(), pcount, sb * 8, cudaMemcpyDeviceToHost, c->stream));
     QDKGB_CUDA(cudaStreamSynchronize(c->stream));
-    if (herr) {
-      for (DeviceBuffer* x : {&bkeys, &bsum, &bhd, &berr, &bcore, &bpart}) dev_free(c, *x);
-      throw Error(QDKGB_ERR_OOM, "ASCI PT2: hash table overflow");
-    }
+    if (herr) throw Error(QDKGB_ERR_OOM, "ASCI PT2: hash table overflow");
     for (unsigned i = 0; i < sb; ++i) {
       ept2 += hp[i];
       count += (int64_t)hc[i];
     }
   }
-  for (DeviceBuffer* x : {&bkeys, &bsum, &bhd, &berr, &bcore, &bpart}) dev_free(c, *x);
   if (npt2) *npt2 = count;
   return ept2;
 }

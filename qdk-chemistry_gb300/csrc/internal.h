@@ -59,6 +59,19 @@ T* dev_array(Context* c, DeviceBuffer& b, size_t n) {
   return (T*)dev_alloc(c, b, n * sizeof(T) + 16);
 }
 
+// Scratch device buffers released on every exit of a scope (exceptions included).
+template <int N>
+struct ScopedBuffers {
+  Context* c;
+  DeviceBuffer b[N];
+  explicit ScopedBuffers(Context* ctx) : c(ctx) {}
+  ~ScopedBuffers() {
+    for (DeviceBuffer& x : b) dev_free(c, x);
+  }
+  ScopedBuffers(const ScopedBuffers&) = delete;
+  ScopedBuffers& operator=(const ScopedBuffers&) = delete;
+};
+
 // Determinant list prepared for the kernels.
 struct DetSpace {
   int64_t ndets = 0;

@@ -197,13 +197,7 @@ double casscf(Context* c, const qdkgb_mcscf_settings& S, int nalpha, int nbeta, 
     return V[p + (size_t)no * (q + (size_t)no * (r + (size_t)no * s))];
   };
   // ---- device buffers for the transform (released on every exit)
-  struct Bufs {
-    Context* c;
-    DeviceBuffer b[4];
-    ~Bufs() {
-      for (DeviceBuffer& x : b) dev_free(c, x);
-    }
-  } bufs{c, {}};
+  ScopedBuffers<4> bufs(c);
   double* dV0 = dev_array<double>(c, bufs.b[0], no4);
   double* dV1 = dev_array<double>(c, bufs.b[1], no4);
   double* dV2 = dev_array<double>(c, bufs.b[2], no4);

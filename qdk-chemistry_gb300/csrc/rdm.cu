@@ -188,7 +188,8 @@ void rdms_spin_dep(Context* c, const double* C, double* aa, double* bb, double* 
   const int n = c->norb;
   const int64_t N = c->dets.ndets;
   const size_t n2 = (size_t)n * n, n4 = n2 * n2;
-  DeviceBuffer bC, b4, b2;
+  ScopedBuffers<3> scratch(c);
+  DeviceBuffer &bC = scratch.b[0], &b4 = scratch.b[1], &b2 = scratch.b[2];
   double* dC = dev_array<double>(c, bC, N);
   QDKGB_CUDA(cudaMemcpyAsync(dC, C, N * 8, cudaMemcpyHostToDevice, c->stream));
   double* d4 = dev_array<double>(c, b4, n4);
@@ -234,9 +235,6 @@ void rdms_spin_dep(Context* c, const double* C, double* aa, double* bb, double* 
       for (size_t i = 0; i < n2; ++i) outs2[blk][i] += h2[i];
     }
   }
-  dev_free(c, bC);
-  dev_free(c, b4);
-  dev_free(c, b2);
 }
 
 // ---------------------------------------------------------------- orbital entropies
@@ -434,7 +432,8 @@ void orbital_entropies(Context* c, const double* C, double* s1, double* s2, doub
   const int64_t N = c->dets.ndets;
   const bool need_s2 = s2 || mi;
   const size_t nn = (size_t)n * n, total = 3 * (size_t)n + (need_s2 ? E_NMAT * nn : 0);
-  DeviceBuffer bC, bg;
+  ScopedBuffers<2> scratch(c);
+  DeviceBuffer &bC = scratch.b[0], &bg = scratch.b[1];
   double* dC = dev_array<double>(c, bC, N);
   double* g = dev_array<double>(c, bg, total);
   QDKGB_CUDA(cudaMemcpyAsync(dC, C, N * 8, cudaMemcpyHostToDevice, c->stream));
@@ -449,8 +448,6 @@ void orbital_entropies(Context* c, const double* C, double* s1, double* s2, doub
   std::vector<double> h(total);
   QDKGB_CUDA(cudaMemcpyAsync(h.data(), g, total * 8, cudaMemcpyDeviceToHost, c->stream));
   QDKGB_CUDA(cudaStreamSynchronize(c->stream));
-  dev_free(c, bC);
-  dev_free(c, bg);
   const double *a_ii = h.data(), *b_ii = a_ii + n, *ab_ii = b_ii + n;
   // build_s1_entropy (entropies.hpp:342-370): the diagonal one-orbital RDM
   // (empty, alpha, beta, double)
