@@ -49,13 +49,14 @@ struct Table {
   double* sum;
   double* hd;
   uint64_t mask;
-  int* err;  // set when probing exhausts the table
+  int* err;  // set when a probe sequence runs past kMaxProbe (the table is too full): the pass is redone larger
 };
+constexpr uint64_t kMaxProbe = 4096;
 
 __device__ __forceinline__ void table_add(const Table& t, uint64_t qa, uint64_t qb, double ch, double hd) {
   const u128 key = ((u128)qb << 64) | (u128)qa;
   uint64_t h = mix64(qa * 0x9e3779b97f4a7c15ULL ^ mix64(qb)) & t.mask;
-  for (uint64_t probe = 0; probe <= t.mask; ++probe) {
+  for (uint64_t probe = 0; probe <= t.mask && probe < kMaxProbe; ++probe) {
     const u128 old = atomicCAS(t.keys + h, kEmpty, key);
     if (old == kEmpty) {
       t.hd[h] = hd;
@@ -260,6 +261,92 @@ __global__ void __launch_bounds__(kAsciWarps * 32) k_asci_enum(CoreArgs A) {
   }
 }
 
+// Number of distinct target determinants of an enumeration (every single
+// and double of every core determinant, and the core itself) as a
+// HyperLogLog sketch: 2^kHllBits registers hold the largest leading-zero rank
+// of a 64-bit hash per bucket (block-local in shared memory, merged with
+// atomicMax).  Sizes the hash table to the targets instead of the
+// contributions (relative error ~1.04 / 2^(kHllBits/2)).
+constexpr int kHllBits = 12, kHllRegs = 1 << kHllBits;
+__device__ __forceinline__ void hll_add(unsigned* reg, uint64_t qa, uint64_t qb) {
+  const uint64_t h = mix64(qb * 0xbf58476d1ce4e5b9ULL ^ mix64(qa + 0x94d049bb133111ebULL));
+  const unsigned idx = (unsigned)(h >> (64 - kHllBits));
+  const uint64_t w = h << kHllBits;
+  const unsigned rank = w ? (unsigned)__clzll(w) + 1u : (unsigned)(64 - kHllBits + 1);
+  if (reg[idx] < rank) atomicMax(reg + idx, rank);
+}
+__global__ void __launch_bounds__(kAsciWarps * 32) k_target_sketch(CoreArgs A, unsigned* __restrict__ regs) {
+  __shared__ unsigned sreg[kHllRegs];
+  __shared__ WarpSm wsm[kAsciWarps];
+  for (int i = threadIdx.x; i < kHllRegs; i += blockDim.x) sreg[i] = 0u;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  WarpSm& s = wsm[w];
+  const int n = A.n;
+  for (int64_t ip = (int64_t)blockIdx.x * kAsciWarps + w; ip < A.ncore; ip += (int64_t)gridDim.x * kAsciWarps) {
+    const uint64_t Pa = A.ca[ip], Pb = A.cb[ip];
+    const int ka = popc64(Pa), kb = popc64(Pb), na_v = n - ka, nb_v = n - kb;
+    if (lane == 0) {
+      int x = 0, y = 0, u = 0, v = 0;
+      for (int p = 0; p < n; ++p) {
+        if ((Pa >> p) & 1)
+          s.oa[x++] = p;
+        else
+          s.va[y++] = p;
+        if ((Pb >> p) & 1)
+          s.ob[u++] = p;
+        else
+          s.vb[v++] = p;
+      }
+      hll_add(sreg, Pa, Pb);
+    }
+    __syncwarp();
+    const int64_t nsa = (int64_t)ka * na_v, nsb = (int64_t)kb * nb_v;
+    const int64_t pa_v = (int64_t)na_v * (na_v - 1) / 2, pb_v = (int64_t)nb_v * (nb_v - 1) / 2;
+    const int64_t nda = (int64_t)ka * (ka - 1) / 2 * pa_v, ndb = (int64_t)kb * (kb - 1) / 2 * pb_v;
+    const int64_t total = nsa + nsb + nda + ndb + nsa * nsb;
+    for (int64_t e = lane; e < total; e += 32) {
+      uint64_t qa = Pa, qb = Pb;
+      int64_t x = e;
+      if (x < nsa + nsb) {
+        const bool alpha = x < nsa;
+        if (!alpha) x -= nsa;
+        const int nv = alpha ? na_v : nb_v;
+        const uint32_t i = alpha ? s.oa[x / nv] : s.ob[x / nv];
+        const uint32_t a = alpha ? s.va[x % nv] : s.vb[x % nv];
+        if (alpha)
+          qa = (Pa ^ (1ull << i)) | (1ull << a);
+        else
+          qb = (Pb ^ (1ull << i)) | (1ull << a);
+      } else if ((x -= nsa + nsb) < nda + ndb) {
+        const bool alpha = x < nda;
+        if (!alpha) x -= nda;
+        const int64_t pv = alpha ? pa_v : pb_v;
+        int ii, jj, aa, bb;
+        pair_of((int)(x / pv), ii, jj);
+        pair_of((int)(x % pv), aa, bb);
+        const uint8_t* occ = alpha ? s.oa : s.ob;
+        const uint8_t* vir = alpha ? s.va : s.vb;
+        const uint64_t full = (1ull << occ[ii]) | (1ull << occ[jj]) | (1ull << vir[aa]) | (1ull << vir[bb]);
+        if (alpha)
+          qa = Pa ^ full;
+        else
+          qb = Pb ^ full;
+      } else {
+        x -= nda + ndb;
+        const int64_t xa = x / nsb, xb = x % nsb;
+        qa = (Pa ^ (1ull << s.oa[xa / na_v])) | (1ull << s.va[xa % na_v]);
+        qb = (Pb ^ (1ull << s.ob[xb / nb_v])) | (1ull << s.vb[xb % nb_v]);
+      }
+      hll_add(sreg, qa, qb);
+    }
+    __syncwarp();
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < kHllRegs; i += blockDim.x)
+    if (sreg[i]) atomicMax(regs + i, sreg[i]);
+}
+
 // candidates: finite score with |rv| > prune; key = bit pattern of |rv|
 __global__ void k_asci_extract(Table T, uint64_t cap, double prune, uint64_t* __restrict__ keys,
                                uint64_t* __restrict__ slots, unsigned long long* __restrict__ count) {
@@ -376,6 +463,29 @@ int64_t binom64(int n, int k) {
   return (int64_t)std::llround(r);
 }
 
+// HyperLogLog estimate of the distinct targets of an enumeration over the
+// core list already on the device in A (small-range correction by linear
+// counting); `regs` is kHllRegs device words of scratch
+double distinct_targets(Context* c, const CoreArgs& A, unsigned* regs) {
+  QDKGB_CUDA(cudaMemsetAsync(regs, 0, kHllRegs * sizeof(unsigned), c->stream));
+  const unsigned eb = (unsigned)std::min<int64_t>((A.ncore + kAsciWarps - 1) / kAsciWarps, (int64_t)c->sm_count * 8);
+  k_target_sketch<<<eb, kAsciWarps * 32, 0, c->stream>>>(A, regs);
+  QDKGB_CHECK_LAUNCH();
+  std::vector<unsigned> h(kHllRegs);
+  QDKGB_CUDA(cudaMemcpyAsync(h.data(), regs, kHllRegs * sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+  QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+  const double m = kHllRegs;
+  double z = 0.;
+  int zeros = 0;
+  for (unsigned r : h) {
+    z += std::ldexp(1., -(int)r);
+    zeros += r == 0;
+  }
+  double e = 0.7213 / (1. + 1.079 / m) * m * m / z;
+  if (e <= 2.5 * m && zeros > 0) e = m * std::log(m / zeros);
+  return e;
+}
+
 }  // namespace
 
 // Returns the new determinant list (top-k candidates followed by the core).
@@ -397,33 +507,17 @@ void asci_search_gpu(Context* c, int64_t ncore, const uint64_t* ca, const uint64
     const int64_t sa = (int64_t)ka * (n - ka), sb = (int64_t)kb * (n - kb);
     total += sa + sb + sa * sb + binom64(ka, 2) * binom64(n - ka, 2) + binom64(kb, 2) * binom64(n - kb, 2);
   }
-  size_t freeb = 0, totb = 0;
-  QDKGB_CUDA(cudaMemGetInfo(&freeb, &totb));
-  const size_t slot_bytes = 16 + 8 + 8 + 16;  // key, sum, hd, candidate key + slot
-  uint64_t cap = 1024;
-  while (cap < (uint64_t)(total + total / 2)) cap <<= 1;
-  while (cap * slot_bytes > freeb / 2 && cap > 1024) cap >>= 1;
-  if ((int64_t)cap < std::min<int64_t>(total, (int64_t)1 << 40) / 2)
-    throw Error(QDKGB_ERR_OOM, "ASCI search: hash table does not fit in device memory");
-  ScopedBuffers<10> scratch(c);
+  ScopedBuffers<11> scratch(c);
   DeviceBuffer &bkeys = scratch.b[0], &bsum = scratch.b[1], &bhd = scratch.b[2], &bck = scratch.b[3],
                &bcs = scratch.b[4], &bcnt = scratch.b[5], &berr = scratch.b[6], &bcore = scratch.b[7],
-               &bout = scratch.b[8], &bhist = scratch.b[9];
-  u128* keys = (u128*)dev_alloc(c, bkeys, cap * 16 + 256);
-  keys = (u128*)(((uintptr_t)keys + 15) & ~(uintptr_t)15);
-  double* sum = dev_array<double>(c, bsum, cap);
-  double* hd = dev_array<double>(c, bhd, cap);
-  int* err = dev_array<int>(c, berr, 1);
-  unsigned long long* cnt = dev_array<unsigned long long>(c, bcnt, 2);
-  QDKGB_CUDA(cudaMemsetAsync(err, 0, sizeof(int), c->stream));
-  QDKGB_CUDA(cudaMemsetAsync(cnt, 0, 2 * sizeof(unsigned long long), c->stream));
-  const unsigned fb = (unsigned)std::min<uint64_t>((cap + 255) / 256, (uint64_t)c->sm_count * 64);
-  k_fill_empty<<<fb, 256, 0, c->stream>>>(keys, sum, cap);
-  QDKGB_CHECK_LAUNCH();
+               &bout = scratch.b[8], &bhist = scratch.b[9], &bhll = scratch.b[10];
   uint64_t* dcore = dev_array<uint64_t>(c, bcore, 3 * ncore);
   QDKGB_CUDA(cudaMemcpyAsync(dcore, ca, ncore * 8, cudaMemcpyHostToDevice, c->stream));
   QDKGB_CUDA(cudaMemcpyAsync(dcore + ncore, cb, ncore * 8, cudaMemcpyHostToDevice, c->stream));
   QDKGB_CUDA(cudaMemcpyAsync(dcore + 2 * ncore, cc, ncore * 8, cudaMemcpyHostToDevice, c->stream));
+  int* err = dev_array<int>(c, berr, 1);
+  unsigned long long* cnt = dev_array<unsigned long long>(c, bcnt, 2);
+  QDKGB_CUDA(cudaMemsetAsync(cnt, 0, 2 * sizeof(unsigned long long), c->stream));
   CoreArgs A;
   A.I = integrals_view(c);
   A.n = n;
@@ -433,10 +527,35 @@ void asci_search_gpu(Context* c, int64_t ncore, const uint64_t* ca, const uint64
   A.cc = (const double*)(dcore + 2 * ncore);
   A.E0 = E0;
   A.h_el_tol = h_el_tol;
-  A.T = Table{keys, sum, hd, cap - 1, err};
+  // table: 2.5 x the estimated distinct targets (at most 1.5 x the
+  // contributions); an overflowing enumeration is redone with twice the slots
+  const double est = distinct_targets(c, A, dev_array<unsigned>(c, bhll, kHllRegs));
+  const double want = std::min((double)(total + total / 2), 2.5 * est + 2. * (double)ncore) + 1024.;
+  uint64_t cap = 1024;
+  while ((double)cap < want) cap <<= 1;
+  size_t freeb = 0, totb = 0;
+  QDKGB_CUDA(cudaMemGetInfo(&freeb, &totb));
+  const size_t slot_bytes = 16 + 8 + 8 + 16;  // key, sum, hd, candidate key + slot
+  if (cap * slot_bytes > freeb / 2) throw Error(QDKGB_ERR_OOM, "ASCI search: hash table does not fit in device memory");
   const unsigned eb = (unsigned)std::min<int64_t>((ncore + kAsciWarps - 1) / kAsciWarps, (int64_t)c->sm_count * 16);
-  k_asci_enum<<<eb, kAsciWarps * 32, 0, c->stream>>>(A);
-  QDKGB_CHECK_LAUNCH();
+  for (;;) {
+    u128* keys = (u128*)dev_alloc(c, bkeys, cap * 16 + 256);
+    keys = (u128*)(((uintptr_t)keys + 15) & ~(uintptr_t)15);
+    A.T = Table{keys, dev_array<double>(c, bsum, cap), dev_array<double>(c, bhd, cap), cap - 1, err};
+    const unsigned fb = (unsigned)std::min<uint64_t>((cap + 255) / 256, (uint64_t)c->sm_count * 64);
+    QDKGB_CUDA(cudaMemsetAsync(err, 0, sizeof(int), c->stream));
+    k_fill_empty<<<fb, 256, 0, c->stream>>>(keys, A.T.sum, cap);
+    QDKGB_CHECK_LAUNCH();
+    k_asci_enum<<<eb, kAsciWarps * 32, 0, c->stream>>>(A);
+    QDKGB_CHECK_LAUNCH();
+    int herr = 0;
+    QDKGB_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+    if (!herr) break;
+    if ((cap << 1) * slot_bytes > freeb / 2) throw Error(QDKGB_ERR_OOM, "ASCI search: hash table overflow");
+    cap <<= 1;
+  }
+  const unsigned fb = (unsigned)std::min<uint64_t>((cap + 255) / 256, (uint64_t)c->sm_count * 64);
   uint64_t* ckeys = dev_array<uint64_t>(c, bck, cap);
   uint64_t* cslots = dev_array<uint64_t>(c, bcs, cap);
   k_asci_extract<<<fb, 256, 0, c->stream>>>(A.T, cap, rv_prune_tol, ckeys, cslots, cnt);
@@ -533,34 +652,14 @@ double asci_pt2_gpu(Context* c, int64_t nd, const uint64_t* a, const uint64_t* b
     const int64_t sa = (int64_t)ka * (n - ka), sb = (int64_t)kb * (n - kb);
     total += sa + sb + sa * sb + binom64(ka, 2) * binom64(n - ka, 2) + binom64(kb, 2) * binom64(n - kb, 2);
   }
-  size_t freeb = 0, totb = 0;
-  QDKGB_CUDA(cudaMemGetInfo(&freeb, &totb));
-  const size_t slot_bytes = 16 + 8 + 8;  // key, sum, E0 - H_QQ
-  const size_t budget = (freeb > (size_t)3 * nd * 8 ? freeb - (size_t)3 * nd * 8 : 0) / 2;
-  const uint64_t slot_max = max_slots > 0 ? (uint64_t)max_slots : ~0ull;
-  uint64_t cap = 1024;
-  while (cap < (uint64_t)(total + total / 2) && (cap << 1) * slot_bytes <= budget && (cap << 1) <= slot_max)
-    cap <<= 1;
-  if (cap * slot_bytes > budget && cap > 1024) cap >>= 1;
-  const uint64_t npass = std::max<uint64_t>(1, ((uint64_t)(total + total / 2) + cap - 1) / cap);
-  if (npass > 0xffffffffull) throw Error(QDKGB_ERR_OOM, "ASCI PT2: too many passes for the device memory");
-  ScopedBuffers<6> scratch(c);
+  ScopedBuffers<7> scratch(c);
   DeviceBuffer &bkeys = scratch.b[0], &bsum = scratch.b[1], &bhd = scratch.b[2], &berr = scratch.b[3],
-               &bcore = scratch.b[4], &bpart = scratch.b[5];
-  u128* keys = (u128*)dev_alloc(c, bkeys, cap * 16 + 256);
-  keys = (u128*)(((uintptr_t)keys + 15) & ~(uintptr_t)15);
-  double* sum = dev_array<double>(c, bsum, cap);
-  double* hd = dev_array<double>(c, bhd, cap);
-  int* err = dev_array<int>(c, berr, 1);
-  const unsigned fb = (unsigned)std::min<uint64_t>((cap + 255) / 256, (uint64_t)c->sm_count * 64);
-  const unsigned sb = (unsigned)std::min<uint64_t>((cap + 255) / 256, (uint64_t)c->sm_count * 8);
-  double* partial = (double*)dev_alloc(c, bpart, (size_t)sb * 16 + 64);
-  unsigned long long* pcount = (unsigned long long*)(partial + sb);
+               &bcore = scratch.b[4], &bpart = scratch.b[5], &bhll = scratch.b[6];
   uint64_t* dcore = dev_array<uint64_t>(c, bcore, 3 * nd);
   QDKGB_CUDA(cudaMemcpyAsync(dcore, a, nd * 8, cudaMemcpyHostToDevice, c->stream));
   QDKGB_CUDA(cudaMemcpyAsync(dcore + nd, b, nd * 8, cudaMemcpyHostToDevice, c->stream));
   QDKGB_CUDA(cudaMemcpyAsync(dcore + 2 * nd, C, nd * 8, cudaMemcpyHostToDevice, c->stream));
-  QDKGB_CUDA(cudaMemsetAsync(err, 0, sizeof(int), c->stream));
+  int* err = dev_array<int>(c, berr, 1);
   CoreArgs A;
   A.I = integrals_view(c);
   A.n = n;
@@ -570,8 +669,27 @@ double asci_pt2_gpu(Context* c, int64_t nd, const uint64_t* a, const uint64_t* b
   A.cc = (const double*)(dcore + 2 * nd);
   A.E0 = E0;
   A.h_el_tol = pt2_tol;
-  A.T = Table{keys, sum, hd, cap - 1, err};
+  // table: 2.5 x the estimated distinct targets (at most 1.5 x the
+  // contributions), split into passes when it exceeds half the free memory or
+  // max_slots; a pass whose probing overflows is redone with twice the slots
+  const double est = distinct_targets(c, A, dev_array<unsigned>(c, bhll, kHllRegs));
+  const double want = std::min((double)(total + total / 2), 2.5 * est + 2. * (double)nd) + 1024.;
+  uint64_t need = 1024;
+  while ((double)need < want) need <<= 1;
+  size_t freeb = 0, totb = 0;
+  QDKGB_CUDA(cudaMemGetInfo(&freeb, &totb));
+  const size_t slot_bytes = 16 + 8 + 8;  // key, sum, E0 - H_QQ
+  const size_t budget = freeb / 2;
+  const uint64_t slot_max = max_slots > 0 ? std::max<uint64_t>((uint64_t)max_slots, 1024) : ~0ull;
+  auto fits = [&](uint64_t cp) { return cp * slot_bytes <= budget && cp <= slot_max; };
+  uint64_t cap = 1024;
+  while (cap < need && fits(cap << 1)) cap <<= 1;
+  const uint64_t npass = std::max<uint64_t>(1, (need + cap - 1) / cap);
+  if (npass > 0xffffffffull) throw Error(QDKGB_ERR_OOM, "ASCI PT2: too many passes for the device memory");
   A.npass = (uint32_t)npass;
+  const unsigned sb = (unsigned)std::min<uint64_t>((need + 255) / 256, (uint64_t)c->sm_count * 8);
+  double* partial = (double*)dev_alloc(c, bpart, (size_t)sb * 16 + 64);
+  unsigned long long* pcount = (unsigned long long*)(partial + sb);
   const unsigned eb = (unsigned)std::min<int64_t>((nd + kAsciWarps - 1) / kAsciWarps, (int64_t)c->sm_count * 16);
   std::vector<double> hp(sb);
   std::vector<unsigned long long> hc(sb);
@@ -579,18 +697,27 @@ double asci_pt2_gpu(Context* c, int64_t nd, const uint64_t* a, const uint64_t* b
   int64_t count = 0;
   for (uint64_t pass = 0; pass < npass; ++pass) {
     A.pass = (uint32_t)pass;
-    k_fill_empty<<<fb, 256, 0, c->stream>>>(keys, sum, cap);
-    QDKGB_CHECK_LAUNCH();
-    k_asci_enum<<<eb, kAsciWarps * 32, 0, c->stream>>>(A);
-    QDKGB_CHECK_LAUNCH();
-    k_pt2_sum<<<sb, 256, 0, c->stream>>>(A.T, cap, partial, pcount);
-    QDKGB_CHECK_LAUNCH();
-    int herr = 0;
-    QDKGB_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-    QDKGB_CUDA(cudaMemcpyAsync(hp.data(), partial, sb * 8, cudaMemcpyDeviceToHost, c->stream));
-    QDKGB_CUDA(cudaMemcpyAsync(hc.data(), pcount, sb * 8, cudaMemcpyDeviceToHost, c->stream));
-    QDKGB_CUDA(cudaStreamSynchronize(c->stream));
-    if (herr) throw Error(QDKGB_ERR_OOM, "ASCI PT2: hash table overflow");
+    for (;;) {
+      u128* keys = (u128*)dev_alloc(c, bkeys, cap * 16 + 256);
+      keys = (u128*)(((uintptr_t)keys + 15) & ~(uintptr_t)15);
+      A.T = Table{keys, dev_array<double>(c, bsum, cap), dev_array<double>(c, bhd, cap), cap - 1, err};
+      const unsigned fb = (unsigned)std::min<uint64_t>((cap + 255) / 256, (uint64_t)c->sm_count * 64);
+      QDKGB_CUDA(cudaMemsetAsync(err, 0, sizeof(int), c->stream));
+      k_fill_empty<<<fb, 256, 0, c->stream>>>(keys, A.T.sum, cap);
+      QDKGB_CHECK_LAUNCH();
+      k_asci_enum<<<eb, kAsciWarps * 32, 0, c->stream>>>(A);
+      QDKGB_CHECK_LAUNCH();
+      k_pt2_sum<<<sb, 256, 0, c->stream>>>(A.T, cap, partial, pcount);
+      QDKGB_CHECK_LAUNCH();
+      int herr = 0;
+      QDKGB_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+      QDKGB_CUDA(cudaMemcpyAsync(hp.data(), partial, sb * 8, cudaMemcpyDeviceToHost, c->stream));
+      QDKGB_CUDA(cudaMemcpyAsync(hc.data(), pcount, sb * 8, cudaMemcpyDeviceToHost, c->stream));
+      QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+      if (!herr) break;
+      if (!fits(cap << 1)) throw Error(QDKGB_ERR_OOM, "ASCI PT2: hash table overflow");
+      cap <<= 1;
+    }
     for (unsigned i = 0; i < sb; ++i) {
       ept2 += hp[i];
       count += (int64_t)hc[i];
