@@ -66,3 +66,17 @@ def test_default_settings_mirror_reference(capi):
     s = capi.default_davidson_settings()
     # ci_max_subspace / max_solver_iterations 200, ci_res_tol 1e-8, clamp 1e-12
     assert s.max_m == 200 and s.res_tol == 1e-8 and s.min_abs_denominator == 1e-12
+
+
+def test_mcscf_and_pt2_defaults(pkg):
+    """qdkgb_mcscf_default_settings = MCSCFSettings (external/macis/include/
+    macis/mcscf/mcscf.hpp:22-52); host-only, no device needed."""
+    capi = pkg.capi
+    s = capi.default_mcscf_settings()
+    assert s.max_macro_iter == 100 and s.max_orbital_step == 0.5 and s.orb_grad_tol == 5e-6
+    assert s.enable_diis == 1 and s.diis_start_iter == 3 and s.diis_nkeep == 10
+    assert s.ci_res_tol == 1e-8 and s.ci_max_subspace == 200 and s.ci_matel_tol == np.finfo(float).eps
+    s2 = capi.default_mcscf_settings(orb_grad_tol=1e-7)
+    assert s2.orb_grad_tol == 1e-7
+    with pytest.raises(KeyError):
+        capi.default_mcscf_settings(no_such_setting=1)
