@@ -1388,6 +1388,332 @@ double asci_pt2(const Ham& H, const std::vector<Det>& dets, const std::vector<do
   return EPT2;
 }
 
+// ---------------------------------------------------------------- CASSCF
+// casscf_diis / mcscf_impl (include/macis/mcscf/mcscf_impl.hpp:25-262) with
+// inactive_fock_matrix, active_hamiltonian, inactive_energy,
+// active_fock_matrix, aux_q_matrix, generalized_fock_matrix
+// (src/macis/mcscf/fock_matrices.cxx:16-186), fock_to_linear_orb_grad and
+// linear_orb_rot_to_matrix (orbital_rotation_utilities.cxx:16-118),
+// approx_diag_hessian (orbital_hessian.cxx:16-62), precond_cg_orbital_step
+// (orbital_steps.cxx:16-37), DIIS (include/macis/mcscf/diis.hpp),
+// compute_orbital_rotation (orbital_gradient.cxx:17-28) and the two- and
+// four-index transforms (src/macis/util/transform.cxx:17-60).  The CASCI of an
+// iteration is compute_casci_rdms (include/macis/mcscf/cas.hpp:33-88): the
+// complete active space, the SDL CSR, selected_ci_diag warm-started from the
+// previous vector, the spin-traced RDMs.  Matrices column-major.
+struct McscfSettings {
+  int64_t max_macro_iter = 100;
+  double max_orbital_step = 0.5, orb_grad_tol = 5e-6;
+  int enable_diis = 1;
+  int64_t diis_start_iter = 3, diis_nkeep = 10;
+  double ci_res_tol = 1e-8;
+  int64_t ci_max_subspace = 200;
+  double ci_matel_tol = std::numeric_limits<double>::epsilon();
+};
+
+// exp(A) of a small square matrix: scaling and squaring of the Taylor series
+std::vector<double> expm(int n, std::vector<double> A) {
+  double nrm = 0.;
+  for (int i = 0; i < n; ++i) {
+    double r = 0.;
+    for (int j = 0; j < n; ++j) r += std::abs(A[i + (size_t)n * j]);
+    nrm = std::max(nrm, r);
+  }
+  int sq = 0;
+  while (nrm > 0.125) {
+    nrm /= 2.;
+    ++sq;
+  }
+  for (double& x : A) x = std::ldexp(x, -sq);
+  const size_t n2 = (size_t)n * n;
+  std::vector<double> E(n2, 0.), P(n2, 0.), Q(n2);
+  for (int i = 0; i < n; ++i) E[i * (n + 1)] = P[i * (n + 1)] = 1.;
+  for (int k = 1; k < 40; ++k) {
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i) {
+        double t = 0.;
+        for (int l = 0; l < n; ++l) t += P[i + (size_t)n * l] * A[l + (size_t)n * j];
+        Q[i + (size_t)n * j] = t / k;
+      }
+    P.swap(Q);
+    double pm = 0.;
+    for (size_t i = 0; i < n2; ++i) {
+      E[i] += P[i];
+      pm = std::max(pm, std::abs(P[i]));
+    }
+    if (pm < 1e-20) break;
+  }
+  for (int s = 0; s < sq; ++s) {
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i) {
+        double t = 0.;
+        for (int l = 0; l < n; ++l) t += E[i + (size_t)n * l] * E[l + (size_t)n * j];
+        Q[i + (size_t)n * j] = t;
+      }
+    E.swap(Q);
+  }
+  return E;
+}
+
+double casscf(const McscfSettings& S, int nalpha, int nbeta, int no, int ni, int na, double E_core, const double* T0,
+              const double* V0, double* A1, double* A2, int64_t* iters_out, int* conv_out) {
+  const int nv = no - ni - na;
+  if (nv < 0 || na < 1 || ni < 0) throw std::runtime_error("bad orbital partition");
+  const size_t no2 = (size_t)no * no, no4 = no2 * no2, na2 = (size_t)na * na, na4 = na2 * na2;
+  const int rot = nv * (ni + na) + na * ni;
+  auto VV = [&](const std::vector<double>& V, int p, int q, int r, int s) {
+    return V[p + (size_t)no * (q + (size_t)no * (r + (size_t)no * s))];
+  };
+  std::vector<double> T(T0, T0 + no2), V(V0, V0 + no4);
+  // complete active space (generate_hilbert_space order)
+  auto strings = [](int n, int k) {
+    std::vector<char> v(n, 0);
+    std::fill_n(v.begin(), k, 1);
+    std::vector<uint64_t> out;
+    do {
+      uint64_t x = 0;
+      for (int i = 0; i < n; ++i)
+        if (v[i]) x |= 1ull << i;
+      out.push_back(x);
+    } while (std::prev_permutation(v.begin(), v.end()));
+    return out;
+  };
+  const std::vector<uint64_t> sa = strings(na, nalpha), sb = strings(na, nbeta);
+  std::vector<uint64_t> da, db;
+  for (uint64_t x : sa)
+    for (uint64_t y : sb) {
+      da.push_back(x);
+      db.push_back(y);
+    }
+  const int64_t nd = (int64_t)da.size();
+  std::vector<double> X(nd, 0.), Fi(no2), Fa(no2), F(no2), Q((size_t)na * no), Ta(na2), Va(na4);
+  double E_inact = 0.;
+  auto active_hamiltonian = [&]() {
+    for (int q = 0; q < no; ++q)
+      for (int p = 0; p < no; ++p) {
+        double t = 0.;
+        for (int i = 0; i < ni; ++i) t += 2. * VV(V, p, q, i, i) - VV(V, p, i, i, q);
+        Fi[p + (size_t)no * q] = T[p + (size_t)no * q] + t;
+      }
+    for (int y = 0; y < na; ++y)
+      for (int x = 0; x < na; ++x) Ta[x + (size_t)na * y] = Fi[(x + ni) + (size_t)no * (y + ni)];
+    for (int w = 0; w < na; ++w)
+      for (int z = 0; z < na; ++z)
+        for (int y = 0; y < na; ++y)
+          for (int x = 0; x < na; ++x)
+            Va[x + na * (y + na * (z + (size_t)na * w))] = VV(V, x + ni, y + ni, z + ni, w + ni);
+    E_inact = E_core;
+    for (int i = 0; i < ni; ++i) E_inact += T[i * (no + 1)] + Fi[i * (no + 1)];
+  };
+  auto casci = [&]() {
+    Ham H;
+    H.init(na, Ta.data(), Va.data());
+    std::unique_ptr<Csr> M(build_csr_sdl(H, da.data(), db.data(), nd, S.ci_matel_tol));
+    std::vector<double> D(nd, 0.);
+    for (int64_t i = 0; i < nd; ++i)
+      for (int64_t k = M->rowptr[i]; k < M->rowptr[i + 1]; ++k)
+        if (M->colind[k] == i) D[i] = M->nzval[k];
+    double mx = 0.;
+    for (double x : X) mx = std::max(mx, std::abs(x));
+    if (!(mx > 1. / (double)nd)) {
+      std::fill(X.begin(), X.end(), 0.);
+      X[std::min_element(D.begin(), D.end()) - D.begin()] = 1.;
+    }
+    double E = 0.;
+    int64_t it = 0;
+    if (nd == 1) {
+      X[0] = 1.;
+      E = M->nzval[0];
+    } else if (davidson(*M, std::min<int64_t>(S.ci_max_subspace, nd), D.data(), S.ci_res_tol, X.data(), &E, &it)) {
+      throw std::runtime_error("Davidson Did Not Converge!");
+    }
+    std::vector<double> aa(na2, 0.), bb(na2, 0.), aaaa(na4, 0.), bbbb(na4, 0.), aabb(na4, 0.);
+    Rdms R{na, aa.data(), bb.data(), aaaa.data(), bbbb.data(), aabb.data()};
+    rdms_spin_dep(da.data(), db.data(), nd, X.data(), R);
+    for (size_t i = 0; i < na2; ++i) A1[i] = aa[i] + bb[i];
+    for (int s4 = 0; s4 < na; ++s4)
+      for (int r = 0; r < na; ++r)
+        for (int q = 0; q < na; ++q)
+          for (int p = 0; p < na; ++p) {
+            const size_t i = p + na * (q + na * (r + (size_t)na * s4)), j = r + na * (s4 + na * (p + (size_t)na * q));
+            A2[i] = aaaa[i] + bbbb[i] + aabb[i] + aabb[j];
+          }
+    return E;
+  };
+  std::vector<double> OG(rot), DH(rot);
+  auto grad = [&]() {
+    for (int q = 0; q < no; ++q)
+      for (int p = 0; p < no; ++p) {
+        double t = 0.;
+        for (int w = 0; w < na; ++w)
+          for (int v = 0; v < na; ++v)
+            t += A1[v + (size_t)na * w] * (VV(V, p, q, v + ni, w + ni) - 0.5 * VV(V, p, w + ni, v + ni, q));
+        Fa[p + (size_t)no * q] = t;
+      }
+    for (int p = 0; p < no; ++p)
+      for (int v = 0; v < na; ++v) {
+        double t = 0.;
+        for (int y = 0; y < na; ++y)
+          for (int x = 0; x < na; ++x)
+            for (int w = 0; w < na; ++w)
+              t += A2[v + na * (w + na * (x + (size_t)na * y))] * VV(V, p, w + ni, x + ni, y + ni);
+        Q[v + (size_t)na * p] = 2. * t;
+      }
+    std::fill(F.begin(), F.end(), 0.);
+    for (int p = 0; p < no; ++p) {
+      for (int i = 0; i < ni; ++i) F[i + (size_t)no * p] = 2. * (Fi[p + (size_t)no * i] + Fa[p + (size_t)no * i]);
+      for (int v = 0; v < na; ++v) {
+        double t = 0.;
+        for (int w = 0; w < na; ++w) t += Fi[p + (size_t)no * (w + ni)] * A1[w + (size_t)na * v];
+        F[(v + ni) + (size_t)no * p] = t + Q[v + (size_t)na * p];
+      }
+    }
+    auto g = [&](int p, int q) { return 2. * (F[p + (size_t)no * q] - F[q + (size_t)no * p]); };
+    int k = 0;
+    for (int i = 0; i < ni; ++i)
+      for (int a = 0; a < nv; ++a) OG[k++] = g(a + ni + na, i);
+    for (int x = 0; x < na; ++x)
+      for (int a = 0; a < nv; ++a) OG[k++] = g(a + ni + na, x + ni);
+    for (int i = 0; i < ni; ++i)
+      for (int x = 0; x < na; ++x) OG[k++] = g(x + ni, i);
+    double n2 = 0.;
+    for (double x : OG) n2 += x * x;
+    return std::sqrt(n2);
+  };
+  auto hess = [&]() {
+    auto f = [&](int p) { return Fi[p * (no + 1)] + Fa[p * (no + 1)]; };
+    int k = 0;
+    for (int i = 0; i < ni; ++i)
+      for (int a = 0; a < nv; ++a) DH[k++] = 4. * (f(a + ni + na) - f(i));
+    for (int x = 0; x < na; ++x)
+      for (int a = 0; a < nv; ++a) DH[k++] = 2. * A1[x * (na + 1)] * f(a + ni + na) - 2. * F[(x + ni) * (no + 1)];
+    for (int i = 0; i < ni; ++i)
+      for (int x = 0; x < na; ++x)
+        DH[k++] = 2. * A1[x * (na + 1)] * f(i) + 4. * (f(x + ni) - f(i)) - 2. * F[(x + ni) * (no + 1)];
+  };
+  auto to_mat = [&](const std::vector<double>& kl) {
+    std::vector<double> K(no2, 0.);
+    int t = 0;
+    auto put = [&](int A, int I) {
+      K[A + (size_t)no * I] = kl[t];
+      K[I + (size_t)no * A] = -kl[t];
+      ++t;
+    };
+    for (int i = 0; i < ni; ++i)
+      for (int a = 0; a < nv; ++a) put(a + ni + na, i);
+    for (int x = 0; x < na; ++x)
+      for (int a = 0; a < nv; ++a) put(a + ni + na, x + ni);
+    for (int i = 0; i < ni; ++i)
+      for (int x = 0; x < na; ++x) put(x + ni, i);
+    return K;
+  };
+  auto transform = [&](const std::vector<double>& U) {
+    // T = U^T T0 U; V(pqrs) = sum U_ap U_bq U_cr U_ds V0(abcd), one index at a time
+    std::vector<double> t1(no2);
+    for (int q = 0; q < no; ++q)
+      for (int a = 0; a < no; ++a) {
+        double t = 0.;
+        for (int b = 0; b < no; ++b) t += T0[a + (size_t)no * b] * U[b + (size_t)no * q];
+        t1[a + (size_t)no * q] = t;
+      }
+    for (int q = 0; q < no; ++q)
+      for (int p = 0; p < no; ++p) {
+        double t = 0.;
+        for (int a = 0; a < no; ++a) t += U[a + (size_t)no * p] * t1[a + (size_t)no * q];
+        T[p + (size_t)no * q] = t;
+      }
+    std::vector<double> A(V0, V0 + no4), B(no4);
+    for (int pass = 0; pass < 4; ++pass) {
+      // B(j,k,l,p) = sum_a A(a,j,k,l) U(a,p): the contracted index moves last
+      const int64_t n3 = (int64_t)no2 * no;
+#pragma omp parallel for schedule(static)
+      for (int64_t t = 0; t < n3 * no; ++t) {
+        const int64_t rest = t % n3, p = t / n3;
+        double acc = 0.;
+        for (int a = 0; a < no; ++a) acc += A[a + no * rest] * U[a + (size_t)no * p];
+        B[t] = acc;
+      }
+      A.swap(B);
+    }
+    V.swap(A);
+  };
+
+  active_hamiltonian();
+  double tr = 0.;
+  for (int i = 0; i < na; ++i) tr += A1[i * (na + 1)];
+  if (std::abs(tr - nalpha - nbeta) > 1e-6) (void)casci();
+  double E0 = E_inact;
+  for (size_t i = 0; i < na2; ++i) E0 += A1[i] * Ta[i];
+  for (size_t i = 0; i < na4; ++i) E0 += A2[i] * Va[i];
+  double gn = grad();
+  bool conv = gn < S.orb_grad_tol;
+  std::vector<double> U(no2, 0.), K(no2, 0.);
+  for (int i = 0; i < no; ++i) U[i * (no + 1)] = 1.;
+  std::vector<std::pair<std::vector<double>, std::vector<double>>> hist;
+  int64_t it = 0;
+  for (; it < S.max_macro_iter && !conv; ++it) {
+    const std::vector<double> Ksav = K;
+    hess();
+    std::vector<double> kl(rot);
+    double amax = 0.;
+    for (int p = 0; p < rot; ++p) {
+      kl[p] = -OG[p] / DH[p];
+      amax = std::max(amax, std::abs(kl[p]));
+    }
+    if (amax > S.max_orbital_step)
+      for (double& x : kl) x *= S.max_orbital_step / amax;
+    const std::vector<double> Ks = to_mat(kl);
+    for (size_t i = 0; i < no2; ++i) K[i] += Ks[i];
+    if (S.enable_diis && it >= S.diis_start_iter) {
+      if ((int64_t)hist.size() == S.diis_nkeep) hist.erase(hist.begin());
+      hist.emplace_back(K, OG);
+      if (it >= S.diis_start_iter + 2) {
+        // min |sum c_i e_i| with sum c_i = 1 (the bordered system, least squares)
+        const int m = (int)hist.size(), mb = m + 1;
+        std::vector<double> B((size_t)mb * mb, 0.), w(mb);
+        for (int i = 0; i < m; ++i)
+          for (int j = 0; j < m; ++j) {
+            double d = 0.;
+            for (int r = 0; r < rot; ++r) d += hist[i].second[r] * hist[j].second[r];
+            B[i + (size_t)mb * j] = d;
+          }
+        for (int i = 0; i < m; ++i) B[i + (size_t)mb * m] = B[m + (size_t)mb * i] = 1.;
+        jacobi_syev(mb, B.data(), mb, w.data());  // B: eigenvectors, w: eigenvalues
+        double wmax = 0.;
+        for (double x : w) wmax = std::max(wmax, std::abs(x));
+        std::vector<double> c(mb, 0.);
+        for (int k = 0; k < mb; ++k) {
+          if (!(std::abs(w[k]) > std::numeric_limits<double>::epsilon() * wmax * mb)) continue;
+          const double f = B[m + (size_t)mb * k] / w[k];
+          for (int i = 0; i < mb; ++i) c[i] += B[i + (size_t)mb * k] * f;
+        }
+        std::fill(K.begin(), K.end(), 0.);
+        for (int i = 0; i < m; ++i)
+          for (size_t r = 0; r < no2; ++r) K[r] += c[i] * hist[i].first[r];
+      }
+    }
+    std::vector<double> dK(no2);
+    for (size_t i = 0; i < no2; ++i) dK[i] = -(it == 0 ? K[i] : K[i] - Ksav[i]);
+    const std::vector<double> Us = expm(no, dK);
+    std::vector<double> Un(no2);
+    for (int j = 0; j < no; ++j)
+      for (int i = 0; i < no; ++i) {
+        double t = 0.;
+        for (int l = 0; l < no; ++l) t += U[i + (size_t)no * l] * Us[l + (size_t)no * j];
+        Un[i + (size_t)no * j] = t;
+      }
+    U.swap(Un);
+    transform(U);
+    active_hamiltonian();
+    E0 = casci() + E_inact;
+    gn = grad();
+    conv = gn / std::sqrt((double)std::max(rot, 1)) < S.orb_grad_tol;
+  }
+  if (iters_out) *iters_out = it;
+  if (conv_out) *conv_out = conv;
+  return E0;
+}
+
 // selected_ci_diag (selected_ci_diag.hpp:111-158) on a sorted determinant list
 double sci_diag(const Ham& H, const AsciSettings& S, const std::vector<Det>& dets, std::vector<double>& X) {
   std::vector<uint64_t> a(dets.size()), b(dets.size());
@@ -1757,6 +2083,23 @@ int orc_asci_pt2(void* h, int64_t nd, const uint64_t* a, const uint64_t* b, cons
     std::vector<double> C(c, c + nd);
     *ept2 = asci_pt2(H, dets, C, E0, tol, npt2, pass_max > 0 ? pass_max : (int64_t)1 << 25);
   });
+}
+
+// casscf_diis from full integrals; settings as a flat double array in the
+// order of McscfSettings; 0 on success
+int orc_casscf(const double* set, int nalpha, int nbeta, int norb, int ninact, int nact, double E_core,
+               const double* T, const double* V, double* A1, double* A2, double* E, int64_t* iters, int* conv) {
+  McscfSettings S;
+  S.max_macro_iter = (int64_t)set[0];
+  S.max_orbital_step = set[1];
+  S.orb_grad_tol = set[2];
+  S.enable_diis = (int)set[3];
+  S.diis_start_iter = (int64_t)set[4];
+  S.diis_nkeep = (int64_t)set[5];
+  S.ci_res_tol = set[6];
+  S.ci_max_subspace = (int64_t)set[7];
+  S.ci_matel_tol = set[8];
+  return guard([&] { *E = casscf(S, nalpha, nbeta, norb, ninact, nact, E_core, T, V, A1, A2, iters, conv); });
 }
 
 // orbital entropies of a CI vector; s2 / mi may be null; 0 on success

@@ -67,6 +67,9 @@ def lib():
                                ctypes.POINTER(f64), ctypes.POINTER(f64)]
         L.orc_asci_search.restype = i64
         L.orc_asci_search.argtypes = [vp, _f64p, i64, _u64p, _u64p, _f64p, f64, i64, i64, _u64p, _u64p]
+        L.orc_casscf.restype = ci
+        L.orc_casscf.argtypes = [_f64p, ci, ci, ci, ci, ci, f64, _f64p, _f64p, _f64p, _f64p, ctypes.POINTER(f64),
+                                 ctypes.POINTER(i64), ctypes.POINTER(ci)]
         L.orc_entropies.restype = ci
         L.orc_entropies.argtypes = [ci, _u64p, _u64p, i64, _f64p, _f64p, _f64p, _f64p]
         L.orc_asci_pt2.restype = ci
@@ -310,3 +313,34 @@ def entropies(norb, alpha, beta, C):
     if rc != 0:
         raise RuntimeError(lib().orc_last_error().decode())
     return s1, s2, mi
+
+
+MCSCF_DEFAULTS = dict(max_macro_iter=100, max_orbital_step=0.5, orb_grad_tol=5e-6, enable_diis=1, diis_start_iter=3,
+                      diis_nkeep=10, ci_res_tol=1e-8, ci_max_subspace=200,
+                      ci_matel_tol=float(np.finfo(np.float64).eps))
+
+
+def casscf(T, V, E_core, nalpha, nbeta, ninact, nact, **settings):
+    """casscf_diis (mcscf.hpp:54-60, mcscf_impl.hpp:25-262) from full
+    molecular-orbital integrals; returns (E, 1-RDM, 2-RDM, macro iterations,
+    converged)."""
+    d = dict(MCSCF_DEFAULTS)
+    for k, v in settings.items():
+        if k not in d:
+            raise KeyError(k)
+        d[k] = v
+    s = np.array([float(d[k]) for k in MCSCF_DEFAULTS])
+    T = np.asarray(T, dtype=np.float64)
+    n = T.shape[0]
+    Tb = np.ascontiguousarray(T.ravel(order="F"))
+    Vb = np.ascontiguousarray(np.asarray(V, dtype=np.float64).reshape(n, n, n, n).ravel(order="F"))
+    A1 = np.zeros(nact * nact)
+    A2 = np.zeros(nact ** 4)
+    E = ctypes.c_double()
+    it = ctypes.c_int64()
+    conv = ctypes.c_int()
+    rc = lib().orc_casscf(s, int(nalpha), int(nbeta), n, int(ninact), int(nact), float(E_core), Tb, Vb, A1, A2,
+                          ctypes.byref(E), ctypes.byref(it), ctypes.byref(conv))
+    if rc != 0:
+        raise RuntimeError(lib().orc_last_error().decode())
+    return E.value, A1.reshape(nact, nact, order="F"), A2.reshape((nact,) * 4, order="F"), it.value, bool(conv.value)

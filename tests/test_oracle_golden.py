@@ -154,3 +154,14 @@ def test_n2_asci_energy(oracle, pkg, n2_14e18o, known):
     assert np.isclose(E, ref["E_total"])
     assert abs(E - ref["E_total"]) < 1e-8
     assert len(a) == ref["ndets"] and np.isclose(np.linalg.norm(c), 1.0)
+
+
+def test_h2o_casscf_energy(oracle, h2o, known):
+    """external/macis/tests/mcscf.cxx:26-66: water cc-pVDZ, 1 inactive +
+    CAS(8e,8o), no starting RDMs, E = -76.1114493227 (1e-8)."""
+    ref = known["h2o_casscf"]
+    E, g, G, iters, conv = oracle.casscf(h2o["T"], h2o["V"], h2o["E_core"], ref["nalpha"], ref["nbeta"],
+                                         ref["ninact"], ref["nact"])
+    assert conv and iters > 0
+    assert abs(E - ref["E_total"]) < ref["atol"]
+    assert abs(np.trace(g) - 8.0) < 1e-10
