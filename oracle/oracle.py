@@ -320,10 +320,11 @@ MCSCF_DEFAULTS = dict(max_macro_iter=100, max_orbital_step=0.5, orb_grad_tol=5e-
                       ci_matel_tol=float(np.finfo(np.float64).eps))
 
 
-def casscf(T, V, E_core, nalpha, nbeta, ninact, nact, **settings):
+def casscf(T, V, E_core, nalpha, nbeta, ninact, nact, rdm1=None, rdm2=None, **settings):
     """casscf_diis (mcscf.hpp:54-60, mcscf_impl.hpp:25-262) from full
-    molecular-orbital integrals; returns (E, 1-RDM, 2-RDM, macro iterations,
-    converged)."""
+    molecular-orbital integrals, optionally from starting active RDMs (used
+    when their trace is the electron count); returns (E, 1-RDM, 2-RDM, macro
+    iterations, converged)."""
     d = dict(MCSCF_DEFAULTS)
     for k, v in settings.items():
         if k not in d:
@@ -334,8 +335,8 @@ def casscf(T, V, E_core, nalpha, nbeta, ninact, nact, **settings):
     n = T.shape[0]
     Tb = np.ascontiguousarray(T.ravel(order="F"))
     Vb = np.ascontiguousarray(np.asarray(V, dtype=np.float64).reshape(n, n, n, n).ravel(order="F"))
-    A1 = np.zeros(nact * nact)
-    A2 = np.zeros(nact ** 4)
+    A1 = np.zeros(nact * nact) if rdm1 is None else np.array(np.asarray(rdm1, dtype=np.float64).ravel(order="F"))
+    A2 = np.zeros(nact ** 4) if rdm2 is None else np.array(np.asarray(rdm2, dtype=np.float64).ravel(order="F"))
     E = ctypes.c_double()
     it = ctypes.c_int64()
     conv = ctypes.c_int()

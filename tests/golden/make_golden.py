@@ -15,6 +15,9 @@ run time:
 * the CSR row-pointer golden of the water CISD Hamiltonian
   (external/macis/tests/ref_data/h2o.ccpvdz.cisd.rowptr.bin, int32)
 * the O2 CI wavefunction external/macis/tests/ref_data/o2.wfn.dat
+* the water CAS(8e,8o) active RDMs external/macis/tests/ref_data/
+  h2o.ccpvdz.cas88.rdms.bin (int32 norb, then the column-major 1-RDM and
+  2-RDM; read_rdms_binary, src/macis/fcidump.cxx:487-527)
 * known_answers.json: the energies / sums the reference tests pin, with the
   file:line each one comes from.
 """
@@ -65,6 +68,12 @@ def main(ref="/root/reference"):
     beta = np.array([sum(1 << i for i, ch in enumerate(s) if ch in "2d") for s in strs], dtype=np.uint64)
     np.savez_compressed(os.path.join(HERE, "o2_wfn.npz"), alpha=alpha, beta=beta, coeffs=np.array(coeffs),
                         norb=norb, nalpha=na, nbeta=nb)
+
+    raw = open(os.path.join(macis, "tests", "ref_data", "h2o.ccpvdz.cas88.rdms.bin"), "rb").read()
+    nact = int(np.frombuffer(raw[:4], dtype=np.int32)[0])
+    vals = np.frombuffer(raw[4:], dtype=np.float64)
+    np.savez_compressed(os.path.join(HERE, "h2o_ccpvdz_cas88_rdms.npz"), nact=nact,
+                        ordm=vals[:nact ** 2].copy(), trdm=vals[nact ** 2:nact ** 2 + nact ** 4].copy())
 
     known = {
         "h2o_cisd_csr": {"n": 12636, "nnz": 3517816, "thresh": 1e-16,

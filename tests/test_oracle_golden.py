@@ -1,5 +1,7 @@
 """The CPU oracle pinned against the reference's own golden vectors and known
 answers (external/macis/tests, external/macis/python/tests).  No GPU."""
+import os
+
 import numpy as np
 import pytest
 
@@ -165,3 +167,17 @@ def test_h2o_casscf_energy(oracle, h2o, known):
     assert conv and iters > 0
     assert abs(E - ref["E_total"]) < ref["atol"]
     assert abs(np.trace(g) - 8.0) < 1e-10
+
+
+def test_h2o_casscf_from_reference_rdms(oracle, h2o, known):
+    """mcscf.cxx:67-79 ("With Guess"): the same CASSCF started from the
+    reference's stored CAS(8e,8o) RDMs (ref_data/h2o.ccpvdz.cas88.rdms.bin)
+    reaches the same energy."""
+    ref = known["h2o_casscf"]
+    d = np.load(os.path.join(GOLDEN, "h2o_ccpvdz_cas88_rdms.npz"))
+    n = int(d["nact"])
+    g0, G0 = d["ordm"].reshape(n, n, order="F"), d["trdm"].reshape((n,) * 4, order="F")
+    assert abs(np.trace(g0) - 8.0) < 1e-10
+    E, _, _, iters, conv = oracle.casscf(h2o["T"], h2o["V"], h2o["E_core"], ref["nalpha"], ref["nbeta"],
+                                         ref["ninact"], ref["nact"], rdm1=g0, rdm2=G0)
+    assert conv and abs(E - ref["E_total"]) < ref["atol"]
