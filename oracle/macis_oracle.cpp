@@ -1455,15 +1455,80 @@ std::vector<double> expm(int n, std::vector<double> A) {
   return E;
 }
 
+// fock_matrices.cxx building blocks (n x n column-major; V n^4; active RDMs
+// na^2 / na^4; active orbitals ni .. ni+na-1)
+inline double v4(const double* V, int n, int p, int q, int r, int s) {
+  return V[p + (size_t)n * (q + (size_t)n * (r + (size_t)n * s))];
+}
+// inactive_fock_matrix (:25-41): Fi = T + sum_i 2 (pq|ii) - (pi|iq)
+void inactive_fock(int n, int ni, const double* T, const double* V, double* Fi) {
+  for (int q = 0; q < n; ++q)
+    for (int p = 0; p < n; ++p) {
+      double t = 0.;
+      for (int i = 0; i < ni; ++i) t += 2. * v4(V, n, p, q, i, i) - v4(V, n, p, i, i, q);
+      Fi[p + (size_t)n * q] = T[p + (size_t)n * q] + t;
+    }
+}
+// inactive_energy (:16-23): sum_i T_ii + Fi_ii
+double inactive_energy(int n, int ni, const double* T, const double* Fi) {
+  double E = 0.;
+  for (int i = 0; i < ni; ++i) E += T[i * (n + 1)] + Fi[i * (n + 1)];
+  return E;
+}
+// active_fock_matrix (:89-110): Fa = sum_vw g_vw [(pq|vw) - 1/2 (pw|vq)]
+void active_fock(int n, int ni, int na, const double* V, const double* A1, double* Fa) {
+  for (int q = 0; q < n; ++q)
+    for (int p = 0; p < n; ++p) {
+      double t = 0.;
+      for (int w = 0; w < na; ++w)
+        for (int v = 0; v < na; ++v)
+          t += A1[v + (size_t)na * w] * (v4(V, n, p, q, v + ni, w + ni) - 0.5 * v4(V, n, p, w + ni, v + ni, q));
+      Fa[p + (size_t)n * q] = t;
+    }
+}
+// aux_q_matrix (:112-137): Q(v, p) = 2 sum_wxy G_vwxy (pw|xy)
+void aux_q(int n, int ni, int na, const double* V, const double* A2, double* Q) {
+  for (int p = 0; p < n; ++p)
+    for (int v = 0; v < na; ++v) {
+      double t = 0.;
+      for (int y = 0; y < na; ++y)
+        for (int x = 0; x < na; ++x)
+          for (int w = 0; w < na; ++w)
+            t += A2[v + na * (w + na * (x + (size_t)na * y))] * v4(V, n, p, w + ni, x + ni, y + ni);
+      Q[v + (size_t)na * p] = 2. * t;
+    }
+}
+// generalized_fock_matrix (:139-163): inactive rows 2 (Fi + Fa), active rows
+// Fi g + Q, virtual rows zero
+void generalized_fock(int n, int ni, int na, const double* Fi, const double* Fa, const double* A1, const double* Q,
+                      double* F) {
+  std::fill(F, F + (size_t)n * n, 0.);
+  for (int p = 0; p < n; ++p) {
+    for (int i = 0; i < ni; ++i) F[i + (size_t)n * p] = 2. * (Fi[p + (size_t)n * i] + Fa[p + (size_t)n * i]);
+    for (int v = 0; v < na; ++v) {
+      double t = 0.;
+      for (int w = 0; w < na; ++w) t += Fi[p + (size_t)n * (w + ni)] * A1[w + (size_t)na * v];
+      F[(v + ni) + (size_t)n * p] = t + Q[v + (size_t)na * p];
+    }
+  }
+}
+// energy_from_generalized_fock (:228-256)
+double energy_from_generalized_fock(int n, int ni, int na, const double* T, const double* A1, const double* F) {
+  double E = 0.;
+  for (int i = 0; i < ni; ++i) E += 2. * T[i * (n + 1)];
+  for (int y = 0; y < na; ++y)
+    for (int x = 0; x < na; ++x) E += A1[x + (size_t)na * y] * T[(x + ni) + (size_t)n * (y + ni)];
+  for (int p = 0; p < ni + na; ++p) E += F[p * (n + 1)];
+  return 0.5 * E;
+}
+
 double casscf(const McscfSettings& S, int nalpha, int nbeta, int no, int ni, int na, double E_core, const double* T0,
               const double* V0, double* A1, double* A2, int64_t* iters_out, int* conv_out) {
   const int nv = no - ni - na;
   if (nv < 0 || na < 1 || ni < 0) throw std::runtime_error("bad orbital partition");
   const size_t no2 = (size_t)no * no, no4 = no2 * no2, na2 = (size_t)na * na, na4 = na2 * na2;
   const int rot = nv * (ni + na) + na * ni;
-  auto VV = [&](const std::vector<double>& V, int p, int q, int r, int s) {
-    return V[p + (size_t)no * (q + (size_t)no * (r + (size_t)no * s))];
-  };
+  auto VV = [&](const std::vector<double>& W, int p, int q, int r, int s4) { return v4(W.data(), no, p, q, r, s4); };
   std::vector<double> T(T0, T0 + no2), V(V0, V0 + no4);
   // complete active space (generate_hilbert_space order)
   auto strings = [](int n, int k) {
@@ -1489,12 +1554,7 @@ double casscf(const McscfSettings& S, int nalpha, int nbeta, int no, int ni, int
   std::vector<double> X(nd, 0.), Fi(no2), Fa(no2), F(no2), Q((size_t)na * no), Ta(na2), Va(na4);
   double E_inact = 0.;
   auto active_hamiltonian = [&]() {
-    for (int q = 0; q < no; ++q)
-      for (int p = 0; p < no; ++p) {
-        double t = 0.;
-        for (int i = 0; i < ni; ++i) t += 2. * VV(V, p, q, i, i) - VV(V, p, i, i, q);
-        Fi[p + (size_t)no * q] = T[p + (size_t)no * q] + t;
-      }
+    inactive_fock(no, ni, T.data(), V.data(), Fi.data());
     for (int y = 0; y < na; ++y)
       for (int x = 0; x < na; ++x) Ta[x + (size_t)na * y] = Fi[(x + ni) + (size_t)no * (y + ni)];
     for (int w = 0; w < na; ++w)
@@ -1502,8 +1562,7 @@ double casscf(const McscfSettings& S, int nalpha, int nbeta, int no, int ni, int
         for (int y = 0; y < na; ++y)
           for (int x = 0; x < na; ++x)
             Va[x + na * (y + na * (z + (size_t)na * w))] = VV(V, x + ni, y + ni, z + ni, w + ni);
-    E_inact = E_core;
-    for (int i = 0; i < ni; ++i) E_inact += T[i * (no + 1)] + Fi[i * (no + 1)];
+    E_inact = E_core + inactive_energy(no, ni, T.data(), Fi.data());
   };
   auto casci = [&]() {
     Ham H;
@@ -1542,32 +1601,9 @@ double casscf(const McscfSettings& S, int nalpha, int nbeta, int no, int ni, int
   };
   std::vector<double> OG(rot), DH(rot);
   auto grad = [&]() {
-    for (int q = 0; q < no; ++q)
-      for (int p = 0; p < no; ++p) {
-        double t = 0.;
-        for (int w = 0; w < na; ++w)
-          for (int v = 0; v < na; ++v)
-            t += A1[v + (size_t)na * w] * (VV(V, p, q, v + ni, w + ni) - 0.5 * VV(V, p, w + ni, v + ni, q));
-        Fa[p + (size_t)no * q] = t;
-      }
-    for (int p = 0; p < no; ++p)
-      for (int v = 0; v < na; ++v) {
-        double t = 0.;
-        for (int y = 0; y < na; ++y)
-          for (int x = 0; x < na; ++x)
-            for (int w = 0; w < na; ++w)
-              t += A2[v + na * (w + na * (x + (size_t)na * y))] * VV(V, p, w + ni, x + ni, y + ni);
-        Q[v + (size_t)na * p] = 2. * t;
-      }
-    std::fill(F.begin(), F.end(), 0.);
-    for (int p = 0; p < no; ++p) {
-      for (int i = 0; i < ni; ++i) F[i + (size_t)no * p] = 2. * (Fi[p + (size_t)no * i] + Fa[p + (size_t)no * i]);
-      for (int v = 0; v < na; ++v) {
-        double t = 0.;
-        for (int w = 0; w < na; ++w) t += Fi[p + (size_t)no * (w + ni)] * A1[w + (size_t)na * v];
-        F[(v + ni) + (size_t)no * p] = t + Q[v + (size_t)na * p];
-      }
-    }
+    active_fock(no, ni, na, V.data(), A1, Fa.data());
+    aux_q(no, ni, na, V.data(), A2, Q.data());
+    generalized_fock(no, ni, na, Fi.data(), Fa.data(), A1, Q.data(), F.data());
     auto g = [&](int p, int q) { return 2. * (F[p + (size_t)no * q] - F[q + (size_t)no * p]); };
     int k = 0;
     for (int i = 0; i < ni; ++i)
@@ -2100,6 +2136,20 @@ int orc_casscf(const double* set, int nalpha, int nbeta, int norb, int ninact, i
   S.ci_max_subspace = (int64_t)set[7];
   S.ci_matel_tol = set[8];
   return guard([&] { *E = casscf(S, nalpha, nbeta, norb, ninact, nact, E_core, T, V, A1, A2, iters, conv); });
+}
+
+// the fock_matrices.cxx building blocks at one orbital partition: Fi, Fa
+// (n^2), Q (na x n), F (n^2), the inactive energy and the energy from F
+void orc_mcscf_fock(int n, int ni, int na, const double* T, const double* V, const double* A1, const double* A2,
+                    double* Fi, double* Fa, double* Q, double* F, double* E_inact, double* E_fock) {
+  inactive_fock(n, ni, T, V, Fi);
+  *E_inact = inactive_energy(n, ni, T, Fi);
+  if (na > 0) {
+    active_fock(n, ni, na, V, A1, Fa);
+    aux_q(n, ni, na, V, A2, Q);
+    generalized_fock(n, ni, na, Fi, Fa, A1, Q, F);
+    *E_fock = energy_from_generalized_fock(n, ni, na, T, A1, F);
+  }
 }
 
 // orbital entropies of a CI vector; s2 / mi may be null; 0 on success

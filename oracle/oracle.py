@@ -67,6 +67,9 @@ def lib():
                                ctypes.POINTER(f64), ctypes.POINTER(f64)]
         L.orc_asci_search.restype = i64
         L.orc_asci_search.argtypes = [vp, _f64p, i64, _u64p, _u64p, _f64p, f64, i64, i64, _u64p, _u64p]
+        L.orc_mcscf_fock.restype = None
+        L.orc_mcscf_fock.argtypes = [ci, ci, ci, _f64p, _f64p, _f64p, _f64p, _f64p, _f64p, _f64p, _f64p,
+                                     ctypes.POINTER(f64), ctypes.POINTER(f64)]
         L.orc_casscf.restype = ci
         L.orc_casscf.argtypes = [_f64p, ci, ci, ci, ci, ci, f64, _f64p, _f64p, _f64p, _f64p, ctypes.POINTER(f64),
                                  ctypes.POINTER(i64), ctypes.POINTER(ci)]
@@ -345,3 +348,23 @@ def casscf(T, V, E_core, nalpha, nbeta, ninact, nact, rdm1=None, rdm2=None, **se
     if rc != 0:
         raise RuntimeError(lib().orc_last_error().decode())
     return E.value, A1.reshape(nact, nact, order="F"), A2.reshape((nact,) * 4, order="F"), it.value, bool(conv.value)
+
+
+def mcscf_fock(T, V, ninact, nact, rdm1=None, rdm2=None):
+    """The fock_matrices.cxx building blocks at one orbital partition:
+    (Fi, Fa, Q, F, inactive energy, energy from F); Fa / Q / F and the last
+    energy need the active RDMs."""
+    T = np.asarray(T, dtype=np.float64)
+    n = T.shape[0]
+    Tb = np.ascontiguousarray(T.ravel(order="F"))
+    Vb = np.ascontiguousarray(np.asarray(V, dtype=np.float64).reshape(n, n, n, n).ravel(order="F"))
+    na = int(nact)
+    A1 = np.zeros(max(na * na, 1)) if rdm1 is None else np.ascontiguousarray(np.asarray(rdm1).ravel(order="F"))
+    A2 = np.zeros(max(na ** 4, 1)) if rdm2 is None else np.ascontiguousarray(np.asarray(rdm2).ravel(order="F"))
+    Fi, Fa, F = np.zeros(n * n), np.zeros(n * n), np.zeros(n * n)
+    Q = np.zeros(max(na * n, 1))
+    Ei, Ef = ctypes.c_double(), ctypes.c_double()
+    lib().orc_mcscf_fock(n, int(ninact), na if rdm1 is not None else 0, Tb, Vb, A1, A2, Fi, Fa, Q, F,
+                         ctypes.byref(Ei), ctypes.byref(Ef))
+    m = lambda x: x.reshape(n, n, order="F")
+    return m(Fi), m(Fa), Q[:na * n].reshape(na, n, order="F"), m(F), Ei.value, Ef.value

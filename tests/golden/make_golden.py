@@ -90,6 +90,24 @@ def main(ref="/root/reference"):
                          "source": "external/macis/tests/asci.cxx:488-574 (EPT2: :556-570)"},
         "h2o_casscf": {"E_total": -7.61114493227e01, "ninact": 1, "nact": 8, "nalpha": 4, "nbeta": 4, "atol": 1e-8,
                        "source": "external/macis/tests/mcscf.cxx:26-66"},
+        "h2o_fock_matrices": {
+            "inactive_sums": [
+                -1.0954327626528054e+02, -7.9049334675325397e+01, -5.5421794916425746e+01, -3.2896413433510098e+01,
+                -9.6790625410977995e+00, 1.3541890926738670e+01, 2.8118988584004747e+01, 4.2282474623774370e+01,
+                6.1330877241905775e+01, 8.0462280904553381e+01, 1.0115739942244966e+02, 1.2234906887017347e+02,
+                1.4193737383338043e+02, 1.6158815460036422e+02, 1.8055391956530423e+02, 1.9946376174456546e+02,
+                2.2023047024882104e+02, 2.3908456464316561e+02, 2.6013779050396846e+02, 2.8151944194600628e+02,
+                3.0499216988942629e+02, 3.2832856341497029e+02, 3.5190406182710450e+02, 3.7494850617879558e+02],
+            "inactive_energies": [
+                0.0000000000000000e+00, -6.1315494224913593e+01, -7.2212778636226929e+01, -7.9040381402513631e+01,
+                -8.3471297093533877e+01, -8.5217981091537155e+01, -8.4546001263510988e+01, -8.2730095439120404e+01,
+                -7.8127776664404351e+01, -7.1592548154010231e+01, -6.2930084392284229e+01, -5.2096342927325999e+01,
+                -3.9855391765969998e+01, -2.5412026151032496e+01, -8.6447385900261242e+00, 9.9027251048627019e+00,
+                3.0946082901947307e+01, 5.3450370843339400e+01, 8.0911983168177073e+01, 1.1078946373217127e+02,
+                1.4537422212238749e+02, 1.8291223010717863e+02, 2.2328918072756994e+02, 2.6673925924545023e+02],
+            "ninact": 1, "nact": 8, "active_fock_sum": 9.2434393637673907e+01, "aux_q_sum": 2.609524939005e+01,
+            "generalized_fock_sum": -4.7465630072124384e+01, "E_from_generalized_fock": -8.5250440649419417e+01,
+            "atol": 1e-6, "source": "external/macis/tests/fock_matrices.cxx:26-256"},
         "o2_rdms": {"n_dets_padded": 5000, "sum_abs_ordm": 8.0000005763, "sum_abs_trdm": 44.1092472977,
                     "atol": 1e-6, "source": "external/macis/tests/double_loop.cxx:506-579"},
     }

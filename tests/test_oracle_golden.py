@@ -181,3 +181,27 @@ def test_h2o_casscf_from_reference_rdms(oracle, h2o, known):
     E, _, _, iters, conv = oracle.casscf(h2o["T"], h2o["V"], h2o["E_core"], ref["nalpha"], ref["nbeta"],
                                          ref["ninact"], ref["nact"], rdm1=g0, rdm2=G0)
     assert conv and abs(E - ref["E_total"]) < ref["atol"]
+
+
+
+def test_casscf_building_blocks_match_reference_sums(oracle, h2o, known):
+    """external/macis/tests/fock_matrices.cxx:26-256 (tolerance 1e-6): the
+    inactive Fock matrix sum and inactive energy for 0 .. 23 inactive
+    orbitals; with the stored CAS(8e,8o) RDMs at 1 inactive + 8 active
+    orbitals the sums of the active Fock matrix, the auxiliary Q matrix and
+    the generalized Fock matrix, and the energy formed from the last."""
+    ref = known["h2o_fock_matrices"]
+    tol = ref["atol"]
+    for ni, (s_ref, e_ref) in enumerate(zip(ref["inactive_sums"], ref["inactive_energies"])):
+        Fi, _, _, _, Ei, _ = oracle.mcscf_fock(h2o["T"], h2o["V"], ni, 0)
+        assert abs(Fi.sum() - s_ref) < tol, ni
+        assert abs(Ei - e_ref) < tol, ni
+    d = np.load(os.path.join(GOLDEN, "h2o_ccpvdz_cas88_rdms.npz"))
+    n = int(d["nact"])
+    assert (ref["ninact"], ref["nact"]) == (1, n)
+    g0, G0 = d["ordm"].reshape(n, n, order="F"), d["trdm"].reshape((n,) * 4, order="F")
+    _, Fa, Q, F, _, Ef = oracle.mcscf_fock(h2o["T"], h2o["V"], ref["ninact"], n, g0, G0)
+    assert abs(Fa.sum() - ref["active_fock_sum"]) < tol
+    assert abs(Q.sum() - ref["aux_q_sum"]) < tol
+    assert abs(F.sum() - ref["generalized_fock_sum"]) < tol
+    assert abs(Ef - ref["E_from_generalized_fock"]) < tol
