@@ -19,7 +19,10 @@ run time:
   h2o.ccpvdz.cas88.rdms.bin (int32 norb, then the column-major 1-RDM and
   2-RDM; read_rdms_binary, src/macis/fcidump.cxx:487-527)
 * known_answers.json: the energies / sums the reference tests pin, with the
-  file:line each one comes from.
+  file:line each one comes from;
+* sd_operations.json: the determinant lists of external/macis/tests/
+  sd_operations.cxx (singles, doubles and the FCI space of small strings, in
+  MACIS's packed wfn_t<64> form: alpha in bits 0-31, beta in bits 32-63).
 """
 import json
 import os
@@ -40,6 +43,14 @@ def parse_fcidump_lines(path):
     rows = np.loadtxt(body.splitlines(), ndmin=2)
     return dict(norb=hdr["NORB"], nelec=hdr["NELEC"], ms2=int(ms2.group(1)) if ms2 else 0,
                 idx=rows[:, 1:5].astype(np.int8), vals=rows[:, 0].astype(np.float64))
+
+
+def parse_wfn_list(text, anchor, name):
+    """The integer list ``name = { ... };`` that follows ``anchor`` in a C++
+    test source (hex and 0b literals)."""
+    start = text.index(anchor)
+    m = re.search(re.escape(name) + r"\s*=\s*\{(.*?)\};", text[start:], re.S)
+    return [int(tok, 0) for tok in re.findall(r"0[xXbB][0-9a-fA-F]+", m.group(1))]
 
 
 def main(ref="/root/reference"):
@@ -75,6 +86,19 @@ def main(ref="/root/reference"):
     np.savez_compressed(os.path.join(HERE, "h2o_ccpvdz_cas88_rdms.npz"), nact=nact,
                         ordm=vals[:nact ** 2].copy(), trdm=vals[nact ** 2:nact ** 2 + nact ** 4].copy())
 
+    sd = open(os.path.join(macis, "tests", "sd_operations.cxx")).read()
+    sd_lists = {
+        "singles_single_spin": parse_wfn_list(sd, 'SECTION("Singles")', "ref_singles"),
+        "singles_both_spins": parse_wfn_list(sd, 'SECTION("Both Spin")', "ref_singles"),
+        "doubles_single_spin": parse_wfn_list(sd, 'SECTION("Doubles")', "ref_doubles"),
+        "doubles_both_spins": parse_wfn_list(sd, 'SECTION("Both Spins")', "ref_doubles"),
+        "fci_combs_4_2": parse_wfn_list(sd, 'SECTION("FCI")', "ref_combs"),
+        "fci_space_4_2_2": parse_wfn_list(sd, 'SECTION("FCI")', "ref_dets"),
+        "source": "external/macis/tests/sd_operations.cxx:45-249",
+    }
+    with open(os.path.join(HERE, "sd_operations.json"), "w") as f:
+        json.dump(sd_lists, f, indent=0)
+
     known = {
         "h2o_cisd_csr": {"n": 12636, "nnz": 3517816, "thresh": 1e-16,
                          "source": "external/macis/tests/csr_hamiltonian.cxx:46-77"},
@@ -108,6 +132,16 @@ def main(ref="/root/reference"):
             "ninact": 1, "nact": 8, "active_fock_sum": 9.2434393637673907e+01, "aux_q_sum": 2.609524939005e+01,
             "generalized_fock_sum": -4.7465630072124384e+01, "E_from_generalized_fock": -8.5250440649419417e+01,
             "atol": 1e-6, "source": "external/macis/tests/fock_matrices.cxx:26-256"},
+        "h2o_fcidump": {
+            "norb": 24, "nelec": 10, "ms2": 0, "E_core": 9.191200742618042, "T_sum": -1.095432762653e+02,
+            "V_sum": 2.701609068389e+02, "nocc": 5,
+            "eps": [-20.5504959651472, -1.33652308180416, -0.699084807015877, -0.566535827115135,
+                    -0.493126779151562, 0.185508268977809, 0.25620321890592, 0.78902083505165,
+                    0.854064342891826, 1.16354210561965, 1.20037835222836, 1.25333579878846,
+                    1.44452900701373, 1.4762147730592, 1.67453827449385, 1.86734472965445,
+                    1.93460967763627, 2.4520550848955, 2.48955724627828, 3.28543361094139,
+                    3.33853354817945, 3.5101570353257, 3.86543012937399, 4.14719831587618],
+            "EMP2": -0.203989305096243, "atol": 1e-6, "source": "external/macis/tests/fcidump.cxx:18-112"},
         "o2_rdms": {"n_dets_padded": 5000, "sum_abs_ordm": 8.0000005763, "sum_abs_trdm": 44.1092472977,
                     "atol": 1e-6, "source": "external/macis/tests/double_loop.cxx:506-579"},
     }
