@@ -142,6 +142,10 @@ def main(ref="/root/reference"):
                     1.93460967763627, 2.4520550848955, 2.48955724627828, 3.28543361094139,
                     3.33853354817945, 3.5101570353257, 3.86543012937399, 4.14719831587618],
             "EMP2": -0.203989305096243, "atol": 1e-6, "source": "external/macis/tests/fcidump.cxx:18-112"},
+        "h2o_double_loop": {"E_HF_total": -76.0267803489191, "E_single_diag": -6.488097259228e+01,
+                            "E_double_ss_diag": -6.314093508151e+01, "E_double_os_diag": -6.304547887231e+01,
+                            "EMP2": -0.203989305096243, "atol": 1e-6,
+                            "source": "external/macis/tests/double_loop.cxx:22-241"},
         "o2_rdms": {"n_dets_padded": 5000, "sum_abs_ordm": 8.0000005763, "sum_abs_trdm": 44.1092472977,
                     "atol": 1e-6, "source": "external/macis/tests/double_loop.cxx:506-579"},
     }

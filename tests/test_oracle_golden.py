@@ -205,3 +205,74 @@ def test_casscf_building_blocks_match_reference_sums(oracle, h2o, known):
     assert abs(Q.sum() - ref["aux_q_sum"]) < tol
     assert abs(F.sum() - ref["generalized_fock_sum"]) < tol
     assert abs(Ef - ref["E_from_generalized_fock"]) < tol
+
+
+def test_water_slater_condon_values(oracle, h2o, known):
+    """external/macis/tests/double_loop.cxx:22-241 on the water cc-pVDZ
+    integrals (tolerance 1e-6): the HF energy, the diagonals of a single, a
+    same-spin and an opposite-spin double excitation, Brillouin's theorem for
+    every single, the MP2 energy summed from <HF|H|D> over all doubles, and the
+    HF RDM energy identities (spin-traced and spin-separated)."""
+    ref = known["h2o_double_loop"]
+    tol = ref["atol"]
+    T, V, n, no = h2o["T"], h2o["V"], h2o["norb"], 5
+    H = oracle.Hamiltonian(T, V)
+    hf = ((1 << no) - 1, (1 << no) - 1)
+    me = lambda bra, ket: H.matrix_element(bra, ket)
+    EHF = me(hf, hf)
+    assert abs(EHF + h2o["E_core"] - ref["E_HF_total"]) < tol
+    s = (hf[0] ^ 1 ^ (1 << no), hf[1])
+    assert abs(me(s, s) - ref["E_single_diag"]) < tol
+    d_ss = (hf[0] ^ 0b11 ^ (0b11 << no), hf[1])
+    assert abs(me(d_ss, d_ss) - ref["E_double_ss_diag"]) < tol
+    d_os = (hf[0] ^ 1 ^ (1 << no), hf[1] ^ 0b10 ^ (0b10 << no))
+    assert abs(me(d_os, d_os) - ref["E_double_os_diag"]) < tol
+    for i in range(no):
+        for a in range(no, n):
+            for ex in ((hf[0] ^ (1 << i) ^ (1 << a), hf[1]), (hf[0], hf[1] ^ (1 << i) ^ (1 << a))):
+                h1, h2 = me(hf, ex), me(ex, hf)
+                assert abs(h1) < tol and abs(h1 - h2) < 1e-14
+    eps = np.array([T[p, p] + sum(2 * V[p, p, i, i] - V[p, i, i, p] for i in range(no)) for p in range(n)])
+    emp2 = 0.0
+    vir, occ = range(no, n), range(no)
+    for a in vir:
+        for b in vir:
+            for i in occ:
+                for j in occ:
+                    den = eps[a] + eps[b] - eps[i] - eps[j]
+                    if a < b and i < j:  # same spin, alpha and beta
+                        m = (1 << i) ^ (1 << j) ^ (1 << a) ^ (1 << b)
+                        for ex in ((hf[0] ^ m, hf[1]), (hf[0], hf[1] ^ m)):
+                            h = me(hf, ex)
+                            emp2 += h * h / den
+                    ex = (hf[0] ^ (1 << i) ^ (1 << a), hf[1] ^ (1 << j) ^ (1 << b))
+                    h = me(hf, ex)
+                    emp2 += h * h / den
+    assert abs(-emp2 - ref["EMP2"]) < tol
+    R = oracle.rdms_spin_dep(n, np.array([hf[0]], np.uint64), np.array([hf[1]], np.uint64), np.ones(1))
+    E_sep = np.sum(T * (R["aa"] + R["bb"])) + np.sum(V * (R["aaaa"] + R["bbbb"])) + 2 * np.sum(V * R["aabb"])
+    G = R["aaaa"] + R["bbbb"] + R["aabb"] + R["aabb"].transpose(2, 3, 0, 1)
+    E_tr = np.sum(T * (R["aa"] + R["bb"])) + np.sum(V * G)
+    assert abs(E_sep - EHF) < tol and abs(E_tr - EHF) < tol
+
+
+def test_hf_rdm_structure_34_orbitals(oracle):
+    """double_loop.cxx:243-298: the spin-traced RDMs of the closed-shell HF
+    determinant (5 doubly occupied of 34 orbitals): Gamma_iikk = 2 (i != k),
+    Gamma_ikki = -1 (i != k), Gamma_iiii = 1, gamma_ii = 2; here checked as
+    equalities, with every other element of both RDMs zero."""
+    n, no = 34, 5
+    hf = np.array([(1 << no) - 1], np.uint64)
+    R = oracle.rdms_spin_dep(n, hf, hf, np.ones(1))
+    G = R["aaaa"] + R["bbbb"] + R["aabb"] + R["aabb"].transpose(2, 3, 0, 1)
+    g = R["aa"] + R["bb"]
+    Gref = np.zeros((n,) * 4)
+    for i in range(no):
+        for k in range(no):
+            if i == k:
+                Gref[i, i, i, i] = 1.0
+            else:
+                Gref[i, i, k, k] = 2.0
+                Gref[i, k, k, i] = -1.0
+    assert np.abs(G - Gref).max() < 1e-14
+    assert np.abs(g - np.diag([2.0] * no + [0.0] * (n - no))).max() < 1e-14
