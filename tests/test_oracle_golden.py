@@ -256,23 +256,30 @@ def test_water_slater_condon_values(oracle, h2o, known):
     assert abs(E_sep - EHF) < tol and abs(E_tr - EHF) < tol
 
 
-def test_hf_rdm_structure_34_orbitals(oracle):
-    """double_loop.cxx:243-298: the spin-traced RDMs of the closed-shell HF
-    determinant (5 doubly occupied of 34 orbitals): Gamma_iikk = 2 (i != k),
-    Gamma_ikki = -1 (i != k), Gamma_iiii = 1, gamma_ii = 2; here checked as
-    equalities, with every other element of both RDMs zero."""
-    n, no = 34, 5
-    hf = np.array([(1 << no) - 1], np.uint64)
-    R = oracle.rdms_spin_dep(n, hf, hf, np.ones(1))
+@pytest.mark.parametrize("na,nb", [(5, 5), (5, 3)])
+def test_hf_rdm_structure_34_orbitals(oracle, na, nb):
+    """double_loop.cxx:243-298 (closed shell, 5+5) and :430-504 (open shell,
+    5+3): the spin-traced RDMs of the HF determinant over 34 orbitals, as
+    equalities: Gamma_iikk = n_i n_k / 2 and Gamma_ikki = -(na_i na_k +
+    nb_i nb_k) / 2 for i != k, Gamma_iiii = na_i nb_i, gamma = diag(n), every
+    other element zero (the reference bounds the same elements: 2 / 1,
+    -1 / -0.5 and 1)."""
+    n = 34
+    A = np.array([(1 << na) - 1], np.uint64)
+    B = np.array([(1 << nb) - 1], np.uint64)
+    R = oracle.rdms_spin_dep(n, A, B, np.ones(1))
     G = R["aaaa"] + R["bbbb"] + R["aabb"] + R["aabb"].transpose(2, 3, 0, 1)
     g = R["aa"] + R["bb"]
+    oa = np.array([1.0 if p < na else 0.0 for p in range(n)])
+    ob = np.array([1.0 if p < nb else 0.0 for p in range(n)])
+    occ = oa + ob
     Gref = np.zeros((n,) * 4)
-    for i in range(no):
-        for k in range(no):
+    for i in range(n):
+        for k in range(n):
             if i == k:
-                Gref[i, i, i, i] = 1.0
+                Gref[i, i, i, i] = oa[i] * ob[i]
             else:
-                Gref[i, i, k, k] = 2.0
-                Gref[i, k, k, i] = -1.0
+                Gref[i, i, k, k] = 0.5 * occ[i] * occ[k]
+                Gref[i, k, k, i] = -0.5 * (oa[i] * oa[k] + ob[i] * ob[k])
     assert np.abs(G - Gref).max() < 1e-14
-    assert np.abs(g - np.diag([2.0] * no + [0.0] * (n - no))).max() < 1e-14
+    assert np.abs(g - np.diag(occ)).max() < 1e-14
