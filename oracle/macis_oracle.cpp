@@ -2043,10 +2043,10 @@ void orc_syev(int k, double* A, double* w) { jacobi_syev(k, A, k, w); }
 // below), the initial wavefunction, and the phase ("grow", "refine" or both).
 // Returns the number of determinants (<= cap) written to out_a/out_b/out_c,
 // or -1 on error (orc_last_error).
-int64_t orc_asci(void* h, const double* set, int64_t n0, const uint64_t* a0, const uint64_t* b0, const double* c0,
-                 double E0, int do_grow, int do_refine, int64_t cap, uint64_t* out_a, uint64_t* out_b, double* out_c,
-                 double* E_out, double* E_grow_out) {
-  const Ham& H = *(Ham*)h;
+}  // extern "C"
+
+// the settings array of oracle.py (_ASCI_ORDER)
+static AsciSettings asci_settings_from(const double* set) {
   AsciSettings S;
   S.ntdets_max = (int64_t)set[0];
   S.ntdets_min = (int64_t)set[1];
@@ -2066,6 +2066,16 @@ int64_t orc_asci(void* h, const double* set, int64_t n0, const uint64_t* a0, con
   S.ci_res_tol = set[15];
   S.ci_max_subspace = (int64_t)set[16];
   S.ci_matel_tol = set[17];
+  return S;
+}
+
+extern "C" {
+
+int64_t orc_asci(void* h, const double* set, int64_t n0, const uint64_t* a0, const uint64_t* b0, const double* c0,
+                 double E0, int do_grow, int do_refine, int64_t cap, uint64_t* out_a, uint64_t* out_b, double* out_c,
+                 double* E_out, double* E_grow_out) {
+  const Ham& H = *(Ham*)h;
+  const AsciSettings S = asci_settings_from(set);
   int64_t nret = -1;
   guard([&] {
     std::vector<Det> wfn(n0);
@@ -2076,6 +2086,28 @@ int64_t orc_asci(void* h, const double* set, int64_t n0, const uint64_t* a0, con
     if (E_grow_out) *E_grow_out = E;
     if (do_refine) E = asci_refine(H, S, E, wfn, X);
     *E_out = E;
+    nret = (int64_t)wfn.size();
+    for (int64_t i = 0; i < std::min(nret, cap); ++i) {
+      out_a[i] = wfn[i].a;
+      out_b[i] = wfn[i].b;
+      out_c[i] = X[i];
+    }
+  });
+  return nret;
+}
+
+// one asci_iter (include/macis/asci/iteration.hpp:50-226) towards ndets_max
+int64_t orc_asci_iter(void* h, const double* set, int64_t n0, const uint64_t* a0, const uint64_t* b0,
+                      const double* c0, double E0, int64_t ndets_max, int64_t cap, uint64_t* out_a, uint64_t* out_b,
+                      double* out_c, double* E_out) {
+  const Ham& H = *(Ham*)h;
+  const AsciSettings S = asci_settings_from(set);
+  int64_t nret = -1;
+  guard([&] {
+    std::vector<Det> wfn(n0);
+    std::vector<double> X(c0, c0 + n0);
+    for (int64_t i = 0; i < n0; ++i) wfn[i] = {a0[i], b0[i]};
+    *E_out = asci_iter(H, S, ndets_max, E0, wfn, X);
     nret = (int64_t)wfn.size();
     for (int64_t i = 0; i < std::min(nret, cap); ++i) {
       out_a[i] = wfn[i].a;

@@ -65,6 +65,9 @@ def lib():
         L.orc_asci.restype = i64
         L.orc_asci.argtypes = [vp, _f64p, i64, _u64p, _u64p, _f64p, f64, ci, ci, i64, _u64p, _u64p, _f64p,
                                ctypes.POINTER(f64), ctypes.POINTER(f64)]
+        L.orc_asci_iter.restype = i64
+        L.orc_asci_iter.argtypes = [vp, _f64p, i64, _u64p, _u64p, _f64p, f64, i64, i64, _u64p, _u64p, _f64p,
+                                    ctypes.POINTER(f64)]
         L.orc_asci_search.restype = i64
         L.orc_asci_search.argtypes = [vp, _f64p, i64, _u64p, _u64p, _f64p, f64, i64, i64, _u64p, _u64p]
         L.orc_mcscf_fock.restype = None
@@ -274,6 +277,24 @@ def asci(ham, alpha0, beta0, c0, E0, grow=True, refine=True, **settings):
     if n < 0:
         raise RuntimeError(lib().orc_last_error().decode())
     return E.value, oa[:n].copy(), ob[:n].copy(), oc[:n].copy(), Eg.value
+
+
+def asci_iter(ham, alpha, beta, c, E0, ndets_max, **settings):
+    """One asci_iter (iteration.hpp:50-226): search for up to ndets_max
+    determinants around the core of (alpha, beta, c), then diagonalise;
+    returns (E, alpha, beta, C)."""
+    s = _asci_settings(**settings)
+    cap = int(max(ndets_max * 4, len(alpha)) + 16)
+    oa = np.zeros(cap, dtype=np.uint64)
+    ob = np.zeros(cap, dtype=np.uint64)
+    oc = np.zeros(cap)
+    E = ctypes.c_double()
+    n = lib().orc_asci_iter(ham._h, s, len(alpha), np.ascontiguousarray(alpha, dtype=np.uint64),
+                            np.ascontiguousarray(beta, dtype=np.uint64), np.ascontiguousarray(c, dtype=np.float64),
+                            float(E0), int(ndets_max), cap, oa, ob, oc, ctypes.byref(E))
+    if n < 0:
+        raise RuntimeError(lib().orc_last_error().decode())
+    return E.value, oa[:n].copy(), ob[:n].copy(), oc[:n].copy()
 
 
 def asci_search(ham, alpha, beta, c, E0, ndets_max, **settings):

@@ -1,0 +1,97 @@
+"""ASCI growth control and core selection, restated in the oracle, against
+the behaviour the reference's tests require on water cc-pVDZ from the HF
+determinant (external/macis/tests/asci.cxx:577-940):
+
+* a fractional grow factor (2.5, 100 determinants, Fixed core) grows to
+  between 50 and 100 determinants;
+* an unreachable request (grow factor 10^4, a one-determinant core) falls
+  short of the request, which is what triggers the backoff, and still
+  returns a valid wavefunction;
+* with a five-determinant core, growth backs off to the minimum factor
+  and stops gracefully;
+* default-like settings reach ntdets_max exactly (1,000, and 5,000 with a
+  Fixed core of 100);
+* three asci_iter steps with Percentage core selection succeed;
+* a 99 % core (Percentage threshold 0.99) keeps more determinants and reaches
+  an energy no higher than a 70 % core.
+
+Every result is checked for C.C = 1.  The library's calculator carries the
+same defaults ("percentage", 0.95; asci.cxx:823-835)."""
+import numpy as np
+import pytest
+
+FIXED = dict(core_fixed=1)
+
+
+@pytest.fixture(scope="module")
+def water(oracle, h2o):
+    H = oracle.Hamiltonian(h2o["T"], h2o["V"])
+    hf = (np.array([31], np.uint64), np.array([31], np.uint64))
+    E_hf = H.matrix_element((31, 31), (31, 31))
+    return H, hf, E_hf
+
+
+def grow(oracle, water, **settings):
+    H, (a0, b0), E_hf = water
+    E, a, b, c, _ = oracle.asci(H, a0, b0, [1.0], E_hf, grow=True, refine=False, **settings)
+    assert len(a) == len(b) == len(c)
+    assert abs(c @ c - 1.0) < 1e-12
+    assert len(set(zip(a.tolist(), b.tolist()))) == len(a)
+    return E, a, b, c
+
+
+def test_fractional_grow_factor(oracle, water):
+    _, a, _, _ = grow(oracle, water, grow_factor=2.5, ntdets_max=100, ntdets_min=10, **FIXED)
+    assert 50 <= len(a) <= 100
+
+
+def test_unreachable_request_backs_off(oracle, water):
+    _, a, _, _ = grow(oracle, water, grow_factor=1e4, ntdets_max=10000, ntdets_min=5, ncdets_max=1)
+    assert 1 < len(a) < 10000
+
+
+def test_minimum_grow_factor(oracle, water):
+    E, a, _, _ = grow(oracle, water, grow_factor=10.0, ntdets_max=1000, ntdets_min=5, ncdets_max=5)
+    assert len(a) > 1 and E < water[2]
+
+
+def test_normal_growth_without_backoff(oracle, water):
+    _, a, _, _ = grow(oracle, water, grow_factor=8.0, ntdets_max=1000, ntdets_min=100, ncdets_max=1000, **FIXED)
+    assert len(a) == 1000
+
+
+def test_fixed_core_strategy(oracle, water):
+    _, a, _, _ = grow(oracle, water, ntdets_max=5000, ncdets_max=100, **FIXED)
+    assert len(a) == 5000
+
+
+def test_percentage_core_iterations(oracle, water):
+    H, (a, b), E = water
+    c = np.ones(1)
+    for _ in range(3):
+        n_new = min(5000, max(100, 8 * len(a)))
+        E, a, b, c = oracle.asci_iter(H, a, b, c, E, n_new, core_fixed=0, core_threshold=0.95,
+                                      ntdets_max=5000, ncdets_max=100)
+    assert len(a) > 1 and abs(c @ c - 1.0) < 1e-12
+
+
+def test_percentage_threshold_values(oracle, water):
+    H, _, E_hf = water
+    E0, a0, b0, c0 = grow(oracle, water, ntdets_max=1000, ncdets_max=100)
+    runs = {}
+    for thr in (0.7, 0.99):
+        E, a, b, c = oracle.asci_iter(H, a0, b0, c0, E0, 10000, core_fixed=0, core_threshold=thr,
+                                      ntdets_max=10000, ncdets_max=10000)
+        assert np.isfinite(E) and E < E_hf and abs(c @ c - 1.0) < 1e-12
+        runs[thr] = (E, len(a))
+    assert runs[0.7][1] <= runs[0.99][1]
+    assert runs[0.99][0] <= runs[0.7][0]
+    w = np.cumsum(np.sort(c0 ** 2)[::-1])
+    core = {thr: int(np.argmax(w >= thr)) + 1 for thr in (0.7, 0.99)}
+    assert core[0.99] > core[0.7]
+
+
+def test_core_selection_defaults(pkg):
+    c = pkg.calculators.create("multi_configuration_calculator", "gb300_asci")
+    assert c.settings().get("core_selection_strategy") == "percentage"
+    assert c.settings().get("core_selection_threshold") == 0.95
