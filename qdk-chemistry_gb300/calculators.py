@@ -260,16 +260,9 @@ class MultiConfigurationCalculator:
             out["mi"] = mi
         return out
 
-    def _solve(self, ctx, hamiltonian, a, b):
-        """H build + Davidson (+ RDMs) on a determinant list; returns (E_total, Wavefunction)."""
+    def _davidson_limits(self, n):
+        """(residual tolerance, subspace size) for an n-dimensional problem."""
         s = self._settings
-        prec = s.get("precision")
-        if prec not in ("fp64", "mixed"):
-            raise ValueError("precision must be 'fp64' or 'mixed'")
-        mixed = prec == "mixed"
-        n = len(a)
-        ctx.set_dets(a, b)
-        ctx.build_hamiltonian(s.get("ci_matel_tol"), capi.H_SPLIT32 if mixed else capi.H_FP64)
         tol = s.get("ci_residual_tolerance")
         max_m = s.get("max_solver_iterations")
         if n <= s.get("iterative_solver_dimension_cutoff"):
@@ -278,8 +271,19 @@ class MultiConfigurationCalculator:
             # up to rounding) with room for the whole space
             tol = min(tol, 1e-10)
             max_m = max(2, min(n, 254))
-        E, C, info = ctx.davidson(max_m=min(max_m, 254), tol=tol,
-                                  precision=capi.PREC_MIXED if mixed else capi.PREC_FP64)
+        return tol, min(max_m, 254)
+
+    def _solve(self, ctx, hamiltonian, a, b):
+        """H build + Davidson (+ RDMs) on a determinant list; returns (E_total, Wavefunction)."""
+        s = self._settings
+        prec = s.get("precision")
+        if prec not in ("fp64", "mixed"):
+            raise ValueError("precision must be 'fp64' or 'mixed'")
+        mixed = prec == "mixed"
+        ctx.set_dets(a, b)
+        ctx.build_hamiltonian(s.get("ci_matel_tol"), capi.H_SPLIT32 if mixed else capi.H_FP64)
+        tol, max_m = self._davidson_limits(len(a))
+        E, C, info = ctx.davidson(max_m=max_m, tol=tol, precision=capi.PREC_MIXED if mixed else capi.PREC_FP64)
         rdms = None
         want = []
         if s.get("calculate_one_rdm"):
@@ -429,12 +433,88 @@ class ProjectedMultiConfigurationCalculator(MultiConfigurationCalculator):
         return self._run_impl(hamiltonian, configurations)
 
 
+def collapse_repeated(alpha, beta):
+    """The distinct determinants of a list in spin order (spin_comparator,
+    raw_bitset.hpp:119-141), the index of each list position among them, and
+    the multiplicity of each."""
+    alpha = np.asarray(alpha, dtype=np.uint64)
+    beta = np.asarray(beta, dtype=np.uint64)
+    order = np.lexsort((beta, alpha))
+    sa, sb = alpha[order], beta[order]
+    first = np.ones(len(sa), dtype=bool)
+    first[1:] = (sa[1:] != sa[:-1]) | (sb[1:] != sb[:-1])
+    group = np.cumsum(first) - 1
+    inverse = np.empty(len(sa), dtype=np.int64)
+    inverse[order] = group
+    return sa[first], sb[first], inverse, np.bincount(group)
+
+
+def multiplicity_scaled(rowptr, colind, values, mult):
+    """The values of M^1/2 H M^1/2 for a CSR H over distinct determinants and
+    their multiplicities M."""
+    w = np.sqrt(np.asarray(mult, dtype=np.float64))
+    rows = np.repeat(np.arange(len(rowptr) - 1), np.diff(rowptr))
+    return values * w[rows] * w[np.asarray(colind)]
+
+
+def repeated_list_solution(E, y, inverse, mult):
+    """The lowest eigenpair of a repeated list's matrix H' = P H P^T from the
+    lowest eigenpair (E, y) of M^1/2 H M^1/2: (E, C = P M^-1/2 y) when E <= 0,
+    else (0, the difference of the first repeated pair over sqrt 2); with
+    c = P^T C = M^1/2 y (zero for the latter), the sum of C over the copies of
+    each distinct determinant.  Returns (E', C, c)."""
+    mult = np.asarray(mult)
+    if E > 0.0:
+        k = int(np.flatnonzero(mult[inverse] > 1)[0])
+        pair = np.flatnonzero(inverse == inverse[k])[:2]
+        C = np.zeros(len(inverse))
+        C[pair] = np.array([1.0, -1.0]) / np.sqrt(2.0)
+        return 0.0, C, np.zeros(len(mult))
+    w = np.sqrt(mult.astype(np.float64))
+    return E, y[inverse] / w[inverse], y * w
+
+
+def add_repeated_pair_terms(rdms, norb, alpha_u, beta_u, C, c, inverse):
+    """form_rdms over a list with repeats (sorted_double_loop.hpp:560-620)
+    visits each unordered pair of list positions once: two copies k < l of a
+    determinant add its diagonal contribution (rdms.hpp:439-516) once with
+    C_k C_l, where a pair of different determinants adds both orderings.  The
+    result is the RDMs of c = P^T C plus, for each distinct determinant u,
+    delta_u = (sum_{k in u} C_k^2 - c_u^2) / 2 times the RDMs of u alone
+    (gamma = diag(n), Gamma_ppqq = n_p n_q / 2, minus n_p n_q / 2 at pqqp
+    within a spin).  Adds that second part to the blocks present in rdms."""
+    s_u = np.bincount(inverse, weights=np.asarray(C) ** 2, minlength=len(c))
+    delta = 0.5 * (s_u - np.asarray(c) ** 2)
+    keep = np.abs(delta) > 0.0
+    if not np.any(keep):
+        return
+    bits = np.arange(norb, dtype=np.uint64)
+    na = ((alpha_u[keep][:, None] >> bits) & np.uint64(1)).astype(np.float64)
+    nb = ((beta_u[keep][:, None] >> bits) & np.uint64(1)).astype(np.float64)
+    d = delta[keep]
+    i = np.arange(norb)
+    P, Q = i[:, None], i[None, :]
+    if "aa" in rdms:
+        rdms["aa"][i, i] += d @ na
+    if "bb" in rdms:
+        rdms["bb"][i, i] += d @ nb
+    for key, occ in (("aaaa", na), ("bbbb", nb)):
+        if key in rdms:
+            M = 0.5 * (occ.T * d) @ occ
+            rdms[key][P, P, Q, Q] += M
+            rdms[key][P, Q, Q, P] -= M
+    if "aabb" in rdms:
+        rdms["aabb"][P, P, Q, Q] += 0.5 * (nb.T * d) @ na
+
+
 class Gb300Pmc(ProjectedMultiConfigurationCalculator):
     """MacisPmc (macis_pmc.cpp:42-178): H build and Davidson on the given
     configurations, in their order (canonical strings '2', 'u', 'd', '0' per
     orbital, or (alpha, beta) bit-string pairs); one determinant gives <D|H|D>.
     The list is solved in spin order and the coefficients come back in the
-    caller's order (the eigenpair does not depend on the order).
+    caller's order (the eigenpair does not depend on the order).  A list that
+    repeats determinants gets the reference's answer for the list as given
+    (see ``_run_repeated``).
     With calculate_one_rdm / calculate_two_rdm the wavefunction carries the
     RDMs (the reference forms the spin-traced ones, macis_pmc.cpp:126-161; here
     the spin-resolved blocks are kept and the traced views derive from them)."""
@@ -471,6 +551,9 @@ class Gb300Pmc(ProjectedMultiConfigurationCalculator):
         if n > 64:
             raise ValueError("at most 64 active orbitals per spin")
         a, b = self._parse(configurations, n)
+        ua, ub, inverse, mult = collapse_repeated(a, b)
+        if len(ua) < len(a):
+            return self._run_repeated(hamiltonian, a, b, ua, ub, inverse, mult)
         with capi.Context(self._settings.get("device")) as ctx:
             ctx.set_integrals(hamiltonian.get_one_body_integrals(), hamiltonian.get_two_body_integrals())
             if len(a) == 1:
@@ -493,6 +576,48 @@ class Gb300Pmc(ProjectedMultiConfigurationCalculator):
             wfn = Wavefunction(n, a, b, C, ws._rdms, ws._ent)
             wfn.info = ws.info
             return E, wfn
+
+    def _run_repeated(self, hamiltonian, a, b, ua, ub, inverse, mult):
+        """A list that names some determinant more than once.  MacisPmc solves
+        the matrix of the list as given (macis_pmc.cpp:93-116), in which two
+        copies of a determinant couple by its diagonal element
+        (sorted_double_loop.hpp:296-323): H' = P H P^T, P mapping each list
+        position to its distinct determinant.  The eigenpairs of H' with a
+        nonzero eigenvalue are those of A = M^1/2 H M^1/2 (M: the
+        multiplicities), mapped back as C = P M^-1/2 y; the others have
+        eigenvalue 0.  A is solved on the device (H build on the distinct
+        determinants in spin order, multiplicity scaling, Davidson in FP64); if
+        its lowest eigenvalue is positive the lowest of H' is 0, with the
+        difference of the first repeated pair as the vector.  The RDMs of C
+        over the list (form_rdms, macis_pmc.cpp:126-161) are formed on the
+        device for c = P^T C = M^1/2 y over the distinct determinants, plus the
+        once-counted pairs of copies (add_repeated_pair_terms); entropies are
+        formed from the state c / |c|."""
+        s = self._settings
+        n = hamiltonian.norb
+        with capi.Context(s.get("device")) as ctx:
+            ctx.set_integrals(hamiltonian.get_one_body_integrals(), hamiltonian.get_two_body_integrals())
+            ctx.set_dets(ua, ub)
+            ctx.build_hamiltonian(s.get("ci_matel_tol"), capi.H_FP64)
+            info = None
+            if len(ua) == 1:
+                E, y = float(ctx.diagonal()[0]) * float(mult[0]), np.ones(1)
+            else:
+                rp, ci, nz = ctx.get_csr()
+                ctx.set_csr(rp, ci, multiplicity_scaled(rp, ci, nz, mult))
+                tol, max_m = self._davidson_limits(len(ua))
+                E, y, info = ctx.davidson(max_m=max_m, tol=tol, precision=capi.PREC_FP64)
+            E, C, c = repeated_list_solution(E, y, inverse, mult)
+            want = self._rdm_blocks()
+            rdms = None
+            if want:
+                rdms = ctx.rdms_spin_dep(c, want=want)
+                add_repeated_pair_terms(rdms, n, ua, ub, C, c, inverse)
+            nc = float(np.linalg.norm(c))
+            ent = self._entropies(ctx, c / nc) if nc > 0.0 else None
+        wfn = Wavefunction(n, a, b, C, rdms, ent)
+        wfn.info = info
+        return E + hamiltonian.get_core_energy(), wfn
 
     def _rdm_blocks(self):
         s = self._settings

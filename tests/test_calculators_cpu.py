@@ -109,3 +109,62 @@ def test_asci_pt2_settings(pkg):
     assert s.get("constraint_level") == 2 and s.get("pair_size_max") == 500000000
     with pytest.raises(ValueError):
         s.set("pt2_tol", 2.0)
+
+
+def test_pmc_repeated_list_math(pkg, oracle, n2_6e6o):
+    """A PMC list that repeats determinants (test_pmc.py:104-141 passes one):
+    the host steps of Gb300Pmc._run_repeated with the oracle standing in for
+    the device.  The lowest eigenpair of M^1/2 H M^1/2 over the distinct
+    determinants, mapped back, is the lowest eigenpair of the matrix the oracle
+    (MACIS's double loop) builds for the list as given; the RDMs of the
+    per-determinant sums c equal the oracle's RDMs of C over the list; a
+    positive lowest eigenvalue gives 0 with a null vector of H'."""
+    import scipy.sparse as sp
+    calc, det = pkg.calculators, pkg.determinants
+    a, b = det.fci_space(6, 3, 3)
+    rng = np.random.default_rng(5)
+    sel = rng.choice(len(a), 30, replace=False)
+    lst = np.concatenate([sel, sel[[3, 7, 7, 12]]])
+    rng.shuffle(lst)
+    la, lb = a[lst], b[lst]
+    ua, ub, inv, mult = calc.collapse_repeated(la, lb)
+    assert len(ua) == 30 and mult.sum() == len(la) and sorted(mult.tolist())[-3:] == [2, 2, 3]
+    assert np.array_equal(ua[inv], la) and np.array_equal(ub[inv], lb)
+    assert np.array_equal(np.lexsort((ub, ua)), np.arange(30))
+    H = oracle.Hamiltonian(n2_6e6o["T"], n2_6e6o["V"])
+    rp, ci, nz = oracle.build_csr(H, ua, ub).arrays()
+    A = sp.csr_matrix((calc.multiplicity_scaled(rp, ci, nz, mult), ci, rp), shape=(30, 30)).toarray()
+    w, Y = np.linalg.eigh(A)
+    E, C, c = calc.repeated_list_solution(w[0], Y[:, 0], inv, mult)
+    rp2, ci2, nz2 = oracle.build_csr(H, la, lb).arrays()
+    Hp = sp.csr_matrix((nz2, ci2, rp2), shape=(len(la),) * 2).toarray()
+    w2, X = np.linalg.eigh(Hp)
+    assert E == w[0] and abs(E - w2[0]) < 1e-12
+    assert abs(C @ C - 1.0) < 1e-12 and abs(abs(C @ X[:, 0]) - 1.0) < 1e-10
+    R1 = oracle.rdms_spin_dep(6, la, lb, C)
+    R2 = oracle.rdms_spin_dep(6, ua, ub, c)
+    assert np.abs(R1["aa"] - R2["aa"]).max() > 1e-3  # the once-counted copies
+    calc.add_repeated_pair_terms(R2, 6, ua, ub, C, c, inv)
+    for k in R1:
+        assert np.abs(R1[k] - R2[k]).max() < 1e-12, k
+    # any vector over the list, not only the eigenvector: C arbitrary, c = P^T C
+    Cr = rng.standard_normal(len(la))
+    cr = np.bincount(inv, weights=Cr)
+    R1 = oracle.rdms_spin_dep(6, la, lb, Cr)
+    R2 = oracle.rdms_spin_dep(6, ua, ub, cr)
+    calc.add_repeated_pair_terms(R2, 6, ua, ub, Cr, cr, inv)
+    for k in R1:
+        assert np.abs(R1[k] - R2[k]).max() < 1e-12, k
+    # one determinant twice: H' = h J, lowest eigenvalue 2h (h < 0) or 0 (h > 0)
+    u1a, u1b, inv1, m1 = calc.collapse_repeated(la[[0, 0]], lb[[0, 0]])
+    h = H.matrix_element((int(la[0]), int(lb[0])), (int(la[0]), int(lb[0])))
+    E1, C1, _ = calc.repeated_list_solution(h * m1[0], np.ones(1), inv1, m1)
+    assert E1 == 2 * h and np.allclose(C1, [2 ** -0.5] * 2)
+    E0, C0, c0 = calc.repeated_list_solution(0.5, Y[:, 0], inv, mult)
+    assert E0 == 0.0 and not np.any(c0) and abs(C0 @ C0 - 1.0) < 1e-15
+    assert np.abs(Hp @ C0).max() < 1e-12
+    R1 = oracle.rdms_spin_dep(6, la, lb, C0)
+    R2 = oracle.rdms_spin_dep(6, ua, ub, c0)
+    calc.add_repeated_pair_terms(R2, 6, ua, ub, C0, c0, inv)
+    for k in R1:
+        assert np.abs(R1[k] - R2[k]).max() < 1e-12, k

@@ -90,3 +90,52 @@ def test_pmc_matches_oracle(pkg, oracle, n2_6e6o):
     E1, w1 = calc.create("projected_multi_configuration_calculator").run(ham, cfgs[:1])
     assert abs(E1 - (Ho.matrix_element((a[sel[0]], b[sel[0]]), (a[sel[0]], b[sel[0]])) + n2_6e6o["E_core"])) < 1e-12
     assert w1.coefficients.tolist() == [1.0]
+
+
+def test_pmc_repeated_configurations(pkg, oracle, n2_6e6o):
+    """A configuration list that repeats determinants (test_pmc.py:104-141
+    passes "222000" twice): the energy and vector are the lowest eigenpair of
+    the matrix MACIS builds for the list as given (the oracle's double loop,
+    dense here) and the RDMs are the oracle's form_rdms over the list with the
+    returned coefficients; one determinant given twice has 2 <D|H|D>."""
+    import scipy.sparse as sp
+    calc, det = pkg.calculators, pkg.determinants
+    a, b = det.fci_space(6, 3, 3)
+    rng = np.random.default_rng(11)
+    sel = rng.choice(len(a), 20, replace=False)
+    lst = np.concatenate([sel, sel[[2, 5, 5]]])
+    rng.shuffle(lst)
+    cfgs = [det.to_canonical_string(a[i], b[i], 6) for i in lst]
+    ham = calc.Hamiltonian(n2_6e6o["T"], n2_6e6o["V"], n2_6e6o["E_core"])
+    H = oracle.Hamiltonian(n2_6e6o["T"], n2_6e6o["V"])
+    E_core = n2_6e6o["E_core"]
+
+    def dense(la, lb):
+        rp, ci, nz = oracle.build_csr(H, la, lb).arrays()
+        return sp.csr_matrix((nz, ci, rp), shape=(len(la),) * 2).toarray()
+
+    p = calc.create("projected_multi_configuration_calculator")
+    p.settings().set("calculate_one_rdm", True)
+    p.settings().set("calculate_two_rdm", True)
+    E, wfn = p.run(ham, cfgs)
+    w, X = np.linalg.eigh(dense(a[lst], b[lst]))
+    assert wfn.size() == len(cfgs) and wfn.get_configurations() == cfgs
+    assert abs(E - (w[0] + E_core)) < 1e-10
+    assert abs(abs(wfn.coefficients @ X[:, 0]) - 1.0) < 1e-8
+    Ro = oracle.rdms_spin_dep(6, a[lst], b[lst], wfn.coefficients)
+    aa, bb = wfn.get_active_one_rdm_spin_dependent()
+    aabb, aaaa, bbbb = wfn.get_active_two_rdm_spin_dependent()
+    np.testing.assert_allclose(aa, Ro["aa"], atol=1e-10, rtol=0)
+    np.testing.assert_allclose(bb, Ro["bb"], atol=1e-10, rtol=0)
+    for got, key in ((aabb, "aabb"), (aaaa, "aaaa"), (bbbb, "bbbb")):
+        np.testing.assert_allclose(got, 2.0 * Ro[key].ravel(order="F"), atol=1e-10, rtol=0)
+    # the reference's three-configuration case, on this active space
+    three = ["222000", "22ud00", "222000"]
+    E3, w3 = calc.create("projected_multi_configuration_calculator").run(ham, three)
+    a3 = np.array([det.from_canonical_string(s)[0] for s in three], np.uint64)
+    b3 = np.array([det.from_canonical_string(s)[1] for s in three], np.uint64)
+    hf = H.matrix_element((7, 7), (7, 7))
+    assert w3.size() == 3 and E3 < hf + E_core
+    assert abs(E3 - (np.linalg.eigvalsh(dense(a3, b3))[0] + E_core)) < 1e-10
+    E2, w2 = calc.create("projected_multi_configuration_calculator").run(ham, ["222000", "222000"])
+    assert abs(E2 - (2 * hf + E_core)) < 1e-10 and w2.size() == 2
