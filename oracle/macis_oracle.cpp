@@ -1994,6 +1994,16 @@ void* orc_csr_build(void* h, const uint64_t* alpha, const uint64_t* beta, int64_
   if (guard([&] { M = build_csr_sdl(*(Ham*)h, alpha, beta, nd, thresh); })) return nullptr;
   return M;
 }
+// a caller's CSR matrix (0-based), as davidson_solver receives it
+// (python/src/pybind11/algorithms/davidson_solver.cpp:60-64)
+void* orc_csr_from_arrays(int64_t n, const int64_t* rowptr, const int64_t* colind, const double* nzval) {
+  Csr* M = new Csr;
+  M->n = n;
+  M->rowptr.assign(rowptr, rowptr + n + 1);
+  M->colind.assign(colind, colind + rowptr[n]);
+  M->nzval.assign(nzval, nzval + rowptr[n]);
+  return M;
+}
 int64_t orc_csr_nnz(void* m) { return (int64_t)((Csr*)m)->colind.size(); }
 void orc_csr_copy(void* m, int64_t* rowptr, int64_t* colind, double* nzval) {
   Csr* M = (Csr*)m;

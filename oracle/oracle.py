@@ -47,6 +47,8 @@ def lib():
         L.orc_matrix_element.argtypes = [vp, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64]
         L.orc_csr_build.restype = vp
         L.orc_csr_build.argtypes = [vp, _u64p, _u64p, i64, f64]
+        L.orc_csr_from_arrays.restype = vp
+        L.orc_csr_from_arrays.argtypes = [i64, _i64p, _i64p, _f64p]
         L.orc_csr_nnz.restype = i64
         L.orc_csr_nnz.argtypes = [vp]
         L.orc_csr_copy.argtypes = [vp, _i64p, _i64p, _f64p]
@@ -176,6 +178,16 @@ class Csr:
         if rc != 0:
             raise RuntimeError(lib().orc_last_error().decode())
         return E.value, X, it.value
+
+
+def csr_from_arrays(rowptr, colind, values):
+    """A caller's CSR matrix as an oracle operator (davidson_solver.cpp:60-64);
+    its selected_ci_diag() is davidson_solver's diagonal guess + davidson."""
+    rp = np.ascontiguousarray(rowptr, dtype=np.int64)
+    ci = np.ascontiguousarray(colind, dtype=np.int64)
+    nz = np.ascontiguousarray(values, dtype=np.float64)
+    n = len(rp) - 1
+    return Csr(lib().orc_csr_from_arrays(n, rp, ci, nz), n)
 
 
 def build_csr(ham, alpha, beta, thresh=np.finfo(np.float64).eps):

@@ -67,3 +67,16 @@ def n2_6e6o():
 @pytest.fixture(scope="session")
 def n2_14e18o():
     return load_fcidump("n2_14e18o")
+
+
+def davidson_solver_cases():
+    """The two analytic cases of python/tests/test_davidson_solver.py:17-71 as
+    (name, CSR matrix, lowest eigenvalue, its eigenvector): the 6 x 6
+    tridiagonal (2 on the diagonal, -1 beside it; 2 - 2 cos(pi/7), v_i =
+    sin(i pi/7)) and the two-site Heisenberg XX + YY + ZZ (-3, the singlet)."""
+    import scipy.sparse as sp
+    tri = 2.0 * np.eye(6) - np.eye(6, k=1) - np.eye(6, k=-1)
+    v = np.sin(np.arange(1, 7) * np.pi / 7)
+    heis = np.array([[1.0, 0, 0, 0], [0, -1, 2, 0], [0, 2, -1, 0], [0, 0, 0, 1]])
+    return [("tridiagonal6", sp.csr_matrix(tri), 2 - 2 * np.cos(np.pi / 7), v / np.linalg.norm(v)),
+            ("heisenberg2", sp.csr_matrix(heis), -3.0, np.array([0.0, 1.0, -1.0, 0.0]) / np.sqrt(2))]

@@ -60,6 +60,17 @@ def test_davidson_solver_on_scipy_csr(pkg, oracle, h2o, known):
     assert abs(X @ (A @ X) - E) < 1e-10
 
 
+def test_davidson_solver_reference_cases(pkg):
+    """python/tests/test_davidson_solver.py:17-71 on the GPU: davidson_solver
+    with its defaults (tol 1e-8, max_m 20) on the 6 x 6 tridiagonal and the
+    two-site Heisenberg model, to the reference's 1e-12."""
+    from conftest import davidson_solver_cases
+    for name, A, E_ref, v_ref in davidson_solver_cases():
+        E, X = pkg.calculators.davidson_solver(A)
+        assert abs(E - E_ref) < 1e-12 + 1e-12 * abs(E_ref), name
+        assert X.shape == v_ref.shape and abs(abs(X @ v_ref) - 1.0) < 1e-12, name
+
+
 def test_autograd_rdm_gradients_match_finite_differences(pkg):
     """dE/dh1 = 1-RDM and dE/dV = 2-RDM against central differences (step 1e-5)
     on 20 seeded integral entries, each perturbed over its whole symmetry orbit."""

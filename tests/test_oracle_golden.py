@@ -283,3 +283,17 @@ def test_hf_rdm_structure_34_orbitals(oracle, na, nb):
                 Gref[i, k, k, i] = -0.5 * (oa[i] * oa[k] + ob[i] * ob[k])
     assert np.abs(G - Gref).max() < 1e-14
     assert np.abs(g - np.diag(occ)).max() < 1e-14
+
+
+def test_davidson_solver_reference_cases(oracle):
+    """python/tests/test_davidson_solver.py:17-71: davidson_solver (diagonal
+    guess + davidson, tol 1e-8, max_m 20) on a 6 x 6 tridiagonal and the
+    two-site Heisenberg model; eigenvalue and |overlap| with the analytic
+    eigenvector to the reference's 1e-12."""
+    from conftest import davidson_solver_cases
+    for name, A, E_ref, v_ref in davidson_solver_cases():
+        A.sort_indices()
+        M = oracle.csr_from_arrays(A.indptr, A.indices, A.data)
+        E, X, _ = M.selected_ci_diag(max_m=20, tol=1e-8)
+        assert abs(E - E_ref) < 1e-12 + 1e-12 * abs(E_ref), name
+        assert X.shape == v_ref.shape and abs(abs(X @ v_ref) - 1.0) < 1e-12, name
