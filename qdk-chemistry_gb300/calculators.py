@@ -316,6 +316,21 @@ class Gb300Cas(MultiConfigurationCalculator):
             return self._solve(ctx, hamiltonian, a, b)
 
 
+def check_growth_settings(grow_factor, min_grow_factor, backoff_rate, recovery_rate):
+    """The growth settings as get_asci_settings_ checks them before any work
+    (cpp/src/qdk/chemistry/algorithms/microsoft/macis_base.cpp:101-124)."""
+    if not grow_factor > 1.0:
+        raise RuntimeError("grow_factor must be > 1.0, got %f" % grow_factor)
+    if not min_grow_factor > 1.0:
+        raise RuntimeError("min_grow_factor must be > 1.0, got %f" % min_grow_factor)
+    if min_grow_factor > grow_factor:
+        raise RuntimeError("min_grow_factor must be <= grow_factor")
+    if not 0.0 < backoff_rate < 1.0:
+        raise RuntimeError("growth_backoff_rate must be in (0, 1), got %f" % backoff_rate)
+    if not recovery_rate > 1.0:
+        raise RuntimeError("growth_recovery_rate must be > 1.0, got %f" % recovery_rate)
+
+
 class Gb300AsciSettings(Gb300Settings):
     """MacisAsciSettings names and defaults (macis_asci.hpp:36-189, from
     ASCISettings, determinant_search.hpp:95-199)."""
@@ -380,6 +395,11 @@ class Gb300Asci(MultiConfigurationCalculator):
         if strategy not in ("percentage", "fixed"):
             raise ValueError("Invalid core_selection_strategy: '%s'. Valid options are 'fixed' or 'percentage'."
                              % strategy)
+        check_growth_settings(s.get("grow_factor"), s.get("min_grow_factor"), s.get("growth_backoff_rate"),
+                              s.get("growth_recovery_rate"))
+        thr = s.get("core_selection_threshold")
+        if strategy == "percentage" and not (np.finfo(np.float64).eps <= thr <= 1.0):
+            raise ValueError("core_selection_threshold must be in [epsilon, 1.0], got %f" % thr)
         from math import comb
         if s.get("ntdets_max") > comb(n, n_alpha) * comb(n, n_beta):
             return Gb300Cas._run_impl(self, hamiltonian, n_alpha, n_beta)

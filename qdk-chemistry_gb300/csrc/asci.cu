@@ -849,6 +849,14 @@ double asci_iter_gpu(Context* c, const qdkgb_asci_settings& S, const qdkgb_david
 void asci_run(Context* c, const qdkgb_asci_settings& S, const qdkgb_davidson_settings& ci, double matel_tol,
               std::vector<uint64_t>& a, std::vector<uint64_t>& b, std::vector<double>& X, double& E0, bool grow,
               bool refine, double* E_grow) {
+  // the growth settings as get_asci_settings_ checks them
+  // (cpp/src/qdk/chemistry/algorithms/microsoft/macis_base.cpp:101-124)
+  if (!(S.grow_factor > 1.0)) throw Error(QDKGB_ERR_INVALID, "grow_factor must be > 1.0");
+  if (!(S.min_grow_factor > 1.0)) throw Error(QDKGB_ERR_INVALID, "min_grow_factor must be > 1.0");
+  if (S.min_grow_factor > S.grow_factor) throw Error(QDKGB_ERR_INVALID, "min_grow_factor must be <= grow_factor");
+  if (!(S.growth_backoff_rate > 0.0 && S.growth_backoff_rate < 1.0))
+    throw Error(QDKGB_ERR_INVALID, "growth_backoff_rate must be in (0, 1)");
+  if (!(S.growth_recovery_rate > 1.0)) throw Error(QDKGB_ERR_INVALID, "growth_recovery_rate must be > 1.0");
   std::vector<HDet> wfn(a.size());
   for (size_t i = 0; i < a.size(); ++i) wfn[i] = {a[i], b[i]};
   int64_t ncand = 0;

@@ -168,3 +168,38 @@ def test_pmc_repeated_list_math(pkg, oracle, n2_6e6o):
     calc.add_repeated_pair_terms(R2, 6, ua, ub, C0, c0, inv)
     for k in R1:
         assert np.abs(R1[k] - R2[k]).max() < 1e-12, k
+
+
+@pytest.mark.parametrize("key,value,match", [
+    ("grow_factor", 1.0, "grow_factor must be > 1.0"),
+    ("min_grow_factor", 1.0, "min_grow_factor must be > 1.0"),
+    ("min_grow_factor", 9.0, "min_grow_factor must be <= grow_factor"),
+    ("growth_backoff_rate", 1.0, "growth_backoff_rate must be in"),
+    ("growth_backoff_rate", 0.0, "growth_backoff_rate must be in"),
+    ("growth_recovery_rate", 1.0, "growth_recovery_rate must be > 1.0"),
+])
+def test_asci_growth_settings_are_checked(pkg, key, value, match):
+    """get_asci_settings_ (macis_base.cpp:101-124; test_macis.cpp:1460-1473
+    for grow_factor = 1): invalid growth settings raise before any device
+    work."""
+    calc = pkg.calculators
+    c = calc.create("multi_configuration_calculator", "gb300_asci")
+    c.settings().set(key, value)
+    H = calc.Hamiltonian(np.eye(6), np.zeros(6 ** 4))
+    with pytest.raises(RuntimeError, match=match):
+        c.run(H, 3, 3)
+
+
+def test_asci_core_threshold_is_checked(pkg):
+    calc = pkg.calculators
+    c = calc.create("multi_configuration_calculator", "gb300_asci")
+    c.settings().set("core_selection_threshold", 0.0)
+    H = calc.Hamiltonian(np.eye(6), np.zeros(6 ** 4))
+    with pytest.raises(ValueError, match="core_selection_threshold"):
+        c.run(H, 3, 3)
+    c2 = calc.create("multi_configuration_calculator", "gb300_asci")
+    c2.settings().set("core_selection_threshold", 0.0)
+    c2.settings().set("core_selection_strategy", "fixed")
+    c2.settings().set("grow_factor", 1.0)  # reaches the growth check: the threshold is not read
+    with pytest.raises(RuntimeError, match="grow_factor"):
+        c2.run(H, 3, 3)
