@@ -141,6 +141,20 @@ class Hamiltonian:
         return self._ecore
 
 
+def single_orbital_entropies(occ_alpha, occ_beta, double_occ):
+    """-sum w ln w over the one-orbital RDM eigenvalues (empty, alpha only,
+    beta only, double: 1 - na - nb + d, na - d, nb - d, d), zero weights
+    skipped (orbital_entropy.hpp:24-37, Boguslawski & Tecmer 2015)."""
+    na = np.asarray(occ_alpha, dtype=np.float64)
+    nb = np.asarray(occ_beta, dtype=np.float64)
+    d = np.asarray(double_occ, dtype=np.float64)
+    out = np.zeros(na.shape)
+    for w in (1.0 - na - nb + d, na - d, nb - d, d):
+        pos = w > 0.0
+        out[pos] -= w[pos] * np.log(w[pos])
+    return out
+
+
 class Wavefunction:
     """Determinants + CI coefficients (+ optional RDMs), the StateVectorContainer
     the reference builds (macis_base.hpp:134-283).  The spin-resolved two-body
@@ -151,8 +165,8 @@ class Wavefunction:
         self.alpha = np.asarray(alpha, dtype=np.uint64)
         self.beta = np.asarray(beta, dtype=np.uint64)
         self.coefficients = np.asarray(coeffs, dtype=np.float64)
-        self._rdms = rdms or {}
-        self._ent = entropies or {}
+        self._rdms = dict(rdms or {})
+        self._ent = dict(entropies or {})
 
     def size(self):
         return len(self.coefficients)
@@ -182,29 +196,56 @@ class Wavefunction:
         f = lambda t: 2.0 * t.ravel(order="F")
         return f(self._rdms["aabb"]), f(self._rdms["aaaa"]), f(self._rdms["bbbb"])
 
+    # Entropies follow WavefunctionContainer (cpp/src/qdk/chemistry/data/
+    # wavefunction.cpp:556-685): stored values first; otherwise single-orbital
+    # entropies come from the spin-dependent 1- and 2-RDMs, and two-orbital
+    # entropies and mutual information from each other with s1.
     def has_single_orbital_entropies(self):
-        return "s1" in self._ent
+        return "s1" in self._ent or (self.has_one_rdm() and self.has_two_rdm())
 
     def has_two_orbital_entropies(self):
-        return "s2" in self._ent
+        return "s2" in self._ent or ("mi" in self._ent and self.has_single_orbital_entropies())
 
     def has_mutual_information(self):
-        return "mi" in self._ent
+        return "mi" in self._ent or ("s2" in self._ent and self.has_single_orbital_entropies())
 
     def get_single_orbital_entropies(self):
-        if "s1" not in self._ent:
-            raise RuntimeError("single-orbital entropies were not requested (calculate_single_orbital_entropies)")
-        return self._ent["s1"]
+        if "s1" in self._ent:
+            return self._ent["s1"]
+        if not (self.has_one_rdm() and self.has_two_rdm()):
+            raise RuntimeError("Spin-dependent one- and two-body RDMs must be set to evaluate "
+                               "single-orbital entropies")
+        i = np.arange(self.norb)
+        # the qdk-normalised aabb element (ii|ii) is <n_ia n_ib> (twice the
+        # stored half-convention block)
+        s1 = single_orbital_entropies(self._rdms["aa"][i, i], self._rdms["bb"][i, i],
+                                      2.0 * self._rdms["aabb"][i, i, i, i])
+        self._ent["s1"] = s1
+        return s1
 
     def get_two_orbital_entropies(self):
-        if "s2" not in self._ent:
-            raise RuntimeError("two-orbital entropies were not requested (calculate_two_orbital_entropies)")
-        return self._ent["s2"]
+        if "s2" in self._ent:
+            return self._ent["s2"]
+        if "mi" in self._ent and self.has_single_orbital_entropies():
+            s1 = self.get_single_orbital_entropies()
+            s2 = s1[:, None] + s1[None, :] - self._ent["mi"]
+            np.fill_diagonal(s2, 0.0)
+            self._ent["s2"] = s2
+            return s2
+        raise RuntimeError("Two-orbital entropies are not available. Provide them at construction time, or "
+                           "provide both single-orbital entropies (or RDMs) and mutual information.")
 
     def get_mutual_information(self):
-        if "mi" not in self._ent:
-            raise RuntimeError("mutual information was not requested (calculate_mutual_information)")
-        return self._ent["mi"]
+        if "mi" in self._ent:
+            return self._ent["mi"]
+        if "s2" in self._ent and self.has_single_orbital_entropies():
+            s1 = self.get_single_orbital_entropies()
+            mi = s1[:, None] + s1[None, :] - self._ent["s2"]
+            np.fill_diagonal(mi, 0.0)
+            self._ent["mi"] = mi
+            return mi
+        raise RuntimeError("Mutual information is not available. Provide it at construction time, or provide "
+                           "both single-orbital entropies (or RDMs) and two-orbital entropies.")
 
     def get_active_two_rdm_spin_traced(self):
         """MACIS spin-traced 2-RDM (E = T.g + V.G): aaaa + bbbb + aabb + aabb^T(rs,pq)."""

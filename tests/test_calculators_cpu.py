@@ -203,3 +203,49 @@ def test_asci_core_threshold_is_checked(pkg):
     c2.settings().set("grow_factor", 1.0)  # reaches the growth check: the threshold is not read
     with pytest.raises(RuntimeError, match="grow_factor"):
         c2.run(H, 3, 3)
+
+
+def test_wavefunction_entropies_from_rdms(pkg, oracle, n2_6e6o):
+    """WavefunctionContainer entropy semantics (wavefunction.cpp:556-685):
+    with only spin-dependent RDMs, single-orbital entropies come from
+    gamma_aa(ii), gamma_bb(ii) and the aabb (ii|ii) element
+    (orbital_entropy.hpp:24-37) and equal form_entropies' (the oracle's
+    restatement); two-orbital entropies and mutual information follow from
+    each other with s1 (off the diagonal; zero on it)."""
+    calc, det = pkg.calculators, pkg.determinants
+    a, b = det.spin_sort(*det.fci_space(6, 3, 3))
+    H = oracle.Hamiltonian(n2_6e6o["T"], n2_6e6o["V"])
+    _, X, _ = oracle.build_csr(H, a, b).selected_ci_diag(tol=1e-10)
+    s1o, s2o, mio = oracle.entropies(6, a, b, X)
+    R = oracle.rdms_spin_dep(6, a, b, X)
+    off = ~np.eye(6, dtype=bool)
+    w = calc.Wavefunction(6, a, b, X, R)
+    assert w.has_single_orbital_entropies()
+    assert not w.has_two_orbital_entropies() and not w.has_mutual_information()
+    np.testing.assert_allclose(w.get_single_orbital_entropies(), s1o, atol=1e-12, rtol=0)
+    with pytest.raises(RuntimeError, match="Two-orbital entropies are not available"):
+        w.get_two_orbital_entropies()
+    with pytest.raises(RuntimeError, match="Mutual information is not available"):
+        w.get_mutual_information()
+    w2 = calc.Wavefunction(6, a, b, X, R, {"mi": mio})
+    assert w2.has_two_orbital_entropies()
+    s2 = w2.get_two_orbital_entropies()
+    np.testing.assert_allclose(s2[off], s2o[off], atol=1e-12, rtol=0)
+    assert not np.any(np.diag(s2))
+    w3 = calc.Wavefunction(6, a, b, X, {k: R[k] for k in ("aa", "bb")}, {"s2": s2o})
+    assert not w3.has_single_orbital_entropies() and not w3.has_mutual_information()
+    with pytest.raises(RuntimeError, match="Spin-dependent one- and two-body RDMs"):
+        w3.get_single_orbital_entropies()
+    w4 = calc.Wavefunction(6, a, b, X, None, {"s1": s1o, "s2": s2o})
+    np.testing.assert_allclose(w4.get_mutual_information()[off], mio[off], atol=1e-12, rtol=0)
+    # a selected space over 12 orbitals with a random vector
+    T, V, _ = pkg.integrals.synthetic_integrals(12, 16, 2)
+    rng = np.random.default_rng(1)
+    sa, sb = det.fci_space(12, 3, 2)
+    keep = np.sort(rng.choice(len(sa), 400, replace=False))
+    sa, sb = det.spin_sort(sa[keep], sb[keep])
+    C = rng.standard_normal(len(sa))
+    C /= np.linalg.norm(C)
+    s1r, _, _ = oracle.entropies(12, sa, sb, C)
+    wr = calc.Wavefunction(12, sa, sb, C, oracle.rdms_spin_dep(12, sa, sb, C))
+    np.testing.assert_allclose(wr.get_single_orbital_entropies(), s1r, atol=1e-12, rtol=0)
