@@ -160,8 +160,15 @@ class Wavefunction:
     the reference builds (macis_base.hpp:134-283).  The spin-resolved two-body
     RDMs carry the reference's factor 2 (macis_base.hpp:203-212)."""
 
-    def __init__(self, norb, alpha, beta, coeffs, rdms=None, entropies=None):
+    def __init__(self, norb, alpha, beta, coeffs, rdms=None, entropies=None, active_indices=None,
+                 inactive_indices=None):
         self.norb = norb
+        # the molecular-orbital indices of the active orbitals (0 .. norb-1
+        # unless given) and of the doubly occupied inactive ones
+        self.active_indices = list(range(norb)) if active_indices is None else [int(i) for i in active_indices]
+        self.inactive_indices = [] if inactive_indices is None else [int(i) for i in inactive_indices]
+        if len(self.active_indices) != norb:
+            raise ValueError("active_indices must name norb orbitals")
         self.alpha = np.asarray(alpha, dtype=np.uint64)
         self.beta = np.asarray(beta, dtype=np.uint64)
         self.coefficients = np.asarray(coeffs, dtype=np.float64)
@@ -170,6 +177,19 @@ class Wavefunction:
 
     def size(self):
         return len(self.coefficients)
+
+    def get_active_indices(self):
+        return list(self.active_indices)
+
+    def get_inactive_indices(self):
+        return list(self.inactive_indices)
+
+    def get_active_num_electrons(self):
+        return (int(self.alpha[0]).bit_count(), int(self.beta[0]).bit_count()) if len(self.alpha) else (0, 0)
+
+    def get_total_num_electrons(self):
+        na, nb = self.get_active_num_electrons()
+        return na + len(self.inactive_indices), nb + len(self.inactive_indices)
 
     def get_configurations(self):
         return [determinants.to_canonical_string(a, b, self.norb) for a, b in zip(self.alpha, self.beta)]
@@ -690,10 +710,167 @@ class Gb300Pmc(ProjectedMultiConfigurationCalculator):
         return tuple(want)
 
 
+class ActiveSpaceSelector:
+    """run(wavefunction) -> Wavefunction over the selected active orbitals
+    (active_space.hpp); Algorithm::run locks the settings first."""
+
+    def __init__(self):
+        self._settings = self._make_settings()
+
+    def settings(self):
+        return self._settings
+
+    def type_name(self):
+        return "active_space_selector"
+
+    def run(self, wavefunction):
+        self._settings.lock()
+        return self._run_impl(wavefunction)
+
+
+class AutocasSettings(Settings):
+    """AutocasActiveSpaceSettings (autocas_active_space.hpp:37-56)."""
+
+    def __init__(self):
+        super().__init__()
+        self.set_default("num_bins", int, 100, "Number of bins for entropy discretization", (2, 2 ** 63 - 1))
+        self.set_default("min_plateau_size", int, 10, "Minimum size of entropy plateau to be considered",
+                         (1, 2 ** 63 - 1))
+        self.set_default("entropy_threshold", float, 0.14,
+                         "Minimum absolute entropy value the plateau has to be above")
+        self.set_default("normalize_entropies", bool, True)
+
+
+class AutocasEosSettings(Settings):
+    """AutocasEosActiveSpaceSettings (entropy_active_space.hpp:40-46)."""
+
+    def __init__(self):
+        super().__init__()
+        self.set_default("normalize_entropies", bool, True)
+        self.set_default("diff_threshold", float, 0.1)
+        self.set_default("entropy_threshold", float, 0.14)
+
+
+def sorted_entropies_and_indices(wavefunction, normalize):
+    """_sort_entropies_and_indices (active_space.cpp:46-117): the single-orbital
+    entropies of the wavefunction's active orbitals in descending order with
+    their orbital indices, normalised by the largest when asked (and that
+    largest is above machine epsilon).  Returns (max entropy, indices,
+    sorted entropies)."""
+    if not wavefunction.has_single_orbital_entropies():
+        raise RuntimeError("Wavefunction does not have single orbital entropies.")
+    s1 = np.asarray(wavefunction.get_single_orbital_entropies(), dtype=np.float64)
+    idx = wavefunction.get_active_indices()
+    if len(s1) != len(idx):
+        raise RuntimeError("Entropy size does not match number of active space orbitals.")
+    order = np.argsort(-s1, kind="stable")
+    ent = s1[order]
+    indices = [idx[i] for i in order]
+    mx = float(ent.max()) if len(ent) else 0.0
+    if normalize and mx > np.finfo(np.float64).eps:
+        ent = ent / mx
+    return mx, indices, ent
+
+
+def selected_active_wavefunction(wavefunction, selected):
+    """new_orbitals + new_wavefunction (active_space.cpp:119-376) for a
+    restricted wavefunction: the selected orbitals (sorted) must lie in its
+    active space; the result holds one determinant over them, that of a
+    one-determinant wavefunction or else the aufbau determinant of the active
+    electrons, with the occupations of the selected orbitals
+    (_extract_active_orbitals :281-321); the inactive orbitals are the lowest
+    nelec/2 not selected (_get_inactive_space_indices :220-239)."""
+    selected = sorted(int(i) for i in selected)
+    old = wavefunction.get_active_indices()
+    for i in selected:
+        if i not in old:
+            raise RuntimeError("Selected orbital (index: %d) is outside of initial active space." % i)
+    na, nb = wavefunction.get_active_num_electrons()
+    if wavefunction.size() == 1:
+        da, db = int(wavefunction.alpha[0]), int(wavefunction.beta[0])
+    else:
+        da, db = (1 << na) - 1, (1 << nb) - 1
+    a = b = 0
+    for k, i in enumerate(selected):
+        p = old.index(i)
+        a |= ((da >> p) & 1) << k
+        b |= ((db >> p) & 1) << k
+    ta, tb = wavefunction.get_total_num_electrons()
+    inactive = [i for i in range((ta + tb) // 2) if i not in selected]
+    return Wavefunction(len(selected), np.array([a], np.uint64), np.array([b], np.uint64), np.ones(1),
+                        active_indices=selected, inactive_indices=inactive)
+
+
+class Gb300Autocas(ActiveSpaceSelector):
+    """AutocasActiveSpaceSelector (autocas_active_space.cpp:15-160): bins the
+    (normalised) single-orbital entropies, finds plateaus of equal "orbitals
+    above the bin" counts at least min_plateau_size bins long, and keeps the
+    orbitals counted at the start of the largest one; no orbital is kept when
+    the largest raw entropy is below entropy_threshold."""
+
+    def _make_settings(self):
+        return AutocasSettings()
+
+    def name(self):
+        return "gb300_autocas"
+
+    def select(self, wavefunction):
+        s = self._settings
+        mx, indices, ent = sorted_entropies_and_indices(wavefunction, s.get("normalize_entropies"))
+        if mx < s.get("entropy_threshold"):
+            return []
+        nbins = s.get("num_bins")
+        bins = np.arange(nbins) * (1.0 / nbins)
+        above = [int(np.count_nonzero(ent > t)) for t in bins]
+        plateaus, start = [], 0
+        for i in range(1, nbins):
+            if above[i] != above[i - 1]:
+                if i - start >= s.get("min_plateau_size"):
+                    plateaus.append(start)
+                start = i
+        if nbins - start >= s.get("min_plateau_size"):
+            plateaus.append(start)
+        sizes = [above[p] for p in plateaus if above[p] > 0]
+        return sorted(indices[:max(sizes) if sizes else 0])
+
+    def _run_impl(self, wavefunction):
+        return selected_active_wavefunction(wavefunction, self.select(wavefunction))
+
+
+class Gb300AutocasEos(ActiveSpaceSelector):
+    """AutocasEosActiveSpaceSelector (entropy_active_space.cpp:14-87): keeps
+    the largest k whose k-th sorted (normalised) entropy lies above
+    entropy_threshold (normalised by the largest entropy when asked) and drops
+    to the next one by more than diff_threshold."""
+
+    def _make_settings(self):
+        return AutocasEosSettings()
+
+    def name(self):
+        return "gb300_autocas_eos"
+
+    def select(self, wavefunction):
+        s = self._settings
+        norm = s.get("normalize_entropies")
+        mx, indices, ent = sorted_entropies_and_indices(wavefunction, norm)
+        thr = s.get("entropy_threshold")
+        if norm:
+            with np.errstate(divide="ignore", invalid="ignore"):
+                thr = np.float64(thr) / np.float64(mx)
+        diff = ent[:-1] - ent[1:]
+        sizes = [i + 1 for i in range(len(diff)) if ent[i] > thr and diff[i] > s.get("diff_threshold")]
+        return sorted(indices[:max(sizes) if sizes else 0])
+
+    def _run_impl(self, wavefunction):
+        return selected_active_wavefunction(wavefunction, self.select(wavefunction))
+
+
 _REGISTRY = {"multi_configuration_calculator": {"gb300_cas": Gb300Cas, "gb300_asci": Gb300Asci},
-             "projected_multi_configuration_calculator": {"gb300_pmc": Gb300Pmc}}
+             "projected_multi_configuration_calculator": {"gb300_pmc": Gb300Pmc},
+             "active_space_selector": {"gb300_autocas": Gb300Autocas, "gb300_autocas_eos": Gb300AutocasEos}}
 _DEFAULT = {"multi_configuration_calculator": "gb300_cas",
-            "projected_multi_configuration_calculator": "gb300_pmc"}
+            "projected_multi_configuration_calculator": "gb300_pmc",
+            "active_space_selector": "gb300_autocas"}
 
 
 def register(kind, factory):
