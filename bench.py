@@ -811,8 +811,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-stride", type=int, default=16)
-    ap.add_argument("--fp64-iters", type=int, default=36,
-                    help="reference arm: sigma applications of the FP64 Davidson (measured on the GPU path)")
+    ap.add_argument("--fp64-iters", type=int, default=66,
+                    help="reference arm: sigma applications of the FP64 Davidson at the default workload "
+                         "(66, the count of the GPU FP64 path, which runs the reference's algorithm)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--norb", type=int, default=NORB)
     ap.add_argument("--nel", type=int, default=NEL)
