@@ -17,6 +17,7 @@ larger than L2 (129 MB), so no L2 flush is needed between steps.
 """
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -220,6 +221,19 @@ def run_reference_batched(args):
 
 
 # ------------------------------------------------------------------ GPU arm
+def max_over_ranks(value, world):
+    """The largest of the ranks' values (a job's step time is its slowest
+    replica's); the value itself on one rank.  Host tensors: the gloo group."""
+    if world <= 1:
+        return float(value)
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(value)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_ours(args):
     import torch
 
@@ -296,10 +310,7 @@ def run_ours(args):
         t_wall = time.perf_counter() - t_wall
     launches = capi.kernel_launches() - launches0
     t_step = float(np.mean(times))
-    if world > 1:
-        tt = torch.tensor([t_step], dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_step = float(tt.item())
+    t_step = max_over_ranks(t_step, world)
     # FP32 SpMV roofline on the split storage (FP32 values + int32 columns)
     x32 = torch.randn(N, dtype=torch.float32, device="cuda")
     y32 = torch.empty_like(x32)
@@ -310,7 +321,13 @@ def run_ours(args):
     # resident), y once; the CSR layout adds int32 columns and int64 rowptr
     if lay32 == capi.OP_SLAB:
         bytes32 = stored32 * 4 + N * 4 + N * 4
-        kern32 = "k_slab_sigma<0> (FP32 sigma, slab layout: values only)"
+        # the slab sigma's variant follows the number of beta strings (and
+        # 16-byte alignment, which device allocations have): 4 or 2 strings per
+        # thread when it divides, else one
+        nbs = math.comb(NORB, NEL // 2)
+        vec = 4 if nbs % 4 == 0 else (2 if nbs % 2 == 0 else 1)
+        kern32 = ("k_slab_sigma32v<%d> (FP32 sigma, slab layout: values only, %d beta strings per thread)"
+                  % (vec, vec) if vec > 1 else "k_slab_sigma<0> (FP32 sigma, slab layout: values only)")
     else:
         bytes32 = nnz * 8 + (N + 1) * 8 + N * 4 + N * 4
         kern32 = "k_spmv_csr<float> (FP32 sigma, CSR)"
