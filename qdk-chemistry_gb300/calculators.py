@@ -53,6 +53,8 @@ class Settings:
             raise TypeError("setting '%s' expects bool" % key)
         if typ in (int, float) and isinstance(value, bool):
             raise TypeError("setting '%s' expects %s" % (key, typ.__name__))
+        if typ is str and not isinstance(value, str):
+            raise TypeError("setting '%s' expects str" % key)
         v = typ(value)
         b = self._bounds.get(key)
         if b is not None:

@@ -31,6 +31,8 @@ def test_settings_validation_and_lock(pkg):
         s.set("max_solver_iterations", 0)
     with pytest.raises(TypeError):
         s.set("calculate_one_rdm", 1)
+    with pytest.raises(TypeError):
+        s.set("precision", 5)
     with pytest.raises(KeyError):
         s.set("not_a_setting", 1)
     s.set("ci_residual_tolerance", 1e-9)
