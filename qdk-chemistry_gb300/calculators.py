@@ -435,6 +435,21 @@ class Gb300AsciSettings(Gb300Settings):
         self.set_default("pt2_max_constraint_level", int, 5, "Maximum constraint level for PT2", (0, big))
         self.set_default("pt2_min_constraint_level", int, 0, "Minimum constraint level for PT2", (0, big))
         self.set_default("pt2_constraint_refine_force", int, 0, "Force constraint refinement for PT2", (0, big))
+        # grow-phase controls (determinant_search.hpp:136-198, macis_asci.hpp:93-182)
+        self.set_default("grow_ci_residual_tolerance", float, 0.0,
+                         "CI residual tolerance during grow phase (0 = use refine tolerance)", (0.0, 1.0))
+        self.set_default("taper_grow_factor", float, 0.0,
+                         "Growth factor for final expansion near ntdets_max (0 = disabled)")
+        self.set_default("just_singles", bool, False)
+        self.set_default("grow_with_rot", bool, False)
+        self.set_default("rot_size_start", int, 1000, "Starting size for rotations", (1, big))
+        # H-build variants of the reference (the same matrix; one GPU build here)
+        self.set_default("hamiltonian_build_algorithm", str, "",
+                         "'' or 'sorted_double_loop' (default), 'residue_arrays', 'dynamic_bit_masking'")
+        self.set_default("dynamic_bit_masking_num_masks", int, 0, "Number of bit masks (0 = generator default)",
+                         (0, big))
+        self.set_default("min_patch_overlap", float, 0.3, "Minimum determinant overlap for incremental H build",
+                         (0.0, 1.0))
 
 
 class Gb300Asci(MultiConfigurationCalculator):
@@ -463,6 +478,15 @@ class Gb300Asci(MultiConfigurationCalculator):
         thr = s.get("core_selection_threshold")
         if strategy == "percentage" and not (np.finfo(np.float64).eps <= thr <= 1.0):
             raise ValueError("core_selection_threshold must be in [epsilon, 1.0], got %f" % thr)
+        if s.get("hamiltonian_build_algorithm") not in ("", "sorted_double_loop", "residue_arrays",
+                                                        "dynamic_bit_masking"):
+            raise ValueError("Unknown hamiltonian_build_algorithm: '%s'" % s.get("hamiltonian_build_algorithm"))
+        # the reference's H-build variants and its incremental patching give the
+        # same matrix as the one GPU build, so those settings are accepted as
+        # they are; the grow-phase options below change the result and are not built
+        for key, off in (("just_singles", False), ("grow_with_rot", False), ("taper_grow_factor", 0.0)):
+            if s.get(key) != off:
+                raise NotImplementedError("%s = %r is not supported by the GPU ASCI (only %r)" % (key, s.get(key), off))
         from math import comb
         if s.get("ntdets_max") > comb(n, n_alpha) * comb(n, n_beta):
             return Gb300Cas._run_impl(self, hamiltonian, n_alpha, n_beta)
@@ -474,9 +498,8 @@ class Gb300Asci(MultiConfigurationCalculator):
             # E0 = <HF|H|HF> (macis_asci.cpp:159-163)
             ctx.build_hamiltonian(0.0)
             E0 = float(ctx.diagonal()[0])
-            E, a, b, C, _ = capi.asci(
-                ctx, [a0], [b0], [1.0], E0, grow=True, refine=s.get("max_refine_iter") > 0,
-                tol=s.get("ci_residual_tolerance"), max_m=min(s.get("max_solver_iterations"), 254),
+            kw = dict(
+                max_m=min(s.get("max_solver_iterations"), 254),
                 precision=capi.PREC_MIXED if prec == "mixed" else capi.PREC_FP64, matel_tol=s.get("ci_matel_tol"),
                 ntdets_max=s.get("ntdets_max"), ntdets_min=s.get("ntdets_min"), ncdets_max=s.get("ncdets_max"),
                 core_selection_fixed=1 if strategy == "fixed" else 0,
@@ -486,6 +509,17 @@ class Gb300Asci(MultiConfigurationCalculator):
                 growth_recovery_rate=s.get("growth_recovery_rate"), max_refine_iter=s.get("max_refine_iter"),
                 refine_energy_tol=s.get("refine_energy_tol"), warm_start=int(s.get("warm_start_davidson")),
                 min_warm_start_overlap=s.get("min_warm_start_overlap"))
+            tol = s.get("ci_residual_tolerance")
+            grow_tol = s.get("grow_ci_residual_tolerance")
+            refine = s.get("max_refine_iter") > 0
+            if grow_tol > 0.0:
+                # asci_grow with its own CI tolerance (grow.hpp:73-78), then
+                # asci_refine with the main one
+                E, a, b, C, _ = capi.asci(ctx, [a0], [b0], [1.0], E0, grow=True, refine=False, tol=grow_tol, **kw)
+                if refine:
+                    E, a, b, C, _ = capi.asci(ctx, a, b, C, E, grow=False, refine=True, tol=tol, **kw)
+            else:
+                E, a, b, C, _ = capi.asci(ctx, [a0], [b0], [1.0], E0, grow=True, refine=refine, tol=tol, **kw)
             rdms = None
             want = []
             if s.get("calculate_one_rdm"):

@@ -251,3 +251,72 @@ def test_wavefunction_entropies_from_rdms(pkg, oracle, n2_6e6o):
     s1r, _, _ = oracle.entropies(12, sa, sb, C)
     wr = calc.Wavefunction(12, sa, sb, C, oracle.rdms_spin_dep(12, sa, sb, C))
     np.testing.assert_allclose(wr.get_single_orbital_entropies(), s1r, atol=1e-12, rtol=0)
+
+
+def test_asci_grow_phase_settings(pkg, monkeypatch):
+    """The grow-phase settings of MacisAsciSettings (macis_asci.hpp:93-182,
+    determinant_search.hpp:136-198): defaults; H-build variants accepted (the
+    same matrix), unknown ones refused; the options that change the result and
+    are not built refused before device work; grow_ci_residual_tolerance runs
+    asci_grow at its tolerance and asci_refine at the main one (grow.hpp:73-78),
+    checked with a recording stand-in for the device calls."""
+    calc = pkg.calculators
+    c = calc.create("multi_configuration_calculator", "gb300_asci")
+    s = c.settings()
+    assert (s.get("grow_ci_residual_tolerance"), s.get("taper_grow_factor"), s.get("just_singles"),
+            s.get("grow_with_rot"), s.get("rot_size_start"), s.get("hamiltonian_build_algorithm"),
+            s.get("dynamic_bit_masking_num_masks"), s.get("min_patch_overlap")) == (0.0, 0.0, False, False, 1000,
+                                                                                    "", 0, 0.3)
+    H = calc.Hamiltonian(np.eye(8), np.zeros(8 ** 4))
+
+    def run(**kv):
+        x = calc.create("multi_configuration_calculator", "gb300_asci")
+        x.settings().set("ntdets_max", 100)
+        for k, v in kv.items():
+            x.settings().set(k, v)
+        return x.run(H, 4, 4)
+
+    with pytest.raises(ValueError, match="hamiltonian_build_algorithm"):
+        run(hamiltonian_build_algorithm="magic")
+    for kv in (dict(just_singles=True), dict(grow_with_rot=True), dict(taper_grow_factor=1.5)):
+        with pytest.raises(NotImplementedError):
+            run(**kv)
+
+    calls = []
+
+    class FakeContext:
+        def __init__(self, device):
+            pass
+
+        def __enter__(self):
+            return self
+
+        def __exit__(self, *a):
+            return False
+
+        def set_integrals(self, T, V):
+            pass
+
+        def set_dets(self, a, b):
+            pass
+
+        def build_hamiltonian(self, thresh):
+            pass
+
+        def diagonal(self):
+            return np.array([-1.0])
+
+    def fake_asci(ctx, a0, b0, c0, E0, grow, refine, tol, **kw):
+        calls.append((grow, refine, tol, E0))
+        return E0 - 0.5, np.array([15], np.uint64), np.array([15], np.uint64), np.ones(1), E0 - 0.25
+
+    monkeypatch.setattr(calc.capi, "Context", FakeContext)
+    monkeypatch.setattr(calc.capi, "asci", fake_asci)
+    E, _ = run(hamiltonian_build_algorithm="residue_arrays", min_patch_overlap=0.9)
+    assert calls == [(True, True, 1e-6, -1.0)] and E == -1.5
+    calls.clear()
+    run(grow_ci_residual_tolerance=1e-4)
+    assert calls == [(True, False, 1e-4, -1.0), (False, True, 1e-6, -1.5)]
+    calls.clear()
+    run(grow_ci_residual_tolerance=1e-4, max_refine_iter=0)
+    assert calls == [(True, False, 1e-4, -1.0)]
