@@ -208,6 +208,7 @@ typedef struct qdkgb_asci_settings {
   double refine_energy_tol;        /* default 1e-6 */
   int warm_start;                  /* default 1 */
   double min_warm_start_overlap;   /* default 0.5 */
+  double taper_grow_factor;        /* default 0 (off): the growth factor of a step that would pass ntdets_max */
 } qdkgb_asci_settings;
 
 void qdkgb_asci_default_settings(qdkgb_asci_settings* s);

@@ -1117,6 +1117,7 @@ struct AsciSettings {
   int core_fixed = 0;  // 0: Percentage, 1: Fixed
   double core_threshold = 0.95, h_el_tol = 1e-8, rv_prune_tol = 1e-8;
   double grow_factor = 8.0, min_grow_factor = 1.01, backoff = 0.5, recovery = 1.1;
+  double taper_grow_factor = 0.;  // off
   int64_t max_refine_iter = 6;
   double refine_energy_tol = 1e-6;
   int warm_start = 1;
@@ -1852,16 +1853,28 @@ double asci_iter(const Ham& H, const AsciSettings& S, int64_t ndets_max, double 
 }
 
 // asci_grow (include/macis/asci/grow.hpp:45-268), without the optional rotations
-double asci_grow(const Ham& H, const AsciSettings& S, double E0, std::vector<Det>& wfn, std::vector<double>& X) {
+// (steps, when given, receives for each asci_iter the size asked and the size
+// reached)
+double asci_grow(const Ham& H, const AsciSettings& S, double E0, std::vector<Det>& wfn, std::vector<double>& X,
+                 std::vector<int64_t>* steps = nullptr) {
   size_t prev = wfn.size();
   double gf = S.grow_factor;
   while ((int64_t)wfn.size() < S.ntdets_max) {
-    int64_t nnew = std::min<int64_t>(std::max<int64_t>(S.ntdets_min, (int64_t)std::ceil(wfn.size() * gf)), S.ntdets_max);
+    // taper (grow.hpp:97-107)
+    double eff = gf;
+    if (S.taper_grow_factor > 0. && (int64_t)std::ceil(wfn.size() * gf) > S.ntdets_max)
+      eff = std::max(S.min_grow_factor, S.taper_grow_factor);
+    int64_t nnew =
+        std::min<int64_t>(std::max<int64_t>(S.ntdets_min, (int64_t)std::ceil(wfn.size() * eff)), S.ntdets_max);
     if (nnew <= (int64_t)wfn.size()) {
       nnew = std::min<int64_t>(wfn.size() + 1, S.ntdets_max);
       if (nnew <= (int64_t)wfn.size()) break;
     }
     const double E = asci_iter(H, S, nnew, E0, wfn, X);
+    if (steps) {
+      steps->push_back(nnew);
+      steps->push_back((int64_t)wfn.size());
+    }
     if ((int64_t)wfn.size() < nnew) {
       gf = std::max(S.min_grow_factor, gf * S.backoff);
       if (wfn.size() <= prev) break;
@@ -2076,6 +2089,7 @@ static AsciSettings asci_settings_from(const double* set) {
   S.ci_res_tol = set[15];
   S.ci_max_subspace = (int64_t)set[16];
   S.ci_matel_tol = set[17];
+  S.taper_grow_factor = set[18];
   return S;
 }
 
@@ -2102,6 +2116,25 @@ int64_t orc_asci(void* h, const double* set, int64_t n0, const uint64_t* a0, con
       out_b[i] = wfn[i].b;
       out_c[i] = X[i];
     }
+  });
+  return nret;
+}
+
+// asci_grow alone; req (up to cap entries) receives, per asci_iter, the size
+// requested and the size reached; returns the number of entries, or -1
+int64_t orc_asci_grow_requests(void* h, const double* set, int64_t n0, const uint64_t* a0, const uint64_t* b0,
+                               const double* c0, double E0, int64_t cap, int64_t* req) {
+  const Ham& H = *(Ham*)h;
+  const AsciSettings S = asci_settings_from(set);
+  int64_t nret = -1;
+  guard([&] {
+    std::vector<Det> wfn(n0);
+    std::vector<double> X(c0, c0 + n0);
+    for (int64_t i = 0; i < n0; ++i) wfn[i] = {a0[i], b0[i]};
+    std::vector<int64_t> steps;
+    asci_grow(H, S, E0, wfn, X, &steps);
+    nret = (int64_t)steps.size();
+    for (int64_t i = 0; i < std::min(nret, cap); ++i) req[i] = steps[i];
   });
   return nret;
 }

@@ -67,6 +67,8 @@ def lib():
         L.orc_asci.restype = i64
         L.orc_asci.argtypes = [vp, _f64p, i64, _u64p, _u64p, _f64p, f64, ci, ci, i64, _u64p, _u64p, _f64p,
                                ctypes.POINTER(f64), ctypes.POINTER(f64)]
+        L.orc_asci_grow_requests.restype = i64
+        L.orc_asci_grow_requests.argtypes = [vp, _f64p, i64, _u64p, _u64p, _f64p, f64, i64, _i64p]
         L.orc_asci_iter.restype = i64
         L.orc_asci_iter.argtypes = [vp, _f64p, i64, _u64p, _u64p, _f64p, f64, i64, i64, _u64p, _u64p, _f64p,
                                     ctypes.POINTER(f64)]
@@ -260,7 +262,7 @@ ASCI_DEFAULTS = dict(ntdets_max=100000, ntdets_min=100, ncdets_max=100, core_fix
                      h_el_tol=1e-8, rv_prune_tol=1e-8, grow_factor=8.0, min_grow_factor=1.01, backoff=0.5,
                      recovery=1.1, max_refine_iter=6, refine_energy_tol=1e-6, warm_start=1,
                      min_warm_start_overlap=0.5, ci_res_tol=1e-8, ci_max_subspace=200,
-                     ci_matel_tol=float(np.finfo(np.float64).eps))
+                     ci_matel_tol=float(np.finfo(np.float64).eps), taper_grow_factor=0.0)
 _ASCI_ORDER = list(ASCI_DEFAULTS)
 
 
@@ -289,6 +291,19 @@ def asci(ham, alpha0, beta0, c0, E0, grow=True, refine=True, **settings):
     if n < 0:
         raise RuntimeError(lib().orc_last_error().decode())
     return E.value, oa[:n].copy(), ob[:n].copy(), oc[:n].copy(), Eg.value
+
+
+def asci_grow_requests(ham, alpha0, beta0, c0, E0, **settings):
+    """asci_grow alone; per asci_iter, (determinants requested, reached)."""
+    s = _asci_settings(**settings)
+    req = np.zeros(256, dtype=np.int64)
+    n = lib().orc_asci_grow_requests(ham._h, s, len(alpha0), np.ascontiguousarray(alpha0, dtype=np.uint64),
+                                     np.ascontiguousarray(beta0, dtype=np.uint64),
+                                     np.ascontiguousarray(c0, dtype=np.float64), float(E0), len(req), req)
+    if n < 0:
+        raise RuntimeError(lib().orc_last_error().decode())
+    r = req[:min(n, len(req))].tolist()
+    return list(zip(r[0::2], r[1::2]))
 
 
 def asci_iter(ham, alpha, beta, c, E0, ndets_max, **settings):

@@ -439,7 +439,7 @@ class Gb300AsciSettings(Gb300Settings):
         self.set_default("grow_ci_residual_tolerance", float, 0.0,
                          "CI residual tolerance during grow phase (0 = use refine tolerance)", (0.0, 1.0))
         self.set_default("taper_grow_factor", float, 0.0,
-                         "Growth factor for final expansion near ntdets_max (0 = disabled)")
+                         "Growth factor for final expansion near ntdets_max (0 = disabled)", (0.0, 1e6))
         self.set_default("just_singles", bool, False)
         self.set_default("grow_with_rot", bool, False)
         self.set_default("rot_size_start", int, 1000, "Starting size for rotations", (1, big))
@@ -484,7 +484,7 @@ class Gb300Asci(MultiConfigurationCalculator):
         # the reference's H-build variants and its incremental patching give the
         # same matrix as the one GPU build, so those settings are accepted as
         # they are; the grow-phase options below change the result and are not built
-        for key, off in (("just_singles", False), ("grow_with_rot", False), ("taper_grow_factor", 0.0)):
+        for key, off in (("just_singles", False), ("grow_with_rot", False)):
             if s.get(key) != off:
                 raise NotImplementedError("%s = %r is not supported by the GPU ASCI (only %r)" % (key, s.get(key), off))
         from math import comb
@@ -508,7 +508,7 @@ class Gb300Asci(MultiConfigurationCalculator):
                 min_grow_factor=s.get("min_grow_factor"), growth_backoff_rate=s.get("growth_backoff_rate"),
                 growth_recovery_rate=s.get("growth_recovery_rate"), max_refine_iter=s.get("max_refine_iter"),
                 refine_energy_tol=s.get("refine_energy_tol"), warm_start=int(s.get("warm_start_davidson")),
-                min_warm_start_overlap=s.get("min_warm_start_overlap"))
+                min_warm_start_overlap=s.get("min_warm_start_overlap"), taper_grow_factor=s.get("taper_grow_factor"))
             tol = s.get("ci_residual_tolerance")
             grow_tol = s.get("grow_ci_residual_tolerance")
             refine = s.get("max_refine_iter") > 0

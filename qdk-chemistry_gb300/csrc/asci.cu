@@ -865,8 +865,13 @@ void asci_run(Context* c, const qdkgb_asci_settings& S, const qdkgb_davidson_set
     size_t prev = wfn.size();
     double gf = S.grow_factor;
     while ((int64_t)wfn.size() < S.ntdets_max) {
+      // taper (grow.hpp:97-107): a step that would pass ntdets_max at the
+      // current factor uses max(min_grow_factor, taper_grow_factor) instead
+      double eff = gf;
+      if (S.taper_grow_factor > 0. && (int64_t)std::ceil((double)wfn.size() * gf) > S.ntdets_max)
+        eff = std::max(S.min_grow_factor, S.taper_grow_factor);
       int64_t nnew = std::min<int64_t>(
-          std::max<int64_t>(S.ntdets_min, (int64_t)std::ceil((double)wfn.size() * gf)), S.ntdets_max);
+          std::max<int64_t>(S.ntdets_min, (int64_t)std::ceil((double)wfn.size() * eff)), S.ntdets_max);
       if (nnew <= (int64_t)wfn.size()) {
         nnew = std::min<int64_t>((int64_t)wfn.size() + 1, S.ntdets_max);
         if (nnew <= (int64_t)wfn.size()) break;

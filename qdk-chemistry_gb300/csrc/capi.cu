@@ -466,6 +466,7 @@ void qdkgb_asci_default_settings(qdkgb_asci_settings* s) {
   s->refine_energy_tol = 1e-6;
   s->warm_start = 1;
   s->min_warm_start_overlap = 0.5;
+  s->taper_grow_factor = 0.0;
 }
 
 int qdkgb_asci_search(qdkgb_context* c, const qdkgb_asci_settings* s, int64_t ncore, const uint64_t* ca,

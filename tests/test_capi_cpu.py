@@ -80,3 +80,27 @@ def test_mcscf_and_pt2_defaults(pkg):
     assert s2.orb_grad_tol == 1e-7
     with pytest.raises(KeyError):
         capi.default_mcscf_settings(no_such_setting=1)
+
+
+def test_settings_struct_layouts_match(pkg):
+    """Each C default-settings call writes exactly the ctypes mirror: called on
+    a buffer longer than the mirror and filled with a sentinel byte, it leaves
+    the tail untouched, and every ASCI field reads back its default
+    (qdkgb_asci_default_settings)."""
+    capi = pkg.capi
+    L = capi.lib()
+    for cls, fn in ((capi.AsciSettings, L.qdkgb_asci_default_settings),
+                    (capi.DavidsonSettings, L.qdkgb_davidson_default_settings),
+                    (capi.McscfSettings, L.qdkgb_mcscf_default_settings),
+                    (capi.BatchSettings, L.qdkgb_batch_default_settings)):
+        n = ctypes.sizeof(cls)
+        buf = (ctypes.c_ubyte * (n + 64))(*([0xAB] * (n + 64)))
+        fn(ctypes.cast(buf, ctypes.POINTER(cls)))
+        assert bytes(buf[n:]) == b"\xab" * 64, cls.__name__
+    s = capi.default_asci_settings()
+    want = dict(ntdets_max=100000, ntdets_min=100, ncdets_max=100, core_selection_fixed=0,
+                core_selection_threshold=0.95, h_el_tol=1e-8, rv_prune_tol=1e-8, grow_factor=8.0,
+                min_grow_factor=1.01, growth_backoff_rate=0.5, growth_recovery_rate=1.1, max_refine_iter=6,
+                refine_energy_tol=1e-6, warm_start=1, min_warm_start_overlap=0.5, taper_grow_factor=0.0)
+    assert [f for f, _ in capi.AsciSettings._fields_] == list(want)
+    assert {k: getattr(s, k) for k in want} == want

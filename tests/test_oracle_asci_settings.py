@@ -95,3 +95,40 @@ def test_core_selection_defaults(pkg):
     c = pkg.calculators.create("multi_configuration_calculator", "gb300_asci")
     assert c.settings().get("core_selection_strategy") == "percentage"
     assert c.settings().get("core_selection_threshold") == 0.95
+
+
+def test_taper_grow_factor(oracle, water):
+    """grow.hpp:97-107: a step whose full-factor expansion would pass
+    ntdets_max asks for max(min_grow_factor, taper_grow_factor) times the size
+    instead.  Fixed core, 1000 determinants, factor 8 (no backoff here: every
+    step reaches its request); each request is checked against the rule from
+    the size the previous step reached (the tie-inclusive selection can return
+    a few more than asked, and which borderline determinants tie can vary with
+    the threads' summation order, so the sizes are not fixed here)."""
+    import math
+    H, (a0, b0), E_hf = water
+
+    def check(steps, nmax, taper, gf=8.0, nmin=100, min_gf=1.01):
+        prev = 1
+        for req, got in steps:
+            eff = gf
+            if taper > 0 and math.ceil(prev * gf) > nmax:
+                eff = max(min_gf, taper)
+            assert req == min(max(nmin, math.ceil(prev * eff)), nmax), (prev, req)
+            assert got >= req
+            prev = got
+        return prev
+
+    plain = oracle.asci_grow_requests(H, a0, b0, [1.0], E_hf, ntdets_max=1000, ncdets_max=100, **FIXED)
+    assert len(plain) == 3 and check(plain, 1000, 0.0) >= 1000
+    tap = oracle.asci_grow_requests(H, a0, b0, [1.0], E_hf, taper_grow_factor=1.1, ntdets_max=1000,
+                                    ncdets_max=100, **FIXED)
+    # ~809 -> ~890 -> ~980 -> 1000: two tapered steps where the plain run jumps
+    assert len(tap) == 5 and check(tap, 1000, 1.1) >= 1000
+    floor = oracle.asci_grow_requests(H, a0, b0, [1.0], E_hf, taper_grow_factor=1.0, ntdets_max=850,
+                                      ncdets_max=100, **FIXED)
+    # taper 1.0 is raised to the minimum factor 1.01: steps of about 1 %
+    assert len(floor) >= 6 and check(floor, 850, 1.0) == 850
+    E, a, _, c, _ = oracle.asci(H, a0, b0, [1.0], E_hf, grow=True, refine=False, taper_grow_factor=1.1,
+                                ntdets_max=1000, ncdets_max=100, **FIXED)
+    assert len(a) == 1000 and abs(c @ c - 1.0) < 1e-12 and E < E_hf
