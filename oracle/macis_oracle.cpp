@@ -1118,6 +1118,7 @@ struct AsciSettings {
   double core_threshold = 0.95, h_el_tol = 1e-8, rv_prune_tol = 1e-8;
   double grow_factor = 8.0, min_grow_factor = 1.01, backoff = 0.5, recovery = 1.1;
   double taper_grow_factor = 0.;  // off
+  int just_singles = 0;            // search: single excitations only
   int64_t max_refine_iter = 6;
   double refine_energy_tol = 1e-6;
   int warm_start = 1;
@@ -1231,7 +1232,9 @@ void os_doubles_contribs(const Ham& H, double coeff, uint64_t sa, uint64_t sb, c
 // order of the reference's per-determinant loop (determinant_search.hpp:
 // 386-474, pt2.hpp:298-344), then P itself with an infinite score (it is in
 // the wavefunction, so it drops out after accumulation).
-void contribs_of(const Ham& H, const Det& P, double c, double E0, double tol, std::vector<Contrib>& out) {
+// (just_singles: the search's option, determinant_search.hpp:274-296)
+void contribs_of(const Ham& H, const Det& P, double c, double E0, double tol, std::vector<Contrib>& out,
+                 bool just_singles = false) {
   const int n = H.n;
   std::vector<uint32_t> oa, va, ob, vb;
   for (int p = 0; p < n; ++p) {
@@ -1241,10 +1244,12 @@ void contribs_of(const Ham& H, const Det& P, double c, double E0, double tol, st
   const double hdiag = H.me_diag(oa, ob);
   const std::vector<double> ea = orbital_ens(H, oa, ob), eb = orbital_ens(H, ob, oa);
   singles_contribs(H, c, P.a, P.b, true, oa, va, ob, ea, hdiag, E0, tol, out);
-  ss_doubles_contribs(H, c, P.a, P.b, true, oa, va, ea, hdiag, E0, tol, out);
-  os_doubles_contribs(H, c, P.a, P.b, oa, va, ob, vb, ea, eb, hdiag, E0, tol, out);
+  if (!just_singles) {
+    ss_doubles_contribs(H, c, P.a, P.b, true, oa, va, ea, hdiag, E0, tol, out);
+    os_doubles_contribs(H, c, P.a, P.b, oa, va, ob, vb, ea, eb, hdiag, E0, tol, out);
+  }
   singles_contribs(H, c, P.b, P.a, false, ob, vb, oa, eb, hdiag, E0, tol, out);
-  ss_doubles_contribs(H, c, P.b, P.a, false, ob, vb, eb, hdiag, E0, tol, out);
+  if (!just_singles) ss_doubles_contribs(H, c, P.b, P.a, false, ob, vb, eb, hdiag, E0, tol, out);
   out.push_back({P, std::numeric_limits<double>::infinity(), 1.0});
 }
 
@@ -1272,7 +1277,7 @@ std::vector<Det> asci_search(const Ham& H, const AsciSettings& S, int64_t ndets_
 #endif
     std::vector<Contrib>& out = per[tid];
 #pragma omp for schedule(dynamic)
-    for (int64_t ip = 0; ip < ncore; ++ip) contribs_of(H, core[ip], C[ip], E0, S.h_el_tol, out);
+    for (int64_t ip = 0; ip < ncore; ++ip) contribs_of(H, core[ip], C[ip], E0, S.h_el_tol, out, S.just_singles != 0);
   }
   (void)n;
   std::vector<Contrib> all;
@@ -2090,6 +2095,7 @@ static AsciSettings asci_settings_from(const double* set) {
   S.ci_max_subspace = (int64_t)set[16];
   S.ci_matel_tol = set[17];
   S.taper_grow_factor = set[18];
+  S.just_singles = (int)set[19];
   return S;
 }
 
@@ -2166,9 +2172,7 @@ int64_t orc_asci_search(void* h, const double* set, int64_t ncore, const uint64_
                         const double* c, double E0, int64_t ndets_max, int64_t cap, uint64_t* out_a,
                         uint64_t* out_b) {
   const Ham& H = *(Ham*)h;
-  AsciSettings S;
-  S.h_el_tol = set[5];
-  S.rv_prune_tol = set[6];
+  const AsciSettings S = asci_settings_from(set);
   int64_t nret = -1;
   guard([&] {
     std::vector<Det> core(ncore);

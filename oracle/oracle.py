@@ -262,7 +262,7 @@ ASCI_DEFAULTS = dict(ntdets_max=100000, ntdets_min=100, ncdets_max=100, core_fix
                      h_el_tol=1e-8, rv_prune_tol=1e-8, grow_factor=8.0, min_grow_factor=1.01, backoff=0.5,
                      recovery=1.1, max_refine_iter=6, refine_energy_tol=1e-6, warm_start=1,
                      min_warm_start_overlap=0.5, ci_res_tol=1e-8, ci_max_subspace=200,
-                     ci_matel_tol=float(np.finfo(np.float64).eps), taper_grow_factor=0.0)
+                     ci_matel_tol=float(np.finfo(np.float64).eps), taper_grow_factor=0.0, just_singles=0)
 _ASCI_ORDER = list(ASCI_DEFAULTS)
 
 

@@ -483,10 +483,9 @@ class Gb300Asci(MultiConfigurationCalculator):
             raise ValueError("Unknown hamiltonian_build_algorithm: '%s'" % s.get("hamiltonian_build_algorithm"))
         # the reference's H-build variants and its incremental patching give the
         # same matrix as the one GPU build, so those settings are accepted as
-        # they are; the grow-phase options below change the result and are not built
-        for key, off in (("just_singles", False), ("grow_with_rot", False)):
-            if s.get(key) != off:
-                raise NotImplementedError("%s = %r is not supported by the GPU ASCI (only %r)" % (key, s.get(key), off))
+        # they are; natural-orbital rotation during the grow is not built
+        if s.get("grow_with_rot"):
+            raise NotImplementedError("grow_with_rot = True is not supported by the GPU ASCI (only False)")
         from math import comb
         if s.get("ntdets_max") > comb(n, n_alpha) * comb(n, n_beta):
             return Gb300Cas._run_impl(self, hamiltonian, n_alpha, n_beta)
@@ -508,7 +507,8 @@ class Gb300Asci(MultiConfigurationCalculator):
                 min_grow_factor=s.get("min_grow_factor"), growth_backoff_rate=s.get("growth_backoff_rate"),
                 growth_recovery_rate=s.get("growth_recovery_rate"), max_refine_iter=s.get("max_refine_iter"),
                 refine_energy_tol=s.get("refine_energy_tol"), warm_start=int(s.get("warm_start_davidson")),
-                min_warm_start_overlap=s.get("min_warm_start_overlap"), taper_grow_factor=s.get("taper_grow_factor"))
+                min_warm_start_overlap=s.get("min_warm_start_overlap"), taper_grow_factor=s.get("taper_grow_factor"),
+                just_singles=int(s.get("just_singles")))
             tol = s.get("ci_residual_tolerance")
             grow_tol = s.get("grow_ci_residual_tolerance")
             refine = s.get("max_refine_iter") > 0

@@ -83,6 +83,7 @@ struct CoreArgs {
   double h_el_tol;
   Table T;
   uint32_t npass = 1, pass = 0;  // targets whose part_of() == pass are inserted (npass > 1: PT2 passes)
+  bool just_singles = false;     // the search's just_singles: single excitations only
 };
 
 // part of the target space of a determinant in a split into npass passes (a
@@ -169,7 +170,7 @@ __global__ void __launch_bounds__(kAsciWarps * 32) k_asci_enum(CoreArgs A) {
     const int64_t pa_o = (int64_t)ka * (ka - 1) / 2, pa_v = (int64_t)na_v * (na_v - 1) / 2;
     const int64_t pb_o = (int64_t)kb * (kb - 1) / 2, pb_v = (int64_t)nb_v * (nb_v - 1) / 2;
     const int64_t nda = pa_o * pa_v, ndb = pb_o * pb_v, nab = nsa * nsb;
-    const int64_t total = nsa + nsb + nda + ndb + nab;
+    const int64_t total = A.just_singles ? nsa + nsb : nsa + nsb + nda + ndb + nab;
     for (int64_t e = lane; e < total; e += 32) {
       double ch = 0., hd = 0.;
       uint64_t qa = Pa, qb = Pb;
@@ -304,7 +305,7 @@ __global__ void __launch_bounds__(kAsciWarps * 32) k_target_sketch(CoreArgs A, u
     const int64_t nsa = (int64_t)ka * na_v, nsb = (int64_t)kb * nb_v;
     const int64_t pa_v = (int64_t)na_v * (na_v - 1) / 2, pb_v = (int64_t)nb_v * (nb_v - 1) / 2;
     const int64_t nda = (int64_t)ka * (ka - 1) / 2 * pa_v, ndb = (int64_t)kb * (kb - 1) / 2 * pb_v;
-    const int64_t total = nsa + nsb + nda + ndb + nsa * nsb;
+    const int64_t total = A.just_singles ? nsa + nsb : nsa + nsb + nda + ndb + nsa * nsb;
     for (int64_t e = lane; e < total; e += 32) {
       uint64_t qa = Pa, qb = Pb;
       int64_t x = e;
@@ -491,7 +492,7 @@ double distinct_targets(Context* c, const CoreArgs& A, unsigned* regs) {
 // Returns the new determinant list (top-k candidates followed by the core).
 void asci_search_gpu(Context* c, int64_t ncore, const uint64_t* ca, const uint64_t* cb, const double* cc, double E0,
                      int64_t ndets_max, double h_el_tol, double rv_prune_tol, std::vector<uint64_t>& out_a,
-                     std::vector<uint64_t>& out_b, int64_t* n_candidates) {
+                     std::vector<uint64_t>& out_b, int64_t* n_candidates, bool just_singles) {
   if (!c->have_ints) throw Error(QDKGB_ERR_STATE, "integrals not set");
   if (ncore <= 0) throw Error(QDKGB_ERR_INVALID, "empty core");
   const int n = c->norb;
@@ -527,6 +528,7 @@ void asci_search_gpu(Context* c, int64_t ncore, const uint64_t* ca, const uint64
   A.cc = (const double*)(dcore + 2 * ncore);
   A.E0 = E0;
   A.h_el_tol = h_el_tol;
+  A.just_singles = just_singles;
   // table: 2.5 x the estimated distinct targets (at most 1.5 x the
   // contributions); an overflowing enumeration is redone with twice the slots
   const double est = distinct_targets(c, A, dev_array<unsigned>(c, bhll, kHllRegs));
@@ -816,7 +818,7 @@ double asci_iter_gpu(Context* c, const qdkgb_asci_settings& S, const qdkgb_david
   }
   std::vector<uint64_t> na, nb;
   asci_search_gpu(c, (int64_t)nkeep, ca.data(), cb.data(), X.data(), E0, ndets_max, S.h_el_tol, S.rv_prune_tol, na,
-                  nb, ncand);
+                  nb, ncand, S.just_singles != 0);
   wfn.resize(na.size());
   for (size_t i = 0; i < na.size(); ++i) wfn[i] = {na[i], nb[i]};
   std::sort(wfn.begin(), wfn.end(), hspin_less);

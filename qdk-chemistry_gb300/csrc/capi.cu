@@ -467,6 +467,7 @@ void qdkgb_asci_default_settings(qdkgb_asci_settings* s) {
   s->warm_start = 1;
   s->min_warm_start_overlap = 0.5;
   s->taper_grow_factor = 0.0;
+  s->just_singles = 0;
 }
 
 int qdkgb_asci_search(qdkgb_context* c, const qdkgb_asci_settings* s, int64_t ncore, const uint64_t* ca,
@@ -477,7 +478,8 @@ int qdkgb_asci_search(qdkgb_context* c, const qdkgb_asci_settings* s, int64_t nc
     if (!s || !ca || !cb || !cc || !n_out) throw Error(QDKGB_ERR_INVALID, "null argument");
     QDKGB_CUDA(cudaSetDevice(c->device));
     std::vector<uint64_t> a, b;
-    asci_search_gpu(c, ncore, ca, cb, cc, E0, ndets_max, s->h_el_tol, s->rv_prune_tol, a, b, nullptr);
+    asci_search_gpu(c, ncore, ca, cb, cc, E0, ndets_max, s->h_el_tol, s->rv_prune_tol, a, b, nullptr,
+                    s->just_singles != 0);
     *n_out = (int64_t)a.size();
     for (int64_t i = 0; i < std::min<int64_t>((int64_t)a.size(), cap); ++i) {
       if (out_a) out_a[i] = a[i];

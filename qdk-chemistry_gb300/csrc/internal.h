@@ -179,7 +179,7 @@ void direct_sigma_fp32(Context* c, const float* x, float* y);
 // asci.cu
 void asci_search_gpu(Context* c, int64_t ncore, const uint64_t* ca, const uint64_t* cb, const double* cc, double E0,
                      int64_t ndets_max, double h_el_tol, double rv_prune_tol, std::vector<uint64_t>& out_a,
-                     std::vector<uint64_t>& out_b, int64_t* n_candidates);
+                     std::vector<uint64_t>& out_b, int64_t* n_candidates, bool just_singles = false);
 double asci_pt2_gpu(Context* c, int64_t nd, const uint64_t* a, const uint64_t* b, const double* C, double E0,
                     double pt2_tol, int64_t max_slots, int64_t* npt2);
 void asci_run(Context* c, const qdkgb_asci_settings& S, const qdkgb_davidson_settings& ci, double matel_tol,

@@ -256,9 +256,9 @@ def test_wavefunction_entropies_from_rdms(pkg, oracle, n2_6e6o):
 def test_asci_grow_phase_settings(pkg, monkeypatch):
     """The grow-phase settings of MacisAsciSettings (macis_asci.hpp:93-182,
     determinant_search.hpp:136-198): defaults; H-build variants accepted (the
-    same matrix), unknown ones refused; just_singles and grow_with_rot (not
-    built) refused before device work; taper_grow_factor passed to the device
-    driver; grow_ci_residual_tolerance runs
+    same matrix), unknown ones refused; grow_with_rot (not built) refused
+    before device work; taper_grow_factor and just_singles passed to the
+    device driver; grow_ci_residual_tolerance runs
     asci_grow at its tolerance and asci_refine at the main one (grow.hpp:73-78),
     checked with a recording stand-in for the device calls."""
     calc = pkg.calculators
@@ -279,9 +279,8 @@ def test_asci_grow_phase_settings(pkg, monkeypatch):
 
     with pytest.raises(ValueError, match="hamiltonian_build_algorithm"):
         run(hamiltonian_build_algorithm="magic")
-    for kv in (dict(just_singles=True), dict(grow_with_rot=True)):
-        with pytest.raises(NotImplementedError):
-            run(**kv)
+    with pytest.raises(NotImplementedError):
+        run(grow_with_rot=True)
 
     calls, seen = [], []
 
@@ -309,7 +308,7 @@ def test_asci_grow_phase_settings(pkg, monkeypatch):
 
     def fake_asci(ctx, a0, b0, c0, E0, grow, refine, tol, **kw):
         calls.append((grow, refine, tol, E0))
-        seen.append(kw["taper_grow_factor"])
+        seen.append((kw["taper_grow_factor"], kw["just_singles"]))
         return E0 - 0.5, np.array([15], np.uint64), np.array([15], np.uint64), np.ones(1), E0 - 0.25
 
     monkeypatch.setattr(calc.capi, "Context", FakeContext)
@@ -324,4 +323,7 @@ def test_asci_grow_phase_settings(pkg, monkeypatch):
     assert calls == [(True, False, 1e-4, -1.0)]
     seen.clear()
     run(taper_grow_factor=1.5)
-    assert seen == [1.5]
+    assert seen == [(1.5, 0)]
+    seen.clear()
+    run(just_singles=True)
+    assert seen == [(0.0, 1)]

@@ -132,3 +132,28 @@ def test_taper_grow_factor(oracle, water):
     E, a, _, c, _ = oracle.asci(H, a0, b0, [1.0], E_hf, grow=True, refine=False, taper_grow_factor=1.1,
                                 ntdets_max=1000, ncdets_max=100, **FIXED)
     assert len(a) == 1000 and abs(c @ c - 1.0) < 1e-12 and E < E_hf
+
+
+def test_just_singles_search(oracle, water):
+    """determinant_search.hpp:274-296: with just_singles the search adds only
+    single excitations of the core determinants.  From the HF determinant
+    every target is one of its singles (their <S|H|HF> are small, Brillouin,
+    but above h_el_tol in these orbitals); from a grown 100-determinant core
+    every new target is one excitation away from some core determinant, and
+    the targets are a subset of those of the full search."""
+    H, (a0, b0), E_hf = water
+    ha, hb = oracle.asci_search(H, a0, b0, np.ones(1), E_hf, 500, just_singles=1)
+    singles = [(x, y) for x, y in zip(ha.tolist(), hb.tolist()) if (x, y) != (31, 31)]
+    assert 0 < len(singles) <= 2 * 5 * 19
+    assert all(bin(x ^ 31).count("1") + bin(y ^ 31).count("1") == 2 for x, y in singles)
+    E, ga, gb, gc, _ = oracle.asci(H, a0, b0, [1.0], E_hf, grow=True, refine=False, ntdets_max=100, **FIXED)
+    order = np.lexsort((gb, ga))
+    ga, gb, gc = ga[order], gb[order], gc[order]
+    sa, sb = oracle.asci_search(H, ga, gb, gc, E, 400, just_singles=1)
+    fa, fb = oracle.asci_search(H, ga, gb, gc, E, 10 ** 6)
+    core = set(zip(ga.tolist(), gb.tolist()))
+    new = [(x, y) for x, y in zip(sa.tolist(), sb.tolist()) if (x, y) not in core]
+    assert len(new) > 0
+    for x, y in new:
+        assert min(bin(x ^ p).count("1") + bin(y ^ q).count("1") for p, q in core) == 2
+    assert set(new) <= set(zip(fa.tolist(), fb.tolist()))
