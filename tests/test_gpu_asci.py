@@ -64,3 +64,27 @@ def test_asci_n2_golden(ctx, pkg, oracle, n2_14e18o, known):
                                   grow_factor=ref["grow_factor"], max_refine_iter=ref["max_refine_iter"], max_m=254)
     assert abs(E - ref["E_total"]) < 1e-8
     assert len(a) == ref["ndets"]
+
+
+def test_asci_just_singles_and_taper_match_oracle(ctx, pkg, oracle, h2o):
+    """The search's just_singles (determinant_search.hpp:274-296) and the
+    grow's taper_grow_factor (grow.hpp:97-107) on the GPU against the oracle:
+    a singles-only search from a 100-determinant water core asked for more
+    determinants than exist (no cut-off, so no tie at a boundary) gives the
+    oracle's set; a tapered grow to 1000 determinants reaches the oracle's
+    energy (1e-6: a borderline tie may differ in one determinant)."""
+    H = oracle.Hamiltonian(h2o["T"], h2o["V"])
+    a0, b0 = pkg.determinants.canonical_hf(5, 5)
+    E0 = H.matrix_element((a0, b0), (a0, b0))
+    E, a, b, c, _ = oracle.asci(H, [a0], [b0], [1.0], E0, ntdets_max=100, core_fixed=1, refine=False)
+    srt = np.lexsort((b, a))
+    ca, cb, cc = a[srt], b[srt], c[srt]
+    oa, ob = oracle.asci_search(H, ca, cb, cc, E, 10 ** 6, just_singles=1)
+    ctx.set_integrals(h2o["T"], h2o["V"])
+    ga, gb = pkg.capi.asci_search(ctx, ca, cb, cc, E, 10 ** 6, just_singles=1)
+    assert len(oa) < 10 ** 6 and _as_set(ga, gb) == _as_set(oa, ob)
+    Eg, ta, _, tc, _ = pkg.capi.asci(ctx, [a0], [b0], [1.0], E0, refine=False, ntdets_max=1000,
+                                     core_selection_fixed=1, taper_grow_factor=1.1)
+    Eo, oa, _, _, _ = oracle.asci(H, [a0], [b0], [1.0], E0, refine=False, ntdets_max=1000, core_fixed=1,
+                                  taper_grow_factor=1.1)
+    assert len(ta) >= 1000 and abs(tc @ tc - 1) < 1e-12 and abs(Eg - Eo) < 1e-6
