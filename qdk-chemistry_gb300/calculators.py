@@ -193,6 +193,58 @@ class Wavefunction:
         na, nb = self.get_active_num_electrons()
         return na + len(self.inactive_indices), nb + len(self.inactive_indices)
 
+    # the StateVectorContainer accessors (state_vector.cpp:171-330, 785-880)
+    def get_coefficients(self):
+        return self.coefficients
+
+    def get_active_determinants(self):
+        return self.get_configurations()
+
+    def get_coefficient(self, configuration):
+        """The coefficient of a determinant (canonical string or (alpha, beta)
+        pair); 0 for one absent from the expansion."""
+        if not len(self.alpha):
+            raise RuntimeError("No determinants available")
+        if isinstance(configuration, str):
+            a, b = determinants.from_canonical_string(configuration)
+        else:
+            a, b = configuration
+        hit = np.flatnonzero((self.alpha == np.uint64(a)) & (self.beta == np.uint64(b)))
+        return float(self.coefficients[hit[0]]) if len(hit) else 0.0
+
+    def get_active_orbital_occupations(self):
+        """(alpha, beta) occupations of the active orbitals: those of the
+        determinant for a single one, else the eigenvalues of the spin-resolved
+        1-RDMs in descending order."""
+        if not len(self.alpha):
+            raise RuntimeError("No determinants available")
+        if self.size() == 1:
+            bits = np.arange(self.norb, dtype=np.uint64)
+            occ = lambda s: ((np.uint64(s) >> bits) & np.uint64(1)).astype(np.float64)
+            return occ(self.alpha[0]), occ(self.beta[0])
+        if not self.has_one_rdm():
+            raise RuntimeError("1RDM must be available to compute orbital occupations")
+        aa, bb = self.get_active_one_rdm_spin_dependent()
+        return np.linalg.eigvalsh(aa)[::-1].copy(), np.linalg.eigvalsh(bb)[::-1].copy()
+
+    def has_one_rdm_spin_dependent(self):
+        return self.has_one_rdm()
+
+    def has_one_rdm_spin_traced(self):
+        return self.has_one_rdm()
+
+    def has_active_one_rdm(self):
+        return self.has_one_rdm()
+
+    def has_two_rdm_spin_dependent(self):
+        return self.has_two_rdm()
+
+    def has_two_rdm_spin_traced(self):
+        return self.has_two_rdm()
+
+    def has_active_two_rdm(self):
+        return self.has_two_rdm()
+
     def get_configurations(self):
         return [determinants.to_canonical_string(a, b, self.norb) for a, b in zip(self.alpha, self.beta)]
 

@@ -327,3 +327,32 @@ def test_asci_grow_phase_settings(pkg, monkeypatch):
     seen.clear()
     run(just_singles=True)
     assert seen == [(0.0, 1)]
+
+
+def test_wavefunction_accessors(pkg, oracle, n2_6e6o):
+    """StateVectorContainer accessors (state_vector.cpp:171-330, 785-880):
+    coefficients by determinant (0 when absent), determinant strings, RDM
+    presence flags, and active occupations (a single determinant's own; else
+    the descending eigenvalues of the spin-resolved 1-RDMs)."""
+    calc, det = pkg.calculators, pkg.determinants
+    a, b = det.spin_sort(*det.fci_space(6, 3, 3))
+    H = oracle.Hamiltonian(n2_6e6o["T"], n2_6e6o["V"])
+    _, X, _ = oracle.build_csr(H, a, b).selected_ci_diag(tol=1e-10)
+    R = oracle.rdms_spin_dep(6, a, b, X, want=("aa", "bb"))
+    w = calc.Wavefunction(6, a, b, X, R)
+    assert w.get_coefficients() is w.coefficients
+    assert w.get_active_determinants() == w.get_configurations()
+    s0 = w.get_active_determinants()[7]
+    assert w.get_coefficient(s0) == X[7] and w.get_coefficient((a[7], b[7])) == X[7]
+    assert w.get_coefficient("000222") == X[np.flatnonzero((a == 0b111000) & (b == 0b111000))[0]]
+    assert calc.Wavefunction(6, a[:5], b[:5], X[:5]).get_coefficient("000222") == 0.0
+    assert w.has_one_rdm_spin_dependent() and w.has_one_rdm_spin_traced() and w.has_active_one_rdm()
+    assert not w.has_two_rdm_spin_dependent() and not w.has_two_rdm_spin_traced() and not w.has_active_two_rdm()
+    na, nb = w.get_active_orbital_occupations()
+    assert np.all(np.diff(na) <= 1e-15) and abs(na.sum() - 3) < 1e-10 and abs(nb.sum() - 3) < 1e-10
+    np.testing.assert_allclose(na, np.sort(np.linalg.eigvalsh(R["aa"]))[::-1], atol=1e-14)
+    one = calc.Wavefunction(6, np.array([0b001011], np.uint64), np.array([0b000111], np.uint64), np.ones(1))
+    oa, ob = one.get_active_orbital_occupations()
+    assert oa.tolist() == [1, 1, 0, 1, 0, 0] and ob.tolist() == [1, 1, 1, 0, 0, 0]
+    with pytest.raises(RuntimeError, match="1RDM must be available"):
+        calc.Wavefunction(6, a, b, X).get_active_orbital_occupations()
