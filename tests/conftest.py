@@ -80,3 +80,54 @@ def davidson_solver_cases():
     heis = np.array([[1.0, 0, 0, 0], [0, -1, 2, 0], [0, 2, -1, 0], [0, 0, 0, 1]])
     return [("tridiagonal6", sp.csr_matrix(tri), 2 - 2 * np.cos(np.pi / 7), v / np.linalg.norm(v)),
             ("heisenberg2", sp.csr_matrix(heis), -3.0, np.array([0.0, 1.0, -1.0, 0.0]) / np.sqrt(2))]
+
+
+class OracleDevice:
+    """A test-only stand-in for capi.Context whose calls are answered by the
+    oracle: it runs the calculators' host orchestration end to end on the
+    CPU (the device numerics are covered by the GPU tests)."""
+
+    def __init__(self, device=0):
+        import oracle
+        self.o = oracle
+        self.M = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        return False
+
+    def set_integrals(self, T, V):
+        self.n = T.shape[0]
+        self.H = self.o.Hamiltonian(T, V)
+
+    def set_dets(self, a, b):
+        self.a, self.b = np.asarray(a, np.uint64), np.asarray(b, np.uint64)
+        self.ndets = len(self.a)
+
+    def build_hamiltonian(self, thresh=np.finfo(np.float64).eps, storage=0):
+        self.M = self.o.build_csr(self.H, self.a, self.b, thresh)
+        return self.M.nnz
+
+    def get_csr(self, index_bits=64):
+        return self.M.arrays()
+
+    def set_csr(self, rp, ci, nz):
+        self.M = self.o.csr_from_arrays(rp, ci, nz)
+        self.ndets = len(rp) - 1
+
+    def diagonal(self):
+        return self.M.diag()
+
+    def davidson(self, max_m=200, tol=1e-8, precision=0, guess=None, want_vector=True):
+        E, X, it = self.M.selected_ci_diag(max_m=max_m, tol=tol)
+        return E, X, {"iterations": it}
+
+    def rdms_spin_dep(self, C, want=("aa", "bb", "aaaa", "bbbb", "aabb")):
+        return self.o.rdms_spin_dep(self.n, self.a, self.b, C, want=want)
+
+    def orbital_entropies(self, C, two_orbital=True, mutual_information=True):
+        s1, s2, mi = self.o.entropies(self.n, self.a, self.b, C)
+        return s1, (s2 if two_orbital else None), (mi if mutual_information else None)
+

@@ -123,3 +123,25 @@ def test_selection_from_rdm_entropies(pkg, oracle, n2_6e6o):
         sel = calc.create("active_space_selector", name).select(w)
         assert set(sel) <= set(range(4, 10))
         assert not sel or top in sel
+
+
+def test_cas_then_autocas_flow(pkg, n2_6e6o, monkeypatch):
+    """The flow of python/tests/test_active_space.py:38-80 (CASCI with 1- and
+    2-RDMs, then each selector on the wavefunction) with the oracle answering
+    the device calls: the entropies come from the RDMs, and both selectors
+    return sorted subsets of the active orbitals as one-determinant
+    wavefunctions."""
+    from conftest import OracleDevice
+    calc = pkg.calculators
+    monkeypatch.setattr(calc.capi, "Context", OracleDevice)
+    mc = calc.create("multi_configuration_calculator", "gb300_cas")
+    mc.settings().set("calculate_one_rdm", True)
+    mc.settings().set("calculate_two_rdm", True)
+    ham = calc.Hamiltonian(n2_6e6o["T"], n2_6e6o["V"], n2_6e6o["E_core"])
+    _, wfn = mc.run(ham, 3, 3)
+    assert wfn.has_single_orbital_entropies() and "s1" not in wfn._ent
+    for name in ("gb300_autocas", "gb300_autocas_eos"):
+        out = calc.create("active_space_selector", name).run(wfn)
+        idx = out.get_active_indices()
+        assert idx == sorted(idx) and set(idx) <= set(range(6)) and out.size() == 1
+        assert out.norb == len(idx)

@@ -356,3 +356,53 @@ def test_wavefunction_accessors(pkg, oracle, n2_6e6o):
     assert oa.tolist() == [1, 1, 0, 1, 0, 0] and ob.tolist() == [1, 1, 1, 0, 0, 0]
     with pytest.raises(RuntimeError, match="1RDM must be available"):
         calc.Wavefunction(6, a, b, X).get_active_orbital_occupations()
+
+
+def test_pmc_repeated_flow_on_oracle_device(pkg, oracle, n2_6e6o, monkeypatch):
+    """Gb300Pmc on lists that repeat determinants, with the oracle answering
+    the device calls: the checks of the GPU test (energy and vector = the
+    lowest eigenpair of MACIS's matrix for the list as given, RDMs = the
+    oracle's form_rdms over the list, one determinant twice = 2 <D|H|D>) hold
+    for the host orchestration itself."""
+    import scipy.sparse as sp
+    from conftest import OracleDevice
+    calc, det = pkg.calculators, pkg.determinants
+    monkeypatch.setattr(calc.capi, "Context", OracleDevice)
+    a, b = det.fci_space(6, 3, 3)
+    rng = np.random.default_rng(11)
+    sel = rng.choice(len(a), 20, replace=False)
+    lst = np.concatenate([sel, sel[[2, 5, 5]]])
+    rng.shuffle(lst)
+    cfgs = [det.to_canonical_string(a[i], b[i], 6) for i in lst]
+    ham = calc.Hamiltonian(n2_6e6o["T"], n2_6e6o["V"], n2_6e6o["E_core"])
+    H = oracle.Hamiltonian(n2_6e6o["T"], n2_6e6o["V"])
+
+    def dense(la, lb):
+        rp, ci, nz = oracle.build_csr(H, la, lb).arrays()
+        return sp.csr_matrix((nz, ci, rp), shape=(len(la),) * 2).toarray()
+
+    p = calc.create("projected_multi_configuration_calculator")
+    p.settings().set("calculate_one_rdm", True)
+    p.settings().set("calculate_two_rdm", True)
+    p.settings().set("calculate_single_orbital_entropies", True)
+    E, wfn = p.run(ham, cfgs)
+    w, X = np.linalg.eigh(dense(a[lst], b[lst]))
+    assert wfn.size() == len(cfgs) and wfn.get_configurations() == cfgs
+    assert abs(E - (w[0] + n2_6e6o["E_core"])) < 1e-10
+    assert abs(abs(wfn.coefficients @ X[:, 0]) - 1.0) < 1e-8
+    Ro = oracle.rdms_spin_dep(6, a[lst], b[lst], wfn.coefficients)
+    aa, bb = wfn.get_active_one_rdm_spin_dependent()
+    aabb, aaaa, bbbb = wfn.get_active_two_rdm_spin_dependent()
+    np.testing.assert_allclose(aa, Ro["aa"], atol=1e-10, rtol=0)
+    np.testing.assert_allclose(bb, Ro["bb"], atol=1e-10, rtol=0)
+    for got, key in ((aabb, "aabb"), (aaaa, "aaaa"), (bbbb, "bbbb")):
+        np.testing.assert_allclose(got, 2.0 * Ro[key].ravel(order="F"), atol=1e-10, rtol=0)
+    assert wfn.has_single_orbital_entropies() and len(wfn.get_single_orbital_entropies()) == 6
+    E2, w2 = calc.create("projected_multi_configuration_calculator").run(ham, ["222000", "222000"])
+    hf = H.matrix_element((7, 7), (7, 7))
+    assert abs(E2 - (2 * hf + n2_6e6o["E_core"])) < 1e-10 and w2.size() == 2
+    three = ["222000", "22ud00", "222000"]
+    E3, w3 = calc.create("projected_multi_configuration_calculator").run(ham, three)
+    a3 = np.array([det.from_canonical_string(s)[0] for s in three], np.uint64)
+    b3 = np.array([det.from_canonical_string(s)[1] for s in three], np.uint64)
+    assert w3.size() == 3 and abs(E3 - (np.linalg.eigvalsh(dense(a3, b3))[0] + n2_6e6o["E_core"])) < 1e-10
