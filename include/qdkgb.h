@@ -63,6 +63,10 @@ const char* qdkgb_last_error(const qdkgb_context* ctx);
 int qdkgb_set_stream(qdkgb_context* ctx, void* stream);
 /* Bytes of device memory currently held by the context. */
 int qdkgb_device_bytes(const qdkgb_context* ctx, int64_t* bytes);
+/* Caps the device memory the context may hold (0: no cap): an allocation that
+ * would pass it fails with QDKGB_ERR_OOM before reaching the device, and the
+ * context stays usable.  The capped allocator behind the out-of-memory tests. */
+int qdkgb_set_device_limit(qdkgb_context* ctx, int64_t bytes);
 
 /* Storage of the operator the last build produced (no counterpart in the
  * reference, whose operator is always a sparsexx::csr_matrix):

@@ -32,7 +32,7 @@ OP_NONE, OP_CSR, OP_SLAB, OP_DIRECT = 0, 1, 2, 3
 
 EXPORTED = [
     "qdkgb_create", "qdkgb_destroy", "qdkgb_last_error", "qdkgb_set_stream", "qdkgb_device_bytes",
-    "qdkgb_operator_layout",
+    "qdkgb_set_device_limit", "qdkgb_operator_layout",
     "qdkgb_set_integrals", "qdkgb_fci_dets", "qdkgb_set_dets", "qdkgb_build_hamiltonian", "qdkgb_get_csr32",
     "qdkgb_get_csr64", "qdkgb_diagonal", "qdkgb_spmv", "qdkgb_spmv_device", "qdkgb_davidson_default_settings",
     "qdkgb_davidson", "qdkgb_rdms_spin_dep", "qdkgb_orbital_entropies", "qdkgb_casci",
@@ -123,6 +123,7 @@ def lib():
     L.qdkgb_last_error.restype = ctypes.c_char_p
     L.qdkgb_set_stream.argtypes = [vp, vp]
     L.qdkgb_device_bytes.argtypes = [vp, P(i64)]
+    L.qdkgb_set_device_limit.argtypes = [vp, i64]
     L.qdkgb_operator_layout.argtypes = [vp, P(ctypes.c_int), P(i64)]
     L.qdkgb_set_integrals.argtypes = [vp, ci, vp, vp, ci]
     L.qdkgb_fci_dets.argtypes = [ci, ci, ci, vp, vp, P(i64)]
@@ -293,6 +294,11 @@ class Context:
         b = ctypes.c_int64()
         self._check(lib().qdkgb_device_bytes(self._h, ctypes.byref(b)))
         return b.value
+
+    def set_device_limit(self, nbytes):
+        """Cap the device memory the context may hold (0: no cap); a larger
+        allocation raises QdkgbError(ERR_OOM) and the context stays usable."""
+        self._check(lib().qdkgb_set_device_limit(self._h, int(nbytes)))
 
     def operator_layout(self):
         """(layout, stored elements): OP_CSR, OP_SLAB (complete space, values

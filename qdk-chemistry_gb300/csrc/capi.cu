@@ -36,6 +36,9 @@ void set_max_dynamic_smem(const void* func, int bytes) {
 void* dev_alloc(Context* c, DeviceBuffer& b, size_t bytes) {
   if (b.ptr && b.bytes >= bytes) return b.ptr;
   dev_free(c, b);
+  if (c->dev_limit > 0 && c->dev_bytes + (int64_t)bytes > c->dev_limit)
+    throw Error(QDKGB_ERR_OOM, "device memory limit of " + std::to_string(c->dev_limit) + " bytes reached (" +
+                                   std::to_string(c->dev_bytes) + " held, " + std::to_string(bytes) + " asked)");
   void* p = nullptr;
   cudaError_t e = cudaMalloc(&p, std::max<size_t>(bytes, 16));
   if (e != cudaSuccess) {
@@ -209,6 +212,12 @@ int qdkgb_set_stream(qdkgb_context* c, void* stream) {
     QDKGB_CUDA(cudaStreamSynchronize(c->stream));
     c->stream = stream ? (cudaStream_t)stream : c->own_stream;
   });
+}
+
+int qdkgb_set_device_limit(qdkgb_context* c, int64_t bytes) {
+  if (!c || bytes < 0) return QDKGB_ERR_INVALID;
+  c->dev_limit = bytes;
+  return QDKGB_OK;
 }
 
 int qdkgb_device_bytes(const qdkgb_context* c, int64_t* bytes) {

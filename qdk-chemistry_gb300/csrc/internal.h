@@ -110,6 +110,7 @@ struct Context {
   cudaStream_t own_stream = nullptr, stream = nullptr;
   std::string err;
   int64_t dev_bytes = 0;
+  int64_t dev_limit = 0;  // cap on dev_bytes (0: none), set by qdkgb_set_device_limit
   int sm_count = 0;
   // integrals
   int norb = 0;

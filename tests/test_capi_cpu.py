@@ -50,6 +50,7 @@ def test_null_context_is_an_error_not_a_crash(capi):
     L = capi.lib()
     assert L.qdkgb_set_dets(None, 1, None, None) == capi.ERR_INVALID
     assert L.qdkgb_build_hamiltonian(None, 0.0, 0, None) == capi.ERR_INVALID
+    assert L.qdkgb_set_device_limit(None, 1 << 20) == capi.ERR_INVALID
     assert L.qdkgb_destroy(None) == capi.OK
 
 

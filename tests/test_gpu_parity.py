@@ -287,3 +287,25 @@ def test_casci_reuses_the_complete_space(ctx, oracle, pkg):
         if seed == 22:
             # a selected list in between must not be mistaken for the space
             ctx.set_dets(a[:100], b[:100])
+
+
+def test_device_limit_gives_oom_and_the_context_recovers(pkg, oracle):
+    """Failure detection with the capped allocator (qdkgb_set_device_limit):
+    a Hamiltonian build that needs more device memory than the cap fails with
+    QDKGB_ERR_OOM before reaching the device; with the cap lifted the same
+    context builds and solves to the oracle's energy."""
+    capi = pkg.capi
+    T, V, _ = pkg.integrals.synthetic_integrals(8, 16, 21)
+    a, b = capi.fci_dets(8, 4, 4)
+    with capi.Context(0) as ctx:
+        ctx.set_integrals(T, V)
+        ctx.set_dets(a, b)
+        ctx.set_device_limit(ctx.device_bytes() + 4096)
+        with pytest.raises(capi.QdkgbError) as ei:
+            ctx.build_hamiltonian()
+        assert ei.value.code == capi.ERR_OOM and "limit" in str(ei.value)
+        ctx.set_device_limit(0)
+        ctx.build_hamiltonian()
+        E, _, _ = ctx.davidson(tol=1e-10)
+    Eo, _, _ = oracle.build_csr(oracle.Hamiltonian(T, V), a, b).selected_ci_diag(tol=1e-10)
+    assert abs(E - Eo) < 1e-10
