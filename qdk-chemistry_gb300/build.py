@@ -61,7 +61,8 @@ def build(force=False, verbose=False, ptxas_info=False):
                 print(err)
     objs = [o for o, _ in results]
     tmp = LIB + ".tmp"
-    cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs]
+    # -ldl: the NVTX ranges load an attached tool with dlopen
+    cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-ldl"]
     subprocess.check_call(cmd)
     os.replace(tmp, LIB)
     return LIB

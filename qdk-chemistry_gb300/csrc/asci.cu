@@ -493,6 +493,7 @@ double distinct_targets(Context* c, const CoreArgs& A, unsigned* regs) {
 void asci_search_gpu(Context* c, int64_t ncore, const uint64_t* ca, const uint64_t* cb, const double* cc, double E0,
                      int64_t ndets_max, double h_el_tol, double rv_prune_tol, std::vector<uint64_t>& out_a,
                      std::vector<uint64_t>& out_b, int64_t* n_candidates, bool just_singles) {
+  NvtxRange nvtx_range("qdkgb.asci_search");
   if (!c->have_ints) throw Error(QDKGB_ERR_STATE, "integrals not set");
   if (ncore <= 0) throw Error(QDKGB_ERR_INVALID, "empty core");
   const int n = c->norb;
@@ -637,6 +638,7 @@ void asci_search_gpu(Context* c, int64_t ncore, const uint64_t* ca, const uint64
 // either split, so the sums are the same.
 double asci_pt2_gpu(Context* c, int64_t nd, const uint64_t* a, const uint64_t* b, const double* C, double E0,
                     double pt2_tol, int64_t max_slots, int64_t* npt2) {
+  NvtxRange nvtx_range("qdkgb.asci_pt2");
   if (!c->have_ints) throw Error(QDKGB_ERR_STATE, "integrals not set");
   if (nd <= 0) throw Error(QDKGB_ERR_INVALID, "empty wavefunction");
   for (int64_t i = 1; i < nd; ++i)
@@ -770,6 +772,7 @@ double sci_diag_gpu(Context* c, const qdkgb_asci_settings& S, const qdkgb_davids
 double asci_iter_gpu(Context* c, const qdkgb_asci_settings& S, const qdkgb_davidson_settings& ci, double matel_tol,
                      int64_t ndets_max, double E0, std::vector<HDet>& wfn, std::vector<double>& X,
                      int64_t* ncand) {
+  NvtxRange nvtx_range("qdkgb.asci_iter");
   if (wfn.size() > 1) {  // reorder_ci_on_coeff (determinant_sort.hpp:45-64)
     std::vector<size_t> idx(wfn.size());
     for (size_t i = 0; i < idx.size(); ++i) idx[i] = i;

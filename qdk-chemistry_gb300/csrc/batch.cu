@@ -543,6 +543,7 @@ struct Shape {
 // spin-summed 1-RDM of instance i at rdm1 + sum_{j<i} norb_j^2.
 void casci_batch(Context* ctx, int ninst, const qdkgb_cas_instance* inst, const qdkgb_batch_settings& st,
                  double* energies, double* rdm1, int* iters, qdkgb_batch_info* info) {
+  NvtxRange nvtx_range("qdkgb.casci_batch");
   const auto t_start = std::chrono::steady_clock::now();
   if (ninst < 0) throw Error(QDKGB_ERR_INVALID, "negative instance count");
   if (st.max_subspace < 2 || st.max_subspace > 64) throw Error(QDKGB_ERR_INVALID, "max_subspace must be in [2, 64]");

@@ -600,6 +600,7 @@ struct Dav {
 }  // namespace
 
 void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C, qdkgb_davidson_info* info) {
+  NvtxRange nvtx_range("qdkgb.davidson");
   using clk = std::chrono::steady_clock;
   const auto t0 = clk::now();
   Hcsr& H = c->H;

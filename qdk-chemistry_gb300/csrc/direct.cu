@@ -342,6 +342,7 @@ __global__ void k_diag_product(Integrals I, int64_t na, int64_t nb, const uint64
 }
 
 void build_direct_sigma(Context* c) {
+  NvtxRange nvtx_range("qdkgb.build_direct_sigma");
   if (!c->have_ints) throw Error(QDKGB_ERR_STATE, "integrals not set");
   if (!c->have_dets) throw Error(QDKGB_ERR_STATE, "determinants not set");
   DetSpace& S = c->dets;

@@ -244,6 +244,7 @@ static void build_conn(Context* c, const uint64_t* d_s, int64_t m, int maxbits, 
 // (generate_hilbert_space), and a topological order of the per-group
 // successions.
 void build_det_space(Context* c, int64_t nd, const uint64_t* alpha, const uint64_t* beta) {
+  NvtxRange nvtx_range("qdkgb.set_dets");
   DetSpace& D = c->dets;
   for (DeviceBuffer* b : {&D.galpha, &D.gstart, &D.det_group, &D.brank, &D.ubeta, &D.gcomplete, &D.acon_ptr,
                           &D.acon_idx, &D.acon_lvl, &D.b2_ptr, &D.b2_idx, &D.b1_ptr, &D.b1_idx})
@@ -645,6 +646,7 @@ void check_dets_in_orbitals(const Context* c) {
 }
 
 void build_hamiltonian(Context* c, double thresh, int storage) {
+  NvtxRange nvtx_range("qdkgb.build_hamiltonian");
   if (!c->have_ints) throw Error(QDKGB_ERR_STATE, "integrals not set");
   if (!c->have_dets) throw Error(QDKGB_ERR_STATE, "determinants not set");
   check_dets_in_orbitals(c);

@@ -7,9 +7,21 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/qdkgb.h"
 
 namespace qdkgb {
+
+// A named NVTX range over a scope: the library's phases (determinant space,
+// H build, Davidson, RDMs, ASCI steps, PT2, CASSCF iterations) appear on the
+// Nsight timelines; without an attached tool the calls return at once.
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 // Thrown inside the library, converted to a status code at the C ABI.
 struct Error : std::runtime_error {

@@ -187,6 +187,7 @@ struct SubContext {
 double casscf(Context* c, const qdkgb_mcscf_settings& S, int nalpha, int nbeta, int norb, int ninact, int nact,
               double E_core, const double* T0, const double* V0, double* A1, double* A2, double* U_out,
               int64_t* iterations, int* converged_out) {
+  NvtxRange nvtx_range("qdkgb.casscf");
   const int no = norb, ni = ninact, na = nact, nv = norb - ninact - nact;
   if (no < 1 || no > 64 || ni < 0 || na < 1 || nv < 0) throw Error(QDKGB_ERR_INVALID, "bad orbital partition");
   if (nalpha < 0 || nbeta < 0 || nalpha > na || nbeta > na) throw Error(QDKGB_ERR_INVALID, "bad active electron count");

@@ -183,6 +183,7 @@ __global__ void __launch_bounds__(kRdmWarps * 32)
 }
 
 void rdms_spin_dep(Context* c, const double* C, double* aa, double* bb, double* aaaa, double* bbbb, double* aabb) {
+  NvtxRange nvtx_range("qdkgb.rdms");
   if (!c->have_ints) throw Error(QDKGB_ERR_STATE, "integrals not set (needed for the orbital count)");
   check_dets_in_orbitals(c);
   const int n = c->norb;
@@ -425,6 +426,7 @@ inline void add_entropy_2x2(double& s, double a, double b, double d) {
 }  // namespace
 
 void orbital_entropies(Context* c, const double* C, double* s1, double* s2, double* mi) {
+  NvtxRange nvtx_range("qdkgb.orbital_entropies");
   if (!c->have_ints) throw Error(QDKGB_ERR_STATE, "integrals not set (needed for the orbital count)");
   if (!c->have_dets) throw Error(QDKGB_ERR_STATE, "determinants not set");
   check_dets_in_orbitals(c);
