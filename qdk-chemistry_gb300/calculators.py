@@ -28,7 +28,9 @@ class SettingsAreLocked(RuntimeError):
 
 
 class Settings:
-    """Typed settings with defaults and optional bounds (data::Settings)."""
+    """Typed settings with defaults and optional constraints (data::Settings):
+    a (lo, hi) tuple bounds a number (BoundConstraint), a list names the
+    allowed values (ListConstraint)."""
 
     def __init__(self):
         self._values = {}
@@ -57,7 +59,10 @@ class Settings:
             raise TypeError("setting '%s' expects str" % key)
         v = typ(value)
         b = self._bounds.get(key)
-        if b is not None:
+        if isinstance(b, list):
+            if v not in b:
+                raise ValueError("setting '%s' = %r not one of %r" % (key, v, b))
+        elif b is not None:
             lo, hi = b
             if not (lo <= v <= hi):
                 raise ValueError("setting '%s' = %r outside [%r, %r]" % (key, v, lo, hi))
@@ -108,7 +113,8 @@ class Gb300Settings(MultiConfigurationSettings):
         super().__init__()
         self.set_default("ci_matel_tol", float, np.finfo(np.float64).eps,
                          "Hamiltonian matrix element sparsification threshold", (0.0, 1.0))
-        self.set_default("precision", str, "fp64", "fp64 or mixed (FP32 sigma with FP64 defect correction)")
+        self.set_default("precision", str, "fp64", "fp64 or mixed (FP32 sigma with FP64 defect correction)",
+                         ["fp64", "mixed"])
         self.set_default("device", int, 0, "CUDA device ordinal", (0, 1024))
 
 
@@ -463,7 +469,8 @@ class Gb300AsciSettings(Gb300Settings):
         self.set_default("growth_backoff_rate", float, 0.5, "grow factor backoff", (0.0, 1.0))
         self.set_default("growth_recovery_rate", float, 1.1, "grow factor recovery", (1.0, 1e6))
         self.set_default("max_refine_iter", int, 6, "maximum refinement iterations", (0, 2 ** 63 - 1))
-        self.set_default("core_selection_strategy", str, "percentage", "'percentage' or 'fixed'")
+        self.set_default("core_selection_strategy", str, "percentage", "'percentage' or 'fixed'",
+                         ["percentage", "fixed"])
         self.set_default("core_selection_threshold", float, 0.95, "core weight fraction", (0.0, 1.0))
         self.set_default("warm_start_davidson", bool, True)
         self.set_default("min_warm_start_overlap", float, 0.5, "", (0.0, 1.0))

@@ -406,3 +406,16 @@ def test_pmc_repeated_flow_on_oracle_device(pkg, oracle, n2_6e6o, monkeypatch):
     a3 = np.array([det.from_canonical_string(s)[0] for s in three], np.uint64)
     b3 = np.array([det.from_canonical_string(s)[1] for s in three], np.uint64)
     assert w3.size() == 3 and abs(E3 - (np.linalg.eigvalsh(dense(a3, b3))[0] + n2_6e6o["E_core"])) < 1e-10
+
+
+def test_list_constrained_settings(pkg):
+    """ListConstraint settings (macis_asci.hpp:141-145 for
+    core_selection_strategy) refuse other values when set."""
+    s = pkg.calculators.create("multi_configuration_calculator", "gb300_asci").settings()
+    with pytest.raises(ValueError, match="not one of"):
+        s.set("core_selection_strategy", "bogus")
+    with pytest.raises(ValueError, match="not one of"):
+        s.set("precision", "fp16")
+    s.set("core_selection_strategy", "fixed")
+    s.set("precision", "mixed")
+    assert (s.get("core_selection_strategy"), s.get("precision")) == ("fixed", "mixed")
