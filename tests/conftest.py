@@ -14,6 +14,18 @@ if ROOT not in sys.path:
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300) and the built sm_103a library")
+    config.addinivalue_line("markers", "late: tests of the newest entry points, run after the others")
+
+
+def pytest_collection_modifyitems(config, items):
+    """Tests marked late run after the rest (before test_zz_no_alloc.py, which
+    is collected last on purpose), so that under -x a failure in one of them
+    leaves every other result in place."""
+    def rank(item):
+        if item.nodeid.startswith("tests/test_zz_") or "/test_zz_" in item.nodeid:
+            return 2
+        return 1 if item.get_closest_marker("late") else 0
+    items[:] = sorted(items, key=rank)
 
 
 def load_package():

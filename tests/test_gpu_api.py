@@ -60,6 +60,7 @@ def test_davidson_solver_on_scipy_csr(pkg, oracle, h2o, known):
     assert abs(X @ (A @ X) - E) < 1e-10
 
 
+@pytest.mark.late
 def test_davidson_solver_reference_cases(pkg):
     """python/tests/test_davidson_solver.py:17-71 on the GPU: davidson_solver
     with its defaults (tol 1e-8, max_m 20) on the 6 x 6 tridiagonal and the

@@ -66,6 +66,7 @@ def test_asci_n2_golden(ctx, pkg, oracle, n2_14e18o, known):
     assert len(a) == ref["ndets"]
 
 
+@pytest.mark.late
 def test_asci_just_singles_and_taper_match_oracle(ctx, pkg, oracle, h2o):
     """The search's just_singles (determinant_search.hpp:274-296) and the
     grow's taper_grow_factor (grow.hpp:97-107) on the GPU against the oracle:

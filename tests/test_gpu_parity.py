@@ -289,6 +289,7 @@ def test_casci_reuses_the_complete_space(ctx, oracle, pkg):
             ctx.set_dets(a[:100], b[:100])
 
 
+@pytest.mark.late
 def test_device_limit_gives_oom_and_the_context_recovers(pkg, oracle):
     """Failure detection with the capped allocator (qdkgb_set_device_limit):
     a Hamiltonian build that needs more device memory than the cap fails with

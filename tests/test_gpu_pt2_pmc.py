@@ -92,6 +92,7 @@ def test_pmc_matches_oracle(pkg, oracle, n2_6e6o):
     assert w1.coefficients.tolist() == [1.0]
 
 
+@pytest.mark.late
 def test_pmc_repeated_configurations(pkg, oracle, n2_6e6o):
     """A configuration list that repeats determinants (test_pmc.py:104-141
     passes "222000" twice): the energy and vector are the lowest eigenpair of
