@@ -27,6 +27,10 @@ class SettingsAreLocked(RuntimeError):
     pass
 
 
+class DuplicateRegistrationError(RuntimeError):
+    pass
+
+
 class Settings:
     """Typed settings with defaults and optional constraints (data::Settings):
     a (lo, hi) tuple bounds a number (BoundConstraint), a list names the
@@ -968,13 +972,26 @@ _DEFAULT = {"multi_configuration_calculator": "gb300_cas",
             "active_space_selector": "gb300_autocas"}
 
 
-def register(kind, factory):
-    """register_instance (algorithm.hpp:310): keyed by the instance's name()."""
-    inst = factory()
-    _REGISTRY.setdefault(kind, {})[inst.name()] = factory
+def register(generator):
+    """register (python/src/qdk_chemistry/algorithms/registry.py:496-538,
+    register_instance algorithm.hpp:310): the algorithm type and name come from
+    an instance; a name already taken raises DuplicateRegistrationError, an
+    unknown type KeyError."""
+    inst = generator()
+    kind = inst.type_name()
+    if kind not in _REGISTRY:
+        raise KeyError("Algorithm type '%s' is not registered. Available algorithm types: %s"
+                       % (kind, ", ".join(sorted(_REGISTRY))))
+    if inst.name() in _REGISTRY[kind]:
+        raise DuplicateRegistrationError("'%s' is already registered as a %s" % (inst.name(), kind))
+    _REGISTRY[kind][inst.name()] = generator
 
 
-def available(kind="multi_configuration_calculator"):
+def available(kind=None):
+    """The registered names of one algorithm type, or a dict over all types
+    (registry.py available)."""
+    if kind is None:
+        return {k: sorted(v) for k, v in _REGISTRY.items()}
     return sorted(_REGISTRY.get(kind, {}))
 
 

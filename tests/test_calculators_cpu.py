@@ -6,7 +6,9 @@ import pytest
 
 def test_registry_and_defaults(pkg):
     calc = pkg.calculators
-    assert "gb300_cas" in calc.available() and "gb300_asci" in calc.available()
+    kinds = calc.available()
+    assert kinds["multi_configuration_calculator"] == ["gb300_asci", "gb300_cas"]
+    assert calc.available("multi_configuration_calculator") == ["gb300_asci", "gb300_cas"]
     c = calc.create("multi_configuration_calculator")
     assert c.name() == "gb300_cas"
     s = c.settings()
@@ -419,3 +421,30 @@ def test_list_constrained_settings(pkg):
     s.set("core_selection_strategy", "fixed")
     s.set("precision", "mixed")
     assert (s.get("core_selection_strategy"), s.get("precision")) == ("fixed", "mixed")
+
+
+def test_register_custom_algorithm(pkg, monkeypatch):
+    """registry.register (registry.py:496-538): type and name from the
+    instance; a taken name raises DuplicateRegistrationError; an unknown type
+    raises KeyError."""
+    calc = pkg.calculators
+    monkeypatch.setattr(calc, "_REGISTRY", {k: dict(v) for k, v in calc._REGISTRY.items()})
+
+    class MyCas(calc.Gb300Cas):
+        def name(self):
+            return "my_cas"
+
+    calc.register(lambda: MyCas())
+    assert "my_cas" in calc.available("multi_configuration_calculator")
+    assert isinstance(calc.create("multi_configuration_calculator", "my_cas"), MyCas)
+    with pytest.raises(calc.DuplicateRegistrationError):
+        calc.register(lambda: MyCas())
+    with pytest.raises(calc.DuplicateRegistrationError):
+        calc.register(lambda: calc.Gb300Pmc())
+
+    class Odd(calc.Gb300Cas):
+        def type_name(self):
+            return "no_such_type"
+
+    with pytest.raises(KeyError):
+        calc.register(lambda: Odd())
