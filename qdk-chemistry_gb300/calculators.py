@@ -969,7 +969,7 @@ _REGISTRY = {"multi_configuration_calculator": {"gb300_cas": Gb300Cas, "gb300_as
              "active_space_selector": {"gb300_autocas": Gb300Autocas, "gb300_autocas_eos": Gb300AutocasEos}}
 _DEFAULT = {"multi_configuration_calculator": "gb300_cas",
             "projected_multi_configuration_calculator": "gb300_pmc",
-            "active_space_selector": "gb300_autocas"}
+            "active_space_selector": "gb300_autocas_eos"}
 
 
 def register(generator):
@@ -995,14 +995,34 @@ def available(kind=None):
     return sorted(_REGISTRY.get(kind, {}))
 
 
-def create(kind, name=None):
-    """create(kind, name) (registry.py:295); the default name as mc.hpp:213."""
+def create(kind, name=None, **settings):
+    """create(kind, name, **settings) (registry.py:295-372): the default name
+    of the type when none is given (mc.hpp:213, pmc.hpp:186,
+    active_space.hpp:206), then the keyword settings applied."""
     if kind not in _REGISTRY:
         raise KeyError("unknown algorithm type '%s'" % kind)
     name = name or _DEFAULT.get(kind)
     if name not in _REGISTRY[kind]:
         raise KeyError("no '%s' named '%s' (available: %s)" % (kind, name, ", ".join(available(kind))))
-    return _REGISTRY[kind][name]()
+    alg = _REGISTRY[kind][name]()
+    for key, value in settings.items():
+        alg.settings().set(key, value)
+    return alg
+
+
+def show_default(kind=None):
+    """The default name of one algorithm type ('' for an unknown one), or a
+    dict over all types (registry.py:593-632)."""
+    if kind is None:
+        return dict(_DEFAULT)
+    return _DEFAULT.get(kind, "")
+
+
+def unregister(kind, name):
+    """Remove a registered implementation (registry.py:635-663)."""
+    if kind not in _REGISTRY or name not in _REGISTRY[kind]:
+        raise KeyError("no '%s' named '%s' is registered" % (kind, name))
+    del _REGISTRY[kind][name]
 
 
 def davidson_solver(csr_matrix, tol=1e-8, max_m=20, device=0):

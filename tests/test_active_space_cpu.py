@@ -29,8 +29,9 @@ ACTIVE = list(range(2, 10))
 def test_registry_and_settings(pkg):
     calc = pkg.calculators
     assert calc.available("active_space_selector") == ["gb300_autocas", "gb300_autocas_eos"]
-    sel = calc.create("active_space_selector")
-    assert sel.name() == "gb300_autocas" and sel.type_name() == "active_space_selector"
+    assert calc.create("active_space_selector").name() == "gb300_autocas_eos"  # active_space.hpp:206
+    sel = calc.create("active_space_selector", "gb300_autocas")
+    assert sel.type_name() == "active_space_selector"
     s = sel.settings()
     assert (s.get("num_bins"), s.get("min_plateau_size"), s.get("entropy_threshold"),
             s.get("normalize_entropies")) == (100, 10, 0.14, True)
@@ -49,15 +50,15 @@ def test_autocas_plateaus(pkg):
     at least 20 only the 5-run (59 bins) is a plateau; with at least 60 none."""
     calc = pkg.calculators
     w = _wfn(calc, PROFILE, ACTIVE, [0, 1])
-    out = calc.create("active_space_selector").run(w)
+    out = calc.create("active_space_selector", "gb300_autocas").run(w)
     assert out.get_active_indices() == [2, 3, 4, 5, 8, 9]
     # aufbau 3 + 3 over orbitals 2 .. 9, truncated: orbitals 2, 3, 4 doubly occupied
     assert out.size() == 1 and int(out.alpha[0]) == 0b000111 and int(out.beta[0]) == 0b000111
     assert out.get_inactive_indices() == [0, 1]
-    s = calc.create("active_space_selector")
+    s = calc.create("active_space_selector", "gb300_autocas")
     s.settings().set("min_plateau_size", 20)
     assert s.select(w) == [2, 3, 4, 5, 9]
-    s = calc.create("active_space_selector")
+    s = calc.create("active_space_selector", "gb300_autocas")
     s.settings().set("min_plateau_size", 60)
     assert s.select(w) == []
 
@@ -65,11 +66,11 @@ def test_autocas_plateaus(pkg):
 def test_autocas_single_reference_and_raw_entropies(pkg):
     calc = pkg.calculators
     small = [0.1, 0.05, 0.02, 0.01, 0.0, 0.0, 0.0, 0.0]  # max 0.1 < 0.14
-    out = calc.create("active_space_selector").run(_wfn(calc, small, ACTIVE, [0, 1]))
+    out = calc.create("active_space_selector", "gb300_autocas").run(_wfn(calc, small, ACTIVE, [0, 1]))
     assert out.get_active_indices() == [] and out.norb == 0
     assert out.get_inactive_indices() == [0, 1, 2, 3, 4]
     # unnormalised: raw entropies above 1 count in every bin (no plateau change)
-    s = calc.create("active_space_selector")
+    s = calc.create("active_space_selector", "gb300_autocas")
     s.settings().set("normalize_entropies", False)
     raw = [1.5, 1.4, 0.305, 0.295, 0.0, 0.0, 0.0, 0.0]
     # counts: bins 0-29 -> 4, 30 -> 3, 31-99 -> 2: plateaus of 30 and 69 bins
@@ -100,7 +101,7 @@ def test_errors(pkg):
     calc = pkg.calculators
     bare = calc.Wavefunction(8, np.array([7], np.uint64), np.array([7], np.uint64), np.ones(1))
     with pytest.raises(RuntimeError, match="does not have single orbital entropies"):
-        calc.create("active_space_selector").run(bare)
+        calc.create("active_space_selector", "gb300_autocas").run(bare)
     with pytest.raises(RuntimeError, match="outside of initial active space"):
         calc.selected_active_wavefunction(_wfn(calc, PROFILE, ACTIVE, []), [1, 2])
     with pytest.raises(ValueError):

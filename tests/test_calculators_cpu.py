@@ -448,3 +448,22 @@ def test_register_custom_algorithm(pkg, monkeypatch):
 
     with pytest.raises(KeyError):
         calc.register(lambda: Odd())
+
+
+def test_create_with_settings_show_default_unregister(pkg, monkeypatch):
+    """registry.create(type, name, **settings), show_default and unregister
+    (registry.py:295-372, 593-663)."""
+    calc = pkg.calculators
+    monkeypatch.setattr(calc, "_REGISTRY", {k: dict(v) for k, v in calc._REGISTRY.items()})
+    c = calc.create("multi_configuration_calculator", "gb300_cas", ci_residual_tolerance=1e-9, calculate_one_rdm=True)
+    assert c.settings().get("ci_residual_tolerance") == 1e-9 and c.settings().get("calculate_one_rdm") is True
+    with pytest.raises(KeyError):
+        calc.create("multi_configuration_calculator", "gb300_cas", no_such_setting=1)
+    assert calc.show_default() == {"multi_configuration_calculator": "gb300_cas",
+                                   "projected_multi_configuration_calculator": "gb300_pmc",
+                                   "active_space_selector": "gb300_autocas_eos"}
+    assert calc.show_default("active_space_selector") == "gb300_autocas_eos" and calc.show_default("nope") == ""
+    calc.unregister("multi_configuration_calculator", "gb300_asci")
+    assert calc.available("multi_configuration_calculator") == ["gb300_cas"]
+    with pytest.raises(KeyError):
+        calc.unregister("multi_configuration_calculator", "gb300_asci")
