@@ -1,10 +1,10 @@
 """qdk-chemistry's multi-configuration plugin surface, backed by the GB300 core.
 
 Mirrors, with the same names, defaults and error behaviour:
-* the algorithm registry: ``create("multi_configuration_calculator", name)``,
-  ``available(...)``, ``register(...)``
-  (python/src/qdk_chemistry/algorithms/registry.py:295,
-  cpp/include/qdk/chemistry/algorithms/algorithm.hpp:242-369);
+* the algorithm registry: ``create(type, name, **settings)``,
+  ``available(...)``, ``register(generator)``, ``unregister(...)``,
+  ``show_default(...)`` (python/src/qdk_chemistry/algorithms/registry.py:
+  295-663, cpp/include/qdk/chemistry/algorithms/algorithm.hpp:242-369);
 * ``MultiConfigurationSettings`` + the MACIS settings
   (cpp/include/qdk/chemistry/algorithms/mc.hpp:26-62,
   cpp/src/qdk/chemistry/algorithms/microsoft/macis_base.hpp:27-36): typed
@@ -14,6 +14,8 @@ Mirrors, with the same names, defaults and error behaviour:
   (macis_cas.cpp:35-148) and the ASCI plugin (macis_asci.cpp:44-234);
 * ``ProjectedMultiConfigurationCalculator.run(hamiltonian, configurations)``
   (pmc.hpp:31-150) and the PMC plugin (macis_pmc.cpp:42-178);
+* the entropy-based active-space selectors over the wavefunction's
+  entropies (autocas_active_space.cpp, entropy_active_space.cpp);
 * ``davidson_solver(csr, tol=1e-8, max_m=20) -> (eigenvalue, eigenvector)``
   (python/src/pybind11/algorithms/davidson_solver.cpp:56-108).
 All computation runs in libqdkgb.so on the GPU.
