@@ -80,6 +80,26 @@ class Settings:
     def get_or_default(self, key, default):
         return self._values.get(key, default)
 
+    def update(self, values=None, **kw):
+        """Set several settings at once (each checked as by set)."""
+        for key, value in dict(values or {}, **kw).items():
+            self.set(key, value)
+
+    def get_expected_python_type(self, key):
+        return self._types[key].__name__
+
+    def has_description(self, key):
+        return bool(self._doc.get(key))
+
+    def get_description(self, key):
+        return self._doc[key]
+
+    def has_limits(self, key):
+        return self._bounds.get(key) is not None
+
+    def get_limits(self, key):
+        return self._bounds[key]
+
     def has(self, key):
         return key in self._values
 
@@ -1010,6 +1030,15 @@ def create(kind, name=None, **settings):
     for key, value in settings.items():
         alg.settings().set(key, value)
     return alg
+
+
+def inspect_settings(kind, name):
+    """The settings schema of one implementation (registry.py:428-494): a
+    (name, python type, default, description or None, limits or None) tuple
+    per setting."""
+    s = create(kind, name).settings()
+    return [(k, s.get_expected_python_type(k), s.get(k), s.get_description(k) if s.has_description(k) else None,
+             s.get_limits(k) if s.has_limits(k) else None) for k in s.keys()]
 
 
 def show_default(kind=None):

@@ -467,3 +467,17 @@ def test_create_with_settings_show_default_unregister(pkg, monkeypatch):
     assert calc.available("multi_configuration_calculator") == ["gb300_cas"]
     with pytest.raises(KeyError):
         calc.unregister("multi_configuration_calculator", "gb300_asci")
+
+
+def test_settings_update_and_inspect(pkg):
+    """Settings.update and registry.inspect_settings (registry.py:428-494)."""
+    calc = pkg.calculators
+    s = calc.create("multi_configuration_calculator", "gb300_asci").settings()
+    s.update({"ntdets_max": 500}, grow_factor=4.0)
+    assert s.get("ntdets_max") == 500 and s.get("grow_factor") == 4.0
+    with pytest.raises(ValueError):
+        s.update(grow_factor=0.5)
+    rows = {r[0]: r for r in calc.inspect_settings("multi_configuration_calculator", "gb300_asci")}
+    assert rows["ntdets_max"][1:3] == ("int", 100000) and rows["ntdets_max"][3] == "Maximum number of determinants"
+    assert rows["core_selection_strategy"][4] == ["percentage", "fixed"]
+    assert rows["just_singles"][3] is None and rows["just_singles"][4] is None
