@@ -229,6 +229,15 @@ class Wavefunction:
     def get_coefficients(self):
         return self.coefficients
 
+    def to_macis_file(self, path):
+        """MACIS's text wavefunction (write_wavefunction, wavefunction_io.hpp:95-116)."""
+        determinants.write_wavefunction(path, self.norb, self.alpha, self.beta, self.coefficients)
+
+    @classmethod
+    def from_macis_file(cls, path):
+        a, b, c, norb, _, _ = determinants.read_wavefunction(path)
+        return cls(norb, a, b, c)
+
     def get_active_determinants(self):
         return self.get_configurations()
 

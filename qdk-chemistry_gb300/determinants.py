@@ -105,3 +105,37 @@ def from_canonical_string(s):
         if ch in "2d":
             b |= 1 << i
     return np.uint64(a), np.uint64(b)
+
+
+def read_wavefunction(path):
+    """read_wavefunction (include/macis/wavefunction_io.hpp:40-93): the
+    header "nstates norb nalpha nbeta", then one "coefficient canonical-string"
+    line per determinant.  Returns (alpha, beta, coeffs, norb, nalpha, nbeta)."""
+    with open(path) as f:
+        head = f.readline().split()
+        if len(head) < 4:
+            raise ValueError("wavefunction file header must hold nstates norb nalpha nbeta")
+        _, norb, na, nb = (int(x) for x in head[:4])
+        a, b, c = [], [], []
+        for line in f:
+            parts = line.split()
+            if not parts:
+                continue
+            x, y = from_canonical_string(parts[1])
+            a.append(x)
+            b.append(y)
+            c.append(float(parts[0]))
+    return (np.array(a, dtype=np.uint64), np.array(b, dtype=np.uint64), np.array(c, dtype=np.float64), norb, na,
+            nb)
+
+
+def write_wavefunction(path, norb, alpha, beta, coeffs):
+    """write_wavefunction (wavefunction_io.hpp:95-116): the header from the
+    first determinant's electron counts, then each coefficient in scientific
+    notation with 16 digits (30 wide) and the determinant's canonical string."""
+    alpha = np.asarray(alpha, dtype=np.uint64)
+    beta = np.asarray(beta, dtype=np.uint64)
+    with open(path, "w") as f:
+        f.write("%d %d %d %d\n" % (len(coeffs), norb, int(alpha[0]).bit_count(), int(beta[0]).bit_count()))
+        for x, y, c in zip(alpha, beta, coeffs):
+            f.write("%30.16e %s \n" % (c, to_canonical_string(x, y, norb)))

@@ -99,3 +99,24 @@ def test_water_fcidump(pkg, oracle, h2o, known):
         - eps[o][None, None, None, :]
     emp2 = -np.sum(dir_ * (2 * dir_ - exh) / den)
     assert abs(emp2 - ref["EMP2"]) < tol
+
+
+def test_macis_wavefunction_files(pkg, tmp_path):
+    """read_wavefunction / write_wavefunction (wavefunction_io.hpp:40-116) on
+    the reference's O2 wavefunction (tests/golden/o2_wfn.npz holds its
+    determinants and coefficients): written and read back exactly, with the
+    reference's header and line layout."""
+    det = pkg.determinants
+    d = np.load(os.path.join(GOLDEN, "o2_wfn.npz"))
+    p = tmp_path / "o2.wfn.dat"
+    det.write_wavefunction(str(p), int(d["norb"]), d["alpha"], d["beta"], d["coeffs"])
+    lines = p.read_text().splitlines()
+    assert lines[0] == "%d %d %d %d" % (len(d["coeffs"]), int(d["norb"]), int(d["nalpha"]), int(d["nbeta"]))
+    assert len(lines[1]) == 30 + 1 + int(d["norb"]) + 1 and "e" in lines[1][:30]
+    a, b, c, norb, na, nb = det.read_wavefunction(str(p))
+    assert (norb, na, nb) == (int(d["norb"]), int(d["nalpha"]), int(d["nbeta"]))
+    assert np.array_equal(a, d["alpha"]) and np.array_equal(b, d["beta"]) and np.array_equal(c, d["coeffs"])
+    w = pkg.calculators.Wavefunction.from_macis_file(str(p))
+    assert w.norb == int(d["norb"]) and np.array_equal(w.coefficients, d["coeffs"])
+    w.to_macis_file(str(tmp_path / "again.dat"))
+    assert (tmp_path / "again.dat").read_text() == p.read_text()
