@@ -120,3 +120,32 @@ def write_fcidump(path, T, V, E_core=0.0, nelec=0, ms2=0, thresh=1e-16):
     lines.append("%.16e 0 0 0 0" % E_core)
     with open(path, "w") as f:
         f.write("\n".join(lines) + "\n")
+
+
+def read_rdms_binary(path, norb=None):
+    """read_rdms_binary (src/macis/fcidump.cxx:486-530): an int norb, then the
+    column-major 1-RDM (norb^2 doubles) and 2-RDM (norb^4 doubles).  Returns
+    (1-RDM [p, q], 2-RDM [p, q, r, s]) indexed as MACIS's (p, q) / (p, q, r, s);
+    a norb that differs from the file's raises RuntimeError."""
+    raw = open(path, "rb").read()
+    n = int(np.frombuffer(raw[:4], dtype=np.int32)[0])
+    if norb is not None and n != int(norb):
+        raise RuntimeError("NORB in RDM file doesn't match %d %d" % (int(norb), n))
+    vals = np.frombuffer(raw[4:], dtype=np.float64)
+    if len(vals) < n * n + n ** 4:
+        raise ValueError("RDM file holds %d values, %d expected" % (len(vals), n * n + n ** 4))
+    g = vals[:n * n].reshape((n, n), order="F").copy()
+    G = vals[n * n:n * n + n ** 4].reshape((n,) * 4, order="F").copy()
+    return g, G
+
+
+def write_rdms_binary(path, ordm, trdm):
+    """write_rdms_binary (src/macis/fcidump.cxx:532-558): the layout
+    read_rdms_binary reads."""
+    g = np.asarray(ordm, dtype=np.float64)
+    n = g.shape[0]
+    G = np.asarray(trdm, dtype=np.float64).reshape((n,) * 4)
+    with open(path, "wb") as f:
+        f.write(np.array([n], dtype=np.int32).tobytes())
+        f.write(g.ravel(order="F").tobytes())
+        f.write(G.ravel(order="F").tobytes())

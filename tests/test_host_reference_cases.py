@@ -120,3 +120,23 @@ def test_macis_wavefunction_files(pkg, tmp_path):
     assert w.norb == int(d["norb"]) and np.array_equal(w.coefficients, d["coeffs"])
     w.to_macis_file(str(tmp_path / "again.dat"))
     assert (tmp_path / "again.dat").read_text() == p.read_text()
+
+
+def test_macis_rdm_files(pkg, tmp_path):
+    """read_rdms_binary / write_rdms_binary (fcidump.cxx:486-558) on the
+    reference's water CAS(8e,8o) RDMs (tests/golden/h2o_ccpvdz_cas88_rdms.npz):
+    the file is an int32 norb and the column-major RDMs; written and read back
+    exactly; a wrong norb is refused."""
+    ints = pkg.integrals
+    d = np.load(os.path.join(GOLDEN, "h2o_ccpvdz_cas88_rdms.npz"))
+    n = int(d["nact"])
+    g0, G0 = d["ordm"].reshape(n, n, order="F"), d["trdm"].reshape((n,) * 4, order="F")
+    p = tmp_path / "rdms.bin"
+    ints.write_rdms_binary(str(p), g0, G0)
+    raw = p.read_bytes()
+    assert len(raw) == 4 + 8 * (n ** 2 + n ** 4)
+    assert raw[:4] == np.array([n], np.int32).tobytes() and raw[4:4 + 8 * n * n] == d["ordm"].tobytes()
+    g, G = ints.read_rdms_binary(str(p), n)
+    assert np.array_equal(g, g0) and np.array_equal(G, G0)
+    with pytest.raises(RuntimeError, match="NORB"):
+        ints.read_rdms_binary(str(p), n + 1)
