@@ -70,3 +70,26 @@ def test_reference_arm_runs_on_rank_zero_only(monkeypatch, capsys):
 
     assert bench.run_reference(Args()) is None
     assert not called and capsys.readouterr().out == ""
+
+
+def test_reference_arm_json_contract():
+    """bench.py --impl reference prints one JSON line with the keys of the
+    bench contract (metric, value, unit, timing, config, cpu_baseline, e2e),
+    here on a CAS(6e,6o) sample so that it runs in about a second."""
+    import json
+    import subprocess
+    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
+                          "--warmup", "0", "--norb", "6", "--nel", "6", "--nchol", "12", "--cpu-stride", "2"],
+                         capture_output=True, text=True, timeout=300, cwd=ROOT)
+    assert out.returncode == 0, out.stderr[-2000:]
+    line = json.loads(out.stdout.strip().splitlines()[-1])
+    for key in ("impl", "metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+                "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert key in line, key
+    assert line["impl"] == "reference" and line["n_gpus"] == 1 and line["steps"] == 1
+    assert line["higher_is_better"] is False and line["value"] > 0
+    assert abs(line["ms_per_step"] - line["value"] * 1e3) < 1e-6 * line["ms_per_step"]
+    cb, e2e = line["cpu_baseline"], line["e2e"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == line["value"] and cb["sample"]
+    assert e2e["value"] == line["value"] and e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
+    assert line["config"]["workload"]
