@@ -133,6 +133,18 @@ int qdkgb_build_direct_sigma(qdkgb_context* ctx);
  * _64bit_ (include/macis/hamiltonian_generator.hpp:32-294). */
 int qdkgb_get_csr32(qdkgb_context* ctx, int32_t* rowptr, int32_t* colind, double* values);
 int qdkgb_get_csr64(qdkgb_context* ctx, int64_t* rowptr, int64_t* colind, double* values);
+/* A bra block: rows [row_begin, row_end) against every ket, as
+ * make_csr_hamiltonian_block_{32,64}bit_(bra_begin, bra_end, ket_begin,
+ * ket_end, thresh) returns it for a sub-range of bras and the full ket range
+ * (include/macis/hamiltonian_generator.hpp:240-293; the distributed build,
+ * include/macis/csr_hamiltonian.hpp:102-136).  rowptr (row_end - row_begin + 1
+ * entries) starts at 0, colind holds global column indices; the element count
+ * of the block is rowptr[row_end - row_begin].  Any buffer may be NULL (not
+ * copied); call with NULL colind/values first to learn the count. */
+int qdkgb_get_csr32_rows(qdkgb_context* ctx, int64_t row_begin, int64_t row_end, int32_t* rowptr,
+                         int32_t* colind, double* values);
+int qdkgb_get_csr64_rows(qdkgb_context* ctx, int64_t row_begin, int64_t row_end, int64_t* rowptr,
+                         int64_t* colind, double* values);
 /* A caller's symmetric CSR matrix (0-based, n rows, host buffers) becomes the
  * device operator for qdkgb_spmv / qdkgb_davidson, FP64 storage.  This is the
  * entry of davidson_solver(csr, tol, max_m) (python/src/pybind11/algorithms/
@@ -349,7 +361,12 @@ int qdkgb_casci_batch(qdkgb_context* ctx, int ninst, const qdkgb_cas_instance* i
  *     device; stream is a cudaStream_t (NULL = legacy default stream).
  *   - The first call on a device looks up the scratch's device address (once
  *     per device, with that device current); make that first call before any
- *     stream capture.
+ *     stream capture.  The address is kept for the life of the process: a
+ *     cudaDeviceReset (which destroys the primary context and the array with
+ *     it) invalidates it, so do not call this entry point on a device after
+ *     resetting that device.
+ *   - A CUDA error already pending on the calling thread is reported
+ *     (QDKGB_ERR_CUDA) without launching and is not cleared.
  *   - The scratch is overwritten completely by every call, so nothing has to
  *     be cleared; all calls share it, so calls that overlap on the GPU (two
  *     streams at once) race.

@@ -34,7 +34,7 @@ EXPORTED = [
     "qdkgb_create", "qdkgb_destroy", "qdkgb_last_error", "qdkgb_set_stream", "qdkgb_device_bytes",
     "qdkgb_set_device_limit", "qdkgb_operator_layout",
     "qdkgb_set_integrals", "qdkgb_fci_dets", "qdkgb_set_dets", "qdkgb_build_hamiltonian", "qdkgb_get_csr32",
-    "qdkgb_get_csr64", "qdkgb_diagonal", "qdkgb_spmv", "qdkgb_spmv_device", "qdkgb_davidson_default_settings",
+    "qdkgb_get_csr64", "qdkgb_get_csr32_rows", "qdkgb_get_csr64_rows", "qdkgb_diagonal", "qdkgb_spmv", "qdkgb_spmv_device", "qdkgb_davidson_default_settings",
     "qdkgb_davidson", "qdkgb_rdms_spin_dep", "qdkgb_orbital_entropies", "qdkgb_casci",
     "qdkgb_mcscf_default_settings", "qdkgb_casscf", "qdkgb_version", "qdkgb_kernel_launches",
     "qdkgb_sigma_split_noalloc", "qdkgb_set_csr", "qdkgb_build_direct_sigma",
@@ -131,6 +131,8 @@ def lib():
     L.qdkgb_build_hamiltonian.argtypes = [vp, dp, ci, P(i64)]
     L.qdkgb_get_csr32.argtypes = [vp, vp, vp, vp]
     L.qdkgb_get_csr64.argtypes = [vp, vp, vp, vp]
+    L.qdkgb_get_csr32_rows.argtypes = [vp, i64, i64, vp, vp, vp]
+    L.qdkgb_get_csr64_rows.argtypes = [vp, i64, i64, vp, vp, vp]
     L.qdkgb_diagonal.argtypes = [vp, vp]
     L.qdkgb_set_csr.argtypes = [vp, i64, vp, vp, vp]
     L.qdkgb_build_direct_sigma.argtypes = [vp]
@@ -350,6 +352,18 @@ class Context:
         nz = np.zeros(nnz, dtype=np.float64)
         fn = lib().qdkgb_get_csr64 if index_bits == 64 else lib().qdkgb_get_csr32
         self._check(fn(self._h, _ptr(rp), _ptr(ci), _ptr(nz)))
+        return rp, ci, nz
+
+    def get_csr_rows(self, row_begin, row_end, index_bits=64):
+        """Rows [row_begin, row_end) of the CSR as a bra block: (rowptr from 0,
+        global colind, values)."""
+        it = np.int64 if index_bits == 64 else np.int32
+        fn = lib().qdkgb_get_csr64_rows if index_bits == 64 else lib().qdkgb_get_csr32_rows
+        rp = np.zeros(row_end - row_begin + 1, dtype=it)
+        self._check(fn(self._h, row_begin, row_end, _ptr(rp), None, None))
+        ci = np.zeros(int(rp[-1]), dtype=it)
+        nz = np.zeros(int(rp[-1]), dtype=np.float64)
+        self._check(fn(self._h, row_begin, row_end, _ptr(rp), _ptr(ci), _ptr(nz)))
         return rp, ci, nz
 
     def set_csr(self, rowptr, colind, values):

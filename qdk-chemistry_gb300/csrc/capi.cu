@@ -155,6 +155,50 @@ static void get_csr(Context* c, I* rowptr, I* colind, double* values) {
     for (int64_t i = 0; i < H.nnz; ++i) colind[i] = (I)ci[i];
 }
 
+// Rows [r0, r1) of the device CSR: rowptr (r1 - r0 + 1 entries) relative to
+// the block's first element, as a bra block of make_csr_hamiltonian_block_
+// returns it; colind are global columns.
+template <typename I>
+static void get_csr_rows(Context* c, int64_t r0, int64_t r1, I* rowptr, I* colind, double* values) {
+  Hcsr& H = c->H;
+  if (!H.valid || c->op_direct) throw Error(QDKGB_ERR_STATE, "no CSR Hamiltonian built");
+  if (r0 < 0 || r1 < r0 || r1 > H.n) throw Error(QDKGB_ERR_INVALID, "row range outside [0, ndets]");
+  std::vector<int64_t> rp(r1 - r0 + 1);
+  QDKGB_CUDA(cudaMemcpyAsync(rp.data(), (const int64_t*)H.rowptr.ptr + r0, (r1 - r0 + 1) * 8,
+                             cudaMemcpyDeviceToHost, c->stream));
+  QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+  const int64_t e0 = rp.front(), cnt = rp.back() - rp.front();
+  if (sizeof(I) == 4 && cnt > INT32_MAX) throw Error(QDKGB_ERR_UNSUPPORTED, "block nnz exceeds int32");
+  std::vector<int32_t> ci(colind ? cnt : 0);
+  DeviceBuffer cib, vb;
+  const int32_t* dci = (const int32_t*)H.colind.ptr;
+  const double* dv = (H.storage == QDKGB_H_FP64 && !H.structured) ? (const double*)H.val.ptr : nullptr;
+  if (H.structured) {
+    // slab layout: the CSR arrays are produced on the device, then sliced
+    const int64_t cap = std::max<int64_t>(H.nnz, 1);
+    int32_t* tci = dev_array<int32_t>(c, cib, cap);
+    double* tv = dev_array<double>(c, vb, cap);
+    struct_export(c, tci, tv, nullptr, nullptr);
+    dci = tci;
+    dv = tv;
+  } else if (!dv && values) {
+    double* tv = dev_array<double>(c, vb, std::max<int64_t>(H.nnz, 1));
+    csr_values_to_double(c, tv);
+    dv = tv;
+  }
+  if (colind && cnt)
+    QDKGB_CUDA(cudaMemcpyAsync(ci.data(), dci + e0, cnt * 4, cudaMemcpyDeviceToHost, c->stream));
+  if (values && cnt)
+    QDKGB_CUDA(cudaMemcpyAsync(values, dv + e0, cnt * 8, cudaMemcpyDeviceToHost, c->stream));
+  QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+  dev_free(c, cib);
+  dev_free(c, vb);
+  if (rowptr)
+    for (int64_t i = 0; i <= r1 - r0; ++i) rowptr[i] = (I)(rp[i] - e0);
+  if (colind)
+    for (int64_t i = 0; i < cnt; ++i) colind[i] = (I)ci[i];
+}
+
 extern "C" {
 
 const char* qdkgb_version(void) { return "qdkgb 0.1 (sm_103a)"; }
@@ -320,6 +364,17 @@ int qdkgb_get_csr32(qdkgb_context* c, int32_t* rowptr, int32_t* colind, double* 
 int qdkgb_get_csr64(qdkgb_context* c, int64_t* rowptr, int64_t* colind, double* values) {
   if (!c) return QDKGB_ERR_INVALID;
   return guarded(c, [&] { get_csr<int64_t>(c, rowptr, colind, values); });
+}
+
+int qdkgb_get_csr32_rows(qdkgb_context* c, int64_t r0, int64_t r1, int32_t* rowptr, int32_t* colind,
+                         double* values) {
+  if (!c) return QDKGB_ERR_INVALID;
+  return guarded(c, [&] { get_csr_rows<int32_t>(c, r0, r1, rowptr, colind, values); });
+}
+int qdkgb_get_csr64_rows(qdkgb_context* c, int64_t r0, int64_t r1, int64_t* rowptr, int64_t* colind,
+                         double* values) {
+  if (!c) return QDKGB_ERR_INVALID;
+  return guarded(c, [&] { get_csr_rows<int64_t>(c, r0, r1, rowptr, colind, values); });
 }
 
 int qdkgb_set_csr(qdkgb_context* c, int64_t n, const int64_t* rowptr, const int64_t* colind, const double* values) {

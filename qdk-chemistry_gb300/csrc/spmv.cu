@@ -266,17 +266,32 @@ extern "C" int qdkgb_sigma_split_noalloc(int64_t n, const int64_t* rowptr, const
     }
     st = d;
   }
+  // An error left pending by the caller's own earlier CUDA work stays the
+  // caller's: report it without launching and without clearing it.
+  e = cudaPeekAtLastError();
+  if (e != cudaSuccess) {
+    set_context_free_error(std::string("qdkgb_sigma_split_noalloc: a CUDA error was already pending before "
+                                       "this call (not cleared): ") + cudaGetErrorString(e));
+    return QDKGB_ERR_CUDA;
+  }
   cudaStream_t s = (cudaStream_t)stream;
   float* xh = st.scratch;
   float* xl = st.scratch + kNoAllocMaxRows;
   k_split_x<<<st.sm_count * 4, 256, 0, s>>>(x, xh, xl, n);
   count_launch();
+  e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_context_free_error(std::string("qdkgb_sigma_split_noalloc: launch of the x split failed: ") +
+                           cudaGetErrorString(e));
+    return QDKGB_ERR_CUDA;
+  }
   const unsigned blocks = (unsigned)std::min<int64_t>((n + kSpmvWarps - 1) / kSpmvWarps, (int64_t)st.sm_count * 32);
   k_spmv_split_ff<<<blocks, kSpmvWarps * 32, 0, s>>>(n, rowptr, colind, hi, lo, xh, xl, y);
   count_launch();
   e = cudaGetLastError();
   if (e != cudaSuccess) {
-    set_context_free_error(std::string("qdkgb_sigma_split_noalloc: launch failed: ") + cudaGetErrorString(e));
+    set_context_free_error(std::string("qdkgb_sigma_split_noalloc: launch of the sigma failed: ") +
+                           cudaGetErrorString(e));
     return QDKGB_ERR_CUDA;
   }
   return QDKGB_OK;

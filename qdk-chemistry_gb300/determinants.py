@@ -130,11 +130,18 @@ def read_wavefunction(path):
 
 
 def write_wavefunction(path, norb, alpha, beta, coeffs):
-    """write_wavefunction (wavefunction_io.hpp:95-116): the header from the
+    """write_wavefunction (wavefunction_io.hpp:95-116): unequal determinant and
+    coefficient counts raise "Invalid Wave Function Dimensions", an empty
+    wavefunction writes no file; otherwise the header from the
     first determinant's electron counts, then each coefficient in scientific
     notation with 16 digits (30 wide) and the determinant's canonical string."""
     alpha = np.asarray(alpha, dtype=np.uint64)
     beta = np.asarray(beta, dtype=np.uint64)
+    coeffs = np.asarray(coeffs, dtype=np.float64)
+    if not (len(alpha) == len(beta) == len(coeffs)):
+        raise RuntimeError("Invalid Wave Function Dimensions")
+    if len(alpha) == 0:
+        return  # the reference writes nothing (not even a header) for an empty wavefunction
     with open(path, "w") as f:
         f.write("%d %d %d %d\n" % (len(coeffs), norb, int(alpha[0]).bit_count(), int(beta[0]).bit_count()))
         for x, y, c in zip(alpha, beta, coeffs):

@@ -60,6 +60,35 @@ def known():
         return json.load(f)
 
 
+def _pair_k(n):
+    p, q = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
+    hi, lo = np.maximum(p, q), np.minimum(p, q)
+    return hi * (hi + 1) // 2 + lo
+
+
+def pack_eri(V):
+    """The unique elements of an 8-fold symmetric V[p, q, r, s] (canonical
+    pairs pq >= rs of canonical orbital pairs p >= q), exactly."""
+    n = V.shape[0]
+    k = _pair_k(n)
+    P = n * (n + 1) // 2
+    out = np.zeros(P * (P + 1) // 2)
+    K1 = k[:, :, None, None]
+    K2 = k[None, None, :, :]
+    hi, lo = np.maximum(K1, K2), np.minimum(K1, K2)
+    out[(hi * (hi + 1) // 2 + lo).ravel()] = np.asarray(V).ravel()
+    return out
+
+
+def unpack_eri(packed, n):
+    """Inverse of pack_eri: the full n^4 array (bitwise equal to the packed V)."""
+    k = _pair_k(n)
+    K1 = k[:, :, None, None]
+    K2 = k[None, None, :, :]
+    hi, lo = np.maximum(K1, K2), np.minimum(K1, K2)
+    return np.ascontiguousarray(packed[hi * (hi + 1) // 2 + lo])
+
+
 def load_fcidump(name):
     pkg = load_package()
     d = np.load(os.path.join(GOLDEN, name + "_fcidump.npz"))

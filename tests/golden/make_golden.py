@@ -1,8 +1,8 @@
 """Regenerate the golden fixtures in this folder from the reference checkout.
 
-Run in a container where the reference is mounted at /root/reference:
+Run where the reference checkout exists, giving its path:
 
-    python tests/golden/make_golden.py [/root/reference]
+    python tests/golden/make_golden.py REFERENCE_CHECKOUT
 
 It copies the reference's own test inputs and known answers for the CI hot
 path into compact numpy files, so that the tests never read the reference at
@@ -53,7 +53,7 @@ def parse_wfn_list(text, anchor, name):
     return [int(tok, 0) for tok in re.findall(r"0[xXbB][0-9a-fA-F]+", m.group(1))]
 
 
-def main(ref="/root/reference"):
+def main(ref):
     macis = os.path.join(ref, "external", "macis")
     dumps = {
         "h2o_ccpvdz": os.path.join(macis, "tests", "ref_data", "h2o.ccpvdz.fci.dat"),
@@ -154,4 +154,6 @@ def main(ref="/root/reference"):
 
 
 if __name__ == "__main__":
-    main(*sys.argv[1:])
+    if len(sys.argv) != 2:
+        sys.exit(__doc__)
+    main(sys.argv[1])

@@ -54,6 +54,18 @@ def test_null_context_is_an_error_not_a_crash(capi):
     assert L.qdkgb_destroy(None) == capi.OK
 
 
+def test_noalloc_rejects_rows_beyond_the_limit(capi):
+    # the size check of the allocation-free sigma runs before any pointer is
+    # touched or any CUDA call is made, so it is checked without a GPU
+    with pytest.raises(capi.QdkgbError) as ei:
+        capi.sigma_split_noalloc(capi.NOALLOC_MAX_ROWS + 1, 16, 16, 16, 16, 16, 16)
+    assert ei.value.code == capi.ERR_INVALID
+    assert "QDKGB_NOALLOC_MAX_ROWS" in str(ei.value)
+    with pytest.raises(capi.QdkgbError) as ei:
+        capi.sigma_split_noalloc(-1, 16, 16, 16, 16, 16, 16)
+    assert ei.value.code == capi.ERR_INVALID
+
+
 def test_create_without_gpu_reports_status(capi):
     import torch
     if torch.cuda.is_available():

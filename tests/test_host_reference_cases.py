@@ -120,6 +120,11 @@ def test_macis_wavefunction_files(pkg, tmp_path):
     assert w.norb == int(d["norb"]) and np.array_equal(w.coefficients, d["coeffs"])
     w.to_macis_file(str(tmp_path / "again.dat"))
     assert (tmp_path / "again.dat").read_text() == p.read_text()
+    # wavefunction_io.hpp:99-102: unequal lengths throw, an empty wavefunction writes nothing
+    with pytest.raises(RuntimeError, match="Invalid Wave Function Dimensions"):
+        det.write_wavefunction(str(tmp_path / "bad.dat"), 4, d["alpha"][:3], d["beta"][:3], d["coeffs"][:2])
+    det.write_wavefunction(str(tmp_path / "empty.dat"), 4, [], [], [])
+    assert not (tmp_path / "empty.dat").exists() and not (tmp_path / "bad.dat").exists()
 
 
 def test_macis_rdm_files(pkg, tmp_path):

@@ -5,8 +5,10 @@ CUDA graph capture, under another allocator's pool): inputs, outputs and the
 stream are theirs, the scratch is a fixed device array inside the library.  Here
 it is called through the C ABI on device arrays the test owns and compared with
 the context-based full-precision sigma (qdkgb_spmv, FP64 mode on the same split
-storage), on two calls in a row, at the tolerance of the other sigma tests
-(1e-12 relative).  This file is collected last on purpose.
+storage) and with the oracle's CSR sigma, on two calls in a row, at the
+tolerance of the other sigma tests (1e-12 relative).  The size check, which
+needs no GPU, is tested in test_capi_cpu.py.  This file is collected last on
+purpose.
 """
 import numpy as np
 import pytest
@@ -20,7 +22,7 @@ def _split(values):
     return hi, lo
 
 
-def test_noalloc_sigma_matches_context_sigma(pkg):
+def test_noalloc_sigma_matches_context_sigma(pkg, oracle):
     import torch
 
     pkg.build.build()
@@ -40,6 +42,7 @@ def test_noalloc_sigma_matches_context_sigma(pkg):
         d_hi = torch.from_numpy(hi).to(dev)
         d_lo = torch.from_numpy(lo).to(dev)
         stream = torch.cuda.Stream()
+        M = oracle.build_csr(oracle.Hamiltonian(T, V), a, b)
         rng = np.random.default_rng(5)
         for call in range(2):
             x = rng.normal(size=n)
@@ -53,13 +56,5 @@ def test_noalloc_sigma_matches_context_sigma(pkg):
             y = d_y.cpu().numpy()
             assert np.all(np.isfinite(y)), call
             assert np.max(np.abs(y - ref)) <= 1e-12 * np.max(np.abs(ref)), call
-
-
-def test_noalloc_rejects_rows_beyond_the_limit(pkg):
-    pkg.build.build()
-    capi = pkg.capi
-    with pytest.raises(capi.QdkgbError) as ei:
-        # rejected on the size alone, before any pointer is touched
-        capi.sigma_split_noalloc(capi.NOALLOC_MAX_ROWS + 1, 16, 16, 16, 16, 16, 16)
-    assert ei.value.code == capi.ERR_INVALID
-    assert "QDKGB_NOALLOC_MAX_ROWS" in str(ei.value)
+            yo = M.spmv(x)
+            assert np.max(np.abs(y - yo)) <= 1e-12 * np.max(np.abs(yo)), call
