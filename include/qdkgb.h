@@ -127,6 +127,21 @@ int qdkgb_build_hamiltonian(qdkgb_context* ctx, double thresh, int storage, int6
  * qdkgb_build_hamiltonian switches back to the CSR. */
 int qdkgb_build_direct_sigma(qdkgb_context* ctx);
 
+/* The Davidson operator of the current determinants, chosen by memory: the
+ * stored Hamiltonian (exactly qdkgb_build_hamiltonian(ctx, thresh, storage))
+ * when it fits in the device memory available to the context (free memory
+ * and the qdkgb_set_device_limit cap, counting what the current operator
+ * holds) together with a Davidson workspace of max_m vectors; otherwise, for
+ * a complete (n_alpha, n_beta) space within the direct sigma's limits, the
+ * direct sigma (qdkgb_build_direct_sigma).  *layout (may be NULL) receives
+ * QDKGB_LAYOUT_SLAB, QDKGB_LAYOUT_CSR or QDKGB_LAYOUT_DIRECT, *nnz (may be
+ * NULL) the element count of the stored matrix's CSR (0 for the direct sigma).  The reference
+ * always stores the matrix (make_csr_hamiltonian_block_ in
+ * selected_ci_diag / compute_casci_rdms, include/macis/mcscf/cas.hpp:52-55);
+ * at CAS(14e,14o) that matrix (3.98e10 elements) exceeds HBM, and this is how
+ * the drop-in calculators reach that size.  qdkgb_casci uses it. */
+int qdkgb_build_operator(qdkgb_context* ctx, double thresh, int storage, int max_m, int* layout, int64_t* nnz);
+
 /* Copies the device CSR to host buffers (rowptr: ndets+1, colind/values: nnz).
  * For QDKGB_H_SPLIT32 storage, values receive (double)hi + (double)lo.
  * The 32-bit and 64-bit variants mirror make_csr_hamiltonian_block_32bit_ /
@@ -167,6 +182,16 @@ typedef struct qdkgb_davidson_settings {
   int precision;      /* QDKGB_PREC_FP64 or QDKGB_PREC_MIXED */
   int use_guess;      /* 1: C holds a guess (used when max|C| > 1/N, selected_ci_diag.hpp:130-140) */
   double min_abs_denominator; /* preconditioner clamp (default 1e-12) */
+  int nroots;         /* lowest roots wanted (default 1).  1: the reference's
+                       * single-root davidson (davidson.hpp:259-372).  > 1: a
+                       * block Davidson (no counterpart in MACIS, whose
+                       * multi-root solver is lobpcgxx::lobpcg,
+                       * src/lobpcgxx/include/lobpcgxx/simplified_interface.hpp:37-72):
+                       * FP64 only, E receives nroots energies and C (if not
+                       * NULL) nroots column-major vectors of ndets, converged
+                       * when every root's residual is below res_tol; max_m
+                       * bounds the subspace, which restarts on the Ritz
+                       * vectors of the roots. */
 } qdkgb_davidson_settings;
 
 typedef struct qdkgb_davidson_info {
@@ -299,7 +324,8 @@ int qdkgb_casscf(qdkgb_context* ctx, const qdkgb_mcscf_settings* s, int nalpha, 
 /* ------------------------------------------------------------ CASCI driver
  * cas_helper::impl / compute_casci_rdms (cpp/src/qdk/chemistry/algorithms/
  * microsoft/macis_cas.cpp:35-117, include/macis/mcscf/cas.hpp:33-64): FCI
- * space, H build, Davidson.  E receives the electronic energy (the caller
+ * space, the operator of qdkgb_build_operator (stored, or the direct sigma
+ * when the stored matrix would not fit), Davidson.  E receives the electronic energy (the caller
  * adds the core energy, macis_cas.cpp:113); C (may be NULL) the CI vector in
  * MACIS determinant order. */
 int qdkgb_casci(qdkgb_context* ctx, int norb, int nalpha, int nbeta, const double* T, const double* V, int layout,

@@ -1,7 +1,9 @@
 """Differentiable CASCI energy: ``torch.autograd.Function`` over the GPU core.
 
 Forward: CASCI ground-state energy of (h1, eri) (+ core energy) on the GPU
-(H build, Davidson, then the spin-resolved RDMs of the converged vector).
+(the stored Hamiltonian, or the direct sigma when the stored matrix would not
+fit on the device, as at CAS(14e,14o); Davidson; then the spin-resolved RDMs
+of the converged vector).
 Backward (Hellmann-Feynman, exact for the variational CI root):
     dE/dh1[p,q]      = gamma[p,q]       = (aa + bb)[p,q]
     dE/deri[p,q,r,s] = Gamma[p,q,r,s]   = (aaaa + bbbb + aabb + aabb^T)[p,q,r,s]
@@ -26,7 +28,7 @@ def _rdm_pair(R):
 
 class CASCIEnergy(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, h1, eri, core, nalpha, nbeta, tol, precision, device):
+    def forward(ctx, h1, eri, core, nalpha, nbeta, tol, precision, device, max_m):
         T = h1.detach().double().cpu().numpy()
         V = eri.detach().double().cpu().numpy()
         n = T.shape[0]
@@ -35,8 +37,9 @@ class CASCIEnergy(torch.autograd.Function):
             a, b = capi.fci_dets(n, nalpha, nbeta)
             c.set_dets(a, b)
             mixed = precision == "mixed"
-            c.build_hamiltonian(storage=capi.H_SPLIT32 if mixed else capi.H_FP64)
-            E, C, info = c.davidson(tol=tol, precision=capi.PREC_MIXED if mixed else capi.PREC_FP64)
+            # stored matrix, or the direct sigma when it would not fit (CAS(14e,14o))
+            c.build_operator(storage=capi.H_SPLIT32 if mixed else capi.H_FP64, max_m=max_m)
+            E, C, info = c.davidson(tol=tol, max_m=max_m, precision=capi.PREC_MIXED if mixed else capi.PREC_FP64)
             R = c.rdms_spin_dep(C)
         gamma, Gamma = _rdm_pair(R)
         ctx.save_for_backward(torch.from_numpy(np.ascontiguousarray(gamma)).to(h1.device),
@@ -48,14 +51,14 @@ class CASCIEnergy(torch.autograd.Function):
     def backward(ctx, gE):
         gamma, Gamma = ctx.saved_tensors
         g = gE.double()
-        return (g * gamma, g * Gamma, g.to(ctx.core_device), None, None, None, None, None)
+        return (g * gamma, g * Gamma, g.to(ctx.core_device), None, None, None, None, None, None)
 
 
-def casci_energy(h1, eri, nalpha, nbeta, core=None, tol=1e-10, precision="fp64", device=0):
+def casci_energy(h1, eri, nalpha, nbeta, core=None, tol=1e-10, precision="fp64", device=0, max_m=200):
     """E(h1, eri) = CASCI ground-state energy, differentiable w.r.t. h1, eri, core."""
     if core is None:
         core = torch.zeros((), dtype=torch.float64, device=h1.device)
-    return CASCIEnergy.apply(h1, eri, core, int(nalpha), int(nbeta), float(tol), precision, int(device))
+    return CASCIEnergy.apply(h1, eri, core, int(nalpha), int(nbeta), float(tol), precision, int(device), int(max_m))
 
 
 def rdms_as_gradients(h1, eri, nalpha, nbeta, tol=1e-10):

@@ -142,6 +142,9 @@ class Gb300Settings(MultiConfigurationSettings):
         self.set_default("precision", str, "fp64", "fp64 or mixed (FP32 sigma with FP64 defect correction)",
                          ["fp64", "mixed"])
         self.set_default("device", int, 0, "CUDA device ordinal", (0, 1024))
+        self.set_default("device_memory_limit", int, 0,
+                         "cap on the device bytes the calculation may hold (0: none); when the stored "
+                         "Hamiltonian would not fit, complete spaces use the direct sigma", (0, 1 << 62))
 
 
 class Hamiltonian:
@@ -437,9 +440,12 @@ class MultiConfigurationCalculator:
             raise ValueError("precision must be 'fp64' or 'mixed'")
         mixed = prec == "mixed"
         ctx.set_dets(a, b)
-        ctx.build_hamiltonian(s.get("ci_matel_tol"), capi.H_SPLIT32 if mixed else capi.H_FP64)
         tol, max_m = self._davidson_limits(len(a))
+        # the stored matrix when it fits on the device, else (complete spaces,
+        # e.g. CAS(14e,14o)) the direct sigma
+        layout = ctx.build_operator(s.get("ci_matel_tol"), capi.H_SPLIT32 if mixed else capi.H_FP64, max_m)
         E, C, info = ctx.davidson(max_m=max_m, tol=tol, precision=capi.PREC_MIXED if mixed else capi.PREC_FP64)
+        info["operator"] = layout
         rdms = None
         want = []
         if s.get("calculate_one_rdm"):
@@ -468,6 +474,8 @@ class Gb300Cas(MultiConfigurationCalculator):
             raise ValueError("at most 64 active orbitals per spin")
         a, b = capi.fci_dets(n, n_alpha, n_beta)
         with capi.Context(self._settings.get("device")) as ctx:
+            if self._settings.get("device_memory_limit"):
+                ctx.set_device_limit(self._settings.get("device_memory_limit"))
             ctx.set_integrals(hamiltonian.get_one_body_integrals(), hamiltonian.get_two_body_integrals())
             return self._solve(ctx, hamiltonian, a, b)
 

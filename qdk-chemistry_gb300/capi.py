@@ -24,6 +24,8 @@ ERR_STATE = 6
 
 LAYOUT_COLMAJOR = 0
 LAYOUT_ROWMAJOR = 1
+# operator layouts (qdkgb_operator_layout, qdkgb_build_operator)
+LAYOUT_NONE, LAYOUT_CSR, LAYOUT_SLAB, LAYOUT_DIRECT = 0, 1, 2, 3
 H_FP64 = 0
 H_SPLIT32 = 1
 PREC_FP64 = 0
@@ -37,7 +39,7 @@ EXPORTED = [
     "qdkgb_get_csr64", "qdkgb_get_csr32_rows", "qdkgb_get_csr64_rows", "qdkgb_diagonal", "qdkgb_spmv", "qdkgb_spmv_device", "qdkgb_davidson_default_settings",
     "qdkgb_davidson", "qdkgb_rdms_spin_dep", "qdkgb_orbital_entropies", "qdkgb_casci",
     "qdkgb_mcscf_default_settings", "qdkgb_casscf", "qdkgb_version", "qdkgb_kernel_launches",
-    "qdkgb_sigma_split_noalloc", "qdkgb_set_csr", "qdkgb_build_direct_sigma",
+    "qdkgb_sigma_split_noalloc", "qdkgb_set_csr", "qdkgb_build_direct_sigma", "qdkgb_build_operator",
     "qdkgb_asci_default_settings", "qdkgb_asci_search", "qdkgb_asci", "qdkgb_asci_pt2",
     "qdkgb_batch_default_settings", "qdkgb_casci_batch",
 ]
@@ -55,7 +57,7 @@ class NotConverged(QdkgbError):
 
 class DavidsonSettings(ctypes.Structure):
     _fields_ = [("max_m", ctypes.c_int64), ("res_tol", ctypes.c_double), ("precision", ctypes.c_int),
-                ("use_guess", ctypes.c_int), ("min_abs_denominator", ctypes.c_double)]
+                ("use_guess", ctypes.c_int), ("min_abs_denominator", ctypes.c_double), ("nroots", ctypes.c_int)]
 
 
 class McscfSettings(ctypes.Structure):
@@ -132,6 +134,7 @@ def lib():
     L.qdkgb_get_csr32.argtypes = [vp, vp, vp, vp]
     L.qdkgb_get_csr64.argtypes = [vp, vp, vp, vp]
     L.qdkgb_get_csr32_rows.argtypes = [vp, i64, i64, vp, vp, vp]
+    L.qdkgb_build_operator.argtypes = [vp, dp, ci, ci, P(ci), P(i64)]
     L.qdkgb_get_csr64_rows.argtypes = [vp, i64, i64, vp, vp, vp]
     L.qdkgb_diagonal.argtypes = [vp, vp]
     L.qdkgb_set_csr.argtypes = [vp, i64, vp, vp, vp]
@@ -339,6 +342,17 @@ class Context:
         self.nnz = nnz.value
         return self.nnz
 
+    def build_operator(self, thresh=np.finfo(np.float64).eps, storage=H_FP64, max_m=200):
+        """The stored Hamiltonian when it fits on the device, else (complete
+        spaces) the direct sigma (qdkgb_build_operator); returns the layout
+        name ("slab", "csr" or "direct")."""
+        lay = ctypes.c_int()
+        nnz = ctypes.c_int64()
+        self._check(lib().qdkgb_build_operator(self._h, float(thresh), int(storage), int(max_m), ctypes.byref(lay),
+                                               ctypes.byref(nnz)))
+        self.nnz = nnz.value
+        return {LAYOUT_CSR: "csr", LAYOUT_SLAB: "slab", LAYOUT_DIRECT: "direct"}[lay.value]
+
     def build_direct_sigma(self):
         """Recompute-on-the-fly sigma for a complete space (no CSR stored)."""
         self._check(lib().qdkgb_build_direct_sigma(self._h))
@@ -390,11 +404,23 @@ class Context:
     def spmv_device(self, x_ptr, y_ptr, precision=PREC_FP64):
         self._check(lib().qdkgb_spmv_device(self._h, precision, x_ptr, y_ptr))
 
-    def davidson(self, max_m=200, tol=1e-8, precision=PREC_FP64, guess=None, want_vector=True):
+    def davidson(self, max_m=200, tol=1e-8, precision=PREC_FP64, guess=None, want_vector=True, nroots=1):
+        """Lowest root (E, C, info); with nroots > 1 the block Davidson:
+        (energies (nroots), C (ndets x nroots), info)."""
         s = default_davidson_settings()
         s.max_m = max_m
         s.res_tol = tol
         s.precision = precision
+        s.nroots = nroots
+        if nroots > 1:
+            C = np.zeros(self.ndets * nroots) if (want_vector or guess is not None) else None
+            if guess is not None:
+                C[:] = np.asarray(guess, dtype=np.float64).ravel(order="F")
+            s.use_guess = 0 if guess is None else 1
+            E = np.zeros(nroots)
+            info = DavidsonInfo()
+            self._check(lib().qdkgb_davidson(self._h, ctypes.byref(s), _ptr(E), _ptr(C), ctypes.byref(info)))
+            return E, (C.reshape((self.ndets, nroots), order="F") if C is not None else None), info.as_dict()
         C = np.zeros(self.ndets) if guess is None else _f64(guess).copy()
         if not want_vector and guess is None:
             C = None

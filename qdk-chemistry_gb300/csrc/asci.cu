@@ -759,6 +759,7 @@ double sci_diag_gpu(Context* c, const qdkgb_asci_settings& S, const qdkgb_davids
   const bool mixed = ci.precision == QDKGB_PREC_MIXED;
   build_hamiltonian(c, matel_tol, mixed ? QDKGB_H_SPLIT32 : QDKGB_H_FP64);
   qdkgb_davidson_settings s = ci;
+  s.nroots = 1;  // the ASCI iterations solve for the lowest root, as the reference's do
   s.use_guess = X.empty() ? 0 : 1;
   X.resize(n, 0.);
   if (!s.use_guess) std::fill(X.begin(), X.end(), 0.);

@@ -155,6 +155,47 @@ static void get_csr(Context* c, I* rowptr, I* colind, double* values) {
     for (int64_t i = 0; i < H.nnz; ++i) colind[i] = (I)ci[i];
 }
 
+// Stored elements of a complete (n, k_a, k_b) space: every row holds the
+// diagonal, the singles and doubles of each spin and the alpha x beta singles.
+static int64_t cas_row_elements(int n, int ka, int kb) {
+  auto C2 = [](int64_t x) { return x * (x - 1) / 2; };
+  const int64_t sa = (int64_t)ka * (n - ka), sb = (int64_t)kb * (n - kb);
+  return 1 + sa + sb + C2(ka) * C2(n - ka) + C2(kb) * C2(n - kb) + sa * sb;
+}
+
+// The stored Hamiltonian when it fits in the device memory available to this
+// context (free memory, and the cap of qdkgb_set_device_limit, counting what
+// the current operator holds) beside the Davidson workspace of max_m
+// vectors; otherwise, for a complete space the direct sigma serves.  Returns
+// true when the direct sigma was built.
+bool qdkgb::build_operator(Context* c, double thresh, int storage, int max_m) {
+  const DetSpace& S = c->dets;
+  if (!c->have_dets) throw Error(QDKGB_ERR_STATE, "determinants not set");
+  bool complete = S.product && S.ngroups > 0;
+  for (int64_t g = 0; complete && g < S.ngroups; ++g) complete = S.h_gstart[g] == g * S.nbeta;
+  if (complete && !S.h_galpha.empty() && !S.h_ubeta.empty()) {
+    const int n = c->norb;
+    const int ka = __builtin_popcountll(S.h_galpha[0]), kb = __builtin_popcountll(S.h_ubeta[0]);
+    const double N = (double)S.ndets;
+    const double stored = N * (double)cas_row_elements(n, ka, kb) * (storage == QDKGB_H_SPLIT32 ? 12.0 : 8.0);
+    const double work = N * 8.0 * (2.0 * (std::max(max_m, 2) + 1) + 16.0);
+    size_t fr = 0, tot = 0;
+    QDKGB_CUDA(cudaMemGetInfo(&fr, &tot));
+    double held = 0;
+    for (const DeviceBuffer* b : {&c->H.rowptr, &c->H.colind, &c->H.val, &c->H.hi, &c->H.lo})
+      held += (double)b->bytes;
+    double avail = (double)fr + held;
+    if (c->dev_limit > 0) avail = std::min(avail, (double)(c->dev_limit - c->dev_bytes) + held);
+    const bool direct_ok = n <= 20 && S.ngroups <= 4096 && S.nbeta <= 4096 && ka > 0 && kb > 0;
+    if (direct_ok && stored + work > 0.92 * avail) {
+      build_direct_sigma(c);
+      return true;
+    }
+  }
+  build_hamiltonian(c, thresh, storage);
+  return false;
+}
+
 // Rows [r0, r1) of the device CSR: rowptr (r1 - r0 + 1 entries) relative to
 // the block's first element, as a bra block of make_csr_hamiltonian_block_
 // returns it; colind are global columns.
@@ -452,6 +493,7 @@ void qdkgb_davidson_default_settings(qdkgb_davidson_settings* s) {
   s->precision = QDKGB_PREC_FP64;
   s->use_guess = 0;
   s->min_abs_denominator = 1e-12;
+  s->nroots = 1;
 }
 
 int qdkgb_davidson(qdkgb_context* c, const qdkgb_davidson_settings* s, double* E, double* C,
@@ -589,6 +631,16 @@ int qdkgb_asci(qdkgb_context* c, const qdkgb_asci_settings* s, const qdkgb_david
   });
 }
 
+int qdkgb_build_operator(qdkgb_context* c, double thresh, int storage, int max_m, int* layout, int64_t* nnz) {
+  if (!c) return QDKGB_ERR_INVALID;
+  return guarded(c, [&] {
+    QDKGB_CUDA(cudaSetDevice(c->device));
+    const bool direct = build_operator(c, thresh, storage, max_m);
+    if (layout) *layout = direct ? QDKGB_LAYOUT_DIRECT : (c->H.structured ? QDKGB_LAYOUT_SLAB : QDKGB_LAYOUT_CSR);
+    if (nnz) *nnz = direct ? 0 : c->H.nnz;
+  });
+}
+
 int qdkgb_casci(qdkgb_context* c, int norb, int nalpha, int nbeta, const double* T, const double* V, int layout,
                 const qdkgb_davidson_settings* s, double matel_tol, double* E, double* C,
                 qdkgb_davidson_info* info) {
@@ -611,7 +663,8 @@ int qdkgb_casci(qdkgb_context* c, int norb, int nalpha, int nbeta, const double*
     qdkgb_davidson_settings def;
     qdkgb_davidson_default_settings(&def);
     const qdkgb_davidson_settings* ss = s ? s : &def;
-    build_hamiltonian(c, matel_tol, ss->precision == QDKGB_PREC_MIXED ? QDKGB_H_SPLIT32 : QDKGB_H_FP64);
+    build_operator(c, matel_tol, ss->precision == QDKGB_PREC_MIXED ? QDKGB_H_SPLIT32 : QDKGB_H_FP64,
+                   (int)ss->max_m);
     davidson(c, ss, E, C, info);
   });
 }

@@ -473,6 +473,7 @@ constexpr int kSlotE = kMaxSubspace + 12;    // full-precision Rayleigh quotient
 constexpr int kSlotFlag = kMaxSubspace + 16; // Gram-Schmidt degeneracy flag
 constexpr int kSlotW2 = kMaxSubspace + 20;   // |w|^2 before a Gram-Schmidt pass
 constexpr int kSlotSkip = kMaxSubspace + 24; // selective second pass: 1 = not needed
+constexpr int kSlotRoots = 2 * kMaxSubspace; // per-root residual norm^2 of the block Davidson (8)
 constexpr int kSlotIdx = 3 * kMaxSubspace;   // argmin index (int64)
 constexpr int kSlotCount = 3 * kMaxSubspace + 16;  // block-completion counters (unsigned, kDotChunks + 1)
 
@@ -595,11 +596,174 @@ struct Dav {
                                                 small + kSlotRes);
     QDKGB_CHECK_LAUNCH();
   }
+  // the same for root r of the last Rayleigh-Ritz (eigenvector column r, ld
+  // k): Ritz vector into Xr, preconditioned residual into Rr, |R|^2 into
+  // small[kSlotRoots + r]
+  void ritz_residual_root(int k, int r, double* Xr, double* Rr, double min_abs) {
+    k_ritz_residual<<<nb, kVecThreads, 0, st>>>(V, AV, n, k, evec + (size_t)r * k, eval + r, Xr, Rr, n, D, min_abs,
+                                                partial, counts(), small + kSlotRoots + r);
+    QDKGB_CHECK_LAUNCH();
+  }
 };
 
 }  // namespace
 
+// ---------------------------------------------------------------- several roots
+// Block Davidson for the `nroots` lowest eigenpairs (FP64).  The reference's
+// davidson is single-root; its multi-root solver is lobpcgxx::lobpcg.  Here:
+// a guess block of the nroots lowest diagonal elements (or the caller's
+// vectors), the projected matrix grown one column at a time as in the
+// single-root solver, Rayleigh-Ritz in FP64 (the Householder / Sturm /
+// inverse-iteration solver with its matrix in global memory), and per
+// iteration one new direction for every unconverged root: its residual
+// preconditioned with (D - theta_r) clamped at min_abs_denominator, then two
+// Gram-Schmidt passes.  When the next block would exceed max_m the basis
+// restarts on the current Ritz vectors (and their sigmas, formed from the
+// basis, so no extra operator application).  Converged when every root's
+// residual 2-norm is below res_tol.
+static void davidson_roots(Context* c, const qdkgb_davidson_settings* s, double* E, double* C,
+                           qdkgb_davidson_info* info) {
+  NvtxRange nvtx_range("qdkgb.davidson_roots");
+  using clk = std::chrono::steady_clock;
+  const auto t0 = clk::now();
+  Hcsr& H = c->H;
+  const int64_t N = H.n;
+  const int R = s->nroots;
+  if (s->precision != QDKGB_PREC_FP64) throw Error(QDKGB_ERR_UNSUPPORTED, "several roots: FP64 precision only");
+  if (R > N) throw Error(QDKGB_ERR_INVALID, "nroots exceeds the number of determinants");
+  if (R > kMaxOut) throw Error(QDKGB_ERR_UNSUPPORTED, "at most 8 roots");
+  int64_t max_m = std::min<int64_t>(s->max_m, N);
+  if (max_m > kMaxSubspace - 2) throw Error(QDKGB_ERR_INVALID, "max_m above 254 is not supported");
+  if (max_m < 2 * R) throw Error(QDKGB_ERR_INVALID, "max_m must hold at least twice nroots vectors");
+  qdkgb_davidson_info loc{};
+  DavidsonWork& W = c->dav;
+  Dav d;
+  d.c = c;
+  d.n = N;
+  d.maxm = max_m;
+  d.st = c->stream;
+  d.sm_count = std::max(1, c->sm_count);
+  d.nb = (int)std::max<int64_t>(1, std::min<int64_t>((N + kVecTile - 1) / kVecTile, (int64_t)d.sm_count * kVecBlocksPerSm));
+  d.V = dev_array<double>(c, W.V, (size_t)N * (max_m + 1));
+  d.AV = dev_array<double>(c, W.AV, (size_t)N * (max_m + 1));
+  // Ritz vectors X_r, their sigmas AX_r and the preconditioned residuals
+  d.X = dev_array<double>(c, W.scratch, (size_t)N * 3 * R);
+  double* AX = d.X + (size_t)N * R;
+  double* Rr = AX + (size_t)N * R;
+  d.work = nullptr;
+  d.Hk = dev_array<double>(c, W.Hk, (size_t)(max_m + 1) * (max_m + 1));
+  d.evec = dev_array<double>(c, W.evec, (size_t)(max_m + 1) * (max_m + 1));
+  d.eval = dev_array<double>(c, W.eval, (size_t)(max_m + 1));
+  d.partial = dev_array<double>(c, W.partial, (size_t)d.nb * (kMaxSubspace + 2));
+  d.small = dev_array<double>(c, W.small, 4 * kMaxSubspace);
+  d.gA = dev_array<double>(c, W.yf, (size_t)(max_m + 1) * (max_m + 1));  // FP64 Rayleigh-Ritz (global matrix)
+  d.D = (double*)H.diag.ptr;
+  d.clear_flag();
+  QDKGB_CUDA(cudaMemsetAsync(d.counts(), 0, (kDotChunks + 1) * sizeof(unsigned), c->stream));
+  auto sigma = [&](const double* x, double* y) {
+    spmv_fp64(c, x, y);
+    loc.spmv_fp64++;
+  };
+  auto fetch_n = [&](const double* a, int cnt, std::vector<double>& out) {
+    std::vector<double> h(cnt);
+    QDKGB_CUDA(cudaMemcpyAsync(h.data(), a, cnt * sizeof(double), cudaMemcpyDeviceToHost, d.st));
+    QDKGB_CUDA(cudaStreamSynchronize(d.st));
+    out = h;
+  };
+  auto lowest_fp64 = [&](int k) {
+    k_lowest_eig<<<1, kEigThreads, 0, d.st>>>(k, d.Hk, (int)(max_m + 1), d.gA, R, d.eval, d.evec);
+    QDKGB_CHECK_LAUNCH();
+  };
+  // append w (already in V[:, k]) : orthonormalise, sigma, projected row
+  int k = 0;
+  auto append = [&](double* w) -> bool {
+    double* vk = d.col(d.V, k);
+    if (w != vk) QDKGB_CUDA(cudaMemcpyAsync(vk, w, N * sizeof(double), cudaMemcpyDeviceToDevice, d.st));
+    d.gram_schmidt(k, vk);
+    double flag = 0.;
+    d.fetch(d.small + kSlotFlag, flag);
+    if (flag != 0.) {  // linearly dependent: drop it
+      d.clear_flag();
+      return false;
+    }
+    sigma(vk, d.col(d.AV, k));
+    d.projected_row(k);
+    ++k;
+    return true;
+  };
+
+  // guess block
+  if (s->use_guess && C) {
+    for (int r = 0; r < R; ++r) append(const_cast<double*>(C) + (size_t)r * N);
+  }
+  if (k < R) {
+    std::vector<double> Dh(N);
+    QDKGB_CUDA(cudaMemcpyAsync(Dh.data(), d.D, N * sizeof(double), cudaMemcpyDeviceToHost, d.st));
+    QDKGB_CUDA(cudaStreamSynchronize(d.st));
+    std::vector<int64_t> idx(N);
+    for (int64_t i = 0; i < N; ++i) idx[i] = i;
+    const int64_t m = std::min<int64_t>(N, 4 * R + 4);
+    std::partial_sort(idx.begin(), idx.begin() + m, idx.end(),
+                      [&](int64_t x, int64_t y) { return Dh[x] < Dh[y] || (Dh[x] == Dh[y] && x < y); });
+    for (int64_t q = 0; q < m && k < R; ++q) {
+      double* w = d.col(d.V, k);
+      QDKGB_CUDA(cudaMemsetAsync(w, 0, N * sizeof(double), d.st));
+      const double one = 1.0;
+      QDKGB_CUDA(cudaMemcpyAsync(w + idx[q], &one, sizeof(double), cudaMemcpyHostToDevice, d.st));
+      append(w);
+    }
+  }
+  if (k < R) throw Error(QDKGB_ERR_INVALID, "several roots: no independent guess block");
+
+  std::vector<double> theta(R), rn(R);
+  bool converged = false;
+  const int64_t max_iter = 50 * max_m;
+  int64_t iter = 0;
+  for (; iter < max_iter; ++iter) {
+    lowest_fp64(k);
+    for (int r = 0; r < R; ++r) {
+      d.ritz_residual_root(k, r, d.col(d.X, r), d.col(Rr, r), s->min_abs_denominator);
+      k_gemv_rows<false><<<d.nb, kVecThreads, 0, d.st>>>(d.AV, N, k, d.evec + (size_t)r * k, 1, AX + (size_t)r * N, N);
+      QDKGB_CHECK_LAUNCH();
+    }
+    fetch_n(d.eval, R, theta);
+    fetch_n(d.small + kSlotRoots, R, rn);
+    double worst = 0.;
+    for (int r = 0; r < R; ++r) worst = std::max(worst, std::sqrt(rn[r]));
+    loc.iterations = iter + 1;
+    loc.residual_norm = worst;
+    if (worst < s->res_tol) {
+      converged = true;
+      break;
+    }
+    int pending = 0;
+    for (int r = 0; r < R; ++r) pending += std::sqrt(rn[r]) >= s->res_tol;
+    if (k + pending > max_m) {
+      // restart on the Ritz vectors and their sigmas
+      QDKGB_CUDA(cudaMemcpyAsync(d.V, d.X, (size_t)N * R * sizeof(double), cudaMemcpyDeviceToDevice, d.st));
+      QDKGB_CUDA(cudaMemcpyAsync(d.AV, AX, (size_t)N * R * sizeof(double), cudaMemcpyDeviceToDevice, d.st));
+      k = R;
+      for (int i = 0; i < R; ++i) d.projected_row(i);
+      loc.restarts++;
+    }
+    for (int r = 0; r < R; ++r)
+      if (std::sqrt(rn[r]) >= s->res_tol && k < max_m) append(d.col(Rr, r));
+  }
+  fetch_n(d.eval, R, theta);
+  for (int r = 0; r < R; ++r) E[r] = theta[r];
+  if (C) QDKGB_CUDA(cudaMemcpyAsync(C, d.X, (size_t)N * R * sizeof(double), cudaMemcpyDeviceToHost, d.st));
+  QDKGB_CUDA(cudaStreamSynchronize(d.st));
+  loc.seconds = std::chrono::duration<double>(clk::now() - t0).count();
+  if (info) *info = loc;
+  if (!converged) throw Error(QDKGB_ERR_NOT_CONVERGED, "Davidson Did Not Converge!");
+}
+
 void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C, qdkgb_davidson_info* info) {
+  if (s->nroots > 1) {
+    if (!c->H.valid) throw Error(QDKGB_ERR_STATE, "Hamiltonian not built");
+    davidson_roots(c, s, E, C, info);
+    return;
+  }
   NvtxRange nvtx_range("qdkgb.davidson");
   using clk = std::chrono::steady_clock;
   const auto t0 = clk::now();

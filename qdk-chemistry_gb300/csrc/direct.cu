@@ -298,6 +298,10 @@ static void transpose(Context* c, const T* in, T* out, int64_t nr, int64_t nc, b
   QDKGB_CHECK_LAUNCH();
 }
 
+void transpose_f64(Context* c, const double* in, double* out, int64_t nr, int64_t nc) {
+  transpose<double>(c, in, out, nr, nc, false);
+}
+
 template <typename T>
 static void direct_sigma_t(Context* c, const T* x, T* y) {
   DirectSigma* d = c->direct;

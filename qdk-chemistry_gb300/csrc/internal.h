@@ -150,6 +150,7 @@ void check_dets_in_orbitals(const Context* c);
 void build_integral_intermediates(Context* c);
 void build_det_space(Context* c, int64_t ndets, const uint64_t* alpha, const uint64_t* beta);
 void build_hamiltonian(Context* c, double thresh, int storage);
+bool build_operator(Context* c, double thresh, int storage, int max_m);  // true: direct sigma
 void set_csr(Context* c, int64_t n, const int64_t* rowptr, const int64_t* colind, const double* values);
 void exclusive_scan_i64(Context* c, const int64_t* in, int64_t* out, int64_t n, DeviceBuffer& tmp);
 
@@ -188,6 +189,8 @@ void build_direct_sigma(Context* c);
 void free_direct(Context* c);
 void direct_sigma_fp64(Context* c, const double* x, double* y);
 void direct_sigma_fp32(Context* c, const float* x, float* y);
+// out (nc x nr) = in^T for a row-major in (nr x nc)
+void transpose_f64(Context* c, const double* in, double* out, int64_t nr, int64_t nc);
 
 // asci.cu
 void asci_search_gpu(Context* c, int64_t ncore, const uint64_t* ca, const uint64_t* cb, const double* cc, double E0,

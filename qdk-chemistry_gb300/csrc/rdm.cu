@@ -13,6 +13,7 @@
 // and the targets rarely collide) the kernel accumulates straight into
 // global memory.
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <limits>
 #include <vector>
@@ -182,6 +183,382 @@ __global__ void __launch_bounds__(kRdmWarps * 32)
   }
 }
 
+// ---------------------------------------------------------------- complete spaces
+// For a complete (n_alpha, n_beta) product space the CI vector is a matrix
+// C[g, b] (determinant g * N_b + b) and the same contributions as above are
+// regrouped by spin, with no pair walk and no atomics on the opposite-spin
+// block:
+//
+//   aabb: every ordered pair (I <- J) with at most one excitation per spin
+//     adds 1/2 s_a s_b C_I C_J to G[i, j, k, l], (i, j) the beta and (k, l)
+//     the alpha orbitals (created in the bra, annihilated in the ket; a
+//     string-diagonal term has i = j or k = l occupied).  For each alpha
+//     transition (gJ -> gI, class (k, l)) the kernel sums over every beta
+//     transition of class (i, j):
+//         t_ij = sum_{(bJ -> bI) in class (i, j)} s_b C[gI, bI] C[gJ, bJ]
+//     with one thread per beta class (its list of (bI, bJ, s_b) streamed
+//     from L2) and the two rows of C staged in shared memory, accumulating
+//     s_a t_ij in registers over a chunk of transitions of one alpha class.
+//     Chunks write partial sums that a second kernel adds in a fixed order
+//     (deterministic).  The reversed alpha transition gives the same value
+//     at G[j, i, l, k], so only classes k >= l are swept.
+//   aaaa + aa: the pairs with equal beta strings, i.e. alpha string pairs
+//     (gI, gJ) within a double excitation weighted by the string overlap
+//     S_a = sum_b C[gI, b] C[gJ, b], then the same-spin formulas above
+//     (rdm_same_spin_double / rdm_single / rdm_diag, block 0); bbbb + bb the
+//     same with S_b over the columns.
+//
+// The reference drops a pair when |C_I C_J| <= 1e-16 (rdms.hpp skip rule,
+// k_rdm above); the same rule is applied to every product here: in the sweep
+// by the exponents of the two factors (one DFMA when the product is surely
+// above or below the bound, the product formed and tested in the narrow band
+// between), in the overlaps by forming each product.
+
+namespace {
+
+constexpr int kCasThreads = 320;  // beta work items per CTA (one per thread)
+constexpr int kCasChunk = 48;     // alpha transitions per CTA
+
+struct CasItem {
+  int32_t cls;    // beta class i + n j
+  int32_t begin;  // into the packed list
+  int32_t len;
+};
+
+// |a b| > 1e-16 decided from the biased exponents where the answer is certain
+// (sum >= 2046 - 53: |ab| >= 2^-53 > 1e-16; sum <= 2046 - 56: |ab| < 2^-54),
+// by the rounded product itself in between.
+__device__ __forceinline__ double cas_acc(double acc, double a, double b, bool neg) {
+  const int ea = (int)((__double_as_longlong(a) >> 52) & 0x7ff);
+  const int eb = (int)((__double_as_longlong(b) >> 52) & 0x7ff);
+  const int es = ea + eb;
+  if (es >= 2046 - 53) return fma(flip_if(a, neg), b, acc);
+  if (es <= 2046 - 56) return acc;
+  const double p = a * b;
+  return fabs(p) > 1e-16 ? acc + flip_if(p, neg) : acc;
+}
+
+__global__ void __launch_bounds__(kCasThreads)
+    k_rdm_cas_ab(int64_t nb, const double* __restrict__ C, const uint32_t* __restrict__ atr,
+                 const int4* __restrict__ chunks, const CasItem* __restrict__ items, int nitems,
+                 const uint32_t* __restrict__ blist, double* __restrict__ partial) {
+  extern __shared__ double rows[];  // rowI | rowJ
+  double* rowI = rows;
+  double* rowJ = rows + nb;
+  const int4 ch = chunks[blockIdx.x];  // (alpha class, first transition, count, unused)
+  const int it = threadIdx.x;
+  CasItem item = {0, 0, 0};
+  if (it < nitems) item = items[it];
+  const uint32_t* lst = blist + item.begin;
+  double acc = 0.;
+  for (int t = 0; t < ch.z; ++t) {
+    const uint32_t w = __ldg(atr + ch.y + t);
+    const int64_t gI = w & 0x7fff, gJ = (w >> 15) & 0x7fff;
+    const bool na = (w >> 31) != 0;
+    __syncthreads();
+    for (int64_t b = threadIdx.x; b < nb; b += blockDim.x) {
+      rowI[b] = C[gI * nb + b];
+      rowJ[b] = C[gJ * nb + b];
+    }
+    __syncthreads();
+    double s0 = 0., s1 = 0., s2 = 0., s3 = 0.;
+    int e = 0;
+    for (; e + 4 <= item.len; e += 4) {
+      const uint32_t x0 = __ldg(lst + e), x1 = __ldg(lst + e + 1), x2 = __ldg(lst + e + 2), x3 = __ldg(lst + e + 3);
+      s0 = cas_acc(s0, rowI[x0 & 0x7fff], rowJ[(x0 >> 15) & 0x7fff], (x0 >> 31) != 0);
+      s1 = cas_acc(s1, rowI[x1 & 0x7fff], rowJ[(x1 >> 15) & 0x7fff], (x1 >> 31) != 0);
+      s2 = cas_acc(s2, rowI[x2 & 0x7fff], rowJ[(x2 >> 15) & 0x7fff], (x2 >> 31) != 0);
+      s3 = cas_acc(s3, rowI[x3 & 0x7fff], rowJ[(x3 >> 15) & 0x7fff], (x3 >> 31) != 0);
+    }
+    for (; e < item.len; ++e) {
+      const uint32_t x0 = __ldg(lst + e);
+      s0 = cas_acc(s0, rowI[x0 & 0x7fff], rowJ[(x0 >> 15) & 0x7fff], (x0 >> 31) != 0);
+    }
+    acc += flip_if((s0 + s1) + (s2 + s3), na);
+  }
+  if (it < nitems) partial[(int64_t)blockIdx.x * nitems + it] = acc;
+}
+
+// G[i, j, k, l] (and G[j, i, l, k] for k > l) = 1/2 sum over the class's
+// chunks and the beta class's items, in a fixed order.  One thread per
+// (alpha class, beta class).
+__global__ void k_rdm_cas_ab_reduce(int n, int nacls, const int2* __restrict__ acls, const int2* __restrict__ acls_chunks,
+                                    const int2* __restrict__ bcls_items, int nitems,
+                                    const double* __restrict__ partial, double* __restrict__ G) {
+  const int n2 = n * n;
+  const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (tid >= (int64_t)nacls * n2) return;
+  const int ac = (int)(tid / n2), bc = (int)(tid % n2);
+  const int2 kl = acls[ac];
+  const int2 chr = acls_chunks[ac];
+  const int2 itr = bcls_items[bc];
+  double v = 0.;
+  for (int q = chr.x; q < chr.y; ++q)
+    for (int m = itr.x; m < itr.y; ++m) v += partial[(int64_t)q * nitems + m];
+  v *= 0.5;
+  const int i = bc % n, j = bc / n, k = kl.x, l = kl.y;
+  G[i + (size_t)n * (j + (size_t)n * (k + (size_t)n * l))] = v;
+  if (k != l) G[j + (size_t)n * (i + (size_t)n * (l + (size_t)n * k))] = v;
+}
+
+// S[p] = sum_b X[r1, b] X[r2, b] over the pair list (rows of X with ld cols),
+// each product kept when |product| > 1e-16.  One warp per pair.
+__global__ void k_pair_overlap(int64_t npairs, const int2* __restrict__ pairs, const double* __restrict__ X,
+                               int64_t cols, double* __restrict__ S) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t p = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; p < npairs;
+       p += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    const int2 pr = pairs[p];
+    const double* x = X + pr.x * cols;
+    const double* y = X + pr.y * cols;
+    double s = 0.;
+    for (int64_t b = lane; b < cols; b += 32) {
+      const double v = __ldg(x + b) * __ldg(y + b);
+      if (fabs(v) > 1e-16) s += v;
+    }
+    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) S[p] = s;
+  }
+}
+
+// same-spin blocks of one spin from the string overlaps (block 0: aaaa + aa,
+// block 1: bbbb + bb); the bra is the lower-ranked string, as the
+// determinant order puts it first.
+__global__ void k_rdm_cas_same_spin(int64_t npairs, const int2* __restrict__ pairs, const uint64_t* __restrict__ str,
+                                    const double* __restrict__ S, RdmTarget T) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < npairs; p += (int64_t)gridDim.x * blockDim.x) {
+    const double val = S[p];
+    if (val == 0.) continue;
+    const int2 pr = pairs[p];
+    const uint64_t bra = str[pr.x], ket = str[pr.y];
+    const uint64_t ex = bra ^ ket;
+    const int c = popc64(ex);
+    if (c == 4)
+      rdm_same_spin_double(T, T.block, bra, ket, ex, val);
+    else if (c == 2)
+      rdm_single(T, T.block, false, bra, ket, ex, 0, val);
+    else
+      rdm_diag(T, bra, bra, val);
+  }
+}
+
+inline bool cas_sign_odd(uint64_t state, uint32_t p, uint32_t q) {
+  const uint32_t lo = p < q ? p : q, hi = p < q ? q : p;
+  const uint64_t m = ((hi >= 64 ? ~0ull : ((1ull << hi) - 1ull))) ^ ((1ull << (lo + 1)) - 1ull);
+  return __builtin_popcountll(state & m) & 1;
+}
+
+}  // namespace
+
+// True when the determinants form a complete product space this path serves.
+static bool cas_rdm_eligible(const Context* c) {
+  const DetSpace& S = c->dets;
+  if (!S.product || c->norb > 16 || S.ngroups < 1 || S.nbeta < 1) return false;
+  if (S.ngroups > 32767 || S.nbeta > 32767) return false;
+  if ((size_t)2 * S.nbeta * 8 > 220 * 1024) return false;  // the two staged rows of C
+  for (int64_t g = 0; g < S.ngroups; ++g)
+    if (S.h_gstart[g] != g * S.nbeta) return false;
+  return true;
+}
+
+// transitions (ket -> bra) of class (v, o) among strs: bra = ket - o + v
+static void cas_string_maps(const std::vector<uint64_t>& strs, std::vector<int32_t>& rank_of, int n) {
+  rank_of.assign((size_t)1 << n, -1);
+  for (size_t i = 0; i < strs.size(); ++i) rank_of[strs[i]] = (int32_t)i;
+}
+
+// Returns false (nothing accumulated) when the space has more beta classes
+// than the kernel's CTA holds; the pair walk serves it then.
+static bool rdms_cas(Context* c, const double* dC, double* aa, double* bb, double* aaaa, double* bbbb, double* aabb) {
+  const DetSpace& S = c->dets;
+  const int n = c->norb;
+  const int64_t na = S.ngroups, nb = S.nbeta, N = na * nb;
+  const size_t n2 = (size_t)n * n, n4 = n2 * n2;
+  std::vector<int32_t> ra, rb;
+  cas_string_maps(S.h_galpha, ra, n);
+  cas_string_maps(S.h_ubeta, rb, n);
+  ScopedBuffers<12> buf(c);
+  std::vector<double> h4(n4), h2(n2);
+
+  // ---------------- opposite spin (aabb)
+  if (aabb) {
+    // beta lists per class (i, j): (bI, bJ, s_b) packed bI | bJ << 15 | s << 31
+    std::vector<uint32_t> blist;
+    std::vector<int32_t> bbeg(n2 + 1, 0);
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i) {
+        const int cls = i + n * j;
+        bbeg[cls] = (int32_t)blist.size();
+        for (int64_t x = 0; x < nb; ++x) {
+          const uint64_t ket = S.h_ubeta[x];
+          if (!((ket >> j) & 1)) continue;
+          if (i == j) {
+            blist.push_back((uint32_t)x | ((uint32_t)x << 15));
+            continue;
+          }
+          if ((ket >> i) & 1) continue;
+          const uint64_t bra = ket ^ (1ull << i) ^ (1ull << j);
+          const int32_t y = rb[bra];
+          if (y < 0) throw Error(QDKGB_ERR_UNSUPPORTED, "RDM: beta strings are not a complete set");
+          const bool neg = cas_sign_odd(ket, (uint32_t)i, (uint32_t)j);
+          blist.push_back((uint32_t)y | ((uint32_t)x << 15) | ((uint32_t)neg << 31));
+        }
+      }
+    bbeg[n2] = (int32_t)blist.size();
+    // work items: lists split to at most the longest off-diagonal length
+    int32_t lmax = 1;
+    for (size_t cl = 0; cl < n2; ++cl)
+      if ((int)(cl % n) != (int)(cl / n)) lmax = std::max(lmax, bbeg[cl + 1] - bbeg[cl]);
+    for (size_t cl = 0; cl < n2; ++cl)
+      if ((int)(cl % n) == (int)(cl / n) && lmax == 1) lmax = std::max(lmax, bbeg[cl + 1] - bbeg[cl]);
+    std::vector<CasItem> items;
+    std::vector<int2> bitems(n2);
+    for (size_t cl = 0; cl < n2; ++cl) {
+      const int32_t len = bbeg[cl + 1] - bbeg[cl];
+      const int parts = std::max(1, (len + lmax - 1) / lmax);
+      bitems[cl].x = (int)items.size();
+      for (int q = 0; q < parts; ++q) {
+        const int32_t b0 = (int32_t)((int64_t)len * q / parts), b1 = (int32_t)((int64_t)len * (q + 1) / parts);
+        items.push_back({(int32_t)cl, bbeg[cl] + b0, b1 - b0});
+      }
+      bitems[cl].y = (int)items.size();
+    }
+    const int nitems = (int)items.size();
+    if (nitems > kCasThreads) return false;
+    // alpha transitions per class (k, l), k >= l: (gI, gJ, s_a)
+    std::vector<uint32_t> atr;
+    std::vector<int2> acls, acls_chunks;
+    std::vector<int4> chunks;
+    for (int k = 0; k < n; ++k)
+      for (int l = 0; l <= k; ++l) {
+        const size_t t0 = atr.size();
+        for (int64_t x = 0; x < na; ++x) {
+          const uint64_t ket = S.h_galpha[x];
+          if (!((ket >> l) & 1)) continue;
+          if (k == l) {
+            atr.push_back((uint32_t)x | ((uint32_t)x << 15));
+            continue;
+          }
+          if ((ket >> k) & 1) continue;
+          const uint64_t bra = ket ^ (1ull << k) ^ (1ull << l);
+          const int32_t y = ra[bra];
+          if (y < 0) throw Error(QDKGB_ERR_UNSUPPORTED, "RDM: alpha strings are not a complete set");
+          const bool neg = cas_sign_odd(ket, (uint32_t)k, (uint32_t)l);
+          atr.push_back((uint32_t)y | ((uint32_t)x << 15) | ((uint32_t)neg << 31));
+        }
+        const size_t t1 = atr.size();
+        if (t1 == t0) continue;
+        acls.push_back({k, l});
+        const int c0 = (int)chunks.size();
+        for (size_t q = t0; q < t1; q += kCasChunk)
+          chunks.push_back({(int)acls.size() - 1, (int)q, (int)std::min<size_t>(kCasChunk, t1 - q), 0});
+        acls_chunks.push_back({c0, (int)chunks.size()});
+      }
+    double* dG = dev_array<double>(c, buf.b[0], n4);
+    QDKGB_CUDA(cudaMemsetAsync(dG, 0, n4 * 8, c->stream));
+    if (!chunks.empty()) {
+      auto up = [&](DeviceBuffer& b, const void* src, size_t bytes) {
+        void* p = dev_alloc(c, b, bytes + 16);
+        QDKGB_CUDA(cudaMemcpyAsync(p, src, bytes, cudaMemcpyHostToDevice, c->stream));
+        return p;
+      };
+      const uint32_t* d_bl = (const uint32_t*)up(buf.b[1], blist.data(), blist.size() * 4);
+      const CasItem* d_it = (const CasItem*)up(buf.b[2], items.data(), items.size() * sizeof(CasItem));
+      const uint32_t* d_at = (const uint32_t*)up(buf.b[3], atr.data(), atr.size() * 4);
+      const int4* d_ch = (const int4*)up(buf.b[4], chunks.data(), chunks.size() * sizeof(int4));
+      const int2* d_ac = (const int2*)up(buf.b[5], acls.data(), acls.size() * sizeof(int2));
+      const int2* d_acc = (const int2*)up(buf.b[6], acls_chunks.data(), acls_chunks.size() * sizeof(int2));
+      const int2* d_bi = (const int2*)up(buf.b[7], bitems.data(), bitems.size() * sizeof(int2));
+      double* d_part = dev_array<double>(c, buf.b[8], chunks.size() * nitems);
+      const size_t smem = (size_t)2 * nb * 8;
+      set_max_dynamic_smem((const void*)k_rdm_cas_ab, (int)std::max<size_t>(smem, 48 * 1024));
+      k_rdm_cas_ab<<<(unsigned)chunks.size(), kCasThreads, smem, c->stream>>>(nb, dC, d_at, d_ch, d_it, nitems, d_bl,
+                                                                               d_part);
+      QDKGB_CHECK_LAUNCH();
+      const int64_t nred = (int64_t)acls.size() * n2;
+      k_rdm_cas_ab_reduce<<<(unsigned)((nred + 127) / 128), 128, 0, c->stream>>>(n, (int)acls.size(), d_ac, d_acc,
+                                                                                   d_bi, nitems, d_part, dG);
+      QDKGB_CHECK_LAUNCH();
+    }
+    QDKGB_CUDA(cudaMemcpyAsync(h4.data(), dG, n4 * 8, cudaMemcpyDeviceToHost, c->stream));
+    QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+    for (size_t i = 0; i < n4; ++i) aabb[i] += h4[i];
+  }
+
+  // ---------------- same spin (aaaa + aa from alpha pairs, bbbb + bb from beta pairs)
+  for (int blk = 0; blk < 2; ++blk) {
+    double* o4 = blk == 0 ? aaaa : bbbb;
+    double* o2 = blk == 0 ? aa : bb;
+    if (!o4 && !o2) continue;
+    const std::vector<uint64_t>& strs = blk == 0 ? S.h_galpha : S.h_ubeta;
+    const std::vector<int32_t>& rk = blk == 0 ? ra : rb;
+    // unordered string pairs within a double excitation, lower rank first
+    std::vector<int2> pairs;
+    const int64_t ns = (int64_t)strs.size();
+    for (int64_t x = 0; x < ns; ++x) {
+      const uint64_t s0 = strs[x];
+      pairs.push_back({(int)x, (int)x});
+      std::vector<int> occ, vir;
+      for (int p = 0; p < n; ++p) ((s0 >> p) & 1 ? occ : vir).push_back(p);
+      auto add = [&](uint64_t t) {
+        const int32_t y = rk[t];
+        if (y < 0) throw Error(QDKGB_ERR_UNSUPPORTED, "RDM: strings are not a complete set");
+        if (y > x) pairs.push_back({(int)x, (int)y});
+      };
+      for (int o : occ)
+        for (int v : vir) add(s0 ^ (1ull << o) ^ (1ull << v));
+      for (size_t a = 0; a < occ.size(); ++a)
+        for (size_t b2 = a + 1; b2 < occ.size(); ++b2)
+          for (size_t u = 0; u < vir.size(); ++u)
+            for (size_t w = u + 1; w < vir.size(); ++w)
+              add(s0 ^ (1ull << occ[a]) ^ (1ull << occ[b2]) ^ (1ull << vir[u]) ^ (1ull << vir[w]));
+    }
+    const int64_t np = (int64_t)pairs.size();
+    int2* d_pairs = (int2*)dev_alloc(c, buf.b[9], np * sizeof(int2) + 16);
+    QDKGB_CUDA(cudaMemcpyAsync(d_pairs, pairs.data(), np * sizeof(int2), cudaMemcpyHostToDevice, c->stream));
+    double* d_S = dev_array<double>(c, buf.b[10], np);
+    const double* X = dC;
+    int64_t cols = nb;
+    if (blk == 1) {  // columns of C as rows
+      double* Ct = dev_array<double>(c, buf.b[11], N);
+      transpose_f64(c, dC, Ct, na, nb);
+      X = Ct;
+      cols = na;
+    }
+    k_pair_overlap<<<(unsigned)std::min<int64_t>((np * 32 + 255) / 256, (int64_t)c->sm_count * 64), 256, 0,
+                     c->stream>>>(np, d_pairs, X, cols, d_S);
+    QDKGB_CHECK_LAUNCH();
+    uint64_t* d_str = (uint64_t*)dev_alloc(c, buf.b[1], strs.size() * 8 + 16);
+    QDKGB_CUDA(cudaMemcpyAsync(d_str, strs.data(), strs.size() * 8, cudaMemcpyHostToDevice, c->stream));
+    double* d4 = dev_array<double>(c, buf.b[2], n4);
+    double* d2 = dev_array<double>(c, buf.b[3], n2);
+    QDKGB_CUDA(cudaMemsetAsync(d4, 0, n4 * 8, c->stream));
+    QDKGB_CUDA(cudaMemsetAsync(d2, 0, n2 * 8, c->stream));
+    RdmTarget T;
+    T.block = blk;
+    T.n = n;
+    T.s_lo = 0;
+    T.s_hi = n;
+    T.t4 = d4;
+    T.t2 = d2;
+    T.shared = false;
+    T.with_ordm = true;
+    k_rdm_cas_same_spin<<<(unsigned)std::min<int64_t>((np + 255) / 256, (int64_t)c->sm_count * 16), 256, 0,
+                          c->stream>>>(np, d_pairs, d_str, d_S, T);
+    QDKGB_CHECK_LAUNCH();
+    QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+    if (o4) {
+      QDKGB_CUDA(cudaMemcpy(h4.data(), d4, n4 * 8, cudaMemcpyDeviceToHost));
+      for (size_t i = 0; i < n4; ++i) o4[i] += h4[i];
+    }
+    if (o2) {
+      QDKGB_CUDA(cudaMemcpy(h2.data(), d2, n2 * 8, cudaMemcpyDeviceToHost));
+      for (size_t i = 0; i < n2; ++i) o2[i] += h2[i];
+    }
+  }
+  return true;
+}
+
 void rdms_spin_dep(Context* c, const double* C, double* aa, double* bb, double* aaaa, double* bbbb, double* aabb) {
   NvtxRange nvtx_range("qdkgb.rdms");
   if (!c->have_ints) throw Error(QDKGB_ERR_STATE, "integrals not set (needed for the orbital count)");
@@ -193,6 +570,11 @@ void rdms_spin_dep(Context* c, const double* C, double* aa, double* bb, double* 
   DeviceBuffer &bC = scratch.b[0], &b4 = scratch.b[1], &b2 = scratch.b[2];
   double* dC = dev_array<double>(c, bC, N);
   QDKGB_CUDA(cudaMemcpyAsync(dC, C, N * 8, cudaMemcpyHostToDevice, c->stream));
+  // QDKGB_RDM_PAIR_WALK=1 keeps complete spaces on the pair walk (a test
+  // compares the two paths)
+  const char* walk = getenv("QDKGB_RDM_PAIR_WALK");
+  const bool force_walk = walk && walk[0] == '1';
+  if (!force_walk && cas_rdm_eligible(c) && rdms_cas(c, dC, aa, bb, aaaa, bbbb, aabb)) return;
   double* d4 = dev_array<double>(c, b4, n4);
   double* d2 = dev_array<double>(c, b2, n2);
   RowArgs a = row_args(c, 0.);

@@ -151,6 +151,13 @@ class OracleDevice:
         self.M = self.o.build_csr(self.H, self.a, self.b, thresh)
         return self.M.nnz
 
+    def build_operator(self, thresh=np.finfo(np.float64).eps, storage=0, max_m=200):
+        self.build_hamiltonian(thresh, storage)
+        return "csr"
+
+    def set_device_limit(self, nbytes):
+        pass
+
     def get_csr(self, index_bits=64):
         return self.M.arrays()
 

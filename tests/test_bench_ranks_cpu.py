@@ -63,10 +63,10 @@ def test_reference_arm_runs_on_rank_zero_only(monkeypatch, capsys):
     monkeypatch.setenv("RANK", "1")
     monkeypatch.setenv("WORLD_SIZE", "2")
     called = []
-    monkeypatch.setattr(bench, "cpu_estimate", lambda *a, **k: called.append(1))
+    monkeypatch.setattr(bench, "cpu_full_run", lambda *a, **k: called.append(1))
 
     class Args:
-        steps, warmup, cpu_stride, fp64_iters = 1, 0, 16, 66
+        steps, warmup, gpus = 1, 0, 2
 
     assert bench.run_reference(Args()) is None
     assert not called and capsys.readouterr().out == ""
@@ -75,11 +75,12 @@ def test_reference_arm_runs_on_rank_zero_only(monkeypatch, capsys):
 def test_reference_arm_json_contract():
     """bench.py --impl reference prints one JSON line with the keys of the
     bench contract (metric, value, unit, timing, config, cpu_baseline, e2e),
-    here on a CAS(6e,6o) sample so that it runs in about a second."""
+    here on CAS(6e,6o) so that a full run takes about a second: the value is
+    the mean of full CPU runs (no extrapolation), each one's time listed."""
     import json
     import subprocess
     out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
-                          "--warmup", "0", "--norb", "6", "--nel", "6", "--nchol", "12", "--cpu-stride", "2"],
+                          "--warmup", "0", "--norb", "6", "--nel", "6", "--nchol", "12"],
                          capture_output=True, text=True, timeout=300, cwd=ROOT)
     assert out.returncode == 0, out.stderr[-2000:]
     line = json.loads(out.stdout.strip().splitlines()[-1])
@@ -91,5 +92,7 @@ def test_reference_arm_json_contract():
     assert abs(line["ms_per_step"] - line["value"] * 1e3) < 1e-6 * line["ms_per_step"]
     cb, e2e = line["cpu_baseline"], line["e2e"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == line["value"] and cb["sample"]
+    assert cb["sample"].startswith("full") and cb["runs"] == 1 and cb["run_values"] == [line["value"]]
+    assert cb["iterations"] > 0 and cb["energy"] < 0
     assert e2e["value"] == line["value"] and e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
     assert line["config"]["workload"]
