@@ -608,6 +608,7 @@ def run_asci(args):
     Eg, a, b, c, _ = capi.asci(ctx, [a0], [b0], [1.0], E0, grow=True, refine=False, **kw)
     torch.cuda.synchronize()
     t_grow = time.perf_counter() - t0
+    phases_grow = capi.asci_phase_times(ctx)
     t0 = time.perf_counter()
     refined = True
     try:
@@ -617,6 +618,7 @@ def run_asci(args):
         E = Eg
     torch.cuda.synchronize()
     t_ref = time.perf_counter() - t0
+    phases_refine = capi.asci_phase_times(ctx)
     # the configuration's two roots: FP64 H build + block Davidson on the final space
     t0 = time.perf_counter()
     ctx.set_dets(a, b)
@@ -634,6 +636,9 @@ def run_asci(args):
                                    "grow factor 8, FP64 H build + Davidson (lowest root)",
                        "ntdets_max": args.asci_dets, "n_chol": nchol, "diag_spacing": 0.1, "seed": SEED},
             "grow_s": t_grow, "refine_s": t_ref, "refine_converged": refined,
+            "phases": {"grow": phases_grow, "refine": phases_refine,
+                       "note": "seconds per phase (determinant search, determinant-space set-up, H build, "
+                               "Davidson), host-synchronised"},
             "two_roots": {"seconds": t_roots, "energies": [float(x) for x in E2],
                           "iterations": info2["iterations"], "sigma_applications": info2["spmv_fp64"],
                           "residual_norm": info2["residual_norm"], "nnz": int(ctx.nnz)},

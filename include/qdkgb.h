@@ -174,6 +174,14 @@ int qdkgb_diagonal(qdkgb_context* ctx, double* D);
 int qdkgb_spmv(qdkgb_context* ctx, int precision, const double* x, double* y);
 /* Same on device vectors: FP64 mode takes double*, MIXED mode float*. */
 int qdkgb_spmv_device(qdkgb_context* ctx, int precision, const void* x, void* y);
+/* The Davidson operator seam of the reference,
+ * SparseMatrixOperator::operator_action(m, alpha, V, LDV, beta, AV, LDAV)
+ * (include/macis/solvers/davidson.hpp:79-90, gespmbv): AV = alpha H V + beta AV
+ * for m column-major host vectors of ndets (leading dimensions LDV, LDAV >=
+ * ndets), FP64, with whichever operator is built (stored or direct sigma).
+ * beta == 0 overwrites AV without reading it, as BLAS does. */
+int qdkgb_operator_action(qdkgb_context* ctx, int64_t m, double alpha, const double* V, int64_t ldv, double beta,
+                          double* AV, int64_t ldav);
 
 /* ------------------------------------------------------------ eigensolver */
 typedef struct qdkgb_davidson_settings {
@@ -212,6 +220,13 @@ int qdkgb_davidson(qdkgb_context* ctx, const qdkgb_davidson_settings* s, double*
                    qdkgb_davidson_info* info);
 
 /* ------------------------------------------------------------ RDMs
+ * SortedDoubleLoopHamiltonianGenerator::form_rdms (sorted_double_loop.hpp:
+ * 512-624): the spin-traced 1-RDM (n x n) and 2-RDM (n^4), ACCUMULATED (+=);
+ * NULL skips.  ordm = aa + bb and trdm(p,q,r,s) = aaaa + bbbb + aabb(p,q,r,s)
+ * + aabb(r,s,p,q) of the spin-resolved blocks below, the identity the
+ * reference's two routines satisfy. */
+int qdkgb_rdms(qdkgb_context* ctx, const double* C, double* ordm, double* trdm);
+/*
  * SortedDoubleLoopHamiltonianGenerator::form_rdms_spin_dep
  * (sorted_double_loop.hpp:626-753, contributions util/rdms.hpp:39-612):
  * spin-resolved 1-RDMs (n x n) and 2-RDMs (n^4), column-major, MACIS index
@@ -273,6 +288,13 @@ int qdkgb_asci(qdkgb_context* ctx, const qdkgb_asci_settings* s, const qdkgb_dav
                int64_t n0, const uint64_t* a0, const uint64_t* b0, const double* c0, double E0, int do_grow,
                int do_refine, int64_t cap, uint64_t* out_a, uint64_t* out_b, double* out_c, int64_t* n_out,
                double* E_out, double* E_grow_out);
+/* Where the last qdkgb_asci call on this context spent its time (no
+ * counterpart; the reference logs the same phases through its asci_search /
+ * h_build / davidson loggers): seconds[0] the determinant searches,
+ * seconds[1] the determinant-space set-ups, seconds[2] the Hamiltonian
+ * builds, seconds[3] the Davidson solves; *iterations (may be NULL) the
+ * asci_iter count. */
+int qdkgb_asci_phase_times(const qdkgb_context* ctx, double* seconds, int64_t* iterations);
 
 /* ASCI-PT2 (asci_pt2_constraint, external/macis/include/macis/asci/pt2.hpp:
  * 59-565): E_PT2 = sum over the determinants Q outside the wavefunction of

@@ -61,10 +61,10 @@ def casci_energy(h1, eri, nalpha, nbeta, core=None, tol=1e-10, precision="fp64",
     return CASCIEnergy.apply(h1, eri, core, int(nalpha), int(nbeta), float(tol), precision, int(device), int(max_m))
 
 
-def rdms_as_gradients(h1, eri, nalpha, nbeta, tol=1e-10):
+def rdms_as_gradients(h1, eri, nalpha, nbeta, tol=1e-10, precision="fp64"):
     """(E, dE/dh1, dE/deri) through autograd (convenience for callers)."""
     h1 = h1.detach().clone().requires_grad_(True)
     eri = eri.detach().clone().requires_grad_(True)
-    E = casci_energy(h1, eri, nalpha, nbeta, tol=tol)
+    E = casci_energy(h1, eri, nalpha, nbeta, tol=tol, precision=precision)
     E.backward()
     return E.detach(), h1.grad, eri.grad

@@ -40,6 +40,7 @@ EXPORTED = [
     "qdkgb_davidson", "qdkgb_rdms_spin_dep", "qdkgb_orbital_entropies", "qdkgb_casci",
     "qdkgb_mcscf_default_settings", "qdkgb_casscf", "qdkgb_version", "qdkgb_kernel_launches",
     "qdkgb_sigma_split_noalloc", "qdkgb_set_csr", "qdkgb_build_direct_sigma", "qdkgb_build_operator",
+    "qdkgb_operator_action", "qdkgb_rdms", "qdkgb_asci_phase_times",
     "qdkgb_asci_default_settings", "qdkgb_asci_search", "qdkgb_asci", "qdkgb_asci_pt2",
     "qdkgb_batch_default_settings", "qdkgb_casci_batch",
 ]
@@ -135,6 +136,9 @@ def lib():
     L.qdkgb_get_csr64.argtypes = [vp, vp, vp, vp]
     L.qdkgb_get_csr32_rows.argtypes = [vp, i64, i64, vp, vp, vp]
     L.qdkgb_build_operator.argtypes = [vp, dp, ci, ci, P(ci), P(i64)]
+    L.qdkgb_operator_action.argtypes = [vp, i64, dp, vp, i64, dp, vp, i64]
+    L.qdkgb_rdms.argtypes = [vp, vp, vp, vp]
+    L.qdkgb_asci_phase_times.argtypes = [vp, vp, P(i64)]
     L.qdkgb_get_csr64_rows.argtypes = [vp, i64, i64, vp, vp, vp]
     L.qdkgb_diagonal.argtypes = [vp, vp]
     L.qdkgb_set_csr.argtypes = [vp, i64, vp, vp, vp]
@@ -419,7 +423,8 @@ class Context:
             s.use_guess = 0 if guess is None else 1
             E = np.zeros(nroots)
             info = DavidsonInfo()
-            self._check(lib().qdkgb_davidson(self._h, ctypes.byref(s), _ptr(E), _ptr(C), ctypes.byref(info)))
+            self._check(lib().qdkgb_davidson(self._h, ctypes.byref(s), E.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                             _ptr(C), ctypes.byref(info)))
             return E, (C.reshape((self.ndets, nroots), order="F") if C is not None else None), info.as_dict()
         C = np.zeros(self.ndets) if guess is None else _f64(guess).copy()
         if not want_vector and guess is None:
@@ -443,6 +448,25 @@ class Context:
                 ptrs.append(None)
         self._check(lib().qdkgb_rdms_spin_dep(self._h, _ptr(C), *ptrs))
         return {k: v.reshape((n, n) if len(k) == 2 else (n, n, n, n), order="F") for k, v in bufs.items()}
+
+    def operator_action(self, V, alpha=1.0, AV=None, beta=0.0):
+        """AV = alpha H V + beta AV for the columns of V (ndets x m), the
+        reference's operator_action block contract (qdkgb_operator_action)."""
+        Vf = np.asfortranarray(np.asarray(V, dtype=np.float64).reshape(self.ndets, -1))
+        m = Vf.shape[1]
+        out = np.zeros((self.ndets, m), order="F") if AV is None else np.asfortranarray(
+            np.array(AV, dtype=np.float64).reshape(self.ndets, m))
+        self._check(lib().qdkgb_operator_action(self._h, m, float(alpha), Vf.ctypes.data, self.ndets, float(beta),
+                                                out.ctypes.data, self.ndets))
+        return out
+
+    def rdms(self, C):
+        """Spin-traced (1-RDM, 2-RDM) of form_rdms (qdkgb_rdms)."""
+        n = self.norb
+        o1 = np.zeros(n * n)
+        o2 = np.zeros(n ** 4)
+        self._check(lib().qdkgb_rdms(self._h, _ptr(_f64(C)), _ptr(o1), _ptr(o2)))
+        return o1.reshape((n, n), order="F"), o2.reshape((n, n, n, n), order="F")
 
     def orbital_entropies(self, C, two_orbital=True, mutual_information=True):
         """(single-orbital entropies (n), two-orbital entropies (n x n) or None,
@@ -543,6 +567,15 @@ def asci(ctx, alpha0, beta0, c0, E0, grow=True, refine=True, tol=1e-8, max_m=200
                                 _ptr(oc), ctypes.byref(n), ctypes.byref(E), ctypes.byref(Eg)))
     m = min(n.value, cap)
     return E.value, oa[:m].copy(), ob[:m].copy(), oc[:m].copy(), Eg.value
+
+
+def asci_phase_times(ctx):
+    """Seconds of the last asci call by phase (search, determinant space,
+    H build, Davidson) and its asci_iter count (qdkgb_asci_phase_times)."""
+    t = np.zeros(4)
+    it = ctypes.c_int64()
+    ctx._check(lib().qdkgb_asci_phase_times(ctx.handle, _ptr(t), ctypes.byref(it)))
+    return {"search_s": t[0], "det_space_s": t[1], "hbuild_s": t[2], "davidson_s": t[3], "iterations": it.value}
 
 
 def default_batch_settings(**kw):

@@ -9,17 +9,20 @@
 // singles, alpha-alpha, beta-beta, alpha-beta doubles), evaluates c_P <Q|H|P>
 // and the fast diagonal E0 - H_QQ exactly as the reference does, drops
 // |c h| < h_el_tol, and accumulates into an open-addressing hash table keyed by
-// the full (alpha, beta) pair (128-bit atomicCAS, FP64 atomicAdd of c h).
-// That replaces the reference's constraint partitioning plus sort-and-
-// accumulate: every Q's contributions meet in one slot.  The core itself is
-// inserted with an infinite score and so drops out.  Then |rv| = |sum / (E0 -
-// H_QQ)| is pruned (|rv| > rv_prune_tol), the k-th largest |rv| is found by a
-// radix select on the bit patterns (four 16-bit digits), and every candidate
-// with |rv| >= that value is kept - the reference's tie-inclusive top-k.
-// Summation order inside a slot follows the atomic order, so scores agree
-// with the reference to rounding; selected sets are identical unless two
-// scores tie to the last bits at the cutoff.
+// the full (alpha, beta) pair (128-bit atomicCAS, then exact fixed-point
+// integer atomics of c h; see Table below).  That replaces the reference's
+// constraint partitioning plus sort-and-accumulate: every Q's contributions
+// meet in one slot.  The core itself is marked and drops out.  Then |rv| =
+// |sum / (E0 - H_QQ)| is pruned (|rv| > rv_prune_tol), the k-th largest |rv|
+// is found by a radix select on the bit patterns (four 16-bit digits), and
+// every candidate with |rv| >= that value is kept - the reference's
+// tie-inclusive top-k.  Sums and diagonals do not depend on the order of the
+// atomics, so a search repeated on the same input selects the same set with
+// the same scores; they agree with the reference's (whose unstable sort
+// fixes its own order) to rounding, and the selected sets are identical
+// unless two scores tie to the last bits at the cutoff.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <vector>
 
@@ -44,32 +47,65 @@ __device__ __forceinline__ uint64_t mix64(uint64_t x) {
   return x;
 }
 
+// A target's accumulated c <Q|H|P> is kept in fixed point, two 64-bit words
+// per slot: x = hi 2^-32 + lo 2^-76 with hi = rint(x 2^32) and lo the rest
+// in units of 2^-76 (the split is exact).  Integer additions are exact and
+// associative, so the sum - and the selection made from it - does not depend
+// on the order in which the atomics land (FP64 atomics would).  |x| < 2^20
+// and up to 2^19 contributions per target keep both words in range.  The
+// slot's diagonal E0 - H_QQ (the fast diagonal, computed from each
+// contributing P, equal up to rounding) is the largest bit pattern among its
+// contributors (atomicMax on the bits: order-independent as well); core
+// determinants set it to kCoreMark and drop out of the candidates.
+constexpr long long kCoreMark = 0x7fffffffffffffffLL;
+constexpr long long kHdEmpty = (long long)0x8000000000000000ULL;
+constexpr double kFixHi = 4294967296.0;               // 2^32
+constexpr double kFixLo = 75557863725914323419136.0;  // 2^76
+
 struct Table {
   u128* keys;
-  double* sum;
-  double* hd;
+  long long* acc;  // 2 words per slot (hi, lo)
+  long long* hd;   // bit pattern of E0 - H_QQ, or kCoreMark
   uint64_t mask;
   int* err;  // set when a probe sequence runs past kMaxProbe (the table is too full): the pass is redone larger
 };
 constexpr uint64_t kMaxProbe = 4096;
 
-__device__ __forceinline__ void table_add(const Table& t, uint64_t qa, uint64_t qb, double ch, double hd) {
+__device__ __forceinline__ double table_sum(const Table& t, uint64_t i) {
+  return (double)t.acc[2 * i] * (1.0 / kFixHi) + (double)t.acc[2 * i + 1] * (1.0 / kFixLo);
+}
+__device__ __forceinline__ bool table_core(const Table& t, uint64_t i) { return t.hd[i] == kCoreMark; }
+
+// slot of (qa, qb), inserting the key; -1 when the probe limit is reached
+__device__ __forceinline__ int64_t table_slot(const Table& t, uint64_t qa, uint64_t qb) {
   const u128 key = ((u128)qb << 64) | (u128)qa;
   uint64_t h = mix64(qa * 0x9e3779b97f4a7c15ULL ^ mix64(qb)) & t.mask;
   for (uint64_t probe = 0; probe <= t.mask && probe < kMaxProbe; ++probe) {
     const u128 old = atomicCAS(t.keys + h, kEmpty, key);
-    if (old == kEmpty) {
-      t.hd[h] = hd;
-      atomicAdd(t.sum + h, ch);
-      return;
-    }
-    if (old == key) {
-      atomicAdd(t.sum + h, ch);
-      return;
-    }
+    if (old == kEmpty || old == key) return (int64_t)h;
     h = (h + 1) & t.mask;
   }
   *t.err = 1;
+  return -1;
+}
+
+__device__ __forceinline__ void table_add(const Table& t, uint64_t qa, uint64_t qb, double ch, double hd) {
+  const int64_t h = table_slot(t, qa, qb);
+  if (h < 0) return;
+  if (!(fabs(ch) < 1048576.0)) {  // outside the fixed-point range (or not finite)
+    *t.err = 2;
+    return;
+  }
+  const double hi = rint(ch * kFixHi);
+  const double lo = rint((ch - hi * (1.0 / kFixHi)) * kFixLo);
+  atomicAdd((unsigned long long*)t.acc + 2 * h, (unsigned long long)(long long)hi);
+  atomicAdd((unsigned long long*)t.acc + 2 * h + 1, (unsigned long long)(long long)lo);
+  atomicMax(t.hd + h, (long long)__double_as_longlong(hd));
+}
+
+__device__ __forceinline__ void table_add_core(const Table& t, uint64_t qa, uint64_t qb) {
+  const int64_t h = table_slot(t, qa, qb);
+  if (h >= 0) atomicMax(t.hd + h, kCoreMark);
 }
 
 struct CoreArgs {
@@ -165,7 +201,7 @@ __global__ void __launch_bounds__(kAsciWarps * 32) k_asci_enum(CoreArgs A) {
     hdiag = __shfl_sync(QDKGB_FULL_MASK, hdiag, 0);
     __syncwarp();
     // the core determinant itself: infinite score (removed later)
-    if (lane == 0 && (A.npass == 1 || part_of(Pa, Pb, A.npass) == A.pass)) table_add(A.T, Pa, Pb, INFINITY, 1.0);
+    if (lane == 0 && (A.npass == 1 || part_of(Pa, Pb, A.npass) == A.pass)) table_add_core(A.T, Pa, Pb);
     const int64_t nsa = (int64_t)ka * na_v, nsb = (int64_t)kb * nb_v;
     const int64_t pa_o = (int64_t)ka * (ka - 1) / 2, pa_v = (int64_t)na_v * (na_v - 1) / 2;
     const int64_t pb_o = (int64_t)kb * (kb - 1) / 2, pb_v = (int64_t)nb_v * (nb_v - 1) / 2;
@@ -356,12 +392,9 @@ __global__ void k_asci_extract(Table T, uint64_t cap, double prune, uint64_t* __
     const uint64_t i = i0 + threadIdx.x;
     bool take = false;
     double arv = 0.;
-    if (i < cap && T.keys[i] != kEmpty) {
-      const double sm = T.sum[i];
-      if (!isinf(sm)) {
-        arv = fabs(sm / T.hd[i]);
-        take = arv > prune;
-      }
+    if (i < cap && T.keys[i] != kEmpty && !table_core(T, i)) {
+      arv = fabs(table_sum(T, i) / __longlong_as_double(T.hd[i]));
+      take = arv > prune;
     }
     const unsigned m = __ballot_sync(QDKGB_FULL_MASK, take);
     unsigned long long base = 0;
@@ -423,12 +456,10 @@ __global__ void __launch_bounds__(256) k_pt2_sum(Table T, uint64_t cap, double* 
   double s = 0.;
   unsigned long long m = 0;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < cap; i += (uint64_t)gridDim.x * blockDim.x) {
-    if (T.keys[i] != kEmpty) {
-      const double v = T.sum[i];
-      if (!isinf(v)) {
-        s += v * v / T.hd[i];
-        ++m;
-      }
+    if (T.keys[i] != kEmpty && !table_core(T, i)) {
+      const double v = table_sum(T, i);
+      s += v * v / __longlong_as_double(T.hd[i]);
+      ++m;
     }
   }
   s = warp_sum(s);
@@ -450,10 +481,12 @@ __global__ void __launch_bounds__(256) k_pt2_sum(Table T, uint64_t cap, double* 
   }
 }
 
-__global__ void k_fill_empty(u128* keys, double* sum, uint64_t cap) {
+__global__ void k_fill_empty(Table T, uint64_t cap) {
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < cap; i += (uint64_t)gridDim.x * blockDim.x) {
-    keys[i] = kEmpty;
-    sum[i] = 0.;
+    T.keys[i] = kEmpty;
+    T.acc[2 * i] = 0;
+    T.acc[2 * i + 1] = 0;
+    T.hd[i] = kHdEmpty;
   }
 }
 
@@ -538,22 +571,23 @@ void asci_search_gpu(Context* c, int64_t ncore, const uint64_t* ca, const uint64
   while ((double)cap < want) cap <<= 1;
   size_t freeb = 0, totb = 0;
   QDKGB_CUDA(cudaMemGetInfo(&freeb, &totb));
-  const size_t slot_bytes = 16 + 8 + 8 + 16;  // key, sum, hd, candidate key + slot
+  const size_t slot_bytes = 16 + 16 + 8 + 16;  // key, fixed-point sum, hd, candidate key + slot
   if (cap * slot_bytes > freeb / 2) throw Error(QDKGB_ERR_OOM, "ASCI search: hash table does not fit in device memory");
   const unsigned eb = (unsigned)std::min<int64_t>((ncore + kAsciWarps - 1) / kAsciWarps, (int64_t)c->sm_count * 16);
   for (;;) {
     u128* keys = (u128*)dev_alloc(c, bkeys, cap * 16 + 256);
     keys = (u128*)(((uintptr_t)keys + 15) & ~(uintptr_t)15);
-    A.T = Table{keys, dev_array<double>(c, bsum, cap), dev_array<double>(c, bhd, cap), cap - 1, err};
+    A.T = Table{keys, dev_array<long long>(c, bsum, 2 * cap), dev_array<long long>(c, bhd, cap), cap - 1, err};
     const unsigned fb = (unsigned)std::min<uint64_t>((cap + 255) / 256, (uint64_t)c->sm_count * 64);
     QDKGB_CUDA(cudaMemsetAsync(err, 0, sizeof(int), c->stream));
-    k_fill_empty<<<fb, 256, 0, c->stream>>>(keys, A.T.sum, cap);
+    k_fill_empty<<<fb, 256, 0, c->stream>>>(A.T, cap);
     QDKGB_CHECK_LAUNCH();
     k_asci_enum<<<eb, kAsciWarps * 32, 0, c->stream>>>(A);
     QDKGB_CHECK_LAUNCH();
     int herr = 0;
     QDKGB_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+    if (herr == 2) throw Error(QDKGB_ERR_UNSUPPORTED, "ASCI: a contribution |c H| >= 2^20 is outside the accumulator range");
     if (!herr) break;
     if ((cap << 1) * slot_bytes > freeb / 2) throw Error(QDKGB_ERR_OOM, "ASCI search: hash table overflow");
     cap <<= 1;
@@ -568,6 +602,7 @@ void asci_search_gpu(Context* c, int64_t ncore, const uint64_t* ca, const uint64
   QDKGB_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   QDKGB_CUDA(cudaMemcpyAsync(&ncand, cnt, sizeof(ncand), cudaMemcpyDeviceToHost, c->stream));
   QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+  if (herr == 2) throw Error(QDKGB_ERR_UNSUPPORTED, "ASCI: a contribution |c H| >= 2^20 is outside the accumulator range");
   if (herr) throw Error(QDKGB_ERR_OOM, "ASCI search: hash table overflow");
   if (n_candidates) *n_candidates = (int64_t)ncand;
   const int64_t topk = ndets_max - ncore;
@@ -682,7 +717,7 @@ double asci_pt2_gpu(Context* c, int64_t nd, const uint64_t* a, const uint64_t* b
   while ((double)need < want) need <<= 1;
   size_t freeb = 0, totb = 0;
   QDKGB_CUDA(cudaMemGetInfo(&freeb, &totb));
-  const size_t slot_bytes = 16 + 8 + 8;  // key, sum, E0 - H_QQ
+  const size_t slot_bytes = 16 + 16 + 8;  // key, fixed-point sum, E0 - H_QQ
   const size_t budget = freeb / 2;
   const uint64_t slot_max = max_slots > 0 ? std::max<uint64_t>((uint64_t)max_slots, 1024) : ~0ull;
   auto fits = [&](uint64_t cp) { return cp * slot_bytes <= budget && cp <= slot_max; };
@@ -704,10 +739,10 @@ double asci_pt2_gpu(Context* c, int64_t nd, const uint64_t* a, const uint64_t* b
     for (;;) {
       u128* keys = (u128*)dev_alloc(c, bkeys, cap * 16 + 256);
       keys = (u128*)(((uintptr_t)keys + 15) & ~(uintptr_t)15);
-      A.T = Table{keys, dev_array<double>(c, bsum, cap), dev_array<double>(c, bhd, cap), cap - 1, err};
+      A.T = Table{keys, dev_array<long long>(c, bsum, 2 * cap), dev_array<long long>(c, bhd, cap), cap - 1, err};
       const unsigned fb = (unsigned)std::min<uint64_t>((cap + 255) / 256, (uint64_t)c->sm_count * 64);
       QDKGB_CUDA(cudaMemsetAsync(err, 0, sizeof(int), c->stream));
-      k_fill_empty<<<fb, 256, 0, c->stream>>>(keys, A.T.sum, cap);
+      k_fill_empty<<<fb, 256, 0, c->stream>>>(A.T, cap);
       QDKGB_CHECK_LAUNCH();
       k_asci_enum<<<eb, kAsciWarps * 32, 0, c->stream>>>(A);
       QDKGB_CHECK_LAUNCH();
@@ -718,7 +753,8 @@ double asci_pt2_gpu(Context* c, int64_t nd, const uint64_t* a, const uint64_t* b
       QDKGB_CUDA(cudaMemcpyAsync(hp.data(), partial, sb * 8, cudaMemcpyDeviceToHost, c->stream));
       QDKGB_CUDA(cudaMemcpyAsync(hc.data(), pcount, sb * 8, cudaMemcpyDeviceToHost, c->stream));
       QDKGB_CUDA(cudaStreamSynchronize(c->stream));
-      if (!herr) break;
+      if (herr == 2) throw Error(QDKGB_ERR_UNSUPPORTED, "ASCI: a contribution |c H| >= 2^20 is outside the accumulator range");
+    if (!herr) break;
       if (!fits(cap << 1)) throw Error(QDKGB_ERR_OOM, "ASCI PT2: hash table overflow");
       cap <<= 1;
     }
@@ -744,6 +780,23 @@ struct HDet {
 inline bool hspin_less(const HDet& x, const HDet& y) { return x.a != y.a ? x.a < y.a : x.b < y.b; }
 inline bool hdet_eq(const HDet& x, const HDet& y) { return x.a == y.a && x.b == y.b; }
 
+// Wall time of the ASCI phases (synchronised: each phase ends in a host
+// sync anyway), accumulated into Context::asci_phase_s.
+struct PhaseClock {
+  Context* c;
+  std::chrono::steady_clock::time_point t;
+  explicit PhaseClock(Context* ctx) : c(ctx) {
+    QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+    t = std::chrono::steady_clock::now();
+  }
+  void lap(int phase) {
+    QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+    const auto now = std::chrono::steady_clock::now();
+    c->asci_phase_s[phase] += std::chrono::duration<double>(now - t).count();
+    t = now;
+  }
+};
+
 // selected_ci_diag (selected_ci_diag.hpp:111-158) on the device for a list
 // sorted by spin_comparator; X is the guess (empty: diagonal guess) and the
 // eigenvector on return.
@@ -755,9 +808,12 @@ double sci_diag_gpu(Context* c, const qdkgb_asci_settings& S, const qdkgb_davids
     a[i] = dets[i].a;
     b[i] = dets[i].b;
   }
+  PhaseClock clock(c);
   build_det_space(c, n, a.data(), b.data());
+  clock.lap(1);
   const bool mixed = ci.precision == QDKGB_PREC_MIXED;
   build_hamiltonian(c, matel_tol, mixed ? QDKGB_H_SPLIT32 : QDKGB_H_FP64);
+  clock.lap(2);
   qdkgb_davidson_settings s = ci;
   s.nroots = 1;  // the ASCI iterations solve for the lowest root, as the reference's do
   s.use_guess = X.empty() ? 0 : 1;
@@ -765,6 +821,7 @@ double sci_diag_gpu(Context* c, const qdkgb_asci_settings& S, const qdkgb_davids
   if (!s.use_guess) std::fill(X.begin(), X.end(), 0.);
   double E = 0.;
   davidson(c, &s, &E, X.data(), nullptr);
+  clock.lap(3);
   (void)S;
   return E;
 }
@@ -774,6 +831,7 @@ double asci_iter_gpu(Context* c, const qdkgb_asci_settings& S, const qdkgb_david
                      int64_t ndets_max, double E0, std::vector<HDet>& wfn, std::vector<double>& X,
                      int64_t* ncand) {
   NvtxRange nvtx_range("qdkgb.asci_iter");
+  ++c->asci_iters;
   if (wfn.size() > 1) {  // reorder_ci_on_coeff (determinant_sort.hpp:45-64)
     std::vector<size_t> idx(wfn.size());
     for (size_t i = 0; i < idx.size(); ++i) idx[i] = i;
@@ -821,8 +879,12 @@ double asci_iter_gpu(Context* c, const qdkgb_asci_settings& S, const qdkgb_david
     cb[i] = wfn[i].b;
   }
   std::vector<uint64_t> na, nb;
-  asci_search_gpu(c, (int64_t)nkeep, ca.data(), cb.data(), X.data(), E0, ndets_max, S.h_el_tol, S.rv_prune_tol, na,
-                  nb, ncand, S.just_singles != 0);
+  {
+    PhaseClock clock(c);
+    asci_search_gpu(c, (int64_t)nkeep, ca.data(), cb.data(), X.data(), E0, ndets_max, S.h_el_tol, S.rv_prune_tol,
+                    na, nb, ncand, S.just_singles != 0);
+    clock.lap(0);
+  }
   wfn.resize(na.size());
   for (size_t i = 0; i < na.size(); ++i) wfn[i] = {na[i], nb[i]};
   std::sort(wfn.begin(), wfn.end(), hspin_less);
@@ -863,6 +925,8 @@ void asci_run(Context* c, const qdkgb_asci_settings& S, const qdkgb_davidson_set
   if (!(S.growth_backoff_rate > 0.0 && S.growth_backoff_rate < 1.0))
     throw Error(QDKGB_ERR_INVALID, "growth_backoff_rate must be in (0, 1)");
   if (!(S.growth_recovery_rate > 1.0)) throw Error(QDKGB_ERR_INVALID, "growth_recovery_rate must be > 1.0");
+  for (double& t : c->asci_phase_s) t = 0.;
+  c->asci_iters = 0;
   std::vector<HDet> wfn(a.size());
   for (size_t i = 0; i < a.size(); ++i) wfn[i] = {a[i], b[i]};
   int64_t ncand = 0;

@@ -508,6 +508,58 @@ int qdkgb_davidson(qdkgb_context* c, const qdkgb_davidson_settings* s, double* E
   });
 }
 
+int qdkgb_operator_action(qdkgb_context* c, int64_t m, double alpha, const double* V, int64_t ldv, double beta,
+                          double* AV, int64_t ldav) {
+  if (!c) return QDKGB_ERR_INVALID;
+  return guarded(c, [&] {
+    Hcsr& H = c->H;
+    if (!H.valid) throw Error(QDKGB_ERR_STATE, "Hamiltonian not built");
+    const int64_t n = H.n;
+    if (m < 0 || (m > 0 && (!V || !AV || ldv < n || ldav < n))) throw Error(QDKGB_ERR_INVALID, "bad block shape");
+    if (m == 0) return;
+    QDKGB_CUDA(cudaSetDevice(c->device));
+    ScopedBuffers<2> buf(c);
+    double* dx = dev_array<double>(c, buf.b[0], n);
+    double* dy = dev_array<double>(c, buf.b[1], n);
+    std::vector<double> y(n);
+    for (int64_t j = 0; j < m; ++j) {
+      QDKGB_CUDA(cudaMemcpyAsync(dx, V + j * ldv, n * 8, cudaMemcpyHostToDevice, c->stream));
+      spmv_fp64(c, dx, dy);
+      QDKGB_CUDA(cudaMemcpyAsync(y.data(), dy, n * 8, cudaMemcpyDeviceToHost, c->stream));
+      QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+      double* out = AV + j * ldav;
+      if (beta == 0.)
+        for (int64_t i = 0; i < n; ++i) out[i] = alpha * y[i];
+      else
+        for (int64_t i = 0; i < n; ++i) out[i] = alpha * y[i] + beta * out[i];
+    }
+  });
+}
+
+int qdkgb_rdms(qdkgb_context* c, const double* C, double* ordm, double* trdm) {
+  if (!c) return QDKGB_ERR_INVALID;
+  return guarded(c, [&] {
+    if (!C) throw Error(QDKGB_ERR_INVALID, "null CI vector");
+    if (!c->have_dets) throw Error(QDKGB_ERR_STATE, "determinants not set");
+    if (!c->have_ints) throw Error(QDKGB_ERR_STATE, "integrals not set (needed for the orbital count)");
+    if (!ordm && !trdm) return;
+    QDKGB_CUDA(cudaSetDevice(c->device));
+    const size_t n = (size_t)c->norb, n2 = n * n, n4 = n2 * n2;
+    std::vector<double> aa(ordm ? n2 : 0), bb(ordm ? n2 : 0), aaaa(trdm ? n4 : 0), bbbb(trdm ? n4 : 0),
+        aabb(trdm ? n4 : 0);
+    rdms_spin_dep(c, C, ordm ? aa.data() : nullptr, ordm ? bb.data() : nullptr, trdm ? aaaa.data() : nullptr,
+                  trdm ? bbbb.data() : nullptr, trdm ? aabb.data() : nullptr);
+    if (ordm)
+      for (size_t i = 0; i < n2; ++i) ordm[i] += aa[i] + bb[i];
+    if (trdm)
+      for (size_t pq = 0; pq < n2; ++pq)
+        for (size_t rs = 0; rs < n2; ++rs) {
+          const size_t i = pq + n2 * rs;
+          trdm[i] += aaaa[i] + bbbb[i] + aabb[i] + aabb[rs + n2 * pq];
+        }
+  });
+}
+
 int qdkgb_rdms_spin_dep(qdkgb_context* c, const double* C, double* aa, double* bb, double* aaaa, double* bbbb,
                         double* aabb) {
   if (!c) return QDKGB_ERR_INVALID;
@@ -629,6 +681,13 @@ int qdkgb_asci(qdkgb_context* c, const qdkgb_asci_settings* s, const qdkgb_david
       if (out_c) out_c[i] = X[i];
     }
   });
+}
+
+int qdkgb_asci_phase_times(const qdkgb_context* c, double* seconds, int64_t* iterations) {
+  if (!c || !seconds) return QDKGB_ERR_INVALID;
+  for (int i = 0; i < 4; ++i) seconds[i] = c->asci_phase_s[i];
+  if (iterations) *iterations = c->asci_iters;
+  return QDKGB_OK;
 }
 
 int qdkgb_build_operator(qdkgb_context* c, double thresh, int storage, int max_m, int* layout, int64_t* nnz) {

@@ -137,6 +137,11 @@ struct Context {
   DirectSigma* direct = nullptr;  // recompute-on-the-fly operator (complete spaces)
   FciStruct* fci = nullptr;       // row-shape tables of a complete space (structured kernels)
   bool op_direct = false;         // Davidson / spmv use the direct sigma instead of the CSR
+  // seconds spent by the last qdkgb_asci call in its phases: the determinant
+  // search, the determinant-space set-up, the Hamiltonian build, Davidson;
+  // and its asci_iter count
+  double asci_phase_s[4] = {0., 0., 0., 0.};
+  int64_t asci_iters = 0;
   DeviceBuffer host_pinned_dummy;
   double* pinned = nullptr;  // small pinned host staging (64 doubles)
 };

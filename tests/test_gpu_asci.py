@@ -89,3 +89,31 @@ def test_asci_just_singles_and_taper_match_oracle(ctx, pkg, oracle, h2o):
     Eo, oa, _, _, _ = oracle.asci(H, [a0], [b0], [1.0], E0, refine=False, ntdets_max=1000, core_fixed=1,
                                   taper_grow_factor=1.1)
     assert len(ta) >= 1000 and abs(tc @ tc - 1) < 1e-12 and abs(Eg - Eo) < 1e-6
+
+
+def test_asci_grow_repeats_bit_for_bit(pkg):
+    """Two grows from the same start on the same context select the same
+    determinants in the same order with bit-identical coefficients and
+    energy: the search's sums and diagonals do not depend on the order in
+    which its atomics land.  The phase timer reports every phase."""
+    import os
+
+    from conftest import GOLDEN, unpack_eri
+    capi = pkg.capi
+    d = np.load(os.path.join(GOLDEN, "ref_asci40.npz"))
+    norb = int(d["norb"])
+    a0, b0 = pkg.determinants.canonical_hf(int(d["nalpha"]), int(d["nbeta"]))
+    runs = []
+    with capi.Context(0) as ctx:
+        ctx.set_integrals(d["T"], unpack_eri(d["V_packed"], norb))
+        ctx.set_dets(np.array([a0], np.uint64), np.array([b0], np.uint64))
+        ctx.build_hamiltonian()
+        E0 = float(ctx.diagonal()[0])
+        for _ in range(2):
+            _, a, b, c, Eg = capi.asci(ctx, [a0], [b0], [1.0], E0, grow=True, refine=False, ntdets_max=50000,
+                                       core_selection_fixed=1, ncdets_max=10000, grow_factor=8)
+            runs.append((a, b, c, Eg, capi.asci_phase_times(ctx)))
+    (a1, b1, c1, E1, t1), (a2, b2, c2, E2, _) = runs
+    assert np.array_equal(a1, a2) and np.array_equal(b1, b2)
+    assert np.array_equal(c1.view(np.uint64), c2.view(np.uint64)) and E1 == E2
+    assert t1["iterations"] > 0 and all(t1[k] > 0 for k in ("search_s", "det_space_s", "hbuild_s", "davidson_s"))

@@ -97,7 +97,7 @@ def test_cas14_rdm_energy_identity(ctx, pkg):
     ctx.set_integrals(T, V)
     ctx.set_dets(a, b)
     ctx.build_direct_sigma()
-    E, C, _ = ctx.davidson(tol=1e-8, max_m=400)
+    E, C, _ = ctx.davidson(tol=1e-8)
     R = ctx.rdms_spin_dep(C)
     E_rdm = np.sum(T * (R["aa"] + R["bb"])) + np.sum(V * (R["aaaa"] + R["bbbb"])) + 2 * np.sum(V * R["aabb"])
     assert abs(E_rdm - E) < 1e-10, (E_rdm, E)
@@ -106,3 +106,36 @@ def test_cas14_rdm_energy_identity(ctx, pkg):
     assert abs(np.einsum("iikk->", R["aabb"]) - 0.5 * 49) < 1e-9
     assert np.max(np.abs(R["aabb"] - R["aabb"].transpose(1, 0, 3, 2))) < 1e-12
     assert np.max(np.abs(R["aa"] - R["aa"].T)) < 1e-12
+
+
+def test_spin_traced_rdms_match_reference_form_rdms(ctx, capi):
+    """qdkgb_rdms against the reference's own form_rdms (tests/golden/
+    ref_cas8.npz, the reference's CI vector), to 1e-12; it accumulates."""
+    from conftest import GOLDEN
+    d = np.load(os.path.join(GOLDEN, "ref_cas8.npz"))
+    a, b = capi.fci_dets(8, 4, 4)
+    ctx.set_integrals(d["T"], d["V"])
+    ctx.set_dets(a, b)
+    o1, o2 = ctx.rdms(d["C"])
+    assert np.max(np.abs(o1 - d["rdm_traced1"])) < 1e-12
+    assert np.max(np.abs(o2 - d["rdm_traced2"])) < 1e-12
+
+
+def test_operator_action_block_contract(ctx, capi, pkg, oracle):
+    """qdkgb_operator_action: AV = alpha H V + beta AV over a block of
+    columns (davidson.hpp:79-90), beta = 0 ignoring AV's contents."""
+    T, V, _ = pkg.integrals.synthetic_integrals(8, 16, seed=90)
+    a, b = capi.fci_dets(8, 4, 4)
+    ctx.set_integrals(T, V)
+    ctx.set_dets(a, b)
+    ctx.build_hamiltonian()
+    M = oracle.build_csr(oracle.Hamiltonian(T, V), a, b)
+    rng = np.random.default_rng(3)
+    X = rng.normal(size=(len(a), 3))
+    Y0 = rng.normal(size=(len(a), 3))
+    Y = ctx.operator_action(X, alpha=2.0, AV=Y0, beta=0.5)
+    ref = np.stack([2.0 * M.spmv(X[:, j]) + 0.5 * Y0[:, j] for j in range(3)], axis=1)
+    assert np.max(np.abs(Y - ref)) < 1e-11 * np.max(np.abs(ref))
+    Z = ctx.operator_action(X, AV=np.full((len(a), 3), np.nan), beta=0.0)
+    assert np.all(np.isfinite(Z))
+    assert np.max(np.abs(Z[:, 1] - M.spmv(X[:, 1]))) < 1e-11 * np.max(np.abs(Z))
