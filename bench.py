@@ -373,6 +373,8 @@ def run_ours(args):
                      "traffic": traffic, "algorithmic_bytes": bytes32, "launch_ms": t_spmv32 * 1e3},
         "spmv_fp64": {"kernel": kern64, "achieved_gbs": achieved64, "frac": achieved64 / peak,
                       "launch_ms": t_spmv64 * 1e3, "algorithmic_bytes": bytes64},
+        "sigma_autotune": {"fp32": dict(zip(("segments", "candidates_ms"), ctx.sigma_plan(capi.PREC_MIXED))),
+                           "fp64": dict(zip(("segments", "candidates_ms"), ctx.sigma_plan(capi.PREC_FP64)))},
         "hbuild_s": float(np.mean(hbs)), "davidson_s": float(np.mean(dvs)),
         "davidson": {k: infos[-1][k] for k in ("iterations", "spmv_fp64", "spmv_fp32", "restarts", "residual_norm")},
         "fp64_path": {"time_to_energy_s": float(np.mean(fp64_times)), "hbuild_s": hb64, "davidson_s": dv64,

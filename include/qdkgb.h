@@ -142,6 +142,17 @@ int qdkgb_build_direct_sigma(qdkgb_context* ctx);
  * the drop-in calculators reach that size.  qdkgb_casci uses it. */
 int qdkgb_build_operator(qdkgb_context* ctx, double thresh, int storage, int max_m, int* layout, int64_t* nnz);
 
+/* Introspection of the complete-space sigma's work split (no counterpart):
+ * each CTA takes one segment of an alpha group's row.  The number of
+ * segments is chosen by a measured autotuner: the first sigma of each
+ * precision on a new space (outside any stream capture) times every
+ * candidate count, one untimed and three timed sigmas each, and keeps the
+ * fastest.  *segments receives the count in use (0: no complete-space
+ * sigma); with ncand (in: capacity, out: candidates tried) the candidates'
+ * counts and mean milliseconds, empty before the first sigma. */
+int qdkgb_sigma_plan(qdkgb_context* ctx, int precision, int* segments, int* ncand, int* cand_segments,
+                     double* cand_ms);
+
 /* Copies the device CSR to host buffers (rowptr: ndets+1, colind/values: nnz).
  * For QDKGB_H_SPLIT32 storage, values receive (double)hi + (double)lo.
  * The 32-bit and 64-bit variants mirror make_csr_hamiltonian_block_32bit_ /

@@ -40,7 +40,7 @@ EXPORTED = [
     "qdkgb_davidson", "qdkgb_rdms_spin_dep", "qdkgb_orbital_entropies", "qdkgb_casci",
     "qdkgb_mcscf_default_settings", "qdkgb_casscf", "qdkgb_version", "qdkgb_kernel_launches",
     "qdkgb_sigma_split_noalloc", "qdkgb_set_csr", "qdkgb_build_direct_sigma", "qdkgb_build_operator",
-    "qdkgb_operator_action", "qdkgb_rdms", "qdkgb_asci_phase_times",
+    "qdkgb_operator_action", "qdkgb_rdms", "qdkgb_asci_phase_times", "qdkgb_sigma_plan",
     "qdkgb_asci_default_settings", "qdkgb_asci_search", "qdkgb_asci", "qdkgb_asci_pt2",
     "qdkgb_batch_default_settings", "qdkgb_casci_batch",
 ]
@@ -139,6 +139,7 @@ def lib():
     L.qdkgb_operator_action.argtypes = [vp, i64, dp, vp, i64, dp, vp, i64]
     L.qdkgb_rdms.argtypes = [vp, vp, vp, vp]
     L.qdkgb_asci_phase_times.argtypes = [vp, vp, P(i64)]
+    L.qdkgb_sigma_plan.argtypes = [vp, ci, P(ci), P(ci), vp, vp]
     L.qdkgb_get_csr64_rows.argtypes = [vp, i64, i64, vp, vp, vp]
     L.qdkgb_diagonal.argtypes = [vp, vp]
     L.qdkgb_set_csr.argtypes = [vp, i64, vp, vp, vp]
@@ -448,6 +449,17 @@ class Context:
                 ptrs.append(None)
         self._check(lib().qdkgb_rdms_spin_dep(self._h, _ptr(C), *ptrs))
         return {k: v.reshape((n, n) if len(k) == 2 else (n, n, n, n), order="F") for k, v in bufs.items()}
+
+    def sigma_plan(self, precision=PREC_MIXED):
+        """(segments in use, [(candidate segments, mean ms), ...]) of the
+        complete-space sigma's autotuner (qdkgb_sigma_plan)."""
+        seg = ctypes.c_int()
+        n = ctypes.c_int(32)
+        cs = np.zeros(32, dtype=np.int32)
+        cm = np.zeros(32)
+        self._check(lib().qdkgb_sigma_plan(self._h, precision, ctypes.byref(seg), ctypes.byref(n), cs.ctypes.data,
+                                           cm.ctypes.data))
+        return seg.value, [(int(cs[i]), float(cm[i])) for i in range(min(n.value, 32))]
 
     def operator_action(self, V, alpha=1.0, AV=None, beta=0.0):
         """AV = alpha H V + beta AV for the columns of V (ndets x m), the

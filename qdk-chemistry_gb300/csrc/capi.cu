@@ -683,6 +683,20 @@ int qdkgb_asci(qdkgb_context* c, const qdkgb_asci_settings* s, const qdkgb_david
   });
 }
 
+int qdkgb_sigma_plan(qdkgb_context* c, int precision, int* segments, int* ncand, int* cand_segments,
+                     double* cand_ms) {
+  if (!c || !segments) return QDKGB_ERR_INVALID;
+  std::vector<std::pair<int, double>> rec;
+  *segments = struct_sigma_plan(c, precision == QDKGB_PREC_MIXED ? 0 : 1, &rec);
+  const int cap = ncand ? *ncand : 0;
+  if (ncand) *ncand = (int)rec.size();
+  for (int i = 0; i < std::min(cap, (int)rec.size()); ++i) {
+    if (cand_segments) cand_segments[i] = rec[i].first;
+    if (cand_ms) cand_ms[i] = rec[i].second;
+  }
+  return QDKGB_OK;
+}
+
 int qdkgb_asci_phase_times(const qdkgb_context* c, double* seconds, int64_t* iterations) {
   if (!c || !seconds) return QDKGB_ERR_INVALID;
   for (int i = 0; i < 4; ++i) seconds[i] = c->asci_phase_s[i];

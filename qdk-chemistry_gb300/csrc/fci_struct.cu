@@ -51,6 +51,11 @@ struct SlabPlan {
   DeviceBuffer rec, segh;
 };
 
+struct PlanHost {
+  int S = 0, M = 0, R = 0;
+  std::vector<int32_t> rec, segh;
+};
+
 struct FciStruct {
   int64_t G = 0, Nb = 0;
   int n1 = 0, n2 = 0;  // beta list lengths (level <= 1, level <= 2), uniform
@@ -59,12 +64,21 @@ struct FciStruct {
   DeviceBuffer gdesc;  // [G][rowlen] h << 11 | list entry (kListAlphaDouble: b itself)
   SlabPlan plan[2];    // staged x of 4 bytes (FP32) / 8 bytes (FP64, split pair)
   DeviceBuffer ypart;  // [S][n] partial sums (S > 1)
+  // segment-count autotuner: candidate plans (host) until the first
+  // single-instance sigma of each plan times them and keeps the fastest;
+  // then the record of that choice: (S, mean ms) per candidate
+  std::vector<PlanHost> cand[2];
+  bool tuned[2] = {false, false};
+  std::vector<std::pair<int, double>> tune_ms[2];
+  // spin-pair tables of the table-driven emission (rebuilt with every build)
+  DeviceBuffer tab_b, tab_bm, tab_a, tab_am;
 };
 
 void free_struct(Context* c) {
   if (!c->fci) return;
   for (DeviceBuffer* b : {&c->fci->blT, &c->fci->gdesc, &c->fci->plan[0].rec, &c->fci->plan[0].segh,
-                          &c->fci->plan[1].rec, &c->fci->plan[1].segh, &c->fci->ypart})
+                          &c->fci->plan[1].rec, &c->fci->plan[1].segh, &c->fci->ypart, &c->fci->tab_b,
+                          &c->fci->tab_bm, &c->fci->tab_a, &c->fci->tab_am})
     dev_free(c, *b);
   delete c->fci;
   c->fci = nullptr;
@@ -102,10 +116,8 @@ void build_struct(Context* c) {
   // (index of the own-group / alpha-single block in the row, -1 for an
   // alpha double)
   int rowlen = -1, c1 = -1, c2 = -1;
-  struct PlanHost {
-    int S, M, R;
-    std::vector<int32_t> rec, segh;
-  } plan_tmp[2];
+  PlanHost plan_tmp[2];
+  std::vector<PlanHost> cand_tmp[2];
   std::vector<uint32_t> gdesc;
   std::vector<int32_t> pblock;  // [G][rowlen]
   {
@@ -202,7 +214,7 @@ void build_struct(Context* c) {
   for (int pl = 0; pl < 2; ++pl) {
     const size_t xsize = pl == 0 ? 4 : 8;
     auto smem_of = [&](int M, int R) { return (size_t)M * Nb * xsize + ((size_t)R * 4 + 15) / 16 * 16; };
-    int best_S = -1, best_M = 0, best_R = 0;
+    int best_S = -1;
     double best = -1.;
     // CTA shape of the sigma that uses the plan (the FP32 one is vectorised
     // over 4 or 2 beta strings when Nb allows)
@@ -216,10 +228,12 @@ void build_struct(Context* c) {
       bz = (int)((Nb + kSlabThreads - 1) / kSlabThreads);
       threads = (int)(((Nb + bz - 1) / bz + 31) / 32 * 32);
     }
+    std::vector<int> feasible;
     for (int S = 1; S <= kMaxS && S <= rowlen; ++S) {
       const int M = shapeM[S], R = shapeR[S];
       const size_t sm = smem_of(M, R);
       if (sm > kSlabPlanMax[pl]) continue;
+      feasible.push_back(S);
       // resident CTAs per SM: threads, 64 registers per thread, shared memory
       const int64_t per_sm = std::max<int64_t>(
           1, std::min<int64_t>(std::min<int64_t>(2048 / threads, 65536 / (64 * threads)), (227 * 1024) / (int64_t)sm));
@@ -229,52 +243,64 @@ void build_struct(Context* c) {
       if (score > best) {
         best = score;
         best_S = S;
-        best_M = M;
-        best_R = R;
       }
     }
     if (best_S < 0) return;
-    const int S = best_S, M = best_M, R = best_R;
-    std::vector<int32_t> rec((size_t)G * S * R, 0), segh((size_t)G * S * M, -1);
-    for (int64_t g = 0; g < G; ++g) {
-      int cur = -1, nslot = 0, nb1 = 0;
-      int32_t* r = nullptr;
-      auto close = [&]() {
-        if (!r) return;
-        r[3] = nb1;
-        r[4 + 2 * nb1] = (int32_t)(dd.size() / 2);
-        std::copy(dd.begin(), dd.end(), r + 6 + 2 * nb1);
-      };
-      for (int i = item0[g]; i < item0[g + 1]; ++i) {
-        const Item& it = items[i];
-        const int sg = seg_of(it, S);
-        if (sg != cur) {
-          close();
-          cur = sg;
-          r = &rec[((size_t)g * S + sg) * R];
-          nslot = nb1 = 0;
-          dd.clear();
+    // the occupancy model's choice first, then the other feasible counts of
+    // at least 4 segments (fewer leave most SMs idle for these row counts)
+    std::vector<int> cands{best_S};
+    for (int S : feasible)
+      if (S != best_S && S >= std::min(4, best_S)) cands.push_back(S);
+    for (int S : cands) {
+      const int M = shapeM[S], R = shapeR[S];
+      std::vector<int32_t> rec((size_t)G * S * R, 0), segh((size_t)G * S * M, -1);
+      for (int64_t g = 0; g < G; ++g) {
+        int cur = -1, nslot = 0, nb1 = 0;
+        int32_t* r = nullptr;
+        auto close = [&]() {
+          if (!r) return;
+          r[3] = nb1;
+          r[4 + 2 * nb1] = (int32_t)(dd.size() / 2);
+          std::copy(dd.begin(), dd.end(), r + 6 + 2 * nb1);
+        };
+        for (int i = item0[g]; i < item0[g + 1]; ++i) {
+          const Item& it = items[i];
+          const int sg = seg_of(it, S);
+          if (sg != cur) {
+            close();
+            cur = sg;
+            r = &rec[((size_t)g * S + sg) * R];
+            nslot = nb1 = 0;
+            dd.clear();
+          }
+          if (it.len == 0) {
+            dd.push_back((int32_t)(it.p * Nb));
+            dd.push_back((int32_t)(it.h * Nb));
+            continue;
+          }
+          const int slot = nslot++;
+          segh[((size_t)g * S + sg) * M + slot] = it.h;
+          if (it.h == g) {
+            r[0] = 1;
+            r[1] = (int32_t)(it.p * Nb);
+            r[2] = (int32_t)(slot * Nb);
+          } else {
+            r[4 + 2 * nb1] = (int32_t)(it.p * Nb);
+            r[5 + 2 * nb1] = (int32_t)(slot * Nb);
+            ++nb1;
+          }
         }
-        if (it.len == 0) {
-          dd.push_back((int32_t)(it.p * Nb));
-          dd.push_back((int32_t)(it.h * Nb));
-          continue;
-        }
-        const int slot = nslot++;
-        segh[((size_t)g * S + sg) * M + slot] = it.h;
-        if (it.h == g) {
-          r[0] = 1;
-          r[1] = (int32_t)(it.p * Nb);
-          r[2] = (int32_t)(slot * Nb);
-        } else {
-          r[4 + 2 * nb1] = (int32_t)(it.p * Nb);
-          r[5 + 2 * nb1] = (int32_t)(slot * Nb);
-          ++nb1;
-        }
+        close();
       }
-      close();
+      PlanHost ph;
+      ph.S = S;
+      ph.M = M;
+      ph.R = R;
+      ph.rec = std::move(rec);
+      ph.segh = std::move(segh);
+      if (S == best_S) plan_tmp[pl] = ph;
+      cand_tmp[pl].push_back(std::move(ph));
     }
-    plan_tmp[pl] = {S, M, R, std::move(rec), std::move(segh)};
   }
   // transposed beta lists
   std::vector<int32_t> b1(Nb * n1), b2(Nb * n2), blT((n1 + n2) * Nb);
@@ -302,6 +328,8 @@ void build_struct(Context* c) {
     F->plan[pl].R = plan_tmp[pl].R;
     up(F->plan[pl].rec, plan_tmp[pl].rec.data(), plan_tmp[pl].rec.size() * 4);
     up(F->plan[pl].segh, plan_tmp[pl].segh.data(), plan_tmp[pl].segh.size() * 4);
+    F->cand[pl] = std::move(cand_tmp[pl]);
+    F->tuned[pl] = F->cand[pl].size() <= 1;
   }
   c->fci = F;
 }
@@ -408,6 +436,169 @@ __global__ void __launch_bounds__(kEmitThreads)
     if (kept) atomicAdd(kept + r, (unsigned long long)cnt);
   }
 }
+
+// ------------------------------------------------------------------ emission from spin-pair tables
+// The single-instance build emits the same values as k_slab_emit (bit for
+// bit) with far fewer FP64 operations per element, by evaluating once per
+// string pair what the reference's element formulas compute from one spin's
+// strings alone, in the same summation order:
+//   * a single excitation of one spin (matrix_element_2,
+//     matrix_elements.hpp:169-189) is h = T(v,o) + sum_{p in bra, same spin}
+//     G_red(p,v,o) + sum_{p in bra, other spin} V_red(p,v,o); its first two
+//     terms depend only on the excited spin's (bra, ket) pair, so the table
+//     holds that partial sum and the element adds the other spin's terms
+//     (6 additions at CAS(12,12) instead of 13);
+//   * a same-spin double (matrix_element_4, :113-121) depends only on that
+//     spin's pair: the table holds the value;
+//   * an opposite-spin double (matrix_element_22, :140-151) is a signed
+//     integral gather, done from the tables' orbital indices and signs.
+// Which determinant is the bra follows the CSR build (the lower index), so
+// the tables are oriented per pair.  Tables: per (beta list entry k, beta
+// string b) for the beta pairs, per (alpha group g, row position p) for the
+// alpha pairs; metadata v | o << 8 | neg << 16 | kind << 24.
+namespace {
+constexpr uint32_t kPairSingle = 1u << 24, kPairDouble = 2u << 24;
+
+__device__ __forceinline__ double single_partial(const Integrals& I, uint64_t bra, const SingleEx& s) {
+  const size_t n = (size_t)I.n;
+  double h = ld(I.T + s.v + n * s.o);
+  const double* g = I.G_red + n * (s.v + n * s.o);
+  for (uint64_t m = bra; m; m &= m - 1) h += ld(g + low_bit(m));
+  return h;
+}
+
+// beta pairs: own-group entries (k < n2) oriented by the beta index (the
+// same group); level-1 entries (alpha-single blocks) unoriented: the orbital
+// only in b, the one only in bc, and the sign (equal in both orientations)
+__global__ void k_emit_beta_table(SlabArgs A, Integrals I, const uint64_t* __restrict__ ubeta,
+                                  double* __restrict__ bt, uint32_t* __restrict__ bm) {
+  const int64_t tot = (int64_t)(A.n2 + A.n1) * A.Nb;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < tot; t += (int64_t)gridDim.x * blockDim.x) {
+    const int k = (int)(t / A.Nb), b = (int)(t - (int64_t)k * A.Nb);
+    const int bc = __ldg(A.blT + t);
+    uint32_t meta = 0;
+    double val = 0.;
+    if (bc != b) {
+      const uint64_t rb = ubeta[b], rc = ubeta[bc];
+      const uint64_t ex = rb ^ rc;
+      if (k < A.n2) {
+        const uint64_t bra = bc > b ? rb : rc, ket = bc > b ? rc : rb;
+        if (popc64(ex) == 2) {
+          const SingleEx sx = single_ex(bra, ket, ex);
+          val = single_partial(I, bra, sx);
+          meta = sx.v | (sx.o << 8) | ((uint32_t)sx.neg << 16) | kPairSingle;
+        } else {
+          val = me_same_spin_double(I, bra, ket, ex);
+          meta = kPairDouble;
+        }
+      } else {
+        const SingleEx sx = single_ex(rb, rc, ex);
+        meta = sx.v | (sx.o << 8) | ((uint32_t)sx.neg << 16) | kPairSingle;
+      }
+    }
+    bt[t] = val;
+    bm[t] = meta;
+  }
+}
+
+// alpha pairs per row position (alpha-single blocks and alpha doubles),
+// oriented by the group index
+__global__ void k_emit_alpha_table(SlabArgs A, Integrals I, const uint64_t* __restrict__ galpha,
+                                   double* __restrict__ at, uint32_t* __restrict__ am) {
+  const int64_t tot = (int64_t)A.G * A.rowlen;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < tot; t += (int64_t)gridDim.x * blockDim.x) {
+    const int g = (int)(t / A.rowlen);
+    const uint32_t d = __ldg(A.gdesc + t);
+    const int h = (int)(d >> 11), k = (int)(d & 2047u);
+    uint32_t meta = 0;
+    double val = 0.;
+    if (h != g) {
+      const uint64_t ra = galpha[g], rh = galpha[h];
+      const uint64_t bra = h > g ? ra : rh, ket = h > g ? rh : ra;
+      const uint64_t ex = ra ^ rh;
+      if (k == kListAlphaDouble) {
+        val = me_same_spin_double(I, bra, ket, ex);
+        meta = kPairDouble;
+      } else {
+        const SingleEx sx = single_ex(bra, ket, ex);
+        val = single_partial(I, bra, sx);
+        meta = sx.v | (sx.o << 8) | ((uint32_t)sx.neg << 16) | kPairSingle;
+      }
+    }
+    at[t] = val;
+    am[t] = meta;
+  }
+}
+
+template <int STORAGE>
+__global__ void __launch_bounds__(kEmitThreads)
+    k_slab_emit_tab(SlabArgs A, Integrals I, const uint64_t* __restrict__ galpha, const uint64_t* __restrict__ ubeta,
+                    const double* __restrict__ bt, const uint32_t* __restrict__ bm, const double* __restrict__ at,
+                    const uint32_t* __restrict__ am, long long tbits, const double* __restrict__ diag_raw,
+                    double* __restrict__ val, float* __restrict__ hi, double* __restrict__ diag,
+                    unsigned long long* __restrict__ kept) {
+  const int g = blockIdx.x / kEmitSegments, s = blockIdx.x - g * kEmitSegments;
+  const int p0 = s * A.seglen, p1 = min(A.rowlen, p0 + A.seglen);
+  const int Nb = A.Nb;
+  const size_t n = (size_t)I.n;
+  const int b = blockIdx.y * blockDim.x + threadIdx.x;
+  if (b >= Nb) return;
+  const int64_t r = (int64_t)g * Nb + b;
+  const uint64_t ra = galpha[g], rb = ubeta[b];
+  unsigned cnt = 0;
+  for (int p = p0; p < p1; ++p) {
+    const int64_t gp = (int64_t)g * A.rowlen + p;
+    const uint32_t d = __ldg(A.gdesc + gp);
+    const int h = (int)(d >> 11), k = (int)(d & 2047u);
+    double v;
+    bool is_diag = false;
+    if (k == kListAlphaDouble) {
+      v = __ldg(at + gp);  // alpha double: one value for the whole group row
+    } else {
+      const int64_t kb = (int64_t)k * Nb + b;
+      const int bc = __ldg(A.blT + kb);
+      if (h == g) {
+        if (bc == b) {
+          is_diag = true;
+          v = diag_raw[r];
+        } else {
+          const uint32_t m = __ldg(bm + kb);
+          if (m & kPairDouble) {
+            v = __ldg(bt + kb);
+          } else {  // beta single: the alpha string's V_red terms
+            double x = __ldg(bt + kb);
+            const double* vr = I.V_red + n * ((m & 255u) + n * ((m >> 8) & 255u));
+            for (uint64_t q = ra; q; q &= q - 1) x += ld(vr + low_bit(q));
+            v = flip_if(x, (m >> 16) & 1u);
+          }
+        }
+      } else {
+        const uint32_t ma = __ldg(am + gp);
+        const uint32_t av = ma & 255u, ao = (ma >> 8) & 255u;
+        if (bc == b) {  // alpha single: the beta string's V_red terms
+          double x = __ldg(at + gp);
+          const double* vr = I.V_red + n * (av + n * ao);
+          for (uint64_t q = rb; q; q &= q - 1) x += ld(vr + low_bit(q));
+          v = flip_if(x, (ma >> 16) & 1u);
+        } else {  // opposite-spin double, oriented like the alpha pair
+          const uint32_t mb = __ldg(bm + kb);
+          const uint32_t xb = mb & 255u, xc = (mb >> 8) & 255u;
+          const uint32_t bv = h > g ? xb : xc, bo = h > g ? xc : xb;
+          v = flip_if(Vat(I, av, ao, bv, bo), ((ma >> 16) & 1u) != ((mb >> 16) & 1u));
+        }
+      }
+    }
+    const bool keep = above_thresh(v, tbits);
+    if (is_diag && diag) diag[r] = keep ? v : 0.;
+    if (!keep) v = 0.;
+    cnt += keep;
+    const int64_t q = gp * Nb + b;
+    val[q] = v;
+    if (STORAGE == kSlabF64F32) hi[q] = __double2float_rn(v);
+  }
+  if (kept) atomicAdd(kept + r, (unsigned long long)cnt);
+}
+}  // namespace
 
 // ------------------------------------------------------------------ export
 // Slab -> CSR (rowptr given): a thread per row writes it in column order.
@@ -827,8 +1018,73 @@ __global__ void k_slab_combine(int64_t n, int S, const T* __restrict__ part, T* 
 }
 
 template <int MODE>
+void slab_sigma_launch(Context* c, int B, const int* active, const void* vals, const float* vlo, const void* x,
+                       const float* xlo, void* y);
+
+// Times every candidate segment count of the plan on this call's inputs
+// (one untimed and three timed sigmas each, CUDA events on the context's
+// stream) and keeps the fastest; single-instance sigmas only, never inside a
+// stream capture.
+template <int MODE>
+void slab_sigma_tune(Context* c, const void* vals, const float* vlo, const void* x, const float* xlo, void* y) {
+  FciStruct* F = c->fci;
+  const int pl = MODE == 0 ? 0 : 1;
+  SlabPlan& PL = F->plan[pl];
+  cudaEvent_t e0, e1;
+  QDKGB_CUDA(cudaEventCreate(&e0));
+  QDKGB_CUDA(cudaEventCreate(&e1));
+  auto load = [&](const PlanHost& ph) {
+    PL.S = ph.S;
+    PL.M = ph.M;
+    PL.R = ph.R;
+    void* r = dev_alloc(c, PL.rec, ph.rec.size() * 4 + 16);
+    void* g = dev_alloc(c, PL.segh, ph.segh.size() * 4 + 16);
+    QDKGB_CUDA(cudaMemcpyAsync(r, ph.rec.data(), ph.rec.size() * 4, cudaMemcpyHostToDevice, c->stream));
+    QDKGB_CUDA(cudaMemcpyAsync(g, ph.segh.data(), ph.segh.size() * 4, cudaMemcpyHostToDevice, c->stream));
+  };
+  int best = 0;
+  double best_ms = 1e300;
+  F->tune_ms[pl].clear();
+  for (size_t i = 0; i < F->cand[pl].size(); ++i) {
+    load(F->cand[pl][i]);
+    slab_sigma_launch<MODE>(c, 1, nullptr, vals, vlo, x, xlo, y);
+    QDKGB_CUDA(cudaEventRecord(e0, c->stream));
+    for (int r = 0; r < 3; ++r) slab_sigma_launch<MODE>(c, 1, nullptr, vals, vlo, x, xlo, y);
+    QDKGB_CUDA(cudaEventRecord(e1, c->stream));
+    QDKGB_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    QDKGB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    F->tune_ms[pl].push_back({F->cand[pl][i].S, ms / 3.0});
+    if (ms / 3.0 < best_ms) {
+      best_ms = ms / 3.0;
+      best = (int)i;
+    }
+  }
+  load(F->cand[pl][best]);
+  QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+  QDKGB_CUDA(cudaEventDestroy(e0));
+  QDKGB_CUDA(cudaEventDestroy(e1));
+  F->cand[pl].clear();
+  F->cand[pl].shrink_to_fit();
+  F->tuned[pl] = true;
+}
+
+template <int MODE>
 void slab_sigma(Context* c, int B, const int* active, const void* vals, const float* vlo, const void* x,
-                const float* xlo, void* y) {
+                const float* xlo, void* y, bool may_tune = false) {
+  FciStruct* F = c->fci;
+  const int pl = MODE == 0 ? 0 : 1;
+  if (may_tune && B == 1 && !F->tuned[pl]) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    QDKGB_CUDA(cudaStreamIsCapturing(c->stream, &cs));
+    if (cs == cudaStreamCaptureStatusNone) slab_sigma_tune<MODE>(c, vals, vlo, x, xlo, y);
+  }
+  slab_sigma_launch<MODE>(c, B, active, vals, vlo, x, xlo, y);
+}
+
+template <int MODE>
+void slab_sigma_launch(Context* c, int B, const int* active, const void* vals, const float* vlo, const void* x,
+                       const float* xlo, void* y) {
   FciStruct* F = c->fci;
   SlabPlan& PL = F->plan[MODE == 0 ? 0 : 1];
   PlanArgs P{PL.S, PL.M, PL.R, (const int32_t*)PL.rec.ptr, (const int32_t*)PL.segh.ptr};
@@ -878,20 +1134,28 @@ void slab_sigma(Context* c, int B, const int* active, const void* vals, const fl
 
 }  // namespace
 
+// the sigma plan of a precision (0: FP32, 1: FP64): segments in use and the
+// autotuner's record (S, ms) per candidate (empty before the first sigma)
+int struct_sigma_plan(Context* c, int pl, std::vector<std::pair<int, double>>* record) {
+  if (!c->fci || pl < 0 || pl > 1) return 0;
+  if (record) *record = c->fci->tune_ms[pl];
+  return c->fci->plan[pl].S;
+}
+
 int64_t struct_slab_elements(Context* c) { return c->fci ? c->fci->G * c->fci->Nb * c->fci->rowlen : 0; }
 
 bool struct_ready(Context* c) { return c->fci && c->H.valid && !c->op_direct && c->H.structured; }
 
 // Both storages keep the FP64 values of a single-instance slab (val).
 void struct_spmv_fp64(Context* c, const double* x, double* y) {
-  slab_sigma<1>(c, 1, nullptr, c->H.val.ptr, nullptr, x, nullptr, y);
+  slab_sigma<1>(c, 1, nullptr, c->H.val.ptr, nullptr, x, nullptr, y, true);
 }
 
 void struct_spmv_fp32(Context* c, const float* x, float* y) {
   Hcsr& H = c->H;
   if (H.storage != QDKGB_H_SPLIT32)
     throw Error(QDKGB_ERR_STATE, "FP32 sigma needs the Hamiltonian built with QDKGB_H_SPLIT32 storage");
-  slab_sigma<0>(c, 1, nullptr, H.hi.ptr, nullptr, x, nullptr, y);
+  slab_sigma<0>(c, 1, nullptr, H.hi.ptr, nullptr, x, nullptr, y, true);
 }
 
 // ------------------------------------------------------------------ batches
@@ -983,12 +1247,24 @@ void build_hamiltonian_struct(Context* c, double thresh, int storage) {
   const uint64_t* ga = (const uint64_t*)D.galpha.ptr;
   const uint64_t* ub = (const uint64_t*)D.ubeta.ptr;
   unsigned long long* kc = (unsigned long long*)kept;
+  // spin-pair tables, then the emission from them
+  const int64_t nbt = (int64_t)(F->n2 + F->n1) * F->Nb, nat = F->G * F->rowlen;
+  double* bt = dev_array<double>(c, F->tab_b, nbt);
+  uint32_t* bm = dev_array<uint32_t>(c, F->tab_bm, nbt);
+  double* at = dev_array<double>(c, F->tab_a, nat);
+  uint32_t* am = dev_array<uint32_t>(c, F->tab_am, nat);
+  k_emit_beta_table<<<(unsigned)std::min<int64_t>((nbt + 255) / 256, (int64_t)c->sm_count * 8), 256, 0, c->stream>>>(
+      A, I, ub, bt, bm);
+  QDKGB_CHECK_LAUNCH();
+  k_emit_alpha_table<<<(unsigned)std::min<int64_t>((nat + 255) / 256, (int64_t)c->sm_count * 8), 256, 0,
+                       c->stream>>>(A, I, ga, at, am);
+  QDKGB_CHECK_LAUNCH();
   if (storage == QDKGB_H_FP64)
-    k_slab_emit<QDKGB_H_FP64><<<grid, thr, 0, c->stream>>>(A, I, nullptr, 0, 0, ga, ub, tbits, diag_raw, val,
-                                                            nullptr, nullptr, diag, kc);
+    k_slab_emit_tab<QDKGB_H_FP64><<<grid, thr, 0, c->stream>>>(A, I, ga, ub, bt, bm, at, am, tbits, diag_raw, val,
+                                                                nullptr, diag, kc);
   else
-    k_slab_emit<kSlabF64F32><<<grid, thr, 0, c->stream>>>(A, I, nullptr, 0, 0, ga, ub, tbits, diag_raw, val, hi,
-                                                           nullptr, diag, kc);
+    k_slab_emit_tab<kSlabF64F32><<<grid, thr, 0, c->stream>>>(A, I, ga, ub, bt, bm, at, am, tbits, diag_raw, val,
+                                                               hi, diag, kc);
   QDKGB_CHECK_LAUNCH();
   int64_t* rowptr = dev_array<int64_t>(c, H.rowptr, n + 1);
   exclusive_scan_i64(c, kept, rowptr, n, H.scan_tmp);
