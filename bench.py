@@ -580,6 +580,92 @@ def run_cas14(args):
     print(json.dumps(line))
 
 
+# ------------------------------------------------------------------ kernels of complete spaces
+def run_rdm(args):
+    """Spin-resolved RDMs (all five blocks) of a normalised random vector over
+    the complete CASCI(nel, norb) space (default CASCI(14e,14o), 11,778,624
+    determinants): seconds per call and the opposite-spin sweep's FP64
+    multiply-adds (one per (alpha transition, beta transition) pair, with the
+    reversed alpha transitions folded)."""
+    import torch
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    pkg = _package()
+    pkg.build.build()
+    capi = pkg.capi
+    norb, nel = args.norb, args.nel
+    T, V, _ = pkg.integrals.synthetic_integrals(norb, args.nchol, SEED)
+    a, b = capi.fci_dets(norb, nel // 2, nel // 2)
+    C = np.random.default_rng(3).normal(size=len(a))
+    C /= np.linalg.norm(C)
+    with capi.Context(local) as ctx:
+        ctx.set_integrals(T, V)
+        ctx.set_dets(a, b)
+        for _ in range(args.warmup):
+            ctx.rdms_spin_dep(C)
+        times = []
+        for _ in range(args.steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            R = ctx.rdms_spin_dep(C)
+            torch.cuda.synchronize()
+            times.append(time.perf_counter() - t0)
+    k = nel // 2
+    na = math.comb(norb, k)
+    # alpha transitions with k >= l: off-diagonal classes C(n-2, k-1) each, diagonal C(n-1, k-1)
+    n_off, n_diag = math.comb(norb - 2, k - 1), math.comb(norb - 1, k - 1)
+    alpha_tr = (norb * (norb - 1) // 2) * n_off + norb * n_diag
+    beta_el = norb * (norb - 1) * n_off + norb * n_diag
+    dfma = alpha_tr * beta_el
+    t = float(np.median(times))
+    print(json.dumps({"metric": "rdm_spin_dep_seconds", "value": t, "unit": "s", "n_gpus": 1, "steps": args.steps,
+                      "warmup": args.warmup, "higher_is_better": False, "dtype": "f64", "data": "synthetic",
+                      "config": {"workload": "spin-resolved RDMs, CASCI(%de,%do), %d determinants" % (nel, norb, na * na),
+                                 "norb": norb, "nalpha": k, "nbeta": k},
+                      "opposite_spin_dfma": dfma, "dfma_per_s": dfma / t, "trace": float(np.trace(R["aa"] + R["bb"]))}))
+
+
+def run_direct(args):
+    """The direct (recompute-on-the-fly) sigma of the complete CASCI(nel, norb)
+    space: milliseconds per FP64 and FP32 application and elements per
+    second (elements = determinants x stored row length)."""
+    import torch
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    pkg = _package()
+    pkg.build.build()
+    capi = pkg.capi
+    norb, nel = args.norb, args.nel
+    T, V, _ = pkg.integrals.synthetic_integrals(norb, args.nchol, SEED)
+    a, b = capi.fci_dets(norb, nel // 2, nel // 2)
+    N = len(a)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    with capi.Context(local) as ctx:
+        ctx.set_stream(stream.cuda_stream)
+        ctx.set_integrals(T, V)
+        ctx.set_dets(a, b)
+        ctx.build_direct_sigma()
+        x64 = torch.randn(N, dtype=torch.float64, device="cuda")
+        y64 = torch.empty_like(x64)
+        x32 = torch.randn(N, dtype=torch.float32, device="cuda")
+        y32 = torch.empty_like(x32)
+        t64 = time_spmv(ctx, capi.PREC_FP64, x64, y64, stream, reps=max(1, args.steps))
+        t32 = time_spmv(ctx, capi.PREC_MIXED, x32, y32, stream, reps=max(1, args.steps))
+    k = nel // 2
+    s1 = k * (norb - k)
+    rowlen = 1 + 2 * s1 + 2 * math.comb(k, 2) * math.comb(norb - k, 2) + s1 * s1
+    elems = N * rowlen
+    print(json.dumps({"metric": "direct_sigma_ms", "value": t32 * 1e3, "unit": "ms", "n_gpus": 1, "steps": args.steps,
+                      "warmup": 0, "higher_is_better": False, "dtype": "f32", "data": "synthetic",
+                      "config": {"workload": "direct sigma, CASCI(%de,%do), %d determinants" % (nel, norb, N),
+                                 "norb": norb, "nalpha": k, "nbeta": k},
+                      "fp32_ms": t32 * 1e3, "fp64_ms": t64 * 1e3, "elements": elems,
+                      "elements_per_s_fp32": elems / t32, "elements_per_s_fp64": elems / t64}))
+
+
 # ------------------------------------------------------------------ ASCI, 40 orbitals
 def run_asci(args):
     """ASCI selected CI over 40 orbitals, n_alpha = n_beta = 8, integrals of
@@ -857,13 +943,17 @@ def main():
     ap.add_argument("--nchol", type=int, default=NCHOL)
     ap.add_argument("--asci-dets", type=int, default=2000000)
     ap.add_argument("--workload", default="cas12",
-                    choices=["cas12", "batched", "cas14", "asci", "pt2", "entropies", "casscf"],
+                    choices=["cas12", "batched", "cas14", "asci", "pt2", "entropies", "casscf", "rdm", "direct"],
                     help="cas12: the headline CASCI(12e,12o); batched: 512 small instances; "
                          "cas14: CASCI(14e,14o) with the direct sigma")
     args = ap.parse_args()
     set_workload(args.norb, args.nel, args.nchol)
     if args.workload == "cas14":
         run_cas14(args)
+    elif args.workload == "rdm":
+        run_rdm(args)
+    elif args.workload == "direct":
+        run_direct(args)
     elif args.workload == "asci":
         run_asci(args)
     elif args.workload == "pt2":
