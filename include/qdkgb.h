@@ -304,8 +304,12 @@ int qdkgb_asci(qdkgb_context* ctx, const qdkgb_asci_settings* s, const qdkgb_dav
  * h_build / davidson loggers): seconds[0] the determinant searches,
  * seconds[1] the determinant-space set-ups, seconds[2] the Hamiltonian
  * builds, seconds[3] the Davidson solves; *iterations (may be NULL) the
- * asci_iter count. */
-int qdkgb_asci_phase_times(const qdkgb_context* ctx, double* seconds, int64_t* iterations);
+ * asci_iter count; *patched (may be NULL) how many of its Hamiltonians were
+ * patched from the previous iteration's instead of built from scratch (the
+ * role of the reference's incremental build, incremental_h_build.hpp:38-356;
+ * the patched CSR is bit-identical to a rebuild; FP64 storage only, and off
+ * when the environment sets QDKGB_ASCI_FULL_BUILD=1). */
+int qdkgb_asci_phase_times(const qdkgb_context* ctx, double* seconds, int64_t* iterations, int64_t* patched);
 
 /* ASCI-PT2 (asci_pt2_constraint, external/macis/include/macis/asci/pt2.hpp:
  * 59-565): E_PT2 = sum over the determinants Q outside the wavefunction of

@@ -138,7 +138,7 @@ def lib():
     L.qdkgb_build_operator.argtypes = [vp, dp, ci, ci, P(ci), P(i64)]
     L.qdkgb_operator_action.argtypes = [vp, i64, dp, vp, i64, dp, vp, i64]
     L.qdkgb_rdms.argtypes = [vp, vp, vp, vp]
-    L.qdkgb_asci_phase_times.argtypes = [vp, vp, P(i64)]
+    L.qdkgb_asci_phase_times.argtypes = [vp, vp, P(i64), P(i64)]
     L.qdkgb_sigma_plan.argtypes = [vp, ci, P(ci), P(ci), vp, vp]
     L.qdkgb_get_csr64_rows.argtypes = [vp, i64, i64, vp, vp, vp]
     L.qdkgb_diagonal.argtypes = [vp, vp]
@@ -583,11 +583,13 @@ def asci(ctx, alpha0, beta0, c0, E0, grow=True, refine=True, tol=1e-8, max_m=200
 
 def asci_phase_times(ctx):
     """Seconds of the last asci call by phase (search, determinant space,
-    H build, Davidson) and its asci_iter count (qdkgb_asci_phase_times)."""
+    H build, Davidson), its asci_iter count and how many of its Hamiltonians
+    were patched from the previous one (qdkgb_asci_phase_times)."""
     t = np.zeros(4)
-    it = ctypes.c_int64()
-    ctx._check(lib().qdkgb_asci_phase_times(ctx.handle, _ptr(t), ctypes.byref(it)))
-    return {"search_s": t[0], "det_space_s": t[1], "hbuild_s": t[2], "davidson_s": t[3], "iterations": it.value}
+    it, pb = ctypes.c_int64(), ctypes.c_int64()
+    ctx._check(lib().qdkgb_asci_phase_times(ctx.handle, _ptr(t), ctypes.byref(it), ctypes.byref(pb)))
+    return {"search_s": t[0], "det_space_s": t[1], "hbuild_s": t[2], "davidson_s": t[3], "iterations": it.value,
+            "patched_builds": pb.value}
 
 
 def default_batch_settings(**kw):

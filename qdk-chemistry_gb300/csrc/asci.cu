@@ -24,6 +24,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <vector>
 
 #include "common.cuh"
@@ -797,23 +798,66 @@ struct PhaseClock {
   }
 };
 
+// The list the context's FP64 CSR was last built for, so that the next
+// iteration patches that matrix instead of rebuilding it (asci_iter's
+// incremental build, include/macis/solvers/incremental_h_build.hpp:38-356).
+struct HPatchCache {
+  std::vector<uint64_t> a, b;
+  double thresh = 0.;
+  bool valid = false;
+};
+
+// patch only when at least this share of the new list was in the old one
+constexpr double kMinPatchOverlap = 0.3;
+
+bool patch_disabled() {
+  const char* e = std::getenv("QDKGB_ASCI_FULL_BUILD");
+  return e && e[0] && e[0] != '0';
+}
+
 // selected_ci_diag (selected_ci_diag.hpp:111-158) on the device for a list
 // sorted by spin_comparator; X is the guess (empty: diagonal guess) and the
-// eigenvector on return.
+// eigenvector on return.  With a cache holding the previous list, the FP64
+// CSR is patched from the previous one (bit-identical to a rebuild).
 double sci_diag_gpu(Context* c, const qdkgb_asci_settings& S, const qdkgb_davidson_settings& ci, double matel_tol,
-                    const std::vector<HDet>& dets, std::vector<double>& X) {
+                    const std::vector<HDet>& dets, std::vector<double>& X, HPatchCache* cache) {
   const int64_t n = (int64_t)dets.size();
   std::vector<uint64_t> a(n), b(n);
   for (int64_t i = 0; i < n; ++i) {
     a[i] = dets[i].a;
     b[i] = dets[i].b;
   }
+  const bool mixed = ci.precision == QDKGB_PREC_MIXED;
+  // the previous CSR leaves the context before the determinant space is reset
+  ScopedBuffers<3> old(c);
+  const bool have_old = cache && cache->valid && !mixed && !patch_disabled() && c->H.valid && !c->op_direct &&
+                        !c->H.structured && c->H.storage == QDKGB_H_FP64 && c->H.thresh == matel_tol &&
+                        c->H.n == (int64_t)cache->a.size() && cache->thresh == matel_tol;
+  if (have_old) {
+    std::swap(old.b[0], c->H.rowptr);
+    std::swap(old.b[1], c->H.colind);
+    std::swap(old.b[2], c->H.val);
+  }
+  if (cache) cache->valid = false;
   PhaseClock clock(c);
   build_det_space(c, n, a.data(), b.data());
   clock.lap(1);
-  const bool mixed = ci.precision == QDKGB_PREC_MIXED;
-  build_hamiltonian(c, matel_tol, mixed ? QDKGB_H_SPLIT32 : QDKGB_H_FP64);
+  bool patched = false;
+  if (have_old && !c->fci)
+    patched = build_hamiltonian_patched(c, matel_tol, cache->a, cache->b, old.b[0], old.b[1], old.b[2],
+                                        kMinPatchOverlap);
+  for (DeviceBuffer& x : old.b) dev_free(c, x);
+  if (patched)
+    ++c->asci_patches;
+  else
+    build_hamiltonian(c, matel_tol, mixed ? QDKGB_H_SPLIT32 : QDKGB_H_FP64);
   clock.lap(2);
+  if (cache && !mixed) {
+    cache->a.swap(a);
+    cache->b.swap(b);
+    cache->thresh = matel_tol;
+    cache->valid = true;
+  }
   qdkgb_davidson_settings s = ci;
   s.nroots = 1;  // the ASCI iterations solve for the lowest root, as the reference's do
   s.use_guess = X.empty() ? 0 : 1;
@@ -828,8 +872,8 @@ double sci_diag_gpu(Context* c, const qdkgb_asci_settings& S, const qdkgb_davids
 
 // asci_iter (include/macis/asci/iteration.hpp:50-226)
 double asci_iter_gpu(Context* c, const qdkgb_asci_settings& S, const qdkgb_davidson_settings& ci, double matel_tol,
-                     int64_t ndets_max, double E0, std::vector<HDet>& wfn, std::vector<double>& X,
-                     int64_t* ncand) {
+                     int64_t ndets_max, double E0, std::vector<HDet>& wfn, std::vector<double>& X, int64_t* ncand,
+                     HPatchCache* cache) {
   NvtxRange nvtx_range("qdkgb.asci_iter");
   ++c->asci_iters;
   if (wfn.size() > 1) {  // reorder_ci_on_coeff (determinant_sort.hpp:45-64)
@@ -871,8 +915,20 @@ double asci_iter_gpu(Context* c, const qdkgb_asci_settings& S, const qdkgb_david
     std::copy(w2.begin(), w2.end(), wfn.begin());
     std::copy(x2.begin(), x2.end(), X.begin());
   }
-  std::vector<HDet> old_wfn = wfn;
-  std::vector<double> old_X = X;
+  // the previous list and vector in spin order, for the warm start's merge scan
+  std::vector<HDet> sorted_wfn;
+  std::vector<double> sorted_X;
+  if (S.warm_start) {
+    std::vector<size_t> idx(wfn.size());
+    for (size_t i = 0; i < idx.size(); ++i) idx[i] = i;
+    std::sort(idx.begin(), idx.end(), [&](size_t i, size_t j) { return hspin_less(wfn[i], wfn[j]); });
+    sorted_wfn.resize(idx.size());
+    sorted_X.resize(idx.size());
+    for (size_t i = 0; i < idx.size(); ++i) {
+      sorted_wfn[i] = wfn[idx[i]];
+      sorted_X[i] = X[idx[i]];
+    }
+  }
   std::vector<uint64_t> ca(nkeep), cb(nkeep);
   for (size_t i = 0; i < nkeep; ++i) {
     ca[i] = wfn[i].a;
@@ -890,14 +946,15 @@ double asci_iter_gpu(Context* c, const qdkgb_asci_settings& S, const qdkgb_david
   std::sort(wfn.begin(), wfn.end(), hspin_less);
   std::vector<double> Xl;
   if (S.warm_start) {
-    std::vector<size_t> idx(old_wfn.size());
-    for (size_t i = 0; i < idx.size(); ++i) idx[i] = i;
-    std::sort(idx.begin(), idx.end(), [&](size_t i, size_t j) { return hspin_less(old_wfn[i], old_wfn[j]); });
     Xl.assign(wfn.size(), 0.);
-    for (size_t i = 0; i < wfn.size(); ++i) {
-      auto it = std::lower_bound(idx.begin(), idx.end(), wfn[i],
-                                 [&](size_t k, const HDet& d) { return hspin_less(old_wfn[k], d); });
-      if (it != idx.end() && hdet_eq(old_wfn[*it], wfn[i])) Xl[i] = old_X[*it];
+    for (size_t i = 0, k = 0; i < wfn.size() && k < sorted_wfn.size();) {
+      if (hspin_less(sorted_wfn[k], wfn[i])) {
+        ++k;
+      } else if (hspin_less(wfn[i], sorted_wfn[k])) {
+        ++i;
+      } else {
+        Xl[i++] = sorted_X[k++];
+      }
     }
     double nrm = 0.;
     for (double x : Xl) nrm += x * x;
@@ -907,7 +964,7 @@ double asci_iter_gpu(Context* c, const qdkgb_asci_settings& S, const qdkgb_david
     else
       for (double& x : Xl) x /= nrm;
   }
-  const double E = sci_diag_gpu(c, S, ci, matel_tol, wfn, Xl);
+  const double E = sci_diag_gpu(c, S, ci, matel_tol, wfn, Xl, cache);
   X = Xl;
   return E;
 }
@@ -927,6 +984,8 @@ void asci_run(Context* c, const qdkgb_asci_settings& S, const qdkgb_davidson_set
   if (!(S.growth_recovery_rate > 1.0)) throw Error(QDKGB_ERR_INVALID, "growth_recovery_rate must be > 1.0");
   for (double& t : c->asci_phase_s) t = 0.;
   c->asci_iters = 0;
+  c->asci_patches = 0;
+  HPatchCache cache;
   std::vector<HDet> wfn(a.size());
   for (size_t i = 0; i < a.size(); ++i) wfn[i] = {a[i], b[i]};
   int64_t ncand = 0;
@@ -946,7 +1005,7 @@ void asci_run(Context* c, const qdkgb_asci_settings& S, const qdkgb_davidson_set
         nnew = std::min<int64_t>((int64_t)wfn.size() + 1, S.ntdets_max);
         if (nnew <= (int64_t)wfn.size()) break;
       }
-      const double E = asci_iter_gpu(c, S, ci, matel_tol, nnew, E0, wfn, X, &ncand);
+      const double E = asci_iter_gpu(c, S, ci, matel_tol, nnew, E0, wfn, X, &ncand, &cache);
       if ((int64_t)wfn.size() < nnew) {
         gf = std::max(S.min_grow_factor, gf * S.growth_backoff_rate);
         if (wfn.size() <= prev) break;
@@ -967,7 +1026,7 @@ void asci_run(Context* c, const qdkgb_asci_settings& S, const qdkgb_davidson_set
     int64_t max_iter = S.max_refine_iter, ext = 0;
     std::vector<HDet> prev_wfn;
     for (int64_t iter = 0; iter < max_iter; ++iter) {
-      const double E = asci_iter_gpu(c, S, ci, matel_tol, ndets, E0, wfn, X, &ncand);
+      const double E = asci_iter_gpu(c, S, ci, matel_tol, ndets, E0, wfn, X, &ncand, &cache);
       if ((int64_t)wfn.size() != ndets) {
         ndets = (int64_t)wfn.size();
         if (ndets < S.ntdets_min) break;
@@ -989,7 +1048,7 @@ void asci_run(Context* c, const qdkgb_asci_settings& S, const qdkgb_davidson_set
             auto it = std::lower_bound(uni.begin(), uni.end(), wfn[i], hspin_less);
             if (it != uni.end() && hdet_eq(*it, wfn[i])) Xu[it - uni.begin()] = X[i];
           }
-          const double Eu = sci_diag_gpu(c, S, ci, matel_tol, uni, Xu);
+          const double Eu = sci_diag_gpu(c, S, ci, matel_tol, uni, Xu, &cache);
           const int64_t e = std::min<int64_t>(osc, S.max_refine_iter - ext);
           if (e > 0) {
             max_iter += e;

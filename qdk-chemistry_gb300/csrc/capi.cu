@@ -697,10 +697,11 @@ int qdkgb_sigma_plan(qdkgb_context* c, int precision, int* segments, int* ncand,
   return QDKGB_OK;
 }
 
-int qdkgb_asci_phase_times(const qdkgb_context* c, double* seconds, int64_t* iterations) {
+int qdkgb_asci_phase_times(const qdkgb_context* c, double* seconds, int64_t* iterations, int64_t* patched) {
   if (!c || !seconds) return QDKGB_ERR_INVALID;
   for (int i = 0; i < 4; ++i) seconds[i] = c->asci_phase_s[i];
   if (iterations) *iterations = c->asci_iters;
+  if (patched) *patched = c->asci_patches;
   return QDKGB_OK;
 }
 

@@ -415,10 +415,13 @@ void k_diag_launch(Context* c, const Integrals& I, double* D, unsigned blocks) {
 // the list.  Integer work only: groups holding every beta string contribute
 // their candidate-list length directly; the others are checked candidate by
 // candidate (binary search or scan).
-__global__ void __launch_bounds__(kRowWarps * 32) k_row_count(RowArgs a, int64_t* __restrict__ row_nnz) {
+// rows: the rows to count (row i of the output is row rows[i]); null: all
+__global__ void __launch_bounds__(kRowWarps * 32)
+    k_row_count(RowArgs a, const int32_t* __restrict__ rows, int64_t nrows, int64_t* __restrict__ row_nnz) {
   __shared__ RowWalkSmem sm;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (int64_t r = (int64_t)blockIdx.x * kRowWarps + w; r < a.ndets; r += (int64_t)gridDim.x * kRowWarps) {
+  for (int64_t i = (int64_t)blockIdx.x * kRowWarps + w; i < nrows; i += (int64_t)gridDim.x * kRowWarps) {
+    const int64_t r = rows ? (int64_t)rows[i] : i;
     const int32_t g = a.det_group[r];
     const int32_t b = a.brank[r];
     const uint64_t rb = a.ubeta[b];
@@ -486,7 +489,7 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_row_count(RowArgs a, int64_t
         __syncwarp();
       }
     }
-    if (lane == 0) row_nnz[r] = cnt;
+    if (lane == 0) row_nnz[i] = cnt;
   }
 }
 
@@ -496,13 +499,15 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_row_count(RowArgs a, int64_t
 // the lower-index determinant as bra (sorted_double_loop.hpp:325-355).
 template <int STORAGE>
 __global__ void __launch_bounds__(kRowWarps * 32)
-    k_row_emit(RowArgs a, long long tbits, const double* __restrict__ diag_raw, const int64_t* __restrict__ rowptr,
-               int64_t* __restrict__ kept, int32_t* __restrict__ colind, double* __restrict__ val,
-               float* __restrict__ hi, float* __restrict__ lo, double* __restrict__ diag) {
+    k_row_emit(RowArgs a, const int32_t* __restrict__ rows, int64_t nrows, long long tbits,
+               const double* __restrict__ diag_raw, const int64_t* __restrict__ rowptr, int64_t* __restrict__ kept,
+               int32_t* __restrict__ colind, double* __restrict__ val, float* __restrict__ hi,
+               float* __restrict__ lo, double* __restrict__ diag) {
   __shared__ RowWalkSmem sm;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (int64_t r = (int64_t)blockIdx.x * kRowWarps + w; r < a.ndets; r += (int64_t)gridDim.x * kRowWarps) {
-    const int64_t start = rowptr[r];
+  for (int64_t i = (int64_t)blockIdx.x * kRowWarps + w; i < nrows; i += (int64_t)gridDim.x * kRowWarps) {
+    const int64_t r = rows ? (int64_t)rows[i] : i;
+    const int64_t start = rowptr[i];
     int64_t pos0 = start;
     walk_row(a, r, w, lane, sm, [&](int64_t ket, int64_t row, uint64_t ra, uint64_t rb, uint64_t ka, uint64_t kb) {
       bool keep = false;
@@ -531,7 +536,7 @@ __global__ void __launch_bounds__(kRowWarps * 32)
       }
       pos0 += __popc(m);
     });
-    if (lane == 0) kept[r] = pos0 - start;
+    if (lane == 0) kept[i] = pos0 - start;
   }
 }
 
@@ -676,7 +681,7 @@ void build_hamiltonian(Context* c, double thresh, int storage) {
   k_diag<<<tblocks, 256, 0, c->stream>>>(a.I, n, a.det_group, a.brank, a.galpha, a.ubeta, diag_raw);
   QDKGB_CHECK_LAUNCH();
   const int64_t blocks = std::min<int64_t>((n + kRowWarps - 1) / kRowWarps, (int64_t)c->sm_count * 64);
-  k_row_count<<<(unsigned)blocks, kRowWarps * 32, 0, c->stream>>>(a, row_nnz);
+  k_row_count<<<(unsigned)blocks, kRowWarps * 32, 0, c->stream>>>(a, nullptr, n, row_nnz);
   QDKGB_CHECK_LAUNCH();
   exclusive_scan_i64(c, row_nnz, rowptr, n, H.scan_tmp);
   int64_t nnz_pre = 0;
@@ -702,11 +707,11 @@ void build_hamiltonian(Context* c, double thresh, int storage) {
   QDKGB_CUDA(cudaMemsetAsync(diag, 0, n * sizeof(double), c->stream));
   // row_nnz now receives the kept counts
   if (storage == QDKGB_H_FP64)
-    k_row_emit<QDKGB_H_FP64><<<(unsigned)blocks, kRowWarps * 32, 0, c->stream>>>(a, tbits, diag_raw, rowptr, row_nnz,
-                                                                                colind, val, hi, lo, diag);
+    k_row_emit<QDKGB_H_FP64><<<(unsigned)blocks, kRowWarps * 32, 0, c->stream>>>(
+        a, nullptr, n, tbits, diag_raw, rowptr, row_nnz, colind, val, hi, lo, diag);
   else
     k_row_emit<QDKGB_H_SPLIT32><<<(unsigned)blocks, kRowWarps * 32, 0, c->stream>>>(
-        a, tbits, diag_raw, rowptr, row_nnz, colind, val, hi, lo, diag);
+        a, nullptr, n, tbits, diag_raw, rowptr, row_nnz, colind, val, hi, lo, diag);
   QDKGB_CHECK_LAUNCH();
   // kept total
   DeviceBuffer newptr_b, tmp;
@@ -752,6 +757,457 @@ void build_hamiltonian(Context* c, double thresh, int storage) {
   H.storage = storage;
   H.thresh = thresh;
   H.valid = true;
+}
+
+
+// ---------------------------------------------------------------- incremental build
+// The reference's asci_iter patches the previous Hamiltonian instead of
+// rebuilding it (PatchedSparseOperator / build_patched_operator,
+// include/macis/solvers/incremental_h_build.hpp:38-356): kept x kept
+// elements come from the old matrix, added rows and kept x added elements are
+// computed.  Here the patch produces the full CSR of the new list, bit
+// identical to a rebuild (the kept determinants keep their relative order,
+// so every kept x kept element has the same bra and value; the new elements
+// are computed with the lower-index determinant as bra, as a rebuild does):
+//   1. the rows of added determinants are walked as in a full build;
+//   2. their elements in kept columns are transposed into the kept rows
+//      (counted, scattered, each row's list sorted by column);
+//   3. every kept row is the merge of its old row (columns renumbered,
+//      dropped determinants skipped) with its transposed list.
+namespace {
+
+constexpr int kSortCap = 1024;  // transposed list length sorted in shared memory
+
+// transposed entries into the kept rows: counts
+__global__ void k_patch_tcount(int64_t nw, const int64_t* __restrict__ rpA, const int32_t* __restrict__ ciA,
+                               const uint8_t* __restrict__ walk, unsigned long long* __restrict__ tcnt) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < nw;
+       i += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    for (int64_t e = rpA[i] + lane; e < rpA[i + 1]; e += 32) {
+      const int32_t col = ciA[e];
+      if (!walk[col]) atomicAdd(tcnt + col, 1ull);
+    }
+  }
+}
+
+// ... scattered (the order within a row is fixed afterwards by the sort)
+__global__ void k_patch_tscatter(int64_t nw, const int32_t* __restrict__ rows, const int64_t* __restrict__ rpA,
+                                 const int32_t* __restrict__ ciA, const double* __restrict__ vA,
+                                 const uint8_t* __restrict__ walk, const int64_t* __restrict__ toff,
+                                 unsigned long long* __restrict__ tcur, int32_t* __restrict__ tcol,
+                                 double* __restrict__ tval) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < nw;
+       i += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    const int32_t w = rows[i];
+    for (int64_t e = rpA[i] + lane; e < rpA[i + 1]; e += 32) {
+      const int32_t col = ciA[e];
+      if (walk[col]) continue;
+      const int64_t p = toff[col] + (int64_t)atomicAdd(tcur + col, 1ull);
+      tcol[p] = w;
+      tval[p] = vA[e];
+    }
+  }
+}
+
+// sorts each kept row's transposed list by column (columns are distinct) with
+// a bitonic sort in shared memory; a list above kSortCap goes to the long
+// list (k_patch_tsort_long)
+__global__ void __launch_bounds__(256) k_patch_tsort(int64_t n, const uint8_t* __restrict__ walk,
+                                                     const int64_t* __restrict__ toff, int32_t* __restrict__ tcol,
+                                                     double* __restrict__ tval, int32_t* __restrict__ long_rows,
+                                                     unsigned* __restrict__ nlong) {
+  __shared__ int32_t key[kSortCap];
+  __shared__ int32_t src[kSortCap];
+  __shared__ double vbuf[kSortCap];
+  for (int64_t r = blockIdx.x; r < n; r += gridDim.x) {
+    const int64_t b = toff[r], len = toff[r + 1] - b;
+    if (walk[r] || len < 2) continue;
+    if (len > kSortCap) {
+      if (threadIdx.x == 0) long_rows[atomicAdd(nlong, 1u)] = (int32_t)r;
+      continue;
+    }
+    int m = 1;
+    while (m < len) m <<= 1;
+    for (int t = threadIdx.x; t < m; t += blockDim.x) {
+      key[t] = t < len ? tcol[b + t] : INT32_MAX;
+      src[t] = t;
+    }
+    __syncthreads();
+    for (int k = 2; k <= m; k <<= 1)
+      for (int j = k >> 1; j > 0; j >>= 1) {
+        for (int t = threadIdx.x; t < m; t += blockDim.x) {
+          const int u = t ^ j;
+          if (u > t) {
+            const bool up = (t & k) == 0;
+            if ((key[t] > key[u]) == up) {
+              const int32_t kk = key[t];
+              key[t] = key[u];
+              key[u] = kk;
+              const int32_t ss = src[t];
+              src[t] = src[u];
+              src[u] = ss;
+            }
+          }
+        }
+        __syncthreads();
+      }
+    for (int t = threadIdx.x; t < len; t += blockDim.x) vbuf[t] = tval[b + src[t]];
+    __syncthreads();
+    for (int t = threadIdx.x; t < len; t += blockDim.x) {
+      tcol[b + t] = key[t];
+      tval[b + t] = vbuf[t];
+    }
+    __syncthreads();
+  }
+}
+
+// the long lists: a list's columns are added rows, so their walked-row
+// indices widx (increasing with the column) mark a bitmap of nw bits; a
+// column's place is the count of marks before it.  Each block owns one
+// bitmap (words words) and its word prefix (words + 1).
+__global__ void __launch_bounds__(256)
+    k_patch_tsort_long(const int32_t* __restrict__ long_rows, const unsigned* __restrict__ nlong,
+                       const int64_t* __restrict__ toff, const int32_t* __restrict__ widx, int64_t words,
+                       unsigned* __restrict__ bitmaps, int64_t* __restrict__ prefixes, int32_t* __restrict__ tcol,
+                       double* __restrict__ tval, int32_t* __restrict__ scol, double* __restrict__ sval) {
+  __shared__ int64_t part[256];
+  unsigned* bm = bitmaps + (int64_t)blockIdx.x * words;
+  int64_t* pre = prefixes + (int64_t)blockIdx.x * (words + 1);
+  const int64_t chunk = (words + blockDim.x - 1) / blockDim.x;
+  const int64_t w0 = (int64_t)threadIdx.x * chunk < words ? (int64_t)threadIdx.x * chunk : words;
+  const int64_t w1 = w0 + chunk < words ? w0 + chunk : words;
+  for (unsigned q = blockIdx.x; q < *nlong; q += gridDim.x) {
+    const int32_t r = long_rows[q];
+    const int64_t b = toff[r], len = toff[r + 1] - b;
+    for (int64_t w = threadIdx.x; w < words; w += blockDim.x) bm[w] = 0u;
+    __syncthreads();
+    for (int64_t e = threadIdx.x; e < len; e += blockDim.x) {
+      const int32_t i = widx[tcol[b + e]];
+      atomicOr(bm + (i >> 5), 1u << (i & 31));
+    }
+    __syncthreads();
+    int64_t sum = 0;
+    for (int64_t w = w0; w < w1; ++w) sum += __popc(bm[w]);
+    part[threadIdx.x] = sum;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int64_t run = 0;
+      for (int t = 0; t < (int)blockDim.x; ++t) {
+        const int64_t x = part[t];
+        part[t] = run;
+        run += x;
+      }
+    }
+    __syncthreads();
+    int64_t run = part[threadIdx.x];
+    for (int64_t w = w0; w < w1; ++w) {
+      pre[w] = run;
+      run += __popc(bm[w]);
+    }
+    __syncthreads();
+    for (int64_t e = threadIdx.x; e < len; e += blockDim.x) {
+      const int32_t col = tcol[b + e];
+      const int32_t i = widx[col];
+      const int64_t rank = pre[i >> 5] + __popc(bm[i >> 5] & ((1u << (i & 31)) - 1u));
+      scol[b + rank] = col;
+      sval[b + rank] = tval[b + e];
+    }
+    __syncthreads();
+    for (int64_t e = threadIdx.x; e < len; e += blockDim.x) {
+      tcol[b + e] = scol[b + e];
+      tval[b + e] = sval[b + e];
+    }
+    __syncthreads();
+  }
+}
+
+// kept entries of each merged row's old row
+__global__ void k_patch_kcount(int64_t n, const uint8_t* __restrict__ walk, const int32_t* __restrict__ n2o,
+                               const int64_t* __restrict__ rpO, const int32_t* __restrict__ ciO,
+                               const int32_t* __restrict__ o2n, int64_t* __restrict__ kcnt) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n;
+       r += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    int64_t cnt = 0;
+    if (!walk[r]) {
+      const int32_t o = n2o[r];
+      for (int64_t e = rpO[o] + lane; e < rpO[o + 1]; e += 32) cnt += o2n[ciO[e]] >= 0;
+      for (int d = 16; d > 0; d >>= 1) cnt += __shfl_xor_sync(QDKGB_FULL_MASK, cnt, d);
+    }
+    if (lane == 0) kcnt[r] = cnt;
+  }
+}
+
+// row lengths of the new matrix
+__global__ void k_patch_rowlen(int64_t n, const uint8_t* __restrict__ walk, const int32_t* __restrict__ widx,
+                               const int64_t* __restrict__ rpA, const int64_t* __restrict__ kcnt,
+                               const unsigned long long* __restrict__ tcnt, int64_t* __restrict__ len) {
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    if (walk[r]) {
+      const int32_t i = widx[r];
+      len[r] = rpA[i + 1] - rpA[i];
+    } else {
+      len[r] = kcnt[r] + (int64_t)tcnt[r];
+    }
+  }
+}
+
+__device__ __forceinline__ int64_t lower_bound_i32(const int32_t* a, int64_t n, int32_t x) {
+  int64_t lo = 0, hi = n;
+  while (lo < hi) {
+    const int64_t mid = (lo + hi) >> 1;
+    if (a[mid] < x)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
+// the new rows: walked rows copied, kept rows merged (a warp per row; the
+// kept entries' renumbered columns go to kcol, where the transposed entries
+// find their places)
+__global__ void k_patch_write(int64_t n, const uint8_t* __restrict__ walk, const int32_t* __restrict__ widx,
+                              const int32_t* __restrict__ n2o, const int32_t* __restrict__ o2n,
+                              const int64_t* __restrict__ rpO, const int32_t* __restrict__ ciO,
+                              const double* __restrict__ vO, const int64_t* __restrict__ rpA,
+                              const int32_t* __restrict__ ciA, const double* __restrict__ vA,
+                              const int64_t* __restrict__ toff, const int32_t* __restrict__ tcol,
+                              const double* __restrict__ tval, const int64_t* __restrict__ koff,
+                              int32_t* __restrict__ kcol, const int64_t* __restrict__ rp, int32_t* __restrict__ ci,
+                              double* __restrict__ v) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n;
+       r += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    const int64_t base = rp[r];
+    if (walk[r]) {
+      const int32_t i = widx[r];
+      const int64_t a0 = rpA[i], len = rpA[i + 1] - a0;
+      for (int64_t e = lane; e < len; e += 32) {
+        ci[base + e] = ciA[a0 + e];
+        v[base + e] = vA[a0 + e];
+      }
+      continue;
+    }
+    const int32_t o = n2o[r];
+    const int64_t e0 = rpO[o], e1 = rpO[o + 1];
+    const int64_t t0 = toff[r], tl = toff[r + 1] - t0;
+    int32_t* kr = kcol + koff[r];
+    // kept entries, in order, after the transposed entries of smaller columns
+    int64_t K = 0;
+    for (int64_t c0 = e0; c0 < e1; c0 += 32) {
+      const int64_t e = c0 + lane;
+      const int32_t nc = e < e1 ? o2n[ciO[e]] : -1;
+      const unsigned m = __ballot_sync(QDKGB_FULL_MASK, nc >= 0);
+      if (nc >= 0) {
+        const int64_t q = K + __popc(m & ((1u << lane) - 1u));
+        kr[q] = nc;
+        const int64_t pos = base + q + lower_bound_i32(tcol + t0, tl, nc);
+        ci[pos] = nc;
+        v[pos] = vO[e];
+      }
+      K += __popc(m);
+    }
+    __syncwarp();
+    // transposed entries after the kept entries of smaller columns
+    for (int64_t t = lane; t < tl; t += 32) {
+      const int32_t j = tcol[t0 + t];
+      const int64_t pos = base + t + lower_bound_i32(kr, K, j);
+      ci[pos] = j;
+      v[pos] = tval[t0 + t];
+    }
+    __syncwarp();
+  }
+}
+
+}  // namespace
+
+bool build_hamiltonian_patched(Context* c, double thresh, const std::vector<uint64_t>& oa,
+                               const std::vector<uint64_t>& ob, DeviceBuffer& old_rowptr, DeviceBuffer& old_colind,
+                               DeviceBuffer& old_val, double min_overlap) {
+  NvtxRange nvtx_range("qdkgb.build_hamiltonian_patched");
+  DetSpace& D = c->dets;
+  const int64_t n = D.ndets, n_old = (int64_t)oa.size();
+  if (n == 0 || n_old == 0 || n >= INT32_MAX || n_old >= INT32_MAX) return false;
+  // classify by a merge scan of the two lists (both sorted by spin_comparator)
+  std::vector<int32_t> o2n(n_old, -1), n2o(n, -1);
+  int64_t kept = 0;
+  for (int64_t io = 0, in = 0; io < n_old && in < n;) {
+    const uint64_t xa = oa[io], xb = ob[io], ya = D.h_alpha[in], yb = D.h_beta[in];
+    if (xa < ya || (xa == ya && xb < yb)) {
+      ++io;
+    } else if (ya < xa || (ya == xa && yb < xb)) {
+      ++in;
+    } else {
+      o2n[io] = (int32_t)in;
+      n2o[in] = (int32_t)io;
+      ++kept;
+      ++io;
+      ++in;
+    }
+  }
+  if ((double)kept < min_overlap * (double)n) return false;
+  // walked rows: the added determinants
+  std::vector<uint8_t> walk(n, 0);
+  std::vector<int32_t> rows, widx(n, -1);
+  for (int64_t r = 0; r < n; ++r)
+    if (n2o[r] < 0) {
+      walk[r] = 1;
+      widx[r] = (int32_t)rows.size();
+      rows.push_back((int32_t)r);
+    }
+  const int64_t nw = (int64_t)rows.size();
+  ScopedBuffers<23> sb(c);
+  auto up = [&](DeviceBuffer& b, const void* src, size_t bytes) {
+    void* p = dev_alloc(c, b, std::max<size_t>(bytes, 8) + 16);
+    if (bytes) QDKGB_CUDA(cudaMemcpyAsync(p, src, bytes, cudaMemcpyHostToDevice, c->stream));
+    return p;
+  };
+  const int32_t* d_o2n = (const int32_t*)up(sb.b[0], o2n.data(), n_old * 4);
+  const int32_t* d_n2o = (const int32_t*)up(sb.b[1], n2o.data(), n * 4);
+  const uint8_t* d_walk = (const uint8_t*)up(sb.b[2], walk.data(), n);
+  const int32_t* d_widx = (const int32_t*)up(sb.b[3], widx.data(), n * 4);
+  const int32_t* d_rows = (const int32_t*)up(sb.b[4], rows.data(), nw * 4);
+  Hcsr& H = c->H;
+  RowArgs a = row_args(c, thresh);
+  long long tbits = -1;
+  if (thresh > 0.) std::memcpy(&tbits, &thresh, sizeof(double));
+  double* diag_raw = dev_array<double>(c, H.diag_raw, n);
+  double* diag = dev_array<double>(c, H.diag, n);
+  const unsigned tblocks = (unsigned)std::min<int64_t>((n + 255) / 256, (int64_t)c->sm_count * 16);
+  k_diag<<<tblocks, 256, 0, c->stream>>>(a.I, n, a.det_group, a.brank, a.galpha, a.ubeta, diag_raw);
+  QDKGB_CHECK_LAUNCH();
+  QDKGB_CUDA(cudaMemsetAsync(diag, 0, n * sizeof(double), c->stream));
+  // 1. walked rows into A (pre-threshold slots, then compacted)
+  int64_t* cntA = dev_array<int64_t>(c, sb.b[5], std::max<int64_t>(nw, n) + 1);
+  int64_t* rpA0 = dev_array<int64_t>(c, sb.b[6], nw + 1);
+  const int64_t wblocks =
+      std::max<int64_t>(1, std::min<int64_t>((nw + kRowWarps - 1) / kRowWarps, (int64_t)c->sm_count * 64));
+  int64_t nA0 = 0;
+  if (nw) {
+    k_row_count<<<(unsigned)wblocks, kRowWarps * 32, 0, c->stream>>>(a, d_rows, nw, cntA);
+    QDKGB_CHECK_LAUNCH();
+    exclusive_scan_i64(c, cntA, rpA0, nw, H.scan_tmp);
+    QDKGB_CUDA(cudaMemcpyAsync(&nA0, rpA0 + nw, 8, cudaMemcpyDeviceToHost, c->stream));
+    QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+  } else {
+    QDKGB_CUDA(cudaMemsetAsync(rpA0, 0, 8, c->stream));
+  }
+  int32_t* ciA0 = dev_array<int32_t>(c, sb.b[7], std::max<int64_t>(nA0, 1));
+  double* vA0 = dev_array<double>(c, sb.b[8], std::max<int64_t>(nA0, 1));
+  int64_t* rpA = dev_array<int64_t>(c, sb.b[9], nw + 1);
+  int64_t nA = 0;
+  int32_t* ciA = ciA0;
+  double* vA = vA0;
+  if (nw) {
+    k_row_emit<QDKGB_H_FP64><<<(unsigned)wblocks, kRowWarps * 32, 0, c->stream>>>(
+        a, d_rows, nw, tbits, diag_raw, rpA0, cntA, ciA0, vA0, nullptr, nullptr, diag);
+    QDKGB_CHECK_LAUNCH();
+    exclusive_scan_i64(c, cntA, rpA, nw, H.scan_tmp);
+    QDKGB_CUDA(cudaMemcpyAsync(&nA, rpA + nw, 8, cudaMemcpyDeviceToHost, c->stream));
+    QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+    if (nA != nA0) {
+      ciA = dev_array<int32_t>(c, sb.b[10], std::max<int64_t>(nA, 1));
+      vA = dev_array<double>(c, sb.b[11], std::max<int64_t>(nA, 1));
+      const unsigned cblocks = (unsigned)std::min<int64_t>((nw + 7) / 8, (int64_t)c->sm_count * 32);
+      k_row_compact<QDKGB_H_FP64><<<cblocks, 256, 0, c->stream>>>(nw, rpA0, rpA, ciA0, vA0, nullptr, nullptr, ciA,
+                                                                   vA, nullptr, nullptr);
+      QDKGB_CHECK_LAUNCH();
+    }
+  } else {
+    QDKGB_CUDA(cudaMemsetAsync(rpA, 0, 8, c->stream));
+  }
+  // 2. transposed entries into the merged rows
+  unsigned long long* tcnt = dev_array<unsigned long long>(c, sb.b[12], 2 * (n + 1));
+  unsigned long long* tcur = tcnt + n + 1;
+  QDKGB_CUDA(cudaMemsetAsync(tcnt, 0, 2 * (n + 1) * 8, c->stream));
+  const unsigned eblocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>((nw + 7) / 8, (int64_t)c->sm_count * 32));
+  if (nw) {
+    k_patch_tcount<<<eblocks, 256, 0, c->stream>>>(nw, rpA, ciA, d_walk, tcnt);
+    QDKGB_CHECK_LAUNCH();
+  }
+  int64_t* toff = dev_array<int64_t>(c, sb.b[13], n + 1);
+  exclusive_scan_i64(c, (const int64_t*)tcnt, toff, n, H.scan_tmp);
+  int64_t nT = 0;
+  QDKGB_CUDA(cudaMemcpyAsync(&nT, toff + n, 8, cudaMemcpyDeviceToHost, c->stream));
+  QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+  int32_t* tcol = dev_array<int32_t>(c, sb.b[14], std::max<int64_t>(nT, 1));
+  double* tval = dev_array<double>(c, sb.b[15], std::max<int64_t>(nT, 1));
+  if (nw) {
+    k_patch_tscatter<<<eblocks, 256, 0, c->stream>>>(nw, d_rows, rpA, ciA, vA, d_walk, toff, tcur, tcol, tval);
+    QDKGB_CHECK_LAUNCH();
+  }
+  // short lists sorted in shared memory; the long ones by the walked-row bitmap
+  int32_t* long_rows = dev_array<int32_t>(c, sb.b[18], n + 2);
+  unsigned* nlong = reinterpret_cast<unsigned*>(long_rows + n);
+  QDKGB_CUDA(cudaMemsetAsync(nlong, 0, sizeof(unsigned), c->stream));
+  k_patch_tsort<<<(unsigned)std::min<int64_t>(n, (int64_t)c->sm_count * 8), 256, 0, c->stream>>>(
+      n, d_walk, toff, tcol, tval, long_rows, nlong);
+  QDKGB_CHECK_LAUNCH();
+  unsigned nlong_h = 0;
+  QDKGB_CUDA(cudaMemcpyAsync(&nlong_h, nlong, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+  QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+  if (nlong_h) {
+    const int64_t words = (nw + 31) / 32;
+    const unsigned lblocks = (unsigned)std::min<int64_t>(nlong_h, c->sm_count);
+    unsigned* bitmaps = dev_array<unsigned>(c, sb.b[19], (size_t)lblocks * words);
+    int64_t* prefixes = dev_array<int64_t>(c, sb.b[20], (size_t)lblocks * (words + 1));
+    int32_t* scol = dev_array<int32_t>(c, sb.b[21], nT);
+    double* sval = dev_array<double>(c, sb.b[22], nT);
+    k_patch_tsort_long<<<lblocks, 256, 0, c->stream>>>(long_rows, nlong, toff, d_widx, words, bitmaps, prefixes,
+                                                       tcol, tval, scol, sval);
+    QDKGB_CHECK_LAUNCH();
+  }
+  // 3. row lengths and the merged matrix
+  int64_t* kcnt = cntA;  // the walked rows' counts are no longer needed
+  const unsigned rblocks = (unsigned)std::min<int64_t>((n + 7) / 8, (int64_t)c->sm_count * 32);
+  k_patch_kcount<<<rblocks, 256, 0, c->stream>>>(n, d_walk, d_n2o, (const int64_t*)old_rowptr.ptr,
+                                                 (const int32_t*)old_colind.ptr, d_o2n, kcnt);
+  QDKGB_CHECK_LAUNCH();
+  int64_t* len = dev_array<int64_t>(c, H.row_nnz, n + 1);
+  k_patch_rowlen<<<tblocks, 256, 0, c->stream>>>(n, d_walk, d_widx, rpA, kcnt, tcnt, len);
+  QDKGB_CHECK_LAUNCH();
+  int64_t* koff = dev_array<int64_t>(c, sb.b[16], n + 1);
+  exclusive_scan_i64(c, kcnt, koff, n, H.scan_tmp);
+  int64_t nK = 0;
+  QDKGB_CUDA(cudaMemcpyAsync(&nK, koff + n, 8, cudaMemcpyDeviceToHost, c->stream));
+  QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+  int32_t* kcol = dev_array<int32_t>(c, sb.b[17], std::max<int64_t>(nK, 1));
+  DeviceBuffer rpb;
+  int64_t* rp = dev_array<int64_t>(c, rpb, n + 1);
+  exclusive_scan_i64(c, len, rp, n, H.scan_tmp);
+  int64_t nnz = 0;
+  QDKGB_CUDA(cudaMemcpyAsync(&nnz, rp + n, 8, cudaMemcpyDeviceToHost, c->stream));
+  QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+  DeviceBuffer cib, vb;
+  int32_t* ci = dev_array<int32_t>(c, cib, std::max<int64_t>(nnz, 1));
+  double* v = dev_array<double>(c, vb, std::max<int64_t>(nnz, 1));
+  k_patch_write<<<rblocks, 256, 0, c->stream>>>(n, d_walk, d_widx, d_n2o, d_o2n, (const int64_t*)old_rowptr.ptr,
+                                                (const int32_t*)old_colind.ptr, (const double*)old_val.ptr, rpA, ciA,
+                                                vA, toff, tcol, tval, koff, kcol, rp, ci, v);
+  QDKGB_CHECK_LAUNCH();
+  // the Davidson diagonal: first stored (i, i) element, 0 when thresholded away
+  k_extract_diag<<<rblocks, 256, 0, c->stream>>>(n, rp, ci, v, diag);
+  QDKGB_CHECK_LAUNCH();
+  QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+  dev_free(c, H.hi);
+  dev_free(c, H.lo);
+  std::swap(H.rowptr, rpb);
+  std::swap(H.colind, cib);
+  std::swap(H.val, vb);
+  dev_free(c, rpb);
+  dev_free(c, cib);
+  dev_free(c, vb);
+  H.n = n;
+  H.nnz = nnz;
+  H.storage = QDKGB_H_FP64;
+  H.thresh = thresh;
+  H.structured = false;
+  H.valid = true;
+  c->op_direct = false;
+  return true;
 }
 
 }  // namespace qdkgb

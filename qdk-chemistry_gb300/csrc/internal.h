@@ -142,6 +142,7 @@ struct Context {
   // and its asci_iter count
   double asci_phase_s[4] = {0., 0., 0., 0.};
   int64_t asci_iters = 0;
+  int64_t asci_patches = 0;  // Hamiltonians of the last qdkgb_asci call built by patching the previous one
   DeviceBuffer host_pinned_dummy;
   double* pinned = nullptr;  // small pinned host staging (64 doubles)
 };
@@ -156,6 +157,12 @@ void build_integral_intermediates(Context* c);
 void build_det_space(Context* c, int64_t ndets, const uint64_t* alpha, const uint64_t* beta);
 void build_hamiltonian(Context* c, double thresh, int storage);
 bool build_operator(Context* c, double thresh, int storage, int max_m);  // true: direct sigma
+// The CSR of the current list from the previous list's CSR (old host lists
+// sorted by spin_comparator, old FP64 CSR buffers, the same threshold); false
+// when fewer than min_overlap of the new determinants were kept.
+bool build_hamiltonian_patched(Context* c, double thresh, const std::vector<uint64_t>& oa,
+                               const std::vector<uint64_t>& ob, DeviceBuffer& old_rowptr, DeviceBuffer& old_colind,
+                               DeviceBuffer& old_val, double min_overlap);
 void set_csr(Context* c, int64_t n, const int64_t* rowptr, const int64_t* colind, const double* values);
 void exclusive_scan_i64(Context* c, const int64_t* in, int64_t* out, int64_t n, DeviceBuffer& tmp);
 

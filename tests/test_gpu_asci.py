@@ -117,3 +117,53 @@ def test_asci_grow_repeats_bit_for_bit(pkg):
     assert np.array_equal(a1, a2) and np.array_equal(b1, b2)
     assert np.array_equal(c1.view(np.uint64), c2.view(np.uint64)) and E1 == E2
     assert t1["iterations"] > 0 and all(t1[k] > 0 for k in ("search_s", "det_space_s", "hbuild_s", "davidson_s"))
+
+
+def test_asci_patched_hamiltonian_equals_full_rebuild(pkg, monkeypatch):
+    """The ASCI iterations patch the previous iteration's Hamiltonian (new
+    rows and long kept rows walked, the new rows' elements transposed into
+    the kept rows, the kept rows merged with their renumbered old rows).  The
+    patched CSR equals a rebuild of the same list element for element, and a
+    grow followed by refine iterations gives bit-identical determinants,
+    coefficients, energies and final matrices with every Hamiltonian rebuilt
+    (QDKGB_ASCI_FULL_BUILD=1).  The 40-orbital space's reference determinant
+    has rows longer than the merge buffer, so the long-row walk is covered."""
+    import os
+
+    from conftest import GOLDEN, unpack_eri
+    pkg.build.build()
+    capi = pkg.capi
+    d = np.load(os.path.join(GOLDEN, "ref_asci40.npz"))
+    norb = int(d["norb"])
+    a0, b0 = pkg.determinants.canonical_hf(int(d["nalpha"]), int(d["nbeta"]))
+    out = {}
+    for full in (False, True):
+        monkeypatch.setenv("QDKGB_ASCI_FULL_BUILD", "1" if full else "0")
+        with capi.Context(0) as ctx:
+            ctx.set_integrals(d["T"], unpack_eri(d["V_packed"], norb))
+            ctx.set_dets(np.array([a0], np.uint64), np.array([b0], np.uint64))
+            ctx.build_hamiltonian()
+            E0 = float(ctx.diagonal()[0])
+            _, a, b, c, Eg = capi.asci(ctx, [a0], [b0], [1.0], E0, grow=True, refine=False, ntdets_max=30000,
+                                       core_selection_fixed=1, ncdets_max=3000, grow_factor=2)
+            tg = capi.asci_phase_times(ctx)
+            grown = ctx.get_csr(64)
+            ctx.set_dets(a, b)
+            ctx.build_hamiltonian()
+            rebuilt = ctx.get_csr(64)
+            for x, y in zip(grown, rebuilt):
+                assert np.array_equal(x.view(np.uint64) if x.dtype == np.float64 else x,
+                                      y.view(np.uint64) if y.dtype == np.float64 else y)
+            with pytest.raises(capi.NotConverged):
+                capi.asci(ctx, a, b, c, Eg, grow=False, refine=True, core_selection_fixed=1, ncdets_max=3000,
+                          ntdets_max=30000, max_refine_iter=3, refine_energy_tol=1e-14)
+            tr = capi.asci_phase_times(ctx)
+            out[full] = (a, b, c, Eg, ctx.get_csr(64), tg, tr)
+    (a1, b1, c1, E1, H1, tg1, tr1), (a2, b2, c2, E2, H2, tg2, tr2) = out[False], out[True]
+    assert tg1["patched_builds"] > 0 and tr1["patched_builds"] > 0
+    assert tg2["patched_builds"] == 0 and tr2["patched_builds"] == 0
+    assert np.array_equal(a1, a2) and np.array_equal(b1, b2)
+    assert np.array_equal(c1.view(np.uint64), c2.view(np.uint64)) and E1 == E2
+    for x, y in zip(H1, H2):
+        assert np.array_equal(x.view(np.uint64) if x.dtype == np.float64 else x,
+                              y.view(np.uint64) if y.dtype == np.float64 else y)
