@@ -83,6 +83,17 @@ int qdkgb_set_device_limit(qdkgb_context* ctx, int64_t bytes);
 #define QDKGB_LAYOUT_DIRECT 3
 int qdkgb_operator_layout(const qdkgb_context* ctx, int* layout, int64_t* stored_elements);
 
+/* The sizes the getters write (no counterpart; the reference's sparsexx
+ * matrix carries its own m() and nnz()): *ndets the dimension of the
+ * operator (the rows of a caller's CSR after qdkgb_set_csr, else the
+ * determinant count of the context's current list; 0 before either), *nnz
+ * the CSR element count of the built operator as qdkgb_get_csr* exports it
+ * (0 when none is built or the operator is the direct sigma).  Either
+ * pointer may be NULL.
+ * qdkgb_asci leaves its final list and that list's Hamiltonian in the
+ * context, so the sizes change across that call. */
+int qdkgb_problem_size(const qdkgb_context* ctx, int64_t* ndets, int64_t* nnz);
+
 /* ------------------------------------------------------------ integrals
  * Replaces the HamiltonianGeneratorBase constructor and
  * generate_integral_intermediates_ (external/macis/src/macis/

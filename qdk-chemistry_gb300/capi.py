@@ -34,7 +34,7 @@ OP_NONE, OP_CSR, OP_SLAB, OP_DIRECT = 0, 1, 2, 3
 
 EXPORTED = [
     "qdkgb_create", "qdkgb_destroy", "qdkgb_last_error", "qdkgb_set_stream", "qdkgb_device_bytes",
-    "qdkgb_set_device_limit", "qdkgb_operator_layout",
+    "qdkgb_set_device_limit", "qdkgb_operator_layout", "qdkgb_problem_size",
     "qdkgb_set_integrals", "qdkgb_fci_dets", "qdkgb_set_dets", "qdkgb_build_hamiltonian", "qdkgb_get_csr32",
     "qdkgb_get_csr64", "qdkgb_get_csr32_rows", "qdkgb_get_csr64_rows", "qdkgb_diagonal", "qdkgb_spmv", "qdkgb_spmv_device", "qdkgb_davidson_default_settings",
     "qdkgb_davidson", "qdkgb_rdms_spin_dep", "qdkgb_orbital_entropies", "qdkgb_casci",
@@ -128,6 +128,7 @@ def lib():
     L.qdkgb_device_bytes.argtypes = [vp, P(i64)]
     L.qdkgb_set_device_limit.argtypes = [vp, i64]
     L.qdkgb_operator_layout.argtypes = [vp, P(ctypes.c_int), P(i64)]
+    L.qdkgb_problem_size.argtypes = [vp, P(i64), P(i64)]
     L.qdkgb_set_integrals.argtypes = [vp, ci, vp, vp, ci]
     L.qdkgb_fci_dets.argtypes = [ci, ci, ci, vp, vp, P(i64)]
     L.qdkgb_set_dets.argtypes = [vp, i64, vp, vp]
@@ -269,8 +270,6 @@ class Context:
             raise QdkgbError(rc, "qdkgb_create failed (no usable CUDA device?)")
         self._h = h
         self.norb = None
-        self.ndets = None
-        self.nnz = None
 
     def close(self):
         if getattr(self, "_h", None):
@@ -295,6 +294,22 @@ class Context:
             if rc == ERR_NOT_CONVERGED:
                 raise NotConverged(rc, msg)
             raise QdkgbError(rc, msg)
+
+    def _sizes(self):
+        nd, nnz = ctypes.c_int64(), ctypes.c_int64()
+        self._check(lib().qdkgb_problem_size(self._h, ctypes.byref(nd), ctypes.byref(nnz)))
+        return nd.value, nnz.value
+
+    @property
+    def ndets(self):
+        """Dimension of the operator (qdkgb_problem_size): the current list's
+        determinant count, or the rows of a caller's CSR."""
+        return self._sizes()[0]
+
+    @property
+    def nnz(self):
+        """CSR elements of the built operator as the getters export them."""
+        return self._sizes()[1]
 
     @property
     def handle(self):
@@ -339,13 +354,11 @@ class Context:
         alpha = np.ascontiguousarray(alpha, dtype=np.uint64)
         beta = np.ascontiguousarray(beta, dtype=np.uint64)
         self._check(lib().qdkgb_set_dets(self._h, len(alpha), _ptr(alpha), _ptr(beta)))
-        self.ndets = len(alpha)
 
     def build_hamiltonian(self, thresh=np.finfo(np.float64).eps, storage=H_FP64):
         nnz = ctypes.c_int64()
         self._check(lib().qdkgb_build_hamiltonian(self._h, float(thresh), storage, ctypes.byref(nnz)))
-        self.nnz = nnz.value
-        return self.nnz
+        return nnz.value
 
     def build_operator(self, thresh=np.finfo(np.float64).eps, storage=H_FP64, max_m=200):
         """The stored Hamiltonian when it fits on the device, else (complete
@@ -355,16 +368,14 @@ class Context:
         nnz = ctypes.c_int64()
         self._check(lib().qdkgb_build_operator(self._h, float(thresh), int(storage), int(max_m), ctypes.byref(lay),
                                                ctypes.byref(nnz)))
-        self.nnz = nnz.value
         return {LAYOUT_CSR: "csr", LAYOUT_SLAB: "slab", LAYOUT_DIRECT: "direct"}[lay.value]
 
     def build_direct_sigma(self):
         """Recompute-on-the-fly sigma for a complete space (no CSR stored)."""
         self._check(lib().qdkgb_build_direct_sigma(self._h))
-        self.nnz = 0  # no CSR: get_csr reports the library's error
 
     def get_csr(self, index_bits=64):
-        n, nnz = self.ndets, self.nnz
+        n, nnz = self._sizes()
         it = np.int64 if index_bits == 64 else np.int32
         rp = np.zeros(n + 1, dtype=it)
         ci = np.zeros(nnz, dtype=it)
@@ -392,8 +403,6 @@ class Context:
         nz = _f64(values)
         n = len(rp) - 1
         self._check(lib().qdkgb_set_csr(self._h, n, _ptr(rp), _ptr(ci), _ptr(nz)))
-        self.ndets = n
-        self.nnz = len(nz)
 
     def diagonal(self):
         d = np.zeros(self.ndets)
@@ -513,7 +522,6 @@ class Context:
                                       ctypes.byref(s), float(matel_tol), ctypes.byref(E), _ptr(C),
                                       ctypes.byref(info)))
         self.norb = n
-        self.ndets = nd.value
         return E.value, C, info.as_dict()
 
 

@@ -311,6 +311,13 @@ int qdkgb_device_bytes(const qdkgb_context* c, int64_t* bytes) {
   return QDKGB_OK;
 }
 
+int qdkgb_problem_size(const qdkgb_context* c, int64_t* ndets, int64_t* nnz) {
+  if (!c) return QDKGB_ERR_INVALID;
+  if (ndets) *ndets = c->H.valid ? c->H.n : (c->have_dets ? c->dets.ndets : 0);
+  if (nnz) *nnz = (c->H.valid && !c->op_direct) ? c->H.nnz : 0;
+  return QDKGB_OK;
+}
+
 int qdkgb_operator_layout(const qdkgb_context* c, int* layout, int64_t* stored) {
   if (!c || !layout) return QDKGB_ERR_INVALID;
   const Hcsr& H = c->H;
