@@ -288,6 +288,7 @@ typedef struct qdkgb_asci_settings {
   double min_warm_start_overlap;   /* default 0.5 */
   double taper_grow_factor;        /* default 0 (off): the growth factor of a step that would pass ntdets_max */
   int just_singles;                /* default 0: 1 = the search enumerates single excitations only */
+  double min_patch_overlap;        /* default 0.3: patch the previous Hamiltonian when kept/new >= this */
 } qdkgb_asci_settings;
 
 void qdkgb_asci_default_settings(qdkgb_asci_settings* s);

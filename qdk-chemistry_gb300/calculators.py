@@ -610,7 +610,7 @@ class Gb300Asci(MultiConfigurationCalculator):
                 growth_recovery_rate=s.get("growth_recovery_rate"), max_refine_iter=s.get("max_refine_iter"),
                 refine_energy_tol=s.get("refine_energy_tol"), warm_start=int(s.get("warm_start_davidson")),
                 min_warm_start_overlap=s.get("min_warm_start_overlap"), taper_grow_factor=s.get("taper_grow_factor"),
-                just_singles=int(s.get("just_singles")))
+                just_singles=int(s.get("just_singles")), min_patch_overlap=s.get("min_patch_overlap"))
             tol = s.get("ci_residual_tolerance")
             grow_tol = s.get("grow_ci_residual_tolerance")
             refine = s.get("max_refine_iter") > 0

@@ -77,7 +77,7 @@ class AsciSettings(ctypes.Structure):
                 ("growth_recovery_rate", ctypes.c_double), ("max_refine_iter", ctypes.c_int64),
                 ("refine_energy_tol", ctypes.c_double), ("warm_start", ctypes.c_int),
                 ("min_warm_start_overlap", ctypes.c_double), ("taper_grow_factor", ctypes.c_double),
-                ("just_singles", ctypes.c_int)]
+                ("just_singles", ctypes.c_int), ("min_patch_overlap", ctypes.c_double)]
 
 
 class CasInstance(ctypes.Structure):

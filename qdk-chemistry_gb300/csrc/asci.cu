@@ -807,9 +807,6 @@ struct HPatchCache {
   bool valid = false;
 };
 
-// patch only when at least this share of the new list was in the old one
-constexpr double kMinPatchOverlap = 0.3;
-
 bool patch_disabled() {
   const char* e = std::getenv("QDKGB_ASCI_FULL_BUILD");
   return e && e[0] && e[0] != '0';
@@ -845,7 +842,7 @@ double sci_diag_gpu(Context* c, const qdkgb_asci_settings& S, const qdkgb_davids
   bool patched = false;
   if (have_old && !c->fci)
     patched = build_hamiltonian_patched(c, matel_tol, cache->a, cache->b, old.b[0], old.b[1], old.b[2],
-                                        kMinPatchOverlap);
+                                        S.min_patch_overlap);
   for (DeviceBuffer& x : old.b) dev_free(c, x);
   if (patched)
     ++c->asci_patches;
@@ -866,7 +863,6 @@ double sci_diag_gpu(Context* c, const qdkgb_asci_settings& S, const qdkgb_davids
   double E = 0.;
   davidson(c, &s, &E, X.data(), nullptr);
   clock.lap(3);
-  (void)S;
   return E;
 }
 

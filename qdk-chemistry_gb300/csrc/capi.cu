@@ -633,6 +633,7 @@ void qdkgb_asci_default_settings(qdkgb_asci_settings* s) {
   s->min_warm_start_overlap = 0.5;
   s->taper_grow_factor = 0.0;
   s->just_singles = 0;
+  s->min_patch_overlap = 0.3;
 }
 
 int qdkgb_asci_search(qdkgb_context* c, const qdkgb_asci_settings* s, int64_t ncore, const uint64_t* ca,

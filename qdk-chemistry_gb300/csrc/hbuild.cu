@@ -1048,7 +1048,7 @@ bool build_hamiltonian_patched(Context* c, double thresh, const std::vector<uint
       ++in;
     }
   }
-  if ((double)kept < min_overlap * (double)n) return false;
+  if ((double)kept / (double)n < min_overlap) return false;
   // walked rows: the added determinants
   std::vector<uint8_t> walk(n, 0);
   std::vector<int32_t> rows, widx(n, -1);

@@ -159,7 +159,8 @@ void build_hamiltonian(Context* c, double thresh, int storage);
 bool build_operator(Context* c, double thresh, int storage, int max_m);  // true: direct sigma
 // The CSR of the current list from the previous list's CSR (old host lists
 // sorted by spin_comparator, old FP64 CSR buffers, the same threshold); false
-// when fewer than min_overlap of the new determinants were kept.
+// when the kept share of the new determinants is below min_overlap
+// (incremental_h_build.hpp:263-282).
 bool build_hamiltonian_patched(Context* c, double thresh, const std::vector<uint64_t>& oa,
                                const std::vector<uint64_t>& ob, DeviceBuffer& old_rowptr, DeviceBuffer& old_colind,
                                DeviceBuffer& old_val, double min_overlap);
