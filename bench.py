@@ -413,6 +413,19 @@ def batch_instances(pkg, n=BATCH_N, seed=BATCH_SEED):
     return out
 
 
+def _slab_elements(no, na, nb):
+    """Stored values of one complete (norb, na, nb) space in the slab layout:
+    determinants x row length."""
+    from math import comb
+
+    ga, gb = comb(no, na), comb(no, nb)
+    ka, kb = na * (no - na), nb * (no - nb)
+    n1b = 1 + kb
+    n2b = 1 + kb + comb(nb, 2) * comb(no - nb, 2)
+    c2a = comb(na, 2) * comb(no - na, 2)
+    return ga * gb * (n2b + ka * n1b + c2a)
+
+
 def _batch_bytes(inst):
     """Stored values read by one FP32 sigma over every instance (slab: rowlen
     per determinant) plus x and y."""
@@ -456,6 +469,17 @@ def run_batched(args):
             infos.append(info)
     launches = capi.kernel_launches() - launches0
     t = float(np.mean(times))
+    plan = capi.batch_plan(ctx)
+    its_last = np.asarray(its)
+    # the lockstep launch sequence (the previous solver) on the same batch
+    t_lock = None
+    if not args.no_cpu:
+        capi.casci_batch(ctx, inst, res_tol=RES_TOL, persistent=0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        capi.casci_batch(ctx, inst, res_tol=RES_TOL, persistent=0)
+        torch.cuda.synchronize()
+        t_lock = time.perf_counter() - t0
     # plain per-instance FP64 GPU path on a sample (every 8th instance), scaled
     sample = inst[::8]
     ctx1 = capi.Context(local)
@@ -472,6 +496,13 @@ def run_batched(args):
     if rank != 0:
         return
     counts = {str(k): int(sum(1 for x in inst if x[0] == k)) for k in BATCH_SIZES}
+    # whole-solve sigma traffic: every sigma application streams the
+    # instance's stored values once (4 bytes each; the full-precision refresh
+    # reads 8, so this is a lower bound) - against the measured HBM peak
+    stored = [_slab_elements(x[0], x[1], x[2]) for x in inst]
+    sigma_bytes = float(sum(int(n_it) * st * 4 for n_it, st in zip(its_last, stored)))
+    peak, peak_kind = _peaks()
+    achieved = sigma_bytes / t / 1e9
     h2d = int(sum(x[3].nbytes + x[4].nbytes for x in inst))
     d2h = int(sum(8 + x[0] ** 2 * 8 for x in inst))
     line = {
@@ -488,6 +519,14 @@ def run_batched(args):
                                   "sample": "every 8th instance (%d) through qdkgb_casci FP64, scaled" % len(sample),
                                   "max_abs_energy_diff_vs_batch": float(max(dE))},
         "batch_speedup_vs_per_instance_fp64": t_loop / t,
+        "roofline": {"bound": "hbm", "kernel": "k_bp_solve (persistent: one cluster per instance, whole Davidson)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_kind, "traffic": None,
+                     "algorithmic_bytes": sigma_bytes,
+                     "note": "sigma bytes of the whole solve (iterations x stored values x 4 B per instance) over "
+                             "the call's wall time, which also holds emission, vector work and the eigensolves"},
+        "persistent_plan": plan,
+        "lockstep_s": t_lock,
         "sigma_gbs_per_fp32_sweep_bytes": _batch_bytes(inst),
         "max_sigma_applications": max(i["iterations"] for i in infos),
         "graph_replays": infos[-1]["graph_replays"],

@@ -404,8 +404,12 @@ typedef struct {
   int max_cycles;             /* restarts before giving up (200) */
   double matel_tol;           /* Hamiltonian threshold (machine epsilon) */
   double min_abs_denominator; /* preconditioner clamp (1e-12) */
-  int use_graph;              /* replay the inner iteration from a CUDA graph (1) */
+  int use_graph;              /* lockstep path: replay the inner iteration from a CUDA graph (1) */
   int64_t max_slab_bytes;     /* stored-matrix bytes per sub-batch (96 GiB) */
+  int persistent;             /* 1 (default): one persistent cluster launch per shape solves every
+                                 instance; 0: the lockstep launch sequence over all instances */
+  int cluster;                /* persistent: CTAs per instance, 1, 2, 4 or 8; 0 (default): measured
+                                 per shape on first use and kept on the context (qdkgb_batch_plan) */
 } qdkgb_batch_settings;
 
 typedef struct {
@@ -415,6 +419,15 @@ typedef struct {
 } qdkgb_batch_info;
 
 int qdkgb_batch_default_settings(qdkgb_batch_settings* s);
+/* The persistent batched solver's tuning record on this context (no
+ * counterpart in the reference): for each shape tuned so far, in tuning
+ * order, shape[3 i .. 3 i + 2] = (norb, nalpha, nbeta), cluster[i] = CTAs
+ * per instance in use, ncand[i] timed candidates with their cluster sizes
+ * cand_cluster[4 i + j] and milliseconds cand_ms[4 i + j] (a tuning run: a
+ * few inner iterations of every instance).  Records up to cap are written;
+ * *nshapes receives the number of records.  Any array may be NULL. */
+int qdkgb_batch_plan(const qdkgb_context* ctx, int cap, int* nshapes, int* shape, int* cluster, int* ncand,
+                     int* cand_cluster, double* cand_ms);
 int qdkgb_casci_batch(qdkgb_context* ctx, int ninst, const qdkgb_cas_instance* inst, const qdkgb_batch_settings* s,
                       double* energies, double* rdm1, int* iterations, qdkgb_batch_info* info);
 

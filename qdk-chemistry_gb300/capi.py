@@ -42,7 +42,7 @@ EXPORTED = [
     "qdkgb_sigma_split_noalloc", "qdkgb_set_csr", "qdkgb_build_direct_sigma", "qdkgb_build_operator",
     "qdkgb_operator_action", "qdkgb_rdms", "qdkgb_asci_phase_times", "qdkgb_sigma_plan",
     "qdkgb_asci_default_settings", "qdkgb_asci_search", "qdkgb_asci", "qdkgb_asci_pt2",
-    "qdkgb_batch_default_settings", "qdkgb_casci_batch",
+    "qdkgb_batch_default_settings", "qdkgb_casci_batch", "qdkgb_batch_plan",
 ]
 
 
@@ -89,7 +89,7 @@ class BatchSettings(ctypes.Structure):
     _fields_ = [("res_tol", ctypes.c_double), ("precision", ctypes.c_int), ("max_subspace", ctypes.c_int),
                 ("max_cycles", ctypes.c_int), ("matel_tol", ctypes.c_double),
                 ("min_abs_denominator", ctypes.c_double), ("use_graph", ctypes.c_int),
-                ("max_slab_bytes", ctypes.c_int64)]
+                ("max_slab_bytes", ctypes.c_int64), ("persistent", ctypes.c_int), ("cluster", ctypes.c_int)]
 
 
 class BatchInfo(ctypes.Structure):
@@ -140,6 +140,7 @@ def lib():
     L.qdkgb_operator_action.argtypes = [vp, i64, dp, vp, i64, dp, vp, i64]
     L.qdkgb_rdms.argtypes = [vp, vp, vp, vp]
     L.qdkgb_asci_phase_times.argtypes = [vp, vp, P(i64), P(i64)]
+    L.qdkgb_batch_plan.argtypes = [vp, ci, P(ci), vp, vp, vp, vp, vp]
     L.qdkgb_sigma_plan.argtypes = [vp, ci, P(ci), P(ci), vp, vp]
     L.qdkgb_get_csr64_rows.argtypes = [vp, i64, i64, vp, vp, vp]
     L.qdkgb_diagonal.argtypes = [vp, vp]
@@ -598,6 +599,25 @@ def asci_phase_times(ctx):
     ctx._check(lib().qdkgb_asci_phase_times(ctx.handle, _ptr(t), ctypes.byref(it), ctypes.byref(pb)))
     return {"search_s": t[0], "det_space_s": t[1], "hbuild_s": t[2], "davidson_s": t[3], "iterations": it.value,
             "patched_builds": pb.value}
+
+
+def batch_plan(ctx, cap=16):
+    """The persistent batched solver's tuning record (qdkgb_batch_plan): per
+    tuned shape, its (norb, nalpha, nbeta), the cluster size in use and the
+    timed candidates as (cluster size, ms)."""
+    n = ctypes.c_int()
+    shape = np.zeros(3 * cap, dtype=np.int32)
+    cl = np.zeros(cap, dtype=np.int32)
+    nc = np.zeros(cap, dtype=np.int32)
+    cc = np.zeros(4 * cap, dtype=np.int32)
+    cm = np.zeros(4 * cap)
+    ctx._check(lib().qdkgb_batch_plan(ctx.handle, cap, ctypes.byref(n), _ptr(shape), _ptr(cl), _ptr(nc), _ptr(cc),
+                                      _ptr(cm)))
+    out = []
+    for i in range(min(n.value, cap)):
+        out.append({"shape": tuple(int(v) for v in shape[3 * i:3 * i + 3]), "cluster": int(cl[i]),
+                    "candidates": [(int(cc[4 * i + j]), float(cm[4 * i + j])) for j in range(int(nc[i]))]})
+    return out
 
 
 def default_batch_settings(**kw):

@@ -27,6 +27,7 @@
 #include <tuple>
 #include <vector>
 
+#include "batch_kernels.cuh"
 #include "common.cuh"
 #include "internal.h"
 
@@ -299,25 +300,6 @@ __global__ void __launch_bounds__(kBT)
   if (threadIdx.x == 0) partial[(int64_t)b * nchunk + blockIdx.x] = acc;
 }
 
-// deterministic filler in [-1, 1): the last-resort second restart vector,
-// inside the spin-flip sector s of an nstr x nstr coefficient matrix when
-// s != 0 (f(i, j) = s f(j, i))
-__device__ __forceinline__ double filler(int64_t i, int64_t nstr, double s) {
-  int64_t key = i;
-  double sg = 1.;
-  if (s != 0.) {
-    const int64_t g = i / nstr, b = i - g * nstr;
-    if (g == b && s < 0.) return 0.;
-    key = g < b ? g * nstr + b : b * nstr + g;
-    sg = (g > b) ? s : 1.;
-  }
-  uint64_t h = (uint64_t)key * 0x9E3779B97F4A7C15ull;
-  h ^= h >> 31;
-  h *= 0xBF58476D1CE4E5B9ull;
-  h ^= h >> 29;
-  return sg * ((double)(h >> 11) * 0x1p-52 - 1.0);
-}
-
 // GD+1 restart: partial sums of x.v and v.v for the candidates
 // v = xprev, r, filler (six sums per chunk)
 __global__ void __launch_bounds__(kBT)
@@ -466,11 +448,7 @@ __global__ void k_b_guess(const double* __restrict__ D, int64_t n, double* __res
   if (threadIdx.x == 0) idx[b] = k;
 }
 
-// spin-summed 1-RDM gamma_pq = <C| a+_p a_q |C> (alpha + beta) of a complete
-// space, one CTA per instance: diagonal from the row / column weights,
-// off-diagonal from one dot product per single excitation of an alpha group
-// (rows) or a beta string (columns) - form_rdms_spin_dep's one-body part
-// (sorted_double_loop.hpp:626-753) on the product structure.
+// spin-summed 1-RDM of each instance's vector (rdm1_cta), one CTA per instance
 __global__ void k_b_rdm1(const double* __restrict__ C, int G, int Nb, int norb, const uint64_t* __restrict__ galpha,
                          const uint64_t* __restrict__ ubeta, const int64_t* __restrict__ acon_ptr,
                          const int32_t* __restrict__ acon_idx, const int8_t* __restrict__ acon_lvl,
@@ -478,53 +456,8 @@ __global__ void k_b_rdm1(const double* __restrict__ C, int G, int Nb, int norb, 
                          double* __restrict__ out, const int64_t* __restrict__ out_off) {
   extern __shared__ double gam[];
   const int b = blockIdx.x;
-  const double* X = C + (int64_t)b * G * Nb;
-  const int nn = norb * norb;
-  for (int i = threadIdx.x; i < nn; i += blockDim.x) gam[i] = 0.;
-  __syncthreads();
-  // diagonal
-  for (int g = threadIdx.x; g < G; g += blockDim.x) {
-    double w = 0.;
-    for (int j = 0; j < Nb; ++j) w += X[(int64_t)g * Nb + j] * X[(int64_t)g * Nb + j];
-    for (uint64_t s = galpha[g]; s; s &= s - 1) atomicAdd(&gam[low_bit(s) * (norb + 1)], w);
-  }
-  for (int j = threadIdx.x; j < Nb; j += blockDim.x) {
-    double w = 0.;
-    for (int g = 0; g < G; ++g) w += X[(int64_t)g * Nb + j] * X[(int64_t)g * Nb + j];
-    for (uint64_t s = ubeta[j]; s; s &= s - 1) atomicAdd(&gam[low_bit(s) * (norb + 1)], w);
-  }
-  // alpha singles: pairs (g, h > g)
-  for (int g = threadIdx.x; g < G; g += blockDim.x) {
-    const uint64_t ket = galpha[g];
-    for (int64_t e = acon_ptr[g]; e < acon_ptr[g + 1]; ++e) {
-      const int h = acon_idx[e];
-      if (acon_lvl[e] != 1 || h <= g) continue;
-      const uint64_t bra = galpha[h];
-      double dot = 0.;
-      for (int j = 0; j < Nb; ++j) dot += X[(int64_t)h * Nb + j] * X[(int64_t)g * Nb + j];
-      const SingleEx sx = single_ex(bra, ket, bra ^ ket);
-      const double v = sx.neg ? -dot : dot;
-      atomicAdd(&gam[sx.v * norb + sx.o], v);
-      atomicAdd(&gam[sx.o * norb + sx.v], v);
-    }
-  }
-  // beta singles: pairs (j, j2 > j)
-  for (int j = threadIdx.x; j < Nb; j += blockDim.x) {
-    const uint64_t ket = ubeta[j];
-    for (int64_t e = b1_ptr[j]; e < b1_ptr[j + 1]; ++e) {
-      const int j2 = b1_idx[e];
-      if (j2 <= j) continue;
-      const uint64_t bra = ubeta[j2];
-      double dot = 0.;
-      for (int g = 0; g < G; ++g) dot += X[(int64_t)g * Nb + j2] * X[(int64_t)g * Nb + j];
-      const SingleEx sx = single_ex(bra, ket, bra ^ ket);
-      const double v = sx.neg ? -dot : dot;
-      atomicAdd(&gam[sx.v * norb + sx.o], v);
-      atomicAdd(&gam[sx.o * norb + sx.v], v);
-    }
-  }
-  __syncthreads();
-  for (int i = threadIdx.x; i < nn; i += blockDim.x) out[out_off[b] + i] = gam[i];
+  rdm1_cta(C + (int64_t)b * G * Nb, G, Nb, norb, galpha, ubeta, acon_ptr, acon_idx, acon_lvl, b1_ptr, b1_idx,
+           out + out_off[b], gam);
 }
 
 unsigned grid_x(int64_t n, int B) {
@@ -642,6 +575,51 @@ void casci_batch(Context* ctx, int ninst, const qdkgb_cas_instance* inst, const 
       } else {
         val = dev_array<double>(cc, dval, (size_t)B * stored);
         slab_emit_batch(cc, B, I, D, QDKGB_H_FP64, val, nullptr, nullptr, thresh);
+      }
+      if (st.persistent) {
+        // ---- one persistent launch over the sub-batch (batch_persist.cu)
+        DeviceBuffer &pe = bs.b[11], &pr = bs.b[12], &pi = bs.b[13];
+        BatchShapeJob job{};
+        job.norb = n;
+        job.na = shape.na;
+        job.nb = shape.nb;
+        job.B = B;
+        job.m = m;
+        job.max_cycles = st.max_cycles;
+        job.cluster = st.cluster;
+        job.mixed = mixed;
+        job.square = square;
+        job.N = N;
+        job.nstr = S.nbeta;
+        job.vstride = stored;
+        job.tol = st.res_tol;
+        job.min_abs = st.min_abs_denominator;
+        job.hi = hi;
+        job.lo = lo;
+        job.val = val;
+        job.D = D;
+        job.energy = dev_array<double>(cc, pe, (size_t)2 * B);
+        job.resid = job.energy + B;
+        job.iters = dev_array<int>(cc, pi, (size_t)2 * B);
+        job.notdone = job.iters + B;
+        job.rdm = rdm1 ? dev_array<double>(cc, pr, (size_t)B * n2) : nullptr;
+        batch_solve_persistent(cc, ctx, job);
+        std::vector<double> hE(2 * (size_t)B);
+        std::vector<int> hI(2 * (size_t)B);
+        QDKGB_CUDA(cudaMemcpyAsync(hE.data(), job.energy, 2 * B * 8, cudaMemcpyDeviceToHost, s0));
+        QDKGB_CUDA(cudaMemcpyAsync(hI.data(), job.iters, 2 * B * 4, cudaMemcpyDeviceToHost, s0));
+        std::vector<double> hout(rdm1 ? (size_t)B * n2 : 0);
+        if (rdm1) QDKGB_CUDA(cudaMemcpyAsync(hout.data(), job.rdm, B * n2 * 8, cudaMemcpyDeviceToHost, s0));
+        QDKGB_CUDA(cudaStreamSynchronize(s0));
+        for (int q = 0; q < B; ++q) {
+          const int i = members[off + q];
+          if (energies) energies[i] = hE[q];
+          if (iters) iters[i] = hI[q];
+          max_it = std::max(max_it, hI[q]);
+          if (hI[B + q]) all_conv = false;
+          if (rdm1) std::memcpy(rdm1 + rdm_off[i], &hout[q * n2], n2 * 8);
+        }
+        continue;
       }
       // ---- Davidson state
       const int KM = m + 1;

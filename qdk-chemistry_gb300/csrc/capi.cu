@@ -761,6 +761,31 @@ int qdkgb_batch_default_settings(qdkgb_batch_settings* s) {
   s->min_abs_denominator = 1e-12;
   s->use_graph = 1;
   s->max_slab_bytes = (int64_t)96 << 30;
+  s->persistent = 1;
+  s->cluster = 0;
+  return QDKGB_OK;
+}
+
+int qdkgb_batch_plan(const qdkgb_context* c, int cap, int* nshapes, int* shape, int* cluster, int* ncand,
+                     int* cand_cluster, double* cand_ms) {
+  if (!c || cap < 0) return QDKGB_ERR_INVALID;
+  const int n = (int)c->batch_tune.size();
+  if (nshapes) *nshapes = n;
+  for (int i = 0; i < std::min(n, cap); ++i) {
+    const BatchTune& t = c->batch_tune[i];
+    if (shape) {
+      shape[3 * i] = t.norb;
+      shape[3 * i + 1] = t.na;
+      shape[3 * i + 2] = t.nb;
+    }
+    if (cluster) cluster[i] = t.cluster;
+    const int nc = std::min<int>(4, (int)t.cand_ms.size());
+    if (ncand) ncand[i] = nc;
+    for (int j = 0; j < nc; ++j) {
+      if (cand_cluster) cand_cluster[4 * i + j] = t.cand_ms[j].first;
+      if (cand_ms) cand_ms[4 * i + j] = t.cand_ms[j].second;
+    }
+  }
   return QDKGB_OK;
 }
 

@@ -5,6 +5,7 @@
 #include <cstdint>
 #include <stdexcept>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include <nvtx3/nvToolsExt.h>
@@ -117,6 +118,14 @@ struct DavidsonWork {
   int64_t n = 0, maxm = 0;
 };
 
+// The batched solver's measured choice for one shape: CTAs per instance
+// (cluster) and the timed candidates (cluster size, ms of a tuning run).
+struct BatchTune {
+  int norb, na, nb, m, mixed;
+  int cluster;
+  std::vector<std::pair<int, double>> cand_ms;
+};
+
 struct Context {
   int device = 0;
   cudaStream_t own_stream = nullptr, stream = nullptr;
@@ -143,6 +152,7 @@ struct Context {
   double asci_phase_s[4] = {0., 0., 0., 0.};
   int64_t asci_iters = 0;
   int64_t asci_patches = 0;  // Hamiltonians of the last qdkgb_asci call built by patching the previous one
+  std::vector<BatchTune> batch_tune;  // persistent batched solver: cluster size per shape
   DeviceBuffer host_pinned_dummy;
   double* pinned = nullptr;  // small pinned host staging (64 doubles)
 };
@@ -187,6 +197,26 @@ int struct_sigma_plan(Context* c, int plan, std::vector<std::pair<int, double>>*
 void casci_batch(Context* ctx, int ninst, const qdkgb_cas_instance* inst, const qdkgb_batch_settings& st,
                  double* energies, double* rdm1, int* iters, qdkgb_batch_info* info);
 // davidson.cu: lowest eigenpair of B small matrices, one CTA each
+// batch_persist.cu: one shape's sub-batch (slabs emitted, diagonals set) solved
+// by the persistent cluster kernel; results in the job's device arrays.
+// cc: the shape's context (space, tables, plans); owner: the caller's
+// context, which keeps the tuned cluster size per shape.
+struct BatchShapeJob {
+  int norb, na, nb, B, m, max_cycles, cluster;
+  bool mixed, square;
+  int64_t N, nstr, vstride;
+  double tol, min_abs;
+  const float* hi;
+  const float* lo;
+  const double* val;
+  const double* D;
+  double* energy;
+  double* resid;
+  int* iters;
+  int* notdone;
+  double* rdm;  // [B][norb^2] or null
+};
+void batch_solve_persistent(Context* cc, Context* owner, const BatchShapeJob& job);
 void lowest_eig_batch(cudaStream_t st, int B, const int* kdev, int kadd, int kmax, const double* Hs, int ldh,
                       int64_t hstride, double* eval, double* evec, int64_t estride, const int* active);
 void slab_emit_batch(Context* c, int B, const Integrals* d_ints, const double* diag_raw, int storage, double* val,

@@ -21,7 +21,7 @@ constexpr int kEigMaxK = QDKGB_EIG_MAX_SUBSPACE;
 constexpr int kEigThreads = 256;
 constexpr int kEigSmemK = 150;  // matrices up to this size live in shared memory
 
-__device__ double block_sum_eig(double v, double* red) {
+static __device__ double block_sum_eig(double v, double* red) {
   v = warp_sum(v);
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   __syncthreads();
@@ -39,7 +39,7 @@ __device__ double block_sum_eig(double v, double* red) {
 
 // number of eigenvalues of tridiag(d, e) below x (division-free Sturm sequence
 // of leading minors, rescaled by exact powers of two)
-__device__ int sturm_count(int k, const double* d, const double* e2, double x) {
+static __device__ int sturm_count(int k, const double* d, const double* e2, double x) {
   double p0 = 1., p1 = d[0] - x;
   int cnt = (p1 < 0.) ? 1 : 0;
   int s_prev = (p1 < 0.) ? -1 : 1;
@@ -62,11 +62,11 @@ __device__ int sturm_count(int k, const double* d, const double* e2, double x) {
   return cnt;
 }
 
-__device__ bool lowest_eig_mixed_cta(int k, const double* __restrict__ H, int ldh, int nev, double* eval,
+static __device__ bool lowest_eig_mixed_cta(int k, const double* __restrict__ H, int ldh, int nev, double* eval,
                                      double* evec, unsigned char* smem);
 constexpr int kEigMixedMaxK = 128;
 
-__device__ void lowest_eig_cta(int k, const double* __restrict__ H, int ldh, double* gA, int nev, double* eval,
+static __device__ void lowest_eig_cta(int k, const double* __restrict__ H, int ldh, double* gA, int nev, double* eval,
                                double* evec) {
   extern __shared__ double dyn[];
   __shared__ double d[kEigMaxK], e[kEigMaxK], e2[kEigMaxK], beta[kEigMaxK];
@@ -294,7 +294,7 @@ __device__ __forceinline__ T group_sum(T v, int g) {
 // the FP64 matrix in the refinement); floats Q[k*ldq] (Q[r*ldq + i] =
 // component r of eigenvector i, ldq = k | 1), d, e, e2, beta, lam, lamhi, vec
 // (kEigMixedMaxK each), red[32]
-__device__ bool lowest_eig_mixed_cta(int k, const double* __restrict__ H, int ldh, int nev, double* eval,
+static __device__ bool lowest_eig_mixed_cta(int k, const double* __restrict__ H, int ldh, int nev, double* eval,
                                      double* evec, unsigned char* smem) {
   const int tid = threadIdx.x, nt = blockDim.x;
   const int wid = tid >> 5, lane = tid & 31;

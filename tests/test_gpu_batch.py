@@ -1,7 +1,9 @@
 """Batched CASCI (qdkgb_casci_batch) against the CPU oracle: per-instance
 energies (mixed form within 1e-8 Eh of the oracle's FP64 Davidson, FP64 form
 within 1e-10) and spin-summed 1-RDMs (1e-6 absolute: the vectors agree to the
-residual tolerance over the gap), for instances of uneven size and shape."""
+residual tolerance over the gap), for instances of uneven size and shape,
+through both solvers: the persistent cluster kernel (default; every cluster
+size agrees with the lockstep path) and the lockstep launch sequence."""
 import numpy as np
 import pytest
 
@@ -41,10 +43,11 @@ def _oracle_ref(oracle, pkg, inst):
 SHAPES = [(6, 3, 3), (4, 2, 2), (8, 4, 4), (6, 3, 3), (6, 3, 2), (8, 4, 4), (4, 2, 2), (6, 3, 3)]
 
 
-def test_batch_mixed_matches_oracle(ctx, oracle, pkg, capi):
+@pytest.mark.parametrize("persistent", [1, 0])
+def test_batch_mixed_matches_oracle(ctx, oracle, pkg, capi, persistent):
     inst = _instances(pkg, SHAPES, 100)
-    E, R, its, info = capi.casci_batch(ctx, inst, res_tol=1e-8)
-    assert info["graph_replays"] > 0
+    E, R, its, info = capi.casci_batch(ctx, inst, res_tol=1e-8, persistent=persistent)
+    assert (info["graph_replays"] > 0) == (persistent == 0)
     for i, q in enumerate(inst):
         Eo, Ro = _oracle_ref(oracle, pkg, q)
         assert abs(E[i] - Eo) < 1e-8, (i, E[i], Eo)
@@ -53,9 +56,10 @@ def test_batch_mixed_matches_oracle(ctx, oracle, pkg, capi):
         assert its[i] > 0
 
 
-def test_batch_fp64_matches_oracle(ctx, oracle, pkg, capi):
+@pytest.mark.parametrize("persistent", [1, 0])
+def test_batch_fp64_matches_oracle(ctx, oracle, pkg, capi, persistent):
     inst = _instances(pkg, SHAPES[:5], 200)
-    E, R, its, info = capi.casci_batch(ctx, inst, res_tol=1e-9, precision=capi.PREC_FP64)
+    E, R, its, info = capi.casci_batch(ctx, inst, res_tol=1e-9, precision=capi.PREC_FP64, persistent=persistent)
     for i, q in enumerate(inst):
         Eo, Ro = _oracle_ref(oracle, pkg, q)
         assert abs(E[i] - Eo) < 1e-10, (i, E[i], Eo)
@@ -64,8 +68,8 @@ def test_batch_fp64_matches_oracle(ctx, oracle, pkg, capi):
 
 def test_batch_graph_replay_is_identical_and_order_independent(ctx, pkg, capi):
     inst = _instances(pkg, SHAPES, 300)
-    E1, _, it1, i1 = capi.casci_batch(ctx, inst, want_rdm1=False, use_graph=1)
-    E2, _, it2, i2 = capi.casci_batch(ctx, inst, want_rdm1=False, use_graph=0)
+    E1, _, it1, i1 = capi.casci_batch(ctx, inst, want_rdm1=False, use_graph=1, persistent=0)
+    E2, _, it2, i2 = capi.casci_batch(ctx, inst, want_rdm1=False, use_graph=0, persistent=0)
     assert i1["graph_replays"] > 0 and i2["graph_replays"] == 0
     assert np.array_equal(E1, E2) and np.array_equal(it1, it2)
     # one instance alone gives the same energy as inside the batch
@@ -96,3 +100,39 @@ def test_batch_rejects_bad_input(ctx, pkg, capi):
         capi.casci_batch(ctx, inst, max_subspace=1)
     E, _, _, _ = capi.casci_batch(ctx, [], want_rdm1=False)
     assert len(E) == 0
+
+
+def test_persistent_cluster_sizes_agree_with_lockstep(ctx, pkg, capi):
+    """Every cluster size of the persistent solver (CTAs per instance) gives
+    the lockstep path's energies and 1-RDMs: the same algorithm, only the
+    reduction order differs."""
+    inst = _instances(pkg, [(8, 4, 4), (8, 4, 4), (8, 4, 3), (6, 3, 3), (8, 4, 4)], 600)
+    E0, R0, it0, _ = capi.casci_batch(ctx, inst, persistent=0)
+    for cl in (1, 2, 4):
+        E, R, its, _ = capi.casci_batch(ctx, inst, persistent=1, cluster=cl)
+        assert np.max(np.abs(E - E0)) < 1e-9, cl
+        for i in range(len(inst)):
+            np.testing.assert_allclose(R[i], R0[i], atol=1e-7, rtol=0)
+        assert np.all(np.abs(its - it0) <= 2), (cl, its, it0)
+
+
+def test_persistent_autotuner_records_its_choice(pkg, capi, oracle):
+    """The first persistent call on a context times the cluster-size
+    candidates of each shape (a few iterations of every instance) and keeps
+    the fastest (qdkgb_batch_plan); the energies match the oracle."""
+    inst = _instances(pkg, [(10, 5, 5)] * 3 + [(6, 3, 3)] * 2, 700)
+    with capi.Context(0) as c:
+        assert capi.batch_plan(c) == []
+        E, _, _, _ = capi.casci_batch(c, inst, want_rdm1=False)
+        plan = {p["shape"]: p for p in capi.batch_plan(c)}
+        E2, _, _, _ = capi.casci_batch(c, inst, want_rdm1=False)
+        assert len(capi.batch_plan(c)) == len(plan)
+    p10 = plan[(10, 5, 5)]
+    assert len(p10["candidates"]) >= 2 and p10["cluster"] in [q for q, _ in p10["candidates"]]
+    assert all(ms > 0 for _, ms in p10["candidates"])
+    assert min(p10["candidates"], key=lambda q: q[1])[0] == p10["cluster"]
+    assert (6, 3, 3) not in plan  # one candidate only: nothing to time
+    assert np.max(np.abs(E - E2)) < 1e-9
+    for j in (0, 3):
+        Eo, _ = _oracle_ref(oracle, pkg, inst[j])
+        assert abs(E[j] - Eo) < 1e-8
