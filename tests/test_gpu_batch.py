@@ -104,16 +104,23 @@ def test_batch_rejects_bad_input(ctx, pkg, capi):
 
 def test_persistent_cluster_sizes_agree_with_lockstep(ctx, pkg, capi):
     """Every cluster size of the persistent solver (CTAs per instance) gives
-    the lockstep path's energies and 1-RDMs: the same algorithm, only the
-    reduction order differs."""
+    the lockstep path's energies and 1-RDMs.  The algorithm is the same; the
+    reductions run in another order, and the lockstep path's FP32 sigma is
+    the vectorised kernel (another rounding of the FP32 products), so the
+    mixed form's iteration counts may differ; the FP64 form's agree to one."""
     inst = _instances(pkg, [(8, 4, 4), (8, 4, 4), (8, 4, 3), (6, 3, 3), (8, 4, 4)], 600)
     E0, R0, it0, _ = capi.casci_batch(ctx, inst, persistent=0)
+    F0, _, f0, _ = capi.casci_batch(ctx, inst, want_rdm1=False, persistent=0, precision=capi.PREC_FP64)
     for cl in (1, 2, 4):
         E, R, its, _ = capi.casci_batch(ctx, inst, persistent=1, cluster=cl)
         assert np.max(np.abs(E - E0)) < 1e-9, cl
         for i in range(len(inst)):
             np.testing.assert_allclose(R[i], R0[i], atol=1e-7, rtol=0)
-        assert np.all(np.abs(its - it0) <= 2), (cl, its, it0)
+        assert np.all(its > 0)
+        F, _, f, _ = capi.casci_batch(ctx, inst, want_rdm1=False, persistent=1, cluster=cl,
+                                      precision=capi.PREC_FP64)
+        assert np.max(np.abs(F - F0)) < 1e-10, cl
+        assert np.all(np.abs(f - f0) <= 1), (cl, f, f0)
 
 
 def test_persistent_autotuner_records_its_choice(pkg, capi, oracle):
