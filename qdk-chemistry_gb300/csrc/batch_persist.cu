@@ -45,12 +45,17 @@ namespace {
 constexpr int kPT = 256;       // threads per CTA (the projected eigensolver's CTA size)
 constexpr int kPW = kPT / 32;  // warps per CTA
 constexpr int kPMaxK = 72;     // values per cluster reduction (subspace + 1, or six restart dots)
+constexpr int kSG = 4;         // FP32 sigma: tile groups per CTA, kPT / kSG threads each
+constexpr int kSGT = kPT / kSG;
+constexpr int kRing = 8;       // FP32 sigma: positions in flight per thread (async copies)
 
 struct BPArgs {
   SlabArgs A;
   PlanArgs P0, P1;  // FP32 plan (4-byte staged x), 8-byte plan (FP64 and float-float)
   int64_t N, nstr;  // determinants; strings per spin of a square space (flip projection)
   int B, m, max_cycles, mixed, square, probe_iters;
+  int pipe32;           // FP32 sigma through the async-copy tiles (beta strings a multiple of 4)
+  int64_t stage_bytes;  // per tile group: staged x slices + segment record (pipelined tiles)
   double tol, min_abs;
   int64_t vstride;  // slab elements per instance
   const float* hi;
@@ -129,6 +134,40 @@ __device__ __forceinline__ double cluster_dot(cg::cluster_group& cl, Red& R, con
   return R.t[0];
 }
 
+// this CTA's partial dots A[j] . w over its rows for j < nj (A: columns N
+// apart), stashed as values j0 + j; four columns per pass over the rows so
+// that each thread keeps five loads in flight.  w is read through L2 when
+// other CTAs may have written it (WCG).
+template <bool WCG>
+__device__ __forceinline__ void slice_multidot(Red& R, const double* __restrict__ A, int64_t N, int nj,
+                                               const double* __restrict__ w, int64_t lo, int64_t hi, int j0) {
+  for (int jb = 0; jb < nj; jb += 4) {
+    const int nb = nj - jb < 4 ? nj - jb : 4;
+    const double* a0 = A + (int64_t)jb * N;
+    double s0 = 0., s1 = 0., s2 = 0., s3 = 0.;
+    if (nb == 4) {
+      for (int64_t i = lo + threadIdx.x; i < hi; i += kPT) {
+        const double wi = WCG ? __ldcg(w + i) : w[i];
+        s0 += a0[i] * wi;
+        s1 += a0[N + i] * wi;
+        s2 += a0[2 * N + i] * wi;
+        s3 += a0[3 * N + i] * wi;
+      }
+    } else {
+      for (int64_t i = lo + threadIdx.x; i < hi; i += kPT) {
+        const double wi = WCG ? __ldcg(w + i) : w[i];
+        s0 += a0[i] * wi;
+        if (nb > 1) s1 += a0[N + i] * wi;
+        if (nb > 2) s2 += a0[2 * N + i] * wi;
+      }
+    }
+    stash(R, s0, j0 + jb);
+    if (nb > 1) stash(R, s1, j0 + jb + 1);
+    if (nb > 2) stash(R, s2, j0 + jb + 2);
+    if (nb > 3) stash(R, s3, j0 + jb + 3);
+  }
+}
+
 // projection on the spin-flip sector s of an nstr x nstr coefficient matrix;
 // the pair (i, j), i < j, belongs to the slice holding i * nstr + j, whose
 // mirror may lie in another CTA's slice (read and written through L2)
@@ -146,6 +185,107 @@ __device__ __forceinline__ void flip_slice(double* t, int64_t nstr, double s, in
   }
 }
 
+
+__device__ __forceinline__ void cp16_cg(void* dst, const void* src) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+__device__ __forceinline__ void group_bar(int id) { asm volatile("bar.sync %0, %1;\n" ::"r"(id), "r"(kSGT) : "memory"); }
+
+// One FP32 sigma tile (group g, segment s, part z) by a tile group of kSGT
+// threads, four adjacent beta strings per thread: the row values stream into
+// a per-thread ring of kRing positions through 16-byte async copies (L2 ->
+// shared, no registers held while in flight), each with its beta-list entries
+// (own-group and alpha-single blocks) or the alpha double's x (through L2:
+// x was written by other CTAs of the kernel).  Per row the products are
+// summed in the order of k_slab_sigma32v<4> (own block, then the
+// alpha-single blocks level-1 entry by entry, then the alpha doubles), so the
+// result is that kernel's bit for bit.
+__device__ void pipe_tile32(const SlabArgs& A, const PlanArgs& P, const float* __restrict__ vals,
+                            const float* __restrict__ x, float* __restrict__ out, int64_t part_stride, int g, int s,
+                            int z, float* xs, int32_t* rec, unsigned char* ring, int bar_id, int lt) {
+  const int Nb = A.Nb, nvec = Nb / 4;
+  const int32_t* rg = P.rec + ((int64_t)g * P.S + s) * P.R;
+  for (int i = lt; i < P.R; i += kSGT) rec[i] = __ldg(rg + i);
+  const int32_t* sh = P.segh + ((int64_t)g * P.S + s) * P.M;
+  const int q4 = P.M * nvec;
+  float4* xs4 = reinterpret_cast<float4*>(xs);
+  const float4* x4 = reinterpret_cast<const float4*>(x);
+#pragma unroll 4
+  for (int q = lt; q < q4; q += kSGT) {
+    const int j = q / nvec, i = q - j * nvec;
+    const int h = __ldg(sh + j);
+    if (h >= 0) xs4[q] = __ldcg(x4 + (int64_t)h * nvec + i);
+  }
+  group_bar(bar_id);
+  const int t = z * kSGT + lt;
+  if (t < nvec) {
+    const int has0 = rec[0], off0 = rec[1], sb0 = rec[2], n1b = rec[3];
+    const int32_t* e1 = rec + 4;
+    const int nd = rec[4 + 2 * n1b];
+    const int32_t* e2 = rec + 6 + 2 * n1b;
+    const int n_own = has0 ? A.n2 : 0, n_sing = A.n1 * n1b;
+    const int L = n_own + n_sing + nd;
+    const int b0 = t * 4;
+    const float* vg = vals + (int64_t)g * A.rowlen * Nb + b0;
+    float4* rv = reinterpret_cast<float4*>(ring);
+    uint4* ra = reinterpret_cast<uint4*>(ring + kRing * 16);
+    auto issue = [&](int q) {
+      const int slot = q & (kRing - 1);
+      int64_t voff;
+      const void* asrc;
+      if (q < n_own) {
+        voff = off0 + (int64_t)q * Nb;
+        asrc = A.blT + (int64_t)q * Nb + b0;
+      } else if (q < n_own + n_sing) {
+        const int u = q - n_own, k = u / n1b, e = u - k * n1b;
+        voff = e1[2 * e] + (int64_t)k * Nb;
+        asrc = A.blT + (int64_t)(A.n2 + k) * Nb + b0;
+      } else {
+        const int j = q - n_own - n_sing;
+        voff = e2[2 * j];
+        asrc = x + e2[2 * j + 1] + b0;
+      }
+      cp16_cg(rv + slot, vg + voff);
+      cp16_cg(ra + slot, asrc);
+    };
+#pragma unroll
+    for (int q = 0; q < kRing; ++q) {
+      if (q < L) issue(q);
+      cp_commit();
+    }
+    float c0 = 0.f, c1 = 0.f, c2 = 0.f, c3 = 0.f;
+    for (int q = 0; q < L; ++q) {
+      cp_wait<kRing - 1>();
+      const int slot = q & (kRing - 1);
+      const float4 v = rv[slot];
+      const uint4 au = ra[slot];
+      if (q < n_own + n_sing) {
+        const int sb = q < n_own ? sb0 : e1[2 * ((q - n_own) % n1b) + 1];
+        c0 = fmaf(v.x, xs[sb + (int)au.x], c0);
+        c1 = fmaf(v.y, xs[sb + (int)au.y], c1);
+        c2 = fmaf(v.z, xs[sb + (int)au.z], c2);
+        c3 = fmaf(v.w, xs[sb + (int)au.w], c3);
+      } else {
+        c0 = fmaf(v.x, __uint_as_float(au.x), c0);
+        c1 = fmaf(v.y, __uint_as_float(au.y), c1);
+        c2 = fmaf(v.z, __uint_as_float(au.z), c2);
+        c3 = fmaf(v.w, __uint_as_float(au.w), c3);
+      }
+      if (q + kRing < L) issue(q + kRing);
+      cp_commit();
+    }
+    cp_wait<0>();
+    *reinterpret_cast<float4*>(out + s * part_stride + (int64_t)g * Nb + b0) = make_float4(c0, c1, c2, c3);
+  }
+  group_bar(bar_id);
+}
+
 // y = H x for the cluster's instance: sigma tiles round-robin over the CTAs
 // into the partial buffer, then each CTA sums its own rows' segments (in
 // order) into y (so y's slice is written by its owner).
@@ -156,14 +296,31 @@ __device__ void cluster_sigma(const BPArgs& a, cg::cluster_group& cl, const void
   using Out = typename SlabPol<MODE>::Out;
   const PlanArgs& P = MODE == 0 ? a.P0 : a.P1;
   const int rank = (int)cl.block_rank(), CL = (int)cl.num_blocks();
-  const int Z = (a.A.Nb + kPT - 1) / kPT;
-  const int64_t tiles = (int64_t)a.A.G * P.S * Z;
-  for (int64_t t = rank; t < tiles; t += CL) {
-    const int z = (int)(t % Z);
-    const int64_t gs = t / Z;
-    const int s = (int)(gs % P.S), g = (int)(gs / P.S);
-    slab_sigma_tile<MODE, true>(a.A, P, vals, vlo, x, xlo, part, a.N, g, s, z, smem);
+  if (MODE == 0 && a.pipe32) {
+    // tile groups of kSGT threads, each on its own tiles and staging
+    const int sg = threadIdx.x / kSGT, lt = threadIdx.x - sg * kSGT;
+    const int Zp = (a.A.Nb / 4 + kSGT - 1) / kSGT;
+    const int64_t tiles = (int64_t)a.A.G * P.S * Zp;
+    float* xs = reinterpret_cast<float*>(smem + sg * a.stage_bytes);
+    int32_t* rec = reinterpret_cast<int32_t*>(smem + sg * a.stage_bytes + (int64_t)P.M * a.A.Nb * 4);
+    unsigned char* ring = smem + kSG * a.stage_bytes + (int64_t)threadIdx.x * (2 * kRing * 16);
+    for (int64_t t = (int64_t)rank * kSG + sg; t < tiles; t += (int64_t)CL * kSG) {
+      const int z = (int)(t % Zp);
+      const int64_t gs = t / Zp;
+      const int s = (int)(gs % P.S), g = (int)(gs / P.S);
+      pipe_tile32(a.A, P, (const float*)vals, (const float*)x, (float*)part, a.N, g, s, z, xs, rec, ring, 1 + sg, lt);
+    }
     __syncthreads();
+  } else {
+    const int Z = (a.A.Nb + kPT - 1) / kPT;
+    const int64_t tiles = (int64_t)a.A.G * P.S * Z;
+    for (int64_t t = rank; t < tiles; t += CL) {
+      const int z = (int)(t % Z);
+      const int64_t gs = t / Z;
+      const int s = (int)(gs % P.S), g = (int)(gs / P.S);
+      slab_sigma_tile<MODE, true>(a.A, P, vals, vlo, x, xlo, part, a.N, g, s, z, smem);
+      __syncthreads();
+    }
   }
   cl.sync();
   const Out* pp = (const Out*)part;
@@ -288,6 +445,7 @@ __global__ void __launch_bounds__(kPT) k_bp_solve(BPArgs a) {
       double acc = 0.;
       for (int64_t i = lo + tid; i < hi; i += kPT) {
         double sx = 0., sa = 0.;
+#pragma unroll 4
         for (int j = 0; j < k; ++j) {
           const double c = R.eg[1 + j];
           sx += V[j * N + i] * c;
@@ -424,14 +582,11 @@ __global__ void __launch_bounds__(kPT) k_bp_solve(BPArgs a) {
         cl.sync();
       }
       for (int pass = 0; pass < 2; ++pass) {  // CGS2 against V[0..k)
-        for (int j = 0; j < k; ++j) {
-          double s = 0.;
-          for (int64_t i = lo + tid; i < hi; i += kPT) s += V[j * N + i] * __ldcg(t + i);
-          stash(R, s, j);
-        }
+        slice_multidot<true>(R, V, N, k, t, lo, hi, 0);
         cluster_total(cl, R, k);
         for (int64_t i = lo + tid; i < hi; i += kPT) {
           double acc = 0.;
+#pragma unroll 4
           for (int j = 0; j < k; ++j) acc += V[j * N + i] * R.t[j];
           __stcg(t + i, __ldcg(t + i) - acc);
         }
@@ -465,11 +620,7 @@ __global__ void __launch_bounds__(kPT) k_bp_solve(BPArgs a) {
         for (int64_t i = lo + tid; i < hi; i += kPT) AV[k * N + i] = y[i];
       }
       // projected row k: Hs(k, j) = AV[j] . V[k], j <= k
-      for (int j = 0; j <= k; ++j) {
-        double s = 0.;
-        for (int64_t i = lo + tid; i < hi; i += kPT) s += AV[j * N + i] * V[k * N + i];
-        stash(R, s, j);
-      }
+      slice_multidot<false>(R, AV, N, k + 1, V + k * N, lo, hi, 0);
       cluster_total(cl, R, k + 1);
       set_row(k);
       ++k;
@@ -574,6 +725,16 @@ void batch_solve_persistent(Context* cc, Context* owner, const BatchShapeJob& jo
   a.b1_ptr = (const int64_t*)S.b1_ptr.ptr;
   a.b1_idx = (const int32_t*)S.b1_idx.ptr;
   size_t smem = std::max(slab_plan_smem(cc, 0, 4), slab_plan_smem(cc, 1, 8));
+  // the FP32 sigma's async-copy tiles: four beta strings per thread in
+  // 16-byte copies (beta strings a multiple of 4), kSG staging areas and the
+  // per-thread rings within the shared-memory budget
+  {
+    const int64_t stage = ((int64_t)a.P0.M * a.A.Nb * 4 + (int64_t)a.P0.R * 4 + 15) / 16 * 16;
+    const int64_t pipe = kSG * stage + (int64_t)kPT * 2 * kRing * 16;
+    a.pipe32 = (a.A.Nb % 4 == 0 && pipe + 32 * 1024 <= 227 * 1024) ? 1 : 0;
+    a.stage_bytes = stage;
+    if (a.pipe32) smem = std::max(smem, (size_t)pipe);
+  }
   smem = std::max(smem, eig_dyn_smem(m));
   smem = std::max(smem, (size_t)n2 * sizeof(double));
   smem = (smem + 15) / 16 * 16;

@@ -368,77 +368,20 @@ unsigned slab_threads(int Nb) {
 }
 
 // ------------------------------------------------------------------ emission
-// CTA per (group, segment), a thread per beta string, positions in order.
-// Every element is written (zero when dropped); kept counts go to kept[r].
-// STORAGE: QDKGB_H_FP64 (val), QDKGB_H_SPLIT32 (hi, lo: the batched layout)
-// or kSlabF64F32 (val and its FP32 rounding in hi: the single-instance layout
-// of QDKGB_H_SPLIT32 storage, one FP64-pipe conversion per element instead of
-// the four of the hi/lo split; the full-precision sigma then runs on val).
+// CTA per (group, segment), a thread per beta string, positions in order
+// (k_slab_emit_tab below).  Every element is written (zero when dropped);
+// kept counts go to kept[r].  kSlabF64F32: the single-instance layout of
+// QDKGB_H_SPLIT32 storage (FP64 values and their FP32 rounding, one FP64-pipe
+// conversion per element instead of the four of the hi/lo split; the
+// full-precision sigma then runs on the FP64 values).
 constexpr int kEmitThreads = 256;
 constexpr int kSlabF64F32 = 2;
 
-template <int STORAGE>
-__global__ void __launch_bounds__(kEmitThreads)
-    k_slab_emit(SlabArgs A, Integrals I0, const Integrals* __restrict__ Iinst, int64_t vstride, int64_t nstride,
-                const uint64_t* __restrict__ galpha, const uint64_t* __restrict__ ubeta, long long tbits,
-                const double* __restrict__ diag_raw, double* __restrict__ val, float* __restrict__ hi,
-                float* __restrict__ lo, double* __restrict__ diag, unsigned long long* __restrict__ kept) {
-  const int g = blockIdx.x / kEmitSegments, s = blockIdx.x - g * kEmitSegments;
-  const int p0 = s * A.seglen, p1 = min(A.rowlen, p0 + A.seglen);
-  const int Nb = A.Nb;
-  const uint64_t ra = galpha[g];
-  const int b = blockIdx.y * blockDim.x + threadIdx.x;  // grid.y tiles the beta strings
-  // grid.z: instance of a batch (integrals Iinst[z], slabs vstride apart,
-  // per-determinant arrays nstride apart); a single build passes I0
-  const int inst = blockIdx.z;
-  const Integrals I = Iinst ? Iinst[inst] : I0;
-  diag_raw += inst * nstride;
-  if (STORAGE != QDKGB_H_SPLIT32) val += inst * vstride;
-  if (STORAGE != QDKGB_H_FP64) hi += inst * vstride;
-  if (STORAGE == QDKGB_H_SPLIT32) lo += inst * vstride;
-  if (b < Nb) {
-    const int64_t r = (int64_t)g * Nb + b;
-    const uint64_t rb = ubeta[b];
-    unsigned cnt = 0;
-    for (int p = p0; p < p1; ++p) {
-      const uint32_t d = __ldg(A.gdesc + (int64_t)g * A.rowlen + p);
-      const int h = (int)(d >> 11), k = (int)(d & 2047u);
-      const int bc = k == kListAlphaDouble ? b : __ldg(A.blT + (int64_t)k * Nb + b);
-      const int64_t col = (int64_t)h * Nb + bc;
-      double v;
-      bool keep;
-      if (col == r) {
-        v = diag_raw[r];
-        keep = above_thresh(v, tbits);
-        if (diag) diag[r] = keep ? v : 0.;
-      } else {
-        const uint64_t ka = galpha[h], kb = ubeta[bc];
-        v = (col > r) ? offdiag_element(I, ra, rb, ka, kb) : offdiag_element(I, ka, kb, ra, rb);
-        keep = above_thresh(v, tbits);
-      }
-      if (!keep) v = 0.;
-      cnt += keep;
-      const int64_t q = ((int64_t)g * A.rowlen + p) * Nb + b;
-      if (STORAGE == QDKGB_H_FP64) {
-        val[q] = v;
-      } else if (STORAGE == kSlabF64F32) {
-        val[q] = v;
-        hi[q] = __double2float_rn(v);
-      } else {
-        const float h32 = __double2float_rn(v);
-        hi[q] = h32;
-        lo[q] = __double2float_rn(v - (double)h32);
-      }
-    }
-    if (kept) atomicAdd(kept + r, (unsigned long long)cnt);
-  }
-}
-
 // ------------------------------------------------------------------ emission from spin-pair tables
-// The single-instance build emits the same values as k_slab_emit (bit for
-// bit) with far fewer FP64 operations per element, by evaluating once per
-// string pair what the reference's element formulas compute from one spin's
-// strings alone, in the same summation order:
+// The build (single instance or a batch) emits the reference's values bit for
+// bit with few FP64 operations per element, by evaluating once per string
+// pair what the reference's element formulas compute from one spin's strings
+// alone, in the same summation order:
 //   * a single excitation of one spin (matrix_element_2,
 //     matrix_elements.hpp:169-189) is h = T(v,o) + sum_{p in bra, same spin}
 //     G_red(p,v,o) + sum_{p in bra, other spin} V_red(p,v,o); its first two
@@ -466,10 +409,16 @@ __device__ __forceinline__ double single_partial(const Integrals& I, uint64_t br
 
 // beta pairs: own-group entries (k < n2) oriented by the beta index (the
 // same group); level-1 entries (alpha-single blocks) unoriented: the orbital
-// only in b, the one only in bc, and the sign (equal in both orientations)
-__global__ void k_emit_beta_table(SlabArgs A, Integrals I, const uint64_t* __restrict__ ubeta,
-                                  double* __restrict__ bt, uint32_t* __restrict__ bm) {
+// only in b, the one only in bc, and the sign (equal in both orientations).
+// Batches: instance blockIdx.y with the integrals Iinst[blockIdx.y] and its
+// own table (tot entries apart).
+__global__ void k_emit_beta_table(SlabArgs A, Integrals I0, const Integrals* __restrict__ Iinst,
+                                  const uint64_t* __restrict__ ubeta, double* __restrict__ bt,
+                                  uint32_t* __restrict__ bm) {
   const int64_t tot = (int64_t)(A.n2 + A.n1) * A.Nb;
+  const Integrals I = Iinst ? Iinst[blockIdx.y] : I0;
+  bt += blockIdx.y * tot;
+  bm += blockIdx.y * tot;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < tot; t += (int64_t)gridDim.x * blockDim.x) {
     const int k = (int)(t / A.Nb), b = (int)(t - (int64_t)k * A.Nb);
     const int bc = __ldg(A.blT + t);
@@ -500,9 +449,13 @@ __global__ void k_emit_beta_table(SlabArgs A, Integrals I, const uint64_t* __res
 
 // alpha pairs per row position (alpha-single blocks and alpha doubles),
 // oriented by the group index
-__global__ void k_emit_alpha_table(SlabArgs A, Integrals I, const uint64_t* __restrict__ galpha,
-                                   double* __restrict__ at, uint32_t* __restrict__ am) {
+__global__ void k_emit_alpha_table(SlabArgs A, Integrals I0, const Integrals* __restrict__ Iinst,
+                                   const uint64_t* __restrict__ galpha, double* __restrict__ at,
+                                   uint32_t* __restrict__ am) {
   const int64_t tot = (int64_t)A.G * A.rowlen;
+  const Integrals I = Iinst ? Iinst[blockIdx.y] : I0;
+  at += blockIdx.y * tot;
+  am += blockIdx.y * tot;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < tot; t += (int64_t)gridDim.x * blockDim.x) {
     const int g = (int)(t / A.rowlen);
     const uint32_t d = __ldg(A.gdesc + t);
@@ -527,19 +480,35 @@ __global__ void k_emit_alpha_table(SlabArgs A, Integrals I, const uint64_t* __re
   }
 }
 
+// STORAGE: QDKGB_H_FP64 (val), kSlabF64F32 (val and its FP32 rounding in
+// hi), QDKGB_H_SPLIT32 (the batched layout: hi and lo only).  Batches:
+// instance blockIdx.z with the integrals Iinst[blockIdx.z]; tables, diagonal
+// and slab of an instance tb_stride / ta_stride, nstride and vstride apart.
 template <int STORAGE>
 __global__ void __launch_bounds__(kEmitThreads)
-    k_slab_emit_tab(SlabArgs A, Integrals I, const uint64_t* __restrict__ galpha, const uint64_t* __restrict__ ubeta,
-                    const double* __restrict__ bt, const uint32_t* __restrict__ bm, const double* __restrict__ at,
-                    const uint32_t* __restrict__ am, long long tbits, const double* __restrict__ diag_raw,
-                    double* __restrict__ val, float* __restrict__ hi, double* __restrict__ diag,
-                    unsigned long long* __restrict__ kept) {
+    k_slab_emit_tab(SlabArgs A, Integrals I0, const Integrals* __restrict__ Iinst, const uint64_t* __restrict__ galpha,
+                    const uint64_t* __restrict__ ubeta, const double* __restrict__ bt,
+                    const uint32_t* __restrict__ bm, const double* __restrict__ at, const uint32_t* __restrict__ am,
+                    long long tbits, const double* __restrict__ diag_raw, double* __restrict__ val,
+                    float* __restrict__ hi, float* __restrict__ lo, double* __restrict__ diag,
+                    unsigned long long* __restrict__ kept, int64_t tb_stride, int64_t ta_stride, int64_t nstride,
+                    int64_t vstride) {
   const int g = blockIdx.x / kEmitSegments, s = blockIdx.x - g * kEmitSegments;
   const int p0 = s * A.seglen, p1 = min(A.rowlen, p0 + A.seglen);
   const int Nb = A.Nb;
-  const size_t n = (size_t)I.n;
   const int b = blockIdx.y * blockDim.x + threadIdx.x;
   if (b >= Nb) return;
+  const int64_t inst = blockIdx.z;
+  const Integrals I = Iinst ? Iinst[inst] : I0;
+  const size_t n = (size_t)I.n;
+  bt += inst * tb_stride;
+  bm += inst * tb_stride;
+  at += inst * ta_stride;
+  am += inst * ta_stride;
+  diag_raw += inst * nstride;
+  if (val) val += inst * vstride;
+  if (hi) hi += inst * vstride;
+  if (lo) lo += inst * vstride;
   const int64_t r = (int64_t)g * Nb + b;
   const uint64_t ra = galpha[g], rb = ubeta[b];
   unsigned cnt = 0;
@@ -590,8 +559,14 @@ __global__ void __launch_bounds__(kEmitThreads)
     if (!keep) v = 0.;
     cnt += keep;
     const int64_t q = gp * Nb + b;
-    val[q] = v;
-    if (STORAGE == kSlabF64F32) hi[q] = __double2float_rn(v);
+    if (STORAGE == QDKGB_H_SPLIT32) {
+      const float h = __double2float_rn(v);
+      hi[q] = h;
+      lo[q] = __double2float_rn(v - (double)h);
+    } else {
+      val[q] = v;
+      if (STORAGE == kSlabF64F32) hi[q] = __double2float_rn(v);
+    }
   }
   if (kept) atomicAdd(kept + r, (unsigned long long)cnt);
 }
@@ -987,20 +962,39 @@ void slab_emit_batch(Context* c, int B, const Integrals* d_ints, const double* d
   const int64_t n = F->G * F->Nb;
   long long tbits = -1;
   if (thresh > 0.) std::memcpy(&tbits, &thresh, sizeof(double));
-  const dim3 grid((unsigned)(F->G * kEmitSegments), (unsigned)((F->Nb + kEmitThreads - 1) / kEmitThreads),
-                  (unsigned)B);
+  SlabArgs A = slab_args(c);
   const uint64_t* ga = (const uint64_t*)c->dets.galpha.ptr;
   const uint64_t* ub = (const uint64_t*)c->dets.ubeta.ptr;
   Integrals none{};
-  if (storage == QDKGB_H_FP64)
-    k_slab_emit<QDKGB_H_FP64><<<grid, kEmitThreads, 0, c->stream>>>(slab_args(c), none, d_ints, n * F->rowlen, n, ga,
-                                                                     ub, tbits, diag_raw, val, hi, lo, nullptr,
-                                                                     nullptr);
-  else
-    k_slab_emit<QDKGB_H_SPLIT32><<<grid, kEmitThreads, 0, c->stream>>>(slab_args(c), none, d_ints, n * F->rowlen, n,
-                                                                        ga, ub, tbits, diag_raw, val, hi, lo, nullptr,
-                                                                        nullptr);
+  // every instance's spin-pair tables, then the emission from them
+  const int64_t nbt = (int64_t)(F->n2 + F->n1) * F->Nb, nat = F->G * F->rowlen;
+  ScopedBuffers<4> tb(c);
+  double* bt = dev_array<double>(c, tb.b[0], (size_t)B * nbt);
+  uint32_t* bm = dev_array<uint32_t>(c, tb.b[1], (size_t)B * nbt);
+  double* at = dev_array<double>(c, tb.b[2], (size_t)B * nat);
+  uint32_t* am = dev_array<uint32_t>(c, tb.b[3], (size_t)B * nat);
+  const dim3 gb((unsigned)std::max<int64_t>(1, std::min<int64_t>((nbt + 255) / 256, (int64_t)c->sm_count * 8 / B)),
+                (unsigned)B);
+  k_emit_beta_table<<<gb, 256, 0, c->stream>>>(A, none, d_ints, ub, bt, bm);
   QDKGB_CHECK_LAUNCH();
+  const dim3 ga2((unsigned)std::max<int64_t>(1, std::min<int64_t>((nat + 255) / 256, (int64_t)c->sm_count * 8 / B)),
+                 (unsigned)B);
+  k_emit_alpha_table<<<ga2, 256, 0, c->stream>>>(A, none, d_ints, ga, at, am);
+  QDKGB_CHECK_LAUNCH();
+  const dim3 grid((unsigned)(F->G * kEmitSegments), (unsigned)((F->Nb + kEmitThreads - 1) / kEmitThreads),
+                  (unsigned)B);
+  const unsigned thr = (unsigned)std::min<int64_t>(kEmitThreads, (F->Nb + 31) / 32 * 32);
+  const int64_t vstride = n * F->rowlen;
+  if (storage == QDKGB_H_FP64)
+    k_slab_emit_tab<QDKGB_H_FP64><<<grid, thr, 0, c->stream>>>(A, none, d_ints, ga, ub, bt, bm, at, am, tbits,
+                                                                diag_raw, val, nullptr, nullptr, nullptr, nullptr,
+                                                                nbt, nat, n, vstride);
+  else
+    k_slab_emit_tab<QDKGB_H_SPLIT32><<<grid, thr, 0, c->stream>>>(A, none, d_ints, ga, ub, bt, bm, at, am, tbits,
+                                                                   diag_raw, nullptr, hi, lo, nullptr, nullptr, nbt,
+                                                                   nat, n, vstride);
+  QDKGB_CHECK_LAUNCH();
+  QDKGB_CUDA(cudaStreamSynchronize(c->stream));  // the tables are freed on return
 }
 
 // Sizes the partial-sum scratch for B instances in every mode, so that no
@@ -1074,17 +1068,17 @@ void build_hamiltonian_struct(Context* c, double thresh, int storage) {
   double* at = dev_array<double>(c, F->tab_a, nat);
   uint32_t* am = dev_array<uint32_t>(c, F->tab_am, nat);
   k_emit_beta_table<<<(unsigned)std::min<int64_t>((nbt + 255) / 256, (int64_t)c->sm_count * 8), 256, 0, c->stream>>>(
-      A, I, ub, bt, bm);
+      A, I, nullptr, ub, bt, bm);
   QDKGB_CHECK_LAUNCH();
   k_emit_alpha_table<<<(unsigned)std::min<int64_t>((nat + 255) / 256, (int64_t)c->sm_count * 8), 256, 0,
-                       c->stream>>>(A, I, ga, at, am);
+                       c->stream>>>(A, I, nullptr, ga, at, am);
   QDKGB_CHECK_LAUNCH();
   if (storage == QDKGB_H_FP64)
-    k_slab_emit_tab<QDKGB_H_FP64><<<grid, thr, 0, c->stream>>>(A, I, ga, ub, bt, bm, at, am, tbits, diag_raw, val,
-                                                                nullptr, diag, kc);
+    k_slab_emit_tab<QDKGB_H_FP64><<<grid, thr, 0, c->stream>>>(A, I, nullptr, ga, ub, bt, bm, at, am, tbits, diag_raw,
+                                                                val, nullptr, nullptr, diag, kc, 0, 0, 0, 0);
   else
-    k_slab_emit_tab<kSlabF64F32><<<grid, thr, 0, c->stream>>>(A, I, ga, ub, bt, bm, at, am, tbits, diag_raw, val,
-                                                               hi, diag, kc);
+    k_slab_emit_tab<kSlabF64F32><<<grid, thr, 0, c->stream>>>(A, I, nullptr, ga, ub, bt, bm, at, am, tbits, diag_raw,
+                                                               val, hi, nullptr, diag, kc, 0, 0, 0, 0);
   QDKGB_CHECK_LAUNCH();
   int64_t* rowptr = dev_array<int64_t>(c, H.rowptr, n + 1);
   exclusive_scan_i64(c, kept, rowptr, n, H.scan_tmp);
