@@ -406,8 +406,8 @@ typedef struct {
   double min_abs_denominator; /* preconditioner clamp (1e-12) */
   int use_graph;              /* lockstep path: replay the inner iteration from a CUDA graph (1) */
   int64_t max_slab_bytes;     /* stored-matrix bytes per sub-batch (96 GiB) */
-  int persistent;             /* 1 (default): one persistent cluster launch per shape solves every
-                                 instance; 0: the lockstep launch sequence over all instances */
+  int persistent;             /* 0 (default): the lockstep launch sequence over all instances;
+                                 1: one persistent cluster launch per shape solves every instance */
   int cluster;                /* persistent: CTAs per instance, 1, 2, 4 or 8; 0 (default): measured
                                  per shape on first use and kept on the context (qdkgb_batch_plan) */
 } qdkgb_batch_settings;

@@ -761,7 +761,7 @@ int qdkgb_batch_default_settings(qdkgb_batch_settings* s) {
   s->min_abs_denominator = 1e-12;
   s->use_graph = 1;
   s->max_slab_bytes = (int64_t)96 << 30;
-  s->persistent = 1;
+  s->persistent = 0;
   s->cluster = 0;
   return QDKGB_OK;
 }

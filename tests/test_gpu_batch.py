@@ -2,8 +2,9 @@
 energies (mixed form within 1e-8 Eh of the oracle's FP64 Davidson, FP64 form
 within 1e-10) and spin-summed 1-RDMs (1e-6 absolute: the vectors agree to the
 residual tolerance over the gap), for instances of uneven size and shape,
-through both solvers: the persistent cluster kernel (default; every cluster
-size agrees with the lockstep path) and the lockstep launch sequence."""
+through both solvers: the lockstep launch sequence (default) and the
+persistent cluster kernel (every cluster size agrees with the lockstep
+path)."""
 import numpy as np
 import pytest
 
@@ -130,9 +131,9 @@ def test_persistent_autotuner_records_its_choice(pkg, capi, oracle):
     inst = _instances(pkg, [(10, 5, 5)] * 3 + [(6, 3, 3)] * 2, 700)
     with capi.Context(0) as c:
         assert capi.batch_plan(c) == []
-        E, _, _, _ = capi.casci_batch(c, inst, want_rdm1=False)
+        E, _, _, _ = capi.casci_batch(c, inst, want_rdm1=False, persistent=1)
         plan = {p["shape"]: p for p in capi.batch_plan(c)}
-        E2, _, _, _ = capi.casci_batch(c, inst, want_rdm1=False)
+        E2, _, _, _ = capi.casci_batch(c, inst, want_rdm1=False, persistent=1)
         assert len(capi.batch_plan(c)) == len(plan)
     p10 = plan[(10, 5, 5)]
     assert len(p10["candidates"]) >= 2 and p10["cluster"] in [q for q, _ in p10["candidates"]]
