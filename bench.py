@@ -321,6 +321,9 @@ def run_ours(args):
         vec = 4 if nbs % 4 == 0 else (2 if nbs % 2 == 0 else 1)
         kern32 = ("k_slab_sigma32v<%d> (FP32 sigma, slab layout: values only, %d beta strings per thread)"
                   % (vec, vec) if vec > 1 else "k_slab_sigma<0> (FP32 sigma, slab layout: values only)")
+        if ctx.sigma_plan(capi.PREC_MIXED, with_kernel=True)[2] == "tma":
+            kern32 = ("k_slab_sigma32t (FP32 sigma, slab layout: values only; rows streamed into shared memory "
+                      "by TMA bulk copies, 4 beta strings per thread)")
     else:
         bytes32 = nnz * 8 + (N + 1) * 8 + N * 4 + N * 4
         kern32 = "k_spmv_csr<float> (FP32 sigma, CSR)"
@@ -378,7 +381,8 @@ def run_ours(args):
                      "traffic": traffic, "algorithmic_bytes": bytes32, "launch_ms": t_spmv32 * 1e3},
         "spmv_fp64": {"kernel": kern64, "achieved_gbs": achieved64, "frac": achieved64 / peak,
                       "launch_ms": t_spmv64 * 1e3, "algorithmic_bytes": bytes64},
-        "sigma_autotune": {"fp32": dict(zip(("segments", "candidates_ms"), ctx.sigma_plan(capi.PREC_MIXED))),
+        "sigma_autotune": {"fp32": dict(zip(("segments", "candidates_ms", "kernel", "tma_candidates_ms"),
+                                            ctx.sigma_plan(capi.PREC_MIXED, with_kernel=True))),
                            "fp64": dict(zip(("segments", "candidates_ms"), ctx.sigma_plan(capi.PREC_FP64)))},
         "hbuild_s": float(np.mean(hbs)), "davidson_s": float(np.mean(dvs)),
         "davidson": {k: infos[-1][k] for k in ("iterations", "spmv_fp64", "spmv_fp32", "restarts", "residual_norm")},

@@ -160,9 +160,13 @@ int qdkgb_build_operator(qdkgb_context* ctx, double thresh, int storage, int max
  * candidate count, one untimed and three timed sigmas each, and keeps the
  * fastest.  *segments receives the count in use (0: no complete-space
  * sigma); with ncand (in: capacity, out: candidates tried) the candidates'
- * counts and mean milliseconds, empty before the first sigma. */
+ * counts and mean milliseconds, empty before the first sigma.  For the FP32
+ * sigma the tuner also times the TMA-fed kernel (slab rows streamed into
+ * shared memory by bulk copies) on every candidate: *kernel (may be NULL)
+ * receives the kernel in use (0 register-fed, 1 TMA-fed), cand_ms_tma (may
+ * be NULL) its milliseconds per candidate (NaN where it was not timed). */
 int qdkgb_sigma_plan(qdkgb_context* ctx, int precision, int* segments, int* ncand, int* cand_segments,
-                     double* cand_ms);
+                     double* cand_ms, int* kernel, double* cand_ms_tma);
 
 /* Copies the device CSR to host buffers (rowptr: ndets+1, colind/values: nnz).
  * For QDKGB_H_SPLIT32 storage, values receive (double)hi + (double)lo.

@@ -239,6 +239,13 @@ __global__ void k_b_hsrow(const double* __restrict__ coef, int KM, double* __res
 
 __global__ void k_b_kinc(int* kdev) { *kdev += 1; }
 
+// second Gram-Schmidt pass where the first removed more than half of |t|^2
+__global__ void k_b_need2(int B, const int* __restrict__ act, const double* __restrict__ nrm2,
+                          const double* __restrict__ w0, int* __restrict__ need2) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b < B) need2[b] = act[b] && !(nrm2[(int64_t)b * 2] > 0.5 * w0[b]);
+}
+
 // after the Ritz step: an instance waits for the next cycle when its
 // estimated residual fell by `ratio` since its last full-precision one, or
 // its subspace is full; nact = active instances (for the host)
@@ -628,7 +635,8 @@ void casci_batch(Context* ctx, int ninst, const qdkgb_cas_instance* inst, const 
                    &bt = bs.b[17], &bt32 = bs.b[18], &bs32 = bs.b[19], &bxh = bs.b[20], &bxl = bs.b[21],
                    &by = bs.b[22], &bev = bs.b[23], &bth = bs.b[24], &bco = bs.b[25], &bpart = bs.b[26],
                    &bsc = bs.b[27], &bsc2 = bs.b[28], &bflip = bs.b[29], &bint = bs.b[30], &bidx = bs.b[31],
-                   &blt = bs.b[32], &ben = bs.b[33], &bres = bs.b[34], &bxp = bs.b[37];
+                   &blt = bs.b[32], &ben = bs.b[33], &bres = bs.b[34], &bxp = bs.b[37], &bw0 = bs.b[38],
+                   &bn2 = bs.b[39];
       const int64_t astride = (int64_t)m * N;
       double* Vb = dev_array<double>(cc, bV, (size_t)B * astride);
       double* AVb = dev_array<double>(cc, bAV, (size_t)B * astride);
@@ -661,6 +669,8 @@ void casci_batch(Context* ctx, int ninst, const qdkgb_cas_instance* inst, const 
       int* kdev = ints + 4 * B;
       int* nact = ints + 4 * B + 1;
       int64_t* idx = dev_array<int64_t>(cc, bidx, (size_t)B);
+      double* w0 = dev_array<double>(cc, bw0, (size_t)B);  // |t|^2 before the first Gram-Schmidt pass
+      int* need2 = dev_array<int>(cc, bn2, (size_t)B);     // instances that take the second pass
       QDKGB_CUDA(cudaMemsetAsync(ints, 0, ((size_t)5 * B + 8) * sizeof(int), s0));
       QDKGB_CUDA(cudaMemsetAsync(Hs, 0, (size_t)B * m * m * 8, s0));
       // guess and its spin-flip sector (kept by the FP64 iteration; FP32
@@ -761,18 +771,37 @@ void casci_batch(Context* ctx, int ninst, const qdkgb_cas_instance* inst, const 
           k_b_flip<<<gv, kBT, 0, s0>>>(t, S.nbeta, flip, act);
           QDKGB_CHECK_LAUNCH();
         }
-        for (int pass = 0; pass < 2; ++pass) {  // CGS2 against V[0..k)
-          k_b_multidot<<<gc, kBT, 0, s0>>>(Vb, astride, ld, kdev, 0, t, N, 0, N, nchunk, partial, KM, act);
+        // Gram-Schmidt against V[0..k): the FP64 form always makes two passes
+        // (the reference's CGS2); the mixed form makes the second only for the
+        // instances whose first pass removed more than half of |t|^2 (the
+        // Daniel-Gragg-Kaufman-Stewart test, as in the single solve)
+        auto gs_pass = [&](const int* mask) {
+          k_b_multidot<<<gc, kBT, 0, s0>>>(Vb, astride, ld, kdev, 0, t, N, 0, N, nchunk, partial, KM, mask);
           QDKGB_CHECK_LAUNCH();
-          k_b_reduce<<<B, 64, 0, s0>>>(partial, nchunk, KM, kdev, 0, coef, KM, act);
+          k_b_reduce<<<B, 64, 0, s0>>>(partial, nchunk, KM, kdev, 0, coef, KM, mask);
           QDKGB_CHECK_LAUNCH();
-          k_b_gemv<<<gv, kBT, 0, s0>>>(Vb, astride, ld, kdev, 0, coef, KM, -1., t, t, N, N, act);
+          k_b_gemv<<<gv, kBT, 0, s0>>>(Vb, astride, ld, kdev, 0, coef, KM, -1., t, t, N, N, mask);
           QDKGB_CHECK_LAUNCH();
+        };
+        auto norm2 = [&](double* out, int ostride, const int* mask) {
+          k_b_multidot<<<gc, kBT, 0, s0>>>(t, N, N, nullptr, 1, t, N, 0, N, nchunk, partial, KM, mask);
+          QDKGB_CHECK_LAUNCH();
+          k_b_reduce<<<B, 32, 0, s0>>>(partial, nchunk, KM, nullptr, 1, out, ostride, mask);
+          QDKGB_CHECK_LAUNCH();
+        };
+        if (mixed) {
+          norm2(w0, 1, act);
+          gs_pass(act);
+          norm2(sc, 2, act);
+          k_b_need2<<<(B + 255) / 256, 256, 0, s0>>>(B, act, sc, w0, need2);
+          QDKGB_CHECK_LAUNCH();
+          gs_pass(need2);
+          norm2(sc, 2, need2);
+        } else {
+          gs_pass(act);
+          gs_pass(act);
+          norm2(sc, 2, act);
         }
-        k_b_multidot<<<gc, kBT, 0, s0>>>(t, N, N, nullptr, 1, t, N, 0, N, nchunk, partial, KM, act);
-        QDKGB_CHECK_LAUNCH();
-        k_b_reduce<<<B, 32, 0, s0>>>(partial, nchunk, KM, nullptr, 1, sc, 2, act);
-        QDKGB_CHECK_LAUNCH();
         k_b_store_dir<<<gv, kBT, 0, s0>>>(t, sc, Vb, astride, ld, kdev, t32, N, act, nsig);
         QDKGB_CHECK_LAUNCH();
         if (mixed) {

@@ -581,7 +581,22 @@ __global__ void __launch_bounds__(kPT) k_bp_solve(BPArgs a) {
         flip_slice(t, a.nstr, flip, lo, hi);
         cl.sync();
       }
-      for (int pass = 0; pass < 2; ++pass) {  // CGS2 against V[0..k)
+      // Gram-Schmidt against V[0..k): two passes in the FP64 form; in the
+      // mixed form the second only when the first removed more than half of
+      // |t|^2 (as the lockstep path)
+      auto tnorm2 = [&]() -> double {
+        double q2 = 0.;
+        for (int64_t i = lo + tid; i < hi; i += kPT) {
+          const double q = __ldcg(t + i);
+          q2 += q * q;
+        }
+        stash(R, q2, 0);
+        cluster_total(cl, R, 1);
+        return R.t[0];
+      };
+      const double w0 = a.mixed ? tnorm2() : 0.;
+      double nn = -1.;
+      for (int pass = 0; pass < 2; ++pass) {
         slice_multidot<true>(R, V, N, k, t, lo, hi, 0);
         cluster_total(cl, R, k);
         for (int64_t i = lo + tid; i < hi; i += kPT) {
@@ -590,15 +605,13 @@ __global__ void __launch_bounds__(kPT) k_bp_solve(BPArgs a) {
           for (int j = 0; j < k; ++j) acc += V[j * N + i] * R.t[j];
           __stcg(t + i, __ldcg(t + i) - acc);
         }
+        if (pass == 0 && a.mixed) {
+          nn = tnorm2();
+          if (nn > 0.5 * w0) break;
+          nn = -1.;
+        }
       }
-      double nn = 0.;
-      for (int64_t i = lo + tid; i < hi; i += kPT) {
-        const double q = __ldcg(t + i);
-        nn += q * q;
-      }
-      stash(R, nn, 0);
-      cluster_total(cl, R, 1);
-      nn = R.t[0];
+      if (nn < 0.) nn = tnorm2();
       if (!(nn > 1e-28)) {  // no new direction: wait for the cycle's end
         act = 0;
         return;

@@ -20,6 +20,8 @@
 // defines are produced from the slab on request (export), or in place of it
 // when most elements are dropped.
 #include <algorithm>
+#include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <type_traits>
 #include <vector>
@@ -70,6 +72,10 @@ struct FciStruct {
   std::vector<PlanHost> cand[2];
   bool tuned[2] = {false, false};
   std::vector<std::pair<int, double>> tune_ms[2];
+  // FP32 sigma kernel in use: 0 register-fed (k_slab_sigma32v), 1 TMA-fed
+  // (k_slab_sigma32t); the autotuner times both per candidate plan
+  int kernel32 = 0;
+  std::vector<std::pair<int, double>> tune_tma_ms;
   // spin-pair tables of the table-driven emission (rebuilt with every build)
   DeviceBuffer tab_b, tab_bm, tab_a, tab_am;
 };
@@ -803,6 +809,219 @@ __global__ void __launch_bounds__(kSlabVecThreads)
   }
 }
 
+// ------------------------------------------------------------------ FP32 sigma, TMA-fed
+// The vectorised FP32 sigma (four beta strings per thread) with the slab
+// values brought in by the Tensor Memory Accelerator: a producer warp issues
+// one 1D bulk copy (cp.async.bulk, global -> shared, completion counted on an
+// mbarrier) per position row of the tile (N_b contiguous FP32 values) into a
+// ring of kTmaStages stages of up to kTmaRows rows, and eight consumer warps
+// read the values from shared memory, so a CTA keeps up to 12 rows in flight
+// without registers held for them.  Stages follow the consumption order of
+// k_slab_sigma32v<4> (own block; level-1 entry by entry over the segment's
+// alpha-single blocks; alpha doubles) and every row is summed in that order:
+// the results are that kernel's bit for bit.  Every wait is bounded
+// (kTmaSpin tries): on a timeout the CTA records it in g_sigma_fault, writes
+// NaN to its rows, waits (bounded) for its own copies still in flight and
+// returns.
+constexpr int kTmaStages = 3;
+constexpr int kTmaRows = 4;
+constexpr int kTmaConsumers = 256;  // eight consumer warps; warp 8 issues the copies
+constexpr uint32_t kTmaSpin = 1u << 24;
+
+__device__ unsigned int g_sigma_fault;  // set by a CTA whose wait timed out
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* b) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(b)) : "memory");
+}
+// true once the phase of the given parity has completed; false after kTmaSpin tries
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity) {
+  for (uint32_t it = 0; it < kTmaSpin; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(smem_u32(b)), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* b) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(b))
+               : "memory");
+}
+
+// stage i of a tile: kind 0 own block (rows k0 .. k0+cnt-1), 1 alpha-single
+// blocks e0 .. e0+cnt-1 at level-1 entry k, 2 alpha doubles j0 .. j0+cnt-1
+struct TmaStage {
+  int kind, k, first, cnt;
+};
+__device__ __forceinline__ TmaStage tma_stage(int i, int n_os, int n_sk, int n_ss, int n2, int n1b, int nd) {
+  TmaStage t;
+  if (i < n_os) {
+    t.kind = 0;
+    t.k = 0;
+    t.first = i * kTmaRows;
+    t.cnt = min(kTmaRows, n2 - t.first);
+  } else if (i < n_os + n_ss) {
+    const int u = i - n_os;
+    t.kind = 1;
+    t.k = u / n_sk;
+    t.first = (u - t.k * n_sk) * kTmaRows;
+    t.cnt = min(kTmaRows, n1b - t.first);
+  } else {
+    t.kind = 2;
+    t.k = 0;
+    t.first = (i - n_os - n_ss) * kTmaRows;
+    t.cnt = min(kTmaRows, nd - t.first);
+  }
+  return t;
+}
+
+__global__ void __launch_bounds__(kTmaConsumers + 32)
+    k_slab_sigma32t(SlabArgs A, PlanArgs P, const float* __restrict__ vals, const float* __restrict__ xv,
+                    float* __restrict__ yv, int64_t part_stride, int64_t vstride, const int* __restrict__ active) {
+  __shared__ __align__(8) uint64_t full[kTmaStages], empty[kTmaStages];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int Nb = A.Nb;
+  const int g = blockIdx.x / P.S, s = blockIdx.x - g * P.S;
+  const int inst = blockIdx.y;
+  if (active && !active[inst]) return;
+  const int64_t n = (int64_t)A.G * Nb;
+  vals += inst * vstride;
+  xv += inst * n;
+  yv += inst * n;
+  float* xs = reinterpret_cast<float*>(smem_raw);
+  int32_t* rec = reinterpret_cast<int32_t*>(xs + (size_t)P.M * Nb);
+  float* ring = reinterpret_cast<float*>(smem_raw + (((size_t)P.M * Nb * 4 + (size_t)P.R * 4 + 15) / 16 * 16));
+  const int tid = threadIdx.x;
+  const int32_t* rg = P.rec + ((int64_t)g * P.S + s) * P.R;
+  for (int i = tid; i < P.R; i += blockDim.x) rec[i] = __ldg(rg + i);
+  if (tid == 0) {
+    for (int i = 0; i < kTmaStages; ++i) {
+      mbar_init(&full[i], 1);
+      mbar_init(&empty[i], kTmaConsumers / 32);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  __syncthreads();
+  const int has0 = rec[0], off0 = rec[1], sb0 = rec[2], n1b = rec[3];
+  const int32_t* e1 = rec + 4;
+  const int nd = rec[4 + 2 * n1b];
+  const int32_t* e2 = rec + 6 + 2 * n1b;
+  const int n_os = has0 ? (A.n2 + kTmaRows - 1) / kTmaRows : 0;
+  const int n_sk = (n1b + kTmaRows - 1) / kTmaRows;
+  const int n_ss = A.n1 * n_sk;
+  const int n_st = n_os + n_ss + (nd + kTmaRows - 1) / kTmaRows;
+  const float* vg = vals + (int64_t)g * A.rowlen * Nb;
+  const uint32_t row_bytes = (uint32_t)Nb * 4u;
+  if (tid >= kTmaConsumers) {
+    // producer: one elected thread issues the copies
+    if (tid != kTmaConsumers) return;
+    bool ok = true;
+    int issued = 0;
+    for (int i = 0; i < n_st; ++i) {
+      const int slot = i % kTmaStages, round = i / kTmaStages;
+      if (round > 0 && !mbar_wait(&empty[slot], (uint32_t)((round - 1) & 1))) {
+        ok = false;
+        break;
+      }
+      const TmaStage t = tma_stage(i, n_os, n_sk, n_ss, A.n2, n1b, nd);
+      float* dst = ring + (size_t)slot * kTmaRows * Nb;
+      mbar_expect_tx(&full[slot], row_bytes * (uint32_t)t.cnt);
+      for (int r = 0; r < t.cnt; ++r) {
+        int64_t off;
+        if (t.kind == 0)
+          off = off0 + (int64_t)(t.first + r) * Nb;
+        else if (t.kind == 1)
+          off = e1[2 * (t.first + r)] + (int64_t)t.k * Nb;
+        else
+          off = e2[2 * (t.first + r)];
+        bulk_g2s(dst + (size_t)r * Nb, vg + off, row_bytes, &full[slot]);
+      }
+      ++issued;
+    }
+    if (!ok) {
+      atomicOr(&g_sigma_fault, 1u);
+      // the copies still in flight land before this thread (and the CTA) ends
+      for (int i = issued - 1; i >= 0 && i >= issued - kTmaStages; --i)
+        (void)mbar_wait(&full[i % kTmaStages], (uint32_t)((i / kTmaStages) & 1));
+    }
+    return;
+  }
+  // consumers: the staged x slices, then the stages in order
+  const int32_t* sh = P.segh + ((int64_t)g * P.S + s) * P.M;
+  for (int j = 0; j < P.M; ++j) {
+    const int h = __ldg(sh + j);
+    if (h < 0) continue;
+    for (int i = tid; i < Nb; i += kTmaConsumers) cp_async4(xs + (size_t)j * Nb + i, xv + (int64_t)h * Nb + i);
+  }
+  cp_async_wait_all();
+  asm volatile("bar.sync 1, %0;\n" ::"r"(kTmaConsumers) : "memory");
+  const int nvec = Nb / 4;
+  const bool live = tid < nvec;
+  const int b0 = tid * 4;
+  float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+  bool ok = true;
+  for (int i = 0; i < n_st; ++i) {
+    const int slot = i % kTmaStages;
+    if (!mbar_wait(&full[slot], (uint32_t)((i / kTmaStages) & 1))) {
+      ok = false;
+      break;
+    }
+    if (live) {
+      const TmaStage t = tma_stage(i, n_os, n_sk, n_ss, A.n2, n1b, nd);
+      const float* src = ring + (size_t)slot * kTmaRows * Nb + b0;
+      if (t.kind == 0) {
+        for (int r = 0; r < t.cnt; ++r) {
+          const float4 v = *reinterpret_cast<const float4*>(src + (size_t)r * Nb);
+          const int4 l = __ldg(reinterpret_cast<const int4*>(A.blT + (int64_t)(t.first + r) * Nb + b0));
+          a0 = fmaf(v.x, xs[sb0 + l.x], a0);
+          a1 = fmaf(v.y, xs[sb0 + l.y], a1);
+          a2 = fmaf(v.z, xs[sb0 + l.z], a2);
+          a3 = fmaf(v.w, xs[sb0 + l.w], a3);
+        }
+      } else if (t.kind == 1) {
+        const int4 l = __ldg(reinterpret_cast<const int4*>(A.blT + (int64_t)(A.n2 + t.k) * Nb + b0));
+        for (int r = 0; r < t.cnt; ++r) {
+          const float4 v = *reinterpret_cast<const float4*>(src + (size_t)r * Nb);
+          const int sb = e1[2 * (t.first + r) + 1];
+          a0 = fmaf(v.x, xs[sb + l.x], a0);
+          a1 = fmaf(v.y, xs[sb + l.y], a1);
+          a2 = fmaf(v.z, xs[sb + l.z], a2);
+          a3 = fmaf(v.w, xs[sb + l.w], a3);
+        }
+      } else {
+        for (int r = 0; r < t.cnt; ++r) {
+          const float4 v = *reinterpret_cast<const float4*>(src + (size_t)r * Nb);
+          const float4 x = __ldg(reinterpret_cast<const float4*>(xv + e2[2 * (t.first + r) + 1] + b0));
+          a0 = fmaf(v.x, x.x, a0);
+          a1 = fmaf(v.y, x.y, a1);
+          a2 = fmaf(v.z, x.z, a2);
+          a3 = fmaf(v.w, x.w, a3);
+        }
+      }
+    }
+    __syncwarp();
+    if ((tid & 31) == 0) mbar_arrive(&empty[slot]);
+  }
+  if (!ok) {
+    atomicOr(&g_sigma_fault, 1u);
+    a0 = a1 = a2 = a3 = __int_as_float(0x7fc00000);
+  }
+  if (live)
+    *reinterpret_cast<float4*>(yv + s * part_stride + (int64_t)g * Nb + b0) = make_float4(a0, a1, a2, a3);
+}
+
 template <typename T>
 __global__ void k_slab_combine(int64_t n, int S, const T* __restrict__ part, T* __restrict__ y) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -815,6 +1034,15 @@ __global__ void k_slab_combine(int64_t n, int S, const T* __restrict__ part, T* 
 template <int MODE>
 void slab_sigma_launch(Context* c, int B, const int* active, const void* vals, const float* vlo, const void* x,
                        const float* xlo, void* y);
+
+// the TMA-fed FP32 sigma needs whole 16-byte rows (N_b a multiple of 4, the
+// slab and x 16-byte aligned) and at most kTmaConsumers threads' worth of
+// beta strings per group
+bool sigma32t_eligible(Context* c, const void* vals, const void* x) {
+  FciStruct* F = c->fci;
+  return F->Nb % 4 == 0 && F->Nb / 4 <= kTmaConsumers && ((uintptr_t)vals & 15) == 0 && ((uintptr_t)x & 15) == 0 &&
+         ((uintptr_t)F->blT.ptr & 15) == 0;
+}
 
 // Times every candidate segment count of the plan on this call's inputs
 // (one untimed and three timed sigmas each, CUDA events on the context's
@@ -837,11 +1065,7 @@ void slab_sigma_tune(Context* c, const void* vals, const float* vlo, const void*
     QDKGB_CUDA(cudaMemcpyAsync(r, ph.rec.data(), ph.rec.size() * 4, cudaMemcpyHostToDevice, c->stream));
     QDKGB_CUDA(cudaMemcpyAsync(g, ph.segh.data(), ph.segh.size() * 4, cudaMemcpyHostToDevice, c->stream));
   };
-  int best = 0;
-  double best_ms = 1e300;
-  F->tune_ms[pl].clear();
-  for (size_t i = 0; i < F->cand[pl].size(); ++i) {
-    load(F->cand[pl][i]);
+  auto time3 = [&]() {
     slab_sigma_launch<MODE>(c, 1, nullptr, vals, vlo, x, xlo, y);
     QDKGB_CUDA(cudaEventRecord(e0, c->stream));
     for (int r = 0; r < 3; ++r) slab_sigma_launch<MODE>(c, 1, nullptr, vals, vlo, x, xlo, y);
@@ -849,13 +1073,41 @@ void slab_sigma_tune(Context* c, const void* vals, const float* vlo, const void*
     QDKGB_CUDA(cudaEventSynchronize(e1));
     float ms = 0.f;
     QDKGB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-    F->tune_ms[pl].push_back({F->cand[pl][i].S, ms / 3.0});
-    if (ms / 3.0 < best_ms) {
-      best_ms = ms / 3.0;
+    return ms / 3.0;
+  };
+  // QDKGB_SIGMA32_KERNEL=register / tma restricts the FP32 choice to one kernel
+  const char* force = std::getenv("QDKGB_SIGMA32_KERNEL");
+  const bool only_reg = force && std::strcmp(force, "register") == 0;
+  const bool only_tma = force && std::strcmp(force, "tma") == 0;
+  const bool tma = MODE == 0 && !only_reg && sigma32t_eligible(c, vals, x);
+  const bool reg = !(tma && only_tma);
+  int best = 0, best_kernel = 0;
+  double best_ms = 1e300;
+  F->tune_ms[pl].clear();
+  if (MODE == 0) F->tune_tma_ms.clear();
+  for (size_t i = 0; i < F->cand[pl].size(); ++i) {
+    load(F->cand[pl][i]);
+    if (MODE == 0) F->kernel32 = 0;
+    const double ms = reg ? time3() : std::nan("");
+    F->tune_ms[pl].push_back({F->cand[pl][i].S, ms});
+    if (reg && ms < best_ms) {
+      best_ms = ms;
       best = (int)i;
+      best_kernel = 0;
+    }
+    if (tma) {
+      F->kernel32 = 1;
+      const double mt = time3();
+      F->tune_tma_ms.push_back({F->cand[pl][i].S, mt});
+      if (mt < best_ms) {
+        best_ms = mt;
+        best = (int)i;
+        best_kernel = 1;
+      }
     }
   }
   load(F->cand[pl][best]);
+  if (MODE == 0) F->kernel32 = best_kernel;
   QDKGB_CUDA(cudaStreamSynchronize(c->stream));
   QDKGB_CUDA(cudaEventDestroy(e0));
   QDKGB_CUDA(cudaEventDestroy(e1));
@@ -901,7 +1153,15 @@ void slab_sigma_launch(Context* c, int B, const int* active, const void* vals, c
                    ((uintptr_t)F->blT.ptr & 15) == 0)
                       ? (Nb % 4 == 0 ? 4 : (Nb % 2 == 0 ? 2 : 1))
                       : 1;
-  if (vec > 1) {
+  if (MODE == 0 && F->kernel32 == 1 && B == 1 && sigma32t_eligible(c, vals, x)) {
+    // TMA-fed FP32 sigma: eight consumer warps and one producer warp per CTA
+    const size_t tsm = ((size_t)PL.M * Nb * 4 + (size_t)PL.R * 4 + 15) / 16 * 16 + (size_t)kTmaStages * kTmaRows * Nb * 4;
+    set_max_dynamic_smem((const void*)k_slab_sigma32t, (int)tsm);
+    const dim3 grid((unsigned)(F->G * PL.S), (unsigned)B);
+    k_slab_sigma32t<<<grid, kTmaConsumers + 32, tsm, c->stream>>>(slab_args(c), P, (const float*)vals,
+                                                                   (const float*)x, (float*)out, (int64_t)B * n,
+                                                                   vstride, active);
+  } else if (vec > 1) {
     // vectorised FP32 sigma: VEC beta strings per thread
     const int nvec = Nb / vec;
     const unsigned thr = (unsigned)std::min(kSlabVecThreads, (nvec + 31) / 32 * 32);
@@ -931,9 +1191,13 @@ void slab_sigma_launch(Context* c, int B, const int* active, const void* vals, c
 
 // the sigma plan of a precision (0: FP32, 1: FP64): segments in use and the
 // autotuner's record (S, ms) per candidate (empty before the first sigma)
-int struct_sigma_plan(Context* c, int pl, std::vector<std::pair<int, double>>* record) {
+int struct_sigma_plan(Context* c, int pl, std::vector<std::pair<int, double>>* record, int* kernel,
+                      std::vector<std::pair<int, double>>* record_tma) {
+  if (kernel) *kernel = 0;
   if (!c->fci || pl < 0 || pl > 1) return 0;
   if (record) *record = c->fci->tune_ms[pl];
+  if (kernel && pl == 0) *kernel = c->fci->kernel32;
+  if (record_tma && pl == 0) *record_tma = c->fci->tune_tma_ms;
   return c->fci->plan[pl].S;
 }
 
