@@ -1075,12 +1075,20 @@ void slab_sigma_tune(Context* c, const void* vals, const float* vlo, const void*
     QDKGB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
     return ms / 3.0;
   };
-  // QDKGB_SIGMA32_KERNEL=register / tma restricts the FP32 choice to one kernel
-  const char* force = std::getenv("QDKGB_SIGMA32_KERNEL");
-  const bool only_reg = force && std::strcmp(force, "register") == 0;
-  const bool only_tma = force && std::strcmp(force, "tma") == 0;
-  const bool tma = MODE == 0 && !only_reg && sigma32t_eligible(c, vals, x);
-  const bool reg = !(tma && only_tma);
+  // QDKGB_SIGMA32_KERNEL=register / tma: no timing, the planner's default
+  // plan with that FP32 kernel (the two kernels then sum every row alike)
+  const char* force = MODE == 0 ? std::getenv("QDKGB_SIGMA32_KERNEL") : nullptr;
+  if (force && (std::strcmp(force, "register") == 0 || std::strcmp(force, "tma") == 0)) {
+    F->kernel32 = (std::strcmp(force, "tma") == 0 && sigma32t_eligible(c, vals, x)) ? 1 : 0;
+    QDKGB_CUDA(cudaEventDestroy(e0));
+    QDKGB_CUDA(cudaEventDestroy(e1));
+    F->cand[pl].clear();
+    F->cand[pl].shrink_to_fit();
+    F->tuned[pl] = true;
+    return;
+  }
+  const bool tma = MODE == 0 && sigma32t_eligible(c, vals, x);
+  const bool reg = true;
   int best = 0, best_kernel = 0;
   double best_ms = 1e300;
   F->tune_ms[pl].clear();

@@ -315,24 +315,37 @@ def test_device_limit_gives_oom_and_the_context_recovers(pkg, oracle):
 def test_tma_fed_fp32_sigma_equals_register_fed(pkg, monkeypatch):
     """The TMA-fed FP32 slab sigma (bulk copies of the slab rows into a
     shared-memory ring) sums every row in the register-fed kernel's order, so
-    both give the same FP32 sigma bit for bit; the autotuner records the
-    kernel it keeps and both kernels' timings."""
+    on the same plan (QDKGB_SIGMA32_KERNEL pins the kernel and the planner's
+    default segments) both give the same FP32 sigma bit for bit; left to
+    itself the autotuner times both kernels on every candidate plan and
+    records the one it keeps."""
     capi = pkg.capi
     pkg.build.build()
     T, V, _ = pkg.integrals.synthetic_integrals(10, 20, seed=31)
     a, b = capi.fci_dets(10, 5, 5)
     x = np.random.default_rng(5).normal(size=len(a)).astype(np.float32)
     out = {}
-    for kern in ("register", "tma"):
-        monkeypatch.setenv("QDKGB_SIGMA32_KERNEL", kern)
+    for kern in ("register", "tma", None):
+        if kern:
+            monkeypatch.setenv("QDKGB_SIGMA32_KERNEL", kern)
+        else:
+            monkeypatch.delenv("QDKGB_SIGMA32_KERNEL", raising=False)
         with capi.Context(0) as ctx:
             ctx.set_integrals(T, V)
             ctx.set_dets(a, b)
             ctx.build_hamiltonian(storage=capi.H_SPLIT32)
             y = ctx.spmv(x, precision=capi.PREC_MIXED)
             seg, cand, used, tma_ms = ctx.sigma_plan(capi.PREC_MIXED, with_kernel=True)
-            out[kern] = (np.asarray(y, dtype=np.float32), used, cand, tma_ms)
+            out[kern] = (np.asarray(y, dtype=np.float32), used, cand, tma_ms, seg)
     assert out["register"][1] == "register" and out["tma"][1] == "tma"
+    assert out["register"][4] == out["tma"][4]
     assert np.array_equal(out["register"][0].view(np.uint32), out["tma"][0].view(np.uint32))
-    assert all(np.isfinite(t) and t > 0 for t in out["tma"][3])
-    assert all(np.isfinite(ms) and ms > 0 for _, ms in out["register"][2])
+    _, used, cand, tma_ms, seg = out[None]
+    assert len(cand) >= 1 and len(tma_ms) == len(cand)
+    assert all(np.isfinite(ms) and ms > 0 for _, ms in cand)
+    assert all(np.isfinite(t) and t > 0 for t in tma_ms)
+    best = min(min(ms for _, ms in cand), min(tma_ms))
+    chosen = [ms for (s, ms) in cand if s == seg] if used == "register" else \
+        [t for (s, _), t in zip(cand, tma_ms) if s == seg]
+    assert abs(min(chosen) - best) < 1e-12
+    assert np.max(np.abs(out[None][0] - out["register"][0])) <= 1e-5 * np.max(np.abs(out["register"][0]))
