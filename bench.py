@@ -458,16 +458,23 @@ def run_batched(args):
     pkg.build.build()
     capi = pkg.capi
     inst = batch_instances(pkg)
+    # a sub-batch for profiling: one shape (--batch-norb), the first
+    # --batch-count instances; --persistent / --cluster select the solver
+    if args.batch_norb:
+        inst = [x for x in inst if x[0] == args.batch_norb]
+    if args.batch_count:
+        inst = inst[:args.batch_count]
+    solver = {"persistent": args.persistent, "cluster": args.cluster}
     ctx = capi.Context(local)
     for _ in range(max(1, args.warmup)):
-        capi.casci_batch(ctx, inst, res_tol=RES_TOL)
+        capi.casci_batch(ctx, inst, res_tol=RES_TOL, **solver)
     launches0 = capi.kernel_launches()
     times, infos = [], []
     with ClockSampler(local) as clk:
         for _ in range(args.steps):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            E, R, its, info = capi.casci_batch(ctx, inst, res_tol=RES_TOL)
+            E, R, its, info = capi.casci_batch(ctx, inst, res_tol=RES_TOL, **solver)
             torch.cuda.synchronize()
             times.append(time.perf_counter() - t0)
             infos.append(info)
@@ -477,7 +484,7 @@ def run_batched(args):
     # the persistent cluster solver (one launch per shape, tuned cluster
     # size) on the same batch, beside the default lockstep path
     t_pers = None
-    if not args.no_cpu:
+    if not args.no_cpu and not args.persistent:
         capi.casci_batch(ctx, inst, res_tol=RES_TOL, persistent=1)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -511,7 +518,8 @@ def run_batched(args):
     h2d = int(sum(x[3].nbytes + x[4].nbytes for x in inst))
     d2h = int(sum(8 + x[0] ** 2 * 8 for x in inst))
     line = {
-        "metric": "casci_batch512_instances_per_s", "value": len(inst) / t, "unit": "instances/s", "n_gpus": 1,
+        "metric": ("casci_batch512_instances_per_s" if not (args.batch_norb or args.batch_count)
+                   else "casci_batch_subset_instances_per_s"), "value": len(inst) / t, "unit": "instances/s", "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 sigma / f64 subspace+refinement",
         "data": "synthetic",
@@ -519,7 +527,10 @@ def run_batched(args):
                                "norb/2: 400 / 4,900 / 63,504 determinants), seeded integrals of the same recipe "
                                "with 2 norb Cholesky vectors; energy to |r| < 1e-8 and spin-summed 1-RDM per "
                                "instance", "instances": counts, "seed": BATCH_SEED, "res_tol": RES_TOL,
-                   "l2": "stored matrices %.1f GB, larger than L2; no flush" % (_batch_bytes(inst) * 2 / 1e9)},
+                   "l2": "stored matrices %.1f GB, larger than L2; no flush" % (_batch_bytes(inst) * 2 / 1e9),
+                   "subset": ({"norb": args.batch_norb or None, "count": args.batch_count or None}
+                              if (args.batch_norb or args.batch_count) else None),
+                   "solver": "persistent" if args.persistent else "lockstep"},
         "per_instance_fp64_gpu": {"instances_per_s": len(inst) / t_loop,
                                   "sample": "every 8th instance (%d) through qdkgb_casci FP64, scaled" % len(sample),
                                   "max_abs_energy_diff_vs_batch": float(max(dE))},
@@ -991,6 +1002,10 @@ def main():
     ap.add_argument("--nel", type=int, default=NEL)
     ap.add_argument("--nchol", type=int, default=NCHOL)
     ap.add_argument("--asci-dets", type=int, default=2000000)
+    ap.add_argument("--batch-norb", type=int, default=0, help="batched: only the instances of this norb")
+    ap.add_argument("--batch-count", type=int, default=0, help="batched: only the first N instances")
+    ap.add_argument("--persistent", type=int, default=0, help="batched: 1 = the persistent cluster solver")
+    ap.add_argument("--cluster", type=int, default=0, help="batched, persistent: CTAs per instance (0: tuned)")
     ap.add_argument("--workload", default="cas12",
                     choices=["cas12", "batched", "cas14", "asci", "pt2", "entropies", "casscf", "rdm", "direct"],
                     help="cas12: the headline CASCI(12e,12o); batched: 512 small instances; "
