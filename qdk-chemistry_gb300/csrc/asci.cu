@@ -25,6 +25,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstdlib>
+#include <thread>
 #include <vector>
 
 #include "common.cuh"
@@ -781,6 +782,43 @@ struct HDet {
 inline bool hspin_less(const HDet& x, const HDet& y) { return x.a != y.a ? x.a < y.a : x.b < y.b; }
 inline bool hdet_eq(const HDet& x, const HDet& y) { return x.a == y.a && x.b == y.b; }
 
+// Sorts a list of distinct keys on the host threads: chunks sorted in
+// parallel, then merged pairwise in parallel rounds (distinct keys have one
+// sorted order, so the split cannot change the result).
+template <class T, class Cmp>
+void parallel_sort_distinct(std::vector<T>& v, Cmp cmp) {
+  const size_t n = v.size();
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  if (n < ((size_t)1 << 16) || hw < 2) {
+    std::sort(v.begin(), v.end(), cmp);
+    return;
+  }
+  unsigned nc = 1;
+  while (nc * 2 <= std::min(hw, 64u)) nc *= 2;
+  std::vector<size_t> bnd(nc + 1);
+  for (unsigned i = 0; i <= nc; ++i) bnd[i] = n * i / nc;
+  {
+    std::vector<std::thread> th;
+    for (unsigned i = 0; i < nc; ++i)
+      th.emplace_back([&v, &bnd, cmp, i] { std::sort(v.begin() + bnd[i], v.begin() + bnd[i + 1], cmp); });
+    for (std::thread& t : th) t.join();
+  }
+  std::vector<T> buf(n);
+  std::vector<T>* src = &v;
+  std::vector<T>* dst = &buf;
+  for (unsigned w = 1; w < nc; w *= 2) {
+    std::vector<std::thread> th;
+    for (unsigned i = 0; i < nc; i += 2 * w)
+      th.emplace_back([src, dst, &bnd, cmp, i, w] {
+        std::merge(src->begin() + bnd[i], src->begin() + bnd[i + w], src->begin() + bnd[i + w],
+                   src->begin() + bnd[i + 2 * w], dst->begin() + bnd[i], cmp);
+      });
+    for (std::thread& t : th) t.join();
+    std::swap(src, dst);
+  }
+  if (src != &v) v.swap(*src);
+}
+
 // Wall time of the ASCI phases (synchronised: each phase ends in a host
 // sync anyway), accumulated into Context::asci_phase_s.
 struct PhaseClock {
@@ -872,15 +910,47 @@ double asci_iter_gpu(Context* c, const qdkgb_asci_settings& S, const qdkgb_david
                      HPatchCache* cache) {
   NvtxRange nvtx_range("qdkgb.asci_iter");
   ++c->asci_iters;
-  if (wfn.size() > 1) {  // reorder_ci_on_coeff (determinant_sort.hpp:45-64)
-    std::vector<size_t> idx(wfn.size());
-    for (size_t i = 0; i < idx.size(); ++i) idx[i] = i;
-    std::sort(idx.begin(), idx.end(), [&](size_t i, size_t j) { return std::fabs(X[i]) > std::fabs(X[j]); });
+  // the list and vector in spin order, for the warm start's merge scan (the
+  // list arrives in that order from the previous iteration)
+  std::vector<HDet> sorted_wfn;
+  std::vector<double> sorted_X;
+  if (S.warm_start) {
+    if (std::is_sorted(wfn.begin(), wfn.end(), hspin_less)) {
+      sorted_wfn = wfn;
+      sorted_X = X;
+    } else {
+      struct DC {
+        HDet d;
+        double c;
+      };
+      std::vector<DC> v(wfn.size());
+      for (size_t i = 0; i < v.size(); ++i) v[i] = {wfn[i], X[i]};
+      parallel_sort_distinct(v, [](const DC& x, const DC& y) { return hspin_less(x.d, y.d); });
+      sorted_wfn.resize(v.size());
+      sorted_X.resize(v.size());
+      for (size_t i = 0; i < v.size(); ++i) {
+        sorted_wfn[i] = v[i].d;
+        sorted_X[i] = v[i].c;
+      }
+    }
+  }
+  if (wfn.size() > 1) {
+    // reorder_ci_on_coeff (determinant_sort.hpp:45-64): std::sort of the
+    // indices by |C| descending.  The (|C|, index) pairs go through the same
+    // std::sort with the same comparisons, so ties come out in the
+    // reference's order; the pairs sit together in memory.
+    struct KI {
+      double k;
+      size_t i;
+    };
+    std::vector<KI> idx(wfn.size());
+    for (size_t i = 0; i < idx.size(); ++i) idx[i] = {std::fabs(X[i]), i};
+    std::sort(idx.begin(), idx.end(), [](const KI& x, const KI& y) { return x.k > y.k; });
     std::vector<HDet> w2(wfn.size());
     std::vector<double> x2(wfn.size());
     for (size_t i = 0; i < idx.size(); ++i) {
-      w2[i] = wfn[idx[i]];
-      x2[i] = X[idx[i]];
+      w2[i] = wfn[idx[i].i];
+      x2[i] = X[idx[i].i];
     }
     wfn.swap(w2);
     X.swap(x2);
@@ -911,20 +981,6 @@ double asci_iter_gpu(Context* c, const qdkgb_asci_settings& S, const qdkgb_david
     std::copy(w2.begin(), w2.end(), wfn.begin());
     std::copy(x2.begin(), x2.end(), X.begin());
   }
-  // the previous list and vector in spin order, for the warm start's merge scan
-  std::vector<HDet> sorted_wfn;
-  std::vector<double> sorted_X;
-  if (S.warm_start) {
-    std::vector<size_t> idx(wfn.size());
-    for (size_t i = 0; i < idx.size(); ++i) idx[i] = i;
-    std::sort(idx.begin(), idx.end(), [&](size_t i, size_t j) { return hspin_less(wfn[i], wfn[j]); });
-    sorted_wfn.resize(idx.size());
-    sorted_X.resize(idx.size());
-    for (size_t i = 0; i < idx.size(); ++i) {
-      sorted_wfn[i] = wfn[idx[i]];
-      sorted_X[i] = X[idx[i]];
-    }
-  }
   std::vector<uint64_t> ca(nkeep), cb(nkeep);
   for (size_t i = 0; i < nkeep; ++i) {
     ca[i] = wfn[i].a;
@@ -939,7 +995,7 @@ double asci_iter_gpu(Context* c, const qdkgb_asci_settings& S, const qdkgb_david
   }
   wfn.resize(na.size());
   for (size_t i = 0; i < na.size(); ++i) wfn[i] = {na[i], nb[i]};
-  std::sort(wfn.begin(), wfn.end(), hspin_less);
+  parallel_sort_distinct(wfn, hspin_less);
   std::vector<double> Xl;
   if (S.warm_start) {
     Xl.assign(wfn.size(), 0.);
