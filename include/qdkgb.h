@@ -293,6 +293,9 @@ typedef struct qdkgb_asci_settings {
   double taper_grow_factor;        /* default 0 (off): the growth factor of a step that would pass ntdets_max */
   int just_singles;                /* default 0: 1 = the search enumerates single excitations only */
   double min_patch_overlap;        /* default 0.3: patch the previous Hamiltonian when kept/new >= this */
+  int grow_with_rot;               /* default 0: 1 = natural-orbital rotation after each grow step from
+                                      rot_size_start determinants on (grow.hpp:163-252) */
+  int64_t rot_size_start;          /* default 1000 */
 } qdkgb_asci_settings;
 
 void qdkgb_asci_default_settings(qdkgb_asci_settings* s);
@@ -315,6 +318,15 @@ int qdkgb_asci(qdkgb_context* ctx, const qdkgb_asci_settings* s, const qdkgb_dav
                int64_t n0, const uint64_t* a0, const uint64_t* b0, const double* c0, double E0, int do_grow,
                int do_refine, int64_t cap, uint64_t* out_a, uint64_t* out_b, double* out_c, int64_t* n_out,
                double* E_out, double* E_grow_out);
+/* The orbital rotation of the last qdkgb_asci call with grow_with_rot (no
+ * counterpart: the reference rotates its generator's integrals in place):
+ * U (norb x norb, column-major) holds the final orbitals as columns over the
+ * orbitals the integrals were given in; the identity when no rotation took
+ * place.  After such a call the context's integrals are the rotated ones and
+ * the returned determinants and coefficients refer to the rotated orbitals,
+ * as the reference's generator does after asci_grow. */
+int qdkgb_asci_rotation(const qdkgb_context* ctx, double* U);
+
 /* Where the last qdkgb_asci call on this context spent its time (no
  * counterpart; the reference logs the same phases through its asci_search /
  * h_build / davidson loggers): seconds[0] the determinant searches,

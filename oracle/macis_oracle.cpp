@@ -417,7 +417,8 @@ void jacobi_syev(int k, double* A, int lda, double* w) {
   }
   std::vector<int> ord(k);
   std::iota(ord.begin(), ord.end(), 0);
-  std::sort(ord.begin(), ord.end(), [&](int x, int y) { return a[x + (size_t)k * x] < a[y + (size_t)k * y]; });
+  std::stable_sort(ord.begin(), ord.end(),
+                   [&](int x, int y) { return a[x + (size_t)k * x] < a[y + (size_t)k * y]; });
   for (int j = 0; j < k; ++j) {
     w[j] = a[ord[j] + (size_t)k * ord[j]];
     for (int i = 0; i < k; ++i) A[i + (size_t)lda * j] = q[i + (size_t)k * ord[j]];
@@ -1127,6 +1128,9 @@ struct AsciSettings {
   double ci_res_tol = 1e-8;
   int64_t ci_max_subspace = 200;
   double ci_matel_tol = 2.220446049250313e-16;
+  // natural-orbital rotation during the grow (determinant_search.hpp:179-181)
+  int grow_with_rot = 0;
+  int64_t rot_size_start = 1000;
 };
 
 struct Det {
@@ -1857,11 +1861,61 @@ double asci_iter(const Ham& H, const AsciSettings& S, int64_t ndets_max, double 
   return E;
 }
 
-// asci_grow (include/macis/asci/grow.hpp:45-268), without the optional rotations
-// (steps, when given, receives for each asci_iter the size asked and the size
-// reached)
-double asci_grow(const Ham& H, const AsciSettings& S, double E0, std::vector<Det>& wfn, std::vector<double>& X,
-                 std::vector<int64_t>* steps = nullptr) {
+// The natural-orbital rotation of asci_grow (grow.hpp:163-252): the
+// spin-summed 1-RDM of (wfn, X), the eigenvectors of -RDM in ascending order
+// (syev: occupations descending), T and V transformed by them
+// (two_index_transform / four_index_transform, transform.cxx), intermediates
+// rebuilt.  U (n x n) receives the rotation.
+void rotate_to_natural_orbitals(Ham& H, const std::vector<Det>& wfn, const std::vector<double>& X,
+                                std::vector<double>& U) {
+  const int n = H.n;
+  const size_t n2 = (size_t)n * n, n4 = n2 * n2;
+  std::vector<uint64_t> a(wfn.size()), b(wfn.size());
+  for (size_t i = 0; i < wfn.size(); ++i) {
+    a[i] = wfn[i].a;
+    b[i] = wfn[i].b;
+  }
+  std::vector<double> aa(n2, 0.), bb(n2, 0.);
+  Rdms R{n, aa.data(), bb.data(), nullptr, nullptr, nullptr};
+  rdms_spin_dep(a.data(), b.data(), (int64_t)wfn.size(), X.data(), R);
+  U.assign(n2, 0.);
+  for (size_t i = 0; i < n2; ++i) U[i] = -(aa[i] + bb[i]);
+  std::vector<double> w(n);
+  jacobi_syev(n, U.data(), n, w.data());
+  std::vector<double> t1(n2), T(n2);
+  for (int q = 0; q < n; ++q)
+    for (int p = 0; p < n; ++p) {
+      double t = 0.;
+      for (int k = 0; k < n; ++k) t += H.T[p + (size_t)n * k] * U[k + (size_t)n * q];
+      t1[p + (size_t)n * q] = t;
+    }
+  for (int q = 0; q < n; ++q)
+    for (int p = 0; p < n; ++p) {
+      double t = 0.;
+      for (int k = 0; k < n; ++k) t += U[k + (size_t)n * p] * t1[k + (size_t)n * q];
+      T[p + (size_t)n * q] = t;
+    }
+  std::vector<double> A(H.V), B(n4);
+  const int64_t n3 = (int64_t)n2 * n;
+  for (int pass = 0; pass < 4; ++pass) {
+#pragma omp parallel for schedule(static)
+    for (int64_t t = 0; t < n3 * n; ++t) {
+      const int64_t rest = t % n3, p = t / n3;
+      double acc = 0.;
+      for (int k = 0; k < n; ++k) acc += A[k + n * rest] * U[k + (size_t)n * p];
+      B[t] = acc;
+    }
+    A.swap(B);
+  }
+  H.init(n, T.data(), A.data());
+}
+
+// asci_grow (include/macis/asci/grow.hpp:45-268), natural-orbital rotation
+// included when S.grow_with_rot (it rotates H; rot accumulates the
+// rotations); steps, when given, receives for each asci_iter the size asked
+// and the size reached
+double asci_grow(Ham& H, const AsciSettings& S, double E0, std::vector<Det>& wfn, std::vector<double>& X,
+                 std::vector<int64_t>* steps = nullptr, std::vector<double>* rot = nullptr) {
   size_t prev = wfn.size();
   double gf = S.grow_factor;
   while ((int64_t)wfn.size() < S.ntdets_max) {
@@ -1887,6 +1941,25 @@ double asci_grow(const Ham& H, const AsciSettings& S, double E0, std::vector<Det
       gf = std::min(S.grow_factor, gf * S.recovery);
     }
     prev = wfn.size();
+    if (S.grow_with_rot && (int64_t)wfn.size() >= S.rot_size_start) {
+      std::vector<double> U;
+      rotate_to_natural_orbitals(H, wfn, X, U);
+      if (rot) {
+        const int n = H.n;
+        if (rot->empty()) {
+          *rot = U;
+        } else {
+          std::vector<double> Rr((size_t)n * n, 0.);
+          for (int j = 0; j < n; ++j)
+            for (int k = 0; k < n; ++k)
+              for (int i = 0; i < n; ++i) Rr[i + (size_t)n * j] += (*rot)[i + (size_t)n * k] * U[k + (size_t)n * j];
+          rot->swap(Rr);
+        }
+      }
+      std::vector<double> Xr;  // rediagonalised from the diagonal guess; the iteration's energy is kept
+      sci_diag(H, S, wfn, Xr);
+      X.swap(Xr);
+    }
     E0 = E;
   }
   return E0;
@@ -2096,6 +2169,8 @@ static AsciSettings asci_settings_from(const double* set) {
   S.ci_matel_tol = set[17];
   S.taper_grow_factor = set[18];
   S.just_singles = (int)set[19];
+  S.grow_with_rot = (int)set[20];
+  S.rot_size_start = (int64_t)set[21];
   return S;
 }
 
@@ -2103,16 +2178,21 @@ extern "C" {
 
 int64_t orc_asci(void* h, const double* set, int64_t n0, const uint64_t* a0, const uint64_t* b0, const double* c0,
                  double E0, int do_grow, int do_refine, int64_t cap, uint64_t* out_a, uint64_t* out_b, double* out_c,
-                 double* E_out, double* E_grow_out) {
-  const Ham& H = *(Ham*)h;
+                 double* E_out, double* E_grow_out, double* rot_out) {
   const AsciSettings S = asci_settings_from(set);
   int64_t nret = -1;
   guard([&] {
+    Ham H = *(Ham*)h;  // the grow's rotation changes this copy, which the refine then uses
     std::vector<Det> wfn(n0);
     std::vector<double> X(c0, c0 + n0);
     for (int64_t i = 0; i < n0; ++i) wfn[i] = {a0[i], b0[i]};
     double E = E0;
-    if (do_grow) E = asci_grow(H, S, E, wfn, X);
+    std::vector<double> rot;
+    if (do_grow) E = asci_grow(H, S, E, wfn, X, nullptr, &rot);
+    if (rot_out)
+      for (int j = 0; j < H.n; ++j)
+        for (int i = 0; i < H.n; ++i)
+          rot_out[i + (size_t)H.n * j] = rot.empty() ? (i == j ? 1. : 0.) : rot[i + (size_t)H.n * j];
     if (E_grow_out) *E_grow_out = E;
     if (do_refine) E = asci_refine(H, S, E, wfn, X);
     *E_out = E;
@@ -2130,7 +2210,7 @@ int64_t orc_asci(void* h, const double* set, int64_t n0, const uint64_t* a0, con
 // requested and the size reached; returns the number of entries, or -1
 int64_t orc_asci_grow_requests(void* h, const double* set, int64_t n0, const uint64_t* a0, const uint64_t* b0,
                                const double* c0, double E0, int64_t cap, int64_t* req) {
-  const Ham& H = *(Ham*)h;
+  Ham H = *(Ham*)h;
   const AsciSettings S = asci_settings_from(set);
   int64_t nret = -1;
   guard([&] {

@@ -66,7 +66,7 @@ def lib():
         L.orc_csr_spmv_block.argtypes = [vp, _f64p, _f64p]
         L.orc_asci.restype = i64
         L.orc_asci.argtypes = [vp, _f64p, i64, _u64p, _u64p, _f64p, f64, ci, ci, i64, _u64p, _u64p, _f64p,
-                               ctypes.POINTER(f64), ctypes.POINTER(f64)]
+                               ctypes.POINTER(f64), ctypes.POINTER(f64), ctypes.c_void_p]
         L.orc_asci_grow_requests.restype = i64
         L.orc_asci_grow_requests.argtypes = [vp, _f64p, i64, _u64p, _u64p, _f64p, f64, i64, _i64p]
         L.orc_asci_iter.restype = i64
@@ -262,7 +262,8 @@ ASCI_DEFAULTS = dict(ntdets_max=100000, ntdets_min=100, ncdets_max=100, core_fix
                      h_el_tol=1e-8, rv_prune_tol=1e-8, grow_factor=8.0, min_grow_factor=1.01, backoff=0.5,
                      recovery=1.1, max_refine_iter=6, refine_energy_tol=1e-6, warm_start=1,
                      min_warm_start_overlap=0.5, ci_res_tol=1e-8, ci_max_subspace=200,
-                     ci_matel_tol=float(np.finfo(np.float64).eps), taper_grow_factor=0.0, just_singles=0)
+                     ci_matel_tol=float(np.finfo(np.float64).eps), taper_grow_factor=0.0, just_singles=0,
+                     grow_with_rot=0, rot_size_start=1000)
 _ASCI_ORDER = list(ASCI_DEFAULTS)
 
 
@@ -275,9 +276,12 @@ def _asci_settings(**kw):
     return np.array([float(d[k]) for k in _ASCI_ORDER])
 
 
-def asci(ham, alpha0, beta0, c0, E0, grow=True, refine=True, **settings):
+def asci(ham, alpha0, beta0, c0, E0, grow=True, refine=True, rotation=None, **settings):
     """asci_grow then asci_refine (MACIS semantics); returns
-    (E, alpha, beta, C, E_after_grow)."""
+    (E, alpha, beta, C, E_after_grow).  With grow_with_rot the integrals are
+    rotated to natural orbitals during the grow (on a copy: ham is left as
+    it is); rotation, an n x n array when given, receives the accumulated
+    rotation (the identity without one)."""
     s = _asci_settings(**settings)
     cap = int(max(s[0] * 4, 16))
     oa = np.zeros(cap, dtype=np.uint64)
@@ -285,11 +289,15 @@ def asci(ham, alpha0, beta0, c0, E0, grow=True, refine=True, **settings):
     oc = np.zeros(cap)
     E = ctypes.c_double()
     Eg = ctypes.c_double()
+    rot = np.zeros(ham.n * ham.n)
     n = lib().orc_asci(ham._h, s, len(alpha0), np.ascontiguousarray(alpha0, dtype=np.uint64),
                        np.ascontiguousarray(beta0, dtype=np.uint64), np.ascontiguousarray(c0, dtype=np.float64),
-                       float(E0), int(grow), int(refine), cap, oa, ob, oc, ctypes.byref(E), ctypes.byref(Eg))
+                       float(E0), int(grow), int(refine), cap, oa, ob, oc, ctypes.byref(E), ctypes.byref(Eg),
+                       rot.ctypes.data)
     if n < 0:
         raise RuntimeError(lib().orc_last_error().decode())
+    if rotation is not None:
+        rotation[...] = rot.reshape((ham.n, ham.n), order="F")
     return E.value, oa[:n].copy(), ob[:n].copy(), oc[:n].copy(), Eg.value
 
 

@@ -583,11 +583,8 @@ class Gb300Asci(MultiConfigurationCalculator):
         if s.get("hamiltonian_build_algorithm") not in ("", "sorted_double_loop", "residue_arrays",
                                                         "dynamic_bit_masking"):
             raise ValueError("Unknown hamiltonian_build_algorithm: '%s'" % s.get("hamiltonian_build_algorithm"))
-        # the reference's H-build variants and its incremental patching give the
-        # same matrix as the one GPU build, so those settings are accepted as
-        # they are; natural-orbital rotation during the grow is not built
-        if s.get("grow_with_rot"):
-            raise NotImplementedError("grow_with_rot = True is not supported by the GPU ASCI (only False)")
+        # the reference's H-build variants give the same matrix as the one GPU
+        # build, so that setting is accepted as it is
         from math import comb
         if s.get("ntdets_max") > comb(n, n_alpha) * comb(n, n_beta):
             return Gb300Cas._run_impl(self, hamiltonian, n_alpha, n_beta)
@@ -610,7 +607,8 @@ class Gb300Asci(MultiConfigurationCalculator):
                 growth_recovery_rate=s.get("growth_recovery_rate"), max_refine_iter=s.get("max_refine_iter"),
                 refine_energy_tol=s.get("refine_energy_tol"), warm_start=int(s.get("warm_start_davidson")),
                 min_warm_start_overlap=s.get("min_warm_start_overlap"), taper_grow_factor=s.get("taper_grow_factor"),
-                just_singles=int(s.get("just_singles")), min_patch_overlap=s.get("min_patch_overlap"))
+                just_singles=int(s.get("just_singles")), min_patch_overlap=s.get("min_patch_overlap"),
+                grow_with_rot=int(s.get("grow_with_rot")), rot_size_start=s.get("rot_size_start"))
             tol = s.get("ci_residual_tolerance")
             grow_tol = s.get("grow_ci_residual_tolerance")
             refine = s.get("max_refine_iter") > 0
@@ -618,10 +616,12 @@ class Gb300Asci(MultiConfigurationCalculator):
                 # asci_grow with its own CI tolerance (grow.hpp:73-78), then
                 # asci_refine with the main one
                 E, a, b, C, _ = capi.asci(ctx, [a0], [b0], [1.0], E0, grow=True, refine=False, tol=grow_tol, **kw)
+                rot = capi.asci_rotation(ctx)
                 if refine:
                     E, a, b, C, _ = capi.asci(ctx, a, b, C, E, grow=False, refine=True, tol=tol, **kw)
             else:
                 E, a, b, C, _ = capi.asci(ctx, [a0], [b0], [1.0], E0, grow=True, refine=refine, tol=tol, **kw)
+                rot = capi.asci_rotation(ctx)
             rdms = None
             want = []
             if s.get("calculate_one_rdm"):
@@ -636,6 +636,11 @@ class Gb300Asci(MultiConfigurationCalculator):
                     rdms = ctx.rdms_spin_dep(C, want=tuple(want))
                 ent = self._entropies(ctx, C)
         wfn = Wavefunction(n, a, b, C, rdms, ent)
+        if s.get("grow_with_rot"):
+            # the determinants, coefficients and RDMs refer to the natural
+            # orbitals of the grow (columns over the given active orbitals),
+            # as the reference's generator holds them after asci_grow
+            wfn.info = dict(getattr(wfn, "info", None) or {}, orbital_rotation=rot)
         return E + hamiltonian.get_core_energy(), wfn
 
 

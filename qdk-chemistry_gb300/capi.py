@@ -42,7 +42,7 @@ EXPORTED = [
     "qdkgb_sigma_split_noalloc", "qdkgb_set_csr", "qdkgb_build_direct_sigma", "qdkgb_build_operator",
     "qdkgb_operator_action", "qdkgb_rdms", "qdkgb_asci_phase_times", "qdkgb_sigma_plan",
     "qdkgb_asci_default_settings", "qdkgb_asci_search", "qdkgb_asci", "qdkgb_asci_pt2",
-    "qdkgb_batch_default_settings", "qdkgb_casci_batch", "qdkgb_batch_plan",
+    "qdkgb_batch_default_settings", "qdkgb_casci_batch", "qdkgb_batch_plan", "qdkgb_asci_rotation",
 ]
 
 
@@ -77,7 +77,8 @@ class AsciSettings(ctypes.Structure):
                 ("growth_recovery_rate", ctypes.c_double), ("max_refine_iter", ctypes.c_int64),
                 ("refine_energy_tol", ctypes.c_double), ("warm_start", ctypes.c_int),
                 ("min_warm_start_overlap", ctypes.c_double), ("taper_grow_factor", ctypes.c_double),
-                ("just_singles", ctypes.c_int), ("min_patch_overlap", ctypes.c_double)]
+                ("just_singles", ctypes.c_int), ("min_patch_overlap", ctypes.c_double),
+                ("grow_with_rot", ctypes.c_int), ("rot_size_start", ctypes.c_int64)]
 
 
 class CasInstance(ctypes.Structure):
@@ -141,6 +142,7 @@ def lib():
     L.qdkgb_rdms.argtypes = [vp, vp, vp, vp]
     L.qdkgb_asci_phase_times.argtypes = [vp, vp, P(i64), P(i64)]
     L.qdkgb_batch_plan.argtypes = [vp, ci, P(ci), vp, vp, vp, vp, vp]
+    L.qdkgb_asci_rotation.argtypes = [vp, vp]
     L.qdkgb_sigma_plan.argtypes = [vp, ci, P(ci), P(ci), vp, vp, P(ci), vp]
     L.qdkgb_get_csr64_rows.argtypes = [vp, i64, i64, vp, vp, vp]
     L.qdkgb_diagonal.argtypes = [vp, vp]
@@ -596,6 +598,16 @@ def asci(ctx, alpha0, beta0, c0, E0, grow=True, refine=True, tol=1e-8, max_m=200
                                 _ptr(oc), ctypes.byref(n), ctypes.byref(E), ctypes.byref(Eg)))
     m = min(n.value, cap)
     return E.value, oa[:m].copy(), ob[:m].copy(), oc[:m].copy(), Eg.value
+
+
+def asci_rotation(ctx):
+    """The last asci call's accumulated natural-orbital rotation (norb x norb,
+    columns = the final orbitals over the given ones; the identity without
+    grow_with_rot) (qdkgb_asci_rotation)."""
+    n = int(ctx.norb)
+    U = np.zeros(n * n)
+    ctx._check(lib().qdkgb_asci_rotation(ctx.handle, _ptr(U)))
+    return U.reshape((n, n), order="F")
 
 
 def asci_phase_times(ctx):

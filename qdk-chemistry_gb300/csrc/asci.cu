@@ -1037,6 +1037,7 @@ void asci_run(Context* c, const qdkgb_asci_settings& S, const qdkgb_davidson_set
   for (double& t : c->asci_phase_s) t = 0.;
   c->asci_iters = 0;
   c->asci_patches = 0;
+  c->asci_rot.clear();
   HPatchCache cache;
   std::vector<HDet> wfn(a.size());
   for (size_t i = 0; i < a.size(); ++i) wfn[i] = {a[i], b[i]};
@@ -1065,6 +1066,34 @@ void asci_run(Context* c, const qdkgb_asci_settings& S, const qdkgb_davidson_set
         gf = std::min(S.grow_factor, gf * S.growth_recovery_rate);
       }
       prev = wfn.size();
+      if (S.grow_with_rot && (int64_t)wfn.size() >= S.rot_size_start) {
+        // natural-orbital rotation (grow.hpp:163-252): the spin-summed 1-RDM
+        // of the current wavefunction (the context holds its list), its
+        // natural orbitals, the integrals rotated to them, and the list
+        // rediagonalised from the diagonal guess in the new orbitals (the
+        // iteration's energy is kept, as the reference keeps it)
+        const int n = c->norb;
+        std::vector<double> aa((size_t)n * n, 0.), bb((size_t)n * n, 0.), ordm((size_t)n * n), U;
+        rdms_spin_dep(c, X.data(), aa.data(), bb.data(), nullptr, nullptr, nullptr);
+        for (size_t i = 0; i < ordm.size(); ++i) ordm[i] = aa[i] + bb[i];
+        natural_orbitals(n, ordm, U);
+        rotate_integrals(c, U);
+        if (c->asci_rot.empty()) {
+          c->asci_rot = U;
+        } else {
+          std::vector<double> R((size_t)n * n, 0.);
+          for (int j = 0; j < n; ++j)
+            for (int k = 0; k < n; ++k) {
+              const double u = U[k + (size_t)n * j];
+              for (int i = 0; i < n; ++i) R[i + (size_t)n * j] += c->asci_rot[i + (size_t)n * k] * u;
+            }
+          c->asci_rot.swap(R);
+        }
+        cache.valid = false;  // the integrals changed
+        std::vector<double> Xr;
+        sci_diag_gpu(c, S, ci, matel_tol, wfn, Xr, nullptr);
+        X.swap(Xr);
+      }
       E0 = E;
     }
   }

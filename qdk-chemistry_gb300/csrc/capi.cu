@@ -634,6 +634,17 @@ void qdkgb_asci_default_settings(qdkgb_asci_settings* s) {
   s->taper_grow_factor = 0.0;
   s->just_singles = 0;
   s->min_patch_overlap = 0.3;
+  s->grow_with_rot = 0;
+  s->rot_size_start = 1000;
+}
+
+int qdkgb_asci_rotation(const qdkgb_context* c, double* U) {
+  if (!c || !U) return QDKGB_ERR_INVALID;
+  const int n = c->norb;
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < n; ++i)
+      U[i + (size_t)n * j] = c->asci_rot.empty() ? (i == j ? 1. : 0.) : c->asci_rot[i + (size_t)n * j];
+  return QDKGB_OK;
 }
 
 int qdkgb_asci_search(qdkgb_context* c, const qdkgb_asci_settings* s, int64_t ncore, const uint64_t* ca,

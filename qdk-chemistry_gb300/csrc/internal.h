@@ -153,6 +153,7 @@ struct Context {
   int64_t asci_iters = 0;
   int64_t asci_patches = 0;  // Hamiltonians of the last qdkgb_asci call built by patching the previous one
   std::vector<BatchTune> batch_tune;  // persistent batched solver: cluster size per shape
+  std::vector<double> asci_rot;       // accumulated natural-orbital rotation of the last qdkgb_asci (empty: none)
   DeviceBuffer host_pinned_dummy;
   double* pinned = nullptr;  // small pinned host staging (64 doubles)
 };
@@ -221,6 +222,12 @@ struct BatchShapeJob {
   double* rdm;  // [B][norb^2] or null
 };
 void batch_solve_persistent(Context* cc, Context* owner, const BatchShapeJob& job);
+// mcscf.cu: the natural orbitals of a spin-summed 1-RDM (columns, occupations
+// descending: syev of -ordm, grow.hpp:181-188) and the rotation of the
+// context's integrals to them (two_index_transform / four_index_transform,
+// grow.hpp:196-199), intermediates rebuilt
+void natural_orbitals(int n, const std::vector<double>& ordm, std::vector<double>& C);
+void rotate_integrals(Context* c, const std::vector<double>& C);
 void lowest_eig_batch(cudaStream_t st, int B, const int* kdev, int kadd, int kmax, const double* Hs, int ldh,
                       int64_t hstride, double* eval, double* evec, int64_t estride, const int* active);
 void slab_emit_batch(Context* c, int B, const Integrals* d_ints, const double* diag_raw, int storage, double* val,

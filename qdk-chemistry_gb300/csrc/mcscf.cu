@@ -429,4 +429,82 @@ double casscf(Context* c, const qdkgb_mcscf_settings& S, int nalpha, int nbeta, 
   return E0;  // the last energy also without convergence, as the reference returns it
 }
 
+
+// eigenvectors of -ordm (symmetrised) by cyclic Jacobi, ascending eigenvalues,
+// ties in index order: the eigensolver the oracle uses in place of syev, so
+// that both rotate to the same orbitals
+void natural_orbitals(int n, const std::vector<double>& ordm, std::vector<double>& C) {
+  const size_t k = (size_t)n;
+  std::vector<double> a(k * k), q(k * k, 0.);
+  for (size_t j = 0; j < k; ++j)
+    for (size_t i = 0; i < k; ++i) a[i + k * j] = -0.5 * (ordm[i + k * j] + ordm[j + k * i]);
+  for (size_t i = 0; i < k; ++i) q[i + k * i] = 1.;
+  for (int sweep = 0; sweep < 100; ++sweep) {
+    double off = 0., tot = 0.;
+    for (size_t j = 0; j < k; ++j)
+      for (size_t i = 0; i < k; ++i) {
+        const double v = a[i + k * j] * a[i + k * j];
+        tot += v;
+        if (i != j) off += v;
+      }
+    if (off <= 1e-32 * tot || off == 0.) break;
+    for (size_t p = 0; p + 1 < k; ++p)
+      for (size_t r = p + 1; r < k; ++r) {
+        const double apq = a[p + k * r];
+        if (apq == 0.) continue;
+        const double app = a[p + k * p], aqq = a[r + k * r];
+        const double theta = (aqq - app) / (2. * apq);
+        const double t = (theta >= 0 ? 1. : -1.) / (std::fabs(theta) + std::sqrt(theta * theta + 1.));
+        const double c = 1. / std::sqrt(t * t + 1.), s = t * c;
+        for (size_t i = 0; i < k; ++i) {
+          const double aip = a[i + k * p], air = a[i + k * r];
+          a[i + k * p] = c * aip - s * air;
+          a[i + k * r] = s * aip + c * air;
+        }
+        for (size_t i = 0; i < k; ++i) {
+          const double api = a[p + k * i], ari = a[r + k * i];
+          a[p + k * i] = c * api - s * ari;
+          a[r + k * i] = s * api + c * ari;
+        }
+        for (size_t i = 0; i < k; ++i) {
+          const double qip = q[i + k * p], qir = q[i + k * r];
+          q[i + k * p] = c * qip - s * qir;
+          q[i + k * r] = s * qip + c * qir;
+        }
+      }
+  }
+  std::vector<int> ord(n);
+  for (int i = 0; i < n; ++i) ord[i] = i;
+  std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return a[x + k * x] < a[y + k * y]; });
+  C.assign(k * k, 0.);
+  for (size_t j = 0; j < k; ++j)
+    for (size_t i = 0; i < k; ++i) C[i + k * j] = q[i + k * ord[j]];
+}
+
+void rotate_integrals(Context* c, const std::vector<double>& C) {
+  const int n = c->norb;
+  const size_t n2 = (size_t)n * n, n4 = n2 * n2;
+  Mat tmp(n2), T(n2);
+  matmul(n, c->h_T.data(), false, C.data(), tmp.data());  // T C
+  matmul(n, C.data(), true, tmp.data(), T.data());        // C^T T C
+  ScopedBuffers<4> sb(c);
+  double* dC = dev_array<double>(c, sb.b[0], n2);
+  double* d0 = dev_array<double>(c, sb.b[1], n4);
+  double* d1 = dev_array<double>(c, sb.b[2], n4);
+  QDKGB_CUDA(cudaMemcpyAsync(dC, C.data(), n2 * 8, cudaMemcpyHostToDevice, c->stream));
+  QDKGB_CUDA(cudaMemcpyAsync(d0, c->h_V.data(), n4 * 8, cudaMemcpyHostToDevice, c->stream));
+  const unsigned nb = (unsigned)std::min<int64_t>(((int64_t)n4 + 255) / 256, (int64_t)c->sm_count * 16);
+  double* bufs[2] = {d1, d0};
+  const double* src = d0;
+  for (int q = 0; q < 4; ++q) {
+    k_quarter_transform<<<nb, 256, 0, c->stream>>>(src, dC, bufs[q & 1], n);
+    QDKGB_CHECK_LAUNCH();
+    src = bufs[q & 1];
+  }
+  QDKGB_CUDA(cudaMemcpyAsync(c->h_V.data(), src, n4 * 8, cudaMemcpyDeviceToHost, c->stream));
+  QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+  c->h_T = T;
+  build_integral_intermediates(c);
+}
+
 }  // namespace qdkgb

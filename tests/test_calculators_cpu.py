@@ -258,9 +258,9 @@ def test_wavefunction_entropies_from_rdms(pkg, oracle, n2_6e6o):
 def test_asci_grow_phase_settings(pkg, monkeypatch):
     """The grow-phase settings of MacisAsciSettings (macis_asci.hpp:93-182,
     determinant_search.hpp:136-198): defaults; H-build variants accepted (the
-    same matrix), unknown ones refused; grow_with_rot (not built) refused
-    before device work; taper_grow_factor and just_singles passed to the
-    device driver; grow_ci_residual_tolerance runs
+    same matrix), unknown ones refused; taper_grow_factor, just_singles,
+    grow_with_rot and rot_size_start passed to the device driver, the grow's
+    orbital rotation recorded on the wavefunction; grow_ci_residual_tolerance runs
     asci_grow at its tolerance and asci_refine at the main one (grow.hpp:73-78),
     checked with a recording stand-in for the device calls."""
     calc = pkg.calculators
@@ -281,8 +281,6 @@ def test_asci_grow_phase_settings(pkg, monkeypatch):
 
     with pytest.raises(ValueError, match="hamiltonian_build_algorithm"):
         run(hamiltonian_build_algorithm="magic")
-    with pytest.raises(NotImplementedError):
-        run(grow_with_rot=True)
 
     calls, seen = [], []
 
@@ -311,10 +309,17 @@ def test_asci_grow_phase_settings(pkg, monkeypatch):
     def fake_asci(ctx, a0, b0, c0, E0, grow, refine, tol, **kw):
         calls.append((grow, refine, tol, E0))
         seen.append((kw["taper_grow_factor"], kw["just_singles"]))
+        rots.append((kw["grow_with_rot"], kw["rot_size_start"]))
         return E0 - 0.5, np.array([15], np.uint64), np.array([15], np.uint64), np.ones(1), E0 - 0.25
 
+    rots = []
+    U = np.linalg.qr(np.random.default_rng(1).normal(size=(8, 8)))[0]
     monkeypatch.setattr(calc.capi, "Context", FakeContext)
     monkeypatch.setattr(calc.capi, "asci", fake_asci)
+    monkeypatch.setattr(calc.capi, "asci_rotation", lambda ctx: U)
+    _, w = run(grow_with_rot=True, rot_size_start=50)
+    assert rots == [(1, 50)] and np.array_equal(w.info["orbital_rotation"], U)
+    calls.clear()
     E, _ = run(hamiltonian_build_algorithm="residue_arrays", min_patch_overlap=0.9)
     assert calls == [(True, True, 1e-6, -1.0)] and E == -1.5
     calls.clear()

@@ -115,6 +115,6 @@ def test_settings_struct_layouts_match(pkg):
                 core_selection_threshold=0.95, h_el_tol=1e-8, rv_prune_tol=1e-8, grow_factor=8.0,
                 min_grow_factor=1.01, growth_backoff_rate=0.5, growth_recovery_rate=1.1, max_refine_iter=6,
                 refine_energy_tol=1e-6, warm_start=1, min_warm_start_overlap=0.5, taper_grow_factor=0.0,
-                just_singles=0, min_patch_overlap=0.3)
+                just_singles=0, min_patch_overlap=0.3, grow_with_rot=0, rot_size_start=1000)
     assert [f for f, _ in capi.AsciSettings._fields_] == list(want)
     assert {k: getattr(s, k) for k in want} == want

@@ -157,3 +157,37 @@ def test_just_singles_search(oracle, water):
     for x, y in new:
         assert min(bin(x ^ p).count("1") + bin(y ^ q).count("1") for p, q in core) == 2
     assert set(new) <= set(zip(fa.tolist(), fb.tolist()))
+
+
+def test_grow_with_rotation_is_self_consistent(oracle, water, h2o):
+    """grow_with_rot (grow.hpp:163-252): from rot_size_start determinants on,
+    the integrals are rotated to the natural orbitals of the current
+    wavefunction and the list rediagonalised.  The accumulated rotation is
+    orthogonal; in the rotated orbitals the returned vector's 1-RDM is the
+    diagonal of occupations of the last rotation's basis (up to that last
+    rediagonalisation), and its Rayleigh quotient over the rotated
+    integrals is the grow's final Davidson energy."""
+    H, (a0, b0), E_hf = water
+    n = H.n
+    U = np.zeros((n, n))
+    E, a, b, c, Eg = oracle.asci(H, a0, b0, [1.0], E_hf, grow=True, refine=False, rotation=U,
+                                 ntdets_max=400, core_fixed=1, ncdets_max=50, grow_factor=2.0,
+                                 grow_with_rot=1, rot_size_start=100)
+    assert np.max(np.abs(U.T @ U - np.eye(n))) < 1e-12
+    assert np.max(np.abs(U - np.eye(n))) > 1e-3  # a rotation happened
+    # the integrals in the final orbitals
+    T, V = h2o["T"], h2o["V"]
+    Tr = U.T @ T @ U
+    Vr = np.einsum("ap,bq,cr,ds,abcd->pqrs", U, U, U, U, V, optimize=True)
+    srt = np.lexsort((b, a))
+    Hr = oracle.Hamiltonian(Tr, Vr)
+    M = oracle.build_csr(Hr, a[srt], b[srt])
+    x = c[srt]
+    Er = x @ M.spmv(x)
+    # the returned vector is the rotated basis' ground state of the final list
+    Ed, _, _ = M.selected_ci_diag(tol=1e-10)
+    assert abs(Er - Ed) < 1e-8
+    # without rotation the same settings give a different space (and energy)
+    E0r, a1, b1, _, _ = oracle.asci(H, a0, b0, [1.0], E_hf, grow=True, refine=False, ntdets_max=400,
+                                    core_fixed=1, ncdets_max=50, grow_factor=2.0)
+    assert set(zip(a1.tolist(), b1.tolist())) != set(zip(a.tolist(), b.tolist()))
