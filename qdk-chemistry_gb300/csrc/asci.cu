@@ -25,10 +25,10 @@
 #include <chrono>
 #include <cmath>
 #include <cstdlib>
-#include <thread>
 #include <vector>
 
 #include "common.cuh"
+#include "host_parallel.h"
 #include "internal.h"
 
 namespace qdkgb {
@@ -782,42 +782,7 @@ struct HDet {
 inline bool hspin_less(const HDet& x, const HDet& y) { return x.a != y.a ? x.a < y.a : x.b < y.b; }
 inline bool hdet_eq(const HDet& x, const HDet& y) { return x.a == y.a && x.b == y.b; }
 
-// Sorts a list of distinct keys on the host threads: chunks sorted in
-// parallel, then merged pairwise in parallel rounds (distinct keys have one
-// sorted order, so the split cannot change the result).
-template <class T, class Cmp>
-void parallel_sort_distinct(std::vector<T>& v, Cmp cmp) {
-  const size_t n = v.size();
-  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-  if (n < ((size_t)1 << 16) || hw < 2) {
-    std::sort(v.begin(), v.end(), cmp);
-    return;
-  }
-  unsigned nc = 1;
-  while (nc * 2 <= std::min(hw, 64u)) nc *= 2;
-  std::vector<size_t> bnd(nc + 1);
-  for (unsigned i = 0; i <= nc; ++i) bnd[i] = n * i / nc;
-  {
-    std::vector<std::thread> th;
-    for (unsigned i = 0; i < nc; ++i)
-      th.emplace_back([&v, &bnd, cmp, i] { std::sort(v.begin() + bnd[i], v.begin() + bnd[i + 1], cmp); });
-    for (std::thread& t : th) t.join();
-  }
-  std::vector<T> buf(n);
-  std::vector<T>* src = &v;
-  std::vector<T>* dst = &buf;
-  for (unsigned w = 1; w < nc; w *= 2) {
-    std::vector<std::thread> th;
-    for (unsigned i = 0; i < nc; i += 2 * w)
-      th.emplace_back([src, dst, &bnd, cmp, i, w] {
-        std::merge(src->begin() + bnd[i], src->begin() + bnd[i + w], src->begin() + bnd[i + w],
-                   src->begin() + bnd[i + 2 * w], dst->begin() + bnd[i], cmp);
-      });
-    for (std::thread& t : th) t.join();
-    std::swap(src, dst);
-  }
-  if (src != &v) v.swap(*src);
-}
+
 
 // Wall time of the ASCI phases (synchronised: each phase ends in a host
 // sync anyway), accumulated into Context::asci_phase_s.
@@ -925,7 +890,7 @@ double asci_iter_gpu(Context* c, const qdkgb_asci_settings& S, const qdkgb_david
       };
       std::vector<DC> v(wfn.size());
       for (size_t i = 0; i < v.size(); ++i) v[i] = {wfn[i], X[i]};
-      parallel_sort_distinct(v, [](const DC& x, const DC& y) { return hspin_less(x.d, y.d); });
+      parallel_sort(v, [](const DC& x, const DC& y) { return hspin_less(x.d, y.d); });
       sorted_wfn.resize(v.size());
       sorted_X.resize(v.size());
       for (size_t i = 0; i < v.size(); ++i) {
@@ -995,7 +960,7 @@ double asci_iter_gpu(Context* c, const qdkgb_asci_settings& S, const qdkgb_david
   }
   wfn.resize(na.size());
   for (size_t i = 0; i < na.size(); ++i) wfn[i] = {na[i], nb[i]};
-  parallel_sort_distinct(wfn, hspin_less);
+  parallel_sort(wfn, hspin_less);
   std::vector<double> Xl;
   if (S.warm_start) {
     Xl.assign(wfn.size(), 0.);

@@ -25,11 +25,13 @@
 // result is deterministic.
 #include <algorithm>
 #include <cstring>
+#include <functional>
 #include <numeric>
 #include <queue>
 #include <unordered_map>
 
 #include "common.cuh"
+#include "host_parallel.h"
 #include "internal.h"
 #include "rowwalk.cuh"
 
@@ -303,10 +305,12 @@ void build_det_space(Context* c, int64_t nd, const uint64_t* alpha, const uint64
     // ranks set above
   } else if (ascending) {
     ubeta.assign(beta, beta + nd);
-    std::sort(ubeta.begin(), ubeta.end());
+    parallel_sort(ubeta, std::less<uint64_t>());
     ubeta.erase(std::unique(ubeta.begin(), ubeta.end()), ubeta.end());
-    for (int64_t i = 0; i < nd; ++i)
-      brank[i] = (int32_t)(std::lower_bound(ubeta.begin(), ubeta.end(), beta[i]) - ubeta.begin());
+    parallel_ranges(nd, [&](int64_t i0, int64_t i1) {
+      for (int64_t i = i0; i < i1; ++i)
+        brank[i] = (int32_t)(std::lower_bound(ubeta.begin(), ubeta.end(), beta[i]) - ubeta.begin());
+    });
   } else {
     // product space: every group repeats group 0's beta sequence
     const int64_t s0 = D.h_gstart[1];
