@@ -143,7 +143,7 @@ def lib():
     L.qdkgb_asci_phase_times.argtypes = [vp, vp, P(i64), P(i64)]
     L.qdkgb_batch_plan.argtypes = [vp, ci, P(ci), vp, vp, vp, vp, vp]
     L.qdkgb_asci_rotation.argtypes = [vp, vp]
-    L.qdkgb_sigma_plan.argtypes = [vp, ci, P(ci), P(ci), vp, vp, P(ci), vp]
+    L.qdkgb_sigma_plan.argtypes = [vp, ci, P(ci), P(ci), vp, vp, P(ci), vp, vp]
     L.qdkgb_get_csr64_rows.argtypes = [vp, i64, i64, vp, vp, vp]
     L.qdkgb_diagonal.argtypes = [vp, vp]
     L.qdkgb_set_csr.argtypes = [vp, i64, vp, vp, vp]
@@ -465,20 +465,23 @@ class Context:
     def sigma_plan(self, precision=PREC_MIXED, with_kernel=False):
         """(segments in use, [(candidate segments, mean ms), ...]) of the
         complete-space sigma's autotuner (qdkgb_sigma_plan); with_kernel adds
-        the FP32 kernel in use ("register" or "tma") and the TMA-fed kernel's
-        ms per candidate (NaN where not timed)."""
+        the FP32 kernel in use ("register", "tma" or "register8") and the
+        TMA-fed and eight-deep kernels' ms per candidate (NaN where not
+        timed)."""
         seg = ctypes.c_int()
         n = ctypes.c_int(32)
         ker = ctypes.c_int()
         cs = np.zeros(32, dtype=np.int32)
         cm = np.zeros(32)
         ct = np.zeros(32)
+        c8 = np.zeros(32)
         self._check(lib().qdkgb_sigma_plan(self._h, precision, ctypes.byref(seg), ctypes.byref(n), cs.ctypes.data,
-                                           cm.ctypes.data, ctypes.byref(ker), ct.ctypes.data))
+                                           cm.ctypes.data, ctypes.byref(ker), ct.ctypes.data, c8.ctypes.data))
         m = min(n.value, 32)
         out = (seg.value, [(int(cs[i]), float(cm[i])) for i in range(m)])
         if with_kernel:
-            out = out + ("tma" if ker.value == 1 else "register", [float(ct[i]) for i in range(m)])
+            out = out + ({1: "tma", 2: "register8"}.get(ker.value, "register"), [float(ct[i]) for i in range(m)],
+                         [float(c8[i]) for i in range(m)])
         return out
 
     def operator_action(self, V, alpha=1.0, AV=None, beta=0.0):

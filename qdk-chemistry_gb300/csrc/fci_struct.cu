@@ -72,10 +72,12 @@ struct FciStruct {
   std::vector<PlanHost> cand[2];
   bool tuned[2] = {false, false};
   std::vector<std::pair<int, double>> tune_ms[2];
-  // FP32 sigma kernel in use: 0 register-fed (k_slab_sigma32v), 1 TMA-fed
-  // (k_slab_sigma32t); the autotuner times both per candidate plan
+  // FP32 sigma kernel in use: 0 register-fed (k_slab_sigma32v, four
+  // positions in flight per thread), 1 TMA-fed (k_slab_sigma32t), 2
+  // register-fed with eight positions in flight; the autotuner times them
+  // per candidate plan
   int kernel32 = 0;
-  std::vector<std::pair<int, double>> tune_tma_ms;
+  std::vector<std::pair<int, double>> tune_tma_ms, tune_u8_ms;
   // spin-pair tables of the table-driven emission (rebuilt with every build)
   DeviceBuffer tab_b, tab_bm, tab_a, tab_am;
 };
@@ -694,14 +696,15 @@ struct VecT<2> {
   static __device__ __forceinline__ int at(const int2& v, int c) { return c == 0 ? v.x : v.y; }
 };
 
-template <int VEC>
+// U positions in flight per thread (U * VEC values); the per-row sums keep
+// one accumulator per row in position order, so every U gives the same result.
+template <int VEC, int U = 4>
 __global__ void __launch_bounds__(kSlabVecThreads)
     k_slab_sigma32v(SlabArgs A, PlanArgs P, const float* __restrict__ vals, const float* __restrict__ xv,
                     float* __restrict__ yv, int64_t part_stride, int64_t vstride, const int* __restrict__ active) {
   using VT = VecT<VEC>;
   using F = typename VT::F;
   using I = typename VT::I;
-  constexpr int U = 4;  // positions in flight per thread (U * VEC values)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int Nb = A.Nb;
   const int g = blockIdx.x / P.S, s = blockIdx.x - g * P.S;
@@ -1078,8 +1081,11 @@ void slab_sigma_tune(Context* c, const void* vals, const float* vlo, const void*
   // QDKGB_SIGMA32_KERNEL=register / tma: no timing, the planner's default
   // plan with that FP32 kernel (the two kernels then sum every row alike)
   const char* force = MODE == 0 ? std::getenv("QDKGB_SIGMA32_KERNEL") : nullptr;
-  if (force && (std::strcmp(force, "register") == 0 || std::strcmp(force, "tma") == 0)) {
-    F->kernel32 = (std::strcmp(force, "tma") == 0 && sigma32t_eligible(c, vals, x)) ? 1 : 0;
+  if (force && (std::strcmp(force, "register") == 0 || std::strcmp(force, "tma") == 0 ||
+                std::strcmp(force, "register8") == 0)) {
+    F->kernel32 = (std::strcmp(force, "tma") == 0 && sigma32t_eligible(c, vals, x))
+                      ? 1
+                      : (std::strcmp(force, "register8") == 0 && F->Nb % 4 == 0 ? 2 : 0);
     QDKGB_CUDA(cudaEventDestroy(e0));
     QDKGB_CUDA(cudaEventDestroy(e1));
     F->cand[pl].clear();
@@ -1088,11 +1094,16 @@ void slab_sigma_tune(Context* c, const void* vals, const float* vlo, const void*
     return;
   }
   const bool tma = MODE == 0 && sigma32t_eligible(c, vals, x);
+  // the eight-deep register kernel exists for four strings per thread
+  const bool u8 = MODE == 0 && F->Nb % 4 == 0 && ((uintptr_t)vals & 15) == 0 && ((uintptr_t)x & 15) == 0;
   const bool reg = true;
   int best = 0, best_kernel = 0;
   double best_ms = 1e300;
   F->tune_ms[pl].clear();
-  if (MODE == 0) F->tune_tma_ms.clear();
+  if (MODE == 0) {
+    F->tune_tma_ms.clear();
+    F->tune_u8_ms.clear();
+  }
   for (size_t i = 0; i < F->cand[pl].size(); ++i) {
     load(F->cand[pl][i]);
     if (MODE == 0) F->kernel32 = 0;
@@ -1111,6 +1122,16 @@ void slab_sigma_tune(Context* c, const void* vals, const float* vlo, const void*
         best_ms = mt;
         best = (int)i;
         best_kernel = 1;
+      }
+    }
+    if (u8) {
+      F->kernel32 = 2;
+      const double m8 = time3();
+      F->tune_u8_ms.push_back({F->cand[pl][i].S, m8});
+      if (m8 < best_ms) {
+        best_ms = m8;
+        best = (int)i;
+        best_kernel = 2;
       }
     }
   }
@@ -1149,6 +1170,7 @@ void slab_sigma_launch(Context* c, int B, const int* active, const void* vals, c
   set_max_dynamic_smem((const void*)k_slab_sigma<MODE>, (int)kSlabSmemMax);
   if (MODE == 0) {
     set_max_dynamic_smem((const void*)k_slab_sigma32v<4>, (int)kSlabSmemMax);
+    set_max_dynamic_smem((const void*)k_slab_sigma32v<4, 8>, (int)kSlabSmemMax);
     set_max_dynamic_smem((const void*)k_slab_sigma32v<2>, (int)kSlabSmemMax);
   }
   const int64_t n = F->G * F->Nb;
@@ -1175,7 +1197,10 @@ void slab_sigma_launch(Context* c, int B, const int* active, const void* vals, c
     const unsigned thr = (unsigned)std::min(kSlabVecThreads, (nvec + 31) / 32 * 32);
     const unsigned bz = (unsigned)((nvec + thr - 1) / thr);
     const dim3 grid((unsigned)(F->G * PL.S), (unsigned)B, bz);
-    if (vec == 4)
+    if (vec == 4 && F->kernel32 == 2)
+      k_slab_sigma32v<4, 8><<<grid, thr, smem, c->stream>>>(slab_args(c), P, (const float*)vals, (const float*)x,
+                                                            (float*)out, (int64_t)B * n, vstride, active);
+    else if (vec == 4)
       k_slab_sigma32v<4><<<grid, thr, smem, c->stream>>>(slab_args(c), P, (const float*)vals, (const float*)x,
                                                          (float*)out, (int64_t)B * n, vstride, active);
     else
@@ -1200,12 +1225,13 @@ void slab_sigma_launch(Context* c, int B, const int* active, const void* vals, c
 // the sigma plan of a precision (0: FP32, 1: FP64): segments in use and the
 // autotuner's record (S, ms) per candidate (empty before the first sigma)
 int struct_sigma_plan(Context* c, int pl, std::vector<std::pair<int, double>>* record, int* kernel,
-                      std::vector<std::pair<int, double>>* record_tma) {
+                      std::vector<std::pair<int, double>>* record_tma, std::vector<std::pair<int, double>>* record_u8) {
   if (kernel) *kernel = 0;
   if (!c->fci || pl < 0 || pl > 1) return 0;
   if (record) *record = c->fci->tune_ms[pl];
   if (kernel && pl == 0) *kernel = c->fci->kernel32;
   if (record_tma && pl == 0) *record_tma = c->fci->tune_tma_ms;
+  if (record_u8 && pl == 0) *record_u8 = c->fci->tune_u8_ms;
   return c->fci->plan[pl].S;
 }
 

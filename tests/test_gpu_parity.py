@@ -325,7 +325,7 @@ def test_tma_fed_fp32_sigma_equals_register_fed(pkg, monkeypatch):
     a, b = capi.fci_dets(10, 5, 5)
     x = np.random.default_rng(5).normal(size=len(a)).astype(np.float32)
     out = {}
-    for kern in ("register", "tma", None):
+    for kern in ("register", "tma", "register8", None):
         if kern:
             monkeypatch.setenv("QDKGB_SIGMA32_KERNEL", kern)
         else:
@@ -335,17 +335,18 @@ def test_tma_fed_fp32_sigma_equals_register_fed(pkg, monkeypatch):
             ctx.set_dets(a, b)
             ctx.build_hamiltonian(storage=capi.H_SPLIT32)
             y = ctx.spmv(x, precision=capi.PREC_MIXED)
-            seg, cand, used, tma_ms = ctx.sigma_plan(capi.PREC_MIXED, with_kernel=True)
-            out[kern] = (np.asarray(y, dtype=np.float32), used, cand, tma_ms, seg)
-    assert out["register"][1] == "register" and out["tma"][1] == "tma"
-    assert out["register"][4] == out["tma"][4]
-    assert np.array_equal(out["register"][0].view(np.uint32), out["tma"][0].view(np.uint32))
-    _, used, cand, tma_ms, seg = out[None]
-    assert len(cand) >= 1 and len(tma_ms) == len(cand)
+            seg, cand, used, tma_ms, u8_ms = ctx.sigma_plan(capi.PREC_MIXED, with_kernel=True)
+            out[kern] = (np.asarray(y, dtype=np.float32), used, cand, (tma_ms, u8_ms), seg)
+    assert [out[k][1] for k in ("register", "tma", "register8")] == ["register", "tma", "register8"]
+    assert out["register"][4] == out["tma"][4] == out["register8"][4]
+    for k in ("tma", "register8"):
+        assert np.array_equal(out["register"][0].view(np.uint32), out[k][0].view(np.uint32)), k
+    _, used, cand, (tma_ms, u8_ms), seg = out[None]
+    assert len(cand) >= 1 and len(tma_ms) == len(cand) == len(u8_ms)
     assert all(np.isfinite(ms) and ms > 0 for _, ms in cand)
-    assert all(np.isfinite(t) and t > 0 for t in tma_ms)
-    best = min(min(ms for _, ms in cand), min(tma_ms))
-    chosen = [ms for (s, ms) in cand if s == seg] if used == "register" else \
-        [t for (s, _), t in zip(cand, tma_ms) if s == seg]
+    assert all(np.isfinite(t) and t > 0 for t in tma_ms + u8_ms)
+    best = min(min(ms for _, ms in cand), min(tma_ms), min(u8_ms))
+    times = {"register": [ms for _, ms in cand], "tma": tma_ms, "register8": u8_ms}[used]
+    chosen = [t for (s, _), t in zip(cand, times) if s == seg]
     assert abs(min(chosen) - best) < 1e-12
     assert np.max(np.abs(out[None][0] - out["register"][0])) <= 1e-5 * np.max(np.abs(out["register"][0]))
