@@ -325,9 +325,9 @@ def run_ours(args):
         if used32 == "tma":
             kern32 = ("k_slab_sigma32t (FP32 sigma, slab layout: values only; rows streamed into shared memory "
                       "by TMA bulk copies, 4 beta strings per thread)")
-        elif used32 == "register8":
-            kern32 = ("k_slab_sigma32v<4, 8> (FP32 sigma, slab layout: values only, 4 beta strings per thread, "
-                      "8 positions in flight)")
+        elif used32 in ("register8", "register16"):
+            kern32 = ("k_slab_sigma32v<4, %d> (FP32 sigma, slab layout: values only, 4 beta strings per thread, "
+                      "%d positions in flight)" % ((8, 8) if used32 == "register8" else (16, 16)))
     else:
         bytes32 = nnz * 8 + (N + 1) * 8 + N * 4 + N * 4
         kern32 = "k_spmv_csr<float> (FP32 sigma, CSR)"
@@ -385,8 +385,7 @@ def run_ours(args):
                      "traffic": traffic, "algorithmic_bytes": bytes32, "launch_ms": t_spmv32 * 1e3},
         "spmv_fp64": {"kernel": kern64, "achieved_gbs": achieved64, "frac": achieved64 / peak,
                       "launch_ms": t_spmv64 * 1e3, "algorithmic_bytes": bytes64},
-        "sigma_autotune": {"fp32": dict(zip(("segments", "candidates_ms", "kernel", "tma_candidates_ms",
-                                             "register8_candidates_ms"),
+        "sigma_autotune": {"fp32": dict(zip(("segments", "candidates_ms", "kernel", "kernel_candidates_ms"),
                                             ctx.sigma_plan(capi.PREC_MIXED, with_kernel=True))),
                            "fp64": dict(zip(("segments", "candidates_ms"), ctx.sigma_plan(capi.PREC_FP64)))},
         "hbuild_s": float(np.mean(hbs)), "davidson_s": float(np.mean(dvs)),

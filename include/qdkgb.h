@@ -162,14 +162,16 @@ int qdkgb_build_operator(qdkgb_context* ctx, double thresh, int storage, int max
  * sigma); with ncand (in: capacity, out: candidates tried) the candidates'
  * counts and mean milliseconds, empty before the first sigma.  For the FP32
  * sigma the tuner also times the TMA-fed kernel (slab rows streamed into
- * shared memory by bulk copies) and the register-fed kernel with eight
- * positions in flight per thread on every candidate: *kernel (may be NULL)
- * receives the kernel in use (0 register-fed, 1 TMA-fed, 2 register-fed
- * eight deep), cand_ms_tma and cand_ms_u8 (may be NULL) their milliseconds
- * per candidate (NaN where not timed).  All of them sum every row in the same
- * order: the same FP32 sigma bit for bit on the same plan. */
+ * shared memory by bulk copies) and the register-fed kernel with eight and
+ * with sixteen positions in flight per thread on every candidate: *kernel
+ * (may be NULL) receives the kernel in use (0 register-fed four deep, 1
+ * TMA-fed, 2 / 3 register-fed eight / sixteen deep); kernel_ms (may be NULL,
+ * QDKGB_SIGMA32_KERNELS rows of the ncand capacity) each kernel's
+ * milliseconds per candidate (NaN where not timed).  All of them sum every
+ * row in the same order: the same FP32 sigma bit for bit on the same plan. */
+#define QDKGB_SIGMA32_KERNELS 4
 int qdkgb_sigma_plan(qdkgb_context* ctx, int precision, int* segments, int* ncand, int* cand_segments,
-                     double* cand_ms, int* kernel, double* cand_ms_tma, double* cand_ms_u8);
+                     double* cand_ms, int* kernel, double* kernel_ms);
 
 /* Copies the device CSR to host buffers (rowptr: ndets+1, colind/values: nnz).
  * For QDKGB_H_SPLIT32 storage, values receive (double)hi + (double)lo.

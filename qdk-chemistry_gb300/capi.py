@@ -46,6 +46,10 @@ EXPORTED = [
 ]
 
 
+# the FP32 sigma kernels of the autotuner (qdkgb_sigma_plan), by index
+SIGMA32_KERNELS = ("register", "tma", "register8", "register16")
+
+
 class QdkgbError(RuntimeError):
     def __init__(self, code, msg):
         super().__init__("qdkgb error %d: %s" % (code, msg))
@@ -143,7 +147,7 @@ def lib():
     L.qdkgb_asci_phase_times.argtypes = [vp, vp, P(i64), P(i64)]
     L.qdkgb_batch_plan.argtypes = [vp, ci, P(ci), vp, vp, vp, vp, vp]
     L.qdkgb_asci_rotation.argtypes = [vp, vp]
-    L.qdkgb_sigma_plan.argtypes = [vp, ci, P(ci), P(ci), vp, vp, P(ci), vp, vp]
+    L.qdkgb_sigma_plan.argtypes = [vp, ci, P(ci), P(ci), vp, vp, P(ci), vp]
     L.qdkgb_get_csr64_rows.argtypes = [vp, i64, i64, vp, vp, vp]
     L.qdkgb_diagonal.argtypes = [vp, vp]
     L.qdkgb_set_csr.argtypes = [vp, i64, vp, vp, vp]
@@ -465,23 +469,21 @@ class Context:
     def sigma_plan(self, precision=PREC_MIXED, with_kernel=False):
         """(segments in use, [(candidate segments, mean ms), ...]) of the
         complete-space sigma's autotuner (qdkgb_sigma_plan); with_kernel adds
-        the FP32 kernel in use ("register", "tma" or "register8") and the
-        TMA-fed and eight-deep kernels' ms per candidate (NaN where not
-        timed)."""
+        the FP32 kernel in use (a name of SIGMA32_KERNELS) and every kernel's
+        ms per candidate ({name: [ms, ...]}, NaN where not timed)."""
         seg = ctypes.c_int()
         n = ctypes.c_int(32)
         ker = ctypes.c_int()
         cs = np.zeros(32, dtype=np.int32)
         cm = np.zeros(32)
-        ct = np.zeros(32)
-        c8 = np.zeros(32)
+        km = np.zeros(4 * 32)
         self._check(lib().qdkgb_sigma_plan(self._h, precision, ctypes.byref(seg), ctypes.byref(n), cs.ctypes.data,
-                                           cm.ctypes.data, ctypes.byref(ker), ct.ctypes.data, c8.ctypes.data))
+                                           cm.ctypes.data, ctypes.byref(ker), km.ctypes.data))
         m = min(n.value, 32)
         out = (seg.value, [(int(cs[i]), float(cm[i])) for i in range(m)])
         if with_kernel:
-            out = out + ({1: "tma", 2: "register8"}.get(ker.value, "register"), [float(ct[i]) for i in range(m)],
-                         [float(c8[i]) for i in range(m)])
+            out = out + (SIGMA32_KERNELS[ker.value],
+                         {SIGMA32_KERNELS[k]: [float(km[32 * k + i]) for i in range(m)] for k in range(4)})
         return out
 
     def operator_action(self, V, alpha=1.0, AV=None, beta=0.0):

@@ -703,17 +703,20 @@ int qdkgb_asci(qdkgb_context* c, const qdkgb_asci_settings* s, const qdkgb_david
 }
 
 int qdkgb_sigma_plan(qdkgb_context* c, int precision, int* segments, int* ncand, int* cand_segments,
-                     double* cand_ms, int* kernel, double* cand_ms_tma, double* cand_ms_u8) {
+                     double* cand_ms, int* kernel, double* kernel_ms) {
   if (!c || !segments) return QDKGB_ERR_INVALID;
-  std::vector<std::pair<int, double>> rec, rec_tma, rec_u8;
-  *segments = struct_sigma_plan(c, precision == QDKGB_PREC_MIXED ? 0 : 1, &rec, kernel, &rec_tma, &rec_u8);
+  std::vector<std::pair<int, double>> rec;
+  std::vector<std::vector<double>> kms;
+  *segments = struct_sigma_plan(c, precision == QDKGB_PREC_MIXED ? 0 : 1, &rec, kernel, &kms);
   const int cap = ncand ? *ncand : 0;
   if (ncand) *ncand = (int)rec.size();
   for (int i = 0; i < std::min(cap, (int)rec.size()); ++i) {
     if (cand_segments) cand_segments[i] = rec[i].first;
     if (cand_ms) cand_ms[i] = rec[i].second;
-    if (cand_ms_tma) cand_ms_tma[i] = i < (int)rec_tma.size() ? rec_tma[i].second : std::nan("");
-    if (cand_ms_u8) cand_ms_u8[i] = i < (int)rec_u8.size() ? rec_u8[i].second : std::nan("");
+    if (kernel_ms)
+      for (int k = 0; k < QDKGB_SIGMA32_KERNELS; ++k)
+        kernel_ms[(size_t)k * cap + i] =
+            (k < (int)kms.size() && i < (int)kms[k].size()) ? kms[k][i] : std::nan("");
   }
   return QDKGB_OK;
 }

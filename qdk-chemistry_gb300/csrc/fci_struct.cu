@@ -39,6 +39,7 @@ constexpr int kSlabVecThreads = 256;         // vectorised FP32 sigma: CTA size 
 constexpr int kSlabThreads = 512;            // sigma CTA size at most; a group's beta strings are split
                                              // over ceil(Nb / 512) CTAs (grid.z)
 constexpr int kEmitSegments = 4;             // position ranges per group in emission / export
+constexpr int kSigma32Kernels = 4;           // FP32 sigma kernels the autotuner chooses from
 
 // Sigma work split for one staged-x element size: CTA per (group, segment);
 // a segment is a run of whole row items (the own-group block, alpha-single
@@ -73,11 +74,12 @@ struct FciStruct {
   bool tuned[2] = {false, false};
   std::vector<std::pair<int, double>> tune_ms[2];
   // FP32 sigma kernel in use: 0 register-fed (k_slab_sigma32v, four
-  // positions in flight per thread), 1 TMA-fed (k_slab_sigma32t), 2
-  // register-fed with eight positions in flight; the autotuner times them
-  // per candidate plan
+  // positions in flight per thread), 1 TMA-fed (k_slab_sigma32t), 2 and 3
+  // register-fed with eight and sixteen positions in flight; the autotuner
+  // times them per candidate plan (tune_kernel_ms[k][i]: kernel k, plan i,
+  // NaN where not eligible)
   int kernel32 = 0;
-  std::vector<std::pair<int, double>> tune_tma_ms, tune_u8_ms;
+  std::vector<double> tune_kernel_ms[kSigma32Kernels];
   // spin-pair tables of the table-driven emission (rebuilt with every build)
   DeviceBuffer tab_b, tab_bm, tab_a, tab_am;
 };
@@ -1078,60 +1080,49 @@ void slab_sigma_tune(Context* c, const void* vals, const float* vlo, const void*
     QDKGB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
     return ms / 3.0;
   };
-  // QDKGB_SIGMA32_KERNEL=register / tma: no timing, the planner's default
-  // plan with that FP32 kernel (the two kernels then sum every row alike)
+  // QDKGB_SIGMA32_KERNEL=register / tma / register8 / register16: no timing,
+  // the planner's default plan with that FP32 kernel (all of them then sum
+  // every row alike)
+  const char* names[kSigma32Kernels] = {"register", "tma", "register8", "register16"};
   const char* force = MODE == 0 ? std::getenv("QDKGB_SIGMA32_KERNEL") : nullptr;
-  if (force && (std::strcmp(force, "register") == 0 || std::strcmp(force, "tma") == 0 ||
-                std::strcmp(force, "register8") == 0)) {
-    F->kernel32 = (std::strcmp(force, "tma") == 0 && sigma32t_eligible(c, vals, x))
-                      ? 1
-                      : (std::strcmp(force, "register8") == 0 && F->Nb % 4 == 0 ? 2 : 0);
-    QDKGB_CUDA(cudaEventDestroy(e0));
-    QDKGB_CUDA(cudaEventDestroy(e1));
-    F->cand[pl].clear();
-    F->cand[pl].shrink_to_fit();
-    F->tuned[pl] = true;
-    return;
+  auto eligible = [&](int k) {
+    if (MODE != 0) return k == 0;
+    if (k == 1) return sigma32t_eligible(c, vals, x);
+    if (k >= 2) return F->Nb % 4 == 0 && ((uintptr_t)vals & 15) == 0 && ((uintptr_t)x & 15) == 0;
+    return true;
+  };
+  if (force) {
+    for (int k = 0; k < kSigma32Kernels; ++k)
+      if (std::strcmp(force, names[k]) == 0) {
+        F->kernel32 = eligible(k) ? k : 0;
+        QDKGB_CUDA(cudaEventDestroy(e0));
+        QDKGB_CUDA(cudaEventDestroy(e1));
+        F->cand[pl].clear();
+        F->cand[pl].shrink_to_fit();
+        F->tuned[pl] = true;
+        return;
+      }
   }
-  const bool tma = MODE == 0 && sigma32t_eligible(c, vals, x);
-  // the eight-deep register kernel exists for four strings per thread
-  const bool u8 = MODE == 0 && F->Nb % 4 == 0 && ((uintptr_t)vals & 15) == 0 && ((uintptr_t)x & 15) == 0;
-  const bool reg = true;
   int best = 0, best_kernel = 0;
   double best_ms = 1e300;
   F->tune_ms[pl].clear();
-  if (MODE == 0) {
-    F->tune_tma_ms.clear();
-    F->tune_u8_ms.clear();
-  }
+  if (MODE == 0)
+    for (std::vector<double>& v : F->tune_kernel_ms) v.clear();
   for (size_t i = 0; i < F->cand[pl].size(); ++i) {
     load(F->cand[pl][i]);
-    if (MODE == 0) F->kernel32 = 0;
-    const double ms = reg ? time3() : std::nan("");
-    F->tune_ms[pl].push_back({F->cand[pl][i].S, ms});
-    if (reg && ms < best_ms) {
-      best_ms = ms;
-      best = (int)i;
-      best_kernel = 0;
-    }
-    if (tma) {
-      F->kernel32 = 1;
-      const double mt = time3();
-      F->tune_tma_ms.push_back({F->cand[pl][i].S, mt});
-      if (mt < best_ms) {
-        best_ms = mt;
-        best = (int)i;
-        best_kernel = 1;
+    for (int k = 0; k < (MODE == 0 ? kSigma32Kernels : 1); ++k) {
+      if (!eligible(k)) {
+        F->tune_kernel_ms[k].push_back(std::nan(""));
+        continue;
       }
-    }
-    if (u8) {
-      F->kernel32 = 2;
-      const double m8 = time3();
-      F->tune_u8_ms.push_back({F->cand[pl][i].S, m8});
-      if (m8 < best_ms) {
-        best_ms = m8;
+      if (MODE == 0) F->kernel32 = k;
+      const double ms = time3();
+      if (k == 0) F->tune_ms[pl].push_back({F->cand[pl][i].S, ms});
+      if (MODE == 0) F->tune_kernel_ms[k].push_back(ms);
+      if (ms < best_ms) {
+        best_ms = ms;
         best = (int)i;
-        best_kernel = 2;
+        best_kernel = k;
       }
     }
   }
@@ -1171,6 +1162,7 @@ void slab_sigma_launch(Context* c, int B, const int* active, const void* vals, c
   if (MODE == 0) {
     set_max_dynamic_smem((const void*)k_slab_sigma32v<4>, (int)kSlabSmemMax);
     set_max_dynamic_smem((const void*)k_slab_sigma32v<4, 8>, (int)kSlabSmemMax);
+    set_max_dynamic_smem((const void*)k_slab_sigma32v<4, 16>, (int)kSlabSmemMax);
     set_max_dynamic_smem((const void*)k_slab_sigma32v<2>, (int)kSlabSmemMax);
   }
   const int64_t n = F->G * F->Nb;
@@ -1200,6 +1192,9 @@ void slab_sigma_launch(Context* c, int B, const int* active, const void* vals, c
     if (vec == 4 && F->kernel32 == 2)
       k_slab_sigma32v<4, 8><<<grid, thr, smem, c->stream>>>(slab_args(c), P, (const float*)vals, (const float*)x,
                                                             (float*)out, (int64_t)B * n, vstride, active);
+    else if (vec == 4 && F->kernel32 == 3)
+      k_slab_sigma32v<4, 16><<<grid, thr, smem, c->stream>>>(slab_args(c), P, (const float*)vals, (const float*)x,
+                                                             (float*)out, (int64_t)B * n, vstride, active);
     else if (vec == 4)
       k_slab_sigma32v<4><<<grid, thr, smem, c->stream>>>(slab_args(c), P, (const float*)vals, (const float*)x,
                                                          (float*)out, (int64_t)B * n, vstride, active);
@@ -1225,13 +1220,13 @@ void slab_sigma_launch(Context* c, int B, const int* active, const void* vals, c
 // the sigma plan of a precision (0: FP32, 1: FP64): segments in use and the
 // autotuner's record (S, ms) per candidate (empty before the first sigma)
 int struct_sigma_plan(Context* c, int pl, std::vector<std::pair<int, double>>* record, int* kernel,
-                      std::vector<std::pair<int, double>>* record_tma, std::vector<std::pair<int, double>>* record_u8) {
+                      std::vector<std::vector<double>>* kernel_ms) {
   if (kernel) *kernel = 0;
+  if (kernel_ms) kernel_ms->clear();
   if (!c->fci || pl < 0 || pl > 1) return 0;
   if (record) *record = c->fci->tune_ms[pl];
   if (kernel && pl == 0) *kernel = c->fci->kernel32;
-  if (record_tma && pl == 0) *record_tma = c->fci->tune_tma_ms;
-  if (record_u8 && pl == 0) *record_u8 = c->fci->tune_u8_ms;
+  if (kernel_ms && pl == 0) kernel_ms->assign(c->fci->tune_kernel_ms, c->fci->tune_kernel_ms + kSigma32Kernels);
   return c->fci->plan[pl].S;
 }
 

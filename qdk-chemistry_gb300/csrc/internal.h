@@ -194,11 +194,11 @@ void struct_spmv_fp32(Context* c, const float* x, float* y);
 void struct_export(Context* c, int32_t* ci, double* v64, float* h32, float* l32);
 int64_t struct_slab_elements(Context* c);
 // segments in use and the autotuner's record (segments, ms) per candidate; for
-// the FP32 plan also the kernel in use (0 register-fed, 1 TMA-fed, 2
-// register-fed eight positions deep) and the other kernels' timings
+// the FP32 plan also the kernel in use (0 register-fed, 1 TMA-fed, 2 / 3
+// register-fed eight / sixteen positions deep) and every kernel's timing per
+// candidate
 int struct_sigma_plan(Context* c, int plan, std::vector<std::pair<int, double>>* record, int* kernel = nullptr,
-                      std::vector<std::pair<int, double>>* record_tma = nullptr,
-                      std::vector<std::pair<int, double>>* record_u8 = nullptr);
+                      std::vector<std::vector<double>>* kernel_ms = nullptr);
 // batch.cu
 void casci_batch(Context* ctx, int ninst, const qdkgb_cas_instance* inst, const qdkgb_batch_settings& st,
                  double* energies, double* rdm1, int* iters, qdkgb_batch_info* info);

@@ -313,19 +313,19 @@ def test_device_limit_gives_oom_and_the_context_recovers(pkg, oracle):
 
 
 def test_tma_fed_fp32_sigma_equals_register_fed(pkg, monkeypatch):
-    """The TMA-fed FP32 slab sigma (bulk copies of the slab rows into a
-    shared-memory ring) sums every row in the register-fed kernel's order, so
-    on the same plan (QDKGB_SIGMA32_KERNEL pins the kernel and the planner's
-    default segments) both give the same FP32 sigma bit for bit; left to
-    itself the autotuner times both kernels on every candidate plan and
-    records the one it keeps."""
+    """The FP32 slab sigma kernels (register-fed four, eight and sixteen
+    positions deep; TMA-fed: bulk copies of the slab rows into a
+    shared-memory ring) sum every row in the same order, so on the same plan
+    (QDKGB_SIGMA32_KERNEL pins the kernel and the planner's default segments)
+    they give the same FP32 sigma bit for bit; left to itself the autotuner
+    times every kernel on every candidate plan and keeps the fastest pair."""
     capi = pkg.capi
     pkg.build.build()
     T, V, _ = pkg.integrals.synthetic_integrals(10, 20, seed=31)
     a, b = capi.fci_dets(10, 5, 5)
     x = np.random.default_rng(5).normal(size=len(a)).astype(np.float32)
     out = {}
-    for kern in ("register", "tma", "register8", None):
+    for kern in capi.SIGMA32_KERNELS + (None,):
         if kern:
             monkeypatch.setenv("QDKGB_SIGMA32_KERNEL", kern)
         else:
@@ -335,18 +335,16 @@ def test_tma_fed_fp32_sigma_equals_register_fed(pkg, monkeypatch):
             ctx.set_dets(a, b)
             ctx.build_hamiltonian(storage=capi.H_SPLIT32)
             y = ctx.spmv(x, precision=capi.PREC_MIXED)
-            seg, cand, used, tma_ms, u8_ms = ctx.sigma_plan(capi.PREC_MIXED, with_kernel=True)
-            out[kern] = (np.asarray(y, dtype=np.float32), used, cand, (tma_ms, u8_ms), seg)
-    assert [out[k][1] for k in ("register", "tma", "register8")] == ["register", "tma", "register8"]
-    assert out["register"][4] == out["tma"][4] == out["register8"][4]
-    for k in ("tma", "register8"):
+            seg, cand, used, kms = ctx.sigma_plan(capi.PREC_MIXED, with_kernel=True)
+            out[kern] = (np.asarray(y, dtype=np.float32), used, cand, kms, seg)
+    for k in capi.SIGMA32_KERNELS:
+        assert out[k][1] == k and out[k][4] == out["register"][4]
         assert np.array_equal(out["register"][0].view(np.uint32), out[k][0].view(np.uint32)), k
-    _, used, cand, (tma_ms, u8_ms), seg = out[None]
-    assert len(cand) >= 1 and len(tma_ms) == len(cand) == len(u8_ms)
-    assert all(np.isfinite(ms) and ms > 0 for _, ms in cand)
-    assert all(np.isfinite(t) and t > 0 for t in tma_ms + u8_ms)
-    best = min(min(ms for _, ms in cand), min(tma_ms), min(u8_ms))
-    times = {"register": [ms for _, ms in cand], "tma": tma_ms, "register8": u8_ms}[used]
-    chosen = [t for (s, _), t in zip(cand, times) if s == seg]
+    _, used, cand, kms, seg = out[None]
+    assert len(cand) >= 1
+    for k in capi.SIGMA32_KERNELS:
+        assert len(kms[k]) == len(cand) and all(np.isfinite(t) and t > 0 for t in kms[k]), k
+    best = min(min(v) for v in kms.values())
+    chosen = [t for (s, _), t in zip(cand, kms[used]) if s == seg]
     assert abs(min(chosen) - best) < 1e-12
     assert np.max(np.abs(out[None][0] - out["register"][0])) <= 1e-5 * np.max(np.abs(out["register"][0]))
