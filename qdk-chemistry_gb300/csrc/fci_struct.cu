@@ -1297,6 +1297,14 @@ void slab_reserve_batch(Context* c, int B) {
   const int64_t n = F->G * F->Nb;
   const size_t need = std::max<size_t>((size_t)F->plan[0].S * 4, (size_t)F->plan[1].S * 8) * B * n;
   dev_alloc(c, F->ypart, need);
+  // the batched FP32 sigma is not autotuned: the four-deep register-fed
+  // kernel unless QDKGB_SIGMA32_KERNEL pins a register-fed depth
+  const char* force = std::getenv("QDKGB_SIGMA32_KERNEL");
+  F->kernel32 = 0;
+  if (force && F->Nb % 4 == 0) {
+    if (std::strcmp(force, "register8") == 0) F->kernel32 = 2;
+    if (std::strcmp(force, "register16") == 0) F->kernel32 = 3;
+  }
 }
 
 // mode 0: FP32 (vals = hi, x/y float); 1: FP64; 2: float-float from (hi, lo)

@@ -4,7 +4,8 @@ GpuHamiltonianGenerator<wfn_t<64>> and <wfn_t<128>> implement every pure
 virtual of macis::HamiltonianGenerator, and GpuSparseOperator fits
 macis::davidson.  The reference's headers need the project's API shims
 (oracle/ref_shims) and its base.cxx; the test is skipped where the reference
-checkout is absent (QDK_REFERENCE names it)."""
+checkout is absent (QDK_REFERENCE names it; else a checkout named
+"reference" beside the repository is used)."""
 import os
 import shutil
 import subprocess
@@ -13,7 +14,7 @@ import pytest
 
 from conftest import ROOT
 
-REFERENCE = os.environ.get("QDK_REFERENCE") or "/root/reference"
+REFERENCE = os.environ.get("QDK_REFERENCE") or os.path.join(os.path.dirname(os.path.abspath(ROOT)), "reference")
 MACIS = os.path.join(REFERENCE, "external", "macis")
 
 
