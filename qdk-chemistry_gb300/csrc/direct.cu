@@ -23,6 +23,7 @@
 // Element values equal the CSR build's up to the rounding of the single
 // excitation's sum (A + W is summed in two parts here).
 #include <algorithm>
+#include <cstdlib>
 #include <unordered_map>
 #include <vector>
 
@@ -58,11 +59,23 @@ inline HSingle hsingle(uint64_t bra, uint64_t ket, uint64_t ex) {
 
 }  // namespace
 
+// FP32 opposite-spin contraction (k_ds_opposite_mm): E is formed in chunks
+// of kMmCols strings J_b by passes of kMmRows pair indices r, each thread
+// computing kMmTM x 8 entries of a pass (32 thread rows x 8 thread columns).
+constexpr int kMmCols = 64;
+constexpr int kMmTM = 4;
+constexpr int kMmRows = 32 * kMmTM;
+constexpr int kMmEStride = kMmCols + 4;  // row stride of E in shared memory (16-byte rows)
+
 struct SpinTables {
   int64_t nstr = 0;
   int ns = 0, nd = 0;
   DeviceBuffer sJ, svo, sA64, sA32, dJ, dval64, dval32, W64, W32;  // W over THIS spin's strings
   DeviceBuffer packed;  // singles packed as Jb | rs << 16 | neg << 31 (opposite-spin walk)
+  // the same singles as Jb | r << 16 | neg << 31 with r the compact pair
+  // index, each string's list sorted by (Jb / kMmCols, r / kMmRows, Jb, r),
+  // stored entry-major: [ns][nstr]
+  DeviceBuffer mm;
 };
 
 struct DirectSigma {
@@ -70,6 +83,13 @@ struct DirectSigma {
   SpinTables a, b;
   bool same = false;  // beta tables alias alpha's (same string set)
   DeviceBuffer V32, tmp64, tmp32, ct64, ct32;
+  // contraction form of the FP32 opposite-spin term: mr = n (n - 1) pair
+  // indices r (pairs (v, o), v != o, by ascending v + n o), mrp = mr rounded
+  // up to 16; V2mm[pq][r] = V(pq, rs_r) in FP32 (zero for r >= mr)
+  bool mm = false;
+  int mr = 0, mrp = 0;
+  size_t mm_smem = 0;
+  DeviceBuffer V2mm;
 };
 
 void free_direct(Context* c) {
@@ -77,9 +97,9 @@ void free_direct(Context* c) {
   DirectSigma* d = c->direct;
   for (SpinTables* t : {&d->a, &d->b})
     for (DeviceBuffer* b : {&t->sJ, &t->svo, &t->sA64, &t->sA32, &t->dJ, &t->dval64, &t->dval32, &t->W64, &t->W32,
-                            &t->packed})
+                            &t->packed, &t->mm})
       dev_free(c, *b);
-  for (DeviceBuffer* b : {&d->V32, &d->tmp64, &d->tmp32, &d->ct64, &d->ct32}) dev_free(c, *b);
+  for (DeviceBuffer* b : {&d->V32, &d->tmp64, &d->tmp32, &d->ct64, &d->ct32, &d->V2mm}) dev_free(c, *b);
   delete d;
   c->direct = nullptr;
 }
@@ -173,6 +193,28 @@ static void build_spin_tables(Context* c, const std::vector<uint64_t>& strs, Spi
   up(t.W64, W.data(), W.size() * 8);
   up(t.W32, W32.data(), W32.size() * 4);
   up(t.packed, packed.data(), packed.size() * 4);
+  // entry-major singles for the contraction form, each list sorted by
+  // (chunk of Jb, pass of r, Jb, r)
+  if (N <= 65535) {
+    std::vector<int32_t> rmap(nn * nn, -1);
+    int32_t m = 0;
+    for (size_t rs = 0; rs < nn * nn; ++rs)
+      if (rs % nn != rs / nn) rmap[rs] = m++;
+    std::vector<uint32_t> mm((size_t)N * ns);
+    std::vector<std::pair<uint64_t, uint32_t>> row(ns);
+    for (int64_t i = 0; i < N; ++i) {
+      for (int l = 0; l < ns; ++l) {
+        const uint32_t w = packed[(size_t)i * ns + l];
+        const uint32_t Jb = w & 0xffff, r = (uint32_t)rmap[(w >> 16) & 0x7fff];
+        const uint64_t key = ((uint64_t)(Jb / kMmCols) << 40) | ((uint64_t)(r / kMmRows) << 32) |
+                             ((uint64_t)Jb << 16) | r;
+        row[l] = {key, Jb | (r << 16) | (w & 0x80000000u)};
+      }
+      std::sort(row.begin(), row.end());
+      for (int l = 0; l < ns; ++l) mm[(size_t)l * N + i] = row[l].second;
+    }
+    up(t.mm, mm.data(), mm.size() * 4);
+  }
   QDKGB_CUDA(cudaStreamSynchronize(c->stream));
 }
 
@@ -270,6 +312,134 @@ __global__ void __launch_bounds__(kDsThreads)
   }
 }
 
+__device__ __forceinline__ void cp_async4_zfill(void* dst, const void* src, bool valid) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(sa), "l"(src), "r"(valid ? 4 : 0) : "memory");
+}
+
+// FP32 opposite-spin term as one contraction per alpha string (the
+// Knowles-Handy factorisation, restricted to the string's own singles).  For
+// alpha string Ia with singles k = (Ja_k, pq_k, s_k):
+//   E[r][Jb]       = sum_k s_k V(pq_k, rs_r) C[Ja_k, Jb]     (register-tiled FMAs)
+//   sigma[Ia, Ib] += sum_{l: beta single of Ib} s_l E[r_l][Jb_l]
+// r runs over the n(n - 1) pairs (v, o), v != o.  E is formed for every
+// (r, Jb): about n^2 / (k_b (n - k_b)) times the element count (3.7x at
+// CAS(14,14)), as FMAs with one shared-memory load per two to four of them,
+// where the element-wise walk spends two shared-memory gathers per element.
+// Jb runs in chunks of kMmCols (the chunk's C rows double-buffered by
+// cp.async), r in passes of kMmRows; after each pass every thread walks the
+// singles of its beta strings that fall in the (chunk, pass), in a fixed
+// order (the lists are sorted by it), so the sums are reproducible.
+// sigma[Ia, :] += diag * C[Ia, :] + the term; JPT beta strings per thread.
+template <int JPT>
+__global__ void __launch_bounds__(kDsThreads, 2)
+    k_ds_opposite_mm(int nb, int nsa, int nsb, int mr, int mrp, const int32_t* __restrict__ a_sJ,
+                     const int32_t* __restrict__ a_svo, const uint32_t* __restrict__ b_mm,
+                     const float* __restrict__ V2, int n, const double* __restrict__ D, const float* __restrict__ C,
+                     float* __restrict__ sigma) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float* Vp = (float*)smem_raw;                     // [nsa][mrp] signed integral rows
+  float* G = Vp + (size_t)nsa * mrp;                // [2][nsa][kMmCols] C rows of the singles' strings
+  float* E = G + (size_t)2 * nsa * kMmCols;         // [kMmRows][kMmEStride]
+  int32_t* Jrow = (int32_t*)(E + kMmRows * kMmEStride);  // [nsa]
+  const int64_t Ia = blockIdx.x;
+  const int tid = threadIdx.x, ty = tid >> 3, tx = tid & 7, warp = tid >> 5;
+  for (int i = tid; i < nsa * mrp; i += kDsThreads) {
+    const int k = i / mrp, r = i - k * mrp;
+    const int32_t vo = __ldg(a_svo + Ia * nsa + k);
+    const int pq = (vo & 0xff) + n * ((vo >> 8) & 0xff);
+    Vp[i] = negate_if<float>(__ldg(V2 + (size_t)pq * mrp + r), (vo >> 16) != 0);
+  }
+  for (int k = tid; k < nsa; k += kDsThreads) Jrow[k] = __ldg(a_sJ + Ia * nsa + k);
+  __syncthreads();
+  auto stage = [&](int chunk, int buf) {
+    const int j0 = chunk * kMmCols;
+    float* g = G + (size_t)buf * nsa * kMmCols;
+    for (int i = tid; i < nsa * kMmCols; i += kDsThreads) {
+      const int k = i / kMmCols, j = i - k * kMmCols;
+      const bool ok = j0 + j < nb;
+      cp_async4_zfill(g + i, C + (int64_t)Jrow[k] * nb + (ok ? j0 + j : 0), ok);
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+  };
+  float acc[JPT];
+  int cur[JPT];
+  uint32_t nxt[JPT];
+#pragma unroll
+  for (int j = 0; j < JPT; ++j) {
+    const int Ib = tid + j * kDsThreads;
+    acc[j] = 0.f;
+    cur[j] = 0;
+    nxt[j] = 0xffffffffu;
+    if (Ib < nb) {
+      acc[j] = sigma[Ia * nb + Ib] + (float)D[Ia * nb + Ib] * C[Ia * nb + Ib];
+      nxt[j] = __ldg(b_mm + Ib);
+    }
+  }
+  const int nchunk = (nb + kMmCols - 1) / kMmCols, npass = (mr + kMmRows - 1) / kMmRows;
+  stage(0, 0);
+  for (int c = 0; c < nchunk; ++c) {
+    const int j0 = c * kMmCols;
+    if (c + 1 < nchunk) {
+      stage(c + 1, (c + 1) & 1);
+      asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+    } else {
+      asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    }
+    __syncthreads();
+    const float* g = G + (size_t)(c & 1) * nsa * kMmCols;
+    for (int p = 0; p < npass; ++p) {
+      const int r0 = p * kMmRows;
+      if (r0 + warp * 16 < mr) {  // warp-uniform: this warp's 16 rows hold a valid pair
+        float a4[kMmTM][8];
+#pragma unroll
+        for (int i = 0; i < kMmTM; ++i)
+#pragma unroll
+          for (int jj = 0; jj < 8; ++jj) a4[i][jj] = 0.f;
+        const float* vrow = Vp + r0 + ty * kMmTM;
+        const float* grow = g + tx * 4;
+#pragma unroll 4
+        for (int k = 0; k < nsa; ++k) {
+          const float4 va = *(const float4*)(vrow + (size_t)k * mrp);
+          const float4 b0 = *(const float4*)(grow + k * kMmCols);
+          const float4 b1 = *(const float4*)(grow + k * kMmCols + 32);
+          const float av[4] = {va.x, va.y, va.z, va.w};
+          const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+          for (int i = 0; i < kMmTM; ++i)
+#pragma unroll
+            for (int jj = 0; jj < 8; ++jj) a4[i][jj] = fmaf(av[i], bv[jj], a4[i][jj]);
+        }
+#pragma unroll
+        for (int i = 0; i < kMmTM; ++i) {
+          float* e = E + (ty * kMmTM + i) * kMmEStride + tx * 4;
+          *(float4*)e = make_float4(a4[i][0], a4[i][1], a4[i][2], a4[i][3]);
+          *(float4*)(e + 32) = make_float4(a4[i][4], a4[i][5], a4[i][6], a4[i][7]);
+        }
+      }
+      __syncthreads();
+      // walk: the singles of this thread's beta strings in (chunk c, pass p)
+#pragma unroll
+      for (int j = 0; j < JPT; ++j) {
+        const int Ib = tid + j * kDsThreads;
+        while (cur[j] < nsb) {
+          const uint32_t w = nxt[j];
+          const int Jb = w & 0xffff, r = (w >> 16) & 0x7fff;
+          if (Jb >= j0 + kMmCols || r >= r0 + kMmRows) break;
+          acc[j] += negate_if<float>(E[(r - r0) * kMmEStride + (Jb - j0)], (w >> 31) != 0);
+          if (++cur[j] < nsb) nxt[j] = __ldg(b_mm + (size_t)cur[j] * nb + Ib);
+        }
+      }
+      __syncthreads();
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < JPT; ++j) {
+    const int Ib = tid + j * kDsThreads;
+    if (Ib < nb) sigma[Ia * nb + Ib] = acc[j];
+  }
+}
+
 // out (nc x nr) = in^T (in: nr x nc); add != 0: out += in^T
 template <typename T>
 __global__ void k_transpose(const T* __restrict__ in, T* __restrict__ out, int64_t nr, int64_t nc, int add) {
@@ -325,6 +495,29 @@ static void direct_sigma_t(Context* c, const T* x, T* y) {
   QDKGB_CHECK_LAUNCH();
   transpose<T>(c, tmp, y, nb, na, true);
   // opposite spin + diagonal
+  if constexpr (sizeof(T) == 4) {
+    if (d->mm) {
+      const uint32_t* bmm = (const uint32_t*)B.mm.ptr;
+      const int32_t* asJ = (const int32_t*)A.sJ.ptr;
+      const int32_t* asvo = (const int32_t*)A.svo.ptr;
+      const float* V2 = (const float*)d->V2mm.ptr;
+      const double* Dg = (const double*)c->H.diag.ptr;
+      auto go = [&](auto kern) {
+        kern<<<(unsigned)na, kDsThreads, d->mm_smem, c->stream>>>((int)nb, A.ns, B.ns, d->mr, d->mrp, asJ, asvo,
+                                                                 bmm, V2, d->n, Dg, (const float*)x, (float*)y);
+      };
+      if (nb <= 4 * kDsThreads)
+        go(k_ds_opposite_mm<4>);
+      else if (nb <= 8 * kDsThreads)
+        go(k_ds_opposite_mm<8>);
+      else if (nb <= 14 * kDsThreads)
+        go(k_ds_opposite_mm<14>);
+      else
+        go(k_ds_opposite_mm<16>);
+      QDKGB_CHECK_LAUNCH();
+      return;
+    }
+  }
   const T* Vt = f64 ? (const T*)c->V.ptr : (const T*)d->V32.ptr;
   constexpr int KC = f64 ? 4 : 8;
   const size_t smem = ((size_t)KC * nb + (size_t)KC * d->n * d->n) * sizeof(T);
@@ -381,6 +574,34 @@ void build_direct_sigma(Context* c) {
   QDKGB_CHECK_LAUNCH();
   set_max_dynamic_smem((const void*)k_ds_opposite<double, 4>, 200 * 1024);
   set_max_dynamic_smem((const void*)k_ds_opposite<float, 8>, 200 * 1024);
+  // contraction form of the FP32 opposite-spin term, where its tables and
+  // shared memory fit (QDKGB_DIRECT_MM=0 keeps the element-wise walk)
+  {
+    const SpinTables& A = d->a;
+    const SpinTables& B = d->same ? d->a : d->b;
+    const int n = d->n, n2 = n * n;
+    d->mr = n * (n - 1);
+    d->mrp = (d->mr + 15) / 16 * 16;
+    d->mm_smem = ((size_t)A.ns * d->mrp + (size_t)2 * A.ns * kMmCols + (size_t)kMmRows * kMmEStride) * 4 +
+                 (size_t)A.ns * 4;
+    const char* env = std::getenv("QDKGB_DIRECT_MM");
+    const bool off = env && env[0] == '0';
+    d->mm = !off && B.mm.ptr != nullptr && B.ns > 0 && A.ns > 0 && d->mm_smem <= 200 * 1024;
+    if (d->mm) {
+      std::vector<float> v2((size_t)n2 * d->mrp, 0.f);
+      for (int pq = 0; pq < n2; ++pq) {
+        int r = 0;
+        for (int rs = 0; rs < n2; ++rs)
+          if (rs % n != rs / n) v2[(size_t)pq * d->mrp + r++] = (float)c->h_V[pq + (size_t)n2 * rs];
+      }
+      float* V2 = dev_array<float>(c, d->V2mm, v2.size());
+      QDKGB_CUDA(cudaMemcpyAsync(V2, v2.data(), v2.size() * 4, cudaMemcpyHostToDevice, c->stream));
+      set_max_dynamic_smem((const void*)k_ds_opposite_mm<4>, 200 * 1024);
+      set_max_dynamic_smem((const void*)k_ds_opposite_mm<8>, 200 * 1024);
+      set_max_dynamic_smem((const void*)k_ds_opposite_mm<14>, 200 * 1024);
+      set_max_dynamic_smem((const void*)k_ds_opposite_mm<16>, 200 * 1024);
+    }
+  }
   QDKGB_CUDA(cudaStreamSynchronize(c->stream));
   H.n = N;
   H.nnz = 0;

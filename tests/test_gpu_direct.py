@@ -39,6 +39,35 @@ def test_direct_sigma_matches_csr(ctx, pkg, norb, na, nb, seed):
         ctx.get_csr()
 
 
+@pytest.mark.parametrize("norb,na,nb,seed", [(12, 3, 3, 11), (12, 3, 4, 12), (11, 5, 5, 13), (7, 3, 2, 14)])
+def test_direct_fp32_contraction_matches_walk(ctx, pkg, monkeypatch, norb, na, nb, seed):
+    """The FP32 opposite-spin term as a per-alpha-string contraction (the
+    default) and as the element-wise walk (QDKGB_DIRECT_MM=0) both agree
+    with the CSR sigma to FP32 accuracy; shapes with more than one chunk of
+    beta strings, more than one pass of pair indices (n >= 12) and unequal
+    string sets."""
+    capi = pkg.capi
+    T, V, _ = pkg.integrals.synthetic_integrals(norb, 2 * norb, seed)
+    a, b = capi.fci_dets(norb, na, nb)
+    ctx.set_integrals(T, V)
+    ctx.set_dets(a, b)
+    ctx.build_hamiltonian(0.0)
+    x = np.random.default_rng(seed).normal(size=len(a))
+    y_csr = ctx.spmv(x, capi.PREC_FP64)
+    scale = np.max(np.abs(y_csr))
+    ys = {}
+    for mm in ("1", "0"):
+        monkeypatch.setenv("QDKGB_DIRECT_MM", mm)
+        ctx.build_direct_sigma()
+        ys[mm] = ctx.spmv(x, capi.PREC_MIXED)
+        assert np.max(np.abs(ys[mm] - y_csr)) / scale < 1e-5, mm
+    y2 = ctx.spmv(x, capi.PREC_MIXED)
+    assert np.array_equal(y2, ys["0"])
+    monkeypatch.setenv("QDKGB_DIRECT_MM", "1")
+    ctx.build_direct_sigma()
+    assert np.array_equal(ctx.spmv(x, capi.PREC_MIXED), ys["1"])  # reproducible
+
+
 def test_direct_davidson_fp64_and_mixed(ctx, pkg, oracle):
     capi = pkg.capi
     T, V, _ = pkg.integrals.synthetic_integrals(10, 20, seed=9)
