@@ -24,6 +24,7 @@
 // excitation's sum (A + W is summed in two parts here).
 #include <algorithm>
 #include <cstdlib>
+#include <cstring>
 #include <unordered_map>
 #include <vector>
 
@@ -59,23 +60,18 @@ inline HSingle hsingle(uint64_t bra, uint64_t ket, uint64_t ex) {
 
 }  // namespace
 
-// FP32 opposite-spin contraction (k_ds_opposite_mm): E is formed in chunks
-// of kMmCols strings J_b by passes of kMmRows pair indices r, each thread
-// computing kMmTM x 8 entries of a pass (32 thread rows x 8 thread columns).
+// FP32 contraction form (k_ds_opposite_mm): beta strings J_b in chunks of
+// kMmCols; E rows 16 per warp, each thread 4 rows x 8 columns.
 constexpr int kMmCols = 64;
-constexpr int kMmTM = 4;
-constexpr int kMmRows = 32 * kMmTM;
 constexpr int kMmEStride = kMmCols + 4;  // row stride of E in shared memory (16-byte rows)
+constexpr int kMmMaxWarps = 16;
 
 struct SpinTables {
   int64_t nstr = 0;
   int ns = 0, nd = 0;
   DeviceBuffer sJ, svo, sA64, sA32, dJ, dval64, dval32, W64, W32;  // W over THIS spin's strings
   DeviceBuffer packed;  // singles packed as Jb | rs << 16 | neg << 31 (opposite-spin walk)
-  // the same singles as Jb | r << 16 | neg << 31 with r the compact pair
-  // index, each string's list sorted by (Jb / kMmCols, r / kMmRows, Jb, r),
-  // stored entry-major: [ns][nstr]
-  DeviceBuffer mm;
+  std::vector<uint32_t> h_packed;  // host copy of `packed` while the contraction tables are built
 };
 
 struct DirectSigma {
@@ -83,13 +79,20 @@ struct DirectSigma {
   SpinTables a, b;
   bool same = false;  // beta tables alias alpha's (same string set)
   DeviceBuffer V32, tmp64, tmp32, ct64, ct32;
-  // contraction form of the FP32 opposite-spin term: mr = n (n - 1) pair
-  // indices r (pairs (v, o), v != o, by ascending v + n o), mrp = mr rounded
-  // up to 16; V2mm[pq][r] = V(pq, rs_r) in FP32 (zero for r >= mr)
+  // contraction form of the FP32 sigma (k_ds_opposite_mm).  Rows r of E:
+  //   r < mr          pair (v, o), v != o, by ascending v + n o (mr = n (n - 1))
+  //   mr + p, p < n   the other spin's occupied orbital p (single excitations' W part)
+  //   mr + n          the string-only part of the alpha singles
+  // mrows = mr + n + 1 rounded up to 16 is mrp (one warp per 16 rows).
+  // V2mm[pq][r]: V(pq, rs_r) for r < mr, V(p p | pq) for r = mr + p, else 0.
+  // lists: per chunk of kMmCols beta strings, the (nb + 1) uint16 offsets of
+  // each beta string's entries (padded to 16 bytes) then the entries
+  // jl | r << 8 | neg << 31 (jl = J_b - chunk start), each string's sorted by
+  // (J_b, r); seg[c] = the chunk's first 4-byte word (16-byte aligned)
   bool mm = false;
-  int mr = 0, mrp = 0;
+  int mr = 0, mrp = 0, mm_threads = 0, mm_jpt = 0, seg_max = 0, off_words = 0;
   size_t mm_smem = 0;
-  DeviceBuffer V2mm;
+  DeviceBuffer V2mm, rs_of, lists, seg;
 };
 
 void free_direct(Context* c) {
@@ -97,9 +100,10 @@ void free_direct(Context* c) {
   DirectSigma* d = c->direct;
   for (SpinTables* t : {&d->a, &d->b})
     for (DeviceBuffer* b : {&t->sJ, &t->svo, &t->sA64, &t->sA32, &t->dJ, &t->dval64, &t->dval32, &t->W64, &t->W32,
-                            &t->packed, &t->mm})
+                            &t->packed})
       dev_free(c, *b);
-  for (DeviceBuffer* b : {&d->V32, &d->tmp64, &d->tmp32, &d->ct64, &d->ct32, &d->V2mm}) dev_free(c, *b);
+  for (DeviceBuffer* b : {&d->V32, &d->tmp64, &d->tmp32, &d->ct64, &d->ct32, &d->V2mm, &d->rs_of, &d->lists, &d->seg})
+    dev_free(c, *b);
   delete d;
   c->direct = nullptr;
 }
@@ -193,34 +197,13 @@ static void build_spin_tables(Context* c, const std::vector<uint64_t>& strs, Spi
   up(t.W64, W.data(), W.size() * 8);
   up(t.W32, W32.data(), W32.size() * 4);
   up(t.packed, packed.data(), packed.size() * 4);
-  // entry-major singles for the contraction form, each list sorted by
-  // (chunk of Jb, pass of r, Jb, r)
-  if (N <= 65535) {
-    std::vector<int32_t> rmap(nn * nn, -1);
-    int32_t m = 0;
-    for (size_t rs = 0; rs < nn * nn; ++rs)
-      if (rs % nn != rs / nn) rmap[rs] = m++;
-    std::vector<uint32_t> mm((size_t)N * ns);
-    std::vector<std::pair<uint64_t, uint32_t>> row(ns);
-    for (int64_t i = 0; i < N; ++i) {
-      for (int l = 0; l < ns; ++l) {
-        const uint32_t w = packed[(size_t)i * ns + l];
-        const uint32_t Jb = w & 0xffff, r = (uint32_t)rmap[(w >> 16) & 0x7fff];
-        const uint64_t key = ((uint64_t)(Jb / kMmCols) << 40) | ((uint64_t)(r / kMmRows) << 32) |
-                             ((uint64_t)Jb << 16) | r;
-        row[l] = {key, Jb | (r << 16) | (w & 0x80000000u)};
-      }
-      std::sort(row.begin(), row.end());
-      for (int l = 0; l < ns; ++l) mm[(size_t)l * N + i] = row[l].second;
-    }
-    up(t.mm, mm.data(), mm.size() * 4);
-  }
+  t.h_packed = std::move(packed);
   QDKGB_CUDA(cudaStreamSynchronize(c->stream));
 }
 
 // out[I, col] (+)= sum over same-spin doubles and singles of row string I
 // (rows: strings of this spin; cols: strings of the other spin; W over the
-// other spin's strings).
+// other spin's strings; W null: the singles' string-only part A alone).
 template <typename T>
 __global__ void __launch_bounds__(kDsThreads)
     k_ds_same_spin(int64_t nrow, int64_t ncol, int ns, int nd, const int32_t* __restrict__ sJ,
@@ -235,7 +218,8 @@ __global__ void __launch_bounds__(kDsThreads)
     for (int m = 0; m < ns; ++m) {
       const int32_t vo = __ldg(svo + I * ns + m);
       const int v = vo & 0xff, o = (vo >> 8) & 0xff;
-      T coef = __ldg(sA + I * ns + m) + __ldg(W + (int64_t)(v + n * o) * ncol + col);
+      T coef = __ldg(sA + I * ns + m);
+      if (W) coef += __ldg(W + (int64_t)(v + n * o) * ncol + col);
       if (vo >> 16) coef = -coef;
       acc += coef * __ldg(C + (int64_t)__ldg(sJ + I * ns + m) * ncol + col);
     }
@@ -317,125 +301,138 @@ __device__ __forceinline__ void cp_async4_zfill(void* dst, const void* src, bool
   asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(sa), "l"(src), "r"(valid ? 4 : 0) : "memory");
 }
 
-// FP32 opposite-spin term as one contraction per alpha string (the
-// Knowles-Handy factorisation, restricted to the string's own singles).  For
-// alpha string Ia with singles k = (Ja_k, pq_k, s_k):
-//   E[r][Jb]       = sum_k s_k V(pq_k, rs_r) C[Ja_k, Jb]     (register-tiled FMAs)
-//   sigma[Ia, Ib] += sum_{l: beta single of Ib} s_l E[r_l][Jb_l]
-// r runs over the n(n - 1) pairs (v, o), v != o.  E is formed for every
-// (r, Jb): about n^2 / (k_b (n - k_b)) times the element count (3.7x at
-// CAS(14,14)), as FMAs with one shared-memory load per two to four of them,
-// where the element-wise walk spends two shared-memory gathers per element.
-// Jb runs in chunks of kMmCols (the chunk's C rows double-buffered by
-// cp.async), r in passes of kMmRows; after each pass every thread walks the
-// singles of its beta strings that fall in the (chunk, pass), in a fixed
-// order (the lists are sorted by it), so the sums are reproducible.
-// sigma[Ia, :] += diag * C[Ia, :] + the term; JPT beta strings per thread.
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(src) : "memory");
+}
+
+// FP32 sigma terms that couple the two spins, as one contraction per alpha
+// string (the Knowles-Handy factorisation restricted to the string's own
+// singles).  For alpha string Ia with singles k = (Ja_k, pq_k, s_k), and
+// k = own (Ja = Ia):
+//   E[r][Jb] = sum_k Vp[k][r] C[Ja_k, Jb]                 (register-tiled FMAs)
+//     Vp[k][r]      = s_k V(pq_k, rs_r)         pair rows
+//     Vp[k][mr + p] = s_k V(p p | pq_k)         W rows
+//     Vp[k][mr + n] = s_k A(Ia, Ja_k)           string-only singles row
+//     Vp[own][r]    = W_a[rs_r](Ia)             (beta singles' W part)
+//   sigma[Ia, Ib] += sum_{l: beta single of Ib} s_l E[r_l][Jb_l]       opposite spin + beta W part
+//                  + sum_{p in Ib} E[mr + p][Ib] + E[mr + n][Ib]       alpha singles
+// so one kernel applies the opposite-spin doubles and every single
+// excitation except the beta singles' string-only part.  E is formed for
+// every (r, Jb), n^2 / (k_b (n - k_b)) times the opposite-spin element count
+// (3.7x at CAS(14,14)), as FMAs with three shared-memory wavefronts per 32 of
+// them, where the element-wise walk spends two shared-memory gathers per
+// element.  J_b runs in chunks of kMmCols: the chunk's C rows and walk lists
+// are copied (cp.async) while the previous chunk is formed; every warp forms
+// 16 rows of E; then each thread walks its beta strings' entries of the
+// chunk in the lists' fixed order, so the sums are reproducible.
+// sigma[Ia, :] += diag * C[Ia, :] + the terms; JPT beta strings per thread.
 template <int JPT>
-__global__ void __launch_bounds__(kDsThreads, 2)
-    k_ds_opposite_mm(int nb, int nsa, int nsb, int mr, int mrp, const int32_t* __restrict__ a_sJ,
-                     const int32_t* __restrict__ a_svo, const uint32_t* __restrict__ b_mm,
+__global__ void __launch_bounds__(kMmMaxWarps * 32)
+    k_ds_opposite_mm(int na, int nb, int nsa, int mr, int mrp, int off_words, int seg_max,
+                     const int32_t* __restrict__ a_sJ, const int32_t* __restrict__ a_svo,
+                     const float* __restrict__ a_sA, const float* __restrict__ a_W, const int32_t* __restrict__ rs_of,
+                     const uint32_t* __restrict__ lists, const int32_t* __restrict__ seg,
                      const float* __restrict__ V2, int n, const double* __restrict__ D, const float* __restrict__ C,
                      float* __restrict__ sigma) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  float* Vp = (float*)smem_raw;                     // [nsa][mrp] signed integral rows
-  float* G = Vp + (size_t)nsa * mrp;                // [2][nsa][kMmCols] C rows of the singles' strings
-  float* E = G + (size_t)2 * nsa * kMmCols;         // [kMmRows][kMmEStride]
-  int32_t* Jrow = (int32_t*)(E + kMmRows * kMmEStride);  // [nsa]
+  const int K = nsa + 1;
+  float* Vp = (float*)smem_raw;                          // [K][mrp]
+  float* G = Vp + (size_t)K * mrp;                       // [2][K][kMmCols]
+  float* E = G + (size_t)2 * K * kMmCols;                // [mrp][kMmEStride]
+  uint32_t* L = (uint32_t*)(E + (size_t)mrp * kMmEStride);  // [2][seg_max]
+  int32_t* Jrow = (int32_t*)(L + (size_t)2 * seg_max);   // [K]
   const int64_t Ia = blockIdx.x;
-  const int tid = threadIdx.x, ty = tid >> 3, tx = tid & 7, warp = tid >> 5;
-  for (int i = tid; i < nsa * mrp; i += kDsThreads) {
+  const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31, warp = tid >> 5;
+  const int ty = lane >> 3, tx = lane & 7;
+  for (int i = tid; i < K * mrp; i += nthr) {
     const int k = i / mrp, r = i - k * mrp;
-    const int32_t vo = __ldg(a_svo + Ia * nsa + k);
-    const int pq = (vo & 0xff) + n * ((vo >> 8) & 0xff);
-    Vp[i] = negate_if<float>(__ldg(V2 + (size_t)pq * mrp + r), (vo >> 16) != 0);
+    float v = 0.f;
+    if (k < nsa) {
+      const int32_t vo = __ldg(a_svo + Ia * nsa + k);
+      const int pq = (vo & 0xff) + n * ((vo >> 8) & 0xff);
+      v = (r == mr + n) ? __ldg(a_sA + Ia * nsa + k) : __ldg(V2 + (size_t)pq * mrp + r);
+      v = negate_if<float>(v, (vo >> 16) != 0);
+    } else if (r < mr) {
+      v = __ldg(a_W + (int64_t)__ldg(rs_of + r) * na + Ia);
+    }
+    Vp[i] = v;
   }
-  for (int k = tid; k < nsa; k += kDsThreads) Jrow[k] = __ldg(a_sJ + Ia * nsa + k);
+  for (int k = tid; k < K; k += nthr) Jrow[k] = k < nsa ? __ldg(a_sJ + Ia * nsa + k) : (int32_t)Ia;
   __syncthreads();
   auto stage = [&](int chunk, int buf) {
     const int j0 = chunk * kMmCols;
-    float* g = G + (size_t)buf * nsa * kMmCols;
-    for (int i = tid; i < nsa * kMmCols; i += kDsThreads) {
+    float* g = G + (size_t)buf * K * kMmCols;
+    for (int i = tid; i < K * kMmCols; i += nthr) {
       const int k = i / kMmCols, j = i - k * kMmCols;
       const bool ok = j0 + j < nb;
       cp_async4_zfill(g + i, C + (int64_t)Jrow[k] * nb + (ok ? j0 + j : 0), ok);
     }
+    const int w0 = __ldg(seg + chunk), nv = (__ldg(seg + chunk + 1) - w0) >> 2;
+    uint32_t* l = L + (size_t)buf * seg_max;
+    for (int i = tid; i < nv; i += nthr) cp_async16(l + 4 * i, lists + w0 + 4 * i);
     asm volatile("cp.async.commit_group;\n" ::: "memory");
   };
   float acc[JPT];
-  int cur[JPT];
-  uint32_t nxt[JPT];
 #pragma unroll
   for (int j = 0; j < JPT; ++j) {
-    const int Ib = tid + j * kDsThreads;
-    acc[j] = 0.f;
-    cur[j] = 0;
-    nxt[j] = 0xffffffffu;
-    if (Ib < nb) {
-      acc[j] = sigma[Ia * nb + Ib] + (float)D[Ia * nb + Ib] * C[Ia * nb + Ib];
-      nxt[j] = __ldg(b_mm + Ib);
-    }
+    const int Ib = tid + j * nthr;
+    acc[j] = Ib < nb ? sigma[Ia * nb + Ib] + (float)D[Ia * nb + Ib] * C[Ia * nb + Ib] : 0.f;
   }
-  const int nchunk = (nb + kMmCols - 1) / kMmCols, npass = (mr + kMmRows - 1) / kMmRows;
+  const int nchunk = (nb + kMmCols - 1) / kMmCols;
   stage(0, 0);
   for (int c = 0; c < nchunk; ++c) {
-    const int j0 = c * kMmCols;
-    if (c + 1 < nchunk) {
-      stage(c + 1, (c + 1) & 1);
-      asm volatile("cp.async.wait_group 1;\n" ::: "memory");
-    } else {
-      asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    __syncthreads();  // chunk c staged by every thread; E and buffer (c + 1) & 1 free
+    if (c + 1 < nchunk) stage(c + 1, (c + 1) & 1);
+    {
+      const float* vrow = Vp + warp * 16 + ty * 4;
+      const float* grow = G + (size_t)(c & 1) * K * kMmCols + tx * 4;
+      float a4[4][8];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int jj = 0; jj < 8; ++jj) a4[i][jj] = 0.f;
+#pragma unroll 4
+      for (int k = 0; k < K; ++k) {
+        const float4 va = *(const float4*)(vrow + (size_t)k * mrp);
+        const float4 b0 = *(const float4*)(grow + k * kMmCols);
+        const float4 b1 = *(const float4*)(grow + k * kMmCols + 32);
+        const float av[4] = {va.x, va.y, va.z, va.w};
+        const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int jj = 0; jj < 8; ++jj) a4[i][jj] = fmaf(av[i], bv[jj], a4[i][jj]);
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        float* e = E + (size_t)(warp * 16 + ty * 4 + i) * kMmEStride + tx * 4;
+        *(float4*)e = make_float4(a4[i][0], a4[i][1], a4[i][2], a4[i][3]);
+        *(float4*)(e + 32) = make_float4(a4[i][4], a4[i][5], a4[i][6], a4[i][7]);
+      }
     }
     __syncthreads();
-    const float* g = G + (size_t)(c & 1) * nsa * kMmCols;
-    for (int p = 0; p < npass; ++p) {
-      const int r0 = p * kMmRows;
-      if (r0 + warp * 16 < mr) {  // warp-uniform: this warp's 16 rows hold a valid pair
-        float a4[kMmTM][8];
+    const uint32_t* l = L + (size_t)(c & 1) * seg_max;
+    const uint16_t* off = (const uint16_t*)l;
+    const uint32_t* ent = l + off_words;
 #pragma unroll
-        for (int i = 0; i < kMmTM; ++i)
-#pragma unroll
-          for (int jj = 0; jj < 8; ++jj) a4[i][jj] = 0.f;
-        const float* vrow = Vp + r0 + ty * kMmTM;
-        const float* grow = g + tx * 4;
-#pragma unroll 4
-        for (int k = 0; k < nsa; ++k) {
-          const float4 va = *(const float4*)(vrow + (size_t)k * mrp);
-          const float4 b0 = *(const float4*)(grow + k * kMmCols);
-          const float4 b1 = *(const float4*)(grow + k * kMmCols + 32);
-          const float av[4] = {va.x, va.y, va.z, va.w};
-          const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
-#pragma unroll
-          for (int i = 0; i < kMmTM; ++i)
-#pragma unroll
-            for (int jj = 0; jj < 8; ++jj) a4[i][jj] = fmaf(av[i], bv[jj], a4[i][jj]);
+    for (int j = 0; j < JPT; ++j) {
+      const int Ib = tid + j * nthr;
+      if (Ib < nb) {
+        const int e1 = off[Ib + 1];
+        float a = acc[j];
+        for (int e = off[Ib]; e < e1; ++e) {
+          const uint32_t w = ent[e];
+          a += negate_if<float>(E[((w >> 8) & 0x7fff) * kMmEStride + (w & 0xff)], (w >> 31) != 0);
         }
-#pragma unroll
-        for (int i = 0; i < kMmTM; ++i) {
-          float* e = E + (ty * kMmTM + i) * kMmEStride + tx * 4;
-          *(float4*)e = make_float4(a4[i][0], a4[i][1], a4[i][2], a4[i][3]);
-          *(float4*)(e + 32) = make_float4(a4[i][4], a4[i][5], a4[i][6], a4[i][7]);
-        }
+        acc[j] = a;
       }
-      __syncthreads();
-      // walk: the singles of this thread's beta strings in (chunk c, pass p)
-#pragma unroll
-      for (int j = 0; j < JPT; ++j) {
-        const int Ib = tid + j * kDsThreads;
-        while (cur[j] < nsb) {
-          const uint32_t w = nxt[j];
-          const int Jb = w & 0xffff, r = (w >> 16) & 0x7fff;
-          if (Jb >= j0 + kMmCols || r >= r0 + kMmRows) break;
-          acc[j] += negate_if<float>(E[(r - r0) * kMmEStride + (Jb - j0)], (w >> 31) != 0);
-          if (++cur[j] < nsb) nxt[j] = __ldg(b_mm + (size_t)cur[j] * nb + Ib);
-        }
-      }
-      __syncthreads();
     }
   }
 #pragma unroll
   for (int j = 0; j < JPT; ++j) {
-    const int Ib = tid + j * kDsThreads;
+    const int Ib = tid + j * nthr;
     if (Ib < nb) sigma[Ia * nb + Ib] = acc[j];
   }
 }
@@ -479,41 +476,43 @@ static void direct_sigma_t(Context* c, const T* x, T* y) {
   const SpinTables& B = d->same ? d->a : d->b;
   const int64_t na = A.nstr, nb = B.nstr, N = na * nb;
   const bool f64 = sizeof(T) == 8;
+  // the contraction form applies every single excitation but the beta
+  // singles' string-only part, so the same-spin kernels then take the
+  // doubles (alpha) and the doubles plus string-only singles (beta)
+  const bool mm = !f64 && d->mm;
   auto P = [&](const DeviceBuffer& b64, const DeviceBuffer& b32) { return (const T*)(f64 ? b64.ptr : b32.ptr); };
   T* ct = (T*)dev_alloc(c, f64 ? d->ct64 : d->ct32, N * sizeof(T));
   T* tmp = (T*)dev_alloc(c, f64 ? d->tmp64 : d->tmp32, N * sizeof(T));
   // alpha-alpha into y
   k_ds_same_spin<T><<<(unsigned)na, kDsThreads, 0, c->stream>>>(
-      na, nb, A.ns, A.nd, (const int32_t*)A.sJ.ptr, (const int32_t*)A.svo.ptr, P(A.sA64, A.sA32),
+      na, nb, mm ? 0 : A.ns, A.nd, (const int32_t*)A.sJ.ptr, (const int32_t*)A.svo.ptr, P(A.sA64, A.sA32),
       (const int32_t*)A.dJ.ptr, P(A.dval64, A.dval32), P(B.W64, B.W32), d->n, x, y);
   QDKGB_CHECK_LAUNCH();
   // beta-beta on C^T, added back transposed
   transpose<T>(c, x, ct, na, nb, false);
   k_ds_same_spin<T><<<(unsigned)nb, kDsThreads, 0, c->stream>>>(
       nb, na, B.ns, B.nd, (const int32_t*)B.sJ.ptr, (const int32_t*)B.svo.ptr, P(B.sA64, B.sA32),
-      (const int32_t*)B.dJ.ptr, P(B.dval64, B.dval32), P(A.W64, A.W32), d->n, ct, tmp);
+      (const int32_t*)B.dJ.ptr, P(B.dval64, B.dval32), mm ? nullptr : P(A.W64, A.W32), d->n, ct, tmp);
   QDKGB_CHECK_LAUNCH();
   transpose<T>(c, tmp, y, nb, na, true);
-  // opposite spin + diagonal
+  // opposite spin + diagonal (+ the singles, contraction form)
   if constexpr (sizeof(T) == 4) {
-    if (d->mm) {
-      const uint32_t* bmm = (const uint32_t*)B.mm.ptr;
-      const int32_t* asJ = (const int32_t*)A.sJ.ptr;
-      const int32_t* asvo = (const int32_t*)A.svo.ptr;
-      const float* V2 = (const float*)d->V2mm.ptr;
-      const double* Dg = (const double*)c->H.diag.ptr;
+    if (mm) {
       auto go = [&](auto kern) {
-        kern<<<(unsigned)na, kDsThreads, d->mm_smem, c->stream>>>((int)nb, A.ns, B.ns, d->mr, d->mrp, asJ, asvo,
-                                                                 bmm, V2, d->n, Dg, (const float*)x, (float*)y);
+        kern<<<(unsigned)na, d->mm_threads, d->mm_smem, c->stream>>>(
+            (int)na, (int)nb, A.ns, d->mr, d->mrp, d->off_words, d->seg_max, (const int32_t*)A.sJ.ptr,
+            (const int32_t*)A.svo.ptr, (const float*)A.sA32.ptr, (const float*)A.W32.ptr, (const int32_t*)d->rs_of.ptr,
+            (const uint32_t*)d->lists.ptr, (const int32_t*)d->seg.ptr, (const float*)d->V2mm.ptr, d->n,
+            (const double*)c->H.diag.ptr, (const float*)x, (float*)y);
       };
-      if (nb <= 4 * kDsThreads)
-        go(k_ds_opposite_mm<4>);
-      else if (nb <= 8 * kDsThreads)
-        go(k_ds_opposite_mm<8>);
-      else if (nb <= 14 * kDsThreads)
-        go(k_ds_opposite_mm<14>);
-      else
-        go(k_ds_opposite_mm<16>);
+      switch (d->mm_jpt) {
+        case 1: go(k_ds_opposite_mm<1>); break;
+        case 2: go(k_ds_opposite_mm<2>); break;
+        case 4: go(k_ds_opposite_mm<4>); break;
+        case 8: go(k_ds_opposite_mm<8>); break;
+        case 12: go(k_ds_opposite_mm<12>); break;
+        default: go(k_ds_opposite_mm<16>); break;
+      }
       QDKGB_CHECK_LAUNCH();
       return;
     }
@@ -536,6 +535,115 @@ __global__ void k_diag_product(Integrals I, int64_t na, int64_t nb, const uint64
     const uint64_t a = sa[r / nb];
     D[r] = a ? me_diag(I, a, sb[r % nb]) : 0.;
   }
+}
+
+// Tables of the contraction form (k_ds_opposite_mm); leaves d->mm false
+// where they do not apply.
+static void build_mm_tables(Context* c, DirectSigma* d) {
+  d->mm = false;
+  const char* env = std::getenv("QDKGB_DIRECT_MM");
+  if (env && env[0] == '0') return;
+  const SpinTables& A = d->a;
+  const SpinTables& B = d->same ? d->a : d->b;
+  const int n = d->n, n2 = n * n;
+  const int64_t nb = B.nstr;
+  if (A.ns <= 0 || B.ns <= 0 || B.h_packed.size() != (size_t)nb * B.ns) return;
+  const int mr = n * (n - 1), mrows = mr + n + 1, mrp = (mrows + 15) / 16 * 16;
+  const int warps = mrp / 16;
+  if (warps > kMmMaxWarps || mrows >= (1 << 15)) return;
+  const int threads = warps * 32;
+  int jpt = (int)((nb + threads - 1) / threads);
+  for (int cand : {1, 2, 4, 8, 12, 16})
+    if (jpt <= cand) {
+      jpt = cand;
+      break;
+    }
+  if ((int64_t)jpt * threads < nb) return;
+  // pair index of each (v, o), v != o
+  std::vector<int32_t> rmap(n2, -1), rs_of(mr);
+  for (int rs = 0, r = 0; rs < n2; ++rs)
+    if (rs % n != rs / n) {
+      rmap[rs] = r;
+      rs_of[r++] = rs;
+    }
+  // per chunk: offsets (uint16) and entries of every beta string
+  const int nchunk = (int)((nb + kMmCols - 1) / kMmCols);
+  const int off_words = (int)(((nb + 1) + 1) / 2 + 3) / 4 * 4;
+  std::vector<std::vector<std::pair<uint32_t, uint32_t>>> per(nb);  // (sort key, entry) by string
+  for (int64_t ib = 0; ib < nb; ++ib) {
+    auto& v = per[ib];
+    for (int l = 0; l < B.ns; ++l) {
+      const uint32_t w = B.h_packed[(size_t)ib * B.ns + l];
+      const uint32_t Jb = w & 0xffff, r = (uint32_t)rmap[(w >> 16) & 0x7fff];
+      v.push_back({(Jb << 16) | r, Jb | (r << 16) | (w & 0x80000000u)});
+    }
+    const uint64_t bits = c->dets.h_ubeta[ib];
+    for (int p = 0; p < n; ++p)
+      if ((bits >> p) & 1) v.push_back({((uint32_t)ib << 16) | (uint32_t)(mr + p), (uint32_t)ib | ((uint32_t)(mr + p) << 16)});
+    v.push_back({((uint32_t)ib << 16) | (uint32_t)(mr + n), (uint32_t)ib | ((uint32_t)(mr + n) << 16)});
+    std::sort(v.begin(), v.end());
+  }
+  std::vector<uint32_t> lists;
+  std::vector<int32_t> seg(nchunk + 1);
+  std::vector<size_t> cur(nb, 0);
+  int seg_max = 0;
+  for (int ch = 0; ch < nchunk; ++ch) {
+    const uint32_t j0 = (uint32_t)ch * kMmCols, j1 = j0 + kMmCols;
+    seg[ch] = (int32_t)lists.size();
+    std::vector<uint16_t> off(nb + 1);
+    std::vector<uint32_t> ent;
+    for (int64_t ib = 0; ib < nb; ++ib) {
+      off[ib] = (uint16_t)ent.size();
+      auto& v = per[ib];
+      while (cur[ib] < v.size() && (v[cur[ib]].second & 0xffff) < j1) {
+        const uint32_t w = v[cur[ib]++].second;
+        const uint32_t jl = (w & 0xffff) - j0, r = (w >> 16) & 0x7fff;
+        ent.push_back(jl | (r << 8) | (w & 0x80000000u));
+      }
+      if (ent.size() > 65535) return;
+    }
+    off[nb] = (uint16_t)ent.size();
+    std::vector<uint32_t> words(off_words, 0);
+    std::memcpy(words.data(), off.data(), off.size() * 2);
+    lists.insert(lists.end(), words.begin(), words.end());
+    lists.insert(lists.end(), ent.begin(), ent.end());
+    while (lists.size() % 4) lists.push_back(0);
+    seg_max = std::max(seg_max, (int)(lists.size() - seg[ch]));
+  }
+  seg[nchunk] = (int32_t)lists.size();
+  if (lists.size() >= (size_t)INT32_MAX) return;
+  const int K = A.ns + 1;
+  const size_t smem = ((size_t)K * mrp + (size_t)2 * K * kMmCols + (size_t)mrp * kMmEStride) * 4 +
+                      (size_t)2 * seg_max * 4 + (size_t)K * 4;
+  if (smem > 220 * 1024) return;
+  // V2mm[pq][r]
+  std::vector<float> v2((size_t)n2 * mrp, 0.f);
+  const std::vector<double>& V = c->h_V;
+  for (int pq = 0; pq < n2; ++pq) {
+    for (int r = 0; r < mr; ++r) v2[(size_t)pq * mrp + r] = (float)V[pq + (size_t)n2 * rs_of[r]];
+    for (int p = 0; p < n; ++p) v2[(size_t)pq * mrp + mr + p] = (float)V[p + (size_t)n * p + (size_t)n2 * pq];
+  }
+  auto up = [&](DeviceBuffer& b, const void* src, size_t bytes) {
+    void* ptr = dev_alloc(c, b, bytes + 16);
+    QDKGB_CUDA(cudaMemcpyAsync(ptr, src, bytes, cudaMemcpyHostToDevice, c->stream));
+  };
+  up(d->V2mm, v2.data(), v2.size() * 4);
+  up(d->rs_of, rs_of.data(), rs_of.size() * 4);
+  up(d->lists, lists.data(), lists.size() * 4);
+  up(d->seg, seg.data(), seg.size() * 4);
+  for (const void* f : {(const void*)k_ds_opposite_mm<1>, (const void*)k_ds_opposite_mm<2>,
+                        (const void*)k_ds_opposite_mm<4>, (const void*)k_ds_opposite_mm<8>,
+                        (const void*)k_ds_opposite_mm<12>, (const void*)k_ds_opposite_mm<16>})
+    set_max_dynamic_smem(f, 220 * 1024);
+  d->mr = mr;
+  d->mrp = mrp;
+  d->mm_threads = threads;
+  d->mm_jpt = jpt;
+  d->seg_max = seg_max;
+  d->off_words = off_words;
+  d->mm_smem = smem;
+  QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+  d->mm = true;
 }
 
 void build_direct_sigma(Context* c) {
@@ -574,34 +682,11 @@ void build_direct_sigma(Context* c) {
   QDKGB_CHECK_LAUNCH();
   set_max_dynamic_smem((const void*)k_ds_opposite<double, 4>, 200 * 1024);
   set_max_dynamic_smem((const void*)k_ds_opposite<float, 8>, 200 * 1024);
-  // contraction form of the FP32 opposite-spin term, where its tables and
-  // shared memory fit (QDKGB_DIRECT_MM=0 keeps the element-wise walk)
-  {
-    const SpinTables& A = d->a;
-    const SpinTables& B = d->same ? d->a : d->b;
-    const int n = d->n, n2 = n * n;
-    d->mr = n * (n - 1);
-    d->mrp = (d->mr + 15) / 16 * 16;
-    d->mm_smem = ((size_t)A.ns * d->mrp + (size_t)2 * A.ns * kMmCols + (size_t)kMmRows * kMmEStride) * 4 +
-                 (size_t)A.ns * 4;
-    const char* env = std::getenv("QDKGB_DIRECT_MM");
-    const bool off = env && env[0] == '0';
-    d->mm = !off && B.mm.ptr != nullptr && B.ns > 0 && A.ns > 0 && d->mm_smem <= 200 * 1024;
-    if (d->mm) {
-      std::vector<float> v2((size_t)n2 * d->mrp, 0.f);
-      for (int pq = 0; pq < n2; ++pq) {
-        int r = 0;
-        for (int rs = 0; rs < n2; ++rs)
-          if (rs % n != rs / n) v2[(size_t)pq * d->mrp + r++] = (float)c->h_V[pq + (size_t)n2 * rs];
-      }
-      float* V2 = dev_array<float>(c, d->V2mm, v2.size());
-      QDKGB_CUDA(cudaMemcpyAsync(V2, v2.data(), v2.size() * 4, cudaMemcpyHostToDevice, c->stream));
-      set_max_dynamic_smem((const void*)k_ds_opposite_mm<4>, 200 * 1024);
-      set_max_dynamic_smem((const void*)k_ds_opposite_mm<8>, 200 * 1024);
-      set_max_dynamic_smem((const void*)k_ds_opposite_mm<14>, 200 * 1024);
-      set_max_dynamic_smem((const void*)k_ds_opposite_mm<16>, 200 * 1024);
-    }
-  }
+  // contraction form of the FP32 sigma, where its tables and shared memory
+  // fit (QDKGB_DIRECT_MM=0 keeps the element-wise walk)
+  build_mm_tables(c, d);
+  d->a.h_packed.clear();
+  d->b.h_packed.clear();
   QDKGB_CUDA(cudaStreamSynchronize(c->stream));
   H.n = N;
   H.nnz = 0;
