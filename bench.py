@@ -328,6 +328,10 @@ def run_ours(args):
         elif used32 in ("register8", "register16"):
             kern32 = ("k_slab_sigma32v<4, %d> (FP32 sigma, slab layout: values only, 4 beta strings per thread, "
                       "%d positions in flight)" % ((8, 8) if used32 == "register8" else (16, 16)))
+    elif lay32 == capi.OP_SLAB_DIRECT32:
+        bytes32 = None
+        kern32 = ("FP32 direct sigma: k_ds_opposite_mm (opposite-spin doubles and every single excitation as one "
+                  "contraction per alpha string, FMA pipe) + the same-spin string-only part")
     else:
         bytes32 = nnz * 8 + (N + 1) * 8 + N * 4 + N * 4
         kern32 = "k_spmv_csr<float> (FP32 sigma, CSR)"
@@ -337,7 +341,29 @@ def run_ours(args):
     else:
         bytes64 = nnz * 12 + (N + 1) * 8 + N * 8 + N * 8
         kern64 = "k_spmv_csr<double> (FP64 sigma, CSR)"
-    achieved32 = bytes32 / t_spmv32 / 1e9
+    roof = None
+    if lay32 == capi.OP_SLAB_DIRECT32:
+        # FLOPs of one FP32 direct sigma as formulated: the contraction forms
+        # E (rows: the n(n-1) pairs, n W rows, one string row; K: the alpha
+        # singles and the own row) for every beta string; the same-spin part
+        # as two dense products (or the element-wise kernels, fewer FLOPs)
+        ka = NEL // 2
+        na_s = math.comb(NORB, ka)
+        nsa = ka * (NORB - ka)
+        rows = NORB * (NORB - 1) + NORB + 1
+        flops = 2.0 * na_s * rows * (nsa + 1) * na_s
+        dense = ctx.direct_plan().get("dense") if hasattr(ctx, "direct_plan") else None
+        if dense:
+            flops += 2.0 * 2 * na_s ** 3
+        fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12
+        achieved = flops / t_spmv32 / 1e12
+        roof = {"bound": "fp32", "kernel": kern32, "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                "frac": achieved / fp32_peak, "peak_source": "nominal FP32 FMA rate (152 SMs x 128 lanes x 2 x "
+                "2.07 GHz; no measured FP32 figure)", "traffic": None, "algorithmic_flops": flops,
+                "launch_ms": t_spmv32 * 1e3}
+        achieved32 = None
+    else:
+        achieved32 = bytes32 / t_spmv32 / 1e9
     achieved64 = bytes64 / t_spmv64 / 1e9
     traffic = None
     tp = os.path.join(ROOT, "profiles", "spmv_traffic.json")
@@ -380,9 +406,10 @@ def run_ours(args):
                    "nnz": nnz, "n_chol": NCHOL, "seed": SEED, "res_tol": RES_TOL, "precision": "mixed",
                    "l2": "inputs larger than L2 (stored H %.1f GB), no flush" % (stored32 * 8 / 1e9),
                    "parallelism": "replicas" if world > 1 else "single GPU"},
-        "roofline": {"bound": "hbm", "kernel": kern32, "achieved": achieved32,
-                     "peak": peak, "unit": "GB/s", "frac": achieved32 / peak, "peak_source": peak_kind,
-                     "traffic": traffic, "algorithmic_bytes": bytes32, "launch_ms": t_spmv32 * 1e3},
+        "roofline": roof or {"bound": "hbm", "kernel": kern32, "achieved": achieved32,
+                             "peak": peak, "unit": "GB/s", "frac": achieved32 / peak, "peak_source": peak_kind,
+                             "traffic": traffic, "algorithmic_bytes": bytes32, "launch_ms": t_spmv32 * 1e3},
+        "operator_mixed": capi.LAYOUT_NAMES.get(lay32),
         "spmv_fp64": {"kernel": kern64, "achieved_gbs": achieved64, "frac": achieved64 / peak,
                       "launch_ms": t_spmv64 * 1e3, "algorithmic_bytes": bytes64},
         "sigma_autotune": {"fp32": dict(zip(("segments", "candidates_ms", "kernel", "kernel_candidates_ms"),

@@ -74,14 +74,29 @@ int qdkgb_set_device_limit(qdkgb_context* ctx, int64_t bytes);
  *   QDKGB_LAYOUT_SLAB    complete (CAS) space: values only, stored
  *                        group-major with beta strings fastest, columns
  *                        implied by the space; qdkgb_get_csr* exports CSR;
- *   QDKGB_LAYOUT_DIRECT  no stored matrix (qdkgb_build_direct_sigma).
+ *   QDKGB_LAYOUT_DIRECT  no stored matrix (qdkgb_build_direct_sigma);
+ *   QDKGB_LAYOUT_SLAB_DIRECT32  complete space built with QDKGB_H_SPLIT32
+ *                        storage: the FP64 slab (full-precision sigma and
+ *                        exports) and, for the mixed form's FP32 sigma, the
+ *                        direct contraction instead of a stored FP32 copy
+ *                        (environment QDKGB_MIXED_FP32=slab keeps the copy).
  * stored_elements = matrix elements held on the device (slab: every
  * position, zeros for thresholded elements); NULL to skip. */
 #define QDKGB_LAYOUT_NONE 0
 #define QDKGB_LAYOUT_CSR 1
 #define QDKGB_LAYOUT_SLAB 2
 #define QDKGB_LAYOUT_DIRECT 3
+#define QDKGB_LAYOUT_SLAB_DIRECT32 4
 int qdkgb_operator_layout(const qdkgb_context* ctx, int* layout, int64_t* stored_elements);
+
+/* The direct sigma's FP32 form (layouts QDKGB_LAYOUT_DIRECT and
+ * QDKGB_LAYOUT_SLAB_DIRECT32; no counterpart in the reference):
+ * *contraction 1 when the opposite-spin doubles and the single excitations
+ * run as one FP32 contraction per alpha string (else the element-wise walk);
+ * *dense the same-spin part's form, -1 until the first FP32 sigma times the
+ * two, 0 element-wise kernels, 1 two dense FP32 products; form_ms[2] their
+ * times (ms).  Any pointer may be NULL. */
+int qdkgb_direct_plan(const qdkgb_context* ctx, int* contraction, int* dense, double* form_ms);
 
 /* The sizes the getters write (no counterpart; the reference's sparsexx
  * matrix carries its own m() and nnz()): *ndets the dimension of the

@@ -25,16 +25,17 @@ ERR_STATE = 6
 LAYOUT_COLMAJOR = 0
 LAYOUT_ROWMAJOR = 1
 # operator layouts (qdkgb_operator_layout, qdkgb_build_operator)
-LAYOUT_NONE, LAYOUT_CSR, LAYOUT_SLAB, LAYOUT_DIRECT = 0, 1, 2, 3
+LAYOUT_NONE, LAYOUT_CSR, LAYOUT_SLAB, LAYOUT_DIRECT, LAYOUT_SLAB_DIRECT32 = 0, 1, 2, 3, 4
+LAYOUT_NAMES = {1: "csr", 2: "slab", 3: "direct", 4: "slab+direct32"}
 H_FP64 = 0
 H_SPLIT32 = 1
 PREC_FP64 = 0
 PREC_MIXED = 1
-OP_NONE, OP_CSR, OP_SLAB, OP_DIRECT = 0, 1, 2, 3
+OP_NONE, OP_CSR, OP_SLAB, OP_DIRECT, OP_SLAB_DIRECT32 = 0, 1, 2, 3, 4
 
 EXPORTED = [
     "qdkgb_create", "qdkgb_destroy", "qdkgb_last_error", "qdkgb_set_stream", "qdkgb_device_bytes",
-    "qdkgb_set_device_limit", "qdkgb_operator_layout", "qdkgb_problem_size",
+    "qdkgb_set_device_limit", "qdkgb_operator_layout", "qdkgb_problem_size", "qdkgb_direct_plan",
     "qdkgb_set_integrals", "qdkgb_fci_dets", "qdkgb_set_dets", "qdkgb_build_hamiltonian", "qdkgb_get_csr32",
     "qdkgb_get_csr64", "qdkgb_get_csr32_rows", "qdkgb_get_csr64_rows", "qdkgb_diagonal", "qdkgb_spmv", "qdkgb_spmv_device", "qdkgb_davidson_default_settings",
     "qdkgb_davidson", "qdkgb_rdms_spin_dep", "qdkgb_orbital_entropies", "qdkgb_casci",
@@ -133,6 +134,7 @@ def lib():
     L.qdkgb_device_bytes.argtypes = [vp, P(i64)]
     L.qdkgb_set_device_limit.argtypes = [vp, i64]
     L.qdkgb_operator_layout.argtypes = [vp, P(ctypes.c_int), P(i64)]
+    L.qdkgb_direct_plan.argtypes = [vp, P(ctypes.c_int), P(ctypes.c_int), P(ctypes.c_double)]
     L.qdkgb_problem_size.argtypes = [vp, P(i64), P(i64)]
     L.qdkgb_set_integrals.argtypes = [vp, ci, vp, vp, ci]
     L.qdkgb_fci_dets.argtypes = [ci, ci, ci, vp, vp, P(i64)]
@@ -334,7 +336,9 @@ class Context:
 
     def operator_layout(self):
         """(layout, stored elements): OP_CSR, OP_SLAB (complete space, values
-        only) or OP_DIRECT (no stored matrix); OP_NONE before a build."""
+        only), OP_SLAB_DIRECT32 (the FP64 slab, and the direct contraction
+        for the mixed form's FP32 sigma) or OP_DIRECT (no stored matrix);
+        OP_NONE before a build."""
         lay = ctypes.c_int()
         st = ctypes.c_int64()
         self._check(lib().qdkgb_operator_layout(self._h, ctypes.byref(lay), ctypes.byref(st)))
@@ -370,12 +374,22 @@ class Context:
     def build_operator(self, thresh=np.finfo(np.float64).eps, storage=H_FP64, max_m=200):
         """The stored Hamiltonian when it fits on the device, else (complete
         spaces) the direct sigma (qdkgb_build_operator); returns the layout
-        name ("slab", "csr" or "direct")."""
+        name ("slab", "slab+direct32", "csr" or "direct")."""
         lay = ctypes.c_int()
         nnz = ctypes.c_int64()
         self._check(lib().qdkgb_build_operator(self._h, float(thresh), int(storage), int(max_m), ctypes.byref(lay),
                                                ctypes.byref(nnz)))
-        return {LAYOUT_CSR: "csr", LAYOUT_SLAB: "slab", LAYOUT_DIRECT: "direct"}[lay.value]
+        return LAYOUT_NAMES[lay.value]
+
+    def direct_plan(self):
+        """The direct sigma's FP32 form (qdkgb_direct_plan): {"contraction":
+        bool, "dense": None (not yet timed) / bool, "form_ms": (element-wise,
+        dense)}."""
+        mm, dense = ctypes.c_int(), ctypes.c_int()
+        ms = (ctypes.c_double * 2)()
+        self._check(lib().qdkgb_direct_plan(self._h, ctypes.byref(mm), ctypes.byref(dense), ms))
+        return {"contraction": bool(mm.value), "dense": None if dense.value < 0 else bool(dense.value),
+                "form_ms": (ms[0], ms[1])}
 
     def build_direct_sigma(self):
         """Recompute-on-the-fly sigma for a complete space (no CSR stored)."""

@@ -318,6 +318,12 @@ int qdkgb_problem_size(const qdkgb_context* c, int64_t* ndets, int64_t* nnz) {
   return QDKGB_OK;
 }
 
+int qdkgb_direct_plan(const qdkgb_context* c, int* contraction, int* dense, double* form_ms) {
+  if (!c) return QDKGB_ERR_INVALID;
+  direct_plan(c, contraction, dense, form_ms);
+  return QDKGB_OK;
+}
+
 int qdkgb_operator_layout(const qdkgb_context* c, int* layout, int64_t* stored) {
   if (!c || !layout) return QDKGB_ERR_INVALID;
   const Hcsr& H = c->H;
@@ -327,7 +333,7 @@ int qdkgb_operator_layout(const qdkgb_context* c, int* layout, int64_t* stored) 
   } else if (c->op_direct) {
     *layout = QDKGB_LAYOUT_DIRECT;
   } else if (H.structured) {
-    *layout = QDKGB_LAYOUT_SLAB;
+    *layout = c->fp32_direct ? QDKGB_LAYOUT_SLAB_DIRECT32 : QDKGB_LAYOUT_SLAB;
     st = struct_slab_elements(const_cast<qdkgb_context*>(c));
   } else {
     *layout = QDKGB_LAYOUT_CSR;

@@ -771,7 +771,7 @@ void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C
   if (!H.valid) throw Error(QDKGB_ERR_STATE, "Hamiltonian not built");
   const int64_t N = H.n;
   const bool mixed = s->precision == QDKGB_PREC_MIXED;
-  if (mixed && !c->op_direct && H.storage != QDKGB_H_SPLIT32)
+  if (mixed && !c->op_direct && !c->fp32_direct && H.storage != QDKGB_H_SPLIT32)
     throw Error(QDKGB_ERR_STATE, "mixed precision needs the Hamiltonian built with QDKGB_H_SPLIT32 storage");
   if (s->precision != QDKGB_PREC_FP64 && !mixed) throw Error(QDKGB_ERR_INVALID, "unknown precision");
   if (s->max_m < 2 && N > 1) throw Error(QDKGB_ERR_INVALID, "max_m must be >= 2");

@@ -63,14 +63,19 @@ inline HSingle hsingle(uint64_t bra, uint64_t ket, uint64_t ex) {
 // FP32 contraction form (k_ds_opposite_mm): beta strings J_b in chunks of
 // kMmCols; E rows 16 per warp, each thread 4 rows x 8 columns.
 constexpr int kMmCols = 64;
-constexpr int kMmEStride = kMmCols + 4;  // row stride of E in shared memory (16-byte rows)
 constexpr int kMmMaxWarps = 16;
 
+// One spin's string tables.  Structure (built once per determinant space):
+// sJ / svo the singles (target string; v | o << 8 | neg << 16), dJ / dvo the
+// doubles (target; v1 | o1 << 5 | v2 << 10 | o2 << 15 | neg << 20), packed
+// the singles as Jb | rs << 16 | neg << 31, str the strings.  Values
+// (recomputed from the integrals by every build, k_ds_values): sA the
+// singles' string-only part, dval the doubles, W over THIS spin's strings.
 struct SpinTables {
   int64_t nstr = 0;
   int ns = 0, nd = 0;
-  DeviceBuffer sJ, svo, sA64, sA32, dJ, dval64, dval32, W64, W32;  // W over THIS spin's strings
-  DeviceBuffer packed;  // singles packed as Jb | rs << 16 | neg << 31 (opposite-spin walk)
+  DeviceBuffer sJ, svo, dJ, dvo, packed, str;
+  DeviceBuffer sA64, sA32, dval64, dval32, W64, W32;
   std::vector<uint32_t> h_packed;  // host copy of `packed` while the contraction tables are built
 };
 
@@ -85,37 +90,45 @@ struct DirectSigma {
   //   mr + n          the string-only part of the alpha singles
   // mrows = mr + n + 1 rounded up to 16 is mrp (one warp per 16 rows).
   // V2mm[pq][r]: V(pq, rs_r) for r < mr, V(p p | pq) for r = mr + p, else 0.
-  // lists: per chunk of kMmCols beta strings, the (nb + 1) uint16 offsets of
-  // each beta string's entries (padded to 16 bytes) then the entries
-  // jl | r << 8 | neg << 31 (jl = J_b - chunk start), each string's sorted by
-  // (J_b, r); seg[c] = the chunk's first 4-byte word (16-byte aligned)
+  // lists (uint16): per chunk of kMmCols beta strings, the (nb + 1) offsets
+  // of each beta string's entries (padded to 16 bytes) then the entries
+  // (r kMmCols + jl) | neg << 15 (jl = J_b - chunk start: the entry's place
+  // in E), each string's sorted by (J_b, r); seg[c] = the chunk's first
+  // element (16-byte aligned); off_u16 = the padded offset count
   bool mm = false;
-  int mr = 0, mrp = 0, mm_threads = 0, mm_jpt = 0, seg_max = 0, off_words = 0;
+  int mr = 0, mrp = 0, mm_threads = 0, mm_jpt = 0, seg_max = 0, off_u16 = 0;
+  bool mm_vec = false;  // C rows 16-byte aligned (nb % 4 == 0): 16-byte staging copies
   size_t mm_smem = 0;
   DeviceBuffer V2mm, rs_of, lists, seg;
+  // same-spin string-only parts as dense FP32 matrices for the contraction
+  // form: Haa[Ia][Ja] the alpha doubles, HbbT[Jb][Ib] the beta doubles and
+  // the beta singles' string-only part; dense_state -1 until the first FP32
+  // sigma times the dense products against the element-wise same-spin
+  // kernels (0 element-wise, 1 dense)
+  int dense_state = -1;
+  double dense_ms[2] = {0., 0.};
+  char mm_env = 0, dense_env = 0;  // QDKGB_DIRECT_MM / QDKGB_DIRECT_DENSE when built
+  DeviceBuffer Haa, HbbT;
 };
 
 void free_direct(Context* c) {
   if (!c->direct) return;
   DirectSigma* d = c->direct;
   for (SpinTables* t : {&d->a, &d->b})
-    for (DeviceBuffer* b : {&t->sJ, &t->svo, &t->sA64, &t->sA32, &t->dJ, &t->dval64, &t->dval32, &t->W64, &t->W32,
-                            &t->packed})
+    for (DeviceBuffer* b : {&t->sJ, &t->svo, &t->dJ, &t->dvo, &t->packed, &t->str, &t->sA64, &t->sA32, &t->dval64,
+                            &t->dval32, &t->W64, &t->W32})
       dev_free(c, *b);
-  for (DeviceBuffer* b : {&d->V32, &d->tmp64, &d->tmp32, &d->ct64, &d->ct32, &d->V2mm, &d->rs_of, &d->lists, &d->seg})
+  for (DeviceBuffer* b : {&d->V32, &d->tmp64, &d->tmp32, &d->ct64, &d->ct32, &d->V2mm, &d->rs_of, &d->lists, &d->seg,
+                          &d->Haa, &d->HbbT})
     dev_free(c, *b);
   delete d;
   c->direct = nullptr;
 }
 
+// Structure of one spin's tables (host, once per determinant space).
 static void build_spin_tables(Context* c, const std::vector<uint64_t>& strs, SpinTables& t) {
   const int n = c->norb;
   const size_t nn = (size_t)n;
-  const std::vector<double>& T = c->h_T;
-  const std::vector<double>& V = c->h_V;
-  auto Vat = [&](uint32_t p, uint32_t q, uint32_t r, uint32_t s) { return V[p + nn * (q + nn * (r + nn * s))]; };
-  auto Gred = [&](uint32_t k, uint32_t i, uint32_t j) { return Vat(k, k, i, j) - Vat(k, j, i, k); };
-  auto Vred = [&](uint32_t k, uint32_t i, uint32_t j) { return Vat(k, k, i, j); };
   const int64_t N = (int64_t)strs.size();
   std::unordered_map<uint64_t, int32_t> rank;
   for (int64_t i = 0; i < N; ++i) rank[strs[i]] = (int32_t)i;
@@ -125,10 +138,7 @@ static void build_spin_tables(Context* c, const std::vector<uint64_t>& strs, Spi
   t.ns = ns;
   t.nd = nd;
   std::vector<int32_t> sJ((size_t)N * ns), svo((size_t)N * ns), dJ((size_t)N * std::max(nd, 1));
-  std::vector<double> sA((size_t)N * ns), dval((size_t)N * std::max(nd, 1));
-  std::vector<uint32_t> packed((size_t)N * ns);
-  std::vector<double> W(nn * nn * N);
-  const uint64_t full = (n == 64) ? ~0ull : ((1ull << n) - 1ull);
+  std::vector<uint32_t> dvo((size_t)N * std::max(nd, 1)), packed((size_t)N * ns);
   for (int64_t i = 0; i < N; ++i) {
     const uint64_t I = strs[i];
     std::vector<uint32_t> occ, vir;
@@ -140,11 +150,8 @@ static void build_spin_tables(Context* c, const std::vector<uint64_t>& strs, Spi
         auto it = rank.find(J);
         if (it == rank.end()) throw Error(QDKGB_ERR_UNSUPPORTED, "direct sigma needs a complete string set");
         HSingle s = hsingle(I, J, I ^ J);  // bra I, ket J: v in I, o in J
-        double a = T[s.v + nn * s.o];
-        for (uint32_t p : occ) a += Gred(p, s.v, s.o);
         sJ[(size_t)i * ns + m] = it->second;
         svo[(size_t)i * ns + m] = (int32_t)(s.v | (s.o << 8) | ((uint32_t)s.neg << 16));
-        sA[(size_t)i * ns + m] = a;
         packed[(size_t)i * ns + m] =
             (uint32_t)it->second | ((uint32_t)(s.v + nn * s.o) << 16) | ((uint32_t)s.neg << 31);
         ++m;
@@ -163,42 +170,87 @@ static void build_spin_tables(Context* c, const std::vector<uint64_t>& strs, Spi
             ket ^= (1ull << s1.o) | (1ull << s1.v);
             ex ^= (1ull << s1.o) | (1ull << s1.v);
             HSingle s2 = hsingle(I, ket, ex);
-            const double g = Vat(s1.v, s1.o, s2.v, s2.o) - Vat(s1.v, s2.o, s2.v, s1.o);
             dJ[(size_t)i * nd + m] = it->second;
-            dval[(size_t)i * nd + m] = (s1.neg != s2.neg) ? -g : g;
+            dvo[(size_t)i * nd + m] = s1.v | (s1.o << 5) | (s2.v << 10) | (s2.o << 15) |
+                                      ((uint32_t)(s1.neg != s2.neg) << 20);
             ++m;
           }
-    // W[(v,o)][i] = sum_{p in I} V_red(p, v, o)
-    for (uint32_t o = 0; o < (uint32_t)n; ++o)
-      for (uint32_t v = 0; v < (uint32_t)n; ++v) {
-        double w = 0.;
-        for (uint32_t p : occ) w += Vred(p, v, o);
-        W[(v + nn * o) * N + i] = w;
-      }
-    (void)full;
   }
   auto up = [&](DeviceBuffer& b, const void* src, size_t bytes) {
     void* p = dev_alloc(c, b, bytes + 16);
     QDKGB_CUDA(cudaMemcpyAsync(p, src, bytes, cudaMemcpyHostToDevice, c->stream));
   };
-  auto to32 = [](const std::vector<double>& x) {
-    std::vector<float> y(x.size());
-    for (size_t i = 0; i < x.size(); ++i) y[i] = (float)x[i];
-    return y;
-  };
   up(t.sJ, sJ.data(), sJ.size() * 4);
   up(t.svo, svo.data(), svo.size() * 4);
-  up(t.sA64, sA.data(), sA.size() * 8);
-  std::vector<float> sA32 = to32(sA), dval32 = to32(dval), W32 = to32(W);
-  up(t.sA32, sA32.data(), sA32.size() * 4);
   up(t.dJ, dJ.data(), dJ.size() * 4);
-  up(t.dval64, dval.data(), dval.size() * 8);
-  up(t.dval32, dval32.data(), dval32.size() * 4);
-  up(t.W64, W.data(), W.size() * 8);
-  up(t.W32, W32.data(), W32.size() * 4);
+  up(t.dvo, dvo.data(), dvo.size() * 4);
   up(t.packed, packed.data(), packed.size() * 4);
-  t.h_packed = std::move(packed);
+  up(t.str, strs.data(), strs.size() * 8);
   QDKGB_CUDA(cudaStreamSynchronize(c->stream));
+  t.h_packed = std::move(packed);
+}
+
+// Values of one spin's tables from the integrals, in the order of the
+// reference's matrix elements (matrix_elements.hpp:65-230): the singles'
+// string-only part A = T(v, o) + sum_{p in I} G_red(p, v, o) (ascending p),
+// the doubles V(v1 o1 | v2 o2) - V(v1 o2 | v2 o1) with the sign pair's
+// parity, and W[(v, o)][I] = sum_{p in I} V(p p | v o); FP64 and its FP32
+// rounding.  One thread per entry.
+__global__ void k_ds_values(int64_t N, int ns, int nd, int n, const uint64_t* __restrict__ strs,
+                            const int32_t* __restrict__ svo, const uint32_t* __restrict__ dvo,
+                            const double* __restrict__ T, const double* __restrict__ V, double* __restrict__ sA64,
+                            float* __restrict__ sA32, double* __restrict__ dval64, float* __restrict__ dval32,
+                            double* __restrict__ W64, float* __restrict__ W32) {
+  const int64_t nn = n, ts = N * ns, td = N * nd, tw = nn * nn * N;
+  auto Vat = [&](int64_t p, int64_t q, int64_t r, int64_t s) { return __ldg(V + p + nn * (q + nn * (r + nn * s))); };
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < ts + td + tw;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    if (t < ts) {
+      const uint64_t I = __ldg(strs + t / ns);
+      const int32_t vo = __ldg(svo + t);
+      const int v = vo & 0xff, o = (vo >> 8) & 0xff;
+      double a = __ldg(T + v + nn * o);
+      for (int p = 0; p < n; ++p)
+        if ((I >> p) & 1) a += Vat(p, p, v, o) - Vat(p, o, v, p);
+      sA64[t] = a;
+      sA32[t] = (float)a;
+    } else if (t < ts + td) {
+      const int64_t u = t - ts;
+      const uint32_t w = __ldg(dvo + u);
+      const int v1 = w & 31, o1 = (w >> 5) & 31, v2 = (w >> 10) & 31, o2 = (w >> 15) & 31;
+      const double g = Vat(v1, o1, v2, o2) - Vat(v1, o2, v2, o1);
+      const double d = ((w >> 20) & 1) ? -g : g;
+      dval64[u] = d;
+      dval32[u] = (float)d;
+    } else {
+      const int64_t u = t - ts - td, vo = u / N;
+      const uint64_t I = __ldg(strs + (u - vo * N));
+      const int v = (int)(vo % nn), o = (int)(vo / nn);
+      double w = 0.;
+      for (int p = 0; p < n; ++p)
+        if ((I >> p) & 1) w += Vat(p, p, v, o);
+      W64[u] = w;
+      W32[u] = (float)w;
+    }
+  }
+}
+
+static void spin_values(Context* c, SpinTables& t) {
+  const int64_t N = t.nstr, n = c->norb;
+  dev_array<double>(c, t.sA64, (size_t)N * t.ns + 1);
+  dev_array<float>(c, t.sA32, (size_t)N * t.ns + 1);
+  dev_array<double>(c, t.dval64, (size_t)N * std::max(t.nd, 1));
+  dev_array<float>(c, t.dval32, (size_t)N * std::max(t.nd, 1));
+  dev_array<double>(c, t.W64, (size_t)(n * n * N));
+  dev_array<float>(c, t.W32, (size_t)(n * n * N));
+  const int64_t tot = N * t.ns + N * t.nd + n * n * N;
+  const unsigned blocks = (unsigned)std::min<int64_t>((tot + 255) / 256, (int64_t)c->sm_count * 16);
+  k_ds_values<<<blocks, 256, 0, c->stream>>>(N, t.ns, t.nd, (int)n, (const uint64_t*)t.str.ptr,
+                                             (const int32_t*)t.svo.ptr, (const uint32_t*)t.dvo.ptr,
+                                             (const double*)c->T.ptr, (const double*)c->V.ptr, (double*)t.sA64.ptr,
+                                             (float*)t.sA32.ptr, (double*)t.dval64.ptr, (float*)t.dval32.ptr,
+                                             (double*)t.W64.ptr, (float*)t.W32.ptr);
+  QDKGB_CHECK_LAUNCH();
 }
 
 // out[I, col] (+)= sum over same-spin doubles and singles of row string I
@@ -327,21 +379,21 @@ __device__ __forceinline__ void cp_async16(void* dst, const void* src) {
 // 16 rows of E; then each thread walks its beta strings' entries of the
 // chunk in the lists' fixed order, so the sums are reproducible.
 // sigma[Ia, :] += diag * C[Ia, :] + the terms; JPT beta strings per thread.
-template <int JPT>
-__global__ void __launch_bounds__(kMmMaxWarps * 32)
-    k_ds_opposite_mm(int na, int nb, int nsa, int mr, int mrp, int off_words, int seg_max,
+template <int JPT, bool BIG>
+__global__ void __launch_bounds__(BIG ? kMmMaxWarps * 32 : 320, BIG ? 1 : 2)
+    k_ds_opposite_mm(int na, int nb, int nsa, int mr, int mrp, int off_u16, int seg_max, int vec,
                      const int32_t* __restrict__ a_sJ, const int32_t* __restrict__ a_svo,
                      const float* __restrict__ a_sA, const float* __restrict__ a_W, const int32_t* __restrict__ rs_of,
-                     const uint32_t* __restrict__ lists, const int32_t* __restrict__ seg,
+                     const uint16_t* __restrict__ lists, const int32_t* __restrict__ seg,
                      const float* __restrict__ V2, int n, const double* __restrict__ D, const float* __restrict__ C,
                      float* __restrict__ sigma) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int K = nsa + 1;
-  float* Vp = (float*)smem_raw;                          // [K][mrp]
-  float* G = Vp + (size_t)K * mrp;                       // [2][K][kMmCols]
-  float* E = G + (size_t)2 * K * kMmCols;                // [mrp][kMmEStride]
-  uint32_t* L = (uint32_t*)(E + (size_t)mrp * kMmEStride);  // [2][seg_max]
-  int32_t* Jrow = (int32_t*)(L + (size_t)2 * seg_max);   // [K]
+  float* Vp = (float*)smem_raw;                           // [K][mrp]
+  float* G = Vp + (size_t)K * mrp;                        // [2][K][kMmCols]
+  float* E = G + (size_t)2 * K * kMmCols;                 // [mrp][kMmCols]
+  uint16_t* L = (uint16_t*)(E + (size_t)mrp * kMmCols);   // [2][seg_max]
+  int32_t* Jrow = (int32_t*)(L + (size_t)2 * seg_max);    // [K]
   const int64_t Ia = blockIdx.x;
   const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31, warp = tid >> 5;
   const int ty = lane >> 3, tx = lane & 7;
@@ -363,14 +415,25 @@ __global__ void __launch_bounds__(kMmMaxWarps * 32)
   auto stage = [&](int chunk, int buf) {
     const int j0 = chunk * kMmCols;
     float* g = G + (size_t)buf * K * kMmCols;
-    for (int i = tid; i < K * kMmCols; i += nthr) {
-      const int k = i / kMmCols, j = i - k * kMmCols;
-      const bool ok = j0 + j < nb;
-      cp_async4_zfill(g + i, C + (int64_t)Jrow[k] * nb + (ok ? j0 + j : 0), ok);
+    if (vec) {
+      for (int i = tid; i < K * (kMmCols / 4); i += nthr) {
+        const int k = i / (kMmCols / 4), j = 4 * (i - k * (kMmCols / 4));
+        const bool ok = j0 + j < nb;
+        const unsigned sa = (unsigned)__cvta_generic_to_shared(g + k * kMmCols + j);
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(sa),
+                     "l"(C + (int64_t)Jrow[k] * nb + (ok ? j0 + j : 0)), "r"(ok ? 16 : 0)
+                     : "memory");
+      }
+    } else {
+      for (int i = tid; i < K * kMmCols; i += nthr) {
+        const int k = i / kMmCols, j = i - k * kMmCols;
+        const bool ok = j0 + j < nb;
+        cp_async4_zfill(g + i, C + (int64_t)Jrow[k] * nb + (ok ? j0 + j : 0), ok);
+      }
     }
-    const int w0 = __ldg(seg + chunk), nv = (__ldg(seg + chunk + 1) - w0) >> 2;
-    uint32_t* l = L + (size_t)buf * seg_max;
-    for (int i = tid; i < nv; i += nthr) cp_async16(l + 4 * i, lists + w0 + 4 * i);
+    const int u0 = __ldg(seg + chunk), nv = (__ldg(seg + chunk + 1) - u0) >> 3;
+    uint16_t* l = L + (size_t)buf * seg_max;
+    for (int i = tid; i < nv; i += nthr) cp_async16(l + 8 * i, lists + u0 + 8 * i);
     asm volatile("cp.async.commit_group;\n" ::: "memory");
   };
   float acc[JPT];
@@ -386,47 +449,46 @@ __global__ void __launch_bounds__(kMmMaxWarps * 32)
     __syncthreads();  // chunk c staged by every thread; E and buffer (c + 1) & 1 free
     if (c + 1 < nchunk) stage(c + 1, (c + 1) & 1);
     {
-      const float* vrow = Vp + warp * 16 + ty * 4;
-      const float* grow = G + (size_t)(c & 1) * K * kMmCols + tx * 4;
-      float a4[4][8];
+      const float* v0 = Vp + warp * 16 + ty * 4;
+      const float* g0 = G + (size_t)(c & 1) * K * kMmCols + tx * 4;
+      float a[4][8];
 #pragma unroll
       for (int i = 0; i < 4; ++i)
 #pragma unroll
-        for (int jj = 0; jj < 8; ++jj) a4[i][jj] = 0.f;
+        for (int jj = 0; jj < 8; ++jj) a[i][jj] = 0.f;
 #pragma unroll 4
       for (int k = 0; k < K; ++k) {
-        const float4 va = *(const float4*)(vrow + (size_t)k * mrp);
-        const float4 b0 = *(const float4*)(grow + k * kMmCols);
-        const float4 b1 = *(const float4*)(grow + k * kMmCols + 32);
+        const float4 va = *(const float4*)(v0 + (size_t)k * mrp);
+        const float4 b0 = *(const float4*)(g0 + k * kMmCols);
+        const float4 b1 = *(const float4*)(g0 + k * kMmCols + 32);
         const float av[4] = {va.x, va.y, va.z, va.w};
         const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
 #pragma unroll
         for (int i = 0; i < 4; ++i)
 #pragma unroll
-          for (int jj = 0; jj < 8; ++jj) a4[i][jj] = fmaf(av[i], bv[jj], a4[i][jj]);
+          for (int jj = 0; jj < 8; ++jj) a[i][jj] = fmaf(av[i], bv[jj], a[i][jj]);
       }
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
-        float* e = E + (size_t)(warp * 16 + ty * 4 + i) * kMmEStride + tx * 4;
-        *(float4*)e = make_float4(a4[i][0], a4[i][1], a4[i][2], a4[i][3]);
-        *(float4*)(e + 32) = make_float4(a4[i][4], a4[i][5], a4[i][6], a4[i][7]);
+        float* e = E + (size_t)(warp * 16 + ty * 4 + i) * kMmCols + tx * 4;
+        *(float4*)e = make_float4(a[i][0], a[i][1], a[i][2], a[i][3]);
+        *(float4*)(e + 32) = make_float4(a[i][4], a[i][5], a[i][6], a[i][7]);
       }
     }
     __syncthreads();
-    const uint32_t* l = L + (size_t)(c & 1) * seg_max;
-    const uint16_t* off = (const uint16_t*)l;
-    const uint32_t* ent = l + off_words;
+    const uint16_t* off = L + (size_t)(c & 1) * seg_max;
+    const uint16_t* ent = off + off_u16;
 #pragma unroll
     for (int j = 0; j < JPT; ++j) {
       const int Ib = tid + j * nthr;
       if (Ib < nb) {
         const int e1 = off[Ib + 1];
-        float a = acc[j];
+        float s = acc[j];
         for (int e = off[Ib]; e < e1; ++e) {
           const uint32_t w = ent[e];
-          a += negate_if<float>(E[((w >> 8) & 0x7fff) * kMmEStride + (w & 0xff)], (w >> 31) != 0);
+          s += negate_if<float>(E[w & 0x7fff], (w >> 15) != 0);
         }
-        acc[j] = a;
+        acc[j] = s;
       }
     }
   }
@@ -469,6 +531,120 @@ void transpose_f64(Context* c, const double* in, double* out, int64_t nr, int64_
   transpose<double>(c, in, out, nr, nc, false);
 }
 
+__global__ void k_ds_v32(const double* __restrict__ V, float* __restrict__ V32, int64_t n4) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n4; i += (int64_t)gridDim.x * blockDim.x)
+    V32[i] = (float)V[i];
+}
+
+// V2mm[pq][r] (see DirectSigma)
+__global__ void k_ds_v2mm(const double* __restrict__ V, const int32_t* __restrict__ rs_of, int n, int mr, int mrp,
+                          float* __restrict__ V2) {
+  const int64_t n2 = (int64_t)n * n, tot = n2 * mrp;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < tot; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t pq = i / mrp;
+    const int r = (int)(i - pq * mrp);
+    float v = 0.f;
+    if (r < mr)
+      v = (float)V[pq + n2 * rs_of[r]];
+    else if (r < mr + n)
+      v = (float)V[(r - mr) * (int64_t)(n + 1) + n2 * pq];
+    V2[i] = v;
+  }
+}
+
+// Dense same-spin matrices of the contraction form (Haa, HbbT zeroed first):
+// Haa[i][dJ] = dval_a; HbbT[dJ_b][j] = dval_b; HbbT[sJ_b][j] = s A_b.
+__global__ void k_ds_dense_fill(int64_t na, int nda, const int32_t* __restrict__ adJ,
+                                const float* __restrict__ adval, int64_t nb, int ndb, int nsb,
+                                const int32_t* __restrict__ bdJ, const float* __restrict__ bdval,
+                                const int32_t* __restrict__ bsJ, const int32_t* __restrict__ bsvo,
+                                const float* __restrict__ bsA, float* __restrict__ Haa, float* __restrict__ HbbT) {
+  const int64_t t1 = na * nda, t2 = nb * ndb, t3 = nb * nsb;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < t1 + t2 + t3;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    if (t < t1) {
+      Haa[(t / nda) * na + adJ[t]] = adval[t];
+    } else if (t < t1 + t2) {
+      const int64_t u = t - t1;
+      HbbT[(int64_t)bdJ[u] * nb + u / ndb] = bdval[u];
+    } else {
+      const int64_t u = t - t1 - t2;
+      HbbT[(int64_t)bsJ[u] * nb + u / nsb] = negate_if<float>(bsA[u], (bsvo[u] >> 16) != 0);
+    }
+  }
+}
+
+// out (M x N) = A1 (M x K1) B1 (K1 x N) + A2 (M x K2) B2 (K2 x N), row-major
+// FP32: 64 x 64 tiles, 256 threads of 4 x 4, K in steps of 16 through
+// register-staged double-buffered shared memory.
+constexpr int kGmT = 64, kGmK = 16;
+__global__ void __launch_bounds__(256) k_ds_gemm2(int M, int N, int K1, int K2, const float* __restrict__ A1,
+                                                  const float* __restrict__ B1, const float* __restrict__ A2,
+                                                  const float* __restrict__ B2, float* __restrict__ out) {
+  __shared__ __align__(16) float As[2][kGmK][kGmT + 4];
+  __shared__ __align__(16) float Bs[2][kGmK][kGmT];
+  const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
+  const int m0 = blockIdx.y * kGmT, n0 = blockIdx.x * kGmT;
+  const int am = tid >> 2, ak = (tid & 3) * 4;   // A loader: row am, k ak..ak+3
+  const int bk = tid >> 4, bn = (tid & 15) * 4;  // B loader: k bk, cols bn..bn+3
+  float acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+  float ra[4], rb[4];
+  for (int phase = 0; phase < 2; ++phase) {
+    const float* A = phase ? A2 : A1;
+    const float* B = phase ? B2 : B1;
+    const int K = phase ? K2 : K1;
+    const int ntile = (K + kGmK - 1) / kGmK;
+    auto load = [&](int t) {
+      const int k0 = t * kGmK;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int m = m0 + am, k = k0 + ak + i;
+        ra[i] = (m < M && k < K) ? __ldg(A + (int64_t)m * K + k) : 0.f;
+        const int kb = k0 + bk, nn = n0 + bn + i;
+        rb[i] = (kb < K && nn < N) ? __ldg(B + (int64_t)kb * N + nn) : 0.f;
+      }
+    };
+    auto store = [&](int buf) {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) As[buf][ak + i][am] = ra[i];
+      *(float4*)&Bs[buf][bk][bn] = make_float4(rb[0], rb[1], rb[2], rb[3]);
+    };
+    load(0);
+    store(0);
+    __syncthreads();
+    for (int t = 0; t < ntile; ++t) {
+      const int buf = t & 1;
+      if (t + 1 < ntile) load(t + 1);
+#pragma unroll
+      for (int kk = 0; kk < kGmK; ++kk) {
+        const float4 a = *(const float4*)&As[buf][kk][ty * 4];
+        const float4 b = *(const float4*)&Bs[buf][kk][tx * 4];
+        const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
+      }
+      if (t + 1 < ntile) store(buf ^ 1);
+      __syncthreads();
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int m = m0 + ty * 4 + i;
+    if (m >= M) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int nn = n0 + tx * 4 + j;
+      if (nn < N) out[(int64_t)m * N + nn] = acc[i][j];
+    }
+  }
+}
+
 template <typename T>
 static void direct_sigma_t(Context* c, const T* x, T* y) {
   DirectSigma* d = c->direct;
@@ -477,46 +653,91 @@ static void direct_sigma_t(Context* c, const T* x, T* y) {
   const int64_t na = A.nstr, nb = B.nstr, N = na * nb;
   const bool f64 = sizeof(T) == 8;
   // the contraction form applies every single excitation but the beta
-  // singles' string-only part, so the same-spin kernels then take the
-  // doubles (alpha) and the doubles plus string-only singles (beta)
+  // singles' string-only part, so the same-spin part is then the alpha
+  // doubles and the beta doubles plus string-only singles
   const bool mm = !f64 && d->mm;
   auto P = [&](const DeviceBuffer& b64, const DeviceBuffer& b32) { return (const T*)(f64 ? b64.ptr : b32.ptr); };
-  T* ct = (T*)dev_alloc(c, f64 ? d->ct64 : d->ct32, N * sizeof(T));
-  T* tmp = (T*)dev_alloc(c, f64 ? d->tmp64 : d->tmp32, N * sizeof(T));
-  // alpha-alpha into y
-  k_ds_same_spin<T><<<(unsigned)na, kDsThreads, 0, c->stream>>>(
-      na, nb, mm ? 0 : A.ns, A.nd, (const int32_t*)A.sJ.ptr, (const int32_t*)A.svo.ptr, P(A.sA64, A.sA32),
-      (const int32_t*)A.dJ.ptr, P(A.dval64, A.dval32), P(B.W64, B.W32), d->n, x, y);
-  QDKGB_CHECK_LAUNCH();
-  // beta-beta on C^T, added back transposed
-  transpose<T>(c, x, ct, na, nb, false);
-  k_ds_same_spin<T><<<(unsigned)nb, kDsThreads, 0, c->stream>>>(
-      nb, na, B.ns, B.nd, (const int32_t*)B.sJ.ptr, (const int32_t*)B.svo.ptr, P(B.sA64, B.sA32),
-      (const int32_t*)B.dJ.ptr, P(B.dval64, B.dval32), mm ? nullptr : P(A.W64, A.W32), d->n, ct, tmp);
-  QDKGB_CHECK_LAUNCH();
-  transpose<T>(c, tmp, y, nb, na, true);
-  // opposite spin + diagonal (+ the singles, contraction form)
+  auto same_spin = [&]() {
+    T* ct = (T*)dev_alloc(c, f64 ? d->ct64 : d->ct32, N * sizeof(T));
+    T* tmp = (T*)dev_alloc(c, f64 ? d->tmp64 : d->tmp32, N * sizeof(T));
+    // alpha-alpha into y
+    k_ds_same_spin<T><<<(unsigned)na, kDsThreads, 0, c->stream>>>(
+        na, nb, mm ? 0 : A.ns, A.nd, (const int32_t*)A.sJ.ptr, (const int32_t*)A.svo.ptr, P(A.sA64, A.sA32),
+        (const int32_t*)A.dJ.ptr, P(A.dval64, A.dval32), P(B.W64, B.W32), d->n, x, y);
+    QDKGB_CHECK_LAUNCH();
+    // beta-beta on C^T, added back transposed
+    transpose<T>(c, x, ct, na, nb, false);
+    k_ds_same_spin<T><<<(unsigned)nb, kDsThreads, 0, c->stream>>>(
+        nb, na, B.ns, B.nd, (const int32_t*)B.sJ.ptr, (const int32_t*)B.svo.ptr, P(B.sA64, B.sA32),
+        (const int32_t*)B.dJ.ptr, P(B.dval64, B.dval32), mm ? nullptr : P(A.W64, A.W32), d->n, ct, tmp);
+    QDKGB_CHECK_LAUNCH();
+    transpose<T>(c, tmp, y, nb, na, true);
+  };
   if constexpr (sizeof(T) == 4) {
     if (mm) {
+      // y = Haa x + x HbbT
+      auto dense = [&]() {
+        dim3 g((unsigned)((nb + kGmT - 1) / kGmT), (unsigned)((na + kGmT - 1) / kGmT));
+        k_ds_gemm2<<<g, 256, 0, c->stream>>>((int)na, (int)nb, (int)na, (int)nb, (const float*)d->Haa.ptr,
+                                              (const float*)x, (const float*)x, (const float*)d->HbbT.ptr,
+                                              (float*)y);
+        QDKGB_CHECK_LAUNCH();
+      };
+      if (d->dense_state < 0) {
+        // first FP32 sigma of this space: time both forms of the same-spin part
+        cudaEvent_t e[3];
+        for (cudaEvent_t& ev : e) QDKGB_CUDA(cudaEventCreate(&ev));
+        for (int form = 0; form < 2; ++form) {
+          form ? dense() : same_spin();  // warm
+          QDKGB_CUDA(cudaEventRecord(e[0], c->stream));
+          for (int r = 0; r < 3; ++r) form ? dense() : same_spin();
+          QDKGB_CUDA(cudaEventRecord(e[1], c->stream));
+          QDKGB_CUDA(cudaEventSynchronize(e[1]));
+          float ms = 0.f;
+          QDKGB_CUDA(cudaEventElapsedTime(&ms, e[0], e[1]));
+          d->dense_ms[form] = ms / 3.0;
+        }
+        for (cudaEvent_t& ev : e) QDKGB_CUDA(cudaEventDestroy(ev));
+        d->dense_state = d->dense_ms[1] < d->dense_ms[0] ? 1 : 0;
+      }
+      if (d->dense_state == 1)
+        dense();
+      else
+        same_spin();
+      // opposite spin + diagonal + the singles
       auto go = [&](auto kern) {
         kern<<<(unsigned)na, d->mm_threads, d->mm_smem, c->stream>>>(
-            (int)na, (int)nb, A.ns, d->mr, d->mrp, d->off_words, d->seg_max, (const int32_t*)A.sJ.ptr,
-            (const int32_t*)A.svo.ptr, (const float*)A.sA32.ptr, (const float*)A.W32.ptr, (const int32_t*)d->rs_of.ptr,
-            (const uint32_t*)d->lists.ptr, (const int32_t*)d->seg.ptr, (const float*)d->V2mm.ptr, d->n,
-            (const double*)c->H.diag.ptr, (const float*)x, (float*)y);
+            (int)na, (int)nb, A.ns, d->mr, d->mrp, d->off_u16, d->seg_max, d->mm_vec ? 1 : 0,
+            (const int32_t*)A.sJ.ptr, (const int32_t*)A.svo.ptr, (const float*)A.sA32.ptr, (const float*)A.W32.ptr,
+            (const int32_t*)d->rs_of.ptr, (const uint16_t*)d->lists.ptr, (const int32_t*)d->seg.ptr,
+            (const float*)d->V2mm.ptr, d->n, (const double*)c->H.diag.ptr, (const float*)x, (float*)y);
       };
-      switch (d->mm_jpt) {
-        case 1: go(k_ds_opposite_mm<1>); break;
-        case 2: go(k_ds_opposite_mm<2>); break;
-        case 4: go(k_ds_opposite_mm<4>); break;
-        case 8: go(k_ds_opposite_mm<8>); break;
-        case 12: go(k_ds_opposite_mm<12>); break;
-        default: go(k_ds_opposite_mm<16>); break;
+      if (d->mm_threads <= 320) {
+        switch (d->mm_jpt) {
+          case 2: go(k_ds_opposite_mm<2, false>); break;
+          case 4: go(k_ds_opposite_mm<4, false>); break;
+          case 6: go(k_ds_opposite_mm<6, false>); break;
+          case 8: go(k_ds_opposite_mm<8, false>); break;
+          case 12: go(k_ds_opposite_mm<12, false>); break;
+          case 16: go(k_ds_opposite_mm<16, false>); break;
+          default: go(k_ds_opposite_mm<24, false>); break;
+        }
+      } else {
+        switch (d->mm_jpt) {
+          case 2: go(k_ds_opposite_mm<2, true>); break;
+          case 4: go(k_ds_opposite_mm<4, true>); break;
+          case 6: go(k_ds_opposite_mm<6, true>); break;
+          case 8: go(k_ds_opposite_mm<8, true>); break;
+          case 12: go(k_ds_opposite_mm<12, true>); break;
+          default: go(k_ds_opposite_mm<16, true>); break;
+        }
       }
       QDKGB_CHECK_LAUNCH();
       return;
     }
   }
+  same_spin();
+  // opposite spin + diagonal
   const T* Vt = f64 ? (const T*)c->V.ptr : (const T*)d->V32.ptr;
   constexpr int KC = f64 ? 4 : 8;
   const size_t smem = ((size_t)KC * nb + (size_t)KC * d->n * d->n) * sizeof(T);
@@ -537,6 +758,42 @@ __global__ void k_diag_product(Integrals I, int64_t na, int64_t nb, const uint64
   }
 }
 
+// Values of every table from the current integrals (GPU).
+static void direct_values(Context* c, DirectSigma* d) {
+  spin_values(c, d->a);
+  if (!d->same) spin_values(c, d->b);
+  const int n = d->n;
+  const int64_t n4 = (int64_t)n * n * n * n;
+  float* V32 = dev_array<float>(c, d->V32, (size_t)n4);
+  const unsigned b4 = (unsigned)std::min<int64_t>((n4 + 255) / 256, (int64_t)c->sm_count * 8);
+  k_ds_v32<<<b4, 256, 0, c->stream>>>((const double*)c->V.ptr, V32, n4);
+  QDKGB_CHECK_LAUNCH();
+  if (!d->mm) return;
+  const int64_t tot = (int64_t)n * n * d->mrp;
+  k_ds_v2mm<<<(unsigned)std::min<int64_t>((tot + 255) / 256, (int64_t)c->sm_count * 8), 256, 0, c->stream>>>(
+      (const double*)c->V.ptr, (const int32_t*)d->rs_of.ptr, n, d->mr, d->mrp, (float*)d->V2mm.ptr);
+  QDKGB_CHECK_LAUNCH();
+  const SpinTables& A = d->a;
+  const SpinTables& B = d->same ? d->a : d->b;
+  const int64_t na = A.nstr, nb = B.nstr;
+  const char* env = std::getenv("QDKGB_DIRECT_DENSE");
+  if (env && env[0] == '0') {
+    d->dense_state = 0;
+    return;
+  }
+  float* Haa = dev_array<float>(c, d->Haa, (size_t)(na * na));
+  float* HbbT = dev_array<float>(c, d->HbbT, (size_t)(nb * nb));
+  QDKGB_CUDA(cudaMemsetAsync(Haa, 0, (size_t)(na * na) * 4, c->stream));
+  QDKGB_CUDA(cudaMemsetAsync(HbbT, 0, (size_t)(nb * nb) * 4, c->stream));
+  const int64_t fill = na * A.nd + nb * B.nd + nb * B.ns;
+  k_ds_dense_fill<<<(unsigned)std::min<int64_t>((fill + 255) / 256, (int64_t)c->sm_count * 8), 256, 0, c->stream>>>(
+      na, A.nd, (const int32_t*)A.dJ.ptr, (const float*)A.dval32.ptr, nb, B.nd, B.ns, (const int32_t*)B.dJ.ptr,
+      (const float*)B.dval32.ptr, (const int32_t*)B.sJ.ptr, (const int32_t*)B.svo.ptr, (const float*)B.sA32.ptr, Haa,
+      HbbT);
+  QDKGB_CHECK_LAUNCH();
+  if (env && env[0] == '1') d->dense_state = 1;
+}
+
 // Tables of the contraction form (k_ds_opposite_mm); leaves d->mm false
 // where they do not apply.
 static void build_mm_tables(Context* c, DirectSigma* d) {
@@ -550,15 +807,15 @@ static void build_mm_tables(Context* c, DirectSigma* d) {
   if (A.ns <= 0 || B.ns <= 0 || B.h_packed.size() != (size_t)nb * B.ns) return;
   const int mr = n * (n - 1), mrows = mr + n + 1, mrp = (mrows + 15) / 16 * 16;
   const int warps = mrp / 16;
-  if (warps > kMmMaxWarps || mrows >= (1 << 15)) return;
+  if (warps > kMmMaxWarps || mrp * kMmCols > (1 << 15)) return;
   const int threads = warps * 32;
   int jpt = (int)((nb + threads - 1) / threads);
-  for (int cand : {1, 2, 4, 8, 12, 16})
+  for (int cand : {2, 4, 6, 8, 12, 16, 24})
     if (jpt <= cand) {
       jpt = cand;
       break;
     }
-  if ((int64_t)jpt * threads < nb) return;
+  if ((int64_t)jpt * threads < nb || (threads > 320 && jpt > 16)) return;
   // pair index of each (v, o), v != o
   std::vector<int32_t> rmap(n2, -1), rs_of(mr);
   for (int rs = 0, r = 0; rs < n2; ++rs)
@@ -568,7 +825,7 @@ static void build_mm_tables(Context* c, DirectSigma* d) {
     }
   // per chunk: offsets (uint16) and entries of every beta string
   const int nchunk = (int)((nb + kMmCols - 1) / kMmCols);
-  const int off_words = (int)(((nb + 1) + 1) / 2 + 3) / 4 * 4;
+  const int off_u16 = (int)((nb + 1 + 7) / 8 * 8);
   std::vector<std::vector<std::pair<uint32_t, uint32_t>>> per(nb);  // (sort key, entry) by string
   for (int64_t ib = 0; ib < nb; ++ib) {
     auto& v = per[ib];
@@ -579,75 +836,72 @@ static void build_mm_tables(Context* c, DirectSigma* d) {
     }
     const uint64_t bits = c->dets.h_ubeta[ib];
     for (int p = 0; p < n; ++p)
-      if ((bits >> p) & 1) v.push_back({((uint32_t)ib << 16) | (uint32_t)(mr + p), (uint32_t)ib | ((uint32_t)(mr + p) << 16)});
+      if ((bits >> p) & 1)
+        v.push_back({((uint32_t)ib << 16) | (uint32_t)(mr + p), (uint32_t)ib | ((uint32_t)(mr + p) << 16)});
     v.push_back({((uint32_t)ib << 16) | (uint32_t)(mr + n), (uint32_t)ib | ((uint32_t)(mr + n) << 16)});
     std::sort(v.begin(), v.end());
   }
-  std::vector<uint32_t> lists;
+  std::vector<uint16_t> lists;
   std::vector<int32_t> seg(nchunk + 1);
   std::vector<size_t> cur(nb, 0);
   int seg_max = 0;
   for (int ch = 0; ch < nchunk; ++ch) {
     const uint32_t j0 = (uint32_t)ch * kMmCols, j1 = j0 + kMmCols;
     seg[ch] = (int32_t)lists.size();
-    std::vector<uint16_t> off(nb + 1);
-    std::vector<uint32_t> ent;
+    std::vector<uint16_t> off(off_u16, 0);
+    std::vector<uint16_t> ent;
     for (int64_t ib = 0; ib < nb; ++ib) {
       off[ib] = (uint16_t)ent.size();
       auto& v = per[ib];
       while (cur[ib] < v.size() && (v[cur[ib]].second & 0xffff) < j1) {
         const uint32_t w = v[cur[ib]++].second;
         const uint32_t jl = (w & 0xffff) - j0, r = (w >> 16) & 0x7fff;
-        ent.push_back(jl | (r << 8) | (w & 0x80000000u));
+        ent.push_back((uint16_t)((r * kMmCols + jl) | ((w >> 31) << 15)));
       }
       if (ent.size() > 65535) return;
     }
     off[nb] = (uint16_t)ent.size();
-    std::vector<uint32_t> words(off_words, 0);
-    std::memcpy(words.data(), off.data(), off.size() * 2);
-    lists.insert(lists.end(), words.begin(), words.end());
+    lists.insert(lists.end(), off.begin(), off.end());
     lists.insert(lists.end(), ent.begin(), ent.end());
-    while (lists.size() % 4) lists.push_back(0);
+    while (lists.size() % 8) lists.push_back(0);
     seg_max = std::max(seg_max, (int)(lists.size() - seg[ch]));
   }
   seg[nchunk] = (int32_t)lists.size();
   if (lists.size() >= (size_t)INT32_MAX) return;
   const int K = A.ns + 1;
-  const size_t smem = ((size_t)K * mrp + (size_t)2 * K * kMmCols + (size_t)mrp * kMmEStride) * 4 +
-                      (size_t)2 * seg_max * 4 + (size_t)K * 4;
+  const size_t smem = ((size_t)K * mrp + (size_t)2 * K * kMmCols + (size_t)mrp * kMmCols) * 4 +
+                      (size_t)2 * seg_max * 2 + (size_t)K * 4;
   if (smem > 220 * 1024) return;
-  // V2mm[pq][r]
-  std::vector<float> v2((size_t)n2 * mrp, 0.f);
-  const std::vector<double>& V = c->h_V;
-  for (int pq = 0; pq < n2; ++pq) {
-    for (int r = 0; r < mr; ++r) v2[(size_t)pq * mrp + r] = (float)V[pq + (size_t)n2 * rs_of[r]];
-    for (int p = 0; p < n; ++p) v2[(size_t)pq * mrp + mr + p] = (float)V[p + (size_t)n * p + (size_t)n2 * pq];
-  }
   auto up = [&](DeviceBuffer& b, const void* src, size_t bytes) {
     void* ptr = dev_alloc(c, b, bytes + 16);
     QDKGB_CUDA(cudaMemcpyAsync(ptr, src, bytes, cudaMemcpyHostToDevice, c->stream));
   };
-  up(d->V2mm, v2.data(), v2.size() * 4);
+  dev_array<float>(c, d->V2mm, (size_t)n2 * mrp);
   up(d->rs_of, rs_of.data(), rs_of.size() * 4);
-  up(d->lists, lists.data(), lists.size() * 4);
+  up(d->lists, lists.data(), lists.size() * 2);
   up(d->seg, seg.data(), seg.size() * 4);
-  for (const void* f : {(const void*)k_ds_opposite_mm<1>, (const void*)k_ds_opposite_mm<2>,
-                        (const void*)k_ds_opposite_mm<4>, (const void*)k_ds_opposite_mm<8>,
-                        (const void*)k_ds_opposite_mm<12>, (const void*)k_ds_opposite_mm<16>})
+  for (const void* f :
+       {(const void*)k_ds_opposite_mm<2, false>, (const void*)k_ds_opposite_mm<4, false>,
+        (const void*)k_ds_opposite_mm<6, false>, (const void*)k_ds_opposite_mm<8, false>,
+        (const void*)k_ds_opposite_mm<12, false>, (const void*)k_ds_opposite_mm<16, false>,
+        (const void*)k_ds_opposite_mm<24, false>, (const void*)k_ds_opposite_mm<2, true>,
+        (const void*)k_ds_opposite_mm<4, true>, (const void*)k_ds_opposite_mm<6, true>,
+        (const void*)k_ds_opposite_mm<8, true>, (const void*)k_ds_opposite_mm<12, true>,
+        (const void*)k_ds_opposite_mm<16, true>})
     set_max_dynamic_smem(f, 220 * 1024);
   d->mr = mr;
   d->mrp = mrp;
   d->mm_threads = threads;
   d->mm_jpt = jpt;
   d->seg_max = seg_max;
-  d->off_words = off_words;
+  d->off_u16 = off_u16;
+  d->mm_vec = nb % 4 == 0;
   d->mm_smem = smem;
   QDKGB_CUDA(cudaStreamSynchronize(c->stream));
   d->mm = true;
 }
 
-void build_direct_sigma(Context* c) {
-  NvtxRange nvtx_range("qdkgb.build_direct_sigma");
+static DirectSigma* direct_prepare(Context* c) {
   if (!c->have_ints) throw Error(QDKGB_ERR_STATE, "integrals not set");
   if (!c->have_dets) throw Error(QDKGB_ERR_STATE, "determinants not set");
   DetSpace& S = c->dets;
@@ -659,18 +913,65 @@ void build_direct_sigma(Context* c) {
   if (c->norb > 20) throw Error(QDKGB_ERR_UNSUPPORTED, "direct sigma supports up to 20 orbitals");
   if (S.h_galpha.empty() || S.h_galpha[0] == 0 || S.h_ubeta.empty() || S.h_ubeta[0] == 0)
     throw Error(QDKGB_ERR_UNSUPPORTED, "direct sigma needs at least one electron of each spin");
-  free_direct(c);
-  c->direct = new DirectSigma();
+  // structure once per determinant space (set_dets frees it), values from
+  // the current integrals on every build
+  auto env0 = [](const char* name) {
+    const char* e = std::getenv(name);
+    return e ? e[0] : (char)0;
+  };
+  const char mm_env = env0("QDKGB_DIRECT_MM"), dense_env = env0("QDKGB_DIRECT_DENSE");
+  if (c->direct && (c->direct->n != c->norb || c->direct->mm_env != mm_env)) free_direct(c);
+  if (c->direct && c->direct->dense_env != dense_env) c->direct->dense_state = -1;
+  if (!c->direct) {
+    c->direct = new DirectSigma();
+    DirectSigma* d = c->direct;
+    d->n = c->norb;
+    d->mm_env = mm_env;
+    build_spin_tables(c, S.h_galpha, d->a);
+    d->same = (S.h_galpha == S.h_ubeta);
+    if (!d->same) build_spin_tables(c, S.h_ubeta, d->b);
+    set_max_dynamic_smem((const void*)k_ds_opposite<double, 4>, 200 * 1024);
+    set_max_dynamic_smem((const void*)k_ds_opposite<float, 8>, 200 * 1024);
+    // contraction form of the FP32 sigma, where its tables and shared memory
+    // fit (QDKGB_DIRECT_MM=0 keeps the element-wise walk)
+    build_mm_tables(c, d);
+    d->a.h_packed.clear();
+    d->b.h_packed.clear();
+  }
   DirectSigma* d = c->direct;
-  d->n = c->norb;
-  build_spin_tables(c, S.h_galpha, d->a);
-  d->same = (S.h_galpha == S.h_ubeta);
-  if (!d->same) build_spin_tables(c, S.h_ubeta, d->b);
-  const size_t n4 = (size_t)d->n * d->n * d->n * d->n;
-  std::vector<float> v32(n4);
-  for (size_t i = 0; i < n4; ++i) v32[i] = (float)c->h_V[i];
-  float* V32 = dev_array<float>(c, d->V32, n4);
-  QDKGB_CUDA(cudaMemcpyAsync(V32, v32.data(), n4 * 4, cudaMemcpyHostToDevice, c->stream));
+  d->dense_env = dense_env;
+  direct_values(c, d);
+  return d;
+}
+
+void direct_plan(const Context* c, int* mm, int* dense, double* ms) {
+  const DirectSigma* d = c->direct;
+  if (mm) *mm = d && d->mm ? 1 : 0;
+  if (dense) *dense = d ? d->dense_state : -1;
+  if (ms) {
+    ms[0] = d ? d->dense_ms[0] : 0.;
+    ms[1] = d ? d->dense_ms[1] : 0.;
+  }
+}
+
+bool attach_direct_fp32(Context* c) {
+  NvtxRange nvtx_range("qdkgb.attach_direct_fp32");
+  const char* env = std::getenv("QDKGB_MIXED_FP32");
+  if (env && env[0] == 's') return false;  // "slab": the stored FP32 copy
+  DirectSigma* d = nullptr;
+  try {
+    d = direct_prepare(c);
+  } catch (const Error&) {
+    return false;
+  }
+  return d->mm;
+}
+
+void build_direct_sigma(Context* c) {
+  NvtxRange nvtx_range("qdkgb.build_direct_sigma");
+  c->fp32_direct = false;
+  direct_prepare(c);
+  DetSpace& S = c->dets;
   // diagonal and operator state
   Hcsr& H = c->H;
   H.valid = false;
@@ -680,13 +981,6 @@ void build_direct_sigma(Context* c) {
   k_diag_product<<<blocks, 256, 0, c->stream>>>(integrals_view(c), S.ngroups, S.nbeta,
                                                (const uint64_t*)S.galpha.ptr, (const uint64_t*)S.ubeta.ptr, D);
   QDKGB_CHECK_LAUNCH();
-  set_max_dynamic_smem((const void*)k_ds_opposite<double, 4>, 200 * 1024);
-  set_max_dynamic_smem((const void*)k_ds_opposite<float, 8>, 200 * 1024);
-  // contraction form of the FP32 sigma, where its tables and shared memory
-  // fit (QDKGB_DIRECT_MM=0 keeps the element-wise walk)
-  build_mm_tables(c, d);
-  d->a.h_packed.clear();
-  d->b.h_packed.clear();
   QDKGB_CUDA(cudaStreamSynchronize(c->stream));
   H.n = N;
   H.nnz = 0;

@@ -258,6 +258,7 @@ void build_det_space(Context* c, int64_t nd, const uint64_t* alpha, const uint64
   free_direct(c);
   free_struct(c);
   c->op_direct = false;
+  c->fp32_direct = false;
   if (nd <= 0) throw Error(QDKGB_ERR_INVALID, "empty determinant list");
   if (nd >= (int64_t)INT32_MAX) throw Error(QDKGB_ERR_UNSUPPORTED, "more than 2^31-1 determinants");
   D.ndets = nd;
@@ -596,6 +597,7 @@ void set_csr(Context* c, int64_t n, const int64_t* rowptr, const int64_t* colind
   H.valid = false;
   H.structured = false;
   c->op_direct = false;
+  c->fp32_direct = false;
   const int64_t nnz = rowptr[n] - rowptr[0];
   if (rowptr[0] != 0 || nnz < 0) throw Error(QDKGB_ERR_INVALID, "row pointers must start at 0 and not decrease");
   std::vector<int32_t> ci(std::max<int64_t>(nnz, 1));
@@ -664,9 +666,19 @@ void build_hamiltonian(Context* c, double thresh, int storage) {
   H.valid = false;
   H.structured = false;
   c->op_direct = false;
+  c->fp32_direct = false;
   // slab layout for complete spaces; its kept rule (nonzero stored value)
   // needs every kept element to stay nonzero in the split pair
   if (c->fci && (!(thresh > 0.) || thresh >= 1e-30)) {
+    // mixed form: the FP64 slab for the full-precision sigma and the direct
+    // contraction for the FP32 one, where it applies (no FP32 copy stored)
+    if (storage == QDKGB_H_SPLIT32) {
+      build_hamiltonian_struct(c, thresh, QDKGB_H_FP64);
+      if (H.structured && attach_direct_fp32(c)) {
+        c->fp32_direct = true;
+        return;
+      }
+    }
     build_hamiltonian_struct(c, thresh, storage);
     return;
   }
@@ -1211,6 +1223,7 @@ bool build_hamiltonian_patched(Context* c, double thresh, const std::vector<uint
   H.structured = false;
   H.valid = true;
   c->op_direct = false;
+  c->fp32_direct = false;
   return true;
 }
 

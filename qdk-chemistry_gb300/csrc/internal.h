@@ -146,6 +146,8 @@ struct Context {
   DirectSigma* direct = nullptr;  // recompute-on-the-fly operator (complete spaces)
   FciStruct* fci = nullptr;       // row-shape tables of a complete space (structured kernels)
   bool op_direct = false;         // Davidson / spmv use the direct sigma instead of the CSR
+  bool fp32_direct = false;       // complete space, mixed form: FP32 sigma by the direct contraction,
+                                  // full-precision sigma by the stored (FP64) slab
   // seconds spent by the last qdkgb_asci call in its phases: the determinant
   // search, the determinant-space set-up, the Hamiltonian build, Davidson;
   // and its asci_iter count
@@ -242,6 +244,13 @@ void k_diag_launch(Context* c, const Integrals& I, double* D, unsigned blocks);
 
 // direct.cu
 void build_direct_sigma(Context* c);
+// The FP32 sigma of a complete space through the direct contraction beside
+// the stored FP64 slab (mixed form); false where the contraction form does
+// not apply.
+bool attach_direct_fp32(Context* c);
+// The direct sigma's FP32 form: contraction in use, same-spin form (-1 not
+// yet timed, 0 element-wise, 1 dense) and the two forms' times (ms).
+void direct_plan(const Context* c, int* mm, int* dense, double* ms);
 void free_direct(Context* c);
 void direct_sigma_fp64(Context* c, const double* x, double* y);
 void direct_sigma_fp32(Context* c, const float* x, float* y);

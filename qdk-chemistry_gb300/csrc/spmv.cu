@@ -155,7 +155,7 @@ void spmv_fp64(Context* c, const double* x, double* y) {
 void spmv_fp32(Context* c, const float* x, float* y) {
   Hcsr& H = c->H;
   if (!H.valid) throw Error(QDKGB_ERR_STATE, "Hamiltonian not built");
-  if (c->op_direct) {
+  if (c->op_direct || c->fp32_direct) {
     direct_sigma_fp32(c, x, y);
     return;
   }

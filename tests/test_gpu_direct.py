@@ -68,6 +68,35 @@ def test_direct_fp32_contraction_matches_walk(ctx, pkg, monkeypatch, norb, na, n
     assert np.array_equal(ctx.spmv(x, capi.PREC_MIXED), ys["1"])  # reproducible
 
 
+@pytest.mark.parametrize("norb,na,nb,seed", [(12, 3, 3, 21), (11, 5, 4, 22), (8, 4, 4, 23)])
+def test_direct_fp32_dense_same_spin_matches_csr(ctx, pkg, monkeypatch, norb, na, nb, seed):
+    """The same-spin string-only part of the contraction form as two dense
+    FP32 products (QDKGB_DIRECT_DENSE=1) and as the element-wise kernels
+    (=0) both agree with the CSR sigma; the structure is kept across builds
+    of one space and the values follow new integrals."""
+    capi = pkg.capi
+    a, b = capi.fci_dets(norb, na, nb)
+    ctx.set_dets(a, b)
+    x = np.random.default_rng(seed).normal(size=len(a))
+    for k, s2 in enumerate((seed, seed + 100)):
+        T, V, _ = pkg.integrals.synthetic_integrals(norb, 2 * norb, s2)
+        ctx.set_integrals(T, V)
+        ctx.build_hamiltonian(0.0)
+        y_csr = ctx.spmv(x, capi.PREC_FP64)
+        scale = np.max(np.abs(y_csr))
+        for dense in ("1", "0"):
+            monkeypatch.setenv("QDKGB_DIRECT_DENSE", dense)
+            ctx.build_direct_sigma()
+            y32 = ctx.spmv(x, capi.PREC_MIXED)
+            assert np.max(np.abs(y32 - y_csr)) / scale < 1e-5, (k, dense)
+            y64 = ctx.spmv(x, capi.PREC_FP64)
+            assert np.max(np.abs(y64 - y_csr)) <= 1e-12 * scale, (k, dense)
+    monkeypatch.delenv("QDKGB_DIRECT_DENSE")
+    ctx.build_direct_sigma()  # the first FP32 sigma times both forms and keeps one
+    y32 = ctx.spmv(x, capi.PREC_MIXED)
+    assert np.max(np.abs(y32 - y_csr)) / scale < 1e-5
+
+
 def test_direct_davidson_fp64_and_mixed(ctx, pkg, oracle):
     capi = pkg.capi
     T, V, _ = pkg.integrals.synthetic_integrals(10, 20, seed=9)

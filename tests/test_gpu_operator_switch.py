@@ -50,7 +50,7 @@ def test_gb300_cas_uses_the_direct_sigma_under_a_memory_cap(pkg):
         calc.settings().set("calculate_one_rdm", True)
         E, wfn = calc.run(H, 4, 4)
         out[cap] = (E, wfn)
-    assert out[0][1].info["operator"] == "slab" and out[24 << 20][1].info["operator"] == "direct"
+    assert out[0][1].info["operator"] in ("slab", "slab+direct32") and out[24 << 20][1].info["operator"] == "direct"
     assert abs(out[0][0] - out[24 << 20][0]) < 1e-10
     g0 = sum(out[0][1].get_active_one_rdm_spin_dependent())
     g1 = sum(out[24 << 20][1].get_active_one_rdm_spin_dependent())
