@@ -154,13 +154,20 @@ def test_davidson_n2_casci_golden(ctx, pkg, n2_6e6o, known):
     assert np.isclose(E, known["n2_6e6o_casci"]["E_total"])
 
 
-def test_mixed_precision_energy(ctx, oracle, pkg, capi):
+@pytest.mark.parametrize("fp32", ["direct", "slab"])
+def test_mixed_precision_energy(ctx, oracle, pkg, capi, monkeypatch, fp32):
+    """Mixed form on a complete space with either FP32 sigma: the direct
+    contraction beside the FP64 slab (default) or the stored FP32 slab copy
+    (QDKGB_MIXED_FP32=slab)."""
     T, V, a, b = _cas(pkg, 10, 10, 20, seed=8)
     M = oracle.build_csr(oracle.Hamiltonian(T, V), a, b)
     Eo, _, _ = M.selected_ci_diag(tol=1e-9)
+    if fp32 == "slab":
+        monkeypatch.setenv("QDKGB_MIXED_FP32", "slab")
     ctx.set_integrals(T, V)
     ctx.set_dets(a, b)
     ctx.build_hamiltonian(storage=capi.H_SPLIT32)
+    assert ctx.operator_layout()[0] == (capi.OP_SLAB if fp32 == "slab" else capi.OP_SLAB_DIRECT32)
     E, C, info = ctx.davidson(tol=1e-8, precision=capi.PREC_MIXED)
     assert abs(E - Eo) < 1e-8, (E - Eo, info)
     assert info["residual_norm"] < 1e-8
@@ -325,6 +332,7 @@ def test_tma_fed_fp32_sigma_equals_register_fed(pkg, monkeypatch):
     a, b = capi.fci_dets(10, 5, 5)
     x = np.random.default_rng(5).normal(size=len(a)).astype(np.float32)
     out = {}
+    monkeypatch.setenv("QDKGB_MIXED_FP32", "slab")  # the stored FP32 copy
     for kern in capi.SIGMA32_KERNELS + (None,):
         if kern:
             monkeypatch.setenv("QDKGB_SIGMA32_KERNEL", kern)
