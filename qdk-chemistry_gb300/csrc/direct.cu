@@ -30,6 +30,7 @@
 
 #include "common.cuh"
 #include "internal.h"
+#include "tcgen05.cuh"
 
 namespace qdkgb {
 
@@ -108,6 +109,7 @@ struct DirectSigma {
   int dense_state = -1;
   double dense_ms[2] = {0., 0.};
   char mm_env = 0, dense_env = 0;  // QDKGB_DIRECT_MM / QDKGB_DIRECT_DENSE when built
+  bool tc = false;                 // dense products on the tensor cores (k_tc_gemm2)
   DeviceBuffer Haa, HbbT;
 };
 
@@ -645,6 +647,119 @@ __global__ void __launch_bounds__(256) k_ds_gemm2(int M, int N, int K1, int K2, 
   }
 }
 
+// Dense same-spin products on the tensor cores: out (M x N) = A1 B1 + A2 B2
+// (row-major FP32) as TF32 x 3 (each operand split into a TF32 high part and
+// the TF32 rounding of the remainder; hi hi + hi lo + lo hi, FP32 accumulation
+// in TMEM: about FP32 accuracy).  A CTA owns a 128 x 64 tile of out (TMEM
+// columns 0..63, lane = row); K runs in blocks of 32 through two shared-
+// memory stages: all threads load and split a block into the canonical
+// K-major layout, one thread issues the twelve MMAs (four K steps of 8, three
+// products) and commits them to the stage's mbarrier, which the threads wait
+// on (bounded) before refilling that stage.
+constexpr int kTcM = 128, kTcN = 64, kTcBK = 32, kTcThreads = 128;
+constexpr int kTcABytes = kTcM * kTcBK * 4, kTcBBytes = kTcN * kTcBK * 4;
+constexpr int kTcStage = 2 * kTcABytes + 2 * kTcBBytes;  // 48 KB
+constexpr uint32_t kTcSpin = 1u << 22;
+__device__ unsigned int g_tc_fault;  // set by a CTA whose wait timed out (its tile is NaN)
+
+__global__ void __launch_bounds__(kTcThreads) k_tc_gemm2(int M, int N, int K1, int K2, const float* __restrict__ A1,
+                                                         const float* __restrict__ B1, const float* __restrict__ A2,
+                                                         const float* __restrict__ B2, float* __restrict__ out) {
+  extern __shared__ __align__(128) unsigned char tc_smem[];
+  __shared__ __align__(8) uint64_t mbar[2];
+  __shared__ uint32_t tslot;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int m0 = blockIdx.y * kTcM, n0 = blockIdx.x * kTcN;
+  if (warp == 0) tc::tmem_alloc(&tslot, kTcN);
+  if (tid == 0) {
+    tc::mbar_init(&mbar[0], 1);
+    tc::mbar_init(&mbar[1], 1);
+    tc::mbar_init_fence();
+  }
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t tmem = tslot;
+  constexpr uint32_t idesc = tc::idesc_tf32(kTcM, kTcN);
+  constexpr uint32_t sbo = (kTcBK / 4) * 128;
+  const int nb1 = (K1 + kTcBK - 1) / kTcBK, nblk = nb1 + (K2 + kTcBK - 1) / kTcBK;
+  uint32_t par[2] = {0u, 0u};
+  bool ok = true;
+  for (int b = 0; b < nblk && ok; ++b) {
+    const int s = b & 1;
+    unsigned char* st = tc_smem + s * kTcStage;
+    unsigned char* Ahi = st;
+    unsigned char* Alo = st + kTcABytes;
+    unsigned char* Bhi = st + 2 * kTcABytes;
+    unsigned char* Blo = st + 2 * kTcABytes + kTcBBytes;
+    if (b >= 2) {  // the stage's previous MMAs (block b - 2) have read it
+      ok = tc::mbar_wait(&mbar[s], par[s], kTcSpin);
+      par[s] ^= 1u;
+      if (!ok) break;
+    }
+    const bool p2 = b >= nb1;
+    const float* A = p2 ? A2 : A1;
+    const float* B = p2 ? B2 : B1;
+    const int K = p2 ? K2 : K1, k0 = (p2 ? b - nb1 : b) * kTcBK;
+    for (int i = tid; i < kTcM * kTcBK; i += kTcThreads) {
+      const int r = i >> 5, k = i & 31;
+      const float v = (m0 + r < M && k0 + k < K) ? __ldg(A + (int64_t)(m0 + r) * K + k0 + k) : 0.f;
+      const float h = tc::to_tf32(v);
+      const uint32_t o = tc::kmajor_off(r, k, kTcBK);
+      *(float*)(Ahi + o) = h;
+      *(float*)(Alo + o) = tc::to_tf32(v - h);
+    }
+    for (int i = tid; i < kTcN * kTcBK; i += kTcThreads) {
+      const int k = i >> 6, n = i & 63;
+      const float v = (k0 + k < K && n0 + n < N) ? __ldg(B + (int64_t)(k0 + k) * N + n0 + n) : 0.f;
+      const float h = tc::to_tf32(v);
+      const uint32_t o = tc::kmajor_off(n, k, kTcBK);
+      *(float*)(Bhi + o) = h;
+      *(float*)(Blo + o) = tc::to_tf32(v - h);
+    }
+    tc::fence_proxy_async();
+    __syncthreads();
+    if (tid == 0) {
+      tc::fence_after();
+      const uint32_t ah = tc::smem_addr(Ahi), al = tc::smem_addr(Alo), bh = tc::smem_addr(Bhi), bl = tc::smem_addr(Blo);
+#pragma unroll
+      for (int ks = 0; ks < kTcBK / 8; ++ks) {
+        const uint32_t ko = ks * 256;  // two core matrices along K per step
+        tc::mma_tf32(tmem, tc::desc(ah + ko, 128, sbo), tc::desc(bh + ko, 128, sbo), idesc, (b | ks) ? 1u : 0u);
+        tc::mma_tf32(tmem, tc::desc(ah + ko, 128, sbo), tc::desc(bl + ko, 128, sbo), idesc, 1u);
+        tc::mma_tf32(tmem, tc::desc(al + ko, 128, sbo), tc::desc(bh + ko, 128, sbo), idesc, 1u);
+      }
+      tc::commit(&mbar[s]);
+    }
+  }
+  // the last (up to two) blocks' MMAs
+  for (int b = nblk >= 2 ? nblk - 2 : 0; ok && b < nblk; ++b) {
+    const int s = b & 1;
+    ok = tc::mbar_wait(&mbar[s], par[s], kTcSpin);
+    par[s] ^= 1u;
+  }
+  tc::fence_after();
+  const int row = m0 + warp * 32 + lane;
+#pragma unroll 1
+  for (int c = 0; c < kTcN; c += 16) {
+    float v[16];
+    if (ok) {
+      tc::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);
+    } else {
+#pragma unroll
+      for (int j = 0; j < 16; ++j) v[j] = __int_as_float(0x7fc00000);
+    }
+    if (row < M)
+#pragma unroll
+      for (int j = 0; j < 16; ++j)
+        if (n0 + c + j < N) out[(int64_t)row * N + n0 + c + j] = v[j];
+  }
+  tc::fence_before();
+  __syncthreads();
+  if (warp == 0) tc::tmem_free(tmem, kTcN);
+  if (!ok && tid == 0) atomicOr(&g_tc_fault, 1u);
+}
+
 template <typename T>
 static void direct_sigma_t(Context* c, const T* x, T* y) {
   DirectSigma* d = c->direct;
@@ -677,10 +792,17 @@ static void direct_sigma_t(Context* c, const T* x, T* y) {
     if (mm) {
       // y = Haa x + x HbbT
       auto dense = [&]() {
-        dim3 g((unsigned)((nb + kGmT - 1) / kGmT), (unsigned)((na + kGmT - 1) / kGmT));
-        k_ds_gemm2<<<g, 256, 0, c->stream>>>((int)na, (int)nb, (int)na, (int)nb, (const float*)d->Haa.ptr,
-                                              (const float*)x, (const float*)x, (const float*)d->HbbT.ptr,
-                                              (float*)y);
+        if (d->tc) {
+          dim3 g((unsigned)((nb + kTcN - 1) / kTcN), (unsigned)((na + kTcM - 1) / kTcM));
+          k_tc_gemm2<<<g, kTcThreads, 2 * kTcStage, c->stream>>>((int)na, (int)nb, (int)na, (int)nb,
+                                                                (const float*)d->Haa.ptr, (const float*)x,
+                                                                (const float*)x, (const float*)d->HbbT.ptr, (float*)y);
+        } else {
+          dim3 g((unsigned)((nb + kGmT - 1) / kGmT), (unsigned)((na + kGmT - 1) / kGmT));
+          k_ds_gemm2<<<g, 256, 0, c->stream>>>((int)na, (int)nb, (int)na, (int)nb, (const float*)d->Haa.ptr,
+                                                (const float*)x, (const float*)x, (const float*)d->HbbT.ptr,
+                                                (float*)y);
+        }
         QDKGB_CHECK_LAUNCH();
       };
       if (d->dense_state < 0) {
@@ -920,6 +1042,7 @@ static DirectSigma* direct_prepare(Context* c) {
     return e ? e[0] : (char)0;
   };
   const char mm_env = env0("QDKGB_DIRECT_MM"), dense_env = env0("QDKGB_DIRECT_DENSE");
+  const bool tc = env0("QDKGB_DIRECT_TC") == '1';
   if (c->direct && (c->direct->n != c->norb || c->direct->mm_env != mm_env)) free_direct(c);
   if (c->direct && c->direct->dense_env != dense_env) c->direct->dense_state = -1;
   if (!c->direct) {
@@ -940,6 +1063,9 @@ static DirectSigma* direct_prepare(Context* c) {
   }
   DirectSigma* d = c->direct;
   d->dense_env = dense_env;
+  if (tc != d->tc) d->dense_state = dense_env ? d->dense_state : -1;
+  d->tc = tc;
+  if (tc) set_max_dynamic_smem((const void*)k_tc_gemm2, 2 * kTcStage);
   direct_values(c, d);
   return d;
 }

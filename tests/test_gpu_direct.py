@@ -97,6 +97,33 @@ def test_direct_fp32_dense_same_spin_matches_csr(ctx, pkg, monkeypatch, norb, na
     assert np.max(np.abs(y32 - y_csr)) / scale < 1e-5
 
 
+@pytest.mark.parametrize("norb,na,nb,seed", [(6, 3, 3, 31), (10, 5, 4, 32), (12, 3, 3, 33)])
+def test_tensor_core_same_spin_products(ctx, pkg, monkeypatch, norb, na, nb, seed):
+    """The dense same-spin products on the tensor cores (tcgen05 TF32 x 3,
+    QDKGB_DIRECT_TC=1) agree with the CSR sigma to FP32 accuracy and with
+    the FMA-pipe products to rounding; shapes with partial 128 x 64 tiles
+    and K blocks."""
+    capi = pkg.capi
+    T, V, _ = pkg.integrals.synthetic_integrals(norb, 2 * norb, seed)
+    a, b = capi.fci_dets(norb, na, nb)
+    ctx.set_integrals(T, V)
+    ctx.set_dets(a, b)
+    ctx.build_hamiltonian(0.0)
+    x = np.random.default_rng(seed).normal(size=len(a))
+    y_csr = ctx.spmv(x, capi.PREC_FP64)
+    scale = np.max(np.abs(y_csr))
+    monkeypatch.setenv("QDKGB_DIRECT_DENSE", "1")
+    ys = {}
+    for tc in ("0", "1"):
+        monkeypatch.setenv("QDKGB_DIRECT_TC", tc)
+        ctx.build_direct_sigma()
+        ys[tc] = ctx.spmv(x, capi.PREC_MIXED)
+        assert np.all(np.isfinite(ys[tc])), tc
+        assert np.max(np.abs(ys[tc] - y_csr)) / scale < 1e-5, tc
+    assert np.max(np.abs(ys["1"] - ys["0"])) / scale < 1e-5
+    monkeypatch.delenv("QDKGB_DIRECT_TC")
+
+
 def test_direct_davidson_fp64_and_mixed(ctx, pkg, oracle):
     capi = pkg.capi
     T, V, _ = pkg.integrals.synthetic_integrals(10, 20, seed=9)
