@@ -109,7 +109,7 @@ struct DirectSigma {
   int dense_state = -1;
   double dense_ms[2] = {0., 0.};
   char mm_env = 0, dense_env = 0;  // QDKGB_DIRECT_MM / QDKGB_DIRECT_DENSE when built
-  bool tc = false;                 // dense products on the tensor cores (k_tc_gemm2)
+  bool tc = false;                 // dense products on the tensor cores (k_tc_gemm2; QDKGB_DIRECT_TC=0: FMA pipe)
   DeviceBuffer Haa, HbbT;
 };
 
@@ -1042,7 +1042,7 @@ static DirectSigma* direct_prepare(Context* c) {
     return e ? e[0] : (char)0;
   };
   const char mm_env = env0("QDKGB_DIRECT_MM"), dense_env = env0("QDKGB_DIRECT_DENSE");
-  const bool tc = env0("QDKGB_DIRECT_TC") == '1';
+  const bool tc = env0("QDKGB_DIRECT_TC") != '0';
   if (c->direct && (c->direct->n != c->norb || c->direct->mm_env != mm_env)) free_direct(c);
   if (c->direct && c->direct->dense_env != dense_env) c->direct->dense_state = -1;
   if (!c->direct) {

@@ -100,9 +100,9 @@ def test_direct_fp32_dense_same_spin_matches_csr(ctx, pkg, monkeypatch, norb, na
 @pytest.mark.parametrize("norb,na,nb,seed", [(6, 3, 3, 31), (10, 5, 4, 32), (12, 3, 3, 33)])
 def test_tensor_core_same_spin_products(ctx, pkg, monkeypatch, norb, na, nb, seed):
     """The dense same-spin products on the tensor cores (tcgen05 TF32 x 3,
-    QDKGB_DIRECT_TC=1) agree with the CSR sigma to FP32 accuracy and with
-    the FMA-pipe products to rounding; shapes with partial 128 x 64 tiles
-    and K blocks."""
+    the default; QDKGB_DIRECT_TC=0 the FMA pipe) agree with the CSR sigma to
+    FP32 accuracy and with the FMA-pipe products to rounding; shapes with
+    partial 128 x 64 tiles and K blocks."""
     capi = pkg.capi
     T, V, _ = pkg.integrals.synthetic_integrals(norb, 2 * norb, seed)
     a, b = capi.fci_dets(norb, na, nb)
