@@ -662,9 +662,79 @@ constexpr int kTcStage = 2 * kTcABytes + 2 * kTcBBytes;  // 48 KB
 constexpr uint32_t kTcSpin = 1u << 22;
 __device__ unsigned int g_tc_fault;  // set by a CTA whose wait timed out (its tile is NaN)
 
-__global__ void __launch_bounds__(kTcThreads) k_tc_gemm2(int M, int N, int K1, int K2, const float* __restrict__ A1,
-                                                         const float* __restrict__ B1, const float* __restrict__ A2,
-                                                         const float* __restrict__ B2, float* __restrict__ out) {
+// Block b of the K loop, loaded into registers: A rows m0.. (128 x 32) as
+// 8 chunks of 4 consecutive K per thread, B (32 x 64, K-major in shared
+// memory) as 4 chunks of 4 K per thread; chunk c of an operand lands at byte
+// 16 c of its K-major layout (core matrix c / 8, row c % 8), so a warp's
+// stores fill 512 contiguous bytes.
+struct TcRegs {
+  float a[8][4], b[4][4];
+};
+
+__device__ __forceinline__ void tc_load(TcRegs& R, int b, int nb1, int M, int N, int K1, int K2, bool vecA,
+                                        const float* __restrict__ A1, const float* __restrict__ B1,
+                                        const float* __restrict__ A2, const float* __restrict__ B2, int m0, int n0,
+                                        int tid) {
+  const bool p2 = b >= nb1;
+  const float* A = p2 ? A2 : A1;
+  const float* B = p2 ? B2 : B1;
+  const int K = p2 ? K2 : K1, k0 = (p2 ? b - nb1 : b) * kTcBK;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const int c = tid + j * kTcThreads, cm = c >> 3, r = (cm >> 3) * 8 + (c & 7), k = k0 + (cm & 7) * 4;
+    const int64_t base = (int64_t)(m0 + r) * K + k;
+    if (m0 + r < M && vecA && k + 3 < K) {
+      const float4 v = __ldg((const float4*)(A + base));
+      R.a[j][0] = v.x;
+      R.a[j][1] = v.y;
+      R.a[j][2] = v.z;
+      R.a[j][3] = v.w;
+    } else {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) R.a[j][q] = (m0 + r < M && k + q < K) ? __ldg(A + base + q) : 0.f;
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int c = tid + j * kTcThreads, cm = c >> 3, n = (cm >> 3) * 8 + (c & 7), k = k0 + (cm & 7) * 4;
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      R.b[j][q] = (n0 + n < N && k + q < K) ? __ldg(B + (int64_t)(k + q) * N + n0 + n) : 0.f;
+  }
+}
+
+__device__ __forceinline__ void tc_store(const TcRegs& R, unsigned char* Ahi, unsigned char* Alo,
+                                         unsigned char* Bhi, unsigned char* Blo, int tid) {
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    float h[4], l[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      h[q] = tc::to_tf32(R.a[j][q]);
+      l[q] = tc::to_tf32(R.a[j][q] - h[q]);
+    }
+    const int c = tid + j * kTcThreads;
+    *(float4*)(Ahi + 16 * c) = make_float4(h[0], h[1], h[2], h[3]);
+    *(float4*)(Alo + 16 * c) = make_float4(l[0], l[1], l[2], l[3]);
+  }
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    float h[4], l[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      h[q] = tc::to_tf32(R.b[j][q]);
+      l[q] = tc::to_tf32(R.b[j][q] - h[q]);
+    }
+    const int c = tid + j * kTcThreads;
+    *(float4*)(Bhi + 16 * c) = make_float4(h[0], h[1], h[2], h[3]);
+    *(float4*)(Blo + 16 * c) = make_float4(l[0], l[1], l[2], l[3]);
+  }
+}
+
+__global__ void __launch_bounds__(kTcThreads) k_tc_gemm2(int M, int N, int K1, int K2, int vecA,
+                                                         const float* __restrict__ A1, const float* __restrict__ B1,
+                                                         const float* __restrict__ A2, const float* __restrict__ B2,
+                                                         float* __restrict__ out) {
   extern __shared__ __align__(128) unsigned char tc_smem[];
   __shared__ __align__(8) uint64_t mbar[2];
   __shared__ uint32_t tslot;
@@ -683,8 +753,10 @@ __global__ void __launch_bounds__(kTcThreads) k_tc_gemm2(int M, int N, int K1, i
   constexpr uint32_t idesc = tc::idesc_tf32(kTcM, kTcN);
   constexpr uint32_t sbo = (kTcBK / 4) * 128;
   const int nb1 = (K1 + kTcBK - 1) / kTcBK, nblk = nb1 + (K2 + kTcBK - 1) / kTcBK;
-  uint32_t par[2] = {0u, 0u};
+  uint32_t par0 = 0u, par1 = 0u;
   bool ok = true;
+  TcRegs R;
+  tc_load(R, 0, nb1, M, N, K1, K2, vecA != 0, A1, B1, A2, B2, m0, n0, tid);
   for (int b = 0; b < nblk && ok; ++b) {
     const int s = b & 1;
     unsigned char* st = tc_smem + s * kTcStage;
@@ -693,30 +765,14 @@ __global__ void __launch_bounds__(kTcThreads) k_tc_gemm2(int M, int N, int K1, i
     unsigned char* Bhi = st + 2 * kTcABytes;
     unsigned char* Blo = st + 2 * kTcABytes + kTcBBytes;
     if (b >= 2) {  // the stage's previous MMAs (block b - 2) have read it
-      ok = tc::mbar_wait(&mbar[s], par[s], kTcSpin);
-      par[s] ^= 1u;
+      ok = tc::mbar_wait(&mbar[s], s ? par1 : par0, kTcSpin);
+      if (s)
+        par1 ^= 1u;
+      else
+        par0 ^= 1u;
       if (!ok) break;
     }
-    const bool p2 = b >= nb1;
-    const float* A = p2 ? A2 : A1;
-    const float* B = p2 ? B2 : B1;
-    const int K = p2 ? K2 : K1, k0 = (p2 ? b - nb1 : b) * kTcBK;
-    for (int i = tid; i < kTcM * kTcBK; i += kTcThreads) {
-      const int r = i >> 5, k = i & 31;
-      const float v = (m0 + r < M && k0 + k < K) ? __ldg(A + (int64_t)(m0 + r) * K + k0 + k) : 0.f;
-      const float h = tc::to_tf32(v);
-      const uint32_t o = tc::kmajor_off(r, k, kTcBK);
-      *(float*)(Ahi + o) = h;
-      *(float*)(Alo + o) = tc::to_tf32(v - h);
-    }
-    for (int i = tid; i < kTcN * kTcBK; i += kTcThreads) {
-      const int k = i >> 6, n = i & 63;
-      const float v = (k0 + k < K && n0 + n < N) ? __ldg(B + (int64_t)(k0 + k) * N + n0 + n) : 0.f;
-      const float h = tc::to_tf32(v);
-      const uint32_t o = tc::kmajor_off(n, k, kTcBK);
-      *(float*)(Bhi + o) = h;
-      *(float*)(Blo + o) = tc::to_tf32(v - h);
-    }
+    tc_store(R, Ahi, Alo, Bhi, Blo, tid);
     tc::fence_proxy_async();
     __syncthreads();
     if (tid == 0) {
@@ -731,12 +787,16 @@ __global__ void __launch_bounds__(kTcThreads) k_tc_gemm2(int M, int N, int K1, i
       }
       tc::commit(&mbar[s]);
     }
+    if (b + 1 < nblk) tc_load(R, b + 1, nb1, M, N, K1, K2, vecA != 0, A1, B1, A2, B2, m0, n0, tid);
   }
   // the last (up to two) blocks' MMAs
   for (int b = nblk >= 2 ? nblk - 2 : 0; ok && b < nblk; ++b) {
     const int s = b & 1;
-    ok = tc::mbar_wait(&mbar[s], par[s], kTcSpin);
-    par[s] ^= 1u;
+    ok = tc::mbar_wait(&mbar[s], s ? par1 : par0, kTcSpin);
+    if (s)
+      par1 ^= 1u;
+    else
+      par0 ^= 1u;
   }
   tc::fence_after();
   const int row = m0 + warp * 32 + lane;
@@ -794,7 +854,8 @@ static void direct_sigma_t(Context* c, const T* x, T* y) {
       auto dense = [&]() {
         if (d->tc) {
           dim3 g((unsigned)((nb + kTcN - 1) / kTcN), (unsigned)((na + kTcM - 1) / kTcM));
-          k_tc_gemm2<<<g, kTcThreads, 2 * kTcStage, c->stream>>>((int)na, (int)nb, (int)na, (int)nb,
+          const int vec = (na % 4 == 0 && nb % 4 == 0 && ((uintptr_t)x & 15) == 0) ? 1 : 0;
+          k_tc_gemm2<<<g, kTcThreads, 2 * kTcStage, c->stream>>>((int)na, (int)nb, (int)na, (int)nb, vec,
                                                                 (const float*)d->Haa.ptr, (const float*)x,
                                                                 (const float*)x, (const float*)d->HbbT.ptr, (float*)y);
         } else {
