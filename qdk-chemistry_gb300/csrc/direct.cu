@@ -62,8 +62,11 @@ inline HSingle hsingle(uint64_t bra, uint64_t ket, uint64_t ex) {
 }  // namespace
 
 // FP32 contraction form (k_ds_opposite_mm): beta strings J_b in chunks of
-// kMmCols; E rows 16 per warp, each thread 4 rows x 8 columns.
+// kMmCols; E rows 16 per warp, each thread 4 rows x 8 columns; E rows
+// kMmEStride floats apart in shared memory (16-byte rows that start four
+// banks apart).
 constexpr int kMmCols = 64;
+constexpr int kMmEStride = kMmCols + 4;
 constexpr int kMmMaxWarps = 16;
 
 // One spin's string tables.  Structure (built once per determinant space):
@@ -93,7 +96,7 @@ struct DirectSigma {
   // V2mm[pq][r]: V(pq, rs_r) for r < mr, V(p p | pq) for r = mr + p, else 0.
   // lists (uint16): per chunk of kMmCols beta strings, the (nb + 1) offsets
   // of each beta string's entries (padded to 16 bytes) then the entries
-  // (r kMmCols + jl) | neg << 15 (jl = J_b - chunk start: the entry's place
+  // (r kMmEStride + jl) | neg << 15 (jl = J_b - chunk start: the entry's place
   // in E), each string's sorted by (J_b, r); seg[c] = the chunk's first
   // element (16-byte aligned); off_u16 = the padded offset count
   bool mm = false;
@@ -110,6 +113,11 @@ struct DirectSigma {
   double dense_ms[2] = {0., 0.};
   char mm_env = 0, dense_env = 0;  // QDKGB_DIRECT_MM / QDKGB_DIRECT_DENSE when built
   bool tc = false;                 // dense products on the tensor cores (k_tc_gemm2; QDKGB_DIRECT_TC=0: FMA pipe)
+  // the contraction's E on the tensor cores (k_ds_opposite_tc): K padded to
+  // kpad, its shared memory, beta strings per thread
+  bool otc = false;
+  int kpad = 0, otc_jpt = 0;
+  size_t otc_smem = 0;
   DeviceBuffer Haa, HbbT;
 };
 
@@ -393,8 +401,8 @@ __global__ void __launch_bounds__(BIG ? kMmMaxWarps * 32 : 320, BIG ? 1 : 2)
   const int K = nsa + 1;
   float* Vp = (float*)smem_raw;                           // [K][mrp]
   float* G = Vp + (size_t)K * mrp;                        // [2][K][kMmCols]
-  float* E = G + (size_t)2 * K * kMmCols;                 // [mrp][kMmCols]
-  uint16_t* L = (uint16_t*)(E + (size_t)mrp * kMmCols);   // [2][seg_max]
+  float* E = G + (size_t)2 * K * kMmCols;                 // [mrp][kMmEStride]
+  uint16_t* L = (uint16_t*)(E + (size_t)mrp * kMmEStride);  // [2][seg_max]
   int32_t* Jrow = (int32_t*)(L + (size_t)2 * seg_max);    // [K]
   const int64_t Ia = blockIdx.x;
   const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31, warp = tid >> 5;
@@ -472,7 +480,7 @@ __global__ void __launch_bounds__(BIG ? kMmMaxWarps * 32 : 320, BIG ? 1 : 2)
       }
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
-        float* e = E + (size_t)(warp * 16 + ty * 4 + i) * kMmCols + tx * 4;
+        float* e = E + (size_t)(warp * 16 + ty * 4 + i) * kMmEStride + tx * 4;
         *(float4*)e = make_float4(a[i][0], a[i][1], a[i][2], a[i][3]);
         *(float4*)(e + 32) = make_float4(a[i][4], a[i][5], a[i][6], a[i][7]);
       }
@@ -820,6 +828,209 @@ __global__ void __launch_bounds__(kTcThreads) k_tc_gemm2(int M, int N, int K1, i
   if (!ok && tid == 0) atomicOr(&g_tc_fault, 1u);
 }
 
+// The contraction form with E formed on the tensor cores (tcgen05, TF32 x 3;
+// the same terms and walk as k_ds_opposite_mm).  Per alpha string: the A
+// operand Vp^T (rows r, K = the singles and the own row, zero-padded to kpad)
+// is split once into TF32 high and low parts in the canonical K-major layout,
+// two M tiles of 128 rows (the second holds the rows past 128; its MMA reads
+// on into the following shared memory for the lanes that are never read).
+// Per chunk of 64 beta strings: the C rows are copied in (cp.async), split
+// into the B operand, one thread issues the 2 tiles x kpad / 8 steps x 3
+// products into TMEM (128 columns: tile t at column 64 t) and commits to an
+// mbarrier; the eight warps read E out of TMEM (warp w: lanes 32 (w % 4)..,
+// tile w / 4) into shared memory and walk it as the FMA kernel does.
+constexpr int kOtThreads = 256;
+
+template <int JPT>
+__global__ void __launch_bounds__(kOtThreads, 1)
+    k_ds_opposite_tc(int na, int nb, int nsa, int mr, int mrows, int kpad, int off_u16, int seg_max, int vec,
+                     const int32_t* __restrict__ a_sJ, const int32_t* __restrict__ a_svo,
+                     const float* __restrict__ a_sA, const float* __restrict__ a_W, const int32_t* __restrict__ rs_of,
+                     const uint16_t* __restrict__ lists, const int32_t* __restrict__ seg,
+                     const float* __restrict__ V2, int mrp, int n, const double* __restrict__ D,
+                     const float* __restrict__ C, float* __restrict__ sigma) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t mbar;
+  __shared__ uint32_t tslot;
+  const int K = nsa + 1, kq4 = kpad >> 2;
+  const int rows1 = (mrows > 128 ? ((mrows - 128 + 7) & ~7) : 0);  // rows held for tile 1
+  const int abytes = (128 + rows1) * kpad * 4, bbytes = 64 * kpad * 4;
+  unsigned char* Ahi = smem_raw;
+  unsigned char* Alo = Ahi + abytes;
+  unsigned char* Bhi = Alo + abytes;
+  unsigned char* Blo = Bhi + bbytes;
+  float* G = (float*)(Blo + bbytes);                              // [2][K][kMmCols]
+  float* E = G + (size_t)2 * K * kMmCols;                         // [mrows][kMmEStride]
+  uint16_t* L = (uint16_t*)(E + (size_t)((mrows + 3) & ~3) * kMmEStride);  // [2][seg_max]
+  int32_t* Jrow = (int32_t*)(L + (size_t)2 * seg_max);            // [K]
+  const int64_t Ia = blockIdx.x;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (warp == 0) tc::tmem_alloc(&tslot, 128);
+  if (tid == 0) {
+    tc::mbar_init(&mbar, 1);
+    tc::mbar_init_fence();
+  }
+  // A operand: element (r, k) of tile t = r / 128 at byte 16 c of the tile,
+  // c = ((r % 128) / 8 * kq4 + k / 4) * 8 + r % 8
+  const int nA = (128 + rows1) * kq4;  // 16-byte chunks, both tiles (tile 1 only its held rows)
+  for (int ci = tid; ci < nA; ci += kOtThreads) {
+    const int t = ci >= 128 * kq4 ? 1 : 0;
+    const int c = ci - t * 128 * kq4;
+    const int cm = c >> 3, rr = c & 7;
+    const int r = t * 128 + (cm / kq4) * 8 + rr, k0 = (cm % kq4) * 4;
+    float h[4], l[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int k = k0 + q;
+      float v = 0.f;
+      if (r < mrows) {
+        if (k < nsa) {
+          const int32_t vo = __ldg(a_svo + Ia * nsa + k);
+          const int pq = (vo & 0xff) + n * ((vo >> 8) & 0xff);
+          v = (r == mr + n) ? __ldg(a_sA + Ia * nsa + k) : __ldg(V2 + (size_t)pq * mrp + r);
+          v = negate_if<float>(v, (vo >> 16) != 0);
+        } else if (k == nsa && r < mr) {
+          v = __ldg(a_W + (int64_t)__ldg(rs_of + r) * na + Ia);
+        }
+      }
+      h[q] = tc::to_tf32(v);
+      l[q] = tc::to_tf32(v - h[q]);
+    }
+    const int off = t * 128 * kpad * 4 + 16 * c;
+    *(float4*)(Ahi + off) = make_float4(h[0], h[1], h[2], h[3]);
+    *(float4*)(Alo + off) = make_float4(l[0], l[1], l[2], l[3]);
+  }
+  for (int k = tid; k < K; k += kOtThreads) Jrow[k] = k < nsa ? __ldg(a_sJ + Ia * nsa + k) : (int32_t)Ia;
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t tmem = tslot;
+  auto stage = [&](int chunk, int buf) {
+    const int j0 = chunk * kMmCols;
+    float* g = G + (size_t)buf * K * kMmCols;
+    if (vec) {
+      for (int i = tid; i < K * (kMmCols / 4); i += kOtThreads) {
+        const int k = i / (kMmCols / 4), j = 4 * (i - k * (kMmCols / 4));
+        const bool ok = j0 + j < nb;
+        const unsigned sa = (unsigned)__cvta_generic_to_shared(g + k * kMmCols + j);
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(sa),
+                     "l"(C + (int64_t)Jrow[k] * nb + (ok ? j0 + j : 0)), "r"(ok ? 16 : 0)
+                     : "memory");
+      }
+    } else {
+      for (int i = tid; i < K * kMmCols; i += kOtThreads) {
+        const int k = i / kMmCols, j = i - k * kMmCols;
+        const bool ok = j0 + j < nb;
+        cp_async4_zfill(g + i, C + (int64_t)Jrow[k] * nb + (ok ? j0 + j : 0), ok);
+      }
+    }
+    const int u0 = __ldg(seg + chunk), nv = (__ldg(seg + chunk + 1) - u0) >> 3;
+    uint16_t* l = L + (size_t)buf * seg_max;
+    for (int i = tid; i < nv; i += kOtThreads) cp_async16(l + 8 * i, lists + u0 + 8 * i);
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+  };
+  float acc[JPT];
+#pragma unroll
+  for (int j = 0; j < JPT; ++j) {
+    const int Ib = tid + j * kOtThreads;
+    acc[j] = Ib < nb ? sigma[Ia * nb + Ib] + (float)D[Ia * nb + Ib] * C[Ia * nb + Ib] : 0.f;
+  }
+  constexpr uint32_t idesc = tc::idesc_tf32(128, kMmCols);
+  const uint32_t sbo = (uint32_t)kq4 * 128;
+  const int nchunk = (nb + kMmCols - 1) / kMmCols;
+  uint32_t parity = 0u;
+  bool ok = true;
+  stage(0, 0);
+  for (int c = 0; c < nchunk && ok; ++c) {
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    __syncthreads();  // chunk c staged; B, E and buffer (c + 1) & 1 free
+    if (c + 1 < nchunk) stage(c + 1, (c + 1) & 1);
+    // B operand: element (j, k) at byte 16 c of Bhi / Blo, c = (j / 8 * kq4 + k / 4) * 8 + j % 8
+    const float* g = G + (size_t)(c & 1) * K * kMmCols;
+    for (int ci = tid; ci < kMmCols * kq4; ci += kOtThreads) {
+      const int cm = ci >> 3, j = (cm / kq4) * 8 + (ci & 7), k0 = (cm % kq4) * 4;
+      float h[4], l[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const float v = k0 + q < K ? g[(k0 + q) * kMmCols + j] : 0.f;
+        h[q] = tc::to_tf32(v);
+        l[q] = tc::to_tf32(v - h[q]);
+      }
+      *(float4*)(Bhi + 16 * ci) = make_float4(h[0], h[1], h[2], h[3]);
+      *(float4*)(Blo + 16 * ci) = make_float4(l[0], l[1], l[2], l[3]);
+    }
+    tc::fence_proxy_async();
+    __syncthreads();
+    if (tid == 0) {
+      tc::fence_after();
+      const uint32_t ah = tc::smem_addr(Ahi), al = tc::smem_addr(Alo), bh = tc::smem_addr(Bhi),
+                     bl = tc::smem_addr(Blo);
+      const int ntile = mrows > 128 ? 2 : 1;
+      for (int t = 0; t < ntile; ++t) {
+        const uint32_t to = (uint32_t)(t * 128 * kpad * 4), dt = tmem + (uint32_t)(t * kMmCols);
+        for (int ks = 0; ks < kpad / 8; ++ks) {
+          const uint32_t ko = ks * 256;
+          tc::mma_tf32(dt, tc::desc(ah + to + ko, 128, sbo), tc::desc(bh + ko, 128, sbo), idesc, ks ? 1u : 0u);
+          tc::mma_tf32(dt, tc::desc(ah + to + ko, 128, sbo), tc::desc(bl + ko, 128, sbo), idesc, 1u);
+          tc::mma_tf32(dt, tc::desc(al + to + ko, 128, sbo), tc::desc(bh + ko, 128, sbo), idesc, 1u);
+        }
+      }
+      tc::commit(&mbar);
+    }
+    ok = tc::mbar_wait(&mbar, parity, kTcSpin);
+    parity ^= 1u;
+    if (!ok) break;
+    tc::fence_after();
+    {
+      const int q = warp & 3, t = warp >> 2;
+      const int row = t * 128 + q * 32 + lane;
+      if (t * 128 < mrows) {
+#pragma unroll 1
+        for (int cb = 0; cb < kMmCols; cb += 16) {
+          float v[16];
+          tc::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(t * kMmCols + cb), v);
+          if (row < mrows) {
+            float* e = E + (size_t)row * kMmEStride + cb;
+#pragma unroll
+            for (int i = 0; i < 16; i += 4) *(float4*)(e + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+          }
+        }
+      }
+    }
+    tc::fence_before();
+    __syncthreads();
+    const uint16_t* off = L + (size_t)(c & 1) * seg_max;
+    const uint16_t* ent = off + off_u16;
+#pragma unroll
+    for (int j = 0; j < JPT; ++j) {
+      const int Ib = tid + j * kOtThreads;
+      if (Ib < nb) {
+        const int e1 = off[Ib + 1];
+        float s = acc[j];
+        for (int e = off[Ib]; e < e1; ++e) {
+          const uint32_t w = ent[e];
+          s += negate_if<float>(E[w & 0x7fff], (w >> 15) != 0);
+        }
+        acc[j] = s;
+      }
+    }
+  }
+  if (!ok) {
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+#pragma unroll
+    for (int j = 0; j < JPT; ++j) acc[j] = __int_as_float(0x7fc00000);
+    if (tid == 0) atomicOr(&g_tc_fault, 1u);
+  }
+#pragma unroll
+  for (int j = 0; j < JPT; ++j) {
+    const int Ib = tid + j * kOtThreads;
+    if (Ib < nb) sigma[Ia * nb + Ib] = acc[j];
+  }
+  tc::fence_before();
+  __syncthreads();
+  if (warp == 0) tc::tmem_free(tmem, 128);
+}
+
 template <typename T>
 static void direct_sigma_t(Context* c, const T* x, T* y) {
   DirectSigma* d = c->direct;
@@ -895,6 +1106,24 @@ static void direct_sigma_t(Context* c, const T* x, T* y) {
             (const int32_t*)d->rs_of.ptr, (const uint16_t*)d->lists.ptr, (const int32_t*)d->seg.ptr,
             (const float*)d->V2mm.ptr, d->n, (const double*)c->H.diag.ptr, (const float*)x, (float*)y);
       };
+      if (d->otc) {
+        auto gt = [&](auto kern) {
+          kern<<<(unsigned)na, kOtThreads, d->otc_smem, c->stream>>>(
+              (int)na, (int)nb, A.ns, d->mr, d->mr + d->n + 1, d->kpad, d->off_u16, d->seg_max, d->mm_vec ? 1 : 0,
+              (const int32_t*)A.sJ.ptr, (const int32_t*)A.svo.ptr, (const float*)A.sA32.ptr,
+              (const float*)A.W32.ptr, (const int32_t*)d->rs_of.ptr, (const uint16_t*)d->lists.ptr,
+              (const int32_t*)d->seg.ptr, (const float*)d->V2mm.ptr, d->mrp, d->n, (const double*)c->H.diag.ptr,
+              (const float*)x, (float*)y);
+        };
+        switch (d->otc_jpt) {
+          case 4: gt(k_ds_opposite_tc<4>); break;
+          case 8: gt(k_ds_opposite_tc<8>); break;
+          case 12: gt(k_ds_opposite_tc<12>); break;
+          default: gt(k_ds_opposite_tc<16>); break;
+        }
+        QDKGB_CHECK_LAUNCH();
+        return;
+      }
       if (d->mm_threads <= 320) {
         switch (d->mm_jpt) {
           case 2: go(k_ds_opposite_mm<2, false>); break;
@@ -990,7 +1219,7 @@ static void build_mm_tables(Context* c, DirectSigma* d) {
   if (A.ns <= 0 || B.ns <= 0 || B.h_packed.size() != (size_t)nb * B.ns) return;
   const int mr = n * (n - 1), mrows = mr + n + 1, mrp = (mrows + 15) / 16 * 16;
   const int warps = mrp / 16;
-  if (warps > kMmMaxWarps || mrp * kMmCols > (1 << 15)) return;
+  if (warps > kMmMaxWarps || mrp * kMmEStride > (1 << 15)) return;
   const int threads = warps * 32;
   int jpt = (int)((nb + threads - 1) / threads);
   for (int cand : {2, 4, 6, 8, 12, 16, 24})
@@ -1039,7 +1268,7 @@ static void build_mm_tables(Context* c, DirectSigma* d) {
       while (cur[ib] < v.size() && (v[cur[ib]].second & 0xffff) < j1) {
         const uint32_t w = v[cur[ib]++].second;
         const uint32_t jl = (w & 0xffff) - j0, r = (w >> 16) & 0x7fff;
-        ent.push_back((uint16_t)((r * kMmCols + jl) | ((w >> 31) << 15)));
+        ent.push_back((uint16_t)((r * kMmEStride + jl) | ((w >> 31) << 15)));
       }
       if (ent.size() > 65535) return;
     }
@@ -1052,7 +1281,7 @@ static void build_mm_tables(Context* c, DirectSigma* d) {
   seg[nchunk] = (int32_t)lists.size();
   if (lists.size() >= (size_t)INT32_MAX) return;
   const int K = A.ns + 1;
-  const size_t smem = ((size_t)K * mrp + (size_t)2 * K * kMmCols + (size_t)mrp * kMmCols) * 4 +
+  const size_t smem = ((size_t)K * mrp + (size_t)2 * K * kMmCols + (size_t)mrp * kMmEStride) * 4 +
                       (size_t)2 * seg_max * 2 + (size_t)K * 4;
   if (smem > 220 * 1024) return;
   auto up = [&](DeviceBuffer& b, const void* src, size_t bytes) {
@@ -1127,6 +1356,27 @@ static DirectSigma* direct_prepare(Context* c) {
   if (tc != d->tc) d->dense_state = dense_env ? d->dense_state : -1;
   d->tc = tc;
   if (tc) set_max_dynamic_smem((const void*)k_tc_gemm2, 2 * kTcStage);
+  d->otc = false;
+  if (tc && d->mm) {
+    const int K = d->a.ns + 1, mrows = d->mr + d->n + 1;
+    const int kpad = (K + 7) / 8 * 8;
+    const int rows1 = mrows > 128 ? ((mrows - 128 + 7) & ~7) : 0;
+    const size_t smem = (size_t)2 * (128 + rows1) * kpad * 4 + (size_t)2 * 64 * kpad * 4 +
+                        (size_t)2 * K * kMmCols * 4 + (size_t)((mrows + 3) & ~3) * kMmEStride * 4 +
+                        (size_t)2 * d->seg_max * 2 + (size_t)K * 4;
+    const int64_t nbs = (d->same ? d->a : d->b).nstr;
+    int jpt = (int)((nbs + kOtThreads - 1) / kOtThreads);
+    jpt = jpt <= 4 ? 4 : jpt <= 8 ? 8 : jpt <= 12 ? 12 : 16;
+    if (mrows <= 256 && smem <= 226 * 1024 && (int64_t)jpt * kOtThreads >= nbs) {
+      d->otc = true;
+      d->kpad = kpad;
+      d->otc_jpt = jpt;
+      d->otc_smem = smem;
+      for (const void* f : {(const void*)k_ds_opposite_tc<4>, (const void*)k_ds_opposite_tc<8>,
+                            (const void*)k_ds_opposite_tc<12>, (const void*)k_ds_opposite_tc<16>})
+        set_max_dynamic_smem(f, (int)smem);
+    }
+  }
   direct_values(c, d);
   return d;
 }
