@@ -850,7 +850,7 @@ __global__ void __launch_bounds__(kOtThreads, 1)
                      const float* __restrict__ V2, int mrp, int n, const double* __restrict__ D,
                      const float* __restrict__ C, float* __restrict__ sigma) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ __align__(8) uint64_t mbar;
+  __shared__ __align__(8) uint64_t mbar[2];
   __shared__ uint32_t tslot;
   const int K = nsa + 1, kq4 = kpad >> 2;
   const int rows1 = (mrows > 128 ? ((mrows - 128 + 7) & ~7) : 0);  // rows held for tile 1
@@ -865,9 +865,10 @@ __global__ void __launch_bounds__(kOtThreads, 1)
   int32_t* Jrow = (int32_t*)(L + (size_t)2 * seg_max);            // [K]
   const int64_t Ia = blockIdx.x;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  if (warp == 0) tc::tmem_alloc(&tslot, 128);
+  if (warp == 0) tc::tmem_alloc(&tslot, 256);
   if (tid == 0) {
-    tc::mbar_init(&mbar, 1);
+    tc::mbar_init(&mbar[0], 1);
+    tc::mbar_init(&mbar[1], 1);
     tc::mbar_init_fence();
   }
   // A operand: element (r, k) of tile t = r / 128 at byte 16 c of the tile,
@@ -938,15 +939,18 @@ __global__ void __launch_bounds__(kOtThreads, 1)
   constexpr uint32_t idesc = tc::idesc_tf32(128, kMmCols);
   const uint32_t sbo = (uint32_t)kq4 * 128;
   const int nchunk = (nb + kMmCols - 1) / kMmCols;
-  uint32_t parity = 0u;
+  const int ntile = mrows > 128 ? 2 : 1;
+  // descriptors of K step 0; a K step moves the start by 256 bytes (16 in
+  // the descriptor's address field), a tile by 128 kpad 4 bytes
+  const uint64_t dah = tc::desc(tc::smem_addr(Ahi), 128, sbo), dal = tc::desc(tc::smem_addr(Alo), 128, sbo);
+  const uint64_t dbh = tc::desc(tc::smem_addr(Bhi), 128, sbo), dbl = tc::desc(tc::smem_addr(Blo), 128, sbo);
+  const uint64_t tstep = (uint64_t)((128 * kpad * 4) >> 4);
+  uint32_t par0 = 0u, par1 = 0u;
   bool ok = true;
-  stage(0, 0);
-  for (int c = 0; c < nchunk && ok; ++c) {
-    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-    __syncthreads();  // chunk c staged; B, E and buffer (c + 1) & 1 free
-    if (c + 1 < nchunk) stage(c + 1, (c + 1) & 1);
-    // B operand: element (j, k) at byte 16 c of Bhi / Blo, c = (j / 8 * kq4 + k / 4) * 8 + j % 8
-    const float* g = G + (size_t)(c & 1) * K * kMmCols;
+  // B operand of chunk cc (G buffer cc & 1): element (j, k) at byte 16 ci of
+  // Bhi / Blo, ci = (j / 8 kq4 + k / 4) 8 + j % 8
+  auto split = [&](int cc) {
+    const float* g = G + (size_t)(cc & 1) * K * kMmCols;
     for (int ci = tid; ci < kMmCols * kq4; ci += kOtThreads) {
       const int cm = ci >> 3, j = (cm / kq4) * 8 + (ci & 7), k0 = (cm % kq4) * 4;
       float h[4], l[4];
@@ -960,26 +964,50 @@ __global__ void __launch_bounds__(kOtThreads, 1)
       *(float4*)(Blo + 16 * ci) = make_float4(l[0], l[1], l[2], l[3]);
     }
     tc::fence_proxy_async();
-    __syncthreads();
+  };
+  // MMAs of chunk cc into TMEM set cc & 1 (columns 128 (cc & 1) + 64 t)
+  auto issue = [&](int cc) {
     if (tid == 0) {
       tc::fence_after();
-      const uint32_t ah = tc::smem_addr(Ahi), al = tc::smem_addr(Alo), bh = tc::smem_addr(Bhi),
-                     bl = tc::smem_addr(Blo);
-      const int ntile = mrows > 128 ? 2 : 1;
+      const uint32_t dset = tmem + (uint32_t)((cc & 1) * 128);
       for (int t = 0; t < ntile; ++t) {
-        const uint32_t to = (uint32_t)(t * 128 * kpad * 4), dt = tmem + (uint32_t)(t * kMmCols);
+        const uint32_t dt = dset + (uint32_t)(t * kMmCols);
         for (int ks = 0; ks < kpad / 8; ++ks) {
-          const uint32_t ko = ks * 256;
-          tc::mma_tf32(dt, tc::desc(ah + to + ko, 128, sbo), tc::desc(bh + ko, 128, sbo), idesc, ks ? 1u : 0u);
-          tc::mma_tf32(dt, tc::desc(ah + to + ko, 128, sbo), tc::desc(bl + ko, 128, sbo), idesc, 1u);
-          tc::mma_tf32(dt, tc::desc(al + to + ko, 128, sbo), tc::desc(bh + ko, 128, sbo), idesc, 1u);
+          const uint64_t ko = (uint64_t)ks * 16, ah = dah + t * tstep + ko, al = dal + t * tstep + ko;
+          tc::mma_tf32(dt, ah, dbh + ko, idesc, ks ? 1u : 0u);
+          tc::mma_tf32(dt, ah, dbl + ko, idesc, 1u);
+          tc::mma_tf32(dt, al, dbh + ko, idesc, 1u);
         }
       }
-      tc::commit(&mbar);
+      tc::commit(&mbar[cc & 1]);
     }
-    ok = tc::mbar_wait(&mbar, parity, kTcSpin);
-    parity ^= 1u;
+  };
+  stage(0, 0);
+  if (nchunk > 1) {
+    stage(1, 1);
+    asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+  } else {
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+  }
+  __syncthreads();
+  split(0);
+  __syncthreads();
+  issue(0);
+  for (int c = 0; c < nchunk; ++c) {
+    // MMA(c) done: the B operand is free and TMEM set c & 1 holds chunk c's E
+    ok = tc::mbar_wait(&mbar[c & 1], (c & 1) ? par1 : par0, kTcSpin);
+    if (c & 1)
+      par1 ^= 1u;
+    else
+      par0 ^= 1u;
     if (!ok) break;
+    if (c + 1 < nchunk) {  // chunk c + 1's products run while chunk c is read out and walked
+      asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+      __syncthreads();
+      split(c + 1);
+      __syncthreads();
+      issue(c + 1);
+    }
     tc::fence_after();
     {
       const int q = warp & 3, t = warp >> 2;
@@ -988,7 +1016,7 @@ __global__ void __launch_bounds__(kOtThreads, 1)
 #pragma unroll 1
         for (int cb = 0; cb < kMmCols; cb += 16) {
           float v[16];
-          tc::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(t * kMmCols + cb), v);
+          tc::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)((c & 1) * 128 + t * kMmCols + cb), v);
           if (row < mrows) {
             float* e = E + (size_t)row * kMmEStride + cb;
 #pragma unroll
@@ -1014,6 +1042,8 @@ __global__ void __launch_bounds__(kOtThreads, 1)
         acc[j] = s;
       }
     }
+    __syncthreads();  // E, L and G buffer c & 1 free
+    if (c + 2 < nchunk) stage(c + 2, c & 1);
   }
   if (!ok) {
     asm volatile("cp.async.wait_group 0;\n" ::: "memory");
@@ -1028,7 +1058,7 @@ __global__ void __launch_bounds__(kOtThreads, 1)
   }
   tc::fence_before();
   __syncthreads();
-  if (warp == 0) tc::tmem_free(tmem, 128);
+  if (warp == 0) tc::tmem_free(tmem, 256);
 }
 
 template <typename T>
