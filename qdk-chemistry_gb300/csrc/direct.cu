@@ -839,7 +839,7 @@ __global__ void __launch_bounds__(kTcThreads) k_tc_gemm2(int M, int N, int K1, i
 // products into TMEM (128 columns: tile t at column 64 t) and commits to an
 // mbarrier; the eight warps read E out of TMEM (warp w: lanes 32 (w % 4)..,
 // tile w / 4) into shared memory and walk it as the FMA kernel does.
-constexpr int kOtThreads = 256;
+constexpr int kOtThreads = 512;
 
 template <int JPT>
 __global__ void __launch_bounds__(kOtThreads, 1)
@@ -906,7 +906,9 @@ __global__ void __launch_bounds__(kOtThreads, 1)
   __syncthreads();
   tc::fence_after();
   const uint32_t tmem = tslot;
-  auto stage = [&](int chunk, int buf) {
+  // copies in (cp.async, one commit group each): the chunk's C rows (G) and
+  // its walk lists (L)
+  auto stage_g = [&](int chunk, int buf) {
     const int j0 = chunk * kMmCols;
     float* g = G + (size_t)buf * K * kMmCols;
     if (vec) {
@@ -925,6 +927,9 @@ __global__ void __launch_bounds__(kOtThreads, 1)
         cp_async4_zfill(g + i, C + (int64_t)Jrow[k] * nb + (ok ? j0 + j : 0), ok);
       }
     }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+  };
+  auto stage_l = [&](int chunk, int buf) {
     const int u0 = __ldg(seg + chunk), nv = (__ldg(seg + chunk + 1) - u0) >> 3;
     uint16_t* l = L + (size_t)buf * seg_max;
     for (int i = tid; i < nv; i += kOtThreads) cp_async16(l + 8 * i, lists + u0 + 8 * i);
@@ -982,18 +987,23 @@ __global__ void __launch_bounds__(kOtThreads, 1)
       tc::commit(&mbar[cc & 1]);
     }
   };
-  stage(0, 0);
+  // copy schedule: G(c + 2) leaves at the start of iteration c (its buffer's
+  // chunk c was split in iteration c - 1), L(c + 2) at its end (after walk c);
+  // "all but the newest group" before split(c + 1) then covers G(c + 1),
+  // L(c + 1) and L(c)
+  stage_g(0, 0);
+  stage_l(0, 0);
   if (nchunk > 1) {
-    stage(1, 1);
-    asm volatile("cp.async.wait_group 1;\n" ::: "memory");
-  } else {
-    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    stage_g(1, 1);
+    stage_l(1, 1);
   }
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
   __syncthreads();
   split(0);
   __syncthreads();
   issue(0);
   for (int c = 0; c < nchunk; ++c) {
+    if (c + 2 < nchunk) stage_g(c + 2, c & 1);
     // MMA(c) done: the B operand is free and TMEM set c & 1 holds chunk c's E
     ok = tc::mbar_wait(&mbar[c & 1], (c & 1) ? par1 : par0, kTcSpin);
     if (c & 1)
@@ -1001,8 +1011,11 @@ __global__ void __launch_bounds__(kOtThreads, 1)
     else
       par0 ^= 1u;
     if (!ok) break;
-    if (c + 1 < nchunk) {  // chunk c + 1's products run while chunk c is read out and walked
+    if (c + 2 < nchunk)
+      asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+    else
       asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    if (c + 1 < nchunk) {  // chunk c + 1's products run while chunk c is read out and walked
       __syncthreads();
       split(c + 1);
       __syncthreads();
@@ -1010,11 +1023,12 @@ __global__ void __launch_bounds__(kOtThreads, 1)
     }
     tc::fence_after();
     {
-      const int q = warp & 3, t = warp >> 2;
+      // warp w: lanes 32 (w % 4).., tile (w / 4) % 2, columns 32 (w / 8)..
+      const int q = warp & 3, t = (warp >> 2) & 1, half = warp >> 3;
       const int row = t * 128 + q * 32 + lane;
       if (t * 128 < mrows) {
 #pragma unroll 1
-        for (int cb = 0; cb < kMmCols; cb += 16) {
+        for (int cb = half * 32; cb < half * 32 + 32; cb += 16) {
           float v[16];
           tc::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)((c & 1) * 128 + t * kMmCols + cb), v);
           if (row < mrows) {
@@ -1035,6 +1049,7 @@ __global__ void __launch_bounds__(kOtThreads, 1)
       if (Ib < nb) {
         const int e1 = off[Ib + 1];
         float s = acc[j];
+#pragma unroll 4
         for (int e = off[Ib]; e < e1; ++e) {
           const uint32_t w = ent[e];
           s += negate_if<float>(E[w & 0x7fff], (w >> 15) != 0);
@@ -1042,8 +1057,8 @@ __global__ void __launch_bounds__(kOtThreads, 1)
         acc[j] = s;
       }
     }
-    __syncthreads();  // E, L and G buffer c & 1 free
-    if (c + 2 < nchunk) stage(c + 2, c & 1);
+    __syncthreads();  // E and L buffer c & 1 free
+    if (c + 2 < nchunk) stage_l(c + 2, c & 1);
   }
   if (!ok) {
     asm volatile("cp.async.wait_group 0;\n" ::: "memory");
@@ -1146,10 +1161,9 @@ static void direct_sigma_t(Context* c, const T* x, T* y) {
               (const float*)x, (float*)y);
         };
         switch (d->otc_jpt) {
+          case 2: gt(k_ds_opposite_tc<2>); break;
           case 4: gt(k_ds_opposite_tc<4>); break;
-          case 8: gt(k_ds_opposite_tc<8>); break;
-          case 12: gt(k_ds_opposite_tc<12>); break;
-          default: gt(k_ds_opposite_tc<16>); break;
+          default: gt(k_ds_opposite_tc<8>); break;
         }
         QDKGB_CHECK_LAUNCH();
         return;
@@ -1396,14 +1410,14 @@ static DirectSigma* direct_prepare(Context* c) {
                         (size_t)2 * d->seg_max * 2 + (size_t)K * 4;
     const int64_t nbs = (d->same ? d->a : d->b).nstr;
     int jpt = (int)((nbs + kOtThreads - 1) / kOtThreads);
-    jpt = jpt <= 4 ? 4 : jpt <= 8 ? 8 : jpt <= 12 ? 12 : 16;
+    jpt = jpt <= 2 ? 2 : jpt <= 4 ? 4 : 8;
     if (mrows <= 256 && smem <= 226 * 1024 && (int64_t)jpt * kOtThreads >= nbs) {
       d->otc = true;
       d->kpad = kpad;
       d->otc_jpt = jpt;
       d->otc_smem = smem;
-      for (const void* f : {(const void*)k_ds_opposite_tc<4>, (const void*)k_ds_opposite_tc<8>,
-                            (const void*)k_ds_opposite_tc<12>, (const void*)k_ds_opposite_tc<16>})
+      for (const void* f : {(const void*)k_ds_opposite_tc<2>, (const void*)k_ds_opposite_tc<4>,
+                            (const void*)k_ds_opposite_tc<8>})
         set_max_dynamic_smem(f, (int)smem);
     }
   }
