@@ -91,11 +91,14 @@ int qdkgb_operator_layout(const qdkgb_context* ctx, int* layout, int64_t* stored
 
 /* The direct sigma's FP32 form (layouts QDKGB_LAYOUT_DIRECT and
  * QDKGB_LAYOUT_SLAB_DIRECT32; no counterpart in the reference):
- * *contraction 1 when the opposite-spin doubles and the single excitations
- * run as one FP32 contraction per alpha string (else the element-wise walk);
- * *dense the same-spin part's form, -1 until the first FP32 sigma times the
- * two, 0 element-wise kernels, 1 two dense FP32 products; form_ms[2] their
- * times (ms).  Any pointer may be NULL. */
+ * *contraction 0 the element-wise walk, 1 the opposite-spin doubles and the
+ * single excitations as one FP32 contraction per alpha string on the FMA
+ * pipe, 2 the same with the contraction on the tensor cores (tcgen05, TF32
+ * x 3); *dense the same-spin part's form, -1 until the first FP32 sigma
+ * times the forms, 0 element-wise kernels, 1 two dense products (tensor
+ * cores unless QDKGB_DIRECT_TC=0); form_ms[4] the times (ms) of the
+ * same-spin forms (element-wise, dense) and of the contractions (FMA pipe,
+ * tensor cores), 0 where not timed.  Any pointer may be NULL. */
 int qdkgb_direct_plan(const qdkgb_context* ctx, int* contraction, int* dense, double* form_ms);
 
 /* The sizes the getters write (no counterpart; the reference's sparsexx

@@ -383,13 +383,15 @@ class Context:
 
     def direct_plan(self):
         """The direct sigma's FP32 form (qdkgb_direct_plan): {"contraction":
-        bool, "dense": None (not yet timed) / bool, "form_ms": (element-wise,
-        dense)}."""
+        "walk" / "fma" / "tensor", "dense": None (not yet timed) / bool,
+        "same_spin_ms": (element-wise, dense), "contraction_ms": (FMA,
+        tensor cores)}."""
         mm, dense = ctypes.c_int(), ctypes.c_int()
-        ms = (ctypes.c_double * 2)()
+        ms = (ctypes.c_double * 4)()
         self._check(lib().qdkgb_direct_plan(self._h, ctypes.byref(mm), ctypes.byref(dense), ms))
-        return {"contraction": bool(mm.value), "dense": None if dense.value < 0 else bool(dense.value),
-                "form_ms": (ms[0], ms[1])}
+        return {"contraction": ("walk", "fma", "tensor")[mm.value],
+                "dense": None if dense.value < 0 else bool(dense.value),
+                "same_spin_ms": (ms[0], ms[1]), "contraction_ms": (ms[2], ms[3])}
 
     def build_direct_sigma(self):
         """Recompute-on-the-fly sigma for a complete space (no CSR stored)."""

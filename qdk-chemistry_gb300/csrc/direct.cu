@@ -115,8 +115,11 @@ struct DirectSigma {
   bool tc = false;                 // dense products on the tensor cores (k_tc_gemm2; QDKGB_DIRECT_TC=0: FMA pipe)
   // the contraction's E on the tensor cores (k_ds_opposite_tc): K padded to
   // kpad, its shared memory, beta strings per thread
+  // otc_state: -1 until the first FP32 sigma times the FMA and tensor-core
+  // contractions (0 FMA kept, 1 tensor cores kept); otc_ms their times
   bool otc = false;
-  int kpad = 0, otc_jpt = 0;
+  int kpad = 0, otc_jpt = 0, otc_state = -1;
+  double otc_ms[2] = {0., 0.};
   size_t otc_smem = 0;
   DeviceBuffer Haa, HbbT;
 };
@@ -1151,43 +1154,81 @@ static void direct_sigma_t(Context* c, const T* x, T* y) {
             (const int32_t*)d->rs_of.ptr, (const uint16_t*)d->lists.ptr, (const int32_t*)d->seg.ptr,
             (const float*)d->V2mm.ptr, d->n, (const double*)c->H.diag.ptr, (const float*)x, (float*)y);
       };
-      if (d->otc) {
-        auto gt = [&](auto kern) {
-          kern<<<(unsigned)na, kOtThreads, d->otc_smem, c->stream>>>(
-              (int)na, (int)nb, A.ns, d->mr, d->mr + d->n + 1, d->kpad, d->off_u16, d->seg_max, d->mm_vec ? 1 : 0,
-              (const int32_t*)A.sJ.ptr, (const int32_t*)A.svo.ptr, (const float*)A.sA32.ptr,
-              (const float*)A.W32.ptr, (const int32_t*)d->rs_of.ptr, (const uint16_t*)d->lists.ptr,
-              (const int32_t*)d->seg.ptr, (const float*)d->V2mm.ptr, d->mrp, d->n, (const double*)c->H.diag.ptr,
-              (const float*)x, (float*)y);
+      // the contraction into yo (which reads yo as its start value): the
+      // FMA-pipe kernel (0) or the tensor-core one (1)
+      auto contract = [&](float* yo, int form) {
+        if (form == 1) {
+          auto gt = [&](auto kern) {
+            kern<<<(unsigned)na, kOtThreads, d->otc_smem, c->stream>>>(
+                (int)na, (int)nb, A.ns, d->mr, d->mr + d->n + 1, d->kpad, d->off_u16, d->seg_max,
+                d->mm_vec ? 1 : 0, (const int32_t*)A.sJ.ptr, (const int32_t*)A.svo.ptr, (const float*)A.sA32.ptr,
+                (const float*)A.W32.ptr, (const int32_t*)d->rs_of.ptr, (const uint16_t*)d->lists.ptr,
+                (const int32_t*)d->seg.ptr, (const float*)d->V2mm.ptr, d->mrp, d->n, (const double*)c->H.diag.ptr,
+                (const float*)x, yo);
+          };
+          switch (d->otc_jpt) {
+            case 2: gt(k_ds_opposite_tc<2>); break;
+            case 4: gt(k_ds_opposite_tc<4>); break;
+            default: gt(k_ds_opposite_tc<8>); break;
+          }
+          QDKGB_CHECK_LAUNCH();
+          return;
+        }
+        auto go = [&](auto kern) {
+          kern<<<(unsigned)na, d->mm_threads, d->mm_smem, c->stream>>>(
+              (int)na, (int)nb, A.ns, d->mr, d->mrp, d->off_u16, d->seg_max, d->mm_vec ? 1 : 0,
+              (const int32_t*)A.sJ.ptr, (const int32_t*)A.svo.ptr, (const float*)A.sA32.ptr, (const float*)A.W32.ptr,
+              (const int32_t*)d->rs_of.ptr, (const uint16_t*)d->lists.ptr, (const int32_t*)d->seg.ptr,
+              (const float*)d->V2mm.ptr, d->n, (const double*)c->H.diag.ptr, (const float*)x, yo);
         };
-        switch (d->otc_jpt) {
-          case 2: gt(k_ds_opposite_tc<2>); break;
-          case 4: gt(k_ds_opposite_tc<4>); break;
-          default: gt(k_ds_opposite_tc<8>); break;
+        if (d->mm_threads <= 320) {
+          switch (d->mm_jpt) {
+            case 2: go(k_ds_opposite_mm<2, false>); break;
+            case 4: go(k_ds_opposite_mm<4, false>); break;
+            case 6: go(k_ds_opposite_mm<6, false>); break;
+            case 8: go(k_ds_opposite_mm<8, false>); break;
+            case 12: go(k_ds_opposite_mm<12, false>); break;
+            case 16: go(k_ds_opposite_mm<16, false>); break;
+            default: go(k_ds_opposite_mm<24, false>); break;
+          }
+        } else {
+          switch (d->mm_jpt) {
+            case 2: go(k_ds_opposite_mm<2, true>); break;
+            case 4: go(k_ds_opposite_mm<4, true>); break;
+            case 6: go(k_ds_opposite_mm<6, true>); break;
+            case 8: go(k_ds_opposite_mm<8, true>); break;
+            case 12: go(k_ds_opposite_mm<12, true>); break;
+            default: go(k_ds_opposite_mm<16, true>); break;
+          }
         }
         QDKGB_CHECK_LAUNCH();
-        return;
-      }
-      if (d->mm_threads <= 320) {
-        switch (d->mm_jpt) {
-          case 2: go(k_ds_opposite_mm<2, false>); break;
-          case 4: go(k_ds_opposite_mm<4, false>); break;
-          case 6: go(k_ds_opposite_mm<6, false>); break;
-          case 8: go(k_ds_opposite_mm<8, false>); break;
-          case 12: go(k_ds_opposite_mm<12, false>); break;
-          case 16: go(k_ds_opposite_mm<16, false>); break;
-          default: go(k_ds_opposite_mm<24, false>); break;
+      };
+      if (d->otc && d->otc_state < 0) {
+        // first FP32 sigma of this space: time both contractions on a copy
+        // of the same-spin result and keep the faster
+        float* sc = (float*)dev_alloc(c, d->tmp32, N * sizeof(float));
+        cudaEvent_t e0, e1;
+        QDKGB_CUDA(cudaEventCreate(&e0));
+        QDKGB_CUDA(cudaEventCreate(&e1));
+        for (int form = 0; form < 2; ++form) {
+          double tot = 0.;
+          for (int r = 0; r < 4; ++r) {
+            QDKGB_CUDA(cudaMemcpyAsync(sc, y, N * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
+            QDKGB_CUDA(cudaEventRecord(e0, c->stream));
+            contract(sc, form);
+            QDKGB_CUDA(cudaEventRecord(e1, c->stream));
+            QDKGB_CUDA(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            QDKGB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            if (r > 0) tot += ms;
+          }
+          d->otc_ms[form] = tot / 3.0;
         }
-      } else {
-        switch (d->mm_jpt) {
-          case 2: go(k_ds_opposite_mm<2, true>); break;
-          case 4: go(k_ds_opposite_mm<4, true>); break;
-          case 6: go(k_ds_opposite_mm<6, true>); break;
-          case 8: go(k_ds_opposite_mm<8, true>); break;
-          case 12: go(k_ds_opposite_mm<12, true>); break;
-          default: go(k_ds_opposite_mm<16, true>); break;
-        }
+        QDKGB_CUDA(cudaEventDestroy(e0));
+        QDKGB_CUDA(cudaEventDestroy(e1));
+        d->otc_state = d->otc_ms[1] < d->otc_ms[0] ? 1 : 0;
       }
+      contract((float*)y, d->otc && d->otc_state == 1 ? 1 : 0);
       QDKGB_CHECK_LAUNCH();
       return;
     }
@@ -1397,7 +1438,10 @@ static DirectSigma* direct_prepare(Context* c) {
   }
   DirectSigma* d = c->direct;
   d->dense_env = dense_env;
-  if (tc != d->tc) d->dense_state = dense_env ? d->dense_state : -1;
+  if (tc != d->tc) {
+    d->dense_state = dense_env ? d->dense_state : -1;
+    d->otc_state = -1;
+  }
   d->tc = tc;
   if (tc) set_max_dynamic_smem((const void*)k_tc_gemm2, 2 * kTcStage);
   d->otc = false;
@@ -1427,11 +1471,13 @@ static DirectSigma* direct_prepare(Context* c) {
 
 void direct_plan(const Context* c, int* mm, int* dense, double* ms) {
   const DirectSigma* d = c->direct;
-  if (mm) *mm = d && d->mm ? 1 : 0;
+  if (mm) *mm = !(d && d->mm) ? 0 : (d->otc && d->otc_state == 1) ? 2 : 1;
   if (dense) *dense = d ? d->dense_state : -1;
   if (ms) {
     ms[0] = d ? d->dense_ms[0] : 0.;
     ms[1] = d ? d->dense_ms[1] : 0.;
+    ms[2] = d ? d->otc_ms[0] : 0.;
+    ms[3] = d ? d->otc_ms[1] : 0.;
   }
 }
 

@@ -248,8 +248,10 @@ void build_direct_sigma(Context* c);
 // the stored FP64 slab (mixed form); false where the contraction form does
 // not apply.
 bool attach_direct_fp32(Context* c);
-// The direct sigma's FP32 form: contraction in use, same-spin form (-1 not
-// yet timed, 0 element-wise, 1 dense) and the two forms' times (ms).
+// The direct sigma's FP32 form: contraction in use (0 element-wise walk,
+// 1 FMA pipe, 2 tensor cores), same-spin form (-1 not yet timed, 0
+// element-wise, 1 dense) and the times (ms) of the same-spin forms
+// (element-wise, dense) and of the contractions (FMA, tensor cores).
 void direct_plan(const Context* c, int* mm, int* dense, double* ms);
 void free_direct(Context* c);
 void direct_sigma_fp64(Context* c, const double* x, double* y);
