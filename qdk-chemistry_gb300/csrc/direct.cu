@@ -845,7 +845,7 @@ __global__ void __launch_bounds__(kTcThreads) k_tc_gemm2(int M, int N, int K1, i
 constexpr int kOtThreads = 512;
 
 template <int JPT>
-__global__ void __launch_bounds__(kOtThreads, 1)
+__global__ void __launch_bounds__(kOtThreads + 32, 1)
     k_ds_opposite_tc(int na, int nb, int nsa, int mr, int mrows, int kpad, int off_u16, int seg_max, int vec,
                      const int32_t* __restrict__ a_sJ, const int32_t* __restrict__ a_svo,
                      const float* __restrict__ a_sA, const float* __restrict__ a_W, const int32_t* __restrict__ rs_of,
@@ -877,7 +877,8 @@ __global__ void __launch_bounds__(kOtThreads, 1)
   // A operand: element (r, k) of tile t = r / 128 at byte 16 c of the tile,
   // c = ((r % 128) / 8 * kq4 + k / 4) * 8 + r % 8
   const int nA = (128 + rows1) * kq4;  // 16-byte chunks, both tiles (tile 1 only its held rows)
-  for (int ci = tid; ci < nA; ci += kOtThreads) {
+  const bool issuer = tid >= kOtThreads;  // the last warp issues the MMAs; the others work
+  for (int ci = issuer ? nA : tid; ci < nA; ci += kOtThreads) {
     const int t = ci >= 128 * kq4 ? 1 : 0;
     const int c = ci - t * 128 * kq4;
     const int cm = c >> 3, rr = c & 7;
@@ -904,7 +905,7 @@ __global__ void __launch_bounds__(kOtThreads, 1)
     *(float4*)(Ahi + off) = make_float4(h[0], h[1], h[2], h[3]);
     *(float4*)(Alo + off) = make_float4(l[0], l[1], l[2], l[3]);
   }
-  for (int k = tid; k < K; k += kOtThreads) Jrow[k] = k < nsa ? __ldg(a_sJ + Ia * nsa + k) : (int32_t)Ia;
+  for (int k = issuer ? K : tid; k < K; k += kOtThreads) Jrow[k] = k < nsa ? __ldg(a_sJ + Ia * nsa + k) : (int32_t)Ia;
   tc::fence_before();
   __syncthreads();
   tc::fence_after();
@@ -942,7 +943,7 @@ __global__ void __launch_bounds__(kOtThreads, 1)
 #pragma unroll
   for (int j = 0; j < JPT; ++j) {
     const int Ib = tid + j * kOtThreads;
-    acc[j] = Ib < nb ? sigma[Ia * nb + Ib] + (float)D[Ia * nb + Ib] * C[Ia * nb + Ib] : 0.f;
+    acc[j] = (!issuer && Ib < nb) ? sigma[Ia * nb + Ib] + (float)D[Ia * nb + Ib] * C[Ia * nb + Ib] : 0.f;
   }
   constexpr uint32_t idesc = tc::idesc_tf32(128, kMmCols);
   const uint32_t sbo = (uint32_t)kq4 * 128;
@@ -975,7 +976,7 @@ __global__ void __launch_bounds__(kOtThreads, 1)
   };
   // MMAs of chunk cc into TMEM set cc & 1 (columns 128 (cc & 1) + 64 t)
   auto issue = [&](int cc) {
-    if (tid == 0) {
+    {
       tc::fence_after();
       const uint32_t dset = tmem + (uint32_t)((cc & 1) * 128);
       for (int t = 0; t < ntile; ++t) {
@@ -990,78 +991,94 @@ __global__ void __launch_bounds__(kOtThreads, 1)
       tc::commit(&mbar[cc & 1]);
     }
   };
-  // copy schedule: G(c + 2) leaves at the start of iteration c (its buffer's
-  // chunk c was split in iteration c - 1), L(c + 2) at its end (after walk c);
-  // "all but the newest group" before split(c + 1) then covers G(c + 1),
-  // L(c + 1) and L(c)
-  stage_g(0, 0);
-  stage_l(0, 0);
-  if (nchunk > 1) {
-    stage_g(1, 1);
-    stage_l(1, 1);
-  }
-  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-  __syncthreads();
-  split(0);
-  __syncthreads();
-  issue(0);
-  for (int c = 0; c < nchunk; ++c) {
-    if (c + 2 < nchunk) stage_g(c + 2, c & 1);
-    // MMA(c) done: the B operand is free and TMEM set c & 1 holds chunk c's E
-    ok = tc::mbar_wait(&mbar[c & 1], (c & 1) ? par1 : par0, kTcSpin);
-    if (c & 1)
-      par1 ^= 1u;
-    else
-      par0 ^= 1u;
-    if (!ok) break;
-    if (c + 2 < nchunk)
-      asm volatile("cp.async.wait_group 1;\n" ::: "memory");
-    else
-      asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-    if (c + 1 < nchunk) {  // chunk c + 1's products run while chunk c is read out and walked
-      __syncthreads();
-      split(c + 1);
-      __syncthreads();
-      issue(c + 1);
+  // Named barriers: 1 the 512 workers; 2 "B operand of the next chunk
+  // written and TMEM set free" (workers arrive, the issuer warp waits).
+  // Copy schedule: G(c + 2) leaves at the start of iteration c (its buffer's
+  // chunk c was split in iteration c - 1), L(c + 2) at its end (after walk
+  // c); "all but the newest group" before split(c + 1) covers G(c + 1),
+  // L(c + 1) and L(c).  A worker reaches arrive(c + 1) only after it has
+  // seen MMA(c) complete, which the issuer started after its wait for c, so
+  // barrier 2 never holds two workers' rounds at once.  After a timed-out
+  // wait the workers keep the barrier rounds (no more waits) so the issuer
+  // finishes, and the output is NaN.
+  auto bar_sync = [](int id, int cnt) { asm volatile("bar.sync %0, %1;\n" ::"r"(id), "r"(cnt) : "memory"); };
+  auto bar_arrive = [](int id, int cnt) { asm volatile("bar.arrive %0, %1;\n" ::"r"(id), "r"(cnt) : "memory"); };
+  constexpr int kAll = kOtThreads + 32;
+  if (issuer) {
+    for (int cc = 0; cc < nchunk; ++cc) {
+      bar_sync(2, kAll);
+      if (lane == 0) issue(cc);
+      __syncwarp();
     }
-    tc::fence_after();
-    {
-      // warp w: lanes 32 (w % 4).., tile (w / 4) % 2, columns 32 (w / 8)..
-      const int q = warp & 3, t = (warp >> 2) & 1, half = warp >> 3;
-      const int row = t * 128 + q * 32 + lane;
-      if (t * 128 < mrows) {
+  } else {
+    stage_g(0, 0);
+    stage_l(0, 0);
+    if (nchunk > 1) {
+      stage_g(1, 1);
+      stage_l(1, 1);
+    }
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    bar_sync(1, kOtThreads);
+    split(0);
+    tc::fence_before();
+    bar_arrive(2, kAll);
+    for (int c = 0; c < nchunk; ++c) {
+      if (c + 2 < nchunk) stage_g(c + 2, c & 1);
+      // MMA(c) done: the B operand is free and TMEM set c & 1 holds chunk c's E
+      if (ok) ok = tc::mbar_wait(&mbar[c & 1], (c & 1) ? par1 : par0, kTcSpin);
+      if (c & 1)
+        par1 ^= 1u;
+      else
+        par0 ^= 1u;
+      if (c + 2 < nchunk)
+        asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+      else
+        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+      if (c + 1 < nchunk) {  // chunk c + 1's products run while chunk c is read out and walked
+        bar_sync(1, kOtThreads);
+        split(c + 1);
+        tc::fence_before();
+        bar_arrive(2, kAll);
+      }
+      tc::fence_after();
+      if (ok) {
+        // warp w: lanes 32 (w % 4).., tile (w / 4) % 2, columns 32 (w / 8)..
+        const int q = warp & 3, t = (warp >> 2) & 1, half = warp >> 3;
+        const int row = t * 128 + q * 32 + lane;
+        if (t * 128 < mrows) {
 #pragma unroll 1
-        for (int cb = half * 32; cb < half * 32 + 32; cb += 16) {
-          float v[16];
-          tc::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)((c & 1) * 128 + t * kMmCols + cb), v);
-          if (row < mrows) {
-            float* e = E + (size_t)row * kMmEStride + cb;
+          for (int cb = half * 32; cb < half * 32 + 32; cb += 16) {
+            float v[16];
+            tc::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)((c & 1) * 128 + t * kMmCols + cb), v);
+            if (row < mrows) {
+              float* e = E + (size_t)row * kMmEStride + cb;
 #pragma unroll
-            for (int i = 0; i < 16; i += 4) *(float4*)(e + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+              for (int i = 0; i < 16; i += 4) *(float4*)(e + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+            }
           }
         }
       }
-    }
-    tc::fence_before();
-    __syncthreads();
-    const uint16_t* off = L + (size_t)(c & 1) * seg_max;
-    const uint16_t* ent = off + off_u16;
+      tc::fence_before();
+      bar_sync(1, kOtThreads);
+      const uint16_t* off = L + (size_t)(c & 1) * seg_max;
+      const uint16_t* ent = off + off_u16;
 #pragma unroll
-    for (int j = 0; j < JPT; ++j) {
-      const int Ib = tid + j * kOtThreads;
-      if (Ib < nb) {
-        const int e1 = off[Ib + 1];
-        float s = acc[j];
+      for (int j = 0; j < JPT; ++j) {
+        const int Ib = tid + j * kOtThreads;
+        if (Ib < nb) {
+          const int e1 = off[Ib + 1];
+          float s = acc[j];
 #pragma unroll 4
-        for (int e = off[Ib]; e < e1; ++e) {
-          const uint32_t w = ent[e];
-          s += negate_if<float>(E[w & 0x7fff], (w >> 15) != 0);
+          for (int e = off[Ib]; e < e1; ++e) {
+            const uint32_t w = ent[e];
+            s += negate_if<float>(E[w & 0x7fff], (w >> 15) != 0);
+          }
+          acc[j] = s;
         }
-        acc[j] = s;
       }
+      bar_sync(1, kOtThreads);  // E and L buffer c & 1 free
+      if (c + 2 < nchunk) stage_l(c + 2, c & 1);
     }
-    __syncthreads();  // E and L buffer c & 1 free
-    if (c + 2 < nchunk) stage_l(c + 2, c & 1);
   }
   if (!ok) {
     asm volatile("cp.async.wait_group 0;\n" ::: "memory");
@@ -1069,10 +1086,12 @@ __global__ void __launch_bounds__(kOtThreads, 1)
     for (int j = 0; j < JPT; ++j) acc[j] = __int_as_float(0x7fc00000);
     if (tid == 0) atomicOr(&g_tc_fault, 1u);
   }
+  if (!issuer) {
 #pragma unroll
-  for (int j = 0; j < JPT; ++j) {
-    const int Ib = tid + j * kOtThreads;
-    if (Ib < nb) sigma[Ia * nb + Ib] = acc[j];
+    for (int j = 0; j < JPT; ++j) {
+      const int Ib = tid + j * kOtThreads;
+      if (Ib < nb) sigma[Ia * nb + Ib] = acc[j];
+    }
   }
   tc::fence_before();
   __syncthreads();
@@ -1159,7 +1178,7 @@ static void direct_sigma_t(Context* c, const T* x, T* y) {
       auto contract = [&](float* yo, int form) {
         if (form == 1) {
           auto gt = [&](auto kern) {
-            kern<<<(unsigned)na, kOtThreads, d->otc_smem, c->stream>>>(
+            kern<<<(unsigned)na, kOtThreads + 32, d->otc_smem, c->stream>>>(
                 (int)na, (int)nb, A.ns, d->mr, d->mr + d->n + 1, d->kpad, d->off_u16, d->seg_max,
                 d->mm_vec ? 1 : 0, (const int32_t*)A.sJ.ptr, (const int32_t*)A.svo.ptr, (const float*)A.sA32.ptr,
                 (const float*)A.W32.ptr, (const int32_t*)d->rs_of.ptr, (const uint16_t*)d->lists.ptr,
