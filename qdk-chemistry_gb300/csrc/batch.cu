@@ -628,6 +628,9 @@ void casci_batch(Context* ctx, int ninst, const qdkgb_cas_instance* inst, const 
         }
         continue;
       }
+      // mixed form: new directions through the direct contraction where it
+      // applies (the stored hi / lo slab still serves the full-precision refresh)
+      const bool dbatch = mixed && direct_batch_prepare(cc, B, T, V);
       // ---- Davidson state
       const int KM = m + 1;
       const int nchunk = (int)((N + kChunk - 1) / kChunk);
@@ -805,7 +808,10 @@ void casci_batch(Context* ctx, int ninst, const qdkgb_cas_instance* inst, const 
         k_b_store_dir<<<gv, kBT, 0, s0>>>(t, sc, Vb, astride, ld, kdev, t32, N, act, nsig);
         QDKGB_CHECK_LAUNCH();
         if (mixed) {
-          slab_sigma_batch(cc, 0, B, act, hi, nullptr, t32, nullptr, s32);
+          if (dbatch)
+            direct_batch_sigma(cc, B, act, D, t32, s32);
+          else
+            slab_sigma_batch(cc, 0, B, act, hi, nullptr, t32, nullptr, s32);
           k_b_f32_to_col<<<gv, kBT, 0, s0>>>(s32, AVb, astride, ld, kdev, N, act);
         } else {
           slab_sigma_batch(cc, 1, B, act, val, nullptr, t, nullptr, yfull);

@@ -67,6 +67,20 @@ inline HSingle hsingle(uint64_t bra, uint64_t ket, uint64_t ex) {
 // banks apart).
 constexpr int kMmCols = 64;
 constexpr int kMmEStride = kMmCols + 4;
+
+// Instance strides of the contraction kernels (grid axis y = instance; a
+// single space has one instance and zero strides): the value tables sA, W
+// and V2mm, and the vectors (diagonal, C, sigma); act, when given, skips the
+// instances whose entry is zero.
+struct DsInst {
+  const int* act;
+  int64_t sA, W, V2, vec;
+};
+// the same for the dense same-spin products (grid axis z = instance)
+struct GmInst {
+  const int* act;
+  int64_t A1, B1, A2, B2, out;
+};
 constexpr int kMmMaxWarps = 16;
 
 // One spin's string tables.  Structure (built once per determinant space):
@@ -122,6 +136,13 @@ struct DirectSigma {
   double otc_ms[2] = {0., 0.};
   size_t otc_smem = 0;
   DeviceBuffer Haa, HbbT;
+  // batched CASCI over instances of this space (direct_batch_*): per-instance
+  // FP32 value tables, their dense same-spin matrices and a scratch copy of
+  // the outputs for the one-time form timing; bform -1 until timed, 0 FMA
+  // contraction, 1 tensor-core contraction
+  int bcap = 0, bform = -1;
+  double bms[2] = {0., 0.};
+  DeviceBuffer bsAa, bWa, bdva, bsAb, bWb, bdvb, bV2, bHaa, bHbbT, bscr;
 };
 
 void free_direct(Context* c) {
@@ -132,7 +153,8 @@ void free_direct(Context* c) {
                             &t->dval32, &t->W64, &t->W32})
       dev_free(c, *b);
   for (DeviceBuffer* b : {&d->V32, &d->tmp64, &d->tmp32, &d->ct64, &d->ct32, &d->V2mm, &d->rs_of, &d->lists, &d->seg,
-                          &d->Haa, &d->HbbT})
+                          &d->Haa, &d->HbbT, &d->bsAa, &d->bWa, &d->bdva, &d->bsAb, &d->bWb, &d->bdvb, &d->bV2,
+                          &d->bHaa, &d->bHbbT, &d->bscr})
     dev_free(c, *b);
   delete d;
   c->direct = nullptr;
@@ -225,7 +247,7 @@ __global__ void k_ds_values(int64_t N, int ns, int nd, int n, const uint64_t* __
       double a = __ldg(T + v + nn * o);
       for (int p = 0; p < n; ++p)
         if ((I >> p) & 1) a += Vat(p, p, v, o) - Vat(p, o, v, p);
-      sA64[t] = a;
+      if (sA64) sA64[t] = a;
       sA32[t] = (float)a;
     } else if (t < ts + td) {
       const int64_t u = t - ts;
@@ -233,7 +255,7 @@ __global__ void k_ds_values(int64_t N, int ns, int nd, int n, const uint64_t* __
       const int v1 = w & 31, o1 = (w >> 5) & 31, v2 = (w >> 10) & 31, o2 = (w >> 15) & 31;
       const double g = Vat(v1, o1, v2, o2) - Vat(v1, o2, v2, o1);
       const double d = ((w >> 20) & 1) ? -g : g;
-      dval64[u] = d;
+      if (dval64) dval64[u] = d;
       dval32[u] = (float)d;
     } else {
       const int64_t u = t - ts - td, vo = u / N;
@@ -242,7 +264,7 @@ __global__ void k_ds_values(int64_t N, int ns, int nd, int n, const uint64_t* __
       double w = 0.;
       for (int p = 0; p < n; ++p)
         if ((I >> p) & 1) w += Vat(p, p, v, o);
-      W64[u] = w;
+      if (W64) W64[u] = w;
       W32[u] = (float)w;
     }
   }
@@ -399,8 +421,18 @@ __global__ void __launch_bounds__(BIG ? kMmMaxWarps * 32 : 320, BIG ? 1 : 2)
                      const float* __restrict__ a_sA, const float* __restrict__ a_W, const int32_t* __restrict__ rs_of,
                      const uint16_t* __restrict__ lists, const int32_t* __restrict__ seg,
                      const float* __restrict__ V2, int n, const double* __restrict__ D, const float* __restrict__ C,
-                     float* __restrict__ sigma) {
+                     float* __restrict__ sigma, DsInst bi) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  {
+    const int inst = blockIdx.y;
+    if (bi.act && !bi.act[inst]) return;
+    a_sA += inst * bi.sA;
+    a_W += inst * bi.W;
+    V2 += inst * bi.V2;
+    D += inst * bi.vec;
+    C += inst * bi.vec;
+    sigma += inst * bi.vec;
+  }
   const int K = nsa + 1;
   float* Vp = (float*)smem_raw;                           // [K][mrp]
   float* G = Vp + (size_t)K * mrp;                        // [2][K][kMmCols]
@@ -593,7 +625,16 @@ __global__ void k_ds_dense_fill(int64_t na, int nda, const int32_t* __restrict__
 constexpr int kGmT = 64, kGmK = 16;
 __global__ void __launch_bounds__(256) k_ds_gemm2(int M, int N, int K1, int K2, const float* __restrict__ A1,
                                                   const float* __restrict__ B1, const float* __restrict__ A2,
-                                                  const float* __restrict__ B2, float* __restrict__ out) {
+                                                  const float* __restrict__ B2, float* __restrict__ out, GmInst bi) {
+  {
+    const int inst = blockIdx.z;
+    if (bi.act && !bi.act[inst]) return;
+    A1 += inst * bi.A1;
+    B1 += inst * bi.B1;
+    A2 += inst * bi.A2;
+    B2 += inst * bi.B2;
+    out += inst * bi.out;
+  }
   __shared__ __align__(16) float As[2][kGmK][kGmT + 4];
   __shared__ __align__(16) float Bs[2][kGmK][kGmT];
   const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
@@ -745,8 +786,17 @@ __device__ __forceinline__ void tc_store(const TcRegs& R, unsigned char* Ahi, un
 __global__ void __launch_bounds__(kTcThreads) k_tc_gemm2(int M, int N, int K1, int K2, int vecA,
                                                          const float* __restrict__ A1, const float* __restrict__ B1,
                                                          const float* __restrict__ A2, const float* __restrict__ B2,
-                                                         float* __restrict__ out) {
+                                                         float* __restrict__ out, GmInst bi) {
   extern __shared__ __align__(128) unsigned char tc_smem[];
+  {
+    const int inst = blockIdx.z;
+    if (bi.act && !bi.act[inst]) return;  // the whole CTA, before any TMEM or barrier
+    A1 += inst * bi.A1;
+    B1 += inst * bi.B1;
+    A2 += inst * bi.A2;
+    B2 += inst * bi.B2;
+    out += inst * bi.out;
+  }
   __shared__ __align__(8) uint64_t mbar[2];
   __shared__ uint32_t tslot;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -851,8 +901,18 @@ __global__ void __launch_bounds__(kOtThreads + 32, 1)
                      const float* __restrict__ a_sA, const float* __restrict__ a_W, const int32_t* __restrict__ rs_of,
                      const uint16_t* __restrict__ lists, const int32_t* __restrict__ seg,
                      const float* __restrict__ V2, int mrp, int n, const double* __restrict__ D,
-                     const float* __restrict__ C, float* __restrict__ sigma) {
+                     const float* __restrict__ C, float* __restrict__ sigma, DsInst bi) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  {
+    const int inst = blockIdx.y;
+    if (bi.act && !bi.act[inst]) return;  // the whole CTA, before any TMEM or barrier
+    a_sA += inst * bi.sA;
+    a_W += inst * bi.W;
+    V2 += inst * bi.V2;
+    D += inst * bi.vec;
+    C += inst * bi.vec;
+    sigma += inst * bi.vec;
+  }
   __shared__ __align__(8) uint64_t mbar[2];
   __shared__ uint32_t tslot;
   const int K = nsa + 1, kq4 = kpad >> 2;
@@ -1135,12 +1195,13 @@ static void direct_sigma_t(Context* c, const T* x, T* y) {
           const int vec = (na % 4 == 0 && nb % 4 == 0 && ((uintptr_t)x & 15) == 0) ? 1 : 0;
           k_tc_gemm2<<<g, kTcThreads, 2 * kTcStage, c->stream>>>((int)na, (int)nb, (int)na, (int)nb, vec,
                                                                 (const float*)d->Haa.ptr, (const float*)x,
-                                                                (const float*)x, (const float*)d->HbbT.ptr, (float*)y);
+                                                                (const float*)x, (const float*)d->HbbT.ptr, (float*)y,
+                                                                GmInst{});
         } else {
           dim3 g((unsigned)((nb + kGmT - 1) / kGmT), (unsigned)((na + kGmT - 1) / kGmT));
           k_ds_gemm2<<<g, 256, 0, c->stream>>>((int)na, (int)nb, (int)na, (int)nb, (const float*)d->Haa.ptr,
                                                 (const float*)x, (const float*)x, (const float*)d->HbbT.ptr,
-                                                (float*)y);
+                                                (float*)y, GmInst{});
         }
         QDKGB_CHECK_LAUNCH();
       };
@@ -1183,7 +1244,7 @@ static void direct_sigma_t(Context* c, const T* x, T* y) {
                 d->mm_vec ? 1 : 0, (const int32_t*)A.sJ.ptr, (const int32_t*)A.svo.ptr, (const float*)A.sA32.ptr,
                 (const float*)A.W32.ptr, (const int32_t*)d->rs_of.ptr, (const uint16_t*)d->lists.ptr,
                 (const int32_t*)d->seg.ptr, (const float*)d->V2mm.ptr, d->mrp, d->n, (const double*)c->H.diag.ptr,
-                (const float*)x, yo);
+                (const float*)x, yo, DsInst{});
           };
           switch (d->otc_jpt) {
             case 2: gt(k_ds_opposite_tc<2>); break;
@@ -1198,7 +1259,7 @@ static void direct_sigma_t(Context* c, const T* x, T* y) {
               (int)na, (int)nb, A.ns, d->mr, d->mrp, d->off_u16, d->seg_max, d->mm_vec ? 1 : 0,
               (const int32_t*)A.sJ.ptr, (const int32_t*)A.svo.ptr, (const float*)A.sA32.ptr, (const float*)A.W32.ptr,
               (const int32_t*)d->rs_of.ptr, (const uint16_t*)d->lists.ptr, (const int32_t*)d->seg.ptr,
-              (const float*)d->V2mm.ptr, d->n, (const double*)c->H.diag.ptr, (const float*)x, yo);
+              (const float*)d->V2mm.ptr, d->n, (const double*)c->H.diag.ptr, (const float*)x, yo, DsInst{});
         };
         if (d->mm_threads <= 320) {
           switch (d->mm_jpt) {
@@ -1417,8 +1478,9 @@ static void build_mm_tables(Context* c, DirectSigma* d) {
   d->mm = true;
 }
 
-static DirectSigma* direct_prepare(Context* c) {
-  if (!c->have_ints) throw Error(QDKGB_ERR_STATE, "integrals not set");
+// The direct sigma's structure for the context's space (built once per
+// space; set_dets frees it) and its per-build settings from the environment.
+static DirectSigma* direct_structure(Context* c) {
   if (!c->have_dets) throw Error(QDKGB_ERR_STATE, "determinants not set");
   DetSpace& S = c->dets;
   for (int64_t g = 0; g < S.ngroups; ++g)
@@ -1484,6 +1546,12 @@ static DirectSigma* direct_prepare(Context* c) {
         set_max_dynamic_smem(f, (int)smem);
     }
   }
+  return d;
+}
+
+static DirectSigma* direct_prepare(Context* c) {
+  if (!c->have_ints) throw Error(QDKGB_ERR_STATE, "integrals not set");
+  DirectSigma* d = direct_structure(c);
   direct_values(c, d);
   return d;
 }
@@ -1532,6 +1600,163 @@ void build_direct_sigma(Context* c) {
   H.nnz = 0;
   H.valid = true;
   c->op_direct = true;
+}
+
+// ---------------------------------------------------------------- batched CASCI
+// FP32 sigma of a sub-batch of instances of one complete space (the batched
+// solver's new directions): the structure of the context's space, the value
+// tables per instance from the instances' integrals (T: [B][n^2], V:
+// [B][n^4] on the device).  False where the contraction form does not apply
+// (the caller keeps the stored FP32 slab).
+bool direct_batch_prepare(Context* c, int B, const double* T, const double* V) {
+  const char* env = std::getenv("QDKGB_BATCH_DIRECT");
+  if (env && env[0] == '0') return false;
+  DirectSigma* d = nullptr;
+  try {
+    d = direct_structure(c);
+  } catch (const Error&) {
+    return false;
+  }
+  if (!d->mm || !d->tc) return false;
+  const SpinTables& A = d->a;
+  const SpinTables& Bt = d->same ? d->a : d->b;
+  const int n = d->n;
+  const int64_t n2 = (int64_t)n * n, n4 = n2 * n2, na = A.nstr, nb = Bt.nstr, N = na * nb;
+  const int64_t sa = na * A.ns, wa = n2 * na, da = na * std::max(A.nd, 1);
+  const int64_t sb = nb * Bt.ns, wb = n2 * nb, db = nb * std::max(Bt.nd, 1);
+  float* sAa = dev_array<float>(c, d->bsAa, (size_t)(B * sa + 1));
+  float* Wa = dev_array<float>(c, d->bWa, (size_t)(B * wa));
+  float* dva = dev_array<float>(c, d->bdva, (size_t)(B * da));
+  float* sAb = d->same ? sAa : dev_array<float>(c, d->bsAb, (size_t)(B * sb + 1));
+  float* Wb = d->same ? Wa : dev_array<float>(c, d->bWb, (size_t)(B * wb));
+  float* dvb = d->same ? dva : dev_array<float>(c, d->bdvb, (size_t)(B * db));
+  float* V2 = dev_array<float>(c, d->bV2, (size_t)(B * n2 * d->mrp));
+  float* Haa = dev_array<float>(c, d->bHaa, (size_t)(B * na * na));
+  float* HbbT = dev_array<float>(c, d->bHbbT, (size_t)(B * nb * nb));
+  dev_array<float>(c, d->bscr, (size_t)(B * N));
+  QDKGB_CUDA(cudaMemsetAsync(Haa, 0, (size_t)(B * na * na) * 4, c->stream));
+  QDKGB_CUDA(cudaMemsetAsync(HbbT, 0, (size_t)(B * nb * nb) * 4, c->stream));
+  auto vals = [&](const SpinTables& t, int q, float* sA, float* W, float* dv) {
+    const int64_t tot = t.nstr * t.ns + t.nstr * t.nd + n2 * t.nstr;
+    const unsigned blocks = (unsigned)std::min<int64_t>((tot + 255) / 256, (int64_t)c->sm_count * 4);
+    k_ds_values<<<blocks, 256, 0, c->stream>>>(t.nstr, t.ns, t.nd, n, (const uint64_t*)t.str.ptr,
+                                               (const int32_t*)t.svo.ptr, (const uint32_t*)t.dvo.ptr, T + q * n2,
+                                               V + q * n4, nullptr, sA, nullptr, dv, nullptr, W);
+    QDKGB_CHECK_LAUNCH();
+  };
+  for (int q = 0; q < B; ++q) {
+    vals(A, q, sAa + q * sa, Wa + q * wa, dva + q * da);
+    if (!d->same) vals(Bt, q, sAb + q * sb, Wb + q * wb, dvb + q * db);
+    const int64_t tot = n2 * d->mrp;
+    k_ds_v2mm<<<(unsigned)std::min<int64_t>((tot + 255) / 256, (int64_t)c->sm_count * 4), 256, 0, c->stream>>>(
+        V + q * n4, (const int32_t*)d->rs_of.ptr, n, d->mr, d->mrp, V2 + q * n2 * d->mrp);
+    QDKGB_CHECK_LAUNCH();
+    const int64_t fill = na * A.nd + nb * Bt.nd + nb * Bt.ns;
+    k_ds_dense_fill<<<(unsigned)std::min<int64_t>((fill + 255) / 256, (int64_t)c->sm_count * 4), 256, 0,
+                      c->stream>>>(na, A.nd, (const int32_t*)A.dJ.ptr, dva + q * da, nb, Bt.nd, Bt.ns,
+                                   (const int32_t*)Bt.dJ.ptr, dvb + q * db, (const int32_t*)Bt.sJ.ptr,
+                                   (const int32_t*)Bt.svo.ptr, sAb + q * sb, Haa + q * na * na, HbbT + q * nb * nb);
+    QDKGB_CHECK_LAUNCH();
+  }
+  set_max_dynamic_smem((const void*)k_tc_gemm2, 2 * kTcStage);
+  d->bcap = B;
+  return true;
+}
+
+// y = sigma(x) in FP32 for the instances with act[q] != 0 (x, y: [B][N];
+// D: [B][N] the FP64 diagonals): the dense same-spin products, then the
+// contraction (tensor cores or FMA pipe, timed on the first call, which is
+// not captured in a graph).
+void direct_batch_sigma(Context* c, int B, const int* act, const double* D, const float* x, float* y) {
+  DirectSigma* d = c->direct;
+  const SpinTables& A = d->a;
+  const SpinTables& Bt = d->same ? d->a : d->b;
+  const int n = d->n;
+  const int64_t n2 = (int64_t)n * n, na = A.nstr, nb = Bt.nstr, N = na * nb;
+  const float* sAa = (const float*)d->bsAa.ptr;
+  const float* Wa = (const float*)d->bWa.ptr;
+  const int vec = (na % 4 == 0 && nb % 4 == 0 && ((uintptr_t)x & 15) == 0) ? 1 : 0;
+  {
+    dim3 g((unsigned)((nb + kTcN - 1) / kTcN), (unsigned)((na + kTcM - 1) / kTcM), (unsigned)B);
+    k_tc_gemm2<<<g, kTcThreads, 2 * kTcStage, c->stream>>>((int)na, (int)nb, (int)na, (int)nb, vec,
+                                                          (const float*)d->bHaa.ptr, x, x, (const float*)d->bHbbT.ptr,
+                                                          y, GmInst{act, na * na, N, N, nb * nb, N});
+    QDKGB_CHECK_LAUNCH();
+  }
+  const DsInst bi{act, na * A.ns, n2 * na, n2 * d->mrp, N};
+  auto contract = [&](float* yo, int form) {
+    if (form == 1) {
+      auto gt = [&](auto kern) {
+        kern<<<dim3((unsigned)na, (unsigned)B), kOtThreads + 32, d->otc_smem, c->stream>>>(
+            (int)na, (int)nb, A.ns, d->mr, d->mr + d->n + 1, d->kpad, d->off_u16, d->seg_max, d->mm_vec ? 1 : 0,
+            (const int32_t*)A.sJ.ptr, (const int32_t*)A.svo.ptr, sAa, Wa, (const int32_t*)d->rs_of.ptr,
+            (const uint16_t*)d->lists.ptr, (const int32_t*)d->seg.ptr, (const float*)d->bV2.ptr, d->mrp, d->n, D, x,
+            yo, bi);
+      };
+      switch (d->otc_jpt) {
+        case 2: gt(k_ds_opposite_tc<2>); break;
+        case 4: gt(k_ds_opposite_tc<4>); break;
+        default: gt(k_ds_opposite_tc<8>); break;
+      }
+    } else {
+      auto go = [&](auto kern) {
+        kern<<<dim3((unsigned)na, (unsigned)B), d->mm_threads, d->mm_smem, c->stream>>>(
+            (int)na, (int)nb, A.ns, d->mr, d->mrp, d->off_u16, d->seg_max, d->mm_vec ? 1 : 0,
+            (const int32_t*)A.sJ.ptr, (const int32_t*)A.svo.ptr, sAa, Wa, (const int32_t*)d->rs_of.ptr,
+            (const uint16_t*)d->lists.ptr, (const int32_t*)d->seg.ptr, (const float*)d->bV2.ptr, d->n, D, x, yo,
+            bi);
+      };
+      if (d->mm_threads <= 320) {
+        switch (d->mm_jpt) {
+          case 2: go(k_ds_opposite_mm<2, false>); break;
+          case 4: go(k_ds_opposite_mm<4, false>); break;
+          case 6: go(k_ds_opposite_mm<6, false>); break;
+          case 8: go(k_ds_opposite_mm<8, false>); break;
+          case 12: go(k_ds_opposite_mm<12, false>); break;
+          case 16: go(k_ds_opposite_mm<16, false>); break;
+          default: go(k_ds_opposite_mm<24, false>); break;
+        }
+      } else {
+        switch (d->mm_jpt) {
+          case 2: go(k_ds_opposite_mm<2, true>); break;
+          case 4: go(k_ds_opposite_mm<4, true>); break;
+          case 6: go(k_ds_opposite_mm<6, true>); break;
+          case 8: go(k_ds_opposite_mm<8, true>); break;
+          case 12: go(k_ds_opposite_mm<12, true>); break;
+          default: go(k_ds_opposite_mm<16, true>); break;
+        }
+      }
+    }
+    QDKGB_CHECK_LAUNCH();
+  };
+  if (d->bform < 0) {
+    if (!d->otc) {
+      d->bform = 0;
+    } else {
+      float* sc = (float*)d->bscr.ptr;
+      cudaEvent_t e0, e1;
+      QDKGB_CUDA(cudaEventCreate(&e0));
+      QDKGB_CUDA(cudaEventCreate(&e1));
+      for (int form = 0; form < 2; ++form) {
+        double tot = 0.;
+        for (int r = 0; r < 3; ++r) {
+          QDKGB_CUDA(cudaMemcpyAsync(sc, y, (size_t)(B * N) * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
+          QDKGB_CUDA(cudaEventRecord(e0, c->stream));
+          contract(sc, form);
+          QDKGB_CUDA(cudaEventRecord(e1, c->stream));
+          QDKGB_CUDA(cudaEventSynchronize(e1));
+          float ms = 0.f;
+          QDKGB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+          if (r > 0) tot += ms;
+        }
+        d->bms[form] = tot / 2.0;
+      }
+      QDKGB_CUDA(cudaEventDestroy(e0));
+      QDKGB_CUDA(cudaEventDestroy(e1));
+      d->bform = d->bms[1] < d->bms[0] ? 1 : 0;
+    }
+  }
+  contract(y, d->bform);
 }
 
 }  // namespace qdkgb

@@ -248,6 +248,12 @@ void build_direct_sigma(Context* c);
 // the stored FP64 slab (mixed form); false where the contraction form does
 // not apply.
 bool attach_direct_fp32(Context* c);
+// Batched CASCI's FP32 sigma through the direct contraction: per-instance
+// value tables of a sub-batch (T: [B][n^2], V: [B][n^4] on the device; false
+// where the form does not apply), then y = sigma(x) for the active instances
+// (x, y: [B][N] FP32; D: [B][N] the diagonals).
+bool direct_batch_prepare(Context* c, int B, const double* T, const double* V);
+void direct_batch_sigma(Context* c, int B, const int* act, const double* D, const float* x, float* y);
 // The direct sigma's FP32 form: contraction in use (0 element-wise walk,
 // 1 FMA pipe, 2 tensor cores), same-spin form (-1 not yet timed, 0
 // element-wise, 1 dense) and the times (ms) of the same-spin forms

@@ -57,6 +57,23 @@ def test_batch_mixed_matches_oracle(ctx, oracle, pkg, capi, persistent):
         assert its[i] > 0
 
 
+def test_batch_direct_sigma_equals_slab_sigma(ctx, pkg, capi, monkeypatch, oracle):
+    """The lockstep solver's new directions through the direct contraction
+    (default for complete spaces) or the stored FP32 slab
+    (QDKGB_BATCH_DIRECT=0): the same energies and 1-RDMs (the full-precision
+    refreshes decide convergence), both at the oracle's."""
+    inst = _instances(pkg, [(10, 5, 5), (8, 4, 4), (10, 5, 4), (6, 3, 3), (8, 4, 4)], 800)
+    E1, R1, _, _ = capi.casci_batch(ctx, inst, persistent=0)
+    monkeypatch.setenv("QDKGB_BATCH_DIRECT", "0")
+    E0, R0, _, _ = capi.casci_batch(ctx, inst, persistent=0)
+    assert np.max(np.abs(E1 - E0)) < 1e-9
+    for i in range(len(inst)):
+        np.testing.assert_allclose(R1[i], R0[i], atol=1e-7, rtol=0)
+    for j in (0, 2):
+        Eo, _ = _oracle_ref(oracle, pkg, inst[j])
+        assert abs(E1[j] - Eo) < 1e-8
+
+
 @pytest.mark.parametrize("persistent", [1, 0])
 def test_batch_fp64_matches_oracle(ctx, oracle, pkg, capi, persistent):
     inst = _instances(pkg, SHAPES[:5], 200)
