@@ -137,12 +137,10 @@ struct DirectSigma {
   size_t otc_smem = 0;
   DeviceBuffer Haa, HbbT;
   // batched CASCI over instances of this space (direct_batch_*): per-instance
-  // FP32 value tables, their dense same-spin matrices and a scratch copy of
-  // the outputs for the one-time form timing; bform -1 until timed, 0 FMA
-  // contraction, 1 tensor-core contraction
+  // FP32 value tables and their dense same-spin matrices; bform -1 until the
+  // first call fixes the contraction form (0 FMA pipe, 1 tensor cores)
   int bcap = 0, bform = -1;
-  double bms[2] = {0., 0.};
-  DeviceBuffer bsAa, bWa, bdva, bsAb, bWb, bdvb, bV2, bHaa, bHbbT, bscr;
+  DeviceBuffer bsAa, bWa, bdva, bsAb, bWb, bdvb, bV2, bHaa, bHbbT;
 };
 
 void free_direct(Context* c) {
@@ -154,7 +152,7 @@ void free_direct(Context* c) {
       dev_free(c, *b);
   for (DeviceBuffer* b : {&d->V32, &d->tmp64, &d->tmp32, &d->ct64, &d->ct32, &d->V2mm, &d->rs_of, &d->lists, &d->seg,
                           &d->Haa, &d->HbbT, &d->bsAa, &d->bWa, &d->bdva, &d->bsAb, &d->bWb, &d->bdvb, &d->bV2,
-                          &d->bHaa, &d->bHbbT, &d->bscr})
+                          &d->bHaa, &d->bHbbT})
     dev_free(c, *b);
   delete d;
   c->direct = nullptr;
@@ -1633,7 +1631,6 @@ bool direct_batch_prepare(Context* c, int B, const double* T, const double* V) {
   float* V2 = dev_array<float>(c, d->bV2, (size_t)(B * n2 * d->mrp));
   float* Haa = dev_array<float>(c, d->bHaa, (size_t)(B * na * na));
   float* HbbT = dev_array<float>(c, d->bHbbT, (size_t)(B * nb * nb));
-  dev_array<float>(c, d->bscr, (size_t)(B * N));
   QDKGB_CUDA(cudaMemsetAsync(Haa, 0, (size_t)(B * na * na) * 4, c->stream));
   QDKGB_CUDA(cudaMemsetAsync(HbbT, 0, (size_t)(B * nb * nb) * 4, c->stream));
   auto vals = [&](const SpinTables& t, int q, float* sA, float* W, float* dv) {
@@ -1665,8 +1662,7 @@ bool direct_batch_prepare(Context* c, int B, const double* T, const double* V) {
 
 // y = sigma(x) in FP32 for the instances with act[q] != 0 (x, y: [B][N];
 // D: [B][N] the FP64 diagonals): the dense same-spin products, then the
-// contraction (tensor cores or FMA pipe, timed on the first call, which is
-// not captured in a graph).
+// contraction (tensor cores or FMA pipe by a fixed rule).
 void direct_batch_sigma(Context* c, int B, const int* act, const double* D, const float* x, float* y) {
   DirectSigma* d = c->direct;
   const SpinTables& A = d->a;
@@ -1730,31 +1726,12 @@ void direct_batch_sigma(Context* c, int B, const int* act, const double* D, cons
     QDKGB_CHECK_LAUNCH();
   };
   if (d->bform < 0) {
-    if (!d->otc) {
-      d->bform = 0;
-    } else {
-      float* sc = (float*)d->bscr.ptr;
-      cudaEvent_t e0, e1;
-      QDKGB_CUDA(cudaEventCreate(&e0));
-      QDKGB_CUDA(cudaEventCreate(&e1));
-      for (int form = 0; form < 2; ++form) {
-        double tot = 0.;
-        for (int r = 0; r < 3; ++r) {
-          QDKGB_CUDA(cudaMemcpyAsync(sc, y, (size_t)(B * N) * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
-          QDKGB_CUDA(cudaEventRecord(e0, c->stream));
-          contract(sc, form);
-          QDKGB_CUDA(cudaEventRecord(e1, c->stream));
-          QDKGB_CUDA(cudaEventSynchronize(e1));
-          float ms = 0.f;
-          QDKGB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-          if (r > 0) tot += ms;
-        }
-        d->bms[form] = tot / 2.0;
-      }
-      QDKGB_CUDA(cudaEventDestroy(e0));
-      QDKGB_CUDA(cudaEventDestroy(e1));
-      d->bform = d->bms[1] < d->bms[0] ? 1 : 0;
-    }
+    // a fixed rule, so that repeated calls (eager or graph-replayed) take the
+    // same form and give the same sums: the tensor cores when E has more than
+    // one 128-row tile, else the FMA pipe (QDKGB_BATCH_CONTRACTION=tc|fma)
+    const char* env = std::getenv("QDKGB_BATCH_CONTRACTION");
+    const int mrows = d->mr + d->n + 1;
+    d->bform = (d->otc && (env ? env[0] == 't' : mrows > 128)) ? 1 : 0;
   }
   contract(y, d->bform);
 }
