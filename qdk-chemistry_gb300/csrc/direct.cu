@@ -1619,7 +1619,7 @@ bool direct_batch_prepare(Context* c, int B, const double* T, const double* V) {
   const SpinTables& A = d->a;
   const SpinTables& Bt = d->same ? d->a : d->b;
   const int n = d->n;
-  const int64_t n2 = (int64_t)n * n, n4 = n2 * n2, na = A.nstr, nb = Bt.nstr, N = na * nb;
+  const int64_t n2 = (int64_t)n * n, n4 = n2 * n2, na = A.nstr, nb = Bt.nstr;
   const int64_t sa = na * A.ns, wa = n2 * na, da = na * std::max(A.nd, 1);
   const int64_t sb = nb * Bt.ns, wb = n2 * nb, db = nb * std::max(Bt.nd, 1);
   float* sAa = dev_array<float>(c, d->bsAa, (size_t)(B * sa + 1));
