@@ -589,13 +589,17 @@ def run_batched(args):
                                   "sample": "every 8th instance (%d) through qdkgb_casci FP64, scaled" % len(sample),
                                   "max_abs_energy_diff_vs_batch": float(max(dE))},
         "batch_speedup_vs_per_instance_fp64": t_loop / t,
-        "roofline": {"bound": "hbm", "kernel": "the lockstep solve (k_slab_sigma32v<4> over all active instances "
-                                               "per inner iteration, batched vector kernels)",
+        "roofline": {"bound": "hbm", "kernel": "the lockstep solve: new directions through the direct contraction "
+                                               "(k_ds_opposite_mm FMA pipe + k_tc_gemm2 tcgen05 same-spin products, "
+                                               "instance grid axis), full-precision refreshes through the stored "
+                                               "split slab (k_slab_sigma<2>), batched vector kernels",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_kind, "traffic": None,
                      "algorithmic_bytes": sigma_bytes,
-                     "note": "sigma bytes of the whole solve (iterations x stored values x 4 B per instance) over "
-                             "the call's wall time, which also holds emission, vector work and the eigensolves"},
+                     "note": "slab-equivalent sigma bytes of the whole solve (iterations x stored values x 4 B per "
+                             "instance) over the call's wall time, which also holds emission, vector work and the "
+                             "eigensolves; the FP32 sigmas no longer stream the stored values "
+                             "(QDKGB_BATCH_DIRECT=0 restores the slab sigma), so this is an equivalent rate"},
         "persistent_s": t_pers, "persistent_plan": plan,
         "sigma_gbs_per_fp32_sweep_bytes": _batch_bytes(inst),
         "max_sigma_applications": max(i["iterations"] for i in infos),
