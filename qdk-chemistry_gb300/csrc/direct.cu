@@ -136,11 +136,17 @@ struct DirectSigma {
   double otc_ms[2] = {0., 0.};
   size_t otc_smem = 0;
   DeviceBuffer Haa, HbbT;
+  // the dense products' operands split into TF32 parts in the blocked layout
+  // (k_tc_split): H_aa (A form), H_bb^T (B form) per build, x in both forms
+  // per sigma; nkb1 / nkb2 the K blocks of the two products
+  DeviceBuffer HaaS, HbbS, XA, XB;
+  int nkb1 = 0, nkb2 = 0;
+  int64_t szA1 = 0, szB1 = 0, szA2 = 0, szB2 = 0;  // floats per split part
   // batched CASCI over instances of this space (direct_batch_*): per-instance
   // FP32 value tables and their dense same-spin matrices; bform -1 until the
   // first call fixes the contraction form (0 FMA pipe, 1 tensor cores)
   int bcap = 0, bform = -1;
-  DeviceBuffer bsAa, bWa, bdva, bsAb, bWb, bdvb, bV2, bHaa, bHbbT;
+  DeviceBuffer bsAa, bWa, bdva, bsAb, bWb, bdvb, bV2, bHaa, bHbbT, bHaaS, bHbbS, bXA, bXB;
 };
 
 void free_direct(Context* c) {
@@ -152,7 +158,8 @@ void free_direct(Context* c) {
       dev_free(c, *b);
   for (DeviceBuffer* b : {&d->V32, &d->tmp64, &d->tmp32, &d->ct64, &d->ct32, &d->V2mm, &d->rs_of, &d->lists, &d->seg,
                           &d->Haa, &d->HbbT, &d->bsAa, &d->bWa, &d->bdva, &d->bsAb, &d->bWb, &d->bdvb, &d->bV2,
-                          &d->bHaa, &d->bHbbT})
+                          &d->bHaa, &d->bHbbT, &d->HaaS, &d->HbbS, &d->XA, &d->XB, &d->bHaaS, &d->bHbbS,
+                          &d->bXA, &d->bXB})
     dev_free(c, *b);
   delete d;
   c->direct = nullptr;
@@ -879,6 +886,191 @@ __global__ void __launch_bounds__(kTcThreads) k_tc_gemm2(int M, int N, int K1, i
   if (!ok && tid == 0) atomicOr(&g_tc_fault, 1u);
 }
 
+// Operands of the dense same-spin products, split once into TF32 high and
+// low parts in the tensor core's blocked K-major layout, so that a K block
+// of a tile is one contiguous 16 KB (A: 128 rows x 32 K) or 8 KB (B: 64
+// rows x 32 K) run per part that one bulk copy (TMA) moves into shared
+// memory.  Block (rb, kb) of an operand with nkb K blocks starts at float
+// (rb nkb + kb) rows 32; inside it the 16-byte chunk c holds rows
+// rb rows + (c / 64) 8 + c % 8, K kb 32 + ((c / 8) % 8) 4 .. + 3.  Source
+// element (r, k): S[r ld + k] (A form) or S[k ld + r] (B form, the second
+// product's C H^T and the first's C read as K x N).
+constexpr int kSpRowsA = 128, kSpRowsB = 64, kSpK = 32;
+__global__ void k_tc_split(const float* __restrict__ S, int R, int K, int64_t ld, int bform, int rows, int nkb,
+                           int64_t nblk, float* __restrict__ hi, float* __restrict__ lo, int64_t sstride,
+                           int64_t dstride, const int* __restrict__ act) {
+  // grid axis y = instance (source and destination strides; act skips)
+  if (act && !act[blockIdx.y]) return;
+  S += blockIdx.y * sstride;
+  hi += blockIdx.y * dstride;
+  lo += blockIdx.y * dstride;
+  const int64_t per = (int64_t)rows * 8, tot = nblk * per;
+  for (int64_t id = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; id < tot; id += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t blk = id / per;
+    const int c = (int)(id - blk * per);
+    const int rb = (int)(blk / nkb), kb = (int)(blk - (int64_t)rb * nkb);
+    const int cm = c >> 3, r = rb * rows + (cm >> 3) * 8 + (c & 7), k0 = kb * kSpK + (cm & 7) * 4;
+    float h[4], l[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int k = k0 + q;
+      const float v = (r < R && k < K) ? (bform ? S[(int64_t)k * ld + r] : S[(int64_t)r * ld + k]) : 0.f;
+      h[q] = tc::to_tf32(v);
+      l[q] = tc::to_tf32(v - h[q]);
+    }
+    *(float4*)(hi + blk * rows * kSpK + (int64_t)c * 4) = make_float4(h[0], h[1], h[2], h[3]);
+    *(float4*)(lo + blk * rows * kSpK + (int64_t)c * 4) = make_float4(l[0], l[1], l[2], l[3]);
+  }
+}
+
+// Pre-split operands of one product pair and their instance strides.
+struct GmSplit {
+  const float *a1h, *a1l, *b1h, *b1l, *a2h, *a2l, *b2h, *b2l;
+  int nkb1, nkb2;
+  const int* act;
+  int64_t sa1, sb1, sa2, sb2, sout;  // per-instance strides (floats)
+};
+
+// out (M x N) = A1 B1 + A2 B2 on tcgen05 (TF32 x 3) from pre-split operands:
+// warp 0 lane 0 fills a ring of kTmStages shared-memory stages with four
+// bulk copies per K block (A hi / lo 16 KB, B hi / lo 8 KB, one mbarrier
+// with the byte count), warp 1 lane 0 issues the twelve MMAs per block and
+// commits each stage back to its producer, warps 2-5 (one per TMEM lane
+// quadrant) read the 128 x 64 FP32 tile out after the last commit.  Every
+// wait is bounded; a timeout sets g_tc_fault and the tile is NaN.
+constexpr int kTmStages = 2, kTmThreads = 192;
+constexpr int kTmStage = 2 * kTcABytes + 2 * kTcBBytes;
+__global__ void __launch_bounds__(kTmThreads) k_tc_gemm2b(int M, int N, GmSplit g, float* __restrict__ out) {
+  extern __shared__ __align__(128) unsigned char tm_smem[];
+  __shared__ __align__(8) uint64_t full[kTmStages], empty[kTmStages], done;
+  __shared__ uint32_t tslot;
+  __shared__ int fail;
+  const int inst = blockIdx.z;
+  if (g.act && !g.act[inst]) return;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int rb = blockIdx.y, nbk = blockIdx.x;
+  if (warp == 0) tc::tmem_alloc(&tslot, kTcN);
+  if (tid == 0) {
+    for (int s = 0; s < kTmStages; ++s) {
+      tc::mbar_init(&full[s], 1);
+      tc::mbar_init(&empty[s], 1);
+    }
+    tc::mbar_init(&done, 1);
+    tc::mbar_init_fence();
+    fail = 0;
+  }
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t tmem = tslot;
+  const int nblk = g.nkb1 + g.nkb2;
+  if (warp == 0 && lane == 0) {
+    // producer
+    for (int b = 0; b < nblk; ++b) {
+      const int s = b % kTmStages;
+      if (b >= kTmStages && !tc::mbar_wait(&empty[s], (uint32_t)((b / kTmStages - 1) & 1), kTcSpin)) {
+        fail = 1;
+        break;
+      }
+      const bool p2 = b >= g.nkb1;
+      const int kb = p2 ? b - g.nkb1 : b, nkb = p2 ? g.nkb2 : g.nkb1;
+      const int64_t ao = (int64_t)inst * (p2 ? g.sa2 : g.sa1) + ((int64_t)rb * nkb + kb) * (kSpRowsA * kSpK);
+      const int64_t bo = (int64_t)inst * (p2 ? g.sb2 : g.sb1) + ((int64_t)nbk * nkb + kb) * (kSpRowsB * kSpK);
+      unsigned char* st = tm_smem + s * kTmStage;
+      tc::mbar_expect_tx(&full[s], (uint32_t)kTmStage);
+      tc::bulk_g2s(st, (p2 ? g.a2h : g.a1h) + ao, kTcABytes, &full[s]);
+      tc::bulk_g2s(st + kTcABytes, (p2 ? g.a2l : g.a1l) + ao, kTcABytes, &full[s]);
+      tc::bulk_g2s(st + 2 * kTcABytes, (p2 ? g.b2h : g.b1h) + bo, kTcBBytes, &full[s]);
+      tc::bulk_g2s(st + 2 * kTcABytes + kTcBBytes, (p2 ? g.b2l : g.b1l) + bo, kTcBBytes, &full[s]);
+    }
+  } else if (warp == 1 && lane == 0) {
+    // MMA issue
+    constexpr uint32_t idesc = tc::idesc_tf32(kTcM, kTcN);
+    constexpr uint32_t sbo = (kTcBK / 4) * 128;
+    bool ok = true;
+    for (int b = 0; b < nblk; ++b) {
+      const int s = b % kTmStages;
+      if (!tc::mbar_wait(&full[s], (uint32_t)((b / kTmStages) & 1), kTcSpin)) {
+        ok = false;
+        break;
+      }
+      tc::fence_after();
+      unsigned char* st = tm_smem + s * kTmStage;
+      const uint32_t ah = tc::smem_addr(st), al = ah + kTcABytes, bh = ah + 2 * kTcABytes, bl = bh + kTcBBytes;
+#pragma unroll
+      for (int ks = 0; ks < kTcBK / 8; ++ks) {
+        const uint32_t ko = ks * 256;
+        tc::mma_tf32(tmem, tc::desc(ah + ko, 128, sbo), tc::desc(bh + ko, 128, sbo), idesc, (b | ks) ? 1u : 0u);
+        tc::mma_tf32(tmem, tc::desc(ah + ko, 128, sbo), tc::desc(bl + ko, 128, sbo), idesc, 1u);
+        tc::mma_tf32(tmem, tc::desc(al + ko, 128, sbo), tc::desc(bh + ko, 128, sbo), idesc, 1u);
+      }
+      tc::commit(&empty[s]);
+    }
+    if (!ok) fail = 1;
+    tc::commit(&done);  // completes when every MMA issued above has
+  } else if (warp >= 2) {
+    // epilogue: warp w reads TMEM lanes 32 (w % 4) ..
+    const int q = warp & 3;
+    const bool ok = __all_sync(0xffffffffu, tc::mbar_wait(&done, 0u, kTcSpin) && !fail);
+    tc::fence_after();
+    const int row = rb * kTcM + q * 32 + lane;
+    float* o = out + (int64_t)inst * g.sout;
+#pragma unroll 1
+    for (int cb = 0; cb < kTcN; cb += 16) {
+      float v[16];
+      if (ok) {
+        tc::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)cb, v);
+      } else {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) v[j] = __int_as_float(0x7fc00000);
+      }
+      if (row < M)
+#pragma unroll
+        for (int j = 0; j < 16; ++j)
+          if (nbk * kTcN + cb + j < N) o[(int64_t)row * N + nbk * kTcN + cb + j] = v[j];
+    }
+    if (!ok && lane == 0) atomicOr(&g_tc_fault, 1u);
+  }
+  tc::fence_before();
+  __syncthreads();
+  if (warp == 0) tc::tmem_free(tmem, kTcN);
+}
+
+// K blocks and split-part sizes (floats) of the dense products' operands
+static void tm_sizes(DirectSigma* d, int64_t na, int64_t nb) {
+  d->nkb1 = (int)((na + kSpK - 1) / kSpK);
+  d->nkb2 = (int)((nb + kSpK - 1) / kSpK);
+  const int64_t nrb = (na + kSpRowsA - 1) / kSpRowsA, nnb = (nb + kSpRowsB - 1) / kSpRowsB;
+  d->szA1 = nrb * d->nkb1 * kSpRowsA * kSpK;  // H_aa, A form
+  d->szB1 = nnb * d->nkb1 * kSpRowsB * kSpK;  // x as K x N, B form
+  d->szA2 = nrb * d->nkb2 * kSpRowsA * kSpK;  // x, A form
+  d->szB2 = nnb * d->nkb2 * kSpRowsB * kSpK;  // H_bb^T as K x N, B form
+}
+// split of B instances (hi at dst, lo at dst + part; instance strides)
+static void tm_split(Context* c, const float* S, int R, int K, int64_t ld, int bform, int nkb, float* dst,
+                     int64_t part, int B, int64_t sstride, int64_t dstride, const int* act) {
+  const int rows = bform ? kSpRowsB : kSpRowsA;
+  const int64_t nblk = (int64_t)((R + rows - 1) / rows) * nkb, tot = nblk * rows * 8;
+  const unsigned bx = (unsigned)std::max<int64_t>(1, std::min<int64_t>((tot + 255) / 256, (int64_t)c->sm_count * 8));
+  k_tc_split<<<dim3(bx, (unsigned)B), 256, 0, c->stream>>>(S, R, K, ld, bform, rows, nkb, nblk, dst, dst + part,
+                                                          sstride, dstride, act);
+  QDKGB_CHECK_LAUNCH();
+}
+// y = H_aa x + x H_bb^T for B instances from the pre-split matrices (hs:
+// H_aa parts, bs: H_bb^T parts, instance strides of the matrices' parts)
+static void tm_products(Context* c, DirectSigma* d, int64_t na, int64_t nb, int B, const int* act,
+                        const float* haa, const float* hbb, int64_t mstride_a, int64_t mstride_b, float* xa,
+                        float* xb, const float* x, float* y) {
+  const int64_t N = na * nb;
+  tm_split(c, x, (int)na, (int)nb, nb, 0, d->nkb2, xa, d->szA2, B, N, 2 * d->szA2, act);  // x as A2
+  tm_split(c, x, (int)nb, (int)na, nb, 1, d->nkb1, xb, d->szB1, B, N, 2 * d->szB1, act);  // x as B1
+  GmSplit g{haa, haa + d->szA1, xb, xb + d->szB1, xa, xa + d->szA2, hbb, hbb + d->szB2, d->nkb1, d->nkb2,
+            act, mstride_a, 2 * d->szB1, 2 * d->szA2, mstride_b, N};
+  dim3 grid((unsigned)((nb + kTcN - 1) / kTcN), (unsigned)((na + kTcM - 1) / kTcM), (unsigned)B);
+  k_tc_gemm2b<<<grid, kTmThreads, kTmStages * kTmStage, c->stream>>>((int)na, (int)nb, g, y);
+  QDKGB_CHECK_LAUNCH();
+}
+
 // The contraction form with E formed on the tensor cores (tcgen05, TF32 x 3;
 // the same terms and walk as k_ds_opposite_mm).  Per alpha string: the A
 // operand Vp^T (rows r, K = the singles and the own row, zero-padded to kpad)
@@ -1189,12 +1381,8 @@ static void direct_sigma_t(Context* c, const T* x, T* y) {
       // y = Haa x + x HbbT
       auto dense = [&]() {
         if (d->tc) {
-          dim3 g((unsigned)((nb + kTcN - 1) / kTcN), (unsigned)((na + kTcM - 1) / kTcM));
-          const int vec = (na % 4 == 0 && nb % 4 == 0 && ((uintptr_t)x & 15) == 0) ? 1 : 0;
-          k_tc_gemm2<<<g, kTcThreads, 2 * kTcStage, c->stream>>>((int)na, (int)nb, (int)na, (int)nb, vec,
-                                                                (const float*)d->Haa.ptr, (const float*)x,
-                                                                (const float*)x, (const float*)d->HbbT.ptr, (float*)y,
-                                                                GmInst{});
+          tm_products(c, d, na, nb, 1, nullptr, (const float*)d->HaaS.ptr, (const float*)d->HbbS.ptr, 0, 0,
+                      (float*)d->XA.ptr, (float*)d->XB.ptr, (const float*)x, (float*)y);
         } else {
           dim3 g((unsigned)((nb + kGmT - 1) / kGmT), (unsigned)((na + kGmT - 1) / kGmT));
           k_ds_gemm2<<<g, 256, 0, c->stream>>>((int)na, (int)nb, (int)na, (int)nb, (const float*)d->Haa.ptr,
@@ -1366,6 +1554,16 @@ static void direct_values(Context* c, DirectSigma* d) {
       (const float*)B.dval32.ptr, (const int32_t*)B.sJ.ptr, (const int32_t*)B.svo.ptr, (const float*)B.sA32.ptr, Haa,
       HbbT);
   QDKGB_CHECK_LAUNCH();
+  if (d->tc) {
+    tm_sizes(d, na, nb);
+    float* hs = dev_array<float>(c, d->HaaS, (size_t)(2 * d->szA1));
+    float* bs = dev_array<float>(c, d->HbbS, (size_t)(2 * d->szB2));
+    dev_array<float>(c, d->XA, (size_t)(2 * d->szA2));
+    dev_array<float>(c, d->XB, (size_t)(2 * d->szB1));
+    tm_split(c, Haa, (int)na, (int)na, na, 0, d->nkb1, hs, d->szA1, 1, 0, 0, nullptr);
+    tm_split(c, HbbT, (int)nb, (int)nb, nb, 1, d->nkb2, bs, d->szB2, 1, 0, 0, nullptr);
+    set_max_dynamic_smem((const void*)k_tc_gemm2b, kTmStages * kTmStage);
+  }
   if (env && env[0] == '1') d->dense_state = 1;
 }
 
@@ -1655,7 +1853,14 @@ bool direct_batch_prepare(Context* c, int B, const double* T, const double* V) {
                                    (const int32_t*)Bt.svo.ptr, sAb + q * sb, Haa + q * na * na, HbbT + q * nb * nb);
     QDKGB_CHECK_LAUNCH();
   }
-  set_max_dynamic_smem((const void*)k_tc_gemm2, 2 * kTcStage);
+  tm_sizes(d, na, nb);
+  float* hs = dev_array<float>(c, d->bHaaS, (size_t)(B * 2 * d->szA1));
+  float* bs = dev_array<float>(c, d->bHbbS, (size_t)(B * 2 * d->szB2));
+  dev_array<float>(c, d->bXA, (size_t)(B * 2 * d->szA2));
+  dev_array<float>(c, d->bXB, (size_t)(B * 2 * d->szB1));
+  tm_split(c, Haa, (int)na, (int)na, na, 0, d->nkb1, hs, d->szA1, B, na * na, 2 * d->szA1, nullptr);
+  tm_split(c, HbbT, (int)nb, (int)nb, nb, 1, d->nkb2, bs, d->szB2, B, nb * nb, 2 * d->szB2, nullptr);
+  set_max_dynamic_smem((const void*)k_tc_gemm2b, kTmStages * kTmStage);
   d->bcap = B;
   return true;
 }
@@ -1671,14 +1876,8 @@ void direct_batch_sigma(Context* c, int B, const int* act, const double* D, cons
   const int64_t n2 = (int64_t)n * n, na = A.nstr, nb = Bt.nstr, N = na * nb;
   const float* sAa = (const float*)d->bsAa.ptr;
   const float* Wa = (const float*)d->bWa.ptr;
-  const int vec = (na % 4 == 0 && nb % 4 == 0 && ((uintptr_t)x & 15) == 0) ? 1 : 0;
-  {
-    dim3 g((unsigned)((nb + kTcN - 1) / kTcN), (unsigned)((na + kTcM - 1) / kTcM), (unsigned)B);
-    k_tc_gemm2<<<g, kTcThreads, 2 * kTcStage, c->stream>>>((int)na, (int)nb, (int)na, (int)nb, vec,
-                                                          (const float*)d->bHaa.ptr, x, x, (const float*)d->bHbbT.ptr,
-                                                          y, GmInst{act, na * na, N, N, nb * nb, N});
-    QDKGB_CHECK_LAUNCH();
-  }
+  tm_products(c, d, na, nb, B, act, (const float*)d->bHaaS.ptr, (const float*)d->bHbbS.ptr, 2 * d->szA1,
+              2 * d->szB2, (float*)d->bXA.ptr, (float*)d->bXB.ptr, x, y);
   const DsInst bi{act, na * A.ns, n2 * na, n2 * d->mrp, N};
   auto contract = [&](float* yo, int form) {
     if (form == 1) {

@@ -88,6 +88,20 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, uint32_t
   return false;
 }
 
+// the expected byte count of the mbarrier's current phase (one arrival)
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_addr(b)), "r"(bytes)
+               : "memory");
+}
+// bulk copy (TMA, 1D) of `bytes` (a multiple of 16, both addresses 16-byte
+// aligned) from global to shared memory, completing on the mbarrier
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* b) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                   smem_addr(dst)),
+               "l"(src), "r"(bytes), "r"(smem_addr(b))
+               : "memory");
+}
+
 // TMEM columns for the CTA (one warp, power of two >= 32); the address lands
 // in *slot (shared memory)
 __device__ __forceinline__ void tmem_alloc(uint32_t* slot, uint32_t ncols) {
