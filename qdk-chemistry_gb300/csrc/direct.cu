@@ -126,7 +126,7 @@ struct DirectSigma {
   int dense_state = -1;
   double dense_ms[2] = {0., 0.};
   char mm_env = 0, dense_env = 0;  // QDKGB_DIRECT_MM / QDKGB_DIRECT_DENSE when built
-  bool tc = false;                 // dense products on the tensor cores (k_tc_gemm2; QDKGB_DIRECT_TC=0: FMA pipe)
+  bool tc = false;                 // tensor cores (k_tc_gemm2b, k_ds_opposite_tc; QDKGB_DIRECT_TC=0: FMA pipe)
   // the contraction's E on the tensor cores (k_ds_opposite_tc): K padded to
   // kpad, its shared memory, beta strings per thread
   // otc_state: -1 until the first FP32 sigma times the FMA and tensor-core
@@ -704,187 +704,14 @@ __global__ void __launch_bounds__(256) k_ds_gemm2(int M, int N, int K1, int K2, 
   }
 }
 
-// Dense same-spin products on the tensor cores: out (M x N) = A1 B1 + A2 B2
-// (row-major FP32) as TF32 x 3 (each operand split into a TF32 high part and
-// the TF32 rounding of the remainder; hi hi + hi lo + lo hi, FP32 accumulation
-// in TMEM: about FP32 accuracy).  A CTA owns a 128 x 64 tile of out (TMEM
-// columns 0..63, lane = row); K runs in blocks of 32 through two shared-
-// memory stages: all threads load and split a block into the canonical
-// K-major layout, one thread issues the twelve MMAs (four K steps of 8, three
-// products) and commits them to the stage's mbarrier, which the threads wait
-// on (bounded) before refilling that stage.
-constexpr int kTcM = 128, kTcN = 64, kTcBK = 32, kTcThreads = 128;
+// Tensor-core tiles (tcgen05, TF32 x 3: each FP32 operand split into a TF32
+// high part and the TF32 rounding of the remainder; hi hi + hi lo + lo hi
+// accumulated in FP32 in TMEM, about FP32 accuracy): 128 x 64 output tiles
+// (TMEM columns 0..63, lane = row), K in blocks of 32.
+constexpr int kTcM = 128, kTcN = 64, kTcBK = 32;
 constexpr int kTcABytes = kTcM * kTcBK * 4, kTcBBytes = kTcN * kTcBK * 4;
-constexpr int kTcStage = 2 * kTcABytes + 2 * kTcBBytes;  // 48 KB
 constexpr uint32_t kTcSpin = 1u << 22;
 __device__ unsigned int g_tc_fault;  // set by a CTA whose wait timed out (its tile is NaN)
-
-// Block b of the K loop, loaded into registers: A rows m0.. (128 x 32) as
-// 8 chunks of 4 consecutive K per thread, B (32 x 64, K-major in shared
-// memory) as 4 chunks of 4 K per thread; chunk c of an operand lands at byte
-// 16 c of its K-major layout (core matrix c / 8, row c % 8), so a warp's
-// stores fill 512 contiguous bytes.
-struct TcRegs {
-  float a[8][4], b[4][4];
-};
-
-__device__ __forceinline__ void tc_load(TcRegs& R, int b, int nb1, int M, int N, int K1, int K2, bool vecA,
-                                        const float* __restrict__ A1, const float* __restrict__ B1,
-                                        const float* __restrict__ A2, const float* __restrict__ B2, int m0, int n0,
-                                        int tid) {
-  const bool p2 = b >= nb1;
-  const float* A = p2 ? A2 : A1;
-  const float* B = p2 ? B2 : B1;
-  const int K = p2 ? K2 : K1, k0 = (p2 ? b - nb1 : b) * kTcBK;
-#pragma unroll
-  for (int j = 0; j < 8; ++j) {
-    const int c = tid + j * kTcThreads, cm = c >> 3, r = (cm >> 3) * 8 + (c & 7), k = k0 + (cm & 7) * 4;
-    const int64_t base = (int64_t)(m0 + r) * K + k;
-    if (m0 + r < M && vecA && k + 3 < K) {
-      const float4 v = __ldg((const float4*)(A + base));
-      R.a[j][0] = v.x;
-      R.a[j][1] = v.y;
-      R.a[j][2] = v.z;
-      R.a[j][3] = v.w;
-    } else {
-#pragma unroll
-      for (int q = 0; q < 4; ++q) R.a[j][q] = (m0 + r < M && k + q < K) ? __ldg(A + base + q) : 0.f;
-    }
-  }
-#pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    const int c = tid + j * kTcThreads, cm = c >> 3, n = (cm >> 3) * 8 + (c & 7), k = k0 + (cm & 7) * 4;
-#pragma unroll
-    for (int q = 0; q < 4; ++q)
-      R.b[j][q] = (n0 + n < N && k + q < K) ? __ldg(B + (int64_t)(k + q) * N + n0 + n) : 0.f;
-  }
-}
-
-__device__ __forceinline__ void tc_store(const TcRegs& R, unsigned char* Ahi, unsigned char* Alo,
-                                         unsigned char* Bhi, unsigned char* Blo, int tid) {
-#pragma unroll
-  for (int j = 0; j < 8; ++j) {
-    float h[4], l[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      h[q] = tc::to_tf32(R.a[j][q]);
-      l[q] = tc::to_tf32(R.a[j][q] - h[q]);
-    }
-    const int c = tid + j * kTcThreads;
-    *(float4*)(Ahi + 16 * c) = make_float4(h[0], h[1], h[2], h[3]);
-    *(float4*)(Alo + 16 * c) = make_float4(l[0], l[1], l[2], l[3]);
-  }
-#pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    float h[4], l[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      h[q] = tc::to_tf32(R.b[j][q]);
-      l[q] = tc::to_tf32(R.b[j][q] - h[q]);
-    }
-    const int c = tid + j * kTcThreads;
-    *(float4*)(Bhi + 16 * c) = make_float4(h[0], h[1], h[2], h[3]);
-    *(float4*)(Blo + 16 * c) = make_float4(l[0], l[1], l[2], l[3]);
-  }
-}
-
-__global__ void __launch_bounds__(kTcThreads) k_tc_gemm2(int M, int N, int K1, int K2, int vecA,
-                                                         const float* __restrict__ A1, const float* __restrict__ B1,
-                                                         const float* __restrict__ A2, const float* __restrict__ B2,
-                                                         float* __restrict__ out, GmInst bi) {
-  extern __shared__ __align__(128) unsigned char tc_smem[];
-  {
-    const int inst = blockIdx.z;
-    if (bi.act && !bi.act[inst]) return;  // the whole CTA, before any TMEM or barrier
-    A1 += inst * bi.A1;
-    B1 += inst * bi.B1;
-    A2 += inst * bi.A2;
-    B2 += inst * bi.B2;
-    out += inst * bi.out;
-  }
-  __shared__ __align__(8) uint64_t mbar[2];
-  __shared__ uint32_t tslot;
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int m0 = blockIdx.y * kTcM, n0 = blockIdx.x * kTcN;
-  if (warp == 0) tc::tmem_alloc(&tslot, kTcN);
-  if (tid == 0) {
-    tc::mbar_init(&mbar[0], 1);
-    tc::mbar_init(&mbar[1], 1);
-    tc::mbar_init_fence();
-  }
-  tc::fence_before();
-  __syncthreads();
-  tc::fence_after();
-  const uint32_t tmem = tslot;
-  constexpr uint32_t idesc = tc::idesc_tf32(kTcM, kTcN);
-  constexpr uint32_t sbo = (kTcBK / 4) * 128;
-  const int nb1 = (K1 + kTcBK - 1) / kTcBK, nblk = nb1 + (K2 + kTcBK - 1) / kTcBK;
-  uint32_t par0 = 0u, par1 = 0u;
-  bool ok = true;
-  TcRegs R;
-  tc_load(R, 0, nb1, M, N, K1, K2, vecA != 0, A1, B1, A2, B2, m0, n0, tid);
-  for (int b = 0; b < nblk && ok; ++b) {
-    const int s = b & 1;
-    unsigned char* st = tc_smem + s * kTcStage;
-    unsigned char* Ahi = st;
-    unsigned char* Alo = st + kTcABytes;
-    unsigned char* Bhi = st + 2 * kTcABytes;
-    unsigned char* Blo = st + 2 * kTcABytes + kTcBBytes;
-    if (b >= 2) {  // the stage's previous MMAs (block b - 2) have read it
-      ok = tc::mbar_wait(&mbar[s], s ? par1 : par0, kTcSpin);
-      if (s)
-        par1 ^= 1u;
-      else
-        par0 ^= 1u;
-      if (!ok) break;
-    }
-    tc_store(R, Ahi, Alo, Bhi, Blo, tid);
-    tc::fence_proxy_async();
-    __syncthreads();
-    if (tid == 0) {
-      tc::fence_after();
-      const uint32_t ah = tc::smem_addr(Ahi), al = tc::smem_addr(Alo), bh = tc::smem_addr(Bhi), bl = tc::smem_addr(Blo);
-#pragma unroll
-      for (int ks = 0; ks < kTcBK / 8; ++ks) {
-        const uint32_t ko = ks * 256;  // two core matrices along K per step
-        tc::mma_tf32(tmem, tc::desc(ah + ko, 128, sbo), tc::desc(bh + ko, 128, sbo), idesc, (b | ks) ? 1u : 0u);
-        tc::mma_tf32(tmem, tc::desc(ah + ko, 128, sbo), tc::desc(bl + ko, 128, sbo), idesc, 1u);
-        tc::mma_tf32(tmem, tc::desc(al + ko, 128, sbo), tc::desc(bh + ko, 128, sbo), idesc, 1u);
-      }
-      tc::commit(&mbar[s]);
-    }
-    if (b + 1 < nblk) tc_load(R, b + 1, nb1, M, N, K1, K2, vecA != 0, A1, B1, A2, B2, m0, n0, tid);
-  }
-  // the last (up to two) blocks' MMAs
-  for (int b = nblk >= 2 ? nblk - 2 : 0; ok && b < nblk; ++b) {
-    const int s = b & 1;
-    ok = tc::mbar_wait(&mbar[s], s ? par1 : par0, kTcSpin);
-    if (s)
-      par1 ^= 1u;
-    else
-      par0 ^= 1u;
-  }
-  tc::fence_after();
-  const int row = m0 + warp * 32 + lane;
-#pragma unroll 1
-  for (int c = 0; c < kTcN; c += 16) {
-    float v[16];
-    if (ok) {
-      tc::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);
-    } else {
-#pragma unroll
-      for (int j = 0; j < 16; ++j) v[j] = __int_as_float(0x7fc00000);
-    }
-    if (row < M)
-#pragma unroll
-      for (int j = 0; j < 16; ++j)
-        if (n0 + c + j < N) out[(int64_t)row * N + n0 + c + j] = v[j];
-  }
-  tc::fence_before();
-  __syncthreads();
-  if (warp == 0) tc::tmem_free(tmem, kTcN);
-  if (!ok && tid == 0) atomicOr(&g_tc_fault, 1u);
-}
 
 // Operands of the dense same-spin products, split once into TF32 high and
 // low parts in the tensor core's blocked K-major layout, so that a K block
@@ -1720,7 +1547,6 @@ static DirectSigma* direct_structure(Context* c) {
     d->otc_state = -1;
   }
   d->tc = tc;
-  if (tc) set_max_dynamic_smem((const void*)k_tc_gemm2, 2 * kTcStage);
   d->otc = false;
   if (tc && d->mm) {
     const int K = d->a.ns + 1, mrows = d->mr + d->n + 1;
