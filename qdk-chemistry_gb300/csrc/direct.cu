@@ -1175,6 +1175,27 @@ __global__ void __launch_bounds__(kOtThreads + 32, 1)
   if (warp == 0) tc::tmem_free(tmem, 256);
 }
 
+// the timed forms of this space's shape on the context (see Context::direct_tune)
+static void tune_record(Context* c, const DirectSigma* d) {
+  const int64_t na = d->a.nstr, nb = (d->same ? d->a : d->b).nstr;
+  for (Context::DirectTune& t : c->direct_tune)
+    if (t.n == d->n && t.na == na && t.nb == nb && t.tc == d->tc) {
+      t.dense = d->dense_state;
+      t.otc = d->otc_state;
+      return;
+    }
+  c->direct_tune.push_back({d->n, na, nb, d->tc, d->dense_state, d->otc_state});
+}
+static void tune_recall(Context* c, DirectSigma* d) {
+  const int64_t na = d->a.nstr, nb = (d->same ? d->a : d->b).nstr;
+  for (const Context::DirectTune& t : c->direct_tune)
+    if (t.n == d->n && t.na == na && t.nb == nb && t.tc == d->tc) {
+      if (d->dense_state < 0) d->dense_state = t.dense;
+      if (d->otc_state < 0) d->otc_state = t.otc;
+      return;
+    }
+}
+
 template <typename T>
 static void direct_sigma_t(Context* c, const T* x, T* y) {
   DirectSigma* d = c->direct;
@@ -1234,6 +1255,7 @@ static void direct_sigma_t(Context* c, const T* x, T* y) {
         }
         for (cudaEvent_t& ev : e) QDKGB_CUDA(cudaEventDestroy(ev));
         d->dense_state = d->dense_ms[1] < d->dense_ms[0] ? 1 : 0;
+        tune_record(c, d);
       }
       if (d->dense_state == 1)
         dense();
@@ -1320,6 +1342,7 @@ static void direct_sigma_t(Context* c, const T* x, T* y) {
         QDKGB_CUDA(cudaEventDestroy(e0));
         QDKGB_CUDA(cudaEventDestroy(e1));
         d->otc_state = d->otc_ms[1] < d->otc_ms[0] ? 1 : 0;
+        tune_record(c, d);
       }
       contract((float*)y, d->otc && d->otc_state == 1 ? 1 : 0);
       QDKGB_CHECK_LAUNCH();
@@ -1568,6 +1591,7 @@ static DirectSigma* direct_structure(Context* c) {
         set_max_dynamic_smem(f, (int)smem);
     }
   }
+  if (!dense_env) tune_recall(c, d);  // forms timed before for this shape
   return d;
 }
 

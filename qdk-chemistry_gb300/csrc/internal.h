@@ -155,6 +155,16 @@ struct Context {
   int64_t asci_iters = 0;
   int64_t asci_patches = 0;  // Hamiltonians of the last qdkgb_asci call built by patching the previous one
   std::vector<BatchTune> batch_tune;  // persistent batched solver: cluster size per shape
+  // the direct sigma's timed FP32 forms per space shape (n, n_alpha strings,
+  // n_beta strings, tensor cores on): same-spin form and contraction form,
+  // kept across rebuilds so that a context's FP32 sigma repeats bit for bit
+  struct DirectTune {
+    int n;
+    int64_t na, nb;
+    bool tc;
+    int dense, otc;
+  };
+  std::vector<DirectTune> direct_tune;
   std::vector<double> asci_rot;       // accumulated natural-orbital rotation of the last qdkgb_asci (empty: none)
   DeviceBuffer host_pinned_dummy;
   double* pinned = nullptr;  // small pinned host staging (64 doubles)

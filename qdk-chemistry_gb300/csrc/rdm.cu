@@ -26,12 +26,24 @@ namespace qdkgb {
 
 constexpr int kRdmWarps = 16;
 
+// The pair walk's 1-RDM is summed in fixed point, two 64-bit words per
+// element: x = hi 2^-32 + lo 2^-76 with hi = rint(x 2^32) and lo the rest in
+// units of 2^-76 (the split of each contribution is exact).  Integer
+// additions are exact and associative, so the 1-RDM does not depend on the
+// order in which the atomics land (FP64 atomics would): the natural orbitals
+// of the ASCI grow's rotation, and every 1-RDM of a selected space, repeat
+// bit for bit.  |x| < 2^20 per contribution and up to ~2^19 contributions
+// per element keep the words in range.
+constexpr double kRdmFixHi = 4294967296.0;               // 2^32
+constexpr double kRdmFixLo = 75557863725914323419136.0;  // 2^76
+
 struct RdmTarget {
   int block;       // 0: aaaa (+aa), 1: bbbb (+bb), 2: aabb
   int n;
   int s_lo, s_hi;  // last-index range held by the tile
   double* t4;      // tile or global n^4 block
-  double* t2;      // tile or global n^2 block (blocks 0, 1)
+  double* t2;      // tile or global n^2 block (blocks 0, 1) when not fixed point
+  unsigned long long* t2fx = nullptr;  // global fixed-point n^2 block (2 words per element), when given
   bool shared;
   bool with_ordm;  // accumulate the 1-RDM (first last-index slice only)
 };
@@ -43,7 +55,16 @@ __device__ __forceinline__ void add4(const RdmTarget& T, int blk, uint32_t p, ui
   atomicAdd(T.t4 + p + n * (q + n * (r + n * (s - T.s_lo))), v);
 }
 __device__ __forceinline__ void add2(const RdmTarget& T, int blk, uint32_t p, uint32_t q, double v) {
-  if (blk != T.block || !T.t2) return;
+  if (blk != T.block) return;
+  if (T.t2fx) {
+    const double hi = rint(v * kRdmFixHi);
+    const double lo = rint((v - hi * (1.0 / kRdmFixHi)) * kRdmFixLo);
+    unsigned long long* e = T.t2fx + 2 * (p + (size_t)T.n * q);
+    atomicAdd(e, (unsigned long long)(long long)hi);
+    atomicAdd(e + 1, (unsigned long long)(long long)lo);
+    return;
+  }
+  if (!T.t2) return;
   atomicAdd(T.t2 + p + (size_t)T.n * q, v);
 }
 
@@ -155,7 +176,7 @@ __global__ void __launch_bounds__(kRdmWarps * 32)
   const size_t n4 = (size_t)n * n * n * (T.s_hi - T.s_lo), n2 = (size_t)n * n;
   if (T.shared) {
     T.t4 = tile;
-    T.t2 = (T.block < 2 && T.with_ordm) ? tile + n4 : nullptr;
+    T.t2 = (T.block < 2 && T.with_ordm && !T.t2fx) ? tile + n4 : nullptr;
     for (size_t i = threadIdx.x; i < n4 + (T.t2 ? n2 : 0); i += blockDim.x) tile[i] = 0.;
     __syncthreads();
   }
@@ -576,7 +597,7 @@ void rdms_spin_dep(Context* c, const double* C, double* aa, double* bb, double* 
   const bool force_walk = walk && walk[0] == '1';
   if (!force_walk && cas_rdm_eligible(c) && rdms_cas(c, dC, aa, bb, aaaa, bbbb, aabb)) return;
   double* d4 = dev_array<double>(c, b4, n4);
-  double* d2 = dev_array<double>(c, b2, n2);
+  unsigned long long* d2 = dev_array<unsigned long long>(c, b2, 2 * n2);
   RowArgs a = row_args(c, 0.);
   const size_t smem_cap = 200 * 1024;
   const size_t slice = (size_t)n * n * n * 8;
@@ -587,11 +608,12 @@ void rdms_spin_dep(Context* c, const double* C, double* aa, double* bb, double* 
   const int64_t blocks = std::min<int64_t>((N + kRdmWarps - 1) / kRdmWarps, (int64_t)c->sm_count * (use_shared ? 1 : 4));
   double* outs4[3] = {aaaa, bbbb, aabb};
   double* outs2[3] = {aa, bb, nullptr};
-  std::vector<double> h4(n4), h2(n2);
+  std::vector<double> h4(n4);
+  std::vector<long long> h2(2 * n2);
   for (int blk = 0; blk < 3; ++blk) {
     if (!outs4[blk] && !outs2[blk]) continue;
     QDKGB_CUDA(cudaMemsetAsync(d4, 0, n4 * 8, c->stream));
-    QDKGB_CUDA(cudaMemsetAsync(d2, 0, n2 * 8, c->stream));
+    QDKGB_CUDA(cudaMemsetAsync(d2, 0, 2 * n2 * 8, c->stream));
     for (int s0 = 0; s0 < n; s0 += s_step) {
       RdmTarget T;
       T.block = blk;
@@ -601,10 +623,10 @@ void rdms_spin_dep(Context* c, const double* C, double* aa, double* bb, double* 
       T.shared = use_shared;
       T.with_ordm = (s0 == 0);
       T.t4 = use_shared ? nullptr : d4;
-      T.t2 = (!use_shared && blk < 2) ? d2 : nullptr;
-      const size_t tile =
-          use_shared ? (n2 * n * (T.s_hi - T.s_lo) + ((blk < 2 && T.with_ordm) ? n2 : 0)) * 8 : 0;
-      k_rdm<<<(unsigned)blocks, kRdmWarps * 32, tile, c->stream>>>(a, dC, T, d4, d2);
+      T.t2 = nullptr;
+      T.t2fx = (blk < 2 && T.with_ordm) ? d2 : nullptr;
+      const size_t tile = use_shared ? n2 * n * (T.s_hi - T.s_lo) * 8 : 0;  // the 1-RDM goes to t2fx
+      k_rdm<<<(unsigned)blocks, kRdmWarps * 32, tile, c->stream>>>(a, dC, T, d4, nullptr);
       QDKGB_CHECK_LAUNCH();
       if (!use_shared) break;
     }
@@ -614,8 +636,9 @@ void rdms_spin_dep(Context* c, const double* C, double* aa, double* bb, double* 
       for (size_t i = 0; i < n4; ++i) outs4[blk][i] += h4[i];
     }
     if (outs2[blk]) {
-      QDKGB_CUDA(cudaMemcpy(h2.data(), d2, n2 * 8, cudaMemcpyDeviceToHost));
-      for (size_t i = 0; i < n2; ++i) outs2[blk][i] += h2[i];
+      QDKGB_CUDA(cudaMemcpy(h2.data(), d2, 2 * n2 * 8, cudaMemcpyDeviceToHost));
+      for (size_t i = 0; i < n2; ++i)
+        outs2[blk][i] += (double)h2[2 * i] * (1.0 / kRdmFixHi) + (double)h2[2 * i + 1] * (1.0 / kRdmFixLo);
     }
   }
 }
