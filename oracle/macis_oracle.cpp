@@ -528,6 +528,8 @@ int davidson(const Csr& A, int64_t max_m, const double* D, double tol, double* X
 struct Rdms {
   int n;
   double *aa, *bb, *aaaa, *bbbb, *aabb;
+  // the 1-RDMs' fixed-point accumulators (see fx_add), when given
+  unsigned long long *aa_fx = nullptr, *bb_fx = nullptr;
   double& r4(double* t, uint32_t p, uint32_t q, uint32_t r, uint32_t s) const {
     return t[p + (size_t)n * (q + (size_t)n * (r + (size_t)n * s))];
   }
@@ -536,6 +538,30 @@ struct Rdms {
 inline void atomic_add(double& x, double v) {
 #pragma omp atomic
   x += v;
+}
+// The 1-RDM is summed in fixed point, two 64-bit words per element: x =
+// hi 2^-32 + lo 2^-76, hi = rint(x 2^32), lo the rest in units of 2^-76 (the
+// split of each contribution is exact).  Integer sums do not depend on the
+// order in which the threads' atomics land, so the 1-RDM - and the natural
+// orbitals of the ASCI grow's rotation - repeat bit for bit, and equal the
+// GPU's, which sums the same contributions the same way.
+constexpr double kFxHi = 4294967296.0;               // 2^32
+constexpr double kFxLo = 75557863725914323419136.0;  // 2^76
+inline void fx_add(unsigned long long* t, size_t i, double v) {
+  const double hi = std::rint(v * kFxHi);
+  const double lo = std::rint((v - hi * (1.0 / kFxHi)) * kFxLo);
+  const unsigned long long uh = (unsigned long long)(long long)hi, ul = (unsigned long long)(long long)lo;
+#pragma omp atomic
+  t[2 * i] += uh;
+#pragma omp atomic
+  t[2 * i + 1] += ul;
+}
+inline void add_ordm(const Rdms& R, double* t, uint32_t p, uint32_t q, double v) {
+  unsigned long long* fx = (t == R.aa) ? R.aa_fx : (t == R.bb) ? R.bb_fx : nullptr;
+  if (fx)
+    fx_add(fx, p + (size_t)R.n * q, v);
+  else
+    atomic_add(R.r2(t, p, q), v);
 }
 
 // rdms.hpp:39-68
@@ -569,8 +595,8 @@ void rdm_2(const Rdms& R, bool transpose, uint64_t bra, uint64_t ket, uint64_t e
   Single s = single_excitation_sign_indices(bra, ket, ex);
   const uint32_t o1 = s.o, v1 = s.v;
   if (ordm_ss) {
-    atomic_add(R.r2(ordm_ss, v1, o1), s.sign * val);
-    atomic_add(R.r2(ordm_ss, o1, v1), s.sign * val);
+    add_ordm(R, ordm_ss, v1, o1, s.sign * val);
+    add_ordm(R, ordm_ss, o1, v1, s.sign * val);
   }
   val *= s.sign * 0.5;
   if (trdm_ss) {
@@ -605,9 +631,9 @@ void rdm_2(const Rdms& R, bool transpose, uint64_t bra, uint64_t ket, uint64_t e
 // rdms.hpp:439-516
 void rdm_diag(const Rdms& R, const std::vector<uint32_t>& oa, const std::vector<uint32_t>& ob, double val) {
   if (R.aa)
-    for (auto p : oa) atomic_add(R.r2(R.aa, p, p), val);
+    for (auto p : oa) add_ordm(R, R.aa, p, p, val);
   if (R.bb)
-    for (auto p : ob) atomic_add(R.r2(R.bb, p, p), val);
+    for (auto p : ob) add_ordm(R, R.bb, p, p, val);
   val *= 0.5;
   if (R.aaaa)
     for (auto q : oa)
@@ -629,11 +655,16 @@ void rdm_diag(const Rdms& R, const std::vector<uint32_t>& oa, const std::vector<
 // SortedDoubleLoopHamiltonianGenerator::form_rdms_spin_dep
 // (sorted_double_loop.hpp:626-753) with rdm_contributions_spin_dep<true>
 // (rdms.hpp:579-612).  Results are accumulated (+=).
-void rdms_spin_dep(const uint64_t* alpha, const uint64_t* beta, int64_t nd, const double* C, const Rdms& R) {
+void rdms_spin_dep(const uint64_t* alpha, const uint64_t* beta, int64_t nd, const double* C, const Rdms& R0) {
   std::vector<uint64_t> ua;
   std::vector<int64_t> off;
   unique_alpha(alpha, nd, ua, off);
   const int64_t nu = (int64_t)ua.size();
+  const size_t n2 = (size_t)R0.n * R0.n;
+  std::vector<unsigned long long> fa(R0.aa ? 2 * n2 : 0, 0ull), fb(R0.bb ? 2 * n2 : 0, 0ull);
+  Rdms R = R0;
+  R.aa_fx = R0.aa ? fa.data() : nullptr;
+  R.bb_fx = R0.bb ? fb.data() : nullptr;
 #pragma omp parallel
   {
     std::vector<uint32_t> oa, ob;
@@ -675,6 +706,10 @@ void rdms_spin_dep(const uint64_t* alpha, const uint64_t* beta, int64_t nd, cons
         }
       }
     }
+  }
+  for (size_t i = 0; i < n2; ++i) {
+    if (R0.aa) R0.aa[i] += (double)(long long)fa[2 * i] / kFxHi + (double)(long long)fa[2 * i + 1] / kFxLo;
+    if (R0.bb) R0.bb[i] += (double)(long long)fb[2 * i] / kFxHi + (double)(long long)fb[2 * i + 1] / kFxLo;
   }
 }
 
