@@ -364,10 +364,22 @@ void spmv(const Csr& A, const double* x, double* y) {
   }
 }
 
+// Summed over fixed blocks of 4096 elements, each in index order, and the
+// block sums in block order: the result does not depend on the thread count
+// or on the order in which threads finish (an OpenMP reduction combines its
+// partial sums in no fixed order), so the Davidson steps repeat bit for bit.
 double dot(int64_t n, const double* a, const double* b) {
+  constexpr int64_t kBlk = 4096;
+  const int64_t nb = (n + kBlk - 1) / kBlk;
+  std::vector<double> part(nb);
+#pragma omp parallel for schedule(static)
+  for (int64_t k = 0; k < nb; ++k) {
+    double s = 0.;
+    for (int64_t i = k * kBlk; i < std::min(n, (k + 1) * kBlk); ++i) s += a[i] * b[i];
+    part[k] = s;
+  }
   double s = 0.;
-#pragma omp parallel for reduction(+ : s) schedule(static)
-  for (int64_t i = 0; i < n; ++i) s += a[i] * b[i];
+  for (int64_t k = 0; k < nb; ++k) s += part[k];
   return s;
 }
 double nrm2(int64_t n, const double* a) { return std::sqrt(dot(n, a, a)); }
@@ -530,6 +542,7 @@ struct Rdms {
   double *aa, *bb, *aaaa, *bbbb, *aabb;
   // the 1-RDMs' fixed-point accumulators (see fx_add), when given
   unsigned long long *aa_fx = nullptr, *bb_fx = nullptr;
+  double fx_inv = 1.;  // 1 / s
   double& r4(double* t, uint32_t p, uint32_t q, uint32_t r, uint32_t s) const {
     return t[p + (size_t)n * (q + (size_t)n * (r + (size_t)n * s))];
   }
@@ -539,15 +552,17 @@ inline void atomic_add(double& x, double v) {
 #pragma omp atomic
   x += v;
 }
-// The 1-RDM is summed in fixed point, two 64-bit words per element: x =
-// hi 2^-32 + lo 2^-76, hi = rint(x 2^32), lo the rest in units of 2^-76 (the
-// split of each contribution is exact).  Integer sums do not depend on the
+// The 1-RDM is summed in fixed point, two 64-bit words per element, in
+// units of s = the power of two at or above max_I C_I^2: x / s = hi 2^-32 +
+// lo 2^-76, hi = rint(x / s 2^32), lo the rest in units of 2^-76 (scaling and
+// split are exact).  Integer sums do not depend on the
 // order in which the threads' atomics land, so the 1-RDM - and the natural
 // orbitals of the ASCI grow's rotation - repeat bit for bit, and equal the
 // GPU's, which sums the same contributions the same way.
 constexpr double kFxHi = 4294967296.0;               // 2^32
 constexpr double kFxLo = 75557863725914323419136.0;  // 2^76
 inline void fx_add(unsigned long long* t, size_t i, double v) {
+  // v already divided by s
   const double hi = std::rint(v * kFxHi);
   const double lo = std::rint((v - hi * (1.0 / kFxHi)) * kFxLo);
   const unsigned long long uh = (unsigned long long)(long long)hi, ul = (unsigned long long)(long long)lo;
@@ -559,7 +574,7 @@ inline void fx_add(unsigned long long* t, size_t i, double v) {
 inline void add_ordm(const Rdms& R, double* t, uint32_t p, uint32_t q, double v) {
   unsigned long long* fx = (t == R.aa) ? R.aa_fx : (t == R.bb) ? R.bb_fx : nullptr;
   if (fx)
-    fx_add(fx, p + (size_t)R.n * q, v);
+    fx_add(fx, p + (size_t)R.n * q, v * R.fx_inv);
   else
     atomic_add(R.r2(t, p, q), v);
 }
@@ -665,6 +680,12 @@ void rdms_spin_dep(const uint64_t* alpha, const uint64_t* beta, int64_t nd, cons
   Rdms R = R0;
   R.aa_fx = R0.aa ? fa.data() : nullptr;
   R.bb_fx = R0.bb ? fb.data() : nullptr;
+  double cmax = 0.;
+  for (int64_t i = 0; i < nd; ++i) cmax = std::max(cmax, std::abs(C[i]));
+  int e2 = 0;
+  if (cmax > 0.) std::frexp(cmax * cmax, &e2);
+  const double fx_s = std::ldexp(1.0, e2);
+  R.fx_inv = std::ldexp(1.0, -e2);
 #pragma omp parallel
   {
     std::vector<uint32_t> oa, ob;
@@ -708,8 +729,10 @@ void rdms_spin_dep(const uint64_t* alpha, const uint64_t* beta, int64_t nd, cons
     }
   }
   for (size_t i = 0; i < n2; ++i) {
-    if (R0.aa) R0.aa[i] += (double)(long long)fa[2 * i] / kFxHi + (double)(long long)fa[2 * i + 1] / kFxLo;
-    if (R0.bb) R0.bb[i] += (double)(long long)fb[2 * i] / kFxHi + (double)(long long)fb[2 * i + 1] / kFxLo;
+    if (R0.aa)
+      R0.aa[i] += ((double)(long long)fa[2 * i] * (1.0 / kFxHi) + (double)(long long)fa[2 * i + 1] * (1.0 / kFxLo)) * fx_s;
+    if (R0.bb)
+      R0.bb[i] += ((double)(long long)fb[2 * i] * (1.0 / kFxHi) + (double)(long long)fb[2 * i + 1] * (1.0 / kFxLo)) * fx_s;
   }
 }
 
@@ -1315,7 +1338,10 @@ std::vector<Det> asci_search(const Ham& H, const AsciSettings& S, int64_t ndets_
     tid = omp_get_thread_num();
 #endif
     std::vector<Contrib>& out = per[tid];
-#pragma omp for schedule(dynamic)
+    // static: thread t takes the t-th contiguous block of the core, so the
+    // lists joined in thread order follow the core's order and the stable
+    // sort below sums each determinant's contributions in a fixed order
+#pragma omp for schedule(static)
     for (int64_t ip = 0; ip < ncore; ++ip) contribs_of(H, core[ip], C[ip], E0, S.h_el_tol, out, S.just_singles != 0);
   }
   (void)n;

@@ -27,8 +27,10 @@ namespace qdkgb {
 constexpr int kRdmWarps = 16;
 
 // The pair walk's 1-RDM is summed in fixed point, two 64-bit words per
-// element: x = hi 2^-32 + lo 2^-76 with hi = rint(x 2^32) and lo the rest in
-// units of 2^-76 (the split of each contribution is exact).  Integer
+// element, in units of s = the power of two at or above max_I C_I^2 (so every
+// contribution x / s lies in [-1, 1]): x / s = hi 2^-32 + lo 2^-76 with
+// hi = rint(x / s 2^32) and lo the rest in units of 2^-76 (scaling by s and
+// the split of each contribution are exact).  Integer
 // additions are exact and associative, so the 1-RDM does not depend on the
 // order in which the atomics land (FP64 atomics would): the natural orbitals
 // of the ASCI grow's rotation, and every 1-RDM of a selected space, repeat
@@ -44,6 +46,7 @@ struct RdmTarget {
   double* t4;      // tile or global n^4 block
   double* t2;      // tile or global n^2 block (blocks 0, 1) when not fixed point
   unsigned long long* t2fx = nullptr;  // global fixed-point n^2 block (2 words per element), when given
+  double fx_inv = 1.;                  // 1 / s of the fixed point
   bool shared;
   bool with_ordm;  // accumulate the 1-RDM (first last-index slice only)
 };
@@ -57,6 +60,7 @@ __device__ __forceinline__ void add4(const RdmTarget& T, int blk, uint32_t p, ui
 __device__ __forceinline__ void add2(const RdmTarget& T, int blk, uint32_t p, uint32_t q, double v) {
   if (blk != T.block) return;
   if (T.t2fx) {
+    v *= T.fx_inv;
     const double hi = rint(v * kRdmFixHi);
     const double lo = rint((v - hi * (1.0 / kRdmFixHi)) * kRdmFixLo);
     unsigned long long* e = T.t2fx + 2 * (p + (size_t)T.n * q);
@@ -610,6 +614,12 @@ void rdms_spin_dep(Context* c, const double* C, double* aa, double* bb, double* 
   double* outs2[3] = {aa, bb, nullptr};
   std::vector<double> h4(n4);
   std::vector<long long> h2(2 * n2);
+  // the fixed point's unit: the power of two at or above max C^2
+  double cmax = 0.;
+  for (int64_t i = 0; i < N; ++i) cmax = std::max(cmax, std::fabs(C[i]));
+  int e2 = 0;
+  if (cmax > 0.) std::frexp(cmax * cmax, &e2);
+  const double fx_s = std::ldexp(1.0, e2), fx_inv = std::ldexp(1.0, -e2);
   for (int blk = 0; blk < 3; ++blk) {
     if (!outs4[blk] && !outs2[blk]) continue;
     QDKGB_CUDA(cudaMemsetAsync(d4, 0, n4 * 8, c->stream));
@@ -625,6 +635,7 @@ void rdms_spin_dep(Context* c, const double* C, double* aa, double* bb, double* 
       T.t4 = use_shared ? nullptr : d4;
       T.t2 = nullptr;
       T.t2fx = (blk < 2 && T.with_ordm) ? d2 : nullptr;
+      T.fx_inv = fx_inv;
       const size_t tile = use_shared ? n2 * n * (T.s_hi - T.s_lo) * 8 : 0;  // the 1-RDM goes to t2fx
       k_rdm<<<(unsigned)blocks, kRdmWarps * 32, tile, c->stream>>>(a, dC, T, d4, nullptr);
       QDKGB_CHECK_LAUNCH();
@@ -638,7 +649,8 @@ void rdms_spin_dep(Context* c, const double* C, double* aa, double* bb, double* 
     if (outs2[blk]) {
       QDKGB_CUDA(cudaMemcpy(h2.data(), d2, 2 * n2 * 8, cudaMemcpyDeviceToHost));
       for (size_t i = 0; i < n2; ++i)
-        outs2[blk][i] += (double)h2[2 * i] * (1.0 / kRdmFixHi) + (double)h2[2 * i + 1] * (1.0 / kRdmFixLo);
+        outs2[blk][i] +=
+            ((double)h2[2 * i] * (1.0 / kRdmFixHi) + (double)h2[2 * i + 1] * (1.0 / kRdmFixLo)) * fx_s;
     }
   }
 }

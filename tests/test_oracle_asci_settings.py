@@ -191,3 +191,39 @@ def test_grow_with_rotation_is_self_consistent(oracle, water, h2o):
     E0r, a1, b1, _, _ = oracle.asci(H, a0, b0, [1.0], E_hf, grow=True, refine=False, ntdets_max=400,
                                     core_fixed=1, ncdets_max=50, grow_factor=2.0)
     assert set(zip(a1.tolist(), b1.tolist())) != set(zip(a.tolist(), b.tolist()))
+
+
+_ROT_GROW = """
+import hashlib, sys, numpy as np
+sys.path[:0] = [{repo!r}, {tests!r}]
+import oracle
+from conftest import load_fcidump
+w = load_fcidump("h2o_ccpvdz")
+H = oracle.Hamiltonian(w["T"], w["V"])
+E_hf = H.matrix_element((31, 31), (31, 31))
+U = np.zeros((H.n, H.n))
+E, a, b, c, Eg = oracle.asci(H, [31], [31], [1.0], E_hf, grow=True, refine=False, rotation=U, ntdets_max=400,
+                             core_fixed=1, ncdets_max=50, grow_factor=2.0, grow_with_rot=1, rot_size_start=100)
+print(repr(E), len(a), hashlib.sha1(np.sort(a * 4096 + b).tobytes()).hexdigest(), hashlib.sha1(U.tobytes()).hexdigest())
+"""
+
+
+def test_rotation_grow_independent_of_thread_count(oracle):
+    """The grow with natural-orbital rotation passes a near tie (two
+    selections 5e-5 Eh apart) that a last-bit change in the Davidson vector
+    or the search's sums can flip.  The oracle sums in a fixed order (dot
+    products over fixed blocks, the search's contributions in core order,
+    the 1-RDM in fixed point), so 1, 3 and 16 threads give the same
+    determinants, energy and rotation, bit for bit."""
+    import os
+    import subprocess
+    import sys
+    here = os.path.dirname(os.path.abspath(__file__))
+    code = _ROT_GROW.format(repo=os.path.dirname(here), tests=here)
+    outs = set()
+    for t in (1, 3, 16, 16):
+        env = dict(os.environ, OMP_NUM_THREADS=str(t))
+        r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=300)
+        assert r.returncode == 0, r.stderr
+        outs.add(r.stdout.strip())
+    assert len(outs) == 1, outs
