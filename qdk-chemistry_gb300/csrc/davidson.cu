@@ -26,6 +26,7 @@
 
 #include "common.cuh"
 #include "internal.h"
+#include "dfloat.cuh"
 #include "small_eig.cuh"
 
 namespace qdkgb {
@@ -437,6 +438,310 @@ __global__ void k_store_row(const double* v, int i, double* Hk, int ld) {
   }
 }
 
+// ---------------------------------------------------------------- double-float subspace
+// The mixed-precision solver keeps V, A V, the Ritz vector and the new
+// directions as double-float pairs (dfloat.cuh): the same bytes as FP64 but
+// FP32-pipe arithmetic.  Each kernel mirrors its FP64 counterpart above (the
+// same launch shapes, row split and fixed reduction order); per-block
+// partial sums leave the block as doubles.
+
+// out[j * out_stride] = A[:, j] . w for j < k (k_multidot in double-float)
+__global__ void __launch_bounds__(kVecThreads)
+    k_df_multidot(const float2* __restrict__ A, int64_t lda, int k, const float2* __restrict__ w, int64_t n,
+                  double* __restrict__ partial, unsigned* __restrict__ count, double* __restrict__ out, int out_stride,
+                  double* __restrict__ self_out, const double* __restrict__ skip) {
+  if (skip && *skip != 0.) return;
+  __shared__ double red[kVecThreads / 32][kDotCols + 1];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int j0 = blockIdx.y * kDotCols;
+  const int nc = min(kDotCols, k - j0);
+  const float2* a = A + (size_t)j0 * lda;
+  const bool self = self_out && blockIdx.y == 0;
+  float2 acc[kDotCols];
+#pragma unroll
+  for (int c = 0; c < kDotCols; ++c) acc[c] = make_float2(0.f, 0.f);
+  float2 accw = make_float2(0.f, 0.f);
+  const float2 zero = make_float2(0.f, 0.f);
+  const int64_t step = (int64_t)gridDim.x * kVecTile;
+  for (int64_t i = (int64_t)blockIdx.x * kVecTile + threadIdx.x; i < n; i += step) {
+    const int64_t i1 = i + kVecThreads;
+    const bool has1 = i1 < n;
+    const float2 w0 = w[i], w1 = has1 ? w[i1] : zero;
+    float2 a0[kDotCols], a1[kDotCols];
+#pragma unroll
+    for (int c = 0; c < kDotCols; ++c) {
+      a0[c] = c < nc ? a[i + (size_t)c * lda] : zero;
+      a1[c] = (c < nc && has1) ? a[i1 + (size_t)c * lda] : zero;
+    }
+    if (self) {
+      df::mac(accw, w0, w0);
+      df::mac(accw, w1, w1);
+    }
+#pragma unroll
+    for (int c = 0; c < kDotCols; ++c) {
+      if (c < nc) {
+        df::mac(acc[c], a0[c], w0);
+        df::mac(acc[c], a1[c], w1);
+      }
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < kDotCols; ++c) {
+    if (c < nc) {
+      const double t = warp_sum(df::to_double(acc[c]));
+      if (lane == 0) red[wid][c] = t;
+    }
+  }
+  if (self) {
+    const double t = warp_sum(df::to_double(accw));
+    if (lane == 0) red[wid][kDotCols] = t;
+  }
+  __syncthreads();
+  if (threadIdx.x < nc) {
+    double t = 0.;
+    for (int q = 0; q < kVecThreads / 32; ++q) t += red[q][threadIdx.x];
+    partial[(size_t)(j0 + threadIdx.x) * gridDim.x + blockIdx.x] = t;
+  }
+  if (self && threadIdx.x == kDotCols) {
+    double t = 0.;
+    for (int q = 0; q < kVecThreads / 32; ++q) t += red[q][kDotCols];
+    partial[(size_t)k * gridDim.x + blockIdx.x] = t;
+  }
+  if (!last_block_done(count, blockIdx.y, gridDim.x)) return;
+  if (wid < nc) {
+    const double* p = partial + (size_t)(j0 + wid) * gridDim.x;
+    double t = 0.;
+    for (int b = lane; b < (int)gridDim.x; b += 32) t += __ldcg(p + b);
+    t = warp_sum(t);
+    if (lane == 0) out[(size_t)(j0 + wid) * out_stride] = t;
+  }
+  if (self && wid == kVecThreads / 32 - 1) {
+    const double* p = partial + (size_t)k * gridDim.x;
+    double t = 0.;
+    for (int b = lane; b < (int)gridDim.x; b += 32) t += __ldcg(p + b);
+    t = warp_sum(t);
+    if (lane == 0) *self_out = t;
+  }
+}
+// y -= A[:, 0:k] coef (k_gemv_rows<true> in double-float; the same skip and
+// selective-reorthogonalisation outputs)
+__global__ void __launch_bounds__(kVecThreads)
+    k_df_gemv_sub(const float2* __restrict__ A, int64_t lda, int k, const double* __restrict__ coef,
+                  float2* __restrict__ y, int64_t n, const double* __restrict__ skip, const double* __restrict__ w2,
+                  double* __restrict__ skip_out) {
+  if (skip && *skip != 0.) return;
+  __shared__ float2 c[kMaxSubspace + 2];
+  for (int j = threadIdx.x; j < k; j += blockDim.x) c[j] = df::split(coef[j]);
+  if (skip_out && blockIdx.x == 0 && threadIdx.x == 0) {
+    double cc = 0.;
+    for (int j = 0; j < k; ++j) cc += coef[j] * coef[j];
+    *skip_out = (*w2 - cc >= 0.5 * *w2) ? 1. : 0.;
+  }
+  __syncthreads();
+  const float2 zero = make_float2(0.f, 0.f);
+  const int64_t step = (int64_t)gridDim.x * kVecTile;
+  for (int64_t i = (int64_t)blockIdx.x * kVecTile + threadIdx.x; i < n; i += step) {
+    const int64_t i1 = i + kVecThreads;
+    const bool has1 = i1 < n;
+    float2 s0 = zero, s1 = zero;
+    int j = 0;
+    for (; j + 4 <= k; j += 4) {
+      float2 a0[4], a1[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        a0[q] = A[i + (size_t)(j + q) * lda];
+        a1[q] = has1 ? A[i1 + (size_t)(j + q) * lda] : zero;
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        df::mac(s0, a0[q], c[j + q]);
+        df::mac(s1, a1[q], c[j + q]);
+      }
+    }
+    for (; j < k; ++j) {
+      df::mac(s0, A[i + (size_t)j * lda], c[j]);
+      if (has1) df::mac(s1, A[i1 + (size_t)j * lda], c[j]);
+    }
+    y[i] = df::sub(y[i], df::normalise(s0));
+    if (has1) y[i1] = df::sub(y[i1], df::normalise(s1));
+  }
+}
+// Y[:, o] = A[:, 0:k] Q[:, o] for o < nout (k_gemv_multi in double-float)
+__global__ void __launch_bounds__(kVecThreads)
+    k_df_gemv_multi(const float2* __restrict__ A, int64_t lda, int k, const double* __restrict__ Q, int nout,
+                    float2* __restrict__ Y, int64_t ldy, int64_t n) {
+  __shared__ float2 q[kMaxSubspace + 2][kMaxOut];
+  for (int t = threadIdx.x; t < k * kMaxOut; t += blockDim.x) {
+    const int j = t / kMaxOut, o = t % kMaxOut;
+    q[j][o] = o < nout ? df::split(Q[(size_t)o * k + j]) : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  for (int64_t i = (int64_t)blockIdx.x * kVecThreads + threadIdx.x; i < n; i += (int64_t)gridDim.x * kVecThreads) {
+    float2 acc[kMaxOut];
+#pragma unroll
+    for (int o = 0; o < kMaxOut; ++o) acc[o] = make_float2(0.f, 0.f);
+    for (int j = 0; j < k; ++j) {
+      const float2 a = A[i + (size_t)j * lda];
+#pragma unroll
+      for (int o = 0; o < kMaxOut; ++o)
+        if (o < nout) df::mac(acc[o], a, q[j][o]);
+    }
+#pragma unroll
+    for (int o = 0; o < kMaxOut; ++o)
+      if (o < nout) Y[i + (size_t)o * ldy] = df::normalise(acc[o]);
+  }
+}
+// w *= 1/sqrt(*nrm2) when sqrt(*nrm2) > min_norm, else raise *flag; xf, when
+// given, receives the FP32 copy of the result (the next FP32 sigma's input)
+__global__ void k_df_normalize(float2* w, int64_t n, const double* nrm2, double min_norm, double* flag, float* xf) {
+  __shared__ float2 sc;
+  __shared__ bool ok;
+  if (threadIdx.x == 0) {
+    const double nrm = sqrt(*nrm2);
+    ok = nrm > min_norm;
+    sc = df::split(ok ? 1. / nrm : 0.);
+    if (!ok && flag && blockIdx.x == 0) *flag = 1.;
+  }
+  __syncthreads();
+  if (!ok) return;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float2 v = df::mul(w[i], sc);
+    w[i] = v;
+    if (xf) xf[i] = v.x;
+  }
+}
+// X = V C0, R = AV C0 - lam0 X, *out = |R|^2 (k_ritz_residual in double-float;
+// with Dd, R is stored preconditioned: -R / (D - lam0) with |D - lam0|
+// clamped to min_abs, formed in FP32 - a search direction, orthogonalised
+// afterwards)
+__global__ void __launch_bounds__(kVecThreads)
+    k_df_ritz_residual(const float2* __restrict__ V, const float2* __restrict__ AV, int64_t ld, int k,
+                       const double* __restrict__ C0, const double* __restrict__ lam, float2* __restrict__ X,
+                       float2* __restrict__ R, int64_t n, const float2* __restrict__ Dd, double min_abs,
+                       double* __restrict__ partial, unsigned* __restrict__ count, double* __restrict__ out) {
+  __shared__ float2 c[kMaxSubspace + 2];
+  __shared__ double red[kVecThreads / 32];
+  for (int j = threadIdx.x; j < k; j += blockDim.x) c[j] = df::split(C0[j]);
+  __syncthreads();
+  const float2 l0 = df::split(lam[0]);
+  const float mina = (float)min_abs;
+  const float2 zero = make_float2(0.f, 0.f);
+  float s2 = 0.f;
+  const int64_t step = (int64_t)gridDim.x * kVecTile;
+  for (int64_t i = (int64_t)blockIdx.x * kVecTile + threadIdx.x; i < n; i += step) {
+    const int64_t i1 = i + kVecThreads;
+    const bool has1 = i1 < n;
+    float2 x0 = zero, ax0 = zero, x1 = zero, ax1 = zero;
+    int j = 0;
+    for (; j + 4 <= k; j += 4) {
+      float2 v0[4], v1[4], w0[4], w1[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const size_t o = (size_t)(j + q) * ld;
+        v0[q] = V[i + o];
+        w0[q] = AV[i + o];
+        v1[q] = has1 ? V[i1 + o] : zero;
+        w1[q] = has1 ? AV[i1 + o] : zero;
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        df::mac(x0, v0[q], c[j + q]);
+        df::mac(ax0, w0[q], c[j + q]);
+        df::mac(x1, v1[q], c[j + q]);
+        df::mac(ax1, w1[q], c[j + q]);
+      }
+    }
+    for (; j < k; ++j) {
+      const size_t o = (size_t)j * ld;
+      df::mac(x0, V[i + o], c[j]);
+      df::mac(ax0, AV[i + o], c[j]);
+      if (has1) {
+        df::mac(x1, V[i1 + o], c[j]);
+        df::mac(ax1, AV[i1 + o], c[j]);
+      }
+    }
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      if (h == 1 && !has1) break;
+      const int64_t r = h ? i1 : i;
+      const float2 xv = df::normalise(h ? x1 : x0);
+      const float2 rv = df::sub(df::normalise(h ? ax1 : ax0), df::mul(l0, xv));
+      X[r] = xv;
+      s2 = __fmaf_rn(rv.x, rv.x, s2);
+      if (Dd) {
+        const float2 dd = Dd[r];
+        float d = __fadd_rn(__fsub_rn(dd.x, l0.x), __fsub_rn(dd.y, l0.y));
+        if (fabsf(d) < mina) d = (d >= 0.f) ? mina : -mina;
+        R[r] = make_float2(__fdiv_rn(-rv.x, d), 0.f);
+      } else {
+        R[r] = rv;
+      }
+    }
+  }
+  const double t = block_sum_vec((double)s2, red);
+  if (threadIdx.x == 0) partial[blockIdx.x] = t;
+  if (!last_block_done(count, kDotChunks, gridDim.x)) return;
+  double u = 0.;
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += kVecThreads) u += __ldcg(partial + b);
+  __syncthreads();
+  u = block_sum_vec(u, red);
+  if (threadIdx.x == 0) *out = u;
+}
+__global__ void k_df_from_f64(const double* __restrict__ x, float2* __restrict__ y, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = df::split(x[i]);
+}
+__global__ void k_df_from_f32(const float* __restrict__ x, float2* __restrict__ y, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = make_float2(x[i], 0.f);
+}
+__global__ void k_df_to_f64(const float2* __restrict__ x, double* __restrict__ y, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = df::to_double(x[i]);
+}
+// k_flip_project in double-float: x <- (x + s x^T) / 2 (s = +-1, so s x and
+// the halving are exact)
+__global__ void __launch_bounds__(kFlipTile * 8) k_df_flip_project(float2* x, int64_t n, float s) {
+  const int I = blockIdx.y, J = blockIdx.x;
+  if (I > J) return;
+  __shared__ float2 P[kFlipTile][kFlipTile + 1], Q[kFlipTile][kFlipTile + 1];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int64_t r0 = (int64_t)I * kFlipTile, c0 = (int64_t)J * kFlipTile;
+  const float2 zero = make_float2(0.f, 0.f);
+  for (int r = ty; r < kFlipTile; r += 8) {
+    const int64_t pr = r0 + r, pc = c0 + tx, qr = c0 + r, qc = r0 + tx;
+    P[r][tx] = (pr < n && pc < n) ? x[pr * n + pc] : zero;
+    Q[r][tx] = (qr < n && qc < n) ? x[qr * n + qc] : zero;
+  }
+  __syncthreads();
+  // (a + s b) / 2, and s times it
+  auto avg = [s](float2 a, float2 b) {
+    const float2 t = df::add(a, make_float2(s * b.x, s * b.y));
+    return make_float2(0.5f * t.x, 0.5f * t.y);
+  };
+  for (int r = ty; r < kFlipTile; r += 8) {
+    const int64_t pr = r0 + r, pc = c0 + tx, qr = c0 + r, qc = r0 + tx;
+    if (I < J) {
+      if (pr < n && pc < n) x[pr * n + pc] = avg(P[r][tx], Q[tx][r]);
+      if (qr < n && qc < n) {
+        const float2 v = avg(P[tx][r], Q[r][tx]);
+        x[qr * n + qc] = make_float2(s * v.x, s * v.y);
+      }
+    } else if (pr < n && pc < n) {
+      float2 v;
+      if (r < tx) {
+        v = avg(P[r][tx], P[tx][r]);
+      } else if (r > tx) {
+        v = avg(P[tx][r], P[r][tx]);
+        v = make_float2(s * v.x, s * v.y);
+      } else {
+        v = s < 0 ? zero : P[r][tx];
+      }
+      x[pr * n + pc] = v;
+    }
+  }
+}
+
 __global__ void __launch_bounds__(kEigThreads) k_lowest_eig(int k, const double* __restrict__ H, int ldh,
                                                             double* gA, int nev, double* eval, double* evec) {
   lowest_eig_cta(k, H, ldh, gA, nev, eval, evec);
@@ -596,6 +901,89 @@ struct Dav {
                                                 small + kSlotRes);
     QDKGB_CHECK_LAUNCH();
   }
+  // ---- the double-float subspace of the mixed-precision solver
+  float2 *Vf = nullptr, *AVf = nullptr;
+  float* xf = nullptr;  // FP32 copy of the newest normalised direction (the FP32 sigma's input)
+  float2* colf(float2* base, int64_t j) { return base + (size_t)j * n; }
+  // grid as multidot's, sized by the blocks of k_df_multidot resident per SM
+  // (its sixteen loads in flight per thread take more registers than four
+  // blocks per SM allow)
+  void df_multidot(const float2* A, int k, const float2* w, double* out, int stride, double* self_out = nullptr,
+                   const double* skip = nullptr) {
+    static const int per_sm = [] {
+      int b = 0;
+      QDKGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_df_multidot, kVecThreads, 0));
+      return std::max(1, std::min(b, kVecBlocksPerSm));
+    }();
+    const int nbd = (int)std::max<int64_t>(1, std::min<int64_t>((n + kVecTile - 1) / kVecTile, (int64_t)sm_count * per_sm));
+    const int chunks = (k + kDotCols - 1) / kDotCols;
+    const int bx = std::max(1, std::min(nbd, std::max(sm_count, nbd / chunks)));
+    k_df_multidot<<<dim3(bx, chunks), kVecThreads, 0, st>>>(A, n, k, w, n, partial, counts(), out, stride, self_out,
+                                                            skip);
+    QDKGB_CHECK_LAUNCH();
+  }
+  void df_orth_passes(int K, float2* w, bool selective = false) {
+    if (K <= 0) return;
+    if (!selective) {
+      for (int pass = 0; pass < 2; ++pass) {
+        df_multidot(Vf, K, w, small, 1);
+        k_df_gemv_sub<<<nb, kVecThreads, 0, st>>>(Vf, n, K, small, w, n, nullptr, nullptr, nullptr);
+        QDKGB_CHECK_LAUNCH();
+      }
+      return;
+    }
+    df_multidot(Vf, K, w, small, 1, small + kSlotW2);
+    k_df_gemv_sub<<<nb, kVecThreads, 0, st>>>(Vf, n, K, small, w, n, nullptr, small + kSlotW2, small + kSlotSkip);
+    QDKGB_CHECK_LAUNCH();
+    df_multidot(Vf, K, w, small, 1, nullptr, small + kSlotSkip);
+    k_df_gemv_sub<<<nb, kVecThreads, 0, st>>>(Vf, n, K, small, w, n, small + kSlotSkip, nullptr, nullptr);
+    QDKGB_CHECK_LAUNCH();
+  }
+  // gram_schmidt on the double-float basis; the normalised result's FP32
+  // copy goes to xf
+  void df_gram_schmidt(int K, float2* w, double min_norm, bool selective) {
+    df_orth_passes(K, w, selective);
+    df_multidot(w, 1, w, small + kSlotNrm, 1);
+    k_df_normalize<<<nb, 256, 0, st>>>(w, n, small + kSlotNrm, min_norm, small + kSlotFlag, xf);
+    QDKGB_CHECK_LAUNCH();
+  }
+  void df_fallback(int K, float2* w, double min_norm = 1e-12) {
+    for (int64_t idx = 0; idx < n; ++idx) {
+      QDKGB_CUDA(cudaMemsetAsync(w, 0, n * sizeof(float2), st));
+      const float2 one = make_float2(1.f, 0.f);
+      QDKGB_CUDA(cudaMemcpyAsync(w + idx, &one, sizeof(float2), cudaMemcpyHostToDevice, st));
+      df_orth_passes(K, w);
+      df_multidot(w, 1, w, small + kSlotNrm, 1);
+      double nv;
+      fetch(small + kSlotNrm, nv);
+      if (std::sqrt(nv) > min_norm) {
+        k_df_normalize<<<nb, 256, 0, st>>>(w, n, small + kSlotNrm, min_norm, nullptr, xf);
+        QDKGB_CHECK_LAUNCH();
+        clear_flag();
+        return;
+      }
+    }
+    throw Error(QDKGB_ERR_INVALID, "gram_schmidt: Unable to find orthogonal vector");
+  }
+  void df_projected_row(int i) {
+    df_multidot(AVf, i + 1, colf(Vf, i), small, 1);
+    k_store_row<<<1, 256, 0, st>>>(small, i, Hk, (int)(maxm + 1));
+    QDKGB_CHECK_LAUNCH();
+  }
+  void df_ritz_residual(int k, float2* Xr, float2* R, const float2* Dd, double min_abs) {
+    k_df_ritz_residual<<<nb, kVecThreads, 0, st>>>(Vf, AVf, n, k, evec, eval, Xr, R, n, Dd, min_abs, partial, counts(),
+                                                   small + kSlotRes);
+    QDKGB_CHECK_LAUNCH();
+  }
+  void df_from_f64(const double* x, float2* y) {
+    k_df_from_f64<<<nb, 256, 0, st>>>(x, y, n);
+    QDKGB_CHECK_LAUNCH();
+  }
+  void df_to_f64(const float2* x, double* y) {
+    k_df_to_f64<<<nb, 256, 0, st>>>(x, y, n);
+    QDKGB_CHECK_LAUNCH();
+  }
+
   // the same for root r of the last Rayleigh-Ritz (eigenvector column r, ld
   // k): Ritz vector into Xr, preconditioned residual into Rr, |R|^2 into
   // small[kSlotRoots + r]
@@ -789,7 +1177,9 @@ void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C
   d.V = dev_array<double>(c, W.V, (size_t)N * (max_m + 1));
   d.AV = dev_array<double>(c, W.AV, (size_t)N * (max_m + 1));
   constexpr int kKeep = 6;  // thick-restart size of the mixed path
-  d.X = dev_array<double>(c, W.scratch, (size_t)N * (3 + 2 * kKeep));
+  // X, then the mixed path's FP64 sig and Rt, kKeep + kKeep restart columns
+  // and three double-float columns (Ritz vector, overflow direction, diagonal)
+  d.X = dev_array<double>(c, W.scratch, (size_t)N * (6 + 2 * kKeep));
   d.work = d.X + N;
   d.Hk = dev_array<double>(c, W.Hk, (size_t)(max_m + 1) * (max_m + 1));
   d.evec = dev_array<double>(c, W.evec, (size_t)(max_m + 1) * (max_m + 1));
@@ -811,19 +1201,11 @@ void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C
     spmv_fp64(c, x, y);
     loc.spmv_fp64++;
   };
-  auto sigma_sub = [&](const double* x, double* y) {
-    if (!mixed) {
-      sigma_full(x, y);
-      return;
-    }
-    f64_to_f32(c, x, xf, N);
-    spmv_fp32(c, xf, yf);
-    f32_to_f64(c, yf, y, N);
-    loc.spmv_fp32++;
-  };
 
-  // guess (selected_ci_diag.hpp:130-140, diagonal_guess davidson.hpp:106-113)
-  double* V0 = d.V;
+  // guess (selected_ci_diag.hpp:130-140, diagonal_guess davidson.hpp:106-113);
+  // the mixed path holds its basis in double-float form, so its FP64 guess
+  // goes to the scratch column X
+  double* V0 = mixed ? d.X : d.V;
   bool use_c = false;
   if (s->use_guess && C) {
     double mx = 0.;
@@ -898,10 +1280,17 @@ void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C
     // is done, otherwise the subspace restarts on the kKeep lowest Ritz
     // vectors, the first carrying the exact sigma, and iterates on.
     const double drop = 1e-4;
-    double* sig = d.work;
-    double* Rt = d.work + N;
-    double* tmpV = d.work + 2 * N;
-    double* tmpAV = d.work + (2 + kKeep) * N;
+    double* sig = d.work;       // exact (full-precision) sigma of the Ritz vector
+    double* Rt = d.work + N;    // its exact residual
+    float2* dfw = (float2*)(d.work + 2 * N);
+    float2* tmpV = dfw;                       // restart columns (kKeep)
+    float2* tmpAV = dfw + (size_t)kKeep * N;  // their sigmas (kKeep)
+    float2* Xf = dfw + (size_t)2 * kKeep * N;  // Ritz vector
+    float2* Rtf = Xf + N;                     // a direction that does not fit the basis
+    float2* Df = Rtf + N;                     // the diagonal
+    d.Vf = (float2*)d.V;
+    d.AVf = (float2*)d.AV;
+    d.xf = xf;
     double* Eptr = d.small + kSlotE;
     // The reference's FP64 iteration keeps the guess's spin-flip symmetry
     // (C[Ia, Ib] = +-C[Ib, Ia] when both spins share one string list): H and
@@ -934,45 +1323,53 @@ void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C
           flip = -1.;
       }
     }
-    auto project = [&](double* v) {
+    auto project = [&](float2* v) {
       if (flip == 0.) return;
       const unsigned nt = (unsigned)((nstr + kFlipTile - 1) / kFlipTile);
-      k_flip_project<<<dim3(nt, nt), dim3(kFlipTile, 8), 0, c->stream>>>(v, nstr, flip);
+      k_df_flip_project<<<dim3(nt, nt), dim3(kFlipTile, 8), 0, c->stream>>>(v, nstr, (float)flip);
       QDKGB_CHECK_LAUNCH();
     };
-    sigma_full(V0, d.AV);
-    QDKGB_CUDA(cudaMemcpyAsync(d.col(d.V, 1), d.AV, N * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
-    project(d.col(d.V, 1));
-    d.gram_schmidt(1, d.col(d.V, 1), 1e-12, true);
-    d.projected_row(0);
+    d.df_from_f64(d.D, Df);
+    sigma_full(V0, sig);
+    d.df_from_f64(V0, d.colf(d.Vf, 0));
+    d.df_from_f64(sig, d.colf(d.AVf, 0));
+    d.df_from_f64(sig, d.colf(d.Vf, 1));
+    project(d.colf(d.Vf, 1));
+    d.df_gram_schmidt(1, d.colf(d.Vf, 1), 1e-12, true);
+    d.df_projected_row(0);
     // residual of the guess (exact): reference level for the first refresh
-    d.multidot(d.AV, 1, V0, Eptr, 1);
-    k_axpy_residual<<<d.nb, 256, 0, c->stream>>>(d.AV, V0, Eptr, Rt, N, d.partial);
+    d.multidot(sig, 1, V0, Eptr, 1);
+    k_axpy_residual<<<d.nb, 256, 0, c->stream>>>(sig, V0, Eptr, Rt, N, d.partial);
     QDKGB_CHECK_LAUNCH();
     k_reduce_partials<<<1, 32, 0, c->stream>>>(d.partial, d.nb, 1, d.small + kSlotRes, 1);
     QDKGB_CHECK_LAUNCH();
     double last_true = 0.;
     d.fetch(d.small + kSlotRes, last_true);
     last_true = std::sqrt(last_true);
-    int k = 1;  // valid columns; V[:, k] holds the next direction
+    int k = 1;  // valid columns; V[:, k] holds the next direction (its FP32 copy in xf)
     int64_t iter = 0;
     double best = 1e300;
     int since_best = 0;
+    bool have_x64 = false;  // d.X holds the FP64 copy of the current Ritz vector
     while (iter < 4 * max_m) {
-      sigma_sub(d.col(d.V, k), d.col(d.AV, k));
-      d.projected_row(k);
+      spmv_fp32(c, xf, yf);
+      loc.spmv_fp32++;
+      k_df_from_f32<<<d.nb, 256, 0, c->stream>>>(yf, d.colf(d.AVf, k), N);
+      QDKGB_CHECK_LAUNCH();
+      d.df_projected_row(k);
       ++k;
       ++iter;
       d.lowest(k);
-      double* R = (k <= max_m - 1) ? d.col(d.V, k) : Rt;
-      d.ritz_residual(k, R, s->min_abs_denominator);
+      float2* R = (k <= max_m - 1) ? d.colf(d.Vf, k) : Rtf;
+      d.df_ritz_residual(k, Xf, R, Df, s->min_abs_denominator);
+      have_x64 = false;
       double r2 = 0.;
       bool degenerate = false;
       d.fetch3(d.small + kSlotRes, d.eval, r2, lam0, degenerate);
       if (degenerate) {
         --k;
         --iter;
-        d.fallback(k, d.col(d.V, k));
+        d.df_fallback(k, d.colf(d.Vf, k));
         continue;
       }
       const double est = std::sqrt(r2);
@@ -987,10 +1384,12 @@ void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C
           est < 0.5 * s->res_tol || est < drop * last_true || since_best >= 6 || k >= max_m - 1;
       if (!refresh) {
         project(R);
-        d.gram_schmidt(k, R, 1e-12, true);
+        d.df_gram_schmidt(k, R, 1e-12, true);
         continue;
       }
       // full-precision sigma, Rayleigh quotient and residual of X (unit norm)
+      d.df_to_f64(Xf, d.X);
+      have_x64 = true;
       sigma_full(d.X, sig);
       d.multidot(sig, 1, d.X, Eptr, 1);
       k_axpy_residual<<<d.nb, 256, 0, c->stream>>>(sig, d.X, Eptr, Rt, N, d.partial);
@@ -1009,31 +1408,32 @@ void davidson(Context* c, const qdkgb_davidson_settings* s, double* E, double* C
       const int kk = std::min(kKeep, k);
       d.lowest(k, kk);  // the kk lowest Ritz vectors (column 0 reproduces X)
       if (kk > 1) {
-        static_assert(kKeep - 1 <= kMaxOut, "restart block wider than k_gemv_multi");
-        k_gemv_multi<<<d.nb, kVecThreads, 0, c->stream>>>(d.V, N, k, d.evec + k, kk - 1, tmpV, N, N);
+        static_assert(kKeep - 1 <= kMaxOut, "restart block wider than k_df_gemv_multi");
+        k_df_gemv_multi<<<d.nb, kVecThreads, 0, c->stream>>>(d.Vf, N, k, d.evec + k, kk - 1, tmpV, N, N);
         QDKGB_CHECK_LAUNCH();
-        k_gemv_multi<<<d.nb, kVecThreads, 0, c->stream>>>(d.AV, N, k, d.evec + k, kk - 1, tmpAV, N, N);
+        k_df_gemv_multi<<<d.nb, kVecThreads, 0, c->stream>>>(d.AVf, N, k, d.evec + k, kk - 1, tmpAV, N, N);
         QDKGB_CHECK_LAUNCH();
       }
-      QDKGB_CUDA(cudaMemcpyAsync(d.col(d.V, 0), d.X, N * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
-      QDKGB_CUDA(cudaMemcpyAsync(d.col(d.AV, 0), sig, N * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+      QDKGB_CUDA(cudaMemcpyAsync(d.colf(d.Vf, 0), Xf, N * sizeof(float2), cudaMemcpyDeviceToDevice, c->stream));
+      d.df_from_f64(sig, d.colf(d.AVf, 0));
       for (int j = 1; j < kk; ++j) {
-        QDKGB_CUDA(cudaMemcpyAsync(d.col(d.V, j), tmpV + (size_t)(j - 1) * N, N * sizeof(double),
+        QDKGB_CUDA(cudaMemcpyAsync(d.colf(d.Vf, j), tmpV + (size_t)(j - 1) * N, N * sizeof(float2),
                                    cudaMemcpyDeviceToDevice, c->stream));
-        QDKGB_CUDA(cudaMemcpyAsync(d.col(d.AV, j), tmpAV + (size_t)(j - 1) * N, N * sizeof(double),
+        QDKGB_CUDA(cudaMemcpyAsync(d.colf(d.AVf, j), tmpAV + (size_t)(j - 1) * N, N * sizeof(float2),
                                    cudaMemcpyDeviceToDevice, c->stream));
       }
-      for (int j = 0; j < kk; ++j) d.projected_row(j);
+      for (int j = 0; j < kk; ++j) d.df_projected_row(j);
       k = kk;
       // next direction: preconditioned true residual
-      QDKGB_CUDA(cudaMemcpyAsync(d.col(d.V, k), Rt, N * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
-      k_precondition<<<d.nb, 256, 0, c->stream>>>(d.col(d.V, k), d.D, Eptr, N, s->min_abs_denominator);
+      k_precondition<<<d.nb, 256, 0, c->stream>>>(Rt, d.D, Eptr, N, s->min_abs_denominator);
       QDKGB_CHECK_LAUNCH();
-      project(d.col(d.V, k));
-      d.gram_schmidt(k, d.col(d.V, k), 1e-12, true);
+      d.df_from_f64(Rt, d.colf(d.Vf, k));
+      project(d.colf(d.Vf, k));
+      d.df_gram_schmidt(k, d.colf(d.Vf, k), 1e-12, true);
       best = 1e300;
       since_best = 0;
     }
+    if (!have_x64) d.df_to_f64(Xf, d.X);
   }
 
   QDKGB_CUDA(cudaStreamSynchronize(c->stream));
