@@ -370,7 +370,7 @@ def run_ours(args):
             tf32_peak = _bf16_peak() / 2
             achieved = 3 * flops / t_spmv32 / 1e12
             kern32 = ("FP32 direct sigma on the tensor cores: k_ds_opposite_tc (opposite-spin doubles and every "
-                      "single excitation as one tcgen05 TF32x3 contraction per alpha string) + k_tc_gemm2 (the "
+                      "single excitation as one tcgen05 TF32x3 contraction per alpha string) + k_tc_gemm2b (the "
                       "same-spin string-only part as two dense tcgen05 TF32x3 products)")
             roof = {"bound": "tensor", "kernel": kern32, "achieved": achieved, "peak": tf32_peak,
                     "unit": "TFLOP/s", "frac": achieved / tf32_peak,
@@ -590,7 +590,7 @@ def run_batched(args):
                                   "max_abs_energy_diff_vs_batch": float(max(dE))},
         "batch_speedup_vs_per_instance_fp64": t_loop / t,
         "roofline": {"bound": "hbm", "kernel": "the lockstep solve: new directions through the direct contraction "
-                                               "(k_ds_opposite_mm FMA pipe + k_tc_gemm2 tcgen05 same-spin products, "
+                                               "(k_ds_opposite_mm or k_ds_opposite_tc + k_tc_gemm2b tcgen05 same-spin products, "
                                                "instance grid axis), full-precision refreshes through the stored "
                                                "split slab (k_slab_sigma<2>), batched vector kernels",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,

@@ -524,12 +524,16 @@ __global__ void __launch_bounds__(kVecThreads)
   }
 }
 // y -= A[:, 0:k] coef (k_gemv_rows<true> in double-float; the same skip and
-// selective-reorthogonalisation outputs)
+// selective-reorthogonalisation outputs).  nrm_out, when given, receives
+// |y|^2 of the result (Dot2 per thread, partial sums per block, the last
+// block adds them in block order), so no separate norm pass follows.
 __global__ void __launch_bounds__(kVecThreads)
     k_df_gemv_sub(const float2* __restrict__ A, int64_t lda, int k, const double* __restrict__ coef,
                   float2* __restrict__ y, int64_t n, const double* __restrict__ skip, const double* __restrict__ w2,
-                  double* __restrict__ skip_out) {
+                  double* __restrict__ skip_out, double* __restrict__ partial, unsigned* __restrict__ count,
+                  double* __restrict__ nrm_out) {
   if (skip && *skip != 0.) return;
+  __shared__ double red[kVecThreads / 32];
   __shared__ float2 c[kMaxSubspace + 2];
   for (int j = threadIdx.x; j < k; j += blockDim.x) c[j] = df::split(coef[j]);
   if (skip_out && blockIdx.x == 0 && threadIdx.x == 0) {
@@ -539,6 +543,7 @@ __global__ void __launch_bounds__(kVecThreads)
   }
   __syncthreads();
   const float2 zero = make_float2(0.f, 0.f);
+  float2 yy = zero;
   const int64_t step = (int64_t)gridDim.x * kVecTile;
   for (int64_t i = (int64_t)blockIdx.x * kVecTile + threadIdx.x; i < n; i += step) {
     const int64_t i1 = i + kVecThreads;
@@ -562,9 +567,24 @@ __global__ void __launch_bounds__(kVecThreads)
       df::mac(s0, A[i + (size_t)j * lda], c[j]);
       if (has1) df::mac(s1, A[i1 + (size_t)j * lda], c[j]);
     }
-    y[i] = df::sub(y[i], df::normalise(s0));
-    if (has1) y[i1] = df::sub(y[i1], df::normalise(s1));
+    const float2 y0 = df::sub(y[i], df::normalise(s0));
+    y[i] = y0;
+    df::mac(yy, y0, y0);
+    if (has1) {
+      const float2 y1 = df::sub(y[i1], df::normalise(s1));
+      y[i1] = y1;
+      df::mac(yy, y1, y1);
+    }
   }
+  if (!nrm_out) return;
+  const double t = block_sum_vec(df::to_double(yy), red);
+  if (threadIdx.x == 0) partial[blockIdx.x] = t;
+  if (!last_block_done(count, kDotChunks, gridDim.x)) return;
+  double u = 0.;
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += kVecThreads) u += __ldcg(partial + b);
+  __syncthreads();
+  u = block_sum_vec(u, red);
+  if (threadIdx.x == 0) *nrm_out = u;
 }
 // Y[:, o] = A[:, 0:k] Q[:, o] for o < nout (k_gemv_multi in double-float)
 __global__ void __launch_bounds__(kVecThreads)
@@ -922,28 +942,37 @@ struct Dav {
                                                             skip);
     QDKGB_CHECK_LAUNCH();
   }
+  // the two CGS passes of df_gram_schmidt; every update that runs leaves
+  // |w|^2 of its result in small[kSlotNrm] (the second, selective one only
+  // when the test asks for it)
   void df_orth_passes(int K, float2* w, bool selective = false) {
-    if (K <= 0) return;
+    if (K <= 0) {
+      df_multidot(w, 1, w, small + kSlotNrm, 1);
+      return;
+    }
+    double* nrm = small + kSlotNrm;
     if (!selective) {
       for (int pass = 0; pass < 2; ++pass) {
         df_multidot(Vf, K, w, small, 1);
-        k_df_gemv_sub<<<nb, kVecThreads, 0, st>>>(Vf, n, K, small, w, n, nullptr, nullptr, nullptr);
+        k_df_gemv_sub<<<nb, kVecThreads, 0, st>>>(Vf, n, K, small, w, n, nullptr, nullptr, nullptr, partial, counts(),
+                                                  nrm);
         QDKGB_CHECK_LAUNCH();
       }
       return;
     }
     df_multidot(Vf, K, w, small, 1, small + kSlotW2);
-    k_df_gemv_sub<<<nb, kVecThreads, 0, st>>>(Vf, n, K, small, w, n, nullptr, small + kSlotW2, small + kSlotSkip);
+    k_df_gemv_sub<<<nb, kVecThreads, 0, st>>>(Vf, n, K, small, w, n, nullptr, small + kSlotW2, small + kSlotSkip,
+                                              partial, counts(), nrm);
     QDKGB_CHECK_LAUNCH();
     df_multidot(Vf, K, w, small, 1, nullptr, small + kSlotSkip);
-    k_df_gemv_sub<<<nb, kVecThreads, 0, st>>>(Vf, n, K, small, w, n, small + kSlotSkip, nullptr, nullptr);
+    k_df_gemv_sub<<<nb, kVecThreads, 0, st>>>(Vf, n, K, small, w, n, small + kSlotSkip, nullptr, nullptr, partial,
+                                              counts(), nrm);
     QDKGB_CHECK_LAUNCH();
   }
   // gram_schmidt on the double-float basis; the normalised result's FP32
   // copy goes to xf
   void df_gram_schmidt(int K, float2* w, double min_norm, bool selective) {
     df_orth_passes(K, w, selective);
-    df_multidot(w, 1, w, small + kSlotNrm, 1);
     k_df_normalize<<<nb, 256, 0, st>>>(w, n, small + kSlotNrm, min_norm, small + kSlotFlag, xf);
     QDKGB_CHECK_LAUNCH();
   }
@@ -953,7 +982,6 @@ struct Dav {
       const float2 one = make_float2(1.f, 0.f);
       QDKGB_CUDA(cudaMemcpyAsync(w + idx, &one, sizeof(float2), cudaMemcpyHostToDevice, st));
       df_orth_passes(K, w);
-      df_multidot(w, 1, w, small + kSlotNrm, 1);
       double nv;
       fetch(small + kSlotNrm, nv);
       if (std::sqrt(nv) > min_norm) {
