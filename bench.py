@@ -262,8 +262,14 @@ def run_ours(args):
         return e
 
     def step(storage, precision):
+        # the FP64 path stores the matrix (the reference's form); the mixed
+        # path takes the operator qdkgb_build_operator picks, as qdkgb_casci
+        # does (for this complete space the direct sigma in both precisions)
         e0 = ev()
-        ctx.build_hamiltonian(storage=storage)
+        if precision == capi.PREC_FP64:
+            ctx.build_hamiltonian(storage=storage)
+        else:
+            ctx.build_operator(storage=storage)
         e1 = ev()
         E, _, info = ctx.davidson(tol=RES_TOL, precision=precision, want_vector=False)
         e2 = ev()
@@ -337,7 +343,7 @@ def run_ours(args):
         elif used32 in ("register8", "register16"):
             kern32 = ("k_slab_sigma32v<4, %d> (FP32 sigma, slab layout: values only, 4 beta strings per thread, "
                       "%d positions in flight)" % ((8, 8) if used32 == "register8" else (16, 16)))
-    elif lay32 == capi.OP_SLAB_DIRECT32:
+    elif lay32 in (capi.OP_SLAB_DIRECT32, capi.OP_DIRECT):
         bytes32 = None
         kern32 = ("FP32 direct sigma: k_ds_opposite_mm (opposite-spin doubles and every single excitation as one "
                   "contraction per alpha string, FMA pipe) + the same-spin string-only part")
@@ -351,7 +357,7 @@ def run_ours(args):
         bytes64 = nnz * 12 + (N + 1) * 8 + N * 8 + N * 8
         kern64 = "k_spmv_csr<double> (FP64 sigma, CSR)"
     roof = None
-    if lay32 == capi.OP_SLAB_DIRECT32:
+    if lay32 in (capi.OP_SLAB_DIRECT32, capi.OP_DIRECT):
         # FLOPs of one FP32 direct sigma as formulated: the contraction forms
         # E (rows: the n(n-1) pairs, n W rows, one string row; K: the alpha
         # singles and the own row) for every beta string; the same-spin part

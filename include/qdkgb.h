@@ -162,7 +162,12 @@ int qdkgb_build_direct_sigma(qdkgb_context* ctx);
  * and the qdkgb_set_device_limit cap, counting what the current operator
  * holds) together with a Davidson workspace of max_m vectors; otherwise, for
  * a complete (n_alpha, n_beta) space within the direct sigma's limits, the
- * direct sigma (qdkgb_build_direct_sigma).  *layout (may be NULL) receives
+ * direct sigma (qdkgb_build_direct_sigma).  A complete space of 131,072
+ * (2^17) or more determinants with storage QDKGB_H_SPLIT32 (a mixed-precision
+ * solve) takes the direct sigma even when the matrix would fit: its FP32
+ * sigma is the direct contraction either way, and recomputing the solve's few
+ * full-precision refreshes costs less than emitting an FP64 matrix for them
+ * (environment QDKGB_MIXED_FP32=slab keeps the stored form).  *layout (may be NULL) receives
  * QDKGB_LAYOUT_SLAB, QDKGB_LAYOUT_CSR or QDKGB_LAYOUT_DIRECT, *nnz (may be
  * NULL) the element count of the stored matrix's CSR (0 for the direct sigma).  The reference
  * always stores the matrix (make_csr_hamiltonian_block_ in
@@ -413,7 +418,8 @@ int qdkgb_casscf(qdkgb_context* ctx, const qdkgb_mcscf_settings* s, int nalpha, 
  * cas_helper::impl / compute_casci_rdms (cpp/src/qdk/chemistry/algorithms/
  * microsoft/macis_cas.cpp:35-117, include/macis/mcscf/cas.hpp:33-64): FCI
  * space, the operator of qdkgb_build_operator (stored, or the direct sigma
- * when the stored matrix would not fit), Davidson.  E receives the electronic energy (the caller
+ * when the stored matrix would not fit or the solve is mixed precision on a
+ * space of 2^17 or more determinants), Davidson.  E receives the electronic energy (the caller
  * adds the core energy, macis_cas.cpp:113); C (may be NULL) the CI vector in
  * MACIS determinant order. */
 int qdkgb_casci(qdkgb_context* ctx, int norb, int nalpha, int nbeta, const double* T, const double* V, int layout,

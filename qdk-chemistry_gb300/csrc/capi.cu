@@ -2,6 +2,7 @@
 // exceptions into a status code plus a message kept in the context.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <map>
@@ -163,11 +164,21 @@ static int64_t cas_row_elements(int n, int ka, int kb) {
   return 1 + sa + sb + C2(ka) * C2(n - ka) + C2(kb) * C2(n - kb) + sa * sb;
 }
 
+// Complete spaces from this many determinants up take the direct sigma for
+// mixed-precision solves (QDKGB_H_SPLIT32): their FP32 sigma is the direct
+// contraction whatever is stored, so a stored FP64 matrix would serve only the
+// few full-precision refreshes of the solve, and emitting it costs more than
+// recomputing them (853,776 determinants: 9.3 ms of emission, refreshes of
+// 2.8 ms from the stored matrix against 3.75 ms recomputed, four refreshes).
+constexpr int64_t kMixedDirectMinDets = (int64_t)1 << 17;
+
 // The stored Hamiltonian when it fits in the device memory available to this
 // context (free memory, and the cap of qdkgb_set_device_limit, counting what
 // the current operator holds) beside the Davidson workspace of max_m
-// vectors; otherwise, for a complete space the direct sigma serves.  Returns
-// true when the direct sigma was built.
+// vectors; otherwise, for a complete space the direct sigma serves.  A large
+// complete space with QDKGB_H_SPLIT32 storage takes the direct sigma as well
+// (kMixedDirectMinDets; QDKGB_MIXED_FP32=slab keeps the stored operator).
+// Returns true when the direct sigma was built.
 bool qdkgb::build_operator(Context* c, double thresh, int storage, int max_m) {
   const DetSpace& S = c->dets;
   if (!c->have_dets) throw Error(QDKGB_ERR_STATE, "determinants not set");
@@ -187,7 +198,10 @@ bool qdkgb::build_operator(Context* c, double thresh, int storage, int max_m) {
     double avail = (double)fr + held;
     if (c->dev_limit > 0) avail = std::min(avail, (double)(c->dev_limit - c->dev_bytes) + held);
     const bool direct_ok = n <= 20 && S.ngroups <= 4096 && S.nbeta <= 4096 && ka > 0 && kb > 0;
-    if (direct_ok && stored + work > 0.92 * avail) {
+    const char* keep = std::getenv("QDKGB_MIXED_FP32");
+    const bool mixed_direct = storage == QDKGB_H_SPLIT32 && S.ndets >= kMixedDirectMinDets &&
+                              !(keep && std::string(keep) == "slab");
+    if (direct_ok && (mixed_direct || stored + work > 0.92 * avail)) {
       build_direct_sigma(c);
       return true;
     }
