@@ -5,10 +5,11 @@ Workload: 853,776 determinants (n_alpha = n_beta = 6 in 12 orbitals), seeded
 synthetic integrals (h1 = diag(-2 + 0.25 p) + N(0, 0.05^2) off-diagonal,
 V = sum over 24 symmetric Cholesky vectors with N(0, 0.1^2) entries).
 One step = the hot path from integrals and determinants resident in HBM to
-the ground-state energy: Hamiltonian build (1.55e9 matrix elements; a
-complete space is stored in the slab layout, values only) + Davidson to a
-full-precision residual norm of 1e-8, in the mixed-precision form (FP32
-sigma, FP64 subspace / refinement).  The plain FP64 path is timed beside it.
+the ground-state energy: the operator (qdkgb_build_operator: for this
+complete space of 1.55e9 matrix elements the direct sigma, nothing stored) +
+Davidson to a full-precision residual norm of 1e-8, in the mixed-precision
+form (FP32 sigma, double-float subspace, FP64 refinement).  The plain FP64
+path (the matrix stored in the slab layout) is timed beside it.
 
 The stored matrix (6.2 GB FP32 + 6.2 GB low parts, or 12.4 GB FP64) is far
 larger than L2 (129 MB), so no L2 flush is needed between steps.
@@ -430,10 +431,13 @@ def run_ours(args):
     line = {
         "metric": METRIC, "value": t_step, "unit": "s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": False, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32 sigma / f64 subspace+refinement", "data": "synthetic",
+        "vs_baseline": None, "dtype": "f32 sigma / double-float subspace / f64 refinement", "data": "synthetic",
         "config": {"workload": WORKLOAD, "norb": NORB, "nalpha": NEL // 2, "nbeta": NEL // 2, "ndets": N,
                    "nnz": nnz, "n_chol": NCHOL, "seed": SEED, "res_tol": RES_TOL, "precision": "mixed",
-                   "l2": "inputs larger than L2 (stored H %.1f GB), no flush" % (stored32 * 8 / 1e9),
+                   "l2": (("working set larger than L2: Davidson subspace columns of %.1f MB (V and A V, tens of "
+                           "columns per solve), no stored matrix; no flush" % (N * 8 / 1e6))
+                          if lay32 == capi.OP_DIRECT else
+                          "inputs larger than L2 (stored H %.1f GB), no flush" % (stored32 * 8 / 1e9)),
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "roofline": roof or {"bound": "hbm", "kernel": kern32, "achieved": achieved32,
                              "peak": peak, "unit": "GB/s", "frac": achieved32 / peak, "peak_source": peak_kind,
@@ -683,7 +687,7 @@ def run_cas14(args):
     line = {
         "metric": "casci_14e14o_time_to_energy", "value": tm, "unit": "s", "n_gpus": 1, "steps": 1, "warmup": 0,
         "ms_per_step": tm * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 sigma / f64 subspace+refinement", "data": "synthetic",
+        "dtype": "f32 sigma / double-float subspace / f64 refinement", "data": "synthetic",
         "config": {"workload": "CASCI(14e,14o) direct sigma, 11,778,624 determinants, Davidson to |r| < 1e-8",
                    "norb": norb, "nalpha": nel // 2, "nbeta": nel // 2, "ndets": N, "n_chol": nchol, "seed": SEED},
         "mixed": {"seconds": tm, "iterations": infom["iterations"], "spmv_fp32": infom["spmv_fp32"],
